@@ -1,0 +1,134 @@
+/*
+ * msplat GB300 engine — device-level C ABI.
+ *
+ * This is the internal boundary of the training hot path: the CUDA
+ * replacement of the reference's msplat_train_step and msplat_render
+ * (core/metal/bindings.h:58-95, implemented at core/metal/msplat_metal.mm:
+ * 1099-1117 and 1118-1740), plus the SGLD step (bindings.h:97-107,
+ * msplat_metal.mm:1746-1812).  Everything takes plain device pointers and
+ * sizes; the public trainer API (msplat_c_api.h) is built on top of it.
+ *
+ * Threading: one engine is driven from one host thread (the reference's
+ * single-trainer rule, core/metal/msplat_metal.mm:411-417).  All work is
+ * enqueued on the engine's own CUDA stream.
+ *
+ * Errors: functions return 0 on success and a negative code on failure;
+ * msplat_engine_last_error() describes the last failure.
+ */
+#ifndef MSPLAT_ENGINE_H
+#define MSPLAT_ENGINE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct MsplatEngine MsplatEngine;
+
+/* Gaussians in device memory, row-major, num_points rows, the reference's
+ * layouts (core/include/model.hpp:65-70): means [N,3], scales [N,3] (log),
+ * quats [N,4] (w,x,y,z), features_dc [N,3], features_rest [N,rest_bases,3],
+ * opacities [N] (logit).  Pointers must be 16-byte aligned. */
+typedef struct {
+    int num_points;
+    int rest_bases;
+    float *means, *scales, *quats, *features_dc, *features_rest, *opacities;
+} MsplatGaussians;
+
+/* Adam moments in device memory, same shapes as the parameters, in the
+ * reference's group order (model.cpp:223): means, scales, quats,
+ * features_dc, features_rest, opacities. */
+typedef struct {
+    float *exp_avg[6];
+    float *exp_avg_sq[6];
+} MsplatAdamState;
+
+/* The scalar arguments of msplat_train_step / msplat_render
+ * (core/metal/bindings.h:58-95, model.cpp:901-969). */
+typedef struct {
+    float viewmat[16];      /* row-major world->camera (model.cpp:857-866) */
+    float projmat[16];      /* row-major projection * view */
+    float fx, fy, cx, cy;
+    int width, height;
+    float cam_pos[3];
+    float background[3];
+    float clip_thresh;      /* near-plane cull, 0.01 in the reference */
+    int degrees_to_use;     /* active SH bands */
+    float ssim_weight;      /* 0.2 */
+    float loss_inv_n;       /* 1 / (3 * pixels), or 1 / (3 * unmasked pixels) */
+    float step_size[6];     /* lr / (1 - beta1^t) per group */
+    float bc2_sqrt[6];      /* sqrt(1 - beta2^t) per group */
+    float beta1, beta2, eps;
+    float op_reg, sc_reg;   /* MCMC regularizer weights (0 before step 500) */
+    float invis_scale;      /* regularizer duty for rendered Gaussians (1 = reference) */
+    int raster_mode;        /* 0: reference rule (chunked iff < 400 tiles), 1: monolithic, 2: chunked */
+    int k_max;              /* chunk count of the chunked raster; 0 = reference rule */
+    int do_optimizer;       /* 1: SH Adam, regularizer and Adam run in the step */
+    int do_sgld;            /* 1: SGLD noise on the means after the optimizer */
+    uint32_t seed;          /* SGLD noise seed (the training step) */
+    float noise_lr, xyz_lr, max_disp;
+} MsplatStepArgs;
+
+/* Per-stage device time of the last step (ms), when timing is enabled. */
+enum {
+    MSPLAT_STAGE_PROJECT = 0, MSPLAT_STAGE_TILES, MSPLAT_STAGE_RASTER_FWD, MSPLAT_STAGE_LOSS,
+    MSPLAT_STAGE_RASTER_BWD, MSPLAT_STAGE_PROJECT_BWD, MSPLAT_STAGE_ADAM, MSPLAT_STAGE_SGLD,
+    MSPLAT_STAGE_COUNT
+};
+
+typedef struct {
+    long long num_intersections;   /* M of the last step */
+    int max_tile_count;
+    int k_max;                     /* 1 = monolithic raster */
+    int num_tiles;
+    uint32_t nan_counts[16];       /* cumulative non-finite telemetry (reference slot numbering) */
+    float stage_ms[MSPLAT_STAGE_COUNT];
+} MsplatEngineStats;
+
+/* Creates an engine on CUDA device `device`.  max_points sizes the
+ * per-Gaussian arena (0 = grow on demand). */
+MsplatEngine *msplat_engine_create(int device, int max_points);
+void msplat_engine_destroy(MsplatEngine *e);
+const char *msplat_engine_last_error(const MsplatEngine *e);
+
+/* One training step (msplat_train_step): projection, tile lists, raster,
+ * SSIM+L1 loss, backward, fused SH Adam, regularizer + Adam, optional SGLD.
+ * gt: device uint8 [H,W,3]; mask: device uint8 [H,W] or NULL.
+ * Parameters and moments are updated in place.  Asynchronous. */
+int msplat_engine_train_step(MsplatEngine *e, const MsplatGaussians *g, const MsplatAdamState *st,
+                             const MsplatStepArgs *args, const uint8_t *gt, const uint8_t *mask);
+
+/* Forward only (msplat_render); the image stays in the engine's "out_img"
+ * buffer (device float [H,W,3]).  Asynchronous. */
+int msplat_engine_render(MsplatEngine *e, const MsplatGaussians *g, const MsplatStepArgs *args);
+
+/* Waits for the engine's stream. */
+int msplat_engine_synchronize(MsplatEngine *e);
+
+/* Loss of the last step (loss_sum / (H*W), msplat_metal.mm:1738); waits. */
+int msplat_engine_loss(MsplatEngine *e, float *loss);
+
+/* Stats of the last step; waits. */
+int msplat_engine_stats(MsplatEngine *e, MsplatEngineStats *out);
+
+/* Enables per-stage CUDA-event timing (adds events to the stream). */
+int msplat_engine_set_timing(MsplatEngine *e, int enabled);
+
+/* Named intermediate buffers ("rec", "depths", "radii", "aabb", "tiles_hit",
+ * "tile_counts", "tile_offsets", "packed", "out_img", "final_T",
+ * "final_idx", "v_img", "grad", "v_mean", "v_scale", "v_quat", ...):
+ * returns the size in bytes and the device pointer (or -1). */
+long long msplat_engine_buffer(MsplatEngine *e, const char *name, void **dev_ptr);
+
+/* Copies the first `bytes` of a named buffer to host memory; waits. */
+int msplat_engine_read(MsplatEngine *e, const char *name, void *dst, long long bytes);
+
+/* The engine's CUDA stream (cudaStream_t). */
+void *msplat_engine_stream(MsplatEngine *e);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

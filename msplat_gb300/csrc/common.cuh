@@ -1,0 +1,116 @@
+// Shared device definitions of the msplat GB300 engine.
+//
+// Layouts (N = active Gaussians, P = H*W pixels, T = 16x16 tiles, M = tile
+// intersections):
+//   params      means[N,3] scales[N,3] (log) quats[N,4] (w,x,y,z)
+//               features_dc[N,3] features_rest[N,B,3] opacities[N] (logit)
+//   SplatRec    per Gaussian, 48 B: projected centre, sigmoid(opacity),
+//               conic, raw SH colour (written by the projection)
+//   PackedRec   per intersection, 48 B, the SplatRec of the splat with its id
+//               in a.w, in per-tile depth order (written by the sort)
+//   GradRec     per Gaussian, 48 B: rasterizer gradients (xy, opacity logit;
+//               conic; colour), accumulated with vector atomics
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace msplat {
+
+constexpr int kTile = 16;           // tile edge (msplat.hpp BLOCK_X/BLOCK_Y)
+constexpr int kTileThreads = 256;   // one thread per tile pixel
+constexpr int kChunk = 512;         // depth-chunk length of the chunked raster
+
+struct SplatRec {
+    float4 a;   // x, y, opacity (sigmoid), unused
+    float4 b;   // conic a, b, c, unused
+    float4 c;   // raw SH colour r, g, b, unused
+};
+
+struct GradRec {
+    float4 a;   // v_x, v_y, v_opacity_logit, 0
+    float4 b;   // v_conic a, b, c, 0
+    float4 c;   // v_colour r, g, b, 0
+};
+
+// Per-step scalars, resident on the device so that a captured step can be
+// replayed with new values (kernels take a pointer, not the values).
+struct StepParams {
+    float viewmat[16];
+    float projmat[16];
+    float fx, fy, cx, cy;
+    float tan_fovx, tan_fovy;
+    float cam_pos[3];
+    float bg[3];
+    float clip_thresh;
+    int degrees_to_use;
+    float ssim_weight, loss_inv_n;
+    float step_size[6], bc2_sqrt[6];
+    float beta1, beta2, eps;
+    float op_reg, sc_reg, invis_scale;
+    uint32_t seed;
+    float noise_lr, xyz_lr, max_disp;
+    int has_mask;
+    int pad_[3];
+};
+
+// Telemetry slots of the non-finite counters (same numbering as the
+// reference's grad_nan_counts, msplat_metal.mm:535-543 and model.cpp:597-636).
+enum NanSlot {
+    kNanMean = 0, kNanScale = 1, kNanQuat = 2, kNanSH = 3, kNanSsimWin = 4, kNanOpacity = 5,
+    kNanVRendered = 6, kNanProj = 7, kNanProjCenter = 8, kNanProjDepth = 9, kNanProjAabb = 10,
+    kNanProjConic = 11, kNanProjRgb = 12, kNanPack = 13, kNanPackOpacity = 14, kNanRasterSigma = 15
+};
+
+__device__ __forceinline__ bool finite_bits(float x) {
+    return (__float_as_uint(x) & 0x7F800000u) != 0x7F800000u;
+}
+
+// Deterministic exp: Cody-Waite reduction x = n*ln2 + r with ln2 split
+// hi/lo, degree-7 Taylor polynomial of e^r (|r| <= ln2/2) in Horner form with
+// fused multiply-adds, exact power-of-two scaling.  Only IEEE-rounded
+// operations, so the host oracle's copy of this algorithm gives the same bits.
+__device__ __forceinline__ float det_expf(float x) {
+    if (x != x) return x;
+    if (x > 88.72283f) return __int_as_float(0x7f800000);
+    if (x < -87.33654f) return 0.0f;
+    const float n = rintf(__fmul_rn(x, 1.44269504088896341f));
+    float r = __fmaf_rn(n, -0.693145751953125f, x);
+    r = __fmaf_rn(n, -1.42860676533018e-06f, r);
+    float p = 1.0f / 5040.0f;
+    p = __fmaf_rn(p, r, 1.0f / 720.0f);
+    p = __fmaf_rn(p, r, 1.0f / 120.0f);
+    p = __fmaf_rn(p, r, 1.0f / 24.0f);
+    p = __fmaf_rn(p, r, 1.0f / 6.0f);
+    p = __fmaf_rn(p, r, 0.5f);
+    p = __fmaf_rn(p, r, 1.0f);
+    p = __fmaf_rn(p, r, 1.0f);
+    int ni = (int)n;
+    float scale_lo = 1.0f;
+    if (ni > 127) { scale_lo = 2.0f; ni -= 1; }
+    if (ni < -126) { scale_lo = 0.5f; ni += 1; }
+    const float two_n = __uint_as_float((uint32_t)(ni + 127) << 23);
+    return __fmul_rn(__fmul_rn(p, two_n), scale_lo);
+}
+
+// Tile rectangle of a splat, inclusive min / exclusive max (get_tile_bbox,
+// msplat_metal.metal:57-87).  Truncating, saturating float->int conversion.
+__device__ __forceinline__ void tile_rect(float cx, float cy, float ax, float ay, int tiles_x, int tiles_y,
+                                          int &x0, int &y0, int &x1, int &y1) {
+    const float tcx = __fdiv_rn(cx, 16.0f), tcy = __fdiv_rn(cy, 16.0f);
+    const float trx = __fdiv_rn(ax, 16.0f), try_ = __fdiv_rn(ay, 16.0f);
+    x0 = min(max(0, __float2int_rz(__fsub_rn(tcx, trx))), tiles_x);
+    x1 = min(max(0, __float2int_rz(__fadd_rn(__fadd_rn(tcx, trx), 1.0f))), tiles_x);
+    y0 = min(max(0, __float2int_rz(__fsub_rn(tcy, try_))), tiles_y);
+    y1 = min(max(0, __float2int_rz(__fadd_rn(__fadd_rn(tcy, try_), 1.0f))), tiles_y);
+}
+
+// Tile list bound clamped to the intersection buffer.
+__device__ __forceinline__ int clamp_off(uint32_t off, long long cap) {
+    return (int)((long long)off < cap ? (long long)off : cap);
+}
+
+__device__ __forceinline__ void atomic_add_f4(float4 *addr, float4 v) {
+    atomicAdd(addr, v);   // sm_90+: one vector reduction in L2
+}
+
+}  // namespace msplat

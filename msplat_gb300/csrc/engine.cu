@@ -1,0 +1,415 @@
+// Host driver of the GB300 training step: a grow-only device arena sized by
+// the largest view and Gaussian count seen, one CUDA stream, and the stage
+// order of msplat_train_step (core/metal/msplat_metal.mm:1118-1740).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <stdexcept>
+#include <string>
+
+#include "kernels.h"
+#include "msplat_engine.h"
+
+namespace msplat {
+
+#define CK(x)                                                                                  \
+    do {                                                                                       \
+        cudaError_t err_ = (x);                                                                \
+        if (err_ != cudaSuccess)                                                               \
+            throw std::runtime_error(std::string(#x) + ": " + cudaGetErrorString(err_));       \
+    } while (0)
+
+struct Buf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+};
+
+class Engine {
+  public:
+    explicit Engine(int device) : device_(device) {
+        CK(cudaSetDevice(device));
+        CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+        cudaDeviceProp prop;
+        CK(cudaGetDeviceProperties(&prop, device));
+        num_sms_ = prop.multiProcessorCount;
+        for (auto &ev : ev_) CK(cudaEventCreate(&ev));
+    }
+    ~Engine() {
+        cudaSetDevice(device_);
+        cudaStreamSynchronize(stream_);
+        for (auto &kv : bufs_) cudaFree(kv.second.ptr);
+        for (auto &ev : ev_) cudaEventDestroy(ev);
+        cudaStreamDestroy(stream_);
+    }
+
+    void reserve_points(int n) { ensure_points(n); }
+
+    void train_step(const MsplatGaussians &g, const MsplatAdamState *st, const MsplatStepArgs &args, const uint8_t *gt,
+                    const uint8_t *mask, bool backward) {
+        CK(cudaSetDevice(device_));
+        validate(g, args);
+        const int N = g.num_points, W = args.width, H = args.height;
+        const int tx = (W + kTile - 1) / kTile, ty = (H + kTile - 1) / kTile, T = tx * ty;
+        const long long P = (long long)W * H;
+        const long long cap = std::max<long long>(48LL * N, 1);   // msplat_metal.mm:1142 legacy capacity
+        const int K = choose_k(args, T, cap);
+        ensure_points(N);
+        ensure_tiles(T);
+        ensure_isect(cap);
+        ensure_pixels(P);
+        if (K > 1) ensure_chunks((long long)K * P);
+        last_T_ = T;
+        last_K_ = K;
+
+        StepParams sp;
+        fill_params(args, sp, mask != nullptr);
+        // pageable source: the copy has consumed it when the call returns
+        CK(cudaMemcpyAsync(ptr<StepParams>("params"), &sp, sizeof(sp), cudaMemcpyHostToDevice, stream_));
+        CK(cudaMemsetAsync(ptr<uint32_t>("tile_counts"), 0, sizeof(uint32_t) * 2 * (size_t)T, stream_));
+        CK(cudaMemsetAsync(ptr<float>("loss_sum"), 0, sizeof(float), stream_));
+
+        mark(0);
+        ProjectArgs pa{};
+        pa.n = N; pa.rest_bases = g.rest_bases; pa.tiles_x = tx; pa.tiles_y = ty;
+        pa.Wf = (float)W; pa.Hf = (float)H;
+        pa.means = g.means; pa.scales = g.scales; pa.quats = g.quats;
+        pa.features_dc = g.features_dc; pa.features_rest = g.features_rest; pa.opacities = g.opacities;
+        pa.sp = ptr<StepParams>("params");
+        pa.rec = ptr<SplatRec>("rec"); pa.depths = ptr<float>("depths"); pa.radii = ptr<int>("radii");
+        pa.aabb = ptr<float2>("aabb"); pa.tiles_hit = ptr<int>("tiles_hit");
+        pa.grad = backward ? ptr<GradRec>("grad") : nullptr;
+        pa.nan_counts = ptr<unsigned>("nan_counts");
+        launch_project_fwd(pa, stream_);
+        mark(1);
+
+        TileArgs ta{};
+        ta.n = N; ta.tiles_x = tx; ta.tiles_y = ty; ta.num_tiles = T; ta.capacity = cap;
+        ta.radii = pa.radii; ta.depths = pa.depths; ta.rec = pa.rec; ta.aabb = pa.aabb;
+        ta.tile_counts = ptr<uint32_t>("tile_counts"); ta.tile_write = ta.tile_counts + T;
+        ta.tile_offsets = ptr<uint32_t>("tile_offsets"); ta.max_tile_count = ptr<uint32_t>("max_tile");
+        ta.keys = ptr<uint64_t>("keys"); ta.keys_alt = ptr<uint64_t>("keys_alt");
+        ta.packed = ptr<SplatRec>("packed"); ta.nan_counts = pa.nan_counts;
+        launch_tiles(ta, stream_);
+        mark(2);
+
+        RasterArgs ra{};
+        ra.width = W; ra.height = H; ra.tiles_x = tx; ra.num_tiles = T; ra.k_max = K; ra.capacity = cap;
+        ra.sp = pa.sp; ra.tile_offsets = ta.tile_offsets; ra.packed = ta.packed;
+        ra.out_img = ptr<float>("out_img"); ra.final_T = ptr<float>("final_T"); ra.final_idx = ptr<int>("final_idx");
+        if (K > 1) {
+            ra.chunk_T = ptr<float>("chunk_T"); ra.chunk_C = ptr<float>("chunk_C"); ra.chunk_idx = ptr<int>("chunk_idx");
+            ra.prefix_T = ptr<float>("prefix_T"); ra.after_C = ptr<float>("after_C");
+        }
+        ra.v_img = ptr<float>("v_img"); ra.grad = ptr<GradRec>("grad"); ra.nan_counts = pa.nan_counts;
+        launch_raster_fwd(ra, stream_);
+        mark(3);
+        if (!gt) { mark(4); mark(5); mark(6); mark(7); mark(8); return; }
+
+        LossArgs la{};
+        la.width = W; la.height = H; la.sp = pa.sp; la.img = ra.out_img; la.gt = gt; la.mask = mask;
+        la.hbuf = ptr<float>("hbuf"); la.dbuf = ptr<float>("dbuf"); la.v_img = ptr<float>("v_img");
+        la.loss_sum = ptr<float>("loss_sum"); la.nan_counts = pa.nan_counts;
+        launch_loss(la, stream_);
+        mark(4);
+        if (!backward) { mark(5); mark(6); mark(7); mark(8); return; }
+
+        launch_raster_bwd(ra, stream_);
+        mark(5);
+
+        ProjectBwdArgs pb{};
+        pb.n = N; pb.rest_bases = g.rest_bases; pb.do_optimizer = args.do_optimizer && st;
+        pb.Wf = (float)W; pb.Hf = (float)H; pb.sp = pa.sp;
+        pb.means = g.means; pb.scales = g.scales; pb.quats = g.quats; pb.radii = pa.radii; pb.rec = pa.rec;
+        pb.grad = ra.grad;
+        pb.v_mean = ptr<float>("v_mean"); pb.v_scale = ptr<float>("v_scale"); pb.v_quat = ptr<float>("v_quat");
+        pb.features_dc = g.features_dc; pb.features_rest = g.features_rest;
+        if (st) {
+            pb.dc_m = st->exp_avg[3]; pb.dc_v = st->exp_avg_sq[3];
+            pb.rest_m = st->exp_avg[4]; pb.rest_v = st->exp_avg_sq[4];
+        }
+        pb.nan_counts = pa.nan_counts;
+        launch_project_bwd(pb, stream_);
+        mark(6);
+
+        AdamArgs aa{};
+        aa.n = N; aa.sp = pa.sp;
+        aa.means = g.means; aa.scales = g.scales; aa.quats = g.quats; aa.opacities = g.opacities;
+        if (st) {
+            const int grp[4] = {0, 1, 2, 5};
+            for (int k = 0; k < 4; k++) { aa.m[k] = st->exp_avg[grp[k]]; aa.v[k] = st->exp_avg_sq[grp[k]]; }
+            aa.dc_v = st->exp_avg_sq[3];
+        }
+        aa.g_mean = pb.v_mean; aa.g_scale = pb.v_scale; aa.g_quat = pb.v_quat; aa.grad = ra.grad;
+        aa.nan_counts = pa.nan_counts;
+        if (args.do_optimizer && st) launch_adam(aa, num_sms_, stream_);
+        mark(7);
+        if (args.do_sgld) launch_sgld(aa, stream_);
+        mark(8);
+        CK(cudaGetLastError());
+    }
+
+    void synchronize() { CK(cudaStreamSynchronize(stream_)); }
+
+    float loss() {
+        float v = 0;
+        CK(cudaMemcpyAsync(&v, ptr<float>("loss_sum"), sizeof(float), cudaMemcpyDeviceToHost, stream_));
+        synchronize();
+        return v / (float)last_P_;
+    }
+
+    void stats(MsplatEngineStats &o) {
+        std::memset(&o, 0, sizeof(o));
+        synchronize();
+        if (last_T_ > 0) {
+            uint32_t tot = 0, mx = 0;
+            CK(cudaMemcpy(&tot, ptr<uint32_t>("tile_offsets") + last_T_, 4, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(&mx, ptr<uint32_t>("max_tile"), 4, cudaMemcpyDeviceToHost));
+            o.num_intersections = tot;
+            o.max_tile_count = (int)mx;
+        }
+        o.k_max = last_K_;
+        o.num_tiles = last_T_;
+        if (has("nan_counts")) CK(cudaMemcpy(o.nan_counts, ptr<unsigned>("nan_counts"), 64, cudaMemcpyDeviceToHost));
+        if (timing_) {
+            for (int s = 0; s < MSPLAT_STAGE_COUNT; s++) {
+                float ms = 0;
+                if (cudaEventElapsedTime(&ms, ev_[s], ev_[s + 1]) == cudaSuccess) o.stage_ms[s] = ms;
+            }
+        }
+    }
+
+    void set_timing(bool on) { timing_ = on; }
+
+    long long buffer(const std::string &name, void **p) {
+        auto it = bufs_.find(name);
+        if (it == bufs_.end()) return -1;
+        if (p) *p = it->second.ptr;
+        return (long long)it->second.bytes;
+    }
+
+    cudaStream_t stream() const { return stream_; }
+    std::string err;
+
+  private:
+    template <class T> T *ptr(const char *name) { return reinterpret_cast<T *>(bufs_.at(name).ptr); }
+    bool has(const char *name) const { return bufs_.count(name) > 0; }
+
+    void alloc(const char *name, size_t bytes, bool zero = false) {
+        Buf &b = bufs_[name];
+        if (b.bytes >= bytes && b.ptr) return;
+        if (b.ptr) { CK(cudaStreamSynchronize(stream_)); CK(cudaFree(b.ptr)); }
+        b.ptr = nullptr;
+        CK(cudaMalloc(&b.ptr, std::max<size_t>(bytes, 256)));
+        b.bytes = bytes;
+        if (zero) CK(cudaMemsetAsync(b.ptr, 0, bytes, stream_));
+    }
+
+    void ensure_points(int n) {
+        if (!has("params")) {
+            alloc("params", sizeof(StepParams));
+            alloc("loss_sum", 256, true);
+            alloc("nan_counts", 64, true);
+            alloc("max_tile", 256, true);
+        }
+        if (n <= cap_points_) return;
+        const size_t m = (size_t)std::max(n, 1);
+        alloc("rec", m * sizeof(SplatRec));
+        alloc("depths", m * 4);
+        alloc("radii", m * 4);
+        alloc("aabb", m * 8);
+        alloc("tiles_hit", m * 4);
+        alloc("grad", m * sizeof(GradRec), true);
+        alloc("v_mean", m * 12);
+        alloc("v_scale", m * 12);
+        alloc("v_quat", m * 16);
+        cap_points_ = n;
+    }
+    void ensure_tiles(int T) {
+        if (T <= cap_tiles_) return;
+        alloc("tile_counts", (size_t)2 * T * 4);
+        alloc("tile_offsets", (size_t)(T + 1) * 4);
+        cap_tiles_ = T;
+    }
+    void ensure_isect(long long c) {
+        if (c <= cap_isect_) return;
+        alloc("keys", (size_t)c * 8);
+        alloc("keys_alt", (size_t)c * 8);
+        alloc("packed", (size_t)c * sizeof(SplatRec));
+        cap_isect_ = c;
+    }
+    void ensure_pixels(long long P) {
+        last_P_ = P;
+        if (P <= cap_pixels_) return;
+        alloc("out_img", (size_t)P * 12);
+        alloc("final_T", (size_t)P * 4);
+        alloc("final_idx", (size_t)P * 4);
+        alloc("hbuf", (size_t)P * 15 * 4);
+        alloc("dbuf", (size_t)P * 9 * 4);
+        alloc("v_img", (size_t)P * 12);
+        cap_pixels_ = P;
+    }
+    void ensure_chunks(long long KP) {
+        if (KP <= cap_chunks_) return;
+        alloc("chunk_T", (size_t)KP * 4);
+        alloc("chunk_C", (size_t)KP * 12);
+        alloc("chunk_idx", (size_t)KP * 4);
+        alloc("prefix_T", (size_t)KP * 4);
+        alloc("after_C", (size_t)KP * 12);
+        cap_chunks_ = KP;
+    }
+
+    // K_max rule, msplat_metal.mm:1204-1224
+    static int choose_k(const MsplatStepArgs &a, int T, long long cap) {
+        if (a.raster_mode == 1) return 1;
+        if (a.raster_mode == 0 && T >= 400) return 1;
+        if (a.k_max > 0) return a.k_max;
+        const uint32_t avg = (uint32_t)(cap / std::max(1, T));
+        const uint32_t cons = avg * 6;
+        uint32_t k = (cons + kChunk - 1) / kChunk;
+        if (k < 2) k = 2;
+        const uint32_t am = (uint32_t)((cap + kChunk - 1) / kChunk);
+        if (k > am) k = am;
+        return (int)k;
+    }
+
+    static void fill_params(const MsplatStepArgs &a, StepParams &sp, bool has_mask) {
+        std::memset(&sp, 0, sizeof(sp));
+        std::memcpy(sp.viewmat, a.viewmat, sizeof(sp.viewmat));
+        std::memcpy(sp.projmat, a.projmat, sizeof(sp.projmat));
+        sp.fx = a.fx; sp.fy = a.fy; sp.cx = a.cx; sp.cy = a.cy;
+        sp.tan_fovx = 0.5f * (float)a.width / a.fx;    // msplat_metal.metal:1771
+        sp.tan_fovy = 0.5f * (float)a.height / a.fy;
+        std::memcpy(sp.cam_pos, a.cam_pos, sizeof(sp.cam_pos));
+        std::memcpy(sp.bg, a.background, sizeof(sp.bg));
+        sp.clip_thresh = a.clip_thresh;
+        sp.degrees_to_use = a.degrees_to_use;
+        sp.ssim_weight = a.ssim_weight;
+        sp.loss_inv_n = a.loss_inv_n;
+        std::memcpy(sp.step_size, a.step_size, sizeof(sp.step_size));
+        std::memcpy(sp.bc2_sqrt, a.bc2_sqrt, sizeof(sp.bc2_sqrt));
+        sp.beta1 = a.beta1; sp.beta2 = a.beta2; sp.eps = a.eps;
+        sp.op_reg = a.op_reg; sp.sc_reg = a.sc_reg; sp.invis_scale = a.invis_scale;
+        sp.seed = a.seed; sp.noise_lr = a.noise_lr; sp.xyz_lr = a.xyz_lr; sp.max_disp = a.max_disp;
+        sp.has_mask = has_mask ? 1 : 0;
+    }
+
+    static void validate(const MsplatGaussians &g, const MsplatStepArgs &a) {
+        if (g.num_points < 0) throw std::runtime_error("num_points < 0");
+        if (a.width <= 0 || a.height <= 0) throw std::runtime_error("image size must be positive");
+        if ((long long)a.width * a.height > (1LL << 31) / 16) throw std::runtime_error("image too large");
+        if (g.rest_bases < 0 || g.rest_bases > 15) throw std::runtime_error("rest_bases must be in [0, 15]");
+        if (g.num_points > 0 && (!g.means || !g.scales || !g.quats || !g.features_dc || !g.opacities ||
+                                 (g.rest_bases > 0 && !g.features_rest)))
+            throw std::runtime_error("null parameter pointer");
+        if (g.num_points > (1 << 26)) throw std::runtime_error("more than 2^26 Gaussians");
+        if (((uintptr_t)g.quats & 15) != 0) throw std::runtime_error("quats must be 16-byte aligned");
+    }
+
+    void mark(int s) {
+        if (timing_) CK(cudaEventRecord(ev_[s], stream_));
+    }
+
+    int device_ = 0, num_sms_ = 1;
+    cudaStream_t stream_ = nullptr;
+    std::map<std::string, Buf> bufs_;
+    int cap_points_ = 0, cap_tiles_ = 0;
+    long long cap_isect_ = 0, cap_pixels_ = 0, cap_chunks_ = 0, last_P_ = 1;
+    int last_T_ = 0, last_K_ = 1;
+    bool timing_ = false;
+    cudaEvent_t ev_[MSPLAT_STAGE_COUNT + 1];
+};
+
+}  // namespace msplat
+
+struct MsplatEngine {
+    msplat::Engine *impl = nullptr;
+    std::string err;
+};
+
+template <class F> static int guarded(MsplatEngine *e, F &&f) {
+    if (!e || !e->impl) return -1;
+    try {
+        f();
+        return 0;
+    } catch (const std::exception &ex) {
+        e->err = ex.what();
+        fprintf(stderr, "msplat engine: %s\n", ex.what());
+        return -2;
+    }
+}
+
+extern "C" {
+
+MsplatEngine *msplat_engine_create(int device, int max_points) {
+    auto *e = new MsplatEngine();
+    try {
+        e->impl = new msplat::Engine(device);
+        if (max_points > 0) e->impl->reserve_points(max_points);
+    } catch (const std::exception &ex) {
+        fprintf(stderr, "msplat engine: %s\n", ex.what());
+        delete e->impl;
+        delete e;
+        return nullptr;
+    }
+    return e;
+}
+
+void msplat_engine_destroy(MsplatEngine *e) {
+    if (!e) return;
+    delete e->impl;
+    delete e;
+}
+
+const char *msplat_engine_last_error(const MsplatEngine *e) { return e ? e->err.c_str() : "null engine"; }
+
+int msplat_engine_train_step(MsplatEngine *e, const MsplatGaussians *g, const MsplatAdamState *st,
+                             const MsplatStepArgs *args, const uint8_t *gt, const uint8_t *mask) {
+    if (!g || !args || !gt) return -1;
+    return guarded(e, [&] { e->impl->train_step(*g, st, *args, gt, mask, true); });
+}
+
+int msplat_engine_render(MsplatEngine *e, const MsplatGaussians *g, const MsplatStepArgs *args) {
+    if (!g || !args) return -1;
+    return guarded(e, [&] { e->impl->train_step(*g, nullptr, *args, nullptr, nullptr, false); });
+}
+
+int msplat_engine_synchronize(MsplatEngine *e) {
+    return guarded(e, [&] { e->impl->synchronize(); });
+}
+
+int msplat_engine_loss(MsplatEngine *e, float *loss) {
+    if (!loss) return -1;
+    return guarded(e, [&] { *loss = e->impl->loss(); });
+}
+
+int msplat_engine_stats(MsplatEngine *e, MsplatEngineStats *out) {
+    if (!out) return -1;
+    return guarded(e, [&] { e->impl->stats(*out); });
+}
+
+int msplat_engine_set_timing(MsplatEngine *e, int enabled) {
+    return guarded(e, [&] { e->impl->set_timing(enabled != 0); });
+}
+
+long long msplat_engine_buffer(MsplatEngine *e, const char *name, void **dev_ptr) {
+    if (!e || !e->impl || !name) return -1;
+    return e->impl->buffer(name, dev_ptr);
+}
+
+int msplat_engine_read(MsplatEngine *e, const char *name, void *dst, long long bytes) {
+    if (!e || !e->impl || !name || !dst) return -1;
+    return guarded(e, [&] {
+        void *p = nullptr;
+        const long long have = e->impl->buffer(name, &p);
+        if (have < 0) throw std::runtime_error(std::string("no buffer ") + name);
+        if (bytes > have) throw std::runtime_error(std::string("read past the end of ") + name);
+        e->impl->synchronize();
+        CK(cudaMemcpy(dst, p, (size_t)bytes, cudaMemcpyDeviceToHost));
+    });
+}
+
+void *msplat_engine_stream(MsplatEngine *e) { return (e && e->impl) ? (void *)e->impl->stream() : nullptr; }
+
+}  // extern "C"

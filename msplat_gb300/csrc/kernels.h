@@ -1,0 +1,102 @@
+// Kernel argument blocks and launchers of the msplat GB300 engine (internal).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace msplat {
+
+struct ProjectArgs {
+    int n, rest_bases, tiles_x, tiles_y;
+    float Wf, Hf;
+    const float *means, *scales, *quats, *features_dc, *features_rest, *opacities;
+    const StepParams *sp;
+    SplatRec *rec;
+    float *depths;
+    int *radii;
+    float2 *aabb;
+    int *tiles_hit;
+    GradRec *grad;          // zeroed here (nullable)
+    unsigned *nan_counts;   // nullable
+};
+
+struct TileArgs {
+    int n, tiles_x, tiles_y, num_tiles;
+    long long capacity;     // intersection slots of keys / packed
+    const int *radii;
+    const float *depths;
+    const SplatRec *rec;
+    const float2 *aabb;
+    uint32_t *tile_counts;  // zeroed before the step
+    uint32_t *tile_write;   // zeroed before the step
+    uint32_t *tile_offsets; // [T+1]
+    uint32_t *max_tile_count;
+    uint64_t *keys, *keys_alt;
+    SplatRec *packed;
+    unsigned *nan_counts;
+};
+
+struct RasterArgs {
+    int width, height, tiles_x, num_tiles, k_max;
+    long long capacity;
+    const StepParams *sp;
+    const uint32_t *tile_offsets;
+    const SplatRec *packed;
+    float *out_img, *final_T;
+    int *final_idx;
+    float *chunk_T, *chunk_C, *prefix_T, *after_C;
+    int *chunk_idx;
+    const float *v_img;
+    GradRec *grad;
+    unsigned *nan_counts;
+};
+
+struct LossArgs {
+    int width, height;
+    const StepParams *sp;
+    const float *img;
+    const uint8_t *gt, *mask;
+    float *hbuf;            // [15, P] channel-planar moments
+    float *dbuf;            // [9, P] horizontally convolved fields
+    float *v_img;           // [P, 3]
+    float *loss_sum;
+    unsigned *nan_counts;
+};
+
+struct ProjectBwdArgs {
+    int n, rest_bases, do_optimizer;
+    float Wf, Hf;
+    const StepParams *sp;
+    const float *means, *scales, *quats;
+    const int *radii;
+    const SplatRec *rec;
+    const GradRec *grad;
+    float *v_mean, *v_scale, *v_quat;
+    float *features_dc, *features_rest, *dc_m, *dc_v, *rest_m, *rest_v;
+    unsigned *nan_counts;
+};
+
+struct AdamArgs {
+    int n;
+    const StepParams *sp;
+    float *means, *scales, *quats, *opacities;
+    float *m[4], *v[4];          // moments of means, scales, quats, opacity
+    const float *g_mean, *g_scale, *g_quat;
+    const GradRec *grad;         // opacity gradient in grad[i].a.z
+    const float *dc_v;           // features_dc second moment (regularizer duty)
+    unsigned *nan_counts;
+};
+
+void launch_project_fwd(const ProjectArgs &a, cudaStream_t s);
+void launch_tiles(const TileArgs &a, cudaStream_t s);
+size_t sort_pack_smem_bytes();
+void launch_raster_fwd(const RasterArgs &a, cudaStream_t s);
+void launch_loss(const LossArgs &a, cudaStream_t s);
+void launch_raster_bwd(const RasterArgs &a, cudaStream_t s);
+void launch_project_bwd(const ProjectBwdArgs &a, cudaStream_t s);
+void launch_adam(const AdamArgs &a, int num_sms, cudaStream_t s);
+void launch_sgld(const AdamArgs &a, cudaStream_t s);
+
+}  // namespace msplat

@@ -1,0 +1,129 @@
+// Optimizer tail of the step:
+//  * one launch of fused Adam over the four flat parameter groups (means,
+//    log-scales, quaternions, opacity logits), with the MCMC opacity/scale
+//    regularizer gradient added in registers (mcmc_reg_grad_kernel +
+//    fused_adam_kernel, msplat_metal.metal:3987-4026 and :1680-1713;
+//    launched as 1 + 4 dispatches by msplat_metal.mm:1454-1488);
+//  * SGLD position noise with the normal samples generated in the same
+//    thread (sgld_noise_gen_kernel + sgld_noise_kernel, :3862-3967).
+#include "common.cuh"
+#include "kernels.h"
+
+namespace msplat {
+
+// Element e of the concatenated groups [means 3N | scales 3N | quats 4N | opacity N].
+__global__ void __launch_bounds__(256) k_adam(AdamArgs a) {
+    const long long n3 = 3LL * a.n, n4 = 4LL * a.n;
+    const long long total = n3 + n3 + n4 + a.n;
+    const StepParams &sp = *a.sp;
+    const float b1 = sp.beta1, b2 = sp.beta2, eps = sp.eps;
+    const bool reg = sp.op_reg > 0.f || sp.sc_reg > 0.f;
+    const float invN_base = 1.0f / (float)a.n;
+    unsigned bad[4] = {0, 0, 0, 0};
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        int grp;
+        long long j;
+        float *p, *m, *v;
+        float g;
+        if (e < n3) { grp = 0; j = e; p = a.means; m = a.m[0]; v = a.v[0]; g = a.g_mean[j]; }
+        else if (e < 2 * n3) { grp = 1; j = e - n3; p = a.scales; m = a.m[1]; v = a.v[1]; g = a.g_scale[j]; }
+        else if (e < 2 * n3 + n4) { grp = 2; j = e - 2 * n3; p = a.quats; m = a.m[2]; v = a.v[2]; g = a.g_quat[j]; }
+        else { grp = 3; j = e - 2 * n3 - n4; p = a.opacities; m = a.m[3]; v = a.v[3]; g = a.grad[j].a.z; }
+        const float pv = p[j];
+        if (reg && (grp == 1 || grp == 3)) {
+            const long long gi = grp == 1 ? j / 3 : j;
+            float duty = 1.0f;
+            if (sp.invis_scale != 1.0f) {
+                const float *dv = a.dc_v + 3 * gi;
+                duty = (dv[0] + dv[1] + dv[2] == 0.0f) ? 1.0f : sp.invis_scale;
+            }
+            const float invN = duty * invN_base;
+            if (grp == 3) {
+                const float sig = 1.0f / (1.0f + det_expf(-pv));
+                g += sp.op_reg * sig * (1.0f - sig) * invN;
+            } else {
+                g += sp.sc_reg * det_expf(fminf(fmaxf(pv, -15.0f), 15.0f)) * (invN * (1.0f / 3.0f));
+            }
+        }
+        if (!finite_bits(g)) { bad[grp]++; continue; }
+        const int sg = grp == 3 ? 5 : grp;
+        const float mm = fmaf(b1, m[j], (1.0f - b1) * g);
+        const float vv = fmaf(b2, v[j], (1.0f - b2) * g * g);
+        p[j] = pv - sp.step_size[sg] * mm / (sqrtf(vv) / sp.bc2_sqrt[sg] + eps);
+        m[j] = mm;
+        v[j] = vv;
+    }
+    if (a.nan_counts) {
+        if (bad[0]) atomicAdd(a.nan_counts + kNanMean, bad[0]);
+        if (bad[1]) atomicAdd(a.nan_counts + kNanScale, bad[1]);
+        if (bad[2]) atomicAdd(a.nan_counts + kNanQuat, bad[2]);
+        if (bad[3]) atomicAdd(a.nan_counts + kNanOpacity, bad[3]);
+    }
+}
+
+__device__ __forceinline__ uint32_t pcg_hash32(uint32_t seed, uint32_t idx) {
+    uint32_t x = seed * 747796405u + idx * 2891336453u;
+    x = ((x >> ((x >> 28) + 4)) ^ x) * 277803737u;
+    return (x >> 22) ^ x;
+}
+__device__ __forceinline__ float pcg_unit(uint32_t h) {
+    return ((float)(h >> 9) + 0.5f) * (1.0f / (float)(1u << 23));
+}
+
+__global__ void __launch_bounds__(256) k_sgld(AdamArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const StepParams &sp = *a.sp;
+    const uint32_t base = (uint32_t)i * 4u;
+    const float u0 = pcg_unit(pcg_hash32(sp.seed, base)), u1 = pcg_unit(pcg_hash32(sp.seed, base + 1u));
+    const float u2 = pcg_unit(pcg_hash32(sp.seed, base + 2u)), u3 = pcg_unit(pcg_hash32(sp.seed, base + 3u));
+    const float r01 = sqrtf(-2.0f * logf(u0)), r23 = sqrtf(-2.0f * logf(u2));
+    const float a01 = 6.283185307179586f * u1, a23 = 6.283185307179586f * u3;
+    const float op = 1.0f / (1.0f + det_expf(-a.opacities[i]));
+    const float wgt = 1.0f / (1.0f + det_expf(-100.0f * ((1.0f - op) - 0.995f)));
+    const float ns = sp.noise_lr * sp.xyz_lr * wgt;
+    const float n0 = r01 * cosf(a01) * ns, n1 = r01 * sinf(a01) * ns, n2 = r23 * cosf(a23) * ns;
+    const float4 q = *reinterpret_cast<const float4 *>(a.quats + 4 * (size_t)i);
+    const float ql = sqrtf(fmaxf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w, 1e-8f));
+    const float qw = q.x / ql, qx = q.y / ql, qy = q.z / ql, qz = q.w / ql;
+    float s[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) s[k] = det_expf(fminf(fmaxf(a.scales[3 * i + k], -15.0f), 15.0f));
+    const float r00 = 1 - 2 * (qy * qy + qz * qz), r01_ = 2 * (qx * qy - qw * qz), r02 = 2 * (qx * qz + qw * qy);
+    const float r10 = 2 * (qx * qy + qw * qz), r11 = 1 - 2 * (qx * qx + qz * qz), r12 = 2 * (qy * qz - qw * qx);
+    const float r20 = 2 * (qx * qz - qw * qy), r21 = 2 * (qy * qz + qw * qx), r22 = 1 - 2 * (qx * qx + qy * qy);
+    float t0 = r00 * n0 + r10 * n1 + r20 * n2;
+    float t1 = r01_ * n0 + r11 * n1 + r21 * n2;
+    float t2 = r02 * n0 + r12 * n1 + r22 * n2;
+    t0 *= s[0] * s[0]; t1 *= s[1] * s[1]; t2 *= s[2] * s[2];
+    float v0 = r00 * t0 + r01_ * t1 + r02 * t2;
+    float v1 = r10 * t0 + r11 * t1 + r12 * t2;
+    float v2 = r20 * t0 + r21 * t1 + r22 * t2;
+    if (!finite_bits(v0) || !finite_bits(v1) || !finite_bits(v2)) return;
+    const float len2 = v0 * v0 + v1 * v1 + v2 * v2;
+    if (!finite_bits(len2)) return;
+    if (len2 > sp.max_disp * sp.max_disp) {
+        const float inv = sp.max_disp / sqrtf(len2);
+        v0 *= inv; v1 *= inv; v2 *= inv;
+    }
+    a.means[3 * i] += v0;
+    a.means[3 * i + 1] += v1;
+    a.means[3 * i + 2] += v2;
+}
+
+void launch_adam(const AdamArgs &a, int num_sms, cudaStream_t s) {
+    if (a.n <= 0) return;
+    const long long total = 11LL * a.n;
+    long long blocks = (total + 255) / 256;
+    const long long cap = (long long)num_sms * 8;
+    if (blocks > cap) blocks = cap;
+    k_adam<<<(unsigned)blocks, 256, 0, s>>>(a);
+}
+
+void launch_sgld(const AdamArgs &a, cudaStream_t s) {
+    if (a.n <= 0) return;
+    k_sgld<<<(a.n + 255) / 256, 256, 0, s>>>(a);
+}
+
+}  // namespace msplat

@@ -1,0 +1,178 @@
+// Fused EWA projection + spherical-harmonics colour, one thread per Gaussian.
+// Follows project_and_sh_forward_kernel (msplat_metal.metal:1719-1834) and its
+// helpers (:53-344, :620-687).  Built with --fmad=false: every float operation
+// is rounded on its own, in the order the reference writes it, so radii, tile
+// rectangles and depths (and therefore the tile lists) are bit-identical to
+// the oracle's float path.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace msplat {
+
+__constant__ float kShC0 = 0.28209479177387814f;
+__constant__ float kShC1 = 0.4886025119029199f;
+__constant__ float kShC2[5] = {1.0925484305920792f, -1.0925484305920792f, 0.31539156525252005f,
+                               -1.0925484305920792f, 0.5462742152960396f};
+__constant__ float kShC3[7] = {-0.5900435899266435f, 2.890611442640554f, -0.4570457994644658f,
+                               0.3731763325901154f, -0.4570457994644658f, 1.445305721320277f,
+                               -0.5900435899266435f};
+
+__global__ void __launch_bounds__(256) k_project_fwd(ProjectArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const StepParams &sp = *a.sp;
+    // the rasterizer gradient record of every Gaussian starts the step at zero
+    if (a.grad) {
+        a.grad[i].a = make_float4(0.f, 0.f, 0.f, 0.f);
+        a.grad[i].b = make_float4(0.f, 0.f, 0.f, 0.f);
+        a.grad[i].c = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    a.radii[i] = 0;
+    a.tiles_hit[i] = 0;
+
+    const float px = a.means[3 * i], py = a.means[3 * i + 1], pz = a.means[3 * i + 2];
+    const float *v = sp.viewmat;
+    // transform_4x3 + clip_near_plane
+    const float vx = v[0] * px + v[1] * py + v[2] * pz + v[3];
+    const float vy = v[4] * px + v[5] * py + v[6] * pz + v[7];
+    const float vz = v[8] * px + v[9] * py + v[10] * pz + v[11];
+    if (vz <= sp.clip_thresh) return;
+
+    // exp_scale_clamped + quat_to_rotmat + scale_rot_to_cov3d (in registers)
+    float s[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) s[k] = det_expf(fminf(fmaxf(a.scales[3 * i + k], -15.f), 15.f));
+    const float4 q = *reinterpret_cast<const float4 *>(a.quats + 4 * (size_t)i);
+    const float qn = 1.0f / sqrtf(fmaxf(q.w * q.w + q.x * q.x + q.y * q.y + q.z * q.z, 1e-8f));
+    const float w = q.x * qn, x = q.y * qn, y = q.z * qn, z = q.w * qn;
+    float R[3][3];
+    R[0][0] = 1.f - 2.f * (y * y + z * z);
+    R[1][0] = 2.f * (x * y + w * z);
+    R[2][0] = 2.f * (x * z - w * y);
+    R[0][1] = 2.f * (x * y - w * z);
+    R[1][1] = 1.f - 2.f * (x * x + z * z);
+    R[2][1] = 2.f * (y * z + w * x);
+    R[0][2] = 2.f * (x * z + w * y);
+    R[1][2] = 2.f * (y * z - w * x);
+    R[2][2] = 1.f - 2.f * (x * x + y * y);
+    float M[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) M[r][c] = R[r][c] * s[c];
+    const float c00 = M[0][0] * M[0][0] + M[0][1] * M[0][1] + M[0][2] * M[0][2];
+    const float c01 = M[0][0] * M[1][0] + M[0][1] * M[1][1] + M[0][2] * M[1][2];
+    const float c02 = M[0][0] * M[2][0] + M[0][1] * M[2][1] + M[0][2] * M[2][2];
+    const float c11 = M[1][0] * M[1][0] + M[1][1] * M[1][1] + M[1][2] * M[1][2];
+    const float c12 = M[1][0] * M[2][0] + M[1][1] * M[2][1] + M[1][2] * M[2][2];
+    const float c22 = M[2][0] * M[2][0] + M[2][1] * M[2][1] + M[2][2] * M[2][2];
+
+    // project_cov3d_ewa
+    const float lim_x = 1.3f * sp.tan_fovx, lim_y = 1.3f * sp.tan_fovy;
+    const float cvx = vz * fminf(lim_x, fmaxf(-lim_x, vx / vz));
+    const float cvy = vz * fminf(lim_y, fmaxf(-lim_y, vy / vz));
+    const float rz = 1.f / vz, rz2 = rz * rz;
+    const float j00 = sp.fx * rz, j11 = sp.fy * rz;
+    const float j20 = -sp.fx * cvx * rz2, j21 = -sp.fy * cvy * rz2;
+    const float t0x = j00 * v[0] + j20 * v[8], t0y = j00 * v[1] + j20 * v[9], t0z = j00 * v[2] + j20 * v[10];
+    const float t1x = j11 * v[4] + j21 * v[8], t1y = j11 * v[5] + j21 * v[9], t1z = j11 * v[6] + j21 * v[10];
+    const float tv0x = t0x * c00 + t0y * c01 + t0z * c02;
+    const float tv0y = t0x * c01 + t0y * c11 + t0z * c12;
+    const float tv0z = t0x * c02 + t0y * c12 + t0z * c22;
+    const float tv1x = t1x * c00 + t1y * c01 + t1z * c02;
+    const float tv1y = t1x * c01 + t1y * c11 + t1z * c12;
+    const float tv1z = t1x * c02 + t1y * c12 + t1z * c22;
+    const float a2 = (tv0x * t0x + tv0y * t0y + tv0z * t0z) + 0.3f;
+    const float b2 = tv0x * t1x + tv0y * t1y + tv0z * t1z;
+    const float d2 = (tv1x * t1x + tv1y * t1y + tv1z * t1z) + 0.3f;
+
+    // compute_cov2d_bounds
+    const float det = a2 * d2 - b2 * b2;
+    if (!(det > 1e-6f)) return;
+    const float inv_det = 1.f / det;
+    const float ca = d2 * inv_det, cb = -b2 * inv_det, cc = a2 * inv_det;
+    const float bm = 0.5f * (a2 + d2);
+    const float disc = sqrtf(fmaxf(0.1f, bm * bm - det));
+    const float radius = ceilf(3.f * sqrtf(bm + disc));
+
+    // project_pix + ndc2pix
+    const float *m = sp.projmat;
+    const float hx = m[0] * px + m[1] * py + m[2] * pz + m[3];
+    const float hy = m[4] * px + m[5] * py + m[6] * pz + m[7];
+    const float hw = m[12] * px + m[13] * py + m[14] * pz + m[15];
+    const float rw = 1.f / (hw + 1e-6f);
+    const float ndx = hx * rw, ndy = hy * rw;
+    const float cxp = 0.5f * a.Wf * ndx + sp.cx - 0.5f;
+    const float cyp = 0.5f * a.Hf * ndy + sp.cy - 0.5f;
+    const float ax = ceilf(3.f * sqrtf(a2)), ay = ceilf(3.f * sqrtf(d2));
+    int x0, y0, x1, y1;
+    tile_rect(cxp, cyp, ax, ay, a.tiles_x, a.tiles_y, x0, y0, x1, y1);
+    const int area = (x1 - x0) * (y1 - y0);
+    if (area <= 0) return;
+
+    // SH colour (degrees_to_use bands) from the normalised view direction
+    const float dx = px - sp.cam_pos[0], dy = py - sp.cam_pos[1], dz = pz - sp.cam_pos[2];
+    const float inv = 1.f / sqrtf(dx * dx + dy * dy + dz * dz);
+    const float vdx = dx * inv, vdy = dy * inv, vdz = dz * inv;
+    const int deg = sp.degrees_to_use;
+    const float *dc = a.features_dc + 3 * (size_t)i;
+    const float *rest = a.features_rest + (size_t)a.rest_bases * 3 * i;
+    const float xx = vdx * vdx, xy = vdx * vdy, xz = vdx * vdz, yy = vdy * vdy, yz = vdy * vdz, zz = vdz * vdz;
+    float col[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        float val = kShC0 * dc[c];
+        if (deg >= 1) {
+            val += kShC1 * (-vdy * rest[0 * 3 + c] + vdz * rest[1 * 3 + c] - vdx * rest[2 * 3 + c]);
+            if (deg >= 2) {
+                val += (kShC2[0] * xy * rest[3 * 3 + c] + kShC2[1] * yz * rest[4 * 3 + c] +
+                        kShC2[2] * (2.f * zz - xx - yy) * rest[5 * 3 + c] + kShC2[3] * xz * rest[6 * 3 + c] +
+                        kShC2[4] * (xx - yy) * rest[7 * 3 + c]);
+                if (deg >= 3) {
+                    val += (kShC3[0] * vdy * (3.f * xx - yy) * rest[8 * 3 + c] + kShC3[1] * xy * vdz * rest[9 * 3 + c] +
+                            kShC3[2] * vdy * (4.f * zz - xx - yy) * rest[10 * 3 + c] +
+                            kShC3[3] * vdz * (2.f * zz - 3.f * xx - 3.f * yy) * rest[11 * 3 + c] +
+                            kShC3[4] * vdx * (4.f * zz - xx - yy) * rest[12 * 3 + c] +
+                            kShC3[5] * vdz * (xx - yy) * rest[13 * 3 + c] +
+                            kShC3[6] * vdx * (xx - 3.f * yy) * rest[14 * 3 + c]);
+                }
+            }
+        }
+        col[c] = val;
+    }
+    // sigmoid(opacity) once per Gaussian (the reference does it per
+    // intersection at pack time; same input, same bits)
+    const float opac = 1.f / (1.f + det_expf(-a.opacities[i]));
+
+    SplatRec rec;
+    rec.a = make_float4(cxp, cyp, opac, 0.f);
+    rec.b = make_float4(ca, cb, cc, 0.f);
+    rec.c = make_float4(col[0], col[1], col[2], 0.f);
+    a.rec[i] = rec;
+    a.depths[i] = vz;
+    a.aabb[i] = make_float2(ax, ay);
+
+    // zombie gate: a non-finite projection output culls the Gaussian this step
+    const bool okc = finite_bits(cxp) && finite_bits(cyp), okd = finite_bits(vz);
+    const bool oka = finite_bits(ax) && finite_bits(ay);
+    const bool okn = finite_bits(ca) && finite_bits(cb) && finite_bits(cc);
+    const bool okr = finite_bits(col[0]) && finite_bits(col[1]) && finite_bits(col[2]);
+    if (okc && okd && oka && okn && okr) {
+        a.tiles_hit[i] = area;
+        a.radii[i] = __float2int_rz(radius);
+    } else if (a.nan_counts) {
+        atomicAdd(a.nan_counts + kNanProj, 1u);
+        if (!okc) atomicAdd(a.nan_counts + kNanProjCenter, 1u);
+        if (!okd) atomicAdd(a.nan_counts + kNanProjDepth, 1u);
+        if (!oka) atomicAdd(a.nan_counts + kNanProjAabb, 1u);
+        if (!okn) atomicAdd(a.nan_counts + kNanProjConic, 1u);
+        if (!okr) atomicAdd(a.nan_counts + kNanProjRgb, 1u);
+    }
+}
+
+void launch_project_fwd(const ProjectArgs &a, cudaStream_t s) {
+    if (a.n <= 0) return;
+    k_project_fwd<<<(a.n + 255) / 256, 256, 0, s>>>(a);
+}
+
+}  // namespace msplat

@@ -1,0 +1,250 @@
+// Back-to-front rasterizer VJP w.r.t. splat centre, conic, raw colour and
+// opacity logit.  One CTA per 16x16 tile (chunked: per (tile, chunk)), one
+// thread per pixel.  Per splat each warp reduces its pixels' 9 partial
+// gradients with a transpose-reduce (9 shuffles for 8 values plus 5 for the
+// ninth, instead of 45), warps combine through shared-memory adds, and each
+// batch flushes one set of three float4 vector atomics per (splat, tile)
+// instead of the reference's nine scalar atomics per (splat, warp).
+// Follows rasterize_backward_kernel (msplat_metal.metal:931-1135),
+// compute_chunk_prefix_suffix_kernel (:3139-3175) and
+// rasterize_backward_chunked_kernel (:3179-3366), including its quirk that a
+// splat whose alpha was clamped to 0.999 gets no gradient and leaves the
+// transmittance unchanged (:1085).
+#include "common.cuh"
+#include "kernels.h"
+
+namespace msplat {
+
+constexpr int kBB = kTileThreads;   // splats per batch
+
+struct BwdSmem {
+    float4 xyo[kBB];    // x, y, opacity, id bits
+    float4 con[kBB];
+    float4 rgb[kBB];    // raw colour
+    float acc[kBB][9];  // r g b | ca cb cc | x y | opacity
+    int wmax[8];
+};
+
+// Sum of 8 per-lane values over the warp: lane 4*j ends with the total of v[j].
+__device__ __forceinline__ float transpose_reduce8(float v[8], int lane) {
+    const bool b16 = lane & 16, b8 = lane & 8, b4 = lane & 4;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const float send = b16 ? v[j] : v[j + 4];
+        const float keep = b16 ? v[j + 4] : v[j];
+        v[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+        const float send = b8 ? v[j] : v[j + 2];
+        const float keep = b8 ? v[j + 2] : v[j];
+        v[j] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
+    {
+        const float send = b4 ? v[0] : v[1];
+        const float keep = b4 ? v[1] : v[0];
+        v[0] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    }
+    v[0] += __shfl_xor_sync(0xffffffffu, v[0], 2);
+    v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+    return v[0];
+}
+
+struct PixelState {
+    float T, br, bg, bb;      // transmittance, colour behind (buffer)
+    float tfr, tfg, tfb;      // T_final * background
+    float vr, vg, vb;         // dL/dpixel
+    float px, py;
+    int bin_final;            // last splat index this pixel may take gradient from (-1: none)
+};
+
+// Processes splat indices [s, hi] back to front for the whole CTA.
+__device__ void backward_range(BwdSmem &sm, const SplatRec *pk, int s, int hi, PixelState &ps, GradRec *grad) {
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int wbin = __reduce_max_sync(0xffffffffu, ps.bin_final);
+    for (int batch_end = hi; batch_end >= s; batch_end -= kBB) {
+        __syncthreads();
+        const int idx = batch_end - tid;
+        if (idx >= s) {
+            const SplatRec r = pk[idx];
+            sm.xyo[tid] = r.a;
+            sm.con[tid] = r.b;
+            sm.rgb[tid] = r.c;
+        }
+#pragma unroll
+        for (int k = 0; k < 9; k++) sm.acc[tid][k] = 0.f;
+        __syncthreads();
+        const int nb = min(kBB, batch_end - s + 1);
+        for (int t = max(0, batch_end - wbin); t < nb; t++) {
+            const int sidx = batch_end - t;
+            const float4 xo = sm.xyo[t];
+            const float4 cn = sm.con[t];
+            bool valid = sidx <= ps.bin_final;
+            float dx = 0.f, dy = 0.f, alpha = 0.f;
+            if (valid) {
+                dx = xo.x - ps.px;
+                dy = xo.y - ps.py;
+                const float sigma = __fmaf_rn(0.5f, __fmaf_rn(cn.x, dx * dx, cn.z * dy * dy), cn.y * dx * dy);
+                if (!finite_bits(sigma) || sigma < 0.f || sigma >= 5.55f) {
+                    valid = false;
+                } else {
+                    alpha = fminf(0.999f, xo.z * det_expf(-sigma));
+                    if (alpha < 1.f / 255.f) valid = false;
+                }
+            }
+            if (!__any_sync(0xffffffffu, valid)) continue;
+            float v[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            float vop = 0.f;
+            if (valid && alpha < 0.999f) {
+                const float4 rc = sm.rgb[t];
+                const float ra = 1.f / (1.f - alpha);
+                ps.T *= ra;
+                const float fac = alpha * ps.T;
+                const float cr = fmaxf(rc.x + 0.5f, 0.f), cg = fmaxf(rc.y + 0.5f, 0.f), cbl = fmaxf(rc.z + 0.5f, 0.f);
+                const float ar = __fmaf_rn(cr, ps.T, __fmaf_rn(-ps.br, ra, -ra * ps.tfr));
+                const float ag = __fmaf_rn(cg, ps.T, __fmaf_rn(-ps.bg, ra, -ra * ps.tfg));
+                const float ab = __fmaf_rn(cbl, ps.T, __fmaf_rn(-ps.bb, ra, -ra * ps.tfb));
+                const float v_alpha = ar * ps.vr + ag * ps.vg + ab * ps.vb;
+                ps.br = __fmaf_rn(cr, fac, ps.br);
+                ps.bg = __fmaf_rn(cg, fac, ps.bg);
+                ps.bb = __fmaf_rn(cbl, fac, ps.bb);
+                const float v_sigma = -alpha * v_alpha;
+                const float hv = 0.5f * v_sigma;
+                v[0] = fac * ps.vr;
+                v[1] = fac * ps.vg;
+                v[2] = fac * ps.vb;
+                v[3] = hv * (dx * dx);
+                v[4] = hv * (dx * dy);
+                v[5] = hv * (dy * dy);
+                v[6] = v_sigma * __fmaf_rn(cn.x, dx, cn.y * dy);
+                v[7] = v_sigma * __fmaf_rn(cn.y, dx, cn.z * dy);
+                vop = -v_sigma * (1.f - xo.z);
+            }
+            const float s8 = transpose_reduce8(v, lane);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) vop += __shfl_xor_sync(0xffffffffu, vop, o);
+            if ((lane & 3) == 0) atomicAdd(&sm.acc[t][lane >> 2], s8);
+            if (lane == 1) atomicAdd(&sm.acc[t][8], vop);
+        }
+        __syncthreads();
+        if (tid < nb) {
+            const float *g = sm.acc[tid];
+            const float4 rc = sm.rgb[tid];
+            const float gr = (rc.x + 0.5f >= 0.f) ? g[0] : 0.f;
+            const float gg = (rc.y + 0.5f >= 0.f) ? g[1] : 0.f;
+            const float gb = (rc.z + 0.5f >= 0.f) ? g[2] : 0.f;
+            const bool any = (gr != 0.f) | (gg != 0.f) | (gb != 0.f) | (g[3] != 0.f) | (g[4] != 0.f) |
+                             (g[5] != 0.f) | (g[6] != 0.f) | (g[7] != 0.f) | (g[8] != 0.f);
+            if (any) {
+                GradRec *dst = grad + __float_as_int(sm.xyo[tid].w);
+                atomic_add_f4(&dst->a, make_float4(g[6], g[7], g[8], 0.f));
+                atomic_add_f4(&dst->b, make_float4(g[3], g[4], g[5], 0.f));
+                atomic_add_f4(&dst->c, make_float4(gr, gg, gb, 0.f));
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ int block_max(int v, int *wmax) {
+    const int w = __reduce_max_sync(0xffffffffu, v);
+    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = w;
+    __syncthreads();
+    int m = wmax[0];
+#pragma unroll
+    for (int k = 1; k < kTileThreads / 32; k++) m = max(m, wmax[k]);
+    __syncthreads();
+    return m;
+}
+
+__device__ __forceinline__ void init_pixel(PixelState &ps, const RasterArgs &a, int x, int y, bool inside, float T0) {
+    const StepParams &sp = *a.sp;
+    const int p = inside ? y * a.width + x : 0;
+    const float Tf = inside ? a.final_T[p] : 0.f;
+    ps.T = T0;
+    ps.br = ps.bg = ps.bb = 0.f;
+    ps.tfr = Tf * sp.bg[0];
+    ps.tfg = Tf * sp.bg[1];
+    ps.tfb = Tf * sp.bg[2];
+    ps.vr = inside ? a.v_img[3 * p] : 0.f;
+    ps.vg = inside ? a.v_img[3 * p + 1] : 0.f;
+    ps.vb = inside ? a.v_img[3 * p + 2] : 0.f;
+    ps.px = (float)x;
+    ps.py = (float)y;
+}
+
+__global__ void __launch_bounds__(kTileThreads) k_raster_bwd(RasterArgs a) {
+    __shared__ BwdSmem sm;
+    const int tile = blockIdx.x;
+    const int tx = tile % a.tiles_x, ty = tile / a.tiles_x;
+    const int x = tx * kTile + (threadIdx.x & 15), y = ty * kTile + (threadIdx.x >> 4);
+    const bool inside = x < a.width && y < a.height;
+    const int s = clamp_off(a.tile_offsets[tile], a.capacity), e = clamp_off(a.tile_offsets[tile + 1], a.capacity);
+    if (s >= e) return;
+    PixelState ps;
+    const float Tf = inside ? a.final_T[y * a.width + x] : 0.f;
+    init_pixel(ps, a, x, y, inside, Tf);
+    ps.bin_final = inside ? a.final_idx[y * a.width + x] : -1;
+    const int hi = min(e - 1, block_max(ps.bin_final, sm.wmax));
+    if (hi < s) return;
+    backward_range(sm, a.packed, s, hi, ps, a.grad);
+}
+
+__global__ void __launch_bounds__(256) k_chunk_prefix_suffix(RasterArgs a) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int P = a.width * a.height;
+    if (p >= P) return;
+    float pT = 1.f;
+    for (int k = 0; k < a.k_max; k++) {
+        const size_t o = (size_t)k * P + p;
+        a.prefix_T[o] = pT;
+        pT *= a.chunk_T[o];
+    }
+    float r = 0.f, g = 0.f, b = 0.f;
+    for (int k = a.k_max - 1; k >= 0; k--) {
+        const size_t o = (size_t)k * P + p;
+        a.after_C[3 * o] = r;
+        a.after_C[3 * o + 1] = g;
+        a.after_C[3 * o + 2] = b;
+        const float t = a.prefix_T[o];
+        r += t * a.chunk_C[3 * o];
+        g += t * a.chunk_C[3 * o + 1];
+        b += t * a.chunk_C[3 * o + 2];
+    }
+}
+
+__global__ void __launch_bounds__(kTileThreads) k_raster_bwd_chunked(RasterArgs a) {
+    __shared__ BwdSmem sm;
+    const int tile = blockIdx.x, k = blockIdx.y;
+    const int tx = tile % a.tiles_x, ty = tile / a.tiles_x;
+    const int x = tx * kTile + (threadIdx.x & 15), y = ty * kTile + (threadIdx.x >> 4);
+    const bool inside = x < a.width && y < a.height;
+    const int s0 = clamp_off(a.tile_offsets[tile], a.capacity), e0 = clamp_off(a.tile_offsets[tile + 1], a.capacity);
+    const int cs = s0 + k * kChunk, ce = min(s0 + (k + 1) * kChunk, e0);
+    if (cs >= ce) return;
+    const size_t P = (size_t)a.width * a.height;
+    const size_t o = (size_t)k * P + (inside ? (size_t)y * a.width + x : 0);
+    PixelState ps;
+    init_pixel(ps, a, x, y, inside, inside ? a.prefix_T[o] * a.chunk_T[o] : 0.f);
+    if (inside) {
+        ps.br = a.after_C[3 * o];
+        ps.bg = a.after_C[3 * o + 1];
+        ps.bb = a.after_C[3 * o + 2];
+    }
+    const int bf = inside ? a.chunk_idx[o] : -1;
+    ps.bin_final = (bf >= cs) ? bf : -1;
+    const int hi = min(ce - 1, block_max(ps.bin_final, sm.wmax));
+    if (hi < cs) return;
+    backward_range(sm, a.packed, cs, hi, ps, a.grad);
+}
+
+void launch_raster_bwd(const RasterArgs &a, cudaStream_t s) {
+    if (a.k_max <= 1) {
+        k_raster_bwd<<<a.num_tiles, kTileThreads, 0, s>>>(a);
+    } else {
+        const int P = a.width * a.height;
+        k_chunk_prefix_suffix<<<(P + 255) / 256, 256, 0, s>>>(a);
+        k_raster_bwd_chunked<<<dim3(a.num_tiles, a.k_max), kTileThreads, 0, s>>>(a);
+    }
+}
+
+}  // namespace msplat

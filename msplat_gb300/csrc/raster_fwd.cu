@@ -1,0 +1,164 @@
+// Front-to-back alpha compositing.  Monolithic: one CTA per 16x16 tile, one
+// thread per pixel, splats staged through shared memory in batches of 256
+// (coalesced 16-byte loads of the packed records); the CTA leaves as soon as
+// every pixel has saturated.  Chunked: one CTA per (tile, 512-splat depth
+// chunk) with chunk-local transmittance, then a per-pixel merge.
+// Follows nd_rasterize_forward_kernel (msplat_metal.metal:499-618),
+// rasterize_forward_chunked_kernel (:2960-3076) and
+// rasterize_forward_merge_kernel (:3081-3134).  Built with --fmad=false; the
+// per-pixel arithmetic is the reference's, fused only where it writes fma(),
+// so the image is bit-identical to the oracle's float path.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace msplat {
+
+struct BatchSmem {
+    float4 xyo[kTileThreads];   // x, y, opacity
+    float4 con[kTileThreads];   // conic
+    float4 rgb[kTileThreads];   // clamped colour max(raw + 0.5, 0)
+};
+
+__device__ __forceinline__ void load_batch(BatchSmem &sm, const SplatRec *pk, int idx, int end) {
+    const int t = threadIdx.x;
+    if (idx < end) {
+        const SplatRec r = pk[idx];
+        sm.xyo[t] = r.a;
+        sm.con[t] = r.b;
+        sm.rgb[t] = make_float4(fmaxf(r.c.x + 0.5f, 0.f), fmaxf(r.c.y + 0.5f, 0.f), fmaxf(r.c.z + 0.5f, 0.f), 0.f);
+    }
+}
+
+// Walks [s, e) for this pixel; the whole CTA iterates together.
+// done: in/out per-thread flag; returns (T, C, last).
+__device__ __forceinline__ void composite_range(BatchSmem &sm, const SplatRec *pk, int s, int e, float px, float py,
+                                                bool done, float &T, float3 &C, int &last, unsigned *nan_sigma) {
+    T = 1.f;
+    C = make_float3(0.f, 0.f, 0.f);
+    last = s - 1;
+    for (int b0 = s; b0 < e; b0 += kTileThreads) {
+        if (__syncthreads_count(done) == kTileThreads) break;
+        load_batch(sm, pk, b0 + (int)threadIdx.x, e);
+        __syncthreads();
+        if (done) continue;
+        const int nb = min(kTileThreads, e - b0);
+        for (int t = 0; t < nb; t++) {
+            const float4 xo = sm.xyo[t];
+            const float4 cn = sm.con[t];
+            const float dx = xo.x - px, dy = xo.y - py;
+            const float sigma = __fmaf_rn(0.5f, __fmaf_rn(cn.x, dx * dx, cn.z * dy * dy), cn.y * dx * dy);
+            if (!finite_bits(sigma)) {
+                if (nan_sigma) atomicAdd(nan_sigma, 1u);
+                continue;
+            }
+            if (sigma < 0.f || sigma >= 5.55f) continue;
+            const float alpha = fminf(0.999f, xo.z * det_expf(-sigma));
+            if (alpha < 1.f / 255.f) continue;
+            const float nT = T * (1.f - alpha);
+            if (nT <= 1e-4f) {
+                last = b0 + t - 1;
+                done = true;
+                break;
+            }
+            const float vis = alpha * T;
+            const float4 c = sm.rgb[t];
+            C.x = __fmaf_rn(c.x, vis, C.x);
+            C.y = __fmaf_rn(c.y, vis, C.y);
+            C.z = __fmaf_rn(c.z, vis, C.z);
+            T = nT;
+            last = b0 + t;
+        }
+    }
+}
+
+__device__ __forceinline__ float sat01(float x) { return fminf(fmaxf(x, 0.f), 1.f); }
+
+__global__ void __launch_bounds__(kTileThreads) k_raster_fwd(RasterArgs a) {
+    __shared__ BatchSmem sm;
+    const int tile = blockIdx.x;
+    const int tx = tile % a.tiles_x, ty = tile / a.tiles_x;
+    const int x = tx * kTile + (threadIdx.x & 15), y = ty * kTile + (threadIdx.x >> 4);
+    const bool inside = x < a.width && y < a.height;
+    const int s = clamp_off(a.tile_offsets[tile], a.capacity), e = clamp_off(a.tile_offsets[tile + 1], a.capacity);
+    float T;
+    float3 C;
+    int last;
+    composite_range(sm, a.packed, s, e, (float)x, (float)y, !inside, T, C, last, nullptr);
+    if (!inside) return;
+    const int p = y * a.width + x;
+    const StepParams &sp = *a.sp;
+    a.final_T[p] = T;
+    a.final_idx[p] = last;
+    a.out_img[3 * p + 0] = sat01(__fmaf_rn(sp.bg[0], T, C.x));
+    a.out_img[3 * p + 1] = sat01(__fmaf_rn(sp.bg[1], T, C.y));
+    a.out_img[3 * p + 2] = sat01(__fmaf_rn(sp.bg[2], T, C.z));
+}
+
+__global__ void __launch_bounds__(kTileThreads) k_raster_fwd_chunked(RasterArgs a) {
+    __shared__ BatchSmem sm;
+    const int tile = blockIdx.x, k = blockIdx.y;
+    const int tx = tile % a.tiles_x, ty = tile / a.tiles_x;
+    const int x = tx * kTile + (threadIdx.x & 15), y = ty * kTile + (threadIdx.x >> 4);
+    const bool inside = x < a.width && y < a.height;
+    const int s0 = clamp_off(a.tile_offsets[tile], a.capacity), e0 = clamp_off(a.tile_offsets[tile + 1], a.capacity);
+    const int cs = s0 + k * kChunk, ce = min(s0 + (k + 1) * kChunk, e0);
+    const size_t P = (size_t)a.width * a.height;
+    const size_t o = (size_t)k * P + (size_t)y * a.width + x;
+    if (cs >= ce) {
+        if (inside) {
+            a.chunk_T[o] = 1.f;
+            a.chunk_C[3 * o] = a.chunk_C[3 * o + 1] = a.chunk_C[3 * o + 2] = 0.f;
+            a.chunk_idx[o] = -1;
+        }
+        return;
+    }
+    float T;
+    float3 C;
+    int last;
+    composite_range(sm, a.packed, cs, ce, (float)x, (float)y, !inside, T, C, last,
+                    a.nan_counts ? a.nan_counts + kNanRasterSigma : nullptr);
+    if (!inside) return;
+    a.chunk_T[o] = T;
+    a.chunk_C[3 * o] = C.x;
+    a.chunk_C[3 * o + 1] = C.y;
+    a.chunk_C[3 * o + 2] = C.z;
+    a.chunk_idx[o] = last;
+}
+
+__global__ void __launch_bounds__(256) k_raster_merge(RasterArgs a) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int P = a.width * a.height;
+    if (p >= P) return;
+    float Tr = 1.f, cr = 0.f, cg = 0.f, cb = 0.f;
+    int last = -1, cut = a.k_max;
+    for (int k = 0; k < a.k_max; k++) {
+        const size_t o = (size_t)k * P + p;
+        const int cf = a.chunk_idx[o];
+        if (cf < 0 && k > 0) break;
+        cr = __fmaf_rn(a.chunk_C[3 * o], Tr, cr);
+        cg = __fmaf_rn(a.chunk_C[3 * o + 1], Tr, cg);
+        cb = __fmaf_rn(a.chunk_C[3 * o + 2], Tr, cb);
+        Tr = Tr * a.chunk_T[o];
+        if (cf >= 0) last = cf;
+        if (Tr <= 1e-4f) { cut = k + 1; break; }
+    }
+    for (int k = cut; k < a.k_max; k++) a.chunk_idx[(size_t)k * P + p] = -1;
+    const StepParams &sp = *a.sp;
+    a.final_T[p] = Tr;
+    a.final_idx[p] = last;
+    a.out_img[3 * p + 0] = sat01(__fmaf_rn(sp.bg[0], Tr, cr));
+    a.out_img[3 * p + 1] = sat01(__fmaf_rn(sp.bg[1], Tr, cg));
+    a.out_img[3 * p + 2] = sat01(__fmaf_rn(sp.bg[2], Tr, cb));
+}
+
+void launch_raster_fwd(const RasterArgs &a, cudaStream_t s) {
+    if (a.k_max <= 1) {
+        k_raster_fwd<<<a.num_tiles, kTileThreads, 0, s>>>(a);
+    } else {
+        k_raster_fwd_chunked<<<dim3(a.num_tiles, a.k_max), kTileThreads, 0, s>>>(a);
+        const int P = a.width * a.height;
+        k_raster_merge<<<(P + 255) / 256, 256, 0, s>>>(a);
+    }
+}
+
+}  // namespace msplat

@@ -1,0 +1,210 @@
+// Training loss L = w * (1 - mean SSIM) + (1 - w) * mean |x - gt| and its
+// image gradient, as three separable passes over 16x16 pixel tiles:
+//   1. horizontal 11-tap moments of (gt, x, gt^2, x^2, gt*x), zero padding
+//   2. vertical moments -> SSIM, L1, loss sum and the derivative fields
+//      (f1, f2, f3), then the horizontal transpose convolution of the fields
+//   3. vertical transpose convolution -> dL/dx
+// Follows ssim_h_fwd_kernel, ssim_fused_v_fwd_h_bwd_kernel and
+// ssim_v_bwd_kernel (msplat_metal.metal:3388-3450, 3563-3681, 3764-3850),
+// including their treatment of window centres in the out-of-image columns a
+// border tile reaches (fields from zero moments).  Intermediates are stored
+// channel-planar so every tile load and store is coalesced.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace msplat {
+
+__constant__ float kGauss[11];
+constexpr float kC1 = 0.0001f, kC2 = 0.0009f;
+constexpr int kS = 16, kHalo = 5, kSpan = kS + 2 * kHalo;   // 26
+
+__global__ void __launch_bounds__(256) k_ssim_h(LossArgs a) {
+    __shared__ float sg[3][kS][kSpan], sr[3][kS][kSpan];
+    const int W = a.width, H = a.height;
+    const int bx = blockIdx.x * kS - kHalo, by = blockIdx.y * kS;
+    const int tid = threadIdx.x;
+    for (int i = tid; i < kS * kSpan; i += 256) {
+        const int sy = i / kSpan, sx = i % kSpan;
+        const int gy = by + sy, gx = bx + sx;
+        const bool in = gx >= 0 && gx < W && gy < H;
+        const size_t p = in ? ((size_t)gy * W + gx) : 0;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            sg[c][sy][sx] = in ? (float)a.gt[3 * p + c] * (1.0f / 255.0f) : 0.f;
+            sr[c][sy][sx] = in ? a.img[3 * p + c] : 0.f;
+        }
+    }
+    __syncthreads();
+    const int lx = tid & 15, ly = tid >> 4;
+    const int x = blockIdx.x * kS + lx, y = by + ly;
+    if (x >= W || y >= H) return;
+    const size_t P = (size_t)W * H, p = (size_t)y * W + x;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        float mx = 0.f, my = 0.f, sx = 0.f, sy = 0.f, cr = 0.f;
+#pragma unroll
+        for (int d = 0; d < 11; d++) {
+            const float w = kGauss[d], g = sg[c][ly][lx + d], r = sr[c][ly][lx + d];
+            mx += w * g; my += w * r; sx += w * g * g; sy += w * r * r; cr += w * g * r;
+        }
+        a.hbuf[(c * 5 + 0) * P + p] = mx;
+        a.hbuf[(c * 5 + 1) * P + p] = my;
+        a.hbuf[(c * 5 + 2) * P + p] = sx;
+        a.hbuf[(c * 5 + 3) * P + p] = sy;
+        a.hbuf[(c * 5 + 4) * P + p] = cr;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_ssim_fields(LossArgs a) {
+    __shared__ float hp[5][kSpan][kSpan];
+    __shared__ float fl[3][kS][kSpan];
+    __shared__ float red[8];
+    const int W = a.width, H = a.height;
+    const size_t P = (size_t)W * H;
+    const int bx = blockIdx.x * kS - kHalo, by = blockIdx.y * kS - kHalo;
+    const int tid = threadIdx.x, lx = tid & 15, ly = tid >> 4;
+    const StepParams &sp = *a.sp;
+    const float sw = sp.ssim_weight;
+    float ssim_acc = 0.f, l1_acc = 0.f;
+    unsigned nwin = 0;
+    for (int c = 0; c < 3; c++) {
+        for (int i = tid; i < kSpan * kSpan; i += 256) {
+            const int sy = i / kSpan, sx = i % kSpan;
+            const int gy = by + sy, gx = bx + sx;
+            const bool in = gx >= 0 && gx < W && gy >= 0 && gy < H;
+            const size_t p = in ? ((size_t)gy * W + gx) : 0;
+#pragma unroll
+            for (int f = 0; f < 5; f++) hp[f][sy][sx] = in ? a.hbuf[(c * 5 + f) * P + p] : 0.f;
+        }
+        __syncthreads();
+        for (int i = tid; i < kS * kSpan; i += 256) {
+            const int fy = i / kSpan, fx = i % kSpan;     // field row (output rows), column incl. halo
+            const int gx = bx + fx, gy = blockIdx.y * kS + fy;
+            float m[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int k = 0; k < 11; k++) {
+                const float w = kGauss[k];
+#pragma unroll
+                for (int f = 0; f < 5; f++) m[f] += w * hp[f][fy + k][fx];
+            }
+            float mval = 1.f;
+            const bool in_img = gx >= 0 && gx < W && gy < H;
+            if (sp.has_mask && in_img && a.mask[(size_t)gy * W + gx] < 128) mval = 0.f;
+            if (!(finite_bits(m[0]) && finite_bits(m[1]) && finite_bits(m[2]) && finite_bits(m[3]) && finite_bits(m[4]))) {
+                fl[0][fy][fx] = fl[1][fy][fx] = fl[2][fy][fx] = 0.f;
+                nwin++;
+                continue;
+            }
+            const float mu_x = m[0], mu_y = m[1];
+            const float sxq = fmaxf(m[2] - mu_x * mu_x, 0.f), syq = fmaxf(m[3] - mu_y * mu_y, 0.f);
+            const float sxy = m[4] - mu_x * mu_y;
+            const float A = 2.f * mu_x * mu_y + kC1, B = 2.f * sxy + kC2;
+            const float Cd = mu_x * mu_x + mu_y * mu_y + kC1, D = sxq + syq + kC2;
+            const float iCD = 1.f / (Cd * D);
+            const float dmu = 2.f * B * (mu_x * Cd - A * mu_y) / (Cd * Cd * D);
+            const float dsyq = -A * B * iCD / D, dsxy = 2.f * A * iCD;
+            fl[0][fy][fx] = mval * (dmu - 2.f * mu_y * dsyq - mu_x * dsxy);
+            fl[1][fy][fx] = mval * (2.f * dsyq);
+            fl[2][fy][fx] = mval * dsxy;
+            if (fx >= kHalo && fx < kHalo + kS && in_img) {
+                ssim_acc += mval * (A * B) / (Cd * D);
+                const size_t p = (size_t)gy * W + gx;
+                l1_acc += mval * fabsf((float)a.gt[3 * p + c] * (1.0f / 255.0f) - a.img[3 * p + c]);
+            }
+        }
+        __syncthreads();
+        const int x = blockIdx.x * kS + lx, y = blockIdx.y * kS + ly;
+        if (x < W && y < H) {
+            float h1 = 0.f, h2 = 0.f, h3 = 0.f;
+#pragma unroll
+            for (int d = 0; d < 11; d++) {
+                const float w = kGauss[10 - d];
+                h1 += w * fl[0][ly][lx + d];
+                h2 += w * fl[1][ly][lx + d];
+                h3 += w * fl[2][ly][lx + d];
+            }
+            const size_t p = (size_t)y * W + x;
+            a.dbuf[(c * 3 + 0) * P + p] = h1;
+            a.dbuf[(c * 3 + 1) * P + p] = h2;
+            a.dbuf[(c * 3 + 2) * P + p] = h3;
+        }
+        __syncthreads();
+    }
+    // loss: each thread whose own pixel is in the image adds w*(1 - s/3) + (1-w)*l/3
+    // over the window centres it evaluated (the reference's partition, so a
+    // partial edge tile sums the same terms)
+    const int x = blockIdx.x * kS + lx, y = blockIdx.y * kS + ly;
+    float v = (x < W && y < H) ? sw * (1.f - ssim_acc / 3.f) + (1.f - sw) * l1_acc / 3.f : 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((tid & 31) == 0) red[tid >> 5] = v;
+    __syncthreads();
+    if (tid == 0) {
+        float s = 0.f;
+        for (int k = 0; k < 8; k++) s += red[k];
+        atomicAdd(a.loss_sum, s);
+    }
+    if (nwin && a.nan_counts) atomicAdd(a.nan_counts + kNanSsimWin, nwin);
+}
+
+__global__ void __launch_bounds__(256) k_ssim_bwd(LossArgs a) {
+    __shared__ float sh[9][kSpan][kS];
+    const int W = a.width, H = a.height;
+    const size_t P = (size_t)W * H;
+    const int bx = blockIdx.x * kS, by = blockIdx.y * kS - kHalo;
+    const int tid = threadIdx.x, lx = tid & 15, ly = tid >> 4;
+    for (int i = tid; i < kSpan * kS; i += 256) {
+        const int sy = i / kS, sx = i % kS;
+        const int gy = by + sy, gx = bx + sx;
+        const bool in = gx < W && gy >= 0 && gy < H;
+        const size_t p = in ? ((size_t)gy * W + gx) : 0;
+#pragma unroll
+        for (int f = 0; f < 9; f++) sh[f][sy][sx] = in ? a.dbuf[f * P + p] : 0.f;
+    }
+    __syncthreads();
+    const int x = bx + lx, y = blockIdx.y * kS + ly;
+    if (x >= W || y >= H) return;
+    const StepParams &sp = *a.sp;
+    const float sw = sp.ssim_weight, invn = sp.loss_inv_n;
+    const size_t p = (size_t)y * W + x;
+    float mc = 1.f;
+    if (sp.has_mask && a.mask[p] < 128) mc = 0.f;
+    unsigned nbad = 0;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        float c1 = 0.f, c2 = 0.f, c3 = 0.f;
+#pragma unroll
+        for (int d = 0; d < 11; d++) {
+            const float w = kGauss[10 - d];
+            c1 += w * sh[c * 3 + 0][ly + d][lx];
+            c2 += w * sh[c * 3 + 1][ly + d][lx];
+            c3 += w * sh[c * 3 + 2][ly + d][lx];
+        }
+        const float r = a.img[3 * p + c], g = (float)a.gt[3 * p + c] * (1.0f / 255.0f);
+        const float vs = c1 + r * c2 + g * c3;
+        const float vl = mc * ((g > r) ? -1.f : ((g < r) ? 1.f : 0.f));
+        float v = invn * (-sw * vs + (1.f - sw) * vl);
+        if (!finite_bits(v)) { nbad++; v = 0.f; }
+        a.v_img[3 * p + c] = v;
+    }
+    if (nbad && a.nan_counts) atomicAdd(a.nan_counts + kNanVRendered, nbad);
+}
+
+static bool g_gauss_ready = false;
+
+void launch_loss(const LossArgs &a, cudaStream_t s) {
+    if (!g_gauss_ready) {
+        double g[11], sum = 0;
+        for (int i = 0; i < 11; i++) { g[i] = exp(-((i - 5) * (i - 5)) / (2.0 * 1.5 * 1.5)); sum += g[i]; }
+        float w[11];
+        for (int i = 0; i < 11; i++) w[i] = (float)(g[i] / sum);
+        cudaMemcpyToSymbol(kGauss, w, sizeof(w));
+        g_gauss_ready = true;
+    }
+    const dim3 grid((a.width + kS - 1) / kS, (a.height + kS - 1) / kS);
+    k_ssim_h<<<grid, 256, 0, s>>>(a);
+    k_ssim_fields<<<grid, 256, 0, s>>>(a);
+    k_ssim_bwd<<<grid, 256, 0, s>>>(a);
+}
+
+}  // namespace msplat

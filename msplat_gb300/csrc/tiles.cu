@@ -1,0 +1,237 @@
+// Tile-intersection mapping: count -> exclusive scan -> scatter -> per-tile
+// sort + pack.  Follows count_intersections_kernel, prefix_sum_tiles_kernel,
+// scatter_intersections_kernel and hybrid_sort_pack_kernel
+// (msplat_metal.metal:2248-2627) with the same keys (depth bits << 32 | id,
+// ascending) and therefore the same per-tile order.  Differences of layout:
+// buckets sit at exact (not power-of-two padded) offsets, and each tile is
+// sorted by one CTA with a stable LSD radix sort (8-bit digits, constant
+// digits skipped) in shared memory, or in global memory for heavy tiles.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace msplat {
+
+__device__ __forceinline__ bool splat_active(int i, const int *radii, const float *depths) {
+    if (radii[i] <= 0) return false;
+    const float d = depths[i];
+    return finite_bits(d) && d > 0.0f;
+}
+
+__global__ void __launch_bounds__(256) k_count(TileArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n || !splat_active(i, a.radii, a.depths)) return;
+    const float4 ra = a.rec[i].a;
+    const float2 ab = a.aabb[i];
+    int x0, y0, x1, y1;
+    tile_rect(ra.x, ra.y, ab.x, ab.y, a.tiles_x, a.tiles_y, x0, y0, x1, y1);
+    for (int y = y0; y < y1; y++)
+        for (int x = x0; x < x1; x++) atomicAdd(a.tile_counts + y * a.tiles_x + x, 1u);
+}
+
+// Exclusive scan of the tile counts by one CTA of 1024 threads: each thread
+// scans a contiguous run, the run totals are scanned across the CTA.
+__global__ void __launch_bounds__(1024) k_scan(TileArgs a) {
+    __shared__ uint32_t warp_tot[32];
+    __shared__ uint32_t max_warp[32];
+    const int T = a.num_tiles;
+    const int per = (T + 1023) / 1024;
+    const int lo = min(T, (int)threadIdx.x * per), hi = min(T, lo + per);
+    uint32_t sum = 0, mx = 0;
+    for (int t = lo; t < hi; t++) { const uint32_t c = a.tile_counts[t]; sum += c; mx = max(mx, c); }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint32_t incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
+    }
+    const uint32_t wmax = __reduce_max_sync(0xffffffffu, mx);
+    if (lane == 31) warp_tot[wid] = incl;
+    if (lane == 0) max_warp[wid] = wmax;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t v = warp_tot[lane], inc = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += u;
+        }
+        warp_tot[lane] = inc - v;
+        const uint32_t m = __reduce_max_sync(0xffffffffu, max_warp[lane]);
+        if (lane == 0) max_warp[0] = m;
+    }
+    __syncthreads();
+    uint32_t run = warp_tot[wid] + incl - sum;
+    for (int t = lo; t < hi; t++) {
+        a.tile_offsets[t] = run;
+        run += a.tile_counts[t];
+    }
+    if (threadIdx.x == 1023) a.tile_offsets[T] = run;
+    if (threadIdx.x == 0) a.max_tile_count[0] = max_warp[0];
+}
+
+__global__ void __launch_bounds__(256) k_scatter(TileArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n || !splat_active(i, a.radii, a.depths)) return;
+    const float4 ra = a.rec[i].a;
+    const float2 ab = a.aabb[i];
+    int x0, y0, x1, y1;
+    tile_rect(ra.x, ra.y, ab.x, ab.y, a.tiles_x, a.tiles_y, x0, y0, x1, y1);
+    const uint64_t key = ((uint64_t)__float_as_uint(a.depths[i]) << 32) | (uint32_t)i;
+    for (int y = y0; y < y1; y++)
+        for (int x = x0; x < x1; x++) {
+            const int t = y * a.tiles_x + x;
+            const uint32_t pos = atomicAdd(a.tile_write + t, 1u);
+            const uint64_t dst = (uint64_t)a.tile_offsets[t] + pos;
+            if (dst < (uint64_t)a.capacity) a.keys[dst] = key;   // overflow is dropped, never written
+        }
+}
+
+// ---------------------------------------------------------------------------
+// Per-tile stable LSD radix sort by one CTA (kSortThreads threads).
+// ---------------------------------------------------------------------------
+constexpr int kSortThreads = 512;
+constexpr int kSortWarps = kSortThreads / 32;
+constexpr int kSortSmemKeys = 4096;   // keys sorted in shared memory; larger tiles sort in place in global
+
+struct SortSmem {
+    uint32_t hist[256];
+    uint32_t base[256];
+    uint16_t wcnt[kSortWarps][256];
+    uint32_t woff[kSortWarps][256];
+    int skip;
+};
+
+// One stable counting pass on digit `shift`: src -> dst.  Returns false when
+// every key has the same digit (nothing written; the caller keeps src).
+__device__ bool radix_pass(const uint64_t *src, uint64_t *dst, int n, int shift, SortSmem &sm) {
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    for (int d = tid; d < 256; d += kSortThreads) sm.hist[d] = 0;
+    __syncthreads();
+    for (int i = tid; i < n; i += kSortThreads) atomicAdd(&sm.hist[(uint32_t)(src[i] >> shift) & 255u], 1u);
+    __syncthreads();
+    if (tid == 0) {
+        int skip = 0;
+        uint32_t run = 0;
+        for (int d = 0; d < 256; d++) {
+            const uint32_t h = sm.hist[d];
+            if (h == (uint32_t)n) skip = 1;
+            sm.base[d] = run;
+            run += h;
+        }
+        sm.skip = skip;
+    }
+    __syncthreads();
+    if (sm.skip) return false;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    for (int c0 = 0; c0 < n; c0 += kSortThreads) {
+        const int i = c0 + tid;
+        const bool valid = i < n;
+        const uint64_t key = valid ? src[i] : 0ull;
+        const uint32_t d = valid ? ((uint32_t)(key >> shift) & 255u) : 256u;
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        const uint32_t rank = __popc(peers & lt_mask);
+        if (valid && rank == 0) sm.wcnt[wid][d] = (uint16_t)__popc(peers);
+        __syncthreads();
+        for (int dd = tid; dd < 256; dd += kSortThreads) {
+            uint32_t acc = sm.base[dd];
+#pragma unroll 4
+            for (int w = 0; w < kSortWarps; w++) {
+                const uint32_t cnt = sm.wcnt[w][dd];
+                sm.woff[w][dd] = acc;
+                sm.wcnt[w][dd] = 0;
+                acc += cnt;
+            }
+            sm.base[dd] = acc;
+        }
+        __syncthreads();
+        if (valid) dst[sm.woff[wid][d] + rank] = key;
+        __syncthreads();
+    }
+    return true;
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_sort_pack(TileArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    SortSmem &sm = *reinterpret_cast<SortSmem *>(smem_raw);
+    uint64_t *sk0 = reinterpret_cast<uint64_t *>(smem_raw + ((sizeof(SortSmem) + 15) & ~size_t(15)));
+    uint64_t *sk1 = sk0 + kSortSmemKeys;
+    const int t = blockIdx.x;
+    const int count = (int)a.tile_counts[t];
+    if (count == 0) return;
+    const uint32_t start = a.tile_offsets[t];
+    const int tid = threadIdx.x;
+    // a tile whose bucket does not fit the buffer is emitted transparent
+    // (hybrid_sort_pack_kernel's region guard, msplat_metal.metal:2523-2535)
+    if ((uint64_t)start + (uint64_t)count > (uint64_t)a.capacity) {
+        for (int j = tid; j < count; j += kSortThreads) {
+            const uint64_t d = (uint64_t)start + j;
+            if (d < (uint64_t)a.capacity) {
+                SplatRec z;
+                z.a = make_float4(0.f, 0.f, 0.f, __int_as_float(0));
+                z.b = make_float4(0.f, 0.f, 0.f, 0.f);
+                z.c = make_float4(0.f, 0.f, 0.f, 0.f);
+                a.packed[d] = z;
+            }
+        }
+        return;
+    }
+    uint64_t *src, *alt;
+    if (count <= kSortSmemKeys) {
+        for (int j = tid; j < count; j += kSortThreads) sk0[j] = a.keys[start + j];
+        __syncthreads();
+        src = sk0; alt = sk1;
+    } else {
+        src = a.keys + start; alt = a.keys_alt + start;
+    }
+    for (int shift = 0; shift < 64; shift += 8) {
+        if (radix_pass(src, alt, count, shift, sm)) { uint64_t *tmp = src; src = alt; alt = tmp; }
+        __syncthreads();
+    }
+    // pack: gather the splat records in sorted order
+    for (int j = tid; j < count; j += kSortThreads) {
+        const uint64_t key = src[j];
+        const uint32_t g = (uint32_t)key;
+        SplatRec r;
+        if (g >= (uint32_t)a.n) {
+            r.a = make_float4(0.f, 0.f, 0.f, __int_as_float(0));
+            r.b = make_float4(0.f, 0.f, 0.f, 0.f);
+            r.c = make_float4(0.f, 0.f, 0.f, 0.f);
+        } else {
+            r = a.rec[g];
+            const bool ok = finite_bits(r.a.x) && finite_bits(r.a.y) && finite_bits(r.a.z) && finite_bits(r.b.x) &&
+                            finite_bits(r.b.y) && finite_bits(r.b.z) && finite_bits(r.c.x) && finite_bits(r.c.y) &&
+                            finite_bits(r.c.z);
+            if (!ok) {
+                if (a.nan_counts) {
+                    atomicAdd(a.nan_counts + kNanPack, 1u);
+                    if (!finite_bits(r.a.z)) atomicAdd(a.nan_counts + kNanPackOpacity, 1u);
+                }
+                r.a = make_float4(0.f, 0.f, 0.f, 0.f);
+                r.b = make_float4(0.f, 0.f, 0.f, 0.f);
+                r.c = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            r.a.w = __int_as_float((int)g);
+        }
+        a.packed[start + j] = r;
+    }
+}
+
+size_t sort_pack_smem_bytes() {
+    return ((sizeof(SortSmem) + 15) & ~size_t(15)) + 2 * kSortSmemKeys * sizeof(uint64_t);
+}
+
+void launch_tiles(const TileArgs &a, cudaStream_t s) {
+    if (a.n > 0) k_count<<<(a.n + 255) / 256, 256, 0, s>>>(a);
+    k_scan<<<1, 1024, 0, s>>>(a);
+    if (a.n > 0) k_scatter<<<(a.n + 255) / 256, 256, 0, s>>>(a);
+    static bool attr_set = false;
+    const size_t smem = sort_pack_smem_bytes();
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_sort_pack, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr_set = true;
+    }
+    k_sort_pack<<<a.num_tiles, kSortThreads, smem, s>>>(a);
+}
+
+}  // namespace msplat

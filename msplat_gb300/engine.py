@@ -1,0 +1,173 @@
+"""Python handle on the CUDA training engine (include/msplat_engine.h).
+
+Device buffers are torch CUDA tensors (PyTorch is used here for device memory
+only); every computation runs in the engine's own kernels.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _native as N
+
+# Adam defaults (core/src/model.cpp:223, core/include/model.hpp:76-78)
+LR_INIT = (0.00016, 0.005, 0.001, 0.0025, 0.000125, 0.05)
+BETA1, BETA2, EPS = 0.9, 0.999, 1e-8
+GROUPS = ("means", "scales", "quats", "features_dc", "features_rest", "opacities")
+
+
+def prepare_cam(c2w, width: int, height: int, fx: float, fy: float):
+    """World->camera and projection*view matrices and camera position
+    (core/src/model.cpp:845-889), computed by the library."""
+    L = N.lib()
+    c2w = np.ascontiguousarray(c2w, np.float32).reshape(16)
+    vm = np.zeros(16, np.float32)
+    pm = np.zeros(16, np.float32)
+    cp = np.zeros(3, np.float32)
+    L.msplat_prepare_camera(c2w.ctypes.data_as(N.FP), width, height, C.c_float(fx), C.c_float(fy),
+                            vm.ctypes.data_as(N.FP), pm.ctypes.data_as(N.FP), cp.ctypes.data_as(N.FP))
+    return vm, pm, cp
+
+
+def step_scalars(step: int, adam_step: int, lr=LR_INIT, sh_degree=3, sh_interval=1000, op_reg=0.01, sc_reg=0.01,
+                 width=None, height=None, noise_lr=5e5, cull_radius=3.0):
+    """Per-step scalars of Model::fullIteration (core/src/model.cpp:901-975)."""
+    bc1 = 1.0 - BETA1 ** adam_step
+    bc2 = 1.0 - BETA2 ** adam_step
+    d = dict(degrees_to_use=min(step // sh_interval, sh_degree),
+             step_size=[float(np.float32(l) / np.float32(bc1)) for l in lr],
+             bc2_sqrt=[float(np.sqrt(np.float32(bc2)))] * 6,
+             beta1=BETA1, beta2=BETA2, eps=EPS,
+             op_reg=op_reg if step >= 500 else 0.0, sc_reg=sc_reg if step >= 500 else 0.0, invis_scale=1.0,
+             seed=step, noise_lr=noise_lr, xyz_lr=lr[0], max_disp=cull_radius * 0.0167 if cull_radius > 0 else 0.05)
+    if width is not None:
+        d["loss_inv_n"] = 1.0 / float(width * height * 3)
+    return d
+
+
+def make_args(cam: dict, step: dict, background=(0.0, 0.0, 0.0), ssim_weight=0.2, raster_mode=0, k_max=0,
+              do_optimizer=True, do_sgld=False) -> N.MsplatStepArgs:
+    a = N.MsplatStepArgs()
+    a.viewmat[:] = [float(v) for v in np.asarray(cam["viewmat"], np.float32).ravel()]
+    a.projmat[:] = [float(v) for v in np.asarray(cam["projmat"], np.float32).ravel()]
+    a.fx, a.fy, a.cx, a.cy = cam["fx"], cam["fy"], cam["cx"], cam["cy"]
+    a.width, a.height = int(cam["width"]), int(cam["height"])
+    a.cam_pos[:] = [float(v) for v in cam["cam_pos"]]
+    a.background[:] = [float(v) for v in background]
+    a.clip_thresh = 0.01
+    a.degrees_to_use = int(step.get("degrees_to_use", 3))
+    a.ssim_weight = ssim_weight
+    a.loss_inv_n = step.get("loss_inv_n", 1.0 / (3.0 * a.width * a.height))
+    a.step_size[:] = [float(v) for v in step.get("step_size", [0.0] * 6)]
+    a.bc2_sqrt[:] = [float(v) for v in step.get("bc2_sqrt", [1.0] * 6)]
+    a.beta1, a.beta2, a.eps = step.get("beta1", BETA1), step.get("beta2", BETA2), step.get("eps", EPS)
+    a.op_reg, a.sc_reg, a.invis_scale = step.get("op_reg", 0.0), step.get("sc_reg", 0.0), step.get("invis_scale", 1.0)
+    a.raster_mode, a.k_max = raster_mode, k_max
+    a.do_optimizer, a.do_sgld = int(do_optimizer), int(do_sgld)
+    a.seed = int(step.get("seed", 0)) & 0xFFFFFFFF
+    a.noise_lr, a.xyz_lr, a.max_disp = step.get("noise_lr", 5e5), step.get("xyz_lr", 1.6e-4), step.get("max_disp", 0.05)
+    return a
+
+
+def camera_dict(cam) -> dict:
+    """synthetic.Camera -> the dict the step helpers use."""
+    vm, pm, cp = prepare_cam(cam.cam_to_world, cam.width, cam.height, cam.fx, cam.fy)
+    return dict(viewmat=vm, projmat=pm, cam_pos=cp, fx=cam.fx, fy=cam.fy, cx=cam.cx, cy=cam.cy,
+                width=cam.width, height=cam.height)
+
+
+class DeviceGaussians:
+    """Parameters and Adam moments as CUDA tensors (reference layouts)."""
+
+    def __init__(self, g, device="cuda"):
+        import torch
+        self.torch = torch
+        self.params = {k: torch.from_numpy(np.ascontiguousarray(a)).to(device) for k, a in zip(GROUPS, g.arrays())}
+        self.params["opacities"] = self.params["opacities"].reshape(-1).contiguous()
+        self.exp_avg = {k: torch.zeros_like(v) for k, v in self.params.items()}
+        self.exp_avg_sq = {k: torch.zeros_like(v) for k, v in self.params.items()}
+        self.rest_bases = int(g.features_rest.shape[1])
+
+    @property
+    def n(self):
+        return int(self.params["means"].shape[0])
+
+    def native(self):
+        p = self.params
+        g = N.MsplatGaussians(self.n, self.rest_bases, p["means"].data_ptr(), p["scales"].data_ptr(),
+                              p["quats"].data_ptr(), p["features_dc"].data_ptr(), p["features_rest"].data_ptr(),
+                              p["opacities"].data_ptr())
+        st = N.MsplatAdamState()
+        for i, k in enumerate(GROUPS):
+            st.exp_avg[i] = self.exp_avg[k].data_ptr()
+            st.exp_avg_sq[i] = self.exp_avg_sq[k].data_ptr()
+        return g, st
+
+    def to_numpy(self):
+        return {k: v.detach().cpu().numpy() for k, v in self.params.items()}, \
+               ({k: v.cpu().numpy() for k, v in self.exp_avg.items()}, {k: v.cpu().numpy() for k, v in self.exp_avg_sq.items()})
+
+
+class Engine:
+    """One CUDA engine (stream + device arena)."""
+
+    def __init__(self, device: int = 0, max_points: int = 0):
+        self.L = N.lib()
+        self.h = self.L.msplat_engine_create(device, max_points)
+        if not self.h:
+            raise RuntimeError("msplat_engine_create failed")
+
+    def close(self):
+        if self.h:
+            self.L.msplat_engine_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != 0:
+            raise RuntimeError(f"msplat engine error {rc}: {self.L.msplat_engine_last_error(self.h).decode()}")
+
+    def train_step(self, dg: DeviceGaussians, args: N.MsplatStepArgs, gt_ptr: int, mask_ptr: int | None = None):
+        g, st = dg.native()
+        self._check(self.L.msplat_engine_train_step(self.h, C.byref(g), C.byref(st), C.byref(args), gt_ptr,
+                                                    mask_ptr or None))
+
+    def render(self, dg: DeviceGaussians, args: N.MsplatStepArgs):
+        g, _ = dg.native()
+        self._check(self.L.msplat_engine_render(self.h, C.byref(g), C.byref(args)))
+
+    def synchronize(self):
+        self._check(self.L.msplat_engine_synchronize(self.h))
+
+    def loss(self) -> float:
+        v = C.c_float()
+        self._check(self.L.msplat_engine_loss(self.h, C.byref(v)))
+        return float(v.value)
+
+    def stats(self) -> N.MsplatEngineStats:
+        s = N.MsplatEngineStats()
+        self._check(self.L.msplat_engine_stats(self.h, C.byref(s)))
+        return s
+
+    def set_timing(self, on: bool):
+        self._check(self.L.msplat_engine_set_timing(self.h, int(on)))
+
+    def buffer(self, name: str):
+        p = C.c_void_p()
+        n = self.L.msplat_engine_buffer(self.h, name.encode(), C.byref(p))
+        return (p.value, n) if n >= 0 else (None, -1)
+
+    def read(self, name: str, dtype, count: int) -> np.ndarray:
+        out = np.zeros(count, dtype)
+        self._check(self.L.msplat_engine_read(self.h, name.encode(), out.ctypes.data, out.nbytes))
+        return out
+
+    def stream(self) -> int:
+        return self.L.msplat_engine_stream(self.h)
