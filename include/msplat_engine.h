@@ -84,6 +84,7 @@ typedef struct {
     int num_tiles;
     uint32_t nan_counts[16];       /* cumulative non-finite telemetry (reference slot numbering) */
     float stage_ms[MSPLAT_STAGE_COUNT];
+    uint32_t check_record[3];      /* checked builds: first failed bound (code, index lo, index hi) */
 } MsplatEngineStats;
 
 /* Creates an engine on CUDA device `device`.  max_points sizes the

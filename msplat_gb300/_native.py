@@ -46,7 +46,8 @@ STAGES = ("project", "tiles", "raster_fwd", "loss", "raster_bwd", "project_bwd",
 
 class MsplatEngineStats(C.Structure):
     _fields_ = [("num_intersections", C.c_longlong), ("max_tile_count", C.c_int), ("k_max", C.c_int),
-                ("num_tiles", C.c_int), ("nan_counts", C.c_uint32 * 16), ("stage_ms", C.c_float * len(STAGES))]
+                ("num_tiles", C.c_int), ("nan_counts", C.c_uint32 * 16), ("stage_ms", C.c_float * len(STAGES)),
+                ("check_record", C.c_uint32 * 3)]
 
 
 def lib(build_if_missing: bool = True):

@@ -38,6 +38,8 @@ def _flags(src: str):
                 "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
     if src in NO_FMAD:
         f.append("--fmad=false")
+    if os.environ.get("MSPLAT_CHECKED"):
+        f.append("-DMSPLAT_CHECKED")
     return f
 
 

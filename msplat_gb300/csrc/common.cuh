@@ -109,6 +109,25 @@ __device__ __forceinline__ int clamp_off(uint32_t off, long long cap) {
     return (int)((long long)off < cap ? (long long)off : cap);
 }
 
+// Checked builds (-DMSPLAT_CHECKED): an index that fails its bound is
+// recorded in dbg[0..2] (code, index, aux) and the access is skipped.  In the
+// normal build the guard is the constant true and compiles away.
+#ifdef MSPLAT_CHECKED
+__device__ __forceinline__ bool ms_guard(bool ok, unsigned code, long long idx, unsigned *dbg) {
+    if (!ok && dbg) {
+        if (atomicCAS(dbg, 0u, code) == 0u) {
+            dbg[1] = (unsigned)idx;
+            dbg[2] = (unsigned)(idx >> 32);
+        }
+    }
+    return ok;
+}
+#define MS_GUARD(ok, code, idx, dbg) ms_guard((ok), (code), (long long)(idx), (dbg))
+#else
+#define MS_GUARD(ok, code, idx, dbg) (true)
+#endif
+constexpr int kDbgSlot = 16;   // nan_counts[16..18]: checked-build violation record
+
 __device__ __forceinline__ void atomic_add_f4(float4 *addr, float4 v) {
     atomicAdd(addr, v);   // sm_90+: one vector reduction in L2
 }

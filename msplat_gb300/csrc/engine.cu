@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <stdexcept>
@@ -20,6 +21,15 @@ namespace msplat {
         if (err_ != cudaSuccess)                                                               \
             throw std::runtime_error(std::string(#x) + ": " + cudaGetErrorString(err_));       \
     } while (0)
+
+static const bool g_sync_check = getenv("MSPLAT_SYNC_CHECK") != nullptr;
+
+void debug_sync(cudaStream_t s, const char *what) {
+    if (!g_sync_check) return;
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) throw std::runtime_error(std::string("kernel ") + what + ": " + cudaGetErrorString(e));
+}
 
 struct Buf {
     void *ptr = nullptr;
@@ -82,6 +92,7 @@ class Engine {
         pa.grad = backward ? ptr<GradRec>("grad") : nullptr;
         pa.nan_counts = ptr<unsigned>("nan_counts");
         launch_project_fwd(pa, stream_);
+        debug_sync(stream_, "project_fwd");
         mark(1);
 
         TileArgs ta{};
@@ -104,6 +115,7 @@ class Engine {
         }
         ra.v_img = ptr<float>("v_img"); ra.grad = ptr<GradRec>("grad"); ra.nan_counts = pa.nan_counts;
         launch_raster_fwd(ra, stream_);
+        debug_sync(stream_, "raster_fwd");
         mark(3);
         if (!gt) { mark(4); mark(5); mark(6); mark(7); mark(8); return; }
 
@@ -112,10 +124,12 @@ class Engine {
         la.hbuf = ptr<float>("hbuf"); la.dbuf = ptr<float>("dbuf"); la.v_img = ptr<float>("v_img");
         la.loss_sum = ptr<float>("loss_sum"); la.nan_counts = pa.nan_counts;
         launch_loss(la, stream_);
+        debug_sync(stream_, "loss");
         mark(4);
         if (!backward) { mark(5); mark(6); mark(7); mark(8); return; }
 
         launch_raster_bwd(ra, stream_);
+        debug_sync(stream_, "raster_bwd");
         mark(5);
 
         ProjectBwdArgs pb{};
@@ -131,6 +145,7 @@ class Engine {
         }
         pb.nan_counts = pa.nan_counts;
         launch_project_bwd(pb, stream_);
+        debug_sync(stream_, "project_bwd");
         mark(6);
 
         AdamArgs aa{};
@@ -144,8 +159,10 @@ class Engine {
         aa.g_mean = pb.v_mean; aa.g_scale = pb.v_scale; aa.g_quat = pb.v_quat; aa.grad = ra.grad;
         aa.nan_counts = pa.nan_counts;
         if (args.do_optimizer && st) launch_adam(aa, num_sms_, stream_);
+        debug_sync(stream_, "adam");
         mark(7);
         if (args.do_sgld) launch_sgld(aa, stream_);
+        debug_sync(stream_, "sgld");
         mark(8);
         CK(cudaGetLastError());
     }
@@ -171,7 +188,12 @@ class Engine {
         }
         o.k_max = last_K_;
         o.num_tiles = last_T_;
-        if (has("nan_counts")) CK(cudaMemcpy(o.nan_counts, ptr<unsigned>("nan_counts"), 64, cudaMemcpyDeviceToHost));
+        if (has("nan_counts")) {
+            unsigned tmp[32];
+            CK(cudaMemcpy(tmp, ptr<unsigned>("nan_counts"), sizeof(tmp), cudaMemcpyDeviceToHost));
+            std::memcpy(o.nan_counts, tmp, 64);
+            std::memcpy(o.check_record, tmp + kDbgSlot, sizeof(o.check_record));
+        }
         if (timing_) {
             for (int s = 0; s < MSPLAT_STAGE_COUNT; s++) {
                 float ms = 0;
@@ -210,7 +232,7 @@ class Engine {
         if (!has("params")) {
             alloc("params", sizeof(StepParams));
             alloc("loss_sum", 256, true);
-            alloc("nan_counts", 64, true);
+            alloc("nan_counts", 128, true);
             alloc("max_tile", 256, true);
         }
         if (n <= cap_points_) return;

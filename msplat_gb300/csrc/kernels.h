@@ -89,6 +89,10 @@ struct AdamArgs {
     unsigned *nan_counts;
 };
 
+// With MSPLAT_SYNC_CHECK set in the environment, waits for the stream after
+// each launch and raises with the kernel's name if it failed.
+void debug_sync(cudaStream_t s, const char *what);
+
 void launch_project_fwd(const ProjectArgs &a, cudaStream_t s);
 void launch_tiles(const TileArgs &a, cudaStream_t s);
 size_t sort_pack_smem_bytes();

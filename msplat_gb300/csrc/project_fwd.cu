@@ -42,6 +42,7 @@ __global__ void __launch_bounds__(256) k_project_fwd(ProjectArgs a) {
     float s[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) s[k] = det_expf(fminf(fmaxf(a.scales[3 * i + k], -15.f), 15.f));
+    if (!MS_GUARD(((uintptr_t)a.quats & 15) == 0, 1, i, a.nan_counts ? a.nan_counts + kDbgSlot : nullptr)) return;
     const float4 q = *reinterpret_cast<const float4 *>(a.quats + 4 * (size_t)i);
     const float qn = 1.0f / sqrtf(fmaxf(q.w * q.w + q.x * q.x + q.y * q.y + q.z * q.z, 1e-8f));
     const float w = q.x * qn, x = q.y * qn, y = q.z * qn, z = q.w * qn;

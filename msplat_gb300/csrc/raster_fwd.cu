@@ -79,13 +79,15 @@ __global__ void __launch_bounds__(kTileThreads) k_raster_fwd(RasterArgs a) {
     const int tx = tile % a.tiles_x, ty = tile / a.tiles_x;
     const int x = tx * kTile + (threadIdx.x & 15), y = ty * kTile + (threadIdx.x >> 4);
     const bool inside = x < a.width && y < a.height;
-    const int s = clamp_off(a.tile_offsets[tile], a.capacity), e = clamp_off(a.tile_offsets[tile + 1], a.capacity);
+    int s = clamp_off(a.tile_offsets[tile], a.capacity), e = clamp_off(a.tile_offsets[tile + 1], a.capacity);
+    if (!MS_GUARD(s >= 0 && s <= e && e <= a.capacity, 5, tile, a.nan_counts ? a.nan_counts + kDbgSlot : nullptr)) e = s = 0;
     float T;
     float3 C;
     int last;
     composite_range(sm, a.packed, s, e, (float)x, (float)y, !inside, T, C, last, nullptr);
     if (!inside) return;
     const int p = y * a.width + x;
+    if (!MS_GUARD(p >= 0 && p < a.width * a.height, 6, p, a.nan_counts ? a.nan_counts + kDbgSlot : nullptr)) return;
     const StepParams &sp = *a.sp;
     a.final_T[p] = T;
     a.final_idx[p] = last;

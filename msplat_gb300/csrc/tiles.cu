@@ -25,7 +25,10 @@ __global__ void __launch_bounds__(256) k_count(TileArgs a) {
     int x0, y0, x1, y1;
     tile_rect(ra.x, ra.y, ab.x, ab.y, a.tiles_x, a.tiles_y, x0, y0, x1, y1);
     for (int y = y0; y < y1; y++)
-        for (int x = x0; x < x1; x++) atomicAdd(a.tile_counts + y * a.tiles_x + x, 1u);
+        for (int x = x0; x < x1; x++)
+            if (MS_GUARD(y * a.tiles_x + x < a.num_tiles && y * a.tiles_x + x >= 0, 2, y * a.tiles_x + x,
+                         a.nan_counts ? a.nan_counts + kDbgSlot : nullptr))
+                atomicAdd(a.tile_counts + y * a.tiles_x + x, 1u);
 }
 
 // Exclusive scan of the tile counts by one CTA of 1024 threads: each thread
@@ -81,6 +84,7 @@ __global__ void __launch_bounds__(256) k_scatter(TileArgs a) {
     for (int y = y0; y < y1; y++)
         for (int x = x0; x < x1; x++) {
             const int t = y * a.tiles_x + x;
+            if (!MS_GUARD(t >= 0 && t < a.num_tiles, 3, t, a.nan_counts ? a.nan_counts + kDbgSlot : nullptr)) continue;
             const uint32_t pos = atomicAdd(a.tile_write + t, 1u);
             const uint64_t dst = (uint64_t)a.tile_offsets[t] + pos;
             if (dst < (uint64_t)a.capacity) a.keys[dst] = key;   // overflow is dropped, never written
@@ -104,7 +108,7 @@ struct SortSmem {
 
 // One stable counting pass on digit `shift`: src -> dst.  Returns false when
 // every key has the same digit (nothing written; the caller keeps src).
-__device__ bool radix_pass(const uint64_t *src, uint64_t *dst, int n, int shift, SortSmem &sm) {
+__device__ bool radix_pass(const uint64_t *src, uint64_t *dst, int n, int shift, SortSmem &sm, unsigned *dbg) {
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     for (int d = tid; d < 256; d += kSortThreads) sm.hist[d] = 0;
     __syncthreads();
@@ -145,7 +149,8 @@ __device__ bool radix_pass(const uint64_t *src, uint64_t *dst, int n, int shift,
             sm.base[dd] = acc;
         }
         __syncthreads();
-        if (valid) dst[sm.woff[wid][d] + rank] = key;
+        if (valid && MS_GUARD(sm.woff[wid][d] + rank < (uint32_t)n, 4, sm.woff[wid][d] + rank, dbg))
+            dst[sm.woff[wid][d] + rank] = key;
         __syncthreads();
     }
     return true;
@@ -185,7 +190,11 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pack(TileArgs a) {
         src = a.keys + start; alt = a.keys_alt + start;
     }
     for (int shift = 0; shift < 64; shift += 8) {
-        if (radix_pass(src, alt, count, shift, sm)) { uint64_t *tmp = src; src = alt; alt = tmp; }
+        if (radix_pass(src, alt, count, shift, sm, a.nan_counts ? a.nan_counts + kDbgSlot : nullptr)) {
+            uint64_t *tmp = src;
+            src = alt;
+            alt = tmp;
+        }
         __syncthreads();
     }
     // pack: gather the splat records in sorted order
@@ -223,8 +232,11 @@ size_t sort_pack_smem_bytes() {
 
 void launch_tiles(const TileArgs &a, cudaStream_t s) {
     if (a.n > 0) k_count<<<(a.n + 255) / 256, 256, 0, s>>>(a);
+    debug_sync(s, "count");
     k_scan<<<1, 1024, 0, s>>>(a);
+    debug_sync(s, "scan");
     if (a.n > 0) k_scatter<<<(a.n + 255) / 256, 256, 0, s>>>(a);
+    debug_sync(s, "scatter");
     static bool attr_set = false;
     const size_t smem = sort_pack_smem_bytes();
     if (!attr_set) {
@@ -232,6 +244,7 @@ void launch_tiles(const TileArgs &a, cudaStream_t s) {
         attr_set = true;
     }
     k_sort_pack<<<a.num_tiles, kSortThreads, smem, s>>>(a);
+    debug_sync(s, "sort_pack");
 }
 
 }  // namespace msplat

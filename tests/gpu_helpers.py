@@ -76,6 +76,8 @@ def run_pair(init: S.GaussianSet, cam, gt, step: dict, *, raster_mode=0, k_max=0
     if do_backward:
         eo["loss"] = eng.loss()
     st = eng.stats()
+    rec = list(st.check_record)
+    assert rec[0] == 0, f"checked build: bound {rec[0]} failed at index {rec[1] | (rec[2] << 32)}"
     eo["k_max"] = st.k_max
     eo["nan_counts"] = np.array(st.nan_counts[:], np.uint32)
     params, moments = dg.to_numpy()
