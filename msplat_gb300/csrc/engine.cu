@@ -235,7 +235,7 @@ class Engine {
             alloc("nan_counts", 128, true);
             alloc("max_tile", 256, true);
         }
-        if (n <= cap_points_) return;
+        if (n <= cap_points_ && has("rec")) return;
         const size_t m = (size_t)std::max(n, 1);
         alloc("rec", m * sizeof(SplatRec));
         alloc("depths", m * 4);

@@ -181,6 +181,10 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pack(TileArgs a) {
         }
         return;
     }
+    // shared memory starts with stale contents: the per-warp digit counts
+    // must start at zero (each chunk of a pass clears what it used)
+    for (int i = tid; i < kSortWarps * 256; i += kSortThreads) (&sm.wcnt[0][0])[i] = 0;
+    __syncthreads();
     uint64_t *src, *alt;
     if (count <= kSortSmemKeys) {
         for (int j = tid; j < count; j += kSortThreads) sk0[j] = a.keys[start + j];
