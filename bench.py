@@ -1,0 +1,344 @@
+#!/usr/bin/env python3
+"""Training-step benchmark of the msplat GB300 engine.
+
+Workload (one step = one training iteration, Model::fullIteration):
+  1,000,000 Gaussians (SH degree 3), one 1297x840 view per step, L1+0.2*SSIM
+  loss, backward, fused SH Adam, regularizer + Adam, SGLD, on a synthetic
+  scene: 1M GT Gaussians + 200k ground-plane Gaussians (synthetic.config_full),
+  ring/elevation-jittered cameras, targets rendered from the GT scene by the
+  engine's forward pass.  The trained model is a 1M subset of the GT scene
+  with jittered means (the steady state of a run at its 1M cap), training
+  steps 3001.. (all SH bands active, regularizer and SGLD on).
+
+Arms:
+  default            the CUDA engine.  `value` = iterations/s with the targets
+                     resident in HBM; `e2e` = the same through the C ABI with
+                     the target image copied from pinned host memory each step
+                     and the loss read back.
+  --impl reference   the reference's own implementation cannot run here
+                     (Metal only), so the arm times the CPU restatement of it
+                     (oracle/, FP64, OpenMP on all host cores) on the same
+                     workload, one full iteration per step.
+
+Under torchrun (N > 1) every rank trains its own replica on its own GPU
+("replicas only": the step has no cross-GPU exchange).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "train iters/s & ms/step at 1M splats 1297×840 vs CPU oracle; learned vs plain time-to-PSNR"
+N_MODEL = 1_000_000
+VIEWS = 8
+
+# Algorithmic bytes per unit (per Gaussian / intersection / pixel) of each
+# stage, SH degree 3: what the stage must read and write at minimum.
+STAGE_BYTES = {
+    "project": dict(g=284),                      # params 232 B in, projection 52 B out
+    "tiles": dict(g=52, i=92),                   # count/scatter; key 16 + pack 76 per intersection
+    "raster_fwd": dict(i=36, p=20),
+    "loss": dict(p=27),
+    "raster_bwd": dict(i=76, p=20),              # packed read 40 + gradient read-modify-write 36
+    "project_bwd": dict(g=1284),                 # incl. SH Adam on 48 coefficients
+    "adam": dict(g=368),                         # 4 groups (308) + regularizer (60)
+    "sgld": dict(g=80),
+}
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def build_workload(seed=0, n_model=N_MODEL, views=VIEWS):
+    import numpy as np
+    from msplat_gb300 import synthetic as S
+    sc = S.config_full(seed, n_train=views, n_test=0)
+    rng = np.random.default_rng(seed + 5)
+    sel = np.sort(rng.choice(sc.gt.n, n_model, replace=False))
+    model = S.GaussianSet(*(np.ascontiguousarray(a[sel]) for a in sc.gt.arrays()))
+    model.means += rng.normal(0.0, 0.01, model.means.shape).astype(np.float32)
+    return sc, model
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+
+    def summary(self):
+        self.f.flush()
+        rows = []
+        try:
+            with open(self.f.name) as fh:
+                for line in fh:
+                    parts = [x.strip() for x in line.split(",")]
+                    if len(parts) >= 9:
+                        rows.append(parts)
+        except OSError:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(model, cam_dict, gt, steps=4):
+    """FP64 oracle (OpenMP, all host cores) timed on full iterations of the workload."""
+    from msplat_gb300 import engine as E
+    from oracle import oracle as O
+    g = model.copy()
+    mom = ([__import__("numpy").zeros_like(a) for a in g.arrays()],
+           [__import__("numpy").zeros_like(a) for a in g.arrays()])
+    times = []
+    for k in range(steps):
+        st = E.step_scalars(3001 + k, 3001 + k, width=cam_dict["width"], height=cam_dict["height"])
+        t0 = time.perf_counter()
+        O.train_step(64, g, cam_dict, st, moments=mom, gt=gt, do_sgld=True, want_ids=False)
+        times.append(time.perf_counter() - t0)
+    sec = statistics.median(times[1:] if len(times) > 2 else times)
+    return {"value": 1.0 / sec, "unit": "iters/s", "cores": O.num_threads(), "kind": "port",
+            "sample": f"{len(times)} full FP64 iterations of the workload (1M Gaussians, 1297x840, view 0), "
+                      f"median {sec:.2f} s/iter"}
+
+
+def run_reference(args):
+    """--impl reference: the CPU restatement of the reference step (oracle)."""
+    import numpy as np
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from msplat_gb300 import engine as E
+    from oracle import oracle as O
+    sc, model = build_workload()
+    cam = sc.train_cams[0]
+    cd = E.camera_dict(cam)
+    ref = O.train_step(64, sc.gt.copy(), cd, {"degrees_to_use": 3}, do_backward=False, do_optimizer=False,
+                       want_ids=False)
+    gt = (np.clip(ref["out_img"], 0, 1) * 255 + 0.5).astype(np.uint8)
+    g = model.copy()
+    mom = ([np.zeros_like(a) for a in g.arrays()], [np.zeros_like(a) for a in g.arrays()])
+
+    def step(k):
+        st = E.step_scalars(3001 + k, 3001 + k, width=cam.width, height=cam.height)
+        O.train_step(64, g, cd, st, moments=mom, gt=gt, do_sgld=True, want_ids=False)
+
+    for k in range(args.warmup):
+        step(k)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        step(args.warmup + k)
+    sec = (time.perf_counter() - t0) / max(1, args.steps)
+    v = 1.0 / sec
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "iters/s", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": config_dict(args),
+           "cpu_baseline": {"value": v, "unit": "iters/s", "cores": O.num_threads(), "kind": "port",
+                            "sample": "full FP64 iterations of the workload (the reference is Metal-only: "
+                                      "unavailable on this box; its CPU restatement is timed)"},
+           "e2e": {"value": v, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def config_dict(args):
+    return {"workload": "1M Gaussians (SH deg 3) training step at 1297x840, synthetic 1M+200k GT scene",
+            "n_gaussians": N_MODEL, "width": 1297, "height": 840, "views": VIEWS, "sh_degree": 3,
+            "raster": "monolithic (4346 tiles >= 400)", "l2": "working set > L2 (params+moments 0.7 GB/step)",
+            "seed": 0}
+
+
+def run_engine(args):
+    import numpy as np
+    import torch
+    from msplat_gb300 import engine as E
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+    sc, model = build_workload()
+    eng = E.Engine(local, N_MODEL)
+    cams = [E.camera_dict(c) for c in sc.train_cams]
+
+    # targets: the GT scene rendered by the engine (forward path, parity-tested)
+    gt_dev = E.DeviceGaussians(sc.gt)
+    gts_host, gts_dev = [], []
+    for cd in cams:
+        eng.render(gt_dev, E.make_args(cd, {"degrees_to_use": 3}))
+        img = eng.read("out_img", np.float32, cd["width"] * cd["height"] * 3).reshape(cd["height"], cd["width"], 3)
+        u8 = (np.clip(img, 0, 1) * 255 + 0.5).astype(np.uint8)
+        gts_host.append(torch.from_numpy(u8).pin_memory())
+        gts_dev.append(torch.from_numpy(u8).cuda())
+    del gt_dev
+    torch.cuda.synchronize()
+
+    dg = E.DeviceGaussians(model)
+    step_base = 3001
+
+    def one(k, host):
+        cd = cams[k % len(cams)]
+        st = E.step_scalars(step_base + k, step_base + k, width=cd["width"], height=cd["height"])
+        a = E.make_args(cd, st, do_sgld=True)
+        if host:
+            eng.train_step_host(dg, a, gts_host[k % len(cams)].data_ptr())
+        else:
+            eng.train_step(dg, a, gts_dev[k % len(cams)].data_ptr())
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+
+    def max_over_ranks(x):
+        if ws == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    for k in range(args.warmup):
+        one(k, False)
+    eng.synchronize()
+
+    # kernel-only: targets resident in HBM
+    launches0 = eng.stats().launches
+    eng.set_timing(True)
+    with Clocks(local) as clk:
+        barrier()
+        torch.cuda.synchronize()
+        eng.synchronize()
+        eng.marker(0)
+        for k in range(args.steps):
+            one(args.warmup + k, False)
+        eng.marker(1)
+        dev_ms = eng.marker_elapsed()
+        eng.synchronize()
+        barrier()
+    st = eng.stats()
+    eng.set_timing(False)
+    launches = st.launches - launches0
+    dev_ms = max_over_ranks(dev_ms)
+    ms_step = dev_ms / args.steps
+    value = ws * args.steps / (dev_ms / 1e3)
+
+    # end to end through the C ABI: pinned host image in, loss out, every step
+    barrier()
+    eng.synchronize()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        one(args.warmup + args.steps + k, True)
+        eng.loss()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e = {"value": ws * args.steps / e2e_s, "unit": "iters/s",
+           "h2d_bytes_per_step": int(gts_host[0].numel()), "d2h_bytes_per_step": 4}
+
+    # roofline of the dominant stage (CUDA events on the engine's stream)
+    stage_ms = {name: st.stage_ms[i] / max(1, st.timed_steps) for i, name in enumerate(E.N.STAGES)}
+    units = {"g": N_MODEL, "i": float(st.num_intersections), "p": 1297 * 840}
+    dom = max(stage_ms, key=stage_ms.get)
+    alg = sum(units[u] * b for u, b in STAGE_BYTES[dom].items())
+    peak, kind = measured_peaks()
+    achieved = alg / (stage_ms[dom] / 1e3) / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tf):
+        try:
+            traffic = json.load(open(tf)).get(dom)
+        except (OSError, ValueError):
+            traffic = None
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_kind": kind, "traffic": traffic,
+                "algorithmic_bytes": alg, "ms": stage_ms[dom]}
+
+    out = {"metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": ws, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_dict(args),
+           "roofline": roofline, "stage_ms": stage_ms, "num_intersections": int(st.num_intersections),
+           "max_tile_count": int(st.max_tile_count), "gpu_launches": int(launches), "e2e": e2e,
+           "clocks": clk.summary()}
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        cd = cams[0]
+        out["cpu_baseline"] = cpu_baseline(model, cd, gts_host[0].numpy(), steps=args.cpu_steps)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    eng.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=4)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        log("warmup raised to 3")
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_engine(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

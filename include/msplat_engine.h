@@ -70,7 +70,7 @@ typedef struct {
     float noise_lr, xyz_lr, max_disp;
 } MsplatStepArgs;
 
-/* Per-stage device time of the last step (ms), when timing is enabled. */
+/* Pipeline stages timed with CUDA events on the engine's stream. */
 enum {
     MSPLAT_STAGE_PROJECT = 0, MSPLAT_STAGE_TILES, MSPLAT_STAGE_RASTER_FWD, MSPLAT_STAGE_LOSS,
     MSPLAT_STAGE_RASTER_BWD, MSPLAT_STAGE_PROJECT_BWD, MSPLAT_STAGE_ADAM, MSPLAT_STAGE_SGLD,
@@ -83,7 +83,9 @@ typedef struct {
     int k_max;                     /* 1 = monolithic raster */
     int num_tiles;
     uint32_t nan_counts[16];       /* cumulative non-finite telemetry (reference slot numbering) */
-    float stage_ms[MSPLAT_STAGE_COUNT];
+    float stage_ms[MSPLAT_STAGE_COUNT];  /* summed over timed_steps steps since timing was enabled */
+    long long timed_steps;         /* steps whose stage times are summed (at most the last 128) */
+    long long launches;            /* engine kernel launches since creation */
     uint32_t check_record[3];      /* checked builds: first failed bound (code, index lo, index hi) */
 } MsplatEngineStats;
 
@@ -100,6 +102,13 @@ const char *msplat_engine_last_error(const MsplatEngine *e);
 int msplat_engine_train_step(MsplatEngine *e, const MsplatGaussians *g, const MsplatAdamState *st,
                              const MsplatStepArgs *args, const uint8_t *gt, const uint8_t *mask);
 
+/* The same step with the target image (and mask) in host memory: they are
+ * copied to the device on the engine's stream first (asynchronously when the
+ * host buffers are page-locked), as the reference reads the camera's image
+ * each step (core/src/msplat_api.mm:104-110). */
+int msplat_engine_train_step_host(MsplatEngine *e, const MsplatGaussians *g, const MsplatAdamState *st,
+                                  const MsplatStepArgs *args, const uint8_t *gt_host, const uint8_t *mask_host);
+
 /* Forward only (msplat_render); the image stays in the engine's "out_img"
  * buffer (device float [H,W,3]).  Asynchronous. */
 int msplat_engine_render(MsplatEngine *e, const MsplatGaussians *g, const MsplatStepArgs *args);
@@ -113,7 +122,8 @@ int msplat_engine_loss(MsplatEngine *e, float *loss);
 /* Stats of the last step; waits. */
 int msplat_engine_stats(MsplatEngine *e, MsplatEngineStats *out);
 
-/* Enables per-stage CUDA-event timing (adds events to the stream). */
+/* Enables (and resets) per-stage CUDA-event timing: each step records
+ * events between its stages on the engine's stream. */
 int msplat_engine_set_timing(MsplatEngine *e, int enabled);
 
 /* Named intermediate buffers ("rec", "depths", "radii", "aabb", "tiles_hit",
@@ -124,6 +134,12 @@ long long msplat_engine_buffer(MsplatEngine *e, const char *name, void **dev_ptr
 
 /* Copies the first `bytes` of a named buffer to host memory; waits. */
 int msplat_engine_read(MsplatEngine *e, const char *name, void *dst, long long bytes);
+
+/* Two CUDA events on the engine's stream for timing a span of steps:
+ * marker(0) before, marker(1) after, then marker_elapsed waits for the second
+ * and returns the device time between them in ms. */
+int msplat_engine_marker(MsplatEngine *e, int which);
+int msplat_engine_marker_elapsed(MsplatEngine *e, float *ms);
 
 /* The engine's CUDA stream (cudaStream_t). */
 void *msplat_engine_stream(MsplatEngine *e);

@@ -47,7 +47,7 @@ STAGES = ("project", "tiles", "raster_fwd", "loss", "raster_bwd", "project_bwd",
 class MsplatEngineStats(C.Structure):
     _fields_ = [("num_intersections", C.c_longlong), ("max_tile_count", C.c_int), ("k_max", C.c_int),
                 ("num_tiles", C.c_int), ("nan_counts", C.c_uint32 * 16), ("stage_ms", C.c_float * len(STAGES)),
-                ("check_record", C.c_uint32 * 3)]
+                ("timed_steps", C.c_longlong), ("launches", C.c_longlong), ("check_record", C.c_uint32 * 3)]
 
 
 def lib(build_if_missing: bool = True):
@@ -69,6 +69,8 @@ def lib(build_if_missing: bool = True):
         L.msplat_engine_last_error.restype = C.c_char_p
         L.msplat_engine_train_step.argtypes = [vp, C.POINTER(MsplatGaussians), C.POINTER(MsplatAdamState),
                                                C.POINTER(MsplatStepArgs), vp, vp]
+        L.msplat_engine_train_step_host.argtypes = [vp, C.POINTER(MsplatGaussians), C.POINTER(MsplatAdamState),
+                                                    C.POINTER(MsplatStepArgs), vp, vp]
         L.msplat_engine_render.argtypes = [vp, C.POINTER(MsplatGaussians), C.POINTER(MsplatStepArgs)]
         L.msplat_engine_synchronize.argtypes = [vp]
         L.msplat_engine_loss.argtypes = [vp, FP]
@@ -77,6 +79,8 @@ def lib(build_if_missing: bool = True):
         L.msplat_engine_buffer.argtypes = [vp, C.c_char_p, C.POINTER(C.c_void_p)]
         L.msplat_engine_buffer.restype = C.c_longlong
         L.msplat_engine_read.argtypes = [vp, C.c_char_p, vp, C.c_longlong]
+        L.msplat_engine_marker.argtypes = [vp, C.c_int]
+        L.msplat_engine_marker_elapsed.argtypes = [vp, FP]
         L.msplat_engine_stream.argtypes = [vp]
         L.msplat_engine_stream.restype = vp
         _lib = L

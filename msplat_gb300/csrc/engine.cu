@@ -44,13 +44,17 @@ class Engine {
         cudaDeviceProp prop;
         CK(cudaGetDeviceProperties(&prop, device));
         num_sms_ = prop.multiProcessorCount;
-        for (auto &ev : ev_) CK(cudaEventCreate(&ev));
+        for (auto &row : ev_)
+            for (auto &ev : row) CK(cudaEventCreate(&ev));
+        for (auto &ev : marker_) CK(cudaEventCreate(&ev));
     }
     ~Engine() {
         cudaSetDevice(device_);
         cudaStreamSynchronize(stream_);
         for (auto &kv : bufs_) cudaFree(kv.second.ptr);
-        for (auto &ev : ev_) cudaEventDestroy(ev);
+        for (auto &row : ev_)
+            for (auto &ev : row) cudaEventDestroy(ev);
+        for (auto &ev : marker_) cudaEventDestroy(ev);
         cudaStreamDestroy(stream_);
     }
 
@@ -72,6 +76,13 @@ class Engine {
         if (K > 1) ensure_chunks((long long)K * P);
         last_T_ = T;
         last_K_ = K;
+        if (timing_) slot_ = (timed_steps_++) % kRing;
+        // kernels of this step: projection, count/scan/scatter/sort, raster
+        // (+ merge when chunked), and for training 3 loss passes, raster
+        // backward (+ prefix/suffix), projection backward, Adam, SGLD
+        launches_ += 5 + (K > 1 ? 2 : 1);
+        if (gt) launches_ += 3;
+        if (gt && backward) launches_ += (K > 1 ? 2 : 1) + 1 + (args.do_optimizer && st ? 1 : 0) + (args.do_sgld ? 1 : 0);
 
         StepParams sp;
         fill_params(args, sp, mask != nullptr);
@@ -167,6 +178,23 @@ class Engine {
         CK(cudaGetLastError());
     }
 
+    // Copies host images into engine-owned device buffers on the engine's
+    // stream (asynchronous for page-locked sources), then runs the step.
+    void train_step_host(const MsplatGaussians &g, const MsplatAdamState *st, const MsplatStepArgs &args,
+                         const uint8_t *gt_host, const uint8_t *mask_host) {
+        CK(cudaSetDevice(device_));
+        const size_t P = (size_t)args.width * args.height;
+        alloc("gt_stage", P * 3);
+        CK(cudaMemcpyAsync(ptr<uint8_t>("gt_stage"), gt_host, P * 3, cudaMemcpyHostToDevice, stream_));
+        const uint8_t *mask_d = nullptr;
+        if (mask_host) {
+            alloc("mask_stage", P);
+            CK(cudaMemcpyAsync(ptr<uint8_t>("mask_stage"), mask_host, P, cudaMemcpyHostToDevice, stream_));
+            mask_d = ptr<uint8_t>("mask_stage");
+        }
+        train_step(g, st, args, ptr<uint8_t>("gt_stage"), mask_d, true);
+    }
+
     void synchronize() { CK(cudaStreamSynchronize(stream_)); }
 
     float loss() {
@@ -194,15 +222,30 @@ class Engine {
             std::memcpy(o.nan_counts, tmp, 64);
             std::memcpy(o.check_record, tmp + kDbgSlot, sizeof(o.check_record));
         }
-        if (timing_) {
+        o.launches = launches_;
+        o.timed_steps = timed_steps_;
+        // stage time summed over the timed steps still held in the ring
+        const long long held = std::min<long long>(timed_steps_, kRing);
+        for (long long r = 0; r < held; r++)
             for (int s = 0; s < MSPLAT_STAGE_COUNT; s++) {
                 float ms = 0;
-                if (cudaEventElapsedTime(&ms, ev_[s], ev_[s + 1]) == cudaSuccess) o.stage_ms[s] = ms;
+                if (cudaEventElapsedTime(&ms, ev_[r][s], ev_[r][s + 1]) == cudaSuccess) o.stage_ms[s] += ms;
             }
-        }
+        o.timed_steps = held;
     }
 
-    void set_timing(bool on) { timing_ = on; }
+    void record_marker(int which) { CK(cudaEventRecord(marker_[which & 1], stream_)); }
+    float marker_elapsed() {
+        CK(cudaEventSynchronize(marker_[1]));
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, marker_[0], marker_[1]));
+        return ms;
+    }
+
+    void set_timing(bool on) {
+        timing_ = on;
+        timed_steps_ = 0;
+    }
 
     long long buffer(const std::string &name, void **p) {
         auto it = bufs_.find(name);
@@ -330,7 +373,7 @@ class Engine {
     }
 
     void mark(int s) {
-        if (timing_) CK(cudaEventRecord(ev_[s], stream_));
+        if (timing_) CK(cudaEventRecord(ev_[slot_][s], stream_));
     }
 
     int device_ = 0, num_sms_ = 1;
@@ -340,7 +383,11 @@ class Engine {
     long long cap_isect_ = 0, cap_pixels_ = 0, cap_chunks_ = 0, last_P_ = 1;
     int last_T_ = 0, last_K_ = 1;
     bool timing_ = false;
-    cudaEvent_t ev_[MSPLAT_STAGE_COUNT + 1];
+    static constexpr int kRing = 128;
+    cudaEvent_t ev_[kRing][MSPLAT_STAGE_COUNT + 1];
+    cudaEvent_t marker_[2];
+    int slot_ = 0;
+    long long timed_steps_ = 0, launches_ = 0;
 };
 
 }  // namespace msplat
@@ -392,6 +439,12 @@ int msplat_engine_train_step(MsplatEngine *e, const MsplatGaussians *g, const Ms
     return guarded(e, [&] { e->impl->train_step(*g, st, *args, gt, mask, true); });
 }
 
+int msplat_engine_train_step_host(MsplatEngine *e, const MsplatGaussians *g, const MsplatAdamState *st,
+                                  const MsplatStepArgs *args, const uint8_t *gt_host, const uint8_t *mask_host) {
+    if (!g || !args || !gt_host) return -1;
+    return guarded(e, [&] { e->impl->train_step_host(*g, st, *args, gt_host, mask_host); });
+}
+
 int msplat_engine_render(MsplatEngine *e, const MsplatGaussians *g, const MsplatStepArgs *args) {
     if (!g || !args) return -1;
     return guarded(e, [&] { e->impl->train_step(*g, nullptr, *args, nullptr, nullptr, false); });
@@ -430,6 +483,15 @@ int msplat_engine_read(MsplatEngine *e, const char *name, void *dst, long long b
         e->impl->synchronize();
         CK(cudaMemcpy(dst, p, (size_t)bytes, cudaMemcpyDeviceToHost));
     });
+}
+
+int msplat_engine_marker(MsplatEngine *e, int which) {
+    return guarded(e, [&] { e->impl->record_marker(which); });
+}
+
+int msplat_engine_marker_elapsed(MsplatEngine *e, float *ms) {
+    if (!ms) return -1;
+    return guarded(e, [&] { *ms = e->impl->marker_elapsed(); });
 }
 
 void *msplat_engine_stream(MsplatEngine *e) { return (e && e->impl) ? (void *)e->impl->stream() : nullptr; }

@@ -139,6 +139,12 @@ class Engine:
         self._check(self.L.msplat_engine_train_step(self.h, C.byref(g), C.byref(st), C.byref(args), gt_ptr,
                                                     mask_ptr or None))
 
+    def train_step_host(self, dg: DeviceGaussians, args: N.MsplatStepArgs, gt_host_ptr: int,
+                        mask_host_ptr: int | None = None):
+        g, st = dg.native()
+        self._check(self.L.msplat_engine_train_step_host(self.h, C.byref(g), C.byref(st), C.byref(args), gt_host_ptr,
+                                                         mask_host_ptr or None))
+
     def render(self, dg: DeviceGaussians, args: N.MsplatStepArgs):
         g, _ = dg.native()
         self._check(self.L.msplat_engine_render(self.h, C.byref(g), C.byref(args)))
@@ -168,6 +174,14 @@ class Engine:
         out = np.zeros(count, dtype)
         self._check(self.L.msplat_engine_read(self.h, name.encode(), out.ctypes.data, out.nbytes))
         return out
+
+    def marker(self, which: int):
+        self._check(self.L.msplat_engine_marker(self.h, which))
+
+    def marker_elapsed(self) -> float:
+        v = C.c_float()
+        self._check(self.L.msplat_engine_marker_elapsed(self.h, C.byref(v)))
+        return float(v.value)
 
     def stream(self) -> int:
         return self.L.msplat_engine_stream(self.h)
