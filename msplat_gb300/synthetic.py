@@ -179,5 +179,5 @@ def config_full(seed: int = 0, n: int = 1_000_000, ground: int = 200_000, n_trai
     w, h = 1297, 840
     fx = 0.5 * w / math.tan(0.5 * math.radians(60.0))
     train = ring_cameras(n_train, w, h, fx, seed=seed + 11, jitter=1.0)
-    test = ring_cameras(n_test, w, h, fx, seed=seed + 13, jitter=1.0, phase=math.pi / n_test)
+    test = ring_cameras(n_test, w, h, fx, seed=seed + 13, jitter=1.0, phase=math.pi / max(n_test, 1))
     return Scene(gt, train, test)
