@@ -26,186 +26,267 @@ __device__ __forceinline__ void adam_el(float *p, float *m, float *v, float g, f
     *v = vv;
 }
 
-__device__ __forceinline__ void mat3mul(const float A[3][3], const float B[3][3], float C[3][3]) {
+// Per-warp staging of the SH Adam inputs: the basis values of the warp's 32
+// Gaussians and their colour gradients (w = number of rest bands to update,
+// 0 when the Gaussian is culled or its colour gradient is non-finite).
+struct ShStage {
+    float bas[32][16];
+    float4 vc[32];
+};
+
+__device__ __forceinline__ void adam4(float4 &p, float4 &m, float4 &v, const float g[4], unsigned active, float st,
+                                      float bc, float b1, float b2, float eps) {
+    float *pp = &p.x, *mm = &m.x, *vv = &v.x;
 #pragma unroll
-    for (int r = 0; r < 3; r++)
-#pragma unroll
-        for (int c = 0; c < 3; c++) C[r][c] = A[r][0] * B[0][c] + A[r][1] * B[1][c] + A[r][2] * B[2][c];
+    for (int k = 0; k < 4; k++) {
+        if (!(active & (1u << k))) continue;
+        const float nm = fmaf(b1, mm[k], (1.0f - b1) * g[k]);
+        const float nv = fmaf(b2, vv[k], (1.0f - b2) * g[k] * g[k]);
+        pp[k] -= st * nm / (sqrtf(nv) / bc + eps);
+        mm[k] = nm;
+        vv[k] = nv;
+    }
 }
 
 __global__ void __launch_bounds__(256) k_project_bwd(ProjectBwdArgs a) {
+    __shared__ ShStage stage[8];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n) return;
-    float *vmean = a.v_mean + 3 * (size_t)i, *vscale = a.v_scale + 3 * (size_t)i, *vquat = a.v_quat + 4 * (size_t)i;
-    if (a.radii[i] <= 0) {
-        vmean[0] = vmean[1] = vmean[2] = 0.f;
-        vscale[0] = vscale[1] = vscale[2] = 0.f;
-        *reinterpret_cast<float4 *>(vquat) = make_float4(0.f, 0.f, 0.f, 0.f);
-        return;
-    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    ShStage &sh = stage[wid];
     const StepParams &sp = *a.sp;
-    const GradRec gr = a.grad[i];
-    const SplatRec rec = a.rec[i];
-    const float px = a.means[3 * i], py = a.means[3 * i + 1], pz = a.means[3 * i + 2];
+    sh.vc[lane] = make_float4(0.f, 0.f, 0.f, 0.f);   // w = 0: nothing to update
+    if (i < a.n) {
+        float *vmean = a.v_mean + 3 * (size_t)i, *vscale = a.v_scale + 3 * (size_t)i, *vquat = a.v_quat + 4 * (size_t)i;
+        if (a.radii[i] <= 0) {
+            vmean[0] = vmean[1] = vmean[2] = 0.f;
+            vscale[0] = vscale[1] = vscale[2] = 0.f;
+            *reinterpret_cast<float4 *>(vquat) = make_float4(0.f, 0.f, 0.f, 0.f);
+        } else {
+            const GradRec gr = a.grad[i];
+            const SplatRec rec = a.rec[i];
+            const float px = a.means[3 * i], py = a.means[3 * i + 1], pz = a.means[3 * i + 2];
 
-    // project_pix_vjp
-    const float *m = sp.projmat;
-    const float hw = m[12] * px + m[13] * py + m[14] * pz + m[15];
-    const float rw = 1.f / (hw + 1e-6f);
-    const float vnx = 0.5f * a.Wf * gr.a.x, vny = 0.5f * a.Hf * gr.a.y;
-    const float vp0 = vnx * rw, vp1 = vny * rw;
-    float vm[3];
+            // project_pix_vjp
+            const float *m = sp.projmat;
+            const float hw = m[12] * px + m[13] * py + m[14] * pz + m[15];
+            const float rw = 1.f / (hw + 1e-6f);
+            const float vnx = 0.5f * a.Wf * gr.a.x, vny = 0.5f * a.Hf * gr.a.y;
+            const float vp0 = vnx * rw, vp1 = vny * rw;
+            float vm[3];
 #pragma unroll
-    for (int c = 0; c < 3; c++) vm[c] = m[c] * vp0 + m[4 + c] * vp1;
+            for (int c = 0; c < 3; c++) vm[c] = m[c] * vp0 + m[4 + c] * vp1;
 
-    // cov2d_to_conic_vjp: v_Sigma = -X G X
-    const float X00 = rec.b.x, X01 = rec.b.y, X11 = rec.b.z;
-    const float G00 = gr.b.x, G01 = gr.b.y, G11 = gr.b.z;
-    const float XG00 = X00 * G00 + X01 * G01, XG01 = X00 * G01 + X01 * G11;
-    const float XG10 = X01 * G00 + X11 * G01, XG11 = X01 * G01 + X11 * G11;
-    const float VS00 = -(XG00 * X00 + XG01 * X01), VS01 = -(XG00 * X01 + XG01 * X11);
-    const float VS10 = -(XG10 * X00 + XG11 * X01), VS11 = -(XG10 * X01 + XG11 * X11);
-    const float vc_a = VS00, vc_b = VS10 + VS01, vc_c = VS11;
+            // cov2d_to_conic_vjp: v_Sigma = -X G X
+            const float X00 = rec.b.x, X01 = rec.b.y, X11 = rec.b.z;
+            const float G00 = gr.b.x, G01 = gr.b.y, G11 = gr.b.z;
+            const float XG00 = X00 * G00 + X01 * G01, XG01 = X00 * G01 + X01 * G11;
+            const float XG10 = X01 * G00 + X11 * G01, XG11 = X01 * G01 + X11 * G11;
+            const float VS00 = -(XG00 * X00 + XG01 * X01), VS01 = -(XG00 * X01 + XG01 * X11);
+            const float VS10 = -(XG10 * X00 + XG11 * X01), VS11 = -(XG10 * X01 + XG11 * X11);
+            const float c00 = VS00, c01 = 0.5f * (VS10 + VS01), c11 = VS11;
 
-    // recompute cov3d
-    float s[3];
+            // recompute cov3d
+            float s[3];
 #pragma unroll
-    for (int k = 0; k < 3; k++) s[k] = det_expf(fminf(fmaxf(a.scales[3 * i + k], -15.f), 15.f));
-    const float4 q = *reinterpret_cast<const float4 *>(a.quats + 4 * (size_t)i);
-    const float qn = 1.0f / sqrtf(fmaxf(q.w * q.w + q.x * q.x + q.y * q.y + q.z * q.z, 1e-8f));
-    const float w = q.x * qn, x = q.y * qn, y = q.z * qn, z = q.w * qn;
-    float R[3][3];
-    R[0][0] = 1.f - 2.f * (y * y + z * z); R[1][0] = 2.f * (x * y + w * z); R[2][0] = 2.f * (x * z - w * y);
-    R[0][1] = 2.f * (x * y - w * z); R[1][1] = 1.f - 2.f * (x * x + z * z); R[2][1] = 2.f * (y * z + w * x);
-    R[0][2] = 2.f * (x * z + w * y); R[1][2] = 2.f * (y * z - w * x); R[2][2] = 1.f - 2.f * (x * x + y * y);
-    float M[3][3], V[3][3];
+            for (int k = 0; k < 3; k++) s[k] = det_expf(fminf(fmaxf(a.scales[3 * i + k], -15.f), 15.f));
+            const float4 q = *reinterpret_cast<const float4 *>(a.quats + 4 * (size_t)i);
+            const float qn = 1.0f / sqrtf(fmaxf(q.w * q.w + q.x * q.x + q.y * q.y + q.z * q.z, 1e-8f));
+            const float w = q.x * qn, x = q.y * qn, y = q.z * qn, z = q.w * qn;
+            float R[3][3];
+            R[0][0] = 1.f - 2.f * (y * y + z * z); R[1][0] = 2.f * (x * y + w * z); R[2][0] = 2.f * (x * z - w * y);
+            R[0][1] = 2.f * (x * y - w * z); R[1][1] = 1.f - 2.f * (x * x + z * z); R[2][1] = 2.f * (y * z + w * x);
+            R[0][2] = 2.f * (x * z + w * y); R[1][2] = 2.f * (y * z - w * x); R[2][2] = 1.f - 2.f * (x * x + y * y);
+            float M[3][3], V[3][3];
 #pragma unroll
-    for (int r = 0; r < 3; r++)
+            for (int r = 0; r < 3; r++)
 #pragma unroll
-        for (int c = 0; c < 3; c++) M[r][c] = R[r][c] * s[c];
+                for (int c = 0; c < 3; c++) M[r][c] = R[r][c] * s[c];
 #pragma unroll
-    for (int r = 0; r < 3; r++)
+            for (int r = 0; r < 3; r++)
 #pragma unroll
-        for (int c = 0; c < 3; c++) V[r][c] = M[r][0] * M[c][0] + M[r][1] * M[c][1] + M[r][2] * M[c][2];
+                for (int c = 0; c < 3; c++) V[r][c] = M[r][0] * M[c][0] + M[r][1] * M[c][1] + M[r][2] * M[c][2];
 
-    // project_cov3d_ewa_vjp
-    const float *v = sp.viewmat;
-    const float vx = v[0] * px + v[1] * py + v[2] * pz + v[3];
-    const float vy = v[4] * px + v[5] * py + v[6] * pz + v[7];
-    const float vz = v[8] * px + v[9] * py + v[10] * pz + v[11];
-    const float lim_x = 1.3f * sp.tan_fovx, lim_y = 1.3f * sp.tan_fovy;
-    const float cvx = vz * fminf(lim_x, fmaxf(-lim_x, vx / vz));
-    const float cvy = vz * fminf(lim_y, fmaxf(-lim_y, vy / vz));
-    const float rz = 1.f / vz, rz2 = rz * rz, rz3 = rz2 * rz;
-    float Wm[3][3], J[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+            // project_cov3d_ewa_vjp
+            const float *v = sp.viewmat;
+            const float vx = v[0] * px + v[1] * py + v[2] * pz + v[3];
+            const float vy = v[4] * px + v[5] * py + v[6] * pz + v[7];
+            const float vz = v[8] * px + v[9] * py + v[10] * pz + v[11];
+            const float lim_x = 1.3f * sp.tan_fovx, lim_y = 1.3f * sp.tan_fovy;
+            const float cvx = vz * fminf(lim_x, fmaxf(-lim_x, vx / vz));
+            const float cvy = vz * fminf(lim_y, fmaxf(-lim_y, vy / vz));
+            const float rz = 1.f / vz, rz2 = rz * rz, rz3 = rz2 * rz;
+            // rows 0, 1 of T = J W (row 2 of J is zero)
+            const float j00 = sp.fx * rz, j11 = sp.fy * rz, j02 = -sp.fx * cvx * rz2, j12 = -sp.fy * cvy * rz2;
+            float T0[3], T1[3];
 #pragma unroll
-    for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) {
+                T0[c] = j00 * v[c] + j02 * v[8 + c];
+                T1[c] = j11 * v[4 + c] + j12 * v[8 + c];
+            }
+            // v_V = T^T v_cov T
+            float vV[3][3];
 #pragma unroll
-        for (int c = 0; c < 3; c++) Wm[r][c] = v[4 * r + c];
-    J[0][0] = sp.fx * rz; J[1][1] = sp.fy * rz;
-    J[0][2] = -sp.fx * cvx * rz2; J[1][2] = -sp.fy * cvy * rz2;
-    float Tm[3][3];
-    mat3mul(J, Wm, Tm);
-    // v_cov (symmetric, only the upper-left 2x2 non-zero)
-    const float c00 = vc_a, c01 = 0.5f * vc_b, c11 = vc_c;
-    // v_V = T^T v_cov T ; only rows 0,1 of T matter
-    float vV[3][3];
+            for (int r = 0; r < 3; r++)
 #pragma unroll
-    for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++)
+                    vV[r][c] = (T0[r] * c00 + T1[r] * c01) * T0[c] + (T0[r] * c01 + T1[r] * c11) * T1[c];
+            // v_T = 2 v_cov T V (rows 0, 1), v_J = v_T W^T
+            float TV0[3], TV1[3];
 #pragma unroll
-        for (int c = 0; c < 3; c++) {
-            const float t0r = Tm[0][r], t1r = Tm[1][r];
-            vV[r][c] = (t0r * c00 + t1r * c01) * Tm[0][c] + (t0r * c01 + t1r * c11) * Tm[1][c];
+            for (int c = 0; c < 3; c++) {
+                TV0[c] = T0[0] * V[0][c] + T0[1] * V[1][c] + T0[2] * V[2][c];
+                TV1[c] = T1[0] * V[0][c] + T1[1] * V[1][c] + T1[2] * V[2][c];
+            }
+            float vT0[3], vT1[3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                vT0[c] = 2.f * (c00 * TV0[c] + c01 * TV1[c]);
+                vT1[c] = 2.f * (c01 * TV0[c] + c11 * TV1[c]);
+            }
+            const float vJ00 = vT0[0] * v[0] + vT0[1] * v[1] + vT0[2] * v[2];
+            const float vJ02 = vT0[0] * v[8] + vT0[1] * v[9] + vT0[2] * v[10];
+            const float vJ11 = vT1[0] * v[4] + vT1[1] * v[5] + vT1[2] * v[6];
+            const float vJ12 = vT1[0] * v[8] + vT1[1] * v[9] + vT1[2] * v[10];
+            const float fxr = sp.fx * rz2, fyr = sp.fy * rz2;
+            const float vt0 = -fxr * vJ02, vt1 = -fyr * vJ12;
+            const float vt2 = -fxr * vJ00 + 2.f * sp.fx * cvx * rz3 * vJ02 - fyr * vJ11 + 2.f * sp.fy * cvy * rz3 * vJ12;
+#pragma unroll
+            for (int c = 0; c < 3; c++) vm[c] += vt0 * v[c] + vt1 * v[4 + c] + vt2 * v[8 + c];
+            vmean[0] = vm[0]; vmean[1] = vm[1]; vmean[2] = vm[2];
+
+            // scale_rot_to_cov3d_vjp + quat_to_rotmat_vjp
+            const float v01 = 0.5f * (vV[0][1] + vV[1][0]), v02 = 0.5f * (vV[0][2] + vV[2][0]);
+            const float v12 = 0.5f * (vV[1][2] + vV[2][1]);
+            const float vVs[3][3] = {{vV[0][0], v01, v02}, {v01, vV[1][1], v12}, {v02, v12, vV[2][2]}};
+            float gR[3][3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                float acc = 0.f;
+#pragma unroll
+                for (int r = 0; r < 3; r++) {
+                    const float vMrc = 2.f * (vVs[r][0] * M[0][c] + vVs[r][1] * M[1][c] + vVs[r][2] * M[2][c]);
+                    acc += R[r][c] * vMrc;
+                    gR[r][c] = vMrc * s[c];
+                }
+                vscale[c] = acc * s[c];
+            }
+            // gR[row][col]; the reference indexes v_R[col][row]
+            float4 vq;
+            vq.x = 2.f * (x * (gR[2][1] - gR[1][2]) + y * (gR[0][2] - gR[2][0]) + z * (gR[1][0] - gR[0][1]));
+            vq.y = 2.f * (-2.f * x * (gR[1][1] + gR[2][2]) + y * (gR[1][0] + gR[0][1]) + z * (gR[2][0] + gR[0][2]) +
+                          w * (gR[2][1] - gR[1][2]));
+            vq.z = 2.f * (x * (gR[1][0] + gR[0][1]) - 2.f * y * (gR[0][0] + gR[2][2]) + z * (gR[2][1] + gR[1][2]) +
+                          w * (gR[0][2] - gR[2][0]));
+            vq.w = 2.f * (x * (gR[2][0] + gR[0][2]) + y * (gR[2][1] + gR[1][2]) - 2.f * z * (gR[0][0] + gR[1][1]) +
+                          w * (gR[1][0] - gR[0][1]));
+            *reinterpret_cast<float4 *>(vquat) = vq;
+
+            // SH VJP inputs for the fused Adam below
+            if (a.do_optimizer) {
+                const float vc0 = gr.c.x, vc1 = gr.c.y, vc2 = gr.c.z;
+                if (!(finite_bits(vc0) && finite_bits(vc1) && finite_bits(vc2))) {
+                    if (a.nan_counts) atomicAdd(a.nan_counts + kNanSH, 1u);
+                } else {
+                    const int deg = sp.degrees_to_use;
+                    int nb = deg >= 3 ? 15 : deg == 2 ? 8 : deg == 1 ? 3 : 0;
+                    nb = min(nb, a.rest_bases);
+                    const float dx = px - sp.cam_pos[0], dy = py - sp.cam_pos[1], dz = pz - sp.cam_pos[2];
+                    const float inv = 1.f / sqrtf(dx * dx + dy * dy + dz * dz);
+                    const float X = dx * inv, Y = dy * inv, Z = dz * inv;
+                    const float xx = X * X, xy = X * Y, xz = X * Z, yy = Y * Y, yz = Y * Z, zz = Z * Z;
+                    float *b = sh.bas[lane];
+                    b[0] = -kBC1 * Y; b[1] = kBC1 * Z; b[2] = -kBC1 * X;
+                    b[3] = kBC2[0] * xy; b[4] = kBC2[1] * yz; b[5] = kBC2[2] * (2.f * zz - xx - yy);
+                    b[6] = kBC2[3] * xz; b[7] = kBC2[4] * (xx - yy);
+                    b[8] = kBC3[0] * Y * (3.f * xx - yy); b[9] = kBC3[1] * xy * Z;
+                    b[10] = kBC3[2] * Y * (4.f * zz - xx - yy); b[11] = kBC3[3] * Z * (2.f * zz - 3.f * xx - 3.f * yy);
+                    b[12] = kBC3[4] * X * (4.f * zz - xx - yy); b[13] = kBC3[5] * Z * (xx - yy);
+                    b[14] = kBC3[6] * X * (xx - 3.f * yy);
+                    b[15] = kBC0;
+                    sh.vc[lane] = make_float4(vc0, vc1, vc2, __int_as_float(nb + 1));   // w - 1 = rest bands
+                }
+            }
         }
-    // v_T = v_cov T V^T + v_cov^T T V = 2 v_cov T V (V symmetric)
-    float TV[3][3];
-    mat3mul(Tm, V, TV);
-    float vT[3][3];
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-        vT[0][c] = 2.f * (c00 * TV[0][c] + c01 * TV[1][c]);
-        vT[1][c] = 2.f * (c01 * TV[0][c] + c11 * TV[1][c]);
-        vT[2][c] = 0.f;
     }
-    // v_J = v_T W^T
-    float vJ[2][3];
-#pragma unroll
-    for (int r = 0; r < 2; r++)
-#pragma unroll
-        for (int c = 0; c < 3; c++) vJ[r][c] = vT[r][0] * Wm[c][0] + vT[r][1] * Wm[c][1] + vT[r][2] * Wm[c][2];
-    const float fxr = sp.fx * rz2, fyr = sp.fy * rz2;
-    const float vt0 = -fxr * vJ[0][2], vt1 = -fyr * vJ[1][2];
-    const float vt2 = -fxr * vJ[0][0] + 2.f * sp.fx * cvx * rz3 * vJ[0][2] - fyr * vJ[1][1] +
-                      2.f * sp.fy * cvy * rz3 * vJ[1][2];
-#pragma unroll
-    for (int c = 0; c < 3; c++) vm[c] += vt0 * Wm[0][c] + vt1 * Wm[1][c] + vt2 * Wm[2][c];
-    vmean[0] = vm[0]; vmean[1] = vm[1]; vmean[2] = vm[2];
-
-    // scale_rot_to_cov3d_vjp + quat_to_rotmat_vjp
-    const float v00 = vV[0][0], v01 = 0.5f * (vV[0][1] + vV[1][0]), v02 = 0.5f * (vV[0][2] + vV[2][0]);
-    const float v11 = vV[1][1], v12 = 0.5f * (vV[1][2] + vV[2][1]), v22 = vV[2][2];
-    const float vVs[3][3] = {{v00, v01, v02}, {v01, v11, v12}, {v02, v12, v22}};
-    float vM[3][3];
-    mat3mul(vVs, M, vM);
-    float gR[3][3];
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-        float acc = 0.f;
-#pragma unroll
-        for (int r = 0; r < 3; r++) {
-            vM[r][c] *= 2.f;
-            acc += R[r][c] * vM[r][c];
-            gR[r][c] = vM[r][c] * s[c];
-        }
-        vscale[c] = acc * s[c];
-    }
-    // gR[row][col]; the reference indexes v_R[col][row]
-    vquat[0] = 2.f * (x * (gR[2][1] - gR[1][2]) + y * (gR[0][2] - gR[2][0]) + z * (gR[1][0] - gR[0][1]));
-    vquat[1] = 2.f * (-2.f * x * (gR[1][1] + gR[2][2]) + y * (gR[1][0] + gR[0][1]) + z * (gR[2][0] + gR[0][2]) +
-                      w * (gR[2][1] - gR[1][2]));
-    vquat[2] = 2.f * (x * (gR[1][0] + gR[0][1]) - 2.f * y * (gR[0][0] + gR[2][2]) + z * (gR[2][1] + gR[1][2]) +
-                      w * (gR[0][2] - gR[2][0]));
-    vquat[3] = 2.f * (x * (gR[2][0] + gR[0][2]) + y * (gR[2][1] + gR[1][2]) - 2.f * z * (gR[0][0] + gR[1][1]) +
-                      w * (gR[1][0] - gR[0][1]));
-
-    // fused SH backward + Adam
     if (!a.do_optimizer) return;
-    const float vc0 = gr.c.x, vc1 = gr.c.y, vc2 = gr.c.z;
-    if (!(finite_bits(vc0) && finite_bits(vc1) && finite_bits(vc2))) {
-        if (a.nan_counts) atomicAdd(a.nan_counts + kNanSH, 1u);
-        return;
-    }
+    __syncwarp();
+    // fused SH Adam, warp-cooperative: the warp's 32 Gaussians own contiguous
+    // rows of features_dc / features_rest and their moments, walked with
+    // coalesced 16-byte accesses (the element's Gaussian, band and channel
+    // are recovered from its offset in the rows).
+    const int i0 = (blockIdx.x * blockDim.x) + wid * 32;
+    if (i0 >= a.n) return;
+    const int ng = min(32, a.n - i0);
     const float b1 = sp.beta1, b2 = sp.beta2, eps = sp.eps;
-    {
-        float *p = a.features_dc + 3 * (size_t)i, *mm = a.dc_m + 3 * (size_t)i, *vv = a.dc_v + 3 * (size_t)i;
-        adam_el(p + 0, mm + 0, vv + 0, kBC0 * vc0, sp.step_size[3], sp.bc2_sqrt[3], b1, b2, eps);
-        adam_el(p + 1, mm + 1, vv + 1, kBC0 * vc1, sp.step_size[3], sp.bc2_sqrt[3], b1, b2, eps);
-        adam_el(p + 2, mm + 2, vv + 2, kBC0 * vc2, sp.step_size[3], sp.bc2_sqrt[3], b1, b2, eps);
+    {   // features_dc: 3 floats per Gaussian
+        const int total = 3 * ng;
+        float *p = a.features_dc + 3 * (size_t)i0, *mm = a.dc_m + 3 * (size_t)i0, *vv = a.dc_v + 3 * (size_t)i0;
+        const float st = sp.step_size[3], bc = sp.bc2_sqrt[3];
+        for (int e0 = lane * 4; e0 < total; e0 += 128) {
+            float g[4];
+            unsigned act = 0;
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int e = e0 + k;
+                g[k] = 0.f;
+                if (e < total) {
+                    const int gi = e / 3, c = e - 3 * gi;
+                    const float4 vc = sh.vc[gi];
+                    if (__float_as_int(vc.w) > 0) {
+                        g[k] = sh.bas[gi][15] * (c == 0 ? vc.x : c == 1 ? vc.y : vc.z);
+                        act |= 1u << k;
+                    }
+                }
+            }
+            if (!act) continue;
+            if (e0 + 4 <= total) {
+                float4 P = *reinterpret_cast<float4 *>(p + e0), Mv = *reinterpret_cast<float4 *>(mm + e0),
+                       Vv = *reinterpret_cast<float4 *>(vv + e0);
+                adam4(P, Mv, Vv, g, act, st, bc, b1, b2, eps);
+                *reinterpret_cast<float4 *>(p + e0) = P;
+                *reinterpret_cast<float4 *>(mm + e0) = Mv;
+                *reinterpret_cast<float4 *>(vv + e0) = Vv;
+            } else {
+                for (int k = 0; k < 4 && e0 + k < total; k++)
+                    if (act & (1u << k)) adam_el(p + e0 + k, mm + e0 + k, vv + e0 + k, g[k], st, bc, b1, b2, eps);
+            }
+        }
     }
-    const int deg = sp.degrees_to_use;
-    int nb = deg >= 3 ? 15 : deg == 2 ? 8 : deg == 1 ? 3 : 0;
-    nb = min(nb, a.rest_bases);
-    if (nb == 0) return;
-    const float dx = px - sp.cam_pos[0], dy = py - sp.cam_pos[1], dz = pz - sp.cam_pos[2];
-    const float inv = 1.f / sqrtf(dx * dx + dy * dy + dz * dz);
-    const float X = dx * inv, Y = dy * inv, Z = dz * inv;
-    const float xx = X * X, xy = X * Y, xz = X * Z, yy = Y * Y, yz = Y * Z, zz = Z * Z;
-    float bas[15];
-    bas[0] = -kBC1 * Y; bas[1] = kBC1 * Z; bas[2] = -kBC1 * X;
-    bas[3] = kBC2[0] * xy; bas[4] = kBC2[1] * yz; bas[5] = kBC2[2] * (2.f * zz - xx - yy);
-    bas[6] = kBC2[3] * xz; bas[7] = kBC2[4] * (xx - yy);
-    bas[8] = kBC3[0] * Y * (3.f * xx - yy); bas[9] = kBC3[1] * xy * Z;
-    bas[10] = kBC3[2] * Y * (4.f * zz - xx - yy); bas[11] = kBC3[3] * Z * (2.f * zz - 3.f * xx - 3.f * yy);
-    bas[12] = kBC3[4] * X * (4.f * zz - xx - yy); bas[13] = kBC3[5] * Z * (xx - yy);
-    bas[14] = kBC3[6] * X * (xx - 3.f * yy);
-    const size_t base = (size_t)a.rest_bases * 3 * i;
-    float *p = a.features_rest + base, *mm = a.rest_m + base, *vv = a.rest_v + base;
-    const float st = sp.step_size[4], bc = sp.bc2_sqrt[4];
-#pragma unroll 1
-    for (int b = 0; b < nb; b++) {
-        adam_el(p + 3 * b + 0, mm + 3 * b + 0, vv + 3 * b + 0, bas[b] * vc0, st, bc, b1, b2, eps);
-        adam_el(p + 3 * b + 1, mm + 3 * b + 1, vv + 3 * b + 1, bas[b] * vc1, st, bc, b1, b2, eps);
-        adam_el(p + 3 * b + 2, mm + 3 * b + 2, vv + 3 * b + 2, bas[b] * vc2, st, bc, b1, b2, eps);
+    if (a.rest_bases == 0) return;
+    {   // features_rest: 3 * rest_bases floats per Gaussian
+        const int rowf = 3 * a.rest_bases, total = rowf * ng;
+        float *p = a.features_rest + (size_t)rowf * i0, *mm = a.rest_m + (size_t)rowf * i0,
+              *vv = a.rest_v + (size_t)rowf * i0;
+        const float st = sp.step_size[4], bc = sp.bc2_sqrt[4];
+        for (int e0 = lane * 4; e0 < total; e0 += 128) {
+            float g[4];
+            unsigned act = 0;
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int e = e0 + k;
+                g[k] = 0.f;
+                if (e < total) {
+                    const int gi = e / rowf, r = e - rowf * gi, band = r / 3, c = r - 3 * band;
+                    const float4 vc = sh.vc[gi];
+                    if (band < __float_as_int(vc.w) - 1) {
+                        g[k] = sh.bas[gi][band] * (c == 0 ? vc.x : c == 1 ? vc.y : vc.z);
+                        act |= 1u << k;
+                    }
+                }
+            }
+            if (!act) continue;
+            if (e0 + 4 <= total) {
+                float4 P = *reinterpret_cast<float4 *>(p + e0), Mv = *reinterpret_cast<float4 *>(mm + e0),
+                       Vv = *reinterpret_cast<float4 *>(vv + e0);
+                adam4(P, Mv, Vv, g, act, st, bc, b1, b2, eps);
+                *reinterpret_cast<float4 *>(p + e0) = P;
+                *reinterpret_cast<float4 *>(mm + e0) = Mv;
+                *reinterpret_cast<float4 *>(vv + e0) = Vv;
+            } else {
+                for (int k = 0; k < 4 && e0 + k < total; k++)
+                    if (act & (1u << k)) adam_el(p + e0 + k, mm + e0 + k, vv + e0 + k, g[k], st, bc, b1, b2, eps);
+            }
+        }
     }
 }
 

@@ -91,12 +91,83 @@ __global__ void __launch_bounds__(256) k_scatter(TileArgs a) {
         }
 }
 
+// Block-aggregated count and scatter: a CTA covers kAggPerCta Gaussians and
+// keeps a shared-memory histogram over all tiles, so the global atomics fall
+// from one per intersection to one per (CTA, touched tile).  Scatter reserves
+// each tile's slot range with that one atomic and hands out slots inside it
+// with shared-memory atomics.  Used while the histogram fits (kAggMaxTiles).
+constexpr int kAggPerCta = 4096;
+constexpr int kAggMaxTiles = 12288;
+
+__global__ void __launch_bounds__(256) k_count_agg(TileArgs a) {
+    extern __shared__ uint32_t bins[];
+    const int T = a.num_tiles;
+    for (int t = threadIdx.x; t < T; t += blockDim.x) bins[t] = 0;
+    __syncthreads();
+    const int g0 = blockIdx.x * kAggPerCta, g1 = min(a.n, g0 + kAggPerCta);
+    for (int i = g0 + threadIdx.x; i < g1; i += blockDim.x) {
+        if (!splat_active(i, a.radii, a.depths)) continue;
+        const float4 ra = a.rec[i].a;
+        const float2 ab = a.aabb[i];
+        int x0, y0, x1, y1;
+        tile_rect(ra.x, ra.y, ab.x, ab.y, a.tiles_x, a.tiles_y, x0, y0, x1, y1);
+        for (int y = y0; y < y1; y++)
+            for (int x = x0; x < x1; x++) atomicAdd(&bins[y * a.tiles_x + x], 1u);
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < T; t += blockDim.x)
+        if (bins[t]) atomicAdd(a.tile_counts + t, bins[t]);
+}
+
+__global__ void __launch_bounds__(256) k_scatter_agg(TileArgs a) {
+    extern __shared__ uint32_t bins[];
+    const int T = a.num_tiles;
+    for (int t = threadIdx.x; t < T; t += blockDim.x) bins[t] = 0;
+    __syncthreads();
+    const int g0 = blockIdx.x * kAggPerCta, g1 = min(a.n, g0 + kAggPerCta);
+    for (int i = g0 + threadIdx.x; i < g1; i += blockDim.x) {
+        if (!splat_active(i, a.radii, a.depths)) continue;
+        const float4 ra = a.rec[i].a;
+        const float2 ab = a.aabb[i];
+        int x0, y0, x1, y1;
+        tile_rect(ra.x, ra.y, ab.x, ab.y, a.tiles_x, a.tiles_y, x0, y0, x1, y1);
+        for (int y = y0; y < y1; y++)
+            for (int x = x0; x < x1; x++) atomicAdd(&bins[y * a.tiles_x + x], 1u);
+    }
+    __syncthreads();
+    // reserve each touched tile's slots; bins[t] becomes the next free slot
+    for (int t = threadIdx.x; t < T; t += blockDim.x) {
+        const uint32_t c = bins[t];
+        if (c) bins[t] = a.tile_offsets[t] + atomicAdd(a.tile_write + t, c);
+    }
+    __syncthreads();
+    for (int i = g0 + threadIdx.x; i < g1; i += blockDim.x) {
+        if (!splat_active(i, a.radii, a.depths)) continue;
+        const float4 ra = a.rec[i].a;
+        const float2 ab = a.aabb[i];
+        int x0, y0, x1, y1;
+        tile_rect(ra.x, ra.y, ab.x, ab.y, a.tiles_x, a.tiles_y, x0, y0, x1, y1);
+        const uint64_t key = ((uint64_t)__float_as_uint(a.depths[i]) << 32) | (uint32_t)i;
+        for (int y = y0; y < y1; y++)
+            for (int x = x0; x < x1; x++) {
+                const uint64_t dst = atomicAdd(&bins[y * a.tiles_x + x], 1u);
+                if (dst < (uint64_t)a.capacity) a.keys[dst] = key;   // overflow is dropped, never written
+            }
+    }
+}
+
 // ---------------------------------------------------------------------------
-// Per-tile stable LSD radix sort by one CTA (kSortThreads threads).
+// Per-tile sort by one CTA.  Keys are (depth bits << 32 | id).  A stable LSD
+// radix sort on the four depth bytes (a byte equal in every key is skipped)
+// orders the tile by depth; runs of equal depth (exact clones) are then put
+// in id order, which gives the reference's (depth, id) order.
+// Tiles up to kSortSmemKeys keys sort in shared memory in one chunk, 8 keys
+// per thread; larger tiles run chunked passes in global memory.
 // ---------------------------------------------------------------------------
 constexpr int kSortThreads = 512;
 constexpr int kSortWarps = kSortThreads / 32;
-constexpr int kSortSmemKeys = 4096;   // keys sorted in shared memory; larger tiles sort in place in global
+constexpr int kItems = 8;
+constexpr int kSortSmemKeys = kSortThreads * kItems;   // 4096
 
 struct SortSmem {
     uint32_t hist[256];
@@ -106,33 +177,104 @@ struct SortSmem {
     int skip;
 };
 
-// One stable counting pass on digit `shift`: src -> dst.  Returns false when
-// every key has the same digit (nothing written; the caller keeps src).
-__device__ bool radix_pass(const uint64_t *src, uint64_t *dst, int n, int shift, SortSmem &sm, unsigned *dbg) {
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    for (int d = tid; d < 256; d += kSortThreads) sm.hist[d] = 0;
-    __syncthreads();
-    for (int i = tid; i < n; i += kSortThreads) atomicAdd(&sm.hist[(uint32_t)(src[i] >> shift) & 255u], 1u);
-    __syncthreads();
-    if (tid == 0) {
-        int skip = 0;
-        uint32_t run = 0;
-        for (int d = 0; d < 256; d++) {
-            const uint32_t h = sm.hist[d];
-            if (h == (uint32_t)n) skip = 1;
-            sm.base[d] = run;
-            run += h;
+__device__ __forceinline__ uint32_t digit_of(uint64_t key, int shift) { return (uint32_t)(key >> shift) & 255u; }
+
+// Exclusive scan of sm.hist into sm.base by the first 256 threads; sets
+// sm.skip when one digit holds all n keys.  Ends with a barrier.
+__device__ void digit_scan(SortSmem &sm, int n) {
+    const int tid = threadIdx.x;
+    if (tid < 256) {
+        const uint32_t h = sm.hist[tid];
+        const int lane = tid & 31, w = tid >> 5;
+        uint32_t inc = h;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += u;
         }
-        sm.skip = skip;
+        sm.base[tid] = inc - h;   // warp-local exclusive
+        if (lane == 31) sm.woff[0][w] = inc;
+        if (h == (uint32_t)n) sm.skip = 1;
     }
     __syncthreads();
+    if (tid < 256) {
+        uint32_t add = 0;
+        for (int w = 0; w < (tid >> 5); w++) add += sm.woff[0][w];
+        sm.base[tid] += add;
+    }
+    __syncthreads();
+}
+
+// One pass on n <= kSortSmemKeys keys, all in one chunk: src -> dst.
+// Returns false (and writes nothing) when the digit is constant.
+__device__ bool radix_pass_1chunk(const uint64_t *src, uint64_t *dst, int n, int shift, SortSmem &sm, unsigned *dbg) {
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    for (int k = tid; k < kSortWarps * 256; k += kSortThreads) (&sm.wcnt[0][0])[k] = 0;
+    if (tid == 0) sm.skip = 0;
+    __syncthreads();
+    uint64_t key[kItems];
+    uint32_t dig[kItems], rank[kItems];
+    const uint32_t lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int j = 0; j < kItems; j++) {
+        const int idx = wid * (32 * kItems) + j * 32 + lane;
+        const bool valid = idx < n;
+        key[j] = valid ? src[idx] : 0ull;
+        dig[j] = valid ? digit_of(key[j], shift) : 256u;
+        const uint32_t peers = __match_any_sync(0xffffffffu, dig[j]);
+        uint32_t old = 0;
+        if (valid) old = sm.wcnt[wid][dig[j]];
+        __syncwarp();
+        rank[j] = old + __popc(peers & lt);
+        if (valid && (peers & lt) == 0) sm.wcnt[wid][dig[j]] = (uint16_t)(old + __popc(peers));
+        __syncwarp();
+    }
+    __syncthreads();
+    // per digit: offsets of each warp, totals -> hist
+    if (tid < 256) {
+        uint32_t run = 0;
+#pragma unroll 4
+        for (int w = 0; w < kSortWarps; w++) {
+            sm.woff[w][tid] = run;
+            run += sm.wcnt[w][tid];
+        }
+        sm.hist[tid] = run;
+    }
+    __syncthreads();
+    // exclusive scan of the totals (hist -> base); woff[0] is reused as warp
+    // sums only after every thread has read its offsets, so keep a copy
+    uint32_t my_off[kItems];
+#pragma unroll
+    for (int j = 0; j < kItems; j++) my_off[j] = (dig[j] < 256u) ? sm.woff[wid][dig[j]] : 0u;
+    __syncthreads();
+    digit_scan(sm, n);
+    if (sm.skip) return false;
+#pragma unroll
+    for (int j = 0; j < kItems; j++) {
+        if (dig[j] >= 256u) continue;
+        const uint32_t pos = sm.base[dig[j]] + my_off[j] + rank[j];
+        if (MS_GUARD(pos < (uint32_t)n, 4, pos, dbg)) dst[pos] = key[j];
+    }
+    __syncthreads();
+    return true;
+}
+
+// One pass on any n in chunks of kSortThreads keys (global-memory tiles).
+__device__ bool radix_pass_chunked(const uint64_t *src, uint64_t *dst, int n, int shift, SortSmem &sm, unsigned *dbg) {
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    for (int d = tid; d < 256; d += kSortThreads) sm.hist[d] = 0;
+    if (tid == 0) sm.skip = 0;
+    __syncthreads();
+    for (int i = tid; i < n; i += kSortThreads) atomicAdd(&sm.hist[digit_of(src[i], shift)], 1u);
+    __syncthreads();
+    digit_scan(sm, n);
     if (sm.skip) return false;
     const uint32_t lt_mask = (1u << lane) - 1u;
     for (int c0 = 0; c0 < n; c0 += kSortThreads) {
         const int i = c0 + tid;
         const bool valid = i < n;
         const uint64_t key = valid ? src[i] : 0ull;
-        const uint32_t d = valid ? ((uint32_t)(key >> shift) & 255u) : 256u;
+        const uint32_t d = valid ? digit_of(key, shift) : 256u;
         const uint32_t peers = __match_any_sync(0xffffffffu, d);
         const uint32_t rank = __popc(peers & lt_mask);
         if (valid && rank == 0) sm.wcnt[wid][d] = (uint16_t)__popc(peers);
@@ -156,6 +298,24 @@ __device__ bool radix_pass(const uint64_t *src, uint64_t *dst, int n, int shift,
     return true;
 }
 
+// Keys sorted by depth: order each run of equal depth by id.
+__device__ void order_ties(uint64_t *a, int n) {
+    for (int j = threadIdx.x; j < n; j += kSortThreads) {
+        const uint32_t dj = (uint32_t)(a[j] >> 32);
+        if (j > 0 && (uint32_t)(a[j - 1] >> 32) == dj) continue;          // not a run start
+        if (j + 1 >= n || (uint32_t)(a[j + 1] >> 32) != dj) continue;      // run of one
+        int e = j + 1;
+        while (e < n && (uint32_t)(a[e] >> 32) == dj) e++;
+        for (int u = j + 1; u < e; u++) {                                  // insertion sort by id
+            const uint64_t v = a[u];
+            int w = u - 1;
+            while (w >= j && (uint32_t)a[w] > (uint32_t)v) { a[w + 1] = a[w]; w--; }
+            a[w + 1] = v;
+        }
+    }
+    __syncthreads();
+}
+
 __global__ void __launch_bounds__(kSortThreads) k_sort_pack(TileArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SortSmem &sm = *reinterpret_cast<SortSmem *>(smem_raw);
@@ -166,6 +326,7 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pack(TileArgs a) {
     if (count == 0) return;
     const uint32_t start = a.tile_offsets[t];
     const int tid = threadIdx.x;
+    unsigned *dbg = a.nan_counts ? a.nan_counts + kDbgSlot : nullptr;
     // a tile whose bucket does not fit the buffer is emitted transparent
     // (hybrid_sort_pack_kernel's region guard, msplat_metal.metal:2523-2535)
     if ((uint64_t)start + (uint64_t)count > (uint64_t)a.capacity) {
@@ -181,26 +342,25 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pack(TileArgs a) {
         }
         return;
     }
-    // shared memory starts with stale contents: the per-warp digit counts
-    // must start at zero (each chunk of a pass clears what it used)
+    // shared memory starts with stale contents: the chunked pass expects its
+    // per-warp digit counts at zero (each chunk clears what it used)
     for (int i = tid; i < kSortWarps * 256; i += kSortThreads) (&sm.wcnt[0][0])[i] = 0;
-    __syncthreads();
     uint64_t *src, *alt;
-    if (count <= kSortSmemKeys) {
+    const bool in_smem = count <= kSortSmemKeys;
+    if (in_smem) {
         for (int j = tid; j < count; j += kSortThreads) sk0[j] = a.keys[start + j];
-        __syncthreads();
         src = sk0; alt = sk1;
     } else {
         src = a.keys + start; alt = a.keys_alt + start;
     }
-    for (int shift = 0; shift < 64; shift += 8) {
-        if (radix_pass(src, alt, count, shift, sm, a.nan_counts ? a.nan_counts + kDbgSlot : nullptr)) {
-            uint64_t *tmp = src;
-            src = alt;
-            alt = tmp;
-        }
+    __syncthreads();
+    for (int shift = 32; shift < 64; shift += 8) {
+        const bool moved = in_smem ? radix_pass_1chunk(src, alt, count, shift, sm, dbg)
+                                   : radix_pass_chunked(src, alt, count, shift, sm, dbg);
+        if (moved) { uint64_t *tmp = src; src = alt; alt = tmp; }
         __syncthreads();
     }
+    order_ties(src, count);
     // pack: gather the splat records in sorted order
     for (int j = tid; j < count; j += kSortThreads) {
         const uint64_t key = src[j];
@@ -235,18 +395,29 @@ size_t sort_pack_smem_bytes() {
 }
 
 void launch_tiles(const TileArgs &a, cudaStream_t s) {
-    if (a.n > 0) k_count<<<(a.n + 255) / 256, 256, 0, s>>>(a);
-    debug_sync(s, "count");
-    k_scan<<<1, 1024, 0, s>>>(a);
-    debug_sync(s, "scan");
-    if (a.n > 0) k_scatter<<<(a.n + 255) / 256, 256, 0, s>>>(a);
-    debug_sync(s, "scatter");
     static bool attr_set = false;
     const size_t smem = sort_pack_smem_bytes();
     if (!attr_set) {
         cudaFuncSetAttribute(k_sort_pack, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_count_agg, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
+        cudaFuncSetAttribute(k_scatter_agg, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
         attr_set = true;
     }
+    const bool agg = a.num_tiles <= kAggMaxTiles;
+    const int agg_blocks = (a.n + kAggPerCta - 1) / kAggPerCta;
+    const size_t agg_smem = (size_t)a.num_tiles * sizeof(uint32_t);
+    if (a.n > 0) {
+        if (agg) k_count_agg<<<agg_blocks, 256, agg_smem, s>>>(a);
+        else k_count<<<(a.n + 255) / 256, 256, 0, s>>>(a);
+    }
+    debug_sync(s, "count");
+    k_scan<<<1, 1024, 0, s>>>(a);
+    debug_sync(s, "scan");
+    if (a.n > 0) {
+        if (agg) k_scatter_agg<<<agg_blocks, 256, agg_smem, s>>>(a);
+        else k_scatter<<<(a.n + 255) / 256, 256, 0, s>>>(a);
+    }
+    debug_sync(s, "scatter");
     k_sort_pack<<<a.num_tiles, kSortThreads, smem, s>>>(a);
     debug_sync(s, "sort_pack");
 }
