@@ -190,16 +190,19 @@ __global__ void __launch_bounds__(256) k_ssim_bwd(LossArgs a) {
     if (nbad && a.nan_counts) atomicAdd(a.nan_counts + kNanVRendered, nbad);
 }
 
-static bool g_gauss_ready = false;
+// The window lives in each device's constant bank: upload it once per device.
+static bool g_gauss_ready[64] = {false};
 
 void launch_loss(const LossArgs &a, cudaStream_t s) {
-    if (!g_gauss_ready) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64 || !g_gauss_ready[dev]) {
         double g[11], sum = 0;
         for (int i = 0; i < 11; i++) { g[i] = exp(-((i - 5) * (i - 5)) / (2.0 * 1.5 * 1.5)); sum += g[i]; }
         float w[11];
         for (int i = 0; i < 11; i++) w[i] = (float)(g[i] / sum);
         cudaMemcpyToSymbol(kGauss, w, sizeof(w));
-        g_gauss_ready = true;
+        if (dev >= 0 && dev < 64) g_gauss_ready[dev] = true;
     }
     const dim3 grid((a.width + kS - 1) / kS, (a.height + kS - 1) / kS);
     k_ssim_h<<<grid, 256, 0, s>>>(a);
