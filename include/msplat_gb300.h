@@ -28,6 +28,23 @@ float msplat_psnr(const float *img, const float *gt, long long n);
 float msplat_l1(const float *img, const float *gt, long long n);
 float msplat_ssim_eval(const float *img, const float *gt, int height, int width);
 
+/* SSIM + L1 training loss and dL/dimage without any device allocation.
+ * No counterpart in the reference: it is for callers that cannot call
+ * cudaMalloc (a host application or server that owns all device memory
+ * through its own allocator, or a loop that cannot take cudaMalloc's
+ * implicit synchronisation).  The same kernels as the training step; their
+ * scratch (24 floats per pixel) and step scalars live in the library's static
+ * device arrays, so images are limited to 512 * 512 = 262,144 pixels (larger
+ * sizes return -3 with a message).  All calls on a device share those arrays:
+ * calls that overlap on the GPU race.  The first call on a device looks up
+ * the arrays' addresses; make it before any stream capture.
+ * img: device float [H,W,3]; gt: device uint8 [H,W,3]; mask: device uint8
+ * [H,W] or NULL; v_img: device float [H,W,3] (out); loss_sum: device float
+ * (out, loss_sum / (H*W) is the loss); stream: cudaStream_t or NULL.
+ * Returns 0, or a negative code. */
+int msplat_loss_ssim_l1_noalloc(const float *img, const uint8_t *gt, const uint8_t *mask, int width, int height,
+                                float ssim_weight, float loss_inv_n, float *v_img, float *loss_sum, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
