@@ -135,6 +135,23 @@ long long msplat_engine_buffer(MsplatEngine *e, const char *name, void **dev_ptr
 /* Copies the first `bytes` of a named buffer to host memory; waits. */
 int msplat_engine_read(MsplatEngine *e, const char *name, void *dst, long long bytes);
 
+/* MCMC relocation + growth (Model::mcmcAfterTrain, core/src/model.cpp:
+ * 497-660), resident on the GPU.  g->num_points is the active count N; the
+ * parameter and moment buffers must hold cap_max rows.  Dead Gaussians
+ * (non-finite, sigmoid(opacity) <= 0.005, |mean| > cull_radius) are moved
+ * onto living ones drawn in proportion to sigmoid(opacity), each source is
+ * rescaled by Eq. 9 (model.cpp:311-332), and min(cap_max, 1.05 N) - N new
+ * slots are filled the same way.  *relocation_count is the reference's
+ * mcmc_relocation_count (seeds the draws); it is advanced in place.  The
+ * chosen (dst, src) pairs stay readable in the "mcmc_moves" buffer
+ * (relocation moves first, then growth).  Waits for the device. */
+typedef struct {
+    int num_dead, num_culled, num_nonfinite, num_relocated, num_grown, num_active;
+} MsplatMcmcStats;
+
+int msplat_engine_mcmc(MsplatEngine *e, const MsplatGaussians *g, const MsplatAdamState *st, int cap_max,
+                       float cull_radius, int *relocation_count, MsplatMcmcStats *out);
+
 /* Two CUDA events on the engine's stream for timing a span of steps:
  * marker(0) before, marker(1) after, then marker_elapsed waits for the second
  * and returns the device time between them in ms. */

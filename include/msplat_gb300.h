@@ -9,7 +9,11 @@
 #ifndef MSPLAT_GB300_H
 #define MSPLAT_GB300_H
 
+#include <stdbool.h>
 #include <stdint.h>
+
+#include "msplat_c_api.h"
+#include "msplat_engine.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -27,6 +31,37 @@ void msplat_prepare_camera(const float cam_to_world[16], int width, int height, 
 float msplat_psnr(const float *img, const float *gt, long long n);
 float msplat_l1(const float *img, const float *gt, long long n);
 float msplat_ssim_eval(const float *img, const float *gt, int height, int width);
+
+/* A dataset from host arrays — the InputData the reference's loaders build
+ * (core/include/input_data.hpp:19-60): num_cameras camera-to-world poses
+ * (row-major 4x4, OpenGL axes), intrinsics (fx, fy, cx, cy), sizes (width,
+ * height), uint8 RGB images [H,W,3] and optional uint8 masks [H,W] (NULL),
+ * plus the seed point cloud (xyz float, rgb uint8).  normalize applies the
+ * reference's camera centring and scaling (input_data.cpp:115-169); with
+ * eval_mode every test_every-th camera is a test camera
+ * (input_data.cpp:199-208).  All inputs are copied. */
+MsplatDataset msplat_dataset_create_from_memory(int num_cameras, const float *cam_to_world, const float *intrinsics,
+                                               const int *sizes, const uint8_t *const *images,
+                                               const uint8_t *const *masks, int num_points, const float *xyz,
+                                               const uint8_t *rgb, bool eval_mode, int test_every, bool normalize);
+
+/* Replaces the trainer's Gaussians (host arrays in the reference layouts, n
+ * rows) and resets the optimizer, as loading a trained PLY does
+ * (Model::loadPly, core/src/model.cpp:675-690). */
+int msplat_trainer_set_gaussians(MsplatTrainer t, int n, int rest_bases, const float *means, const float *scales,
+                                 const float *quats, const float *features_dc, const float *features_rest,
+                                 const float *opacities);
+
+/* Copies the active Gaussians to host arrays (any pointer may be NULL). */
+int msplat_trainer_get_gaussians(MsplatTrainer t, float *means, float *scales, float *quats, float *features_dc,
+                                 float *features_rest, float *opacities);
+
+/* Loss of the last training step (waits for the device); the reference
+ * computes it in msplat_train_step but Trainer::step does not return it. */
+float msplat_trainer_last_loss(MsplatTrainer t);
+
+/* The trainer's engine (for stats, timing and buffer inspection). */
+MsplatEngine *msplat_trainer_engine(MsplatTrainer t);
 
 /* SSIM + L1 training loss and dL/dimage without any device allocation.
  * No counterpart in the reference: it is for callers that cannot call

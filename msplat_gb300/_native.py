@@ -50,6 +50,11 @@ class MsplatEngineStats(C.Structure):
                 ("timed_steps", C.c_longlong), ("launches", C.c_longlong), ("check_record", C.c_uint32 * 3)]
 
 
+class MsplatMcmcStats(C.Structure):
+    _fields_ = [("num_dead", C.c_int), ("num_culled", C.c_int), ("num_nonfinite", C.c_int),
+                ("num_relocated", C.c_int), ("num_grown", C.c_int), ("num_active", C.c_int)]
+
+
 def lib(build_if_missing: bool = True):
     global _lib
     with _lock:
@@ -79,6 +84,8 @@ def lib(build_if_missing: bool = True):
         L.msplat_engine_buffer.argtypes = [vp, C.c_char_p, C.POINTER(C.c_void_p)]
         L.msplat_engine_buffer.restype = C.c_longlong
         L.msplat_engine_read.argtypes = [vp, C.c_char_p, vp, C.c_longlong]
+        L.msplat_engine_mcmc.argtypes = [vp, C.POINTER(MsplatGaussians), C.POINTER(MsplatAdamState), C.c_int,
+                                         C.c_float, C.POINTER(C.c_int), C.POINTER(MsplatMcmcStats)]
         L.msplat_engine_marker.argtypes = [vp, C.c_int]
         L.msplat_engine_marker_elapsed.argtypes = [vp, FP]
         L.msplat_engine_stream.argtypes = [vp]

@@ -1,0 +1,328 @@
+"""Python surface of msplat's trainer (the reference's python/msplat/_core.pyi:
+TrainingConfig, Dataset, GaussianTrainer, sync, cleanup) over the public C API
+of libmsplat_gb300.so.  No torch; images come back as numpy arrays."""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _native as N
+
+
+class _MsplatConfig(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("shDegree", C.c_int), ("shDegreeInterval", C.c_int),
+                ("ssimWeight", C.c_float), ("capMax", C.c_int), ("noiseLr", C.c_float), ("opacityReg", C.c_float),
+                ("scaleReg", C.c_float), ("cullRadius", C.c_float), ("keepCrs", C.c_bool),
+                ("downscaleFactor", C.c_float), ("bgColor", C.c_float * 3)]
+
+
+class _Stats(C.Structure):
+    _fields_ = [("iteration", C.c_int), ("splatCount", C.c_int), ("msPerStep", C.c_float)]
+
+
+class _Eval(C.Structure):
+    _fields_ = [("psnr", C.c_float), ("ssim", C.c_float), ("l1", C.c_float), ("numTest", C.c_int),
+                ("numGaussians", C.c_int)]
+
+
+class _Pixels(C.Structure):
+    _fields_ = [("data", C.POINTER(C.c_float)), ("width", C.c_int), ("height", C.c_int)]
+
+
+_bound = False
+
+
+def _lib():
+    global _bound
+    L = N.lib()
+    if _bound:
+        return L
+    vp, cp, fp = C.c_void_p, C.c_char_p, C.POINTER(C.c_float)
+    L.msplat_dataset_create.argtypes = [cp, C.c_float, C.c_bool, C.c_int]
+    L.msplat_dataset_create.restype = vp
+    L.msplat_dataset_create_from_memory.argtypes = [C.c_int, fp, fp, C.POINTER(C.c_int), C.POINTER(vp),
+                                                    C.POINTER(vp), C.c_int, fp, C.POINTER(C.c_uint8), C.c_bool,
+                                                    C.c_int, C.c_bool]
+    L.msplat_dataset_create_from_memory.restype = vp
+    L.msplat_dataset_destroy.argtypes = [vp]
+    L.msplat_dataset_num_train.argtypes = [vp]
+    L.msplat_dataset_num_test.argtypes = [vp]
+    L.msplat_dataset_camera_pose.argtypes = [vp, C.c_int, fp]
+    L.msplat_trainer_create.argtypes = [vp, _MsplatConfig]
+    L.msplat_trainer_create.restype = vp
+    L.msplat_trainer_destroy.argtypes = [vp]
+    L.msplat_trainer_step.argtypes = [vp]
+    L.msplat_trainer_step.restype = _Stats
+    L.msplat_trainer_train.argtypes = [vp]
+    L.msplat_trainer_evaluate.argtypes = [vp]
+    L.msplat_trainer_evaluate.restype = _Eval
+    L.msplat_trainer_render.argtypes = [vp, C.c_int, C.c_bool]
+    L.msplat_trainer_render.restype = _Pixels
+    L.msplat_trainer_render_pose.argtypes = [vp, fp, C.c_int]
+    L.msplat_trainer_render_pose.restype = _Pixels
+    L.msplat_trainer_render_pose_to_buffer.argtypes = [vp, fp, C.c_int, C.POINTER(C.c_uint8),
+                                                       C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    for n in ("export_ply", "export_splat", "save_checkpoint"):
+        getattr(L, f"msplat_trainer_{n}").argtypes = [vp, cp]
+    L.msplat_trainer_load_checkpoint.argtypes = [vp, cp]
+    L.msplat_trainer_splat_count.argtypes = [vp]
+    L.msplat_trainer_iteration.argtypes = [vp]
+    L.msplat_trainer_set_gaussians.argtypes = [vp, C.c_int, C.c_int, fp, fp, fp, fp, fp, fp]
+    L.msplat_trainer_get_gaussians.argtypes = [vp, fp, fp, fp, fp, fp, fp]
+    L.msplat_trainer_last_loss.argtypes = [vp]
+    L.msplat_trainer_last_loss.restype = C.c_float
+    L.msplat_trainer_engine.argtypes = [vp]
+    L.msplat_trainer_engine.restype = vp
+    L.msplat_viewer_create.argtypes = [cp, C.c_int, C.c_int, C.c_float]
+    L.msplat_viewer_create.restype = vp
+    L.msplat_viewer_render.argtypes = [vp, fp, C.POINTER(C.c_uint8)]
+    L.msplat_viewer_splat_count.argtypes = [vp]
+    L.msplat_viewer_get_size.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.msplat_viewer_bounds.argtypes = [vp, fp, fp]
+    L.msplat_viewer_density_center.argtypes = [vp, fp]
+    L.msplat_viewer_render_buffer.argtypes = [vp, fp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.msplat_viewer_render_buffer.restype = vp
+    L.msplat_viewer_set_background.argtypes = [vp, C.c_float, C.c_float, C.c_float]
+    L.msplat_viewer_resize.argtypes = [vp, C.c_int, C.c_int]
+    L.msplat_viewer_set_fov.argtypes = [vp, C.c_float]
+    L.msplat_viewer_destroy.argtypes = [vp]
+    _bound = True
+    return L
+
+
+def _fp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+@dataclass
+class TrainingConfig:
+    """Defaults of the reference (core/include/msplat_c_api.h:32-47); the
+    densification knobs of the stale python binding are accepted and ignored,
+    as the reference's MCMC core ignores them."""
+    iterations: int = 30000
+    sh_degree: int = 3
+    sh_degree_interval: int = 1000
+    ssim_weight: float = 0.2
+    cap_max: int = 1_000_000
+    noise_lr: float = 5e5
+    opacity_reg: float = 0.01
+    scale_reg: float = 0.01
+    cull_radius: float = 3.0
+    keep_crs: bool = False
+    downscale_factor: float = 1.0
+    bg_color: list = field(default_factory=lambda: [0.6130, 0.0101, 0.3984])
+    num_downscales: int = 2
+    resolution_schedule: int = 3000
+    refine_every: int = 100
+    warmup_length: int = 500
+    reset_alpha_every: int = 30
+    densify_grad_thresh: float = 0.0002
+    densify_size_thresh: float = 0.01
+    stop_screen_size_at: int = 4000
+    split_screen_size: float = 0.05
+    output: str = "splat.ply"
+    save_every: int = -1
+
+    def native(self) -> _MsplatConfig:
+        c = _MsplatConfig()
+        c.iterations, c.shDegree, c.shDegreeInterval = self.iterations, self.sh_degree, self.sh_degree_interval
+        c.ssimWeight, c.capMax, c.noiseLr = self.ssim_weight, self.cap_max, self.noise_lr
+        c.opacityReg, c.scaleReg, c.cullRadius = self.opacity_reg, self.scale_reg, self.cull_radius
+        c.keepCrs, c.downscaleFactor = self.keep_crs, self.downscale_factor
+        c.bgColor[:] = [float(v) for v in self.bg_color]
+        return c
+
+
+@dataclass
+class TrainingStats:
+    iteration: int
+    splat_count: int
+    ms_per_step: float
+
+
+class Dataset:
+    def __init__(self, path: str | None = None, downscale_factor: float = 1.0, eval_mode: bool = False,
+                 test_every: int = 8, _handle=None):
+        L = _lib()
+        self.h = _handle if _handle is not None else L.msplat_dataset_create(path.encode(), downscale_factor,
+                                                                             eval_mode, test_every)
+        if not self.h:
+            raise RuntimeError(f"could not load dataset {path!r}")
+
+    @classmethod
+    def from_arrays(cls, cameras, images, points_xyz, points_rgb, eval_mode=False, test_every=8, normalize=False,
+                    masks=None):
+        """cameras: list of synthetic.Camera (cam_to_world, width, height, fx, fy, cx, cy)."""
+        L = _lib()
+        n = len(cameras)
+        c2w = np.ascontiguousarray(np.stack([np.asarray(c.cam_to_world, np.float32).reshape(16) for c in cameras]))
+        intr = np.ascontiguousarray(np.array([[c.fx, c.fy, c.cx, c.cy] for c in cameras], np.float32))
+        sizes = np.ascontiguousarray(np.array([[c.width, c.height] for c in cameras], np.int32))
+        imgs = [np.ascontiguousarray(im, np.uint8) for im in images]
+        ptrs = (C.c_void_p * n)(*[im.ctypes.data for im in imgs])
+        mptrs = None
+        if masks is not None:
+            ms = [np.ascontiguousarray(m, np.uint8) if m is not None else None for m in masks]
+            mptrs = (C.c_void_p * n)(*[m.ctypes.data if m is not None else None for m in ms])
+        xyz = np.ascontiguousarray(points_xyz, np.float32)
+        rgb = np.ascontiguousarray(points_rgb, np.uint8)
+        h = L.msplat_dataset_create_from_memory(n, _fp(c2w), _fp(intr), sizes.ctypes.data_as(C.POINTER(C.c_int)),
+                                                ptrs, mptrs, xyz.shape[0], _fp(xyz),
+                                                rgb.ctypes.data_as(C.POINTER(C.c_uint8)), eval_mode, test_every,
+                                                normalize)
+        return cls(_handle=h)
+
+    @property
+    def num_train(self) -> int:
+        return _lib().msplat_dataset_num_train(self.h)
+
+    @property
+    def num_test(self) -> int:
+        return _lib().msplat_dataset_num_test(self.h)
+
+    def camera_pose(self, index: int) -> np.ndarray:
+        out = np.zeros(16, np.float32)
+        _lib().msplat_dataset_camera_pose(self.h, index, _fp(out))
+        return out.reshape(4, 4)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            _lib().msplat_dataset_destroy(self.h)
+            self.h = None
+
+
+def _take(px: _Pixels) -> np.ndarray:
+    if not px.data:
+        return np.zeros((0, 0, 3), np.float32)
+    n = px.width * px.height * 3
+    out = np.ctypeslib.as_array(px.data, shape=(n,)).copy().reshape(px.height, px.width, 3)
+    C.CDLL(None).free(C.cast(px.data, C.c_void_p))
+    return out
+
+
+class GaussianTrainer:
+    def __init__(self, dataset: Dataset, config: TrainingConfig):
+        self.dataset = dataset   # the dataset must outlive the trainer
+        self.config = config
+        self.h = _lib().msplat_trainer_create(dataset.h, config.native())
+        if not self.h:
+            raise RuntimeError("could not create trainer")
+
+    def step(self) -> TrainingStats:
+        s = _lib().msplat_trainer_step(self.h)
+        return TrainingStats(s.iteration, s.splatCount, s.msPerStep)
+
+    def train(self, callback=None, callback_every: int = 100):
+        while self.iteration < self.config.iterations:
+            s = self.step()
+            if callback and s.iteration % callback_every == 0:
+                callback(s)
+
+    def evaluate(self) -> dict:
+        m = _lib().msplat_trainer_evaluate(self.h)
+        return {"psnr": m.psnr, "ssim": m.ssim, "l1": m.l1, "num_test": m.numTest, "num_gaussians": m.numGaussians}
+
+    def render(self, cam_idx: int, use_test: bool = False) -> np.ndarray:
+        return _take(_lib().msplat_trainer_render(self.h, cam_idx, use_test))
+
+    def render_from_pose(self, cam_to_world, ref_cam_idx: int = 0) -> np.ndarray:
+        m = np.ascontiguousarray(cam_to_world, np.float32).reshape(16)
+        return _take(_lib().msplat_trainer_render_pose(self.h, _fp(m), ref_cam_idx))
+
+    def render_to_rgba(self, cam_to_world, ref_cam_idx: int = 0) -> np.ndarray:
+        L = _lib()
+        m = np.ascontiguousarray(cam_to_world, np.float32).reshape(16)
+        w, h = C.c_int(), C.c_int()
+        L.msplat_trainer_render_pose_to_buffer(self.h, _fp(m), ref_cam_idx, None, C.byref(w), C.byref(h))
+        out = np.zeros((h.value, w.value, 4), np.uint8)
+        L.msplat_trainer_render_pose_to_buffer(self.h, _fp(m), ref_cam_idx,
+                                               out.ctypes.data_as(C.POINTER(C.c_uint8)), C.byref(w), C.byref(h))
+        return out
+
+    def export_ply(self, path: str):
+        _lib().msplat_trainer_export_ply(self.h, path.encode())
+
+    def export_splat(self, path: str):
+        _lib().msplat_trainer_export_splat(self.h, path.encode())
+
+    def save_checkpoint(self, path: str):
+        _lib().msplat_trainer_save_checkpoint(self.h, path.encode())
+
+    def load_checkpoint(self, path: str) -> int:
+        return _lib().msplat_trainer_load_checkpoint(self.h, path.encode())
+
+    def set_gaussians(self, g):
+        L = _lib()
+        arrs = [np.ascontiguousarray(a, np.float32) for a in g.arrays()]
+        rc = L.msplat_trainer_set_gaussians(self.h, arrs[0].shape[0], arrs[4].shape[1], *[_fp(a) for a in arrs])
+        if rc != 0:
+            raise RuntimeError("set_gaussians failed")
+
+    def get_gaussians(self, rest_bases: int = 15):
+        n = self.splat_count
+        shapes = [(n, 3), (n, 3), (n, 4), (n, 3), (n, rest_bases, 3), (n,)]
+        arrs = [np.zeros(s, np.float32) for s in shapes]
+        _lib().msplat_trainer_get_gaussians(self.h, *[_fp(a) for a in arrs])
+        return arrs
+
+    @property
+    def last_loss(self) -> float:
+        return float(_lib().msplat_trainer_last_loss(self.h))
+
+    @property
+    def splat_count(self) -> int:
+        return _lib().msplat_trainer_splat_count(self.h)
+
+    @property
+    def iteration(self) -> int:
+        return _lib().msplat_trainer_iteration(self.h)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            _lib().msplat_trainer_destroy(self.h)
+            self.h = None
+
+
+class Viewer:
+    def __init__(self, ply_path: str, width: int, height: int, fov_y: float):
+        self.h = _lib().msplat_viewer_create(ply_path.encode(), width, height, fov_y)
+        if not self.h:
+            raise RuntimeError(f"could not load {ply_path!r}")
+
+    def render(self, cam_to_world) -> np.ndarray:
+        L = _lib()
+        w, h = C.c_int(), C.c_int()
+        L.msplat_viewer_get_size(self.h, C.byref(w), C.byref(h))
+        out = np.zeros((h.value, w.value, 4), np.uint8)
+        m = np.ascontiguousarray(cam_to_world, np.float32).reshape(16)
+        L.msplat_viewer_render(self.h, _fp(m), out.ctypes.data_as(C.POINTER(C.c_uint8)))
+        return out
+
+    @property
+    def splat_count(self) -> int:
+        return _lib().msplat_viewer_splat_count(self.h)
+
+    def bounds(self):
+        lo, hi = np.zeros(3, np.float32), np.zeros(3, np.float32)
+        _lib().msplat_viewer_bounds(self.h, _fp(lo), _fp(hi))
+        return lo, hi
+
+    def density_center(self):
+        c = np.zeros(3, np.float32)
+        _lib().msplat_viewer_density_center(self.h, _fp(c))
+        return c
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            _lib().msplat_viewer_destroy(self.h)
+            self.h = None
+
+
+def sync():
+    N.lib().msplat_sync()
+
+
+def cleanup():
+    N.lib().msplat_cleanup()

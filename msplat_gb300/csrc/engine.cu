@@ -195,6 +195,39 @@ class Engine {
         train_step(g, st, args, ptr<uint8_t>("gt_stage"), mask_d, true);
     }
 
+    void mcmc(const MsplatGaussians &g, const MsplatAdamState &st, int cap_max, float cull_radius,
+              int &relocation_count, MsplatMcmcStats &out) {
+        CK(cudaSetDevice(device_));
+        if (cap_max < g.num_points) throw std::runtime_error("cap_max below the active count");
+        const size_t cap = (size_t)std::max(cap_max, 1);
+        const size_t parts = cap / 2048 + 2;
+        alloc("mcmc_flags", cap * 4);
+        alloc("mcmc_pos", cap * 4);
+        alloc("mcmc_copies", cap * 4);
+        alloc("mcmc_weights", cap * 8);
+        alloc("mcmc_cumw", cap * 8);
+        alloc("mcmc_upart", parts * 4);
+        alloc("mcmc_dpart", parts * 8);
+        alloc("mcmc_dead", cap * 4);
+        alloc("mcmc_moves", cap * 16);
+        alloc("mcmc_counters", 64, true);
+        McmcArgs a{};
+        a.n = g.num_points; a.rest_bases = g.rest_bases;
+        a.means = g.means; a.scales = g.scales; a.quats = g.quats; a.features_dc = g.features_dc;
+        a.features_rest = g.features_rest; a.opacities = g.opacities;
+        for (int k = 0; k < 6; k++) { a.exp_avg[k] = st.exp_avg[k]; a.exp_avg_sq[k] = st.exp_avg_sq[k]; }
+        a.cull_r2 = cull_radius > 0.f ? cull_radius * cull_radius : -1.f;
+        a.flags = ptr<uint32_t>("mcmc_flags"); a.flag_pos = ptr<uint32_t>("mcmc_pos");
+        a.upart = ptr<uint32_t>("mcmc_upart"); a.copies = ptr<uint32_t>("mcmc_copies");
+        a.weights = ptr<double>("mcmc_weights"); a.cumw = ptr<double>("mcmc_cumw"); a.dpart = ptr<double>("mcmc_dpart");
+        a.dead_list = ptr<int>("mcmc_dead"); a.moves = ptr<int>("mcmc_moves");
+        a.counters = ptr<unsigned>("mcmc_counters");
+        McmcResult r;
+        run_mcmc(a, cap_max, relocation_count, r, stream_);
+        out.num_dead = r.num_dead; out.num_culled = r.num_culled; out.num_nonfinite = r.num_nonfinite;
+        out.num_relocated = r.num_relocated; out.num_grown = r.num_grown; out.num_active = r.num_active;
+    }
+
     void synchronize() { CK(cudaStreamSynchronize(stream_)); }
 
     float loss() {
@@ -483,6 +516,12 @@ int msplat_engine_read(MsplatEngine *e, const char *name, void *dst, long long b
         e->impl->synchronize();
         CK(cudaMemcpy(dst, p, (size_t)bytes, cudaMemcpyDeviceToHost));
     });
+}
+
+int msplat_engine_mcmc(MsplatEngine *e, const MsplatGaussians *g, const MsplatAdamState *st, int cap_max,
+                       float cull_radius, int *relocation_count, MsplatMcmcStats *out) {
+    if (!g || !st || !relocation_count || !out) return -1;
+    return guarded(e, [&] { e->impl->mcmc(*g, *st, cap_max, cull_radius, *relocation_count, *out); });
 }
 
 int msplat_engine_marker(MsplatEngine *e, int which) {

@@ -89,6 +89,21 @@ struct AdamArgs {
     unsigned *nan_counts;
 };
 
+struct McmcArgs {
+    int n, rest_bases;
+    float *means, *scales, *quats, *features_dc, *features_rest, *opacities;
+    float *exp_avg[6], *exp_avg_sq[6];
+    float cull_r2;
+    uint32_t *flags, *flag_pos, *upart, *copies;
+    double *weights, *cumw, *dpart;
+    int *dead_list, *moves;
+    unsigned *counters;
+};
+
+struct McmcResult {
+    int num_dead, num_culled, num_nonfinite, num_relocated, num_grown, num_active;
+};
+
 // With MSPLAT_SYNC_CHECK set in the environment, waits for the stream after
 // each launch and raises with the kernel's name if it failed.
 void debug_sync(cudaStream_t s, const char *what);
@@ -102,5 +117,6 @@ void launch_raster_bwd(const RasterArgs &a, cudaStream_t s);
 void launch_project_bwd(const ProjectBwdArgs &a, cudaStream_t s);
 void launch_adam(const AdamArgs &a, int num_sms, cudaStream_t s);
 void launch_sgld(const AdamArgs &a, cudaStream_t s);
+void run_mcmc(McmcArgs a, int cap_max, int &relocation_count, McmcResult &res, cudaStream_t s);
 
 }  // namespace msplat
