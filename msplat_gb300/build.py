@@ -3,7 +3,9 @@
 Translation units compile in parallel.  The files whose float results decide
 integer outputs or must match the oracle bit for bit (projection, tile
 mapping, forward raster) are built with --fmad=false: there every product is
-rounded before it is added, and fused only where the source says fmaf.
+rounded before it is added, and fused only where the source says fmaf.  Host
+code is built with -ffp-contract=off so that its float results (camera
+matrices, metrics, seed scales) are the same on x86-64 and AArch64.
 """
 from __future__ import annotations
 
@@ -35,6 +37,7 @@ def sources():
 
 def _flags(src: str):
     f = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+                "-Xcompiler", "-ffp-contract=off",
                 "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
     if src in NO_FMAD:
         f.append("--fmad=false")
@@ -43,12 +46,17 @@ def _flags(src: str):
     return f
 
 
+def _flavor() -> str:
+    return "checked" if os.environ.get("MSPLAT_CHECKED") else "release"
+
+
 def _compile(src: str) -> str:
-    obj = os.path.join(BUILD, src + ".o")
+    obj = os.path.join(BUILD, _flavor(), src + ".o")
     path = os.path.join(CSRC, src)
     deps = [path] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
     deps.append(os.path.join(ROOT, "include", "msplat_engine.h"))
     deps.append(os.path.join(ROOT, "include", "msplat_c_api.h"))
+    deps.append(os.path.abspath(__file__))   # flags live here
     if os.path.exists(obj) and all(os.path.getmtime(d) <= os.path.getmtime(obj) for d in deps if os.path.exists(d)):
         return obj
     cmd = [nvcc()] + _flags(src) + ["-c", path, "-o", obj]
@@ -59,15 +67,20 @@ def _compile(src: str) -> str:
 
 
 def build(verbose: bool = False) -> str:
-    os.makedirs(BUILD, exist_ok=True)
+    os.makedirs(os.path.join(BUILD, _flavor()), exist_ok=True)
     srcs = sources()
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(_compile, srcs))
-    if not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
+    stamp = os.path.join(BUILD, "linked_flavor")
+    last = open(stamp).read() if os.path.exists(stamp) else ""
+    if (not os.path.exists(LIB) or last != _flavor()
+            or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs)):
         cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        with open(stamp, "w") as f:
+            f.write(_flavor())
     if verbose:
         print(LIB)
     return LIB

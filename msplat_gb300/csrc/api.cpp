@@ -159,11 +159,12 @@ static std::vector<float> knn3_mean_distance(const std::vector<float> &xyz) {
             const float reach = (float)r * cell;
             if (best[2] <= reach * reach || r > std::max({dim[0], dim[1], dim[2]})) break;
         }
-        int have = 0;
+        // with fewer than 3 neighbours the missing distances count as 0,
+        // as in the reference's k = 4 search over a too-small cloud
         float s = 0;
         for (int k = 0; k < 3; k++)
-            if (best[k] < 1e29f) { s += std::sqrt(best[k]); have++; }
-        out[i] = have ? s / (float)have : 1.0f;
+            if (best[k] < 1e29f) s += std::sqrt(best[k]);
+        out[i] = s / 3.0f;
     }
     return out;
 }
@@ -423,10 +424,11 @@ struct TrainerImpl {
         h.a[2].resize(4 * n);
         for (int64_t i = 0; i < n; i++) {
             const float u = u01(qr), v = u01(qr), w = u01(qr);
-            h.a[2][4 * i + 0] = std::sqrt(1 - u) * std::sin(2 * (float)M_PI * v);
-            h.a[2][4 * i + 1] = std::sqrt(1 - u) * std::cos(2 * (float)M_PI * v);
-            h.a[2][4 * i + 2] = std::sqrt(u) * std::sin(2 * (float)M_PI * w);
-            h.a[2][4 * i + 3] = std::sqrt(u) * std::cos(2 * (float)M_PI * w);
+            // float radius times a double-precision angle term, rounded once
+            h.a[2][4 * i + 0] = (float)(std::sqrt(1 - u) * std::sin(2 * M_PI * v));
+            h.a[2][4 * i + 1] = (float)(std::sqrt(1 - u) * std::cos(2 * M_PI * v));
+            h.a[2][4 * i + 2] = (float)(std::sqrt(u) * std::sin(2 * M_PI * w));
+            h.a[2][4 * i + 3] = (float)(std::sqrt(u) * std::cos(2 * M_PI * w));
         }
         h.a[3].resize(3 * n);
         for (int64_t i = 0; i < 3 * n; i++) h.a[3][i] = (float)((ds->rgb[i] / 255.0 - 0.5) / kShC0);
@@ -483,8 +485,9 @@ struct TrainerImpl {
         a.beta1 = 0.9f; a.beta2 = 0.999f; a.eps = 1e-8f;
         a.invis_scale = 1.0f;
         if (!training) return;
-        const float bc1 = 1.0f - std::pow(0.9f, (float)adam_step_count);
-        const float bc2 = 1.0f - std::pow(0.999f, (float)adam_step_count);
+        // float beta raised to an int power: evaluated in double, rounded once
+        const float bc1 = (float)(1.0 - std::pow((double)0.9f, (double)adam_step_count));
+        const float bc2 = (float)(1.0 - std::pow((double)0.999f, (double)adam_step_count));
         for (int g = 0; g < 6; g++) { a.step_size[g] = adam_lr[g] / bc1; a.bc2_sqrt[g] = std::sqrt(bc2); }
         const bool masked = !cam.mask.empty() && cam.unmasked > 0;
         a.loss_inv_n = masked ? 1.0f / (float)(cam.unmasked * 3) : 1.0f / (float)((long long)cam.width * cam.height * 3);

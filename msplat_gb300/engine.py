@@ -34,11 +34,12 @@ def prepare_cam(c2w, width: int, height: int, fx: float, fy: float):
 def step_scalars(step: int, adam_step: int, lr=LR_INIT, sh_degree=3, sh_interval=1000, op_reg=0.01, sc_reg=0.01,
                  width=None, height=None, noise_lr=5e5, cull_radius=3.0):
     """Per-step scalars of Model::fullIteration (core/src/model.cpp:901-975)."""
-    bc1 = 1.0 - BETA1 ** adam_step
-    bc2 = 1.0 - BETA2 ** adam_step
+    # float betas raised to an int power in double, rounded once (model.cpp:915-916)
+    bc1 = np.float32(1.0 - float(np.float32(BETA1)) ** adam_step)
+    bc2 = np.float32(1.0 - float(np.float32(BETA2)) ** adam_step)
     d = dict(degrees_to_use=min(step // sh_interval, sh_degree),
-             step_size=[float(np.float32(l) / np.float32(bc1)) for l in lr],
-             bc2_sqrt=[float(np.sqrt(np.float32(bc2)))] * 6,
+             step_size=[float(np.float32(l) / bc1) for l in lr],
+             bc2_sqrt=[float(np.sqrt(bc2))] * 6,
              beta1=BETA1, beta2=BETA2, eps=EPS,
              op_reg=op_reg if step >= 500 else 0.0, sc_reg=sc_reg if step >= 500 else 0.0, invis_scale=1.0,
              seed=step, noise_lr=noise_lr, xyz_lr=lr[0], max_disp=cull_radius * 0.0167 if cull_radius > 0 else 0.05)
@@ -79,19 +80,33 @@ def camera_dict(cam) -> dict:
 
 
 class DeviceGaussians:
-    """Parameters and Adam moments as CUDA tensors (reference layouts)."""
+    """Parameters and Adam moments as CUDA tensors (reference layouts).
 
-    def __init__(self, g, device="cuda"):
+    With `cap` the tensors hold `cap` rows (the MCMC budget, Model::cap_max)
+    of which the first `active` are live; MCMC growth raises `active`."""
+
+    def __init__(self, g, device="cuda", cap: int | None = None):
         import torch
         self.torch = torch
-        self.params = {k: torch.from_numpy(np.ascontiguousarray(a)).to(device) for k, a in zip(GROUPS, g.arrays())}
-        self.params["opacities"] = self.params["opacities"].reshape(-1).contiguous()
+        cap = g.n if cap is None else int(cap)
+        if cap < g.n:
+            raise ValueError("cap below the number of Gaussians")
+        self.params = {}
+        for k, a in zip(GROUPS, g.arrays()):
+            t = torch.zeros((cap,) + a.shape[1:], dtype=torch.float32, device=device)
+            t[:g.n] = torch.from_numpy(np.ascontiguousarray(a, np.float32)).to(device)
+            self.params[k] = t
         self.exp_avg = {k: torch.zeros_like(v) for k, v in self.params.items()}
         self.exp_avg_sq = {k: torch.zeros_like(v) for k, v in self.params.items()}
         self.rest_bases = int(g.features_rest.shape[1])
+        self.active = g.n
 
     @property
     def n(self):
+        return self.active
+
+    @property
+    def cap(self):
         return int(self.params["means"].shape[0])
 
     def native(self):
@@ -105,9 +120,11 @@ class DeviceGaussians:
             st.exp_avg_sq[i] = self.exp_avg_sq[k].data_ptr()
         return g, st
 
-    def to_numpy(self):
-        return {k: v.detach().cpu().numpy() for k, v in self.params.items()}, \
-               ({k: v.cpu().numpy() for k, v in self.exp_avg.items()}, {k: v.cpu().numpy() for k, v in self.exp_avg_sq.items()})
+    def to_numpy(self, rows: int | None = None):
+        r = self.n if rows is None else rows
+        return {k: v[:r].detach().cpu().numpy() for k, v in self.params.items()}, \
+               ({k: v[:r].cpu().numpy() for k, v in self.exp_avg.items()},
+                {k: v[:r].cpu().numpy() for k, v in self.exp_avg_sq.items()})
 
 
 class Engine:
@@ -148,6 +165,16 @@ class Engine:
     def render(self, dg: DeviceGaussians, args: N.MsplatStepArgs):
         g, _ = dg.native()
         self._check(self.L.msplat_engine_render(self.h, C.byref(g), C.byref(args)))
+
+    def mcmc(self, dg: DeviceGaussians, cull_radius: float, relocation_count: int):
+        """One relocation + growth round on the device; returns (stats, new relocation_count)."""
+        g, st = dg.native()
+        rc = C.c_int(relocation_count)
+        out = N.MsplatMcmcStats()
+        self._check(self.L.msplat_engine_mcmc(self.h, C.byref(g), C.byref(st), dg.cap, cull_radius, C.byref(rc),
+                                              C.byref(out)))
+        dg.active = out.num_active
+        return out, rc.value
 
     def synchronize(self):
         self._check(self.L.msplat_engine_synchronize(self.h))
