@@ -197,8 +197,9 @@ def run_reference(args):
 
 
 def config_dict(args):
-    return {"workload": "1M Gaussians (SH deg 3) training step at 1297x840, synthetic 1M+200k GT scene",
-            "n_gaussians": N_MODEL, "width": 1297, "height": 840, "views": VIEWS, "sh_degree": 3,
+    n = getattr(args, "gaussians", N_MODEL)
+    return {"workload": f"{n / 1e6:g}M Gaussians (SH deg 3) training step at 1297x840, synthetic 1M+200k GT scene",
+            "n_gaussians": n, "width": 1297, "height": 840, "views": VIEWS, "sh_degree": 3,
             "raster": "monolithic (4346 tiles >= 400)", "l2": "working set > L2 (params+moments 0.7 GB/step)",
             "seed": 0}
 
@@ -213,8 +214,9 @@ def run_engine(args):
         import torch.distributed as dist
         dist.init_process_group("gloo")
     torch.cuda.set_device(local)
-    sc, model = build_workload()
-    eng = E.Engine(local, N_MODEL)
+    n_model = args.gaussians
+    sc, model = build_workload(n_model=n_model)
+    eng = E.Engine(local, n_model)
     cams = [E.camera_dict(c) for c in sc.train_cams]
 
     # targets: the GT scene rendered by the engine (forward path, parity-tested)
@@ -290,7 +292,7 @@ def run_engine(args):
 
     # roofline of the dominant stage (CUDA events on the engine's stream)
     stage_ms = {name: st.stage_ms[i] / max(1, st.timed_steps) for i, name in enumerate(E.N.STAGES)}
-    units = {"g": N_MODEL, "i": float(st.num_intersections), "p": 1297 * 840}
+    units = {"g": n_model, "i": float(st.num_intersections), "p": 1297 * 840}
     dom = max(stage_ms, key=stage_ms.get)
     alg = sum(units[u] * b for u, b in STAGE_BYTES[dom].items())
     peak, kind = measured_peaks()
@@ -331,6 +333,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--gaussians", type=int, default=N_MODEL,
+                    help="trained Gaussians (default 1M; smaller only for profiling captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3")

@@ -80,7 +80,7 @@ class Engine {
         // kernels of this step: projection, count/scan/scatter/sort, raster
         // (+ merge when chunked), and for training 3 loss passes, raster
         // backward (+ prefix/suffix), projection backward, Adam, SGLD
-        launches_ += 5 + (K > 1 ? 2 : 1);
+        launches_ += 1 + (K > 1 ? 2 : 1);   // + the tile-mapping launches, counted below
         if (gt) launches_ += 3;
         if (gt && backward) launches_ += (K > 1 ? 2 : 1) + 1 + (args.do_optimizer && st ? 1 : 0) + (args.do_sgld ? 1 : 0);
 
@@ -113,7 +113,11 @@ class Engine {
         ta.tile_offsets = ptr<uint32_t>("tile_offsets"); ta.max_tile_count = ptr<uint32_t>("max_tile");
         ta.keys = ptr<uint64_t>("keys"); ta.keys_alt = ptr<uint64_t>("keys_alt");
         ta.packed = ptr<SplatRec>("packed"); ta.nan_counts = pa.nan_counts;
-        launch_tiles(ta, stream_);
+        const size_t cb = tile_cta_bins_bytes(N, T);
+        if (cb) alloc("cta_bins", cb);
+        ta.cta_bins = cb ? ptr<uint32_t>("cta_bins") : nullptr;
+        ta.tile_lists = ptr<uint32_t>("tile_lists"); ta.tile_class = ptr<uint32_t>("tile_class");
+        launches_ += launch_tiles(ta, num_sms_, stream_);
         mark(2);
 
         RasterArgs ra{};
@@ -328,6 +332,8 @@ class Engine {
         if (T <= cap_tiles_) return;
         alloc("tile_counts", (size_t)2 * T * 4);
         alloc("tile_offsets", (size_t)(T + 1) * 4);
+        alloc("tile_lists", (size_t)3 * T * 4);
+        alloc("tile_class", 64, true);
         cap_tiles_ = T;
     }
     void ensure_isect(long long c) {

@@ -31,6 +31,9 @@ struct TileArgs {
     const float2 *aabb;
     uint32_t *tile_counts;  // zeroed before the step
     uint32_t *tile_write;   // zeroed before the step
+    uint32_t *cta_bins;     // [ceil(n / 4096), T] per-CTA tile histograms (block-aggregated path)
+    uint32_t *tile_lists;   // [3, T] tiles of each sort class (written by the scan)
+    uint32_t *tile_class;   // [6]: list lengths, then the sort kernels' work counters
     uint32_t *tile_offsets; // [T+1]
     uint32_t *max_tile_count;
     uint64_t *keys, *keys_alt;
@@ -109,8 +112,9 @@ struct McmcResult {
 void debug_sync(cudaStream_t s, const char *what);
 
 void launch_project_fwd(const ProjectArgs &a, cudaStream_t s);
-void launch_tiles(const TileArgs &a, cudaStream_t s);
+int launch_tiles(const TileArgs &a, int num_sms, cudaStream_t s);   // returns the kernel launches
 size_t sort_pack_smem_bytes();
+size_t tile_cta_bins_bytes(int n, int num_tiles);   // 0 when the block-aggregated path is not used
 void launch_raster_fwd(const RasterArgs &a, cudaStream_t s);
 void launch_loss(const LossArgs &a, cudaStream_t s);
 void launch_raster_bwd(const RasterArgs &a, cudaStream_t s);

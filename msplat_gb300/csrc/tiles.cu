@@ -11,6 +11,11 @@
 
 namespace msplat {
 
+// per-tile sort classes (by key count)
+constexpr int kSortItems = 8;                    // keys per thread in the shared-memory sorts
+constexpr int kSortLightKeys = 512 * kSortItems;   // 4096: 512-thread CTA, two per SM
+constexpr int kSortHeavyKeys = 1024 * kSortItems;  // 8192: 1024-thread CTA, one per SM
+
 __device__ __forceinline__ bool splat_active(int i, const int *radii, const float *depths) {
     if (radii[i] <= 0) return false;
     const float d = depths[i];
@@ -36,7 +41,9 @@ __global__ void __launch_bounds__(256) k_count(TileArgs a) {
 __global__ void __launch_bounds__(1024) k_scan(TileArgs a) {
     __shared__ uint32_t warp_tot[32];
     __shared__ uint32_t max_warp[32];
+    __shared__ uint32_t class_n[3];
     const int T = a.num_tiles;
+    if (threadIdx.x < 3) class_n[threadIdx.x] = 0;
     const int per = (T + 1023) / 1024;
     const int lo = min(T, (int)threadIdx.x * per), hi = min(T, lo + per);
     uint32_t sum = 0, mx = 0;
@@ -66,11 +73,24 @@ __global__ void __launch_bounds__(1024) k_scan(TileArgs a) {
     __syncthreads();
     uint32_t run = warp_tot[wid] + incl - sum;
     for (int t = lo; t < hi; t++) {
+        const uint32_t c = a.tile_counts[t];
         a.tile_offsets[t] = run;
-        run += a.tile_counts[t];
+        run += c;
+        // sort class of the tile: shared-memory sort by a 512- or a
+        // 1024-thread CTA, or the global-memory sort above kSortHeavyKeys
+        if (c > 0) {
+            const int cls = c <= (uint32_t)kSortLightKeys ? 0 : (c <= (uint32_t)kSortHeavyKeys ? 1 : 2);
+            const uint32_t pos = atomicAdd(&class_n[cls], 1u);
+            a.tile_lists[(size_t)cls * T + pos] = (uint32_t)t;
+        }
     }
     if (threadIdx.x == 1023) a.tile_offsets[T] = run;
     if (threadIdx.x == 0) a.max_tile_count[0] = max_warp[0];
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        a.tile_class[threadIdx.x] = class_n[threadIdx.x];      // list lengths
+        a.tile_class[3 + threadIdx.x] = 0;                     // work counters of the sort kernels
+    }
 }
 
 __global__ void __launch_bounds__(256) k_scatter(TileArgs a) {
@@ -91,35 +111,24 @@ __global__ void __launch_bounds__(256) k_scatter(TileArgs a) {
         }
 }
 
-// Block-aggregated count and scatter: a CTA covers kAggPerCta Gaussians and
-// keeps a shared-memory histogram over all tiles, so the global atomics fall
-// from one per intersection to one per (CTA, touched tile).  Scatter reserves
-// each tile's slot range with that one atomic and hands out slots inside it
-// with shared-memory atomics.  Used while the histogram fits (kAggMaxTiles).
+// Block-aggregated count and scatter.  A CTA of kAggThreads covers
+// kAggPerCta Gaussians and keeps a shared-memory histogram over all tiles.
+// Count stores the CTA's histogram row to cta_bins[cta][T]; a column scan
+// turns the rows into per-(CTA, tile) start offsets and the tile totals; the
+// scatter CTA loads its row, adds the tile offsets, and hands out slots with
+// shared-memory atomics.  No global atomics, and each tile's bucket is
+// filled CTA by CTA.  Used while the histogram fits (kAggMaxTiles).
 constexpr int kAggPerCta = 4096;
+constexpr int kAggThreads = 1024;
 constexpr int kAggMaxTiles = 12288;
 
-__global__ void __launch_bounds__(256) k_count_agg(TileArgs a) {
-    extern __shared__ uint32_t bins[];
-    const int T = a.num_tiles;
-    for (int t = threadIdx.x; t < T; t += blockDim.x) bins[t] = 0;
-    __syncthreads();
-    const int g0 = blockIdx.x * kAggPerCta, g1 = min(a.n, g0 + kAggPerCta);
-    for (int i = g0 + threadIdx.x; i < g1; i += blockDim.x) {
-        if (!splat_active(i, a.radii, a.depths)) continue;
-        const float4 ra = a.rec[i].a;
-        const float2 ab = a.aabb[i];
-        int x0, y0, x1, y1;
-        tile_rect(ra.x, ra.y, ab.x, ab.y, a.tiles_x, a.tiles_y, x0, y0, x1, y1);
-        for (int y = y0; y < y1; y++)
-            for (int x = x0; x < x1; x++) atomicAdd(&bins[y * a.tiles_x + x], 1u);
-    }
-    __syncthreads();
-    for (int t = threadIdx.x; t < T; t += blockDim.x)
-        if (bins[t]) atomicAdd(a.tile_counts + t, bins[t]);
+__device__ __forceinline__ void agg_rect(const TileArgs &a, int i, int &x0, int &y0, int &x1, int &y1) {
+    const float4 ra = a.rec[i].a;
+    const float2 ab = a.aabb[i];
+    tile_rect(ra.x, ra.y, ab.x, ab.y, a.tiles_x, a.tiles_y, x0, y0, x1, y1);
 }
 
-__global__ void __launch_bounds__(256) k_scatter_agg(TileArgs a) {
+__global__ void __launch_bounds__(kAggThreads) k_count_agg(TileArgs a) {
     extern __shared__ uint32_t bins[];
     const int T = a.num_tiles;
     for (int t = threadIdx.x; t < T; t += blockDim.x) bins[t] = 0;
@@ -127,61 +136,320 @@ __global__ void __launch_bounds__(256) k_scatter_agg(TileArgs a) {
     const int g0 = blockIdx.x * kAggPerCta, g1 = min(a.n, g0 + kAggPerCta);
     for (int i = g0 + threadIdx.x; i < g1; i += blockDim.x) {
         if (!splat_active(i, a.radii, a.depths)) continue;
-        const float4 ra = a.rec[i].a;
-        const float2 ab = a.aabb[i];
         int x0, y0, x1, y1;
-        tile_rect(ra.x, ra.y, ab.x, ab.y, a.tiles_x, a.tiles_y, x0, y0, x1, y1);
+        agg_rect(a, i, x0, y0, x1, y1);
         for (int y = y0; y < y1; y++)
             for (int x = x0; x < x1; x++) atomicAdd(&bins[y * a.tiles_x + x], 1u);
     }
     __syncthreads();
-    // reserve each touched tile's slots; bins[t] becomes the next free slot
-    for (int t = threadIdx.x; t < T; t += blockDim.x) {
-        const uint32_t c = bins[t];
-        if (c) bins[t] = a.tile_offsets[t] + atomicAdd(a.tile_write + t, c);
+    uint32_t *row = a.cta_bins + (size_t)blockIdx.x * T;
+    for (int t = threadIdx.x; t < T; t += blockDim.x) row[t] = bins[t];
+}
+
+// One thread per tile: exclusive scan down the column of CTA rows; the
+// column total is the tile's count.
+__global__ void __launch_bounds__(256) k_cta_scan(TileArgs a, int ctas) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int T = a.num_tiles;
+    if (t >= T) return;
+    uint32_t run = 0;
+    int c = 0;
+    for (; c + 4 <= ctas; c += 4) {
+        uint32_t v[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) v[k] = a.cta_bins[(size_t)(c + k) * T + t];
+#pragma unroll
+        for (int k = 0; k < 4; k++) { a.cta_bins[(size_t)(c + k) * T + t] = run; run += v[k]; }
     }
+    for (; c < ctas; c++) {
+        const uint32_t v = a.cta_bins[(size_t)c * T + t];
+        a.cta_bins[(size_t)c * T + t] = run;
+        run += v;
+    }
+    a.tile_counts[t] = run;
+}
+
+__global__ void __launch_bounds__(kAggThreads) k_scatter_agg(TileArgs a) {
+    extern __shared__ uint32_t bins[];
+    const int T = a.num_tiles;
+    const uint32_t *row = a.cta_bins + (size_t)blockIdx.x * T;
+    for (int t = threadIdx.x; t < T; t += blockDim.x) bins[t] = a.tile_offsets[t] + row[t];
     __syncthreads();
+    const int g0 = blockIdx.x * kAggPerCta, g1 = min(a.n, g0 + kAggPerCta);
     for (int i = g0 + threadIdx.x; i < g1; i += blockDim.x) {
         if (!splat_active(i, a.radii, a.depths)) continue;
-        const float4 ra = a.rec[i].a;
-        const float2 ab = a.aabb[i];
         int x0, y0, x1, y1;
-        tile_rect(ra.x, ra.y, ab.x, ab.y, a.tiles_x, a.tiles_y, x0, y0, x1, y1);
+        agg_rect(a, i, x0, y0, x1, y1);
         const uint64_t key = ((uint64_t)__float_as_uint(a.depths[i]) << 32) | (uint32_t)i;
         for (int y = y0; y < y1; y++)
             for (int x = x0; x < x1; x++) {
-                const uint64_t dst = atomicAdd(&bins[y * a.tiles_x + x], 1u);
+                const uint32_t dst = atomicAdd(&bins[y * a.tiles_x + x], 1u);
                 if (dst < (uint64_t)a.capacity) a.keys[dst] = key;   // overflow is dropped, never written
             }
     }
 }
 
-// ---------------------------------------------------------------------------
-// Per-tile sort by one CTA.  Keys are (depth bits << 32 | id).  A stable LSD
-// radix sort on the four depth bytes (a byte equal in every key is skipped)
-// orders the tile by depth; runs of equal depth (exact clones) are then put
-// in id order, which gives the reference's (depth, id) order.
-// Tiles up to kSortSmemKeys keys sort in shared memory in one chunk, 8 keys
-// per thread; larger tiles run chunked passes in global memory.
-// ---------------------------------------------------------------------------
-constexpr int kSortThreads = 512;
-constexpr int kSortWarps = kSortThreads / 32;
-constexpr int kItems = 8;
-constexpr int kSortSmemKeys = kSortThreads * kItems;   // 4096
+size_t tile_cta_bins_bytes(int n, int num_tiles) {
+    if (num_tiles > kAggMaxTiles || n <= 0) return 0;
+    return (size_t)((n + kAggPerCta - 1) / kAggPerCta) * (size_t)num_tiles * sizeof(uint32_t);
+}
 
-struct SortSmem {
-    uint32_t hist[256];
-    uint32_t base[256];
-    uint16_t wcnt[kSortWarps][256];
-    uint32_t woff[kSortWarps][256];
-    int skip;
-};
+// ---------------------------------------------------------------------------
+// Per-tile sort + pack.  Keys are (depth bits << 32 | id); the reference
+// orders each tile by (depth, id) ascending.
+//
+// Tiles up to kSortHeavyKeys sort in shared memory: the 32-bit depth keys with
+// a 16-bit local index as payload go through a stable LSD radix sort on 8-bit
+// digits (bytes above the highest bit that differs within the tile are
+// skipped, and so is any byte that turns out constant), then runs of equal
+// depth (exact clones) are put in id order.  A 512-thread CTA takes tiles up
+// to 4096 keys, a 1024-thread CTA tiles up to 8192; larger tiles sort their
+// 64-bit keys in global memory in chunks.  Each class runs as a persistent
+// grid that takes tiles from its list (built by k_scan) through an atomic
+// work counter.  The pack step gathers the 48-byte splat record of every key
+// in sorted order.
+// ---------------------------------------------------------------------------
 
 __device__ __forceinline__ uint32_t digit_of(uint64_t key, int shift) { return (uint32_t)(key >> shift) & 255u; }
 
+// the record written for one sorted key (the id rides in a.w)
+__device__ __forceinline__ SplatRec pack_record(const TileArgs &a, uint32_t g) {
+    SplatRec r;
+    if (g >= (uint32_t)a.n) {
+        r.a = make_float4(0.f, 0.f, 0.f, __int_as_float(0));
+        r.b = make_float4(0.f, 0.f, 0.f, 0.f);
+        r.c = make_float4(0.f, 0.f, 0.f, 0.f);
+        return r;
+    }
+    r = a.rec[g];
+    const bool ok = finite_bits(r.a.x) && finite_bits(r.a.y) && finite_bits(r.a.z) && finite_bits(r.b.x) &&
+                    finite_bits(r.b.y) && finite_bits(r.b.z) && finite_bits(r.c.x) && finite_bits(r.c.y) &&
+                    finite_bits(r.c.z);
+    if (!ok) {
+        if (a.nan_counts) {
+            atomicAdd(a.nan_counts + kNanPack, 1u);
+            if (!finite_bits(r.a.z)) atomicAdd(a.nan_counts + kNanPackOpacity, 1u);
+        }
+        r.a = make_float4(0.f, 0.f, 0.f, 0.f);
+        r.b = make_float4(0.f, 0.f, 0.f, 0.f);
+        r.c = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    r.a.w = __int_as_float((int)g);
+    return r;
+}
+
+// A tile whose bucket does not fit the buffer is emitted transparent
+// (hybrid_sort_pack_kernel's region guard, msplat_metal.metal:2523-2535).
+// Returns true when it did so.
+template <int THREADS> __device__ bool emit_if_overflow(const TileArgs &a, uint32_t start, int count) {
+    if ((uint64_t)start + (uint64_t)count <= (uint64_t)a.capacity) return false;
+    for (int j = threadIdx.x; j < count; j += THREADS) {
+        const uint64_t d = (uint64_t)start + j;
+        if (d < (uint64_t)a.capacity) {
+            SplatRec z;
+            z.a = make_float4(0.f, 0.f, 0.f, __int_as_float(0));
+            z.b = make_float4(0.f, 0.f, 0.f, 0.f);
+            z.c = make_float4(0.f, 0.f, 0.f, 0.f);
+            a.packed[d] = z;
+        }
+    }
+    return true;
+}
+
+// next tile of class `cls` for this CTA, or -1; ends with a barrier
+__device__ __forceinline__ int next_tile(const TileArgs &a, int cls, int *slot) {
+    if (threadIdx.x == 0) {
+        const uint32_t k = atomicAdd(a.tile_class + 3 + cls, 1u);
+        *slot = k < a.tile_class[cls] ? (int)a.tile_lists[(size_t)cls * a.num_tiles + k] : -1;
+    }
+    __syncthreads();
+    return *slot;
+}
+
+// ---- shared-memory pair sort (tiles up to THREADS * kSortItems keys) ----
+
+template <int THREADS> struct PairSmem {
+    static constexpr int kWarps = THREADS / 32;
+    static constexpr int kCap = THREADS * kSortItems;
+    uint32_t key[2][kCap];        // depth bits
+    uint32_t id[kCap];            // Gaussian id of local index i
+    uint16_t idx[2][kCap];        // local index riding with the key
+    uint16_t wcnt[kWarps][256];   // per-warp digit counts
+    uint16_t woff[kWarps][256];   // per-warp offsets inside a digit
+    uint32_t base[256];
+    uint32_t dsum[8];
+    uint32_t dlo, dhi;
+    int skip_shift;
+    int slot;
+};
+
+// One LSD pass over n keys, buffer b -> 1 - b.  The keys are spread over the
+// warps in contiguous segments of 32 * ipt (ipt = ceil(n / THREADS)), so small
+// tiles keep few warps busy for few rounds.  Expects wcnt == 0 for the warps
+// holding keys and leaves it so.  Returns false (nothing moved) when one digit
+// holds every key.
+template <int THREADS>
+__device__ bool pair_pass(PairSmem<THREADS> &sm, int b, int n, int shift, unsigned *dbg) {
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int ipt = (n + THREADS - 1) / THREADS;   // 1..kSortItems
+    const int seg = 32 * ipt;
+    const int nw = (n + seg - 1) / seg;
+    uint32_t kv[kSortItems], rank[kSortItems];
+    uint16_t iv[kSortItems];
+    const uint32_t lt = (1u << lane) - 1u;
+    if (wid < nw) {
+#pragma unroll
+        for (int j = 0; j < kSortItems; j++) {
+            if (j >= ipt) continue;
+            const int i = wid * seg + j * 32 + lane;
+            const bool valid = i < n;
+            kv[j] = valid ? sm.key[b][i] : 0u;
+            iv[j] = valid ? sm.idx[b][i] : (uint16_t)0;
+            const uint32_t d = valid ? ((kv[j] >> shift) & 255u) : 256u;
+            const uint32_t peers = __match_any_sync(0xffffffffu, d);
+            uint32_t old = 0;
+            if (valid) old = sm.wcnt[wid][d];
+            __syncwarp();
+            rank[j] = valid ? old + __popc(peers & lt) : 0xffffffffu;
+            if (valid && (peers & lt) == 0) sm.wcnt[wid][d] = (uint16_t)(old + __popc(peers));
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+    uint32_t total = 0, incl = 0;
+    if (tid < 256) {
+        for (int w = 0; w < nw; w++) {
+            const uint32_t c = sm.wcnt[w][tid];
+            sm.woff[w][tid] = (uint16_t)total;
+            sm.wcnt[w][tid] = 0;
+            total += c;
+        }
+        incl = total;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += u;
+        }
+        if (lane == 31) sm.dsum[wid] = incl;
+        if (total == (uint32_t)n) sm.skip_shift = shift;
+    }
+    __syncthreads();
+    if (sm.skip_shift == shift) return false;   // uniform
+    if (tid < 256) {
+        uint32_t add = 0;
+        for (int w = 0; w < wid; w++) add += sm.dsum[w];
+        sm.base[tid] = add + incl - total;
+    }
+    __syncthreads();
+    if (wid < nw) {
+#pragma unroll
+        for (int j = 0; j < kSortItems; j++) {
+            if (j >= ipt || rank[j] == 0xffffffffu) continue;
+            const uint32_t d = (kv[j] >> shift) & 255u;
+            const uint32_t pos = sm.base[d] + sm.woff[wid][d] + rank[j];
+            if (MS_GUARD(pos < (uint32_t)n, 4, pos, dbg)) {
+                sm.key[1 - b][pos] = kv[j];
+                sm.idx[1 - b][pos] = iv[j];
+            }
+        }
+    }
+    __syncthreads();
+    return true;
+}
+
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) k_sort_pack_smem(TileArgs a, int cls) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    PairSmem<THREADS> &sm = *reinterpret_cast<PairSmem<THREADS> *>(smem_raw);
+    const int tid = threadIdx.x;
+    unsigned *dbg = a.nan_counts ? a.nan_counts + kDbgSlot : nullptr;
+    // shared memory starts stale: the passes expect zero digit counts
+    for (int i = tid; i < PairSmem<THREADS>::kWarps * 256; i += THREADS) (&sm.wcnt[0][0])[i] = 0;
+    for (;;) {
+        const int t = next_tile(a, cls, &sm.slot);   // barrier inside
+        if (t < 0) break;
+        const int count = (int)a.tile_counts[t];
+        const uint32_t start = a.tile_offsets[t];
+        if (!MS_GUARD(count <= PairSmem<THREADS>::kCap, 5, count, dbg) || emit_if_overflow<THREADS>(a, start, count)) {
+            __syncthreads();
+            continue;
+        }
+        if (tid == 0) { sm.dlo = 0xffffffffu; sm.dhi = 0u; sm.skip_shift = -1; }
+        __syncthreads();
+        uint32_t lo = 0xffffffffu, hi = 0u;
+        for (int j = tid; j < count; j += THREADS) {
+            const uint64_t k = a.keys[start + j];
+            const uint32_t d = (uint32_t)(k >> 32);
+            sm.key[0][j] = d;
+            sm.idx[0][j] = (uint16_t)j;
+            sm.id[j] = (uint32_t)k;
+            lo = min(lo, d);
+            hi = max(hi, d);
+        }
+        lo = __reduce_min_sync(0xffffffffu, lo);
+        hi = __reduce_max_sync(0xffffffffu, hi);
+        if ((tid & 31) == 0) { atomicMin(&sm.dlo, lo); atomicMax(&sm.dhi, hi); }
+        __syncthreads();
+        const uint32_t diff = sm.dlo ^ sm.dhi;
+        int b = 0;
+        for (int shift = 0; shift < 32; shift += 8) {
+            if ((diff >> shift) == 0u) break;   // this byte and all above are equal in every key
+            if (pair_pass<THREADS>(sm, b, count, shift, dbg)) b ^= 1;
+        }
+        // equal depths (exact clones): order the run by id
+        for (int j = tid; j < count; j += THREADS) {
+            const uint32_t dj = sm.key[b][j];
+            if (j > 0 && sm.key[b][j - 1] == dj) continue;
+            if (j + 1 >= count || sm.key[b][j + 1] != dj) continue;
+            int e = j + 1;
+            while (e < count && sm.key[b][e] == dj) e++;
+            for (int u = j + 1; u < e; u++) {
+                const uint16_t v = sm.idx[b][u];
+                const uint32_t vid = sm.id[v];
+                int w = u - 1;
+                while (w >= j && sm.id[sm.idx[b][w]] > vid) { sm.idx[b][w + 1] = sm.idx[b][w]; w--; }
+                sm.idx[b][w + 1] = v;
+            }
+        }
+        __syncthreads();
+        // pack, two records in flight per thread
+        for (int j = tid; j < count; j += 2 * THREADS) {
+            const int j2 = j + THREADS;
+            const uint32_t g0 = sm.id[sm.idx[b][j]];
+            const uint32_t g1 = j2 < count ? sm.id[sm.idx[b][j2]] : 0u;
+            const SplatRec r0 = pack_record(a, g0);
+            if (j2 < count) {
+                const SplatRec r1 = pack_record(a, g1);
+                a.packed[start + j] = r0;
+                a.packed[start + j2] = r1;
+            } else {
+                a.packed[start + j] = r0;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <int THREADS> constexpr size_t pair_smem_bytes() { return sizeof(PairSmem<THREADS>); }
+
+// ---- global-memory sort for tiles above kSortHeavyKeys ----
+
+constexpr int kGlobThreads = 512;
+constexpr int kGlobWarps = kGlobThreads / 32;
+
+struct GlobSmem {
+    uint32_t hist[256];
+    uint32_t base[256];
+    uint16_t wcnt[kGlobWarps][256];
+    uint32_t woff[kGlobWarps][256];
+    uint32_t dlo, dhi;
+    int skip;
+    int slot;
+};
+
 // Exclusive scan of sm.hist into sm.base by the first 256 threads; sets
 // sm.skip when one digit holds all n keys.  Ends with a barrier.
-__device__ void digit_scan(SortSmem &sm, int n) {
+__device__ void digit_scan(GlobSmem &sm, int n) {
     const int tid = threadIdx.x;
     if (tid < 256) {
         const uint32_t h = sm.hist[tid];
@@ -205,72 +473,18 @@ __device__ void digit_scan(SortSmem &sm, int n) {
     __syncthreads();
 }
 
-// One pass on n <= kSortSmemKeys keys, all in one chunk: src -> dst.
-// Returns false (and writes nothing) when the digit is constant.
-__device__ bool radix_pass_1chunk(const uint64_t *src, uint64_t *dst, int n, int shift, SortSmem &sm, unsigned *dbg) {
+// One stable pass on n keys in chunks of kGlobThreads: src -> dst.
+__device__ bool radix_pass_chunked(const uint64_t *src, uint64_t *dst, int n, int shift, GlobSmem &sm, unsigned *dbg) {
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    for (int k = tid; k < kSortWarps * 256; k += kSortThreads) (&sm.wcnt[0][0])[k] = 0;
+    for (int d = tid; d < 256; d += kGlobThreads) sm.hist[d] = 0;
     if (tid == 0) sm.skip = 0;
     __syncthreads();
-    uint64_t key[kItems];
-    uint32_t dig[kItems], rank[kItems];
-    const uint32_t lt = (1u << lane) - 1u;
-#pragma unroll
-    for (int j = 0; j < kItems; j++) {
-        const int idx = wid * (32 * kItems) + j * 32 + lane;
-        const bool valid = idx < n;
-        key[j] = valid ? src[idx] : 0ull;
-        dig[j] = valid ? digit_of(key[j], shift) : 256u;
-        const uint32_t peers = __match_any_sync(0xffffffffu, dig[j]);
-        uint32_t old = 0;
-        if (valid) old = sm.wcnt[wid][dig[j]];
-        __syncwarp();
-        rank[j] = old + __popc(peers & lt);
-        if (valid && (peers & lt) == 0) sm.wcnt[wid][dig[j]] = (uint16_t)(old + __popc(peers));
-        __syncwarp();
-    }
-    __syncthreads();
-    // per digit: offsets of each warp, totals -> hist
-    if (tid < 256) {
-        uint32_t run = 0;
-#pragma unroll 4
-        for (int w = 0; w < kSortWarps; w++) {
-            sm.woff[w][tid] = run;
-            run += sm.wcnt[w][tid];
-        }
-        sm.hist[tid] = run;
-    }
-    __syncthreads();
-    // exclusive scan of the totals (hist -> base); woff[0] is reused as warp
-    // sums only after every thread has read its offsets, so keep a copy
-    uint32_t my_off[kItems];
-#pragma unroll
-    for (int j = 0; j < kItems; j++) my_off[j] = (dig[j] < 256u) ? sm.woff[wid][dig[j]] : 0u;
-    __syncthreads();
-    digit_scan(sm, n);
-    if (sm.skip) return false;
-#pragma unroll
-    for (int j = 0; j < kItems; j++) {
-        if (dig[j] >= 256u) continue;
-        const uint32_t pos = sm.base[dig[j]] + my_off[j] + rank[j];
-        if (MS_GUARD(pos < (uint32_t)n, 4, pos, dbg)) dst[pos] = key[j];
-    }
-    __syncthreads();
-    return true;
-}
-
-// One pass on any n in chunks of kSortThreads keys (global-memory tiles).
-__device__ bool radix_pass_chunked(const uint64_t *src, uint64_t *dst, int n, int shift, SortSmem &sm, unsigned *dbg) {
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    for (int d = tid; d < 256; d += kSortThreads) sm.hist[d] = 0;
-    if (tid == 0) sm.skip = 0;
-    __syncthreads();
-    for (int i = tid; i < n; i += kSortThreads) atomicAdd(&sm.hist[digit_of(src[i], shift)], 1u);
+    for (int i = tid; i < n; i += kGlobThreads) atomicAdd(&sm.hist[digit_of(src[i], shift)], 1u);
     __syncthreads();
     digit_scan(sm, n);
     if (sm.skip) return false;
     const uint32_t lt_mask = (1u << lane) - 1u;
-    for (int c0 = 0; c0 < n; c0 += kSortThreads) {
+    for (int c0 = 0; c0 < n; c0 += kGlobThreads) {
         const int i = c0 + tid;
         const bool valid = i < n;
         const uint64_t key = valid ? src[i] : 0ull;
@@ -279,10 +493,10 @@ __device__ bool radix_pass_chunked(const uint64_t *src, uint64_t *dst, int n, in
         const uint32_t rank = __popc(peers & lt_mask);
         if (valid && rank == 0) sm.wcnt[wid][d] = (uint16_t)__popc(peers);
         __syncthreads();
-        for (int dd = tid; dd < 256; dd += kSortThreads) {
+        for (int dd = tid; dd < 256; dd += kGlobThreads) {
             uint32_t acc = sm.base[dd];
 #pragma unroll 4
-            for (int w = 0; w < kSortWarps; w++) {
+            for (int w = 0; w < kGlobWarps; w++) {
                 const uint32_t cnt = sm.wcnt[w][dd];
                 sm.woff[w][dd] = acc;
                 sm.wcnt[w][dd] = 0;
@@ -300,7 +514,7 @@ __device__ bool radix_pass_chunked(const uint64_t *src, uint64_t *dst, int n, in
 
 // Keys sorted by depth: order each run of equal depth by id.
 __device__ void order_ties(uint64_t *a, int n) {
-    for (int j = threadIdx.x; j < n; j += kSortThreads) {
+    for (int j = threadIdx.x; j < n; j += kGlobThreads) {
         const uint32_t dj = (uint32_t)(a[j] >> 32);
         if (j > 0 && (uint32_t)(a[j - 1] >> 32) == dj) continue;          // not a run start
         if (j + 1 >= n || (uint32_t)(a[j + 1] >> 32) != dj) continue;      // run of one
@@ -316,110 +530,90 @@ __device__ void order_ties(uint64_t *a, int n) {
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(kSortThreads) k_sort_pack(TileArgs a) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    SortSmem &sm = *reinterpret_cast<SortSmem *>(smem_raw);
-    uint64_t *sk0 = reinterpret_cast<uint64_t *>(smem_raw + ((sizeof(SortSmem) + 15) & ~size_t(15)));
-    uint64_t *sk1 = sk0 + kSortSmemKeys;
-    const int t = blockIdx.x;
-    const int count = (int)a.tile_counts[t];
-    if (count == 0) return;
-    const uint32_t start = a.tile_offsets[t];
+__global__ void __launch_bounds__(kGlobThreads) k_sort_pack_global(TileArgs a, int cls) {
+    __shared__ GlobSmem sm;
     const int tid = threadIdx.x;
     unsigned *dbg = a.nan_counts ? a.nan_counts + kDbgSlot : nullptr;
-    // a tile whose bucket does not fit the buffer is emitted transparent
-    // (hybrid_sort_pack_kernel's region guard, msplat_metal.metal:2523-2535)
-    if ((uint64_t)start + (uint64_t)count > (uint64_t)a.capacity) {
-        for (int j = tid; j < count; j += kSortThreads) {
-            const uint64_t d = (uint64_t)start + j;
-            if (d < (uint64_t)a.capacity) {
-                SplatRec z;
-                z.a = make_float4(0.f, 0.f, 0.f, __int_as_float(0));
-                z.b = make_float4(0.f, 0.f, 0.f, 0.f);
-                z.c = make_float4(0.f, 0.f, 0.f, 0.f);
-                a.packed[d] = z;
-            }
+    for (int i = tid; i < kGlobWarps * 256; i += kGlobThreads) (&sm.wcnt[0][0])[i] = 0;
+    for (;;) {
+        const int t = next_tile(a, cls, &sm.slot);
+        if (t < 0) break;
+        const int count = (int)a.tile_counts[t];
+        const uint32_t start = a.tile_offsets[t];
+        if (emit_if_overflow<kGlobThreads>(a, start, count)) {
+            __syncthreads();
+            continue;
         }
-        return;
-    }
-    // shared memory starts with stale contents: the chunked pass expects its
-    // per-warp digit counts at zero (each chunk clears what it used)
-    for (int i = tid; i < kSortWarps * 256; i += kSortThreads) (&sm.wcnt[0][0])[i] = 0;
-    uint64_t *src, *alt;
-    const bool in_smem = count <= kSortSmemKeys;
-    if (in_smem) {
-        for (int j = tid; j < count; j += kSortThreads) sk0[j] = a.keys[start + j];
-        src = sk0; alt = sk1;
-    } else {
-        src = a.keys + start; alt = a.keys_alt + start;
-    }
-    __syncthreads();
-    for (int shift = 32; shift < 64; shift += 8) {
-        const bool moved = in_smem ? radix_pass_1chunk(src, alt, count, shift, sm, dbg)
-                                   : radix_pass_chunked(src, alt, count, shift, sm, dbg);
-        if (moved) { uint64_t *tmp = src; src = alt; alt = tmp; }
+        if (tid == 0) { sm.dlo = 0xffffffffu; sm.dhi = 0u; }
+        __syncthreads();
+        uint32_t lo = 0xffffffffu, hi = 0u;
+        for (int j = tid; j < count; j += kGlobThreads) {
+            const uint32_t d = (uint32_t)(a.keys[start + j] >> 32);
+            lo = min(lo, d);
+            hi = max(hi, d);
+        }
+        lo = __reduce_min_sync(0xffffffffu, lo);
+        hi = __reduce_max_sync(0xffffffffu, hi);
+        if ((tid & 31) == 0) { atomicMin(&sm.dlo, lo); atomicMax(&sm.dhi, hi); }
+        __syncthreads();
+        const uint32_t diff = sm.dlo ^ sm.dhi;
+        uint64_t *src = a.keys + start, *alt = a.keys_alt + start;
+        for (int shift = 32; shift < 64; shift += 8) {
+            if ((diff >> (shift - 32)) == 0u) break;
+            if (radix_pass_chunked(src, alt, count, shift, sm, dbg)) { uint64_t *tmp = src; src = alt; alt = tmp; }
+            __syncthreads();
+        }
+        order_ties(src, count);
+        for (int j = tid; j < count; j += kGlobThreads) a.packed[start + j] = pack_record(a, (uint32_t)src[j]);
         __syncthreads();
     }
-    order_ties(src, count);
-    // pack: gather the splat records in sorted order
-    for (int j = tid; j < count; j += kSortThreads) {
-        const uint64_t key = src[j];
-        const uint32_t g = (uint32_t)key;
-        SplatRec r;
-        if (g >= (uint32_t)a.n) {
-            r.a = make_float4(0.f, 0.f, 0.f, __int_as_float(0));
-            r.b = make_float4(0.f, 0.f, 0.f, 0.f);
-            r.c = make_float4(0.f, 0.f, 0.f, 0.f);
-        } else {
-            r = a.rec[g];
-            const bool ok = finite_bits(r.a.x) && finite_bits(r.a.y) && finite_bits(r.a.z) && finite_bits(r.b.x) &&
-                            finite_bits(r.b.y) && finite_bits(r.b.z) && finite_bits(r.c.x) && finite_bits(r.c.y) &&
-                            finite_bits(r.c.z);
-            if (!ok) {
-                if (a.nan_counts) {
-                    atomicAdd(a.nan_counts + kNanPack, 1u);
-                    if (!finite_bits(r.a.z)) atomicAdd(a.nan_counts + kNanPackOpacity, 1u);
-                }
-                r.a = make_float4(0.f, 0.f, 0.f, 0.f);
-                r.b = make_float4(0.f, 0.f, 0.f, 0.f);
-                r.c = make_float4(0.f, 0.f, 0.f, 0.f);
-            }
-            r.a.w = __int_as_float((int)g);
-        }
-        a.packed[start + j] = r;
-    }
 }
 
-size_t sort_pack_smem_bytes() {
-    return ((sizeof(SortSmem) + 15) & ~size_t(15)) + 2 * kSortSmemKeys * sizeof(uint64_t);
-}
+size_t sort_pack_smem_bytes() { return pair_smem_bytes<1024>(); }
 
-void launch_tiles(const TileArgs &a, cudaStream_t s) {
+int launch_tiles(const TileArgs &a, int num_sms, cudaStream_t s) {
     static bool attr_set = false;
-    const size_t smem = sort_pack_smem_bytes();
     if (!attr_set) {
-        cudaFuncSetAttribute(k_sort_pack, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_sort_pack_smem<512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)pair_smem_bytes<512>());
+        cudaFuncSetAttribute(k_sort_pack_smem<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)pair_smem_bytes<1024>());
         cudaFuncSetAttribute(k_count_agg, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
         cudaFuncSetAttribute(k_scatter_agg, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
         attr_set = true;
     }
-    const bool agg = a.num_tiles <= kAggMaxTiles;
+    int launches = 0;
+    const bool agg = a.num_tiles <= kAggMaxTiles && a.cta_bins != nullptr;
     const int agg_blocks = (a.n + kAggPerCta - 1) / kAggPerCta;
     const size_t agg_smem = (size_t)a.num_tiles * sizeof(uint32_t);
-    if (a.n > 0) {
-        if (agg) k_count_agg<<<agg_blocks, 256, agg_smem, s>>>(a);
-        else k_count<<<(a.n + 255) / 256, 256, 0, s>>>(a);
+    if (a.n > 0 && agg) {
+        k_count_agg<<<agg_blocks, kAggThreads, agg_smem, s>>>(a);
+        debug_sync(s, "count");
+        k_cta_scan<<<(a.num_tiles + 255) / 256, 256, 0, s>>>(a, agg_blocks);
+        debug_sync(s, "cta_scan");
+        launches += 2;
+    } else if (a.n > 0) {
+        k_count<<<(a.n + 255) / 256, 256, 0, s>>>(a);
+        debug_sync(s, "count");
+        launches += 1;
     }
-    debug_sync(s, "count");
     k_scan<<<1, 1024, 0, s>>>(a);
     debug_sync(s, "scan");
+    launches += 1;
     if (a.n > 0) {
-        if (agg) k_scatter_agg<<<agg_blocks, 256, agg_smem, s>>>(a);
+        if (agg) k_scatter_agg<<<agg_blocks, kAggThreads, agg_smem, s>>>(a);
         else k_scatter<<<(a.n + 255) / 256, 256, 0, s>>>(a);
+        debug_sync(s, "scatter");
+        launches += 1;
     }
-    debug_sync(s, "scatter");
-    k_sort_pack<<<a.num_tiles, kSortThreads, smem, s>>>(a);
-    debug_sync(s, "sort_pack");
+    // persistent sort grids, one per class; idle classes exit at once
+    k_sort_pack_smem<512><<<2 * num_sms, 512, pair_smem_bytes<512>(), s>>>(a, 0);
+    debug_sync(s, "sort_pack_512");
+    k_sort_pack_smem<1024><<<num_sms, 1024, pair_smem_bytes<1024>(), s>>>(a, 1);
+    debug_sync(s, "sort_pack_1024");
+    k_sort_pack_global<<<num_sms, kGlobThreads, 0, s>>>(a, 2);
+    debug_sync(s, "sort_pack_global");
+    return launches + 3;
 }
 
 }  // namespace msplat
