@@ -45,10 +45,10 @@ VIEWS = 8
 # stage, SH degree 3: what the stage must read and write at minimum.
 STAGE_BYTES = {
     "project": dict(g=284),                      # params 232 B in, projection 52 B out
-    "tiles": dict(g=52, i=92),                   # count/scatter; key 16 + pack 76 per intersection
-    "raster_fwd": dict(i=36, p=20),
+    "tiles": dict(g=52, i=20),                   # count/scatter; key write 8, key read 8, id write 4 per intersection
+    "raster_fwd": dict(i=40, p=20),              # id 4 + record gather 36 per intersection
     "loss": dict(p=27),
-    "raster_bwd": dict(i=76, p=20),              # packed read 40 + gradient read-modify-write 36
+    "raster_bwd": dict(i=80, p=20),              # id 4 + record gather 40 + gradient read-modify-write 36
     "project_bwd": dict(g=1284),                 # incl. SH Adam on 48 coefficients
     "adam": dict(g=368),                         # 4 groups (308) + regularizer (60)
     "sgld": dict(g=80),

@@ -127,7 +127,7 @@ int msplat_engine_stats(MsplatEngine *e, MsplatEngineStats *out);
 int msplat_engine_set_timing(MsplatEngine *e, int enabled);
 
 /* Named intermediate buffers ("rec", "depths", "radii", "aabb", "tiles_hit",
- * "tile_counts", "tile_offsets", "packed", "out_img", "final_T",
+ * "tile_counts", "tile_offsets", "isect_ids", "out_img", "final_T",
  * "final_idx", "v_img", "grad", "v_mean", "v_scale", "v_quat", ...):
  * returns the size in bytes and the device pointer (or -1). */
 long long msplat_engine_buffer(MsplatEngine *e, const char *name, void **dev_ptr);

@@ -128,6 +128,23 @@ __device__ __forceinline__ bool ms_guard(bool ok, unsigned code, long long idx, 
 #endif
 constexpr int kDbgSlot = 16;   // nan_counts[16..18]: checked-build violation record
 
+// Splat record behind intersection slot idx.  Tile lists hold Gaussian ids;
+// an id past n (the slots of a tile that overflowed the buffer) reads as a
+// transparent record.  The id rides in a.w.
+__device__ __forceinline__ SplatRec isect_record(const uint32_t *ids, const SplatRec *rec, int n, int idx) {
+    const uint32_t g = ids[idx];
+    SplatRec r;
+    if (g < (uint32_t)n) {
+        r = rec[g];
+        r.a.w = __int_as_float((int)g);
+    } else {
+        r.a = make_float4(0.f, 0.f, 0.f, __int_as_float(0));
+        r.b = make_float4(0.f, 0.f, 0.f, 0.f);
+        r.c = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    return r;
+}
+
 __device__ __forceinline__ void atomic_add_f4(float4 *addr, float4 v) {
     atomicAdd(addr, v);   // sm_90+: one vector reduction in L2
 }

@@ -112,7 +112,7 @@ class Engine {
         ta.tile_counts = ptr<uint32_t>("tile_counts"); ta.tile_write = ta.tile_counts + T;
         ta.tile_offsets = ptr<uint32_t>("tile_offsets"); ta.max_tile_count = ptr<uint32_t>("max_tile");
         ta.keys = ptr<uint64_t>("keys"); ta.keys_alt = ptr<uint64_t>("keys_alt");
-        ta.packed = ptr<SplatRec>("packed"); ta.nan_counts = pa.nan_counts;
+        ta.isect_ids = ptr<uint32_t>("isect_ids"); ta.nan_counts = pa.nan_counts;
         const size_t cb = tile_cta_bins_bytes(N, T);
         if (cb) alloc("cta_bins", cb);
         ta.cta_bins = cb ? ptr<uint32_t>("cta_bins") : nullptr;
@@ -122,7 +122,8 @@ class Engine {
 
         RasterArgs ra{};
         ra.width = W; ra.height = H; ra.tiles_x = tx; ra.num_tiles = T; ra.k_max = K; ra.capacity = cap;
-        ra.sp = pa.sp; ra.tile_offsets = ta.tile_offsets; ra.packed = ta.packed;
+        ra.sp = pa.sp; ra.tile_offsets = ta.tile_offsets; ra.isect_ids = ta.isect_ids;
+        ra.n = N; ra.rec = pa.rec;
         ra.out_img = ptr<float>("out_img"); ra.final_T = ptr<float>("final_T"); ra.final_idx = ptr<int>("final_idx");
         if (K > 1) {
             ra.chunk_T = ptr<float>("chunk_T"); ra.chunk_C = ptr<float>("chunk_C"); ra.chunk_idx = ptr<int>("chunk_idx");
@@ -340,7 +341,7 @@ class Engine {
         if (c <= cap_isect_) return;
         alloc("keys", (size_t)c * 8);
         alloc("keys_alt", (size_t)c * 8);
-        alloc("packed", (size_t)c * sizeof(SplatRec));
+        alloc("isect_ids", (size_t)c * 4);
         cap_isect_ = c;
     }
     void ensure_pixels(long long P) {

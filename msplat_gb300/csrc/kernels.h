@@ -24,20 +24,20 @@ struct ProjectArgs {
 
 struct TileArgs {
     int n, tiles_x, tiles_y, num_tiles;
-    long long capacity;     // intersection slots of keys / packed
+    long long capacity;     // intersection slots of keys / isect_ids
     const int *radii;
     const float *depths;
     const SplatRec *rec;
     const float2 *aabb;
     uint32_t *tile_counts;  // zeroed before the step
     uint32_t *tile_write;   // zeroed before the step
-    uint32_t *cta_bins;     // [ceil(n / 4096), T] per-CTA tile histograms (block-aggregated path)
+    uint32_t *cta_bins;     // [ceil(n / 2048), T] per-CTA tile histograms (block-aggregated path)
     uint32_t *tile_lists;   // [3, T] tiles of each sort class (written by the scan)
     uint32_t *tile_class;   // [6]: list lengths, then the sort kernels' work counters
     uint32_t *tile_offsets; // [T+1]
     uint32_t *max_tile_count;
     uint64_t *keys, *keys_alt;
-    SplatRec *packed;
+    uint32_t *isect_ids;    // per-tile sorted Gaussian ids (0xffffffff: transparent)
     unsigned *nan_counts;
 };
 
@@ -46,7 +46,9 @@ struct RasterArgs {
     long long capacity;
     const StepParams *sp;
     const uint32_t *tile_offsets;
-    const SplatRec *packed;
+    int n;                      // Gaussians (ids at or past n read as transparent)
+    const uint32_t *isect_ids;  // per-tile sorted Gaussian ids
+    const SplatRec *rec;        // projection records, gathered by id
     float *out_img, *final_T;
     int *final_idx;
     float *chunk_T, *chunk_C, *prefix_T, *after_C;

@@ -145,8 +145,12 @@ __global__ void __launch_bounds__(256) k_project_fwd(ProjectArgs a) {
     // intersection at pack time; same input, same bits)
     const float opac = 1.f / (1.f + det_expf(-a.opacities[i]));
 
+    // A non-finite opacity does not cull (the reference zeroes such a record
+    // when it packs each intersection, hybrid_sort_pack_kernel): store 0,
+    // which rasterizes the same way, and count the intersections.
+    const bool oko = finite_bits(opac);
     SplatRec rec;
-    rec.a = make_float4(cxp, cyp, opac, 0.f);
+    rec.a = make_float4(cxp, cyp, oko ? opac : 0.f, 0.f);
     rec.b = make_float4(ca, cb, cc, 0.f);
     rec.c = make_float4(col[0], col[1], col[2], 0.f);
     a.rec[i] = rec;
@@ -161,6 +165,10 @@ __global__ void __launch_bounds__(256) k_project_fwd(ProjectArgs a) {
     if (okc && okd && oka && okn && okr) {
         a.tiles_hit[i] = area;
         a.radii[i] = __float2int_rz(radius);
+        if (!oko && a.nan_counts && area > 0) {
+            atomicAdd(a.nan_counts + kNanPack, (unsigned)area);
+            atomicAdd(a.nan_counts + kNanPackOpacity, (unsigned)area);
+        }
     } else if (a.nan_counts) {
         atomicAdd(a.nan_counts + kNanProj, 1u);
         if (!okc) atomicAdd(a.nan_counts + kNanProjCenter, 1u);

@@ -59,14 +59,14 @@ struct PixelState {
 };
 
 // Processes splat indices [s, hi] back to front for the whole CTA.
-__device__ void backward_range(BwdSmem &sm, const SplatRec *pk, int s, int hi, PixelState &ps, GradRec *grad) {
+__device__ void backward_range(BwdSmem &sm, const RasterArgs &a, int s, int hi, PixelState &ps, GradRec *grad) {
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int wbin = __reduce_max_sync(0xffffffffu, ps.bin_final);
     for (int batch_end = hi; batch_end >= s; batch_end -= kBB) {
         __syncthreads();
         const int idx = batch_end - tid;
         if (idx >= s) {
-            const SplatRec r = pk[idx];
+            const SplatRec r = isect_record(a.isect_ids, a.rec, a.n, idx);
             sm.xyo[tid] = r.a;
             sm.con[tid] = r.b;
             sm.rgb[tid] = r.c;
@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(kTileThreads) k_raster_bwd(RasterArgs a) {
     ps.bin_final = inside ? a.final_idx[y * a.width + x] : -1;
     const int hi = min(e - 1, block_max(ps.bin_final, sm.wmax));
     if (hi < s) return;
-    backward_range(sm, a.packed, s, hi, ps, a.grad);
+    backward_range(sm, a, s, hi, ps, a.grad);
 }
 
 __global__ void __launch_bounds__(256) k_chunk_prefix_suffix(RasterArgs a) {
@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(kTileThreads) k_raster_bwd_chunked(RasterArgs 
     ps.bin_final = (bf >= cs) ? bf : -1;
     const int hi = min(ce - 1, block_max(ps.bin_final, sm.wmax));
     if (hi < cs) return;
-    backward_range(sm, a.packed, cs, hi, ps, a.grad);
+    backward_range(sm, a, cs, hi, ps, a.grad);
 }
 
 void launch_raster_bwd(const RasterArgs &a, cudaStream_t s) {

@@ -1,6 +1,7 @@
 // Front-to-back alpha compositing.  Monolithic: one CTA per 16x16 tile, one
 // thread per pixel, splats staged through shared memory in batches of 256
-// (coalesced 16-byte loads of the packed records); the CTA leaves as soon as
+// (each thread gathers one splat record by the id in the tile list); the
+// CTA leaves as soon as
 // every pixel has saturated.  Chunked: one CTA per (tile, 512-splat depth
 // chunk) with chunk-local transmittance, then a per-pixel merge.
 // Follows nd_rasterize_forward_kernel (msplat_metal.metal:499-618),
@@ -19,10 +20,10 @@ struct BatchSmem {
     float4 rgb[kTileThreads];   // clamped colour max(raw + 0.5, 0)
 };
 
-__device__ __forceinline__ void load_batch(BatchSmem &sm, const SplatRec *pk, int idx, int end) {
+__device__ __forceinline__ void load_batch(BatchSmem &sm, const RasterArgs &a, int idx, int end) {
     const int t = threadIdx.x;
     if (idx < end) {
-        const SplatRec r = pk[idx];
+        const SplatRec r = isect_record(a.isect_ids, a.rec, a.n, idx);
         sm.xyo[t] = r.a;
         sm.con[t] = r.b;
         sm.rgb[t] = make_float4(fmaxf(r.c.x + 0.5f, 0.f), fmaxf(r.c.y + 0.5f, 0.f), fmaxf(r.c.z + 0.5f, 0.f), 0.f);
@@ -31,14 +32,14 @@ __device__ __forceinline__ void load_batch(BatchSmem &sm, const SplatRec *pk, in
 
 // Walks [s, e) for this pixel; the whole CTA iterates together.
 // done: in/out per-thread flag; returns (T, C, last).
-__device__ __forceinline__ void composite_range(BatchSmem &sm, const SplatRec *pk, int s, int e, float px, float py,
+__device__ __forceinline__ void composite_range(BatchSmem &sm, const RasterArgs &a, int s, int e, float px, float py,
                                                 bool done, float &T, float3 &C, int &last, unsigned *nan_sigma) {
     T = 1.f;
     C = make_float3(0.f, 0.f, 0.f);
     last = s - 1;
     for (int b0 = s; b0 < e; b0 += kTileThreads) {
         if (__syncthreads_count(done) == kTileThreads) break;
-        load_batch(sm, pk, b0 + (int)threadIdx.x, e);
+        load_batch(sm, a, b0 + (int)threadIdx.x, e);
         __syncthreads();
         if (done) continue;
         const int nb = min(kTileThreads, e - b0);
@@ -84,7 +85,7 @@ __global__ void __launch_bounds__(kTileThreads) k_raster_fwd(RasterArgs a) {
     float T;
     float3 C;
     int last;
-    composite_range(sm, a.packed, s, e, (float)x, (float)y, !inside, T, C, last, nullptr);
+    composite_range(sm, a, s, e, (float)x, (float)y, !inside, T, C, last, nullptr);
     if (!inside) return;
     const int p = y * a.width + x;
     if (!MS_GUARD(p >= 0 && p < a.width * a.height, 6, p, a.nan_counts ? a.nan_counts + kDbgSlot : nullptr)) return;
@@ -117,7 +118,7 @@ __global__ void __launch_bounds__(kTileThreads) k_raster_fwd_chunked(RasterArgs 
     float T;
     float3 C;
     int last;
-    composite_range(sm, a.packed, cs, ce, (float)x, (float)y, !inside, T, C, last,
+    composite_range(sm, a, cs, ce, (float)x, (float)y, !inside, T, C, last,
                     a.nan_counts ? a.nan_counts + kNanRasterSigma : nullptr);
     if (!inside) return;
     a.chunk_T[o] = T;

@@ -118,8 +118,8 @@ __global__ void __launch_bounds__(256) k_scatter(TileArgs a) {
 // scatter CTA loads its row, adds the tile offsets, and hands out slots with
 // shared-memory atomics.  No global atomics, and each tile's bucket is
 // filled CTA by CTA.  Used while the histogram fits (kAggMaxTiles).
-constexpr int kAggPerCta = 4096;
-constexpr int kAggThreads = 1024;
+constexpr int kAggPerCta = 2048;
+constexpr int kAggThreads = 512;   // four CTAs per SM: 1M Gaussians fill one wave
 constexpr int kAggMaxTiles = 12288;
 
 __device__ __forceinline__ void agg_rect(const TileArgs &a, int i, int &x0, int &y0, int &x1, int &y1) {
@@ -146,27 +146,36 @@ __global__ void __launch_bounds__(kAggThreads) k_count_agg(TileArgs a) {
     for (int t = threadIdx.x; t < T; t += blockDim.x) row[t] = bins[t];
 }
 
-// One thread per tile: exclusive scan down the column of CTA rows; the
-// column total is the tile's count.
-__global__ void __launch_bounds__(256) k_cta_scan(TileArgs a, int ctas) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+// Exclusive scan down each tile's column of CTA rows; the column total is the
+// tile's count.  A CTA covers 32 tiles (one per lane, so each row access is a
+// 128-byte line) and splits the rows over its 32 warps: row sums, a scan of
+// the 32 partial sums per tile in shared memory, then the rows rewritten.
+__global__ void __launch_bounds__(1024) k_cta_scan(TileArgs a, int ctas) {
+    __shared__ uint32_t part[32][33];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int T = a.num_tiles;
-    if (t >= T) return;
-    uint32_t run = 0;
-    int c = 0;
-    for (; c + 4 <= ctas; c += 4) {
-        uint32_t v[4];
-#pragma unroll
-        for (int k = 0; k < 4; k++) v[k] = a.cta_bins[(size_t)(c + k) * T + t];
-#pragma unroll
-        for (int k = 0; k < 4; k++) { a.cta_bins[(size_t)(c + k) * T + t] = run; run += v[k]; }
+    const int t = blockIdx.x * 32 + lane;
+    const int per = (ctas + 31) / 32;
+    const int c0 = min(ctas, w * per), c1 = min(ctas, c0 + per);
+    uint32_t sum = 0;
+    if (t < T)
+        for (int c = c0; c < c1; c++) sum += a.cta_bins[(size_t)c * T + t];
+    part[w][lane] = sum;
+    __syncthreads();
+    uint32_t run = 0, total = 0;
+    for (int k = 0; k < 32; k++) {
+        const uint32_t v = part[k][lane];
+        if (k < w) run += v;
+        total += v;
     }
-    for (; c < ctas; c++) {
-        const uint32_t v = a.cta_bins[(size_t)c * T + t];
-        a.cta_bins[(size_t)c * T + t] = run;
-        run += v;
+    if (t < T) {
+        for (int c = c0; c < c1; c++) {
+            const uint32_t v = a.cta_bins[(size_t)c * T + t];
+            a.cta_bins[(size_t)c * T + t] = run;
+            run += v;
+        }
+        if (w == 0) a.tile_counts[t] = total;
     }
-    a.tile_counts[t] = run;
 }
 
 __global__ void __launch_bounds__(kAggThreads) k_scatter_agg(TileArgs a) {
@@ -206,52 +215,21 @@ size_t tile_cta_bins_bytes(int n, int num_tiles) {
 // to 4096 keys, a 1024-thread CTA tiles up to 8192; larger tiles sort their
 // 64-bit keys in global memory in chunks.  Each class runs as a persistent
 // grid that takes tiles from its list (built by k_scan) through an atomic
-// work counter.  The pack step gathers the 48-byte splat record of every key
-// in sorted order.
+// work counter.  The output is the sorted Gaussian ids; the rasterizers
+// gather each splat's record by id (the records of all Gaussians stay in L2
+// at 1M), instead of reading a 48-byte record per intersection written here.
 // ---------------------------------------------------------------------------
 
 __device__ __forceinline__ uint32_t digit_of(uint64_t key, int shift) { return (uint32_t)(key >> shift) & 255u; }
 
-// the record written for one sorted key (the id rides in a.w)
-__device__ __forceinline__ SplatRec pack_record(const TileArgs &a, uint32_t g) {
-    SplatRec r;
-    if (g >= (uint32_t)a.n) {
-        r.a = make_float4(0.f, 0.f, 0.f, __int_as_float(0));
-        r.b = make_float4(0.f, 0.f, 0.f, 0.f);
-        r.c = make_float4(0.f, 0.f, 0.f, 0.f);
-        return r;
-    }
-    r = a.rec[g];
-    const bool ok = finite_bits(r.a.x) && finite_bits(r.a.y) && finite_bits(r.a.z) && finite_bits(r.b.x) &&
-                    finite_bits(r.b.y) && finite_bits(r.b.z) && finite_bits(r.c.x) && finite_bits(r.c.y) &&
-                    finite_bits(r.c.z);
-    if (!ok) {
-        if (a.nan_counts) {
-            atomicAdd(a.nan_counts + kNanPack, 1u);
-            if (!finite_bits(r.a.z)) atomicAdd(a.nan_counts + kNanPackOpacity, 1u);
-        }
-        r.a = make_float4(0.f, 0.f, 0.f, 0.f);
-        r.b = make_float4(0.f, 0.f, 0.f, 0.f);
-        r.c = make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-    r.a.w = __int_as_float((int)g);
-    return r;
-}
-
 // A tile whose bucket does not fit the buffer is emitted transparent
-// (hybrid_sort_pack_kernel's region guard, msplat_metal.metal:2523-2535).
-// Returns true when it did so.
+// (hybrid_sort_pack_kernel's region guard, msplat_metal.metal:2523-2535): its
+// slots that exist get an id no Gaussian has.  Returns true when it did so.
 template <int THREADS> __device__ bool emit_if_overflow(const TileArgs &a, uint32_t start, int count) {
     if ((uint64_t)start + (uint64_t)count <= (uint64_t)a.capacity) return false;
     for (int j = threadIdx.x; j < count; j += THREADS) {
         const uint64_t d = (uint64_t)start + j;
-        if (d < (uint64_t)a.capacity) {
-            SplatRec z;
-            z.a = make_float4(0.f, 0.f, 0.f, __int_as_float(0));
-            z.b = make_float4(0.f, 0.f, 0.f, 0.f);
-            z.c = make_float4(0.f, 0.f, 0.f, 0.f);
-            a.packed[d] = z;
-        }
+        if (d < (uint64_t)a.capacity) a.isect_ids[d] = 0xffffffffu;
     }
     return true;
 }
@@ -306,7 +284,13 @@ __device__ bool pair_pass(PairSmem<THREADS> &sm, int b, int n, int shift, unsign
             kv[j] = valid ? sm.key[b][i] : 0u;
             iv[j] = valid ? sm.idx[b][i] : (uint16_t)0;
             const uint32_t d = valid ? ((kv[j] >> shift) & 255u) : 256u;
-            const uint32_t peers = __match_any_sync(0xffffffffu, d);
+            // lanes holding the same digit: eight ballots, one per digit bit
+            uint32_t peers = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+            for (int bit = 0; bit < 8; bit++) {
+                const uint32_t m = __ballot_sync(0xffffffffu, (d >> bit) & 1u);
+                peers &= ((d >> bit) & 1u) ? m : ~m;
+            }
             uint32_t old = 0;
             if (valid) old = sm.wcnt[wid][d];
             __syncwarp();
@@ -412,20 +396,7 @@ __global__ void __launch_bounds__(THREADS) k_sort_pack_smem(TileArgs a, int cls)
             }
         }
         __syncthreads();
-        // pack, two records in flight per thread
-        for (int j = tid; j < count; j += 2 * THREADS) {
-            const int j2 = j + THREADS;
-            const uint32_t g0 = sm.id[sm.idx[b][j]];
-            const uint32_t g1 = j2 < count ? sm.id[sm.idx[b][j2]] : 0u;
-            const SplatRec r0 = pack_record(a, g0);
-            if (j2 < count) {
-                const SplatRec r1 = pack_record(a, g1);
-                a.packed[start + j] = r0;
-                a.packed[start + j2] = r1;
-            } else {
-                a.packed[start + j] = r0;
-            }
-        }
+        for (int j = tid; j < count; j += THREADS) a.isect_ids[start + j] = sm.id[sm.idx[b][j]];
         __syncthreads();
     }
 }
@@ -564,7 +535,7 @@ __global__ void __launch_bounds__(kGlobThreads) k_sort_pack_global(TileArgs a, i
             __syncthreads();
         }
         order_ties(src, count);
-        for (int j = tid; j < count; j += kGlobThreads) a.packed[start + j] = pack_record(a, (uint32_t)src[j]);
+        for (int j = tid; j < count; j += kGlobThreads) a.isect_ids[start + j] = (uint32_t)src[j];
         __syncthreads();
     }
 }
@@ -589,7 +560,7 @@ int launch_tiles(const TileArgs &a, int num_sms, cudaStream_t s) {
     if (a.n > 0 && agg) {
         k_count_agg<<<agg_blocks, kAggThreads, agg_smem, s>>>(a);
         debug_sync(s, "count");
-        k_cta_scan<<<(a.num_tiles + 255) / 256, 256, 0, s>>>(a, agg_blocks);
+        k_cta_scan<<<(a.num_tiles + 31) / 32, 1024, 0, s>>>(a, agg_blocks);
         debug_sync(s, "cta_scan");
         launches += 2;
     } else if (a.n > 0) {

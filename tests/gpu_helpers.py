@@ -40,8 +40,7 @@ def engine_outputs(eng, n, W, H, with_grads=True):
     o["tile_offsets"] = offs
     M = int(offs[-1])
     o["num_isect"] = M
-    pk = eng.read("packed", np.float32, max(M, 1) * 12).reshape(-1, 12)[:M]
-    o["gaussian_ids"] = pk[:, 3].view(np.int32).copy()
+    o["gaussian_ids"] = eng.read("isect_ids", np.int32, max(M, 1))[:M].copy()
     o["out_img"] = eng.read("out_img", np.float32, P * 3).reshape(H, W, 3)
     o["final_Ts"] = eng.read("final_T", np.float32, P).reshape(H, W)
     o["final_idx"] = eng.read("final_idx", np.int32, P).reshape(H, W)
