@@ -11,48 +11,94 @@
 
 namespace msplat {
 
-// Element e of the concatenated groups [means 3N | scales 3N | quats 4N | opacity N].
+// Regularizer gradient of element j of group grp (1: log-scales, 3: opacity
+// logits) added to g (mcmc_reg_grad_kernel, msplat_metal.metal:3987-4026).
+__device__ __forceinline__ float reg_grad(const AdamArgs &a, const StepParams &sp, int grp, long long j, float pv,
+                                          float g, float invN_base) {
+    const long long gi = grp == 1 ? j / 3 : j;
+    float duty = 1.0f;
+    if (sp.invis_scale != 1.0f) {
+        const float *dv = a.dc_v + 3 * gi;
+        duty = (dv[0] + dv[1] + dv[2] == 0.0f) ? 1.0f : sp.invis_scale;
+    }
+    const float invN = duty * invN_base;
+    if (grp == 3) {
+        const float sig = 1.0f / (1.0f + det_expf(-pv));
+        return g + sp.op_reg * sig * (1.0f - sig) * invN;
+    }
+    return g + sp.sc_reg * det_expf(fminf(fmaxf(pv, -15.0f), 15.0f)) * (invN * (1.0f / 3.0f));
+}
+
+// Adam on one element; returns false (and leaves it) for a non-finite gradient.
+__device__ __forceinline__ bool adam_step(float &p, float &m, float &v, float g, float b1, float b2, float eps,
+                                          float st, float bc) {
+    if (!finite_bits(g)) return false;
+    const float mm = fmaf(b1, m, (1.0f - b1) * g);
+    const float vv = fmaf(b2, v, (1.0f - b2) * g * g);
+    p = p - st * mm / (sqrtf(vv) / bc + eps);
+    m = mm;
+    v = vv;
+    return true;
+}
+
+// The four groups (means 3N, log-scales 3N, quaternions 4N, opacity logits N)
+// in one launch.  Each group is walked in 16-byte steps (parameter, moments
+// and gradient loaded as float4, every load of a step issued before any
+// use); a group length that is not a multiple of 4 ends with scalar steps.
 __global__ void __launch_bounds__(256) k_adam(AdamArgs a) {
-    const long long n3 = 3LL * a.n, n4 = 4LL * a.n;
-    const long long total = n3 + n3 + n4 + a.n;
     const StepParams &sp = *a.sp;
     const float b1 = sp.beta1, b2 = sp.beta2, eps = sp.eps;
     const bool reg = sp.op_reg > 0.f || sp.sc_reg > 0.f;
     const float invN_base = 1.0f / (float)a.n;
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long nthreads = (long long)gridDim.x * blockDim.x;
     unsigned bad[4] = {0, 0, 0, 0};
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
-         e += (long long)gridDim.x * blockDim.x) {
-        int grp;
-        long long j;
+#pragma unroll 1
+    for (int grp = 0; grp < 4; grp++) {
         float *p, *m, *v;
-        float g;
-        if (e < n3) { grp = 0; j = e; p = a.means; m = a.m[0]; v = a.v[0]; g = a.g_mean[j]; }
-        else if (e < 2 * n3) { grp = 1; j = e - n3; p = a.scales; m = a.m[1]; v = a.v[1]; g = a.g_scale[j]; }
-        else if (e < 2 * n3 + n4) { grp = 2; j = e - 2 * n3; p = a.quats; m = a.m[2]; v = a.v[2]; g = a.g_quat[j]; }
-        else { grp = 3; j = e - 2 * n3 - n4; p = a.opacities; m = a.m[3]; v = a.v[3]; g = a.grad[j].a.z; }
-        const float pv = p[j];
-        if (reg && (grp == 1 || grp == 3)) {
-            const long long gi = grp == 1 ? j / 3 : j;
-            float duty = 1.0f;
-            if (sp.invis_scale != 1.0f) {
-                const float *dv = a.dc_v + 3 * gi;
-                duty = (dv[0] + dv[1] + dv[2] == 0.0f) ? 1.0f : sp.invis_scale;
-            }
-            const float invN = duty * invN_base;
-            if (grp == 3) {
-                const float sig = 1.0f / (1.0f + det_expf(-pv));
-                g += sp.op_reg * sig * (1.0f - sig) * invN;
-            } else {
-                g += sp.sc_reg * det_expf(fminf(fmaxf(pv, -15.0f), 15.0f)) * (invN * (1.0f / 3.0f));
-            }
-        }
-        if (!finite_bits(g)) { bad[grp]++; continue; }
+        const float *gsrc = nullptr;
+        long long len;
+        if (grp == 0) { p = a.means; m = a.m[0]; v = a.v[0]; gsrc = a.g_mean; len = 3LL * a.n; }
+        else if (grp == 1) { p = a.scales; m = a.m[1]; v = a.v[1]; gsrc = a.g_scale; len = 3LL * a.n; }
+        else if (grp == 2) { p = a.quats; m = a.m[2]; v = a.v[2]; gsrc = a.g_quat; len = 4LL * a.n; }
+        else { p = a.opacities; m = a.m[3]; v = a.v[3]; len = a.n; }
         const int sg = grp == 3 ? 5 : grp;
-        const float mm = fmaf(b1, m[j], (1.0f - b1) * g);
-        const float vv = fmaf(b2, v[j], (1.0f - b2) * g * g);
-        p[j] = pv - sp.step_size[sg] * mm / (sqrtf(vv) / sp.bc2_sqrt[sg] + eps);
-        m[j] = mm;
-        v[j] = vv;
+        const float st = sp.step_size[sg], bc = sp.bc2_sqrt[sg];
+        const bool greg = reg && (grp == 1 || grp == 3);
+        // float4 steps need 16-byte aligned arrays (caller-owned parameters may not be)
+        const uintptr_t al = (uintptr_t)p | (uintptr_t)m | (uintptr_t)v | (uintptr_t)gsrc;
+        const long long n4 = (al & 15u) ? 0 : len / 4;
+        for (long long q = tid; q < n4; q += nthreads) {
+            float4 P = reinterpret_cast<const float4 *>(p)[q];
+            float4 M = reinterpret_cast<const float4 *>(m)[q];
+            float4 V = reinterpret_cast<const float4 *>(v)[q];
+            float4 G;
+            if (grp == 3) {
+                const long long j = 4 * q;
+                G = make_float4(a.grad[j].a.z, a.grad[j + 1].a.z, a.grad[j + 2].a.z, a.grad[j + 3].a.z);
+            } else {
+                G = reinterpret_cast<const float4 *>(gsrc)[q];
+            }
+            float *pp = &P.x, *mm = &M.x, *vv = &V.x, *gg = &G.x;
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                float g = gg[k];
+                if (greg) g = reg_grad(a, sp, grp, 4 * q + k, pp[k], g, invN_base);
+                if (!adam_step(pp[k], mm[k], vv[k], g, b1, b2, eps, st, bc)) bad[grp]++;
+            }
+            reinterpret_cast<float4 *>(p)[q] = P;
+            reinterpret_cast<float4 *>(m)[q] = M;
+            reinterpret_cast<float4 *>(v)[q] = V;
+        }
+        for (long long j = 4 * n4 + tid; j < len; j += nthreads) {
+            float pv = p[j], mv = m[j], vv = v[j];
+            float g = grp == 3 ? a.grad[j].a.z : gsrc[j];
+            if (greg) g = reg_grad(a, sp, grp, j, pv, g, invN_base);
+            if (!adam_step(pv, mv, vv, g, b1, b2, eps, st, bc)) { bad[grp]++; continue; }
+            p[j] = pv;
+            m[j] = mv;
+            v[j] = vv;
+        }
     }
     if (a.nan_counts) {
         if (bad[0]) atomicAdd(a.nan_counts + kNanMean, bad[0]);

@@ -253,38 +253,55 @@ __global__ void __launch_bounds__(256) k_project_bwd(ProjectBwdArgs a) {
         }
     }
     if (a.rest_bases == 0) return;
-    {   // features_rest: 3 * rest_bases floats per Gaussian
+    {   // features_rest: 3 * rest_bases floats per Gaussian; kRestUnroll
+        // 16-byte steps per lane are loaded before any is updated, so a warp
+        // keeps 3 * kRestUnroll loads in flight
+        constexpr int kRestUnroll = 3;
         const int rowf = 3 * a.rest_bases, total = rowf * ng;
         float *p = a.features_rest + (size_t)rowf * i0, *mm = a.rest_m + (size_t)rowf * i0,
               *vv = a.rest_v + (size_t)rowf * i0;
         const float st = sp.step_size[4], bc = sp.bc2_sqrt[4];
-        for (int e0 = lane * 4; e0 < total; e0 += 128) {
-            float g[4];
-            unsigned act = 0;
+        for (int base = lane * 4; base < total; base += 128 * kRestUnroll) {
+            float4 P[kRestUnroll], Mv[kRestUnroll], Vv[kRestUnroll];
 #pragma unroll
-            for (int k = 0; k < 4; k++) {
-                const int e = e0 + k;
-                g[k] = 0.f;
-                if (e < total) {
-                    const int gi = e / rowf, r = e - rowf * gi, band = r / 3, c = r - 3 * band;
-                    const float4 vc = sh.vc[gi];
-                    if (band < __float_as_int(vc.w) - 1) {
-                        g[k] = sh.bas[gi][band] * (c == 0 ? vc.x : c == 1 ? vc.y : vc.z);
-                        act |= 1u << k;
-                    }
+            for (int u = 0; u < kRestUnroll; u++) {
+                const int e0 = base + 128 * u;
+                if (e0 + 4 <= total) {
+                    P[u] = *reinterpret_cast<const float4 *>(p + e0);
+                    Mv[u] = *reinterpret_cast<const float4 *>(mm + e0);
+                    Vv[u] = *reinterpret_cast<const float4 *>(vv + e0);
                 }
             }
-            if (!act) continue;
-            if (e0 + 4 <= total) {
-                float4 P = *reinterpret_cast<float4 *>(p + e0), Mv = *reinterpret_cast<float4 *>(mm + e0),
-                       Vv = *reinterpret_cast<float4 *>(vv + e0);
-                adam4(P, Mv, Vv, g, act, st, bc, b1, b2, eps);
-                *reinterpret_cast<float4 *>(p + e0) = P;
-                *reinterpret_cast<float4 *>(mm + e0) = Mv;
-                *reinterpret_cast<float4 *>(vv + e0) = Vv;
-            } else {
-                for (int k = 0; k < 4 && e0 + k < total; k++)
-                    if (act & (1u << k)) adam_el(p + e0 + k, mm + e0 + k, vv + e0 + k, g[k], st, bc, b1, b2, eps);
+#pragma unroll
+            for (int u = 0; u < kRestUnroll; u++) {
+                const int e0 = base + 128 * u;
+                if (e0 >= total) break;
+                float g[4];
+                unsigned act = 0;
+                int gi = e0 / rowf, r = e0 - rowf * gi;
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    g[k] = 0.f;
+                    if (e0 + k < total) {
+                        const int band = r / 3, c = r - 3 * band;
+                        const float4 vc = sh.vc[gi];
+                        if (band < __float_as_int(vc.w) - 1) {
+                            g[k] = sh.bas[gi][band] * (c == 0 ? vc.x : c == 1 ? vc.y : vc.z);
+                            act |= 1u << k;
+                        }
+                    }
+                    if (++r == rowf) { r = 0; gi++; }
+                }
+                if (!act) continue;
+                if (e0 + 4 <= total) {
+                    adam4(P[u], Mv[u], Vv[u], g, act, st, bc, b1, b2, eps);
+                    *reinterpret_cast<float4 *>(p + e0) = P[u];
+                    *reinterpret_cast<float4 *>(mm + e0) = Mv[u];
+                    *reinterpret_cast<float4 *>(vv + e0) = Vv[u];
+                } else {
+                    for (int k = 0; k < 4 && e0 + k < total; k++)
+                        if (act & (1u << k)) adam_el(p + e0 + k, mm + e0 + k, vv + e0 + k, g[k], st, bc, b1, b2, eps);
+                }
             }
         }
     }
