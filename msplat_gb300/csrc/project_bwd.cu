@@ -48,7 +48,11 @@ __device__ __forceinline__ void adam4(float4 &p, float4 &m, float4 &v, const flo
     }
 }
 
-__global__ void __launch_bounds__(256) k_project_bwd(ProjectBwdArgs a) {
+// kRowF: floats per features_rest row when known at compile time (45 for SH
+// degree 3), so the element -> (Gaussian, band, channel) arithmetic of the SH
+// Adam walk uses constant divisors; 0 reads it from the arguments.
+template <int kRowF>
+__global__ void __launch_bounds__(256, 4) k_project_bwd(ProjectBwdArgs a) {
     __shared__ ShStage stage[8];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -257,7 +261,7 @@ __global__ void __launch_bounds__(256) k_project_bwd(ProjectBwdArgs a) {
         // 16-byte steps per lane are loaded before any is updated, so a warp
         // keeps 3 * kRestUnroll loads in flight
         constexpr int kRestUnroll = 3;
-        const int rowf = 3 * a.rest_bases, total = rowf * ng;
+        const int rowf = kRowF > 0 ? kRowF : 3 * a.rest_bases, total = rowf * ng;
         float *p = a.features_rest + (size_t)rowf * i0, *mm = a.rest_m + (size_t)rowf * i0,
               *vv = a.rest_v + (size_t)rowf * i0;
         const float st = sp.step_size[4], bc = sp.bc2_sqrt[4];
@@ -309,7 +313,8 @@ __global__ void __launch_bounds__(256) k_project_bwd(ProjectBwdArgs a) {
 
 void launch_project_bwd(const ProjectBwdArgs &a, cudaStream_t s) {
     if (a.n <= 0) return;
-    k_project_bwd<<<(a.n + 255) / 256, 256, 0, s>>>(a);
+    if (a.rest_bases == 15) k_project_bwd<45><<<(a.n + 255) / 256, 256, 0, s>>>(a);
+    else k_project_bwd<0><<<(a.n + 255) / 256, 256, 0, s>>>(a);
 }
 
 }  // namespace msplat

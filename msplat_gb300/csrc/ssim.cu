@@ -57,6 +57,7 @@ __global__ void __launch_bounds__(256) k_ssim_h(LossArgs a) {
 
 __global__ void __launch_bounds__(256) k_ssim_fields(LossArgs a) {
     __shared__ float hp[5][kSpan][kSpan];
+    __shared__ float mv[5][kS][kSpan];   // vertical moments at the window centres
     __shared__ float fl[3][kS][kSpan];
     __shared__ float red[8];
     const int W = a.width, H = a.height;
@@ -77,16 +78,28 @@ __global__ void __launch_bounds__(256) k_ssim_fields(LossArgs a) {
             for (int f = 0; f < 5; f++) hp[f][sy][sx] = in ? a.hbuf[(c * 5 + f) * P + p] : 0.f;
         }
         __syncthreads();
+        // vertical 11-tap pass, one (moment, column) per thread: the 26 inputs
+        // of the column are read once into registers for all 16 outputs
+        if (tid < 5 * kSpan) {
+            const int f = tid / kSpan, fx = tid % kSpan;
+            float col[kSpan];
+#pragma unroll
+            for (int r = 0; r < kSpan; r++) col[r] = hp[f][r][fx];
+#pragma unroll
+            for (int fy = 0; fy < kS; fy++) {
+                float acc = 0.f;
+#pragma unroll
+                for (int k = 0; k < 11; k++) acc += kGauss[k] * col[fy + k];
+                mv[f][fy][fx] = acc;
+            }
+        }
+        __syncthreads();
         for (int i = tid; i < kS * kSpan; i += 256) {
             const int fy = i / kSpan, fx = i % kSpan;     // field row (output rows), column incl. halo
             const int gx = bx + fx, gy = blockIdx.y * kS + fy;
-            float m[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+            float m[5];
 #pragma unroll
-            for (int k = 0; k < 11; k++) {
-                const float w = kGauss[k];
-#pragma unroll
-                for (int f = 0; f < 5; f++) m[f] += w * hp[f][fy + k][fx];
-            }
+            for (int f = 0; f < 5; f++) m[f] = mv[f][fy][fx];
             float mval = 1.f;
             const bool in_img = gx >= 0 && gx < W && gy < H;
             if (sp.has_mask && in_img && a.mask[(size_t)gy * W + gx] < 128) mval = 0.f;
