@@ -254,13 +254,15 @@ def run_engine(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         return float(t.item())
 
+    # the step runs as a captured CUDA graph: the first step of this shape
+    # runs eagerly, the second is captured, later ones replay it
+    eng.set_graphs(True)
     for k in range(args.warmup):
         one(k, False)
     eng.synchronize()
 
     # kernel-only: targets resident in HBM
     launches0 = eng.stats().launches
-    eng.set_timing(True)
     with Clocks(local) as clk:
         barrier()
         torch.cuda.synchronize()
@@ -272,9 +274,7 @@ def run_engine(args):
         dev_ms = eng.marker_elapsed()
         eng.synchronize()
         barrier()
-    st = eng.stats()
-    eng.set_timing(False)
-    launches = st.launches - launches0
+    launches = eng.stats().launches - launches0
     dev_ms = max_over_ranks(dev_ms)
     ms_step = dev_ms / args.steps
     value = ws * args.steps / (dev_ms / 1e3)
@@ -289,6 +289,15 @@ def run_engine(args):
     e2e_s = max_over_ranks(time.perf_counter() - t0)
     e2e = {"value": ws * args.steps / e2e_s, "unit": "iters/s",
            "h2d_bytes_per_step": int(gts_host[0].numel()), "d2h_bytes_per_step": 4}
+
+    # per-stage times: CUDA events between the stages of eager steps (events
+    # inside a step need it launched kernel by kernel)
+    eng.set_timing(True)
+    for k in range(min(args.steps, 20)):
+        one(args.warmup + 2 * args.steps + k, False)
+    eng.synchronize()
+    st = eng.stats()
+    eng.set_timing(False)
 
     # roofline of the dominant stage (CUDA events on the engine's stream)
     stage_ms = {name: st.stage_ms[i] / max(1, st.timed_steps) for i, name in enumerate(E.N.STAGES)}
@@ -313,6 +322,7 @@ def run_engine(args):
            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_dict(args),
            "roofline": roofline, "stage_ms": stage_ms, "num_intersections": int(st.num_intersections),
            "max_tile_count": int(st.max_tile_count), "gpu_launches": int(launches), "e2e": e2e,
+           "cuda_graph": True,
            "clocks": clk.summary()}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         cd = cams[0]

@@ -152,6 +152,14 @@ typedef struct {
 int msplat_engine_mcmc(MsplatEngine *e, const MsplatGaussians *g, const MsplatAdamState *st, int cap_max,
                        float cull_radius, int *relocation_count, MsplatMcmcStats *out);
 
+/* CUDA graph mode (off by default).  When on, the second training step with
+ * the same shapes, flags and buffers (parameters, moments, target, mask) is
+ * captured into a CUDA graph and later such steps replay it with one launch;
+ * the step scalars are uploaded before each replay, outside the graph.
+ * Per-stage timing and MSPLAT_SYNC_CHECK run steps eagerly.  Growing any
+ * engine buffer drops the captured graphs. */
+int msplat_engine_set_graphs(MsplatEngine *e, int enabled);
+
 /* Two CUDA events on the engine's stream for timing a span of steps:
  * marker(0) before, marker(1) after, then marker_elapsed waits for the second
  * and returns the device time between them in ms. */

@@ -87,6 +87,7 @@ def lib(build_if_missing: bool = True):
         L.msplat_engine_mcmc.argtypes = [vp, C.POINTER(MsplatGaussians), C.POINTER(MsplatAdamState), C.c_int,
                                          C.c_float, C.POINTER(C.c_int), C.POINTER(MsplatMcmcStats)]
         L.msplat_engine_marker.argtypes = [vp, C.c_int]
+        L.msplat_engine_set_graphs.argtypes = [vp, C.c_int]
         L.msplat_engine_marker_elapsed.argtypes = [vp, FP]
         L.msplat_engine_stream.argtypes = [vp]
         L.msplat_engine_stream.restype = vp

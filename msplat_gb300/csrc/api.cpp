@@ -388,6 +388,7 @@ struct TrainerImpl {
         CKA(cudaGetDevice(&dev));
         eng = msplat_engine_create(dev, std::max(1, cfg.capMax));
         if (!eng) throw std::runtime_error("engine creation failed");
+        msplat_engine_set_graphs(eng, 1);   // a camera's repeated steps replay one graph
         init_from_points();
         cam_order.resize(ds->train.size());
         std::iota(cam_order.begin(), cam_order.end(), 0);

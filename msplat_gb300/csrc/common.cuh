@@ -51,6 +51,11 @@ struct StepParams {
     float noise_lr, xyz_lr, max_disp;
     int has_mask;
     int pad_[3];
+    // target image and mask of this step (device; the mask may be null): read
+    // from here, not from kernel arguments, so one captured step serves every
+    // view of the same size
+    const uint8_t *gt;
+    const uint8_t *mask;
 };
 
 // Telemetry slots of the non-finite counters (same numbering as the

@@ -7,6 +7,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <set>
 #include <stdexcept>
 #include <string>
 
@@ -51,6 +52,7 @@ class Engine {
     ~Engine() {
         cudaSetDevice(device_);
         cudaStreamSynchronize(stream_);
+        clear_graphs();
         for (auto &kv : bufs_) cudaFree(kv.second.ptr);
         for (auto &row : ev_)
             for (auto &ev : row) cudaEventDestroy(ev);
@@ -80,14 +82,28 @@ class Engine {
         // kernels of this step: projection, count/scan/scatter/sort, raster
         // (+ merge when chunked), and for training 3 loss passes, raster
         // backward (+ prefix/suffix), projection backward, Adam, SGLD
-        launches_ += 1 + (K > 1 ? 2 : 1);   // + the tile-mapping launches, counted below
-        if (gt) launches_ += 3;
-        if (gt && backward) launches_ += (K > 1 ? 2 : 1) + 1 + (args.do_optimizer && st ? 1 : 0) + (args.do_sgld ? 1 : 0);
 
         StepParams sp;
         fill_params(args, sp, mask != nullptr);
-        // pageable source: the copy has consumed it when the call returns
+        sp.gt = gt;
+        sp.mask = mask;
+        // pageable source: the copy has consumed it when the call returns.
+        // It stays outside any captured graph: kernels read the scalars
+        // through this device block, so a replay sees this step's values.
         CK(cudaMemcpyAsync(ptr<StepParams>("params"), &sp, sizeof(sp), cudaMemcpyHostToDevice, stream_));
+        // every buffer the step touches exists now (sized above), so a capture
+        // below allocates nothing
+        const size_t cb = tile_cta_bins_bytes(N, T);
+        if (cb) alloc("cta_bins", cb);
+
+        auto issue = [&]() {
+        // kernels of this step: projection, the tile-mapping launches (counted
+        // where they are issued), raster (+ merge when chunked), and for
+        // training 3 loss passes, raster backward (+ prefix/suffix),
+        // projection backward, Adam, SGLD
+        launches_ += 1 + (K > 1 ? 2 : 1);
+        if (gt) launches_ += 3;
+        if (gt && backward) launches_ += (K > 1 ? 2 : 1) + 1 + (args.do_optimizer && st ? 1 : 0) + (args.do_sgld ? 1 : 0);
         CK(cudaMemsetAsync(ptr<uint32_t>("tile_counts"), 0, sizeof(uint32_t) * 2 * (size_t)T, stream_));
         CK(cudaMemsetAsync(ptr<float>("loss_sum"), 0, sizeof(float), stream_));
 
@@ -113,8 +129,6 @@ class Engine {
         ta.tile_offsets = ptr<uint32_t>("tile_offsets"); ta.max_tile_count = ptr<uint32_t>("max_tile");
         ta.keys = ptr<uint64_t>("keys"); ta.keys_alt = ptr<uint64_t>("keys_alt");
         ta.isect_ids = ptr<uint32_t>("isect_ids"); ta.nan_counts = pa.nan_counts;
-        const size_t cb = tile_cta_bins_bytes(N, T);
-        if (cb) alloc("cta_bins", cb);
         ta.cta_bins = cb ? ptr<uint32_t>("cta_bins") : nullptr;
         ta.tile_lists = ptr<uint32_t>("tile_lists"); ta.tile_class = ptr<uint32_t>("tile_class");
         launches_ += launch_tiles(ta, num_sms_, stream_);
@@ -136,7 +150,8 @@ class Engine {
         if (!gt) { mark(4); mark(5); mark(6); mark(7); mark(8); return; }
 
         LossArgs la{};
-        la.width = W; la.height = H; la.sp = pa.sp; la.img = ra.out_img; la.gt = gt; la.mask = mask;
+        la.width = W; la.height = H; la.sp = pa.sp; la.img = ra.out_img;
+        la.gt = nullptr; la.mask = nullptr;   // read from StepParams (see common.cuh)
         la.hbuf = ptr<float>("hbuf"); la.dbuf = ptr<float>("dbuf"); la.v_img = ptr<float>("v_img");
         la.loss_sum = ptr<float>("loss_sum"); la.nan_counts = pa.nan_counts;
         launch_loss(la, stream_);
@@ -181,6 +196,49 @@ class Engine {
         debug_sync(stream_, "sgld");
         mark(8);
         CK(cudaGetLastError());
+        };   // issue
+
+        // CUDA graph mode: the second step with the same shapes and buffers
+        // is captured, later ones replay it (one launch for the whole step)
+        const bool graphable = use_graphs_ && !timing_ && !g_sync_check;
+        if (graphable) {
+            GraphKey key{};
+            key.n = N; key.w = W; key.h = H; key.k = K; key.rest = g.rest_bases;
+            key.flags = (args.do_optimizer ? 1 : 0) | (args.do_sgld ? 2 : 0) | (backward ? 4 : 0) | (st ? 8 : 0) |
+                        (gt ? 16 : 0);   // the target and mask themselves come through StepParams
+            key.ptr[0] = g.means; key.ptr[1] = g.scales; key.ptr[2] = g.quats; key.ptr[3] = g.features_dc;
+            key.ptr[4] = g.features_rest; key.ptr[5] = g.opacities;
+            for (int k = 0; k < 6 && st; k++) { key.ptr[8 + k] = st->exp_avg[k]; key.ptr[14 + k] = st->exp_avg_sq[k]; }
+            const std::string ks(reinterpret_cast<const char *>(&key), sizeof(key));
+            auto it = graphs_.find(ks);
+            if (it != graphs_.end()) {
+                CK(cudaGraphLaunch(it->second.exec, stream_));
+                launches_ += it->second.launches;
+                return;
+            }
+            if (graph_seen_.count(ks) && graphs_.size() < kMaxGraphs) {
+                const long long l0 = launches_;
+                cudaGraph_t graph = nullptr;
+                CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+                try {
+                    issue();
+                } catch (...) {
+                    cudaStreamEndCapture(stream_, &graph);
+                    if (graph) cudaGraphDestroy(graph);
+                    throw;
+                }
+                CK(cudaStreamEndCapture(stream_, &graph));
+                cudaGraphExec_t exec = nullptr;
+                const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+                cudaGraphDestroy(graph);
+                CK(ie);
+                graphs_[ks] = GraphEntry{exec, launches_ - l0};
+                CK(cudaGraphLaunch(exec, stream_));
+                return;
+            }
+            graph_seen_.insert(ks);
+        }
+        issue();
     }
 
     // Copies host images into engine-owned device buffers on the engine's
@@ -302,7 +360,11 @@ class Engine {
     void alloc(const char *name, size_t bytes, bool zero = false) {
         Buf &b = bufs_[name];
         if (b.bytes >= bytes && b.ptr) return;
-        if (b.ptr) { CK(cudaStreamSynchronize(stream_)); CK(cudaFree(b.ptr)); }
+        if (b.ptr) {
+            CK(cudaStreamSynchronize(stream_));
+            CK(cudaFree(b.ptr));
+            clear_graphs();   // captured steps hold the old address
+        }
         b.ptr = nullptr;
         CK(cudaMalloc(&b.ptr, std::max<size_t>(bytes, 256)));
         b.bytes = bytes;
@@ -428,6 +490,31 @@ class Engine {
     cudaEvent_t marker_[2];
     int slot_ = 0;
     long long timed_steps_ = 0, launches_ = 0;
+
+    // captured steps, keyed by shapes, flags and every pointer they bake in
+    struct GraphKey {
+        int n, w, h, k, rest, flags;
+        const void *ptr[20];
+    };
+    struct GraphEntry {
+        cudaGraphExec_t exec;
+        long long launches;
+    };
+    static constexpr size_t kMaxGraphs = 512;
+    bool use_graphs_ = false;
+    std::map<std::string, GraphEntry> graphs_;
+    std::set<std::string> graph_seen_;
+
+  public:
+    void set_graphs(bool on) {
+        use_graphs_ = on;
+        if (!on) clear_graphs();
+    }
+    void clear_graphs() {
+        for (auto &kv : graphs_) cudaGraphExecDestroy(kv.second.exec);
+        graphs_.clear();
+        graph_seen_.clear();
+    }
 };
 
 }  // namespace msplat
@@ -529,6 +616,10 @@ int msplat_engine_mcmc(MsplatEngine *e, const MsplatGaussians *g, const MsplatAd
                        float cull_radius, int *relocation_count, MsplatMcmcStats *out) {
     if (!g || !st || !relocation_count || !out) return -1;
     return guarded(e, [&] { e->impl->mcmc(*g, *st, cap_max, cull_radius, *relocation_count, *out); });
+}
+
+int msplat_engine_set_graphs(MsplatEngine *e, int enabled) {
+    return guarded(e, [&] { e->impl->set_graphs(enabled != 0); });
 }
 
 int msplat_engine_marker(MsplatEngine *e, int which) {

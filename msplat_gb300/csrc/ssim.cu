@@ -18,8 +18,13 @@ __constant__ float kGauss[11];
 constexpr float kC1 = 0.0001f, kC2 = 0.0009f;
 constexpr int kS = 16, kHalo = 5, kSpan = kS + 2 * kHalo;   // 26
 
+// Target and mask: the arguments' when set, else this step's in StepParams.
+__device__ __forceinline__ const uint8_t *step_gt(const LossArgs &a) { return a.gt ? a.gt : a.sp->gt; }
+__device__ __forceinline__ const uint8_t *step_mask(const LossArgs &a) { return a.gt ? a.mask : a.sp->mask; }
+
 __global__ void __launch_bounds__(256) k_ssim_h(LossArgs a) {
     __shared__ float sg[3][kS][kSpan], sr[3][kS][kSpan];
+    const uint8_t *gt = step_gt(a);
     const int W = a.width, H = a.height;
     const int bx = blockIdx.x * kS - kHalo, by = blockIdx.y * kS;
     const int tid = threadIdx.x;
@@ -30,7 +35,7 @@ __global__ void __launch_bounds__(256) k_ssim_h(LossArgs a) {
         const size_t p = in ? ((size_t)gy * W + gx) : 0;
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-            sg[c][sy][sx] = in ? (float)a.gt[3 * p + c] * (1.0f / 255.0f) : 0.f;
+            sg[c][sy][sx] = in ? (float)gt[3 * p + c] * (1.0f / 255.0f) : 0.f;
             sr[c][sy][sx] = in ? a.img[3 * p + c] : 0.f;
         }
     }
@@ -65,6 +70,7 @@ __global__ void __launch_bounds__(256) k_ssim_fields(LossArgs a) {
     const int bx = blockIdx.x * kS - kHalo, by = blockIdx.y * kS - kHalo;
     const int tid = threadIdx.x, lx = tid & 15, ly = tid >> 4;
     const StepParams &sp = *a.sp;
+    const uint8_t *gt = step_gt(a), *mask = step_mask(a);
     const float sw = sp.ssim_weight;
     float ssim_acc = 0.f, l1_acc = 0.f;
     unsigned nwin = 0;
@@ -102,7 +108,7 @@ __global__ void __launch_bounds__(256) k_ssim_fields(LossArgs a) {
             for (int f = 0; f < 5; f++) m[f] = mv[f][fy][fx];
             float mval = 1.f;
             const bool in_img = gx >= 0 && gx < W && gy < H;
-            if (sp.has_mask && in_img && a.mask[(size_t)gy * W + gx] < 128) mval = 0.f;
+            if (sp.has_mask && in_img && mask[(size_t)gy * W + gx] < 128) mval = 0.f;
             if (!(finite_bits(m[0]) && finite_bits(m[1]) && finite_bits(m[2]) && finite_bits(m[3]) && finite_bits(m[4]))) {
                 fl[0][fy][fx] = fl[1][fy][fx] = fl[2][fy][fx] = 0.f;
                 nwin++;
@@ -122,7 +128,7 @@ __global__ void __launch_bounds__(256) k_ssim_fields(LossArgs a) {
             if (fx >= kHalo && fx < kHalo + kS && in_img) {
                 ssim_acc += mval * (A * B) / (Cd * D);
                 const size_t p = (size_t)gy * W + gx;
-                l1_acc += mval * fabsf((float)a.gt[3 * p + c] * (1.0f / 255.0f) - a.img[3 * p + c]);
+                l1_acc += mval * fabsf((float)gt[3 * p + c] * (1.0f / 255.0f) - a.img[3 * p + c]);
             }
         }
         __syncthreads();
@@ -178,10 +184,11 @@ __global__ void __launch_bounds__(256) k_ssim_bwd(LossArgs a) {
     const int x = bx + lx, y = blockIdx.y * kS + ly;
     if (x >= W || y >= H) return;
     const StepParams &sp = *a.sp;
+    const uint8_t *gt = step_gt(a), *mask = step_mask(a);
     const float sw = sp.ssim_weight, invn = sp.loss_inv_n;
     const size_t p = (size_t)y * W + x;
     float mc = 1.f;
-    if (sp.has_mask && a.mask[p] < 128) mc = 0.f;
+    if (sp.has_mask && mask[p] < 128) mc = 0.f;
     unsigned nbad = 0;
 #pragma unroll
     for (int c = 0; c < 3; c++) {
@@ -193,7 +200,7 @@ __global__ void __launch_bounds__(256) k_ssim_bwd(LossArgs a) {
             c2 += w * sh[c * 3 + 1][ly + d][lx];
             c3 += w * sh[c * 3 + 2][ly + d][lx];
         }
-        const float r = a.img[3 * p + c], g = (float)a.gt[3 * p + c] * (1.0f / 255.0f);
+        const float r = a.img[3 * p + c], g = (float)gt[3 * p + c] * (1.0f / 255.0f);
         const float vs = c1 + r * c2 + g * c3;
         const float vl = mc * ((g > r) ? -1.f : ((g < r) ? 1.f : 0.f));
         float v = invn * (-sw * vs + (1.f - sw) * vl);

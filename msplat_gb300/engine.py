@@ -192,6 +192,10 @@ class Engine:
     def set_timing(self, on: bool):
         self._check(self.L.msplat_engine_set_timing(self.h, int(on)))
 
+    def set_graphs(self, on: bool):
+        """Capture repeated steps into CUDA graphs and replay them."""
+        self._check(self.L.msplat_engine_set_graphs(self.h, int(on)))
+
     def buffer(self, name: str):
         p = C.c_void_p()
         n = self.L.msplat_engine_buffer(self.h, name.encode(), C.byref(p))
