@@ -132,7 +132,8 @@ int msplat_engine_set_timing(MsplatEngine *e, int enabled);
  * returns the size in bytes and the device pointer (or -1). */
 long long msplat_engine_buffer(MsplatEngine *e, const char *name, void **dev_ptr);
 
-/* Copies the first `bytes` of a named buffer to host memory; waits. */
+/* Copies the first `bytes` of a named buffer to host or device memory (any
+ * address CUDA can reach); waits. */
 int msplat_engine_read(MsplatEngine *e, const char *name, void *dst, long long bytes);
 
 /* MCMC relocation + growth (Model::mcmcAfterTrain, core/src/model.cpp:
@@ -151,6 +152,20 @@ typedef struct {
 
 int msplat_engine_mcmc(MsplatEngine *e, const MsplatGaussians *g, const MsplatAdamState *st, int cap_max,
                        float cull_radius, int *relocation_count, MsplatMcmcStats *out);
+
+/* Parameter gradients for a caller-supplied image gradient (the autograd
+ * binding's backward).  The forward of (g, args) is recomputed, then the
+ * rasterizer and projection backward passes run without any optimizer and
+ * write dL/d(parameter) for every Gaussian into the caller's device buffers
+ * (shapes of the parameters; zero for culled Gaussians and for SH bands
+ * above args->degrees_to_use).  v_img: device float [H,W,3].  Same VJPs as
+ * the training step (rasterize_backward_kernel, project_and_sh_backward_kernel). */
+typedef struct {
+    float *v_means, *v_scales, *v_quats, *v_features_dc, *v_features_rest, *v_opacities;
+} MsplatGradients;
+
+int msplat_engine_backward(MsplatEngine *e, const MsplatGaussians *g, const MsplatStepArgs *args, const float *v_img,
+                           const MsplatGradients *out);
 
 /* CUDA graph mode (off by default).  When on, the second training step with
  * the same shapes, flags and buffers (parameters, moments, target, mask) is

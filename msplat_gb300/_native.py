@@ -55,6 +55,11 @@ class MsplatMcmcStats(C.Structure):
                 ("num_relocated", C.c_int), ("num_grown", C.c_int), ("num_active", C.c_int)]
 
 
+class MsplatGradients(C.Structure):
+    _fields_ = [("v_means", C.c_void_p), ("v_scales", C.c_void_p), ("v_quats", C.c_void_p),
+                ("v_features_dc", C.c_void_p), ("v_features_rest", C.c_void_p), ("v_opacities", C.c_void_p)]
+
+
 def lib(build_if_missing: bool = True):
     global _lib
     with _lock:
@@ -88,6 +93,8 @@ def lib(build_if_missing: bool = True):
                                          C.c_float, C.POINTER(C.c_int), C.POINTER(MsplatMcmcStats)]
         L.msplat_engine_marker.argtypes = [vp, C.c_int]
         L.msplat_engine_set_graphs.argtypes = [vp, C.c_int]
+        L.msplat_engine_backward.argtypes = [vp, C.POINTER(MsplatGaussians), C.POINTER(MsplatStepArgs), vp,
+                                             C.POINTER(MsplatGradients)]
         L.msplat_engine_marker_elapsed.argtypes = [vp, FP]
         L.msplat_engine_stream.argtypes = [vp]
         L.msplat_engine_stream.restype = vp

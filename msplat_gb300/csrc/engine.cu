@@ -146,6 +146,7 @@ class Engine {
         ra.v_img = ptr<float>("v_img"); ra.grad = ptr<GradRec>("grad"); ra.nan_counts = pa.nan_counts;
         launch_raster_fwd(ra, stream_);
         debug_sync(stream_, "raster_fwd");
+        last_ra_ = ra;
         mark(3);
         if (!gt) { mark(4); mark(5); mark(6); mark(7); mark(8); return; }
 
@@ -256,6 +257,48 @@ class Engine {
             mask_d = ptr<uint8_t>("mask_stage");
         }
         train_step(g, st, args, ptr<uint8_t>("gt_stage"), mask_d, true);
+    }
+
+    // dL/d(parameters) for a caller-supplied dL/d(image): the forward is run
+    // again (projection, tile lists, raster) rather than kept from an
+    // earlier call, then the raster and projection backward passes write
+    // the gradients into the caller's buffers.  No optimizer step.
+    void backward_image(const MsplatGaussians &g, const MsplatStepArgs &args, const float *v_img,
+                        const MsplatGradients &out) {
+        if (!v_img) throw std::runtime_error("v_img is null");
+        if (!out.v_means || !out.v_scales || !out.v_quats || !out.v_opacities || !out.v_features_dc ||
+            (g.rest_bases > 0 && !out.v_features_rest))
+            throw std::runtime_error("null gradient pointer");
+        const bool graphs = use_graphs_;
+        use_graphs_ = false;   // the raster arguments of this forward are needed below
+        try {
+            train_step(g, nullptr, args, nullptr, nullptr, false);
+        } catch (...) {
+            use_graphs_ = graphs;
+            throw;
+        }
+        use_graphs_ = graphs;
+        const int N = g.num_points;
+        if (N <= 0) return;
+        CK(cudaMemsetAsync(ptr<GradRec>("grad"), 0, sizeof(GradRec) * (size_t)N, stream_));
+        RasterArgs ra = last_ra_;
+        ra.v_img = v_img;
+        ra.grad = ptr<GradRec>("grad");
+        launch_raster_bwd(ra, stream_);
+        debug_sync(stream_, "raster_bwd");
+        ProjectBwdArgs pb{};
+        pb.n = N; pb.rest_bases = g.rest_bases; pb.do_optimizer = 0;
+        pb.Wf = (float)args.width; pb.Hf = (float)args.height; pb.sp = ptr<StepParams>("params");
+        pb.means = g.means; pb.scales = g.scales; pb.quats = g.quats;
+        pb.radii = ptr<int>("radii"); pb.rec = ptr<SplatRec>("rec"); pb.grad = ra.grad;
+        pb.v_mean = out.v_means; pb.v_scale = out.v_scales; pb.v_quat = out.v_quats;
+        pb.features_dc = g.features_dc; pb.features_rest = g.features_rest;
+        pb.v_dc_out = out.v_features_dc; pb.v_rest_out = out.v_features_rest; pb.v_opac_out = out.v_opacities;
+        pb.nan_counts = ptr<unsigned>("nan_counts");
+        launch_project_bwd(pb, stream_);
+        debug_sync(stream_, "project_bwd");
+        launches_ += (last_K_ > 1 ? 2 : 1) + 1;
+        CK(cudaGetLastError());
     }
 
     void mcmc(const MsplatGaussians &g, const MsplatAdamState &st, int cap_max, float cull_radius,
@@ -490,6 +533,7 @@ class Engine {
     cudaEvent_t marker_[2];
     int slot_ = 0;
     long long timed_steps_ = 0, launches_ = 0;
+    RasterArgs last_ra_{};   // raster arguments of the last eagerly issued step
 
     // captured steps, keyed by shapes, flags and every pointer they bake in
     struct GraphKey {
@@ -607,8 +651,9 @@ int msplat_engine_read(MsplatEngine *e, const char *name, void *dst, long long b
         const long long have = e->impl->buffer(name, &p);
         if (have < 0) throw std::runtime_error(std::string("no buffer ") + name);
         if (bytes > have) throw std::runtime_error(std::string("read past the end of ") + name);
+        // on the engine's stream, host or device destination; done on return
+        CK(cudaMemcpyAsync(dst, p, (size_t)bytes, cudaMemcpyDefault, e->impl->stream()));
         e->impl->synchronize();
-        CK(cudaMemcpy(dst, p, (size_t)bytes, cudaMemcpyDeviceToHost));
     });
 }
 
@@ -616,6 +661,12 @@ int msplat_engine_mcmc(MsplatEngine *e, const MsplatGaussians *g, const MsplatAd
                        float cull_radius, int *relocation_count, MsplatMcmcStats *out) {
     if (!g || !st || !relocation_count || !out) return -1;
     return guarded(e, [&] { e->impl->mcmc(*g, *st, cap_max, cull_radius, *relocation_count, *out); });
+}
+
+int msplat_engine_backward(MsplatEngine *e, const MsplatGaussians *g, const MsplatStepArgs *args, const float *v_img,
+                           const MsplatGradients *out) {
+    if (!g || !args || !out) return -1;
+    return guarded(e, [&] { e->impl->backward_image(*g, *args, v_img, *out); });
 }
 
 int msplat_engine_set_graphs(MsplatEngine *e, int enabled) {

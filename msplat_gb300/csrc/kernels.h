@@ -80,6 +80,9 @@ struct ProjectBwdArgs {
     const GradRec *grad;
     float *v_mean, *v_scale, *v_quat;
     float *features_dc, *features_rest, *dc_m, *dc_v, *rest_m, *rest_v;
+    // gradient export (no optimizer): when set, the SH gradients and the
+    // opacity-logit gradient are written here instead of feeding Adam
+    float *v_dc_out, *v_rest_out, *v_opac_out;
     unsigned *nan_counts;
 };
 

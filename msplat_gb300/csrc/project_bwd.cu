@@ -59,8 +59,10 @@ __global__ void __launch_bounds__(256, 4) k_project_bwd(ProjectBwdArgs a) {
     ShStage &sh = stage[wid];
     const StepParams &sp = *a.sp;
     sh.vc[lane] = make_float4(0.f, 0.f, 0.f, 0.f);   // w = 0: nothing to update
+    const bool want_sh = a.do_optimizer || a.v_dc_out;
     if (i < a.n) {
         float *vmean = a.v_mean + 3 * (size_t)i, *vscale = a.v_scale + 3 * (size_t)i, *vquat = a.v_quat + 4 * (size_t)i;
+        if (a.v_opac_out) a.v_opac_out[i] = a.radii[i] > 0 ? a.grad[i].a.z : 0.f;
         if (a.radii[i] <= 0) {
             vmean[0] = vmean[1] = vmean[2] = 0.f;
             vscale[0] = vscale[1] = vscale[2] = 0.f;
@@ -185,8 +187,8 @@ __global__ void __launch_bounds__(256, 4) k_project_bwd(ProjectBwdArgs a) {
                           w * (gR[1][0] - gR[0][1]));
             *reinterpret_cast<float4 *>(vquat) = vq;
 
-            // SH VJP inputs for the fused Adam below
-            if (a.do_optimizer) {
+            // SH VJP inputs for the fused Adam (or the gradient export) below
+            if (want_sh) {
                 const float vc0 = gr.c.x, vc1 = gr.c.y, vc2 = gr.c.z;
                 if (!(finite_bits(vc0) && finite_bits(vc1) && finite_bits(vc2))) {
                     if (a.nan_counts) atomicAdd(a.nan_counts + kNanSH, 1u);
@@ -212,7 +214,7 @@ __global__ void __launch_bounds__(256, 4) k_project_bwd(ProjectBwdArgs a) {
             }
         }
     }
-    if (!a.do_optimizer) return;
+    if (!want_sh) return;
     __syncwarp();
     // fused SH Adam, warp-cooperative: the warp's 32 Gaussians own contiguous
     // rows of features_dc / features_rest and their moments, walked with
@@ -221,6 +223,24 @@ __global__ void __launch_bounds__(256, 4) k_project_bwd(ProjectBwdArgs a) {
     const int i0 = (blockIdx.x * blockDim.x) + wid * 32;
     if (i0 >= a.n) return;
     const int ng = min(32, a.n - i0);
+    if (a.v_dc_out) {
+        // export: dL/d(SH coefficient) = basis value x colour gradient, zero
+        // where Adam would not update (culled, non-finite, band not in use)
+        for (int e = lane; e < 3 * ng; e += 32) {
+            const int gi = e / 3, c = e - 3 * gi;
+            const float4 vc = sh.vc[gi];
+            a.v_dc_out[3 * (size_t)i0 + e] =
+                __float_as_int(vc.w) > 0 ? sh.bas[gi][15] * (c == 0 ? vc.x : c == 1 ? vc.y : vc.z) : 0.f;
+        }
+        const int rowf = 3 * a.rest_bases;
+        for (int e = lane; e < rowf * ng; e += 32) {
+            const int gi = e / rowf, r = e - rowf * gi, band = r / 3, c = r - 3 * band;
+            const float4 vc = sh.vc[gi];
+            a.v_rest_out[(size_t)rowf * i0 + e] =
+                band < __float_as_int(vc.w) - 1 ? sh.bas[gi][band] * (c == 0 ? vc.x : c == 1 ? vc.y : vc.z) : 0.f;
+        }
+        return;
+    }
     const float b1 = sp.beta1, b2 = sp.beta2, eps = sp.eps;
     {   // features_dc: 3 floats per Gaussian
         const int total = 3 * ng;

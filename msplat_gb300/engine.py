@@ -166,6 +166,14 @@ class Engine:
         g, _ = dg.native()
         self._check(self.L.msplat_engine_render(self.h, C.byref(g), C.byref(args)))
 
+    def backward(self, g: N.MsplatGaussians, args: N.MsplatStepArgs, v_img_ptr: int, grads: N.MsplatGradients):
+        """dL/d(parameters) for dL/d(image) at v_img_ptr (device float [H,W,3]); the
+        forward of (g, args) is recomputed.  Gradients go to the pointers in grads."""
+        self._check(self.L.msplat_engine_backward(self.h, C.byref(g), C.byref(args), v_img_ptr, C.byref(grads)))
+
+    def render_raw(self, g: N.MsplatGaussians, args: N.MsplatStepArgs):
+        self._check(self.L.msplat_engine_render(self.h, C.byref(g), C.byref(args)))
+
     def mcmc(self, dg: DeviceGaussians, cull_radius: float, relocation_count: int):
         """One relocation + growth round on the device; returns (stats, new relocation_count)."""
         g, st = dg.native()

@@ -932,7 +932,8 @@ template <class R> struct Step {
         raster_forward();
         const bool has_gt = in.gt != nullptr;
         if (has_gt) loss();
-        if (in.do_backward && has_gt) {
+        if (in.v_img_in) v_rend.assign(in.v_img_in, in.v_img_in + 3 * (size_t)P);
+        if (in.do_backward && (has_gt || in.v_img_in)) {
             raster_backward();
             project_backward();
             if (in.do_optimizer) optimizer();

@@ -67,6 +67,8 @@ typedef struct {
     int do_optimizer;     /* SH Adam, reg, 4-group Adam */
     int no_cutoff;        /* test switch: drop the sigma >= 5.55 and alpha < 1/255
                              cutoffs (finite-difference checks of the VJPs) */
+    const float *v_img_in; /* H*W*3 or NULL: backward from this dL/dimage instead
+                             of the loss's (the autograd binding's contract) */
 } OrStepIn;
 
 typedef struct {

@@ -41,6 +41,7 @@ class OrStepIn(C.Structure):
         ("do_sgld", C.c_int), ("seed", C.c_uint32), ("noise_lr", C.c_float), ("xyz_lr", C.c_float),
         ("max_disp", C.c_float),
         ("do_backward", C.c_int), ("do_optimizer", C.c_int), ("no_cutoff", C.c_int),
+        ("v_img_in", FP),
     ]
 
 
@@ -141,7 +142,7 @@ def num_threads() -> int:
 
 def train_step(prec: int, g, cam, step, *, moments=None, gt=None, mask=None, background=(0.0, 0.0, 0.0),
                ssim_weight=0.2, do_backward=True, do_optimizer=True, do_sgld=False, raster_mode=0, k_max=0,
-               isect_capacity=0, want_ids=True, no_cutoff=False):
+               isect_capacity=0, want_ids=True, no_cutoff=False, v_img=None):
     """Run one oracle step.
 
     g        : GaussianSet, UPDATED IN PLACE when do_optimizer / do_sgld.
@@ -196,6 +197,10 @@ def train_step(prec: int, g, cam, step, *, moments=None, gt=None, mask=None, bac
     ins.noise_lr, ins.xyz_lr, ins.max_disp = step.get("noise_lr", 5e5), step.get("xyz_lr", 1.6e-4), step.get("max_disp", 0.05)
     ins.do_backward, ins.do_optimizer = int(do_backward), int(do_optimizer)
     ins.no_cutoff = int(no_cutoff)
+    if v_img is not None:
+        v_img = np.ascontiguousarray(v_img, np.float32)
+        keep.append(v_img)
+        ins.v_img_in = _fp(v_img)
 
     o = {
         "xys": np.zeros((N, 2), np.float32), "depths": np.zeros(N, np.float32), "conics": np.zeros((N, 3), np.float32),
