@@ -63,6 +63,33 @@ float msplat_trainer_last_loss(MsplatTrainer t);
 /* The trainer's engine (for stats, timing and buffer inspection). */
 MsplatEngine *msplat_trainer_engine(MsplatTrainer t);
 
+/* Host-side views of a dataset (no counterpart in the reference's C API):
+ * camera i of the training (use_test = 0) or test list — intrinsics
+ * (fx, fy, cx, cy), size (width, height), camera-to-world (OpenGL axes,
+ * row-major) and the 8-bit RGB image [H,W,3]; any output may be NULL.
+ * Returns 0, or -1 for a bad index. */
+int msplat_dataset_camera(MsplatDataset ds, int i, int use_test, float intrinsics[4], int size[2], float c2w[16],
+                          uint8_t *image);
+
+/* msplat_dataset_create with the COLMAP image folder given explicitly (the
+ * reference CLI's --colmap-image-path); NULL = images/ next to the model. */
+MsplatDataset msplat_dataset_create_ex(const char *path, float downscaleFactor, bool evalMode, int testEvery,
+                                       const char *colmapImagePath);
+
+/* Replaces the trainer's Gaussians with a trained PLY (Model::loadPly, the
+ * CLI's --resume); optimizer state starts fresh.  Returns the iteration
+ * recorded in the file, or a negative code. */
+int msplat_trainer_load_ply(MsplatTrainer t, const char *path);
+
+/* Seed points (xyz [N,3] in training coordinates, rgb [N,3]); either output
+ * may be NULL.  Returns N. */
+int msplat_dataset_points(MsplatDataset ds, float *xyz, uint8_t *rgb);
+
+/* Decodes an image file (PNG, baseline JPEG, binary PPM/PGM) to float RGB in
+ * [0, 1]; with rgb == NULL only the size is returned.  Returns 0, or a
+ * negative code with the reason on stderr. */
+int msplat_image_read(const char *path, float *rgb, int *width, int *height);
+
 /* SSIM + L1 training loss and dL/dimage without any device allocation.
  * No counterpart in the reference: it is for callers that cannot call
  * cudaMalloc (a host application or server that owns all device memory

@@ -42,6 +42,11 @@ def _lib():
     vp, cp, fp = C.c_void_p, C.c_char_p, C.POINTER(C.c_float)
     L.msplat_dataset_create.argtypes = [cp, C.c_float, C.c_bool, C.c_int]
     L.msplat_dataset_create.restype = vp
+    L.msplat_dataset_create_ex.argtypes = [cp, C.c_float, C.c_bool, C.c_int, cp]
+    L.msplat_dataset_create_ex.restype = vp
+    L.msplat_dataset_camera.argtypes = [vp, C.c_int, C.c_int, fp, C.POINTER(C.c_int), fp, C.POINTER(C.c_uint8)]
+    L.msplat_dataset_points.argtypes = [vp, fp, C.POINTER(C.c_uint8)]
+    L.msplat_trainer_load_ply.argtypes = [vp, cp]
     L.msplat_dataset_create_from_memory.argtypes = [C.c_int, fp, fp, C.POINTER(C.c_int), C.POINTER(vp),
                                                     C.POINTER(vp), C.c_int, fp, C.POINTER(C.c_uint8), C.c_bool,
                                                     C.c_int, C.c_bool]
@@ -144,10 +149,13 @@ class TrainingStats:
 
 class Dataset:
     def __init__(self, path: str | None = None, downscale_factor: float = 1.0, eval_mode: bool = False,
-                 test_every: int = 8, _handle=None):
+                 test_every: int = 8, colmap_image_path: str | None = None, _handle=None):
         L = _lib()
-        self.h = _handle if _handle is not None else L.msplat_dataset_create(path.encode(), downscale_factor,
-                                                                             eval_mode, test_every)
+        if _handle is not None:
+            self.h = _handle
+        else:
+            self.h = L.msplat_dataset_create_ex(path.encode(), downscale_factor, eval_mode, test_every,
+                                                colmap_image_path.encode() if colmap_image_path else None)
         if not self.h:
             raise RuntimeError(f"could not load dataset {path!r}")
 
@@ -181,6 +189,21 @@ class Dataset:
     @property
     def num_test(self) -> int:
         return _lib().msplat_dataset_num_test(self.h)
+
+    def camera(self, index: int, use_test: bool = False) -> dict:
+        """Intrinsics, size, pose and the 8-bit image of a training (or test) view."""
+        L = _lib()
+        intr = np.zeros(4, np.float32)
+        size = np.zeros(2, np.int32)
+        c2w = np.zeros(16, np.float32)
+        if L.msplat_dataset_camera(self.h, index, int(use_test), _fp(intr), size.ctypes.data_as(C.POINTER(C.c_int)),
+                                   _fp(c2w), None) != 0:
+            raise IndexError(index)
+        img = np.zeros((int(size[1]), int(size[0]), 3), np.uint8)
+        L.msplat_dataset_camera(self.h, index, int(use_test), None, None, None,
+                                img.ctypes.data_as(C.POINTER(C.c_uint8)))
+        return {"fx": float(intr[0]), "fy": float(intr[1]), "cx": float(intr[2]), "cy": float(intr[3]),
+                "width": int(size[0]), "height": int(size[1]), "cam_to_world": c2w.reshape(4, 4), "image": img}
 
     def camera_pose(self, index: int) -> np.ndarray:
         out = np.zeros(16, np.float32)
@@ -246,6 +269,13 @@ class GaussianTrainer:
 
     def export_splat(self, path: str):
         _lib().msplat_trainer_export_splat(self.h, path.encode())
+
+    def load_ply(self, path: str) -> int:
+        """Replace the Gaussians with a trained PLY (fresh optimizer); returns its iteration."""
+        rc = _lib().msplat_trainer_load_ply(self.h, path.encode())
+        if rc < 0:
+            raise RuntimeError(f"could not load {path!r}")
+        return rc
 
     def save_checkpoint(self, path: str):
         _lib().msplat_trainer_save_checkpoint(self.h, path.encode())

@@ -1,0 +1,155 @@
+"""Command-line training driver: `python -m msplat_gb300.cli <dataset> [options]`.
+
+The options and the run follow the reference's `msplat` CLI (cli/msplat.mm)
+and `msplat-train` (python/msplat/cli.py): load a COLMAP / Nerfstudio /
+Polycam dataset, train with MCMC densification to --num-iters, optionally
+resume from a trained PLY, save every N steps, stop early when the held-out
+PSNR stops improving (two consecutive 5000-step gates below --early-stop dB,
+from step 10000, needs --eval), export PLY or .splat, evaluate PSNR / SSIM /
+L1 on the held-out views and write their renders.  Everything runs through
+the library's C API; no training math lives here.
+"""
+from __future__ import annotations
+
+import argparse
+import math
+import os
+import struct
+import sys
+import time
+import zlib
+
+import numpy as np
+
+from . import api as A
+
+
+def _write_png(path: str, rgb: np.ndarray):
+    """8-bit RGB PNG (filter 0 rows, zlib) for the evaluation renders."""
+    img = np.clip(np.round(rgb * 255.0), 0, 255).astype(np.uint8) if rgb.dtype != np.uint8 else rgb
+    h, w, _ = img.shape
+    raw = b"".join(b"\x00" + img[y].tobytes() for y in range(h))
+
+    def chunk(t, d):
+        return struct.pack(">I", len(d)) + t + d + struct.pack(">I", zlib.crc32(t + d) & 0xFFFFFFFF)
+
+    data = (b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 2, 0, 0, 0)) +
+            chunk(b"IDAT", zlib.compress(raw, 6)) + chunk(b"IEND", b""))
+    with open(path, "wb") as f:
+        f.write(data)
+
+
+def _psnr(img: np.ndarray, gt_u8: np.ndarray) -> float:
+    mse = float(np.mean((img.astype(np.float64) - gt_u8.astype(np.float64) / 255.0) ** 2))
+    return 10.0 * math.log10(1.0 / max(mse, 1e-12))
+
+
+def parse(argv=None):
+    p = argparse.ArgumentParser(prog="msplat", description="Train 3D Gaussian Splatting on a dataset (GB300).")
+    p.add_argument("input", help="dataset (COLMAP, Nerfstudio, Polycam)")
+    p.add_argument("-o", "--output", default="splat.ply", help="output scene (.ply or .splat)")
+    p.add_argument("-s", "--save-every", type=int, default=-1, help="save every N steps (-1 to disable)")
+    p.add_argument("--resume", default="", help="resume training from a PLY file")
+    p.add_argument("--eval", action="store_true", help="evaluate on held-out test views")
+    p.add_argument("--test-every", type=int, default=8, help="hold out every Nth image for eval")
+    p.add_argument("--eval-render", default="", help="directory for each eval view's render and ground truth (PNG)")
+    p.add_argument("-n", "--num-iters", type=int, default=30000, help="number of iterations")
+    p.add_argument("-d", "--downscale-factor", type=float, default=1.0, help="image downscale factor")
+    p.add_argument("--sh-degree", type=int, default=3, help="max spherical harmonics degree")
+    p.add_argument("--sh-degree-interval", type=int, default=1000, help="increase SH degree every N steps")
+    p.add_argument("--ssim-weight", type=float, default=0.2, help="SSIM loss weight (0 = L1 only)")
+    p.add_argument("--cap-max", type=int, default=1_000_000, help="maximum Gaussian budget")
+    p.add_argument("--noise-lr", type=float, default=5e5, help="SGLD noise learning rate")
+    p.add_argument("--opacity-reg", type=float, default=0.01, help="opacity regularization weight")
+    p.add_argument("--scale-reg", type=float, default=0.01, help="scale regularization weight")
+    p.add_argument("--cull-radius", type=float, default=3.0, help="cull splats with |mean| > r (0 = off)")
+    p.add_argument("--keep-crs", action="store_true", help="export in the input coordinate system")
+    p.add_argument("--bg-color", type=float, nargs=3, default=[0.6130, 0.0101, 0.3984], help="background RGB (0-1)")
+    p.add_argument("--colmap-image-path", default="", help="override the COLMAP image directory")
+    p.add_argument("--early-stop", type=float, default=0.0,
+                   help="stop when test-subset PSNR improves less than this (dB) over 5000 steps (needs --eval)")
+    p.add_argument("--log-every", type=int, default=100, help="print progress every N steps")
+    a = p.parse_args(argv)
+    a.downscale_factor = max(a.downscale_factor, 1.0)
+    return a
+
+
+def _save(trainer: A.GaussianTrainer, path: str):
+    if path.endswith(".splat"):
+        trainer.export_splat(path)
+    else:
+        trainer.export_ply(path)
+
+
+def main(argv=None) -> int:
+    a = parse(argv)
+    t0 = time.time()
+    ds = A.Dataset(a.input, downscale_factor=a.downscale_factor, eval_mode=a.eval, test_every=a.test_every,
+                   colmap_image_path=a.colmap_image_path or None)
+    print(f"Loaded {ds.num_train} train cameras" + (f", {ds.num_test} test cameras" if a.eval else "") +
+          f" in {time.time() - t0:.1f} s", flush=True)
+    cfg = A.TrainingConfig(iterations=a.num_iters, sh_degree=a.sh_degree, sh_degree_interval=a.sh_degree_interval,
+                           ssim_weight=a.ssim_weight, cap_max=a.cap_max, noise_lr=a.noise_lr,
+                           opacity_reg=a.opacity_reg, scale_reg=a.scale_reg, cull_radius=a.cull_radius,
+                           keep_crs=a.keep_crs, downscale_factor=a.downscale_factor, bg_color=list(a.bg_color),
+                           output=a.output, save_every=a.save_every)
+    trainer = A.GaussianTrainer(ds, cfg)
+    if a.resume:
+        step0 = trainer.load_ply(a.resume)
+        print(f"Resumed from {a.resume} at step {step0}", flush=True)
+    if ds.num_train == 0 and trainer.iteration < a.num_iters:
+        print("No training views (--test-every 1) but training steps were requested", file=sys.stderr)
+        return 1
+    last_gate, misses, stopped = -1e9, 0, 0
+    t_start = time.time()
+    while trainer.iteration < a.num_iters:
+        s = trainer.step()
+        step = s.iteration
+        if a.log_every > 0 and step % a.log_every == 0:
+            el = time.time() - t_start
+            print(f"step={step:>6}  splats={s.splat_count:>9,}  loss={trainer.last_loss:.5f}  "
+                  f"ms={s.ms_per_step:.2f}  elapsed={el:.1f}s", flush=True)
+        if a.save_every > 0 and step % a.save_every == 0:
+            root, ext = os.path.splitext(a.output)
+            _save(trainer, f"{root}_{step}{ext or '.ply'}")
+        if (a.early_stop > 0 and a.eval and ds.num_test > 0 and step >= 10000 and step % 5000 == 0 and
+                step < a.num_iters):
+            n_sub = min(30, ds.num_test)
+            stride = max(1, ds.num_test // n_sub)
+            vals = [_psnr(trainer.render(i, use_test=True), ds.camera(i, use_test=True)["image"])
+                    for i in range(0, ds.num_test, stride)][:n_sub]
+            gate = float(np.mean(vals))
+            msg = f"[early-stop] step={step} subset_psnr={gate:.4f}"
+            if last_gate > -1e8:
+                msg += f" delta={gate - last_gate:.4f}"
+            print(msg, flush=True)
+            if last_gate > -1e8 and gate - last_gate < a.early_stop:
+                misses += 1
+                if misses >= 2:
+                    print(f"early-stop: two gates below {a.early_stop} dB per 5000 steps; stopping at step {step}")
+                    stopped = step
+            else:
+                misses = 0
+            last_gate = gate
+            if stopped:
+                break
+    _save(trainer, a.output)
+    print(f"Saved {a.output} ({trainer.splat_count:,} Gaussians, {time.time() - t_start:.1f} s of training)")
+    if a.eval and ds.num_test > 0:
+        m = trainer.evaluate()
+        print(f"\n=== Evaluation ({m['num_test']} test views) ===")
+        print(f"  PSNR:  {m['psnr']:.4f}")
+        print(f"  SSIM:  {m['ssim']:.4f}")
+        print(f"  L1:    {m['l1']:.4f}")
+        print(f"  Gaussians: {m['num_gaussians']:,}")
+        if a.eval_render:
+            os.makedirs(a.eval_render, exist_ok=True)
+            for i in range(ds.num_test):
+                _write_png(os.path.join(a.eval_render, f"test_{i:04d}.png"), trainer.render(i, use_test=True))
+                _write_png(os.path.join(a.eval_render, f"test_{i:04d}_gt.png"), ds.camera(i, use_test=True)["image"])
+    A.cleanup()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -4,6 +4,8 @@
 // Parameters and Adam moments live in cap-sized device buffers with an
 // N-row active prefix, as in the reference (model.cpp:168-254).
 #include <algorithm>
+#include <thread>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -21,6 +23,7 @@
 
 #include "msplat_c_api.h"
 #include "msplat_engine.h"
+#include "dataset_io.h"
 #include "msplat_gb300.h"
 
 namespace msplat {
@@ -92,10 +95,9 @@ struct DatasetImpl {
 // to 1 (autoScaleAndCenter, core/src/input_data.cpp:115-169).
 static void auto_scale_and_center(std::vector<HostCamera> &cams, std::vector<float> &xyz, float &scale, float t[3]) {
     if (cams.empty()) return;
-    double mean[3] = {0, 0, 0};
-    for (auto &c : cams) { mean[0] += c.c2w[3]; mean[1] += c.c2w[7]; mean[2] += c.c2w[11]; }
-    float m[3];
-    for (int k = 0; k < 3; k++) m[k] = (float)(mean[k] / cams.size());
+    float m[3] = {0.f, 0.f, 0.f};   // float sums, as the reference accumulates
+    for (auto &c : cams) { m[0] += c.c2w[3]; m[1] += c.c2w[7]; m[2] += c.c2w[11]; }
+    for (int k = 0; k < 3; k++) m[k] /= (float)(int)cams.size();
     float mx = 0;
     for (auto &c : cams) {
         c.c2w[3] -= m[0]; c.c2w[7] -= m[1]; c.c2w[11] -= m[2];
@@ -634,6 +636,16 @@ struct TrainerImpl {
         for (int g = 0; g < 6; g++) tensor(model.v, g);
     }
 
+    // Model::loadPly (model.cpp:683-694): trained Gaussians, fresh optimizer
+    int load_ply(const std::string &path) {
+        int step = 0;
+        HostGaussians h = read_ply(path, &step, cfg.keepCrs, ds->scale, ds->translation);
+        set_model(h, false);
+        current_step = step;
+        shuffle_cameras();
+        return step;
+    }
+
     int load_checkpoint(const std::string &path) {
         std::ifstream f(path, std::ios::binary);
         if (!f) throw std::runtime_error("cannot open checkpoint " + path);
@@ -763,12 +775,70 @@ template <class F> static auto guard(const char *what, F &&f, decltype(f()) fall
 
 using namespace msplat;
 
-// Datasets on disk (COLMAP / Nerfstudio / Polycam with JPEG/PNG images, the
-// reference's inputDataFromX, core/src/input_data.cpp:244-261) are not read
-// yet; msplat_dataset_create_from_memory builds a dataset from arrays.
-static MsplatDataset msplat_dataset_load(const char *path, float, bool, int) {
-    throw std::runtime_error(std::string("reading datasets from disk is not supported yet (") + (path ? path : "") +
-                             "); use msplat_dataset_create_from_memory");
+// A dataset directory (Camera::loadImage + inputDataFromX,
+// core/src/input_data.cpp:22-73 and 244-261): cameras and seed points from
+// the layout, poses centred and scaled, then every image decoded, its
+// intrinsics rescaled to the decoded size, area-downscaled by the factor,
+// undistorted when the camera has distortion, and quantised to 8 bits.
+// Images decode on all host threads.
+static MsplatDataset msplat_dataset_load(const char *path, float downscale, bool eval_mode, int test_every,
+                                         const char *colmap_image_dir = nullptr) {
+    if (!path) throw std::runtime_error("dataset path is null");
+    io::LoadedScene sc = io::load_scene(path, colmap_image_dir ? colmap_image_dir : "");
+    auto d = std::make_unique<DatasetImpl>();
+    std::vector<HostCamera> cams(sc.cameras.size());
+    for (size_t i = 0; i < cams.size(); i++) std::memcpy(cams[i].c2w, sc.cameras[i].c2w, 64);
+    d->xyz = std::move(sc.xyz);
+    d->rgb = std::move(sc.rgb);
+    if (d->xyz.empty()) throw std::runtime_error(std::string("dataset has no seed points: ") + path);
+    auto_scale_and_center(cams, d->xyz, d->scale, d->translation);
+    std::vector<std::string> errors(cams.size());
+    std::atomic<size_t> next{0};
+    auto work = [&]() {
+        for (size_t i = next++; i < cams.size(); i = next++) {
+            try {
+                const io::LoadedCamera &lc = sc.cameras[i];
+                HostCamera &c = cams[i];
+                io::Image img = io::read_image(lc.path);
+                c.width = lc.width; c.height = lc.height;
+                c.fx = lc.fx; c.fy = lc.fy; c.cx = lc.cx; c.cy = lc.cy;
+                if (c.width > 0 && c.height > 0 && (img.width != c.width || img.height != c.height)) {
+                    const float sx = (float)img.width / (float)c.width, sy = (float)img.height / (float)c.height;
+                    c.fx *= sx; c.fy *= sy; c.cx *= sx; c.cy *= sy;
+                }
+                c.width = img.width;
+                c.height = img.height;
+                if (downscale > 1.0f) {
+                    const int nw = (int)(c.width / downscale), nh = (int)(c.height / downscale);
+                    img = io::resize_area(img, nw, nh);
+                    const float sx = (float)nw / (float)c.width, sy = (float)nh / (float)c.height;
+                    c.fx *= sx; c.fy *= sy; c.cx *= sx; c.cy *= sy;
+                    c.width = nw;
+                    c.height = nh;
+                }
+                if (lc.k1 != 0.f || lc.k2 != 0.f || lc.k3 != 0.f || lc.p1 != 0.f || lc.p2 != 0.f)
+                    img = io::undistort(img, c.fx, c.fy, c.cx, c.cy, lc.k1, lc.k2, lc.p1, lc.p2, lc.k3);
+                c.image.resize(img.rgb.size());
+                for (size_t k = 0; k < img.rgb.size(); k++)
+                    c.image[k] = (uint8_t)std::min(std::max(std::round(img.rgb[k] * 255.0f), 0.0f), 255.0f);
+            } catch (const std::exception &e) {
+                errors[i] = e.what();
+            }
+        }
+    };
+    const unsigned nt = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), 32u));
+    std::vector<std::thread> pool;
+    for (unsigned t = 0; t < nt; t++) pool.emplace_back(work);
+    for (auto &t : pool) t.join();
+    for (size_t i = 0; i < cams.size(); i++)
+        if (!errors[i].empty()) throw std::runtime_error(sc.cameras[i].path + ": " + errors[i]);
+    if (eval_mode) {
+        const int every = std::max(1, test_every);
+        for (size_t i = 0; i < cams.size(); i++) (i % every == 0 ? d->test : d->train).push_back(std::move(cams[i]));
+    } else {
+        d->train = std::move(cams);
+    }
+    return d.release();
 }
 
 static DatasetImpl *DS(MsplatDataset d) { return static_cast<DatasetImpl *>(d); }
@@ -780,6 +850,13 @@ extern "C" {
 MsplatDataset msplat_dataset_create(const char *path, float downscaleFactor, bool evalMode, int testEvery) {
     return guard("dataset", [&]() -> MsplatDataset {
         return msplat_dataset_load(path, downscaleFactor, evalMode, testEvery);
+    }, (MsplatDataset) nullptr);
+}
+
+MsplatDataset msplat_dataset_create_ex(const char *path, float downscaleFactor, bool evalMode, int testEvery,
+                                       const char *colmapImagePath) {
+    return guard("dataset", [&]() -> MsplatDataset {
+        return msplat_dataset_load(path, downscaleFactor, evalMode, testEvery, colmapImagePath);
     }, (MsplatDataset) nullptr);
 }
 
@@ -820,6 +897,38 @@ MsplatDataset msplat_dataset_create_from_memory(int num_cameras, const float *ca
 }
 
 void msplat_dataset_destroy(MsplatDataset ds) { delete DS(ds); }
+
+int msplat_dataset_camera(MsplatDataset ds, int i, int use_test, float intrinsics[4], int size[2], float c2w[16],
+                          uint8_t *image) {
+    if (!ds) return -1;
+    auto &cams = use_test ? DS(ds)->test : DS(ds)->train;
+    if (i < 0 || i >= (int)cams.size()) return -1;
+    const HostCamera &c = cams[i];
+    if (intrinsics) { intrinsics[0] = c.fx; intrinsics[1] = c.fy; intrinsics[2] = c.cx; intrinsics[3] = c.cy; }
+    if (size) { size[0] = c.width; size[1] = c.height; }
+    if (c2w) std::memcpy(c2w, c.c2w, 64);
+    if (image) std::memcpy(image, c.image.data(), c.image.size());
+    return 0;
+}
+
+int msplat_dataset_points(MsplatDataset ds, float *xyz, uint8_t *rgb) {
+    if (!ds) return -1;
+    const DatasetImpl *d = DS(ds);
+    if (xyz) std::memcpy(xyz, d->xyz.data(), d->xyz.size() * sizeof(float));
+    if (rgb) std::memcpy(rgb, d->rgb.data(), d->rgb.size());
+    return (int)(d->xyz.size() / 3);
+}
+
+int msplat_image_read(const char *path, float *rgb, int *width, int *height) {
+    if (!path) return -1;
+    return guard("image", [&]() {
+        io::Image im = io::read_image(path);
+        if (width) *width = im.width;
+        if (height) *height = im.height;
+        if (rgb) std::memcpy(rgb, im.rgb.data(), im.rgb.size() * sizeof(float));
+        return 0;
+    }, -2);
+}
 int msplat_dataset_num_train(MsplatDataset ds) { return ds ? (int)DS(ds)->train.size() : 0; }
 int msplat_dataset_num_test(MsplatDataset ds) { return ds ? (int)DS(ds)->test.size() : 0; }
 
@@ -973,6 +1082,11 @@ int msplat_trainer_get_gaussians(MsplatTrainer t, float *means, float *scales, f
             if (dst[g]) std::memcpy(dst[g], h.a[g].data(), h.a[g].size() * 4);
         return 0;
     }, -2);
+}
+
+int msplat_trainer_load_ply(MsplatTrainer t, const char *path) {
+    if (!t || !path) return -1;
+    return guard("load_ply", [&]() { return TR(t)->load_ply(path); }, -2);
 }
 
 float msplat_trainer_last_loss(MsplatTrainer t) {
