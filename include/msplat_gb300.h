@@ -63,6 +63,13 @@ float msplat_trainer_last_loss(MsplatTrainer t);
 /* The trainer's engine (for stats, timing and buffer inspection). */
 MsplatEngine *msplat_trainer_engine(MsplatTrainer t);
 
+/* Tensor-core self-test (the MMA path of the learned relocation proposal):
+ * D[128 x N] = A[128 x K] * B[N x K]^T for row-major BF16 A, B (host, as
+ * uint16 bit patterns) into row-major F32 D (host), N, K in {16, 32, 64}, on
+ * the current device.  Returns 0, or -1 (bad size), -2 (CUDA error), -3 (the
+ * MMA did not complete within the wait limit). */
+int msplat_tc_gemm_check(const uint16_t *A, const uint16_t *B, float *D, int N, int K);
+
 /* Host-side views of a dataset (no counterpart in the reference's C API):
  * camera i of the training (use_test = 0) or test list — intrinsics
  * (fx, fy, cx, cy), size (width, height), camera-to-world (OpenGL axes,
