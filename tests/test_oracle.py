@@ -159,3 +159,34 @@ def test_eval_metrics():
     assert abs(O.l1(a, b) - np.mean(np.abs(a - b))) < 1e-6
     assert abs(O.ssim_eval(a, a) - 1.0) < 1e-6
     assert 0.0 < O.ssim_eval(a, b) < 1.0
+
+
+def test_mlp_oracle_gradients_finite_differences():
+    """The MLP restatement's analytic gradient (float64, no rounding) against
+    central differences of its own loss."""
+    from oracle import mlp_oracle as M
+    rng = np.random.default_rng(4)
+    X = np.zeros((40, 32))
+    X[:, :M.N_IN] = rng.normal(0, 1, (40, M.N_IN))
+    T = rng.normal(0, 0.5, (40, 2))
+    P = M.init_params(1).astype(np.float64)
+    P[M.OFF["b1"][0]:M.OFF["b1"][0] + 64] = rng.normal(0, 0.1, 64)
+    loss, g = M.loss_and_grad(X, T, P, rounding=False)
+    idx = rng.choice(np.nonzero(g)[0], 60, replace=False)
+    h = 1e-6
+    fd = []
+    for i in idx:
+        Pp, Pm = P.copy(), P.copy()
+        Pp[i] += h
+        Pm[i] -= h
+        fd.append((M.loss_and_grad(X, T, Pp, False)[0] - M.loss_and_grad(X, T, Pm, False)[0]) / (2 * h))
+    fd = np.array(fd)
+    assert np.linalg.norm(fd - g[idx]) / np.linalg.norm(fd) < 1e-6
+
+
+def test_mlp_oracle_bf16_rounding():
+    from oracle import mlp_oracle as M
+    x = np.array([1.0, 1.00390625, 1.005859375, -3.14159, 0.0, 65504.0], np.float32)
+    r = M.bf16(x)
+    assert r[0] == 1.0 and r[1] == 1.0 and r[2] == 1.0078125   # ties to even; 1 + 1.5 ulp rounds up
+    assert abs(r[3] + 3.140625) < 1e-6 and r[4] == 0.0
