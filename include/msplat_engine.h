@@ -167,6 +167,20 @@ typedef struct {
 int msplat_engine_backward(MsplatEngine *e, const MsplatGaussians *g, const MsplatStepArgs *args, const float *v_img,
                            const MsplatGradients *out);
 
+/* Learned relocation proposal support.  `stats` (device float4 per
+ * Gaussian, cap-sized, caller-owned, zeroed by the caller; NULL to stop)
+ * accumulates per training step: x += |dL/d(pixel centre)| and y += 1 when
+ * the Gaussian is visible, z += 1 (age).  MCMC clears the entry of every
+ * slot it fills with a copy. */
+int msplat_engine_set_activity_stats(MsplatEngine *e, void *stats);
+
+/* msplat_engine_mcmc with the sampling weight of each Gaussian taken from
+ * `score` (device float [num_points]; non-positive or non-finite = never
+ * drawn) instead of sigmoid(opacity).  The dead/culled classification is
+ * unchanged. */
+int msplat_engine_mcmc_scored(MsplatEngine *e, const MsplatGaussians *g, const MsplatAdamState *st, int cap_max,
+                              float cull_radius, int *relocation_count, const float *score, MsplatMcmcStats *out);
+
 /* CUDA graph mode (off by default).  When on, the second training step with
  * the same shapes, flags and buffers (parameters, moments, target, mask) is
  * captured into a CUDA graph and later such steps replay it with one launch;

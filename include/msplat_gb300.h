@@ -83,6 +83,18 @@ int msplat_dataset_camera(MsplatDataset ds, int i, int use_test, float intrinsic
 MsplatDataset msplat_dataset_create_ex(const char *path, float downscaleFactor, bool evalMode, int testEvery,
                                        const char *colmapImagePath);
 
+/* Learned relocation proposal (no counterpart in the reference; off by
+ * default): per-Gaussian activity statistics are gathered during the steps,
+ * a 22-64-64-2 MLP on the tensor cores is trained every 500 steps on the
+ * run's own (state -> opacity and activity 500 steps later) pairs, and once
+ * trained its predictions replace sigmoid(opacity) as the weights of the
+ * MCMC source draws.  Returns 0 or a negative code. */
+int msplat_trainer_set_learned_relocation(MsplatTrainer t, int enabled);
+
+/* Last training loss of the proposal MLP and its training rounds so far;
+ * returns 1 when the proposal is enabled, 0 when not, -1 on a bad handle. */
+int msplat_trainer_learned_stats(MsplatTrainer t, float *last_loss, int *rounds);
+
 /* Replaces the trainer's Gaussians with a trained PLY (Model::loadPly, the
  * CLI's --resume); optimizer state starts fresh.  Returns the iteration
  * recorded in the file, or a negative code. */

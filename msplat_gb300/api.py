@@ -47,6 +47,8 @@ def _lib():
     L.msplat_dataset_camera.argtypes = [vp, C.c_int, C.c_int, fp, C.POINTER(C.c_int), fp, C.POINTER(C.c_uint8)]
     L.msplat_dataset_points.argtypes = [vp, fp, C.POINTER(C.c_uint8)]
     L.msplat_trainer_load_ply.argtypes = [vp, cp]
+    L.msplat_trainer_set_learned_relocation.argtypes = [vp, C.c_int]
+    L.msplat_trainer_learned_stats.argtypes = [vp, fp, C.POINTER(C.c_int)]
     L.msplat_dataset_create_from_memory.argtypes = [C.c_int, fp, fp, C.POINTER(C.c_int), C.POINTER(vp),
                                                     C.POINTER(vp), C.c_int, fp, C.POINTER(C.c_uint8), C.c_bool,
                                                     C.c_int, C.c_bool]
@@ -269,6 +271,17 @@ class GaussianTrainer:
 
     def export_splat(self, path: str):
         _lib().msplat_trainer_export_splat(self.h, path.encode())
+
+    def set_learned_relocation(self, enabled: bool = True):
+        """Weight MCMC source draws by the online-trained proposal MLP (see msplat_gb300.h)."""
+        if _lib().msplat_trainer_set_learned_relocation(self.h, int(enabled)) != 0:
+            raise RuntimeError("could not switch the learned relocation proposal")
+
+    def learned_stats(self) -> dict:
+        loss = (C.c_float * 1)()
+        rounds = C.c_int()
+        on = _lib().msplat_trainer_learned_stats(self.h, loss, C.byref(rounds))
+        return {"enabled": on == 1, "last_loss": float(loss[0]), "rounds": rounds.value}
 
     def load_ply(self, path: str) -> int:
         """Replace the Gaussians with a trained PLY (fresh optimizer); returns its iteration."""

@@ -24,6 +24,7 @@
 #include "msplat_c_api.h"
 #include "msplat_engine.h"
 #include "dataset_io.h"
+#include "mlp.h"
 #include "msplat_gb300.h"
 
 namespace msplat {
@@ -385,6 +386,27 @@ struct TrainerImpl {
     std::mt19937 rng{42};
     float last_loss = 0.f;
 
+    // learned relocation proposal (off unless enabled): activity statistics
+    // accumulated by the step, an MLP trained online every `window` steps on
+    // (state -> opacity and activity `window` steps later) pairs the run
+    // itself produces, whose predictions weight the MCMC source draws once it
+    // has been trained; plain opacity weights before that and when disabled
+    struct Learned {
+        bool enabled = false;
+        int window = 500, samples = 16384, epochs = 40;
+        float lr = 1e-3f;
+        float *P = nullptr, *G = nullptr, *M = nullptr, *V = nullptr, *loss = nullptr, *score = nullptr;
+        uint8_t *img = nullptr;
+        unsigned *err = nullptr;
+        float4 *gstats = nullptr, *snap = nullptr;
+        __nv_bfloat16 *X = nullptr, *Xs = nullptr;
+        float2 *Y = nullptr, *T = nullptr;
+        int *idx = nullptr;
+        int pending = -1, rounds = 0, adam_steps = 0, cap = 0;
+        float last_loss = NAN;
+        std::mt19937 rng{7};
+    } lrn;
+
     TrainerImpl(DatasetImpl *d, const MsplatConfig &c) : cfg(c), ds(d) {
         int dev = 0;
         CKA(cudaGetDevice(&dev));
@@ -397,7 +419,115 @@ struct TrainerImpl {
         shuffle_cameras();
     }
     ~TrainerImpl() {
+        free_learned();
         if (eng) msplat_engine_destroy(eng);
+    }
+
+    void free_learned() {
+        void *ptrs[] = {lrn.P, lrn.G, lrn.M, lrn.V, lrn.loss, lrn.score, lrn.img, lrn.err, lrn.gstats, lrn.snap,
+                        lrn.X, lrn.Xs, lrn.Y, lrn.T, lrn.idx};
+        for (void *q : ptrs)
+            if (q) cudaFree(q);
+        lrn = Learned{};
+    }
+
+    void enable_learned(bool on) {
+        if (!on) {
+            if (eng) msplat_engine_set_activity_stats(eng, nullptr);
+            free_learned();
+            return;
+        }
+        if (lrn.enabled) return;
+        const int cap = std::max(1, model.cap);
+        lrn.cap = cap;
+        CKA(cudaMalloc(&lrn.P, kMlpParams * 4));
+        CKA(cudaMalloc(&lrn.G, kMlpParams * 4));
+        CKA(cudaMalloc(&lrn.M, kMlpParams * 4));
+        CKA(cudaMalloc(&lrn.V, kMlpParams * 4));
+        CKA(cudaMalloc(&lrn.loss, 4));
+        CKA(cudaMalloc(&lrn.err, 4));
+        CKA(cudaMalloc(&lrn.img, kImgBytes));
+        CKA(cudaMalloc(&lrn.gstats, sizeof(float4) * (size_t)cap));
+        CKA(cudaMalloc(&lrn.score, 4 * (size_t)cap));
+        CKA(cudaMalloc(&lrn.X, 64 * (size_t)cap));
+        CKA(cudaMalloc(&lrn.Y, 8 * (size_t)cap));
+        CKA(cudaMalloc(&lrn.Xs, 64 * (size_t)lrn.samples));
+        CKA(cudaMalloc(&lrn.T, 8 * (size_t)lrn.samples));
+        CKA(cudaMalloc(&lrn.snap, sizeof(float4) * (size_t)lrn.samples));
+        CKA(cudaMalloc(&lrn.idx, 4 * (size_t)lrn.samples));
+        CKA(cudaMemset(lrn.gstats, 0, sizeof(float4) * (size_t)cap));
+        CKA(cudaMemset(lrn.G, 0, kMlpParams * 4));
+        CKA(cudaMemset(lrn.M, 0, kMlpParams * 4));
+        CKA(cudaMemset(lrn.V, 0, kMlpParams * 4));
+        CKA(cudaMemset(lrn.err, 0, 4));
+        // uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) weights, zero biases
+        std::vector<float> P(kMlpParams, 0.f);
+        std::mt19937 r(1234);
+        std::uniform_real_distribution<float> u(-1.f, 1.f);
+        for (int i = 0; i < kMlpIn; i++)
+            for (int o = 0; o < 64; o++) P[kMlpW1 + i * 64 + o] = u(r) / std::sqrt((float)kMlpIn);
+        for (int i = 0; i < 64 * 64; i++) P[kMlpW2 + i] = u(r) / 8.f;
+        for (int i = 0; i < 64; i++)
+            for (int o = 0; o < 2; o++) P[kMlpW3 + i * 16 + o] = u(r) / 8.f;
+        CKA(cudaMemcpy(lrn.P, P.data(), kMlpParams * 4, cudaMemcpyHostToDevice));
+        lrn.enabled = true;
+        msplat_engine_set_activity_stats(eng, lrn.gstats);
+    }
+
+    cudaStream_t stream() const { return static_cast<cudaStream_t>(msplat_engine_stream(eng)); }
+
+    MlpFeatArgs feat_args(int rows, const int *idx, __nv_bfloat16 *X) {
+        MlpFeatArgs fa{};
+        fa.rows = rows;
+        fa.idx = idx;
+        fa.means = model.p[0]; fa.scales = model.p[1]; fa.quats = model.p[2];
+        fa.features_dc = model.p[3]; fa.opacities = model.p[5];
+        fa.gstats = lrn.gstats;
+        void *radii = nullptr;
+        const long long rb = msplat_engine_buffer(eng, "radii", &radii);
+        fa.radii = (rb >= 4LL * model.n) ? static_cast<const int *>(radii) : nullptr;
+        fa.X = X;
+        return fa;
+    }
+
+    // every `window` steps: label the previous snapshot and train, then take a new one
+    void learned_after_step(int step) {
+        if (!lrn.enabled || step < lrn.window || step % lrn.window != 0 || model.n <= 0) return;
+        cudaStream_t s = stream();
+        if (lrn.pending >= 0) {
+            mlp_targets(lrn.idx, lrn.snap, lrn.samples, model.p[5], lrn.gstats, lrn.T, s);
+            for (int e = 0; e < lrn.epochs; e++) {
+                mlp_pack(lrn.P, lrn.img, s);
+                CKA(cudaMemsetAsync(lrn.loss, 0, 4, s));
+                mlp_train_batch(lrn.Xs, lrn.T, lrn.samples, lrn.img, lrn.P, lrn.G, lrn.loss, lrn.err, s);
+                mlp_adam(lrn.P, lrn.G, lrn.M, lrn.V, lrn.lr, ++lrn.adam_steps, s);
+            }
+            CKA(cudaMemcpyAsync(&lrn.last_loss, lrn.loss, 4, cudaMemcpyDeviceToHost, s));
+            unsigned err = 0;
+            CKA(cudaMemcpyAsync(&err, lrn.err, 4, cudaMemcpyDeviceToHost, s));
+            CKA(cudaStreamSynchronize(s));
+            if (err) throw std::runtime_error("learned relocation: tensor-core MMA did not complete");
+            lrn.rounds++;
+        }
+        std::vector<int> idx(lrn.samples);
+        std::uniform_int_distribution<int> pick(0, model.n - 1);
+        for (auto &v : idx) v = pick(lrn.rng);
+        CKA(cudaMemcpyAsync(lrn.idx, idx.data(), 4 * idx.size(), cudaMemcpyHostToDevice, s));
+        mlp_features(feat_args(lrn.samples, lrn.idx, lrn.Xs), s);
+        mlp_snapshot(lrn.idx, lrn.samples, lrn.gstats, lrn.snap, s);
+        CKA(cudaStreamSynchronize(s));   // idx is a host vector
+        lrn.pending = step;
+    }
+
+    // MCMC source weights from the trained MLP, or null for the plain rule
+    const float *learned_scores() {
+        if (!lrn.enabled || lrn.rounds == 0 || model.n <= 0) return nullptr;
+        cudaStream_t s = stream();
+        mlp_pack(lrn.P, lrn.img, s);
+        mlp_features(feat_args(model.n, nullptr, lrn.X), s);
+        mlp_forward(lrn.X, model.n, lrn.img, lrn.P, lrn.Y, lrn.err, s);
+        mlp_scores(lrn.Y, model.n, lrn.score, s);
+        return lrn.score;
     }
 
     void shuffle_cameras() {
@@ -521,6 +651,7 @@ struct TrainerImpl {
         MsplatGaussians g = model.gaussians();
         MsplatAdamState st = model.adam();
         check(msplat_engine_train_step(eng, &g, &st, &a, cam.d_image, cam.d_mask), "train step");
+        learned_after_step(current_step);
         // schedulersStep (model.cpp:256-261)
         const float t = std::clamp((float)current_step / (float)position_lr_max_steps, 0.f, 1.f);
         adam_lr[0] = std::exp(std::log(means_lr_init) * (1.f - t) + std::log(means_lr_final) * t);
@@ -540,7 +671,8 @@ struct TrainerImpl {
         MsplatGaussians g = model.gaussians();
         MsplatAdamState st = model.adam();
         MsplatMcmcStats ms;
-        check(msplat_engine_mcmc(eng, &g, &st, model.cap, cfg.cullRadius, &reloc_count, &ms), "mcmc");
+        const float *score = learned_scores();
+        check(msplat_engine_mcmc_scored(eng, &g, &st, model.cap, cfg.cullRadius, &reloc_count, score, &ms), "mcmc");
         model.n = ms.num_active;
         if (step % 1000 == 0)
             printf("MCMC step=%d active=%d dead=%d culled=%d nonfinite=%d grown=%d\n", step, ms.num_active,
@@ -1082,6 +1214,18 @@ int msplat_trainer_get_gaussians(MsplatTrainer t, float *means, float *scales, f
             if (dst[g]) std::memcpy(dst[g], h.a[g].data(), h.a[g].size() * 4);
         return 0;
     }, -2);
+}
+
+int msplat_trainer_set_learned_relocation(MsplatTrainer t, int enabled) {
+    if (!t) return -1;
+    return guard("learned_relocation", [&]() { TR(t)->enable_learned(enabled != 0); return 0; }, -2);
+}
+
+int msplat_trainer_learned_stats(MsplatTrainer t, float *last_loss, int *rounds) {
+    if (!t) return -1;
+    if (last_loss) *last_loss = TR(t)->lrn.last_loss;
+    if (rounds) *rounds = TR(t)->lrn.rounds;
+    return TR(t)->lrn.enabled ? 1 : 0;
 }
 
 int msplat_trainer_load_ply(MsplatTrainer t, const char *path) {

@@ -176,6 +176,7 @@ class Engine {
             pb.rest_m = st->exp_avg[4]; pb.rest_v = st->exp_avg_sq[4];
         }
         pb.nan_counts = pa.nan_counts;
+        pb.gstats = gstats_;
         launch_project_bwd(pb, stream_);
         debug_sync(stream_, "project_bwd");
         mark(6);
@@ -208,7 +209,7 @@ class Engine {
             key.flags = (args.do_optimizer ? 1 : 0) | (args.do_sgld ? 2 : 0) | (backward ? 4 : 0) | (st ? 8 : 0) |
                         (gt ? 16 : 0);   // the target and mask themselves come through StepParams
             key.ptr[0] = g.means; key.ptr[1] = g.scales; key.ptr[2] = g.quats; key.ptr[3] = g.features_dc;
-            key.ptr[4] = g.features_rest; key.ptr[5] = g.opacities;
+            key.ptr[4] = g.features_rest; key.ptr[5] = g.opacities; key.ptr[6] = gstats_;
             for (int k = 0; k < 6 && st; k++) { key.ptr[8 + k] = st->exp_avg[k]; key.ptr[14 + k] = st->exp_avg_sq[k]; }
             const std::string ks(reinterpret_cast<const char *>(&key), sizeof(key));
             auto it = graphs_.find(ks);
@@ -302,7 +303,7 @@ class Engine {
     }
 
     void mcmc(const MsplatGaussians &g, const MsplatAdamState &st, int cap_max, float cull_radius,
-              int &relocation_count, MsplatMcmcStats &out) {
+              int &relocation_count, MsplatMcmcStats &out, const float *score = nullptr) {
         CK(cudaSetDevice(device_));
         if (cap_max < g.num_points) throw std::runtime_error("cap_max below the active count");
         const size_t cap = (size_t)std::max(cap_max, 1);
@@ -328,6 +329,8 @@ class Engine {
         a.weights = ptr<double>("mcmc_weights"); a.cumw = ptr<double>("mcmc_cumw"); a.dpart = ptr<double>("mcmc_dpart");
         a.dead_list = ptr<int>("mcmc_dead"); a.moves = ptr<int>("mcmc_moves");
         a.counters = ptr<unsigned>("mcmc_counters");
+        a.score = score;
+        a.gstats = gstats_;
         McmcResult r;
         run_mcmc(a, cap_max, relocation_count, r, stream_);
         out.num_dead = r.num_dead; out.num_culled = r.num_culled; out.num_nonfinite = r.num_nonfinite;
@@ -534,6 +537,12 @@ class Engine {
     int slot_ = 0;
     long long timed_steps_ = 0, launches_ = 0;
     RasterArgs last_ra_{};   // raster arguments of the last eagerly issued step
+    float4 *gstats_ = nullptr;   // caller's activity statistics (learned relocation), or null
+
+  public:
+    void set_gstats(void *p) { gstats_ = static_cast<float4 *>(p); }
+
+  private:
 
     // captured steps, keyed by shapes, flags and every pointer they bake in
     struct GraphKey {
@@ -667,6 +676,16 @@ int msplat_engine_backward(MsplatEngine *e, const MsplatGaussians *g, const Mspl
                            const MsplatGradients *out) {
     if (!g || !args || !out) return -1;
     return guarded(e, [&] { e->impl->backward_image(*g, *args, v_img, *out); });
+}
+
+int msplat_engine_set_activity_stats(MsplatEngine *e, void *stats) {
+    return guarded(e, [&] { e->impl->set_gstats(stats); });
+}
+
+int msplat_engine_mcmc_scored(MsplatEngine *e, const MsplatGaussians *g, const MsplatAdamState *st, int cap_max,
+                              float cull_radius, int *relocation_count, const float *score, MsplatMcmcStats *out) {
+    if (!g || !st || !relocation_count || !out) return -1;
+    return guarded(e, [&] { e->impl->mcmc(*g, *st, cap_max, cull_radius, *relocation_count, *out, score); });
 }
 
 int msplat_engine_set_graphs(MsplatEngine *e, int enabled) {

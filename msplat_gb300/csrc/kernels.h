@@ -4,9 +4,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
-#include <cuda_bf16.h>
-
 #include "common.cuh"
+#include "mlp.h"
 
 namespace msplat {
 
@@ -85,6 +84,9 @@ struct ProjectBwdArgs {
     // gradient export (no optimizer): when set, the SH gradients and the
     // opacity-logit gradient are written here instead of feeding Adam
     float *v_dc_out, *v_rest_out, *v_opac_out;
+    // per-Gaussian activity statistics for the learned relocation proposal
+    // (or null): x += |dL/d(pixel centre)| and y += 1 when visible, z += 1
+    float4 *gstats;
     unsigned *nan_counts;
 };
 
@@ -108,6 +110,8 @@ struct McmcArgs {
     double *weights, *cumw, *dpart;
     int *dead_list, *moves;
     unsigned *counters;
+    const float *score;   // sampling weight per Gaussian in place of sigmoid(opacity), or null
+    float4 *gstats;       // activity statistics, cleared for every slot that receives a copy, or null
 };
 
 struct McmcResult {
@@ -121,20 +125,7 @@ void debug_sync(cudaStream_t s, const char *what);
 void launch_project_fwd(const ProjectArgs &a, cudaStream_t s);
 int launch_tiles(const TileArgs &a, int num_sms, cudaStream_t s);
 
-// ---- learned relocation proposal MLP (mlp.cu) ----
-// FP32 master parameters, flat: W1 [32][64] (rows past kMlpIn unused), b1 [64],
-// W2 [64][64], b2 [64], W3 [64][16] (columns past 2 unused), b3 [16]
-constexpr int kMlpIn = 22;
-constexpr int kMlpW1 = 0, kMlpB1 = 2048, kMlpW2 = 2112, kMlpB2 = 6208, kMlpW3 = 6272, kMlpB3 = 7296;
-constexpr int kMlpParams = 7312;
-// BF16 operand images (bytes): forward W1t, W2t, W3t; backward W2b, W3b
-constexpr int kImgW1t = 0, kImgW2t = 4096, kImgW3t = 12288, kImgW2b = 14336, kImgW3b = 22528, kImgBytes = 24576;
-void mlp_pack(const float *P, uint8_t *img, cudaStream_t s);
-void mlp_forward(const __nv_bfloat16 *X, int n, const uint8_t *img, const float *P, float2 *out, unsigned *err,
-                 cudaStream_t s);
-void mlp_train_batch(const __nv_bfloat16 *X, const float2 *T, int n, const uint8_t *img, const float *P, float *G,
-                     float *loss, unsigned *err, cudaStream_t s);
-void mlp_adam(float *P, float *G, float *M, float *V, float lr, int step, cudaStream_t s);   // returns the kernel launches
+   // returns the kernel launches
 size_t sort_pack_smem_bytes();
 size_t tile_cta_bins_bytes(int n, int num_tiles);   // 0 when the block-aggregated path is not used
 void launch_raster_fwd(const RasterArgs &a, cudaStream_t s);

@@ -9,7 +9,8 @@
 //  3. every dead slot draws a source with probability proportional to its
 //     weight (counter-based uniform + binary search in the cumulative
 //     weights; the reference's std::discrete_distribution over mt19937 is
-//     the same distribution, not the same stream);
+//     the same distribution, not the same stream).  The weight is
+//     sigmoid(opacity), or, with the learned proposal, the MLP's score;
 //  4. each drawn source with c copies is rescaled by Eq. 9 with n = c + 1
 //     and its Adam moments zeroed; then every dead slot copies its source
 //     and has its moments zeroed;
@@ -57,7 +58,8 @@ __global__ void k_mcmc_classify(McmcArgs a) {
         if (x * x + y * y + z * z > a.cull_r2) { dead = true; culled = true; }
     }
     a.flags[i] = dead ? 1u : 0u;
-    a.weights[i] = dead ? 0.0 : (finite_bits(sig) ? (double)sig : 0.0);
+    const float w = a.score ? a.score[i] : sig;
+    a.weights[i] = dead ? 0.0 : ((finite_bits(w) && w > 0.f) ? (double)w : 0.0);
     if (!fin) atomicAdd(a.counters + 0, 1u);
     if (culled) atomicAdd(a.counters + 1, 1u);
 }
@@ -67,7 +69,8 @@ __global__ void k_mcmc_weights(McmcArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     const float sig = 1.0f / (1.0f + expf(-a.opacities[i]));
-    a.weights[i] = finite_bits(sig) ? (double)sig : 0.0;
+    const float w = a.score ? a.score[i] : sig;
+    a.weights[i] = (finite_bits(w) && w > 0.f) ? (double)w : 0.0;
 }
 
 // ---- block scans (one level per launch; the partials are scanned by one CTA) ----
@@ -228,6 +231,7 @@ __global__ void k_mcmc_copy(McmcArgs a, int moves) {
     a.opacities[dst] = a.opacities[src];
     for (int k = 0; k < 3; k++) a.scales[3 * (size_t)dst + k] = a.scales[3 * (size_t)src + k];
     zero_moments(a, dst);
+    if (a.gstats) a.gstats[dst] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 static void ck(cudaError_t e, const char *what) {

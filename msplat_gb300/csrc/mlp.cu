@@ -406,7 +406,98 @@ void mlp_adam(float *P, float *G, float *M, float *V, float lr, int step, cudaSt
     k_mlp_adam<<<(kMlpParams + 255) / 256, 256, 0, s>>>(P, G, M, V, lr, bc1, bc2);
 }
 
+// ---------------------------------------------------------------------------
+// Features and training targets of the learned relocation proposal.
+// 22 inputs per Gaussian: mean (3), log-scale (3), unit quaternion (4),
+// opacity logit (1), SH DC (3), activity (2: log of the mean |dL/d centre|
+// while visible, visible fraction of its life), age (1, in kilo-steps), four
+// host-candidate descriptors (sigmoid(opacity), largest scale, distance from
+// the scene centre, log(1 + visible steps)) and the screen radius in the
+// last view (log).  Inputs 22..31 are zero.
+// ---------------------------------------------------------------------------
+
+constexpr float kActScale = 1e5f;   // gradient magnitudes of a normalised loss are ~1e-7..1e-4
+
+__global__ void k_mlp_features(MlpFeatArgs a) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= a.rows) return;
+    const int i = a.idx ? a.idx[r] : r;
+    float f[32];
+    for (int k = 0; k < 32; k++) f[k] = 0.f;
+    for (int k = 0; k < 3; k++) {
+        f[k] = a.means[3 * (size_t)i + k];
+        f[3 + k] = a.scales[3 * (size_t)i + k];
+        f[11 + k] = a.features_dc[3 * (size_t)i + k];
+    }
+    const float4 q = *reinterpret_cast<const float4 *>(a.quats + 4 * (size_t)i);
+    const float qn = rsqrtf(fmaxf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w, 1e-12f));
+    f[6] = q.x * qn; f[7] = q.y * qn; f[8] = q.z * qn; f[9] = q.w * qn;
+    const float o = a.opacities[i];
+    f[10] = o;
+    const float4 st = a.gstats ? a.gstats[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    f[14] = log1pf(kActScale * st.x / fmaxf(st.y, 1.f));
+    f[15] = st.y / fmaxf(st.z, 1.f);
+    f[16] = st.z * 1e-3f;
+    f[17] = 1.f / (1.f + __expf(-o));
+    f[18] = __expf(fmaxf(fmaxf(f[3], f[4]), f[5]));
+    f[19] = sqrtf(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+    f[20] = log1pf(st.y);
+    f[21] = a.radii ? log1pf((float)max(a.radii[i], 0)) : 0.f;   // screen radius of the last view
+    for (int k = 0; k < 32; k++) {
+        if (!finite_bits(f[k])) f[k] = 0.f;
+        f[k] = fminf(fmaxf(f[k], -64.f), 64.f);
+    }
+    uint4 *dst = reinterpret_cast<uint4 *>(a.X + (size_t)r * 32);
+    for (int k = 0; k < 4; k++) dst[k] = pack8(f + 8 * k);
+}
+
+__global__ void k_mlp_snapshot(const int *idx, int S, const float4 *gstats, float4 *snap) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < S) snap[s] = gstats[idx[s]];
+}
+
+__global__ void k_mlp_targets(const int *idx, const float4 *snap, int S, const float *opacities, const float4 *gstats,
+                              float2 *T) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    const int i = idx[s];
+    const float4 now = gstats[i], then = snap[s];
+    if (now.z < then.z) {   // the slot was cleared (relocated onto or regrown) since the snapshot
+        T[s] = make_float2(0.f, 0.f);
+        return;
+    }
+    const float sig = 1.f / (1.f + __expf(-opacities[i]));
+    const float vis = now.y - then.y;
+    const float act = vis > 0.f ? log1pf(kActScale * (now.x - then.x) / vis) : 0.f;
+    T[s] = make_float2(finite_bits(sig) ? sig : 0.f, finite_bits(act) ? act : 0.f);
+}
+
+// sampling weight: predicted opacity a window ahead, raised by predicted activity
+__global__ void k_mlp_scores(const float2 *y, int n, float *score) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float2 v = y[i];
+    const float o = fminf(fmaxf(v.x, 0.f), 1.f);
+    const float act = fminf(fmaxf(v.y, 0.f), 8.f);
+    score[i] = fmaxf(o * (1.f + 0.25f * act), 1e-6f);
+}
+
+void mlp_features(const MlpFeatArgs &a, cudaStream_t s) {
+    if (a.rows > 0) k_mlp_features<<<(a.rows + 255) / 256, 256, 0, s>>>(a);
+}
+void mlp_snapshot(const int *idx, int S, const float4 *gstats, float4 *snap, cudaStream_t s) {
+    if (S > 0) k_mlp_snapshot<<<(S + 255) / 256, 256, 0, s>>>(idx, S, gstats, snap);
+}
+void mlp_targets(const int *idx, const float4 *snap, int S, const float *opacities, const float4 *gstats, float2 *T,
+                 cudaStream_t s) {
+    if (S > 0) k_mlp_targets<<<(S + 255) / 256, 256, 0, s>>>(idx, snap, S, opacities, gstats, T);
+}
+void mlp_scores(const float2 *y, int n, float *score, cudaStream_t s) {
+    if (n > 0) k_mlp_scores<<<(n + 255) / 256, 256, 0, s>>>(y, n, score);
+}
+
 }  // namespace msplat
+
 
 // ---- C ABI of the MLP (device pointers; `stream` is a cudaStream_t or NULL) ----
 

@@ -63,6 +63,16 @@ __global__ void __launch_bounds__(256, 4) k_project_bwd(ProjectBwdArgs a) {
     if (i < a.n) {
         float *vmean = a.v_mean + 3 * (size_t)i, *vscale = a.v_scale + 3 * (size_t)i, *vquat = a.v_quat + 4 * (size_t)i;
         if (a.v_opac_out) a.v_opac_out[i] = a.radii[i] > 0 ? a.grad[i].a.z : 0.f;
+        if (a.gstats) {
+            float4 st = a.gstats[i];
+            st.z += 1.f;
+            if (a.radii[i] > 0) {
+                const float4 g0 = a.grad[i].a;
+                st.x += sqrtf(g0.x * g0.x + g0.y * g0.y);
+                st.y += 1.f;
+            }
+            a.gstats[i] = st;
+        }
         if (a.radii[i] <= 0) {
             vmean[0] = vmean[1] = vmean[2] = 0.f;
             vscale[0] = vscale[1] = vscale[2] = 0.f;

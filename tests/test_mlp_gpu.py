@@ -117,3 +117,30 @@ def test_mlp_training_reduces_loss():
     assert int(err.item()) == 0
     print(losses)
     assert losses[1] < 0.2 * losses[0]
+
+
+def test_learned_relocation_in_training():
+    """A short MCMC run with the learned proposal: the MLP trains on the run's
+    own pairs (snapshot at 500, labels and first training at 1000) and then
+    weights the relocation draws; the run stays finite and learns."""
+    pytest.importorskip("torch")
+    from msplat_gb300 import api as A
+    from msplat_gb300 import synthetic as S
+    from gpu_helpers import gt_image
+    gt = S.gaussians(3000, seed=31)
+    cams = S.ring_cameras(6, 96, 64, 80.0)
+    imgs = [gt_image(gt, c) for c in cams]
+    rng = np.random.default_rng(2)
+    xyz = (gt.means[:2000] + rng.normal(0, 0.03, (2000, 3))).astype(np.float32)
+    rgb = rng.integers(0, 256, (2000, 3), dtype=np.uint8)
+    ds = A.Dataset.from_arrays(cams, imgs, xyz, rgb, eval_mode=True, test_every=3)
+    cfg = A.TrainingConfig(iterations=1500, cap_max=6000, bg_color=[0.0, 0.0, 0.0])
+    t = A.GaussianTrainer(ds, cfg)
+    t.set_learned_relocation(True)
+    for _ in range(1200):
+        t.step()
+    st = t.learned_stats()
+    assert st["enabled"] and st["rounds"] >= 1 and np.isfinite(st["last_loss"]), st
+    assert t.splat_count > 2000                       # grew toward the cap
+    m = t.evaluate()
+    assert np.isfinite(m["psnr"]) and m["psnr"] > 15.0, m
