@@ -324,6 +324,26 @@ def run_engine(args):
            "max_tile_count": int(st.max_tile_count), "gpu_launches": int(launches), "e2e": e2e,
            "cuda_graph": True,
            "clocks": clk.summary()}
+    if rank == 0 and not args.no_time_to_psnr:
+        # the metric's second half: learned vs plain relocation, time to PSNR
+        # (small synthetic scene, one seed; msplat_gb300.relocation_ab)
+        try:
+            from msplat_gb300 import relocation_ab as AB
+            cams_ab, imgs_ab, xyz_ab, col_ab = AB._scene(0)
+            plain = AB.run_arm(cams_ab, imgs_ab, xyz_ab, col_ab, False, 6000, 250)
+            learned = AB.run_arm(cams_ab, imgs_ab, xyz_ab, col_ab, True, 6000, 250)
+            target = plain["final_psnr"] - 0.1
+            _, tp = AB.time_to(plain["curve"], target)
+            _, tl = AB.time_to(learned["curve"], target)
+            out["time_to_psnr"] = {
+                "workload": "16,384-Gaussian synthetic scene, 8 train + 4 held-out views at 256x256, MCMC cap "
+                            "32,768, 6000 iterations, seed 0",
+                "target_psnr": target, "plain_s": tp, "learned_s": tl,
+                "ratio": (tl / tp) if (tl is not None and tp) else None,
+                "plain_final_psnr": plain["final_psnr"], "learned_final_psnr": learned["final_psnr"],
+                "proposal_rounds": learned["proposal"]["rounds"]}
+        except Exception as ex:   # reported, never fatal to the throughput line
+            out["time_to_psnr"] = {"error": str(ex)[:200]}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         cd = cams[0]
         out["cpu_baseline"] = cpu_baseline(model, cd, gts_host[0].numpy(), steps=args.cpu_steps)
@@ -343,6 +363,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-time-to-psnr", action="store_true",
+                    help="skip the learned-vs-plain relocation time-to-PSNR runs")
     ap.add_argument("--gaussians", type=int, default=N_MODEL,
                     help="trained Gaussians (default 1M; smaller only for profiling captures)")
     args = ap.parse_args()
