@@ -93,6 +93,9 @@ def lib(build_if_missing: bool = True):
                                          C.c_float, C.POINTER(C.c_int), C.POINTER(MsplatMcmcStats)]
         L.msplat_engine_marker.argtypes = [vp, C.c_int]
         L.msplat_engine_set_graphs.argtypes = [vp, C.c_int]
+        L.msplat_engine_train_step_batch.argtypes = [vp, C.POINTER(MsplatGaussians), C.POINTER(MsplatAdamState),
+                                                     C.POINTER(MsplatStepArgs), C.c_int, C.POINTER(vp),
+                                                     C.POINTER(vp)]
         L.msplat_engine_backward.argtypes = [vp, C.POINTER(MsplatGaussians), C.POINTER(MsplatStepArgs), vp,
                                              C.POINTER(MsplatGradients)]
         L.msplat_engine_marker_elapsed.argtypes = [vp, FP]

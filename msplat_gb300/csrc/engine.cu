@@ -10,6 +10,7 @@
 #include <set>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "kernels.h"
 #include "msplat_engine.h"
@@ -78,6 +79,7 @@ class Engine {
         if (K > 1) ensure_chunks((long long)K * P);
         last_T_ = T;
         last_K_ = K;
+        last_batch_P_.clear();
         if (timing_) slot_ = (timed_steps_++) % kRing;
         // kernels of this step: projection, count/scan/scatter/sort, raster
         // (+ merge when chunked), and for training 3 loss passes, raster
@@ -260,6 +262,207 @@ class Engine {
         train_step(g, st, args, ptr<uint8_t>("gt_stage"), mask_d, true);
     }
 
+    // Multi-view step: B views (any sizes) rendered and back-propagated one
+    // after another on the stream, their gradients averaged (each view's
+    // image gradient is scaled by 1/B), then one optimizer update: the
+    // 4-group Adam with the regularizer, the SH Adam over the coefficients of
+    // Gaussians visible in any view, and SGLD.  Scalars of the optimizer come
+    // from args[0].  In graph mode the whole batch is one captured graph.
+    void train_step_batch(const MsplatGaussians &g, const MsplatAdamState &st, const MsplatStepArgs *args, int B,
+                          const uint8_t *const *gts, const uint8_t *const *masks) {
+        CK(cudaSetDevice(device_));
+        if (B <= 0) throw std::runtime_error("batch of no views");
+        if (B == 1) {
+            train_step(g, &st, args[0], gts[0], masks ? masks[0] : nullptr, true);
+            return;
+        }
+        const int N = g.num_points;
+        struct View { int W, H, tx, ty, T, K; long long P; };
+        std::vector<View> vw(B);
+        const long long cap = std::max<long long>(48LL * N, 1);
+        int maxT = 1;
+        long long maxP = 1, maxKP = 0;
+        for (int v = 0; v < B; v++) {
+            validate(g, args[v]);
+            if (!gts[v]) throw std::runtime_error("multi-view step without a target image");
+            View &w = vw[v];
+            w.W = args[v].width; w.H = args[v].height;
+            w.tx = (w.W + kTile - 1) / kTile; w.ty = (w.H + kTile - 1) / kTile; w.T = w.tx * w.ty;
+            w.P = (long long)w.W * w.H;
+            w.K = choose_k(args[v], w.T, cap);
+            maxT = std::max(maxT, w.T);
+            maxP = std::max(maxP, w.P);
+            if (w.K > 1) maxKP = std::max(maxKP, (long long)w.K * w.P);
+        }
+        ensure_points(N);
+        ensure_tiles(maxT);
+        ensure_isect(cap);
+        ensure_pixels(maxP);
+        if (maxKP) ensure_chunks(maxKP);
+        const size_t cb = tile_cta_bins_bytes(N, maxT);
+        if (cb) alloc("cta_bins", cb);
+        alloc("params_batch", sizeof(StepParams) * (size_t)B);
+        alloc("loss_batch", sizeof(float) * (size_t)B);
+        const size_t rb = (size_t)3 * g.rest_bases;
+        alloc("acc_opac", 4 * (size_t)std::max(N, 1));
+        alloc("acc_dc", 12 * (size_t)std::max(N, 1));
+        alloc("acc_rest", 4 * rb * (size_t)std::max(N, 1) + 16);
+        alloc("acc_vis", (size_t)std::max(N, 1) + 16);
+        std::vector<StepParams> sps(B);
+        for (int v = 0; v < B; v++) {
+            fill_params(args[v], sps[v], masks && masks[v]);
+            sps[v].gt = gts[v];
+            sps[v].mask = masks ? masks[v] : nullptr;
+            sps[v].loss_inv_n = args[v].loss_inv_n / (float)B;
+        }
+        CK(cudaMemcpyAsync(ptr<StepParams>("params_batch"), sps.data(), sizeof(StepParams) * B,
+                           cudaMemcpyHostToDevice, stream_));
+        last_batch_P_.assign(B, 0);
+        for (int v = 0; v < B; v++) last_batch_P_[v] = vw[v].P;
+        last_T_ = vw[B - 1].T;
+        last_K_ = vw[B - 1].K;
+        last_P_ = vw[B - 1].P;
+
+        auto issue = [&]() {
+            StepParams *spb = ptr<StepParams>("params_batch");
+            CK(cudaMemsetAsync(ptr<float>("loss_batch"), 0, sizeof(float) * B, stream_));
+            CK(cudaMemsetAsync(ptr<float>("v_mean"), 0, 12 * (size_t)N, stream_));
+            CK(cudaMemsetAsync(ptr<float>("v_scale"), 0, 12 * (size_t)N, stream_));
+            CK(cudaMemsetAsync(ptr<float>("v_quat"), 0, 16 * (size_t)N, stream_));
+            CK(cudaMemsetAsync(ptr<float>("acc_opac"), 0, 4 * (size_t)N, stream_));
+            CK(cudaMemsetAsync(ptr<float>("acc_dc"), 0, 12 * (size_t)N, stream_));
+            if (rb) CK(cudaMemsetAsync(ptr<float>("acc_rest"), 0, 4 * rb * (size_t)N, stream_));
+            CK(cudaMemsetAsync(ptr<uint8_t>("acc_vis"), 0, (size_t)N, stream_));
+            for (int v = 0; v < B; v++) {
+                const View &w = vw[v];
+                const StepParams *sp = spb + v;
+                CK(cudaMemsetAsync(ptr<uint32_t>("tile_counts"), 0, sizeof(uint32_t) * 2 * (size_t)w.T, stream_));
+                ProjectArgs pa{};
+                pa.n = N; pa.rest_bases = g.rest_bases; pa.tiles_x = w.tx; pa.tiles_y = w.ty;
+                pa.Wf = (float)w.W; pa.Hf = (float)w.H;
+                pa.means = g.means; pa.scales = g.scales; pa.quats = g.quats;
+                pa.features_dc = g.features_dc; pa.features_rest = g.features_rest; pa.opacities = g.opacities;
+                pa.sp = sp;
+                pa.rec = ptr<SplatRec>("rec"); pa.depths = ptr<float>("depths"); pa.radii = ptr<int>("radii");
+                pa.aabb = ptr<float2>("aabb"); pa.tiles_hit = ptr<int>("tiles_hit");
+                pa.grad = ptr<GradRec>("grad");
+                pa.nan_counts = ptr<unsigned>("nan_counts");
+                launch_project_fwd(pa, stream_);
+                launches_ += 1;
+                TileArgs ta{};
+                ta.n = N; ta.tiles_x = w.tx; ta.tiles_y = w.ty; ta.num_tiles = w.T; ta.capacity = cap;
+                ta.radii = pa.radii; ta.depths = pa.depths; ta.rec = pa.rec; ta.aabb = pa.aabb;
+                ta.tile_counts = ptr<uint32_t>("tile_counts"); ta.tile_write = ta.tile_counts + w.T;
+                ta.tile_offsets = ptr<uint32_t>("tile_offsets"); ta.max_tile_count = ptr<uint32_t>("max_tile");
+                ta.keys = ptr<uint64_t>("keys"); ta.keys_alt = ptr<uint64_t>("keys_alt");
+                ta.isect_ids = ptr<uint32_t>("isect_ids"); ta.nan_counts = pa.nan_counts;
+                ta.cta_bins = cb ? ptr<uint32_t>("cta_bins") : nullptr;
+                ta.tile_lists = ptr<uint32_t>("tile_lists"); ta.tile_class = ptr<uint32_t>("tile_class");
+                launches_ += launch_tiles(ta, num_sms_, stream_);
+                RasterArgs ra{};
+                ra.width = w.W; ra.height = w.H; ra.tiles_x = w.tx; ra.num_tiles = w.T; ra.k_max = w.K;
+                ra.capacity = cap; ra.sp = sp; ra.tile_offsets = ta.tile_offsets; ra.isect_ids = ta.isect_ids;
+                ra.n = N; ra.rec = pa.rec;
+                ra.out_img = ptr<float>("out_img"); ra.final_T = ptr<float>("final_T"); ra.final_idx = ptr<int>("final_idx");
+                if (w.K > 1) {
+                    ra.chunk_T = ptr<float>("chunk_T"); ra.chunk_C = ptr<float>("chunk_C");
+                    ra.chunk_idx = ptr<int>("chunk_idx");
+                    ra.prefix_T = ptr<float>("prefix_T"); ra.after_C = ptr<float>("after_C");
+                }
+                ra.v_img = ptr<float>("v_img"); ra.grad = ptr<GradRec>("grad"); ra.nan_counts = pa.nan_counts;
+                launch_raster_fwd(ra, stream_);
+                LossArgs la{};
+                la.width = w.W; la.height = w.H; la.sp = sp; la.img = ra.out_img;
+                la.gt = nullptr; la.mask = nullptr;
+                la.hbuf = ptr<float>("hbuf"); la.dbuf = ptr<float>("dbuf"); la.v_img = ptr<float>("v_img");
+                la.loss_sum = ptr<float>("loss_batch") + v; la.nan_counts = pa.nan_counts;
+                launch_loss(la, stream_);
+                launch_raster_bwd(ra, stream_);
+                launches_ += (w.K > 1 ? 2 : 1) * 2 + 3;
+                ProjectBwdArgs pb{};
+                pb.n = N; pb.rest_bases = g.rest_bases; pb.do_optimizer = 0;
+                pb.Wf = (float)w.W; pb.Hf = (float)w.H; pb.sp = sp;
+                pb.means = g.means; pb.scales = g.scales; pb.quats = g.quats; pb.radii = pa.radii; pb.rec = pa.rec;
+                pb.grad = ra.grad;
+                pb.v_mean = ptr<float>("v_mean"); pb.v_scale = ptr<float>("v_scale"); pb.v_quat = ptr<float>("v_quat");
+                pb.features_dc = g.features_dc; pb.features_rest = g.features_rest;
+                pb.accumulate = 1;
+                pb.acc_opac = ptr<float>("acc_opac"); pb.acc_dc = ptr<float>("acc_dc");
+                pb.acc_rest = ptr<float>("acc_rest"); pb.acc_vis = ptr<uint8_t>("acc_vis");
+                pb.gstats = gstats_;
+                pb.nan_counts = pa.nan_counts;
+                launch_project_bwd(pb, stream_);
+                launches_ += 1;
+            }
+            AdamArgs aa{};
+            aa.n = N; aa.sp = spb;
+            aa.means = g.means; aa.scales = g.scales; aa.quats = g.quats; aa.opacities = g.opacities;
+            const int grp[4] = {0, 1, 2, 5};
+            for (int k = 0; k < 4; k++) { aa.m[k] = st.exp_avg[grp[k]]; aa.v[k] = st.exp_avg_sq[grp[k]]; }
+            aa.dc_v = st.exp_avg_sq[3];
+            aa.g_mean = ptr<float>("v_mean"); aa.g_scale = ptr<float>("v_scale"); aa.g_quat = ptr<float>("v_quat");
+            aa.grad = ptr<GradRec>("grad"); aa.g_opac = ptr<float>("acc_opac");
+            aa.nan_counts = ptr<unsigned>("nan_counts");
+            if (args[0].do_optimizer) {
+                launch_adam(aa, num_sms_, stream_);
+                ShAdamArgs sa{};
+                sa.n = N; sa.rest_bases = g.rest_bases; sa.sp = spb;
+                sa.features_dc = g.features_dc; sa.features_rest = g.features_rest;
+                sa.dc_m = st.exp_avg[3]; sa.dc_v = st.exp_avg_sq[3]; sa.rest_m = st.exp_avg[4]; sa.rest_v = st.exp_avg_sq[4];
+                sa.acc_dc = ptr<float>("acc_dc"); sa.acc_rest = ptr<float>("acc_rest"); sa.acc_vis = ptr<uint8_t>("acc_vis");
+                sa.nan_counts = aa.nan_counts;
+                launch_sh_adam(sa, stream_);
+                launches_ += 2;
+            }
+            if (args[0].do_sgld) {
+                launch_sgld(aa, stream_);
+                launches_ += 1;
+            }
+            CK(cudaGetLastError());
+        };
+
+        const bool graphable = use_graphs_ && !timing_ && !g_sync_check;
+        if (graphable) {
+            std::string ks = "batch";
+            auto put = [&](const void *p, size_t n) { ks.append(reinterpret_cast<const char *>(p), n); };
+            put(&N, 4); put(&B, 4);
+            for (int v = 0; v < B; v++) put(&vw[v], sizeof(View));
+            const int fl = (args[0].do_optimizer ? 1 : 0) | (args[0].do_sgld ? 2 : 0) | (g.rest_bases << 4);
+            put(&fl, 4);
+            const void *ps[20] = {g.means, g.scales, g.quats, g.features_dc, g.features_rest, g.opacities, gstats_};
+            for (int k = 0; k < 6; k++) { ps[8 + k] = st.exp_avg[k]; ps[14 + k] = st.exp_avg_sq[k]; }
+            put(ps, sizeof(ps));
+            auto it = graphs_.find(ks);
+            if (it != graphs_.end()) {
+                CK(cudaGraphLaunch(it->second.exec, stream_));
+                launches_ += it->second.launches;
+                return;
+            }
+            if (graph_seen_.count(ks) && graphs_.size() < kMaxGraphs) {
+                const long long l0 = launches_;
+                cudaGraph_t graph = nullptr;
+                CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+                try {
+                    issue();
+                } catch (...) {
+                    cudaStreamEndCapture(stream_, &graph);
+                    if (graph) cudaGraphDestroy(graph);
+                    throw;
+                }
+                CK(cudaStreamEndCapture(stream_, &graph));
+                cudaGraphExec_t exec = nullptr;
+                const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+                cudaGraphDestroy(graph);
+                CK(ie);
+                graphs_[ks] = GraphEntry{exec, launches_ - l0};
+                CK(cudaGraphLaunch(exec, stream_));
+                return;
+            }
+            graph_seen_.insert(ks);
+        }
+        issue();
+    }
+
     // dL/d(parameters) for a caller-supplied dL/d(image): the forward is run
     // again (projection, tile lists, raster) rather than kept from an
     // earlier call, then the raster and projection backward passes write
@@ -340,6 +543,15 @@ class Engine {
     void synchronize() { CK(cudaStreamSynchronize(stream_)); }
 
     float loss() {
+        if (!last_batch_P_.empty()) {   // multi-view step: mean of the views' losses
+            std::vector<float> v(last_batch_P_.size());
+            CK(cudaMemcpyAsync(v.data(), ptr<float>("loss_batch"), sizeof(float) * v.size(), cudaMemcpyDeviceToHost,
+                               stream_));
+            synchronize();
+            double acc = 0;
+            for (size_t k = 0; k < v.size(); k++) acc += (double)v[k] / (double)last_batch_P_[k];
+            return (float)(acc / (double)v.size());
+        }
         float v = 0;
         CK(cudaMemcpyAsync(&v, ptr<float>("loss_sum"), sizeof(float), cudaMemcpyDeviceToHost, stream_));
         synchronize();
@@ -537,6 +749,7 @@ class Engine {
     int slot_ = 0;
     long long timed_steps_ = 0, launches_ = 0;
     RasterArgs last_ra_{};   // raster arguments of the last eagerly issued step
+    std::vector<long long> last_batch_P_;   // pixel counts of the last multi-view step's views
     float4 *gstats_ = nullptr;   // caller's activity statistics (learned relocation), or null
 
   public:
@@ -676,6 +889,13 @@ int msplat_engine_backward(MsplatEngine *e, const MsplatGaussians *g, const Mspl
                            const MsplatGradients *out) {
     if (!g || !args || !out) return -1;
     return guarded(e, [&] { e->impl->backward_image(*g, *args, v_img, *out); });
+}
+
+int msplat_engine_train_step_batch(MsplatEngine *e, const MsplatGaussians *g, const MsplatAdamState *st,
+                                   const MsplatStepArgs *args, int num_views, const uint8_t *const *gt,
+                                   const uint8_t *const *mask) {
+    if (!g || !st || !args || !gt || num_views <= 0) return -1;
+    return guarded(e, [&] { e->impl->train_step_batch(*g, *st, args, num_views, gt, mask); });
 }
 
 int msplat_engine_set_activity_stats(MsplatEngine *e, void *stats) {

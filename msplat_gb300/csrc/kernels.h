@@ -87,6 +87,11 @@ struct ProjectBwdArgs {
     // per-Gaussian activity statistics for the learned relocation proposal
     // (or null): x += |dL/d(pixel centre)| and y += 1 when visible, z += 1
     float4 *gstats;
+    // multi-view accumulation (no optimizer): v_mean / v_scale / v_quat and
+    // the buffers below are added to for the Gaussians visible in this view
+    int accumulate;
+    float *acc_opac, *acc_dc, *acc_rest;   // [N], [N,3], [N,rest,3]
+    uint8_t *acc_vis;                      // 1 once visible in any view
     unsigned *nan_counts;
 };
 
@@ -98,6 +103,19 @@ struct AdamArgs {
     const float *g_mean, *g_scale, *g_quat;
     const GradRec *grad;         // opacity gradient in grad[i].a.z
     const float *dc_v;           // features_dc second moment (regularizer duty)
+    const float *g_opac;         // opacity gradient [N] in place of grad[i].a.z, or null
+    unsigned *nan_counts;
+};
+
+// Adam on the SH groups from accumulated gradients (multi-view steps): the
+// elements of Gaussians visible in at least one view, bands below
+// degrees_to_use (the fused per-view SH Adam's rule over the union)
+struct ShAdamArgs {
+    int n, rest_bases;
+    const StepParams *sp;
+    float *features_dc, *features_rest, *dc_m, *dc_v, *rest_m, *rest_v;
+    const float *acc_dc, *acc_rest;
+    const uint8_t *acc_vis;
     unsigned *nan_counts;
 };
 
@@ -134,6 +152,7 @@ void launch_raster_bwd(const RasterArgs &a, cudaStream_t s);
 void launch_project_bwd(const ProjectBwdArgs &a, cudaStream_t s);
 void launch_adam(const AdamArgs &a, int num_sms, cudaStream_t s);
 void launch_sgld(const AdamArgs &a, cudaStream_t s);
+void launch_sh_adam(const ShAdamArgs &a, cudaStream_t s);
 void run_mcmc(McmcArgs a, int cap_max, int &relocation_count, McmcResult &res, cudaStream_t s);
 
 }  // namespace msplat

@@ -59,7 +59,7 @@ __global__ void __launch_bounds__(256, 4) k_project_bwd(ProjectBwdArgs a) {
     ShStage &sh = stage[wid];
     const StepParams &sp = *a.sp;
     sh.vc[lane] = make_float4(0.f, 0.f, 0.f, 0.f);   // w = 0: nothing to update
-    const bool want_sh = a.do_optimizer || a.v_dc_out;
+    const bool want_sh = a.do_optimizer || a.v_dc_out || a.accumulate;
     if (i < a.n) {
         float *vmean = a.v_mean + 3 * (size_t)i, *vscale = a.v_scale + 3 * (size_t)i, *vquat = a.v_quat + 4 * (size_t)i;
         if (a.v_opac_out) a.v_opac_out[i] = a.radii[i] > 0 ? a.grad[i].a.z : 0.f;
@@ -74,10 +74,16 @@ __global__ void __launch_bounds__(256, 4) k_project_bwd(ProjectBwdArgs a) {
             a.gstats[i] = st;
         }
         if (a.radii[i] <= 0) {
-            vmean[0] = vmean[1] = vmean[2] = 0.f;
-            vscale[0] = vscale[1] = vscale[2] = 0.f;
-            *reinterpret_cast<float4 *>(vquat) = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (!a.accumulate) {
+                vmean[0] = vmean[1] = vmean[2] = 0.f;
+                vscale[0] = vscale[1] = vscale[2] = 0.f;
+                *reinterpret_cast<float4 *>(vquat) = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
         } else {
+            if (a.accumulate) {
+                a.acc_opac[i] += a.grad[i].a.z;
+                a.acc_vis[i] = 1;
+            }
             const GradRec gr = a.grad[i];
             const SplatRec rec = a.rec[i];
             const float px = a.means[3 * i], py = a.means[3 * i + 1], pz = a.means[3 * i + 2];
@@ -168,7 +174,11 @@ __global__ void __launch_bounds__(256, 4) k_project_bwd(ProjectBwdArgs a) {
             const float vt2 = -fxr * vJ00 + 2.f * sp.fx * cvx * rz3 * vJ02 - fyr * vJ11 + 2.f * sp.fy * cvy * rz3 * vJ12;
 #pragma unroll
             for (int c = 0; c < 3; c++) vm[c] += vt0 * v[c] + vt1 * v[4 + c] + vt2 * v[8 + c];
-            vmean[0] = vm[0]; vmean[1] = vm[1]; vmean[2] = vm[2];
+            if (a.accumulate) {
+                vmean[0] += vm[0]; vmean[1] += vm[1]; vmean[2] += vm[2];
+            } else {
+                vmean[0] = vm[0]; vmean[1] = vm[1]; vmean[2] = vm[2];
+            }
 
             // scale_rot_to_cov3d_vjp + quat_to_rotmat_vjp
             const float v01 = 0.5f * (vV[0][1] + vV[1][0]), v02 = 0.5f * (vV[0][2] + vV[2][0]);
@@ -184,7 +194,7 @@ __global__ void __launch_bounds__(256, 4) k_project_bwd(ProjectBwdArgs a) {
                     acc += R[r][c] * vMrc;
                     gR[r][c] = vMrc * s[c];
                 }
-                vscale[c] = acc * s[c];
+                vscale[c] = a.accumulate ? vscale[c] + acc * s[c] : acc * s[c];
             }
             // gR[row][col]; the reference indexes v_R[col][row]
             float4 vq;
@@ -195,6 +205,10 @@ __global__ void __launch_bounds__(256, 4) k_project_bwd(ProjectBwdArgs a) {
                           w * (gR[0][2] - gR[2][0]));
             vq.w = 2.f * (x * (gR[2][0] + gR[0][2]) + y * (gR[2][1] + gR[1][2]) - 2.f * z * (gR[0][0] + gR[1][1]) +
                           w * (gR[1][0] - gR[0][1]));
+            if (a.accumulate) {
+                const float4 o = *reinterpret_cast<const float4 *>(vquat);
+                vq.x += o.x; vq.y += o.y; vq.z += o.z; vq.w += o.w;
+            }
             *reinterpret_cast<float4 *>(vquat) = vq;
 
             // SH VJP inputs for the fused Adam (or the gradient export) below
@@ -233,6 +247,23 @@ __global__ void __launch_bounds__(256, 4) k_project_bwd(ProjectBwdArgs a) {
     const int i0 = (blockIdx.x * blockDim.x) + wid * 32;
     if (i0 >= a.n) return;
     const int ng = min(32, a.n - i0);
+    if (a.accumulate) {
+        // add dL/d(SH coefficient) of the active elements into the accumulators
+        for (int e = lane; e < 3 * ng; e += 32) {
+            const int gi = e / 3, c = e - 3 * gi;
+            const float4 vc = sh.vc[gi];
+            if (__float_as_int(vc.w) > 0)
+                a.acc_dc[3 * (size_t)i0 + e] += sh.bas[gi][15] * (c == 0 ? vc.x : c == 1 ? vc.y : vc.z);
+        }
+        const int rowf = 3 * a.rest_bases;
+        for (int e = lane; e < rowf * ng; e += 32) {
+            const int gi = e / rowf, r = e - rowf * gi, band = r / 3, c = r - 3 * band;
+            const float4 vc = sh.vc[gi];
+            if (band < __float_as_int(vc.w) - 1)
+                a.acc_rest[(size_t)rowf * i0 + e] += sh.bas[gi][band] * (c == 0 ? vc.x : c == 1 ? vc.y : vc.z);
+        }
+        return;
+    }
     if (a.v_dc_out) {
         // export: dL/d(SH coefficient) = basis value x colour gradient, zero
         // where Adam would not update (culled, non-finite, band not in use)

@@ -156,6 +156,15 @@ class Engine:
         self._check(self.L.msplat_engine_train_step(self.h, C.byref(g), C.byref(st), C.byref(args), gt_ptr,
                                                     mask_ptr or None))
 
+    def train_step_batch(self, dg: DeviceGaussians, args: list, gt_ptrs: list, mask_ptrs: list | None = None):
+        """One optimizer update from the mean gradient of several views (any sizes)."""
+        g, st = dg.native()
+        n = len(args)
+        arr = (N.MsplatStepArgs * n)(*args)
+        gts = (C.c_void_p * n)(*gt_ptrs)
+        masks = (C.c_void_p * n)(*(mask_ptrs or [None] * n)) if mask_ptrs else None
+        self._check(self.L.msplat_engine_train_step_batch(self.h, C.byref(g), C.byref(st), arr, n, gts, masks))
+
     def train_step_host(self, dg: DeviceGaussians, args: N.MsplatStepArgs, gt_host_ptr: int,
                         mask_host_ptr: int | None = None):
         g, st = dg.native()
