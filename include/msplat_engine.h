@@ -167,23 +167,28 @@ typedef struct {
 int msplat_engine_backward(MsplatEngine *e, const MsplatGaussians *g, const MsplatStepArgs *args, const float *v_img,
                            const MsplatGradients *out);
 
-/* Multi-view training step: num_views views (each with its own camera and
- * size in args[v], target gt[v], mask mask[v] or NULL; mask may be NULL for
- * none) rendered and back-propagated, the image gradients scaled by
- * 1/num_views so the parameter gradients are the views' mean, then one
- * optimizer update: the 4-group Adam with the regularizer, an SH Adam over
- * the coefficients of Gaussians visible in at least one view (bands below
- * degrees_to_use), and SGLD; optimizer scalars from args[0].
- * msplat_engine_loss then returns the mean of the views' losses.  With one
- * view this is msplat_engine_train_step.  Graph mode captures the batch. */
+/* Multi-view training step: num_views (1..16) views, each with its own
+ * camera and size in args[v], target gt[v] and mask mask[v] (mask may be
+ * NULL for none), rendered and back-propagated by the same launches as one
+ * view: every stage (projection, tile mapping, raster, loss, raster
+ * backward, projection backward) is one launch over all views.  Each view's
+ * image gradient is scaled by 1/num_views, so the parameter gradients are the
+ * views' mean; then one optimizer update: the 4-group Adam with the
+ * regularizer, the SH Adam over the coefficients of Gaussians visible in at
+ * least one view (bands below degrees_to_use), and SGLD; optimizer scalars
+ * and raster mode from args[0].  The engine's record buffers (rec, depths,
+ * radii, grad) are then [num_views, num_points] and its image buffers the
+ * views' images one after another.  msplat_engine_loss returns the mean of
+ * the views' losses.  With one view this is msplat_engine_train_step.  Graph
+ * mode captures the batch. */
 int msplat_engine_train_step_batch(MsplatEngine *e, const MsplatGaussians *g, const MsplatAdamState *st,
                                    const MsplatStepArgs *args, int num_views, const uint8_t *const *gt,
                                    const uint8_t *const *mask);
 
 /* Learned relocation proposal support.  `stats` (device float4 per
  * Gaussian, cap-sized, caller-owned, zeroed by the caller; NULL to stop)
- * accumulates per training step: x += |dL/d(pixel centre)| and y += 1 when
- * the Gaussian is visible, z += 1 (age).  MCMC clears the entry of every
+ * accumulates per training step, for each view in which the Gaussian is
+ * visible: x += |dL/d(pixel centre)| and y += 1; and z += 1 (age).  MCMC clears the entry of every
  * slot it fills with a copy. */
 int msplat_engine_set_activity_stats(MsplatEngine *e, void *stats);
 

@@ -95,6 +95,14 @@ int msplat_trainer_set_learned_relocation(MsplatTrainer t, int enabled);
  * returns 1 when the proposal is enabled, 0 when not, -1 on a bad handle. */
 int msplat_trainer_learned_stats(MsplatTrainer t, float *last_loss, int *rounds);
 
+/* Views per optimizer step (no counterpart in the reference; default 1).
+ * With num_views > 1 each msplat_trainer_step renders the next num_views
+ * cameras of the shuffled order and applies one update from the mean of
+ * their gradients (msplat_engine_train_step_batch); the step counter, the
+ * schedules and MCMC still advance once per step.  Returns 0, or -1 on a
+ * bad handle or num_views < 1. */
+int msplat_trainer_set_batch_views(MsplatTrainer t, int num_views);
+
 /* Replaces the trainer's Gaussians with a trained PLY (Model::loadPly, the
  * CLI's --resume); optimizer state starts fresh.  Returns the iteration
  * recorded in the file, or a negative code. */

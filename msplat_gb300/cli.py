@@ -69,6 +69,10 @@ def parse(argv=None):
     p.add_argument("--early-stop", type=float, default=0.0,
                    help="stop when test-subset PSNR improves less than this (dB) over 5000 steps (needs --eval)")
     p.add_argument("--log-every", type=int, default=100, help="print progress every N steps")
+    p.add_argument("--batch-views", type=int, default=1,
+                   help="cameras per optimizer step (mean gradient; 1 = one camera per step)")
+    p.add_argument("--learned-relocation", action="store_true",
+                   help="weight MCMC relocation sources by the online-trained proposal MLP")
     a = p.parse_args(argv)
     a.downscale_factor = max(a.downscale_factor, 1.0)
     return a
@@ -94,6 +98,10 @@ def main(argv=None) -> int:
                            keep_crs=a.keep_crs, downscale_factor=a.downscale_factor, bg_color=list(a.bg_color),
                            output=a.output, save_every=a.save_every)
     trainer = A.GaussianTrainer(ds, cfg)
+    if a.batch_views > 1:
+        trainer.set_batch_views(a.batch_views)
+    if a.learned_relocation:
+        trainer.set_learned_relocation(True)
     if a.resume:
         step0 = trainer.load_ply(a.resume)
         print(f"Resumed from {a.resume} at step {step0}", flush=True)

@@ -385,6 +385,7 @@ struct TrainerImpl {
     size_t cam_pos = 0;
     std::mt19937 rng{42};
     float last_loss = 0.f;
+    int batch_views = 1;   // views per optimizer step (1 = the reference's one-camera step)
 
     // learned relocation proposal (off unless enabled): activity statistics
     // accumulated by the step, an MLP trained online every `window` steps on
@@ -643,14 +644,29 @@ struct TrainerImpl {
         const auto t0 = std::chrono::high_resolution_clock::now();
         current_step++;
         if (ds->train.empty()) throw std::runtime_error("dataset has no training cameras");
-        HostCamera &cam = ds->train[next_camera()];
-        cam.upload();
         adam_step_count++;
-        MsplatStepArgs a;
-        step_args(cam, current_step, a, true);
         MsplatGaussians g = model.gaussians();
         MsplatAdamState st = model.adam();
-        check(msplat_engine_train_step(eng, &g, &st, &a, cam.d_image, cam.d_mask), "train step");
+        if (batch_views <= 1) {
+            HostCamera &cam = ds->train[next_camera()];
+            cam.upload();
+            MsplatStepArgs a;
+            step_args(cam, current_step, a, true);
+            check(msplat_engine_train_step(eng, &g, &st, &a, cam.d_image, cam.d_mask), "train step");
+        } else {
+            // the next batch_views cameras of the shuffled order: one update from their mean gradient
+            const int B = batch_views;
+            std::vector<MsplatStepArgs> a(B);
+            std::vector<const uint8_t *> gt(B), mk(B);
+            for (int v = 0; v < B; v++) {
+                HostCamera &cam = ds->train[next_camera()];
+                cam.upload();
+                step_args(cam, current_step, a[v], true);
+                gt[v] = cam.d_image;
+                mk[v] = cam.d_mask;
+            }
+            check(msplat_engine_train_step_batch(eng, &g, &st, a.data(), B, gt.data(), mk.data()), "batch step");
+        }
         learned_after_step(current_step);
         // schedulersStep (model.cpp:256-261)
         const float t = std::clamp((float)current_step / (float)position_lr_max_steps, 0.f, 1.f);
@@ -1219,6 +1235,12 @@ int msplat_trainer_get_gaussians(MsplatTrainer t, float *means, float *scales, f
 int msplat_trainer_set_learned_relocation(MsplatTrainer t, int enabled) {
     if (!t) return -1;
     return guard("learned_relocation", [&]() { TR(t)->enable_learned(enabled != 0); return 0; }, -2);
+}
+
+int msplat_trainer_set_batch_views(MsplatTrainer t, int num_views) {
+    if (!t || num_views < 1) return -1;
+    TR(t)->batch_views = num_views;
+    return 0;
 }
 
 int msplat_trainer_learned_stats(MsplatTrainer t, float *last_loss, int *rounds) {

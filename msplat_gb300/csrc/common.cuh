@@ -6,8 +6,8 @@
 //               features_dc[N,3] features_rest[N,B,3] opacities[N] (logit)
 //   SplatRec    per Gaussian, 48 B: projected centre, sigmoid(opacity),
 //               conic, raw SH colour (written by the projection)
-//   PackedRec   per intersection, 48 B, the SplatRec of the splat with its id
-//               in a.w, in per-tile depth order (written by the sort)
+//   isect_ids   per intersection, 4 B: the Gaussian (record) id, in per-tile
+//               depth order (written by the sort)
 //   GradRec     per Gaussian, 48 B: rasterizer gradients (xy, opacity logit;
 //               conic; colour), accumulated with vector atomics
 #pragma once
@@ -136,10 +136,10 @@ constexpr int kDbgSlot = 16;   // nan_counts[16..18]: checked-build violation re
 // Splat record behind intersection slot idx.  Tile lists hold Gaussian ids;
 // an id past n (the slots of a tile that overflowed the buffer) reads as a
 // transparent record.  The id rides in a.w.
-__device__ __forceinline__ SplatRec isect_record(const uint32_t *ids, const SplatRec *rec, int n, int idx) {
+__device__ __forceinline__ SplatRec isect_record(const uint32_t *ids, const SplatRec *rec, uint32_t n, int idx) {
     const uint32_t g = ids[idx];
     SplatRec r;
-    if (g < (uint32_t)n) {
+    if (g < n) {
         r = rec[g];
         r.a.w = __int_as_float((int)g);
     } else {
@@ -152,6 +152,62 @@ __device__ __forceinline__ SplatRec isect_record(const uint32_t *ids, const Spla
 
 __device__ __forceinline__ void atomic_add_f4(float4 *addr, float4 v) {
     atomicAdd(addr, v);   // sm_90+: one vector reduction in L2
+}
+
+// ---------------------------------------------------------------------------
+// Views of one step.  Every stage covers all views of the step in one launch:
+// record u = v * n + i is Gaussian i seen from view v (projection records,
+// depths, radii and rasterizer gradients are [views, n]); the tiles of all
+// views form one global tile range, view v owning [tile_base[v],
+// tile_base[v+1]); the images are concatenated, view v's pixel (x, y) at
+// pix_base[v] + y * width[v] + x; StepParams are one per view.  A plain step
+// is a table of one view.
+// ---------------------------------------------------------------------------
+constexpr int kMaxViews = 16;
+
+struct ViewTable {
+    int count;                         // views (1..kMaxViews)
+    int n;                             // Gaussians per view
+    int tile_base[kMaxViews + 1];
+    int tiles_x[kMaxViews], tiles_y[kMaxViews];
+    int width[kMaxViews], height[kMaxViews];
+    long long pix_base[kMaxViews + 1];
+};
+
+// Geometry of one view, selected with constant indices only (the table stays
+// in the kernel's parameter bank; no local copy).
+struct ViewGeom {
+    int tile_base, tiles_x, tiles_y, width, height;
+    long long pix_base;
+};
+
+__host__ __device__ __forceinline__ ViewGeom view_geom(const ViewTable &vt, int v) {
+    ViewGeom g{vt.tile_base[0], vt.tiles_x[0], vt.tiles_y[0], vt.width[0], vt.height[0], vt.pix_base[0]};
+#pragma unroll
+    for (int k = 1; k < kMaxViews; k++)
+        if (k == v) {
+            g.tile_base = vt.tile_base[k];
+            g.tiles_x = vt.tiles_x[k];
+            g.tiles_y = vt.tiles_y[k];
+            g.width = vt.width[k];
+            g.height = vt.height[k];
+            g.pix_base = vt.pix_base[k];
+        }
+    return g;
+}
+
+// view owning global tile t / global pixel p
+__host__ __device__ __forceinline__ int view_of_tile(const ViewTable &vt, int t) {
+    int v = 0;
+#pragma unroll
+    for (int k = 1; k < kMaxViews; k++) v += (k < vt.count && t >= vt.tile_base[k]) ? 1 : 0;
+    return v;
+}
+__host__ __device__ __forceinline__ int view_of_pixel(const ViewTable &vt, long long p) {
+    int v = 0;
+#pragma unroll
+    for (int k = 1; k < kMaxViews; k++) v += (k < vt.count && p >= vt.pix_base[k]) ? 1 : 0;
+    return v;
 }
 
 }  // namespace msplat

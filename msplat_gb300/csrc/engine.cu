@@ -65,54 +65,107 @@ class Engine {
 
     void train_step(const MsplatGaussians &g, const MsplatAdamState *st, const MsplatStepArgs &args, const uint8_t *gt,
                     const uint8_t *mask, bool backward) {
+        const uint8_t *gts[1] = {gt}, *masks[1] = {mask};
+        run_views(g, st, &args, 1, gt ? gts : nullptr, masks, backward);
+    }
+
+    // Copies host images into engine-owned device buffers on the engine's
+    // stream (asynchronous for page-locked sources), then runs the step.
+    void train_step_host(const MsplatGaussians &g, const MsplatAdamState *st, const MsplatStepArgs &args,
+                         const uint8_t *gt_host, const uint8_t *mask_host) {
         CK(cudaSetDevice(device_));
-        validate(g, args);
-        const int N = g.num_points, W = args.width, H = args.height;
-        const int tx = (W + kTile - 1) / kTile, ty = (H + kTile - 1) / kTile, T = tx * ty;
-        const long long P = (long long)W * H;
-        const long long cap = std::max<long long>(48LL * N, 1);   // msplat_metal.mm:1142 legacy capacity
-        const int K = choose_k(args, T, cap);
-        ensure_points(N);
+        const size_t P = (size_t)args.width * args.height;
+        alloc("gt_stage", P * 3);
+        CK(cudaMemcpyAsync(ptr<uint8_t>("gt_stage"), gt_host, P * 3, cudaMemcpyHostToDevice, stream_));
+        const uint8_t *mask_d = nullptr;
+        if (mask_host) {
+            alloc("mask_stage", P);
+            CK(cudaMemcpyAsync(ptr<uint8_t>("mask_stage"), mask_host, P, cudaMemcpyHostToDevice, stream_));
+            mask_d = ptr<uint8_t>("mask_stage");
+        }
+        train_step(g, st, args, ptr<uint8_t>("gt_stage"), mask_d, true);
+    }
+
+    // Multi-view step: B views (any sizes) rendered and back-propagated by
+    // the same launches as one view (each stage covers all views), each
+    // view's image gradient scaled by 1/B so the parameter gradients are the
+    // views' mean, then one optimizer update with the scalars of args[0]: the
+    // 4-group Adam with the regularizer, the SH Adam (fused in the projection
+    // backward) over Gaussians visible in any view, and SGLD.
+    void train_step_batch(const MsplatGaussians &g, const MsplatAdamState &st, const MsplatStepArgs *args, int B,
+                          const uint8_t *const *gts, const uint8_t *const *masks) {
+        if (B <= 0) throw std::runtime_error("batch of no views");
+        if (B > kMaxViews) throw std::runtime_error("more than 16 views in one step");
+        for (int v = 0; v < B; v++)
+            if (!gts || !gts[v]) throw std::runtime_error("multi-view step without a target image");
+        run_views(g, &st, args, B, gts, masks, true);
+    }
+
+  private:
+    // One step over B views; gts == nullptr renders only (one view).
+    void run_views(const MsplatGaussians &g, const MsplatAdamState *st, const MsplatStepArgs *args, int B,
+                   const uint8_t *const *gts, const uint8_t *const *masks, bool backward) {
+        CK(cudaSetDevice(device_));
+        int w[kMaxViews], h[kMaxViews];
+        for (int v = 0; v < B; v++) {
+            validate(g, args[v]);
+            w[v] = args[v].width;
+            h[v] = args[v].height;
+        }
+        const int N = g.num_points;
+        if ((long long)N * B >= (1LL << 31)) throw std::runtime_error("views x Gaussians exceeds 2^31 records");
+        const ViewTable vt = make_view_table(N, B, w, h);
+        const int T = vt.tile_base[B];
+        const long long P = vt.pix_base[B];
+        if (P > (1LL << 31) / 16) throw std::runtime_error("views too large for one step");
+        const long long cap = std::max<long long>(48LL * N * B, 1);   // msplat_metal.mm:1142 legacy capacity, per view
+        const int K = choose_k(args[0], T, cap);
+        const bool has_gt = gts != nullptr;
+        ensure_points(N, B);
         ensure_tiles(T);
         ensure_isect(cap);
         ensure_pixels(P);
         if (K > 1) ensure_chunks((long long)K * P);
         last_T_ = T;
         last_K_ = K;
-        last_batch_P_.clear();
+        last_views_ = B;
+        for (int v = 0; v < B; v++) last_view_P_[v] = (long long)w[v] * h[v];
         if (timing_) slot_ = (timed_steps_++) % kRing;
-        // kernels of this step: projection, count/scan/scatter/sort, raster
-        // (+ merge when chunked), and for training 3 loss passes, raster
-        // backward (+ prefix/suffix), projection backward, Adam, SGLD
 
-        StepParams sp;
-        fill_params(args, sp, mask != nullptr);
-        sp.gt = gt;
-        sp.mask = mask;
+        StepParams sps[kMaxViews];
+        for (int v = 0; v < B; v++) {
+            const uint8_t *mk = (has_gt && masks) ? masks[v] : nullptr;
+            fill_params(args[v], sps[v], mk != nullptr);
+            sps[v].gt = has_gt ? gts[v] : nullptr;
+            sps[v].mask = mk;
+            if (B > 1) sps[v].loss_inv_n = args[v].loss_inv_n / (float)B;
+        }
         // pageable source: the copy has consumed it when the call returns.
         // It stays outside any captured graph: kernels read the scalars
         // through this device block, so a replay sees this step's values.
-        CK(cudaMemcpyAsync(ptr<StepParams>("params"), &sp, sizeof(sp), cudaMemcpyHostToDevice, stream_));
+        CK(cudaMemcpyAsync(ptr<StepParams>("params"), sps, sizeof(StepParams) * B, cudaMemcpyHostToDevice, stream_));
         // every buffer the step touches exists now (sized above), so a capture
         // below allocates nothing
-        const size_t cb = tile_cta_bins_bytes(N, T);
+        const size_t cb = tile_cta_bins_bytes(vt);
         if (cb) alloc("cta_bins", cb);
+        const MsplatStepArgs &a0 = args[0];
+        const bool opt = a0.do_optimizer && st;
 
         auto issue = [&]() {
-        // kernels of this step: projection, the tile-mapping launches (counted
-        // where they are issued), raster (+ merge when chunked), and for
-        // training 3 loss passes, raster backward (+ prefix/suffix),
-        // projection backward, Adam, SGLD
+        // kernels of this step, one launch per stage whatever the views:
+        // projection, the tile-mapping launches (counted where they are
+        // issued), raster (+ merge when chunked), and for training 3 loss
+        // passes, raster backward (+ prefix/suffix), projection backward,
+        // Adam, SGLD
         launches_ += 1 + (K > 1 ? 2 : 1);
-        if (gt) launches_ += 3;
-        if (gt && backward) launches_ += (K > 1 ? 2 : 1) + 1 + (args.do_optimizer && st ? 1 : 0) + (args.do_sgld ? 1 : 0);
+        if (has_gt) launches_ += 3;
+        if (has_gt && backward) launches_ += (K > 1 ? 2 : 1) + 1 + (opt ? 1 : 0) + (a0.do_sgld ? 1 : 0);
         CK(cudaMemsetAsync(ptr<uint32_t>("tile_counts"), 0, sizeof(uint32_t) * 2 * (size_t)T, stream_));
-        CK(cudaMemsetAsync(ptr<float>("loss_sum"), 0, sizeof(float), stream_));
+        CK(cudaMemsetAsync(ptr<float>("loss_sum"), 0, sizeof(float) * B, stream_));
 
         mark(0);
         ProjectArgs pa{};
-        pa.n = N; pa.rest_bases = g.rest_bases; pa.tiles_x = tx; pa.tiles_y = ty;
-        pa.Wf = (float)W; pa.Hf = (float)H;
+        pa.vt = vt; pa.rest_bases = g.rest_bases;
         pa.means = g.means; pa.scales = g.scales; pa.quats = g.quats;
         pa.features_dc = g.features_dc; pa.features_rest = g.features_rest; pa.opacities = g.opacities;
         pa.sp = ptr<StepParams>("params");
@@ -125,7 +178,7 @@ class Engine {
         mark(1);
 
         TileArgs ta{};
-        ta.n = N; ta.tiles_x = tx; ta.tiles_y = ty; ta.num_tiles = T; ta.capacity = cap;
+        ta.vt = vt; ta.num_tiles = T; ta.capacity = cap;
         ta.radii = pa.radii; ta.depths = pa.depths; ta.rec = pa.rec; ta.aabb = pa.aabb;
         ta.tile_counts = ptr<uint32_t>("tile_counts"); ta.tile_write = ta.tile_counts + T;
         ta.tile_offsets = ptr<uint32_t>("tile_offsets"); ta.max_tile_count = ptr<uint32_t>("max_tile");
@@ -137,9 +190,9 @@ class Engine {
         mark(2);
 
         RasterArgs ra{};
-        ra.width = W; ra.height = H; ra.tiles_x = tx; ra.num_tiles = T; ra.k_max = K; ra.capacity = cap;
+        ra.vt = vt; ra.num_tiles = T; ra.k_max = K; ra.capacity = cap;
         ra.sp = pa.sp; ra.tile_offsets = ta.tile_offsets; ra.isect_ids = ta.isect_ids;
-        ra.n = N; ra.rec = pa.rec;
+        ra.n = (uint32_t)((long long)N * B); ra.rec = pa.rec;
         ra.out_img = ptr<float>("out_img"); ra.final_T = ptr<float>("final_T"); ra.final_idx = ptr<int>("final_idx");
         if (K > 1) {
             ra.chunk_T = ptr<float>("chunk_T"); ra.chunk_C = ptr<float>("chunk_C"); ra.chunk_idx = ptr<int>("chunk_idx");
@@ -150,10 +203,10 @@ class Engine {
         debug_sync(stream_, "raster_fwd");
         last_ra_ = ra;
         mark(3);
-        if (!gt) { mark(4); mark(5); mark(6); mark(7); mark(8); return; }
+        if (!has_gt) { mark(4); mark(5); mark(6); mark(7); mark(8); return; }
 
         LossArgs la{};
-        la.width = W; la.height = H; la.sp = pa.sp; la.img = ra.out_img;
+        la.vt = vt; la.num_tiles = T; la.sp = pa.sp; la.img = ra.out_img;
         la.gt = nullptr; la.mask = nullptr;   // read from StepParams (see common.cuh)
         la.hbuf = ptr<float>("hbuf"); la.dbuf = ptr<float>("dbuf"); la.v_img = ptr<float>("v_img");
         la.loss_sum = ptr<float>("loss_sum"); la.nan_counts = pa.nan_counts;
@@ -167,11 +220,12 @@ class Engine {
         mark(5);
 
         ProjectBwdArgs pb{};
-        pb.n = N; pb.rest_bases = g.rest_bases; pb.do_optimizer = args.do_optimizer && st;
-        pb.Wf = (float)W; pb.Hf = (float)H; pb.sp = pa.sp;
+        pb.vt = vt; pb.rest_bases = g.rest_bases; pb.do_optimizer = opt;
+        pb.sp = pa.sp;
         pb.means = g.means; pb.scales = g.scales; pb.quats = g.quats; pb.radii = pa.radii; pb.rec = pa.rec;
         pb.grad = ra.grad;
         pb.v_mean = ptr<float>("v_mean"); pb.v_scale = ptr<float>("v_scale"); pb.v_quat = ptr<float>("v_quat");
+        pb.v_opac = B > 1 ? ptr<float>("v_opac") : nullptr;
         pb.features_dc = g.features_dc; pb.features_rest = g.features_rest;
         if (st) {
             pb.dc_m = st->exp_avg[3]; pb.dc_v = st->exp_avg_sq[3];
@@ -192,245 +246,32 @@ class Engine {
             aa.dc_v = st->exp_avg_sq[3];
         }
         aa.g_mean = pb.v_mean; aa.g_scale = pb.v_scale; aa.g_quat = pb.v_quat; aa.grad = ra.grad;
+        aa.g_opac = pb.v_opac;
         aa.nan_counts = pa.nan_counts;
-        if (args.do_optimizer && st) launch_adam(aa, num_sms_, stream_);
+        if (opt) launch_adam(aa, num_sms_, stream_);
         debug_sync(stream_, "adam");
         mark(7);
-        if (args.do_sgld) launch_sgld(aa, stream_);
+        if (a0.do_sgld) launch_sgld(aa, stream_);
         debug_sync(stream_, "sgld");
         mark(8);
         CK(cudaGetLastError());
         };   // issue
 
         // CUDA graph mode: the second step with the same shapes and buffers
-        // is captured, later ones replay it (one launch for the whole step)
+        // is captured, later ones replay it (one launch for the whole step).
+        // The targets and masks come through StepParams, not the key.
         const bool graphable = use_graphs_ && !timing_ && !g_sync_check;
         if (graphable) {
-            GraphKey key{};
-            key.n = N; key.w = W; key.h = H; key.k = K; key.rest = g.rest_bases;
-            key.flags = (args.do_optimizer ? 1 : 0) | (args.do_sgld ? 2 : 0) | (backward ? 4 : 0) | (st ? 8 : 0) |
-                        (gt ? 16 : 0);   // the target and mask themselves come through StepParams
-            key.ptr[0] = g.means; key.ptr[1] = g.scales; key.ptr[2] = g.quats; key.ptr[3] = g.features_dc;
-            key.ptr[4] = g.features_rest; key.ptr[5] = g.opacities; key.ptr[6] = gstats_;
-            for (int k = 0; k < 6 && st; k++) { key.ptr[8 + k] = st->exp_avg[k]; key.ptr[14 + k] = st->exp_avg_sq[k]; }
-            const std::string ks(reinterpret_cast<const char *>(&key), sizeof(key));
-            auto it = graphs_.find(ks);
-            if (it != graphs_.end()) {
-                CK(cudaGraphLaunch(it->second.exec, stream_));
-                launches_ += it->second.launches;
-                return;
-            }
-            if (graph_seen_.count(ks) && graphs_.size() < kMaxGraphs) {
-                const long long l0 = launches_;
-                cudaGraph_t graph = nullptr;
-                CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
-                try {
-                    issue();
-                } catch (...) {
-                    cudaStreamEndCapture(stream_, &graph);
-                    if (graph) cudaGraphDestroy(graph);
-                    throw;
-                }
-                CK(cudaStreamEndCapture(stream_, &graph));
-                cudaGraphExec_t exec = nullptr;
-                const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
-                cudaGraphDestroy(graph);
-                CK(ie);
-                graphs_[ks] = GraphEntry{exec, launches_ - l0};
-                CK(cudaGraphLaunch(exec, stream_));
-                return;
-            }
-            graph_seen_.insert(ks);
-        }
-        issue();
-    }
-
-    // Copies host images into engine-owned device buffers on the engine's
-    // stream (asynchronous for page-locked sources), then runs the step.
-    void train_step_host(const MsplatGaussians &g, const MsplatAdamState *st, const MsplatStepArgs &args,
-                         const uint8_t *gt_host, const uint8_t *mask_host) {
-        CK(cudaSetDevice(device_));
-        const size_t P = (size_t)args.width * args.height;
-        alloc("gt_stage", P * 3);
-        CK(cudaMemcpyAsync(ptr<uint8_t>("gt_stage"), gt_host, P * 3, cudaMemcpyHostToDevice, stream_));
-        const uint8_t *mask_d = nullptr;
-        if (mask_host) {
-            alloc("mask_stage", P);
-            CK(cudaMemcpyAsync(ptr<uint8_t>("mask_stage"), mask_host, P, cudaMemcpyHostToDevice, stream_));
-            mask_d = ptr<uint8_t>("mask_stage");
-        }
-        train_step(g, st, args, ptr<uint8_t>("gt_stage"), mask_d, true);
-    }
-
-    // Multi-view step: B views (any sizes) rendered and back-propagated one
-    // after another on the stream, their gradients averaged (each view's
-    // image gradient is scaled by 1/B), then one optimizer update: the
-    // 4-group Adam with the regularizer, the SH Adam over the coefficients of
-    // Gaussians visible in any view, and SGLD.  Scalars of the optimizer come
-    // from args[0].  In graph mode the whole batch is one captured graph.
-    void train_step_batch(const MsplatGaussians &g, const MsplatAdamState &st, const MsplatStepArgs *args, int B,
-                          const uint8_t *const *gts, const uint8_t *const *masks) {
-        CK(cudaSetDevice(device_));
-        if (B <= 0) throw std::runtime_error("batch of no views");
-        if (B == 1) {
-            train_step(g, &st, args[0], gts[0], masks ? masks[0] : nullptr, true);
-            return;
-        }
-        const int N = g.num_points;
-        struct View { int W, H, tx, ty, T, K; long long P; };
-        std::vector<View> vw(B);
-        const long long cap = std::max<long long>(48LL * N, 1);
-        int maxT = 1;
-        long long maxP = 1, maxKP = 0;
-        for (int v = 0; v < B; v++) {
-            validate(g, args[v]);
-            if (!gts[v]) throw std::runtime_error("multi-view step without a target image");
-            View &w = vw[v];
-            w.W = args[v].width; w.H = args[v].height;
-            w.tx = (w.W + kTile - 1) / kTile; w.ty = (w.H + kTile - 1) / kTile; w.T = w.tx * w.ty;
-            w.P = (long long)w.W * w.H;
-            w.K = choose_k(args[v], w.T, cap);
-            maxT = std::max(maxT, w.T);
-            maxP = std::max(maxP, w.P);
-            if (w.K > 1) maxKP = std::max(maxKP, (long long)w.K * w.P);
-        }
-        ensure_points(N);
-        ensure_tiles(maxT);
-        ensure_isect(cap);
-        ensure_pixels(maxP);
-        if (maxKP) ensure_chunks(maxKP);
-        const size_t cb = tile_cta_bins_bytes(N, maxT);
-        if (cb) alloc("cta_bins", cb);
-        alloc("params_batch", sizeof(StepParams) * (size_t)B);
-        alloc("loss_batch", sizeof(float) * (size_t)B);
-        const size_t rb = (size_t)3 * g.rest_bases;
-        alloc("acc_opac", 4 * (size_t)std::max(N, 1));
-        alloc("acc_dc", 12 * (size_t)std::max(N, 1));
-        alloc("acc_rest", 4 * rb * (size_t)std::max(N, 1) + 16);
-        alloc("acc_vis", (size_t)std::max(N, 1) + 16);
-        std::vector<StepParams> sps(B);
-        for (int v = 0; v < B; v++) {
-            fill_params(args[v], sps[v], masks && masks[v]);
-            sps[v].gt = gts[v];
-            sps[v].mask = masks ? masks[v] : nullptr;
-            sps[v].loss_inv_n = args[v].loss_inv_n / (float)B;
-        }
-        CK(cudaMemcpyAsync(ptr<StepParams>("params_batch"), sps.data(), sizeof(StepParams) * B,
-                           cudaMemcpyHostToDevice, stream_));
-        last_batch_P_.assign(B, 0);
-        for (int v = 0; v < B; v++) last_batch_P_[v] = vw[v].P;
-        last_T_ = vw[B - 1].T;
-        last_K_ = vw[B - 1].K;
-        last_P_ = vw[B - 1].P;
-
-        auto issue = [&]() {
-            StepParams *spb = ptr<StepParams>("params_batch");
-            CK(cudaMemsetAsync(ptr<float>("loss_batch"), 0, sizeof(float) * B, stream_));
-            CK(cudaMemsetAsync(ptr<float>("v_mean"), 0, 12 * (size_t)N, stream_));
-            CK(cudaMemsetAsync(ptr<float>("v_scale"), 0, 12 * (size_t)N, stream_));
-            CK(cudaMemsetAsync(ptr<float>("v_quat"), 0, 16 * (size_t)N, stream_));
-            CK(cudaMemsetAsync(ptr<float>("acc_opac"), 0, 4 * (size_t)N, stream_));
-            CK(cudaMemsetAsync(ptr<float>("acc_dc"), 0, 12 * (size_t)N, stream_));
-            if (rb) CK(cudaMemsetAsync(ptr<float>("acc_rest"), 0, 4 * rb * (size_t)N, stream_));
-            CK(cudaMemsetAsync(ptr<uint8_t>("acc_vis"), 0, (size_t)N, stream_));
-            for (int v = 0; v < B; v++) {
-                const View &w = vw[v];
-                const StepParams *sp = spb + v;
-                CK(cudaMemsetAsync(ptr<uint32_t>("tile_counts"), 0, sizeof(uint32_t) * 2 * (size_t)w.T, stream_));
-                ProjectArgs pa{};
-                pa.n = N; pa.rest_bases = g.rest_bases; pa.tiles_x = w.tx; pa.tiles_y = w.ty;
-                pa.Wf = (float)w.W; pa.Hf = (float)w.H;
-                pa.means = g.means; pa.scales = g.scales; pa.quats = g.quats;
-                pa.features_dc = g.features_dc; pa.features_rest = g.features_rest; pa.opacities = g.opacities;
-                pa.sp = sp;
-                pa.rec = ptr<SplatRec>("rec"); pa.depths = ptr<float>("depths"); pa.radii = ptr<int>("radii");
-                pa.aabb = ptr<float2>("aabb"); pa.tiles_hit = ptr<int>("tiles_hit");
-                pa.grad = ptr<GradRec>("grad");
-                pa.nan_counts = ptr<unsigned>("nan_counts");
-                launch_project_fwd(pa, stream_);
-                launches_ += 1;
-                TileArgs ta{};
-                ta.n = N; ta.tiles_x = w.tx; ta.tiles_y = w.ty; ta.num_tiles = w.T; ta.capacity = cap;
-                ta.radii = pa.radii; ta.depths = pa.depths; ta.rec = pa.rec; ta.aabb = pa.aabb;
-                ta.tile_counts = ptr<uint32_t>("tile_counts"); ta.tile_write = ta.tile_counts + w.T;
-                ta.tile_offsets = ptr<uint32_t>("tile_offsets"); ta.max_tile_count = ptr<uint32_t>("max_tile");
-                ta.keys = ptr<uint64_t>("keys"); ta.keys_alt = ptr<uint64_t>("keys_alt");
-                ta.isect_ids = ptr<uint32_t>("isect_ids"); ta.nan_counts = pa.nan_counts;
-                ta.cta_bins = cb ? ptr<uint32_t>("cta_bins") : nullptr;
-                ta.tile_lists = ptr<uint32_t>("tile_lists"); ta.tile_class = ptr<uint32_t>("tile_class");
-                launches_ += launch_tiles(ta, num_sms_, stream_);
-                RasterArgs ra{};
-                ra.width = w.W; ra.height = w.H; ra.tiles_x = w.tx; ra.num_tiles = w.T; ra.k_max = w.K;
-                ra.capacity = cap; ra.sp = sp; ra.tile_offsets = ta.tile_offsets; ra.isect_ids = ta.isect_ids;
-                ra.n = N; ra.rec = pa.rec;
-                ra.out_img = ptr<float>("out_img"); ra.final_T = ptr<float>("final_T"); ra.final_idx = ptr<int>("final_idx");
-                if (w.K > 1) {
-                    ra.chunk_T = ptr<float>("chunk_T"); ra.chunk_C = ptr<float>("chunk_C");
-                    ra.chunk_idx = ptr<int>("chunk_idx");
-                    ra.prefix_T = ptr<float>("prefix_T"); ra.after_C = ptr<float>("after_C");
-                }
-                ra.v_img = ptr<float>("v_img"); ra.grad = ptr<GradRec>("grad"); ra.nan_counts = pa.nan_counts;
-                launch_raster_fwd(ra, stream_);
-                LossArgs la{};
-                la.width = w.W; la.height = w.H; la.sp = sp; la.img = ra.out_img;
-                la.gt = nullptr; la.mask = nullptr;
-                la.hbuf = ptr<float>("hbuf"); la.dbuf = ptr<float>("dbuf"); la.v_img = ptr<float>("v_img");
-                la.loss_sum = ptr<float>("loss_batch") + v; la.nan_counts = pa.nan_counts;
-                launch_loss(la, stream_);
-                launch_raster_bwd(ra, stream_);
-                launches_ += (w.K > 1 ? 2 : 1) * 2 + 3;
-                ProjectBwdArgs pb{};
-                pb.n = N; pb.rest_bases = g.rest_bases; pb.do_optimizer = 0;
-                pb.Wf = (float)w.W; pb.Hf = (float)w.H; pb.sp = sp;
-                pb.means = g.means; pb.scales = g.scales; pb.quats = g.quats; pb.radii = pa.radii; pb.rec = pa.rec;
-                pb.grad = ra.grad;
-                pb.v_mean = ptr<float>("v_mean"); pb.v_scale = ptr<float>("v_scale"); pb.v_quat = ptr<float>("v_quat");
-                pb.features_dc = g.features_dc; pb.features_rest = g.features_rest;
-                pb.accumulate = 1;
-                pb.acc_opac = ptr<float>("acc_opac"); pb.acc_dc = ptr<float>("acc_dc");
-                pb.acc_rest = ptr<float>("acc_rest"); pb.acc_vis = ptr<uint8_t>("acc_vis");
-                pb.gstats = gstats_;
-                pb.nan_counts = pa.nan_counts;
-                launch_project_bwd(pb, stream_);
-                launches_ += 1;
-            }
-            AdamArgs aa{};
-            aa.n = N; aa.sp = spb;
-            aa.means = g.means; aa.scales = g.scales; aa.quats = g.quats; aa.opacities = g.opacities;
-            const int grp[4] = {0, 1, 2, 5};
-            for (int k = 0; k < 4; k++) { aa.m[k] = st.exp_avg[grp[k]]; aa.v[k] = st.exp_avg_sq[grp[k]]; }
-            aa.dc_v = st.exp_avg_sq[3];
-            aa.g_mean = ptr<float>("v_mean"); aa.g_scale = ptr<float>("v_scale"); aa.g_quat = ptr<float>("v_quat");
-            aa.grad = ptr<GradRec>("grad"); aa.g_opac = ptr<float>("acc_opac");
-            aa.nan_counts = ptr<unsigned>("nan_counts");
-            if (args[0].do_optimizer) {
-                launch_adam(aa, num_sms_, stream_);
-                ShAdamArgs sa{};
-                sa.n = N; sa.rest_bases = g.rest_bases; sa.sp = spb;
-                sa.features_dc = g.features_dc; sa.features_rest = g.features_rest;
-                sa.dc_m = st.exp_avg[3]; sa.dc_v = st.exp_avg_sq[3]; sa.rest_m = st.exp_avg[4]; sa.rest_v = st.exp_avg_sq[4];
-                sa.acc_dc = ptr<float>("acc_dc"); sa.acc_rest = ptr<float>("acc_rest"); sa.acc_vis = ptr<uint8_t>("acc_vis");
-                sa.nan_counts = aa.nan_counts;
-                launch_sh_adam(sa, stream_);
-                launches_ += 2;
-            }
-            if (args[0].do_sgld) {
-                launch_sgld(aa, stream_);
-                launches_ += 1;
-            }
-            CK(cudaGetLastError());
-        };
-
-        const bool graphable = use_graphs_ && !timing_ && !g_sync_check;
-        if (graphable) {
-            std::string ks = "batch";
+            std::string ks;
             auto put = [&](const void *p, size_t n) { ks.append(reinterpret_cast<const char *>(p), n); };
-            put(&N, 4); put(&B, 4);
-            for (int v = 0; v < B; v++) put(&vw[v], sizeof(View));
-            const int fl = (args[0].do_optimizer ? 1 : 0) | (args[0].do_sgld ? 2 : 0) | (g.rest_bases << 4);
-            put(&fl, 4);
+            const int head[5] = {N, B, K, g.rest_bases,
+                                 (a0.do_optimizer ? 1 : 0) | (a0.do_sgld ? 2 : 0) | (backward ? 4 : 0) | (st ? 8 : 0) |
+                                     (has_gt ? 16 : 0)};
+            put(head, sizeof(head));
+            put(w, sizeof(int) * B);
+            put(h, sizeof(int) * B);
             const void *ps[20] = {g.means, g.scales, g.quats, g.features_dc, g.features_rest, g.opacities, gstats_};
-            for (int k = 0; k < 6; k++) { ps[8 + k] = st.exp_avg[k]; ps[14 + k] = st.exp_avg_sq[k]; }
+            for (int k = 0; k < 6 && st; k++) { ps[8 + k] = st->exp_avg[k]; ps[14 + k] = st->exp_avg_sq[k]; }
             put(ps, sizeof(ps));
             auto it = graphs_.find(ks);
             if (it != graphs_.end()) {
@@ -463,6 +304,7 @@ class Engine {
         issue();
     }
 
+  public:
     // dL/d(parameters) for a caller-supplied dL/d(image): the forward is run
     // again (projection, tile lists, raster) rather than kept from an
     // earlier call, then the raster and projection backward passes write
@@ -485,14 +327,14 @@ class Engine {
         const int N = g.num_points;
         if (N <= 0) return;
         CK(cudaMemsetAsync(ptr<GradRec>("grad"), 0, sizeof(GradRec) * (size_t)N, stream_));
-        RasterArgs ra = last_ra_;
+        RasterArgs ra = last_ra_;   // one view
         ra.v_img = v_img;
         ra.grad = ptr<GradRec>("grad");
         launch_raster_bwd(ra, stream_);
         debug_sync(stream_, "raster_bwd");
         ProjectBwdArgs pb{};
-        pb.n = N; pb.rest_bases = g.rest_bases; pb.do_optimizer = 0;
-        pb.Wf = (float)args.width; pb.Hf = (float)args.height; pb.sp = ptr<StepParams>("params");
+        pb.vt = ra.vt; pb.rest_bases = g.rest_bases; pb.do_optimizer = 0;
+        pb.sp = ptr<StepParams>("params");
         pb.means = g.means; pb.scales = g.scales; pb.quats = g.quats;
         pb.radii = ptr<int>("radii"); pb.rec = ptr<SplatRec>("rec"); pb.grad = ra.grad;
         pb.v_mean = out.v_means; pb.v_scale = out.v_scales; pb.v_quat = out.v_quats;
@@ -543,19 +385,14 @@ class Engine {
     void synchronize() { CK(cudaStreamSynchronize(stream_)); }
 
     float loss() {
-        if (!last_batch_P_.empty()) {   // multi-view step: mean of the views' losses
-            std::vector<float> v(last_batch_P_.size());
-            CK(cudaMemcpyAsync(v.data(), ptr<float>("loss_batch"), sizeof(float) * v.size(), cudaMemcpyDeviceToHost,
-                               stream_));
-            synchronize();
-            double acc = 0;
-            for (size_t k = 0; k < v.size(); k++) acc += (double)v[k] / (double)last_batch_P_[k];
-            return (float)(acc / (double)v.size());
-        }
-        float v = 0;
-        CK(cudaMemcpyAsync(&v, ptr<float>("loss_sum"), sizeof(float), cudaMemcpyDeviceToHost, stream_));
+        float v[kMaxViews] = {0.f};
+        const int B = std::max(1, last_views_);
+        CK(cudaMemcpyAsync(v, ptr<float>("loss_sum"), sizeof(float) * B, cudaMemcpyDeviceToHost, stream_));
         synchronize();
-        return v / (float)last_P_;
+        if (B == 1) return v[0] / (float)last_view_P_[0];
+        double acc = 0;   // several views: the mean of the views' losses
+        for (int k = 0; k < B; k++) acc += (double)v[k] / (double)last_view_P_[k];
+        return (float)(acc / (double)B);
     }
 
     void stats(MsplatEngineStats &o) {
@@ -629,25 +466,33 @@ class Engine {
         if (zero) CK(cudaMemsetAsync(b.ptr, 0, bytes, stream_));
     }
 
-    void ensure_points(int n) {
+    // per-record buffers for `views` x n records, per-Gaussian gradients for n
+    void ensure_points(int n, int views = 1) {
         if (!has("params")) {
-            alloc("params", sizeof(StepParams));
+            alloc("params", sizeof(StepParams) * kMaxViews);
             alloc("loss_sum", 256, true);
             alloc("nan_counts", 128, true);
             alloc("max_tile", 256, true);
         }
-        if (n <= cap_points_ && has("rec")) return;
-        const size_t m = (size_t)std::max(n, 1);
-        alloc("rec", m * sizeof(SplatRec));
-        alloc("depths", m * 4);
-        alloc("radii", m * 4);
-        alloc("aabb", m * 8);
-        alloc("tiles_hit", m * 4);
-        alloc("grad", m * sizeof(GradRec), true);
-        alloc("v_mean", m * 12);
-        alloc("v_scale", m * 12);
-        alloc("v_quat", m * 16);
-        cap_points_ = n;
+        const long long recs = (long long)n * views;
+        if (recs > cap_records_ || !has("rec")) {
+            const size_t m = (size_t)std::max<long long>(recs, 1);
+            alloc("rec", m * sizeof(SplatRec));
+            alloc("depths", m * 4);
+            alloc("radii", m * 4);
+            alloc("aabb", m * 8);
+            alloc("tiles_hit", m * 4);
+            alloc("grad", m * sizeof(GradRec), true);
+            cap_records_ = recs;
+        }
+        if (n > cap_points_ || !has("v_mean")) {
+            const size_t m = (size_t)std::max(n, 1);
+            alloc("v_mean", m * 12);
+            alloc("v_scale", m * 12);
+            alloc("v_quat", m * 16);
+            alloc("v_opac", m * 4);
+            cap_points_ = n;
+        }
     }
     void ensure_tiles(int T) {
         if (T <= cap_tiles_) return;
@@ -665,7 +510,6 @@ class Engine {
         cap_isect_ = c;
     }
     void ensure_pixels(long long P) {
-        last_P_ = P;
         if (P <= cap_pixels_) return;
         alloc("out_img", (size_t)P * 12);
         alloc("final_T", (size_t)P * 4);
@@ -740,8 +584,9 @@ class Engine {
     cudaStream_t stream_ = nullptr;
     std::map<std::string, Buf> bufs_;
     int cap_points_ = 0, cap_tiles_ = 0;
-    long long cap_isect_ = 0, cap_pixels_ = 0, cap_chunks_ = 0, last_P_ = 1;
-    int last_T_ = 0, last_K_ = 1;
+    long long cap_records_ = 0, cap_isect_ = 0, cap_pixels_ = 0, cap_chunks_ = 0;
+    int last_T_ = 0, last_K_ = 1, last_views_ = 1;
+    long long last_view_P_[kMaxViews] = {1};   // pixels of each view of the last step
     bool timing_ = false;
     static constexpr int kRing = 128;
     cudaEvent_t ev_[kRing][MSPLAT_STAGE_COUNT + 1];
@@ -749,7 +594,6 @@ class Engine {
     int slot_ = 0;
     long long timed_steps_ = 0, launches_ = 0;
     RasterArgs last_ra_{};   // raster arguments of the last eagerly issued step
-    std::vector<long long> last_batch_P_;   // pixel counts of the last multi-view step's views
     float4 *gstats_ = nullptr;   // caller's activity statistics (learned relocation), or null
 
   public:
@@ -758,10 +602,6 @@ class Engine {
   private:
 
     // captured steps, keyed by shapes, flags and every pointer they bake in
-    struct GraphKey {
-        int n, w, h, k, rest, flags;
-        const void *ptr[20];
-    };
     struct GraphEntry {
         cudaGraphExec_t exec;
         long long launches;

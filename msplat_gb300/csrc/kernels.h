@@ -9,11 +9,34 @@
 
 namespace msplat {
 
+// Table of `count` views (sizes w[v] x h[v]) over n Gaussians.
+inline ViewTable make_view_table(int n, int count, const int *w, const int *h) {
+    ViewTable vt{};
+    vt.count = count;
+    vt.n = n;
+    for (int v = 0; v < count; v++) {
+        vt.width[v] = w[v];
+        vt.height[v] = h[v];
+        vt.tiles_x[v] = (w[v] + kTile - 1) / kTile;
+        vt.tiles_y[v] = (h[v] + kTile - 1) / kTile;
+        vt.tile_base[v + 1] = vt.tile_base[v] + vt.tiles_x[v] * vt.tiles_y[v];
+        vt.pix_base[v + 1] = vt.pix_base[v] + (long long)w[v] * h[v];
+    }
+    for (int v = count; v < kMaxViews; v++) {   // past the end: empty views at the end of the ranges
+        vt.tile_base[v + 1] = vt.tile_base[v];
+        vt.pix_base[v + 1] = vt.pix_base[v];
+    }
+    return vt;
+}
+inline ViewTable single_view_table(int n, int w, int h) { return make_view_table(n, 1, &w, &h); }
+
+// Record arrays (rec, depths, radii, aabb, tiles_hit, grad) are [views, n]
+// (see ViewTable); the parameters are read once per view.
 struct ProjectArgs {
-    int n, rest_bases, tiles_x, tiles_y;
-    float Wf, Hf;
+    ViewTable vt;
+    int rest_bases;
     const float *means, *scales, *quats, *features_dc, *features_rest, *opacities;
-    const StepParams *sp;
+    const StepParams *sp;   // [views]
     SplatRec *rec;
     float *depths;
     int *radii;
@@ -24,7 +47,8 @@ struct ProjectArgs {
 };
 
 struct TileArgs {
-    int n, tiles_x, tiles_y, num_tiles;
+    ViewTable vt;
+    int num_tiles;          // over all views
     long long capacity;     // intersection slots of keys / isect_ids
     const int *radii;
     const float *depths;
@@ -32,7 +56,7 @@ struct TileArgs {
     const float2 *aabb;
     uint32_t *tile_counts;  // zeroed before the step
     uint32_t *tile_write;   // zeroed before the step
-    uint32_t *cta_bins;     // [ceil(n / 2048), T] per-CTA tile histograms (block-aggregated path)
+    uint32_t *cta_bins;     // per view: [ceil(n / 2048), T_v] per-CTA tile histograms (block-aggregated path)
     uint32_t *tile_lists;   // [3, T] tiles of each sort class (written by the scan)
     uint32_t *tile_class;   // [6]: list lengths, then the sort kernels' work counters
     uint32_t *tile_offsets; // [T+1]
@@ -43,11 +67,12 @@ struct TileArgs {
 };
 
 struct RasterArgs {
-    int width, height, tiles_x, num_tiles, k_max;
+    ViewTable vt;
+    int num_tiles, k_max;       // tiles over all views; depth chunks (1 = monolithic)
     long long capacity;
-    const StepParams *sp;
+    const StepParams *sp;       // [views]
     const uint32_t *tile_offsets;
-    int n;                      // Gaussians (ids at or past n read as transparent)
+    uint32_t n;                 // records, views * Gaussians (ids at or past n read as transparent)
     const uint32_t *isect_ids;  // per-tile sorted Gaussian ids
     const SplatRec *rec;        // projection records, gathered by id
     float *out_img, *final_T;
@@ -60,38 +85,36 @@ struct RasterArgs {
 };
 
 struct LossArgs {
-    int width, height;
-    const StepParams *sp;
+    ViewTable vt;
+    int num_tiles;          // 16x16 blocks over all views (the tiles)
+    const StepParams *sp;   // [views]
     const float *img;
-    const uint8_t *gt, *mask;
-    float *hbuf;            // [15, P] channel-planar moments
+    const uint8_t *gt, *mask;   // one view: override StepParams' target and mask (nullable)
+    float *hbuf;            // [15, P] channel-planar moments, P = pixels of all views
     float *dbuf;            // [9, P] horizontally convolved fields
     float *v_img;           // [P, 3]
-    float *loss_sum;
+    float *loss_sum;        // [views]
     unsigned *nan_counts;
 };
 
 struct ProjectBwdArgs {
-    int n, rest_bases, do_optimizer;
-    float Wf, Hf;
-    const StepParams *sp;
+    ViewTable vt;
+    int rest_bases, do_optimizer;
+    const StepParams *sp;   // [views]; the optimizer scalars are view 0's
     const float *means, *scales, *quats;
-    const int *radii;
-    const SplatRec *rec;
-    const GradRec *grad;
-    float *v_mean, *v_scale, *v_quat;
+    const int *radii;       // [views, n]
+    const SplatRec *rec;    // [views, n]
+    const GradRec *grad;    // [views, n]
+    float *v_mean, *v_scale, *v_quat;   // [n]: summed over the views
+    float *v_opac;          // [n] summed opacity-logit gradient (several views; Adam reads it)
     float *features_dc, *features_rest, *dc_m, *dc_v, *rest_m, *rest_v;
-    // gradient export (no optimizer): when set, the SH gradients and the
-    // opacity-logit gradient are written here instead of feeding Adam
+    // gradient export (one view, no optimizer): when set, the SH gradients
+    // and the opacity-logit gradient are written here instead of feeding Adam
     float *v_dc_out, *v_rest_out, *v_opac_out;
     // per-Gaussian activity statistics for the learned relocation proposal
-    // (or null): x += |dL/d(pixel centre)| and y += 1 when visible, z += 1
+    // (or null): per view x += |dL/d(pixel centre)| and y += 1 when visible;
+    // z += 1 per step
     float4 *gstats;
-    // multi-view accumulation (no optimizer): v_mean / v_scale / v_quat and
-    // the buffers below are added to for the Gaussians visible in this view
-    int accumulate;
-    float *acc_opac, *acc_dc, *acc_rest;   // [N], [N,3], [N,rest,3]
-    uint8_t *acc_vis;                      // 1 once visible in any view
     unsigned *nan_counts;
 };
 
@@ -104,18 +127,6 @@ struct AdamArgs {
     const GradRec *grad;         // opacity gradient in grad[i].a.z
     const float *dc_v;           // features_dc second moment (regularizer duty)
     const float *g_opac;         // opacity gradient [N] in place of grad[i].a.z, or null
-    unsigned *nan_counts;
-};
-
-// Adam on the SH groups from accumulated gradients (multi-view steps): the
-// elements of Gaussians visible in at least one view, bands below
-// degrees_to_use (the fused per-view SH Adam's rule over the union)
-struct ShAdamArgs {
-    int n, rest_bases;
-    const StepParams *sp;
-    float *features_dc, *features_rest, *dc_m, *dc_v, *rest_m, *rest_v;
-    const float *acc_dc, *acc_rest;
-    const uint8_t *acc_vis;
     unsigned *nan_counts;
 };
 
@@ -141,18 +152,16 @@ struct McmcResult {
 void debug_sync(cudaStream_t s, const char *what);
 
 void launch_project_fwd(const ProjectArgs &a, cudaStream_t s);
-int launch_tiles(const TileArgs &a, int num_sms, cudaStream_t s);
-
-   // returns the kernel launches
+int launch_tiles(const TileArgs &a, int num_sms, cudaStream_t s);   // returns the kernel launches
 size_t sort_pack_smem_bytes();
-size_t tile_cta_bins_bytes(int n, int num_tiles);   // 0 when the block-aggregated path is not used
+// cta_bins bytes for these views, 0 when the block-aggregated path is not used
+size_t tile_cta_bins_bytes(const ViewTable &vt);
 void launch_raster_fwd(const RasterArgs &a, cudaStream_t s);
 void launch_loss(const LossArgs &a, cudaStream_t s);
 void launch_raster_bwd(const RasterArgs &a, cudaStream_t s);
 void launch_project_bwd(const ProjectBwdArgs &a, cudaStream_t s);
 void launch_adam(const AdamArgs &a, int num_sms, cudaStream_t s);
 void launch_sgld(const AdamArgs &a, cudaStream_t s);
-void launch_sh_adam(const ShAdamArgs &a, cudaStream_t s);
 void run_mcmc(McmcArgs a, int cap_max, int &relocation_count, McmcResult &res, cudaStream_t s);
 
 }  // namespace msplat

@@ -170,50 +170,6 @@ void launch_adam(const AdamArgs &a, int num_sms, cudaStream_t s) {
     k_adam<<<(unsigned)blocks, 256, 0, s>>>(a);
 }
 
-// SH Adam from accumulated gradients: one thread per coefficient of
-// [features_dc | features_rest]; same update as the fused per-view SH Adam
-__global__ void __launch_bounds__(256) k_sh_adam(ShAdamArgs a) {
-    const StepParams &sp = *a.sp;
-    const int rowf = 3 * a.rest_bases;
-    const long long ndc = 3LL * a.n, total = ndc + (long long)rowf * a.n;
-    const int deg = sp.degrees_to_use;
-    int nb = deg >= 3 ? 15 : deg == 2 ? 8 : deg == 1 ? 3 : 0;
-    nb = min(nb, a.rest_bases);
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
-         e += (long long)gridDim.x * blockDim.x) {
-        float *p, *m, *v;
-        float g;
-        int grp;
-        long long j;
-        if (e < ndc) {
-            j = e;
-            if (!a.acc_vis[j / 3]) continue;
-            p = a.features_dc; m = a.dc_m; v = a.dc_v; g = a.acc_dc[j]; grp = 3;
-        } else {
-            j = e - ndc;
-            const long long gi = j / rowf;
-            const int band = (int)(j - gi * rowf) / 3;
-            if (!a.acc_vis[gi] || band >= nb) continue;
-            p = a.features_rest; m = a.rest_m; v = a.rest_v; g = a.acc_rest[j]; grp = 4;
-        }
-        if (!finite_bits(g)) continue;
-        const float b1 = sp.beta1, b2 = sp.beta2;
-        const float mm = fmaf(b1, m[j], (1.0f - b1) * g);
-        const float vv = fmaf(b2, v[j], (1.0f - b2) * g * g);
-        p[j] -= sp.step_size[grp] * mm / (sqrtf(vv) / sp.bc2_sqrt[grp] + sp.eps);
-        m[j] = mm;
-        v[j] = vv;
-    }
-}
-
-void launch_sh_adam(const ShAdamArgs &a, cudaStream_t s) {
-    if (a.n <= 0) return;
-    const long long total = (3LL + 3LL * a.rest_bases) * a.n;
-    long long blocks = (total + 255) / 256;
-    if (blocks > 152LL * 8) blocks = 152LL * 8;
-    k_sh_adam<<<(unsigned)blocks, 256, 0, s>>>(a);
-}
-
 void launch_sgld(const AdamArgs &a, cudaStream_t s) {
     if (a.n <= 0) return;
     k_sgld<<<(a.n + 255) / 256, 256, 0, s>>>(a);

@@ -1,6 +1,10 @@
 // Projection VJP (centre, conic -> mean, log-scale, quaternion) with the SH
 // colour VJP fused straight into Adam for features_dc / features_rest, one
-// thread per Gaussian.  The 3D covariance is recomputed in registers.
+// thread per Gaussian.  The 3D covariance is recomputed in registers.  With
+// several views the thread walks the Gaussian's record in each view and
+// sums the gradients (the views' image gradients already carry 1/views), so
+// one launch ends the backward of the whole step and the SH Adam sees the
+// summed gradient.
 // Follows project_and_sh_backward_kernel (msplat_metal.metal:1860-2042) and
 // the VJPs it calls (:1252-1569): gradients flow to the raw quaternion as if
 // it were normalised, and bands above degrees_to_use are not updated.
@@ -26,14 +30,6 @@ __device__ __forceinline__ void adam_el(float *p, float *m, float *v, float g, f
     *v = vv;
 }
 
-// Per-warp staging of the SH Adam inputs: the basis values of the warp's 32
-// Gaussians and their colour gradients (w = number of rest bands to update,
-// 0 when the Gaussian is culled or its colour gradient is non-finite).
-struct ShStage {
-    float bas[32][16];
-    float4 vc[32];
-};
-
 __device__ __forceinline__ void adam4(float4 &p, float4 &m, float4 &v, const float g[4], unsigned active, float st,
                                       float bc, float b1, float b2, float eps) {
     float *pp = &p.x, *mm = &m.x, *vv = &v.x;
@@ -48,237 +44,202 @@ __device__ __forceinline__ void adam4(float4 &p, float4 &m, float4 &v, const flo
     }
 }
 
-// kRowF: floats per features_rest row when known at compile time (45 for SH
-// degree 3), so the element -> (Gaussian, band, channel) arithmetic of the SH
-// Adam walk uses constant divisors; 0 reads it from the arguments.
-template <int kRowF>
-__global__ void __launch_bounds__(256, 4) k_project_bwd(ProjectBwdArgs a) {
-    __shared__ ShStage stage[8];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    ShStage &sh = stage[wid];
-    const StepParams &sp = *a.sp;
-    sh.vc[lane] = make_float4(0.f, 0.f, 0.f, 0.f);   // w = 0: nothing to update
-    const bool want_sh = a.do_optimizer || a.v_dc_out || a.accumulate;
-    if (i < a.n) {
-        float *vmean = a.v_mean + 3 * (size_t)i, *vscale = a.v_scale + 3 * (size_t)i, *vquat = a.v_quat + 4 * (size_t)i;
-        if (a.v_opac_out) a.v_opac_out[i] = a.radii[i] > 0 ? a.grad[i].a.z : 0.f;
-        if (a.gstats) {
-            float4 st = a.gstats[i];
-            st.z += 1.f;
-            if (a.radii[i] > 0) {
-                const float4 g0 = a.grad[i].a;
-                st.x += sqrtf(g0.x * g0.x + g0.y * g0.y);
-                st.y += 1.f;
-            }
-            a.gstats[i] = st;
-        }
-        if (a.radii[i] <= 0) {
-            if (!a.accumulate) {
-                vmean[0] = vmean[1] = vmean[2] = 0.f;
-                vscale[0] = vscale[1] = vscale[2] = 0.f;
-                *reinterpret_cast<float4 *>(vquat) = make_float4(0.f, 0.f, 0.f, 0.f);
-            }
-        } else {
-            if (a.accumulate) {
-                a.acc_opac[i] += a.grad[i].a.z;
-                a.acc_vis[i] = 1;
-            }
-            const GradRec gr = a.grad[i];
-            const SplatRec rec = a.rec[i];
-            const float px = a.means[3 * i], py = a.means[3 * i + 1], pz = a.means[3 * i + 2];
 
-            // project_pix_vjp
-            const float *m = sp.projmat;
-            const float hw = m[12] * px + m[13] * py + m[14] * pz + m[15];
-            const float rw = 1.f / (hw + 1e-6f);
-            const float vnx = 0.5f * a.Wf * gr.a.x, vny = 0.5f * a.Hf * gr.a.y;
-            const float vp0 = vnx * rw, vp1 = vny * rw;
-            float vm[3];
-#pragma unroll
-            for (int c = 0; c < 3; c++) vm[c] = m[c] * vp0 + m[4 + c] * vp1;
+// Per-warp staging of the SH Adam inputs, one view: the basis values of the
+// warp's 32 Gaussians and their colour gradients (w = number of rest bands
+// to update + 1, 0 when the Gaussian is culled or its colour gradient is
+// non-finite).
+struct ShStage {
+    float bas[32][16];
+    float4 vc[32];
+};
 
-            // cov2d_to_conic_vjp: v_Sigma = -X G X
-            const float X00 = rec.b.x, X01 = rec.b.y, X11 = rec.b.z;
-            const float G00 = gr.b.x, G01 = gr.b.y, G11 = gr.b.z;
-            const float XG00 = X00 * G00 + X01 * G01, XG01 = X00 * G01 + X01 * G11;
-            const float XG10 = X01 * G00 + X11 * G01, XG11 = X01 * G01 + X11 * G11;
-            const float VS00 = -(XG00 * X00 + XG01 * X01), VS01 = -(XG00 * X01 + XG01 * X11);
-            const float VS10 = -(XG10 * X00 + XG11 * X01), VS11 = -(XG10 * X01 + XG11 * X11);
-            const float c00 = VS00, c01 = 0.5f * (VS10 + VS01), c11 = VS11;
+// Several views: the summed SH coefficient gradients of the warp's 32
+// Gaussians (rest bands 0..14 x 3 channels, then DC x 3; row padded to 49
+// floats so that lanes walking their own rows do not share banks) and w.
+constexpr int kAccRow = 49;
+struct ShAccStage {
+    float g[32][kAccRow];
+    int w[32];
+};
 
-            // recompute cov3d
-            float s[3];
-#pragma unroll
-            for (int k = 0; k < 3; k++) s[k] = det_expf(fminf(fmaxf(a.scales[3 * i + k], -15.f), 15.f));
-            const float4 q = *reinterpret_cast<const float4 *>(a.quats + 4 * (size_t)i);
-            const float qn = 1.0f / sqrtf(fmaxf(q.w * q.w + q.x * q.x + q.y * q.y + q.z * q.z, 1e-8f));
-            const float w = q.x * qn, x = q.y * qn, y = q.z * qn, z = q.w * qn;
-            float R[3][3];
-            R[0][0] = 1.f - 2.f * (y * y + z * z); R[1][0] = 2.f * (x * y + w * z); R[2][0] = 2.f * (x * z - w * y);
-            R[0][1] = 2.f * (x * y - w * z); R[1][1] = 1.f - 2.f * (x * x + z * z); R[2][1] = 2.f * (y * z + w * x);
-            R[0][2] = 2.f * (x * z + w * y); R[1][2] = 2.f * (y * z - w * x); R[2][2] = 1.f - 2.f * (x * x + y * y);
-            float M[3][3], V[3][3];
-#pragma unroll
-            for (int r = 0; r < 3; r++)
-#pragma unroll
-                for (int c = 0; c < 3; c++) M[r][c] = R[r][c] * s[c];
-#pragma unroll
-            for (int r = 0; r < 3; r++)
-#pragma unroll
-                for (int c = 0; c < 3; c++) V[r][c] = M[r][0] * M[c][0] + M[r][1] * M[c][1] + M[r][2] * M[c][2];
+// View-independent state of one Gaussian: mean, scales, normalised
+// quaternion, rotation, M = R S and the 3D covariance V = M M^T.
+struct CovState {
+    float px, py, pz;
+    float s[3];
+    float w, x, y, z;
+    float R[3][3], M[3][3], V[3][3];
+};
 
-            // project_cov3d_ewa_vjp
-            const float *v = sp.viewmat;
-            const float vx = v[0] * px + v[1] * py + v[2] * pz + v[3];
-            const float vy = v[4] * px + v[5] * py + v[6] * pz + v[7];
-            const float vz = v[8] * px + v[9] * py + v[10] * pz + v[11];
-            const float lim_x = 1.3f * sp.tan_fovx, lim_y = 1.3f * sp.tan_fovy;
-            const float cvx = vz * fminf(lim_x, fmaxf(-lim_x, vx / vz));
-            const float cvy = vz * fminf(lim_y, fmaxf(-lim_y, vy / vz));
-            const float rz = 1.f / vz, rz2 = rz * rz, rz3 = rz2 * rz;
-            // rows 0, 1 of T = J W (row 2 of J is zero)
-            const float j00 = sp.fx * rz, j11 = sp.fy * rz, j02 = -sp.fx * cvx * rz2, j12 = -sp.fy * cvy * rz2;
-            float T0[3], T1[3];
+__device__ __forceinline__ void cov_state(const ProjectBwdArgs &a, int i, CovState &cs) {
+    cs.px = a.means[3 * i]; cs.py = a.means[3 * i + 1]; cs.pz = a.means[3 * i + 2];
 #pragma unroll
-            for (int c = 0; c < 3; c++) {
-                T0[c] = j00 * v[c] + j02 * v[8 + c];
-                T1[c] = j11 * v[4 + c] + j12 * v[8 + c];
-            }
-            // v_V = T^T v_cov T
-            float vV[3][3];
+    for (int k = 0; k < 3; k++) cs.s[k] = det_expf(fminf(fmaxf(a.scales[3 * i + k], -15.f), 15.f));
+    const float4 q = *reinterpret_cast<const float4 *>(a.quats + 4 * (size_t)i);
+    const float qn = 1.0f / sqrtf(fmaxf(q.w * q.w + q.x * q.x + q.y * q.y + q.z * q.z, 1e-8f));
+    const float w = q.x * qn, x = q.y * qn, y = q.z * qn, z = q.w * qn;
+    cs.w = w; cs.x = x; cs.y = y; cs.z = z;
+    float (&R)[3][3] = cs.R;
+    R[0][0] = 1.f - 2.f * (y * y + z * z); R[1][0] = 2.f * (x * y + w * z); R[2][0] = 2.f * (x * z - w * y);
+    R[0][1] = 2.f * (x * y - w * z); R[1][1] = 1.f - 2.f * (x * x + z * z); R[2][1] = 2.f * (y * z + w * x);
+    R[0][2] = 2.f * (x * z + w * y); R[1][2] = 2.f * (y * z - w * x); R[2][2] = 1.f - 2.f * (x * x + y * y);
 #pragma unroll
-            for (int r = 0; r < 3; r++)
+    for (int r = 0; r < 3; r++)
 #pragma unroll
-                for (int c = 0; c < 3; c++)
-                    vV[r][c] = (T0[r] * c00 + T1[r] * c01) * T0[c] + (T0[r] * c01 + T1[r] * c11) * T1[c];
-            // v_T = 2 v_cov T V (rows 0, 1), v_J = v_T W^T
-            float TV0[3], TV1[3];
+        for (int c = 0; c < 3; c++) cs.M[r][c] = R[r][c] * cs.s[c];
 #pragma unroll
-            for (int c = 0; c < 3; c++) {
-                TV0[c] = T0[0] * V[0][c] + T0[1] * V[1][c] + T0[2] * V[2][c];
-                TV1[c] = T1[0] * V[0][c] + T1[1] * V[1][c] + T1[2] * V[2][c];
-            }
-            float vT0[3], vT1[3];
+    for (int r = 0; r < 3; r++)
 #pragma unroll
-            for (int c = 0; c < 3; c++) {
-                vT0[c] = 2.f * (c00 * TV0[c] + c01 * TV1[c]);
-                vT1[c] = 2.f * (c01 * TV0[c] + c11 * TV1[c]);
-            }
-            const float vJ00 = vT0[0] * v[0] + vT0[1] * v[1] + vT0[2] * v[2];
-            const float vJ02 = vT0[0] * v[8] + vT0[1] * v[9] + vT0[2] * v[10];
-            const float vJ11 = vT1[0] * v[4] + vT1[1] * v[5] + vT1[2] * v[6];
-            const float vJ12 = vT1[0] * v[8] + vT1[1] * v[9] + vT1[2] * v[10];
-            const float fxr = sp.fx * rz2, fyr = sp.fy * rz2;
-            const float vt0 = -fxr * vJ02, vt1 = -fyr * vJ12;
-            const float vt2 = -fxr * vJ00 + 2.f * sp.fx * cvx * rz3 * vJ02 - fyr * vJ11 + 2.f * sp.fy * cvy * rz3 * vJ12;
-#pragma unroll
-            for (int c = 0; c < 3; c++) vm[c] += vt0 * v[c] + vt1 * v[4 + c] + vt2 * v[8 + c];
-            if (a.accumulate) {
-                vmean[0] += vm[0]; vmean[1] += vm[1]; vmean[2] += vm[2];
-            } else {
-                vmean[0] = vm[0]; vmean[1] = vm[1]; vmean[2] = vm[2];
-            }
+        for (int c = 0; c < 3; c++)
+            cs.V[r][c] = cs.M[r][0] * cs.M[c][0] + cs.M[r][1] * cs.M[c][1] + cs.M[r][2] * cs.M[c][2];
+}
 
-            // scale_rot_to_cov3d_vjp + quat_to_rotmat_vjp
-            const float v01 = 0.5f * (vV[0][1] + vV[1][0]), v02 = 0.5f * (vV[0][2] + vV[2][0]);
-            const float v12 = 0.5f * (vV[1][2] + vV[2][1]);
-            const float vVs[3][3] = {{vV[0][0], v01, v02}, {v01, vV[1][1], v12}, {v02, v12, vV[2][2]}};
-            float gR[3][3];
+// One view's VJP (project_pix_vjp, cov2d_to_conic_vjp, project_cov3d_ewa_vjp,
+// scale_rot_to_cov3d_vjp, quat_to_rotmat_vjp) added into vm, vsc, vq.
+__device__ __forceinline__ void view_vjp(const CovState &cs, const StepParams &sp, float Wf, float Hf,
+                                         const GradRec &gr, const SplatRec &rec, float vm[3], float vsc[3],
+                                         float vq[4]) {
+    const float px = cs.px, py = cs.py, pz = cs.pz;
+    // project_pix_vjp
+    const float *m = sp.projmat;
+    const float hw = m[12] * px + m[13] * py + m[14] * pz + m[15];
+    const float rw = 1.f / (hw + 1e-6f);
+    const float vnx = 0.5f * Wf * gr.a.x, vny = 0.5f * Hf * gr.a.y;
+    const float vp0 = vnx * rw, vp1 = vny * rw;
+    float gm[3];
 #pragma unroll
-            for (int c = 0; c < 3; c++) {
-                float acc = 0.f;
-#pragma unroll
-                for (int r = 0; r < 3; r++) {
-                    const float vMrc = 2.f * (vVs[r][0] * M[0][c] + vVs[r][1] * M[1][c] + vVs[r][2] * M[2][c]);
-                    acc += R[r][c] * vMrc;
-                    gR[r][c] = vMrc * s[c];
-                }
-                vscale[c] = a.accumulate ? vscale[c] + acc * s[c] : acc * s[c];
-            }
-            // gR[row][col]; the reference indexes v_R[col][row]
-            float4 vq;
-            vq.x = 2.f * (x * (gR[2][1] - gR[1][2]) + y * (gR[0][2] - gR[2][0]) + z * (gR[1][0] - gR[0][1]));
-            vq.y = 2.f * (-2.f * x * (gR[1][1] + gR[2][2]) + y * (gR[1][0] + gR[0][1]) + z * (gR[2][0] + gR[0][2]) +
-                          w * (gR[2][1] - gR[1][2]));
-            vq.z = 2.f * (x * (gR[1][0] + gR[0][1]) - 2.f * y * (gR[0][0] + gR[2][2]) + z * (gR[2][1] + gR[1][2]) +
-                          w * (gR[0][2] - gR[2][0]));
-            vq.w = 2.f * (x * (gR[2][0] + gR[0][2]) + y * (gR[2][1] + gR[1][2]) - 2.f * z * (gR[0][0] + gR[1][1]) +
-                          w * (gR[1][0] - gR[0][1]));
-            if (a.accumulate) {
-                const float4 o = *reinterpret_cast<const float4 *>(vquat);
-                vq.x += o.x; vq.y += o.y; vq.z += o.z; vq.w += o.w;
-            }
-            *reinterpret_cast<float4 *>(vquat) = vq;
+    for (int c = 0; c < 3; c++) gm[c] = m[c] * vp0 + m[4 + c] * vp1;
 
-            // SH VJP inputs for the fused Adam (or the gradient export) below
-            if (want_sh) {
-                const float vc0 = gr.c.x, vc1 = gr.c.y, vc2 = gr.c.z;
-                if (!(finite_bits(vc0) && finite_bits(vc1) && finite_bits(vc2))) {
-                    if (a.nan_counts) atomicAdd(a.nan_counts + kNanSH, 1u);
-                } else {
-                    const int deg = sp.degrees_to_use;
-                    int nb = deg >= 3 ? 15 : deg == 2 ? 8 : deg == 1 ? 3 : 0;
-                    nb = min(nb, a.rest_bases);
-                    const float dx = px - sp.cam_pos[0], dy = py - sp.cam_pos[1], dz = pz - sp.cam_pos[2];
-                    const float inv = 1.f / sqrtf(dx * dx + dy * dy + dz * dz);
-                    const float X = dx * inv, Y = dy * inv, Z = dz * inv;
-                    const float xx = X * X, xy = X * Y, xz = X * Z, yy = Y * Y, yz = Y * Z, zz = Z * Z;
-                    float *b = sh.bas[lane];
-                    b[0] = -kBC1 * Y; b[1] = kBC1 * Z; b[2] = -kBC1 * X;
-                    b[3] = kBC2[0] * xy; b[4] = kBC2[1] * yz; b[5] = kBC2[2] * (2.f * zz - xx - yy);
-                    b[6] = kBC2[3] * xz; b[7] = kBC2[4] * (xx - yy);
-                    b[8] = kBC3[0] * Y * (3.f * xx - yy); b[9] = kBC3[1] * xy * Z;
-                    b[10] = kBC3[2] * Y * (4.f * zz - xx - yy); b[11] = kBC3[3] * Z * (2.f * zz - 3.f * xx - 3.f * yy);
-                    b[12] = kBC3[4] * X * (4.f * zz - xx - yy); b[13] = kBC3[5] * Z * (xx - yy);
-                    b[14] = kBC3[6] * X * (xx - 3.f * yy);
-                    b[15] = kBC0;
-                    sh.vc[lane] = make_float4(vc0, vc1, vc2, __int_as_float(nb + 1));   // w - 1 = rest bands
-                }
-            }
-        }
+    // cov2d_to_conic_vjp: v_Sigma = -X G X
+    const float X00 = rec.b.x, X01 = rec.b.y, X11 = rec.b.z;
+    const float G00 = gr.b.x, G01 = gr.b.y, G11 = gr.b.z;
+    const float XG00 = X00 * G00 + X01 * G01, XG01 = X00 * G01 + X01 * G11;
+    const float XG10 = X01 * G00 + X11 * G01, XG11 = X01 * G01 + X11 * G11;
+    const float VS00 = -(XG00 * X00 + XG01 * X01), VS01 = -(XG00 * X01 + XG01 * X11);
+    const float VS10 = -(XG10 * X00 + XG11 * X01), VS11 = -(XG10 * X01 + XG11 * X11);
+    const float c00 = VS00, c01 = 0.5f * (VS10 + VS01), c11 = VS11;
+
+    // project_cov3d_ewa_vjp
+    const float *v = sp.viewmat;
+    const float vx = v[0] * px + v[1] * py + v[2] * pz + v[3];
+    const float vy = v[4] * px + v[5] * py + v[6] * pz + v[7];
+    const float vz = v[8] * px + v[9] * py + v[10] * pz + v[11];
+    const float lim_x = 1.3f * sp.tan_fovx, lim_y = 1.3f * sp.tan_fovy;
+    const float cvx = vz * fminf(lim_x, fmaxf(-lim_x, vx / vz));
+    const float cvy = vz * fminf(lim_y, fmaxf(-lim_y, vy / vz));
+    const float rz = 1.f / vz, rz2 = rz * rz, rz3 = rz2 * rz;
+    // rows 0, 1 of T = J W (row 2 of J is zero)
+    const float j00 = sp.fx * rz, j11 = sp.fy * rz, j02 = -sp.fx * cvx * rz2, j12 = -sp.fy * cvy * rz2;
+    float T0[3], T1[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        T0[c] = j00 * v[c] + j02 * v[8 + c];
+        T1[c] = j11 * v[4 + c] + j12 * v[8 + c];
     }
-    if (!want_sh) return;
-    __syncwarp();
-    // fused SH Adam, warp-cooperative: the warp's 32 Gaussians own contiguous
-    // rows of features_dc / features_rest and their moments, walked with
-    // coalesced 16-byte accesses (the element's Gaussian, band and channel
-    // are recovered from its offset in the rows).
-    const int i0 = (blockIdx.x * blockDim.x) + wid * 32;
-    if (i0 >= a.n) return;
-    const int ng = min(32, a.n - i0);
-    if (a.accumulate) {
-        // add dL/d(SH coefficient) of the active elements into the accumulators
-        for (int e = lane; e < 3 * ng; e += 32) {
-            const int gi = e / 3, c = e - 3 * gi;
-            const float4 vc = sh.vc[gi];
-            if (__float_as_int(vc.w) > 0)
-                a.acc_dc[3 * (size_t)i0 + e] += sh.bas[gi][15] * (c == 0 ? vc.x : c == 1 ? vc.y : vc.z);
-        }
-        const int rowf = 3 * a.rest_bases;
-        for (int e = lane; e < rowf * ng; e += 32) {
-            const int gi = e / rowf, r = e - rowf * gi, band = r / 3, c = r - 3 * band;
-            const float4 vc = sh.vc[gi];
-            if (band < __float_as_int(vc.w) - 1)
-                a.acc_rest[(size_t)rowf * i0 + e] += sh.bas[gi][band] * (c == 0 ? vc.x : c == 1 ? vc.y : vc.z);
-        }
-        return;
+    // v_V = T^T v_cov T
+    float vV[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+            vV[r][c] = (T0[r] * c00 + T1[r] * c01) * T0[c] + (T0[r] * c01 + T1[r] * c11) * T1[c];
+    // v_T = 2 v_cov T V (rows 0, 1), v_J = v_T W^T
+    float TV0[3], TV1[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        TV0[c] = T0[0] * cs.V[0][c] + T0[1] * cs.V[1][c] + T0[2] * cs.V[2][c];
+        TV1[c] = T1[0] * cs.V[0][c] + T1[1] * cs.V[1][c] + T1[2] * cs.V[2][c];
     }
+    float vT0[3], vT1[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        vT0[c] = 2.f * (c00 * TV0[c] + c01 * TV1[c]);
+        vT1[c] = 2.f * (c01 * TV0[c] + c11 * TV1[c]);
+    }
+    const float vJ00 = vT0[0] * v[0] + vT0[1] * v[1] + vT0[2] * v[2];
+    const float vJ02 = vT0[0] * v[8] + vT0[1] * v[9] + vT0[2] * v[10];
+    const float vJ11 = vT1[0] * v[4] + vT1[1] * v[5] + vT1[2] * v[6];
+    const float vJ12 = vT1[0] * v[8] + vT1[1] * v[9] + vT1[2] * v[10];
+    const float fxr = sp.fx * rz2, fyr = sp.fy * rz2;
+    const float vt0 = -fxr * vJ02, vt1 = -fyr * vJ12;
+    const float vt2 = -fxr * vJ00 + 2.f * sp.fx * cvx * rz3 * vJ02 - fyr * vJ11 + 2.f * sp.fy * cvy * rz3 * vJ12;
+#pragma unroll
+    for (int c = 0; c < 3; c++) vm[c] += gm[c] + (vt0 * v[c] + vt1 * v[4 + c] + vt2 * v[8 + c]);
+
+    // scale_rot_to_cov3d_vjp + quat_to_rotmat_vjp
+    const float v01 = 0.5f * (vV[0][1] + vV[1][0]), v02 = 0.5f * (vV[0][2] + vV[2][0]);
+    const float v12 = 0.5f * (vV[1][2] + vV[2][1]);
+    const float vVs[3][3] = {{vV[0][0], v01, v02}, {v01, vV[1][1], v12}, {v02, v12, vV[2][2]}};
+    float gR[3][3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        float acc = 0.f;
+#pragma unroll
+        for (int r = 0; r < 3; r++) {
+            const float vMrc = 2.f * (vVs[r][0] * cs.M[0][c] + vVs[r][1] * cs.M[1][c] + vVs[r][2] * cs.M[2][c]);
+            acc += cs.R[r][c] * vMrc;
+            gR[r][c] = vMrc * cs.s[c];
+        }
+        vsc[c] += acc * cs.s[c];
+    }
+    // gR[row][col]; the reference indexes v_R[col][row]
+    const float w = cs.w, x = cs.x, y = cs.y, z = cs.z;
+    vq[0] += 2.f * (x * (gR[2][1] - gR[1][2]) + y * (gR[0][2] - gR[2][0]) + z * (gR[1][0] - gR[0][1]));
+    vq[1] += 2.f * (-2.f * x * (gR[1][1] + gR[2][2]) + y * (gR[1][0] + gR[0][1]) + z * (gR[2][0] + gR[0][2]) +
+                    w * (gR[2][1] - gR[1][2]));
+    vq[2] += 2.f * (x * (gR[1][0] + gR[0][1]) - 2.f * y * (gR[0][0] + gR[2][2]) + z * (gR[2][1] + gR[1][2]) +
+                    w * (gR[0][2] - gR[2][0]));
+    vq[3] += 2.f * (x * (gR[2][0] + gR[0][2]) + y * (gR[2][1] + gR[1][2]) - 2.f * z * (gR[0][0] + gR[1][1]) +
+                    w * (gR[1][0] - gR[0][1]));
+}
+
+// SH basis (bands 1..3 in b[0..14], the DC constant in b[15]) of the
+// direction from the camera to the Gaussian
+__device__ __forceinline__ void sh_basis(const CovState &cs, const StepParams &sp, float b[16]) {
+    const float dx = cs.px - sp.cam_pos[0], dy = cs.py - sp.cam_pos[1], dz = cs.pz - sp.cam_pos[2];
+    const float inv = 1.f / sqrtf(dx * dx + dy * dy + dz * dz);
+    const float X = dx * inv, Y = dy * inv, Z = dz * inv;
+    const float xx = X * X, xy = X * Y, xz = X * Z, yy = Y * Y, yz = Y * Z, zz = Z * Z;
+    b[0] = -kBC1 * Y; b[1] = kBC1 * Z; b[2] = -kBC1 * X;
+    b[3] = kBC2[0] * xy; b[4] = kBC2[1] * yz; b[5] = kBC2[2] * (2.f * zz - xx - yy);
+    b[6] = kBC2[3] * xz; b[7] = kBC2[4] * (xx - yy);
+    b[8] = kBC3[0] * Y * (3.f * xx - yy); b[9] = kBC3[1] * xy * Z;
+    b[10] = kBC3[2] * Y * (4.f * zz - xx - yy); b[11] = kBC3[3] * Z * (2.f * zz - 3.f * xx - 3.f * yy);
+    b[12] = kBC3[4] * X * (4.f * zz - xx - yy); b[13] = kBC3[5] * Z * (xx - yy);
+    b[14] = kBC3[6] * X * (xx - 3.f * yy);
+    b[15] = kBC0;
+}
+
+__device__ __forceinline__ int bands_in_use(const StepParams &sp, int rest_bases) {
+    const int deg = sp.degrees_to_use;
+    const int nb = deg >= 3 ? 15 : deg == 2 ? 8 : deg == 1 ? 3 : 0;
+    return min(nb, rest_bases);
+}
+
+// Fused SH Adam (or the gradient export), warp-cooperative: the warp's 32
+// Gaussians own contiguous rows of features_dc / features_rest and their
+// moments, walked with coalesced 16-byte accesses (the element's Gaussian,
+// band and channel are recovered from its offset in the rows).
+// grad(gi, band, c, g) -> true with g set when the element is updated;
+// band 15 is the DC band.
+template <int kRowF, class GradFn>
+__device__ __forceinline__ void sh_update(const ProjectBwdArgs &a, const StepParams &sp, int i0, int ng, int lane,
+                                          GradFn grad) {
     if (a.v_dc_out) {
-        // export: dL/d(SH coefficient) = basis value x colour gradient, zero
-        // where Adam would not update (culled, non-finite, band not in use)
+        // export: zero where Adam would not update (culled, non-finite, band not in use)
         for (int e = lane; e < 3 * ng; e += 32) {
             const int gi = e / 3, c = e - 3 * gi;
-            const float4 vc = sh.vc[gi];
-            a.v_dc_out[3 * (size_t)i0 + e] =
-                __float_as_int(vc.w) > 0 ? sh.bas[gi][15] * (c == 0 ? vc.x : c == 1 ? vc.y : vc.z) : 0.f;
+            float g = 0.f;
+            if (!grad(gi, 15, c, g)) g = 0.f;
+            a.v_dc_out[3 * (size_t)i0 + e] = g;
         }
         const int rowf = 3 * a.rest_bases;
         for (int e = lane; e < rowf * ng; e += 32) {
             const int gi = e / rowf, r = e - rowf * gi, band = r / 3, c = r - 3 * band;
-            const float4 vc = sh.vc[gi];
-            a.v_rest_out[(size_t)rowf * i0 + e] =
-                band < __float_as_int(vc.w) - 1 ? sh.bas[gi][band] * (c == 0 ? vc.x : c == 1 ? vc.y : vc.z) : 0.f;
+            float g = 0.f;
+            if (!grad(gi, band, c, g)) g = 0.f;
+            a.v_rest_out[(size_t)rowf * i0 + e] = g;
         }
         return;
     }
@@ -296,11 +257,7 @@ __global__ void __launch_bounds__(256, 4) k_project_bwd(ProjectBwdArgs a) {
                 g[k] = 0.f;
                 if (e < total) {
                     const int gi = e / 3, c = e - 3 * gi;
-                    const float4 vc = sh.vc[gi];
-                    if (__float_as_int(vc.w) > 0) {
-                        g[k] = sh.bas[gi][15] * (c == 0 ? vc.x : c == 1 ? vc.y : vc.z);
-                        act |= 1u << k;
-                    }
+                    if (grad(gi, 15, c, g[k])) act |= 1u << k;
                 }
             }
             if (!act) continue;
@@ -349,11 +306,7 @@ __global__ void __launch_bounds__(256, 4) k_project_bwd(ProjectBwdArgs a) {
                     g[k] = 0.f;
                     if (e0 + k < total) {
                         const int band = r / 3, c = r - 3 * band;
-                        const float4 vc = sh.vc[gi];
-                        if (band < __float_as_int(vc.w) - 1) {
-                            g[k] = sh.bas[gi][band] * (c == 0 ? vc.x : c == 1 ? vc.y : vc.z);
-                            act |= 1u << k;
-                        }
+                        if (grad(gi, band, c, g[k])) act |= 1u << k;
                     }
                     if (++r == rowf) { r = 0; gi++; }
                 }
@@ -372,10 +325,151 @@ __global__ void __launch_bounds__(256, 4) k_project_bwd(ProjectBwdArgs a) {
     }
 }
 
+// One view.  kRowF: floats per features_rest row when known at compile time
+// (45 for SH degree 3), so the element -> (Gaussian, band, channel)
+// arithmetic of the SH walk uses constant divisors; 0 reads it from the
+// arguments.
+template <int kRowF>
+__global__ void __launch_bounds__(256, 4) k_project_bwd(ProjectBwdArgs a) {
+    __shared__ ShStage stage[8];
+    const int n = a.vt.n;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    ShStage &sh = stage[wid];
+    const StepParams &sp = a.sp[0];
+    sh.vc[lane] = make_float4(0.f, 0.f, 0.f, 0.f);   // w = 0: nothing to update
+    const bool want_sh = a.do_optimizer || a.v_dc_out;
+    if (i < n) {
+        float *vmean = a.v_mean + 3 * (size_t)i, *vscale = a.v_scale + 3 * (size_t)i, *vquat = a.v_quat + 4 * (size_t)i;
+        if (a.v_opac_out) a.v_opac_out[i] = a.radii[i] > 0 ? a.grad[i].a.z : 0.f;
+        if (a.gstats) {
+            float4 st = a.gstats[i];
+            st.z += 1.f;
+            if (a.radii[i] > 0) {
+                const float4 g0 = a.grad[i].a;
+                st.x += sqrtf(g0.x * g0.x + g0.y * g0.y);
+                st.y += 1.f;
+            }
+            a.gstats[i] = st;
+        }
+        float vm[3] = {0.f, 0.f, 0.f}, vsc[3] = {0.f, 0.f, 0.f}, vq[4] = {0.f, 0.f, 0.f, 0.f};
+        if (a.radii[i] > 0) {
+            const GradRec gr = a.grad[i];
+            CovState cs;
+            cov_state(a, i, cs);
+            view_vjp(cs, sp, (float)a.vt.width[0], (float)a.vt.height[0], gr, a.rec[i], vm, vsc, vq);
+            // SH VJP inputs for the fused Adam (or the gradient export) below
+            if (want_sh) {
+                const float vc0 = gr.c.x, vc1 = gr.c.y, vc2 = gr.c.z;
+                if (!(finite_bits(vc0) && finite_bits(vc1) && finite_bits(vc2))) {
+                    if (a.nan_counts) atomicAdd(a.nan_counts + kNanSH, 1u);
+                } else {
+                    sh_basis(cs, sp, sh.bas[lane]);
+                    sh.vc[lane] = make_float4(vc0, vc1, vc2, __int_as_float(bands_in_use(sp, a.rest_bases) + 1));
+                }
+            }
+        }
+        vmean[0] = vm[0]; vmean[1] = vm[1]; vmean[2] = vm[2];
+        vscale[0] = vsc[0]; vscale[1] = vsc[1]; vscale[2] = vsc[2];
+        *reinterpret_cast<float4 *>(vquat) = make_float4(vq[0], vq[1], vq[2], vq[3]);
+    }
+    if (!want_sh) return;
+    __syncwarp();
+    const int i0 = (blockIdx.x * blockDim.x) + wid * 32;
+    if (i0 >= n) return;
+    sh_update<kRowF>(a, sp, i0, min(32, n - i0), lane, [&](int gi, int band, int c, float &g) {
+        const float4 vc = sh.vc[gi];
+        const int w = __float_as_int(vc.w);
+        if (band == 15 ? w <= 0 : band >= w - 1) return false;
+        g = sh.bas[gi][band] * (c == 0 ? vc.x : c == 1 ? vc.y : vc.z);
+        return true;
+    });
+}
+
+// Several views: the thread walks the Gaussian's record in every view of the
+// step and sums; the SH gradients are summed in shared memory; v_opac gets the
+// summed opacity-logit gradient.  A Gaussian visible in no view gets zero
+// gradients and no SH update.
+template <int kRowF>
+__global__ void __launch_bounds__(128, 4) k_project_bwd_views(ProjectBwdArgs a) {
+    __shared__ ShAccStage stage[4];
+    const int n = a.vt.n, views = a.vt.count;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    ShAccStage &sh = stage[wid];
+    const StepParams &sp0 = a.sp[0];
+    float *acc = sh.g[lane];
+#pragma unroll
+    for (int k = 0; k < 48; k++) acc[k] = 0.f;
+    sh.w[lane] = 0;
+    if (i < n) {
+        float vm[3] = {0.f, 0.f, 0.f}, vsc[3] = {0.f, 0.f, 0.f}, vq[4] = {0.f, 0.f, 0.f, 0.f};
+        float vop = 0.f, act_xy = 0.f, act_vis = 0.f;
+        bool any = false, sh_ok = false;
+        CovState cs;
+        const int nb = bands_in_use(sp0, a.rest_bases);
+        for (int v = 0; v < views; v++) {
+            const size_t u = (size_t)v * n + i;
+            if (a.radii[u] <= 0) continue;
+            if (!any) { cov_state(a, i, cs); any = true; }
+            const GradRec gr = a.grad[u];
+            const StepParams &sp = a.sp[v];
+            vop += gr.a.z;
+            act_xy += sqrtf(gr.a.x * gr.a.x + gr.a.y * gr.a.y);
+            act_vis += 1.f;
+            const ViewGeom vg = view_geom(a.vt, v);
+            view_vjp(cs, sp, (float)vg.width, (float)vg.height, gr, a.rec[u], vm, vsc, vq);
+            const float vc0 = gr.c.x, vc1 = gr.c.y, vc2 = gr.c.z;
+            if (!(finite_bits(vc0) && finite_bits(vc1) && finite_bits(vc2))) {
+                if (a.nan_counts) atomicAdd(a.nan_counts + kNanSH, 1u);
+                continue;
+            }
+            float b[16];
+            sh_basis(cs, sp, b);
+            acc[45] += b[15] * vc0; acc[46] += b[15] * vc1; acc[47] += b[15] * vc2;
+            for (int k = 0; k < nb; k++) {
+                acc[3 * k] += b[k] * vc0;
+                acc[3 * k + 1] += b[k] * vc1;
+                acc[3 * k + 2] += b[k] * vc2;
+            }
+            sh_ok = true;
+        }
+        if (sh_ok) sh.w[lane] = nb + 1;
+        float *vmean = a.v_mean + 3 * (size_t)i, *vscale = a.v_scale + 3 * (size_t)i, *vquat = a.v_quat + 4 * (size_t)i;
+        vmean[0] = vm[0]; vmean[1] = vm[1]; vmean[2] = vm[2];
+        vscale[0] = vsc[0]; vscale[1] = vsc[1]; vscale[2] = vsc[2];
+        *reinterpret_cast<float4 *>(vquat) = make_float4(vq[0], vq[1], vq[2], vq[3]);
+        a.v_opac[i] = vop;
+        if (a.gstats) {
+            float4 st = a.gstats[i];
+            st.x += act_xy;
+            st.y += act_vis;
+            st.z += 1.f;
+            a.gstats[i] = st;
+        }
+    }
+    if (!a.do_optimizer) return;
+    __syncwarp();
+    const int i0 = (blockIdx.x * blockDim.x) + wid * 32;
+    if (i0 >= n) return;
+    sh_update<kRowF>(a, sp0, i0, min(32, n - i0), lane, [&](int gi, int band, int c, float &g) {
+        const int w = sh.w[gi];
+        if (band == 15 ? w <= 0 : band >= w - 1) return false;
+        g = sh.g[gi][band == 15 ? 45 + c : 3 * band + c];
+        return true;
+    });
+}
+
 void launch_project_bwd(const ProjectBwdArgs &a, cudaStream_t s) {
-    if (a.n <= 0) return;
-    if (a.rest_bases == 15) k_project_bwd<45><<<(a.n + 255) / 256, 256, 0, s>>>(a);
-    else k_project_bwd<0><<<(a.n + 255) / 256, 256, 0, s>>>(a);
+    const int n = a.vt.n;
+    if (n <= 0) return;
+    if (a.vt.count > 1) {
+        if (a.rest_bases == 15) k_project_bwd_views<45><<<(n + 127) / 128, 128, 0, s>>>(a);
+        else k_project_bwd_views<0><<<(n + 127) / 128, 128, 0, s>>>(a);
+        return;
+    }
+    if (a.rest_bases == 15) k_project_bwd<45><<<(n + 255) / 256, 256, 0, s>>>(a);
+    else k_project_bwd<0><<<(n + 255) / 256, 256, 0, s>>>(a);
 }
 
 }  // namespace msplat

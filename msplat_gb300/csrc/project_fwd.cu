@@ -1,4 +1,5 @@
-// Fused EWA projection + spherical-harmonics colour, one thread per Gaussian.
+// Fused EWA projection + spherical-harmonics colour, one thread per
+// (Gaussian, view): blockIdx.y is the view, records land at v * n + i.
 // Follows project_and_sh_forward_kernel (msplat_metal.metal:1719-1834) and its
 // helpers (:53-344, :620-687).  Built with --fmad=false: every float operation
 // is rounded on its own, in the order the reference writes it, so radii, tile
@@ -19,16 +20,20 @@ __constant__ float kShC3[7] = {-0.5900435899266435f, 2.890611442640554f, -0.4570
 
 __global__ void __launch_bounds__(256) k_project_fwd(ProjectArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n) return;
-    const StepParams &sp = *a.sp;
+    if (i >= a.vt.n) return;
+    const int view = blockIdx.y;
+    const ViewGeom vg = view_geom(a.vt, view);
+    const size_t u = (size_t)view * a.vt.n + i;   // this view's record of Gaussian i
+    const StepParams &sp = a.sp[view];
+    const float Wf = (float)vg.width, Hf = (float)vg.height;
     // the rasterizer gradient record of every Gaussian starts the step at zero
     if (a.grad) {
-        a.grad[i].a = make_float4(0.f, 0.f, 0.f, 0.f);
-        a.grad[i].b = make_float4(0.f, 0.f, 0.f, 0.f);
-        a.grad[i].c = make_float4(0.f, 0.f, 0.f, 0.f);
+        a.grad[u].a = make_float4(0.f, 0.f, 0.f, 0.f);
+        a.grad[u].b = make_float4(0.f, 0.f, 0.f, 0.f);
+        a.grad[u].c = make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    a.radii[i] = 0;
-    a.tiles_hit[i] = 0;
+    a.radii[u] = 0;
+    a.tiles_hit[u] = 0;
 
     const float px = a.means[3 * i], py = a.means[3 * i + 1], pz = a.means[3 * i + 2];
     const float *v = sp.viewmat;
@@ -103,11 +108,11 @@ __global__ void __launch_bounds__(256) k_project_fwd(ProjectArgs a) {
     const float hw = m[12] * px + m[13] * py + m[14] * pz + m[15];
     const float rw = 1.f / (hw + 1e-6f);
     const float ndx = hx * rw, ndy = hy * rw;
-    const float cxp = 0.5f * a.Wf * ndx + sp.cx - 0.5f;
-    const float cyp = 0.5f * a.Hf * ndy + sp.cy - 0.5f;
+    const float cxp = 0.5f * Wf * ndx + sp.cx - 0.5f;
+    const float cyp = 0.5f * Hf * ndy + sp.cy - 0.5f;
     const float ax = ceilf(3.f * sqrtf(a2)), ay = ceilf(3.f * sqrtf(d2));
     int x0, y0, x1, y1;
-    tile_rect(cxp, cyp, ax, ay, a.tiles_x, a.tiles_y, x0, y0, x1, y1);
+    tile_rect(cxp, cyp, ax, ay, vg.tiles_x, vg.tiles_y, x0, y0, x1, y1);
     const int area = (x1 - x0) * (y1 - y0);
     if (area <= 0) return;
 
@@ -153,9 +158,9 @@ __global__ void __launch_bounds__(256) k_project_fwd(ProjectArgs a) {
     rec.a = make_float4(cxp, cyp, oko ? opac : 0.f, 0.f);
     rec.b = make_float4(ca, cb, cc, 0.f);
     rec.c = make_float4(col[0], col[1], col[2], 0.f);
-    a.rec[i] = rec;
-    a.depths[i] = vz;
-    a.aabb[i] = make_float2(ax, ay);
+    a.rec[u] = rec;
+    a.depths[u] = vz;
+    a.aabb[u] = make_float2(ax, ay);
 
     // zombie gate: a non-finite projection output culls the Gaussian this step
     const bool okc = finite_bits(cxp) && finite_bits(cyp), okd = finite_bits(vz);
@@ -163,8 +168,8 @@ __global__ void __launch_bounds__(256) k_project_fwd(ProjectArgs a) {
     const bool okn = finite_bits(ca) && finite_bits(cb) && finite_bits(cc);
     const bool okr = finite_bits(col[0]) && finite_bits(col[1]) && finite_bits(col[2]);
     if (okc && okd && oka && okn && okr) {
-        a.tiles_hit[i] = area;
-        a.radii[i] = __float2int_rz(radius);
+        a.tiles_hit[u] = area;
+        a.radii[u] = __float2int_rz(radius);
         if (!oko && a.nan_counts && area > 0) {
             atomicAdd(a.nan_counts + kNanPack, (unsigned)area);
             atomicAdd(a.nan_counts + kNanPackOpacity, (unsigned)area);
@@ -180,8 +185,8 @@ __global__ void __launch_bounds__(256) k_project_fwd(ProjectArgs a) {
 }
 
 void launch_project_fwd(const ProjectArgs &a, cudaStream_t s) {
-    if (a.n <= 0) return;
-    k_project_fwd<<<(a.n + 255) / 256, 256, 0, s>>>(a);
+    if (a.vt.n <= 0) return;
+    k_project_fwd<<<dim3((a.vt.n + 255) / 256, a.vt.count), 256, 0, s>>>(a);
 }
 
 }  // namespace msplat

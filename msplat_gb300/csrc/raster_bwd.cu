@@ -9,7 +9,8 @@
 // compute_chunk_prefix_suffix_kernel (:3139-3175) and
 // rasterize_backward_chunked_kernel (:3179-3366), including its quirk that a
 // splat whose alpha was clamped to 0.999 gets no gradient and leaves the
-// transmittance unchanged (:1085).
+// transmittance unchanged (:1085).  One launch covers the tiles of every
+// view of the step; gradients go to the record (view, Gaussian) of each id.
 #include "common.cuh"
 #include "kernels.h"
 
@@ -156,42 +157,59 @@ __device__ __forceinline__ int block_max(int v, int *wmax) {
     return m;
 }
 
-__device__ __forceinline__ void init_pixel(PixelState &ps, const RasterArgs &a, int x, int y, bool inside, float T0) {
-    const StepParams &sp = *a.sp;
-    const int p = inside ? y * a.width + x : 0;
-    const float Tf = inside ? a.final_T[p] : 0.f;
+struct BwdPixel {
+    int view, x, y;
+    bool inside;
+    long long p;   // global pixel index (0 when outside)
+};
+
+__device__ __forceinline__ BwdPixel bwd_pixel(const RasterArgs &a, int tile) {
+    BwdPixel tp;
+    tp.view = view_of_tile(a.vt, tile);
+    const ViewGeom vg = view_geom(a.vt, tp.view);
+    const int lt = tile - vg.tile_base;
+    const int tx = lt % vg.tiles_x, ty = lt / vg.tiles_x;
+    tp.x = tx * kTile + (threadIdx.x & 15);
+    tp.y = ty * kTile + (threadIdx.x >> 4);
+    tp.inside = tp.x < vg.width && tp.y < vg.height;
+    tp.p = tp.inside ? vg.pix_base + (long long)tp.y * vg.width + tp.x : 0;
+    return tp;
+}
+
+__device__ __forceinline__ void init_pixel(PixelState &ps, const RasterArgs &a, const BwdPixel &tp, float T0) {
+    const StepParams &sp = a.sp[tp.view];
+    const long long p = tp.p;
+    const float Tf = tp.inside ? a.final_T[p] : 0.f;
     ps.T = T0;
     ps.br = ps.bg = ps.bb = 0.f;
     ps.tfr = Tf * sp.bg[0];
     ps.tfg = Tf * sp.bg[1];
     ps.tfb = Tf * sp.bg[2];
-    ps.vr = inside ? a.v_img[3 * p] : 0.f;
-    ps.vg = inside ? a.v_img[3 * p + 1] : 0.f;
-    ps.vb = inside ? a.v_img[3 * p + 2] : 0.f;
-    ps.px = (float)x;
-    ps.py = (float)y;
+    ps.vr = tp.inside ? a.v_img[3 * p] : 0.f;
+    ps.vg = tp.inside ? a.v_img[3 * p + 1] : 0.f;
+    ps.vb = tp.inside ? a.v_img[3 * p + 2] : 0.f;
+    ps.px = (float)tp.x;
+    ps.py = (float)tp.y;
 }
 
 __global__ void __launch_bounds__(kTileThreads) k_raster_bwd(RasterArgs a) {
     __shared__ BwdSmem sm;
     const int tile = blockIdx.x;
-    const int tx = tile % a.tiles_x, ty = tile / a.tiles_x;
-    const int x = tx * kTile + (threadIdx.x & 15), y = ty * kTile + (threadIdx.x >> 4);
-    const bool inside = x < a.width && y < a.height;
     const int s = clamp_off(a.tile_offsets[tile], a.capacity), e = clamp_off(a.tile_offsets[tile + 1], a.capacity);
     if (s >= e) return;
+    const BwdPixel tp = bwd_pixel(a, tile);
     PixelState ps;
-    const float Tf = inside ? a.final_T[y * a.width + x] : 0.f;
-    init_pixel(ps, a, x, y, inside, Tf);
-    ps.bin_final = inside ? a.final_idx[y * a.width + x] : -1;
+    const float Tf = tp.inside ? a.final_T[tp.p] : 0.f;
+    init_pixel(ps, a, tp, Tf);
+    ps.bin_final = tp.inside ? a.final_idx[tp.p] : -1;
     const int hi = min(e - 1, block_max(ps.bin_final, sm.wmax));
     if (hi < s) return;
     backward_range(sm, a, s, hi, ps, a.grad);
 }
 
 __global__ void __launch_bounds__(256) k_chunk_prefix_suffix(RasterArgs a) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    const int P = a.width * a.height;
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long P = a.vt.pix_base[a.vt.count];
     if (p >= P) return;
     float pT = 1.f;
     for (int k = 0; k < a.k_max; k++) {
@@ -215,22 +233,20 @@ __global__ void __launch_bounds__(256) k_chunk_prefix_suffix(RasterArgs a) {
 __global__ void __launch_bounds__(kTileThreads) k_raster_bwd_chunked(RasterArgs a) {
     __shared__ BwdSmem sm;
     const int tile = blockIdx.x, k = blockIdx.y;
-    const int tx = tile % a.tiles_x, ty = tile / a.tiles_x;
-    const int x = tx * kTile + (threadIdx.x & 15), y = ty * kTile + (threadIdx.x >> 4);
-    const bool inside = x < a.width && y < a.height;
     const int s0 = clamp_off(a.tile_offsets[tile], a.capacity), e0 = clamp_off(a.tile_offsets[tile + 1], a.capacity);
     const int cs = s0 + k * kChunk, ce = min(s0 + (k + 1) * kChunk, e0);
     if (cs >= ce) return;
-    const size_t P = (size_t)a.width * a.height;
-    const size_t o = (size_t)k * P + (inside ? (size_t)y * a.width + x : 0);
+    const BwdPixel tp = bwd_pixel(a, tile);
+    const size_t P = (size_t)a.vt.pix_base[a.vt.count];
+    const size_t o = (size_t)k * P + (size_t)tp.p;
     PixelState ps;
-    init_pixel(ps, a, x, y, inside, inside ? a.prefix_T[o] * a.chunk_T[o] : 0.f);
-    if (inside) {
+    init_pixel(ps, a, tp, tp.inside ? a.prefix_T[o] * a.chunk_T[o] : 0.f);
+    if (tp.inside) {
         ps.br = a.after_C[3 * o];
         ps.bg = a.after_C[3 * o + 1];
         ps.bb = a.after_C[3 * o + 2];
     }
-    const int bf = inside ? a.chunk_idx[o] : -1;
+    const int bf = tp.inside ? a.chunk_idx[o] : -1;
     ps.bin_final = (bf >= cs) ? bf : -1;
     const int hi = min(ce - 1, block_max(ps.bin_final, sm.wmax));
     if (hi < cs) return;
@@ -241,8 +257,8 @@ void launch_raster_bwd(const RasterArgs &a, cudaStream_t s) {
     if (a.k_max <= 1) {
         k_raster_bwd<<<a.num_tiles, kTileThreads, 0, s>>>(a);
     } else {
-        const int P = a.width * a.height;
-        k_chunk_prefix_suffix<<<(P + 255) / 256, 256, 0, s>>>(a);
+        const long long P = a.vt.pix_base[a.vt.count];
+        k_chunk_prefix_suffix<<<(unsigned)((P + 255) / 256), 256, 0, s>>>(a);
         k_raster_bwd_chunked<<<dim3(a.num_tiles, a.k_max), kTileThreads, 0, s>>>(a);
     }
 }

@@ -8,7 +8,9 @@
 // rasterize_forward_chunked_kernel (:2960-3076) and
 // rasterize_forward_merge_kernel (:3081-3134).  Built with --fmad=false; the
 // per-pixel arithmetic is the reference's, fused only where it writes fma(),
-// so the image is bit-identical to the oracle's float path.
+// so the image is bit-identical to the oracle's float path.  One launch
+// covers the tiles of every view of the step (the view of a CTA is found from
+// its global tile index; chunk buffers are [K, pixels of all views]).
 #include "common.cuh"
 #include "kernels.h"
 
@@ -74,22 +76,41 @@ __device__ __forceinline__ void composite_range(BatchSmem &sm, const RasterArgs 
 
 __device__ __forceinline__ float sat01(float x) { return fminf(fmaxf(x, 0.f), 1.f); }
 
+// Pixel of this thread in the CTA's tile: view geometry, coordinates, global index.
+struct TilePixel {
+    ViewGeom vg;
+    int view, x, y;
+    bool inside;
+    long long p;   // global pixel index (valid when inside)
+};
+
+__device__ __forceinline__ TilePixel tile_pixel(const RasterArgs &a, int tile) {
+    TilePixel tp;
+    tp.view = view_of_tile(a.vt, tile);
+    tp.vg = view_geom(a.vt, tp.view);
+    const int lt = tile - tp.vg.tile_base;
+    const int tx = lt % tp.vg.tiles_x, ty = lt / tp.vg.tiles_x;
+    tp.x = tx * kTile + (threadIdx.x & 15);
+    tp.y = ty * kTile + (threadIdx.x >> 4);
+    tp.inside = tp.x < tp.vg.width && tp.y < tp.vg.height;
+    tp.p = tp.vg.pix_base + (long long)tp.y * tp.vg.width + tp.x;
+    return tp;
+}
+
 __global__ void __launch_bounds__(kTileThreads) k_raster_fwd(RasterArgs a) {
     __shared__ BatchSmem sm;
     const int tile = blockIdx.x;
-    const int tx = tile % a.tiles_x, ty = tile / a.tiles_x;
-    const int x = tx * kTile + (threadIdx.x & 15), y = ty * kTile + (threadIdx.x >> 4);
-    const bool inside = x < a.width && y < a.height;
+    const TilePixel tp = tile_pixel(a, tile);
     int s = clamp_off(a.tile_offsets[tile], a.capacity), e = clamp_off(a.tile_offsets[tile + 1], a.capacity);
     if (!MS_GUARD(s >= 0 && s <= e && e <= a.capacity, 5, tile, a.nan_counts ? a.nan_counts + kDbgSlot : nullptr)) e = s = 0;
     float T;
     float3 C;
     int last;
-    composite_range(sm, a, s, e, (float)x, (float)y, !inside, T, C, last, nullptr);
-    if (!inside) return;
-    const int p = y * a.width + x;
-    if (!MS_GUARD(p >= 0 && p < a.width * a.height, 6, p, a.nan_counts ? a.nan_counts + kDbgSlot : nullptr)) return;
-    const StepParams &sp = *a.sp;
+    composite_range(sm, a, s, e, (float)tp.x, (float)tp.y, !tp.inside, T, C, last, nullptr);
+    if (!tp.inside) return;
+    const long long p = tp.p;
+    if (!MS_GUARD(p >= 0 && p < a.vt.pix_base[a.vt.count], 6, p, a.nan_counts ? a.nan_counts + kDbgSlot : nullptr)) return;
+    const StepParams &sp = a.sp[tp.view];
     a.final_T[p] = T;
     a.final_idx[p] = last;
     a.out_img[3 * p + 0] = sat01(__fmaf_rn(sp.bg[0], T, C.x));
@@ -100,15 +121,13 @@ __global__ void __launch_bounds__(kTileThreads) k_raster_fwd(RasterArgs a) {
 __global__ void __launch_bounds__(kTileThreads) k_raster_fwd_chunked(RasterArgs a) {
     __shared__ BatchSmem sm;
     const int tile = blockIdx.x, k = blockIdx.y;
-    const int tx = tile % a.tiles_x, ty = tile / a.tiles_x;
-    const int x = tx * kTile + (threadIdx.x & 15), y = ty * kTile + (threadIdx.x >> 4);
-    const bool inside = x < a.width && y < a.height;
+    const TilePixel tp = tile_pixel(a, tile);
     const int s0 = clamp_off(a.tile_offsets[tile], a.capacity), e0 = clamp_off(a.tile_offsets[tile + 1], a.capacity);
     const int cs = s0 + k * kChunk, ce = min(s0 + (k + 1) * kChunk, e0);
-    const size_t P = (size_t)a.width * a.height;
-    const size_t o = (size_t)k * P + (size_t)y * a.width + x;
+    const size_t P = (size_t)a.vt.pix_base[a.vt.count];
+    const size_t o = (size_t)k * P + (size_t)tp.p;
     if (cs >= ce) {
-        if (inside) {
+        if (tp.inside) {
             a.chunk_T[o] = 1.f;
             a.chunk_C[3 * o] = a.chunk_C[3 * o + 1] = a.chunk_C[3 * o + 2] = 0.f;
             a.chunk_idx[o] = -1;
@@ -118,9 +137,9 @@ __global__ void __launch_bounds__(kTileThreads) k_raster_fwd_chunked(RasterArgs 
     float T;
     float3 C;
     int last;
-    composite_range(sm, a, cs, ce, (float)x, (float)y, !inside, T, C, last,
+    composite_range(sm, a, cs, ce, (float)tp.x, (float)tp.y, !tp.inside, T, C, last,
                     a.nan_counts ? a.nan_counts + kNanRasterSigma : nullptr);
-    if (!inside) return;
+    if (!tp.inside) return;
     a.chunk_T[o] = T;
     a.chunk_C[3 * o] = C.x;
     a.chunk_C[3 * o + 1] = C.y;
@@ -129,8 +148,8 @@ __global__ void __launch_bounds__(kTileThreads) k_raster_fwd_chunked(RasterArgs 
 }
 
 __global__ void __launch_bounds__(256) k_raster_merge(RasterArgs a) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    const int P = a.width * a.height;
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long P = a.vt.pix_base[a.vt.count];
     if (p >= P) return;
     float Tr = 1.f, cr = 0.f, cg = 0.f, cb = 0.f;
     int last = -1, cut = a.k_max;
@@ -146,7 +165,7 @@ __global__ void __launch_bounds__(256) k_raster_merge(RasterArgs a) {
         if (Tr <= 1e-4f) { cut = k + 1; break; }
     }
     for (int k = cut; k < a.k_max; k++) a.chunk_idx[(size_t)k * P + p] = -1;
-    const StepParams &sp = *a.sp;
+    const StepParams &sp = a.sp[view_of_pixel(a.vt, p)];
     a.final_T[p] = Tr;
     a.final_idx[p] = last;
     a.out_img[3 * p + 0] = sat01(__fmaf_rn(sp.bg[0], Tr, cr));
@@ -159,8 +178,8 @@ void launch_raster_fwd(const RasterArgs &a, cudaStream_t s) {
         k_raster_fwd<<<a.num_tiles, kTileThreads, 0, s>>>(a);
     } else {
         k_raster_fwd_chunked<<<dim3(a.num_tiles, a.k_max), kTileThreads, 0, s>>>(a);
-        const int P = a.width * a.height;
-        k_raster_merge<<<(P + 255) / 256, 256, 0, s>>>(a);
+        const long long P = a.vt.pix_base[a.vt.count];
+        k_raster_merge<<<(unsigned)((P + 255) / 256), 256, 0, s>>>(a);
     }
 }
 

@@ -8,7 +8,10 @@
 // ssim_v_bwd_kernel (msplat_metal.metal:3388-3450, 3563-3681, 3764-3850),
 // including their treatment of window centres in the out-of-image columns a
 // border tile reaches (fields from zero moments).  Intermediates are stored
-// channel-planar so every tile load and store is coalesced.
+// channel-planar so every tile load and store is coalesced.  The 16x16 blocks
+// are the tiles: one launch per pass covers every view of the step (the
+// rendered image, the planes and dL/dx are indexed by global pixel, each
+// view's target and mask by its own pixel).
 #include "common.cuh"
 #include "kernels.h"
 
@@ -18,15 +21,35 @@ __constant__ float kGauss[11];
 constexpr float kC1 = 0.0001f, kC2 = 0.0009f;
 constexpr int kS = 16, kHalo = 5, kSpan = kS + 2 * kHalo;   // 26
 
-// Target and mask: the arguments' when set, else this step's in StepParams.
-__device__ __forceinline__ const uint8_t *step_gt(const LossArgs &a) { return a.gt ? a.gt : a.sp->gt; }
-__device__ __forceinline__ const uint8_t *step_mask(const LossArgs &a) { return a.gt ? a.mask : a.sp->mask; }
+// Target and mask: the arguments' when set (one view), else the view's in StepParams.
+__device__ __forceinline__ const uint8_t *step_gt(const LossArgs &a, int v) { return a.gt ? a.gt : a.sp[v].gt; }
+__device__ __forceinline__ const uint8_t *step_mask(const LossArgs &a, int v) { return a.gt ? a.mask : a.sp[v].mask; }
+
+// The CTA's block: view, geometry, block origin (pixels)
+struct LossBlock {
+    int view, W, H, x0, y0;
+    long long pb;   // global index of the view's pixel 0
+};
+__device__ __forceinline__ LossBlock loss_block(const LossArgs &a) {
+    LossBlock b;
+    const int tile = blockIdx.x;
+    b.view = view_of_tile(a.vt, tile);
+    const ViewGeom vg = view_geom(a.vt, b.view);
+    const int lt = tile - vg.tile_base;
+    b.W = vg.width;
+    b.H = vg.height;
+    b.x0 = (lt % vg.tiles_x) * kS;
+    b.y0 = (lt / vg.tiles_x) * kS;
+    b.pb = vg.pix_base;
+    return b;
+}
 
 __global__ void __launch_bounds__(256) k_ssim_h(LossArgs a) {
     __shared__ float sg[3][kS][kSpan], sr[3][kS][kSpan];
-    const uint8_t *gt = step_gt(a);
-    const int W = a.width, H = a.height;
-    const int bx = blockIdx.x * kS - kHalo, by = blockIdx.y * kS;
+    const LossBlock lb = loss_block(a);
+    const uint8_t *gt = step_gt(a, lb.view);
+    const int W = lb.W, H = lb.H;
+    const int bx = lb.x0 - kHalo, by = lb.y0;
     const int tid = threadIdx.x;
     for (int i = tid; i < kS * kSpan; i += 256) {
         const int sy = i / kSpan, sx = i % kSpan;
@@ -36,14 +59,14 @@ __global__ void __launch_bounds__(256) k_ssim_h(LossArgs a) {
 #pragma unroll
         for (int c = 0; c < 3; c++) {
             sg[c][sy][sx] = in ? (float)gt[3 * p + c] * (1.0f / 255.0f) : 0.f;
-            sr[c][sy][sx] = in ? a.img[3 * p + c] : 0.f;
+            sr[c][sy][sx] = in ? a.img[3 * (lb.pb + p) + c] : 0.f;
         }
     }
     __syncthreads();
     const int lx = tid & 15, ly = tid >> 4;
-    const int x = blockIdx.x * kS + lx, y = by + ly;
+    const int x = lb.x0 + lx, y = by + ly;
     if (x >= W || y >= H) return;
-    const size_t P = (size_t)W * H, p = (size_t)y * W + x;
+    const size_t P = (size_t)a.vt.pix_base[a.vt.count], p = lb.pb + (size_t)y * W + x;
 #pragma unroll
     for (int c = 0; c < 3; c++) {
         float mx = 0.f, my = 0.f, sx = 0.f, sy = 0.f, cr = 0.f;
@@ -65,12 +88,13 @@ __global__ void __launch_bounds__(256) k_ssim_fields(LossArgs a) {
     __shared__ float mv[5][kS][kSpan];   // vertical moments at the window centres
     __shared__ float fl[3][kS][kSpan];
     __shared__ float red[8];
-    const int W = a.width, H = a.height;
-    const size_t P = (size_t)W * H;
-    const int bx = blockIdx.x * kS - kHalo, by = blockIdx.y * kS - kHalo;
+    const LossBlock lb = loss_block(a);
+    const int W = lb.W, H = lb.H;
+    const size_t P = (size_t)a.vt.pix_base[a.vt.count];
+    const int bx = lb.x0 - kHalo, by = lb.y0 - kHalo;
     const int tid = threadIdx.x, lx = tid & 15, ly = tid >> 4;
-    const StepParams &sp = *a.sp;
-    const uint8_t *gt = step_gt(a), *mask = step_mask(a);
+    const StepParams &sp = a.sp[lb.view];
+    const uint8_t *gt = step_gt(a, lb.view), *mask = step_mask(a, lb.view);
     const float sw = sp.ssim_weight;
     float ssim_acc = 0.f, l1_acc = 0.f;
     unsigned nwin = 0;
@@ -79,7 +103,7 @@ __global__ void __launch_bounds__(256) k_ssim_fields(LossArgs a) {
             const int sy = i / kSpan, sx = i % kSpan;
             const int gy = by + sy, gx = bx + sx;
             const bool in = gx >= 0 && gx < W && gy >= 0 && gy < H;
-            const size_t p = in ? ((size_t)gy * W + gx) : 0;
+            const size_t p = in ? lb.pb + ((size_t)gy * W + gx) : 0;
 #pragma unroll
             for (int f = 0; f < 5; f++) hp[f][sy][sx] = in ? a.hbuf[(c * 5 + f) * P + p] : 0.f;
         }
@@ -102,7 +126,7 @@ __global__ void __launch_bounds__(256) k_ssim_fields(LossArgs a) {
         __syncthreads();
         for (int i = tid; i < kS * kSpan; i += 256) {
             const int fy = i / kSpan, fx = i % kSpan;     // field row (output rows), column incl. halo
-            const int gx = bx + fx, gy = blockIdx.y * kS + fy;
+            const int gx = bx + fx, gy = lb.y0 + fy;
             float m[5];
 #pragma unroll
             for (int f = 0; f < 5; f++) m[f] = mv[f][fy][fx];
@@ -128,11 +152,11 @@ __global__ void __launch_bounds__(256) k_ssim_fields(LossArgs a) {
             if (fx >= kHalo && fx < kHalo + kS && in_img) {
                 ssim_acc += mval * (A * B) / (Cd * D);
                 const size_t p = (size_t)gy * W + gx;
-                l1_acc += mval * fabsf((float)gt[3 * p + c] * (1.0f / 255.0f) - a.img[3 * p + c]);
+                l1_acc += mval * fabsf((float)gt[3 * p + c] * (1.0f / 255.0f) - a.img[3 * (lb.pb + p) + c]);
             }
         }
         __syncthreads();
-        const int x = blockIdx.x * kS + lx, y = blockIdx.y * kS + ly;
+        const int x = lb.x0 + lx, y = lb.y0 + ly;
         if (x < W && y < H) {
             float h1 = 0.f, h2 = 0.f, h3 = 0.f;
 #pragma unroll
@@ -142,7 +166,7 @@ __global__ void __launch_bounds__(256) k_ssim_fields(LossArgs a) {
                 h2 += w * fl[1][ly][lx + d];
                 h3 += w * fl[2][ly][lx + d];
             }
-            const size_t p = (size_t)y * W + x;
+            const size_t p = lb.pb + (size_t)y * W + x;
             a.dbuf[(c * 3 + 0) * P + p] = h1;
             a.dbuf[(c * 3 + 1) * P + p] = h2;
             a.dbuf[(c * 3 + 2) * P + p] = h3;
@@ -152,7 +176,7 @@ __global__ void __launch_bounds__(256) k_ssim_fields(LossArgs a) {
     // loss: each thread whose own pixel is in the image adds w*(1 - s/3) + (1-w)*l/3
     // over the window centres it evaluated (the reference's partition, so a
     // partial edge tile sums the same terms)
-    const int x = blockIdx.x * kS + lx, y = blockIdx.y * kS + ly;
+    const int x = lb.x0 + lx, y = lb.y0 + ly;
     float v = (x < W && y < H) ? sw * (1.f - ssim_acc / 3.f) + (1.f - sw) * l1_acc / 3.f : 0.f;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -161,34 +185,35 @@ __global__ void __launch_bounds__(256) k_ssim_fields(LossArgs a) {
     if (tid == 0) {
         float s = 0.f;
         for (int k = 0; k < 8; k++) s += red[k];
-        atomicAdd(a.loss_sum, s);
+        atomicAdd(a.loss_sum + lb.view, s);
     }
     if (nwin && a.nan_counts) atomicAdd(a.nan_counts + kNanSsimWin, nwin);
 }
 
 __global__ void __launch_bounds__(256) k_ssim_bwd(LossArgs a) {
     __shared__ float sh[9][kSpan][kS];
-    const int W = a.width, H = a.height;
-    const size_t P = (size_t)W * H;
-    const int bx = blockIdx.x * kS, by = blockIdx.y * kS - kHalo;
+    const LossBlock lb = loss_block(a);
+    const int W = lb.W, H = lb.H;
+    const size_t P = (size_t)a.vt.pix_base[a.vt.count];
+    const int bx = lb.x0, by = lb.y0 - kHalo;
     const int tid = threadIdx.x, lx = tid & 15, ly = tid >> 4;
     for (int i = tid; i < kSpan * kS; i += 256) {
         const int sy = i / kS, sx = i % kS;
         const int gy = by + sy, gx = bx + sx;
         const bool in = gx < W && gy >= 0 && gy < H;
-        const size_t p = in ? ((size_t)gy * W + gx) : 0;
+        const size_t p = in ? lb.pb + ((size_t)gy * W + gx) : 0;
 #pragma unroll
         for (int f = 0; f < 9; f++) sh[f][sy][sx] = in ? a.dbuf[f * P + p] : 0.f;
     }
     __syncthreads();
-    const int x = bx + lx, y = blockIdx.y * kS + ly;
+    const int x = bx + lx, y = lb.y0 + ly;
     if (x >= W || y >= H) return;
-    const StepParams &sp = *a.sp;
-    const uint8_t *gt = step_gt(a), *mask = step_mask(a);
+    const StepParams &sp = a.sp[lb.view];
+    const uint8_t *gt = step_gt(a, lb.view), *mask = step_mask(a, lb.view);
     const float sw = sp.ssim_weight, invn = sp.loss_inv_n;
-    const size_t p = (size_t)y * W + x;
+    const size_t pl = (size_t)y * W + x, p = lb.pb + pl;   // this view's pixel, global pixel
     float mc = 1.f;
-    if (sp.has_mask && mask[p] < 128) mc = 0.f;
+    if (sp.has_mask && mask[pl] < 128) mc = 0.f;
     unsigned nbad = 0;
 #pragma unroll
     for (int c = 0; c < 3; c++) {
@@ -200,7 +225,7 @@ __global__ void __launch_bounds__(256) k_ssim_bwd(LossArgs a) {
             c2 += w * sh[c * 3 + 1][ly + d][lx];
             c3 += w * sh[c * 3 + 2][ly + d][lx];
         }
-        const float r = a.img[3 * p + c], g = (float)gt[3 * p + c] * (1.0f / 255.0f);
+        const float r = a.img[3 * p + c], g = (float)gt[3 * pl + c] * (1.0f / 255.0f);
         const float vs = c1 + r * c2 + g * c3;
         const float vl = mc * ((g > r) ? -1.f : ((g < r) ? 1.f : 0.f));
         float v = invn * (-sw * vs + (1.f - sw) * vl);
@@ -224,10 +249,9 @@ void launch_loss(const LossArgs &a, cudaStream_t s) {
         cudaMemcpyToSymbol(kGauss, w, sizeof(w));
         if (dev >= 0 && dev < 64) g_gauss_ready[dev] = true;
     }
-    const dim3 grid((a.width + kS - 1) / kS, (a.height + kS - 1) / kS);
-    k_ssim_h<<<grid, 256, 0, s>>>(a);
-    k_ssim_fields<<<grid, 256, 0, s>>>(a);
-    k_ssim_bwd<<<grid, 256, 0, s>>>(a);
+    k_ssim_h<<<a.num_tiles, 256, 0, s>>>(a);
+    k_ssim_fields<<<a.num_tiles, 256, 0, s>>>(a);
+    k_ssim_bwd<<<a.num_tiles, 256, 0, s>>>(a);
 }
 
 }  // namespace msplat

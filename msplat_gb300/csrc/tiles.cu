@@ -6,6 +6,11 @@
 // buckets sit at exact (not power-of-two padded) offsets, and each tile is
 // sorted by one CTA with a stable LSD radix sort (8-bit digits, constant
 // digits skipped) in shared memory, or in global memory for heavy tiles.
+// All views of a step are mapped together: the count and scatter grids have
+// one row (blockIdx.y) per view, the scan and the sorts run over the global
+// tile range, and the ids in the keys are record ids v * n + i.
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -16,24 +21,28 @@ constexpr int kSortItems = 8;                    // keys per thread in the share
 constexpr int kSortLightKeys = 512 * kSortItems;   // 4096: 512-thread CTA, two per SM
 constexpr int kSortHeavyKeys = 1024 * kSortItems;  // 8192: 1024-thread CTA, one per SM
 
-__device__ __forceinline__ bool splat_active(int i, const int *radii, const float *depths) {
-    if (radii[i] <= 0) return false;
-    const float d = depths[i];
+__device__ __forceinline__ bool splat_active(size_t u, const int *radii, const float *depths) {
+    if (radii[u] <= 0) return false;
+    const float d = depths[u];
     return finite_bits(d) && d > 0.0f;
 }
 
 __global__ void __launch_bounds__(256) k_count(TileArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n || !splat_active(i, a.radii, a.depths)) return;
-    const float4 ra = a.rec[i].a;
-    const float2 ab = a.aabb[i];
+    const int view = blockIdx.y;
+    const size_t u = (size_t)view * a.vt.n + i;
+    if (i >= a.vt.n || !splat_active(u, a.radii, a.depths)) return;
+    const ViewGeom vg = view_geom(a.vt, view);
+    const float4 ra = a.rec[u].a;
+    const float2 ab = a.aabb[u];
     int x0, y0, x1, y1;
-    tile_rect(ra.x, ra.y, ab.x, ab.y, a.tiles_x, a.tiles_y, x0, y0, x1, y1);
+    tile_rect(ra.x, ra.y, ab.x, ab.y, vg.tiles_x, vg.tiles_y, x0, y0, x1, y1);
     for (int y = y0; y < y1; y++)
-        for (int x = x0; x < x1; x++)
-            if (MS_GUARD(y * a.tiles_x + x < a.num_tiles && y * a.tiles_x + x >= 0, 2, y * a.tiles_x + x,
-                         a.nan_counts ? a.nan_counts + kDbgSlot : nullptr))
-                atomicAdd(a.tile_counts + y * a.tiles_x + x, 1u);
+        for (int x = x0; x < x1; x++) {
+            const int t = vg.tile_base + y * vg.tiles_x + x;
+            if (MS_GUARD(t < a.num_tiles && t >= 0, 2, t, a.nan_counts ? a.nan_counts + kDbgSlot : nullptr))
+                atomicAdd(a.tile_counts + t, 1u);
+        }
 }
 
 // Exclusive scan of the tile counts by one CTA of 1024 threads: each thread
@@ -95,15 +104,18 @@ __global__ void __launch_bounds__(1024) k_scan(TileArgs a) {
 
 __global__ void __launch_bounds__(256) k_scatter(TileArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n || !splat_active(i, a.radii, a.depths)) return;
-    const float4 ra = a.rec[i].a;
-    const float2 ab = a.aabb[i];
+    const int view = blockIdx.y;
+    const size_t u = (size_t)view * a.vt.n + i;
+    if (i >= a.vt.n || !splat_active(u, a.radii, a.depths)) return;
+    const ViewGeom vg = view_geom(a.vt, view);
+    const float4 ra = a.rec[u].a;
+    const float2 ab = a.aabb[u];
     int x0, y0, x1, y1;
-    tile_rect(ra.x, ra.y, ab.x, ab.y, a.tiles_x, a.tiles_y, x0, y0, x1, y1);
-    const uint64_t key = ((uint64_t)__float_as_uint(a.depths[i]) << 32) | (uint32_t)i;
+    tile_rect(ra.x, ra.y, ab.x, ab.y, vg.tiles_x, vg.tiles_y, x0, y0, x1, y1);
+    const uint64_t key = ((uint64_t)__float_as_uint(a.depths[u]) << 32) | (uint32_t)u;
     for (int y = y0; y < y1; y++)
         for (int x = x0; x < x1; x++) {
-            const int t = y * a.tiles_x + x;
+            const int t = vg.tile_base + y * vg.tiles_x + x;
             if (!MS_GUARD(t >= 0 && t < a.num_tiles, 3, t, a.nan_counts ? a.nan_counts + kDbgSlot : nullptr)) continue;
             const uint32_t pos = atomicAdd(a.tile_write + t, 1u);
             const uint64_t dst = (uint64_t)a.tile_offsets[t] + pos;
@@ -112,54 +124,63 @@ __global__ void __launch_bounds__(256) k_scatter(TileArgs a) {
 }
 
 // Block-aggregated count and scatter.  A CTA of kAggThreads covers
-// kAggPerCta Gaussians and keeps a shared-memory histogram over all tiles.
-// Count stores the CTA's histogram row to cta_bins[cta][T]; a column scan
-// turns the rows into per-(CTA, tile) start offsets and the tile totals; the
-// scatter CTA loads its row, adds the tile offsets, and hands out slots with
+// kAggPerCta Gaussians of one view and keeps a shared-memory histogram over
+// that view's tiles.  Count stores the CTA's histogram row to cta_bins (view
+// v's rows [ctas, T_v] start at ctas * tile_base[v]); a column scan turns the
+// rows into per-(CTA, tile) start offsets and the tile totals; the scatter
+// CTA loads its row, adds the tile offsets, and hands out slots with
 // shared-memory atomics.  No global atomics, and each tile's bucket is
-// filled CTA by CTA.  Used while the histogram fits (kAggMaxTiles).
+// filled CTA by CTA.  Used while every view's histogram fits (kAggMaxTiles).
 constexpr int kAggPerCta = 2048;
 constexpr int kAggThreads = 512;   // four CTAs per SM: 1M Gaussians fill one wave
 constexpr int kAggMaxTiles = 12288;
 
-__device__ __forceinline__ void agg_rect(const TileArgs &a, int i, int &x0, int &y0, int &x1, int &y1) {
-    const float4 ra = a.rec[i].a;
-    const float2 ab = a.aabb[i];
-    tile_rect(ra.x, ra.y, ab.x, ab.y, a.tiles_x, a.tiles_y, x0, y0, x1, y1);
+__device__ __forceinline__ void agg_rect(const TileArgs &a, const ViewGeom &vg, size_t u, int &x0, int &y0, int &x1,
+                                         int &y1) {
+    const float4 ra = a.rec[u].a;
+    const float2 ab = a.aabb[u];
+    tile_rect(ra.x, ra.y, ab.x, ab.y, vg.tiles_x, vg.tiles_y, x0, y0, x1, y1);
 }
 
 __global__ void __launch_bounds__(kAggThreads) k_count_agg(TileArgs a) {
     extern __shared__ uint32_t bins[];
-    const int T = a.num_tiles;
+    const int view = blockIdx.y;
+    const ViewGeom vg = view_geom(a.vt, view);
+    const int T = vg.tiles_x * vg.tiles_y;
     for (int t = threadIdx.x; t < T; t += blockDim.x) bins[t] = 0;
     __syncthreads();
-    const int g0 = blockIdx.x * kAggPerCta, g1 = min(a.n, g0 + kAggPerCta);
+    const size_t ubase = (size_t)view * a.vt.n;
+    const int g0 = blockIdx.x * kAggPerCta, g1 = min(a.vt.n, g0 + kAggPerCta);
     for (int i = g0 + threadIdx.x; i < g1; i += blockDim.x) {
-        if (!splat_active(i, a.radii, a.depths)) continue;
+        if (!splat_active(ubase + i, a.radii, a.depths)) continue;
         int x0, y0, x1, y1;
-        agg_rect(a, i, x0, y0, x1, y1);
+        agg_rect(a, vg, ubase + i, x0, y0, x1, y1);
         for (int y = y0; y < y1; y++)
-            for (int x = x0; x < x1; x++) atomicAdd(&bins[y * a.tiles_x + x], 1u);
+            for (int x = x0; x < x1; x++) atomicAdd(&bins[y * vg.tiles_x + x], 1u);
     }
     __syncthreads();
-    uint32_t *row = a.cta_bins + (size_t)blockIdx.x * T;
+    uint32_t *row = a.cta_bins + (size_t)gridDim.x * vg.tile_base + (size_t)blockIdx.x * T;
     for (int t = threadIdx.x; t < T; t += blockDim.x) row[t] = bins[t];
 }
 
 // Exclusive scan down each tile's column of CTA rows; the column total is the
-// tile's count.  A CTA covers 32 tiles (one per lane, so each row access is a
-// 128-byte line) and splits the rows over its 32 warps: row sums, a scan of
-// the 32 partial sums per tile in shared memory, then the rows rewritten.
+// tile's count.  A CTA covers 32 global tiles (one per lane, so each row
+// access is a 128-byte line while the lanes share a view) and splits the
+// rows over its 32 warps: row sums, a scan of the 32 partial sums per tile in
+// shared memory, then the rows rewritten.
 __global__ void __launch_bounds__(1024) k_cta_scan(TileArgs a, int ctas) {
     __shared__ uint32_t part[32][33];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int T = a.num_tiles;
     const int t = blockIdx.x * 32 + lane;
+    const int tc = min(t, a.num_tiles - 1);
+    const ViewGeom vg = view_geom(a.vt, view_of_tile(a.vt, tc));
+    const int Tv = vg.tiles_x * vg.tiles_y;
+    uint32_t *col = a.cta_bins + (size_t)ctas * vg.tile_base + (tc - vg.tile_base);
     const int per = (ctas + 31) / 32;
     const int c0 = min(ctas, w * per), c1 = min(ctas, c0 + per);
     uint32_t sum = 0;
-    if (t < T)
-        for (int c = c0; c < c1; c++) sum += a.cta_bins[(size_t)c * T + t];
+    if (t < a.num_tiles)
+        for (int c = c0; c < c1; c++) sum += col[(size_t)c * Tv];
     part[w][lane] = sum;
     __syncthreads();
     uint32_t run = 0, total = 0;
@@ -168,10 +189,10 @@ __global__ void __launch_bounds__(1024) k_cta_scan(TileArgs a, int ctas) {
         if (k < w) run += v;
         total += v;
     }
-    if (t < T) {
+    if (t < a.num_tiles) {
         for (int c = c0; c < c1; c++) {
-            const uint32_t v = a.cta_bins[(size_t)c * T + t];
-            a.cta_bins[(size_t)c * T + t] = run;
+            const uint32_t v = col[(size_t)c * Tv];
+            col[(size_t)c * Tv] = run;
             run += v;
         }
         if (w == 0) a.tile_counts[t] = total;
@@ -180,27 +201,37 @@ __global__ void __launch_bounds__(1024) k_cta_scan(TileArgs a, int ctas) {
 
 __global__ void __launch_bounds__(kAggThreads) k_scatter_agg(TileArgs a) {
     extern __shared__ uint32_t bins[];
-    const int T = a.num_tiles;
-    const uint32_t *row = a.cta_bins + (size_t)blockIdx.x * T;
-    for (int t = threadIdx.x; t < T; t += blockDim.x) bins[t] = a.tile_offsets[t] + row[t];
+    const int view = blockIdx.y;
+    const ViewGeom vg = view_geom(a.vt, view);
+    const int T = vg.tiles_x * vg.tiles_y;
+    const uint32_t *row = a.cta_bins + (size_t)gridDim.x * vg.tile_base + (size_t)blockIdx.x * T;
+    for (int t = threadIdx.x; t < T; t += blockDim.x) bins[t] = a.tile_offsets[vg.tile_base + t] + row[t];
     __syncthreads();
-    const int g0 = blockIdx.x * kAggPerCta, g1 = min(a.n, g0 + kAggPerCta);
+    const size_t ubase = (size_t)view * a.vt.n;
+    const int g0 = blockIdx.x * kAggPerCta, g1 = min(a.vt.n, g0 + kAggPerCta);
     for (int i = g0 + threadIdx.x; i < g1; i += blockDim.x) {
-        if (!splat_active(i, a.radii, a.depths)) continue;
+        const size_t u = ubase + i;
+        if (!splat_active(u, a.radii, a.depths)) continue;
         int x0, y0, x1, y1;
-        agg_rect(a, i, x0, y0, x1, y1);
-        const uint64_t key = ((uint64_t)__float_as_uint(a.depths[i]) << 32) | (uint32_t)i;
+        agg_rect(a, vg, u, x0, y0, x1, y1);
+        const uint64_t key = ((uint64_t)__float_as_uint(a.depths[u]) << 32) | (uint32_t)u;
         for (int y = y0; y < y1; y++)
             for (int x = x0; x < x1; x++) {
-                const uint32_t dst = atomicAdd(&bins[y * a.tiles_x + x], 1u);
+                const uint32_t dst = atomicAdd(&bins[y * vg.tiles_x + x], 1u);
                 if (dst < (uint64_t)a.capacity) a.keys[dst] = key;   // overflow is dropped, never written
             }
     }
 }
 
-size_t tile_cta_bins_bytes(int n, int num_tiles) {
-    if (num_tiles > kAggMaxTiles || n <= 0) return 0;
-    return (size_t)((n + kAggPerCta - 1) / kAggPerCta) * (size_t)num_tiles * sizeof(uint32_t);
+static int max_view_tiles(const ViewTable &vt) {
+    int m = 0;
+    for (int v = 0; v < vt.count; v++) m = std::max(m, vt.tiles_x[v] * vt.tiles_y[v]);
+    return m;
+}
+
+size_t tile_cta_bins_bytes(const ViewTable &vt) {
+    if (max_view_tiles(vt) > kAggMaxTiles || vt.n <= 0) return 0;
+    return (size_t)((vt.n + kAggPerCta - 1) / kAggPerCta) * (size_t)vt.tile_base[vt.count] * sizeof(uint32_t);
 }
 
 // ---------------------------------------------------------------------------
@@ -554,26 +585,27 @@ int launch_tiles(const TileArgs &a, int num_sms, cudaStream_t s) {
         attr_set = true;
     }
     int launches = 0;
-    const bool agg = a.num_tiles <= kAggMaxTiles && a.cta_bins != nullptr;
-    const int agg_blocks = (a.n + kAggPerCta - 1) / kAggPerCta;
-    const size_t agg_smem = (size_t)a.num_tiles * sizeof(uint32_t);
-    if (a.n > 0 && agg) {
-        k_count_agg<<<agg_blocks, kAggThreads, agg_smem, s>>>(a);
+    const int n = a.vt.n, views = a.vt.count, maxT = max_view_tiles(a.vt);
+    const bool agg = maxT <= kAggMaxTiles && a.cta_bins != nullptr;
+    const int agg_blocks = (n + kAggPerCta - 1) / kAggPerCta;
+    const size_t agg_smem = (size_t)maxT * sizeof(uint32_t);
+    if (n > 0 && agg) {
+        k_count_agg<<<dim3(agg_blocks, views), kAggThreads, agg_smem, s>>>(a);
         debug_sync(s, "count");
         k_cta_scan<<<(a.num_tiles + 31) / 32, 1024, 0, s>>>(a, agg_blocks);
         debug_sync(s, "cta_scan");
         launches += 2;
-    } else if (a.n > 0) {
-        k_count<<<(a.n + 255) / 256, 256, 0, s>>>(a);
+    } else if (n > 0) {
+        k_count<<<dim3((n + 255) / 256, views), 256, 0, s>>>(a);
         debug_sync(s, "count");
         launches += 1;
     }
     k_scan<<<1, 1024, 0, s>>>(a);
     debug_sync(s, "scan");
     launches += 1;
-    if (a.n > 0) {
-        if (agg) k_scatter_agg<<<agg_blocks, kAggThreads, agg_smem, s>>>(a);
-        else k_scatter<<<(a.n + 255) / 256, 256, 0, s>>>(a);
+    if (n > 0) {
+        if (agg) k_scatter_agg<<<dim3(agg_blocks, views), kAggThreads, agg_smem, s>>>(a);
+        else k_scatter<<<dim3((n + 255) / 256, views), 256, 0, s>>>(a);
         debug_sync(s, "scatter");
         launches += 1;
     }

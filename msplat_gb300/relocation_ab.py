@@ -1,7 +1,7 @@
 """Time-to-PSNR of the learned relocation proposal against plain
 opacity-weighted MCMC relocation, on the small synthetic scene.
 
-    python -m msplat_gb300.relocation_ab [--iters 6000] [--seed 0]
+    python -m msplat_gb300.relocation_ab [--iters 6000] [--seed 0] [--arms plain,learned,batch4]
 
 Scene: 16,384 ground-truth Gaussians (synthetic.config_small), 8 training
 views at 256x256 and 4 held-out views between them, targets rendered by the
@@ -10,7 +10,9 @@ means, colours from the ground truth) and the same configuration (MCMC cap
 32,768, black background); the learned arm switches the proposal on.
 Held-out PSNR is measured every `--eval-every` steps outside the timed
 training time.  Time-to-PSNR: the training wall-clock at which each arm
-first reaches the plain arm's final PSNR minus 0.1 dB.  Prints one JSON
+first reaches the plain arm's final PSNR minus 0.1 dB.  Optional arms
+`batchB` and `batchB_learned` train with B views per optimizer step (the
+mean gradient of B cameras, one update), same step count.  Prints one JSON
 line.
 """
 from __future__ import annotations
@@ -43,7 +45,7 @@ def _scene(seed):
     return list(sc.train_cams) + list(test), imgs, xyz, col
 
 
-def run_arm(cams, imgs, xyz, col, learned, iters, eval_every):
+def run_arm(cams, imgs, xyz, col, learned, iters, eval_every, batch=1):
     import torch
     from . import api as A
     # the last 4 views are held out: train on the first 8, evaluate the others by pose
@@ -52,6 +54,8 @@ def run_arm(cams, imgs, xyz, col, learned, iters, eval_every):
     t = A.GaussianTrainer(ds, cfg)
     if learned:
         t.set_learned_relocation(True)
+    if batch > 1:
+        t.set_batch_views(batch)
 
     def held_out_psnr():
         vals = []
@@ -84,26 +88,50 @@ def time_to(curve, target):
     return None, None
 
 
+def _arm_spec(name):
+    """'plain' | 'learned' | 'batch<B>' | 'batch<B>_learned' -> (learned, B)"""
+    learned = name.endswith("learned")
+    base = name[:-len("_learned")] if name.endswith("_learned") else name
+    if base.startswith("batch"):
+        return learned, int(base[len("batch"):])
+    if base in ("plain", "learned"):
+        return learned, 1
+    raise ValueError(f"unknown arm {name!r}")
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--iters", type=int, default=6000)
     ap.add_argument("--eval-every", type=int, default=250)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--arms", default="plain,learned", help="comma-separated; the first is the target's source")
     a = ap.parse_args(argv)
+    names = [x.strip() for x in a.arms.split(",") if x.strip()]
+    if "plain" not in names:
+        names.insert(0, "plain")
+    names.remove("plain")
+    names.insert(0, "plain")
     cams, imgs, xyz, col = _scene(a.seed)
-    plain = run_arm(cams, imgs, xyz, col, False, a.iters, a.eval_every)
-    learned = run_arm(cams, imgs, xyz, col, True, a.iters, a.eval_every)
+    runs = {}
+    for nm in names:
+        learned, b = _arm_spec(nm)
+        runs[nm] = run_arm(cams, imgs, xyz, col, learned, a.iters, a.eval_every, batch=b)
+    plain = runs["plain"]
     target = plain["final_psnr"] - 0.1
     ps, pt = time_to(plain["curve"], target)
-    ls, lt = time_to(learned["curve"], target)
     res = {"workload": "learned vs plain MCMC relocation, 16,384-Gaussian synthetic scene, 8 train + 4 held-out "
-                       "views at 256x256, cap 32,768", "iters": a.iters, "target_psnr": target,
-           "plain": {"final_psnr": plain["final_psnr"], "train_s": plain["train_s"], "time_to_target_s": pt,
-                     "step_to_target": ps, "splats": plain["splats"]},
-           "learned": {"final_psnr": learned["final_psnr"], "train_s": learned["train_s"], "time_to_target_s": lt,
-                       "step_to_target": ls, "splats": learned["splats"], "proposal": learned["proposal"]},
-           "time_ratio": (lt / pt) if (lt is not None and pt) else None,
-           "curves": {"plain": plain["curve"], "learned": learned["curve"]}}
+                       "views at 256x256, cap 32,768", "iters": a.iters, "target_psnr": target}
+    for nm, r in runs.items():
+        st, tt = time_to(r["curve"], target)
+        res[nm] = {"final_psnr": r["final_psnr"], "train_s": r["train_s"], "time_to_target_s": tt,
+                   "step_to_target": st, "splats": r["splats"]}
+        if "proposal" in r:
+            res[nm]["proposal"] = r["proposal"]
+        if nm != "plain":
+            res[nm]["time_ratio"] = (tt / pt) if (tt is not None and pt) else None
+    if "learned" in runs:
+        res["time_ratio"] = res["learned"]["time_ratio"]
+    res["curves"] = {nm: r["curve"] for nm, r in runs.items()}
     print(json.dumps(res), flush=True)
     return 0
 

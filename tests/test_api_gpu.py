@@ -127,6 +127,45 @@ def test_training_render_evaluate(scene):
     np.testing.assert_array_equal(rgba[..., :3], exp8)
 
 
+def test_batch_views_step(scene):
+    """set_batch_views(4) with four training cameras: step 1 renders each
+    camera once and applies one update from their mean gradient, the
+    engine's multi-view step on the same views (any order: the mean does
+    not depend on it beyond float rounding); training then still converges."""
+    torch = pytest.importorskip("torch")
+    gt, cams, imgs, xyz, rgb = scene
+    ds = A.Dataset.from_arrays(cams[:4], imgs[:4], xyz, rgb)
+    t = A.GaussianTrainer(ds, _config(bg_color=[0.0, 0.0, 0.0]))
+    t.set_batch_views(4)
+    with pytest.raises(ValueError):
+        t.set_batch_views(0)
+    g0 = S.GaussianSet(*t.get_gaussians())
+    s = t.step()
+    assert s.iteration == 1
+    g1 = t.get_gaussians()
+    eng = E.Engine(0)
+    dg = E.DeviceGaussians(g0)
+    args = [E.make_args(E.camera_dict(c), E.step_scalars(1, 1, width=c.width, height=c.height), do_sgld=True)
+            for c in cams[:4]]
+    gts = [torch.from_numpy(im).cuda() for im in imgs[:4]]
+    eng.train_step_batch(dg, args, [g.data_ptr() for g in gts])
+    eng.synchronize()
+    ref, _ = dg.to_numpy()
+    assert abs(t.last_loss - eng.loss()) <= 1e-5 * abs(eng.loss())
+    eng.close()
+    for k, a, a0 in zip(E.GROUPS, g1, g0.arrays()):
+        upd_t, upd_e = a - a0.reshape(a.shape), ref[k].reshape(a.shape) - a0.reshape(a.shape)
+        if not upd_e.any():
+            assert not upd_t.any(), k
+            continue
+        assert rel_l2(upd_t, upd_e) <= 1e-4, k
+    losses = [t.last_loss]
+    for _ in range(40):
+        t.step()
+        losses.append(t.last_loss)
+    assert np.mean(losses[-6:]) < 0.9 * np.mean(losses[:6]), losses
+
+
 def _read_ply(path):
     with open(path, "rb") as f:
         props, n, comment = [], 0, ""

@@ -1,7 +1,9 @@
-"""Multi-view training step (msplat_engine_train_step_batch): three views of
-different sizes give one update from the mean of their gradients.  Checked
-against the oracle's per-view gradients (FP32 path) averaged and pushed
-through Adam in numpy with the engine's rules (GPU only)."""
+"""Multi-view training step (msplat_engine_train_step_batch): views of
+different sizes go through one launch per stage and give one update from the
+mean of their gradients.  The batched forward is checked bit for bit against
+one-view renders (records, per-tile sorted lists, images); the update against
+the oracle's per-view gradients (FP32 path) averaged and pushed through Adam
+in numpy with the engine's rules (GPU only)."""
 import numpy as np
 import pytest
 
@@ -35,12 +37,64 @@ def _adam(p, m, v, g, st, bc2, b1=0.9, b2=0.999, eps=1e-8):
     return p - st * m2 / (np.sqrt(v2) / bc2 + eps), m2, v2
 
 
+def _mixed_views(sc):
+    base = sc.train_cams
+    return [base[0], S.Camera(base[3].cam_to_world, 200, 150, 160.0, 160.0, 100.0, 75.0),
+            S.Camera(base[5].cam_to_world, 128, 96, 100.0, 100.0, 64.0, 48.0)]
+
+
+@pytest.mark.parametrize("raster_mode", [1, 2])
+def test_batch_forward_matches_single_views(raster_mode):
+    """One launch per stage over three views = three one-view renders: the
+    same radii and records, each view's tile lists equal to its own with the
+    record ids offset by view * n (depth ties still ordered by Gaussian), and
+    the same image bits.  raster_mode 1: monolithic; 2: 512-splat chunks."""
+    torch = pytest.importorskip("torch")
+    sc = S.config_small(4)
+    cams = _mixed_views(sc)
+    init = S.init_from_gt(sc.gt, 4)
+    n = init.n
+    kw = dict(raster_mode=raster_mode, k_max=3 if raster_mode == 2 else 0, do_optimizer=False)
+    gts = [torch.from_numpy(gt_image(sc.gt, c)).cuda() for c in cams]
+    eng = E.Engine(0)
+    dg = E.DeviceGaussians(init)
+    args = [E.make_args(E.camera_dict(c), E.step_scalars(10, 10, width=c.width, height=c.height), **kw)
+            for c in cams]
+    eng.train_step_batch(dg, args, [g.data_ptr() for g in gts])
+    eng.synchronize()
+    Ts = [((c.width + 15) // 16) * ((c.height + 15) // 16) for c in cams]
+    Ps = [c.width * c.height for c in cams]
+    B = len(cams)
+    offs = eng.read("tile_offsets", np.uint32, sum(Ts) + 1).astype(np.int64)
+    ids = eng.read("isect_ids", np.uint32, int(offs[-1]))
+    img = eng.read("out_img", np.float32, 3 * sum(Ps))
+    radii = eng.read("radii", np.int32, B * n)
+    rec = eng.read("rec", np.float32, B * n * 12)
+    assert eng.stats().check_record[0] == 0
+    eng.close()
+    t0 = p0 = 0
+    for v, c in enumerate(cams):
+        e1 = E.Engine(0)
+        dg1 = E.DeviceGaussians(init)
+        e1.render(dg1, E.make_args(E.camera_dict(c), E.step_scalars(10, 10, width=c.width, height=c.height), **kw))
+        e1.synchronize()
+        o1 = e1.read("tile_offsets", np.uint32, Ts[v] + 1).astype(np.int64)
+        i1 = e1.read("isect_ids", np.uint32, max(int(o1[-1]), 1))[:int(o1[-1])]
+        np.testing.assert_array_equal(e1.read("radii", np.int32, n), radii[v * n:(v + 1) * n])
+        np.testing.assert_array_equal(e1.read("rec", np.float32, n * 12), rec[v * n * 12:(v + 1) * n * 12])
+        np.testing.assert_array_equal(np.diff(o1), np.diff(offs[t0:t0 + Ts[v] + 1]))
+        seg = ids[offs[t0]:offs[t0 + Ts[v]]].astype(np.int64)
+        np.testing.assert_array_equal(seg, i1.astype(np.int64) + v * n)
+        np.testing.assert_array_equal(e1.read("out_img", np.float32, 3 * Ps[v]), img[3 * p0:3 * (p0 + Ps[v])])
+        e1.close()
+        t0 += Ts[v]
+        p0 += Ps[v]
+
+
 def test_batch_step_matches_oracle_mean_gradient():
     torch = pytest.importorskip("torch")
     sc = S.config_small(2)
-    base = sc.train_cams
-    cams = [base[0], S.Camera(base[3].cam_to_world, 200, 150, 160.0, 160.0, 100.0, 75.0),
-            S.Camera(base[5].cam_to_world, 128, 96, 100.0, 100.0, 64.0, 48.0)]
+    cams = _mixed_views(sc)
     gts = [gt_image(sc.gt, c) for c in cams]
     init = S.init_from_gt(sc.gt, 2)
     B = len(cams)
@@ -52,7 +106,9 @@ def test_batch_step_matches_oracle_mean_gradient():
     nb = {0: 0, 1: 3, 2: 8, 3: 15}[steps[0]["degrees_to_use"]]
     assert nb == 15
     cds = [E.camera_dict(c) for c in cams]
-    args = [E.make_args(cd, st) for cd, st in zip(cds, steps)]   # SGLD off: deterministic reference
+    # SGLD off: deterministic reference; monolithic raster in both (the batch
+    # picks its raster mode from the tiles of all views, the oracle per view)
+    args = [E.make_args(cd, st, raster_mode=1) for cd, st in zip(cds, steps)]
     # engine
     eng = E.Engine(0)
     dg = E.DeviceGaussians(init)
@@ -73,7 +129,8 @@ def test_batch_step_matches_oracle_mean_gradient():
     for cd, st, gt in zip(cds, steps, gts):
         st = dict(st)
         st["loss_inv_n"] = st["loss_inv_n"] / B
-        r = O.train_step(32, init.copy(), cd, st, gt=gt, do_backward=True, do_optimizer=False, want_ids=False)
+        r = O.train_step(32, init.copy(), cd, st, gt=gt, do_backward=True, do_optimizer=False, want_ids=False,
+                         raster_mode=1)
         losses.append(r["loss"])            # the loss value is not scaled by loss_inv_n
         v = r["radii"] > 0
         vis |= v
