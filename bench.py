@@ -20,6 +20,11 @@ Arms:
                      (oracle/, FP64, OpenMP on all host cores) on the same
                      workload, one full iteration per step.
 
+Also reported (key "batched"): the multi-view step on the same model, 8
+views of mixed sizes per step (2 each of 1297x840, 979x546, 648x420 and
+2594x1680, same camera poses, focal length scaled with the width), one
+launch per stage over all views, as a captured graph.
+
 Under torchrun (N > 1) every rank trains its own replica on its own GPU
 ("replicas only": the step has no cross-GPU exchange).
 """
@@ -196,6 +201,57 @@ def run_reference(args):
     return 0
 
 
+BATCH_SIZES = [(1297, 840), (979, 546), (648, 420), (2594, 1680)] * 2
+
+
+def batched_cameras(sc):
+    """The batched workload's 8 views: ring poses 0..7, sizes BATCH_SIZES."""
+    from msplat_gb300 import synthetic as S
+    out = []
+    for k, (w, h) in enumerate(BATCH_SIZES):
+        c = sc.train_cams[k % len(sc.train_cams)]
+        f = c.fx * w / c.width
+        out.append(S.Camera(c.cam_to_world, w, h, f, f, 0.5 * w, 0.5 * h))
+    return out
+
+
+def run_batched(eng, E, sc, dg, warmup, steps, step_base):
+    """Multi-view steps of the batched workload; returns its JSON object."""
+    import numpy as np
+    import torch
+    cams = [E.camera_dict(c) for c in batched_cameras(sc)]
+    gt_dev = E.DeviceGaussians(sc.gt)
+    gts = []
+    for cd in cams:
+        eng.render(gt_dev, E.make_args(cd, {"degrees_to_use": 3}))
+        img = eng.read("out_img", np.float32, cd["width"] * cd["height"] * 3)
+        gts.append(torch.from_numpy((np.clip(img, 0, 1) * 255 + 0.5).astype(np.uint8)).cuda())
+    del gt_dev
+    ptrs = [g.data_ptr() for g in gts]
+
+    def one(k):
+        args = [E.make_args(cd, E.step_scalars(step_base + k, step_base + k, width=cd["width"], height=cd["height"]),
+                            do_sgld=True) for cd in cams]
+        eng.train_step_batch(dg, args, ptrs)
+
+    for k in range(warmup):
+        one(k)
+    eng.synchronize()
+    l0 = eng.stats().launches
+    eng.marker(0)
+    for k in range(steps):
+        one(warmup + k)
+    eng.marker(1)
+    ms = eng.marker_elapsed() / steps
+    launches = (eng.stats().launches - l0) / steps
+    px = sum(w * h for w, h in BATCH_SIZES)
+    return {"workload": "8 views per step: 2 each of 1297x840, 979x546, 648x420, 2594x1680 "
+                        f"({px / 1e6:.2f} Mpx), {dg.n / 1e6:g}M Gaussians, one launch per stage, CUDA graph",
+            "views_per_step": len(cams), "ms_per_step": ms, "iters_per_s": 1e3 / ms,
+            "views_per_s": len(cams) * 1e3 / ms, "mpx_per_s": px / 1e6 * 1e3 / ms,
+            "launches_per_step": launches, "loss": eng.loss()}
+
+
 def config_dict(args):
     n = getattr(args, "gaussians", N_MODEL)
     return {"workload": f"{n / 1e6:g}M Gaussians (SH deg 3) training step at 1297x840, synthetic 1M+200k GT scene",
@@ -317,12 +373,20 @@ def run_engine(args):
                 "frac": achieved / peak, "peak_kind": kind, "traffic": traffic,
                 "algorithmic_bytes": alg, "ms": stage_ms[dom]}
 
+    batched = None
+    if not args.no_batched:
+        try:
+            batched = run_batched(eng, E, sc, dg, 3, max(5, args.steps // 4), step_base + 100000)
+            batched["single_view_mpx_per_s"] = value / ws * 1297 * 840 / 1e6
+        except Exception as ex:   # reported, never fatal to the throughput line
+            batched = {"error": str(ex)[:200]}
+
     out = {"metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_dict(args),
            "roofline": roofline, "stage_ms": stage_ms, "num_intersections": int(st.num_intersections),
            "max_tile_count": int(st.max_tile_count), "gpu_launches": int(launches), "e2e": e2e,
-           "cuda_graph": True,
+           "cuda_graph": True, "batched": batched,
            "clocks": clk.summary()}
     if rank == 0 and not args.no_time_to_psnr:
         # the metric's second half: learned vs plain relocation, time to PSNR
@@ -332,15 +396,20 @@ def run_engine(args):
             cams_ab, imgs_ab, xyz_ab, col_ab = AB._scene(0)
             plain = AB.run_arm(cams_ab, imgs_ab, xyz_ab, col_ab, False, 6000, 250)
             learned = AB.run_arm(cams_ab, imgs_ab, xyz_ab, col_ab, True, 6000, 250)
+            both = AB.run_arm(cams_ab, imgs_ab, xyz_ab, col_ab, True, 6000, 250, batch=4)
             target = plain["final_psnr"] - 0.1
             _, tp = AB.time_to(plain["curve"], target)
             _, tl = AB.time_to(learned["curve"], target)
+            _, tb = AB.time_to(both["curve"], target)
             out["time_to_psnr"] = {
                 "workload": "16,384-Gaussian synthetic scene, 8 train + 4 held-out views at 256x256, MCMC cap "
-                            "32,768, 6000 iterations, seed 0",
-                "target_psnr": target, "plain_s": tp, "learned_s": tl,
+                            "32,768, 6000 iterations (views), seed 0; learned+batched: the learned proposal with "
+                            "4 views per step (one launch per stage, learning rates x 4^0.75)",
+                "target_psnr": target, "plain_s": tp, "learned_s": tl, "learned_batched_s": tb,
                 "ratio": (tl / tp) if (tl is not None and tp) else None,
+                "ratio_learned_batched": (tb / tp) if (tb is not None and tp) else None,
                 "plain_final_psnr": plain["final_psnr"], "learned_final_psnr": learned["final_psnr"],
+                "learned_batched_final_psnr": both["final_psnr"],
                 "proposal_rounds": learned["proposal"]["rounds"]}
         except Exception as ex:   # reported, never fatal to the throughput line
             out["time_to_psnr"] = {"error": str(ex)[:200]}
@@ -365,6 +434,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-time-to-psnr", action="store_true",
                     help="skip the learned-vs-plain relocation time-to-PSNR runs")
+    ap.add_argument("--no-batched", action="store_true", help="skip the multi-view (8 views per step) measurement")
     ap.add_argument("--gaussians", type=int, default=N_MODEL,
                     help="trained Gaussians (default 1M; smaller only for profiling captures)")
     args = ap.parse_args()

@@ -98,10 +98,13 @@ int msplat_trainer_learned_stats(MsplatTrainer t, float *last_loss, int *rounds)
 /* Views per optimizer step (no counterpart in the reference; default 1).
  * With num_views > 1 each msplat_trainer_step renders the next num_views
  * cameras of the shuffled order and applies one update from the mean of
- * their gradients (msplat_engine_train_step_batch); the step counter, the
- * schedules and MCMC still advance once per step.  Returns 0, or -1 on a
- * bad handle or num_views < 1. */
-int msplat_trainer_set_batch_views(MsplatTrainer t, int num_views);
+ * their gradients (msplat_engine_train_step_batch), with the learning rates
+ * multiplied by lr_scale (<= 0: num_views^0.75).  The iteration counter
+ * counts views: a step advances it by num_views, and the schedules keyed on
+ * it (learning-rate decay, SH degree, regularizer start, MCMC every 100
+ * iterations, the learned proposal's window) fire when their boundary is
+ * crossed.  Returns 0, or -1 on a bad handle or num_views outside 1..16. */
+int msplat_trainer_set_batch_views(MsplatTrainer t, int num_views, float lr_scale);
 
 /* Replaces the trainer's Gaussians with a trained PLY (Model::loadPly, the
  * CLI's --resume); optimizer state starts fresh.  Returns the iteration

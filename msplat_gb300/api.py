@@ -49,7 +49,7 @@ def _lib():
     L.msplat_trainer_load_ply.argtypes = [vp, cp]
     L.msplat_trainer_set_learned_relocation.argtypes = [vp, C.c_int]
     L.msplat_trainer_learned_stats.argtypes = [vp, fp, C.POINTER(C.c_int)]
-    L.msplat_trainer_set_batch_views.argtypes = [vp, C.c_int]
+    L.msplat_trainer_set_batch_views.argtypes = [vp, C.c_int, C.c_float]
     L.msplat_dataset_create_from_memory.argtypes = [C.c_int, fp, fp, C.POINTER(C.c_int), C.POINTER(vp),
                                                     C.POINTER(vp), C.c_int, fp, C.POINTER(C.c_uint8), C.c_bool,
                                                     C.c_int, C.c_bool]
@@ -278,9 +278,10 @@ class GaussianTrainer:
         if _lib().msplat_trainer_set_learned_relocation(self.h, int(enabled)) != 0:
             raise RuntimeError("could not switch the learned relocation proposal")
 
-    def set_batch_views(self, num_views: int):
-        """Render `num_views` cameras per step and update from their mean gradient."""
-        if _lib().msplat_trainer_set_batch_views(self.h, int(num_views)) != 0:
+    def set_batch_views(self, num_views: int, lr_scale: float = 0.0):
+        """Render `num_views` cameras per step and update from their mean gradient,
+        learning rates times lr_scale (0: num_views ** 0.75); iterations count views."""
+        if _lib().msplat_trainer_set_batch_views(self.h, int(num_views), float(lr_scale)) != 0:
             raise ValueError(f"invalid number of views per step: {num_views}")
 
     def learned_stats(self) -> dict:

@@ -70,7 +70,9 @@ def parse(argv=None):
                    help="stop when test-subset PSNR improves less than this (dB) over 5000 steps (needs --eval)")
     p.add_argument("--log-every", type=int, default=100, help="print progress every N steps")
     p.add_argument("--batch-views", type=int, default=1,
-                   help="cameras per optimizer step (mean gradient; 1 = one camera per step)")
+                   help="cameras per optimizer step (mean gradient; iterations count views; 1 = one camera per step)")
+    p.add_argument("--batch-lr-scale", type=float, default=0.0,
+                   help="learning-rate factor of multi-view steps (0 = batch views ** 0.75)")
     p.add_argument("--learned-relocation", action="store_true",
                    help="weight MCMC relocation sources by the online-trained proposal MLP")
     a = p.parse_args(argv)
@@ -99,7 +101,7 @@ def main(argv=None) -> int:
                            output=a.output, save_every=a.save_every)
     trainer = A.GaussianTrainer(ds, cfg)
     if a.batch_views > 1:
-        trainer.set_batch_views(a.batch_views)
+        trainer.set_batch_views(a.batch_views, a.batch_lr_scale)
     if a.learned_relocation:
         trainer.set_learned_relocation(True)
     if a.resume:
@@ -110,17 +112,22 @@ def main(argv=None) -> int:
         return 1
     last_gate, misses, stopped = -1e9, 0, 0
     t_start = time.time()
+
+    def crossed(prev, cur, period):   # a period boundary in (prev, cur]: steps may advance by several views
+        return period > 0 and cur // period > prev // period
+
     while trainer.iteration < a.num_iters:
+        prev = trainer.iteration
         s = trainer.step()
         step = s.iteration
-        if a.log_every > 0 and step % a.log_every == 0:
+        if crossed(prev, step, a.log_every):
             el = time.time() - t_start
             print(f"step={step:>6}  splats={s.splat_count:>9,}  loss={trainer.last_loss:.5f}  "
                   f"ms={s.ms_per_step:.2f}  elapsed={el:.1f}s", flush=True)
-        if a.save_every > 0 and step % a.save_every == 0:
+        if crossed(prev, step, a.save_every):
             root, ext = os.path.splitext(a.output)
             _save(trainer, f"{root}_{step}{ext or '.ply'}")
-        if (a.early_stop > 0 and a.eval and ds.num_test > 0 and step >= 10000 and step % 5000 == 0 and
+        if (a.early_stop > 0 and a.eval and ds.num_test > 0 and step >= 10000 and crossed(prev, step, 5000) and
                 step < a.num_iters):
             n_sub = min(30, ds.num_test)
             stride = max(1, ds.num_test // n_sub)

@@ -385,7 +385,11 @@ struct TrainerImpl {
     size_t cam_pos = 0;
     std::mt19937 rng{42};
     float last_loss = 0.f;
-    int batch_views = 1;   // views per optimizer step (1 = the reference's one-camera step)
+    int batch_views = 1;          // views per optimizer step (1 = the reference's one-camera step)
+    float batch_lr_scale = 1.0f;  // learning-rate factor of multi-view steps
+
+    // a period boundary crossed between iterations prev (exclusive) and cur (inclusive)
+    static bool crossed(int prev, int cur, int period) { return cur / period > prev / period; }
 
     // learned relocation proposal (off unless enabled): activity statistics
     // accumulated by the step, an MLP trained online every `window` steps on
@@ -492,8 +496,8 @@ struct TrainerImpl {
     }
 
     // every `window` steps: label the previous snapshot and train, then take a new one
-    void learned_after_step(int step) {
-        if (!lrn.enabled || step < lrn.window || step % lrn.window != 0 || model.n <= 0) return;
+    void learned_after_step(int prev, int step) {
+        if (!lrn.enabled || step < lrn.window || !crossed(prev, step, lrn.window) || model.n <= 0) return;
         cudaStream_t s = stream();
         if (lrn.pending >= 0) {
             mlp_targets(lrn.idx, lrn.snap, lrn.samples, model.p[5], lrn.gstats, lrn.T, s);
@@ -639,39 +643,45 @@ struct TrainerImpl {
         if (rc != 0) throw std::runtime_error(std::string(what) + ": " + msplat_engine_last_error(eng));
     }
 
-    // Trainer::step (msplat_api.mm:104-127) + Model::fullIteration
+    // Trainer::step (msplat_api.mm:104-127) + Model::fullIteration.  With
+    // batch_views B > 1 one step renders the next B cameras and applies one
+    // update from their mean gradient; the iteration counter advances by B
+    // (it counts views), and every schedule keyed on it (learning-rate decay,
+    // SH degree, regularizer start, MCMC every 100, the learned proposal's
+    // window) fires when its boundary is crossed.
     MsplatStats step() {
         const auto t0 = std::chrono::high_resolution_clock::now();
-        current_step++;
         if (ds->train.empty()) throw std::runtime_error("dataset has no training cameras");
+        const int B = std::max(1, batch_views);
+        const int prev = current_step;
+        current_step += B;
         adam_step_count++;
         MsplatGaussians g = model.gaussians();
         MsplatAdamState st = model.adam();
-        if (batch_views <= 1) {
+        if (B == 1) {
             HostCamera &cam = ds->train[next_camera()];
             cam.upload();
             MsplatStepArgs a;
             step_args(cam, current_step, a, true);
             check(msplat_engine_train_step(eng, &g, &st, &a, cam.d_image, cam.d_mask), "train step");
         } else {
-            // the next batch_views cameras of the shuffled order: one update from their mean gradient
-            const int B = batch_views;
             std::vector<MsplatStepArgs> a(B);
             std::vector<const uint8_t *> gt(B), mk(B);
             for (int v = 0; v < B; v++) {
                 HostCamera &cam = ds->train[next_camera()];
                 cam.upload();
                 step_args(cam, current_step, a[v], true);
+                for (int k = 0; k < 6; k++) a[v].step_size[k] *= batch_lr_scale;
                 gt[v] = cam.d_image;
                 mk[v] = cam.d_mask;
             }
             check(msplat_engine_train_step_batch(eng, &g, &st, a.data(), B, gt.data(), mk.data()), "batch step");
         }
-        learned_after_step(current_step);
+        learned_after_step(prev, current_step);
         // schedulersStep (model.cpp:256-261)
         const float t = std::clamp((float)current_step / (float)position_lr_max_steps, 0.f, 1.f);
         adam_lr[0] = std::exp(std::log(means_lr_init) * (1.f - t) + std::log(means_lr_final) * t);
-        mcmc_after_train(current_step);
+        mcmc_after_train(prev, current_step);
         const auto t1 = std::chrono::high_resolution_clock::now();
         MsplatStats s;
         s.iteration = current_step;
@@ -681,8 +691,8 @@ struct TrainerImpl {
     }
 
     // Model::mcmcAfterTrain (model.cpp:497-660), on the GPU
-    void mcmc_after_train(int step) {
-        if (step < 500 || step % 100 != 0) return;
+    void mcmc_after_train(int prev, int step) {
+        if (step < 500 || !crossed(prev, step, 100)) return;
         if (step >= (int)(cfg.iterations * 0.833f)) return;
         MsplatGaussians g = model.gaussians();
         MsplatAdamState st = model.adam();
@@ -690,7 +700,7 @@ struct TrainerImpl {
         const float *score = learned_scores();
         check(msplat_engine_mcmc_scored(eng, &g, &st, model.cap, cfg.cullRadius, &reloc_count, score, &ms), "mcmc");
         model.n = ms.num_active;
-        if (step % 1000 == 0)
+        if (crossed(prev, step, 1000))
             printf("MCMC step=%d active=%d dead=%d culled=%d nonfinite=%d grown=%d\n", step, ms.num_active,
                    ms.num_dead, ms.num_culled, ms.num_nonfinite, ms.num_grown);
         if (ms.num_nonfinite > 0) printf("MCMC nonfinite step=%d count=%d\n", step, ms.num_nonfinite);
@@ -701,7 +711,7 @@ struct TrainerImpl {
             const char *e = std::getenv("MSPLAT_NAN_INJECT");
             inject = e ? std::atoi(e) : -1;
         }
-        if (step == inject && model.n > 0) {
+        if (inject > prev && inject <= step && model.n > 0) {
             std::mt19937 r(1234);
             std::uniform_int_distribution<int> pick(0, model.n - 1);
             const float nan3[3] = {NAN, NAN, NAN};
@@ -1237,9 +1247,10 @@ int msplat_trainer_set_learned_relocation(MsplatTrainer t, int enabled) {
     return guard("learned_relocation", [&]() { TR(t)->enable_learned(enabled != 0); return 0; }, -2);
 }
 
-int msplat_trainer_set_batch_views(MsplatTrainer t, int num_views) {
-    if (!t || num_views < 1) return -1;
+int msplat_trainer_set_batch_views(MsplatTrainer t, int num_views, float lr_scale) {
+    if (!t || num_views < 1 || num_views > 16) return -1;
     TR(t)->batch_views = num_views;
+    TR(t)->batch_lr_scale = lr_scale > 0.f ? lr_scale : std::pow((float)num_views, 0.75f);
     return 0;
 }
 

@@ -168,6 +168,8 @@ constexpr int kMaxViews = 16;
 struct ViewTable {
     int count;                         // views (1..kMaxViews)
     int n;                             // Gaussians per view
+    int tiles;                         // tiles of all views (= tile_base[count])
+    long long pixels;                  // pixels of all views (= pix_base[count])
     int tile_base[kMaxViews + 1];
     int tiles_x[kMaxViews], tiles_y[kMaxViews];
     int width[kMaxViews], height[kMaxViews];

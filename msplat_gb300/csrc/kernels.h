@@ -26,6 +26,8 @@ inline ViewTable make_view_table(int n, int count, const int *w, const int *h) {
         vt.tile_base[v + 1] = vt.tile_base[v];
         vt.pix_base[v + 1] = vt.pix_base[v];
     }
+    vt.tiles = vt.tile_base[count];
+    vt.pixels = vt.pix_base[count];
     return vt;
 }
 inline ViewTable single_view_table(int n, int w, int h) { return make_view_table(n, 1, &w, &h); }

@@ -95,30 +95,43 @@ __device__ __forceinline__ void cov_state(const ProjectBwdArgs &a, int i, CovSta
             cs.V[r][c] = cs.M[r][0] * cs.M[c][0] + cs.M[r][1] * cs.M[c][1] + cs.M[r][2] * cs.M[c][2];
 }
 
-// One view's VJP (project_pix_vjp, cov2d_to_conic_vjp, project_cov3d_ewa_vjp,
-// scale_rot_to_cov3d_vjp, quat_to_rotmat_vjp) added into vm, vsc, vq.
-__device__ __forceinline__ void view_vjp(const CovState &cs, const StepParams &sp, float Wf, float Hf,
-                                         const GradRec &gr, const SplatRec &rec, float vm[3], float vsc[3],
-                                         float vq[4]) {
-    const float px = cs.px, py = cs.py, pz = cs.pz;
-    // project_pix_vjp
+// First half of one view's VJP, before the 3D covariance is needed:
+// project_pix_vjp (dL/dmean through the projected centre, gm) and
+// cov2d_to_conic_vjp (v_Sigma = -X G X, symmetric part c00, c01, c11).
+struct PixConicVjp {
+    float gm[3];
+    float c00, c01, c11;
+};
+
+__device__ __forceinline__ PixConicVjp pix_conic_vjp(float px, float py, float pz, const StepParams &sp, float Wf,
+                                                     float Hf, const GradRec &gr, const SplatRec &rec) {
+    PixConicVjp o;
     const float *m = sp.projmat;
     const float hw = m[12] * px + m[13] * py + m[14] * pz + m[15];
     const float rw = 1.f / (hw + 1e-6f);
     const float vnx = 0.5f * Wf * gr.a.x, vny = 0.5f * Hf * gr.a.y;
     const float vp0 = vnx * rw, vp1 = vny * rw;
-    float gm[3];
 #pragma unroll
-    for (int c = 0; c < 3; c++) gm[c] = m[c] * vp0 + m[4 + c] * vp1;
-
-    // cov2d_to_conic_vjp: v_Sigma = -X G X
+    for (int c = 0; c < 3; c++) o.gm[c] = m[c] * vp0 + m[4 + c] * vp1;
     const float X00 = rec.b.x, X01 = rec.b.y, X11 = rec.b.z;
     const float G00 = gr.b.x, G01 = gr.b.y, G11 = gr.b.z;
     const float XG00 = X00 * G00 + X01 * G01, XG01 = X00 * G01 + X01 * G11;
     const float XG10 = X01 * G00 + X11 * G01, XG11 = X01 * G01 + X11 * G11;
     const float VS00 = -(XG00 * X00 + XG01 * X01), VS01 = -(XG00 * X01 + XG01 * X11);
     const float VS10 = -(XG10 * X00 + XG11 * X01), VS11 = -(XG10 * X01 + XG11 * X11);
-    const float c00 = VS00, c01 = 0.5f * (VS10 + VS01), c11 = VS11;
+    o.c00 = VS00;
+    o.c01 = 0.5f * (VS10 + VS01);
+    o.c11 = VS11;
+    return o;
+}
+
+// Second half (project_cov3d_ewa_vjp, scale_rot_to_cov3d_vjp,
+// quat_to_rotmat_vjp); the whole VJP is added into vm, vsc, vq.
+__device__ __forceinline__ void cov_vjp(const CovState &cs, const StepParams &sp, const PixConicVjp &pc, float vm[3],
+                                        float vsc[3], float vq[4]) {
+    const float px = cs.px, py = cs.py, pz = cs.pz;
+    const float *gm = pc.gm;
+    const float c00 = pc.c00, c01 = pc.c01, c11 = pc.c11;
 
     // project_cov3d_ewa_vjp
     const float *v = sp.viewmat;
@@ -221,24 +234,24 @@ __device__ __forceinline__ int bands_in_use(const StepParams &sp, int rest_bases
 // Gaussians own contiguous rows of features_dc / features_rest and their
 // moments, walked with coalesced 16-byte accesses (the element's Gaussian,
 // band and channel are recovered from its offset in the rows).
-// grad(gi, band, c, g) -> true with g set when the element is updated;
-// band 15 is the DC band.
-template <int kRowF, class GradFn>
+// dc(gi, c, g) / rest(gi, band, c, g) -> true with g set when the element
+// is updated.
+template <int kRowF, class DcFn, class RestFn>
 __device__ __forceinline__ void sh_update(const ProjectBwdArgs &a, const StepParams &sp, int i0, int ng, int lane,
-                                          GradFn grad) {
+                                          DcFn dc, RestFn rest) {
     if (a.v_dc_out) {
         // export: zero where Adam would not update (culled, non-finite, band not in use)
         for (int e = lane; e < 3 * ng; e += 32) {
             const int gi = e / 3, c = e - 3 * gi;
             float g = 0.f;
-            if (!grad(gi, 15, c, g)) g = 0.f;
+            if (!dc(gi, c, g)) g = 0.f;
             a.v_dc_out[3 * (size_t)i0 + e] = g;
         }
         const int rowf = 3 * a.rest_bases;
         for (int e = lane; e < rowf * ng; e += 32) {
             const int gi = e / rowf, r = e - rowf * gi, band = r / 3, c = r - 3 * band;
             float g = 0.f;
-            if (!grad(gi, band, c, g)) g = 0.f;
+            if (!rest(gi, band, c, g)) g = 0.f;
             a.v_rest_out[(size_t)rowf * i0 + e] = g;
         }
         return;
@@ -257,7 +270,7 @@ __device__ __forceinline__ void sh_update(const ProjectBwdArgs &a, const StepPar
                 g[k] = 0.f;
                 if (e < total) {
                     const int gi = e / 3, c = e - 3 * gi;
-                    if (grad(gi, 15, c, g[k])) act |= 1u << k;
+                    if (dc(gi, c, g[k])) act |= 1u << k;
                 }
             }
             if (!act) continue;
@@ -306,7 +319,7 @@ __device__ __forceinline__ void sh_update(const ProjectBwdArgs &a, const StepPar
                     g[k] = 0.f;
                     if (e0 + k < total) {
                         const int band = r / 3, c = r - 3 * band;
-                        if (grad(gi, band, c, g[k])) act |= 1u << k;
+                        if (rest(gi, band, c, g[k])) act |= 1u << k;
                     }
                     if (++r == rowf) { r = 0; gi++; }
                 }
@@ -355,9 +368,11 @@ __global__ void __launch_bounds__(256, 4) k_project_bwd(ProjectBwdArgs a) {
         float vm[3] = {0.f, 0.f, 0.f}, vsc[3] = {0.f, 0.f, 0.f}, vq[4] = {0.f, 0.f, 0.f, 0.f};
         if (a.radii[i] > 0) {
             const GradRec gr = a.grad[i];
+            const PixConicVjp pc = pix_conic_vjp(a.means[3 * i], a.means[3 * i + 1], a.means[3 * i + 2], sp,
+                                                 (float)a.vt.width[0], (float)a.vt.height[0], gr, a.rec[i]);
             CovState cs;
             cov_state(a, i, cs);
-            view_vjp(cs, sp, (float)a.vt.width[0], (float)a.vt.height[0], gr, a.rec[i], vm, vsc, vq);
+            cov_vjp(cs, sp, pc, vm, vsc, vq);
             // SH VJP inputs for the fused Adam (or the gradient export) below
             if (want_sh) {
                 const float vc0 = gr.c.x, vc1 = gr.c.y, vc2 = gr.c.z;
@@ -377,13 +392,20 @@ __global__ void __launch_bounds__(256, 4) k_project_bwd(ProjectBwdArgs a) {
     __syncwarp();
     const int i0 = (blockIdx.x * blockDim.x) + wid * 32;
     if (i0 >= n) return;
-    sh_update<kRowF>(a, sp, i0, min(32, n - i0), lane, [&](int gi, int band, int c, float &g) {
-        const float4 vc = sh.vc[gi];
-        const int w = __float_as_int(vc.w);
-        if (band == 15 ? w <= 0 : band >= w - 1) return false;
-        g = sh.bas[gi][band] * (c == 0 ? vc.x : c == 1 ? vc.y : vc.z);
-        return true;
-    });
+    sh_update<kRowF>(
+        a, sp, i0, min(32, n - i0), lane,
+        [&](int gi, int c, float &g) {
+            const float4 vc = sh.vc[gi];
+            if (__float_as_int(vc.w) <= 0) return false;
+            g = sh.bas[gi][15] * (c == 0 ? vc.x : c == 1 ? vc.y : vc.z);
+            return true;
+        },
+        [&](int gi, int band, int c, float &g) {
+            const float4 vc = sh.vc[gi];
+            if (band >= __float_as_int(vc.w) - 1) return false;
+            g = sh.bas[gi][band] * (c == 0 ? vc.x : c == 1 ? vc.y : vc.z);
+            return true;
+        });
 }
 
 // Several views: the thread walks the Gaussian's record in every view of the
@@ -418,7 +440,8 @@ __global__ void __launch_bounds__(128, 4) k_project_bwd_views(ProjectBwdArgs a) 
             act_xy += sqrtf(gr.a.x * gr.a.x + gr.a.y * gr.a.y);
             act_vis += 1.f;
             const ViewGeom vg = view_geom(a.vt, v);
-            view_vjp(cs, sp, (float)vg.width, (float)vg.height, gr, a.rec[u], vm, vsc, vq);
+            const PixConicVjp pc = pix_conic_vjp(cs.px, cs.py, cs.pz, sp, (float)vg.width, (float)vg.height, gr, a.rec[u]);
+            cov_vjp(cs, sp, pc, vm, vsc, vq);
             const float vc0 = gr.c.x, vc1 = gr.c.y, vc2 = gr.c.z;
             if (!(finite_bits(vc0) && finite_bits(vc1) && finite_bits(vc2))) {
                 if (a.nan_counts) atomicAdd(a.nan_counts + kNanSH, 1u);
@@ -452,12 +475,18 @@ __global__ void __launch_bounds__(128, 4) k_project_bwd_views(ProjectBwdArgs a) 
     __syncwarp();
     const int i0 = (blockIdx.x * blockDim.x) + wid * 32;
     if (i0 >= n) return;
-    sh_update<kRowF>(a, sp0, i0, min(32, n - i0), lane, [&](int gi, int band, int c, float &g) {
-        const int w = sh.w[gi];
-        if (band == 15 ? w <= 0 : band >= w - 1) return false;
-        g = sh.g[gi][band == 15 ? 45 + c : 3 * band + c];
-        return true;
-    });
+    sh_update<kRowF>(
+        a, sp0, i0, min(32, n - i0), lane,
+        [&](int gi, int c, float &g) {
+            if (sh.w[gi] <= 0) return false;
+            g = sh.g[gi][45 + c];
+            return true;
+        },
+        [&](int gi, int band, int c, float &g) {
+            if (band >= sh.w[gi] - 1) return false;
+            g = sh.g[gi][3 * band + c];
+            return true;
+        });
 }
 
 void launch_project_bwd(const ProjectBwdArgs &a, cudaStream_t s) {

@@ -18,12 +18,15 @@ __constant__ float kShC3[7] = {-0.5900435899266435f, 2.890611442640554f, -0.4570
                                0.3731763325901154f, -0.4570457994644658f, 1.445305721320277f,
                                -0.5900435899266435f};
 
+// kViews: several views (blockIdx.y); false compiles the one-view step with
+// the geometry read straight from the parameter bank
+template <bool kViews>
 __global__ void __launch_bounds__(256) k_project_fwd(ProjectArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.vt.n) return;
-    const int view = blockIdx.y;
+    const int view = kViews ? (int)blockIdx.y : 0;
     const ViewGeom vg = view_geom(a.vt, view);
-    const size_t u = (size_t)view * a.vt.n + i;   // this view's record of Gaussian i
+    const size_t u = kViews ? (size_t)view * a.vt.n + i : (size_t)i;   // this view's record of Gaussian i
     const StepParams &sp = a.sp[view];
     const float Wf = (float)vg.width, Hf = (float)vg.height;
     // the rasterizer gradient record of every Gaussian starts the step at zero
@@ -186,7 +189,8 @@ __global__ void __launch_bounds__(256) k_project_fwd(ProjectArgs a) {
 
 void launch_project_fwd(const ProjectArgs &a, cudaStream_t s) {
     if (a.vt.n <= 0) return;
-    k_project_fwd<<<dim3((a.vt.n + 255) / 256, a.vt.count), 256, 0, s>>>(a);
+    if (a.vt.count > 1) k_project_fwd<true><<<dim3((a.vt.n + 255) / 256, a.vt.count), 256, 0, s>>>(a);
+    else k_project_fwd<false><<<(a.vt.n + 255) / 256, 256, 0, s>>>(a);
 }
 
 }  // namespace msplat

@@ -163,9 +163,10 @@ struct BwdPixel {
     long long p;   // global pixel index (0 when outside)
 };
 
-__device__ __forceinline__ BwdPixel bwd_pixel(const RasterArgs &a, int tile) {
+// kViews: look the view up from the global tile index; false: one view
+template <bool kViews> __device__ __forceinline__ BwdPixel bwd_pixel(const RasterArgs &a, int tile) {
     BwdPixel tp;
-    tp.view = view_of_tile(a.vt, tile);
+    tp.view = kViews ? view_of_tile(a.vt, tile) : 0;
     const ViewGeom vg = view_geom(a.vt, tp.view);
     const int lt = tile - vg.tile_base;
     const int tx = lt % vg.tiles_x, ty = lt / vg.tiles_x;
@@ -192,12 +193,13 @@ __device__ __forceinline__ void init_pixel(PixelState &ps, const RasterArgs &a, 
     ps.py = (float)tp.y;
 }
 
+template <bool kViews>
 __global__ void __launch_bounds__(kTileThreads) k_raster_bwd(RasterArgs a) {
     __shared__ BwdSmem sm;
     const int tile = blockIdx.x;
     const int s = clamp_off(a.tile_offsets[tile], a.capacity), e = clamp_off(a.tile_offsets[tile + 1], a.capacity);
     if (s >= e) return;
-    const BwdPixel tp = bwd_pixel(a, tile);
+    const BwdPixel tp = bwd_pixel<kViews>(a, tile);
     PixelState ps;
     const float Tf = tp.inside ? a.final_T[tp.p] : 0.f;
     init_pixel(ps, a, tp, Tf);
@@ -209,7 +211,7 @@ __global__ void __launch_bounds__(kTileThreads) k_raster_bwd(RasterArgs a) {
 
 __global__ void __launch_bounds__(256) k_chunk_prefix_suffix(RasterArgs a) {
     const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long P = a.vt.pix_base[a.vt.count];
+    const long long P = a.vt.pixels;
     if (p >= P) return;
     float pT = 1.f;
     for (int k = 0; k < a.k_max; k++) {
@@ -230,14 +232,15 @@ __global__ void __launch_bounds__(256) k_chunk_prefix_suffix(RasterArgs a) {
     }
 }
 
+template <bool kViews>
 __global__ void __launch_bounds__(kTileThreads) k_raster_bwd_chunked(RasterArgs a) {
     __shared__ BwdSmem sm;
     const int tile = blockIdx.x, k = blockIdx.y;
     const int s0 = clamp_off(a.tile_offsets[tile], a.capacity), e0 = clamp_off(a.tile_offsets[tile + 1], a.capacity);
     const int cs = s0 + k * kChunk, ce = min(s0 + (k + 1) * kChunk, e0);
     if (cs >= ce) return;
-    const BwdPixel tp = bwd_pixel(a, tile);
-    const size_t P = (size_t)a.vt.pix_base[a.vt.count];
+    const BwdPixel tp = bwd_pixel<kViews>(a, tile);
+    const size_t P = (size_t)a.vt.pixels;
     const size_t o = (size_t)k * P + (size_t)tp.p;
     PixelState ps;
     init_pixel(ps, a, tp, tp.inside ? a.prefix_T[o] * a.chunk_T[o] : 0.f);
@@ -254,12 +257,15 @@ __global__ void __launch_bounds__(kTileThreads) k_raster_bwd_chunked(RasterArgs 
 }
 
 void launch_raster_bwd(const RasterArgs &a, cudaStream_t s) {
+    const bool views = a.vt.count > 1;
     if (a.k_max <= 1) {
-        k_raster_bwd<<<a.num_tiles, kTileThreads, 0, s>>>(a);
+        if (views) k_raster_bwd<true><<<a.num_tiles, kTileThreads, 0, s>>>(a);
+        else k_raster_bwd<false><<<a.num_tiles, kTileThreads, 0, s>>>(a);
     } else {
-        const long long P = a.vt.pix_base[a.vt.count];
+        const long long P = a.vt.pixels;
         k_chunk_prefix_suffix<<<(unsigned)((P + 255) / 256), 256, 0, s>>>(a);
-        k_raster_bwd_chunked<<<dim3(a.num_tiles, a.k_max), kTileThreads, 0, s>>>(a);
+        if (views) k_raster_bwd_chunked<true><<<dim3(a.num_tiles, a.k_max), kTileThreads, 0, s>>>(a);
+        else k_raster_bwd_chunked<false><<<dim3(a.num_tiles, a.k_max), kTileThreads, 0, s>>>(a);
     }
 }
 

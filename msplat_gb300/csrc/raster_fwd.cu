@@ -76,31 +76,36 @@ __device__ __forceinline__ void composite_range(BatchSmem &sm, const RasterArgs 
 
 __device__ __forceinline__ float sat01(float x) { return fminf(fmaxf(x, 0.f), 1.f); }
 
-// Pixel of this thread in the CTA's tile: view geometry, coordinates, global index.
+// Pixel of this thread in the CTA's tile: view, coordinates, the view's row
+// length and first global pixel (the global index is formed where it is
+// used, so nothing wider than the coordinates stays live across the walk).
 struct TilePixel {
-    ViewGeom vg;
-    int view, x, y;
+    int view, x, y, width;
     bool inside;
-    long long p;   // global pixel index (valid when inside)
+    long long pix_base;
+    __device__ __forceinline__ long long p() const { return pix_base + (long long)y * width + x; }
 };
 
-__device__ __forceinline__ TilePixel tile_pixel(const RasterArgs &a, int tile) {
+// kViews: look the view up from the global tile index; false: one view
+template <bool kViews> __device__ __forceinline__ TilePixel tile_pixel(const RasterArgs &a, int tile) {
     TilePixel tp;
-    tp.view = view_of_tile(a.vt, tile);
-    tp.vg = view_geom(a.vt, tp.view);
-    const int lt = tile - tp.vg.tile_base;
-    const int tx = lt % tp.vg.tiles_x, ty = lt / tp.vg.tiles_x;
+    tp.view = kViews ? view_of_tile(a.vt, tile) : 0;
+    const ViewGeom vg = view_geom(a.vt, tp.view);
+    const int lt = tile - vg.tile_base;
+    const int tx = lt % vg.tiles_x, ty = lt / vg.tiles_x;
     tp.x = tx * kTile + (threadIdx.x & 15);
     tp.y = ty * kTile + (threadIdx.x >> 4);
-    tp.inside = tp.x < tp.vg.width && tp.y < tp.vg.height;
-    tp.p = tp.vg.pix_base + (long long)tp.y * tp.vg.width + tp.x;
+    tp.width = vg.width;
+    tp.inside = tp.x < vg.width && tp.y < vg.height;
+    tp.pix_base = vg.pix_base;
     return tp;
 }
 
+template <bool kViews>
 __global__ void __launch_bounds__(kTileThreads) k_raster_fwd(RasterArgs a) {
     __shared__ BatchSmem sm;
     const int tile = blockIdx.x;
-    const TilePixel tp = tile_pixel(a, tile);
+    const TilePixel tp = tile_pixel<kViews>(a, tile);
     int s = clamp_off(a.tile_offsets[tile], a.capacity), e = clamp_off(a.tile_offsets[tile + 1], a.capacity);
     if (!MS_GUARD(s >= 0 && s <= e && e <= a.capacity, 5, tile, a.nan_counts ? a.nan_counts + kDbgSlot : nullptr)) e = s = 0;
     float T;
@@ -108,8 +113,8 @@ __global__ void __launch_bounds__(kTileThreads) k_raster_fwd(RasterArgs a) {
     int last;
     composite_range(sm, a, s, e, (float)tp.x, (float)tp.y, !tp.inside, T, C, last, nullptr);
     if (!tp.inside) return;
-    const long long p = tp.p;
-    if (!MS_GUARD(p >= 0 && p < a.vt.pix_base[a.vt.count], 6, p, a.nan_counts ? a.nan_counts + kDbgSlot : nullptr)) return;
+    const long long p = tp.p();
+    if (!MS_GUARD(p >= 0 && p < a.vt.pixels, 6, p, a.nan_counts ? a.nan_counts + kDbgSlot : nullptr)) return;
     const StepParams &sp = a.sp[tp.view];
     a.final_T[p] = T;
     a.final_idx[p] = last;
@@ -118,14 +123,15 @@ __global__ void __launch_bounds__(kTileThreads) k_raster_fwd(RasterArgs a) {
     a.out_img[3 * p + 2] = sat01(__fmaf_rn(sp.bg[2], T, C.z));
 }
 
+template <bool kViews>
 __global__ void __launch_bounds__(kTileThreads) k_raster_fwd_chunked(RasterArgs a) {
     __shared__ BatchSmem sm;
     const int tile = blockIdx.x, k = blockIdx.y;
-    const TilePixel tp = tile_pixel(a, tile);
+    const TilePixel tp = tile_pixel<kViews>(a, tile);
     const int s0 = clamp_off(a.tile_offsets[tile], a.capacity), e0 = clamp_off(a.tile_offsets[tile + 1], a.capacity);
     const int cs = s0 + k * kChunk, ce = min(s0 + (k + 1) * kChunk, e0);
-    const size_t P = (size_t)a.vt.pix_base[a.vt.count];
-    const size_t o = (size_t)k * P + (size_t)tp.p;
+    const size_t P = (size_t)a.vt.pixels;
+    const size_t o = (size_t)k * P + (size_t)tp.p();
     if (cs >= ce) {
         if (tp.inside) {
             a.chunk_T[o] = 1.f;
@@ -149,7 +155,7 @@ __global__ void __launch_bounds__(kTileThreads) k_raster_fwd_chunked(RasterArgs 
 
 __global__ void __launch_bounds__(256) k_raster_merge(RasterArgs a) {
     const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long P = a.vt.pix_base[a.vt.count];
+    const long long P = a.vt.pixels;
     if (p >= P) return;
     float Tr = 1.f, cr = 0.f, cg = 0.f, cb = 0.f;
     int last = -1, cut = a.k_max;
@@ -165,7 +171,7 @@ __global__ void __launch_bounds__(256) k_raster_merge(RasterArgs a) {
         if (Tr <= 1e-4f) { cut = k + 1; break; }
     }
     for (int k = cut; k < a.k_max; k++) a.chunk_idx[(size_t)k * P + p] = -1;
-    const StepParams &sp = a.sp[view_of_pixel(a.vt, p)];
+    const StepParams &sp = a.sp[a.vt.count > 1 ? view_of_pixel(a.vt, p) : 0];
     a.final_T[p] = Tr;
     a.final_idx[p] = last;
     a.out_img[3 * p + 0] = sat01(__fmaf_rn(sp.bg[0], Tr, cr));
@@ -174,11 +180,14 @@ __global__ void __launch_bounds__(256) k_raster_merge(RasterArgs a) {
 }
 
 void launch_raster_fwd(const RasterArgs &a, cudaStream_t s) {
+    const bool views = a.vt.count > 1;
     if (a.k_max <= 1) {
-        k_raster_fwd<<<a.num_tiles, kTileThreads, 0, s>>>(a);
+        if (views) k_raster_fwd<true><<<a.num_tiles, kTileThreads, 0, s>>>(a);
+        else k_raster_fwd<false><<<a.num_tiles, kTileThreads, 0, s>>>(a);
     } else {
-        k_raster_fwd_chunked<<<dim3(a.num_tiles, a.k_max), kTileThreads, 0, s>>>(a);
-        const long long P = a.vt.pix_base[a.vt.count];
+        if (views) k_raster_fwd_chunked<true><<<dim3(a.num_tiles, a.k_max), kTileThreads, 0, s>>>(a);
+        else k_raster_fwd_chunked<false><<<dim3(a.num_tiles, a.k_max), kTileThreads, 0, s>>>(a);
+        const long long P = a.vt.pixels;
         k_raster_merge<<<(unsigned)((P + 255) / 256), 256, 0, s>>>(a);
     }
 }

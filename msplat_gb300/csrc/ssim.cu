@@ -25,13 +25,24 @@ constexpr int kS = 16, kHalo = 5, kSpan = kS + 2 * kHalo;   // 26
 __device__ __forceinline__ const uint8_t *step_gt(const LossArgs &a, int v) { return a.gt ? a.gt : a.sp[v].gt; }
 __device__ __forceinline__ const uint8_t *step_mask(const LossArgs &a, int v) { return a.gt ? a.mask : a.sp[v].mask; }
 
-// The CTA's block: view, geometry, block origin (pixels)
+// The CTA's block: view, geometry, block origin (pixels).  kViews: the grid
+// is the global tile range of several views; false: one view, a 2D grid of
+// its blocks, geometry straight from the parameter bank.
 struct LossBlock {
     int view, W, H, x0, y0;
     long long pb;   // global index of the view's pixel 0
 };
-__device__ __forceinline__ LossBlock loss_block(const LossArgs &a) {
+template <bool kViews> __device__ __forceinline__ LossBlock loss_block(const LossArgs &a) {
     LossBlock b;
+    if (!kViews) {
+        b.view = 0;
+        b.W = a.vt.width[0];
+        b.H = a.vt.height[0];
+        b.x0 = blockIdx.x * kS;
+        b.y0 = blockIdx.y * kS;
+        b.pb = 0;
+        return b;
+    }
     const int tile = blockIdx.x;
     b.view = view_of_tile(a.vt, tile);
     const ViewGeom vg = view_geom(a.vt, b.view);
@@ -44,9 +55,10 @@ __device__ __forceinline__ LossBlock loss_block(const LossArgs &a) {
     return b;
 }
 
+template <bool kViews>
 __global__ void __launch_bounds__(256) k_ssim_h(LossArgs a) {
     __shared__ float sg[3][kS][kSpan], sr[3][kS][kSpan];
-    const LossBlock lb = loss_block(a);
+    const LossBlock lb = loss_block<kViews>(a);
     const uint8_t *gt = step_gt(a, lb.view);
     const int W = lb.W, H = lb.H;
     const int bx = lb.x0 - kHalo, by = lb.y0;
@@ -66,7 +78,7 @@ __global__ void __launch_bounds__(256) k_ssim_h(LossArgs a) {
     const int lx = tid & 15, ly = tid >> 4;
     const int x = lb.x0 + lx, y = by + ly;
     if (x >= W || y >= H) return;
-    const size_t P = (size_t)a.vt.pix_base[a.vt.count], p = lb.pb + (size_t)y * W + x;
+    const size_t P = (size_t)a.vt.pixels, p = lb.pb + (size_t)y * W + x;
 #pragma unroll
     for (int c = 0; c < 3; c++) {
         float mx = 0.f, my = 0.f, sx = 0.f, sy = 0.f, cr = 0.f;
@@ -83,14 +95,15 @@ __global__ void __launch_bounds__(256) k_ssim_h(LossArgs a) {
     }
 }
 
-__global__ void __launch_bounds__(256) k_ssim_fields(LossArgs a) {
+template <bool kViews>
+__global__ void __launch_bounds__(256, 6) k_ssim_fields(LossArgs a) {
     __shared__ float hp[5][kSpan][kSpan];
     __shared__ float mv[5][kS][kSpan];   // vertical moments at the window centres
     __shared__ float fl[3][kS][kSpan];
     __shared__ float red[8];
-    const LossBlock lb = loss_block(a);
+    const LossBlock lb = loss_block<kViews>(a);
     const int W = lb.W, H = lb.H;
-    const size_t P = (size_t)a.vt.pix_base[a.vt.count];
+    const size_t P = (size_t)a.vt.pixels;
     const int bx = lb.x0 - kHalo, by = lb.y0 - kHalo;
     const int tid = threadIdx.x, lx = tid & 15, ly = tid >> 4;
     const StepParams &sp = a.sp[lb.view];
@@ -190,11 +203,12 @@ __global__ void __launch_bounds__(256) k_ssim_fields(LossArgs a) {
     if (nwin && a.nan_counts) atomicAdd(a.nan_counts + kNanSsimWin, nwin);
 }
 
+template <bool kViews>
 __global__ void __launch_bounds__(256) k_ssim_bwd(LossArgs a) {
     __shared__ float sh[9][kSpan][kS];
-    const LossBlock lb = loss_block(a);
+    const LossBlock lb = loss_block<kViews>(a);
     const int W = lb.W, H = lb.H;
-    const size_t P = (size_t)a.vt.pix_base[a.vt.count];
+    const size_t P = (size_t)a.vt.pixels;
     const int bx = lb.x0, by = lb.y0 - kHalo;
     const int tid = threadIdx.x, lx = tid & 15, ly = tid >> 4;
     for (int i = tid; i < kSpan * kS; i += 256) {
@@ -249,9 +263,16 @@ void launch_loss(const LossArgs &a, cudaStream_t s) {
         cudaMemcpyToSymbol(kGauss, w, sizeof(w));
         if (dev >= 0 && dev < 64) g_gauss_ready[dev] = true;
     }
-    k_ssim_h<<<a.num_tiles, 256, 0, s>>>(a);
-    k_ssim_fields<<<a.num_tiles, 256, 0, s>>>(a);
-    k_ssim_bwd<<<a.num_tiles, 256, 0, s>>>(a);
+    if (a.vt.count > 1) {
+        k_ssim_h<true><<<a.num_tiles, 256, 0, s>>>(a);
+        k_ssim_fields<true><<<a.num_tiles, 256, 0, s>>>(a);
+        k_ssim_bwd<true><<<a.num_tiles, 256, 0, s>>>(a);
+    } else {
+        const dim3 grid(a.vt.tiles_x[0], a.vt.tiles_y[0]);
+        k_ssim_h<false><<<grid, 256, 0, s>>>(a);
+        k_ssim_fields<false><<<grid, 256, 0, s>>>(a);
+        k_ssim_bwd<false><<<grid, 256, 0, s>>>(a);
+    }
 }
 
 }  // namespace msplat

@@ -27,10 +27,11 @@ __device__ __forceinline__ bool splat_active(size_t u, const int *radii, const f
     return finite_bits(d) && d > 0.0f;
 }
 
+template <bool kViews>
 __global__ void __launch_bounds__(256) k_count(TileArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int view = blockIdx.y;
-    const size_t u = (size_t)view * a.vt.n + i;
+    const int view = kViews ? (int)blockIdx.y : 0;
+    const size_t u = kViews ? (size_t)view * a.vt.n + i : (size_t)i;
     if (i >= a.vt.n || !splat_active(u, a.radii, a.depths)) return;
     const ViewGeom vg = view_geom(a.vt, view);
     const float4 ra = a.rec[u].a;
@@ -102,10 +103,11 @@ __global__ void __launch_bounds__(1024) k_scan(TileArgs a) {
     }
 }
 
+template <bool kViews>
 __global__ void __launch_bounds__(256) k_scatter(TileArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int view = blockIdx.y;
-    const size_t u = (size_t)view * a.vt.n + i;
+    const int view = kViews ? (int)blockIdx.y : 0;
+    const size_t u = kViews ? (size_t)view * a.vt.n + i : (size_t)i;
     if (i >= a.vt.n || !splat_active(u, a.radii, a.depths)) return;
     const ViewGeom vg = view_geom(a.vt, view);
     const float4 ra = a.rec[u].a;
@@ -142,14 +144,15 @@ __device__ __forceinline__ void agg_rect(const TileArgs &a, const ViewGeom &vg, 
     tile_rect(ra.x, ra.y, ab.x, ab.y, vg.tiles_x, vg.tiles_y, x0, y0, x1, y1);
 }
 
+template <bool kViews>
 __global__ void __launch_bounds__(kAggThreads) k_count_agg(TileArgs a) {
     extern __shared__ uint32_t bins[];
-    const int view = blockIdx.y;
+    const int view = kViews ? (int)blockIdx.y : 0;
     const ViewGeom vg = view_geom(a.vt, view);
     const int T = vg.tiles_x * vg.tiles_y;
     for (int t = threadIdx.x; t < T; t += blockDim.x) bins[t] = 0;
     __syncthreads();
-    const size_t ubase = (size_t)view * a.vt.n;
+    const size_t ubase = kViews ? (size_t)view * a.vt.n : 0;
     const int g0 = blockIdx.x * kAggPerCta, g1 = min(a.vt.n, g0 + kAggPerCta);
     for (int i = g0 + threadIdx.x; i < g1; i += blockDim.x) {
         if (!splat_active(ubase + i, a.radii, a.depths)) continue;
@@ -168,12 +171,13 @@ __global__ void __launch_bounds__(kAggThreads) k_count_agg(TileArgs a) {
 // access is a 128-byte line while the lanes share a view) and splits the
 // rows over its 32 warps: row sums, a scan of the 32 partial sums per tile in
 // shared memory, then the rows rewritten.
+template <bool kViews>
 __global__ void __launch_bounds__(1024) k_cta_scan(TileArgs a, int ctas) {
     __shared__ uint32_t part[32][33];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int t = blockIdx.x * 32 + lane;
     const int tc = min(t, a.num_tiles - 1);
-    const ViewGeom vg = view_geom(a.vt, view_of_tile(a.vt, tc));
+    const ViewGeom vg = view_geom(a.vt, kViews ? view_of_tile(a.vt, tc) : 0);
     const int Tv = vg.tiles_x * vg.tiles_y;
     uint32_t *col = a.cta_bins + (size_t)ctas * vg.tile_base + (tc - vg.tile_base);
     const int per = (ctas + 31) / 32;
@@ -199,15 +203,16 @@ __global__ void __launch_bounds__(1024) k_cta_scan(TileArgs a, int ctas) {
     }
 }
 
+template <bool kViews>
 __global__ void __launch_bounds__(kAggThreads) k_scatter_agg(TileArgs a) {
     extern __shared__ uint32_t bins[];
-    const int view = blockIdx.y;
+    const int view = kViews ? (int)blockIdx.y : 0;
     const ViewGeom vg = view_geom(a.vt, view);
     const int T = vg.tiles_x * vg.tiles_y;
     const uint32_t *row = a.cta_bins + (size_t)gridDim.x * vg.tile_base + (size_t)blockIdx.x * T;
     for (int t = threadIdx.x; t < T; t += blockDim.x) bins[t] = a.tile_offsets[vg.tile_base + t] + row[t];
     __syncthreads();
-    const size_t ubase = (size_t)view * a.vt.n;
+    const size_t ubase = kViews ? (size_t)view * a.vt.n : 0;
     const int g0 = blockIdx.x * kAggPerCta, g1 = min(a.vt.n, g0 + kAggPerCta);
     for (int i = g0 + threadIdx.x; i < g1; i += blockDim.x) {
         const size_t u = ubase + i;
@@ -580,8 +585,10 @@ int launch_tiles(const TileArgs &a, int num_sms, cudaStream_t s) {
                              (int)pair_smem_bytes<512>());
         cudaFuncSetAttribute(k_sort_pack_smem<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)pair_smem_bytes<1024>());
-        cudaFuncSetAttribute(k_count_agg, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
-        cudaFuncSetAttribute(k_scatter_agg, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
+        cudaFuncSetAttribute(k_count_agg<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
+        cudaFuncSetAttribute(k_count_agg<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
+        cudaFuncSetAttribute(k_scatter_agg<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
+        cudaFuncSetAttribute(k_scatter_agg<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
         attr_set = true;
     }
     int launches = 0;
@@ -589,14 +596,18 @@ int launch_tiles(const TileArgs &a, int num_sms, cudaStream_t s) {
     const bool agg = maxT <= kAggMaxTiles && a.cta_bins != nullptr;
     const int agg_blocks = (n + kAggPerCta - 1) / kAggPerCta;
     const size_t agg_smem = (size_t)maxT * sizeof(uint32_t);
+    const bool mv = views > 1;
     if (n > 0 && agg) {
-        k_count_agg<<<dim3(agg_blocks, views), kAggThreads, agg_smem, s>>>(a);
+        if (mv) k_count_agg<true><<<dim3(agg_blocks, views), kAggThreads, agg_smem, s>>>(a);
+        else k_count_agg<false><<<agg_blocks, kAggThreads, agg_smem, s>>>(a);
         debug_sync(s, "count");
-        k_cta_scan<<<(a.num_tiles + 31) / 32, 1024, 0, s>>>(a, agg_blocks);
+        if (mv) k_cta_scan<true><<<(a.num_tiles + 31) / 32, 1024, 0, s>>>(a, agg_blocks);
+        else k_cta_scan<false><<<(a.num_tiles + 31) / 32, 1024, 0, s>>>(a, agg_blocks);
         debug_sync(s, "cta_scan");
         launches += 2;
     } else if (n > 0) {
-        k_count<<<dim3((n + 255) / 256, views), 256, 0, s>>>(a);
+        if (mv) k_count<true><<<dim3((n + 255) / 256, views), 256, 0, s>>>(a);
+        else k_count<false><<<(n + 255) / 256, 256, 0, s>>>(a);
         debug_sync(s, "count");
         launches += 1;
     }
@@ -604,8 +615,13 @@ int launch_tiles(const TileArgs &a, int num_sms, cudaStream_t s) {
     debug_sync(s, "scan");
     launches += 1;
     if (n > 0) {
-        if (agg) k_scatter_agg<<<dim3(agg_blocks, views), kAggThreads, agg_smem, s>>>(a);
-        else k_scatter<<<dim3((n + 255) / 256, views), 256, 0, s>>>(a);
+        if (agg) {
+            if (mv) k_scatter_agg<true><<<dim3(agg_blocks, views), kAggThreads, agg_smem, s>>>(a);
+            else k_scatter_agg<false><<<agg_blocks, kAggThreads, agg_smem, s>>>(a);
+        } else {
+            if (mv) k_scatter<true><<<dim3((n + 255) / 256, views), 256, 0, s>>>(a);
+            else k_scatter<false><<<(n + 255) / 256, 256, 0, s>>>(a);
+        }
         debug_sync(s, "scatter");
         launches += 1;
     }

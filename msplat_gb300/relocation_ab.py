@@ -1,7 +1,7 @@
 """Time-to-PSNR of the learned relocation proposal against plain
 opacity-weighted MCMC relocation, on the small synthetic scene.
 
-    python -m msplat_gb300.relocation_ab [--iters 6000] [--seed 0] [--arms plain,learned,batch4]
+    python -m msplat_gb300.relocation_ab [--iters 6000] [--seed 0] [--arms plain,learned,batch4x3_learned]
 
 Scene: 16,384 ground-truth Gaussians (synthetic.config_small), 8 training
 views at 256x256 and 4 held-out views between them, targets rendered by the
@@ -11,8 +11,10 @@ means, colours from the ground truth) and the same configuration (MCMC cap
 Held-out PSNR is measured every `--eval-every` steps outside the timed
 training time.  Time-to-PSNR: the training wall-clock at which each arm
 first reaches the plain arm's final PSNR minus 0.1 dB.  Optional arms
-`batchB` and `batchB_learned` train with B views per optimizer step (the
-mean gradient of B cameras, one update), same step count.  Prints one JSON
+`batchB[xS][_learned]` train with B views per optimizer step (the mean
+gradient of B cameras, one update, learning rates x S, default
+`--batch-lr-scale` or B ** 0.75); iterations count views, so every arm sees
+the same number of views.  Prints one JSON
 line.
 """
 from __future__ import annotations
@@ -45,7 +47,7 @@ def _scene(seed):
     return list(sc.train_cams) + list(test), imgs, xyz, col
 
 
-def run_arm(cams, imgs, xyz, col, learned, iters, eval_every, batch=1):
+def run_arm(cams, imgs, xyz, col, learned, iters, eval_every, batch=1, lr_scale=0.0):
     import torch
     from . import api as A
     # the last 4 views are held out: train on the first 8, evaluate the others by pose
@@ -55,7 +57,7 @@ def run_arm(cams, imgs, xyz, col, learned, iters, eval_every, batch=1):
     if learned:
         t.set_learned_relocation(True)
     if batch > 1:
-        t.set_batch_views(batch)
+        t.set_batch_views(batch, lr_scale)
 
     def held_out_psnr():
         vals = []
@@ -70,7 +72,8 @@ def run_arm(cams, imgs, xyz, col, learned, iters, eval_every, batch=1):
     torch.cuda.synchronize()
     while t.iteration < iters:
         t0 = time.perf_counter()
-        for _ in range(eval_every):
+        stop = min(iters, t.iteration + eval_every)   # iterations count views
+        while t.iteration < stop:
             t.step()
         A.sync()
         train_s += time.perf_counter() - t0
@@ -88,14 +91,18 @@ def time_to(curve, target):
     return None, None
 
 
-def _arm_spec(name):
-    """'plain' | 'learned' | 'batch<B>' | 'batch<B>_learned' -> (learned, B)"""
+def _arm_spec(name, default_lr=0.0):
+    """'plain' | 'learned' | 'batch<B>[x<lr scale>][_learned]' -> (learned, B, lr scale)"""
     learned = name.endswith("learned")
     base = name[:-len("_learned")] if name.endswith("_learned") else name
     if base.startswith("batch"):
-        return learned, int(base[len("batch"):])
+        spec = base[len("batch"):]
+        if "x" in spec:
+            b, lr = spec.split("x", 1)
+            return learned, int(b), float(lr)
+        return learned, int(spec), default_lr
     if base in ("plain", "learned"):
-        return learned, 1
+        return learned, 1, 0.0
     raise ValueError(f"unknown arm {name!r}")
 
 
@@ -105,6 +112,7 @@ def main(argv=None):
     ap.add_argument("--eval-every", type=int, default=250)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--arms", default="plain,learned", help="comma-separated; the first is the target's source")
+    ap.add_argument("--batch-lr-scale", type=float, default=0.0, help="learning-rate factor of batch arms (0: B ** 0.75)")
     a = ap.parse_args(argv)
     names = [x.strip() for x in a.arms.split(",") if x.strip()]
     if "plain" not in names:
@@ -114,8 +122,8 @@ def main(argv=None):
     cams, imgs, xyz, col = _scene(a.seed)
     runs = {}
     for nm in names:
-        learned, b = _arm_spec(nm)
-        runs[nm] = run_arm(cams, imgs, xyz, col, learned, a.iters, a.eval_every, batch=b)
+        learned, b, lr = _arm_spec(nm, a.batch_lr_scale)
+        runs[nm] = run_arm(cams, imgs, xyz, col, learned, a.iters, a.eval_every, batch=b, lr_scale=lr)
     plain = runs["plain"]
     target = plain["final_psnr"] - 0.1
     ps, pt = time_to(plain["curve"], target)

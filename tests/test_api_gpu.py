@@ -128,24 +128,25 @@ def test_training_render_evaluate(scene):
 
 
 def test_batch_views_step(scene):
-    """set_batch_views(4) with four training cameras: step 1 renders each
-    camera once and applies one update from their mean gradient, the
-    engine's multi-view step on the same views (any order: the mean does
-    not depend on it beyond float rounding); training then still converges."""
+    """set_batch_views(4, 1.0) with four training cameras: the first step
+    renders each camera once and applies one update from their mean
+    gradient, the engine's multi-view step on the same views (any order: the
+    mean does not depend on it beyond float rounding), and advances the
+    iteration counter by 4; training then still converges."""
     torch = pytest.importorskip("torch")
     gt, cams, imgs, xyz, rgb = scene
     ds = A.Dataset.from_arrays(cams[:4], imgs[:4], xyz, rgb)
     t = A.GaussianTrainer(ds, _config(bg_color=[0.0, 0.0, 0.0]))
-    t.set_batch_views(4)
+    t.set_batch_views(4, 1.0)
     with pytest.raises(ValueError):
         t.set_batch_views(0)
     g0 = S.GaussianSet(*t.get_gaussians())
     s = t.step()
-    assert s.iteration == 1
+    assert s.iteration == 4
     g1 = t.get_gaussians()
     eng = E.Engine(0)
     dg = E.DeviceGaussians(g0)
-    args = [E.make_args(E.camera_dict(c), E.step_scalars(1, 1, width=c.width, height=c.height), do_sgld=True)
+    args = [E.make_args(E.camera_dict(c), E.step_scalars(4, 1, width=c.width, height=c.height), do_sgld=True)
             for c in cams[:4]]
     gts = [torch.from_numpy(im).cuda() for im in imgs[:4]]
     eng.train_step_batch(dg, args, [g.data_ptr() for g in gts])
