@@ -199,6 +199,36 @@ int msplat_engine_set_activity_stats(MsplatEngine *e, void *stats);
 int msplat_engine_mcmc_scored(MsplatEngine *e, const MsplatGaussians *g, const MsplatAdamState *st, int cap_max,
                               float cull_radius, int *relocation_count, const float *score, MsplatMcmcStats *out);
 
+/* Launch configuration of the tunable stages (no counterpart in the
+ * reference; the defaults are the reference's choices).  None changes the
+ * tile lists; sort_width and raster_batch leave every output bit-identical,
+ * raster_mode and chunk change the image at float rounding (as the
+ * reference's own monolithic / chunked choice does). */
+typedef struct {
+    int sort_width;    /* CTA width of the lightest shared-memory tile sort: 256 (tiles up to
+                          2048 keys) or 512 (up to 4096); default 512 */
+    int raster_batch;  /* splats staged per shared-memory round in the rasterizers: 128 or 256;
+                          default 256 */
+    int chunk;         /* splats per depth chunk of the chunked rasterizer: 256, 512 or 1024;
+                          default 512 */
+    int raster_mode;   /* used when args->raster_mode is 0: 0 the reference's rule (monolithic
+                          from 400 tiles), 1 monolithic, 2 chunked; default 0 */
+} MsplatTuning;
+
+int msplat_engine_set_tuning(MsplatEngine *e, const MsplatTuning *t);
+int msplat_engine_get_tuning(MsplatEngine *e, MsplatTuning *t);
+
+/* Autotuner: times full training steps of the given views (forward, loss,
+ * backward; no optimizer update and no SGLD, so the parameters do not
+ * change) under candidate configurations, one coordinate at a time (sort
+ * width, tile batch, then raster mode with chunk length when
+ * args[0].raster_mode is 0), keeps the fastest (the median of `reps` timed
+ * steps) and leaves it set.  gt[v] must be given for every view.  `out`
+ * receives the chosen configuration and *ms (nullable) its step time. */
+int msplat_engine_autotune(MsplatEngine *e, const MsplatGaussians *g, const MsplatStepArgs *args, int num_views,
+                           const uint8_t *const *gt, const uint8_t *const *mask, int reps, MsplatTuning *out,
+                           float *ms);
+
 /* CUDA graph mode (off by default).  When on, the second training step with
  * the same shapes, flags and buffers (parameters, moments, target, mask) is
  * captured into a CUDA graph and later such steps replay it with one launch;

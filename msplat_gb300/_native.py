@@ -60,6 +60,11 @@ class MsplatGradients(C.Structure):
                 ("v_features_dc", C.c_void_p), ("v_features_rest", C.c_void_p), ("v_opacities", C.c_void_p)]
 
 
+class MsplatTuning(C.Structure):
+    """include/msplat_engine.h MsplatTuning"""
+    _fields_ = [("sort_width", C.c_int), ("raster_batch", C.c_int), ("chunk", C.c_int), ("raster_mode", C.c_int)]
+
+
 def lib(build_if_missing: bool = True):
     global _lib
     with _lock:
@@ -98,6 +103,10 @@ def lib(build_if_missing: bool = True):
                                                      C.POINTER(vp)]
         L.msplat_engine_backward.argtypes = [vp, C.POINTER(MsplatGaussians), C.POINTER(MsplatStepArgs), vp,
                                              C.POINTER(MsplatGradients)]
+        L.msplat_engine_set_tuning.argtypes = [vp, C.POINTER(MsplatTuning)]
+        L.msplat_engine_get_tuning.argtypes = [vp, C.POINTER(MsplatTuning)]
+        L.msplat_engine_autotune.argtypes = [vp, C.POINTER(MsplatGaussians), C.POINTER(MsplatStepArgs), C.c_int,
+                                             C.POINTER(vp), C.POINTER(vp), C.c_int, C.POINTER(MsplatTuning), FP]
         L.msplat_engine_marker_elapsed.argtypes = [vp, FP]
         L.msplat_engine_stream.argtypes = [vp]
         L.msplat_engine_stream.restype = vp

@@ -18,7 +18,7 @@ namespace msplat {
 
 constexpr int kTile = 16;           // tile edge (msplat.hpp BLOCK_X/BLOCK_Y)
 constexpr int kTileThreads = 256;   // one thread per tile pixel
-constexpr int kChunk = 512;         // depth-chunk length of the chunked raster
+constexpr int kChunk = 512;         // depth-chunk length of the chunked raster (the reference's; tunable)
 
 struct SplatRec {
     float4 a;   // x, y, opacity (sigmoid), unused

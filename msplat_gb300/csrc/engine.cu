@@ -119,7 +119,8 @@ class Engine {
         const long long P = vt.pix_base[B];
         if (P > (1LL << 31) / 16) throw std::runtime_error("views too large for one step");
         const long long cap = std::max<long long>(48LL * N * B, 1);   // msplat_metal.mm:1142 legacy capacity, per view
-        const int K = choose_k(args[0], T, cap);
+        const MsplatTuning tune = tuning_;
+        const int K = choose_k(args[0], T, cap, tune);
         const bool has_gt = gts != nullptr;
         ensure_points(N, B);
         ensure_tiles(T);
@@ -178,7 +179,7 @@ class Engine {
         mark(1);
 
         TileArgs ta{};
-        ta.vt = vt; ta.num_tiles = T; ta.capacity = cap;
+        ta.vt = vt; ta.num_tiles = T; ta.capacity = cap; ta.sort_width = tune.sort_width;
         ta.radii = pa.radii; ta.depths = pa.depths; ta.rec = pa.rec; ta.aabb = pa.aabb;
         ta.tile_counts = ptr<uint32_t>("tile_counts"); ta.tile_write = ta.tile_counts + T;
         ta.tile_offsets = ptr<uint32_t>("tile_offsets"); ta.max_tile_count = ptr<uint32_t>("max_tile");
@@ -191,6 +192,7 @@ class Engine {
 
         RasterArgs ra{};
         ra.vt = vt; ra.num_tiles = T; ra.k_max = K; ra.capacity = cap;
+        ra.chunk = tune.chunk; ra.batch = tune.raster_batch;
         ra.sp = pa.sp; ra.tile_offsets = ta.tile_offsets; ra.isect_ids = ta.isect_ids;
         ra.n = (uint32_t)((long long)N * B); ra.rec = pa.rec;
         ra.out_img = ptr<float>("out_img"); ra.final_T = ptr<float>("final_T"); ra.final_idx = ptr<int>("final_idx");
@@ -268,6 +270,7 @@ class Engine {
                                  (a0.do_optimizer ? 1 : 0) | (a0.do_sgld ? 2 : 0) | (backward ? 4 : 0) | (st ? 8 : 0) |
                                      (has_gt ? 16 : 0)};
             put(head, sizeof(head));
+            put(&tune, sizeof(tune));
             put(w, sizeof(int) * B);
             put(h, sizeof(int) * B);
             const void *ps[20] = {g.means, g.scales, g.quats, g.features_dc, g.features_rest, g.opacities, gstats_};
@@ -345,6 +348,77 @@ class Engine {
         debug_sync(stream_, "project_bwd");
         launches_ += (last_K_ > 1 ? 2 : 1) + 1;
         CK(cudaGetLastError());
+    }
+
+    void set_tuning(const MsplatTuning &t) {
+        if (t.sort_width != 256 && t.sort_width != 512) throw std::runtime_error("sort_width must be 256 or 512");
+        if (t.raster_batch != 128 && t.raster_batch != 256) throw std::runtime_error("raster_batch must be 128 or 256");
+        if (t.chunk != 256 && t.chunk != 512 && t.chunk != 1024) throw std::runtime_error("chunk must be 256, 512 or 1024");
+        if (t.raster_mode < 0 || t.raster_mode > 2) throw std::runtime_error("raster_mode must be 0, 1 or 2");
+        if (std::memcmp(&t, &tuning_, sizeof(t)) != 0) clear_graphs();
+        tuning_ = t;
+    }
+    MsplatTuning tuning() const { return tuning_; }
+
+    // Coordinate-wise search over the tunable launch configuration, timing
+    // whole steps (no optimizer, no SGLD, no activity statistics) eagerly.
+    MsplatTuning autotune(const MsplatGaussians &g, const MsplatStepArgs *args, int B, const uint8_t *const *gts,
+                          const uint8_t *const *masks, int reps, float *best_ms) {
+        if (B <= 0 || B > kMaxViews) throw std::runtime_error("autotune: 1 to 16 views");
+        for (int v = 0; v < B; v++)
+            if (!gts || !gts[v]) throw std::runtime_error("autotune: a target image per view is needed");
+        reps = std::max(1, std::min(reps, 50));
+        std::vector<MsplatStepArgs> a(args, args + B);
+        for (auto &x : a) { x.do_optimizer = 0; x.do_sgld = 0; }
+        float4 *gs = gstats_;
+        const bool graphs = use_graphs_, timing = timing_;
+        gstats_ = nullptr;
+        use_graphs_ = false;
+        timing_ = false;
+        const MsplatTuning start = tuning_;
+        auto measure = [&](const MsplatTuning &t) {
+            tuning_ = t;
+            run_views(g, nullptr, a.data(), B, gts, masks, true);   // warm-up (and buffer growth)
+            std::vector<float> ms(reps);
+            for (int r = 0; r < reps; r++) {
+                CK(cudaEventRecord(marker_[0], stream_));
+                run_views(g, nullptr, a.data(), B, gts, masks, true);
+                CK(cudaEventRecord(marker_[1], stream_));
+                CK(cudaEventSynchronize(marker_[1]));
+                CK(cudaEventElapsedTime(&ms[r], marker_[0], marker_[1]));
+            }
+            std::sort(ms.begin(), ms.end());
+            return ms[reps / 2];
+        };
+        MsplatTuning best = start;
+        float bms = 0.f;
+        try {
+            bms = measure(best);
+            auto consider = [&](MsplatTuning c) {
+                if (std::memcmp(&c, &best, sizeof(c)) == 0) return;
+                const float m = measure(c);
+                if (m < bms) { bms = m; best = c; }
+            };
+            for (int w : {256, 512}) { MsplatTuning c = best; c.sort_width = w; consider(c); }
+            for (int b : {128, 256}) { MsplatTuning c = best; c.raster_batch = b; consider(c); }
+            if (a[0].raster_mode == 0) {
+                { MsplatTuning c = best; c.raster_mode = 1; consider(c); }
+                for (int ch : {256, 512, 1024}) { MsplatTuning c = best; c.raster_mode = 2; c.chunk = ch; consider(c); }
+            }
+        } catch (...) {
+            tuning_ = start;
+            gstats_ = gs;
+            use_graphs_ = graphs;
+            timing_ = timing;
+            throw;
+        }
+        gstats_ = gs;
+        use_graphs_ = graphs;
+        timing_ = timing;
+        tuning_ = best;
+        clear_graphs();
+        if (best_ms) *best_ms = bms;
+        return best;
     }
 
     void mcmc(const MsplatGaussians &g, const MsplatAdamState &st, int cap_max, float cull_radius,
@@ -498,7 +572,7 @@ class Engine {
         if (T <= cap_tiles_) return;
         alloc("tile_counts", (size_t)2 * T * 4);
         alloc("tile_offsets", (size_t)(T + 1) * 4);
-        alloc("tile_lists", (size_t)3 * T * 4);
+        alloc("tile_lists", (size_t)4 * T * 4);
         alloc("tile_class", 64, true);
         cap_tiles_ = T;
     }
@@ -529,16 +603,20 @@ class Engine {
         cap_chunks_ = KP;
     }
 
-    // K_max rule, msplat_metal.mm:1204-1224
-    static int choose_k(const MsplatStepArgs &a, int T, long long cap) {
-        if (a.raster_mode == 1) return 1;
-        if (a.raster_mode == 0 && T >= 400) return 1;
+    // K_max rule, msplat_metal.mm:1204-1224; a step in auto mode takes the
+    // tuned mode, and the chunk length is the tuned one (the reference's 512
+    // by default)
+    static int choose_k(const MsplatStepArgs &a, int T, long long cap, const MsplatTuning &t) {
+        const int mode = a.raster_mode != 0 ? a.raster_mode : t.raster_mode;
+        if (mode == 1) return 1;
+        if (mode == 0 && T >= 400) return 1;
         if (a.k_max > 0) return a.k_max;
+        const uint32_t chunk = (uint32_t)t.chunk;
         const uint32_t avg = (uint32_t)(cap / std::max(1, T));
         const uint32_t cons = avg * 6;
-        uint32_t k = (cons + kChunk - 1) / kChunk;
+        uint32_t k = (cons + chunk - 1) / chunk;
         if (k < 2) k = 2;
-        const uint32_t am = (uint32_t)((cap + kChunk - 1) / kChunk);
+        const uint32_t am = (uint32_t)((cap + chunk - 1) / chunk);
         if (k > am) k = am;
         return (int)k;
     }
@@ -595,6 +673,7 @@ class Engine {
     long long timed_steps_ = 0, launches_ = 0;
     RasterArgs last_ra_{};   // raster arguments of the last eagerly issued step
     float4 *gstats_ = nullptr;   // caller's activity statistics (learned relocation), or null
+    MsplatTuning tuning_{512, 256, kChunk, 0};   // launch configuration of the tunable stages
 
   public:
     void set_gstats(void *p) { gstats_ = static_cast<float4 *>(p); }
@@ -746,6 +825,23 @@ int msplat_engine_mcmc_scored(MsplatEngine *e, const MsplatGaussians *g, const M
                               float cull_radius, int *relocation_count, const float *score, MsplatMcmcStats *out) {
     if (!g || !st || !relocation_count || !out) return -1;
     return guarded(e, [&] { e->impl->mcmc(*g, *st, cap_max, cull_radius, *relocation_count, *out, score); });
+}
+
+int msplat_engine_set_tuning(MsplatEngine *e, const MsplatTuning *t) {
+    if (!t) return -1;
+    return guarded(e, [&] { e->impl->set_tuning(*t); });
+}
+
+int msplat_engine_get_tuning(MsplatEngine *e, MsplatTuning *t) {
+    if (!t) return -1;
+    return guarded(e, [&] { *t = e->impl->tuning(); });
+}
+
+int msplat_engine_autotune(MsplatEngine *e, const MsplatGaussians *g, const MsplatStepArgs *args, int num_views,
+                           const uint8_t *const *gt, const uint8_t *const *mask, int reps, MsplatTuning *out,
+                           float *ms) {
+    if (!g || !args || !out) return -1;
+    return guarded(e, [&] { *out = e->impl->autotune(*g, args, num_views, gt, mask, reps, ms); });
 }
 
 int msplat_engine_set_graphs(MsplatEngine *e, int enabled) {

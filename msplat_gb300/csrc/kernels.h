@@ -51,6 +51,7 @@ struct ProjectArgs {
 struct TileArgs {
     ViewTable vt;
     int num_tiles;          // over all views
+    int sort_width;         // CTA width of the lightest shared-memory sort class: 256 or 512
     long long capacity;     // intersection slots of keys / isect_ids
     const int *radii;
     const float *depths;
@@ -59,8 +60,8 @@ struct TileArgs {
     uint32_t *tile_counts;  // zeroed before the step
     uint32_t *tile_write;   // zeroed before the step
     uint32_t *cta_bins;     // per view: [ceil(n / 2048), T_v] per-CTA tile histograms (block-aggregated path)
-    uint32_t *tile_lists;   // [3, T] tiles of each sort class (written by the scan)
-    uint32_t *tile_class;   // [6]: list lengths, then the sort kernels' work counters
+    uint32_t *tile_lists;   // [4, T] tiles of each sort class (written by the scan)
+    uint32_t *tile_class;   // [8]: list lengths, then the sort kernels' work counters
     uint32_t *tile_offsets; // [T+1]
     uint32_t *max_tile_count;
     uint64_t *keys, *keys_alt;
@@ -71,6 +72,8 @@ struct TileArgs {
 struct RasterArgs {
     ViewTable vt;
     int num_tiles, k_max;       // tiles over all views; depth chunks (1 = monolithic)
+    int chunk;                  // splats per depth chunk (chunked raster)
+    int batch;                  // splats staged per shared-memory round: 128 or 256
     long long capacity;
     const StepParams *sp;       // [views]
     const uint32_t *tile_offsets;

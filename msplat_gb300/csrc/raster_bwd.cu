@@ -16,9 +16,8 @@
 
 namespace msplat {
 
-constexpr int kBB = kTileThreads;   // splats per batch
-
-struct BwdSmem {
+// kBB splats staged per round (the tile batch: 128 or 256)
+template <int kBB> struct BwdSmem {
     float4 xyo[kBB];    // x, y, opacity, id bits
     float4 con[kBB];
     float4 rgb[kBB];    // raw colour
@@ -60,20 +59,23 @@ struct PixelState {
 };
 
 // Processes splat indices [s, hi] back to front for the whole CTA.
-__device__ void backward_range(BwdSmem &sm, const RasterArgs &a, int s, int hi, PixelState &ps, GradRec *grad) {
+template <int kBB>
+__device__ void backward_range(BwdSmem<kBB> &sm, const RasterArgs &a, int s, int hi, PixelState &ps, GradRec *grad) {
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int wbin = __reduce_max_sync(0xffffffffu, ps.bin_final);
     for (int batch_end = hi; batch_end >= s; batch_end -= kBB) {
         __syncthreads();
         const int idx = batch_end - tid;
-        if (idx >= s) {
-            const SplatRec r = isect_record(a.isect_ids, a.rec, a.n, idx);
-            sm.xyo[tid] = r.a;
-            sm.con[tid] = r.b;
-            sm.rgb[tid] = r.c;
-        }
+        if (tid < kBB) {
+            if (idx >= s) {
+                const SplatRec r = isect_record(a.isect_ids, a.rec, a.n, idx);
+                sm.xyo[tid] = r.a;
+                sm.con[tid] = r.b;
+                sm.rgb[tid] = r.c;
+            }
 #pragma unroll
-        for (int k = 0; k < 9; k++) sm.acc[tid][k] = 0.f;
+            for (int k = 0; k < 9; k++) sm.acc[tid][k] = 0.f;
+        }
         __syncthreads();
         const int nb = min(kBB, batch_end - s + 1);
         for (int t = max(0, batch_end - wbin); t < nb; t++) {
@@ -193,9 +195,9 @@ __device__ __forceinline__ void init_pixel(PixelState &ps, const RasterArgs &a, 
     ps.py = (float)tp.y;
 }
 
-template <bool kViews>
+template <bool kViews, int kBB>
 __global__ void __launch_bounds__(kTileThreads) k_raster_bwd(RasterArgs a) {
-    __shared__ BwdSmem sm;
+    __shared__ BwdSmem<kBB> sm;
     const int tile = blockIdx.x;
     const int s = clamp_off(a.tile_offsets[tile], a.capacity), e = clamp_off(a.tile_offsets[tile + 1], a.capacity);
     if (s >= e) return;
@@ -206,7 +208,7 @@ __global__ void __launch_bounds__(kTileThreads) k_raster_bwd(RasterArgs a) {
     ps.bin_final = tp.inside ? a.final_idx[tp.p] : -1;
     const int hi = min(e - 1, block_max(ps.bin_final, sm.wmax));
     if (hi < s) return;
-    backward_range(sm, a, s, hi, ps, a.grad);
+    backward_range<kBB>(sm, a, s, hi, ps, a.grad);
 }
 
 __global__ void __launch_bounds__(256) k_chunk_prefix_suffix(RasterArgs a) {
@@ -232,12 +234,12 @@ __global__ void __launch_bounds__(256) k_chunk_prefix_suffix(RasterArgs a) {
     }
 }
 
-template <bool kViews>
+template <bool kViews, int kBB>
 __global__ void __launch_bounds__(kTileThreads) k_raster_bwd_chunked(RasterArgs a) {
-    __shared__ BwdSmem sm;
+    __shared__ BwdSmem<kBB> sm;
     const int tile = blockIdx.x, k = blockIdx.y;
     const int s0 = clamp_off(a.tile_offsets[tile], a.capacity), e0 = clamp_off(a.tile_offsets[tile + 1], a.capacity);
-    const int cs = s0 + k * kChunk, ce = min(s0 + (k + 1) * kChunk, e0);
+    const int cs = s0 + k * a.chunk, ce = min(s0 + (k + 1) * a.chunk, e0);
     if (cs >= ce) return;
     const BwdPixel tp = bwd_pixel<kViews>(a, tile);
     const size_t P = (size_t)a.vt.pixels;
@@ -253,20 +255,25 @@ __global__ void __launch_bounds__(kTileThreads) k_raster_bwd_chunked(RasterArgs 
     ps.bin_final = (bf >= cs) ? bf : -1;
     const int hi = min(ce - 1, block_max(ps.bin_final, sm.wmax));
     if (hi < cs) return;
-    backward_range(sm, a, cs, hi, ps, a.grad);
+    backward_range<kBB>(sm, a, cs, hi, ps, a.grad);
 }
 
-void launch_raster_bwd(const RasterArgs &a, cudaStream_t s) {
+template <int kBB> static void raster_bwd_batch(const RasterArgs &a, cudaStream_t s) {
     const bool views = a.vt.count > 1;
     if (a.k_max <= 1) {
-        if (views) k_raster_bwd<true><<<a.num_tiles, kTileThreads, 0, s>>>(a);
-        else k_raster_bwd<false><<<a.num_tiles, kTileThreads, 0, s>>>(a);
+        if (views) k_raster_bwd<true, kBB><<<a.num_tiles, kTileThreads, 0, s>>>(a);
+        else k_raster_bwd<false, kBB><<<a.num_tiles, kTileThreads, 0, s>>>(a);
     } else {
         const long long P = a.vt.pixels;
         k_chunk_prefix_suffix<<<(unsigned)((P + 255) / 256), 256, 0, s>>>(a);
-        if (views) k_raster_bwd_chunked<true><<<dim3(a.num_tiles, a.k_max), kTileThreads, 0, s>>>(a);
-        else k_raster_bwd_chunked<false><<<dim3(a.num_tiles, a.k_max), kTileThreads, 0, s>>>(a);
+        if (views) k_raster_bwd_chunked<true, kBB><<<dim3(a.num_tiles, a.k_max), kTileThreads, 0, s>>>(a);
+        else k_raster_bwd_chunked<false, kBB><<<dim3(a.num_tiles, a.k_max), kTileThreads, 0, s>>>(a);
     }
+}
+
+void launch_raster_bwd(const RasterArgs &a, cudaStream_t s) {
+    if (a.batch == 128) raster_bwd_batch<128>(a, s);
+    else raster_bwd_batch<256>(a, s);
 }
 
 }  // namespace msplat

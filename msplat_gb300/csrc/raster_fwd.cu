@@ -16,15 +16,18 @@
 
 namespace msplat {
 
-struct BatchSmem {
-    float4 xyo[kTileThreads];   // x, y, opacity
-    float4 con[kTileThreads];   // conic
-    float4 rgb[kTileThreads];   // clamped colour max(raw + 0.5, 0)
+// kBatch splats staged per round (the tile batch: 128 or 256, one per
+// thread of the first kBatch threads)
+template <int kBatch> struct BatchSmem {
+    float4 xyo[kBatch];   // x, y, opacity
+    float4 con[kBatch];   // conic
+    float4 rgb[kBatch];   // clamped colour max(raw + 0.5, 0)
 };
 
-__device__ __forceinline__ void load_batch(BatchSmem &sm, const RasterArgs &a, int idx, int end) {
+template <int kBatch>
+__device__ __forceinline__ void load_batch(BatchSmem<kBatch> &sm, const RasterArgs &a, int idx, int end) {
     const int t = threadIdx.x;
-    if (idx < end) {
+    if (t < kBatch && idx < end) {
         const SplatRec r = isect_record(a.isect_ids, a.rec, a.n, idx);
         sm.xyo[t] = r.a;
         sm.con[t] = r.b;
@@ -34,17 +37,19 @@ __device__ __forceinline__ void load_batch(BatchSmem &sm, const RasterArgs &a, i
 
 // Walks [s, e) for this pixel; the whole CTA iterates together.
 // done: in/out per-thread flag; returns (T, C, last).
-__device__ __forceinline__ void composite_range(BatchSmem &sm, const RasterArgs &a, int s, int e, float px, float py,
-                                                bool done, float &T, float3 &C, int &last, unsigned *nan_sigma) {
+template <int kBatch>
+__device__ __forceinline__ void composite_range(BatchSmem<kBatch> &sm, const RasterArgs &a, int s, int e, float px,
+                                                float py, bool done, float &T, float3 &C, int &last,
+                                                unsigned *nan_sigma) {
     T = 1.f;
     C = make_float3(0.f, 0.f, 0.f);
     last = s - 1;
-    for (int b0 = s; b0 < e; b0 += kTileThreads) {
+    for (int b0 = s; b0 < e; b0 += kBatch) {
         if (__syncthreads_count(done) == kTileThreads) break;
-        load_batch(sm, a, b0 + (int)threadIdx.x, e);
+        load_batch<kBatch>(sm, a, b0 + (int)threadIdx.x, e);
         __syncthreads();
         if (done) continue;
-        const int nb = min(kTileThreads, e - b0);
+        const int nb = min(kBatch, e - b0);
         for (int t = 0; t < nb; t++) {
             const float4 xo = sm.xyo[t];
             const float4 cn = sm.con[t];
@@ -101,9 +106,9 @@ template <bool kViews> __device__ __forceinline__ TilePixel tile_pixel(const Ras
     return tp;
 }
 
-template <bool kViews>
+template <bool kViews, int kBatch>
 __global__ void __launch_bounds__(kTileThreads) k_raster_fwd(RasterArgs a) {
-    __shared__ BatchSmem sm;
+    __shared__ BatchSmem<kBatch> sm;
     const int tile = blockIdx.x;
     const TilePixel tp = tile_pixel<kViews>(a, tile);
     int s = clamp_off(a.tile_offsets[tile], a.capacity), e = clamp_off(a.tile_offsets[tile + 1], a.capacity);
@@ -123,13 +128,13 @@ __global__ void __launch_bounds__(kTileThreads) k_raster_fwd(RasterArgs a) {
     a.out_img[3 * p + 2] = sat01(__fmaf_rn(sp.bg[2], T, C.z));
 }
 
-template <bool kViews>
+template <bool kViews, int kBatch>
 __global__ void __launch_bounds__(kTileThreads) k_raster_fwd_chunked(RasterArgs a) {
-    __shared__ BatchSmem sm;
+    __shared__ BatchSmem<kBatch> sm;
     const int tile = blockIdx.x, k = blockIdx.y;
     const TilePixel tp = tile_pixel<kViews>(a, tile);
     const int s0 = clamp_off(a.tile_offsets[tile], a.capacity), e0 = clamp_off(a.tile_offsets[tile + 1], a.capacity);
-    const int cs = s0 + k * kChunk, ce = min(s0 + (k + 1) * kChunk, e0);
+    const int cs = s0 + k * a.chunk, ce = min(s0 + (k + 1) * a.chunk, e0);
     const size_t P = (size_t)a.vt.pixels;
     const size_t o = (size_t)k * P + (size_t)tp.p();
     if (cs >= ce) {
@@ -179,17 +184,22 @@ __global__ void __launch_bounds__(256) k_raster_merge(RasterArgs a) {
     a.out_img[3 * p + 2] = sat01(__fmaf_rn(sp.bg[2], Tr, cb));
 }
 
-void launch_raster_fwd(const RasterArgs &a, cudaStream_t s) {
+template <int kBatch> static void raster_fwd_batch(const RasterArgs &a, cudaStream_t s) {
     const bool views = a.vt.count > 1;
     if (a.k_max <= 1) {
-        if (views) k_raster_fwd<true><<<a.num_tiles, kTileThreads, 0, s>>>(a);
-        else k_raster_fwd<false><<<a.num_tiles, kTileThreads, 0, s>>>(a);
+        if (views) k_raster_fwd<true, kBatch><<<a.num_tiles, kTileThreads, 0, s>>>(a);
+        else k_raster_fwd<false, kBatch><<<a.num_tiles, kTileThreads, 0, s>>>(a);
     } else {
-        if (views) k_raster_fwd_chunked<true><<<dim3(a.num_tiles, a.k_max), kTileThreads, 0, s>>>(a);
-        else k_raster_fwd_chunked<false><<<dim3(a.num_tiles, a.k_max), kTileThreads, 0, s>>>(a);
+        if (views) k_raster_fwd_chunked<true, kBatch><<<dim3(a.num_tiles, a.k_max), kTileThreads, 0, s>>>(a);
+        else k_raster_fwd_chunked<false, kBatch><<<dim3(a.num_tiles, a.k_max), kTileThreads, 0, s>>>(a);
         const long long P = a.vt.pixels;
         k_raster_merge<<<(unsigned)((P + 255) / 256), 256, 0, s>>>(a);
     }
+}
+
+void launch_raster_fwd(const RasterArgs &a, cudaStream_t s) {
+    if (a.batch == 128) raster_fwd_batch<128>(a, s);
+    else raster_fwd_batch<256>(a, s);
 }
 
 }  // namespace msplat

@@ -16,10 +16,15 @@
 
 namespace msplat {
 
-// per-tile sort classes (by key count)
-constexpr int kSortItems = 8;                    // keys per thread in the shared-memory sorts
+// per-tile sort classes (by key count): 0 up to kSortSmallKeys (256-thread
+// CTAs, when the sort width chosen is 256; else class 0 stays empty), 1 up
+// to kSortLightKeys (512-thread CTAs), 2 up to kSortHeavyKeys (1024-thread
+// CTAs), 3 above (global-memory sort)
+constexpr int kSortItems = 8;                      // keys per thread in the shared-memory sorts
+constexpr int kSortSmallKeys = 256 * kSortItems;   // 2048
 constexpr int kSortLightKeys = 512 * kSortItems;   // 4096: 512-thread CTA, two per SM
 constexpr int kSortHeavyKeys = 1024 * kSortItems;  // 8192: 1024-thread CTA, one per SM
+constexpr int kSortClasses = 4;
 
 __device__ __forceinline__ bool splat_active(size_t u, const int *radii, const float *depths) {
     if (radii[u] <= 0) return false;
@@ -51,9 +56,10 @@ __global__ void __launch_bounds__(256) k_count(TileArgs a) {
 __global__ void __launch_bounds__(1024) k_scan(TileArgs a) {
     __shared__ uint32_t warp_tot[32];
     __shared__ uint32_t max_warp[32];
-    __shared__ uint32_t class_n[3];
+    __shared__ uint32_t class_n[kSortClasses];
     const int T = a.num_tiles;
-    if (threadIdx.x < 3) class_n[threadIdx.x] = 0;
+    const uint32_t small_keys = a.sort_width == 256 ? (uint32_t)kSortSmallKeys : 0u;
+    if (threadIdx.x < kSortClasses) class_n[threadIdx.x] = 0;
     const int per = (T + 1023) / 1024;
     const int lo = min(T, (int)threadIdx.x * per), hi = min(T, lo + per);
     uint32_t sum = 0, mx = 0;
@@ -86,10 +92,12 @@ __global__ void __launch_bounds__(1024) k_scan(TileArgs a) {
         const uint32_t c = a.tile_counts[t];
         a.tile_offsets[t] = run;
         run += c;
-        // sort class of the tile: shared-memory sort by a 512- or a
+        // sort class of the tile: shared-memory sort by a 256-, 512- or
         // 1024-thread CTA, or the global-memory sort above kSortHeavyKeys
         if (c > 0) {
-            const int cls = c <= (uint32_t)kSortLightKeys ? 0 : (c <= (uint32_t)kSortHeavyKeys ? 1 : 2);
+            const int cls = c <= small_keys ? 0
+                            : c <= (uint32_t)kSortLightKeys ? 1
+                            : c <= (uint32_t)kSortHeavyKeys ? 2 : 3;
             const uint32_t pos = atomicAdd(&class_n[cls], 1u);
             a.tile_lists[(size_t)cls * T + pos] = (uint32_t)t;
         }
@@ -97,9 +105,9 @@ __global__ void __launch_bounds__(1024) k_scan(TileArgs a) {
     if (threadIdx.x == 1023) a.tile_offsets[T] = run;
     if (threadIdx.x == 0) a.max_tile_count[0] = max_warp[0];
     __syncthreads();
-    if (threadIdx.x < 3) {
-        a.tile_class[threadIdx.x] = class_n[threadIdx.x];      // list lengths
-        a.tile_class[3 + threadIdx.x] = 0;                     // work counters of the sort kernels
+    if (threadIdx.x < kSortClasses) {
+        a.tile_class[threadIdx.x] = class_n[threadIdx.x];                  // list lengths
+        a.tile_class[kSortClasses + threadIdx.x] = 0;                      // work counters of the sort kernels
     }
 }
 
@@ -273,7 +281,7 @@ template <int THREADS> __device__ bool emit_if_overflow(const TileArgs &a, uint3
 // next tile of class `cls` for this CTA, or -1; ends with a barrier
 __device__ __forceinline__ int next_tile(const TileArgs &a, int cls, int *slot) {
     if (threadIdx.x == 0) {
-        const uint32_t k = atomicAdd(a.tile_class + 3 + cls, 1u);
+        const uint32_t k = atomicAdd(a.tile_class + kSortClasses + cls, 1u);
         *slot = k < a.tile_class[cls] ? (int)a.tile_lists[(size_t)cls * a.num_tiles + k] : -1;
     }
     __syncthreads();
@@ -581,6 +589,8 @@ size_t sort_pack_smem_bytes() { return pair_smem_bytes<1024>(); }
 int launch_tiles(const TileArgs &a, int num_sms, cudaStream_t s) {
     static bool attr_set = false;
     if (!attr_set) {
+        cudaFuncSetAttribute(k_sort_pack_smem<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)pair_smem_bytes<256>());
         cudaFuncSetAttribute(k_sort_pack_smem<512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)pair_smem_bytes<512>());
         cudaFuncSetAttribute(k_sort_pack_smem<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -626,11 +636,16 @@ int launch_tiles(const TileArgs &a, int num_sms, cudaStream_t s) {
         launches += 1;
     }
     // persistent sort grids, one per class; idle classes exit at once
-    k_sort_pack_smem<512><<<2 * num_sms, 512, pair_smem_bytes<512>(), s>>>(a, 0);
+    if (a.sort_width == 256) {
+        k_sort_pack_smem<256><<<4 * num_sms, 256, pair_smem_bytes<256>(), s>>>(a, 0);
+        debug_sync(s, "sort_pack_256");
+        launches += 1;
+    }
+    k_sort_pack_smem<512><<<2 * num_sms, 512, pair_smem_bytes<512>(), s>>>(a, 1);
     debug_sync(s, "sort_pack_512");
-    k_sort_pack_smem<1024><<<num_sms, 1024, pair_smem_bytes<1024>(), s>>>(a, 1);
+    k_sort_pack_smem<1024><<<num_sms, 1024, pair_smem_bytes<1024>(), s>>>(a, 2);
     debug_sync(s, "sort_pack_1024");
-    k_sort_pack_global<<<num_sms, kGlobThreads, 0, s>>>(a, 2);
+    k_sort_pack_global<<<num_sms, kGlobThreads, 0, s>>>(a, 3);
     debug_sync(s, "sort_pack_global");
     return launches + 3;
 }

@@ -213,6 +213,38 @@ class Engine:
         """Capture repeated steps into CUDA graphs and replay them."""
         self._check(self.L.msplat_engine_set_graphs(self.h, int(on)))
 
+    TUNING_FIELDS = ("sort_width", "raster_batch", "chunk", "raster_mode")
+
+    def set_tuning(self, **kw):
+        """Change fields of the launch configuration (see MsplatTuning)."""
+        t = N.MsplatTuning()
+        self._check(self.L.msplat_engine_get_tuning(self.h, C.byref(t)))
+        for k, v in kw.items():
+            if k not in self.TUNING_FIELDS:
+                raise KeyError(k)
+            setattr(t, k, int(v))
+        self._check(self.L.msplat_engine_set_tuning(self.h, C.byref(t)))
+
+    def tuning(self) -> dict:
+        t = N.MsplatTuning()
+        self._check(self.L.msplat_engine_get_tuning(self.h, C.byref(t)))
+        return {k: getattr(t, k) for k in self.TUNING_FIELDS}
+
+    def autotune(self, dg: "DeviceGaussians", args: list, gt_ptrs: list, mask_ptrs: list | None = None,
+                 reps: int = 3):
+        """Time the candidate launch configurations on these views and keep the
+        fastest; returns (configuration dict, step ms)."""
+        g, _ = dg.native()
+        n = len(args)
+        arr = (N.MsplatStepArgs * n)(*args)
+        gts = (C.c_void_p * n)(*gt_ptrs)
+        masks = (C.c_void_p * n)(*(mask_ptrs or [None] * n))
+        t = N.MsplatTuning()
+        ms = C.c_float()
+        self._check(self.L.msplat_engine_autotune(self.h, C.byref(g), arr, n, gts, masks, int(reps), C.byref(t),
+                                                  C.byref(ms)))
+        return {k: getattr(t, k) for k in self.TUNING_FIELDS}, float(ms.value)
+
     def buffer(self, name: str):
         p = C.c_void_p()
         n = self.L.msplat_engine_buffer(self.h, name.encode(), C.byref(p))
