@@ -234,6 +234,12 @@ def run_batched(eng, E, sc, dg, warmup, steps, step_base):
                             do_sgld=True) for cd in cams]
         eng.train_step_batch(dg, args, ptrs)
 
+    # the launch configuration: tuned on this workload (CUDA events, whole
+    # steps without updates), then the timed steps replay the tuned graph
+    untuned = eng.tuning()
+    args0 = [E.make_args(cd, E.step_scalars(step_base, step_base, width=cd["width"], height=cd["height"]))
+             for cd in cams]
+    tuned, tuned_ms = eng.autotune(dg, args0, ptrs, reps=3)
     for k in range(warmup):
         one(k)
     eng.synchronize()
@@ -244,12 +250,22 @@ def run_batched(eng, E, sc, dg, warmup, steps, step_base):
     eng.marker(1)
     ms = eng.marker_elapsed() / steps
     launches = (eng.stats().launches - l0) / steps
+    # per-stage times from eager steps with events between the stages
+    eng.set_timing(True)
+    for k in range(5):
+        one(warmup + steps + k)
+    eng.synchronize()
+    st = eng.stats()
+    eng.set_timing(False)
+    stage_ms = {name: st.stage_ms[i] / max(1, st.timed_steps) for i, name in enumerate(E.N.STAGES)}
     px = sum(w * h for w, h in BATCH_SIZES)
     return {"workload": "8 views per step: 2 each of 1297x840, 979x546, 648x420, 2594x1680 "
                         f"({px / 1e6:.2f} Mpx), {dg.n / 1e6:g}M Gaussians, one launch per stage, CUDA graph",
             "views_per_step": len(cams), "ms_per_step": ms, "iters_per_s": 1e3 / ms,
             "views_per_s": len(cams) * 1e3 / ms, "mpx_per_s": px / 1e6 * 1e3 / ms,
-            "launches_per_step": launches, "loss": eng.loss()}
+            "launches_per_step": launches, "loss": eng.loss(), "stage_ms": stage_ms,
+            "num_intersections": int(st.num_intersections), "tuning": tuned, "untuned": untuned,
+            "autotune_step_ms": tuned_ms}
 
 
 def config_dict(args):

@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(256) k_scatter(TileArgs a) {
 // filled CTA by CTA.  Used while every view's histogram fits (kAggMaxTiles).
 constexpr int kAggPerCta = 2048;
 constexpr int kAggThreads = 512;   // four CTAs per SM: 1M Gaussians fill one wave
-constexpr int kAggMaxTiles = 12288;
+constexpr int kAggMaxTiles = 20480;   // 80 KB of histogram: two 512-thread CTAs per SM at the largest
 
 __device__ __forceinline__ void agg_rect(const TileArgs &a, const ViewGeom &vg, size_t u, int &x0, int &y0, int &x1,
                                          int &y1) {
