@@ -701,9 +701,9 @@ struct TrainerImpl {
         check(msplat_engine_mcmc_scored(eng, &g, &st, model.cap, cfg.cullRadius, &reloc_count, score, &ms), "mcmc");
         model.n = ms.num_active;
         if (crossed(prev, step, 1000))
-            printf("MCMC step=%d active=%d dead=%d culled=%d nonfinite=%d grown=%d\n", step, ms.num_active,
+            fprintf(stderr, "MCMC step=%d active=%d dead=%d culled=%d nonfinite=%d grown=%d\n", step, ms.num_active,
                    ms.num_dead, ms.num_culled, ms.num_nonfinite, ms.num_grown);
-        if (ms.num_nonfinite > 0) printf("MCMC nonfinite step=%d count=%d\n", step, ms.num_nonfinite);
+        if (ms.num_nonfinite > 0) fprintf(stderr, "MCMC nonfinite step=%d count=%d\n", step, ms.num_nonfinite);
         // MSPLAT_NAN_INJECT=<step>: poison features_dc of 100 Gaussians (host-side fault injection,
         // model.cpp:638-659)
         static int inject = -2;
@@ -717,7 +717,7 @@ struct TrainerImpl {
             const float nan3[3] = {NAN, NAN, NAN};
             for (int k = 0; k < 100; k++)
                 CKA(cudaMemcpy(model.p[3] + 3 * (size_t)pick(r), nan3, 12, cudaMemcpyHostToDevice));
-            printf("MCMC nan-inject step=%d poisoned=100 (featuresDc)\n", step);
+            fprintf(stderr, "MCMC nan-inject step=%d poisoned=100 (featuresDc)\n", step);
         }
     }
 
