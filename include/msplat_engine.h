@@ -87,6 +87,7 @@ typedef struct {
     long long timed_steps;         /* steps whose stage times are summed (at most the last 128) */
     long long launches;            /* engine kernel launches since creation */
     uint32_t check_record[3];      /* checked builds: first failed bound (code, index lo, index hi) */
+    int isect_groups;              /* tile groups of the last step (fixed intersection budget; 1 otherwise) */
 } MsplatEngineStats;
 
 /* Creates an engine on CUDA device `device`.  max_points sizes the
@@ -198,6 +199,19 @@ int msplat_engine_set_activity_stats(MsplatEngine *e, void *stats);
  * unchanged. */
 int msplat_engine_mcmc_scored(MsplatEngine *e, const MsplatGaussians *g, const MsplatAdamState *st, int cap_max,
                               float cull_radius, int *relocation_count, const float *score, MsplatMcmcStats *out);
+
+/* Fixed intersection budget (the reference CLI's fixed buffers,
+ * cli/msplat.mm:199-235 and msplat_metal.mm:1519-1596): `slots`
+ * intersection slots (20 bytes each: key, sort scratch, id) allocated once
+ * instead of the legacy 48 per Gaussian and view.  A step whose views need
+ * more is rastered in groups of consecutive tiles that fit: after the
+ * projection and the tile counts the host reads the counts, then each group's
+ * lists are built and rastered forward, the loss runs on the whole image, and
+ * each group's lists are rebuilt for its backward.  Monolithic raster only
+ * (steps that choose the chunked raster keep the legacy buffers); such steps
+ * run eagerly (no graph).  A tile with more intersections than `slots` is an
+ * error.  0 restores the legacy buffers. */
+int msplat_engine_set_isect_budget(MsplatEngine *e, long long slots);
 
 /* Launch configuration of the tunable stages (no counterpart in the
  * reference; the defaults are the reference's choices).  None changes the

@@ -106,6 +106,13 @@ int msplat_trainer_learned_stats(MsplatTrainer t, float *last_loss, int *rounds)
  * crossed.  Returns 0, or -1 on a bad handle or num_views outside 1..16. */
 int msplat_trainer_set_batch_views(MsplatTrainer t, int num_views, float lr_scale);
 
+/* Fixed intersection budget of the reference CLI (cli/msplat.mm:199-235):
+ * bytes_per_gaussian x the Gaussian cap of intersection buffers, allocated
+ * once (at least one slot per Gaussian of the cap); views that need more are
+ * rastered in tile groups (msplat_engine_set_isect_budget).  0 = the legacy
+ * buffers grown with the model.  Returns 0 or a negative code. */
+int msplat_trainer_set_isect_budget(MsplatTrainer t, float bytes_per_gaussian);
+
 /* Replaces the trainer's Gaussians with a trained PLY (Model::loadPly, the
  * CLI's --resume); optimizer state starts fresh.  Returns the iteration
  * recorded in the file, or a negative code. */

@@ -47,7 +47,8 @@ STAGES = ("project", "tiles", "raster_fwd", "loss", "raster_bwd", "project_bwd",
 class MsplatEngineStats(C.Structure):
     _fields_ = [("num_intersections", C.c_longlong), ("max_tile_count", C.c_int), ("k_max", C.c_int),
                 ("num_tiles", C.c_int), ("nan_counts", C.c_uint32 * 16), ("stage_ms", C.c_float * len(STAGES)),
-                ("timed_steps", C.c_longlong), ("launches", C.c_longlong), ("check_record", C.c_uint32 * 3)]
+                ("timed_steps", C.c_longlong), ("launches", C.c_longlong), ("check_record", C.c_uint32 * 3),
+                ("isect_groups", C.c_int)]
 
 
 class MsplatMcmcStats(C.Structure):
@@ -103,6 +104,7 @@ def lib(build_if_missing: bool = True):
                                                      C.POINTER(vp)]
         L.msplat_engine_backward.argtypes = [vp, C.POINTER(MsplatGaussians), C.POINTER(MsplatStepArgs), vp,
                                              C.POINTER(MsplatGradients)]
+        L.msplat_engine_set_isect_budget.argtypes = [vp, C.c_longlong]
         L.msplat_engine_set_tuning.argtypes = [vp, C.POINTER(MsplatTuning)]
         L.msplat_engine_get_tuning.argtypes = [vp, C.POINTER(MsplatTuning)]
         L.msplat_engine_autotune.argtypes = [vp, C.POINTER(MsplatGaussians), C.POINTER(MsplatStepArgs), C.c_int,

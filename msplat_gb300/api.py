@@ -50,6 +50,7 @@ def _lib():
     L.msplat_trainer_set_learned_relocation.argtypes = [vp, C.c_int]
     L.msplat_trainer_learned_stats.argtypes = [vp, fp, C.POINTER(C.c_int)]
     L.msplat_trainer_set_batch_views.argtypes = [vp, C.c_int, C.c_float]
+    L.msplat_trainer_set_isect_budget.argtypes = [vp, C.c_float]
     L.msplat_dataset_create_from_memory.argtypes = [C.c_int, fp, fp, C.POINTER(C.c_int), C.POINTER(vp),
                                                     C.POINTER(vp), C.c_int, fp, C.POINTER(C.c_uint8), C.c_bool,
                                                     C.c_int, C.c_bool]
@@ -283,6 +284,11 @@ class GaussianTrainer:
         learning rates times lr_scale (0: num_views ** 0.75); iterations count views."""
         if _lib().msplat_trainer_set_batch_views(self.h, int(num_views), float(lr_scale)) != 0:
             raise ValueError(f"invalid number of views per step: {num_views}")
+
+    def set_isect_budget(self, bytes_per_gaussian: float):
+        """Fixed intersection buffers (bytes per Gaussian of the cap; 0 = legacy), tile groups beyond."""
+        if _lib().msplat_trainer_set_isect_budget(self.h, float(bytes_per_gaussian)) != 0:
+            raise ValueError(f"invalid intersection budget: {bytes_per_gaussian}")
 
     def learned_stats(self) -> dict:
         loss = (C.c_float * 1)()

@@ -73,6 +73,9 @@ def parse(argv=None):
                    help="cameras per optimizer step (mean gradient; iterations count views; 1 = one camera per step)")
     p.add_argument("--batch-lr-scale", type=float, default=0.0,
                    help="learning-rate factor of multi-view steps (0 = batch views ** 0.75)")
+    p.add_argument("--isect-budget", type=float, default=0.0,
+                   help="fixed intersection buffers in bytes per Gaussian of --cap-max (the reference's "
+                        "MSPLAT_ISECT_BUDGET, e.g. 1000); larger views are rastered in tile groups; 0 = legacy")
     p.add_argument("--learned-relocation", action="store_true",
                    help="weight MCMC relocation sources by the online-trained proposal MLP")
     a = p.parse_args(argv)
@@ -104,6 +107,8 @@ def main(argv=None) -> int:
         trainer.set_batch_views(a.batch_views, a.batch_lr_scale)
     if a.learned_relocation:
         trainer.set_learned_relocation(True)
+    if a.isect_budget > 0:
+        trainer.set_isect_budget(a.isect_budget)
     if a.resume:
         step0 = trainer.load_ply(a.resume)
         print(f"Resumed from {a.resume} at step {step0}", flush=True)

@@ -1254,6 +1254,21 @@ int msplat_trainer_set_batch_views(MsplatTrainer t, int num_views, float lr_scal
     return 0;
 }
 
+int msplat_trainer_set_isect_budget(MsplatTrainer t, float bytes_per_gaussian) {
+    if (!t || !(bytes_per_gaussian >= 0.f)) return -1;
+    return guard("isect_budget", [&]() {
+        TrainerImpl *tr = TR(t);
+        long long slots = 0;
+        if (bytes_per_gaussian > 0.f) {
+            // 20 bytes per slot (key, sort scratch, id); at least one view's worth
+            // of one Gaussian per tile slot count, so that any single tile fits
+            const long long cap = std::max(1, tr->model.cap);
+            slots = std::max<long long>(cap, (long long)((double)bytes_per_gaussian * (double)cap / 20.0));
+        }
+        return msplat_engine_set_isect_budget(tr->eng, slots);
+    }, -2);
+}
+
 int msplat_trainer_learned_stats(MsplatTrainer t, float *last_loss, int *rounds) {
     if (!t) return -1;
     if (last_loss) *last_loss = TR(t)->lrn.last_loss;

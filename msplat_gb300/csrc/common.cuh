@@ -109,9 +109,12 @@ __device__ __forceinline__ void tile_rect(float cx, float cy, float ax, float ay
     y1 = min(max(0, __float2int_rz(__fadd_rn(__fadd_rn(tcy, try_), 1.0f))), tiles_y);
 }
 
-// Tile list bound clamped to the intersection buffer.
-__device__ __forceinline__ int clamp_off(uint32_t off, long long cap) {
-    return (int)((long long)off < cap ? (long long)off : cap);
+// Tile list bound as a slot of the intersection buffer, which holds the
+// global slots [lo, lo + cap) (lo = 0 unless a tile group is being rastered),
+// clamped to the buffer.
+__device__ __forceinline__ int clamp_off(uint32_t off, long long lo, long long cap) {
+    const long long r = (long long)off - lo;
+    return (int)(r < 0 ? 0 : (r < cap ? r : cap));
 }
 
 // Checked builds (-DMSPLAT_CHECKED): an index that fails its bound is

@@ -118,9 +118,13 @@ class Engine {
         const int T = vt.tile_base[B];
         const long long P = vt.pix_base[B];
         if (P > (1LL << 31) / 16) throw std::runtime_error("views too large for one step");
-        const long long cap = std::max<long long>(48LL * N * B, 1);   // msplat_metal.mm:1142 legacy capacity, per view
+        const long long legacy = std::max<long long>(48LL * N * B, 1);   // msplat_metal.mm:1142 legacy capacity, per view
         const MsplatTuning tune = tuning_;
-        const int K = choose_k(args[0], T, cap, tune);
+        const int K = choose_k(args[0], T, legacy, tune);
+        // fixed intersection budget (monolithic raster only, as in the
+        // reference): a view that does not fit is rastered in tile groups
+        const bool fixed = isect_slots_ > 0 && K == 1;
+        const long long cap = fixed ? isect_slots_ : legacy;
         const bool has_gt = gts != nullptr;
         ensure_points(N, B);
         ensure_tiles(T);
@@ -187,11 +191,36 @@ class Engine {
         ta.isect_ids = ptr<uint32_t>("isect_ids"); ta.nan_counts = pa.nan_counts;
         ta.cta_bins = cb ? ptr<uint32_t>("cta_bins") : nullptr;
         ta.tile_lists = ptr<uint32_t>("tile_lists"); ta.tile_class = ptr<uint32_t>("tile_class");
-        launches_ += launch_tiles(ta, num_sms_, stream_);
+        ta.tile_lo = 0; ta.tile_hi = T; ta.isect_lo = 0;
+        std::vector<TileGroup> groups;
+        if (!fixed) {
+            launches_ += launch_tiles(ta, num_sms_, stream_);
+        } else {
+            // the group boundaries need the tile counts on the host
+            launches_ += launch_tile_count(ta, stream_);
+            std::vector<uint32_t> counts((size_t)T);
+            CK(cudaMemcpyAsync(counts.data(), ta.tile_counts, sizeof(uint32_t) * (size_t)T, cudaMemcpyDeviceToHost,
+                               stream_));
+            CK(cudaStreamSynchronize(stream_));
+            groups = tile_groups(counts, cap);
+        }
+        last_groups_ = fixed ? (int)groups.size() : 1;
+        // (re)build the lists of one tile group; every build after the first
+        // re-zeroes the scatter's write counters and the sorts' work counters
+        int builds = 0;
+        auto build_group = [&](const TileGroup &gr) {
+            TileArgs tg = ta;
+            tg.tile_lo = gr.lo; tg.tile_hi = gr.hi; tg.isect_lo = gr.base;
+            if (builds++ > 0) {
+                CK(cudaMemsetAsync(ta.tile_write, 0, sizeof(uint32_t) * (size_t)T, stream_));
+                CK(cudaMemsetAsync(ta.tile_class + 4, 0, sizeof(uint32_t) * 4, stream_));
+            }
+            launches_ += launch_tile_build(tg, num_sms_, stream_);
+        };
         mark(2);
 
         RasterArgs ra{};
-        ra.vt = vt; ra.num_tiles = T; ra.k_max = K; ra.capacity = cap;
+        ra.vt = vt; ra.num_tiles = T; ra.k_max = K; ra.capacity = cap; ra.tile_lo = 0; ra.isect_lo = 0;
         ra.chunk = tune.chunk; ra.batch = tune.raster_batch;
         ra.sp = pa.sp; ra.tile_offsets = ta.tile_offsets; ra.isect_ids = ta.isect_ids;
         ra.n = (uint32_t)((long long)N * B); ra.rec = pa.rec;
@@ -201,7 +230,20 @@ class Engine {
             ra.prefix_T = ptr<float>("prefix_T"); ra.after_C = ptr<float>("after_C");
         }
         ra.v_img = ptr<float>("v_img"); ra.grad = ptr<GradRec>("grad"); ra.nan_counts = pa.nan_counts;
-        launch_raster_fwd(ra, stream_);
+        auto group_raster = [&](const TileGroup &gr) {
+            RasterArgs rg = ra;
+            rg.tile_lo = gr.lo; rg.num_tiles = gr.hi - gr.lo; rg.isect_lo = gr.base;
+            return rg;
+        };
+        if (!fixed) {
+            launch_raster_fwd(ra, stream_);
+        } else {
+            for (const TileGroup &gr : groups) {
+                build_group(gr);
+                launch_raster_fwd(group_raster(gr), stream_);
+            }
+            launches_ += (long long)groups.size() - 1;
+        }
         debug_sync(stream_, "raster_fwd");
         last_ra_ = ra;
         mark(3);
@@ -217,7 +259,17 @@ class Engine {
         mark(4);
         if (!backward) { mark(5); mark(6); mark(7); mark(8); return; }
 
-        launch_raster_bwd(ra, stream_);
+        if (!fixed) {
+            launch_raster_bwd(ra, stream_);
+        } else {
+            // one group: its lists are still in the buffer; several: each
+            // group's lists are rebuilt (the same sorted order) for its backward
+            for (const TileGroup &gr : groups) {
+                if (groups.size() > 1) build_group(gr);
+                launch_raster_bwd(group_raster(gr), stream_);
+            }
+            launches_ += (long long)groups.size() - 1;
+        }
         debug_sync(stream_, "raster_bwd");
         mark(5);
 
@@ -262,7 +314,7 @@ class Engine {
         // CUDA graph mode: the second step with the same shapes and buffers
         // is captured, later ones replay it (one launch for the whole step).
         // The targets and masks come through StepParams, not the key.
-        const bool graphable = use_graphs_ && !timing_ && !g_sync_check;
+        const bool graphable = use_graphs_ && !timing_ && !g_sync_check && !fixed;
         if (graphable) {
             std::string ks;
             auto put = [&](const void *p, size_t n) { ks.append(reinterpret_cast<const char *>(p), n); };
@@ -319,14 +371,18 @@ class Engine {
             (g.rest_bases > 0 && !out.v_features_rest))
             throw std::runtime_error("null gradient pointer");
         const bool graphs = use_graphs_;
-        use_graphs_ = false;   // the raster arguments of this forward are needed below
+        const long long slots = isect_slots_;
+        use_graphs_ = false;   // the raster arguments of this forward are needed below,
+        isect_slots_ = 0;      // for the whole view at once
         try {
             train_step(g, nullptr, args, nullptr, nullptr, false);
         } catch (...) {
             use_graphs_ = graphs;
+            isect_slots_ = slots;
             throw;
         }
         use_graphs_ = graphs;
+        isect_slots_ = slots;
         const int N = g.num_points;
         if (N <= 0) return;
         CK(cudaMemsetAsync(ptr<GradRec>("grad"), 0, sizeof(GradRec) * (size_t)N, stream_));
@@ -348,6 +404,12 @@ class Engine {
         debug_sync(stream_, "project_bwd");
         launches_ += (last_K_ > 1 ? 2 : 1) + 1;
         CK(cudaGetLastError());
+    }
+
+    void set_isect_budget(long long slots) {
+        if (slots < 0) throw std::runtime_error("negative intersection budget");
+        if (slots != isect_slots_) clear_graphs();
+        isect_slots_ = slots;
     }
 
     void set_tuning(const MsplatTuning &t) {
@@ -481,6 +543,7 @@ class Engine {
         }
         o.k_max = last_K_;
         o.num_tiles = last_T_;
+        o.isect_groups = last_groups_;
         if (has("nan_counts")) {
             unsigned tmp[32];
             CK(cudaMemcpy(tmp, ptr<unsigned>("nan_counts"), sizeof(tmp), cudaMemcpyDeviceToHost));
@@ -603,6 +666,34 @@ class Engine {
         cap_chunks_ = KP;
     }
 
+    // Consecutive tiles whose intersections fit `slots` (isect_tile_groups,
+    // msplat_metal.mm:693-718, with exact rather than padded bucket sizes).
+    struct TileGroup {
+        int lo, hi;
+        long long base;   // global slot of the group's first intersection
+    };
+    static std::vector<TileGroup> tile_groups(const std::vector<uint32_t> &counts, long long slots) {
+        std::vector<TileGroup> groups;
+        long long used = 0, base = 0;
+        int lo = 0;
+        for (int t = 0; t < (int)counts.size(); t++) {
+            const long long c = counts[t];
+            if (c == 0) continue;
+            if (c > slots)
+                throw std::runtime_error("tile " + std::to_string(t) + " has " + std::to_string(c) +
+                                         " intersections, more than the fixed budget's " + std::to_string(slots));
+            if (used + c > slots) {
+                groups.push_back({lo, t, base});
+                lo = t;
+                base += used;
+                used = 0;
+            }
+            used += c;
+        }
+        groups.push_back({lo, (int)counts.size(), base});
+        return groups;
+    }
+
     // K_max rule, msplat_metal.mm:1204-1224; a step in auto mode takes the
     // tuned mode, and the chunk length is the tuned one (the reference's 512
     // by default)
@@ -674,6 +765,8 @@ class Engine {
     RasterArgs last_ra_{};   // raster arguments of the last eagerly issued step
     float4 *gstats_ = nullptr;   // caller's activity statistics (learned relocation), or null
     MsplatTuning tuning_{512, 256, kChunk, 0};   // launch configuration of the tunable stages
+    long long isect_slots_ = 0;   // fixed intersection budget in slots (0: legacy 48 per Gaussian and view)
+    int last_groups_ = 1;         // tile groups of the last step
 
   public:
     void set_gstats(void *p) { gstats_ = static_cast<float4 *>(p); }
@@ -825,6 +918,10 @@ int msplat_engine_mcmc_scored(MsplatEngine *e, const MsplatGaussians *g, const M
                               float cull_radius, int *relocation_count, const float *score, MsplatMcmcStats *out) {
     if (!g || !st || !relocation_count || !out) return -1;
     return guarded(e, [&] { e->impl->mcmc(*g, *st, cap_max, cull_radius, *relocation_count, *out, score); });
+}
+
+int msplat_engine_set_isect_budget(MsplatEngine *e, long long slots) {
+    return guarded(e, [&] { e->impl->set_isect_budget(slots); });
 }
 
 int msplat_engine_set_tuning(MsplatEngine *e, const MsplatTuning *t) {

@@ -52,7 +52,12 @@ struct TileArgs {
     ViewTable vt;
     int num_tiles;          // over all views
     int sort_width;         // CTA width of the lightest shared-memory sort class: 256 or 512
-    long long capacity;     // intersection slots of keys / isect_ids
+    // tile group being built (fixed intersection budget): tiles [tile_lo,
+    // tile_hi) only, their intersections stored from global slot isect_lo on
+    // (the whole range and 0 when the view fits)
+    int tile_lo, tile_hi;
+    long long isect_lo;
+    long long capacity;     // intersection slots of keys / isect_ids (held from isect_lo on)
     const int *radii;
     const float *depths;
     const SplatRec *rec;
@@ -71,7 +76,9 @@ struct TileArgs {
 
 struct RasterArgs {
     ViewTable vt;
-    int num_tiles, k_max;       // tiles over all views; depth chunks (1 = monolithic)
+    int num_tiles, k_max;       // tiles of this launch; depth chunks (1 = monolithic)
+    int tile_lo;                // first global tile of this launch (tile group), 0 otherwise
+    long long isect_lo;         // global intersection slot held at isect_ids[0]
     int chunk;                  // splats per depth chunk (chunked raster)
     int batch;                  // splats staged per shared-memory round: 128 or 256
     long long capacity;
@@ -157,7 +164,12 @@ struct McmcResult {
 void debug_sync(cudaStream_t s, const char *what);
 
 void launch_project_fwd(const ProjectArgs &a, cudaStream_t s);
-int launch_tiles(const TileArgs &a, int num_sms, cudaStream_t s);   // returns the kernel launches
+// Tile mapping in two halves: counting + scans (all tiles), then the build
+// (scatter + per-tile sorts) of the tiles [tile_lo, tile_hi); launch_tiles
+// runs both.  Each returns its kernel launches.
+int launch_tile_count(const TileArgs &a, cudaStream_t s);
+int launch_tile_build(const TileArgs &a, int num_sms, cudaStream_t s);
+int launch_tiles(const TileArgs &a, int num_sms, cudaStream_t s);
 size_t sort_pack_smem_bytes();
 // cta_bins bytes for these views, 0 when the block-aggregated path is not used
 size_t tile_cta_bins_bytes(const ViewTable &vt);

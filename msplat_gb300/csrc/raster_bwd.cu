@@ -198,8 +198,8 @@ __device__ __forceinline__ void init_pixel(PixelState &ps, const RasterArgs &a, 
 template <bool kViews, int kBB>
 __global__ void __launch_bounds__(kTileThreads) k_raster_bwd(RasterArgs a) {
     __shared__ BwdSmem<kBB> sm;
-    const int tile = blockIdx.x;
-    const int s = clamp_off(a.tile_offsets[tile], a.capacity), e = clamp_off(a.tile_offsets[tile + 1], a.capacity);
+    const int tile = blockIdx.x + a.tile_lo;
+    const int s = clamp_off(a.tile_offsets[tile], a.isect_lo, a.capacity), e = clamp_off(a.tile_offsets[tile + 1], a.isect_lo, a.capacity);
     if (s >= e) return;
     const BwdPixel tp = bwd_pixel<kViews>(a, tile);
     PixelState ps;
@@ -237,8 +237,8 @@ __global__ void __launch_bounds__(256) k_chunk_prefix_suffix(RasterArgs a) {
 template <bool kViews, int kBB>
 __global__ void __launch_bounds__(kTileThreads) k_raster_bwd_chunked(RasterArgs a) {
     __shared__ BwdSmem<kBB> sm;
-    const int tile = blockIdx.x, k = blockIdx.y;
-    const int s0 = clamp_off(a.tile_offsets[tile], a.capacity), e0 = clamp_off(a.tile_offsets[tile + 1], a.capacity);
+    const int tile = blockIdx.x + a.tile_lo, k = blockIdx.y;
+    const int s0 = clamp_off(a.tile_offsets[tile], a.isect_lo, a.capacity), e0 = clamp_off(a.tile_offsets[tile + 1], a.isect_lo, a.capacity);
     const int cs = s0 + k * a.chunk, ce = min(s0 + (k + 1) * a.chunk, e0);
     if (cs >= ce) return;
     const BwdPixel tp = bwd_pixel<kViews>(a, tile);

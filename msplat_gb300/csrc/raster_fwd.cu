@@ -109,9 +109,9 @@ template <bool kViews> __device__ __forceinline__ TilePixel tile_pixel(const Ras
 template <bool kViews, int kBatch>
 __global__ void __launch_bounds__(kTileThreads) k_raster_fwd(RasterArgs a) {
     __shared__ BatchSmem<kBatch> sm;
-    const int tile = blockIdx.x;
+    const int tile = blockIdx.x + a.tile_lo;
     const TilePixel tp = tile_pixel<kViews>(a, tile);
-    int s = clamp_off(a.tile_offsets[tile], a.capacity), e = clamp_off(a.tile_offsets[tile + 1], a.capacity);
+    int s = clamp_off(a.tile_offsets[tile], a.isect_lo, a.capacity), e = clamp_off(a.tile_offsets[tile + 1], a.isect_lo, a.capacity);
     if (!MS_GUARD(s >= 0 && s <= e && e <= a.capacity, 5, tile, a.nan_counts ? a.nan_counts + kDbgSlot : nullptr)) e = s = 0;
     float T;
     float3 C;
@@ -131,9 +131,9 @@ __global__ void __launch_bounds__(kTileThreads) k_raster_fwd(RasterArgs a) {
 template <bool kViews, int kBatch>
 __global__ void __launch_bounds__(kTileThreads) k_raster_fwd_chunked(RasterArgs a) {
     __shared__ BatchSmem<kBatch> sm;
-    const int tile = blockIdx.x, k = blockIdx.y;
+    const int tile = blockIdx.x + a.tile_lo, k = blockIdx.y;
     const TilePixel tp = tile_pixel<kViews>(a, tile);
-    const int s0 = clamp_off(a.tile_offsets[tile], a.capacity), e0 = clamp_off(a.tile_offsets[tile + 1], a.capacity);
+    const int s0 = clamp_off(a.tile_offsets[tile], a.isect_lo, a.capacity), e0 = clamp_off(a.tile_offsets[tile + 1], a.isect_lo, a.capacity);
     const int cs = s0 + k * a.chunk, ce = min(s0 + (k + 1) * a.chunk, e0);
     const size_t P = (size_t)a.vt.pixels;
     const size_t o = (size_t)k * P + (size_t)tp.p();

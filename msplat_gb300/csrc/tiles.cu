@@ -111,7 +111,9 @@ __global__ void __launch_bounds__(1024) k_scan(TileArgs a) {
     }
 }
 
-template <bool kViews>
+// kGroup: a tile group of a fixed intersection budget is being built (tiles
+// outside [tile_lo, tile_hi) skipped, slots from isect_lo); false: all tiles
+template <bool kViews, bool kGroup>
 __global__ void __launch_bounds__(256) k_scatter(TileArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int view = kViews ? (int)blockIdx.y : 0;
@@ -127,8 +129,9 @@ __global__ void __launch_bounds__(256) k_scatter(TileArgs a) {
         for (int x = x0; x < x1; x++) {
             const int t = vg.tile_base + y * vg.tiles_x + x;
             if (!MS_GUARD(t >= 0 && t < a.num_tiles, 3, t, a.nan_counts ? a.nan_counts + kDbgSlot : nullptr)) continue;
+            if (kGroup && (t < a.tile_lo || t >= a.tile_hi)) continue;   // another tile group
             const uint32_t pos = atomicAdd(a.tile_write + t, 1u);
-            const uint64_t dst = (uint64_t)a.tile_offsets[t] + pos;
+            const uint64_t dst = (uint64_t)a.tile_offsets[t] + pos - (kGroup ? (uint64_t)a.isect_lo : 0ull);
             if (dst < (uint64_t)a.capacity) a.keys[dst] = key;   // overflow is dropped, never written
         }
 }
@@ -211,7 +214,7 @@ __global__ void __launch_bounds__(1024) k_cta_scan(TileArgs a, int ctas) {
     }
 }
 
-template <bool kViews>
+template <bool kViews, bool kGroup>
 __global__ void __launch_bounds__(kAggThreads) k_scatter_agg(TileArgs a) {
     extern __shared__ uint32_t bins[];
     const int view = kViews ? (int)blockIdx.y : 0;
@@ -230,7 +233,9 @@ __global__ void __launch_bounds__(kAggThreads) k_scatter_agg(TileArgs a) {
         const uint64_t key = ((uint64_t)__float_as_uint(a.depths[u]) << 32) | (uint32_t)u;
         for (int y = y0; y < y1; y++)
             for (int x = x0; x < x1; x++) {
-                const uint32_t dst = atomicAdd(&bins[y * vg.tiles_x + x], 1u);
+                const int lt = y * vg.tiles_x + x;
+                if (kGroup && (vg.tile_base + lt < a.tile_lo || vg.tile_base + lt >= a.tile_hi)) continue;
+                const uint64_t dst = (uint64_t)atomicAdd(&bins[lt], 1u) - (kGroup ? (uint64_t)a.isect_lo : 0ull);
                 if (dst < (uint64_t)a.capacity) a.keys[dst] = key;   // overflow is dropped, never written
             }
     }
@@ -396,8 +401,12 @@ __global__ void __launch_bounds__(THREADS) k_sort_pack_smem(TileArgs a, int cls)
     for (;;) {
         const int t = next_tile(a, cls, &sm.slot);   // barrier inside
         if (t < 0) break;
+        if (t < a.tile_lo || t >= a.tile_hi) {   // another tile group (t is CTA-uniform)
+            __syncthreads();                      // every thread has read the slot before it is reused
+            continue;
+        }
         const int count = (int)a.tile_counts[t];
-        const uint32_t start = a.tile_offsets[t];
+        const uint32_t start = a.tile_offsets[t] - (uint32_t)a.isect_lo;   // offsets and isect_lo are below 2^32
         if (!MS_GUARD(count <= PairSmem<THREADS>::kCap, 5, count, dbg) || emit_if_overflow<THREADS>(a, start, count)) {
             __syncthreads();
             continue;
@@ -553,8 +562,12 @@ __global__ void __launch_bounds__(kGlobThreads) k_sort_pack_global(TileArgs a, i
     for (;;) {
         const int t = next_tile(a, cls, &sm.slot);
         if (t < 0) break;
+        if (t < a.tile_lo || t >= a.tile_hi) {   // another tile group (t is CTA-uniform)
+            __syncthreads();                      // every thread has read the slot before it is reused
+            continue;
+        }
         const int count = (int)a.tile_counts[t];
-        const uint32_t start = a.tile_offsets[t];
+        const uint32_t start = a.tile_offsets[t] - (uint32_t)a.isect_lo;   // offsets and isect_lo are below 2^32
         if (emit_if_overflow<kGlobThreads>(a, start, count)) {
             __syncthreads();
             continue;
@@ -586,7 +599,7 @@ __global__ void __launch_bounds__(kGlobThreads) k_sort_pack_global(TileArgs a, i
 
 size_t sort_pack_smem_bytes() { return pair_smem_bytes<1024>(); }
 
-int launch_tiles(const TileArgs &a, int num_sms, cudaStream_t s) {
+static void tile_attrs() {
     static bool attr_set = false;
     if (!attr_set) {
         cudaFuncSetAttribute(k_sort_pack_smem<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -597,10 +610,16 @@ int launch_tiles(const TileArgs &a, int num_sms, cudaStream_t s) {
                              (int)pair_smem_bytes<1024>());
         cudaFuncSetAttribute(k_count_agg<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
         cudaFuncSetAttribute(k_count_agg<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
-        cudaFuncSetAttribute(k_scatter_agg<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
-        cudaFuncSetAttribute(k_scatter_agg<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
+        cudaFuncSetAttribute(k_scatter_agg<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
+        cudaFuncSetAttribute(k_scatter_agg<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
+        cudaFuncSetAttribute(k_scatter_agg<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
+        cudaFuncSetAttribute(k_scatter_agg<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
         attr_set = true;
     }
+}
+
+int launch_tile_count(const TileArgs &a, cudaStream_t s) {
+    tile_attrs();
     int launches = 0;
     const int n = a.vt.n, views = a.vt.count, maxT = max_view_tiles(a.vt);
     const bool agg = maxT <= kAggMaxTiles && a.cta_bins != nullptr;
@@ -624,13 +643,36 @@ int launch_tiles(const TileArgs &a, int num_sms, cudaStream_t s) {
     k_scan<<<1, 1024, 0, s>>>(a);
     debug_sync(s, "scan");
     launches += 1;
+    return launches;
+}
+
+int launch_tile_build(const TileArgs &a, int num_sms, cudaStream_t s) {
+    tile_attrs();
+    int launches = 0;
+    const int n = a.vt.n, views = a.vt.count, maxT = max_view_tiles(a.vt);
+    const bool agg = maxT <= kAggMaxTiles && a.cta_bins != nullptr;
+    const int agg_blocks = (n + kAggPerCta - 1) / kAggPerCta;
+    const size_t agg_smem = (size_t)maxT * sizeof(uint32_t);
+    const bool mv = views > 1;
+    const bool grp = a.tile_lo > 0 || a.tile_hi < a.num_tiles || a.isect_lo > 0;
     if (n > 0) {
+        const dim3 ga(agg_blocks, views), gs((n + 255) / 256, views);
         if (agg) {
-            if (mv) k_scatter_agg<true><<<dim3(agg_blocks, views), kAggThreads, agg_smem, s>>>(a);
-            else k_scatter_agg<false><<<agg_blocks, kAggThreads, agg_smem, s>>>(a);
+            if (grp) {
+                if (mv) k_scatter_agg<true, true><<<ga, kAggThreads, agg_smem, s>>>(a);
+                else k_scatter_agg<false, true><<<ga, kAggThreads, agg_smem, s>>>(a);
+            } else {
+                if (mv) k_scatter_agg<true, false><<<ga, kAggThreads, agg_smem, s>>>(a);
+                else k_scatter_agg<false, false><<<ga, kAggThreads, agg_smem, s>>>(a);
+            }
         } else {
-            if (mv) k_scatter<true><<<dim3((n + 255) / 256, views), 256, 0, s>>>(a);
-            else k_scatter<false><<<(n + 255) / 256, 256, 0, s>>>(a);
+            if (grp) {
+                if (mv) k_scatter<true, true><<<gs, 256, 0, s>>>(a);
+                else k_scatter<false, true><<<gs, 256, 0, s>>>(a);
+            } else {
+                if (mv) k_scatter<true, false><<<gs, 256, 0, s>>>(a);
+                else k_scatter<false, false><<<gs, 256, 0, s>>>(a);
+            }
         }
         debug_sync(s, "scatter");
         launches += 1;
@@ -648,6 +690,10 @@ int launch_tiles(const TileArgs &a, int num_sms, cudaStream_t s) {
     k_sort_pack_global<<<num_sms, kGlobThreads, 0, s>>>(a, 3);
     debug_sync(s, "sort_pack_global");
     return launches + 3;
+}
+
+int launch_tiles(const TileArgs &a, int num_sms, cudaStream_t s) {
+    return launch_tile_count(a, s) + launch_tile_build(a, num_sms, s);
 }
 
 }  // namespace msplat

@@ -213,6 +213,10 @@ class Engine:
         """Capture repeated steps into CUDA graphs and replay them."""
         self._check(self.L.msplat_engine_set_graphs(self.h, int(on)))
 
+    def set_isect_budget(self, slots: int):
+        """Fixed intersection buffers of `slots` slots (0: legacy); larger views in tile groups."""
+        self._check(self.L.msplat_engine_set_isect_budget(self.h, int(slots)))
+
     TUNING_FIELDS = ("sort_width", "raster_batch", "chunk", "raster_mode")
 
     def set_tuning(self, **kw):

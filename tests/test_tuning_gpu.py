@@ -108,3 +108,44 @@ def test_autotune(scene):
     with pytest.raises(RuntimeError):
         eng.set_tuning(sort_width=300)
     eng.close()
+
+
+@pytest.mark.parametrize("views", [1, 2])
+def test_isect_budget_tile_groups(scene, views):
+    """A fixed intersection budget smaller than the step's intersections: the
+    step runs in tile groups (lists built and rastered group by group, rebuilt
+    for the backward) and gives the legacy step's image bit for bit and its
+    gradients and update to rounding (float atomics)."""
+    sc, cams, gts, init = scene
+    ref = _step(init, cams, gts, {}, views)
+    M = int(ref["offs"][-1])
+    counts = np.diff(ref["offs"].astype(np.int64))
+    slots = max(int(counts.max()), M // 4)
+
+    eng = E.Engine(0)
+    eng.set_isect_budget(slots)
+    dg = E.DeviceGaussians(init)
+    cs = cams[:views]
+    args = [E.make_args(E.camera_dict(c), E.step_scalars(700, 700, width=c.width, height=c.height),
+                        raster_mode=1, do_sgld=True) for c in cs]
+    if views == 1:
+        eng.train_step(dg, args[0], gts[0].data_ptr())
+    else:
+        eng.train_step_batch(dg, args, [g.data_ptr() for g in gts[:views]])
+    eng.synchronize()
+    st = eng.stats()
+    assert st.isect_groups >= 4, st.isect_groups
+    assert st.num_intersections == M
+    P = sum(c.width * c.height for c in cs)
+    np.testing.assert_array_equal(eng.read("out_img", np.float32, 3 * P), ref["img"])
+    np.testing.assert_array_equal(eng.read("v_img", np.float32, 3 * P), ref["v_img"])
+    assert rel_l2(eng.read("grad", np.float32, 12 * views * init.n), ref["grad"]) <= 1e-5
+    p, _ = dg.to_numpy()
+    for k in E.GROUPS:
+        assert rel_l2(p[k], ref["p_" + k]) <= 1e-6, k
+    # a tile larger than the budget is refused (view 0's largest, stepped alone)
+    T0 = ((cs[0].width + 15) // 16) * ((cs[0].height + 15) // 16)
+    eng.set_isect_budget(int(counts[:T0].max()) - 1)
+    with pytest.raises(RuntimeError):
+        eng.train_step(dg, args[0], gts[0].data_ptr())
+    eng.close()
