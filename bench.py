@@ -250,11 +250,20 @@ def run_batched(eng, E, sc, dg, warmup, steps, step_base):
     eng.marker(1)
     ms = eng.marker_elapsed() / steps
     launches = (eng.stats().launches - l0) / steps
-    # per-stage times from eager steps with events between the stages
+    # per-stage times from eager steps with events between the stages (an
+    # NVTX range names them for profilers: ncu --nvtx --nvtx-include batched_steps/)
     eng.set_timing(True)
+    nvtx = getattr(torch.cuda, "nvtx", None)
+    if nvtx is not None:
+        try:
+            nvtx.range_push("batched_steps")
+        except Exception:   # a build without NVTX: no range
+            nvtx = None
     for k in range(5):
         one(warmup + steps + k)
     eng.synchronize()
+    if nvtx is not None:
+        nvtx.range_pop()
     st = eng.stats()
     eng.set_timing(False)
     stage_ms = {name: st.stage_ms[i] / max(1, st.timed_steps) for i, name in enumerate(E.N.STAGES)}
