@@ -236,6 +236,7 @@ def run_batched(eng, E, sc, dg, warmup, steps, step_base):
 
     # the launch configuration: tuned on this workload (CUDA events, whole
     # steps without updates), then the timed steps replay the tuned graph
+    eng.set_tuning(sort_width=512, raster_batch=256, chunk=512, raster_mode=0)   # the defaults
     untuned = eng.tuning()
     args0 = [E.make_args(cd, E.step_scalars(step_base, step_base, width=cd["width"], height=cd["height"]))
              for cd in cams]
@@ -335,6 +336,14 @@ def run_engine(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         return float(t.item())
 
+    # launch configuration: the autotuner times whole steps of this workload
+    # (no updates) over its candidates and keeps the fastest
+    tuned, tuned_ms = None, None
+    if not args.no_autotune:
+        cd0 = cams[0]
+        a0 = E.make_args(cd0, E.step_scalars(step_base, step_base, width=cd0["width"], height=cd0["height"]))
+        tuned, tuned_ms = eng.autotune(dg, [a0], [gts_dev[0].data_ptr()], reps=5)
+
     # the step runs as a captured CUDA graph: the first step of this shape
     # runs eagerly, the second is captured, later ones replay it
     eng.set_graphs(True)
@@ -411,7 +420,7 @@ def run_engine(args):
            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_dict(args),
            "roofline": roofline, "stage_ms": stage_ms, "num_intersections": int(st.num_intersections),
            "max_tile_count": int(st.max_tile_count), "gpu_launches": int(launches), "e2e": e2e,
-           "cuda_graph": True, "batched": batched,
+           "cuda_graph": True, "tuning": tuned, "autotune_step_ms": tuned_ms, "batched": batched,
            "clocks": clk.summary()}
     if rank == 0 and not args.no_time_to_psnr:
         # the metric's second half: learned vs plain relocation, time to PSNR
@@ -460,6 +469,7 @@ def main():
     ap.add_argument("--no-time-to-psnr", action="store_true",
                     help="skip the learned-vs-plain relocation time-to-PSNR runs")
     ap.add_argument("--no-batched", action="store_true", help="skip the multi-view (8 views per step) measurement")
+    ap.add_argument("--no-autotune", action="store_true", help="time the default launch configuration")
     ap.add_argument("--gaussians", type=int, default=N_MODEL,
                     help="trained Gaussians (default 1M; smaller only for profiling captures)")
     args = ap.parse_args()

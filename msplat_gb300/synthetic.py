@@ -181,3 +181,15 @@ def config_full(seed: int = 0, n: int = 1_000_000, ground: int = 200_000, n_trai
     train = ring_cameras(n_train, w, h, fx, seed=seed + 11, jitter=1.0)
     test = ring_cameras(n_test, w, h, fx, seed=seed + 13, jitter=1.0, phase=math.pi / max(n_test, 1))
     return Scene(gt, train, test)
+
+
+def config_heavy(seed: int = 0, n: int = 3_000_000, n_views: int = 40, ball_frac: float = 0.3,
+                 width: int = 4946, height: int = 3286) -> Scene:
+    """Heavy-tile stress: n GT Gaussians, ball_frac of them in a 0.1-radius ball
+    0.8 in front of the first ring camera (on the camera path), n_views ring
+    views at 4946x3286 with a 60-degree horizontal field of view."""
+    ball = int(ball_frac * n)
+    gt = gaussians(n - ball, seed, ball=ball, ball_center=(2.2, 0.0, 0.45), ball_radius=0.1)
+    fx = 0.5 * width / math.tan(0.5 * math.radians(60.0))
+    return Scene(gt, ring_cameras(n_views, width, height, fx), [])
+

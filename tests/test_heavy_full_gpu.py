@@ -1,0 +1,126 @@
+"""Heavy-tile stress at full size: 3,000,000 Gaussians, 30 % of them in a
+0.1-radius ball just in front of the camera, one 4946x3286 view (63,620
+tiles).  The oracle cannot run this size, so the checks are the
+size-independent ones (GPU only):
+
+- the per-tile lists of sampled tiles (the heaviest and random ones) equal a
+  numpy restatement built from the engine's own projection outputs: every
+  Gaussian whose tile rectangle (get_tile_bbox arithmetic in float32) covers
+  the tile, ordered by (depth bits, id) - bit-exact;
+- tile counts beyond the shared-memory sort classes occur (global sort used),
+  and the counts sum to the intersection total;
+- the view needs more intersections than the legacy 48 per Gaussian, so it
+  runs with a fixed intersection budget: one buffer holding all of them, and
+  tile groups under a third of that give the same image bits;
+- the step's loss and gradients are finite.
+"""
+import numpy as np
+import pytest
+
+from msplat_gb300 import engine as E
+from msplat_gb300 import synthetic as S
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def heavy():
+    torch = pytest.importorskip("torch")
+    sc = S.config_heavy(0, n_views=1)
+    cam = sc.train_cams[0]
+    eng = E.Engine(0)
+    dg = E.DeviceGaussians(sc.gt)
+    cd = E.camera_dict(cam)
+    eng.render(dg, E.make_args(cd, {"degrees_to_use": 3}, raster_mode=1))
+    eng.synchronize()
+    total = int(eng.stats().num_intersections)   # counted in full even where the legacy buffer is short
+    eng.set_isect_budget(total)                  # one buffer that holds every intersection
+    eng.render(dg, E.make_args(cd, {"degrees_to_use": 3}, raster_mode=1))
+    eng.synchronize()
+    n, W, H = sc.gt.n, cam.width, cam.height
+    tx, ty = (W + 15) // 16, (H + 15) // 16
+    o = {"n": n, "tx": tx, "ty": ty}
+    rec = eng.read("rec", np.float32, n * 12).reshape(n, 12)
+    o["cx"], o["cy"] = rec[:, 0].copy(), rec[:, 1].copy()
+    o["depth"] = eng.read("depths", np.float32, n)
+    o["radii"] = eng.read("radii", np.int32, n)
+    o["aabb"] = eng.read("aabb", np.float32, 2 * n).reshape(n, 2)
+    offs = eng.read("tile_offsets", np.uint32, tx * ty + 1).astype(np.int64)
+    o["offs"] = offs
+    o["ids"] = eng.read("isect_ids", np.uint32, int(offs[-1]))
+    o["stats"] = eng.stats()
+    o["total"] = total
+    img = eng.read("out_img", np.float32, W * H * 3)
+    o["gt"] = torch.from_numpy((np.clip(img, 0, 1) * 255 + 0.5).astype(np.uint8)).cuda()
+    eng.close()
+    return sc, cam, o
+
+
+def _tile_rects(o):
+    """get_tile_bbox (msplat_metal.metal:57-87) in float32, as tile_rect does."""
+    f = np.float32
+    tcx, tcy = o["cx"] / f(16), o["cy"] / f(16)
+    trx, try_ = o["aabb"][:, 0] / f(16), o["aabb"][:, 1] / f(16)
+
+    def conv(v, hi):
+        v = np.where(np.isfinite(v), v, 0)
+        return np.clip(np.trunc(np.clip(v, -2e9, 2e9)).astype(np.int64), 0, hi)
+    x0, x1 = conv(tcx - trx, o["tx"]), conv((tcx + trx) + f(1), o["tx"])
+    y0, y1 = conv(tcy - try_, o["ty"]), conv((tcy + try_) + f(1), o["ty"])
+    return x0, y0, x1, y1
+
+
+def test_heavy_tile_lists_full_size(heavy):
+    sc, cam, o = heavy
+    offs, ids = o["offs"], o["ids"]
+    counts = np.diff(offs)
+    assert counts.sum() == int(offs[-1]) == o["stats"].num_intersections == o["total"]
+    assert o["stats"].isect_groups == 1
+    assert o["total"] > 48 * o["n"]                      # beyond the legacy buffer: the budget is needed
+    assert counts.max() > 8192 and (counts > 2048).sum() > 100, (counts.max(), (counts > 2048).sum())
+    x0, y0, x1, y1 = _tile_rects(o)
+    active = (o["radii"] > 0) & np.isfinite(o["depth"]) & (o["depth"] > 0)
+    rng = np.random.default_rng(0)
+    nonempty = np.flatnonzero(counts)
+    sample = np.unique(np.concatenate([np.argsort(counts)[-8:], rng.choice(nonempty, 24, replace=False)]))
+    dbits = o["depth"].view(np.uint32).astype(np.uint64)
+    for t in sample:
+        tyy, txx = divmod(int(t), o["tx"])
+        g = np.flatnonzero(active & (x0 <= txx) & (txx < x1) & (y0 <= tyy) & (tyy < y1))
+        keys = (dbits[g] << np.uint64(32)) | g.astype(np.uint64)
+        ref = g[np.argsort(keys, kind="stable")]
+        got = ids[offs[t]:offs[t + 1]].astype(np.int64)
+        np.testing.assert_array_equal(got, ref, err_msg=f"tile {t} ({counts[t]} keys)")
+
+
+def test_heavy_step_groups_full_size(heavy):
+    sc, cam, o = heavy
+    init = S.init_from_gt(sc.gt, 3)
+    cd = E.camera_dict(cam)
+    args = E.make_args(cd, E.step_scalars(3001, 3001, width=cam.width, height=cam.height), raster_mode=1)
+
+    def step(slots):
+        eng = E.Engine(0)
+        eng.set_isect_budget(slots)
+        dg = E.DeviceGaussians(init)
+        eng.train_step(dg, args, o["gt"].data_ptr())
+        eng.synchronize()
+        img = eng.read("out_img", np.float32, cam.width * cam.height * 3)
+        st = eng.stats()
+        loss = eng.loss()
+        grad = eng.read("grad", np.float32, init.n * 12)
+        eng.close()
+        return img, st, loss, grad
+
+    # every intersection in one buffer (sized by a first step's count), then a third of it
+    probe = E.Engine(0)
+    probe.render(E.DeviceGaussians(init), args)
+    probe.synchronize()
+    total, biggest = int(probe.stats().num_intersections), int(probe.stats().max_tile_count)
+    probe.close()
+    img1, st1, loss1, grad1 = step(total)
+    assert st1.isect_groups == 1 and np.isfinite(loss1) and np.isfinite(grad1).all()
+    img2, st2, loss2, grad2 = step(max(biggest, total // 3))
+    assert st2.isect_groups >= 3, st2.isect_groups
+    np.testing.assert_array_equal(img2, img1)
+    assert abs(loss2 - loss1) <= 1e-6 * abs(loss1)
