@@ -20,7 +20,7 @@ namespace msplat {
 template <int kBB> struct BwdSmem {
     float4 xyo[kBB];    // x, y, opacity, id bits
     float4 con[kBB];
-    float4 rgb[kBB];    // raw colour
+    float4 rgb[kBB];    // clamped colour, w: bits of the channels with raw + 0.5 >= 0
     float acc[kBB][9];  // r g b | ca cb cc | x y | opacity
     int wmax[8];
 };
@@ -50,9 +50,14 @@ __device__ __forceinline__ float transpose_reduce8(float v[8], int lane) {
     return v[0];
 }
 
+// Per-pixel state of the back-to-front walk.  The reference keeps the colour
+// behind the splat per channel (buffer) and T_final * background; both only
+// enter dL/dalpha through their dot product with dL/dpixel, so the walk keeps
+// that one number: S = (buffer + T_final * background) . dL/dpixel, updated
+// by fac * (colour . dL/dpixel) per splat.
 struct PixelState {
-    float T, br, bg, bb;      // transmittance, colour behind (buffer)
-    float tfr, tfg, tfb;      // T_final * background
+    float T;                  // transmittance in front of the current splat
+    float S;                  // (colour behind + T_final * background) . dL/dpixel
     float vr, vg, vb;         // dL/dpixel
     float px, py;
     int bin_final;            // last splat index this pixel may take gradient from (-1: none)
@@ -61,7 +66,7 @@ struct PixelState {
 // Processes splat indices [s, hi] back to front for the whole CTA.
 template <int kBB>
 __device__ void backward_range(BwdSmem<kBB> &sm, const RasterArgs &a, int s, int hi, PixelState &ps, GradRec *grad) {
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int tid = threadIdx.x, lane = tid & 31;
     const int wbin = __reduce_max_sync(0xffffffffu, ps.bin_final);
     for (int batch_end = hi; batch_end >= s; batch_end -= kBB) {
         __syncthreads();
@@ -71,7 +76,11 @@ __device__ void backward_range(BwdSmem<kBB> &sm, const RasterArgs &a, int s, int
                 const SplatRec r = isect_record(a.isect_ids, a.rec, a.n, idx);
                 sm.xyo[tid] = r.a;
                 sm.con[tid] = r.b;
-                sm.rgb[tid] = r.c;
+                // clamped colour max(raw + 0.5, 0); w: channels whose raw + 0.5 >= 0
+                // (the only ones that pass a colour gradient back)
+                const float cr = r.c.x + 0.5f, cg = r.c.y + 0.5f, cb = r.c.z + 0.5f;
+                const int mask = (cr >= 0.f ? 1 : 0) | (cg >= 0.f ? 2 : 0) | (cb >= 0.f ? 4 : 0);
+                sm.rgb[tid] = make_float4(fmaxf(cr, 0.f), fmaxf(cg, 0.f), fmaxf(cb, 0.f), __int_as_float(mask));
             }
 #pragma unroll
             for (int k = 0; k < 9; k++) sm.acc[tid][k] = 0.f;
@@ -96,21 +105,18 @@ __device__ void backward_range(BwdSmem<kBB> &sm, const RasterArgs &a, int s, int
                 }
             }
             if (!__any_sync(0xffffffffu, valid)) continue;
+            // v[0..2] colour, v[3..5] conic, v[6..7] centre, v8 sum of dL/dsigma
+            // (the opacity-logit gradient is -(1 - opacity) times it, applied once)
             float v[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-            float vop = 0.f;
+            float v8 = 0.f;
             if (valid && alpha < 0.999f) {
                 const float4 rc = sm.rgb[t];
                 const float ra = 1.f / (1.f - alpha);
                 ps.T *= ra;
                 const float fac = alpha * ps.T;
-                const float cr = fmaxf(rc.x + 0.5f, 0.f), cg = fmaxf(rc.y + 0.5f, 0.f), cbl = fmaxf(rc.z + 0.5f, 0.f);
-                const float ar = __fmaf_rn(cr, ps.T, __fmaf_rn(-ps.br, ra, -ra * ps.tfr));
-                const float ag = __fmaf_rn(cg, ps.T, __fmaf_rn(-ps.bg, ra, -ra * ps.tfg));
-                const float ab = __fmaf_rn(cbl, ps.T, __fmaf_rn(-ps.bb, ra, -ra * ps.tfb));
-                const float v_alpha = ar * ps.vr + ag * ps.vg + ab * ps.vb;
-                ps.br = __fmaf_rn(cr, fac, ps.br);
-                ps.bg = __fmaf_rn(cg, fac, ps.bg);
-                ps.bb = __fmaf_rn(cbl, fac, ps.bb);
+                const float cv = __fmaf_rn(rc.x, ps.vr, __fmaf_rn(rc.y, ps.vg, rc.z * ps.vb));
+                const float v_alpha = __fmaf_rn(ps.T, cv, -ra * ps.S);
+                ps.S = __fmaf_rn(fac, cv, ps.S);
                 const float v_sigma = -alpha * v_alpha;
                 const float hv = 0.5f * v_sigma;
                 v[0] = fac * ps.vr;
@@ -121,26 +127,27 @@ __device__ void backward_range(BwdSmem<kBB> &sm, const RasterArgs &a, int s, int
                 v[5] = hv * (dy * dy);
                 v[6] = v_sigma * __fmaf_rn(cn.x, dx, cn.y * dy);
                 v[7] = v_sigma * __fmaf_rn(cn.y, dx, cn.z * dy);
-                vop = -v_sigma * (1.f - xo.z);
+                v8 = v_sigma;
             }
             const float s8 = transpose_reduce8(v, lane);
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) vop += __shfl_xor_sync(0xffffffffu, vop, o);
+            for (int o = 16; o > 0; o >>= 1) v8 += __shfl_xor_sync(0xffffffffu, v8, o);
             if ((lane & 3) == 0) atomicAdd(&sm.acc[t][lane >> 2], s8);
-            if (lane == 1) atomicAdd(&sm.acc[t][8], vop);
+            if (lane == 1) atomicAdd(&sm.acc[t][8], v8);
         }
         __syncthreads();
         if (tid < nb) {
             const float *g = sm.acc[tid];
-            const float4 rc = sm.rgb[tid];
-            const float gr = (rc.x + 0.5f >= 0.f) ? g[0] : 0.f;
-            const float gg = (rc.y + 0.5f >= 0.f) ? g[1] : 0.f;
-            const float gb = (rc.z + 0.5f >= 0.f) ? g[2] : 0.f;
+            const int mask = __float_as_int(sm.rgb[tid].w);
+            const float gr = (mask & 1) ? g[0] : 0.f;
+            const float gg = (mask & 2) ? g[1] : 0.f;
+            const float gb = (mask & 4) ? g[2] : 0.f;
+            const float gop = -(1.f - sm.xyo[tid].z) * g[8];
             const bool any = (gr != 0.f) | (gg != 0.f) | (gb != 0.f) | (g[3] != 0.f) | (g[4] != 0.f) |
-                             (g[5] != 0.f) | (g[6] != 0.f) | (g[7] != 0.f) | (g[8] != 0.f);
+                             (g[5] != 0.f) | (g[6] != 0.f) | (g[7] != 0.f) | (gop != 0.f);
             if (any) {
                 GradRec *dst = grad + __float_as_int(sm.xyo[tid].w);
-                atomic_add_f4(&dst->a, make_float4(g[6], g[7], g[8], 0.f));
+                atomic_add_f4(&dst->a, make_float4(g[6], g[7], gop, 0.f));
                 atomic_add_f4(&dst->b, make_float4(g[3], g[4], g[5], 0.f));
                 atomic_add_f4(&dst->c, make_float4(gr, gg, gb, 0.f));
             }
@@ -179,18 +186,17 @@ template <bool kViews> __device__ __forceinline__ BwdPixel bwd_pixel(const Raste
     return tp;
 }
 
-__device__ __forceinline__ void init_pixel(PixelState &ps, const RasterArgs &a, const BwdPixel &tp, float T0) {
+// S at the back of the walk: (colour behind + T_final * background) . dL/dpixel
+__device__ __forceinline__ void init_pixel(PixelState &ps, const RasterArgs &a, const BwdPixel &tp, float T0,
+                                           float behind_r, float behind_g, float behind_b) {
     const StepParams &sp = a.sp[tp.view];
     const long long p = tp.p;
     const float Tf = tp.inside ? a.final_T[p] : 0.f;
     ps.T = T0;
-    ps.br = ps.bg = ps.bb = 0.f;
-    ps.tfr = Tf * sp.bg[0];
-    ps.tfg = Tf * sp.bg[1];
-    ps.tfb = Tf * sp.bg[2];
     ps.vr = tp.inside ? a.v_img[3 * p] : 0.f;
     ps.vg = tp.inside ? a.v_img[3 * p + 1] : 0.f;
     ps.vb = tp.inside ? a.v_img[3 * p + 2] : 0.f;
+    ps.S = (behind_r + Tf * sp.bg[0]) * ps.vr + (behind_g + Tf * sp.bg[1]) * ps.vg + (behind_b + Tf * sp.bg[2]) * ps.vb;
     ps.px = (float)tp.x;
     ps.py = (float)tp.y;
 }
@@ -204,7 +210,7 @@ __global__ void __launch_bounds__(kTileThreads) k_raster_bwd(RasterArgs a) {
     const BwdPixel tp = bwd_pixel<kViews>(a, tile);
     PixelState ps;
     const float Tf = tp.inside ? a.final_T[tp.p] : 0.f;
-    init_pixel(ps, a, tp, Tf);
+    init_pixel(ps, a, tp, Tf, 0.f, 0.f, 0.f);
     ps.bin_final = tp.inside ? a.final_idx[tp.p] : -1;
     const int hi = min(e - 1, block_max(ps.bin_final, sm.wmax));
     if (hi < s) return;
@@ -245,12 +251,8 @@ __global__ void __launch_bounds__(kTileThreads) k_raster_bwd_chunked(RasterArgs 
     const size_t P = (size_t)a.vt.pixels;
     const size_t o = (size_t)k * P + (size_t)tp.p;
     PixelState ps;
-    init_pixel(ps, a, tp, tp.inside ? a.prefix_T[o] * a.chunk_T[o] : 0.f);
-    if (tp.inside) {
-        ps.br = a.after_C[3 * o];
-        ps.bg = a.after_C[3 * o + 1];
-        ps.bb = a.after_C[3 * o + 2];
-    }
+    init_pixel(ps, a, tp, tp.inside ? a.prefix_T[o] * a.chunk_T[o] : 0.f, tp.inside ? a.after_C[3 * o] : 0.f,
+               tp.inside ? a.after_C[3 * o + 1] : 0.f, tp.inside ? a.after_C[3 * o + 2] : 0.f);
     const int bf = tp.inside ? a.chunk_idx[o] : -1;
     ps.bin_final = (bf >= cs) ? bf : -1;
     const int hi = min(ce - 1, block_max(ps.bin_final, sm.wmax));
