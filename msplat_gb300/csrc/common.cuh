@@ -97,6 +97,25 @@ __device__ __forceinline__ float det_expf(float x) {
     return __fmul_rn(__fmul_rn(p, two_n), scale_lo);
 }
 
+// det_expf for x in [-87, 0] (the rasterizers' -sigma, sigma in [0, 5.55)):
+// the same operations without the NaN, overflow and subnormal branches, which
+// cannot trigger there, so the same bits.
+__device__ __forceinline__ float det_expf_neg(float x) {
+    const float n = rintf(__fmul_rn(x, 1.44269504088896341f));
+    float r = __fmaf_rn(n, -0.693145751953125f, x);
+    r = __fmaf_rn(n, -1.42860676533018e-06f, r);
+    float p = 1.0f / 5040.0f;
+    p = __fmaf_rn(p, r, 1.0f / 720.0f);
+    p = __fmaf_rn(p, r, 1.0f / 120.0f);
+    p = __fmaf_rn(p, r, 1.0f / 24.0f);
+    p = __fmaf_rn(p, r, 1.0f / 6.0f);
+    p = __fmaf_rn(p, r, 0.5f);
+    p = __fmaf_rn(p, r, 1.0f);
+    p = __fmaf_rn(p, r, 1.0f);
+    const float two_n = __uint_as_float((uint32_t)((int)n + 127) << 23);
+    return __fmul_rn(p, two_n);
+}
+
 // Tile rectangle of a splat, inclusive min / exclusive max (get_tile_bbox,
 // msplat_metal.metal:57-87).  Truncating, saturating float->int conversion.
 __device__ __forceinline__ void tile_rect(float cx, float cy, float ax, float ay, int tiles_x, int tiles_y,

@@ -94,19 +94,25 @@ __device__ void backward_range(BwdSmem<kBB> &sm, const RasterArgs &a, int s, int
             bool valid = sidx <= ps.bin_final;
             float dx = 0.f, dy = 0.f, alpha = 0.f;
             if (valid) {
-                dx = xo.x - ps.px;
-                dy = xo.y - ps.py;
-                const float sigma = __fmaf_rn(0.5f, __fmaf_rn(cn.x, dx * dx, cn.z * dy * dy), cn.y * dx * dy);
+                // sigma and alpha exactly as the forward pass rounds them (no
+                // contraction), so both passes take the same splats
+                dx = __fsub_rn(xo.x, ps.px);
+                dy = __fsub_rn(xo.y, ps.py);
+                const float sigma = __fmaf_rn(0.5f, __fmaf_rn(cn.x, __fmul_rn(dx, dx), __fmul_rn(__fmul_rn(cn.z, dy), dy)),
+                                              __fmul_rn(__fmul_rn(cn.y, dx), dy));
                 if (!finite_bits(sigma) || sigma < 0.f || sigma >= 5.55f) {
                     valid = false;
                 } else {
-                    alpha = fminf(0.999f, xo.z * det_expf(-sigma));
+                    alpha = fminf(0.999f, __fmul_rn(xo.z, det_expf_neg(-sigma)));
                     if (alpha < 1.f / 255.f) valid = false;
                 }
             }
             if (!__any_sync(0xffffffffu, valid)) continue;
-            // v[0..2] colour, v[3..5] conic, v[6..7] centre, v8 sum of dL/dsigma
-            // (the opacity-logit gradient is -(1 - opacity) times it, applied once)
+            // per lane, with A = dL/dsigma dx and B = dL/dsigma dy: v[0..2] the
+            // colour gradient, v[3..5] = (A dx, A dy, B dy) (half the conic
+            // gradient), v[6..7] = (A, B), v8 = dL/dsigma.  The splat's constants
+            // are applied once to the sums: conic x 0.5, centre = conic-weighted
+            // (A, B), opacity logit -(1 - opacity) x sum(dL/dsigma)
             float v[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             float v8 = 0.f;
             if (valid && alpha < 0.999f) {
@@ -118,15 +124,15 @@ __device__ void backward_range(BwdSmem<kBB> &sm, const RasterArgs &a, int s, int
                 const float v_alpha = __fmaf_rn(ps.T, cv, -ra * ps.S);
                 ps.S = __fmaf_rn(fac, cv, ps.S);
                 const float v_sigma = -alpha * v_alpha;
-                const float hv = 0.5f * v_sigma;
+                const float A = v_sigma * dx, B = v_sigma * dy;
                 v[0] = fac * ps.vr;
                 v[1] = fac * ps.vg;
                 v[2] = fac * ps.vb;
-                v[3] = hv * (dx * dx);
-                v[4] = hv * (dx * dy);
-                v[5] = hv * (dy * dy);
-                v[6] = v_sigma * __fmaf_rn(cn.x, dx, cn.y * dy);
-                v[7] = v_sigma * __fmaf_rn(cn.y, dx, cn.z * dy);
+                v[3] = A * dx;
+                v[4] = A * dy;
+                v[5] = B * dy;
+                v[6] = A;
+                v[7] = B;
                 v8 = v_sigma;
             }
             const float s8 = transpose_reduce8(v, lane);
@@ -142,13 +148,16 @@ __device__ void backward_range(BwdSmem<kBB> &sm, const RasterArgs &a, int s, int
             const float gr = (mask & 1) ? g[0] : 0.f;
             const float gg = (mask & 2) ? g[1] : 0.f;
             const float gb = (mask & 4) ? g[2] : 0.f;
+            const float4 cn = sm.con[tid];
             const float gop = -(1.f - sm.xyo[tid].z) * g[8];
-            const bool any = (gr != 0.f) | (gg != 0.f) | (gb != 0.f) | (g[3] != 0.f) | (g[4] != 0.f) |
-                             (g[5] != 0.f) | (g[6] != 0.f) | (g[7] != 0.f) | (gop != 0.f);
+            const float gx = __fmaf_rn(cn.x, g[6], cn.y * g[7]), gy = __fmaf_rn(cn.y, g[6], cn.z * g[7]);
+            const float ca = 0.5f * g[3], cb = 0.5f * g[4], cc = 0.5f * g[5];
+            const bool any = (gr != 0.f) | (gg != 0.f) | (gb != 0.f) | (ca != 0.f) | (cb != 0.f) | (cc != 0.f) |
+                             (gx != 0.f) | (gy != 0.f) | (gop != 0.f);
             if (any) {
                 GradRec *dst = grad + __float_as_int(sm.xyo[tid].w);
-                atomic_add_f4(&dst->a, make_float4(g[6], g[7], gop, 0.f));
-                atomic_add_f4(&dst->b, make_float4(g[3], g[4], g[5], 0.f));
+                atomic_add_f4(&dst->a, make_float4(gx, gy, gop, 0.f));
+                atomic_add_f4(&dst->b, make_float4(ca, cb, cc, 0.f));
                 atomic_add_f4(&dst->c, make_float4(gr, gg, gb, 0.f));
             }
         }

@@ -60,7 +60,7 @@ __device__ __forceinline__ void composite_range(BatchSmem<kBatch> &sm, const Ras
                 continue;
             }
             if (sigma < 0.f || sigma >= 5.55f) continue;
-            const float alpha = fminf(0.999f, xo.z * det_expf(-sigma));
+            const float alpha = fminf(0.999f, xo.z * det_expf_neg(-sigma));
             if (alpha < 1.f / 255.f) continue;
             const float nT = T * (1.f - alpha);
             if (nT <= 1e-4f) {
