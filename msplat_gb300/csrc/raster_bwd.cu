@@ -100,7 +100,7 @@ __device__ void backward_range(BwdSmem<kBB> &sm, const RasterArgs &a, int s, int
                 dy = __fsub_rn(xo.y, ps.py);
                 const float sigma = __fmaf_rn(0.5f, __fmaf_rn(cn.x, __fmul_rn(dx, dx), __fmul_rn(__fmul_rn(cn.z, dy), dy)),
                                               __fmul_rn(__fmul_rn(cn.y, dx), dy));
-                if (!finite_bits(sigma) || sigma < 0.f || sigma >= 5.55f) {
+                if (!(sigma >= 0.f && sigma < 5.55f)) {   // NaN fails too
                     valid = false;
                 } else {
                     alpha = fminf(0.999f, __fmul_rn(xo.z, det_expf_neg(-sigma)));

@@ -55,11 +55,10 @@ __device__ __forceinline__ void composite_range(BatchSmem<kBatch> &sm, const Ras
             const float4 cn = sm.con[t];
             const float dx = xo.x - px, dy = xo.y - py;
             const float sigma = __fmaf_rn(0.5f, __fmaf_rn(cn.x, dx * dx, cn.z * dy * dy), cn.y * dx * dy);
-            if (!finite_bits(sigma)) {
-                if (nan_sigma) atomicAdd(nan_sigma, 1u);
+            if (!(sigma >= 0.f && sigma < 5.55f)) {   // NaN fails too
+                if (nan_sigma && !finite_bits(sigma)) atomicAdd(nan_sigma, 1u);
                 continue;
             }
-            if (sigma < 0.f || sigma >= 5.55f) continue;
             const float alpha = fminf(0.999f, xo.z * det_expf_neg(-sigma));
             if (alpha < 1.f / 255.f) continue;
             const float nT = T * (1.f - alpha);
