@@ -97,6 +97,14 @@ __device__ __forceinline__ float det_expf(float x) {
     return __fmul_rn(__fmul_rn(p, two_n), scale_lo);
 }
 
+// Adam's parameter step st * m / (sqrt(v) / bc + eps) (fused_adam_kernel,
+// msplat_metal.metal:1680-1713), both divisions by the fast reciprocal
+// (within 2 ulp, as the reference's fast-math division): the IEEE divisions
+// were most of the optimizer kernels' instructions.
+__device__ __forceinline__ float adam_delta(float st, float m, float v, float bc, float eps) {
+    return __fdividef(st * m, __fdividef(sqrtf(v), bc) + eps);
+}
+
 // det_expf for x in [-87, 0] (the rasterizers' -sigma, sigma in [0, 5.55)):
 // the same operations without the NaN, overflow and subnormal branches, which
 // cannot trigger there, so the same bits.

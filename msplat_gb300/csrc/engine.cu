@@ -164,7 +164,10 @@ class Engine {
         // Adam, SGLD
         launches_ += 1 + (K > 1 ? 2 : 1);
         if (has_gt) launches_ += 3;
-        if (has_gt && backward) launches_ += (K > 1 ? 2 : 1) + 1 + (opt ? 1 : 0) + (a0.do_sgld ? 1 : 0);
+        // (the one-view projection backward is two launches with the optimizer:
+        // the VJP, then the SH Adam walk)
+        if (has_gt && backward)
+            launches_ += (K > 1 ? 2 : 1) + 1 + (opt && B == 1 ? 1 : 0) + (opt ? 1 : 0) + (a0.do_sgld ? 1 : 0);
         CK(cudaMemsetAsync(ptr<uint32_t>("tile_counts"), 0, sizeof(uint32_t) * 2 * (size_t)T, stream_));
         CK(cudaMemsetAsync(ptr<float>("loss_sum"), 0, sizeof(float) * B, stream_));
 
@@ -280,6 +283,7 @@ class Engine {
         pb.grad = ra.grad;
         pb.v_mean = ptr<float>("v_mean"); pb.v_scale = ptr<float>("v_scale"); pb.v_quat = ptr<float>("v_quat");
         pb.v_opac = B > 1 ? ptr<float>("v_opac") : nullptr;
+        pb.sh_in = ptr<float4>("sh_in");
         pb.features_dc = g.features_dc; pb.features_rest = g.features_rest;
         if (st) {
             pb.dc_m = st->exp_avg[3]; pb.dc_v = st->exp_avg_sq[3];
@@ -399,10 +403,11 @@ class Engine {
         pb.v_mean = out.v_means; pb.v_scale = out.v_scales; pb.v_quat = out.v_quats;
         pb.features_dc = g.features_dc; pb.features_rest = g.features_rest;
         pb.v_dc_out = out.v_features_dc; pb.v_rest_out = out.v_features_rest; pb.v_opac_out = out.v_opacities;
+        pb.sh_in = ptr<float4>("sh_in");
         pb.nan_counts = ptr<unsigned>("nan_counts");
         launch_project_bwd(pb, stream_);
         debug_sync(stream_, "project_bwd");
-        launches_ += (last_K_ > 1 ? 2 : 1) + 1;
+        launches_ += (last_K_ > 1 ? 2 : 1) + 2;
         CK(cudaGetLastError());
     }
 
@@ -628,6 +633,7 @@ class Engine {
             alloc("v_scale", m * 12);
             alloc("v_quat", m * 16);
             alloc("v_opac", m * 4);
+            alloc("sh_in", m * 16);
             cap_points_ = n;
         }
     }

@@ -119,6 +119,7 @@ struct ProjectBwdArgs {
     const GradRec *grad;    // [views, n]
     float *v_mean, *v_scale, *v_quat;   // [n]: summed over the views
     float *v_opac;          // [n] summed opacity-logit gradient (several views; Adam reads it)
+    float4 *sh_in;          // [n] one view: colour gradient and whether it feeds the SH walk (scratch)
     float *features_dc, *features_rest, *dc_m, *dc_v, *rest_m, *rest_v;
     // gradient export (one view, no optimizer): when set, the SH gradients
     // and the opacity-logit gradient are written here instead of feeding Adam

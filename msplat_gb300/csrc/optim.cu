@@ -35,7 +35,7 @@ __device__ __forceinline__ bool adam_step(float &p, float &m, float &v, float g,
     if (!finite_bits(g)) return false;
     const float mm = fmaf(b1, m, (1.0f - b1) * g);
     const float vv = fmaf(b2, v, (1.0f - b2) * g * g);
-    p = p - st * mm / (sqrtf(vv) / bc + eps);
+    p = p - adam_delta(st, mm, vv, bc, eps);
     m = mm;
     v = vv;
     return true;

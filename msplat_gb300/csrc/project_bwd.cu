@@ -25,7 +25,7 @@ __device__ __forceinline__ void adam_el(float *p, float *m, float *v, float g, f
                                         float b2, float eps) {
     const float mm = fmaf(b1, *m, (1.0f - b1) * g);
     const float vv = fmaf(b2, *v, (1.0f - b2) * g * g);
-    *p -= step * mm / (sqrtf(vv) / bc2s + eps);
+    *p -= adam_delta(step, mm, vv, bc2s, eps);
     *m = mm;
     *v = vv;
 }
@@ -38,30 +38,26 @@ __device__ __forceinline__ void adam4(float4 &p, float4 &m, float4 &v, const flo
         if (!(active & (1u << k))) continue;
         const float nm = fmaf(b1, mm[k], (1.0f - b1) * g[k]);
         const float nv = fmaf(b2, vv[k], (1.0f - b2) * g[k] * g[k]);
-        pp[k] -= st * nm / (sqrtf(nv) / bc + eps);
+        pp[k] -= adam_delta(st, nm, nv, bc, eps);
         mm[k] = nm;
         vv[k] = nv;
     }
 }
 
 
-// Per-warp staging of the SH Adam inputs, one view: the basis values of the
-// warp's 32 Gaussians and their colour gradients (w = number of rest bands
-// to update + 1, 0 when the Gaussian is culled or its colour gradient is
-// non-finite).
-struct ShStage {
-    float bas[32][16];
-    float4 vc[32];
+// Per-warp staging of the SH gradients: the warp's 32 Gaussians' rows of
+// dL/d(features_rest) and dL/d(features_dc), laid out exactly like their rows
+// in global memory (so the walk reads the gradient of element e at offset e),
+// kInactive in the slots of elements Adam leaves alone (culled Gaussian,
+// non-finite colour gradient, band not in use).  The row stride of 45 floats
+// keeps the 32 lanes writing their own rows on distinct banks.
+constexpr uint32_t kInactive = 0xffffffffu;
+struct ShFlat {
+    float rest[32 * 45];
+    float dc[32 * 3];
 };
 
-// Several views: the summed SH coefficient gradients of the warp's 32
-// Gaussians (rest bands 0..14 x 3 channels, then DC x 3; row padded to 49
-// floats so that lanes walking their own rows do not share banks) and w.
-constexpr int kAccRow = 49;
-struct ShAccStage {
-    float g[32][kAccRow];
-    int w[32];
-};
+__device__ __forceinline__ bool active_slot(float g) { return __float_as_uint(g) != kInactive; }
 
 // View-independent state of one Gaussian: mean, scales, normalised
 // quaternion, rotation, M = R S and the 3D covariance V = M M^T.
@@ -232,27 +228,21 @@ __device__ __forceinline__ int bands_in_use(const StepParams &sp, int rest_bases
 
 // Fused SH Adam (or the gradient export), warp-cooperative: the warp's 32
 // Gaussians own contiguous rows of features_dc / features_rest and their
-// moments, walked with coalesced 16-byte accesses (the element's Gaussian,
-// band and channel are recovered from its offset in the rows).
-// dc(gi, c, g) / rest(gi, band, c, g) -> true with g set when the element
-// is updated.
-template <int kRowF, class DcFn, class RestFn>
-__device__ __forceinline__ void sh_update(const ProjectBwdArgs &a, const StepParams &sp, int i0, int ng, int lane,
-                                          DcFn dc, RestFn rest) {
+// moments, walked with coalesced 16-byte accesses; the gradient of element e
+// is slot e of the staged rows.
+template <int kRowF>
+__device__ __forceinline__ void sh_update(const ProjectBwdArgs &a, const StepParams &sp, const ShFlat &st, int i0,
+                                          int ng, int lane) {
+    const int rowf = kRowF > 0 ? kRowF : 3 * a.rest_bases;
     if (a.v_dc_out) {
-        // export: zero where Adam would not update (culled, non-finite, band not in use)
+        // export: zero where Adam would not update
         for (int e = lane; e < 3 * ng; e += 32) {
-            const int gi = e / 3, c = e - 3 * gi;
-            float g = 0.f;
-            if (!dc(gi, c, g)) g = 0.f;
-            a.v_dc_out[3 * (size_t)i0 + e] = g;
+            const float g = st.dc[e];
+            a.v_dc_out[3 * (size_t)i0 + e] = active_slot(g) ? g : 0.f;
         }
-        const int rowf = 3 * a.rest_bases;
         for (int e = lane; e < rowf * ng; e += 32) {
-            const int gi = e / rowf, r = e - rowf * gi, band = r / 3, c = r - 3 * band;
-            float g = 0.f;
-            if (!rest(gi, band, c, g)) g = 0.f;
-            a.v_rest_out[(size_t)rowf * i0 + e] = g;
+            const float g = st.rest[e];
+            a.v_rest_out[(size_t)rowf * i0 + e] = active_slot(g) ? g : 0.f;
         }
         return;
     }
@@ -260,42 +250,38 @@ __device__ __forceinline__ void sh_update(const ProjectBwdArgs &a, const StepPar
     {   // features_dc: 3 floats per Gaussian
         const int total = 3 * ng;
         float *p = a.features_dc + 3 * (size_t)i0, *mm = a.dc_m + 3 * (size_t)i0, *vv = a.dc_v + 3 * (size_t)i0;
-        const float st = sp.step_size[3], bc = sp.bc2_sqrt[3];
+        const float stp = sp.step_size[3], bc = sp.bc2_sqrt[3];
         for (int e0 = lane * 4; e0 < total; e0 += 128) {
             float g[4];
             unsigned act = 0;
 #pragma unroll
             for (int k = 0; k < 4; k++) {
-                const int e = e0 + k;
-                g[k] = 0.f;
-                if (e < total) {
-                    const int gi = e / 3, c = e - 3 * gi;
-                    if (dc(gi, c, g[k])) act |= 1u << k;
-                }
+                g[k] = e0 + k < total ? st.dc[e0 + k] : __uint_as_float(kInactive);
+                if (active_slot(g[k])) act |= 1u << k;
             }
             if (!act) continue;
             if (e0 + 4 <= total) {
                 float4 P = *reinterpret_cast<float4 *>(p + e0), Mv = *reinterpret_cast<float4 *>(mm + e0),
                        Vv = *reinterpret_cast<float4 *>(vv + e0);
-                adam4(P, Mv, Vv, g, act, st, bc, b1, b2, eps);
+                adam4(P, Mv, Vv, g, act, stp, bc, b1, b2, eps);
                 *reinterpret_cast<float4 *>(p + e0) = P;
                 *reinterpret_cast<float4 *>(mm + e0) = Mv;
                 *reinterpret_cast<float4 *>(vv + e0) = Vv;
             } else {
                 for (int k = 0; k < 4 && e0 + k < total; k++)
-                    if (act & (1u << k)) adam_el(p + e0 + k, mm + e0 + k, vv + e0 + k, g[k], st, bc, b1, b2, eps);
+                    if (act & (1u << k)) adam_el(p + e0 + k, mm + e0 + k, vv + e0 + k, g[k], stp, bc, b1, b2, eps);
             }
         }
     }
     if (a.rest_bases == 0) return;
-    {   // features_rest: 3 * rest_bases floats per Gaussian; kRestUnroll
-        // 16-byte steps per lane are loaded before any is updated, so a warp
-        // keeps 3 * kRestUnroll loads in flight
+    {   // features_rest: rowf floats per Gaussian; kRestUnroll 16-byte steps
+        // per lane are loaded before any is updated, so a warp keeps
+        // 3 * kRestUnroll loads in flight
         constexpr int kRestUnroll = 3;
-        const int rowf = kRowF > 0 ? kRowF : 3 * a.rest_bases, total = rowf * ng;
+        const int total = rowf * ng;
         float *p = a.features_rest + (size_t)rowf * i0, *mm = a.rest_m + (size_t)rowf * i0,
               *vv = a.rest_v + (size_t)rowf * i0;
-        const float st = sp.step_size[4], bc = sp.bc2_sqrt[4];
+        const float stp = sp.step_size[4], bc = sp.bc2_sqrt[4];
         for (int base = lane * 4; base < total; base += 128 * kRestUnroll) {
             float4 P[kRestUnroll], Mv[kRestUnroll], Vv[kRestUnroll];
 #pragma unroll
@@ -313,29 +299,60 @@ __device__ __forceinline__ void sh_update(const ProjectBwdArgs &a, const StepPar
                 if (e0 >= total) break;
                 float g[4];
                 unsigned act = 0;
-                int gi = e0 / rowf, r = e0 - rowf * gi;
+                if (e0 + 4 <= total) {
+                    const float4 g4 = *reinterpret_cast<const float4 *>(st.rest + e0);
+                    g[0] = g4.x; g[1] = g4.y; g[2] = g4.z; g[3] = g4.w;
+                } else {
 #pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    g[k] = 0.f;
-                    if (e0 + k < total) {
-                        const int band = r / 3, c = r - 3 * band;
-                        if (rest(gi, band, c, g[k])) act |= 1u << k;
-                    }
-                    if (++r == rowf) { r = 0; gi++; }
+                    for (int k = 0; k < 4; k++) g[k] = e0 + k < total ? st.rest[e0 + k] : __uint_as_float(kInactive);
                 }
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    if (active_slot(g[k])) act |= 1u << k;
                 if (!act) continue;
                 if (e0 + 4 <= total) {
-                    adam4(P[u], Mv[u], Vv[u], g, act, st, bc, b1, b2, eps);
+                    adam4(P[u], Mv[u], Vv[u], g, act, stp, bc, b1, b2, eps);
                     *reinterpret_cast<float4 *>(p + e0) = P[u];
                     *reinterpret_cast<float4 *>(mm + e0) = Mv[u];
                     *reinterpret_cast<float4 *>(vv + e0) = Vv[u];
                 } else {
                     for (int k = 0; k < 4 && e0 + k < total; k++)
-                        if (act & (1u << k)) adam_el(p + e0 + k, mm + e0 + k, vv + e0 + k, g[k], st, bc, b1, b2, eps);
+                        if (act & (1u << k)) adam_el(p + e0 + k, mm + e0 + k, vv + e0 + k, g[k], stp, bc, b1, b2, eps);
                 }
             }
         }
     }
+}
+
+// Stage one Gaussian's SH gradient rows (this lane's): dc[c] = C0 * vc_c,
+// rest[3 band + c] = basis_band * vc_c for bands below nb, the other rest
+// slots inactive.
+template <int kRowF>
+__device__ __forceinline__ void stage_sh_row(ShFlat &st, int lane, int rest_bases, int nb, const float b[16],
+                                             float vc0, float vc1, float vc2) {
+    const int rowf = kRowF > 0 ? kRowF : 3 * rest_bases;
+    float *gd = st.dc + 3 * lane, *gr = st.rest + rowf * lane;
+    const float off = __uint_as_float(kInactive);
+    gd[0] = b[15] * vc0;
+    gd[1] = b[15] * vc1;
+    gd[2] = b[15] * vc2;
+#pragma unroll
+    for (int band = 0; band < 15; band++) {
+        if (band >= rest_bases) break;
+        const bool on = band < nb;
+        gr[3 * band + 0] = on ? b[band] * vc0 : off;
+        gr[3 * band + 1] = on ? b[band] * vc1 : off;
+        gr[3 * band + 2] = on ? b[band] * vc2 : off;
+    }
+}
+
+// Every slot of this lane's rows inactive.
+template <int kRowF> __device__ __forceinline__ void stage_sh_inactive(ShFlat &st, int lane, int rest_bases) {
+    const int rowf = kRowF > 0 ? kRowF : 3 * rest_bases;
+    float *gd = st.dc + 3 * lane, *gr = st.rest + rowf * lane;
+    const float off = __uint_as_float(kInactive);
+    gd[0] = gd[1] = gd[2] = off;
+    for (int k = 0; k < rowf; k++) gr[k] = off;
 }
 
 // One view.  kRowF: floats per features_rest row when known at compile time
@@ -344,68 +361,74 @@ __device__ __forceinline__ void sh_update(const ProjectBwdArgs &a, const StepPar
 // arguments.
 template <int kRowF>
 __global__ void __launch_bounds__(256, 4) k_project_bwd(ProjectBwdArgs a) {
-    __shared__ ShStage stage[8];
+    const int n = a.vt.n;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const StepParams &sp = a.sp[0];
+    const bool want_sh = a.do_optimizer || a.v_dc_out;
+    float *vmean = a.v_mean + 3 * (size_t)i, *vscale = a.v_scale + 3 * (size_t)i, *vquat = a.v_quat + 4 * (size_t)i;
+    if (a.v_opac_out) a.v_opac_out[i] = a.radii[i] > 0 ? a.grad[i].a.z : 0.f;
+    if (a.gstats) {
+        float4 st = a.gstats[i];
+        st.z += 1.f;
+        if (a.radii[i] > 0) {
+            const float4 g0 = a.grad[i].a;
+            st.x += sqrtf(g0.x * g0.x + g0.y * g0.y);
+            st.y += 1.f;
+        }
+        a.gstats[i] = st;
+    }
+    float vm[3] = {0.f, 0.f, 0.f}, vsc[3] = {0.f, 0.f, 0.f}, vq[4] = {0.f, 0.f, 0.f, 0.f};
+    float4 shin = make_float4(0.f, 0.f, 0.f, __int_as_float(0));   // colour gradient, w = 1 when it feeds SH
+    if (a.radii[i] > 0) {
+        const GradRec gr = a.grad[i];
+        const PixConicVjp pc = pix_conic_vjp(a.means[3 * i], a.means[3 * i + 1], a.means[3 * i + 2], sp,
+                                             (float)a.vt.width[0], (float)a.vt.height[0], gr, a.rec[i]);
+        CovState cs;
+        cov_state(a, i, cs);
+        cov_vjp(cs, sp, pc, vm, vsc, vq);
+        if (want_sh) {
+            if (!(finite_bits(gr.c.x) && finite_bits(gr.c.y) && finite_bits(gr.c.z))) {
+                if (a.nan_counts) atomicAdd(a.nan_counts + kNanSH, 1u);
+            } else {
+                shin = make_float4(gr.c.x, gr.c.y, gr.c.z, __int_as_float(1));
+            }
+        }
+    }
+    vmean[0] = vm[0]; vmean[1] = vm[1]; vmean[2] = vm[2];
+    vscale[0] = vsc[0]; vscale[1] = vsc[1]; vscale[2] = vsc[2];
+    *reinterpret_cast<float4 *>(vquat) = make_float4(vq[0], vq[1], vq[2], vq[3]);
+    if (want_sh) a.sh_in[i] = shin;
+}
+
+// The SH Adam (or the gradient export) of one view, after the projection
+// VJP: each lane recomputes its Gaussian's SH basis from the mean and the
+// camera, stages its gradient rows, and the warp walks the rows of its 32
+// Gaussians.
+template <int kRowF>
+__global__ void __launch_bounds__(128) k_sh_walk(ProjectBwdArgs a) {
+    __shared__ __align__(16) ShFlat stage[4];
     const int n = a.vt.n;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    ShStage &sh = stage[wid];
+    const int i0 = blockIdx.x * blockDim.x + wid * 32;
+    if (i0 >= n) return;   // warp-uniform
+    ShFlat &sh = stage[wid];
     const StepParams &sp = a.sp[0];
-    sh.vc[lane] = make_float4(0.f, 0.f, 0.f, 0.f);   // w = 0: nothing to update
-    const bool want_sh = a.do_optimizer || a.v_dc_out;
     if (i < n) {
-        float *vmean = a.v_mean + 3 * (size_t)i, *vscale = a.v_scale + 3 * (size_t)i, *vquat = a.v_quat + 4 * (size_t)i;
-        if (a.v_opac_out) a.v_opac_out[i] = a.radii[i] > 0 ? a.grad[i].a.z : 0.f;
-        if (a.gstats) {
-            float4 st = a.gstats[i];
-            st.z += 1.f;
-            if (a.radii[i] > 0) {
-                const float4 g0 = a.grad[i].a;
-                st.x += sqrtf(g0.x * g0.x + g0.y * g0.y);
-                st.y += 1.f;
-            }
-            a.gstats[i] = st;
+        const float4 shin = a.sh_in[i];
+        if (__float_as_int(shin.w)) {
+            CovState cs;   // only the mean is used by the basis
+            cs.px = a.means[3 * i]; cs.py = a.means[3 * i + 1]; cs.pz = a.means[3 * i + 2];
+            float b[16];
+            sh_basis(cs, sp, b);
+            stage_sh_row<kRowF>(sh, lane, a.rest_bases, bands_in_use(sp, a.rest_bases), b, shin.x, shin.y, shin.z);
+        } else {
+            stage_sh_inactive<kRowF>(sh, lane, a.rest_bases);
         }
-        float vm[3] = {0.f, 0.f, 0.f}, vsc[3] = {0.f, 0.f, 0.f}, vq[4] = {0.f, 0.f, 0.f, 0.f};
-        if (a.radii[i] > 0) {
-            const GradRec gr = a.grad[i];
-            const PixConicVjp pc = pix_conic_vjp(a.means[3 * i], a.means[3 * i + 1], a.means[3 * i + 2], sp,
-                                                 (float)a.vt.width[0], (float)a.vt.height[0], gr, a.rec[i]);
-            CovState cs;
-            cov_state(a, i, cs);
-            cov_vjp(cs, sp, pc, vm, vsc, vq);
-            // SH VJP inputs for the fused Adam (or the gradient export) below
-            if (want_sh) {
-                const float vc0 = gr.c.x, vc1 = gr.c.y, vc2 = gr.c.z;
-                if (!(finite_bits(vc0) && finite_bits(vc1) && finite_bits(vc2))) {
-                    if (a.nan_counts) atomicAdd(a.nan_counts + kNanSH, 1u);
-                } else {
-                    sh_basis(cs, sp, sh.bas[lane]);
-                    sh.vc[lane] = make_float4(vc0, vc1, vc2, __int_as_float(bands_in_use(sp, a.rest_bases) + 1));
-                }
-            }
-        }
-        vmean[0] = vm[0]; vmean[1] = vm[1]; vmean[2] = vm[2];
-        vscale[0] = vsc[0]; vscale[1] = vsc[1]; vscale[2] = vsc[2];
-        *reinterpret_cast<float4 *>(vquat) = make_float4(vq[0], vq[1], vq[2], vq[3]);
     }
-    if (!want_sh) return;
     __syncwarp();
-    const int i0 = (blockIdx.x * blockDim.x) + wid * 32;
-    if (i0 >= n) return;
-    sh_update<kRowF>(
-        a, sp, i0, min(32, n - i0), lane,
-        [&](int gi, int c, float &g) {
-            const float4 vc = sh.vc[gi];
-            if (__float_as_int(vc.w) <= 0) return false;
-            g = sh.bas[gi][15] * (c == 0 ? vc.x : c == 1 ? vc.y : vc.z);
-            return true;
-        },
-        [&](int gi, int band, int c, float &g) {
-            const float4 vc = sh.vc[gi];
-            if (band >= __float_as_int(vc.w) - 1) return false;
-            g = sh.bas[gi][band] * (c == 0 ? vc.x : c == 1 ? vc.y : vc.z);
-            return true;
-        });
+    sh_update<kRowF>(a, sp, sh, i0, min(32, n - i0), lane);
 }
 
 // Several views: the thread walks the Gaussian's record in every view of the
@@ -414,50 +437,50 @@ __global__ void __launch_bounds__(256, 4) k_project_bwd(ProjectBwdArgs a) {
 // gradients and no SH update.
 template <int kRowF>
 __global__ void __launch_bounds__(128, 4) k_project_bwd_views(ProjectBwdArgs a) {
-    __shared__ ShAccStage stage[4];
+    __shared__ __align__(16) ShFlat stage[4];
     const int n = a.vt.n, views = a.vt.count;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    ShAccStage &sh = stage[wid];
+    ShFlat &sh = stage[wid];
     const StepParams &sp0 = a.sp[0];
-    float *acc = sh.g[lane];
-#pragma unroll
-    for (int k = 0; k < 48; k++) acc[k] = 0.f;
-    sh.w[lane] = 0;
+    const int rowf = kRowF > 0 ? kRowF : 3 * a.rest_bases;
+    const int nb = bands_in_use(sp0, a.rest_bases);
+    float *gd = sh.dc + 3 * lane, *gr = sh.rest + rowf * lane;   // this lane's rows: summed over the views
+    gd[0] = gd[1] = gd[2] = 0.f;
+    for (int k = 0; k < rowf; k++) gr[k] = 0.f;
+    bool sh_ok = false;
     if (i < n) {
         float vm[3] = {0.f, 0.f, 0.f}, vsc[3] = {0.f, 0.f, 0.f}, vq[4] = {0.f, 0.f, 0.f, 0.f};
         float vop = 0.f, act_xy = 0.f, act_vis = 0.f;
-        bool any = false, sh_ok = false;
+        bool any = false;
         CovState cs;
-        const int nb = bands_in_use(sp0, a.rest_bases);
         for (int v = 0; v < views; v++) {
             const size_t u = (size_t)v * n + i;
             if (a.radii[u] <= 0) continue;
             if (!any) { cov_state(a, i, cs); any = true; }
-            const GradRec gr = a.grad[u];
+            const GradRec g = a.grad[u];
             const StepParams &sp = a.sp[v];
-            vop += gr.a.z;
-            act_xy += sqrtf(gr.a.x * gr.a.x + gr.a.y * gr.a.y);
+            vop += g.a.z;
+            act_xy += sqrtf(g.a.x * g.a.x + g.a.y * g.a.y);
             act_vis += 1.f;
             const ViewGeom vg = view_geom(a.vt, v);
-            const PixConicVjp pc = pix_conic_vjp(cs.px, cs.py, cs.pz, sp, (float)vg.width, (float)vg.height, gr, a.rec[u]);
+            const PixConicVjp pc = pix_conic_vjp(cs.px, cs.py, cs.pz, sp, (float)vg.width, (float)vg.height, g, a.rec[u]);
             cov_vjp(cs, sp, pc, vm, vsc, vq);
-            const float vc0 = gr.c.x, vc1 = gr.c.y, vc2 = gr.c.z;
+            const float vc0 = g.c.x, vc1 = g.c.y, vc2 = g.c.z;
             if (!(finite_bits(vc0) && finite_bits(vc1) && finite_bits(vc2))) {
                 if (a.nan_counts) atomicAdd(a.nan_counts + kNanSH, 1u);
                 continue;
             }
             float b[16];
             sh_basis(cs, sp, b);
-            acc[45] += b[15] * vc0; acc[46] += b[15] * vc1; acc[47] += b[15] * vc2;
+            gd[0] += b[15] * vc0; gd[1] += b[15] * vc1; gd[2] += b[15] * vc2;
             for (int k = 0; k < nb; k++) {
-                acc[3 * k] += b[k] * vc0;
-                acc[3 * k + 1] += b[k] * vc1;
-                acc[3 * k + 2] += b[k] * vc2;
+                gr[3 * k] += b[k] * vc0;
+                gr[3 * k + 1] += b[k] * vc1;
+                gr[3 * k + 2] += b[k] * vc2;
             }
             sh_ok = true;
         }
-        if (sh_ok) sh.w[lane] = nb + 1;
         float *vmean = a.v_mean + 3 * (size_t)i, *vscale = a.v_scale + 3 * (size_t)i, *vquat = a.v_quat + 4 * (size_t)i;
         vmean[0] = vm[0]; vmean[1] = vm[1]; vmean[2] = vm[2];
         vscale[0] = vsc[0]; vscale[1] = vsc[1]; vscale[2] = vsc[2];
@@ -471,22 +494,20 @@ __global__ void __launch_bounds__(128, 4) k_project_bwd_views(ProjectBwdArgs a) 
             a.gstats[i] = st;
         }
     }
+    // slots Adam leaves alone: every slot without a finite visible view, and
+    // the bands not in use
+    const float off = __uint_as_float(kInactive);
+    if (!sh_ok) {
+        gd[0] = gd[1] = gd[2] = off;
+        for (int k = 0; k < rowf; k++) gr[k] = off;
+    } else {
+        for (int k = 3 * nb; k < rowf; k++) gr[k] = off;
+    }
     if (!a.do_optimizer) return;
     __syncwarp();
     const int i0 = (blockIdx.x * blockDim.x) + wid * 32;
     if (i0 >= n) return;
-    sh_update<kRowF>(
-        a, sp0, i0, min(32, n - i0), lane,
-        [&](int gi, int c, float &g) {
-            if (sh.w[gi] <= 0) return false;
-            g = sh.g[gi][45 + c];
-            return true;
-        },
-        [&](int gi, int band, int c, float &g) {
-            if (band >= sh.w[gi] - 1) return false;
-            g = sh.g[gi][3 * band + c];
-            return true;
-        });
+    sh_update<kRowF>(a, sp0, sh, i0, min(32, n - i0), lane);
 }
 
 void launch_project_bwd(const ProjectBwdArgs &a, cudaStream_t s) {
@@ -499,6 +520,10 @@ void launch_project_bwd(const ProjectBwdArgs &a, cudaStream_t s) {
     }
     if (a.rest_bases == 15) k_project_bwd<45><<<(n + 255) / 256, 256, 0, s>>>(a);
     else k_project_bwd<0><<<(n + 255) / 256, 256, 0, s>>>(a);
+    if (a.do_optimizer || a.v_dc_out) {
+        if (a.rest_bases == 15) k_sh_walk<45><<<(n + 127) / 128, 128, 0, s>>>(a);
+        else k_sh_walk<0><<<(n + 127) / 128, 128, 0, s>>>(a);
+    }
 }
 
 }  // namespace msplat
