@@ -117,7 +117,7 @@ __device__ void backward_range(BwdSmem<kBB> &sm, const RasterArgs &a, int s, int
             float v8 = 0.f;
             if (valid && alpha < 0.999f) {
                 const float4 rc = sm.rgb[t];
-                const float ra = 1.f / (1.f - alpha);
+                const float ra = __fdividef(1.f, 1.f - alpha);   // fast reciprocal, 1 - alpha in [0.001, 0.997]
                 ps.T *= ra;
                 const float fac = alpha * ps.T;
                 const float cv = __fmaf_rn(rc.x, ps.vr, __fmaf_rn(rc.y, ps.vg, rc.z * ps.vb));
