@@ -126,10 +126,12 @@ __device__ __forceinline__ float det_expf_neg(float x) {
 
 // Tile rectangle of a splat, inclusive min / exclusive max (get_tile_bbox,
 // msplat_metal.metal:57-87).  Truncating, saturating float->int conversion.
+// The divisions by 16 are exact scalings: multiplying by 1/16 gives the same
+// bits as the IEEE division.
 __device__ __forceinline__ void tile_rect(float cx, float cy, float ax, float ay, int tiles_x, int tiles_y,
                                           int &x0, int &y0, int &x1, int &y1) {
-    const float tcx = __fdiv_rn(cx, 16.0f), tcy = __fdiv_rn(cy, 16.0f);
-    const float trx = __fdiv_rn(ax, 16.0f), try_ = __fdiv_rn(ay, 16.0f);
+    const float tcx = __fmul_rn(cx, 0.0625f), tcy = __fmul_rn(cy, 0.0625f);
+    const float trx = __fmul_rn(ax, 0.0625f), try_ = __fmul_rn(ay, 0.0625f);
     x0 = min(max(0, __float2int_rz(__fsub_rn(tcx, trx))), tiles_x);
     x1 = min(max(0, __float2int_rz(__fadd_rn(__fadd_rn(tcx, trx), 1.0f))), tiles_x);
     y0 = min(max(0, __float2int_rz(__fsub_rn(tcy, try_))), tiles_y);
