@@ -379,12 +379,16 @@ void mlp_pack(const float *P, uint8_t *img, cudaStream_t s) { k_mlp_pack<<<16, 2
 
 // The MLP kernels take 124 KB of shared memory, so one CTA holds an SM and
 // its 512 tensor-memory columns: allocation never waits on another CTA.
+// Set once on each device (function attributes belong to the current device).
 static void mlp_attrs() {
-    static bool done = false;
-    if (done) return;
+    static bool done[64] = {false};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const bool track = dev >= 0 && dev < 64;
+    if (track && done[dev]) return;
     cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmTrainEnd);
     cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmTrainEnd);
-    done = true;
+    if (track) done[dev] = true;
 }
 
 void mlp_forward(const __nv_bfloat16 *X, int n, const uint8_t *img, const float *P, float2 *out, unsigned *err,

@@ -599,9 +599,14 @@ __global__ void __launch_bounds__(kGlobThreads) k_sort_pack_global(TileArgs a, i
 
 size_t sort_pack_smem_bytes() { return pair_smem_bytes<1024>(); }
 
+// The kernels' shared-memory limits, set once on each device (function
+// attributes belong to the device the call is made on).
 static void tile_attrs() {
-    static bool attr_set = false;
-    if (!attr_set) {
+    static bool attr_set[64] = {false};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const bool track = dev >= 0 && dev < 64;
+    if (!track || !attr_set[dev]) {
         cudaFuncSetAttribute(k_sort_pack_smem<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)pair_smem_bytes<256>());
         cudaFuncSetAttribute(k_sort_pack_smem<512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -614,7 +619,7 @@ static void tile_attrs() {
         cudaFuncSetAttribute(k_scatter_agg<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
         cudaFuncSetAttribute(k_scatter_agg<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
         cudaFuncSetAttribute(k_scatter_agg<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
-        attr_set = true;
+        if (track) attr_set[dev] = true;
     }
 }
 
