@@ -215,7 +215,8 @@ int msplat_engine_set_isect_budget(MsplatEngine *e, long long slots);
 
 /* Launch configuration of the tunable stages (no counterpart in the
  * reference; the defaults are the reference's choices).  None changes the
- * tile lists; sort_width and raster_batch leave every output bit-identical,
+ * tile lists; sort_width, raster_batch and tile_order leave every output
+ * bit-identical,
  * raster_mode and chunk change the image at float rounding (as the
  * reference's own monolithic / chunked choice does). */
 typedef struct {
@@ -227,6 +228,10 @@ typedef struct {
                           default 512 */
     int raster_mode;   /* used when args->raster_mode is 0: 0 the reference's rule (monolithic
                           from 400 tiles), 1 monolithic, 2 chunked; default 0 */
+    int tile_order;    /* how the per-tile lists get their (depth, id) order: 0 a radix sort of
+                          each tile's keys (default), 1 one depth sort per view before the
+                          scatter, then each tile's per-CTA runs put in order (same lists; views
+                          of at most 20480 tiles, else 0) */
 } MsplatTuning;
 
 int msplat_engine_set_tuning(MsplatEngine *e, const MsplatTuning *t);
@@ -234,8 +239,8 @@ int msplat_engine_get_tuning(MsplatEngine *e, MsplatTuning *t);
 
 /* Autotuner: times full training steps of the given views (forward, loss,
  * backward; no optimizer update and no SGLD, so the parameters do not
- * change) under candidate configurations, one coordinate at a time (sort
- * width, tile batch, then raster mode with chunk length when
+ * change) under candidate configurations, one coordinate at a time (tile
+ * order, sort width, tile batch, then raster mode with chunk length when
  * args[0].raster_mode is 0), keeps the fastest (the median of `reps` timed
  * steps) and leaves it set.  gt[v] must be given for every view.  `out`
  * receives the chosen configuration and *ms (nullable) its step time. */

@@ -1,0 +1,306 @@
+// Depth-presorted tile ordering: the per-tile lists come out in (depth, id)
+// order without a per-tile sort.
+//
+//   1. Each view's Gaussians are sorted once by depth: a stable LSD radix sort
+//      of (depth bits, Gaussian id) on 8-bit digits, four passes of
+//      histogram -> scan -> scatter; inactive Gaussians (culled, or depth not
+//      finite and positive) carry the key 0xffffffff and sort last.  Stability
+//      puts equal depths in id order, the reference's tie rule.
+//   2. Their tile rectangles are written in that order (8 bytes each).
+//   3. The block-aggregated count and scatter of the other path run over the
+//      sorted positions p: CTA c covers p in [2048 c, 2048 c + 2048), so each
+//      tile's bucket is a sequence of per-CTA runs in increasing depth, and
+//      the key stored is p itself.
+//   4. Inside a run the scatter's shared-memory slot order is arbitrary: each
+//      key's place is the run's start plus the number of smaller keys in the
+//      run (positions are unique), and the id written there is the Gaussian at
+//      position p.  Runs are short (a CTA's 2048 Gaussians are a thin depth
+//      slab spread over the image); the count is quadratic in a run's length,
+//      which stays within 2048.
+// The lists are the same as the per-tile radix sort's (same keys, same
+// order); the scan and the class lists of tiles.cu are shared.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace msplat {
+
+constexpr int kGsThreads = 256;
+constexpr int kGsItems = 8;
+constexpr int kGsPerCta = kGsThreads * kGsItems;   // 2048 keys per radix-sort CTA
+static_assert(kAggPerCta == 2048, "run index p >> 11 needs 2048 Gaussians per count CTA");
+
+__device__ __forceinline__ uint32_t gs_key0(const TileArgs &a, size_t u) {
+    if (a.radii[u] <= 0) return 0xffffffffu;
+    const float d = a.depths[u];
+    return (finite_bits(d) && d > 0.0f) ? __float_as_uint(d) : 0xffffffffu;
+}
+
+// Digit counts of one 2048-key block: hist[view][digit][block].
+template <bool kFirst>
+__global__ void __launch_bounds__(kGsThreads) k_gs_hist(TileArgs a, int shift, const uint32_t *key_in) {
+    __shared__ uint32_t h[256];
+    const int view = blockIdx.y, n = a.vt.n, nb = gridDim.x;
+    const size_t vb = (size_t)view * n;
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const int e0 = blockIdx.x * kGsPerCta;
+    for (int k = threadIdx.x; k < kGsPerCta; k += kGsThreads) {
+        const int e = e0 + k;
+        if (e >= n) break;
+        const uint32_t key = kFirst ? gs_key0(a, vb + e) : key_in[vb + e];
+        atomicAdd(&h[(key >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    a.gs_hist[(size_t)view * 256 * nb + (size_t)threadIdx.x * nb + blockIdx.x] = h[threadIdx.x];
+}
+
+// Exclusive scan of one view's [digit][block] counts (digit-major: the
+// offsets of digit d in block b), one 1024-thread CTA per view: each thread
+// scans a contiguous run, the run totals are scanned across the CTA.
+__global__ void __launch_bounds__(1024) k_gs_scan(TileArgs a, int nb) {
+    __shared__ uint32_t warp_tot[32];
+    uint32_t *h = a.gs_hist + (size_t)blockIdx.x * 256 * nb;
+    const int len = 256 * nb;
+    const int per = (len + 1023) / 1024;
+    const int lo = min(len, (int)threadIdx.x * per), hi = min(len, lo + per);
+    uint32_t sum = 0;
+    for (int t = lo; t < hi; t++) sum += h[t];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint32_t incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
+    }
+    if (lane == 31) warp_tot[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        const uint32_t v = warp_tot[lane];
+        uint32_t inc = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += u;
+        }
+        warp_tot[lane] = inc - v;
+    }
+    __syncthreads();
+    uint32_t run = warp_tot[wid] + incl - sum;
+    for (int t = lo; t < hi; t++) {
+        const uint32_t c = h[t];
+        h[t] = run;
+        run += c;
+    }
+}
+
+// Stable scatter of one 2048-key block: warp w holds keys [256 w, 256 w + 256)
+// of the block in eight rounds of 32; a key's place is its digit's offset for
+// the block + the same digit's keys in earlier warps + in earlier rounds of
+// its warp + in lower lanes of its round (peers found with eight ballots).
+template <bool kFirst>
+__global__ void __launch_bounds__(kGsThreads) k_gs_scatter(TileArgs a, int shift, const uint32_t *key_in,
+                                                           const uint32_t *val_in, uint32_t *key_out,
+                                                           uint32_t *val_out) {
+    __shared__ uint16_t wcnt[kGsThreads / 32][256];
+    __shared__ uint16_t woff[kGsThreads / 32][256];
+    __shared__ uint32_t base[256];
+    const int view = blockIdx.y, n = a.vt.n, nb = gridDim.x;
+    const size_t vb = (size_t)view * n;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    for (int k = tid; k < (kGsThreads / 32) * 256; k += kGsThreads) (&wcnt[0][0])[k] = 0;
+    base[tid] = a.gs_hist[(size_t)view * 256 * nb + (size_t)tid * nb + blockIdx.x];
+    __syncthreads();
+    const int e0 = blockIdx.x * kGsPerCta + wid * (32 * kGsItems);
+    const uint32_t lt = (1u << lane) - 1u;
+    uint32_t kv[kGsItems], vv[kGsItems], rank[kGsItems];
+#pragma unroll
+    for (int j = 0; j < kGsItems; j++) {
+        const int e = e0 + j * 32 + lane;
+        const bool valid = e < n;
+        kv[j] = valid ? (kFirst ? gs_key0(a, vb + e) : key_in[vb + e]) : 0u;
+        vv[j] = valid ? (kFirst ? (uint32_t)e : val_in[vb + e]) : 0u;
+        const uint32_t d = valid ? ((kv[j] >> shift) & 255u) : 256u;
+        uint32_t peers = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+        for (int bit = 0; bit < 8; bit++) {
+            const uint32_t m = __ballot_sync(0xffffffffu, (d >> bit) & 1u);
+            peers &= ((d >> bit) & 1u) ? m : ~m;
+        }
+        uint32_t old = 0;
+        if (valid) old = wcnt[wid][d];
+        __syncwarp();
+        rank[j] = valid ? old + __popc(peers & lt) : 0xffffffffu;
+        if (valid && (peers & lt) == 0) wcnt[wid][d] = (uint16_t)(old + __popc(peers));
+        __syncwarp();
+    }
+    __syncthreads();
+    {   // per digit (one thread each), the counts of the earlier warps
+        uint32_t run = 0;
+#pragma unroll
+        for (int w = 0; w < kGsThreads / 32; w++) {
+            const uint32_t c = wcnt[w][tid];
+            woff[w][tid] = (uint16_t)run;
+            run += c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kGsItems; j++) {
+        if (rank[j] == 0xffffffffu) continue;
+        const uint32_t d = (kv[j] >> shift) & 255u;
+        const uint32_t pos = base[d] + woff[wid][d] + rank[j];
+        if (MS_GUARD(pos < (uint32_t)n, 7, pos, a.nan_counts ? a.nan_counts + kDbgSlot : nullptr)) {
+            key_out[vb + pos] = kv[j];
+            val_out[vb + pos] = vv[j];
+        }
+    }
+}
+
+// Tile rectangle of the Gaussian at each sorted position (empty when inactive).
+__global__ void __launch_bounds__(256) k_gs_rect(TileArgs a) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int view = blockIdx.y, n = a.vt.n;
+    if (p >= n) return;
+    const size_t vb = (size_t)view * n;
+    ushort4 r = make_ushort4(0, 0, 0, 0);
+    if (a.gs_key[0][vb + p] != 0xffffffffu) {
+        const uint32_t i = a.gs_val[0][vb + p];
+        const ViewGeom vg = view_geom(a.vt, view);
+        const float4 ra = a.rec[vb + i].a;
+        const float2 ab = a.aabb[vb + i];
+        int x0, y0, x1, y1;
+        tile_rect(ra.x, ra.y, ab.x, ab.y, vg.tiles_x, vg.tiles_y, x0, y0, x1, y1);
+        r = make_ushort4((unsigned short)x0, (unsigned short)y0, (unsigned short)x1, (unsigned short)y1);
+    }
+    a.srect[vb + p] = r;
+}
+
+// Block-aggregated count over sorted positions (k_count_agg's rows).
+__global__ void __launch_bounds__(kAggThreads) k_count_agg_sorted(TileArgs a) {
+    extern __shared__ uint32_t bins[];
+    const int view = blockIdx.y;
+    const ViewGeom vg = view_geom(a.vt, view);
+    const int T = vg.tiles_x * vg.tiles_y;
+    for (int t = threadIdx.x; t < T; t += blockDim.x) bins[t] = 0;
+    __syncthreads();
+    const size_t vb = (size_t)view * a.vt.n;
+    const int g0 = blockIdx.x * kAggPerCta, g1 = min(a.vt.n, g0 + kAggPerCta);
+    for (int p = g0 + threadIdx.x; p < g1; p += blockDim.x) {
+        const ushort4 r = a.srect[vb + p];
+        for (int y = r.y; y < r.w; y++)
+            for (int x = r.x; x < r.z; x++) atomicAdd(&bins[y * vg.tiles_x + x], 1u);
+    }
+    __syncthreads();
+    uint32_t *row = a.cta_bins + (size_t)gridDim.x * vg.tile_base + (size_t)blockIdx.x * T;
+    for (int t = threadIdx.x; t < T; t += blockDim.x) row[t] = bins[t];
+}
+
+// Block-aggregated scatter over sorted positions: the key is the position p.
+template <bool kGroup>
+__global__ void __launch_bounds__(kAggThreads) k_scatter_agg_sorted(TileArgs a) {
+    extern __shared__ uint32_t bins[];
+    const int view = blockIdx.y;
+    const ViewGeom vg = view_geom(a.vt, view);
+    const int T = vg.tiles_x * vg.tiles_y;
+    const uint32_t *row = a.cta_bins + (size_t)gridDim.x * vg.tile_base + (size_t)blockIdx.x * T;
+    for (int t = threadIdx.x; t < T; t += blockDim.x) bins[t] = a.tile_offsets[vg.tile_base + t] + row[t];
+    __syncthreads();
+    uint32_t *keys = reinterpret_cast<uint32_t *>(a.keys);
+    const size_t vb = (size_t)view * a.vt.n;
+    const int g0 = blockIdx.x * kAggPerCta, g1 = min(a.vt.n, g0 + kAggPerCta);
+    for (int p = g0 + threadIdx.x; p < g1; p += blockDim.x) {
+        const ushort4 r = a.srect[vb + p];
+        for (int y = r.y; y < r.w; y++)
+            for (int x = r.x; x < r.z; x++) {
+                const int lt = y * vg.tiles_x + x;
+                if (kGroup && (vg.tile_base + lt < a.tile_lo || vg.tile_base + lt >= a.tile_hi)) continue;
+                const uint64_t dst = (uint64_t)atomicAdd(&bins[lt], 1u) - (kGroup ? (uint64_t)a.isect_lo : 0ull);
+                if (dst < (uint64_t)a.capacity) keys[dst] = (uint32_t)p;   // overflow is dropped, never written
+            }
+    }
+}
+
+// Each tile's runs in order: the key at slot j (a sorted position p) goes to
+// its run's start + the number of smaller keys in the run; the record id of
+// the Gaussian at p is written there.  A tile whose bucket does not fit the
+// buffer is emitted transparent.
+__global__ void __launch_bounds__(128) k_tile_order(TileArgs a, int ctas) {
+    const int t = a.tile_lo + blockIdx.x;
+    if (t >= a.tile_hi) return;
+    const int count = (int)a.tile_counts[t];
+    if (count == 0) return;
+    const uint64_t start = (uint64_t)a.tile_offsets[t] - (uint64_t)a.isect_lo;
+    if (start + (uint64_t)count > (uint64_t)a.capacity) {
+        for (int j = threadIdx.x; j < count; j += blockDim.x)
+            if (start + j < (uint64_t)a.capacity) a.isect_ids[start + j] = 0xffffffffu;
+        return;
+    }
+    const int view = view_of_tile(a.vt, t);
+    const ViewGeom vg = view_geom(a.vt, view);
+    const int Tv = vg.tiles_x * vg.tiles_y;
+    const uint32_t *col = a.cta_bins + (size_t)ctas * vg.tile_base + (t - vg.tile_base);   // run starts: col[c * Tv]
+    const uint32_t *keys = reinterpret_cast<const uint32_t *>(a.keys) + start;
+    const size_t vb = (size_t)view * a.vt.n;
+    for (int j = threadIdx.x; j < count; j += blockDim.x) {
+        const uint32_t p = keys[j];
+        const int c = (int)(p >> 11);
+        const uint32_t rs = col[(size_t)c * Tv];
+        const uint32_t re = c + 1 < ctas ? col[(size_t)(c + 1) * Tv] : (uint32_t)count;
+        uint32_t below = 0;
+        for (uint32_t q = rs; q < re; q++) below += keys[q] < p ? 1u : 0u;
+        const uint32_t dst = rs + below;
+        if (MS_GUARD(dst < (uint32_t)count, 8, dst, a.nan_counts ? a.nan_counts + kDbgSlot : nullptr))
+            a.isect_ids[start + dst] = (uint32_t)(vb + a.gs_val[0][vb + p]);
+    }
+}
+
+int launch_presorted_count(const TileArgs &a, cudaStream_t s) {
+    const int n = a.vt.n, views = a.vt.count;
+    const int nb = (n + kGsPerCta - 1) / kGsPerCta;
+    const dim3 g(nb, views);
+    // pass 0 reads the keys from the projection; passes alternate buffers 1, 0, 1, 0
+    k_gs_hist<true><<<g, kGsThreads, 0, s>>>(a, 0, nullptr);
+    k_gs_scan<<<views, 1024, 0, s>>>(a, nb);
+    k_gs_scatter<true><<<g, kGsThreads, 0, s>>>(a, 0, nullptr, nullptr, a.gs_key[1], a.gs_val[1]);
+    for (int pass = 1; pass < 4; pass++) {
+        const int src = pass & 1, dst = src ^ 1;
+        k_gs_hist<false><<<g, kGsThreads, 0, s>>>(a, 8 * pass, a.gs_key[src]);
+        k_gs_scan<<<views, 1024, 0, s>>>(a, nb);
+        k_gs_scatter<false><<<g, kGsThreads, 0, s>>>(a, 8 * pass, a.gs_key[src], a.gs_val[src], a.gs_key[dst],
+                                                      a.gs_val[dst]);
+    }
+    debug_sync(s, "depth_sort");
+    k_gs_rect<<<dim3((n + 255) / 256, views), 256, 0, s>>>(a);
+    debug_sync(s, "depth_rect");
+    const int agg_blocks = (n + kAggPerCta - 1) / kAggPerCta;
+    const size_t smem = (size_t)max_view_tiles(a.vt) * sizeof(uint32_t);
+    static bool attr_set[64] = {false};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64 || !attr_set[dev]) {
+        cudaFuncSetAttribute(k_count_agg_sorted, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
+        cudaFuncSetAttribute(k_scatter_agg_sorted<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kAggMaxTiles * 4);
+        cudaFuncSetAttribute(k_scatter_agg_sorted<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kAggMaxTiles * 4);
+        if (dev >= 0 && dev < 64) attr_set[dev] = true;
+    }
+    k_count_agg_sorted<<<dim3(agg_blocks, views), kAggThreads, smem, s>>>(a);
+    debug_sync(s, "count_sorted");
+    return 12 + 1 + 1;
+}
+
+int launch_presorted_build(const TileArgs &a, cudaStream_t s) {
+    const int n = a.vt.n, views = a.vt.count;
+    const int agg_blocks = (n + kAggPerCta - 1) / kAggPerCta;
+    const size_t smem = (size_t)max_view_tiles(a.vt) * sizeof(uint32_t);
+    const bool grp = a.tile_lo > 0 || a.tile_hi < a.num_tiles || a.isect_lo > 0;
+    if (grp) k_scatter_agg_sorted<true><<<dim3(agg_blocks, views), kAggThreads, smem, s>>>(a);
+    else k_scatter_agg_sorted<false><<<dim3(agg_blocks, views), kAggThreads, smem, s>>>(a);
+    debug_sync(s, "scatter_sorted");
+    if (a.tile_hi > a.tile_lo) k_tile_order<<<a.tile_hi - a.tile_lo, 128, 0, s>>>(a, agg_blocks);
+    debug_sync(s, "tile_order");
+    return 2;
+}
+
+}  // namespace msplat

@@ -153,6 +153,14 @@ class Engine {
         // below allocates nothing
         const size_t cb = tile_cta_bins_bytes(vt);
         if (cb) alloc("cta_bins", cb);
+        const bool presorted = tune.tile_order == 1 && cb > 0 && N > 0;
+        if (presorted) {
+            const size_t recs = (size_t)N * B;
+            alloc("gs_key0", 4 * recs); alloc("gs_key1", 4 * recs);
+            alloc("gs_val0", 4 * recs); alloc("gs_val1", 4 * recs);
+            alloc("gs_hist", 4 * (size_t)B * 256 * ((N + 2047) / 2048));
+            alloc("srect", 8 * recs);
+        }
         const MsplatStepArgs &a0 = args[0];
         const bool opt = a0.do_optimizer && st;
 
@@ -195,6 +203,13 @@ class Engine {
         ta.cta_bins = cb ? ptr<uint32_t>("cta_bins") : nullptr;
         ta.tile_lists = ptr<uint32_t>("tile_lists"); ta.tile_class = ptr<uint32_t>("tile_class");
         ta.tile_lo = 0; ta.tile_hi = T; ta.isect_lo = 0;
+        ta.sort_width = tune.sort_width;
+        ta.presorted = presorted ? 1 : 0;
+        if (presorted) {
+            ta.gs_key[0] = ptr<uint32_t>("gs_key0"); ta.gs_key[1] = ptr<uint32_t>("gs_key1");
+            ta.gs_val[0] = ptr<uint32_t>("gs_val0"); ta.gs_val[1] = ptr<uint32_t>("gs_val1");
+            ta.gs_hist = ptr<uint32_t>("gs_hist"); ta.srect = ptr<ushort4>("srect");
+        }
         std::vector<TileGroup> groups;
         if (!fixed) {
             launches_ += launch_tiles(ta, num_sms_, stream_);
@@ -422,6 +437,7 @@ class Engine {
         if (t.raster_batch != 128 && t.raster_batch != 256) throw std::runtime_error("raster_batch must be 128 or 256");
         if (t.chunk != 256 && t.chunk != 512 && t.chunk != 1024) throw std::runtime_error("chunk must be 256, 512 or 1024");
         if (t.raster_mode < 0 || t.raster_mode > 2) throw std::runtime_error("raster_mode must be 0, 1 or 2");
+        if (t.tile_order < 0 || t.tile_order > 1) throw std::runtime_error("tile_order must be 0 or 1");
         if (std::memcmp(&t, &tuning_, sizeof(t)) != 0) clear_graphs();
         tuning_ = t;
     }
@@ -466,6 +482,7 @@ class Engine {
                 const float m = measure(c);
                 if (m < bms) { bms = m; best = c; }
             };
+            for (int o : {0, 1}) { MsplatTuning c = best; c.tile_order = o; consider(c); }
             for (int w : {256, 512}) { MsplatTuning c = best; c.sort_width = w; consider(c); }
             for (int b : {128, 256}) { MsplatTuning c = best; c.raster_batch = b; consider(c); }
             if (a[0].raster_mode == 0) {
@@ -770,7 +787,7 @@ class Engine {
     long long timed_steps_ = 0, launches_ = 0;
     RasterArgs last_ra_{};   // raster arguments of the last eagerly issued step
     float4 *gstats_ = nullptr;   // caller's activity statistics (learned relocation), or null
-    MsplatTuning tuning_{512, 256, kChunk, 0};   // launch configuration of the tunable stages
+    MsplatTuning tuning_{512, 256, kChunk, 0, 0};   // launch configuration of the tunable stages
     long long isect_slots_ = 0;   // fixed intersection budget in slots (0: legacy 48 per Gaussian and view)
     int last_groups_ = 1;         // tile groups of the last step
 

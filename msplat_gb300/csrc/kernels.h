@@ -32,6 +32,18 @@ inline ViewTable make_view_table(int n, int count, const int *w, const int *h) {
 }
 inline ViewTable single_view_table(int n, int w, int h) { return make_view_table(n, 1, &w, &h); }
 
+// Block-aggregated tile mapping: a CTA of kAggThreads covers kAggPerCta
+// Gaussians of one view; used while every view has at most kAggMaxTiles tiles.
+constexpr int kAggPerCta = 2048;
+constexpr int kAggThreads = 512;      // four CTAs per SM: 1M Gaussians fill one wave
+constexpr int kAggMaxTiles = 20480;   // 80 KB of histogram: two 512-thread CTAs per SM at the largest
+
+inline int max_view_tiles(const ViewTable &vt) {
+    int m = 0;
+    for (int v = 0; v < vt.count; v++) m = vt.tiles_x[v] * vt.tiles_y[v] > m ? vt.tiles_x[v] * vt.tiles_y[v] : m;
+    return m;
+}
+
 // Record arrays (rec, depths, radii, aabb, tiles_hit, grad) are [views, n]
 // (see ViewTable); the parameters are read once per view.
 struct ProjectArgs {
@@ -72,6 +84,13 @@ struct TileArgs {
     uint64_t *keys, *keys_alt;
     uint32_t *isect_ids;    // per-tile sorted Gaussian ids (0xffffffff: transparent)
     unsigned *nan_counts;
+    // depth-presorted ordering (block-aggregated path only): one stable
+    // radix sort of each view's Gaussians by depth, the count and scatter in
+    // that order, then each tile's per-CTA runs put in order
+    int presorted;
+    uint32_t *gs_key[2], *gs_val[2];   // [views, n] sort buffers; ids in depth order end in gs_val[0]
+    uint32_t *gs_hist;                 // [views, 256, ceil(n / 2048)] digit counts, then offsets
+    ushort4 *srect;                    // [views, n] tile rectangles in depth order
 };
 
 struct RasterArgs {
@@ -171,6 +190,11 @@ void launch_project_fwd(const ProjectArgs &a, cudaStream_t s);
 int launch_tile_count(const TileArgs &a, cudaStream_t s);
 int launch_tile_build(const TileArgs &a, int num_sms, cudaStream_t s);
 int launch_tiles(const TileArgs &a, int num_sms, cudaStream_t s);
+// the depth-presorted ordering (depth_order.cu): sort + rectangles + count,
+// then the column and tile scans (tiles.cu); and its build
+int launch_presorted_count(const TileArgs &a, cudaStream_t s);
+int launch_tile_scans(const TileArgs &a, cudaStream_t s);
+int launch_presorted_build(const TileArgs &a, cudaStream_t s);
 size_t sort_pack_smem_bytes();
 // cta_bins bytes for these views, 0 when the block-aggregated path is not used
 size_t tile_cta_bins_bytes(const ViewTable &vt);

@@ -144,9 +144,6 @@ __global__ void __launch_bounds__(256) k_scatter(TileArgs a) {
 // CTA loads its row, adds the tile offsets, and hands out slots with
 // shared-memory atomics.  No global atomics, and each tile's bucket is
 // filled CTA by CTA.  Used while every view's histogram fits (kAggMaxTiles).
-constexpr int kAggPerCta = 2048;
-constexpr int kAggThreads = 512;   // four CTAs per SM: 1M Gaussians fill one wave
-constexpr int kAggMaxTiles = 20480;   // 80 KB of histogram: two 512-thread CTAs per SM at the largest
 
 __device__ __forceinline__ void agg_rect(const TileArgs &a, const ViewGeom &vg, size_t u, int &x0, int &y0, int &x1,
                                          int &y1) {
@@ -241,11 +238,6 @@ __global__ void __launch_bounds__(kAggThreads) k_scatter_agg(TileArgs a) {
     }
 }
 
-static int max_view_tiles(const ViewTable &vt) {
-    int m = 0;
-    for (int v = 0; v < vt.count; v++) m = std::max(m, vt.tiles_x[v] * vt.tiles_y[v]);
-    return m;
-}
 
 size_t tile_cta_bins_bytes(const ViewTable &vt) {
     if (max_view_tiles(vt) > kAggMaxTiles || vt.n <= 0) return 0;
@@ -623,8 +615,24 @@ static void tile_attrs() {
     }
 }
 
+static bool presorted_path(const TileArgs &a) {
+    return a.presorted && a.vt.n > 0 && max_view_tiles(a.vt) <= kAggMaxTiles && a.cta_bins != nullptr;
+}
+
+// the column scan of the per-CTA histograms and the tile scan
+int launch_tile_scans(const TileArgs &a, cudaStream_t s) {
+    const int agg_blocks = (a.vt.n + kAggPerCta - 1) / kAggPerCta;
+    if (a.vt.count > 1) k_cta_scan<true><<<(a.num_tiles + 31) / 32, 1024, 0, s>>>(a, agg_blocks);
+    else k_cta_scan<false><<<(a.num_tiles + 31) / 32, 1024, 0, s>>>(a, agg_blocks);
+    debug_sync(s, "cta_scan");
+    k_scan<<<1, 1024, 0, s>>>(a);
+    debug_sync(s, "scan");
+    return 2;
+}
+
 int launch_tile_count(const TileArgs &a, cudaStream_t s) {
     tile_attrs();
+    if (presorted_path(a)) return launch_presorted_count(a, s) + launch_tile_scans(a, s);
     int launches = 0;
     const int n = a.vt.n, views = a.vt.count, maxT = max_view_tiles(a.vt);
     const bool agg = maxT <= kAggMaxTiles && a.cta_bins != nullptr;
@@ -653,6 +661,7 @@ int launch_tile_count(const TileArgs &a, cudaStream_t s) {
 
 int launch_tile_build(const TileArgs &a, int num_sms, cudaStream_t s) {
     tile_attrs();
+    if (presorted_path(a)) return launch_presorted_build(a, s);
     int launches = 0;
     const int n = a.vt.n, views = a.vt.count, maxT = max_view_tiles(a.vt);
     const bool agg = maxT <= kAggMaxTiles && a.cta_bins != nullptr;

@@ -1,7 +1,8 @@
 """Tunable launch configuration (include/msplat_engine.h MsplatTuning) and
-the autotuner.  The sort width and the rasterizers' tile batch must leave
-every output of a step bit-identical (tile lists, image, loss, gradients,
-updated parameters); the chunk length changes the chunked image only at
+the autotuner.  The sort width, the rasterizers' tile batch and the tile
+order (per-tile radix sort or one depth sort per view) must leave every
+output of a step bit-identical (tile lists, image; loss, gradients and
+updated parameters to float-atomic rounding); the chunk length changes the chunked image only at
 float rounding; the autotuner returns a valid configuration and leaves it
 set (GPU only)."""
 import numpy as np
@@ -52,13 +53,13 @@ def _step(init, cams, gts, tuning, views, raster_mode=1):
 
 
 @pytest.mark.parametrize("views", [1, 2])
-def test_sort_width_and_tile_batch_are_bit_identical(scene, views):
+def test_sort_width_tile_batch_and_tile_order_are_bit_identical(scene, views):
     sc, cams, gts, init = scene
     ref = _step(init, cams, gts, dict(sort_width=512, raster_batch=256), views)
     counts = np.diff(ref["offs"].astype(np.int64))
     assert (counts > 0).sum() > 50   # the 256-thread sort class takes the tiles up to 2048 keys
     for tun in (dict(sort_width=256, raster_batch=256), dict(sort_width=512, raster_batch=128),
-                dict(sort_width=256, raster_batch=128)):
+                dict(sort_width=256, raster_batch=128), dict(tile_order=1), dict(tile_order=1, raster_batch=128)):
         o = _step(init, cams, gts, tun, views)
         for k in ("offs", "ids", "img", "v_img"):
             np.testing.assert_array_equal(o[k], ref[k], err_msg=f"{tun} {k}")
@@ -110,19 +111,21 @@ def test_autotune(scene):
     eng.close()
 
 
+@pytest.mark.parametrize("tile_order", [0, 1])
 @pytest.mark.parametrize("views", [1, 2])
-def test_isect_budget_tile_groups(scene, views):
+def test_isect_budget_tile_groups(scene, views, tile_order):
     """A fixed intersection budget smaller than the step's intersections: the
     step runs in tile groups (lists built and rastered group by group, rebuilt
     for the backward) and gives the legacy step's image bit for bit and its
     gradients and update to rounding (float atomics)."""
     sc, cams, gts, init = scene
-    ref = _step(init, cams, gts, {}, views)
+    ref = _step(init, cams, gts, dict(tile_order=tile_order), views)
     M = int(ref["offs"][-1])
     counts = np.diff(ref["offs"].astype(np.int64))
     slots = max(int(counts.max()), M // 4)
 
     eng = E.Engine(0)
+    eng.set_tuning(tile_order=tile_order)
     eng.set_isect_budget(slots)
     dg = E.DeviceGaussians(init)
     cs = cams[:views]
