@@ -19,6 +19,8 @@
 //      which stays within 2048.
 // The lists are the same as the per-tile radix sort's (same keys, same
 // order); the scan and the class lists of tiles.cu are shared.
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -54,43 +56,35 @@ __global__ void __launch_bounds__(kGsThreads) k_gs_hist(TileArgs a, int shift, c
     a.gs_hist[(size_t)view * 256 * nb + (size_t)threadIdx.x * nb + blockIdx.x] = h[threadIdx.x];
 }
 
-// Exclusive scan of one view's [digit][block] counts (digit-major: the
-// offsets of digit d in block b), one 1024-thread CTA per view: each thread
-// scans a contiguous run, the run totals are scanned across the CTA.
-__global__ void __launch_bounds__(1024) k_gs_scan(TileArgs a, int nb) {
-    __shared__ uint32_t warp_tot[32];
-    uint32_t *h = a.gs_hist + (size_t)blockIdx.x * 256 * nb;
-    const int len = 256 * nb;
-    const int per = (len + 1023) / 1024;
-    const int lo = min(len, (int)threadIdx.x * per), hi = min(len, lo + per);
-    uint32_t sum = 0;
-    for (int t = lo; t < hi; t++) sum += h[t];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    uint32_t incl = sum;
+// Per digit (one warp each), the exclusive scan of its blocks' counts in
+// place, and the digit's total to dtot[view][digit].  Each lane takes every
+// 32nd block; four rounds of loads are issued before they are scanned.
+__global__ void __launch_bounds__(256) k_gs_digit_scan(TileArgs a, int nb) {
+    const int lane = threadIdx.x & 31;
+    const int d = blockIdx.x * 8 + (threadIdx.x >> 5), view = blockIdx.y;
+    uint32_t *h = a.gs_hist + (size_t)view * 256 * nb + (size_t)d * nb;
+    uint32_t carry = 0;
+    for (int b0 = 0; b0 < nb; b0 += 128) {
+        uint32_t v[4];
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += u;
-    }
-    if (lane == 31) warp_tot[wid] = incl;
-    __syncthreads();
-    if (wid == 0) {
-        const uint32_t v = warp_tot[lane];
-        uint32_t inc = v;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
-            if (lane >= o) inc += u;
+        for (int k = 0; k < 4; k++) {
+            const int b = b0 + 32 * k + lane;
+            v[k] = b < nb ? h[b] : 0u;
         }
-        warp_tot[lane] = inc - v;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            uint32_t inc = v[k];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += u;
+            }
+            const int b = b0 + 32 * k + lane;
+            if (b < nb) h[b] = carry + inc - v[k];
+            carry += __shfl_sync(0xffffffffu, inc, 31);
+        }
     }
-    __syncthreads();
-    uint32_t run = warp_tot[wid] + incl - sum;
-    for (int t = lo; t < hi; t++) {
-        const uint32_t c = h[t];
-        h[t] = run;
-        run += c;
-    }
+    if (lane == 0) a.gs_dtot[(size_t)view * 256 + d] = carry;
 }
 
 // Stable scatter of one 2048-key block: warp w holds keys [256 w, 256 w + 256)
@@ -104,11 +98,26 @@ __global__ void __launch_bounds__(kGsThreads) k_gs_scatter(TileArgs a, int shift
     __shared__ uint16_t wcnt[kGsThreads / 32][256];
     __shared__ uint16_t woff[kGsThreads / 32][256];
     __shared__ uint32_t base[256];
+    __shared__ uint32_t wsum[kGsThreads / 32];
     const int view = blockIdx.y, n = a.vt.n, nb = gridDim.x;
     const size_t vb = (size_t)view * n;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     for (int k = tid; k < (kGsThreads / 32) * 256; k += kGsThreads) (&wcnt[0][0])[k] = 0;
-    base[tid] = a.gs_hist[(size_t)view * 256 * nb + (size_t)tid * nb + blockIdx.x];
+    {   // this block's start for digit tid: the digit's start (exclusive scan of
+        // the digit totals) + the earlier blocks' keys of that digit
+        const uint32_t tot = a.gs_dtot[(size_t)view * 256 + tid];
+        uint32_t inc = tot;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += u;
+        }
+        if (lane == 31) wsum[wid] = inc;
+        __syncthreads();
+        uint32_t add = 0;
+        for (int w = 0; w < wid; w++) add += wsum[w];
+        base[tid] = add + inc - tot + a.gs_hist[(size_t)view * 256 * nb + (size_t)tid * nb + blockIdx.x];
+    }
     __syncthreads();
     const int e0 = blockIdx.x * kGsPerCta + wid * (32 * kGsItems);
     const uint32_t lt = (1u << lane) - 1u;
@@ -222,9 +231,15 @@ __global__ void __launch_bounds__(kAggThreads) k_scatter_agg_sorted(TileArgs a) 
 
 // Each tile's runs in order: the key at slot j (a sorted position p) goes to
 // its run's start + the number of smaller keys in the run; the record id of
-// the Gaussian at p is written there.  A tile whose bucket does not fit the
-// buffer is emitted transparent.
-__global__ void __launch_bounds__(128) k_tile_order(TileArgs a, int ctas) {
+// the Gaussian at p is written there.  The runs' starts (one column of
+// cta_bins) and, when they fit, the tile's keys are staged in shared memory
+// first; the id gather is issued before the count.  A tile whose bucket does
+// not fit the buffer is emitted transparent.
+constexpr int kOrderThreads = 256;
+constexpr int kOrderSmemWords = 12288;   // 48 KB: run starts + staged keys
+
+__global__ void __launch_bounds__(kOrderThreads) k_tile_order(TileArgs a, int ctas, int stage_runs, int key_cap) {
+    extern __shared__ uint32_t osm[];
     const int t = a.tile_lo + blockIdx.x;
     if (t >= a.tile_hi) return;
     const int count = (int)a.tile_counts[t];
@@ -239,18 +254,36 @@ __global__ void __launch_bounds__(128) k_tile_order(TileArgs a, int ctas) {
     const ViewGeom vg = view_geom(a.vt, view);
     const int Tv = vg.tiles_x * vg.tiles_y;
     const uint32_t *col = a.cta_bins + (size_t)ctas * vg.tile_base + (t - vg.tile_base);   // run starts: col[c * Tv]
-    const uint32_t *keys = reinterpret_cast<const uint32_t *>(a.keys) + start;
+    const uint32_t *gkeys = reinterpret_cast<const uint32_t *>(a.keys) + start;
+    uint32_t *runs = osm;                                 // [ctas + 1] when stage_runs
+    uint32_t *staged = osm + (stage_runs ? ctas + 1 : 0);
+    const bool in_smem = count <= key_cap;                // CTA-uniform
+    if (stage_runs) {
+        for (int c = threadIdx.x; c < ctas; c += blockDim.x) runs[c] = col[(size_t)c * Tv];
+        if (threadIdx.x == 0) runs[ctas] = (uint32_t)count;
+    }
+    if (in_smem)
+        for (int j = threadIdx.x; j < count; j += blockDim.x) staged[j] = gkeys[j];
+    __syncthreads();
+    const uint32_t *keys = in_smem ? staged : gkeys;
     const size_t vb = (size_t)view * a.vt.n;
     for (int j = threadIdx.x; j < count; j += blockDim.x) {
         const uint32_t p = keys[j];
+        const uint32_t gid = a.gs_val[0][vb + p];
         const int c = (int)(p >> 11);
-        const uint32_t rs = col[(size_t)c * Tv];
-        const uint32_t re = c + 1 < ctas ? col[(size_t)(c + 1) * Tv] : (uint32_t)count;
+        uint32_t rs, re;
+        if (stage_runs) {
+            rs = runs[c];
+            re = runs[c + 1];
+        } else {
+            rs = col[(size_t)c * Tv];
+            re = c + 1 < ctas ? col[(size_t)(c + 1) * Tv] : (uint32_t)count;
+        }
         uint32_t below = 0;
         for (uint32_t q = rs; q < re; q++) below += keys[q] < p ? 1u : 0u;
         const uint32_t dst = rs + below;
         if (MS_GUARD(dst < (uint32_t)count, 8, dst, a.nan_counts ? a.nan_counts + kDbgSlot : nullptr))
-            a.isect_ids[start + dst] = (uint32_t)(vb + a.gs_val[0][vb + p]);
+            a.isect_ids[start + dst] = (uint32_t)(vb + gid);
     }
 }
 
@@ -259,13 +292,14 @@ int launch_presorted_count(const TileArgs &a, cudaStream_t s) {
     const int nb = (n + kGsPerCta - 1) / kGsPerCta;
     const dim3 g(nb, views);
     // pass 0 reads the keys from the projection; passes alternate buffers 1, 0, 1, 0
+    const dim3 gd(32, views);   // 256 digits, 8 per CTA
     k_gs_hist<true><<<g, kGsThreads, 0, s>>>(a, 0, nullptr);
-    k_gs_scan<<<views, 1024, 0, s>>>(a, nb);
+    k_gs_digit_scan<<<gd, 256, 0, s>>>(a, nb);
     k_gs_scatter<true><<<g, kGsThreads, 0, s>>>(a, 0, nullptr, nullptr, a.gs_key[1], a.gs_val[1]);
     for (int pass = 1; pass < 4; pass++) {
         const int src = pass & 1, dst = src ^ 1;
         k_gs_hist<false><<<g, kGsThreads, 0, s>>>(a, 8 * pass, a.gs_key[src]);
-        k_gs_scan<<<views, 1024, 0, s>>>(a, nb);
+        k_gs_digit_scan<<<gd, 256, 0, s>>>(a, nb);
         k_gs_scatter<false><<<g, kGsThreads, 0, s>>>(a, 8 * pass, a.gs_key[src], a.gs_val[src], a.gs_key[dst],
                                                       a.gs_val[dst]);
     }
@@ -298,7 +332,14 @@ int launch_presorted_build(const TileArgs &a, cudaStream_t s) {
     if (grp) k_scatter_agg_sorted<true><<<dim3(agg_blocks, views), kAggThreads, smem, s>>>(a);
     else k_scatter_agg_sorted<false><<<dim3(agg_blocks, views), kAggThreads, smem, s>>>(a);
     debug_sync(s, "scatter_sorted");
-    if (a.tile_hi > a.tile_lo) k_tile_order<<<a.tile_hi - a.tile_lo, 128, 0, s>>>(a, agg_blocks);
+    // shared memory: the run starts when they take at most two thirds of it,
+    // then up to 4096 keys (a small footprint keeps eight CTAs per SM; larger
+    // tiles count from global memory)
+    const int stage_runs = agg_blocks + 1 <= (2 * kOrderSmemWords) / 3 ? 1 : 0;
+    const int key_cap = std::min(4096, kOrderSmemWords - (stage_runs ? agg_blocks + 1 : 0));
+    const size_t osmem = sizeof(uint32_t) * ((stage_runs ? agg_blocks + 1 : 0) + key_cap);
+    if (a.tile_hi > a.tile_lo)
+        k_tile_order<<<a.tile_hi - a.tile_lo, kOrderThreads, osmem, s>>>(a, agg_blocks, stage_runs, key_cap);
     debug_sync(s, "tile_order");
     return 2;
 }

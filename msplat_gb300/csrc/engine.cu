@@ -159,6 +159,7 @@ class Engine {
             alloc("gs_key0", 4 * recs); alloc("gs_key1", 4 * recs);
             alloc("gs_val0", 4 * recs); alloc("gs_val1", 4 * recs);
             alloc("gs_hist", 4 * (size_t)B * 256 * ((N + 2047) / 2048));
+            alloc("gs_dtot", 4 * (size_t)B * 256);
             alloc("srect", 8 * recs);
         }
         const MsplatStepArgs &a0 = args[0];
@@ -209,6 +210,7 @@ class Engine {
             ta.gs_key[0] = ptr<uint32_t>("gs_key0"); ta.gs_key[1] = ptr<uint32_t>("gs_key1");
             ta.gs_val[0] = ptr<uint32_t>("gs_val0"); ta.gs_val[1] = ptr<uint32_t>("gs_val1");
             ta.gs_hist = ptr<uint32_t>("gs_hist"); ta.srect = ptr<ushort4>("srect");
+            ta.gs_dtot = ptr<uint32_t>("gs_dtot");
         }
         std::vector<TileGroup> groups;
         if (!fixed) {

@@ -89,7 +89,8 @@ struct TileArgs {
     // that order, then each tile's per-CTA runs put in order
     int presorted;
     uint32_t *gs_key[2], *gs_val[2];   // [views, n] sort buffers; ids in depth order end in gs_val[0]
-    uint32_t *gs_hist;                 // [views, 256, ceil(n / 2048)] digit counts, then offsets
+    uint32_t *gs_hist;                 // [views, 256, ceil(n / 2048)] digit counts, then offsets in the digit
+    uint32_t *gs_dtot;                 // [views, 256] keys per digit
     ushort4 *srect;                    // [views, n] tile rectangles in depth order
 };
 
