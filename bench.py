@@ -339,7 +339,10 @@ def run_engine(args):
     # launch configuration: the autotuner times whole steps of this workload
     # (no updates) over its candidates and keeps the fastest
     tuned, tuned_ms = None, None
-    if not args.no_autotune:
+    if args.tuning:   # a fixed configuration, e.g. "tile_order=1,sort_width=512"
+        eng.set_tuning(**{k: int(v) for k, v in (kv.split("=") for kv in args.tuning.split(","))})
+        tuned = eng.tuning()
+    elif not args.no_autotune:
         cd0 = cams[0]
         a0 = E.make_args(cd0, E.step_scalars(step_base, step_base, width=cd0["width"], height=cd0["height"]))
         tuned, tuned_ms = eng.autotune(dg, [a0], [gts_dev[0].data_ptr()], reps=5)
@@ -470,6 +473,8 @@ def main():
                     help="skip the learned-vs-plain relocation time-to-PSNR runs")
     ap.add_argument("--no-batched", action="store_true", help="skip the multi-view (8 views per step) measurement")
     ap.add_argument("--no-autotune", action="store_true", help="time the default launch configuration")
+    ap.add_argument("--tuning", default="", help="fixed launch configuration instead of the autotuner, "
+                                                 "e.g. tile_order=1,sort_width=512")
     ap.add_argument("--gaussians", type=int, default=N_MODEL,
                     help="trained Gaussians (default 1M; smaller only for profiling captures)")
     args = ap.parse_args()

@@ -113,6 +113,13 @@ int msplat_trainer_set_batch_views(MsplatTrainer t, int num_views, float lr_scal
  * buffers grown with the model.  Returns 0 or a negative code. */
 int msplat_trainer_set_isect_budget(MsplatTrainer t, float bytes_per_gaussian);
 
+/* Runs the engine's autotuner (msplat_engine_autotune) on the trainer's
+ * next training cameras (as many as the views per step) and keeps the
+ * fastest launch configuration for the rest of the run; `out` (nullable)
+ * receives it.  The parameters are not changed.  Returns 0 or a negative
+ * code. */
+int msplat_trainer_autotune(MsplatTrainer t, MsplatTuning *out);
+
 /* Replaces the trainer's Gaussians with a trained PLY (Model::loadPly, the
  * CLI's --resume); optimizer state starts fresh.  Returns the iteration
  * recorded in the file, or a negative code. */

@@ -51,6 +51,7 @@ def _lib():
     L.msplat_trainer_learned_stats.argtypes = [vp, fp, C.POINTER(C.c_int)]
     L.msplat_trainer_set_batch_views.argtypes = [vp, C.c_int, C.c_float]
     L.msplat_trainer_set_isect_budget.argtypes = [vp, C.c_float]
+    L.msplat_trainer_autotune.argtypes = [vp, vp]
     L.msplat_dataset_create_from_memory.argtypes = [C.c_int, fp, fp, C.POINTER(C.c_int), C.POINTER(vp),
                                                     C.POINTER(vp), C.c_int, fp, C.POINTER(C.c_uint8), C.c_bool,
                                                     C.c_int, C.c_bool]
@@ -289,6 +290,14 @@ class GaussianTrainer:
         """Fixed intersection buffers (bytes per Gaussian of the cap; 0 = legacy), tile groups beyond."""
         if _lib().msplat_trainer_set_isect_budget(self.h, float(bytes_per_gaussian)) != 0:
             raise ValueError(f"invalid intersection budget: {bytes_per_gaussian}")
+
+    def autotune(self) -> dict:
+        """Time the engine's launch configurations on the next training views and keep the fastest."""
+        from ._native import MsplatTuning
+        t = MsplatTuning()
+        if _lib().msplat_trainer_autotune(self.h, C.cast(C.byref(t), C.c_void_p)) != 0:
+            raise RuntimeError("autotune failed")
+        return {k: getattr(t, k) for k, _ in MsplatTuning._fields_}
 
     def learned_stats(self) -> dict:
         loss = (C.c_float * 1)()

@@ -76,6 +76,8 @@ def parse(argv=None):
     p.add_argument("--isect-budget", type=float, default=0.0,
                    help="fixed intersection buffers in bytes per Gaussian of --cap-max (the reference's "
                         "MSPLAT_ISECT_BUDGET, e.g. 1000); larger views are rastered in tile groups; 0 = legacy")
+    p.add_argument("--autotune", action="store_true",
+                   help="time the engine's launch configurations on the first training views and keep the fastest")
     p.add_argument("--learned-relocation", action="store_true",
                    help="weight MCMC relocation sources by the online-trained proposal MLP")
     a = p.parse_args(argv)
@@ -109,6 +111,8 @@ def main(argv=None) -> int:
         trainer.set_learned_relocation(True)
     if a.isect_budget > 0:
         trainer.set_isect_budget(a.isect_budget)
+    if a.autotune:
+        print(f"Launch configuration: {trainer.autotune()}", flush=True)
     if a.resume:
         step0 = trainer.load_ply(a.resume)
         print(f"Resumed from {a.resume} at step {step0}", flush=True)

@@ -1269,6 +1269,30 @@ int msplat_trainer_set_isect_budget(MsplatTrainer t, float bytes_per_gaussian) {
     }, -2);
 }
 
+int msplat_trainer_autotune(MsplatTrainer t, MsplatTuning *out) {
+    if (!t) return -1;
+    return guard("autotune", [&]() {
+        TrainerImpl *tr = TR(t);
+        if (tr->ds->train.empty()) throw std::runtime_error("dataset has no training cameras");
+        // the next batch of cameras of the shuffled order (without advancing it)
+        const int B = std::max(1, tr->batch_views);
+        std::vector<MsplatStepArgs> a(B);
+        std::vector<const uint8_t *> gt(B), mk(B);
+        for (int v = 0; v < B; v++) {
+            HostCamera &cam = tr->ds->train[tr->cam_order[(tr->cam_pos + v) % tr->cam_order.size()]];
+            cam.upload();
+            tr->step_args(cam, std::max(1, tr->current_step), a[v], true);
+            gt[v] = cam.d_image;
+            mk[v] = cam.d_mask;
+        }
+        MsplatGaussians g = tr->model.gaussians();
+        MsplatTuning tun{};
+        const int rc = msplat_engine_autotune(tr->eng, &g, a.data(), B, gt.data(), mk.data(), 3, &tun, nullptr);
+        if (rc == 0 && out) *out = tun;
+        return rc;
+    }, -2);
+}
+
 int msplat_trainer_learned_stats(MsplatTrainer t, float *last_loss, int *rounds) {
     if (!t) return -1;
     if (last_loss) *last_loss = TR(t)->lrn.last_loss;

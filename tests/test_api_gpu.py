@@ -161,6 +161,9 @@ def test_batch_views_step(scene):
             continue
         assert rel_l2(upd_t, upd_e) <= 1e-4, k
     losses = [t.last_loss]
+    cfg = t.autotune()                         # the launch configuration, timed on the next views
+    assert cfg["tile_order"] in (0, 1) and cfg["sort_width"] in (256, 512)
+    np.testing.assert_array_equal(t.get_gaussians()[0], g1[0])   # autotuning leaves the model alone
     for _ in range(40):
         t.step()
         losses.append(t.last_loss)
