@@ -138,6 +138,12 @@ __device__ __forceinline__ void tile_rect(float cx, float cy, float ax, float ay
     y1 = min(max(0, __float2int_rz(__fadd_rn(__fadd_rn(tcy, try_), 1.0f))), tiles_y);
 }
 
+// Pixel of thread tid in its 16x16 tile: each warp covers an 8x4 block (two
+// warps across, four down), a squarer footprint than two 16-pixel rows, so a
+// small splat misses more warps entirely.
+__device__ __forceinline__ int tile_px(int tid) { return (tid & 7) | ((tid >> 2) & 8); }
+__device__ __forceinline__ int tile_py(int tid) { return ((tid >> 3) & 3) | ((tid >> 4) & 12); }
+
 // Tile list bound as a slot of the intersection buffer, which holds the
 // global slots [lo, lo + cap) (lo = 0 unless a tile group is being rastered),
 // clamped to the buffer.

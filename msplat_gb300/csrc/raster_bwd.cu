@@ -188,8 +188,8 @@ template <bool kViews> __device__ __forceinline__ BwdPixel bwd_pixel(const Raste
     const ViewGeom vg = view_geom(a.vt, tp.view);
     const int lt = tile - vg.tile_base;
     const int tx = lt % vg.tiles_x, ty = lt / vg.tiles_x;
-    tp.x = tx * kTile + (threadIdx.x & 15);
-    tp.y = ty * kTile + (threadIdx.x >> 4);
+    tp.x = tx * kTile + tile_px(threadIdx.x);
+    tp.y = ty * kTile + tile_py(threadIdx.x);
     tp.inside = tp.x < vg.width && tp.y < vg.height;
     tp.p = tp.inside ? vg.pix_base + (long long)tp.y * vg.width + tp.x : 0;
     return tp;
