@@ -65,10 +65,8 @@ def log(*a):
 
 
 def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    from msplat_gb300 import replicas
+    return replicas.dist_env()
 
 
 def build_workload(seed=0, n_model=N_MODEL, views=VIEWS):
@@ -291,10 +289,9 @@ def run_engine(args):
     import torch
     from msplat_gb300 import engine as E
 
+    from msplat_gb300 import replicas as R
     ws, rank, local = dist_env()
-    if ws > 1:
-        import torch.distributed as dist
-        dist.init_process_group("gloo")
+    R.init(ws)
     torch.cuda.set_device(local)
     n_model = args.gaussians
     sc, model = build_workload(n_model=n_model)
@@ -326,15 +323,10 @@ def run_engine(args):
             eng.train_step(dg, a, gts_dev[k % len(cams)].data_ptr())
 
     def barrier():
-        if ws > 1:
-            torch.distributed.barrier()
+        R.barrier(ws)
 
     def max_over_ranks(x):
-        if ws == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
+        return R.max_over_ranks(ws, x)
 
     # launch configuration: the autotuner times whole steps of this workload
     # (no updates) over its candidates and keeps the fastest
@@ -370,7 +362,7 @@ def run_engine(args):
     launches = eng.stats().launches - launches0
     dev_ms = max_over_ranks(dev_ms)
     ms_step = dev_ms / args.steps
-    value = ws * args.steps / (dev_ms / 1e3)
+    value = R.job_rate(ws, args.steps, dev_ms / 1e3)
 
     # end to end through the C ABI: pinned host image in, loss out, every step
     barrier()
@@ -380,7 +372,7 @@ def run_engine(args):
         one(args.warmup + args.steps + k, True)
         eng.loss()
     e2e_s = max_over_ranks(time.perf_counter() - t0)
-    e2e = {"value": ws * args.steps / e2e_s, "unit": "iters/s",
+    e2e = {"value": R.job_rate(ws, args.steps, e2e_s), "unit": "iters/s",
            "h2d_bytes_per_step": int(gts_host[0].numel()), "d2h_bytes_per_step": 4}
 
     # per-stage times: CUDA events between the stages of eager steps (events
@@ -456,8 +448,7 @@ def run_engine(args):
     if rank == 0:
         print(json.dumps(out), flush=True)
     eng.close()
-    if ws > 1:
-        torch.distributed.destroy_process_group()
+    R.finish(ws)
     return 0
 
 
