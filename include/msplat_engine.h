@@ -103,10 +103,13 @@ const char *msplat_engine_last_error(const MsplatEngine *e);
 int msplat_engine_train_step(MsplatEngine *e, const MsplatGaussians *g, const MsplatAdamState *st,
                              const MsplatStepArgs *args, const uint8_t *gt, const uint8_t *mask);
 
-/* The same step with the target image (and mask) in host memory: they are
- * copied to the device on the engine's stream first (asynchronously when the
- * host buffers are page-locked), as the reference reads the camera's image
- * each step (core/src/msplat_api.mm:104-110). */
+/* The same step with the target image (and mask) in host memory, as the
+ * reference reads the camera's image each step (core/src/msplat_api.mm:
+ * 104-110): they are copied to the device on a copy stream into one of two
+ * alternating engine buffers (asynchronously when the host buffers are
+ * page-locked), so one step's upload overlaps the step before it; the step
+ * itself waits for its copy.  The host buffer must stay valid until the
+ * copy has run (msplat_engine_synchronize). */
 int msplat_engine_train_step_host(MsplatEngine *e, const MsplatGaussians *g, const MsplatAdamState *st,
                                   const MsplatStepArgs *args, const uint8_t *gt_host, const uint8_t *mask_host);
 
@@ -119,6 +122,12 @@ int msplat_engine_synchronize(MsplatEngine *e);
 
 /* Loss of the last step (loss_sum / (H*W), msplat_metal.mm:1738); waits. */
 int msplat_engine_loss(MsplatEngine *e, float *loss);
+
+/* Without waiting: copies the last step's loss sums (one float per view of
+ * the step; the loss is the sum divided by the view's pixel count) to dst on
+ * the engine's stream.  With page-locked dst the values are there once the
+ * stream has passed this point (msplat_engine_synchronize). */
+int msplat_engine_loss_async(MsplatEngine *e, float *dst);
 
 /* Stats of the last step; waits. */
 int msplat_engine_stats(MsplatEngine *e, MsplatEngineStats *out);

@@ -91,6 +91,7 @@ def lib(build_if_missing: bool = True):
         L.msplat_engine_render.argtypes = [vp, C.POINTER(MsplatGaussians), C.POINTER(MsplatStepArgs)]
         L.msplat_engine_synchronize.argtypes = [vp]
         L.msplat_engine_loss.argtypes = [vp, FP]
+        L.msplat_engine_loss_async.argtypes = [vp, vp]
         L.msplat_engine_stats.argtypes = [vp, C.POINTER(MsplatEngineStats)]
         L.msplat_engine_set_timing.argtypes = [vp, C.c_int]
         L.msplat_engine_buffer.argtypes = [vp, C.c_char_p, C.POINTER(C.c_void_p)]

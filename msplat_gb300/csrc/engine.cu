@@ -43,6 +43,12 @@ class Engine {
     explicit Engine(int device) : device_(device) {
         CK(cudaSetDevice(device));
         CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+        CK(cudaStreamCreateWithFlags(&copy_stream_, cudaStreamNonBlocking));
+        for (int k = 0; k < 2; k++) {
+            CK(cudaEventCreateWithFlags(&stage_ready_[k], cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&stage_free_[k], cudaEventDisableTiming));
+            CK(cudaEventRecord(stage_free_[k], stream_));
+        }
         cudaDeviceProp prop;
         CK(cudaGetDeviceProperties(&prop, device));
         num_sms_ = prop.multiProcessorCount;
@@ -58,6 +64,12 @@ class Engine {
         for (auto &row : ev_)
             for (auto &ev : row) cudaEventDestroy(ev);
         for (auto &ev : marker_) cudaEventDestroy(ev);
+        cudaStreamSynchronize(copy_stream_);
+        for (int k = 0; k < 2; k++) {
+            cudaEventDestroy(stage_ready_[k]);
+            cudaEventDestroy(stage_free_[k]);
+        }
+        cudaStreamDestroy(copy_stream_);
         cudaStreamDestroy(stream_);
     }
 
@@ -71,19 +83,39 @@ class Engine {
 
     // Copies host images into engine-owned device buffers on the engine's
     // stream (asynchronous for page-locked sources), then runs the step.
+    // The copies run on a second stream into two alternating stage buffers,
+    // so a step's upload overlaps the step before it: the engine stream waits
+    // for this step's copy, and a buffer is refilled only after the step that
+    // read it.  Asynchronous for page-locked sources.
     void train_step_host(const MsplatGaussians &g, const MsplatAdamState *st, const MsplatStepArgs &args,
                          const uint8_t *gt_host, const uint8_t *mask_host) {
         CK(cudaSetDevice(device_));
         const size_t P = (size_t)args.width * args.height;
-        alloc("gt_stage", P * 3);
-        CK(cudaMemcpyAsync(ptr<uint8_t>("gt_stage"), gt_host, P * 3, cudaMemcpyHostToDevice, stream_));
+        const int k = stage_slot_;
+        stage_slot_ ^= 1;
+        const std::string gname = k ? "gt_stage1" : "gt_stage0", mname = k ? "mask_stage1" : "mask_stage0";
+        alloc(gname.c_str(), P * 3);
+        if (mask_host) alloc(mname.c_str(), P);
+        CK(cudaStreamWaitEvent(copy_stream_, stage_free_[k], 0));   // the step that last read this buffer is done
+        CK(cudaMemcpyAsync(ptr<uint8_t>(gname.c_str()), gt_host, P * 3, cudaMemcpyHostToDevice, copy_stream_));
         const uint8_t *mask_d = nullptr;
         if (mask_host) {
-            alloc("mask_stage", P);
-            CK(cudaMemcpyAsync(ptr<uint8_t>("mask_stage"), mask_host, P, cudaMemcpyHostToDevice, stream_));
-            mask_d = ptr<uint8_t>("mask_stage");
+            CK(cudaMemcpyAsync(ptr<uint8_t>(mname.c_str()), mask_host, P, cudaMemcpyHostToDevice, copy_stream_));
+            mask_d = ptr<uint8_t>(mname.c_str());
         }
-        train_step(g, st, args, ptr<uint8_t>("gt_stage"), mask_d, true);
+        CK(cudaEventRecord(stage_ready_[k], copy_stream_));
+        CK(cudaStreamWaitEvent(stream_, stage_ready_[k], 0));
+        train_step(g, st, args, ptr<uint8_t>(gname.c_str()), mask_d, true);
+        CK(cudaEventRecord(stage_free_[k], stream_));
+    }
+
+    // Copies the last step's per-view loss sums (loss_sum[v], v < views; the
+    // loss is the sum over the view's pixel count) to `dst` on the engine's
+    // stream without waiting: page-locked `dst` is filled when the stream
+    // gets there.
+    void loss_async(float *dst) {
+        CK(cudaMemcpyAsync(dst, ptr<float>("loss_sum"), sizeof(float) * std::max(1, last_views_),
+                           cudaMemcpyDeviceToHost, stream_));
     }
 
     // Multi-view step: B views (any sizes) rendered and back-propagated by
@@ -776,6 +808,9 @@ class Engine {
 
     int device_ = 0, num_sms_ = 1;
     cudaStream_t stream_ = nullptr;
+    cudaStream_t copy_stream_ = nullptr;          // host-image uploads
+    cudaEvent_t stage_ready_[2], stage_free_[2];  // per stage buffer: upload done / last reader done
+    int stage_slot_ = 0;
     std::map<std::string, Buf> bufs_;
     int cap_points_ = 0, cap_tiles_ = 0;
     long long cap_records_ = 0, cap_isect_ = 0, cap_pixels_ = 0, cap_chunks_ = 0;
@@ -882,6 +917,11 @@ int msplat_engine_render(MsplatEngine *e, const MsplatGaussians *g, const Msplat
 
 int msplat_engine_synchronize(MsplatEngine *e) {
     return guarded(e, [&] { e->impl->synchronize(); });
+}
+
+int msplat_engine_loss_async(MsplatEngine *e, float *dst) {
+    if (!dst) return -1;
+    return guarded(e, [&] { e->impl->loss_async(dst); });
 }
 
 int msplat_engine_loss(MsplatEngine *e, float *loss) {

@@ -209,6 +209,11 @@ class Engine:
     def set_timing(self, on: bool):
         self._check(self.L.msplat_engine_set_timing(self.h, int(on)))
 
+    def loss_async(self, dst_ptr: int):
+        """Enqueue the copy of the last step's loss sums (one float per view) to
+        page-locked host memory at dst_ptr; valid after synchronize()."""
+        self._check(self.L.msplat_engine_loss_async(self.h, C.c_void_p(dst_ptr)))
+
     def set_graphs(self, on: bool):
         """Capture repeated steps into CUDA graphs and replay them."""
         self._check(self.L.msplat_engine_set_graphs(self.h, int(on)))
