@@ -5,7 +5,7 @@
 //   params      means[N,3] scales[N,3] (log) quats[N,4] (w,x,y,z)
 //               features_dc[N,3] features_rest[N,B,3] opacities[N] (logit)
 //   SplatRec    per Gaussian, 48 B: projected centre, sigmoid(opacity),
-//               conic, raw SH colour (written by the projection)
+//               conic, raw SH colour, reach box (written by the projection)
 //   isect_ids   per intersection, 4 B: the Gaussian (record) id, in per-tile
 //               depth order (written by the sort)
 //   GradRec     per Gaussian, 48 B: rasterizer gradients (xy, opacity logit;
@@ -22,8 +22,8 @@ constexpr int kChunk = 512;         // depth-chunk length of the chunked raster 
 
 struct SplatRec {
     float4 a;   // x, y, opacity (sigmoid), unused
-    float4 b;   // conic a, b, c, unused
-    float4 c;   // raw SH colour r, g, b, unused
+    float4 b;   // conic a, b, c, reach half-extent x (pixels)
+    float4 c;   // raw SH colour r, g, b, reach half-extent y
 };
 
 struct GradRec {
@@ -143,6 +143,27 @@ __device__ __forceinline__ void tile_rect(float cx, float cy, float ax, float ay
 // small splat misses more warps entirely.
 __device__ __forceinline__ int tile_px(int tid) { return (tid & 7) | ((tid >> 2) & 8); }
 __device__ __forceinline__ int tile_py(int tid) { return ((tid >> 3) & 3) | ((tid >> 4) & 12); }
+
+// Warps of a tile that a splat can reach: bit w is set when the 8x4 block of
+// warp w (tile-local x in [8(w&1), 8(w&1)+7], y in [4(w>>1), 4(w>>1)+3])
+// meets the box centre +- (hx, hy), the splat's reach from the projection
+// (outside it no pixel passes the rasterizers' sigma and alpha tests).
+// (ox, oy) is the tile's first pixel.  Non-finite extents reach every warp,
+// negative ones none; the box edges get a margin well above the rounding of
+// the tile-local offsets.  A warp whose bit is clear skips the splat: every
+// one of its pixels would have rejected it, so nothing changes.
+__device__ __forceinline__ uint32_t warp_reach(float x, float y, float hx, float hy, float ox, float oy) {
+    if (!(hx <= 3.0e38f && hy <= 3.0e38f)) return 0xFFu;
+    if (hx < 0.f || hy < 0.f) return 0u;
+    const float lx = x - ox, ly = y - oy;
+    const float rx = hx + 0.02f + 1e-6f * (fabsf(lx) + hx + fabsf(ox));
+    const float ry = hy + 0.02f + 1e-6f * (fabsf(ly) + hy + fabsf(oy));
+    const float x0 = lx - rx, x1 = lx + rx, y0 = ly - ry, y1 = ly + ry;
+    const uint32_t cols = (x1 >= 0.f && x0 <= 7.f ? 0x55u : 0u) | (x1 >= 8.f && x0 <= 15.f ? 0xAAu : 0u);
+    const uint32_t rows = (y1 >= 0.f && y0 <= 3.f ? 0x03u : 0u) | (y1 >= 4.f && y0 <= 7.f ? 0x0Cu : 0u) |
+                          (y1 >= 8.f && y0 <= 11.f ? 0x30u : 0u) | (y1 >= 12.f && y0 <= 15.f ? 0xC0u : 0u);
+    return cols & rows;
+}
 
 // Tile list bound as a slot of the intersection buffer, which holds the
 // global slots [lo, lo + cap) (lo = 0 unless a tile group is being rastered),

@@ -18,6 +18,38 @@ __constant__ float kShC3[7] = {-0.5900435899266435f, 2.890611442640554f, -0.4570
                                0.3731763325901154f, -0.4570457994644658f, 1.445305721320277f,
                                -0.5900435899266435f};
 
+// Reach of a splat, (hx, hy): the half-extents of a box around its centre
+// outside which no pixel passes the rasterizers' tests sigma in [0, 5.55)
+// and opacity * exp(-sigma) >= 1/255 (warp_reach turns it into the warps of
+// a tile that the splat can touch).
+//  - alpha >= 1/255 needs sigma <= ln(255 opacity); s = min(5.55, that)
+//    + 1e-4 covers the rounding of the exponential, the product and the log.
+//  - The rasterizers' rounded sigma is within 3.5 u (a dx^2 + c dy^2) of the
+//    exact quadratic form (u = 2^-24; |b dx dy| <= (a dx^2 + c dy^2) / 2 for a
+//    positive-definite conic), so rounded sigma <= s implies the exact form
+//    of the conic with a and c shrunk by 1e-5 is <= s.  That ellipse's box is
+//    sqrt(2 s c' / det'), sqrt(2 s a' / det'), det' by Kahan's fma
+//    determinant (relative error 2 u), widened by 1e-5 for the rounding of
+//    the box, of the rasterizers' dx, dy and of the shrink itself.
+//  - Unbounded (+inf) unless the centre and conic are finite and moderate
+//    (then no sigma can overflow, and every pair a warp skips had a finite
+//    sigma); empty (-1) when s < 0.
+__device__ __forceinline__ float2 reach_extent(float x, float y, float opac, float ca, float cb, float cc) {
+    const float inf = __int_as_float(0x7f800000);
+    const bool moderate = fabsf(x) <= 1e8f && fabsf(y) <= 1e8f && fabsf(ca) <= 1e20f && fabsf(cb) <= 1e20f &&
+                          fabsf(cc) <= 1e20f;   // false for NaN
+    if (!moderate) return make_float2(inf, inf);
+    const float s = fminf(5.55f, logf(255.f * opac)) + 1e-4f;
+    if (!(s >= 0.f)) return make_float2(-1.f, -1.f);
+    const float a = ca * (1.f - 1e-5f), c = cc * (1.f - 1e-5f);
+    if (!(a > 0.f && c > 0.f)) return make_float2(inf, inf);
+    const float w = cb * cb;
+    const float det = fmaf(a, c, -w) + fmaf(-cb, cb, w);
+    if (!(det > 0.f)) return make_float2(inf, inf);
+    const float k = 2.f * s / det;
+    return make_float2(sqrtf(k * c) * (1.f + 1e-5f), sqrtf(k * a) * (1.f + 1e-5f));
+}
+
 // kViews: several views (blockIdx.y); false compiles the one-view step with
 // the geometry read straight from the parameter bank
 template <bool kViews>
@@ -157,10 +189,12 @@ __global__ void __launch_bounds__(256) k_project_fwd(ProjectArgs a) {
     // when it packs each intersection, hybrid_sort_pack_kernel): store 0,
     // which rasterizes the same way, and count the intersections.
     const bool oko = finite_bits(opac);
+    const float op_rec = oko ? opac : 0.f;
+    const float2 reach = reach_extent(cxp, cyp, op_rec, ca, cb, cc);
     SplatRec rec;
-    rec.a = make_float4(cxp, cyp, oko ? opac : 0.f, 0.f);
-    rec.b = make_float4(ca, cb, cc, 0.f);
-    rec.c = make_float4(col[0], col[1], col[2], 0.f);
+    rec.a = make_float4(cxp, cyp, op_rec, 0.f);
+    rec.b = make_float4(ca, cb, cc, reach.x);
+    rec.c = make_float4(col[0], col[1], col[2], reach.y);
     a.rec[u] = rec;
     a.depths[u] = vz;
     a.aabb[u] = make_float2(ax, ay);

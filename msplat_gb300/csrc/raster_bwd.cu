@@ -4,7 +4,8 @@
 // gradients with a transpose-reduce (9 shuffles for 8 values plus 5 for the
 // ninth, instead of 45), warps combine through shared-memory adds, and each
 // batch flushes one set of three float4 vector atomics per (splat, tile)
-// instead of the reference's nine scalar atomics per (splat, warp).
+// instead of the reference's nine scalar atomics per (splat, warp).  A warp
+// skips the splats whose reach box (warp_reach) misses its 8x4 pixel block.
 // Follows rasterize_backward_kernel (msplat_metal.metal:931-1135),
 // compute_chunk_prefix_suffix_kernel (:3139-3175) and
 // rasterize_backward_chunked_kernel (:3179-3366), including its quirk that a
@@ -19,7 +20,7 @@ namespace msplat {
 // kBB splats staged per round (the tile batch: 128 or 256)
 template <int kBB> struct BwdSmem {
     float4 xyo[kBB];    // x, y, opacity, id bits
-    float4 con[kBB];
+    float4 con[kBB];    // conic, bits of the warps the splat reaches (warp_reach)
     float4 rgb[kBB];    // clamped colour, w: bits of the channels with raw + 0.5 >= 0
     float acc[kBB][9];  // r g b | ca cb cc | x y | opacity
     int wmax[8];
@@ -66,8 +67,9 @@ struct PixelState {
 // Processes splat indices [s, hi] back to front for the whole CTA.
 template <int kBB>
 __device__ void backward_range(BwdSmem<kBB> &sm, const RasterArgs &a, int s, int hi, PixelState &ps, GradRec *grad) {
-    const int tid = threadIdx.x, lane = tid & 31;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int wbin = __reduce_max_sync(0xffffffffu, ps.bin_final);
+    const float ox = ps.px - (float)tile_px(tid), oy = ps.py - (float)tile_py(tid);
     for (int batch_end = hi; batch_end >= s; batch_end -= kBB) {
         __syncthreads();
         const int idx = batch_end - tid;
@@ -75,7 +77,8 @@ __device__ void backward_range(BwdSmem<kBB> &sm, const RasterArgs &a, int s, int
             if (idx >= s) {
                 const SplatRec r = isect_record(a.isect_ids, a.rec, a.n, idx);
                 sm.xyo[tid] = r.a;
-                sm.con[tid] = r.b;
+                sm.con[tid] = make_float4(r.b.x, r.b.y, r.b.z,
+                                          __uint_as_float(warp_reach(r.a.x, r.a.y, r.b.w, r.c.w, ox, oy)));
                 // clamped colour max(raw + 0.5, 0); w: channels whose raw + 0.5 >= 0
                 // (the only ones that pass a colour gradient back)
                 const float cr = r.c.x + 0.5f, cg = r.c.y + 0.5f, cb = r.c.z + 0.5f;
@@ -88,9 +91,10 @@ __device__ void backward_range(BwdSmem<kBB> &sm, const RasterArgs &a, int s, int
         __syncthreads();
         const int nb = min(kBB, batch_end - s + 1);
         for (int t = max(0, batch_end - wbin); t < nb; t++) {
+            const float4 cn = sm.con[t];
+            if (!((__float_as_uint(cn.w) >> warp) & 1u)) continue;   // no pixel of this warp takes it
             const int sidx = batch_end - t;
             const float4 xo = sm.xyo[t];
-            const float4 cn = sm.con[t];
             bool valid = sidx <= ps.bin_final;
             float dx = 0.f, dy = 0.f, alpha = 0.f;
             if (valid) {

@@ -19,23 +19,27 @@ namespace msplat {
 // kBatch splats staged per round (the tile batch: 128 or 256, one per
 // thread of the first kBatch threads)
 template <int kBatch> struct BatchSmem {
-    float4 xyo[kBatch];   // x, y, opacity
+    float4 xyo[kBatch];   // x, y, opacity, bits of the warps the splat reaches (warp_reach)
     float4 con[kBatch];   // conic
     float4 rgb[kBatch];   // clamped colour max(raw + 0.5, 0)
 };
 
+// (px, py): this thread's pixel
 template <int kBatch>
-__device__ __forceinline__ void load_batch(BatchSmem<kBatch> &sm, const RasterArgs &a, int idx, int end) {
+__device__ __forceinline__ void load_batch(BatchSmem<kBatch> &sm, const RasterArgs &a, int idx, int end, float px,
+                                           float py) {
     const int t = threadIdx.x;
     if (t < kBatch && idx < end) {
         const SplatRec r = isect_record(a.isect_ids, a.rec, a.n, idx);
-        sm.xyo[t] = r.a;
+        const float ox = px - (float)tile_px(t), oy = py - (float)tile_py(t);   // the tile's first pixel
+        sm.xyo[t] = make_float4(r.a.x, r.a.y, r.a.z, __uint_as_float(warp_reach(r.a.x, r.a.y, r.b.w, r.c.w, ox, oy)));
         sm.con[t] = r.b;
         sm.rgb[t] = make_float4(fmaxf(r.c.x + 0.5f, 0.f), fmaxf(r.c.y + 0.5f, 0.f), fmaxf(r.c.z + 0.5f, 0.f), 0.f);
     }
 }
 
-// Walks [s, e) for this pixel; the whole CTA iterates together.
+// Walks [s, e) for this pixel; the whole CTA iterates together.  A warp
+// skips the splats that cannot reach its 8x4 block.
 // done: in/out per-thread flag; returns (T, C, last).
 template <int kBatch>
 __device__ __forceinline__ void composite_range(BatchSmem<kBatch> &sm, const RasterArgs &a, int s, int e, float px,
@@ -44,14 +48,16 @@ __device__ __forceinline__ void composite_range(BatchSmem<kBatch> &sm, const Ras
     T = 1.f;
     C = make_float3(0.f, 0.f, 0.f);
     last = s - 1;
+    const int warp = threadIdx.x >> 5;
     for (int b0 = s; b0 < e; b0 += kBatch) {
         if (__syncthreads_count(done) == kTileThreads) break;
-        load_batch<kBatch>(sm, a, b0 + (int)threadIdx.x, e);
+        load_batch<kBatch>(sm, a, b0 + (int)threadIdx.x, e, px, py);
         __syncthreads();
         if (done) continue;
         const int nb = min(kBatch, e - b0);
         for (int t = 0; t < nb; t++) {
             const float4 xo = sm.xyo[t];
+            if (!((__float_as_uint(xo.w) >> warp) & 1u)) continue;
             const float4 cn = sm.con[t];
             const float dx = xo.x - px, dy = xo.y - py;
             const float sigma = __fmaf_rn(0.5f, __fmaf_rn(cn.x, dx * dx, cn.z * dy * dy), cn.y * dx * dy);
@@ -106,7 +112,7 @@ template <bool kViews> __device__ __forceinline__ TilePixel tile_pixel(const Ras
 }
 
 template <bool kViews, int kBatch>
-__global__ void __launch_bounds__(kTileThreads) k_raster_fwd(RasterArgs a) {
+__global__ void __launch_bounds__(kTileThreads, 8) k_raster_fwd(RasterArgs a) {
     __shared__ BatchSmem<kBatch> sm;
     const int tile = blockIdx.x + a.tile_lo;
     const TilePixel tp = tile_pixel<kViews>(a, tile);

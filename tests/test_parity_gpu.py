@@ -131,6 +131,35 @@ def test_edge_cases(small):
         assert rel_l2(upd_e, upd_o) <= GRAD_TOL, k
 
 
+@pytest.mark.parametrize("raster_mode", [0, 1])
+def test_needles_and_faint_splats(small, raster_mode):
+    """Warp culling by each splat's reach box at its edges: needle-thin
+    Gaussians (scales e^-1.5 by e^-8, random rotations: conics close to
+    singular), huge ones, and opacities on both sides of the 1/255 cut.
+    Tile lists, last contributors and the image equal the oracle's (which
+    tests every pixel), gradients within the usual bar."""
+    sc, cam, gt, init = small
+    rng = np.random.default_rng(7)
+    g = init.copy()
+    n = g.n
+    k = rng.integers(0, 3, n)
+    sc3 = np.full((n, 3), -8.0, np.float32)
+    sc3[np.arange(n), k] = rng.uniform(-3.0, -1.5, n)
+    big = rng.random(n) < 0.01
+    sc3[big] = rng.uniform(-1.5, -0.5, (int(big.sum()), 3))
+    g.scales[:] = sc3
+    cut = np.log(1.0 / 254.0)   # logit of 1/255
+    g.opacities[:, 0] = np.where(rng.random(n) < 0.5, cut + rng.normal(0.0, 0.05, n),
+                                 rng.uniform(-7.0, 6.0, n)).astype(np.float32)
+    step = E.step_scalars(1, 1, width=cam.width, height=cam.height)
+    step["degrees_to_use"] = 3
+    eo, res = run_pair(g, cam, gt, step, raster_mode=raster_mode, precs=(32,))
+    r32 = res[32]
+    _check_forward(eo, r32, g.n)
+    for key in ("v_xy", "v_conic", "v_colors", "v_opacity", "v_mean3d", "v_scale"):
+        assert rel_l2(eo[key], r32[key]) <= GRAD_TOL, key
+
+
 def test_empty_scene(small):
     sc, cam, gt, init = small
     g = S.GaussianSet(*(a[:0].copy() for a in init.arrays()))
