@@ -138,12 +138,11 @@ int msplat_image_read(const char *path, float *rgb, int *width, int *height);
  * No counterpart in the reference: it is for callers that cannot call
  * cudaMalloc (a host application or server that owns all device memory
  * through its own allocator, or a loop that cannot take cudaMalloc's
- * implicit synchronisation).  The same kernels as the training step; their
- * scratch (24 floats per pixel) and step scalars live in the library's static
- * device arrays, so images are limited to 512 * 512 = 262,144 pixels (larger
- * sizes return -3 with a message).  All calls on a device share those arrays:
- * calls that overlap on the GPU race.  The first call on a device looks up
- * the arrays' addresses; make it before any stream capture.
+ * implicit synchronisation).  The same kernel as the training step, which
+ * keeps its intermediates in shared memory; the three step scalars live in
+ * the library's static device copy, so any image size works.  All calls on a
+ * device share that copy: calls that overlap on the GPU race.  The first call
+ * on a device looks up its address; make it before any stream capture.
  * img: device float [H,W,3]; gt: device uint8 [H,W,3]; mask: device uint8
  * [H,W] or NULL; v_img: device float [H,W,3] (out); loss_sum: device float
  * (out, loss_sum / (H*W) is the loss); stream: cudaStream_t or NULL.

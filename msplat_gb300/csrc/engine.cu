@@ -304,7 +304,7 @@ class Engine {
         LossArgs la{};
         la.vt = vt; la.num_tiles = T; la.sp = pa.sp; la.img = ra.out_img;
         la.gt = nullptr; la.mask = nullptr;   // read from StepParams (see common.cuh)
-        la.hbuf = ptr<float>("hbuf"); la.dbuf = ptr<float>("dbuf"); la.v_img = ptr<float>("v_img");
+        la.v_img = ptr<float>("v_img");
         la.loss_sum = ptr<float>("loss_sum"); la.nan_counts = pa.nan_counts;
         launch_loss(la, stream_);
         debug_sync(stream_, "loss");
@@ -708,8 +708,6 @@ class Engine {
         alloc("out_img", (size_t)P * 12);
         alloc("final_T", (size_t)P * 4);
         alloc("final_idx", (size_t)P * 4);
-        alloc("hbuf", (size_t)P * 15 * 4);
-        alloc("dbuf", (size_t)P * 9 * 4);
         alloc("v_img", (size_t)P * 12);
         cap_pixels_ = P;
     }

@@ -122,8 +122,6 @@ struct LossArgs {
     const StepParams *sp;   // [views]
     const float *img;
     const uint8_t *gt, *mask;   // one view: override StepParams' target and mask (nullable)
-    float *hbuf;            // [15, P] channel-planar moments, P = pixels of all views
-    float *dbuf;            // [9, P] horizontally convolved fields
     float *v_img;           // [P, 3]
     float *loss_sum;        // [views]
     unsigned *nan_counts;

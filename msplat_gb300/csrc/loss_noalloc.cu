@@ -5,20 +5,17 @@
 // memory — an application with its own pool allocator, a serving or training
 // process that has already reserved the GPU's memory, or a loop that must not
 // take cudaMalloc's implicit device-wide synchronisation.  Such callers pass
-// only their inputs and outputs; the loss's scratch (15 moment planes and 9
-// derivative-field planes per pixel) and its three step scalars live in this
-// file's static device arrays, which every GPU that loads the library holds
-// until the process exits.
+// only their inputs and outputs.  The loss kernel keeps all its intermediates
+// in shared memory, so the only device state is the three step scalars, in
+// this file's static device copy of StepParams, which every GPU that loads
+// the library holds until the process exits.  Any image size.
 //
-// Limit: at most kNoAllocMaxPixels = 512 * 512 = 262,144 pixels per image
-// (24 floats per pixel: 25.2 MB of scratch).  Larger images are rejected.
+// Sharing: every call on a device uses the same scalars, rewritten by each
+// call before its kernel runs, and each call zeroes the caller's loss
+// output, so no state carries over between calls — but calls that overlap on
+// the GPU (different streams, no ordering) race on the scalars.
 //
-// Sharing: every call on a device uses the same arrays, which keep the last
-// call's contents.  Each call rewrites all the scratch it reads and zeroes the
-// caller's loss output, so no state carries over between calls — but calls
-// that overlap on the GPU (different streams, no ordering) race on the arrays.
-//
-// Set-up: the first call on each device looks up the arrays' device addresses
+// Set-up: the first call on each device looks up the scalars' device address
 // (cudaGetSymbolAddress) with that device current; make that first call
 // before any stream capture.
 #include <cstdio>
@@ -31,39 +28,28 @@
 
 namespace msplat {
 
-constexpr long long kNoAllocMaxPixels = 512LL * 512LL;
-constexpr int kNoAllocPlanes = 15 + 9;
-
-static __device__ __align__(256) float g_noalloc_scratch[kNoAllocPlanes * kNoAllocMaxPixels];
 static __device__ __align__(256) StepParams g_noalloc_params;
 
 struct NoAllocDevice {
     bool ready = false;
-    float *scratch = nullptr;
     StepParams *params = nullptr;
 };
 
 static NoAllocDevice g_noalloc_dev[64];
 static std::mutex g_noalloc_mu;
 
-// Device addresses of this device's copies of the arrays (looked up once per
-// device; host code must not use the symbols' host-side names as addresses).
+// Device address of this device's copy of the scalars (looked up once per
+// device; host code must not use the symbol's host-side name as an address).
 static int noalloc_setup(int dev, NoAllocDevice &out) {
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
     NoAllocDevice &d = g_noalloc_dev[dev];
     if (!d.ready) {
-        void *s = nullptr, *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&s, g_noalloc_scratch);
-        if (e != cudaSuccess) {
-            fprintf(stderr, "msplat_loss_ssim_l1_noalloc: cudaGetSymbolAddress(scratch): %s\n", cudaGetErrorString(e));
-            return -4;
-        }
-        e = cudaGetSymbolAddress(&p, g_noalloc_params);
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_params);
         if (e != cudaSuccess) {
             fprintf(stderr, "msplat_loss_ssim_l1_noalloc: cudaGetSymbolAddress(params): %s\n", cudaGetErrorString(e));
             return -4;
         }
-        d.scratch = static_cast<float *>(s);
         d.params = static_cast<StepParams *>(p);
         d.ready = true;
     }
@@ -79,11 +65,8 @@ extern "C" int msplat_loss_ssim_l1_noalloc(const float *img, const uint8_t *gt, 
     using namespace msplat;
     if (!img || !gt || !v_img || !loss_sum) return -1;
     if (width <= 0 || height <= 0) return -2;
-    const long long P = (long long)width * height;
-    if (P > kNoAllocMaxPixels) {
-        fprintf(stderr,
-                "msplat_loss_ssim_l1_noalloc: %d x %d = %lld pixels exceeds the no-allocation limit of %lld pixels\n",
-                width, height, P, kNoAllocMaxPixels);
+    if ((long long)width * height > 0x7fffffffLL || (height + 31) / 32 > 65535) {
+        fprintf(stderr, "msplat_loss_ssim_l1_noalloc: %d x %d is beyond the kernel's grid\n", width, height);
         return -3;
     }
     int dev = 0;
@@ -112,8 +95,6 @@ extern "C" int msplat_loss_ssim_l1_noalloc(const float *img, const uint8_t *gt, 
     la.img = img;
     la.gt = gt;
     la.mask = mask;
-    la.hbuf = d.scratch;             // 15 planes of P floats
-    la.dbuf = d.scratch + 15 * P;    // 9 planes of P floats
     la.v_img = v_img;
     la.loss_sum = loss_sum;
     la.nan_counts = nullptr;

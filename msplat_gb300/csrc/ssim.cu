@@ -1,17 +1,24 @@
 // Training loss L = w * (1 - mean SSIM) + (1 - w) * mean |x - gt| and its
-// image gradient, as three separable passes over 16x16 pixel tiles:
-//   1. horizontal 11-tap moments of (gt, x, gt^2, x^2, gt*x), zero padding
-//   2. vertical moments -> SSIM, L1, loss sum and the derivative fields
-//      (f1, f2, f3), then the horizontal transpose convolution of the fields
-//   3. vertical transpose convolution -> dL/dx
-// Follows ssim_h_fwd_kernel, ssim_fused_v_fwd_h_bwd_kernel and
-// ssim_v_bwd_kernel (msplat_metal.metal:3388-3450, 3563-3681, 3764-3850),
-// including their treatment of window centres in the out-of-image columns a
-// border tile reaches (fields from zero moments).  Intermediates are stored
-// channel-planar so every tile load and store is coalesced.  The 16x16 blocks
-// are the tiles: one launch per pass covers every view of the step (the
-// rendered image, the planes and dL/dx are indexed by global pixel, each
-// view's target and mask by its own pixel).
+// image gradient in one kernel: one CTA per 32x32 block of output pixels,
+// the three channels in turn, everything between the image and dL/dx in
+// shared memory (no intermediate planes in HBM):
+//   load    target and render over the block plus a 10-pixel halo (once)
+//   A       vertical 11-tap moments of (gt, x, gt^2, x^2, gt*x) at the 42
+//           window-centre rows, every input column (zero padding)
+//   B       horizontal 11-tap moments at the 42x42 window centres -> SSIM,
+//           L1 and the derivative fields (f1, f2, f3)
+//   C       horizontal transpose convolution of the fields
+//   D       vertical transpose convolution -> dL/dx of the block
+// The loss and gradient are those of ssim_h_fwd_kernel,
+// ssim_fused_v_fwd_h_bwd_kernel and ssim_v_bwd_kernel
+// (msplat_metal.metal:3388-3450, 3563-3681, 3764-3850) with their edge
+// rules: moments at window centres in out-of-image columns are zero (the
+// reference's horizontal moments exist only inside the image) and their
+// fields still enter the horizontal transpose convolution, centres in
+// out-of-image rows contribute nothing, and the loss sum keeps the
+// reference's 16x16-tile partition (loss_counted).  One launch covers every view of the
+// step (blocks are numbered view by view; the render and dL/dx are indexed
+// by global pixel, each view's target and mask by its own pixel).
 #include "common.cuh"
 #include "kernels.h"
 
@@ -19,235 +26,304 @@ namespace msplat {
 
 __constant__ float kGauss[11];
 constexpr float kC1 = 0.0001f, kC2 = 0.0009f;
-constexpr int kS = 16, kHalo = 5, kSpan = kS + 2 * kHalo;   // 26
 
 // Target and mask: the arguments' when set (one view), else the view's in StepParams.
 __device__ __forceinline__ const uint8_t *step_gt(const LossArgs &a, int v) { return a.gt ? a.gt : a.sp[v].gt; }
 __device__ __forceinline__ const uint8_t *step_mask(const LossArgs &a, int v) { return a.gt ? a.mask : a.sp[v].mask; }
 
-// The CTA's block: view, geometry, block origin (pixels).  kViews: the grid
-// is the global tile range of several views; false: one view, a 2D grid of
-// its blocks, geometry straight from the parameter bank.
-struct LossBlock {
+constexpr int kFB = 32;              // output block edge
+constexpr int kFIn = kFB + 20;       // 52: input rows / columns (halo 10)
+constexpr int kFF = kFB + 10;        // 42: window-centre rows / columns (halo 5)
+
+// Padded row strides keep the column-wise and row-wise walks conflict-free.
+struct FusedSmem {
+    float r[3][kFIn + 2][kFIn + 1];      // render, channel-planar, zero outside the image (+2 pad rows)
+    uint8_t g[3][kFIn + 2][kFIn + 4];    // target, channel-planar, zero outside the image (+2 pad rows)
+    union {
+        float v[5][kFF][kFIn + 1];   // A: vertical moments [moment][centre row][input column]
+        float dh[3][kFF][kFB + 1];   // C: horizontally transposed fields [field][centre row][output column]
+    } u;
+    float f[3][kFF][kFF + 1];        // B: fields at the window centres
+    float red[8];
+};
+
+struct FusedBlock {
     int view, W, H, x0, y0;
     long long pb;   // global index of the view's pixel 0
 };
-template <bool kViews> __device__ __forceinline__ LossBlock loss_block(const LossArgs &a) {
-    LossBlock b;
+
+// kViews: blocks numbered view by view over every view of the step; false:
+// one view, a 2D grid, geometry from the parameter bank
+template <bool kViews> __device__ __forceinline__ FusedBlock fused_block(const LossArgs &a) {
+    FusedBlock b;
     if (!kViews) {
         b.view = 0;
         b.W = a.vt.width[0];
         b.H = a.vt.height[0];
-        b.x0 = blockIdx.x * kS;
-        b.y0 = blockIdx.y * kS;
+        b.x0 = blockIdx.x * kFB;
+        b.y0 = blockIdx.y * kFB;
         b.pb = 0;
         return b;
     }
-    const int tile = blockIdx.x;
-    b.view = view_of_tile(a.vt, tile);
-    const ViewGeom vg = view_geom(a.vt, b.view);
-    const int lt = tile - vg.tile_base;
+    const int blk = blockIdx.x;
+    int v = 0, base = 0, run = 0;
+#pragma unroll
+    for (int k = 0; k < kMaxViews; k++) {
+        if (k < a.vt.count) {
+            if (blk >= run) { v = k; base = run; }
+            run += ((a.vt.width[k] + kFB - 1) / kFB) * ((a.vt.height[k] + kFB - 1) / kFB);
+        }
+    }
+    const ViewGeom vg = view_geom(a.vt, v);
+    const int bxn = (vg.width + kFB - 1) / kFB, lb = blk - base;
+    b.view = v;
     b.W = vg.width;
     b.H = vg.height;
-    b.x0 = (lt % vg.tiles_x) * kS;
-    b.y0 = (lt / vg.tiles_x) * kS;
+    b.x0 = (lb % bxn) * kFB;
+    b.y0 = (lb / bxn) * kFB;
     b.pb = vg.pix_base;
     return b;
 }
 
-template <bool kViews>
-__global__ void __launch_bounds__(256) k_ssim_h(LossArgs a) {
-    __shared__ float sg[3][kS][kSpan], sr[3][kS][kSpan];
-    const LossBlock lb = loss_block<kViews>(a);
-    const uint8_t *gt = step_gt(a, lb.view);
-    const int W = lb.W, H = lb.H;
-    const int bx = lb.x0 - kHalo, by = lb.y0;
-    const int tid = threadIdx.x;
-    for (int i = tid; i < kS * kSpan; i += 256) {
-        const int sy = i / kSpan, sx = i % kSpan;
-        const int gy = by + sy, gx = bx + sx;
-        const bool in = gx >= 0 && gx < W && gy < H;
-        const size_t p = in ? ((size_t)gy * W + gx) : 0;
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-            sg[c][sy][sx] = in ? (float)gt[3 * p + c] * (1.0f / 255.0f) : 0.f;
-            sr[c][sy][sx] = in ? a.img[3 * (lb.pb + p) + c] : 0.f;
-        }
-    }
-    __syncthreads();
-    const int lx = tid & 15, ly = tid >> 4;
-    const int x = lb.x0 + lx, y = by + ly;
-    if (x >= W || y >= H) return;
-    const size_t P = (size_t)a.vt.pixels, p = lb.pb + (size_t)y * W + x;
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-        float mx = 0.f, my = 0.f, sx = 0.f, sy = 0.f, cr = 0.f;
-#pragma unroll
-        for (int d = 0; d < 11; d++) {
-            const float w = kGauss[d], g = sg[c][ly][lx + d], r = sr[c][ly][lx + d];
-            mx += w * g; my += w * r; sx += w * g * g; sy += w * r * r; cr += w * g * r;
-        }
-        a.hbuf[(c * 5 + 0) * P + p] = mx;
-        a.hbuf[(c * 5 + 1) * P + p] = my;
-        a.hbuf[(c * 5 + 2) * P + p] = sx;
-        a.hbuf[(c * 5 + 3) * P + p] = sy;
-        a.hbuf[(c * 5 + 4) * P + p] = cr;
-    }
+static int fused_blocks(const ViewTable &vt) {
+    int nb = 0;
+    for (int k = 0; k < vt.count; k++) nb += ((vt.width[k] + kFB - 1) / kFB) * ((vt.height[k] + kFB - 1) / kFB);
+    return nb;
+}
+
+// Whether the reference's loss sum includes window centre (x, y) of the
+// image.  It sums per thread of a 16x16 tile: thread t evaluates centres t
+// and t + 256 of the tile's 16 x 26 centre grid (its own rows, columns with a
+// 5-pixel halo), and only a thread whose own pixel lies in the image adds
+// what it evaluated (.metal:3598-3671).  Centres of full tiles always count;
+// in a partial edge tile some in-image centres fall to threads outside.
+__device__ __forceinline__ bool loss_counted(int x, int y, int W, int H) {
+    const int i = (y & 15) * 26 + (x & 15) + 5;
+    const int t = i < 256 ? i : i - 256;
+    return (x & ~15) + (t & 15) < W && (y & ~15) + (t >> 4) < H;
 }
 
 template <bool kViews>
-__global__ void __launch_bounds__(256, 6) k_ssim_fields(LossArgs a) {
-    __shared__ float hp[5][kSpan][kSpan];
-    __shared__ float mv[5][kS][kSpan];   // vertical moments at the window centres
-    __shared__ float fl[3][kS][kSpan];
-    __shared__ float red[8];
-    const LossBlock lb = loss_block<kViews>(a);
-    const int W = lb.W, H = lb.H;
-    const size_t P = (size_t)a.vt.pixels;
-    const int bx = lb.x0 - kHalo, by = lb.y0 - kHalo;
-    const int tid = threadIdx.x, lx = tid & 15, ly = tid >> 4;
-    const StepParams &sp = a.sp[lb.view];
-    const uint8_t *gt = step_gt(a, lb.view), *mask = step_mask(a, lb.view);
-    const float sw = sp.ssim_weight;
-    float ssim_acc = 0.f, l1_acc = 0.f;
-    unsigned nwin = 0;
-    for (int c = 0; c < 3; c++) {
-        for (int i = tid; i < kSpan * kSpan; i += 256) {
-            const int sy = i / kSpan, sx = i % kSpan;
-            const int gy = by + sy, gx = bx + sx;
-            const bool in = gx >= 0 && gx < W && gy >= 0 && gy < H;
-            const size_t p = in ? lb.pb + ((size_t)gy * W + gx) : 0;
+__global__ void __launch_bounds__(256, 2) k_ssim_fused(LossArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    FusedSmem &sm = *reinterpret_cast<FusedSmem *>(smem_raw);
+    const FusedBlock fb = fused_block<kViews>(a);
+    const int W = fb.W, H = fb.H, X0 = fb.x0, Y0 = fb.y0;
+    const StepParams &sp = a.sp[fb.view];
+    const uint8_t *gt = step_gt(a, fb.view), *mask = step_mask(a, fb.view);
+    const bool has_mask = sp.has_mask != 0;
+    const float sw = sp.ssim_weight, invn = sp.loss_inv_n;
+    const int tid = threadIdx.x;
+    const int dx_ = tid & 31, dy0 = (tid >> 5) * 4;   // D: output column, first of four output rows
+    float ssim_acc = 0.f, l1_acc = 0.f, inside = 0.f;
+    unsigned nwin = 0, nbad = 0;
+
+    // the block's render and target with their halo, all three channels:
+    // each row's 52 pixels are 156 contiguous floats / bytes.  Eight loads of
+    // each kind in flight per thread, then the shared-memory stores.
+    constexpr int kLoadElems = kFIn * kFIn * 3, kLoadUnroll = 8;
+    for (int base = 0; base < kLoadElems; base += 256 * kLoadUnroll) {
+        float rv[kLoadUnroll];
+        uint32_t gv[kLoadUnroll];
 #pragma unroll
-            for (int f = 0; f < 5; f++) hp[f][sy][sx] = in ? a.hbuf[(c * 5 + f) * P + p] : 0.f;
-        }
-        __syncthreads();
-        // vertical 11-tap pass, one (moment, column) per thread: the 26 inputs
-        // of the column are read once into registers for all 16 outputs
-        if (tid < 5 * kSpan) {
-            const int f = tid / kSpan, fx = tid % kSpan;
-            float col[kSpan];
-#pragma unroll
-            for (int r = 0; r < kSpan; r++) col[r] = hp[f][r][fx];
-#pragma unroll
-            for (int fy = 0; fy < kS; fy++) {
-                float acc = 0.f;
-#pragma unroll
-                for (int k = 0; k < 11; k++) acc += kGauss[k] * col[fy + k];
-                mv[f][fy][fx] = acc;
+        for (int u = 0; u < kLoadUnroll; u++) {
+            const int i = base + u * 256 + tid;
+            const int iy = i / (kFIn * 3), e = i - iy * (kFIn * 3);
+            const int ix = e / 3, c = e - ix * 3;
+            const int y = Y0 - 10 + iy, x = X0 - 10 + ix;
+            rv[u] = 0.f;
+            gv[u] = 0;
+            if (i < kLoadElems && x >= 0 && x < W && y >= 0 && y < H) {
+                const size_t pl = (size_t)y * W + x;
+                gv[u] = gt[3 * pl + c];
+                rv[u] = a.img[3 * (fb.pb + pl) + c];
             }
         }
-        __syncthreads();
-        for (int i = tid; i < kS * kSpan; i += 256) {
-            const int fy = i / kSpan, fx = i % kSpan;     // field row (output rows), column incl. halo
-            const int gx = bx + fx, gy = lb.y0 + fy;
-            float m[5];
 #pragma unroll
-            for (int f = 0; f < 5; f++) m[f] = mv[f][fy][fx];
-            float mval = 1.f;
-            const bool in_img = gx >= 0 && gx < W && gy < H;
-            if (sp.has_mask && in_img && mask[(size_t)gy * W + gx] < 128) mval = 0.f;
-            if (!(finite_bits(m[0]) && finite_bits(m[1]) && finite_bits(m[2]) && finite_bits(m[3]) && finite_bits(m[4]))) {
-                fl[0][fy][fx] = fl[1][fy][fx] = fl[2][fy][fx] = 0.f;
-                nwin++;
-                continue;
-            }
-            const float mu_x = m[0], mu_y = m[1];
-            const float sxq = fmaxf(m[2] - mu_x * mu_x, 0.f), syq = fmaxf(m[3] - mu_y * mu_y, 0.f);
-            const float sxy = m[4] - mu_x * mu_y;
-            const float A = 2.f * mu_x * mu_y + kC1, B = 2.f * sxy + kC2;
-            const float Cd = mu_x * mu_x + mu_y * mu_y + kC1, D = sxq + syq + kC2;
-            // two fast reciprocals (within 2 ulp) in place of four IEEE divisions
-            const float rCd = __fdividef(1.f, Cd), rD = __fdividef(1.f, D);
-            const float iCD = rCd * rD;
-            const float dmu = 2.f * B * (mu_x * Cd - A * mu_y) * iCD * rCd;
-            const float dsyq = -A * B * iCD * rD, dsxy = 2.f * A * iCD;
-            fl[0][fy][fx] = mval * (dmu - 2.f * mu_y * dsyq - mu_x * dsxy);
-            fl[1][fy][fx] = mval * (2.f * dsyq);
-            fl[2][fy][fx] = mval * dsxy;
-            if (fx >= kHalo && fx < kHalo + kS && in_img) {
-                ssim_acc += mval * (A * B) * iCD;
-                const size_t p = (size_t)gy * W + gx;
-                l1_acc += mval * fabsf((float)gt[3 * p + c] * (1.0f / 255.0f) - a.img[3 * (lb.pb + p) + c]);
+        for (int u = 0; u < kLoadUnroll; u++) {
+            const int i = base + u * 256 + tid;
+            if (i < kLoadElems) {
+                const int iy = i / (kFIn * 3), e = i - iy * (kFIn * 3);
+                const int ix = e / 3, c = e - ix * 3;
+                sm.r[c][iy][ix] = rv[u];
+                sm.g[c][iy][ix] = (uint8_t)gv[u];
             }
         }
-        __syncthreads();
-        const int x = lb.x0 + lx, y = lb.y0 + ly;
-        if (x < W && y < H) {
-            float h1 = 0.f, h2 = 0.f, h3 = 0.f;
-#pragma unroll
-            for (int d = 0; d < 11; d++) {
-                const float w = kGauss[10 - d];
-                h1 += w * fl[0][ly][lx + d];
-                h2 += w * fl[1][ly][lx + d];
-                h3 += w * fl[2][ly][lx + d];
-            }
-            const size_t p = lb.pb + (size_t)y * W + x;
-            a.dbuf[(c * 3 + 0) * P + p] = h1;
-            a.dbuf[(c * 3 + 1) * P + p] = h2;
-            a.dbuf[(c * 3 + 2) * P + p] = h3;
-        }
-        __syncthreads();
     }
-    // loss: each thread whose own pixel is in the image adds w*(1 - s/3) + (1-w)*l/3
-    // over the window centres it evaluated (the reference's partition, so a
-    // partial edge tile sums the same terms)
-    const int x = lb.x0 + lx, y = lb.y0 + ly;
-    float v = (x < W && y < H) ? sw * (1.f - ssim_acc / 3.f) + (1.f - sw) * l1_acc / 3.f : 0.f;
+    for (int i = tid; i < 3 * 2 * kFIn; i += 256) {   // the pad rows A reads past the last input row
+        const int c = i / (2 * kFIn), e = i - c * 2 * kFIn;
+        sm.r[c][kFIn + e / kFIn][e % kFIn] = 0.f;
+        sm.g[c][kFIn + e / kFIn][e % kFIn] = 0;
+    }
+    __syncthreads();
+
+    for (int c = 0; c < 3; c++) {
+        // A: (input column, 11 centre rows) per item; the 21 inputs and their
+        // products in registers.  The target stays in 0..255 here (exact in
+        // float); its moments are scaled by 1/255 and 1/255^2 at the end.
+        for (int it = tid; it < kFIn * 4; it += 256) {
+            const int ix = it % kFIn, s = it / kFIn;
+            const int vy0 = 11 * s, n = min(11, kFF - vy0);
+            float gv[21], rv[21], gg[21], rr[21], gr[21];
+#pragma unroll
+            for (int j = 0; j < 21; j++) {
+                gv[j] = (float)sm.g[c][vy0 + j][ix];
+                rv[j] = sm.r[c][vy0 + j][ix];
+                gg[j] = gv[j] * gv[j];
+                rr[j] = rv[j] * rv[j];
+                gr[j] = gv[j] * rv[j];
+            }
+#pragma unroll
+            for (int k = 0; k < 11; k++) {
+                if (k < n) {
+                    float m0 = 0.f, m1 = 0.f, m2 = 0.f, m3 = 0.f, m4 = 0.f;
+#pragma unroll
+                    for (int d = 0; d < 11; d++) {
+                        const float w = kGauss[d];
+                        m0 += w * gv[k + d];
+                        m1 += w * rv[k + d];
+                        m2 += w * gg[k + d];
+                        m3 += w * rr[k + d];
+                        m4 += w * gr[k + d];
+                    }
+                    sm.u.v[0][vy0 + k][ix] = m0 * (1.0f / 255.0f);
+                    sm.u.v[1][vy0 + k][ix] = m1;
+                    sm.u.v[2][vy0 + k][ix] = m2 * (1.0f / 65025.0f);
+                    sm.u.v[3][vy0 + k][ix] = m3;
+                    sm.u.v[4][vy0 + k][ix] = m4 * (1.0f / 255.0f);
+                }
+            }
+        }
+        __syncthreads();
+
+        // B: (centre row, 7 centre columns) per item -> moments, SSIM, fields
+        for (int it = tid; it < kFF * 6; it += 256) {
+            const int fy = it % kFF, s = it / kFF, fx0 = 7 * s;
+            float m[5][7];
+#pragma unroll
+            for (int f = 0; f < 5; f++) {
+                float row[17];
+#pragma unroll
+                for (int j = 0; j < 17; j++) row[j] = sm.u.v[f][fy][fx0 + j];
+#pragma unroll
+                for (int k = 0; k < 7; k++) {
+                    float acc = 0.f;
+#pragma unroll
+                    for (int d = 0; d < 11; d++) acc += kGauss[d] * row[k + d];
+                    m[f][k] = acc;
+                }
+            }
+            const int yc = Y0 - 5 + fy;
+            const bool in_row = yc >= 0 && yc < H;
+            const bool own_row = fy >= 5 && fy < 5 + kFB;
+#pragma unroll
+            for (int k = 0; k < 7; k++) {
+                const int fx = fx0 + k, xc = X0 - 5 + fx;
+                const bool in_col = xc >= 0 && xc < W;
+                const bool in_img = in_row && in_col;
+                const bool own = in_img && own_row && fx >= 5 && fx < 5 + kFB;
+                float mu_x = m[0][k], mu_y = m[1][k], q_x = m[2][k], q_y = m[3][k], q_xy = m[4][k];
+                if (!in_col) mu_x = mu_y = q_x = q_y = q_xy = 0.f;
+                float f1 = 0.f, f2 = 0.f, f3 = 0.f;
+                if (!(finite_bits(mu_x) && finite_bits(mu_y) && finite_bits(q_x) && finite_bits(q_y) &&
+                      finite_bits(q_xy))) {
+                    if (own) nwin++;
+                } else {
+                    float mval = 1.f;
+                    if (has_mask && in_img && mask[(size_t)yc * W + xc] < 128) mval = 0.f;
+                    const float sxq = fmaxf(q_x - mu_x * mu_x, 0.f), syq = fmaxf(q_y - mu_y * mu_y, 0.f);
+                    const float sxy = q_xy - mu_x * mu_y;
+                    const float A = 2.f * mu_x * mu_y + kC1, B = 2.f * sxy + kC2;
+                    const float Cd = mu_x * mu_x + mu_y * mu_y + kC1, D = sxq + syq + kC2;
+                    // two fast reciprocals (within 2 ulp) in place of four IEEE divisions
+                    const float rCd = __fdividef(1.f, Cd), rD = __fdividef(1.f, D);
+                    const float iCD = rCd * rD;
+                    const float dmu = 2.f * B * (mu_x * Cd - A * mu_y) * iCD * rCd;
+                    const float dsyq = -A * B * iCD * rD, dsxy = 2.f * A * iCD;
+                    if (in_row) {
+                        f1 = mval * (dmu - 2.f * mu_y * dsyq - mu_x * dsxy);
+                        f2 = mval * (2.f * dsyq);
+                        f3 = mval * dsxy;
+                    }
+                    if (own && loss_counted(xc, yc, W, H)) {
+                        ssim_acc += mval * (A * B) * iCD;
+                        l1_acc += mval * fabsf((float)sm.g[c][fy + 5][fx + 5] * (1.0f / 255.0f) - sm.r[c][fy + 5][fx + 5]);
+                    }
+                }
+                sm.f[0][fy][fx] = f1;
+                sm.f[1][fy][fx] = f2;
+                sm.f[2][fy][fx] = f3;
+            }
+        }
+        __syncthreads();
+
+        // C: (centre row, 8 output columns) per item
+        for (int it = tid; it < kFF * 4; it += 256) {
+            const int fy = it % kFF, ox0 = 8 * (it / kFF);
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                float row[18];
+#pragma unroll
+                for (int t = 0; t < 18; t++) row[t] = sm.f[j][fy][ox0 + t];
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    float acc = 0.f;
+#pragma unroll
+                    for (int d = 0; d < 11; d++) acc += kGauss[10 - d] * row[k + d];
+                    sm.u.dh[j][fy][ox0 + k] = acc;
+                }
+            }
+        }
+        __syncthreads();
+
+        // D: (output column, 4 output rows) per thread -> dL/dx of channel c
+        {
+            float cf[3][4];
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                float col[14];
+#pragma unroll
+                for (int t = 0; t < 14; t++) col[t] = sm.u.dh[j][dy0 + t][dx_];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    float acc = 0.f;
+#pragma unroll
+                    for (int d = 0; d < 11; d++) acc += kGauss[10 - d] * col[k + d];
+                    cf[j][k] = acc;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int y = Y0 + dy0 + k, x = X0 + dx_;
+                if (x < W && y < H) {
+                    const float R = sm.r[c][dy0 + k + 10][dx_ + 10];
+                    const float G = (float)sm.g[c][dy0 + k + 10][dx_ + 10] * (1.0f / 255.0f);
+                    const float mc = (has_mask && mask[(size_t)y * W + x] < 128) ? 0.f : 1.f;
+                    const float vs = cf[0][k] + R * cf[1][k] + G * cf[2][k];
+                    const float vl = mc * ((G > R) ? -1.f : ((G < R) ? 1.f : 0.f));
+                    float v = invn * (-sw * vs + (1.f - sw) * vl);
+                    if (!finite_bits(v)) { nbad++; v = 0.f; }
+                    if (c == 0) inside += 1.f;
+                    a.v_img[3 * (fb.pb + (size_t)y * W + x) + c] = v;
+                }
+            }
+        }
+        __syncthreads();   // the next channel's moments overwrite dh
+    }
+
+    // loss: sum over the block's pixels in the image of w*(1 - s/3) + (1-w)*l/3,
+    // s and l summed over the channels
+    float v = sw * (inside - ssim_acc / 3.f) + (1.f - sw) * l1_acc / 3.f;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if ((tid & 31) == 0) red[tid >> 5] = v;
+    if ((tid & 31) == 0) sm.red[tid >> 5] = v;
     __syncthreads();
     if (tid == 0) {
-        float s = 0.f;
-        for (int k = 0; k < 8; k++) s += red[k];
-        atomicAdd(a.loss_sum + lb.view, s);
+        float t = 0.f;
+        for (int k = 0; k < 8; k++) t += sm.red[k];
+        atomicAdd(a.loss_sum + fb.view, t);
     }
     if (nwin && a.nan_counts) atomicAdd(a.nan_counts + kNanSsimWin, nwin);
-}
-
-template <bool kViews>
-__global__ void __launch_bounds__(256) k_ssim_bwd(LossArgs a) {
-    __shared__ float sh[9][kSpan][kS];
-    const LossBlock lb = loss_block<kViews>(a);
-    const int W = lb.W, H = lb.H;
-    const size_t P = (size_t)a.vt.pixels;
-    const int bx = lb.x0, by = lb.y0 - kHalo;
-    const int tid = threadIdx.x, lx = tid & 15, ly = tid >> 4;
-    for (int i = tid; i < kSpan * kS; i += 256) {
-        const int sy = i / kS, sx = i % kS;
-        const int gy = by + sy, gx = bx + sx;
-        const bool in = gx < W && gy >= 0 && gy < H;
-        const size_t p = in ? lb.pb + ((size_t)gy * W + gx) : 0;
-#pragma unroll
-        for (int f = 0; f < 9; f++) sh[f][sy][sx] = in ? a.dbuf[f * P + p] : 0.f;
-    }
-    __syncthreads();
-    const int x = bx + lx, y = lb.y0 + ly;
-    if (x >= W || y >= H) return;
-    const StepParams &sp = a.sp[lb.view];
-    const uint8_t *gt = step_gt(a, lb.view), *mask = step_mask(a, lb.view);
-    const float sw = sp.ssim_weight, invn = sp.loss_inv_n;
-    const size_t pl = (size_t)y * W + x, p = lb.pb + pl;   // this view's pixel, global pixel
-    float mc = 1.f;
-    if (sp.has_mask && mask[pl] < 128) mc = 0.f;
-    unsigned nbad = 0;
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-        float c1 = 0.f, c2 = 0.f, c3 = 0.f;
-#pragma unroll
-        for (int d = 0; d < 11; d++) {
-            const float w = kGauss[10 - d];
-            c1 += w * sh[c * 3 + 0][ly + d][lx];
-            c2 += w * sh[c * 3 + 1][ly + d][lx];
-            c3 += w * sh[c * 3 + 2][ly + d][lx];
-        }
-        const float r = a.img[3 * p + c], g = (float)gt[3 * pl + c] * (1.0f / 255.0f);
-        const float vs = c1 + r * c2 + g * c3;
-        const float vl = mc * ((g > r) ? -1.f : ((g < r) ? 1.f : 0.f));
-        float v = invn * (-sw * vs + (1.f - sw) * vl);
-        if (!finite_bits(v)) { nbad++; v = 0.f; }
-        a.v_img[3 * p + c] = v;
-    }
     if (nbad && a.nan_counts) atomicAdd(a.nan_counts + kNanVRendered, nbad);
 }
 
@@ -265,15 +341,19 @@ void launch_loss(const LossArgs &a, cudaStream_t s) {
         cudaMemcpyToSymbol(kGauss, w, sizeof(w));
         if (dev >= 0 && dev < 64) g_gauss_ready[dev] = true;
     }
+    static bool attr_set[64] = {false};
+    if (dev < 0 || dev >= 64 || !attr_set[dev]) {
+        cudaFuncSetAttribute(k_ssim_fused<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FusedSmem));
+        cudaFuncSetAttribute(k_ssim_fused<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FusedSmem));
+        if (dev >= 0 && dev < 64) attr_set[dev] = true;
+    }
+    const size_t smem = sizeof(FusedSmem);
     if (a.vt.count > 1) {
-        k_ssim_h<true><<<a.num_tiles, 256, 0, s>>>(a);
-        k_ssim_fields<true><<<a.num_tiles, 256, 0, s>>>(a);
-        k_ssim_bwd<true><<<a.num_tiles, 256, 0, s>>>(a);
+        const int nb = fused_blocks(a.vt);
+        if (nb > 0) k_ssim_fused<true><<<nb, 256, smem, s>>>(a);
     } else {
-        const dim3 grid(a.vt.tiles_x[0], a.vt.tiles_y[0]);
-        k_ssim_h<false><<<grid, 256, 0, s>>>(a);
-        k_ssim_fields<false><<<grid, 256, 0, s>>>(a);
-        k_ssim_bwd<false><<<grid, 256, 0, s>>>(a);
+        const dim3 grid((a.vt.width[0] + kFB - 1) / kFB, (a.vt.height[0] + kFB - 1) / kFB);
+        if (grid.x > 0 && grid.y > 0) k_ssim_fused<false><<<grid, 256, smem, s>>>(a);
     }
 }
 

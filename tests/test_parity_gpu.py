@@ -115,12 +115,17 @@ def test_edge_cases(small):
     g.means[7] = np.array([30.0, 0.0, 0.0])   # far outside / behind
     mask = np.full((cam.height, cam.width), 255, np.uint8)
     mask[40:70, 50:120] = 0
+    mask[140:, 190:] = 0                      # across the bottom-right corner
     step = E.step_scalars(700, 700, width=cam.width, height=cam.height)
     eo, res = run_pair(g, cam, gt, step, mask=mask, precs=(32,))
     r32 = res[32]
     _check_forward(eo, r32, g.n)
     assert eo["radii"][5] == 0
     assert eo["nan_counts"][7] >= 1
+    # loss and dL/dimage on partial edge blocks with a mask (the reference's
+    # loss partition of edge tiles)
+    assert abs(eo["loss"] - r32["loss"]) <= 1e-5 * max(1.0, abs(r32["loss"]))
+    assert rel_l2(eo["v_rendered"], r32["v_rendered"]) <= 1e-5
     for k in ("v_xy", "v_conic", "v_colors", "v_mean3d"):
         assert rel_l2(eo[k], r32[k]) <= GRAD_TOL, k
     for k in E.GROUPS:

@@ -3,10 +3,12 @@ the loss stage of the regular training step (GPU only).
 
 The entry point serves callers that cannot call cudaMalloc (a host that owns
 all device memory through its own allocator, or a loop that cannot take
-cudaMalloc's implicit synchronisation): it keeps its scratch in the library's
-static device arrays.  Two calls in a row must both reproduce the training
-step's image gradient and loss, with the tolerance the parity tests use for
-the image gradient (1e-5 relative L2).  This file is collected last.
+cudaMalloc's implicit synchronisation): its only device state is the step
+scalars, in the library's static device copy.  Two calls in a row must both
+reproduce the training step's image gradient and loss, with the tolerance
+the parity tests use for the image gradient (1e-5 relative L2), on a small
+image with partial edge blocks and on one above 512 x 512 pixels.  This file
+is collected last.
 """
 import ctypes as C
 
@@ -28,7 +30,8 @@ def _rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
 
 
-def test_noalloc_loss_matches_training_step():
+@pytest.mark.parametrize("size", [(203, 150, 130.0), (700, 413, 450.0)])
+def test_noalloc_loss_matches_training_step(size):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
@@ -38,7 +41,7 @@ def test_noalloc_loss_matches_training_step():
     L.msplat_loss_ssim_l1_noalloc.restype = C.c_int
 
     gt_scene = S.gaussians(3000, 11)
-    cam = S.ring_cameras(4, 203, 150, 130.0)[2]          # partial edge tiles
+    cam = S.ring_cameras(4, size[0], size[1], size[2])[2]   # partial edge blocks
     cd = E.camera_dict(cam)
     W, H = cam.width, cam.height
     eng = E.Engine(0)
@@ -49,6 +52,7 @@ def test_noalloc_loss_matches_training_step():
     gt_d = torch.from_numpy(gt).cuda()
     mask = np.full((H, W), 255, np.uint8)
     mask[30:60, 40:90] = 0
+    mask[H - 20:, W - 37:] = 0
     mask_d = torch.from_numpy(mask).cuda()
 
     dg = E.DeviceGaussians(S.init_from_gt(gt_scene, 11))
@@ -78,7 +82,7 @@ def test_noalloc_loss_matches_training_step():
         assert _rel(v, v_ref) <= TOL, f"call {call}: gradient differs"
         assert abs(loss - loss_ref) <= TOL * max(1.0, abs(loss_ref)), f"call {call}: loss {loss} vs {loss_ref}"
 
-    # sizes beyond the static scratch are rejected without touching the GPU
-    rc = L.msplat_loss_ssim_l1_noalloc(img_d.data_ptr(), gt_d.data_ptr(), None, 1297, 840, C.c_float(0.2),
+    # a size beyond the kernel's grid is refused without touching the GPU
+    rc = L.msplat_loss_ssim_l1_noalloc(img_d.data_ptr(), gt_d.data_ptr(), None, 16, 2100000, C.c_float(0.2),
                                        C.c_float(1.0), v_out.data_ptr(), loss_d.data_ptr(), None)
     assert rc == -3
