@@ -199,12 +199,10 @@ class Engine {
 
         auto issue = [&]() {
         // kernels of this step, one launch per stage whatever the views:
-        // projection, the tile-mapping launches (counted where they are
-        // issued), raster (+ merge when chunked), and for training 3 loss
-        // passes, raster backward (+ prefix/suffix), projection backward,
-        // Adam, SGLD
+        // projection, the tile-mapping and loss launches (counted where they
+        // are issued), raster (+ merge when chunked), and for training raster
+        // backward (+ prefix/suffix), projection backward, Adam, SGLD
         launches_ += 1 + (K > 1 ? 2 : 1);
-        if (has_gt) launches_ += 3;
         // (the one-view projection backward is two launches with the optimizer:
         // the VJP, then the SH Adam walk)
         if (has_gt && backward)
@@ -306,7 +304,7 @@ class Engine {
         la.gt = nullptr; la.mask = nullptr;   // read from StepParams (see common.cuh)
         la.v_img = ptr<float>("v_img");
         la.loss_sum = ptr<float>("loss_sum"); la.nan_counts = pa.nan_counts;
-        launch_loss(la, stream_);
+        launches_ += launch_loss(la, stream_);
         debug_sync(stream_, "loss");
         mark(4);
         if (!backward) { mark(5); mark(6); mark(7); mark(8); return; }

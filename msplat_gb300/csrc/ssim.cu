@@ -330,7 +330,7 @@ __global__ void __launch_bounds__(256, 2) k_ssim_fused(LossArgs a) {
 // The window lives in each device's constant bank: upload it once per device.
 static bool g_gauss_ready[64] = {false};
 
-void launch_loss(const LossArgs &a, cudaStream_t s) {
+int launch_loss(const LossArgs &a, cudaStream_t s) {
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64 || !g_gauss_ready[dev]) {
@@ -350,11 +350,14 @@ void launch_loss(const LossArgs &a, cudaStream_t s) {
     const size_t smem = sizeof(FusedSmem);
     if (a.vt.count > 1) {
         const int nb = fused_blocks(a.vt);
-        if (nb > 0) k_ssim_fused<true><<<nb, 256, smem, s>>>(a);
+        if (nb <= 0) return 0;
+        k_ssim_fused<true><<<nb, 256, smem, s>>>(a);
     } else {
         const dim3 grid((a.vt.width[0] + kFB - 1) / kFB, (a.vt.height[0] + kFB - 1) / kFB);
-        if (grid.x > 0 && grid.y > 0) k_ssim_fused<false><<<grid, 256, smem, s>>>(a);
+        if (grid.x == 0 || grid.y == 0) return 0;
+        k_ssim_fused<false><<<grid, 256, smem, s>>>(a);
     }
+    return 1;
 }
 
 }  // namespace msplat
