@@ -50,13 +50,68 @@ __device__ __forceinline__ float2 reach_extent(float x, float y, float opac, flo
     return make_float2(sqrtf(k * c) * (1.f + 1e-5f), sqrtf(k * a) * (1.f + 1e-5f));
 }
 
+// SH colour from the first deg bands (rest: the Gaussian's [15, 3] block, in
+// shared or global memory), in the reference's operation order.
+__device__ __forceinline__ void sh_colour(const float *dc, const float *rest, int deg, float vdx, float vdy,
+                                          float vdz, float col[3]) {
+    const float xx = vdx * vdx, xy = vdx * vdy, xz = vdx * vdz, yy = vdy * vdy, yz = vdy * vdz, zz = vdz * vdz;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        float val = kShC0 * dc[c];
+        if (deg >= 1) {
+            val += kShC1 * (-vdy * rest[0 * 3 + c] + vdz * rest[1 * 3 + c] - vdx * rest[2 * 3 + c]);
+            if (deg >= 2) {
+                val += (kShC2[0] * xy * rest[3 * 3 + c] + kShC2[1] * yz * rest[4 * 3 + c] +
+                        kShC2[2] * (2.f * zz - xx - yy) * rest[5 * 3 + c] + kShC2[3] * xz * rest[6 * 3 + c] +
+                        kShC2[4] * (xx - yy) * rest[7 * 3 + c]);
+                if (deg >= 3) {
+                    val += (kShC3[0] * vdy * (3.f * xx - yy) * rest[8 * 3 + c] + kShC3[1] * xy * vdz * rest[9 * 3 + c] +
+                            kShC3[2] * vdy * (4.f * zz - xx - yy) * rest[10 * 3 + c] +
+                            kShC3[3] * vdz * (2.f * zz - 3.f * xx - 3.f * yy) * rest[11 * 3 + c] +
+                            kShC3[4] * vdx * (4.f * zz - xx - yy) * rest[12 * 3 + c] +
+                            kShC3[5] * vdz * (xx - yy) * rest[13 * 3 + c] +
+                            kShC3[6] * vdx * (xx - 3.f * yy) * rest[14 * 3 + c]);
+                }
+            }
+        }
+        col[c] = val;
+    }
+}
+
+constexpr int kStageFloats = 45;   // 15 SH bases x 3 channels per Gaussian
+
 // kViews: several views (blockIdx.y); false compiles the one-view step with
-// the geometry read straight from the parameter bank
+// the geometry read straight from the parameter bank.  At degree 3 with 15
+// bases each warp first copies its 32 Gaussians' SH rows (32 x 180 contiguous
+// bytes) to shared memory with coalesced loads, 16 bytes a lane when the rows
+// are 16-byte aligned; a lane's row there (45 floats apart) is conflict-free.
 template <bool kViews>
 __global__ void __launch_bounds__(256) k_project_fwd(ProjectArgs a) {
+    __shared__ __align__(16) float stage[8][32 * kStageFloats];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.vt.n) return;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int view = kViews ? (int)blockIdx.y : 0;
+    const bool staged = a.rest_bases == 15 && a.sp[view].degrees_to_use >= 3;   // uniform over the CTA
+    if (staged) {
+        const int i0 = i - lane;
+        const int cnt = min(32, a.vt.n - i0);
+        if (cnt > 0) {
+            const float *src = a.features_rest + (size_t)i0 * kStageFloats;
+            float *dst = stage[wid];
+            const int nf = cnt * kStageFloats;
+            int done = 0;
+            if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+                const int nv = nf >> 2;
+                const float4 *s4 = reinterpret_cast<const float4 *>(src);
+                float4 *d4 = reinterpret_cast<float4 *>(dst);
+                for (int k = lane; k < nv; k += 32) d4[k] = s4[k];
+                done = nv << 2;
+            }
+            for (int k = done + lane; k < nf; k += 32) dst[k] = src[k];
+        }
+        __syncwarp();
+    }
+    if (i >= a.vt.n) return;
     const ViewGeom vg = view_geom(a.vt, view);
     const size_t u = kViews ? (size_t)view * a.vt.n + i : (size_t)i;   // this view's record of Gaussian i
     const StepParams &sp = a.sp[view];
@@ -157,30 +212,9 @@ __global__ void __launch_bounds__(256) k_project_fwd(ProjectArgs a) {
     const float vdx = dx * inv, vdy = dy * inv, vdz = dz * inv;
     const int deg = sp.degrees_to_use;
     const float *dc = a.features_dc + 3 * (size_t)i;
-    const float *rest = a.features_rest + (size_t)a.rest_bases * 3 * i;
-    const float xx = vdx * vdx, xy = vdx * vdy, xz = vdx * vdz, yy = vdy * vdy, yz = vdy * vdz, zz = vdz * vdz;
     float col[3];
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-        float val = kShC0 * dc[c];
-        if (deg >= 1) {
-            val += kShC1 * (-vdy * rest[0 * 3 + c] + vdz * rest[1 * 3 + c] - vdx * rest[2 * 3 + c]);
-            if (deg >= 2) {
-                val += (kShC2[0] * xy * rest[3 * 3 + c] + kShC2[1] * yz * rest[4 * 3 + c] +
-                        kShC2[2] * (2.f * zz - xx - yy) * rest[5 * 3 + c] + kShC2[3] * xz * rest[6 * 3 + c] +
-                        kShC2[4] * (xx - yy) * rest[7 * 3 + c]);
-                if (deg >= 3) {
-                    val += (kShC3[0] * vdy * (3.f * xx - yy) * rest[8 * 3 + c] + kShC3[1] * xy * vdz * rest[9 * 3 + c] +
-                            kShC3[2] * vdy * (4.f * zz - xx - yy) * rest[10 * 3 + c] +
-                            kShC3[3] * vdz * (2.f * zz - 3.f * xx - 3.f * yy) * rest[11 * 3 + c] +
-                            kShC3[4] * vdx * (4.f * zz - xx - yy) * rest[12 * 3 + c] +
-                            kShC3[5] * vdz * (xx - yy) * rest[13 * 3 + c] +
-                            kShC3[6] * vdx * (xx - 3.f * yy) * rest[14 * 3 + c]);
-                }
-            }
-        }
-        col[c] = val;
-    }
+    if (staged) sh_colour(dc, &stage[wid][lane * kStageFloats], deg, vdx, vdy, vdz, col);
+    else sh_colour(dc, a.features_rest + (size_t)a.rest_bases * 3 * i, deg, vdx, vdy, vdz, col);
     // sigmoid(opacity) once per Gaussian (the reference does it per
     // intersection at pack time; same input, same bits)
     const float opac = 1.f / (1.f + det_expf(-a.opacities[i]));
