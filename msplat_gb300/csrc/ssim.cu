@@ -40,10 +40,18 @@ struct FusedSmem {
     float r[3][kFIn + 2][kFIn + 1];      // render, channel-planar, zero outside the image (+2 pad rows)
     uint8_t g[3][kFIn + 2][kFIn + 4];    // target, channel-planar, zero outside the image (+2 pad rows)
     union {
-        float v[5][kFF][kFIn + 1];   // A: vertical moments [moment][centre row][input column]
-        float dh[3][kFF][kFB + 1];   // C: horizontally transposed fields [field][centre row][output column]
+        struct {                     // A: vertical moments [centre row][input column]
+            float2 m01[kFF][kFIn + 1];   // (gt, x)
+            float2 m23[kFF][kFIn + 1];   // (gt^2, x^2)
+            float m4[kFF][kFIn + 1];     // gt * x
+        } v;
+        struct {                     // C: horizontally transposed fields [centre row][output column]
+            float2 f12[kFF][kFB + 1];
+            float f3[kFF][kFB + 1];
+        } dh;
     } u;
-    float f[3][kFF][kFF + 1];        // B: fields at the window centres
+    float2 f12[kFF][kFF + 1];        // B: fields (f1, f2) at the window centres
+    float f3[kFF][kFF + 1];          //    and f3
     float red[8];
 };
 
@@ -159,38 +167,43 @@ __global__ void __launch_bounds__(256, 2) k_ssim_fused(LossArgs a) {
 
     for (int c = 0; c < 3; c++) {
         // A: (input column, 11 centre rows) per item; the 21 inputs and their
-        // products in registers.  The target stays in 0..255 here (exact in
-        // float); its moments are scaled by 1/255 and 1/255^2 at the end.
+        // products in registers, moments in pairs (paired fp32 arithmetic).
+        // The target stays in 0..255 here (exact in float); its moments are
+        // scaled by 1/255 and 1/255^2 at the end.
         for (int it = tid; it < kFIn * 4; it += 256) {
             const int ix = it % kFIn, s = it / kFIn;
             const int vy0 = 11 * s, n = min(11, kFF - vy0);
-            float gv[21], rv[21], gg[21], rr[21], gr[21];
+            float2 gr[21];   // (gt, x), then (gt^2, x^2)
+            float gx[21];    // gt * x
 #pragma unroll
             for (int j = 0; j < 21; j++) {
-                gv[j] = (float)sm.g[c][vy0 + j][ix];
-                rv[j] = sm.r[c][vy0 + j][ix];
-                gg[j] = gv[j] * gv[j];
-                rr[j] = rv[j] * rv[j];
-                gr[j] = gv[j] * rv[j];
+                gr[j] = make_float2((float)sm.g[c][vy0 + j][ix], sm.r[c][vy0 + j][ix]);
+                gx[j] = gr[j].x * gr[j].y;
             }
 #pragma unroll
             for (int k = 0; k < 11; k++) {
                 if (k < n) {
-                    float m0 = 0.f, m1 = 0.f, m2 = 0.f, m3 = 0.f, m4 = 0.f;
+                    float2 m01 = make_float2(0.f, 0.f);
+                    float m4 = 0.f;
 #pragma unroll
                     for (int d = 0; d < 11; d++) {
                         const float w = kGauss[d];
-                        m0 += w * gv[k + d];
-                        m1 += w * rv[k + d];
-                        m2 += w * gg[k + d];
-                        m3 += w * rr[k + d];
-                        m4 += w * gr[k + d];
+                        m01 = __ffma2_rn(make_float2(w, w), gr[k + d], m01);
+                        m4 = fmaf(w, gx[k + d], m4);
                     }
-                    sm.u.v[0][vy0 + k][ix] = m0 * (1.0f / 255.0f);
-                    sm.u.v[1][vy0 + k][ix] = m1;
-                    sm.u.v[2][vy0 + k][ix] = m2 * (1.0f / 65025.0f);
-                    sm.u.v[3][vy0 + k][ix] = m3;
-                    sm.u.v[4][vy0 + k][ix] = m4 * (1.0f / 255.0f);
+                    sm.u.v.m01[vy0 + k][ix] = __fmul2_rn(m01, make_float2(1.0f / 255.0f, 1.f));
+                    sm.u.v.m4[vy0 + k][ix] = m4 * (1.0f / 255.0f);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < 21; j++) gr[j] = __fmul2_rn(gr[j], gr[j]);
+#pragma unroll
+            for (int k = 0; k < 11; k++) {
+                if (k < n) {
+                    float2 m23 = make_float2(0.f, 0.f);
+#pragma unroll
+                    for (int d = 0; d < 11; d++) m23 = __ffma2_rn(make_float2(kGauss[d], kGauss[d]), gr[k + d], m23);
+                    sm.u.v.m23[vy0 + k][ix] = __fmul2_rn(m23, make_float2(1.0f / 65025.0f, 1.f));
                 }
             }
         }
@@ -199,18 +212,39 @@ __global__ void __launch_bounds__(256, 2) k_ssim_fused(LossArgs a) {
         // B: (centre row, 7 centre columns) per item -> moments, SSIM, fields
         for (int it = tid; it < kFF * 6; it += 256) {
             const int fy = it % kFF, s = it / kFF, fx0 = 7 * s;
-            float m[5][7];
+            float2 m01[7], m23[7];
+            float m4[7];
+            {
+                float2 row[17];
 #pragma unroll
-            for (int f = 0; f < 5; f++) {
+                for (int j = 0; j < 17; j++) row[j] = sm.u.v.m01[fy][fx0 + j];
+#pragma unroll
+                for (int k = 0; k < 7; k++) {
+                    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+                    for (int d = 0; d < 11; d++) acc = __ffma2_rn(make_float2(kGauss[d], kGauss[d]), row[k + d], acc);
+                    m01[k] = acc;
+                }
+#pragma unroll
+                for (int j = 0; j < 17; j++) row[j] = sm.u.v.m23[fy][fx0 + j];
+#pragma unroll
+                for (int k = 0; k < 7; k++) {
+                    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+                    for (int d = 0; d < 11; d++) acc = __ffma2_rn(make_float2(kGauss[d], kGauss[d]), row[k + d], acc);
+                    m23[k] = acc;
+                }
+            }
+            {
                 float row[17];
 #pragma unroll
-                for (int j = 0; j < 17; j++) row[j] = sm.u.v[f][fy][fx0 + j];
+                for (int j = 0; j < 17; j++) row[j] = sm.u.v.m4[fy][fx0 + j];
 #pragma unroll
                 for (int k = 0; k < 7; k++) {
                     float acc = 0.f;
 #pragma unroll
                     for (int d = 0; d < 11; d++) acc += kGauss[d] * row[k + d];
-                    m[f][k] = acc;
+                    m4[k] = acc;
                 }
             }
             const int yc = Y0 - 5 + fy;
@@ -222,7 +256,7 @@ __global__ void __launch_bounds__(256, 2) k_ssim_fused(LossArgs a) {
                 const bool in_col = xc >= 0 && xc < W;
                 const bool in_img = in_row && in_col;
                 const bool own = in_img && own_row && fx >= 5 && fx < 5 + kFB;
-                float mu_x = m[0][k], mu_y = m[1][k], q_x = m[2][k], q_y = m[3][k], q_xy = m[4][k];
+                float mu_x = m01[k].x, mu_y = m01[k].y, q_x = m23[k].x, q_y = m23[k].y, q_xy = m4[k];
                 if (!in_col) mu_x = mu_y = q_x = q_y = q_xy = 0.f;
                 float f1 = 0.f, f2 = 0.f, f3 = 0.f;
                 if (!(finite_bits(mu_x) && finite_bits(mu_y) && finite_bits(q_x) && finite_bits(q_y) &&
@@ -250,9 +284,8 @@ __global__ void __launch_bounds__(256, 2) k_ssim_fused(LossArgs a) {
                         l1_acc += mval * fabsf((float)sm.g[c][fy + 5][fx + 5] * (1.0f / 255.0f) - sm.r[c][fy + 5][fx + 5]);
                     }
                 }
-                sm.f[0][fy][fx] = f1;
-                sm.f[1][fy][fx] = f2;
-                sm.f[2][fy][fx] = f3;
+                sm.f12[fy][fx] = make_float2(f1, f2);
+                sm.f3[fy][fx] = f3;
             }
         }
         __syncthreads();
@@ -260,17 +293,29 @@ __global__ void __launch_bounds__(256, 2) k_ssim_fused(LossArgs a) {
         // C: (centre row, 8 output columns) per item
         for (int it = tid; it < kFF * 4; it += 256) {
             const int fy = it % kFF, ox0 = 8 * (it / kFF);
+            {
+                float2 row[18];
 #pragma unroll
-            for (int j = 0; j < 3; j++) {
+                for (int t = 0; t < 18; t++) row[t] = sm.f12[fy][ox0 + t];
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+                    for (int d = 0; d < 11; d++)
+                        acc = __ffma2_rn(make_float2(kGauss[10 - d], kGauss[10 - d]), row[k + d], acc);
+                    sm.u.dh.f12[fy][ox0 + k] = acc;
+                }
+            }
+            {
                 float row[18];
 #pragma unroll
-                for (int t = 0; t < 18; t++) row[t] = sm.f[j][fy][ox0 + t];
+                for (int t = 0; t < 18; t++) row[t] = sm.f3[fy][ox0 + t];
 #pragma unroll
                 for (int k = 0; k < 8; k++) {
                     float acc = 0.f;
 #pragma unroll
                     for (int d = 0; d < 11; d++) acc += kGauss[10 - d] * row[k + d];
-                    sm.u.dh[j][fy][ox0 + k] = acc;
+                    sm.u.dh.f3[fy][ox0 + k] = acc;
                 }
             }
         }
@@ -278,18 +323,31 @@ __global__ void __launch_bounds__(256, 2) k_ssim_fused(LossArgs a) {
 
         // D: (output column, 4 output rows) per thread -> dL/dx of channel c
         {
-            float cf[3][4];
+            float2 c12[4];
+            float c3[4];
+            {
+                float2 col[14];
 #pragma unroll
-            for (int j = 0; j < 3; j++) {
+                for (int t = 0; t < 14; t++) col[t] = sm.u.dh.f12[dy0 + t][dx_];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+                    for (int d = 0; d < 11; d++)
+                        acc = __ffma2_rn(make_float2(kGauss[10 - d], kGauss[10 - d]), col[k + d], acc);
+                    c12[k] = acc;
+                }
+            }
+            {
                 float col[14];
 #pragma unroll
-                for (int t = 0; t < 14; t++) col[t] = sm.u.dh[j][dy0 + t][dx_];
+                for (int t = 0; t < 14; t++) col[t] = sm.u.dh.f3[dy0 + t][dx_];
 #pragma unroll
                 for (int k = 0; k < 4; k++) {
                     float acc = 0.f;
 #pragma unroll
                     for (int d = 0; d < 11; d++) acc += kGauss[10 - d] * col[k + d];
-                    cf[j][k] = acc;
+                    c3[k] = acc;
                 }
             }
 #pragma unroll
@@ -299,7 +357,7 @@ __global__ void __launch_bounds__(256, 2) k_ssim_fused(LossArgs a) {
                     const float R = sm.r[c][dy0 + k + 10][dx_ + 10];
                     const float G = (float)sm.g[c][dy0 + k + 10][dx_ + 10] * (1.0f / 255.0f);
                     const float mc = (has_mask && mask[(size_t)y * W + x] < 128) ? 0.f : 1.f;
-                    const float vs = cf[0][k] + R * cf[1][k] + G * cf[2][k];
+                    const float vs = c12[k].x + R * c12[k].y + G * c3[k];
                     const float vl = mc * ((G > R) ? -1.f : ((G < R) ? 1.f : 0.f));
                     float v = invn * (-sw * vs + (1.f - sw) * vl);
                     if (!finite_bits(v)) { nbad++; v = 0.f; }
