@@ -66,6 +66,35 @@ enum NanSlot {
     kNanProjConic = 11, kNanProjRgb = 12, kNanPack = 13, kNanPackOpacity = 14, kNanRasterSigma = 15
 };
 
+// Programmatic dependent launch.  The step's kernels are launched with
+// launch_pdl, so a kernel's launch is prepared while its predecessor in the
+// stream drains; every such kernel starts with pdl_enter, which waits for
+// the predecessor grid to complete with its memory visible (before any
+// global load or store).  The predecessor lets it go when its blocks exit
+// (no early trigger: successor blocks parked on SMs during the predecessor's
+// last wave made the captured step slower, 1.392 -> 1.456 ms, against
+// 1.377 ms this way).  A kernel after a non-kernel stream operation, or
+// launched plainly, behaves as usual.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 __device__ __forceinline__ bool finite_bits(float x) {
     return (__float_as_uint(x) & 0x7F800000u) != 0x7F800000u;
 }

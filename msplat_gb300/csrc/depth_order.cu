@@ -40,6 +40,7 @@ __device__ __forceinline__ uint32_t gs_key0(const TileArgs &a, size_t u) {
 // Digit counts of one 2048-key block: hist[view][digit][block].
 template <bool kFirst>
 __global__ void __launch_bounds__(kGsThreads) k_gs_hist(TileArgs a, int shift, const uint32_t *key_in) {
+    pdl_enter();
     __shared__ uint32_t h[256];
     const int view = blockIdx.y, n = a.vt.n, nb = gridDim.x;
     const size_t vb = (size_t)view * n;
@@ -60,6 +61,7 @@ __global__ void __launch_bounds__(kGsThreads) k_gs_hist(TileArgs a, int shift, c
 // place, and the digit's total to dtot[view][digit].  Each lane takes every
 // 32nd block; four rounds of loads are issued before they are scanned.
 __global__ void __launch_bounds__(256) k_gs_digit_scan(TileArgs a, int nb) {
+    pdl_enter();
     const int lane = threadIdx.x & 31;
     const int d = blockIdx.x * 8 + (threadIdx.x >> 5), view = blockIdx.y;
     uint32_t *h = a.gs_hist + (size_t)view * 256 * nb + (size_t)d * nb;
@@ -95,6 +97,7 @@ template <bool kFirst>
 __global__ void __launch_bounds__(kGsThreads) k_gs_scatter(TileArgs a, int shift, const uint32_t *key_in,
                                                            const uint32_t *val_in, uint32_t *key_out,
                                                            uint32_t *val_out) {
+    pdl_enter();
     __shared__ uint16_t wcnt[kGsThreads / 32][256];
     __shared__ uint16_t woff[kGsThreads / 32][256];
     __shared__ uint32_t base[256];
@@ -167,6 +170,7 @@ __global__ void __launch_bounds__(kGsThreads) k_gs_scatter(TileArgs a, int shift
 
 // Tile rectangle of the Gaussian at each sorted position (empty when inactive).
 __global__ void __launch_bounds__(256) k_gs_rect(TileArgs a) {
+    pdl_enter();
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const int view = blockIdx.y, n = a.vt.n;
     if (p >= n) return;
@@ -186,6 +190,7 @@ __global__ void __launch_bounds__(256) k_gs_rect(TileArgs a) {
 
 // Block-aggregated count over sorted positions (k_count_agg's rows).
 __global__ void __launch_bounds__(kAggThreads) k_count_agg_sorted(TileArgs a) {
+    pdl_enter();
     extern __shared__ uint32_t bins[];
     const int view = blockIdx.y;
     const ViewGeom vg = view_geom(a.vt, view);
@@ -207,6 +212,7 @@ __global__ void __launch_bounds__(kAggThreads) k_count_agg_sorted(TileArgs a) {
 // Block-aggregated scatter over sorted positions: the key is the position p.
 template <bool kGroup>
 __global__ void __launch_bounds__(kAggThreads) k_scatter_agg_sorted(TileArgs a) {
+    pdl_enter();
     extern __shared__ uint32_t bins[];
     const int view = blockIdx.y;
     const ViewGeom vg = view_geom(a.vt, view);
@@ -239,6 +245,7 @@ constexpr int kOrderThreads = 256;
 constexpr int kOrderSmemWords = 12288;   // 48 KB: run starts + staged keys
 
 __global__ void __launch_bounds__(kOrderThreads) k_tile_order(TileArgs a, int ctas, int stage_runs, int key_cap) {
+    pdl_enter();
     extern __shared__ uint32_t osm[];
     const int t = a.tile_lo + blockIdx.x;
     if (t >= a.tile_hi) return;
@@ -293,18 +300,18 @@ int launch_presorted_count(const TileArgs &a, cudaStream_t s) {
     const dim3 g(nb, views);
     // pass 0 reads the keys from the projection; passes alternate buffers 1, 0, 1, 0
     const dim3 gd(32, views);   // 256 digits, 8 per CTA
-    k_gs_hist<true><<<g, kGsThreads, 0, s>>>(a, 0, nullptr);
-    k_gs_digit_scan<<<gd, 256, 0, s>>>(a, nb);
-    k_gs_scatter<true><<<g, kGsThreads, 0, s>>>(a, 0, nullptr, nullptr, a.gs_key[1], a.gs_val[1]);
+    launch_pdl(k_gs_hist<true>, g, kGsThreads, 0, s, a, 0, nullptr);
+    launch_pdl(k_gs_digit_scan, gd, 256, 0, s, a, nb);
+    launch_pdl(k_gs_scatter<true>, g, kGsThreads, 0, s, a, 0, nullptr, nullptr, a.gs_key[1], a.gs_val[1]);
     for (int pass = 1; pass < 4; pass++) {
         const int src = pass & 1, dst = src ^ 1;
-        k_gs_hist<false><<<g, kGsThreads, 0, s>>>(a, 8 * pass, a.gs_key[src]);
-        k_gs_digit_scan<<<gd, 256, 0, s>>>(a, nb);
-        k_gs_scatter<false><<<g, kGsThreads, 0, s>>>(a, 8 * pass, a.gs_key[src], a.gs_val[src], a.gs_key[dst],
+        launch_pdl(k_gs_hist<false>, g, kGsThreads, 0, s, a, 8 * pass, a.gs_key[src]);
+        launch_pdl(k_gs_digit_scan, gd, 256, 0, s, a, nb);
+        launch_pdl(k_gs_scatter<false>, g, kGsThreads, 0, s, a, 8 * pass, a.gs_key[src], a.gs_val[src], a.gs_key[dst],
                                                       a.gs_val[dst]);
     }
     debug_sync(s, "depth_sort");
-    k_gs_rect<<<dim3((n + 255) / 256, views), 256, 0, s>>>(a);
+    launch_pdl(k_gs_rect, dim3((n + 255) / 256, views), 256, 0, s, a);
     debug_sync(s, "depth_rect");
     const int agg_blocks = (n + kAggPerCta - 1) / kAggPerCta;
     const size_t smem = (size_t)max_view_tiles(a.vt) * sizeof(uint32_t);
@@ -319,7 +326,7 @@ int launch_presorted_count(const TileArgs &a, cudaStream_t s) {
                              kAggMaxTiles * 4);
         if (dev >= 0 && dev < 64) attr_set[dev] = true;
     }
-    k_count_agg_sorted<<<dim3(agg_blocks, views), kAggThreads, smem, s>>>(a);
+    launch_pdl(k_count_agg_sorted, dim3(agg_blocks, views), kAggThreads, smem, s, a);
     debug_sync(s, "count_sorted");
     return 12 + 1 + 1;
 }
@@ -329,8 +336,8 @@ int launch_presorted_build(const TileArgs &a, cudaStream_t s) {
     const int agg_blocks = (n + kAggPerCta - 1) / kAggPerCta;
     const size_t smem = (size_t)max_view_tiles(a.vt) * sizeof(uint32_t);
     const bool grp = a.tile_lo > 0 || a.tile_hi < a.num_tiles || a.isect_lo > 0;
-    if (grp) k_scatter_agg_sorted<true><<<dim3(agg_blocks, views), kAggThreads, smem, s>>>(a);
-    else k_scatter_agg_sorted<false><<<dim3(agg_blocks, views), kAggThreads, smem, s>>>(a);
+    if (grp) launch_pdl(k_scatter_agg_sorted<true>, dim3(agg_blocks, views), kAggThreads, smem, s, a);
+    else launch_pdl(k_scatter_agg_sorted<false>, dim3(agg_blocks, views), kAggThreads, smem, s, a);
     debug_sync(s, "scatter_sorted");
     // shared memory: the run starts when they take at most two thirds of it,
     // then up to 4096 keys (a small footprint keeps eight CTAs per SM; larger
@@ -339,7 +346,7 @@ int launch_presorted_build(const TileArgs &a, cudaStream_t s) {
     const int key_cap = std::min(4096, kOrderSmemWords - (stage_runs ? agg_blocks + 1 : 0));
     const size_t osmem = sizeof(uint32_t) * ((stage_runs ? agg_blocks + 1 : 0) + key_cap);
     if (a.tile_hi > a.tile_lo)
-        k_tile_order<<<a.tile_hi - a.tile_lo, kOrderThreads, osmem, s>>>(a, agg_blocks, stage_runs, key_cap);
+        launch_pdl(k_tile_order, a.tile_hi - a.tile_lo, kOrderThreads, osmem, s, a, agg_blocks, stage_runs, key_cap);
     debug_sync(s, "tile_order");
     return 2;
 }

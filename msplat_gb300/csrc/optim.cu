@@ -46,6 +46,7 @@ __device__ __forceinline__ bool adam_step(float &p, float &m, float &v, float g,
 // and gradient loaded as float4, every load of a step issued before any
 // use); a group length that is not a multiple of 4 ends with scalar steps.
 __global__ void __launch_bounds__(256) k_adam(AdamArgs a) {
+    pdl_enter();
     const StepParams &sp = *a.sp;
     const float b1 = sp.beta1, b2 = sp.beta2, eps = sp.eps;
     const bool reg = sp.op_reg > 0.f || sp.sc_reg > 0.f;
@@ -121,6 +122,7 @@ __device__ __forceinline__ float pcg_unit(uint32_t h) {
 }
 
 __global__ void __launch_bounds__(256) k_sgld(AdamArgs a) {
+    pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     const StepParams &sp = *a.sp;
@@ -167,12 +169,12 @@ void launch_adam(const AdamArgs &a, int num_sms, cudaStream_t s) {
     long long blocks = (total + 255) / 256;
     const long long cap = (long long)num_sms * 8;
     if (blocks > cap) blocks = cap;
-    k_adam<<<(unsigned)blocks, 256, 0, s>>>(a);
+    launch_pdl(k_adam, (unsigned)blocks, 256, 0, s, a);
 }
 
 void launch_sgld(const AdamArgs &a, cudaStream_t s) {
     if (a.n <= 0) return;
-    k_sgld<<<(a.n + 255) / 256, 256, 0, s>>>(a);
+    launch_pdl(k_sgld, (a.n + 255) / 256, 256, 0, s, a);
 }
 
 }  // namespace msplat

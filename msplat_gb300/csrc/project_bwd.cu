@@ -361,6 +361,7 @@ template <int kRowF> __device__ __forceinline__ void stage_sh_inactive(ShFlat &s
 // arguments.
 template <int kRowF>
 __global__ void __launch_bounds__(256, 4) k_project_bwd(ProjectBwdArgs a) {
+    pdl_enter();
     const int n = a.vt.n;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -407,6 +408,7 @@ __global__ void __launch_bounds__(256, 4) k_project_bwd(ProjectBwdArgs a) {
 // Gaussians.
 template <int kRowF>
 __global__ void __launch_bounds__(128) k_sh_walk(ProjectBwdArgs a) {
+    pdl_enter();
     __shared__ __align__(16) ShFlat stage[4];
     const int n = a.vt.n;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -437,6 +439,7 @@ __global__ void __launch_bounds__(128) k_sh_walk(ProjectBwdArgs a) {
 // gradients and no SH update.
 template <int kRowF>
 __global__ void __launch_bounds__(128, 4) k_project_bwd_views(ProjectBwdArgs a) {
+    pdl_enter();
     __shared__ __align__(16) ShFlat stage[4];
     const int n = a.vt.n, views = a.vt.count;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -514,15 +517,15 @@ void launch_project_bwd(const ProjectBwdArgs &a, cudaStream_t s) {
     const int n = a.vt.n;
     if (n <= 0) return;
     if (a.vt.count > 1) {
-        if (a.rest_bases == 15) k_project_bwd_views<45><<<(n + 127) / 128, 128, 0, s>>>(a);
-        else k_project_bwd_views<0><<<(n + 127) / 128, 128, 0, s>>>(a);
+        if (a.rest_bases == 15) launch_pdl(k_project_bwd_views<45>, (n + 127) / 128, 128, 0, s, a);
+        else launch_pdl(k_project_bwd_views<0>, (n + 127) / 128, 128, 0, s, a);
         return;
     }
-    if (a.rest_bases == 15) k_project_bwd<45><<<(n + 255) / 256, 256, 0, s>>>(a);
-    else k_project_bwd<0><<<(n + 255) / 256, 256, 0, s>>>(a);
+    if (a.rest_bases == 15) launch_pdl(k_project_bwd<45>, (n + 255) / 256, 256, 0, s, a);
+    else launch_pdl(k_project_bwd<0>, (n + 255) / 256, 256, 0, s, a);
     if (a.do_optimizer || a.v_dc_out) {
-        if (a.rest_bases == 15) k_sh_walk<45><<<(n + 127) / 128, 128, 0, s>>>(a);
-        else k_sh_walk<0><<<(n + 127) / 128, 128, 0, s>>>(a);
+        if (a.rest_bases == 15) launch_pdl(k_sh_walk<45>, (n + 127) / 128, 128, 0, s, a);
+        else launch_pdl(k_sh_walk<0>, (n + 127) / 128, 128, 0, s, a);
     }
 }
 

@@ -87,6 +87,7 @@ constexpr int kStageFloats = 45;   // 15 SH bases x 3 channels per Gaussian
 // are 16-byte aligned; a lane's row there (45 floats apart) is conflict-free.
 template <bool kViews>
 __global__ void __launch_bounds__(256) k_project_fwd(ProjectArgs a) {
+    pdl_enter();
     __shared__ __align__(16) float stage[8][32 * kStageFloats];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -257,8 +258,8 @@ __global__ void __launch_bounds__(256) k_project_fwd(ProjectArgs a) {
 
 void launch_project_fwd(const ProjectArgs &a, cudaStream_t s) {
     if (a.vt.n <= 0) return;
-    if (a.vt.count > 1) k_project_fwd<true><<<dim3((a.vt.n + 255) / 256, a.vt.count), 256, 0, s>>>(a);
-    else k_project_fwd<false><<<(a.vt.n + 255) / 256, 256, 0, s>>>(a);
+    if (a.vt.count > 1) launch_pdl(k_project_fwd<true>, dim3((a.vt.n + 255) / 256, a.vt.count), 256, 0, s, a);
+    else launch_pdl(k_project_fwd<false>, (a.vt.n + 255) / 256, 256, 0, s, a);
 }
 
 }  // namespace msplat

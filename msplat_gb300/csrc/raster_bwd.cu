@@ -216,6 +216,7 @@ __device__ __forceinline__ void init_pixel(PixelState &ps, const RasterArgs &a, 
 
 template <bool kViews, int kBB>
 __global__ void __launch_bounds__(kTileThreads) k_raster_bwd(RasterArgs a) {
+    pdl_enter();
     __shared__ BwdSmem<kBB> sm;
     const int tile = blockIdx.x + a.tile_lo;
     const int s = clamp_off(a.tile_offsets[tile], a.isect_lo, a.capacity), e = clamp_off(a.tile_offsets[tile + 1], a.isect_lo, a.capacity);
@@ -231,6 +232,7 @@ __global__ void __launch_bounds__(kTileThreads) k_raster_bwd(RasterArgs a) {
 }
 
 __global__ void __launch_bounds__(256) k_chunk_prefix_suffix(RasterArgs a) {
+    pdl_enter();
     const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long P = a.vt.pixels;
     if (p >= P) return;
@@ -255,6 +257,7 @@ __global__ void __launch_bounds__(256) k_chunk_prefix_suffix(RasterArgs a) {
 
 template <bool kViews, int kBB>
 __global__ void __launch_bounds__(kTileThreads) k_raster_bwd_chunked(RasterArgs a) {
+    pdl_enter();
     __shared__ BwdSmem<kBB> sm;
     const int tile = blockIdx.x + a.tile_lo, k = blockIdx.y;
     const int s0 = clamp_off(a.tile_offsets[tile], a.isect_lo, a.capacity), e0 = clamp_off(a.tile_offsets[tile + 1], a.isect_lo, a.capacity);
@@ -276,13 +279,13 @@ __global__ void __launch_bounds__(kTileThreads) k_raster_bwd_chunked(RasterArgs 
 template <int kBB> static void raster_bwd_batch(const RasterArgs &a, cudaStream_t s) {
     const bool views = a.vt.count > 1;
     if (a.k_max <= 1) {
-        if (views) k_raster_bwd<true, kBB><<<a.num_tiles, kTileThreads, 0, s>>>(a);
-        else k_raster_bwd<false, kBB><<<a.num_tiles, kTileThreads, 0, s>>>(a);
+        if (views) launch_pdl(k_raster_bwd<true, kBB>, a.num_tiles, kTileThreads, 0, s, a);
+        else launch_pdl(k_raster_bwd<false, kBB>, a.num_tiles, kTileThreads, 0, s, a);
     } else {
         const long long P = a.vt.pixels;
-        k_chunk_prefix_suffix<<<(unsigned)((P + 255) / 256), 256, 0, s>>>(a);
-        if (views) k_raster_bwd_chunked<true, kBB><<<dim3(a.num_tiles, a.k_max), kTileThreads, 0, s>>>(a);
-        else k_raster_bwd_chunked<false, kBB><<<dim3(a.num_tiles, a.k_max), kTileThreads, 0, s>>>(a);
+        launch_pdl(k_chunk_prefix_suffix, (unsigned)((P + 255) / 256), 256, 0, s, a);
+        if (views) launch_pdl(k_raster_bwd_chunked<true, kBB>, dim3(a.num_tiles, a.k_max), kTileThreads, 0, s, a);
+        else launch_pdl(k_raster_bwd_chunked<false, kBB>, dim3(a.num_tiles, a.k_max), kTileThreads, 0, s, a);
     }
 }
 

@@ -113,6 +113,7 @@ template <bool kViews> __device__ __forceinline__ TilePixel tile_pixel(const Ras
 
 template <bool kViews, int kBatch>
 __global__ void __launch_bounds__(kTileThreads, 8) k_raster_fwd(RasterArgs a) {
+    pdl_enter();
     __shared__ BatchSmem<kBatch> sm;
     const int tile = blockIdx.x + a.tile_lo;
     const TilePixel tp = tile_pixel<kViews>(a, tile);
@@ -135,6 +136,7 @@ __global__ void __launch_bounds__(kTileThreads, 8) k_raster_fwd(RasterArgs a) {
 
 template <bool kViews, int kBatch>
 __global__ void __launch_bounds__(kTileThreads) k_raster_fwd_chunked(RasterArgs a) {
+    pdl_enter();
     __shared__ BatchSmem<kBatch> sm;
     const int tile = blockIdx.x + a.tile_lo, k = blockIdx.y;
     const TilePixel tp = tile_pixel<kViews>(a, tile);
@@ -164,6 +166,7 @@ __global__ void __launch_bounds__(kTileThreads) k_raster_fwd_chunked(RasterArgs 
 }
 
 __global__ void __launch_bounds__(256) k_raster_merge(RasterArgs a) {
+    pdl_enter();
     const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long P = a.vt.pixels;
     if (p >= P) return;
@@ -192,13 +195,13 @@ __global__ void __launch_bounds__(256) k_raster_merge(RasterArgs a) {
 template <int kBatch> static void raster_fwd_batch(const RasterArgs &a, cudaStream_t s) {
     const bool views = a.vt.count > 1;
     if (a.k_max <= 1) {
-        if (views) k_raster_fwd<true, kBatch><<<a.num_tiles, kTileThreads, 0, s>>>(a);
-        else k_raster_fwd<false, kBatch><<<a.num_tiles, kTileThreads, 0, s>>>(a);
+        if (views) launch_pdl(k_raster_fwd<true, kBatch>, a.num_tiles, kTileThreads, 0, s, a);
+        else launch_pdl(k_raster_fwd<false, kBatch>, a.num_tiles, kTileThreads, 0, s, a);
     } else {
-        if (views) k_raster_fwd_chunked<true, kBatch><<<dim3(a.num_tiles, a.k_max), kTileThreads, 0, s>>>(a);
-        else k_raster_fwd_chunked<false, kBatch><<<dim3(a.num_tiles, a.k_max), kTileThreads, 0, s>>>(a);
+        if (views) launch_pdl(k_raster_fwd_chunked<true, kBatch>, dim3(a.num_tiles, a.k_max), kTileThreads, 0, s, a);
+        else launch_pdl(k_raster_fwd_chunked<false, kBatch>, dim3(a.num_tiles, a.k_max), kTileThreads, 0, s, a);
         const long long P = a.vt.pixels;
-        k_raster_merge<<<(unsigned)((P + 255) / 256), 256, 0, s>>>(a);
+        launch_pdl(k_raster_merge, (unsigned)((P + 255) / 256), 256, 0, s, a);
     }
 }
 

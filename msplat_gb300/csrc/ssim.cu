@@ -113,6 +113,7 @@ __device__ __forceinline__ bool loss_counted(int x, int y, int W, int H) {
 
 template <bool kViews>
 __global__ void __launch_bounds__(256, 2) k_ssim_fused(LossArgs a) {
+    pdl_enter();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     FusedSmem &sm = *reinterpret_cast<FusedSmem *>(smem_raw);
     const FusedBlock fb = fused_block<kViews>(a);
@@ -409,11 +410,11 @@ int launch_loss(const LossArgs &a, cudaStream_t s) {
     if (a.vt.count > 1) {
         const int nb = fused_blocks(a.vt);
         if (nb <= 0) return 0;
-        k_ssim_fused<true><<<nb, 256, smem, s>>>(a);
+        launch_pdl(k_ssim_fused<true>, nb, 256, smem, s, a);
     } else {
         const dim3 grid((a.vt.width[0] + kFB - 1) / kFB, (a.vt.height[0] + kFB - 1) / kFB);
         if (grid.x == 0 || grid.y == 0) return 0;
-        k_ssim_fused<false><<<grid, 256, smem, s>>>(a);
+        launch_pdl(k_ssim_fused<false>, grid, 256, smem, s, a);
     }
     return 1;
 }

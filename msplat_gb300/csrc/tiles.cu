@@ -34,6 +34,7 @@ __device__ __forceinline__ bool splat_active(size_t u, const int *radii, const f
 
 template <bool kViews>
 __global__ void __launch_bounds__(256) k_count(TileArgs a) {
+    pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int view = kViews ? (int)blockIdx.y : 0;
     const size_t u = kViews ? (size_t)view * a.vt.n + i : (size_t)i;
@@ -54,6 +55,7 @@ __global__ void __launch_bounds__(256) k_count(TileArgs a) {
 // Exclusive scan of the tile counts by one CTA of 1024 threads: each thread
 // scans a contiguous run, the run totals are scanned across the CTA.
 __global__ void __launch_bounds__(1024) k_scan(TileArgs a) {
+    pdl_enter();
     __shared__ uint32_t warp_tot[32];
     __shared__ uint32_t max_warp[32];
     __shared__ uint32_t class_n[kSortClasses];
@@ -115,6 +117,7 @@ __global__ void __launch_bounds__(1024) k_scan(TileArgs a) {
 // outside [tile_lo, tile_hi) skipped, slots from isect_lo); false: all tiles
 template <bool kViews, bool kGroup>
 __global__ void __launch_bounds__(256) k_scatter(TileArgs a) {
+    pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int view = kViews ? (int)blockIdx.y : 0;
     const size_t u = kViews ? (size_t)view * a.vt.n + i : (size_t)i;
@@ -154,6 +157,7 @@ __device__ __forceinline__ void agg_rect(const TileArgs &a, const ViewGeom &vg, 
 
 template <bool kViews>
 __global__ void __launch_bounds__(kAggThreads) k_count_agg(TileArgs a) {
+    pdl_enter();
     extern __shared__ uint32_t bins[];
     const int view = kViews ? (int)blockIdx.y : 0;
     const ViewGeom vg = view_geom(a.vt, view);
@@ -181,6 +185,7 @@ __global__ void __launch_bounds__(kAggThreads) k_count_agg(TileArgs a) {
 // shared memory, then the rows rewritten.
 template <bool kViews>
 __global__ void __launch_bounds__(1024) k_cta_scan(TileArgs a, int ctas) {
+    pdl_enter();
     __shared__ uint32_t part[32][33];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int t = blockIdx.x * 32 + lane;
@@ -213,6 +218,7 @@ __global__ void __launch_bounds__(1024) k_cta_scan(TileArgs a, int ctas) {
 
 template <bool kViews, bool kGroup>
 __global__ void __launch_bounds__(kAggThreads) k_scatter_agg(TileArgs a) {
+    pdl_enter();
     extern __shared__ uint32_t bins[];
     const int view = kViews ? (int)blockIdx.y : 0;
     const ViewGeom vg = view_geom(a.vt, view);
@@ -384,6 +390,7 @@ __device__ bool pair_pass(PairSmem<THREADS> &sm, int b, int n, int shift, unsign
 
 template <int THREADS>
 __global__ void __launch_bounds__(THREADS) k_sort_pack_smem(TileArgs a, int cls) {
+    pdl_enter();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     PairSmem<THREADS> &sm = *reinterpret_cast<PairSmem<THREADS> *>(smem_raw);
     const int tid = threadIdx.x;
@@ -547,6 +554,7 @@ __device__ void order_ties(uint64_t *a, int n) {
 }
 
 __global__ void __launch_bounds__(kGlobThreads) k_sort_pack_global(TileArgs a, int cls) {
+    pdl_enter();
     __shared__ GlobSmem sm;
     const int tid = threadIdx.x;
     unsigned *dbg = a.nan_counts ? a.nan_counts + kDbgSlot : nullptr;
@@ -622,10 +630,10 @@ static bool presorted_path(const TileArgs &a) {
 // the column scan of the per-CTA histograms and the tile scan
 int launch_tile_scans(const TileArgs &a, cudaStream_t s) {
     const int agg_blocks = (a.vt.n + kAggPerCta - 1) / kAggPerCta;
-    if (a.vt.count > 1) k_cta_scan<true><<<(a.num_tiles + 31) / 32, 1024, 0, s>>>(a, agg_blocks);
-    else k_cta_scan<false><<<(a.num_tiles + 31) / 32, 1024, 0, s>>>(a, agg_blocks);
+    if (a.vt.count > 1) launch_pdl(k_cta_scan<true>, (a.num_tiles + 31) / 32, 1024, 0, s, a, agg_blocks);
+    else launch_pdl(k_cta_scan<false>, (a.num_tiles + 31) / 32, 1024, 0, s, a, agg_blocks);
     debug_sync(s, "cta_scan");
-    k_scan<<<1, 1024, 0, s>>>(a);
+    launch_pdl(k_scan, 1, 1024, 0, s, a);
     debug_sync(s, "scan");
     return 2;
 }
@@ -640,20 +648,20 @@ int launch_tile_count(const TileArgs &a, cudaStream_t s) {
     const size_t agg_smem = (size_t)maxT * sizeof(uint32_t);
     const bool mv = views > 1;
     if (n > 0 && agg) {
-        if (mv) k_count_agg<true><<<dim3(agg_blocks, views), kAggThreads, agg_smem, s>>>(a);
-        else k_count_agg<false><<<agg_blocks, kAggThreads, agg_smem, s>>>(a);
+        if (mv) launch_pdl(k_count_agg<true>, dim3(agg_blocks, views), kAggThreads, agg_smem, s, a);
+        else launch_pdl(k_count_agg<false>, agg_blocks, kAggThreads, agg_smem, s, a);
         debug_sync(s, "count");
-        if (mv) k_cta_scan<true><<<(a.num_tiles + 31) / 32, 1024, 0, s>>>(a, agg_blocks);
-        else k_cta_scan<false><<<(a.num_tiles + 31) / 32, 1024, 0, s>>>(a, agg_blocks);
+        if (mv) launch_pdl(k_cta_scan<true>, (a.num_tiles + 31) / 32, 1024, 0, s, a, agg_blocks);
+        else launch_pdl(k_cta_scan<false>, (a.num_tiles + 31) / 32, 1024, 0, s, a, agg_blocks);
         debug_sync(s, "cta_scan");
         launches += 2;
     } else if (n > 0) {
-        if (mv) k_count<true><<<dim3((n + 255) / 256, views), 256, 0, s>>>(a);
-        else k_count<false><<<(n + 255) / 256, 256, 0, s>>>(a);
+        if (mv) launch_pdl(k_count<true>, dim3((n + 255) / 256, views), 256, 0, s, a);
+        else launch_pdl(k_count<false>, (n + 255) / 256, 256, 0, s, a);
         debug_sync(s, "count");
         launches += 1;
     }
-    k_scan<<<1, 1024, 0, s>>>(a);
+    launch_pdl(k_scan, 1, 1024, 0, s, a);
     debug_sync(s, "scan");
     launches += 1;
     return launches;
@@ -673,19 +681,19 @@ int launch_tile_build(const TileArgs &a, int num_sms, cudaStream_t s) {
         const dim3 ga(agg_blocks, views), gs((n + 255) / 256, views);
         if (agg) {
             if (grp) {
-                if (mv) k_scatter_agg<true, true><<<ga, kAggThreads, agg_smem, s>>>(a);
-                else k_scatter_agg<false, true><<<ga, kAggThreads, agg_smem, s>>>(a);
+                if (mv) launch_pdl(k_scatter_agg<true, true>, ga, kAggThreads, agg_smem, s, a);
+                else launch_pdl(k_scatter_agg<false, true>, ga, kAggThreads, agg_smem, s, a);
             } else {
-                if (mv) k_scatter_agg<true, false><<<ga, kAggThreads, agg_smem, s>>>(a);
-                else k_scatter_agg<false, false><<<ga, kAggThreads, agg_smem, s>>>(a);
+                if (mv) launch_pdl(k_scatter_agg<true, false>, ga, kAggThreads, agg_smem, s, a);
+                else launch_pdl(k_scatter_agg<false, false>, ga, kAggThreads, agg_smem, s, a);
             }
         } else {
             if (grp) {
-                if (mv) k_scatter<true, true><<<gs, 256, 0, s>>>(a);
-                else k_scatter<false, true><<<gs, 256, 0, s>>>(a);
+                if (mv) launch_pdl(k_scatter<true, true>, gs, 256, 0, s, a);
+                else launch_pdl(k_scatter<false, true>, gs, 256, 0, s, a);
             } else {
-                if (mv) k_scatter<true, false><<<gs, 256, 0, s>>>(a);
-                else k_scatter<false, false><<<gs, 256, 0, s>>>(a);
+                if (mv) launch_pdl(k_scatter<true, false>, gs, 256, 0, s, a);
+                else launch_pdl(k_scatter<false, false>, gs, 256, 0, s, a);
             }
         }
         debug_sync(s, "scatter");
@@ -693,15 +701,15 @@ int launch_tile_build(const TileArgs &a, int num_sms, cudaStream_t s) {
     }
     // persistent sort grids, one per class; idle classes exit at once
     if (a.sort_width == 256) {
-        k_sort_pack_smem<256><<<4 * num_sms, 256, pair_smem_bytes<256>(), s>>>(a, 0);
+        launch_pdl(k_sort_pack_smem<256>, 4 * num_sms, 256, pair_smem_bytes<256>(), s, a, 0);
         debug_sync(s, "sort_pack_256");
         launches += 1;
     }
-    k_sort_pack_smem<512><<<2 * num_sms, 512, pair_smem_bytes<512>(), s>>>(a, 1);
+    launch_pdl(k_sort_pack_smem<512>, 2 * num_sms, 512, pair_smem_bytes<512>(), s, a, 1);
     debug_sync(s, "sort_pack_512");
-    k_sort_pack_smem<1024><<<num_sms, 1024, pair_smem_bytes<1024>(), s>>>(a, 2);
+    launch_pdl(k_sort_pack_smem<1024>, num_sms, 1024, pair_smem_bytes<1024>(), s, a, 2);
     debug_sync(s, "sort_pack_1024");
-    k_sort_pack_global<<<num_sms, kGlobThreads, 0, s>>>(a, 3);
+    launch_pdl(k_sort_pack_global, num_sms, kGlobThreads, 0, s, a, 3);
     debug_sync(s, "sort_pack_global");
     return launches + 3;
 }
