@@ -300,7 +300,7 @@ class Engine {
         if (!has_gt) { mark(4); mark(5); mark(6); mark(7); mark(8); return; }
 
         LossArgs la{};
-        la.vt = vt; la.num_tiles = T; la.sp = pa.sp; la.img = ra.out_img;
+        la.vt = vt; la.sp = pa.sp; la.img = ra.out_img;
         la.gt = nullptr; la.mask = nullptr;   // read from StepParams (see common.cuh)
         la.v_img = ptr<float>("v_img");
         la.loss_sum = ptr<float>("loss_sum"); la.nan_counts = pa.nan_counts;

@@ -118,7 +118,6 @@ struct RasterArgs {
 
 struct LossArgs {
     ViewTable vt;
-    int num_tiles;          // 16x16 blocks over all views (the tiles)
     const StepParams *sp;   // [views]
     const float *img;
     const uint8_t *gt, *mask;   // one view: override StepParams' target and mask (nullable)

@@ -90,7 +90,6 @@ extern "C" int msplat_loss_ssim_l1_noalloc(const float *img, const uint8_t *gt, 
     }
     LossArgs la{};
     la.vt = single_view_table(0, width, height);
-    la.num_tiles = la.vt.tile_base[1];
     la.sp = d.params;
     la.img = img;
     la.gt = gt;
