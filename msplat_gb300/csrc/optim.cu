@@ -134,10 +134,12 @@ __global__ void __launch_bounds__(256) k_sgld(AdamArgs a) {
     const float op = 1.0f / (1.0f + det_expf(-a.opacities[i]));
     const float wgt = 1.0f / (1.0f + det_expf(-100.0f * ((1.0f - op) - 0.995f)));
     const float ns = sp.noise_lr * sp.xyz_lr * wgt;
-    const float n0 = r01 * cosf(a01) * ns, n1 = r01 * sinf(a01) * ns, n2 = r23 * cosf(a23) * ns;
+    float s01, c01;
+    sincosf(a01, &s01, &c01);   // one range reduction for both
+    const float n0 = r01 * c01 * ns, n1 = r01 * s01 * ns, n2 = r23 * cosf(a23) * ns;
     const float4 q = *reinterpret_cast<const float4 *>(a.quats + 4 * (size_t)i);
-    const float ql = sqrtf(fmaxf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w, 1e-8f));
-    const float qw = q.x / ql, qx = q.y / ql, qy = q.z / ql, qz = q.w / ql;
+    const float rql = 1.0f / sqrtf(fmaxf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w, 1e-8f));
+    const float qw = q.x * rql, qx = q.y * rql, qy = q.z * rql, qz = q.w * rql;
     float s[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) s[k] = det_expf(fminf(fmaxf(a.scales[3 * i + k], -15.0f), 15.0f));
