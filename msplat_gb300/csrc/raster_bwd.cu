@@ -2,7 +2,8 @@
 // opacity logit.  One CTA per 16x16 tile (chunked: per (tile, chunk)), one
 // thread per pixel.  Per splat each warp reduces its pixels' 9 partial
 // gradients with a transpose-reduce (9 shuffles for 8 values plus 5 for the
-// ninth, instead of 45), warps combine through shared-memory adds, and each
+// ninth, instead of 45; paired fp32 adds), warps combine through
+// shared-memory adds, and each
 // batch flushes one set of three float4 vector atomics per (splat, tile)
 // instead of the reference's nine scalar atomics per (splat, warp).  A warp
 // skips the splats whose reach box (warp_reach) misses its 8x4 pixel block.
@@ -26,29 +27,37 @@ template <int kBB> struct BwdSmem {
     int wmax[8];
 };
 
-// Sum of 8 per-lane values over the warp: lane 4*j ends with the total of v[j].
-__device__ __forceinline__ float transpose_reduce8(float v[8], int lane) {
+// Sums over the warp of 8 per-lane values v[] and of one more value w: lane
+// 4*j ends with the total of v[j] (returned), every lane with the total of
+// w (in w).  A transpose-reduce: at each of the first three levels a lane
+// keeps half of its values and sends the other half, so 7 shuffles reduce
+// 8 values; the additions run on paired fp32 arithmetic where two are
+// independent (the same IEEE sums, half the instructions).
+__device__ __forceinline__ float transpose_reduce8(float v[8], float &w, int lane) {
     const bool b16 = lane & 16, b8 = lane & 8, b4 = lane & 4;
+    float2 keep[2], recv[2];
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
-        const float send = b16 ? v[j] : v[j + 4];
-        const float keep = b16 ? v[j + 4] : v[j];
-        v[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    for (int h = 0; h < 2; h++) {
+        const float s0 = b16 ? v[2 * h] : v[2 * h + 4], s1 = b16 ? v[2 * h + 1] : v[2 * h + 5];
+        keep[h] = make_float2(b16 ? v[2 * h + 4] : v[2 * h], b16 ? v[2 * h + 5] : v[2 * h + 1]);
+        recv[h] = make_float2(__shfl_xor_sync(0xffffffffu, s0, 16), __shfl_xor_sync(0xffffffffu, s1, 16));
     }
-#pragma unroll
-    for (int j = 0; j < 2; j++) {
-        const float send = b8 ? v[j] : v[j + 2];
-        const float keep = b8 ? v[j + 2] : v[j];
-        v[j] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
-    }
-    {
-        const float send = b4 ? v[0] : v[1];
-        const float keep = b4 ? v[1] : v[0];
-        v[0] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
-    }
-    v[0] += __shfl_xor_sync(0xffffffffu, v[0], 2);
-    v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
-    return v[0];
+    const float2 v01 = __fadd2_rn(keep[0], recv[0]), v23 = __fadd2_rn(keep[1], recv[1]);
+    // level 8: pairs (0, 2) and (1, 3)
+    const float t0 = b8 ? v01.x : v23.x, t1 = b8 ? v01.y : v23.y;
+    const float2 k8 = make_float2(b8 ? v23.x : v01.x, b8 ? v23.y : v01.y);
+    const float2 r8 = make_float2(__shfl_xor_sync(0xffffffffu, t0, 8), __shfl_xor_sync(0xffffffffu, t1, 8));
+    const float2 u = __fadd2_rn(k8, r8);
+    // level 4: one value per lane from here, reduced together with w
+    const float send = b4 ? u.x : u.y;
+    float2 x = make_float2(b4 ? u.y : u.x, w);
+    w += __shfl_xor_sync(0xffffffffu, w, 16);
+    w += __shfl_xor_sync(0xffffffffu, w, 8);
+    x = make_float2(x.x + __shfl_xor_sync(0xffffffffu, send, 4), w + __shfl_xor_sync(0xffffffffu, w, 4));
+    x = __fadd2_rn(x, make_float2(__shfl_xor_sync(0xffffffffu, x.x, 2), __shfl_xor_sync(0xffffffffu, x.y, 2)));
+    x = __fadd2_rn(x, make_float2(__shfl_xor_sync(0xffffffffu, x.x, 1), __shfl_xor_sync(0xffffffffu, x.y, 1)));
+    w = x.y;
+    return x.x;
 }
 
 // Per-pixel state of the back-to-front walk.  The reference keeps the colour
@@ -139,9 +148,7 @@ __device__ void backward_range(BwdSmem<kBB> &sm, const RasterArgs &a, int s, int
                 v[7] = B;
                 v8 = v_sigma;
             }
-            const float s8 = transpose_reduce8(v, lane);
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v8 += __shfl_xor_sync(0xffffffffu, v8, o);
+            const float s8 = transpose_reduce8(v, v8, lane);
             if ((lane & 3) == 0) atomicAdd(&sm.acc[t][lane >> 2], s8);
             if (lane == 1) atomicAdd(&sm.acc[t][8], v8);
         }
