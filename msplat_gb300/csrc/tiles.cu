@@ -52,64 +52,86 @@ __global__ void __launch_bounds__(256) k_count(TileArgs a) {
         }
 }
 
-// Exclusive scan of the tile counts by one CTA of 1024 threads: each thread
-// scans a contiguous run, the run totals are scanned across the CTA.
+// Exclusive scan of the tile counts by one CTA of 1024 threads, in chunks of
+// 4096 tiles: each thread takes four consecutive tiles of the chunk (one
+// 16-byte load; a warp reads 512 contiguous bytes), the thread sums are
+// scanned across the CTA, and a carry runs from chunk to chunk.  Each tile
+// with intersections is filed into its sort class.
 __global__ void __launch_bounds__(1024) k_scan(TileArgs a) {
     pdl_enter();
     __shared__ uint32_t warp_tot[32];
     __shared__ uint32_t max_warp[32];
     __shared__ uint32_t class_n[kSortClasses];
+    __shared__ uint32_t carry;
     const int T = a.num_tiles;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const uint32_t small_keys = a.sort_width == 256 ? (uint32_t)kSortSmallKeys : 0u;
-    if (threadIdx.x < kSortClasses) class_n[threadIdx.x] = 0;
-    const int per = (T + 1023) / 1024;
-    const int lo = min(T, (int)threadIdx.x * per), hi = min(T, lo + per);
-    uint32_t sum = 0, mx = 0;
-    for (int t = lo; t < hi; t++) { const uint32_t c = a.tile_counts[t]; sum += c; mx = max(mx, c); }
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    uint32_t incl = sum;
+    if (tid < kSortClasses) class_n[tid] = 0;
+    if (tid == 0) carry = 0;
+    uint32_t mx = 0;
+    for (int base = 0; base < T; base += 4096) {
+        const int t0 = base + 4 * tid;
+        uint32_t c[4] = {0u, 0u, 0u, 0u};
+        if (t0 + 3 < T) {
+            const uint4 q = *reinterpret_cast<const uint4 *>(a.tile_counts + t0);
+            c[0] = q.x; c[1] = q.y; c[2] = q.z; c[3] = q.w;
+        } else {
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += u;
-    }
-    const uint32_t wmax = __reduce_max_sync(0xffffffffu, mx);
-    if (lane == 31) warp_tot[wid] = incl;
-    if (lane == 0) max_warp[wid] = wmax;
-    __syncthreads();
-    if (wid == 0) {
-        uint32_t v = warp_tot[lane], inc = v;
+            for (int k = 0; k < 4; k++) c[k] = t0 + k < T ? a.tile_counts[t0 + k] : 0u;
+        }
+        const uint32_t sum = c[0] + c[1] + c[2] + c[3];
+        mx = max(mx, max(max(c[0], c[1]), max(c[2], c[3])));
+        uint32_t incl = sum;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
-            if (lane >= o) inc += u;
+            const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += u;
         }
-        warp_tot[lane] = inc - v;
-        const uint32_t m = __reduce_max_sync(0xffffffffu, max_warp[lane]);
-        if (lane == 0) max_warp[0] = m;
-    }
-    __syncthreads();
-    uint32_t run = warp_tot[wid] + incl - sum;
-    for (int t = lo; t < hi; t++) {
-        const uint32_t c = a.tile_counts[t];
-        a.tile_offsets[t] = run;
-        run += c;
-        // sort class of the tile: shared-memory sort by a 256-, 512- or
-        // 1024-thread CTA, or the global-memory sort above kSortHeavyKeys
-        if (c > 0) {
-            const int cls = c <= small_keys ? 0
-                            : c <= (uint32_t)kSortLightKeys ? 1
-                            : c <= (uint32_t)kSortHeavyKeys ? 2 : 3;
-            const uint32_t pos = atomicAdd(&class_n[cls], 1u);
-            a.tile_lists[(size_t)cls * T + pos] = (uint32_t)t;
+        if (lane == 31) warp_tot[wid] = incl;
+        __syncthreads();   // warp totals written; carry and class counts settled
+        if (wid == 0) {
+            const uint32_t v = warp_tot[lane];
+            uint32_t inc = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += u;
+            }
+            warp_tot[lane] = inc - v;
         }
+        __syncthreads();
+        uint32_t run = carry + warp_tot[wid] + incl - sum;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int t = t0 + k;
+            if (t >= T) break;
+            a.tile_offsets[t] = run;
+            run += c[k];
+            // sort class of the tile: shared-memory sort by a 256-, 512- or
+            // 1024-thread CTA, or the global-memory sort above kSortHeavyKeys
+            if (c[k] > 0) {
+                const int cls = c[k] <= small_keys ? 0
+                                : c[k] <= (uint32_t)kSortLightKeys ? 1
+                                : c[k] <= (uint32_t)kSortHeavyKeys ? 2 : 3;
+                const uint32_t pos = atomicAdd(&class_n[cls], 1u);
+                a.tile_lists[(size_t)cls * T + pos] = (uint32_t)t;
+            }
+        }
+        __syncthreads();   // every thread has read carry and warp_tot
+        if (tid == 1023) carry = run;   // the last thread's run ends the chunk
     }
-    if (threadIdx.x == 1023) a.tile_offsets[T] = run;
-    if (threadIdx.x == 0) a.max_tile_count[0] = max_warp[0];
+    const uint32_t wmax = __reduce_max_sync(0xffffffffu, mx);
+    if (lane == 0) max_warp[wid] = wmax;
     __syncthreads();
-    if (threadIdx.x < kSortClasses) {
-        a.tile_class[threadIdx.x] = class_n[threadIdx.x];                  // list lengths
-        a.tile_class[kSortClasses + threadIdx.x] = 0;                      // work counters of the sort kernels
+    if (tid == 0) {
+        uint32_t m = 0;
+        for (int k = 0; k < 32; k++) m = max(m, max_warp[k]);
+        a.max_tile_count[0] = m;
+        a.tile_offsets[T] = carry;
+    }
+    if (tid < kSortClasses) {
+        a.tile_class[tid] = class_n[tid];                  // list lengths
+        a.tile_class[kSortClasses + tid] = 0;              // work counters of the sort kernels
     }
 }
 
@@ -181,8 +203,9 @@ __global__ void __launch_bounds__(kAggThreads) k_count_agg(TileArgs a) {
 // Exclusive scan down each tile's column of CTA rows; the column total is the
 // tile's count.  A CTA covers 32 global tiles (one per lane, so each row
 // access is a 128-byte line while the lanes share a view) and splits the
-// rows over its 32 warps: row sums, a scan of the 32 partial sums per tile in
-// shared memory, then the rows rewritten.
+// rows over its 32 warps: row sums (the rows held in registers when a warp
+// has at most 16), a scan of the 32 partial sums per tile in shared memory,
+// then the rows rewritten.
 template <bool kViews>
 __global__ void __launch_bounds__(1024) k_cta_scan(TileArgs a, int ctas) {
     pdl_enter();
@@ -195,9 +218,24 @@ __global__ void __launch_bounds__(1024) k_cta_scan(TileArgs a, int ctas) {
     uint32_t *col = a.cta_bins + (size_t)ctas * vg.tile_base + (tc - vg.tile_base);
     const int per = (ctas + 31) / 32;
     const int c0 = min(ctas, w * per), c1 = min(ctas, c0 + per);
+    const bool in = t < a.num_tiles;
+    // up to kHeld rows per warp (2^20 Gaussians per view): all loads issued
+    // at once and kept in registers for the rewrite; more rows loop
+    constexpr int kHeld = 16;
+    const bool held_rows = per <= kHeld;   // CTA-uniform
+    uint32_t held[kHeld];
     uint32_t sum = 0;
-    if (t < a.num_tiles)
+    if (held_rows) {
+#pragma unroll
+        for (int k = 0; k < kHeld; k++) {
+            const int c = c0 + k;
+            held[k] = (in && c < c1) ? col[(size_t)c * Tv] : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < kHeld; k++) sum += held[k];
+    } else if (in) {
         for (int c = c0; c < c1; c++) sum += col[(size_t)c * Tv];
+    }
     part[w][lane] = sum;
     __syncthreads();
     uint32_t run = 0, total = 0;
@@ -206,11 +244,22 @@ __global__ void __launch_bounds__(1024) k_cta_scan(TileArgs a, int ctas) {
         if (k < w) run += v;
         total += v;
     }
-    if (t < a.num_tiles) {
-        for (int c = c0; c < c1; c++) {
-            const uint32_t v = col[(size_t)c * Tv];
-            col[(size_t)c * Tv] = run;
-            run += v;
+    if (in) {
+        if (held_rows) {
+#pragma unroll
+            for (int k = 0; k < kHeld; k++) {
+                const int c = c0 + k;
+                if (c < c1) {
+                    col[(size_t)c * Tv] = run;
+                    run += held[k];
+                }
+            }
+        } else {
+            for (int c = c0; c < c1; c++) {
+                const uint32_t v = col[(size_t)c * Tv];
+                col[(size_t)c * Tv] = run;
+                run += v;
+            }
         }
         if (w == 0) a.tile_counts[t] = total;
     }
