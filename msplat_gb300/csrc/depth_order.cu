@@ -6,7 +6,8 @@
 //      histogram -> scan -> scatter; inactive Gaussians (culled, or depth not
 //      finite and positive) carry the key 0xffffffff and sort last.  Stability
 //      puts equal depths in id order, the reference's tie rule.
-//   2. Their tile rectangles are written in that order (8 bytes each).
+//   2. Their tile rectangles (computed by the projection) are written in that
+//      order by the last sort pass (8 bytes each).
 //   3. The block-aggregated count and scatter of the other path run over the
 //      sorted positions p: CTA c covers p in [2048 c, 2048 c + 2048), so each
 //      tile's bucket is a sequence of per-CTA runs in increasing depth, and
@@ -93,10 +94,12 @@ __global__ void __launch_bounds__(256) k_gs_digit_scan(TileArgs a, int nb) {
 // of the block in eight rounds of 32; a key's place is its digit's offset for
 // the block + the same digit's keys in earlier warps + in earlier rounds of
 // its warp + in lower lanes of its round (peers found with eight ballots).
+// The last pass also writes each sorted position's tile rectangle (srect,
+// gathered from the projection's; empty for inactive keys).
 template <bool kFirst>
 __global__ void __launch_bounds__(kGsThreads) k_gs_scatter(TileArgs a, int shift, const uint32_t *key_in,
                                                            const uint32_t *val_in, uint32_t *key_out,
-                                                           uint32_t *val_out) {
+                                                           uint32_t *val_out, ushort4 *srect_out) {
     pdl_enter();
     __shared__ uint16_t wcnt[kGsThreads / 32][256];
     __shared__ uint16_t woff[kGsThreads / 32][256];
@@ -164,28 +167,10 @@ __global__ void __launch_bounds__(kGsThreads) k_gs_scatter(TileArgs a, int shift
         if (MS_GUARD(pos < (uint32_t)n, 7, pos, a.nan_counts ? a.nan_counts + kDbgSlot : nullptr)) {
             key_out[vb + pos] = kv[j];
             val_out[vb + pos] = vv[j];
+            if (srect_out)
+                srect_out[vb + pos] = kv[j] == 0xffffffffu ? make_ushort4(0, 0, 0, 0) : a.rect[vb + vv[j]];
         }
     }
-}
-
-// Tile rectangle of the Gaussian at each sorted position (empty when inactive).
-__global__ void __launch_bounds__(256) k_gs_rect(TileArgs a) {
-    pdl_enter();
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    const int view = blockIdx.y, n = a.vt.n;
-    if (p >= n) return;
-    const size_t vb = (size_t)view * n;
-    ushort4 r = make_ushort4(0, 0, 0, 0);
-    if (a.gs_key[0][vb + p] != 0xffffffffu) {
-        const uint32_t i = a.gs_val[0][vb + p];
-        const ViewGeom vg = view_geom(a.vt, view);
-        const float4 ra = a.rec[vb + i].a;
-        const float2 ab = a.aabb[vb + i];
-        int x0, y0, x1, y1;
-        tile_rect(ra.x, ra.y, ab.x, ab.y, vg.tiles_x, vg.tiles_y, x0, y0, x1, y1);
-        r = make_ushort4((unsigned short)x0, (unsigned short)y0, (unsigned short)x1, (unsigned short)y1);
-    }
-    a.srect[vb + p] = r;
 }
 
 // Block-aggregated count over sorted positions (k_count_agg's rows).
@@ -302,17 +287,16 @@ int launch_presorted_count(const TileArgs &a, cudaStream_t s) {
     const dim3 gd(32, views);   // 256 digits, 8 per CTA
     launch_pdl(k_gs_hist<true>, g, kGsThreads, 0, s, a, 0, nullptr);
     launch_pdl(k_gs_digit_scan, gd, 256, 0, s, a, nb);
-    launch_pdl(k_gs_scatter<true>, g, kGsThreads, 0, s, a, 0, nullptr, nullptr, a.gs_key[1], a.gs_val[1]);
+    launch_pdl(k_gs_scatter<true>, g, kGsThreads, 0, s, a, 0, nullptr, nullptr, a.gs_key[1], a.gs_val[1],
+               (ushort4 *)nullptr);
     for (int pass = 1; pass < 4; pass++) {
         const int src = pass & 1, dst = src ^ 1;
         launch_pdl(k_gs_hist<false>, g, kGsThreads, 0, s, a, 8 * pass, a.gs_key[src]);
         launch_pdl(k_gs_digit_scan, gd, 256, 0, s, a, nb);
         launch_pdl(k_gs_scatter<false>, g, kGsThreads, 0, s, a, 8 * pass, a.gs_key[src], a.gs_val[src], a.gs_key[dst],
-                                                      a.gs_val[dst]);
+                   a.gs_val[dst], pass == 3 ? a.srect : (ushort4 *)nullptr);
     }
     debug_sync(s, "depth_sort");
-    launch_pdl(k_gs_rect, dim3((n + 255) / 256, views), 256, 0, s, a);
-    debug_sync(s, "depth_rect");
     const int agg_blocks = (n + kAggPerCta - 1) / kAggPerCta;
     const size_t smem = (size_t)max_view_tiles(a.vt) * sizeof(uint32_t);
     static bool attr_set[64] = {false};
@@ -328,7 +312,7 @@ int launch_presorted_count(const TileArgs &a, cudaStream_t s) {
     }
     launch_pdl(k_count_agg_sorted, dim3(agg_blocks, views), kAggThreads, smem, s, a);
     debug_sync(s, "count_sorted");
-    return 12 + 1 + 1;
+    return 12 + 1;
 }
 
 int launch_presorted_build(const TileArgs &a, cudaStream_t s) {

@@ -193,6 +193,7 @@ class Engine {
             alloc("gs_hist", 4 * (size_t)B * 256 * ((N + 2047) / 2048));
             alloc("gs_dtot", 4 * (size_t)B * 256);
             alloc("srect", 8 * recs);
+            alloc("rect", 8 * recs);
         }
         const MsplatStepArgs &a0 = args[0];
         const bool opt = a0.do_optimizer && st;
@@ -218,6 +219,7 @@ class Engine {
         pa.sp = ptr<StepParams>("params");
         pa.rec = ptr<SplatRec>("rec"); pa.depths = ptr<float>("depths"); pa.radii = ptr<int>("radii");
         pa.aabb = ptr<float2>("aabb"); pa.tiles_hit = ptr<int>("tiles_hit");
+        pa.rect = presorted ? ptr<ushort4>("rect") : nullptr;
         pa.grad = backward ? ptr<GradRec>("grad") : nullptr;
         pa.nan_counts = ptr<unsigned>("nan_counts");
         launch_project_fwd(pa, stream_);
@@ -226,7 +228,7 @@ class Engine {
 
         TileArgs ta{};
         ta.vt = vt; ta.num_tiles = T; ta.capacity = cap; ta.sort_width = tune.sort_width;
-        ta.radii = pa.radii; ta.depths = pa.depths; ta.rec = pa.rec; ta.aabb = pa.aabb;
+        ta.radii = pa.radii; ta.depths = pa.depths; ta.rec = pa.rec; ta.aabb = pa.aabb; ta.rect = pa.rect;
         ta.tile_counts = ptr<uint32_t>("tile_counts"); ta.tile_write = ta.tile_counts + T;
         ta.tile_offsets = ptr<uint32_t>("tile_offsets"); ta.max_tile_count = ptr<uint32_t>("max_tile");
         ta.keys = ptr<uint64_t>("keys"); ta.keys_alt = ptr<uint64_t>("keys_alt");

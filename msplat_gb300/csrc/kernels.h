@@ -56,6 +56,7 @@ struct ProjectArgs {
     int *radii;
     float2 *aabb;
     int *tiles_hit;
+    ushort4 *rect;          // tile rectangle (x0, y0, x1, y1) where radii > 0 (nullable)
     GradRec *grad;          // zeroed here (nullable)
     unsigned *nan_counts;   // nullable
 };
@@ -91,6 +92,7 @@ struct TileArgs {
     uint32_t *gs_key[2], *gs_val[2];   // [views, n] sort buffers; ids in depth order end in gs_val[0]
     uint32_t *gs_hist;                 // [views, 256, ceil(n / 2048)] digit counts, then offsets in the digit
     uint32_t *gs_dtot;                 // [views, 256] keys per digit
+    const ushort4 *rect;               // [views, n] tile rectangles from the projection
     ushort4 *srect;                    // [views, n] tile rectangles in depth order
 };
 

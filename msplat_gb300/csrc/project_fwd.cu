@@ -233,6 +233,7 @@ __global__ void __launch_bounds__(256) k_project_fwd(ProjectArgs a) {
     a.rec[u] = rec;
     a.depths[u] = vz;
     a.aabb[u] = make_float2(ax, ay);
+    if (a.rect) a.rect[u] = make_ushort4((unsigned short)x0, (unsigned short)y0, (unsigned short)x1, (unsigned short)y1);
 
     // zombie gate: a non-finite projection output culls the Gaussian this step
     const bool okc = finite_bits(cxp) && finite_bits(cyp), okd = finite_bits(vz);
