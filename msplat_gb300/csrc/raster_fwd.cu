@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(kTileThreads, 8) k_raster_fwd(RasterArgs a) {
 }
 
 template <bool kViews, int kBatch>
-__global__ void __launch_bounds__(kTileThreads) k_raster_fwd_chunked(RasterArgs a) {
+__global__ void __launch_bounds__(kTileThreads, 8) k_raster_fwd_chunked(RasterArgs a) {
     pdl_enter();
     __shared__ BatchSmem<kBatch> sm;
     const int tile = blockIdx.x + a.tile_lo, k = blockIdx.y;

@@ -192,3 +192,51 @@ def test_batch_graph_replay_matches_eager():
     for k in E.GROUPS:
         base = getattr(init, k).reshape(pe[k].shape)
         assert rel_l2(pg[k] - base, pe[k] - base) <= 1e-4, k
+
+
+def test_batch_loss_with_masks_matches_single_views():
+    """The loss stage of a multi-view step with per-view masks (two masked
+    views, one without; masks reaching the image borders) against one-view
+    steps of the same views: each view's dL/dimage (scaled by 1/B in the
+    batch) and loss.  The one-view loss stage is the one the parity tests
+    hold to the oracle."""
+    torch = pytest.importorskip("torch")
+    sc = S.config_small(5)
+    cams = _mixed_views(sc)
+    gts = [torch.from_numpy(gt_image(sc.gt, c)).cuda() for c in cams]
+    init = S.init_from_gt(sc.gt, 5)
+    rng = np.random.default_rng(5)
+    masks = []
+    for k, c in enumerate(cams):
+        if k == 1:
+            masks.append(None)
+            continue
+        m = np.full((c.height, c.width), 255, np.uint8)
+        m[rng.random((c.height, c.width)) < 0.1] = 0
+        m[:7, :] = 0
+        m[:, -9:] = 0
+        masks.append(torch.from_numpy(m).cuda())
+    B = len(cams)
+    args = [E.make_args(E.camera_dict(c), E.step_scalars(10, 10, width=c.width, height=c.height), raster_mode=1)
+            for c in cams]
+    eng = E.Engine(0)
+    dg = E.DeviceGaussians(init)
+    eng.train_step_batch(dg, args, [g.data_ptr() for g in gts], [m.data_ptr() if m is not None else None for m in masks])
+    eng.synchronize()
+    P = [c.width * c.height for c in cams]
+    v_batch = eng.read("v_img", np.float32, 3 * sum(P))
+    loss_batch = eng.loss()
+    eng.close()
+    off, losses = 0, []
+    for k, c in enumerate(cams):
+        e1 = E.Engine(0)
+        d1 = E.DeviceGaussians(init)
+        e1.train_step(d1, args[k], gts[k].data_ptr(), masks[k].data_ptr() if masks[k] is not None else None)
+        e1.synchronize()
+        v1 = e1.read("v_img", np.float32, 3 * P[k])
+        losses.append(e1.loss())
+        e1.close()
+        vb = v_batch[off:off + 3 * P[k]].astype(np.float64) * B
+        off += 3 * P[k]
+        assert rel_l2(vb, v1) <= 1e-6, k
+    assert abs(loss_batch - np.mean(losses)) <= 1e-6 * abs(np.mean(losses))
