@@ -225,9 +225,9 @@ int msplat_engine_set_isect_budget(MsplatEngine *e, long long slots);
 /* Launch configuration of the tunable stages (no counterpart in the
  * reference; the defaults are the reference's choices).  None changes the
  * tile lists; sort_width, raster_batch and tile_order leave every output
- * bit-identical,
- * raster_mode and chunk change the image at float rounding (as the
- * reference's own monolithic / chunked choice does). */
+ * bit-identical, bwd_pixels changes the gradients at float rounding (the
+ * order of the sums), raster_mode and chunk change the image at float
+ * rounding (as the reference's own monolithic / chunked choice does). */
 typedef struct {
     int sort_width;    /* CTA width of the lightest shared-memory tile sort: 256 (tiles up to
                           2048 keys) or 512 (up to 4096); default 512 */
@@ -241,6 +241,9 @@ typedef struct {
                           each tile's keys (default), 1 one depth sort per view before the
                           scatter, then each tile's per-CTA runs put in order (same lists; views
                           of at most 20480 tiles, else 0) */
+    int bwd_pixels;    /* pixels per thread of the raster backward: 1 (256 threads per tile,
+                          8x4-pixel warps; default) or 2 (128 threads, 8x8-pixel warps: one
+                          warp reduction per 64 pixels, more work per CTA) */
 } MsplatTuning;
 
 int msplat_engine_set_tuning(MsplatEngine *e, const MsplatTuning *t);
@@ -249,8 +252,8 @@ int msplat_engine_get_tuning(MsplatEngine *e, MsplatTuning *t);
 /* Autotuner: times full training steps of the given views (forward, loss,
  * backward; no optimizer update and no SGLD, so the parameters do not
  * change) under candidate configurations, one coordinate at a time (tile
- * order, sort width, tile batch, then raster mode with chunk length when
- * args[0].raster_mode is 0), keeps the fastest (the median of `reps` timed
+ * order, sort width, tile batch, backward pixels per thread, then raster
+ * mode with chunk length when args[0].raster_mode is 0), keeps the fastest (the median of `reps` timed
  * steps) and leaves it set.  gt[v] must be given for every view.  `out`
  * receives the chosen configuration and *ms (nullable) its step time. */
 int msplat_engine_autotune(MsplatEngine *e, const MsplatGaussians *g, const MsplatStepArgs *args, int num_views,

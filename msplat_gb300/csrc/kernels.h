@@ -103,6 +103,7 @@ struct RasterArgs {
     long long isect_lo;         // global intersection slot held at isect_ids[0]
     int chunk;                  // splats per depth chunk (chunked raster)
     int batch;                  // splats staged per shared-memory round: 128 or 256
+    int bwd_px;                 // pixels per thread of the backward: 1 (256 threads) or 2 (128)
     long long capacity;
     const StepParams *sp;       // [views]
     const uint32_t *tile_offsets;

@@ -1,12 +1,15 @@
 // Back-to-front rasterizer VJP w.r.t. splat centre, conic, raw colour and
-// opacity logit.  One CTA per 16x16 tile (chunked: per (tile, chunk)), one
-// thread per pixel.  Per splat each warp reduces its pixels' 9 partial
-// gradients with a transpose-reduce (9 shuffles for 8 values plus 5 for the
-// ninth, instead of 45; paired fp32 adds), warps combine through
-// shared-memory adds, and each
-// batch flushes one set of three float4 vector atomics per (splat, tile)
-// instead of the reference's nine scalar atomics per (splat, warp).  A warp
-// skips the splats whose reach box (warp_reach) misses its 8x4 pixel block.
+// opacity logit.  One CTA per 16x16 tile (chunked: per (tile, chunk)), in one
+// of two layouts (MsplatTuning.bwd_pixels): one pixel per thread, 256
+// threads, each warp an 8x4 block; or two pixels per thread (four rows
+// apart), 128 threads, each warp an 8x8 block, so one warp reduction serves
+// 64 pixels (fewer reductions, more work per CTA).  Per splat each warp
+// reduces its pixels' 9 partial gradients with a transpose-reduce (9
+// shuffles for 8 values plus 5 for the ninth, instead of 45; paired fp32
+// adds), warps combine through shared-memory adds, and each batch flushes one
+// set of three float4 vector atomics per (splat, tile) instead of the
+// reference's nine scalar atomics per (splat, warp).  A warp skips the
+// splats whose reach box misses its block.
 // Follows rasterize_backward_kernel (msplat_metal.metal:931-1135),
 // compute_chunk_prefix_suffix_kernel (:3139-3175) and
 // rasterize_backward_chunked_kernel (:3179-3366), including its quirk that a
@@ -18,13 +21,45 @@
 
 namespace msplat {
 
+// Thread layouts.  kPx = 1: warp w covers the 8x4 block of tile_px /
+// tile_py.  kPx = 2: warp w covers x in [8(w&1), 8(w&1)+8), y in
+// [8(w>>1), 8(w>>1)+8); the thread's column is lane & 7, its rows
+// (lane >> 3) and (lane >> 3) + 4.
+template <int kPx> struct BwdLayout;
+template <> struct BwdLayout<1> {
+    static constexpr int kThreads = 256;
+    static __device__ __forceinline__ int px(int tid) { return tile_px(tid); }
+    static __device__ __forceinline__ int py(int tid) { return tile_py(tid); }
+    static __device__ __forceinline__ uint32_t reach(float x, float y, float hx, float hy, float ox, float oy) {
+        return warp_reach(x, y, hx, hy, ox, oy);
+    }
+};
+template <> struct BwdLayout<2> {
+    static constexpr int kThreads = 128;
+    static __device__ __forceinline__ int px(int tid) { return (tid & 7) | ((tid >> 2) & 8); }
+    static __device__ __forceinline__ int py(int tid) { return (tid >> 3) & 11; }
+    // warp_reach for the 8x8 blocks: bit w when block w meets the splat's
+    // reach box (the same conservative margins)
+    static __device__ __forceinline__ uint32_t reach(float x, float y, float hx, float hy, float ox, float oy) {
+        if (!(hx <= 3.0e38f && hy <= 3.0e38f)) return 0xFu;
+        if (hx < 0.f || hy < 0.f) return 0u;
+        const float lx = x - ox, ly = y - oy;
+        const float rx = hx + 0.02f + 1e-6f * (fabsf(lx) + hx + fabsf(ox));
+        const float ry = hy + 0.02f + 1e-6f * (fabsf(ly) + hy + fabsf(oy));
+        const float x0 = lx - rx, x1 = lx + rx, y0 = ly - ry, y1 = ly + ry;
+        const uint32_t cols = (x1 >= 0.f && x0 <= 7.f ? 0x5u : 0u) | (x1 >= 8.f && x0 <= 15.f ? 0xAu : 0u);
+        const uint32_t rows = (y1 >= 0.f && y0 <= 7.f ? 0x3u : 0u) | (y1 >= 8.f && y0 <= 15.f ? 0xCu : 0u);
+        return cols & rows;
+    }
+};
+
 // kBB splats staged per round (the tile batch: 128 or 256)
-template <int kBB> struct BwdSmem {
+template <int kBB, int kPx> struct BwdSmem {
     float4 xyo[kBB];    // x, y, opacity, id bits
-    float4 con[kBB];    // conic, bits of the warps the splat reaches (warp_reach)
+    float4 con[kBB];    // conic, bits of the warps the splat reaches
     float4 rgb[kBB];    // clamped colour, w: bits of the channels with raw + 0.5 >= 0
     float acc[kBB][9];  // r g b | ca cb cc | x y | opacity
-    int wmax[8];
+    int wmax[BwdLayout<kPx>::kThreads / 32];
 };
 
 // Sums over the warp of 8 per-lane values v[] and of one more value w: lane
@@ -69,33 +104,71 @@ struct PixelState {
     float T;                  // transmittance in front of the current splat
     float S;                  // (colour behind + T_final * background) . dL/dpixel
     float vr, vg, vb;         // dL/dpixel
-    float px, py;
+    float py;                 // row (the column is shared by the thread's two pixels)
     int bin_final;            // last splat index this pixel may take gradient from (-1: none)
 };
 
-// Processes splat indices [s, hi] back to front for the whole CTA.
-template <int kBB>
-__device__ void backward_range(BwdSmem<kBB> &sm, const RasterArgs &a, int s, int hi, PixelState &ps, GradRec *grad) {
+// One pixel's part of splat (xo, cn) of batch slot t: its transmittance and
+// S updates and its gradient contributions added to v, v8 (valid: the
+// pixel takes the splat; alpha < 0.999 checked here).
+// kAdd: add to v (a second pixel), else assign (the first)
+template <bool kAdd>
+__device__ __forceinline__ void pixel_step(PixelState &ps, float dx, float dy, float alpha, const float4 &rc,
+                                           float v[8], float &v8) {
+    if (!(alpha < 0.999f)) return;
+    const float ra = __fdividef(1.f, 1.f - alpha);   // fast reciprocal, 1 - alpha in [0.001, 0.997]
+    ps.T *= ra;
+    const float fac = alpha * ps.T;
+    const float cv = __fmaf_rn(rc.x, ps.vr, __fmaf_rn(rc.y, ps.vg, rc.z * ps.vb));
+    const float v_alpha = __fmaf_rn(ps.T, cv, -ra * ps.S);
+    ps.S = __fmaf_rn(fac, cv, ps.S);
+    const float v_sigma = -alpha * v_alpha;
+    const float A = v_sigma * dx, B = v_sigma * dy;
+    const float c[9] = {fac * ps.vr, fac * ps.vg, fac * ps.vb, A * dx, A * dy, B * dy, A, B, v_sigma};
+#pragma unroll
+    for (int k = 0; k < 8; k++) v[k] = kAdd ? v[k] + c[k] : c[k];
+    v8 = kAdd ? v8 + c[8] : c[8];
+}
+
+// sigma and alpha exactly as the forward pass rounds them (no contraction),
+// so both passes take the same splats; false when the pixel does not take it
+__device__ __forceinline__ bool splat_alpha(const float4 &xo, const float4 &cn, float dx, float dy, float &alpha) {
+    const float sigma = __fmaf_rn(0.5f, __fmaf_rn(cn.x, __fmul_rn(dx, dx), __fmul_rn(__fmul_rn(cn.z, dy), dy)),
+                                  __fmul_rn(__fmul_rn(cn.y, dx), dy));
+    if (!(sigma >= 0.f && sigma < 5.55f)) return false;   // NaN fails too
+    alpha = fminf(0.999f, __fmul_rn(xo.z, det_expf_neg(-sigma)));
+    return !(alpha < 1.f / 255.f);
+}
+
+// Processes splat indices [s, hi] back to front for the whole CTA; px is
+// the thread's column, ps its kPx pixels.
+template <int kBB, int kPx>
+__device__ void backward_range(BwdSmem<kBB, kPx> &sm, const RasterArgs &a, int s, int hi, PixelState (&ps)[kPx],
+                               float px, GradRec *grad) {
+    using L = BwdLayout<kPx>;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int wbin = __reduce_max_sync(0xffffffffu, ps.bin_final);
-    const float ox = ps.px - (float)tile_px(tid), oy = ps.py - (float)tile_py(tid);
+    int bmax = ps[0].bin_final;
+#pragma unroll
+    for (int r = 1; r < kPx; r++) bmax = max(bmax, ps[r].bin_final);
+    const int wbin = __reduce_max_sync(0xffffffffu, bmax);
+    const float ox = px - (float)L::px(tid), oy = ps[0].py - (float)L::py(tid);   // the tile's first pixel
     for (int batch_end = hi; batch_end >= s; batch_end -= kBB) {
         __syncthreads();
-        const int idx = batch_end - tid;
-        if (tid < kBB) {
+        for (int k = tid; k < kBB; k += L::kThreads) {
+            const int idx = batch_end - k;
             if (idx >= s) {
                 const SplatRec r = isect_record(a.isect_ids, a.rec, a.n, idx);
-                sm.xyo[tid] = r.a;
-                sm.con[tid] = make_float4(r.b.x, r.b.y, r.b.z,
-                                          __uint_as_float(warp_reach(r.a.x, r.a.y, r.b.w, r.c.w, ox, oy)));
+                sm.xyo[k] = r.a;
+                sm.con[k] = make_float4(r.b.x, r.b.y, r.b.z,
+                                        __uint_as_float(L::reach(r.a.x, r.a.y, r.b.w, r.c.w, ox, oy)));
                 // clamped colour max(raw + 0.5, 0); w: channels whose raw + 0.5 >= 0
                 // (the only ones that pass a colour gradient back)
                 const float cr = r.c.x + 0.5f, cg = r.c.y + 0.5f, cb = r.c.z + 0.5f;
                 const int mask = (cr >= 0.f ? 1 : 0) | (cg >= 0.f ? 2 : 0) | (cb >= 0.f ? 4 : 0);
-                sm.rgb[tid] = make_float4(fmaxf(cr, 0.f), fmaxf(cg, 0.f), fmaxf(cb, 0.f), __int_as_float(mask));
+                sm.rgb[k] = make_float4(fmaxf(cr, 0.f), fmaxf(cg, 0.f), fmaxf(cb, 0.f), __int_as_float(mask));
             }
 #pragma unroll
-            for (int k = 0; k < 9; k++) sm.acc[tid][k] = 0.f;
+            for (int j = 0; j < 9; j++) sm.acc[k][j] = 0.f;
         }
         __syncthreads();
         const int nb = min(kBB, batch_end - s + 1);
@@ -104,69 +177,49 @@ __device__ void backward_range(BwdSmem<kBB> &sm, const RasterArgs &a, int s, int
             if (!((__float_as_uint(cn.w) >> warp) & 1u)) continue;   // no pixel of this warp takes it
             const int sidx = batch_end - t;
             const float4 xo = sm.xyo[t];
-            bool valid = sidx <= ps.bin_final;
-            float dx = 0.f, dy = 0.f, alpha = 0.f;
-            if (valid) {
-                // sigma and alpha exactly as the forward pass rounds them (no
-                // contraction), so both passes take the same splats
-                dx = __fsub_rn(xo.x, ps.px);
-                dy = __fsub_rn(xo.y, ps.py);
-                const float sigma = __fmaf_rn(0.5f, __fmaf_rn(cn.x, __fmul_rn(dx, dx), __fmul_rn(__fmul_rn(cn.z, dy), dy)),
-                                              __fmul_rn(__fmul_rn(cn.y, dx), dy));
-                if (!(sigma >= 0.f && sigma < 5.55f)) {   // NaN fails too
-                    valid = false;
-                } else {
-                    alpha = fminf(0.999f, __fmul_rn(xo.z, det_expf_neg(-sigma)));
-                    if (alpha < 1.f / 255.f) valid = false;
-                }
+            const float dx = __fsub_rn(xo.x, px);
+            float dy[kPx], al[kPx];
+            bool on[kPx], any_on = false;
+#pragma unroll
+            for (int r = 0; r < kPx; r++) {
+                dy[r] = __fsub_rn(xo.y, ps[r].py);
+                al[r] = 0.f;
+                on[r] = sidx <= ps[r].bin_final && splat_alpha(xo, cn, dx, dy[r], al[r]);
+                any_on |= on[r];
             }
-            if (!__any_sync(0xffffffffu, valid)) continue;
+            if (!__any_sync(0xffffffffu, any_on)) continue;
             // per lane, with A = dL/dsigma dx and B = dL/dsigma dy: v[0..2] the
             // colour gradient, v[3..5] = (A dx, A dy, B dy) (half the conic
-            // gradient), v[6..7] = (A, B), v8 = dL/dsigma.  The splat's constants
-            // are applied once to the sums: conic x 0.5, centre = conic-weighted
-            // (A, B), opacity logit -(1 - opacity) x sum(dL/dsigma)
+            // gradient), v[6..7] = (A, B), v8 = dL/dsigma, both pixels summed.
+            // The splat's constants are applied once to the sums: conic x 0.5,
+            // centre = conic-weighted (A, B), opacity logit -(1 - opacity) x
+            // sum(dL/dsigma)
             float v[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             float v8 = 0.f;
-            if (valid && alpha < 0.999f) {
-                const float4 rc = sm.rgb[t];
-                const float ra = __fdividef(1.f, 1.f - alpha);   // fast reciprocal, 1 - alpha in [0.001, 0.997]
-                ps.T *= ra;
-                const float fac = alpha * ps.T;
-                const float cv = __fmaf_rn(rc.x, ps.vr, __fmaf_rn(rc.y, ps.vg, rc.z * ps.vb));
-                const float v_alpha = __fmaf_rn(ps.T, cv, -ra * ps.S);
-                ps.S = __fmaf_rn(fac, cv, ps.S);
-                const float v_sigma = -alpha * v_alpha;
-                const float A = v_sigma * dx, B = v_sigma * dy;
-                v[0] = fac * ps.vr;
-                v[1] = fac * ps.vg;
-                v[2] = fac * ps.vb;
-                v[3] = A * dx;
-                v[4] = A * dy;
-                v[5] = B * dy;
-                v[6] = A;
-                v[7] = B;
-                v8 = v_sigma;
-            }
+            const float4 rc = sm.rgb[t];
+            if (on[0]) pixel_step<false>(ps[0], dx, dy[0], al[0], rc, v, v8);
+#pragma unroll
+            for (int r = 1; r < kPx; r++)
+                if (on[r]) pixel_step<true>(ps[r], dx, dy[r], al[r], rc, v, v8);
             const float s8 = transpose_reduce8(v, v8, lane);
             if ((lane & 3) == 0) atomicAdd(&sm.acc[t][lane >> 2], s8);
             if (lane == 1) atomicAdd(&sm.acc[t][8], v8);
         }
         __syncthreads();
-        if (tid < nb) {
-            const float *g = sm.acc[tid];
-            const int mask = __float_as_int(sm.rgb[tid].w);
+        for (int k = tid; k < nb; k += L::kThreads) {
+            const float *g = sm.acc[k];
+            const int mask = __float_as_int(sm.rgb[k].w);
             const float gr = (mask & 1) ? g[0] : 0.f;
             const float gg = (mask & 2) ? g[1] : 0.f;
             const float gb = (mask & 4) ? g[2] : 0.f;
-            const float4 cn = sm.con[tid];
-            const float gop = -(1.f - sm.xyo[tid].z) * g[8];
+            const float4 cn = sm.con[k];
+            const float gop = -(1.f - sm.xyo[k].z) * g[8];
             const float gx = __fmaf_rn(cn.x, g[6], cn.y * g[7]), gy = __fmaf_rn(cn.y, g[6], cn.z * g[7]);
             const float ca = 0.5f * g[3], cb = 0.5f * g[4], cc = 0.5f * g[5];
             const bool any = (gr != 0.f) | (gg != 0.f) | (gb != 0.f) | (ca != 0.f) | (cb != 0.f) | (cc != 0.f) |
                              (gx != 0.f) | (gy != 0.f) | (gop != 0.f);
             if (any) {
-                GradRec *dst = grad + __float_as_int(sm.xyo[tid].w);
+                GradRec *dst = grad + __float_as_int(sm.xyo[k].w);
                 atomic_add_f4(&dst->a, make_float4(gx, gy, gop, 0.f));
                 atomic_add_f4(&dst->b, make_float4(ca, cb, cc, 0.f));
                 atomic_add_f4(&dst->c, make_float4(gr, gg, gb, 0.f));
@@ -175,13 +228,13 @@ __device__ void backward_range(BwdSmem<kBB> &sm, const RasterArgs &a, int s, int
     }
 }
 
-__device__ __forceinline__ int block_max(int v, int *wmax) {
+template <int kWarps> __device__ __forceinline__ int block_max(int v, int *wmax) {
     const int w = __reduce_max_sync(0xffffffffu, v);
     if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = w;
     __syncthreads();
     int m = wmax[0];
 #pragma unroll
-    for (int k = 1; k < kTileThreads / 32; k++) m = max(m, wmax[k]);
+    for (int k = 1; k < kWarps; k++) m = max(m, wmax[k]);
     __syncthreads();
     return m;
 }
@@ -193,14 +246,15 @@ struct BwdPixel {
 };
 
 // kViews: look the view up from the global tile index; false: one view
-template <bool kViews> __device__ __forceinline__ BwdPixel bwd_pixel(const RasterArgs &a, int tile) {
+// row: the thread's r-th pixel (4 r rows down)
+template <bool kViews, int kPx> __device__ __forceinline__ BwdPixel bwd_pixel(const RasterArgs &a, int tile, int row) {
     BwdPixel tp;
     tp.view = kViews ? view_of_tile(a.vt, tile) : 0;
     const ViewGeom vg = view_geom(a.vt, tp.view);
     const int lt = tile - vg.tile_base;
     const int tx = lt % vg.tiles_x, ty = lt / vg.tiles_x;
-    tp.x = tx * kTile + tile_px(threadIdx.x);
-    tp.y = ty * kTile + tile_py(threadIdx.x);
+    tp.x = tx * kTile + BwdLayout<kPx>::px(threadIdx.x);
+    tp.y = ty * kTile + BwdLayout<kPx>::py(threadIdx.x) + 4 * row;
     tp.inside = tp.x < vg.width && tp.y < vg.height;
     tp.p = tp.inside ? vg.pix_base + (long long)tp.y * vg.width + tp.x : 0;
     return tp;
@@ -217,25 +271,31 @@ __device__ __forceinline__ void init_pixel(PixelState &ps, const RasterArgs &a, 
     ps.vg = tp.inside ? a.v_img[3 * p + 1] : 0.f;
     ps.vb = tp.inside ? a.v_img[3 * p + 2] : 0.f;
     ps.S = (behind_r + Tf * sp.bg[0]) * ps.vr + (behind_g + Tf * sp.bg[1]) * ps.vg + (behind_b + Tf * sp.bg[2]) * ps.vb;
-    ps.px = (float)tp.x;
     ps.py = (float)tp.y;
 }
 
-template <bool kViews, int kBB>
-__global__ void __launch_bounds__(kTileThreads) k_raster_bwd(RasterArgs a) {
+template <bool kViews, int kBB, int kPx>
+__global__ void __launch_bounds__(BwdLayout<kPx>::kThreads, kPx == 2 ? 8 : 6) k_raster_bwd(RasterArgs a) {
     pdl_enter();
-    __shared__ BwdSmem<kBB> sm;
+    __shared__ BwdSmem<kBB, kPx> sm;
     const int tile = blockIdx.x + a.tile_lo;
     const int s = clamp_off(a.tile_offsets[tile], a.isect_lo, a.capacity), e = clamp_off(a.tile_offsets[tile + 1], a.isect_lo, a.capacity);
     if (s >= e) return;
-    const BwdPixel tp = bwd_pixel<kViews>(a, tile);
-    PixelState ps;
-    const float Tf = tp.inside ? a.final_T[tp.p] : 0.f;
-    init_pixel(ps, a, tp, Tf, 0.f, 0.f, 0.f);
-    ps.bin_final = tp.inside ? a.final_idx[tp.p] : -1;
-    const int hi = min(e - 1, block_max(ps.bin_final, sm.wmax));
+    PixelState ps[kPx];
+    float px = 0.f;
+    int bmax = -1;
+#pragma unroll
+    for (int r = 0; r < kPx; r++) {
+        const BwdPixel tp = bwd_pixel<kViews, kPx>(a, tile, r);
+        const float Tf = tp.inside ? a.final_T[tp.p] : 0.f;
+        init_pixel(ps[r], a, tp, Tf, 0.f, 0.f, 0.f);
+        ps[r].bin_final = tp.inside ? a.final_idx[tp.p] : -1;
+        bmax = max(bmax, ps[r].bin_final);
+        px = (float)tp.x;
+    }
+    const int hi = min(e - 1, block_max<BwdLayout<kPx>::kThreads / 32>(bmax, sm.wmax));
     if (hi < s) return;
-    backward_range<kBB>(sm, a, s, hi, ps, a.grad);
+    backward_range<kBB, kPx>(sm, a, s, hi, ps, px, a.grad);
 }
 
 __global__ void __launch_bounds__(256) k_chunk_prefix_suffix(RasterArgs a) {
@@ -262,43 +322,56 @@ __global__ void __launch_bounds__(256) k_chunk_prefix_suffix(RasterArgs a) {
     }
 }
 
-template <bool kViews, int kBB>
-__global__ void __launch_bounds__(kTileThreads) k_raster_bwd_chunked(RasterArgs a) {
+template <bool kViews, int kBB, int kPx>
+__global__ void __launch_bounds__(BwdLayout<kPx>::kThreads, kPx == 2 ? 8 : 6) k_raster_bwd_chunked(RasterArgs a) {
     pdl_enter();
-    __shared__ BwdSmem<kBB> sm;
+    __shared__ BwdSmem<kBB, kPx> sm;
     const int tile = blockIdx.x + a.tile_lo, k = blockIdx.y;
     const int s0 = clamp_off(a.tile_offsets[tile], a.isect_lo, a.capacity), e0 = clamp_off(a.tile_offsets[tile + 1], a.isect_lo, a.capacity);
     const int cs = s0 + k * a.chunk, ce = min(s0 + (k + 1) * a.chunk, e0);
     if (cs >= ce) return;
-    const BwdPixel tp = bwd_pixel<kViews>(a, tile);
     const size_t P = (size_t)a.vt.pixels;
-    const size_t o = (size_t)k * P + (size_t)tp.p;
-    PixelState ps;
-    init_pixel(ps, a, tp, tp.inside ? a.prefix_T[o] * a.chunk_T[o] : 0.f, tp.inside ? a.after_C[3 * o] : 0.f,
-               tp.inside ? a.after_C[3 * o + 1] : 0.f, tp.inside ? a.after_C[3 * o + 2] : 0.f);
-    const int bf = tp.inside ? a.chunk_idx[o] : -1;
-    ps.bin_final = (bf >= cs) ? bf : -1;
-    const int hi = min(ce - 1, block_max(ps.bin_final, sm.wmax));
+    PixelState ps[kPx];
+    float px = 0.f;
+    int bmax = -1;
+#pragma unroll
+    for (int r = 0; r < kPx; r++) {
+        const BwdPixel tp = bwd_pixel<kViews, kPx>(a, tile, r);
+        const size_t o = (size_t)k * P + (size_t)tp.p;
+        init_pixel(ps[r], a, tp, tp.inside ? a.prefix_T[o] * a.chunk_T[o] : 0.f, tp.inside ? a.after_C[3 * o] : 0.f,
+                   tp.inside ? a.after_C[3 * o + 1] : 0.f, tp.inside ? a.after_C[3 * o + 2] : 0.f);
+        const int bf = tp.inside ? a.chunk_idx[o] : -1;
+        ps[r].bin_final = (bf >= cs) ? bf : -1;
+        bmax = max(bmax, ps[r].bin_final);
+        px = (float)tp.x;
+    }
+    const int hi = min(ce - 1, block_max<BwdLayout<kPx>::kThreads / 32>(bmax, sm.wmax));
     if (hi < cs) return;
-    backward_range<kBB>(sm, a, cs, hi, ps, a.grad);
+    backward_range<kBB, kPx>(sm, a, cs, hi, ps, px, a.grad);
 }
 
-template <int kBB> static void raster_bwd_batch(const RasterArgs &a, cudaStream_t s) {
+template <int kBB, int kPx> static void raster_bwd_batch(const RasterArgs &a, cudaStream_t s) {
     const bool views = a.vt.count > 1;
+    constexpr int kT = BwdLayout<kPx>::kThreads;
     if (a.k_max <= 1) {
-        if (views) launch_pdl(k_raster_bwd<true, kBB>, a.num_tiles, kTileThreads, 0, s, a);
-        else launch_pdl(k_raster_bwd<false, kBB>, a.num_tiles, kTileThreads, 0, s, a);
+        if (views) launch_pdl(k_raster_bwd<true, kBB, kPx>, a.num_tiles, kT, 0, s, a);
+        else launch_pdl(k_raster_bwd<false, kBB, kPx>, a.num_tiles, kT, 0, s, a);
     } else {
         const long long P = a.vt.pixels;
         launch_pdl(k_chunk_prefix_suffix, (unsigned)((P + 255) / 256), 256, 0, s, a);
-        if (views) launch_pdl(k_raster_bwd_chunked<true, kBB>, dim3(a.num_tiles, a.k_max), kTileThreads, 0, s, a);
-        else launch_pdl(k_raster_bwd_chunked<false, kBB>, dim3(a.num_tiles, a.k_max), kTileThreads, 0, s, a);
+        if (views) launch_pdl(k_raster_bwd_chunked<true, kBB, kPx>, dim3(a.num_tiles, a.k_max), kT, 0, s, a);
+        else launch_pdl(k_raster_bwd_chunked<false, kBB, kPx>, dim3(a.num_tiles, a.k_max), kT, 0, s, a);
     }
 }
 
 void launch_raster_bwd(const RasterArgs &a, cudaStream_t s) {
-    if (a.batch == 128) raster_bwd_batch<128>(a, s);
-    else raster_bwd_batch<256>(a, s);
+    if (a.bwd_px == 2) {
+        if (a.batch == 128) raster_bwd_batch<128, 2>(a, s);
+        else raster_bwd_batch<256, 2>(a, s);
+    } else {
+        if (a.batch == 128) raster_bwd_batch<128, 1>(a, s);
+        else raster_bwd_batch<256, 1>(a, s);
+    }
 }
 
 }  // namespace msplat
