@@ -38,6 +38,26 @@ struct Buf {
     size_t bytes = 0;
 };
 
+// The step scalars of every view as one kernel argument: the upload before
+// each step (or graph replay) is a kernel launch on the engine's stream, not
+// a copy-engine transfer between the previous step's kernels and the next.
+struct ParamsPack {
+    StepParams p[kMaxViews];
+};
+static_assert(sizeof(ParamsPack) <= 32000, "kernel argument size");
+static_assert(sizeof(StepParams) % 4 == 0, "StepParams is copied in words");
+
+__global__ void __launch_bounds__(256) k_set_params(StepParams *dst, const __grid_constant__ ParamsPack pk, int words) {
+    const uint32_t *src = reinterpret_cast<const uint32_t *>(&pk);
+    uint32_t *d = reinterpret_cast<uint32_t *>(dst);
+    for (int i = threadIdx.x; i < words; i += blockDim.x) d[i] = src[i];
+}
+
+// n floats to page-locked host memory (through its device mapping)
+__global__ void k_copy_out(float *dst, const float *src, int n) {
+    if ((int)threadIdx.x < n) dst[threadIdx.x] = src[threadIdx.x];
+}
+
 class Engine {
   public:
     explicit Engine(int device) : device_(device) {
@@ -114,8 +134,17 @@ class Engine {
     // stream without waiting: page-locked `dst` is filled when the stream
     // gets there.
     void loss_async(float *dst) {
-        CK(cudaMemcpyAsync(dst, ptr<float>("loss_sum"), sizeof(float) * std::max(1, last_views_),
-                           cudaMemcpyDeviceToHost, stream_));
+        const int n = std::max(1, last_views_);
+        cudaPointerAttributes at{};
+        if (cudaPointerGetAttributes(&at, dst) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer) {
+            // page-locked: a one-warp kernel writes through the mapping (no
+            // copy-engine transfer on the step stream)
+            k_copy_out<<<1, 32, 0, stream_>>>(static_cast<float *>(at.devicePointer), ptr<float>("loss_sum"), n);
+            CK(cudaGetLastError());
+        } else {
+            cudaGetLastError();   // an unregistered pointer is not an error here
+            CK(cudaMemcpyAsync(dst, ptr<float>("loss_sum"), sizeof(float) * n, cudaMemcpyDeviceToHost, stream_));
+        }
     }
 
     // Multi-view step: B views (any sizes) rendered and back-propagated by
@@ -169,7 +198,9 @@ class Engine {
         for (int v = 0; v < B; v++) last_view_P_[v] = (long long)w[v] * h[v];
         if (timing_) slot_ = (timed_steps_++) % kRing;
 
-        StepParams sps[kMaxViews];
+        ParamsPack pack;
+        std::memset(&pack, 0, sizeof(pack));
+        StepParams *sps = pack.p;
         for (int v = 0; v < B; v++) {
             const uint8_t *mk = (has_gt && masks) ? masks[v] : nullptr;
             fill_params(args[v], sps[v], mk != nullptr);
@@ -177,10 +208,13 @@ class Engine {
             sps[v].mask = mk;
             if (B > 1) sps[v].loss_inv_n = args[v].loss_inv_n / (float)B;
         }
-        // pageable source: the copy has consumed it when the call returns.
-        // It stays outside any captured graph: kernels read the scalars
-        // through this device block, so a replay sees this step's values.
-        CK(cudaMemcpyAsync(ptr<StepParams>("params"), sps, sizeof(StepParams) * B, cudaMemcpyHostToDevice, stream_));
+        // The upload stays outside any captured graph: kernels read the
+        // scalars through this device block, so a replay sees this step's
+        // values.  A plain launch: it runs after the previous step's kernels
+        // (which read the block) have finished.
+        k_set_params<<<1, 256, 0, stream_>>>(ptr<StepParams>("params"), pack,
+                                             (int)(sizeof(StepParams) * B / 4));
+        CK(cudaGetLastError());
         // every buffer the step touches exists now (sized above), so a capture
         // below allocates nothing
         const size_t cb = tile_cta_bins_bytes(vt);
