@@ -143,7 +143,7 @@ class Engine {
             CK(cudaGetLastError());
         } else {
             cudaGetLastError();   // an unregistered pointer is not an error here
-            CK(cudaMemcpyAsync(dst, ptr<float>("loss_sum"), sizeof(float) * n, cudaMemcpyDeviceToHost, stream_));
+            CK(cudaMemcpyAsync(dst, ptr<float>("loss_sum"), sizeof(float) * n, cudaMemcpyDefault, stream_));
         }
     }
 
