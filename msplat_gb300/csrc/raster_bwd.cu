@@ -104,14 +104,13 @@ struct PixelState {
     float T;                  // transmittance in front of the current splat
     float S;                  // (colour behind + T_final * background) . dL/dpixel
     float vr, vg, vb;         // dL/dpixel
-    float py;                 // row (the column is shared by the thread's two pixels)
+    float py;                 // row (the column is shared by the thread's pixels)
     int bin_final;            // last splat index this pixel may take gradient from (-1: none)
 };
 
-// One pixel's part of splat (xo, cn) of batch slot t: its transmittance and
-// S updates and its gradient contributions added to v, v8 (valid: the
-// pixel takes the splat; alpha < 0.999 checked here).
-// kAdd: add to v (a second pixel), else assign (the first)
+// One pixel's part of a splat it takes: its transmittance and S updates and
+// its gradient contributions in v, v8 (an alpha clamped to 0.999 is skipped
+// here).  kAdd: add to v (the thread's second pixel), else assign (its first).
 template <bool kAdd>
 __device__ __forceinline__ void pixel_step(PixelState &ps, float dx, float dy, float alpha, const float4 &rc,
                                            float v[8], float &v8) {
