@@ -55,13 +55,16 @@ def engine_outputs(eng, n, W, H, with_grads=True):
 
 
 def run_pair(init: S.GaussianSet, cam, gt, step: dict, *, raster_mode=0, k_max=0, do_sgld=False, mask=None,
-             background=(0.0, 0.0, 0.0), precs=(32, 64), do_backward=True):
+             background=(0.0, 0.0, 0.0), precs=(32, 64), do_backward=True, tuning=None):
     """One step on the engine and on the oracle (each precision in `precs`).
+    tuning: engine launch configuration fields (MsplatTuning) set first.
     Returns (engine outputs + updated params, {prec: oracle outputs + params})."""
     import torch
     cd = E.camera_dict(cam)
     W, H = cam.width, cam.height
     eng = E.Engine(0)
+    if tuning:
+        eng.set_tuning(**tuning)
     dg = E.DeviceGaussians(init)
     args = E.make_args(cd, step, background=background, raster_mode=raster_mode, k_max=k_max, do_sgld=do_sgld)
     if do_backward:

@@ -105,8 +105,11 @@ def test_sgld_parity(small):
     assert e <= GRAD_TOL
 
 
-def test_edge_cases(small):
-    """Partial edge tiles, splats behind the camera, a NaN colour, a mask."""
+@pytest.mark.parametrize("tuning", [None, dict(bwd_pixels=2, tile_order=1)])
+def test_edge_cases(small, tuning):
+    """Partial edge tiles, splats behind the camera, a NaN colour, a mask;
+    also with the two-pixels-per-thread raster backward (second pixels below
+    the image in the bottom tiles) and the depth-presorted tile ordering."""
     sc, cam0, gt0, init = small
     cam = S.Camera(cam0.cam_to_world, 203, 150, 160.0, 160.0, 101.5, 75.0)
     gt = gt_image(sc.gt, cam)
@@ -117,7 +120,7 @@ def test_edge_cases(small):
     mask[40:70, 50:120] = 0
     mask[140:, 190:] = 0                      # across the bottom-right corner
     step = E.step_scalars(700, 700, width=cam.width, height=cam.height)
-    eo, res = run_pair(g, cam, gt, step, mask=mask, precs=(32,))
+    eo, res = run_pair(g, cam, gt, step, mask=mask, precs=(32,), tuning=tuning)
     r32 = res[32]
     _check_forward(eo, r32, g.n)
     assert eo["radii"][5] == 0
@@ -136,13 +139,14 @@ def test_edge_cases(small):
         assert rel_l2(upd_e, upd_o) <= GRAD_TOL, k
 
 
-@pytest.mark.parametrize("raster_mode", [0, 1])
-def test_needles_and_faint_splats(small, raster_mode):
+@pytest.mark.parametrize("raster_mode,tuning", [(0, None), (1, None), (0, dict(bwd_pixels=2))])
+def test_needles_and_faint_splats(small, raster_mode, tuning):
     """Warp culling by each splat's reach box at its edges: needle-thin
     Gaussians (scales e^-1.5 by e^-8, random rotations: conics close to
     singular), huge ones, and opacities on both sides of the 1/255 cut.
     Tile lists, last contributors and the image equal the oracle's (which
-    tests every pixel), gradients within the usual bar."""
+    tests every pixel), gradients within the usual bar; the backward also in
+    its two-pixels-per-thread layout (8x8 warp blocks)."""
     sc, cam, gt, init = small
     rng = np.random.default_rng(7)
     g = init.copy()
@@ -158,7 +162,7 @@ def test_needles_and_faint_splats(small, raster_mode):
                                  rng.uniform(-7.0, 6.0, n)).astype(np.float32)
     step = E.step_scalars(1, 1, width=cam.width, height=cam.height)
     step["degrees_to_use"] = 3
-    eo, res = run_pair(g, cam, gt, step, raster_mode=raster_mode, precs=(32,))
+    eo, res = run_pair(g, cam, gt, step, raster_mode=raster_mode, precs=(32,), tuning=tuning)
     r32 = res[32]
     _check_forward(eo, r32, g.n)
     for key in ("v_xy", "v_conic", "v_colors", "v_opacity", "v_mean3d", "v_scale"):
