@@ -215,6 +215,7 @@ class Engine {
         k_set_params<<<1, 256, 0, stream_>>>(ptr<StepParams>("params"), pack,
                                              (int)(sizeof(StepParams) * B / 4));
         CK(cudaGetLastError());
+        launches_ += 1;
         // every buffer the step touches exists now (sized above), so a capture
         // below allocates nothing
         const size_t cb = tile_cta_bins_bytes(vt);
