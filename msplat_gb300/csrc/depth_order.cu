@@ -9,15 +9,16 @@
 //   2. Their tile rectangles (computed by the projection) are written in that
 //      order by the last sort pass (8 bytes each).
 //   3. The block-aggregated count and scatter of the other path run over the
-//      sorted positions p: CTA c covers p in [2048 c, 2048 c + 2048), so each
+//      sorted positions p: CTA c covers p in [1024 c, 1024 c + 1024), so each
 //      tile's bucket is a sequence of per-CTA runs in increasing depth, and
 //      the key stored is p itself.
 //   4. Inside a run the scatter's shared-memory slot order is arbitrary: each
 //      key's place is the run's start plus the number of smaller keys in the
 //      run (positions are unique), and the id written there is the Gaussian at
-//      position p.  Runs are short (a CTA's 2048 Gaussians are a thin depth
+//      position p.  Runs are short (a CTA's 1024 Gaussians are a thin depth
 //      slab spread over the image); the count is quadratic in a run's length,
-//      which stays within 2048.
+//      which stays within 1024 (1024 Gaussians per CTA rather than 2048 or
+//      512: shorter runs against a larger count table).
 // The lists are the same as the per-tile radix sort's (same keys, same
 // order); the scan and the class lists of tiles.cu are shared.
 #include <algorithm>
@@ -30,7 +31,7 @@ namespace msplat {
 constexpr int kGsThreads = 256;
 constexpr int kGsItems = 8;
 constexpr int kGsPerCta = kGsThreads * kGsItems;   // 2048 keys per radix-sort CTA
-static_assert(kAggPerCta == 2048, "run index p >> 11 needs 2048 Gaussians per count CTA");
+static_assert(kAggPerCta == 1 << kAggShift, "a run is the positions p with equal p >> kAggShift");
 
 __device__ __forceinline__ uint32_t gs_key0(const TileArgs &a, size_t u) {
     if (a.radii[u] <= 0) return 0xffffffffu;
@@ -262,7 +263,7 @@ __global__ void __launch_bounds__(kOrderThreads) k_tile_order(TileArgs a, int ct
     for (int j = threadIdx.x; j < count; j += blockDim.x) {
         const uint32_t p = keys[j];
         const uint32_t gid = a.gs_val[0][vb + p];
-        const int c = (int)(p >> 11);
+        const int c = (int)(p >> kAggShift);
         uint32_t rs, re;
         if (stage_runs) {
             rs = runs[c];

@@ -34,7 +34,8 @@ inline ViewTable single_view_table(int n, int w, int h) { return make_view_table
 
 // Block-aggregated tile mapping: a CTA of kAggThreads covers kAggPerCta
 // Gaussians of one view; used while every view has at most kAggMaxTiles tiles.
-constexpr int kAggPerCta = 2048;
+constexpr int kAggShift = 10;
+constexpr int kAggPerCta = 1 << kAggShift;   // Gaussians per count / scatter CTA
 constexpr int kAggThreads = 512;      // four CTAs per SM: 1M Gaussians fill one wave
 constexpr int kAggMaxTiles = 20480;   // 80 KB of histogram: two 512-thread CTAs per SM at the largest
 
@@ -77,7 +78,7 @@ struct TileArgs {
     const float2 *aabb;
     uint32_t *tile_counts;  // zeroed before the step
     uint32_t *tile_write;   // zeroed before the step
-    uint32_t *cta_bins;     // per view: [ceil(n / 2048), T_v] per-CTA tile histograms (block-aggregated path)
+    uint32_t *cta_bins;     // per view: [ceil(n / kAggPerCta), T_v] per-CTA tile histograms (block-aggregated path)
     uint32_t *tile_lists;   // [4, T] tiles of each sort class (written by the scan)
     uint32_t *tile_class;   // [8]: list lengths, then the sort kernels' work counters
     uint32_t *tile_offsets; // [T+1]

@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(1024) k_cta_scan(TileArgs a, int ctas) {
     const bool in = t < a.num_tiles;
     // up to kHeld rows per warp (2^20 Gaussians per view): all loads issued
     // at once and kept in registers for the rewrite; more rows loop
-    constexpr int kHeld = 16;
+    constexpr int kHeld = 32;
     const bool held_rows = per <= kHeld;   // CTA-uniform
     uint32_t held[kHeld];
     uint32_t sum = 0;
