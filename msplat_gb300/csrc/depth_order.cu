@@ -29,8 +29,8 @@
 namespace msplat {
 
 constexpr int kGsThreads = 256;
-constexpr int kGsItems = 8;
-constexpr int kGsPerCta = kGsThreads * kGsItems;   // 2048 keys per radix-sort CTA
+constexpr int kGsItems = kGsPerCta / kGsThreads;   // keys per thread of a radix-sort CTA
+static_assert(kGsItems * kGsThreads == kGsPerCta, "whole rounds of 32 keys per warp");
 static_assert(kAggPerCta == 1 << kAggShift, "a run is the positions p with equal p >> kAggShift");
 
 __device__ __forceinline__ uint32_t gs_key0(const TileArgs &a, size_t u) {
@@ -39,7 +39,7 @@ __device__ __forceinline__ uint32_t gs_key0(const TileArgs &a, size_t u) {
     return (finite_bits(d) && d > 0.0f) ? __float_as_uint(d) : 0xffffffffu;
 }
 
-// Digit counts of one 2048-key block: hist[view][digit][block].
+// Digit counts of one kGsPerCta-key block: hist[view][digit][block].
 template <bool kFirst>
 __global__ void __launch_bounds__(kGsThreads) k_gs_hist(TileArgs a, int shift, const uint32_t *key_in) {
     pdl_enter();
@@ -91,8 +91,9 @@ __global__ void __launch_bounds__(256) k_gs_digit_scan(TileArgs a, int nb) {
     if (lane == 0) a.gs_dtot[(size_t)view * 256 + d] = carry;
 }
 
-// Stable scatter of one 2048-key block: warp w holds keys [256 w, 256 w + 256)
-// of the block in eight rounds of 32; a key's place is its digit's offset for
+// Stable scatter of one kGsPerCta-key block: warp w holds keys
+// [32 kGsItems w, 32 kGsItems (w + 1)) of the block in kGsItems rounds of 32;
+// a key's place is its digit's offset for
 // the block + the same digit's keys in earlier warps + in earlier rounds of
 // its warp + in lower lanes of its round (peers found with eight ballots).
 // The last pass also writes each sorted position's tile rectangle (srect,

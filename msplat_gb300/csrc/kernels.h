@@ -34,6 +34,7 @@ inline ViewTable single_view_table(int n, int w, int h) { return make_view_table
 
 // Block-aggregated tile mapping: a CTA of kAggThreads covers kAggPerCta
 // Gaussians of one view; used while every view has at most kAggMaxTiles tiles.
+constexpr int kGsPerCta = 1024;   // keys per block of the depth-presorted ordering's radix sort
 constexpr int kAggShift = 10;
 constexpr int kAggPerCta = 1 << kAggShift;   // Gaussians per count / scatter CTA
 constexpr int kAggThreads = 512;      // four CTAs per SM: 1M Gaussians fill one wave
@@ -91,7 +92,7 @@ struct TileArgs {
     // that order, then each tile's per-CTA runs put in order
     int presorted;
     uint32_t *gs_key[2], *gs_val[2];   // [views, n] sort buffers; ids in depth order end in gs_val[0]
-    uint32_t *gs_hist;                 // [views, 256, ceil(n / 2048)] digit counts, then offsets in the digit
+    uint32_t *gs_hist;                 // [views, 256, ceil(n / kGsPerCta)] digit counts, then offsets in the digit
     uint32_t *gs_dtot;                 // [views, 256] keys per digit
     const ushort4 *rect;               // [views, n] tile rectangles from the projection
     ushort4 *srect;                    // [views, n] tile rectangles in depth order
