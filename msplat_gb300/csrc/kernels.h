@@ -37,7 +37,7 @@ inline ViewTable single_view_table(int n, int w, int h) { return make_view_table
 constexpr int kGsPerCta = 1024;   // keys per block of the depth-presorted ordering's radix sort
 constexpr int kAggShift = 10;
 constexpr int kAggPerCta = 1 << kAggShift;   // Gaussians per count / scatter CTA
-constexpr int kAggThreads = 512;      // four CTAs per SM: 1M Gaussians fill one wave
+constexpr int kAggThreads = 512;      // count / scatter CTA width (256 measured slower)
 constexpr int kAggMaxTiles = 20480;   // 80 KB of histogram: two 512-thread CTAs per SM at the largest
 
 inline int max_view_tiles(const ViewTable &vt) {
