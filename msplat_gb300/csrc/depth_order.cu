@@ -224,16 +224,16 @@ __global__ void __launch_bounds__(kAggThreads) k_scatter_agg_sorted(TileArgs a) 
 
 // Each tile's runs in order: the key at slot j (a sorted position p) goes to
 // its run's start + the number of smaller keys in the run; the record id of
-// the Gaussian at p is written there.  The runs' starts (one column of
-// cta_bins) and, when they fit, the tile's keys are staged in shared memory
-// first; the id gather is issued before the count.  A tile whose bucket does
-// not fit the buffer is emitted transparent.
+// the Gaussian at p is written there.  The run's bounds are two entries of
+// the tile's column of cta_bins; keys and bounds are read through L1 (staging
+// them in shared memory measured slower at 1M Gaussians, 1297x840: 1.354 ms
+// per step with up to 4096 staged keys, 1.369 with 8192, 1.343 without); the
+// id gather is issued before the count.  A tile whose bucket does not fit the
+// buffer is emitted transparent.
 constexpr int kOrderThreads = 256;
-constexpr int kOrderSmemWords = 12288;   // 48 KB: run starts + staged keys
 
-__global__ void __launch_bounds__(kOrderThreads) k_tile_order(TileArgs a, int ctas, int stage_runs, int key_cap) {
+__global__ void __launch_bounds__(kOrderThreads) k_tile_order(TileArgs a, int ctas) {
     pdl_enter();
-    extern __shared__ uint32_t osm[];
     const int t = a.tile_lo + blockIdx.x;
     if (t >= a.tile_hi) return;
     const int count = (int)a.tile_counts[t];
@@ -248,31 +248,14 @@ __global__ void __launch_bounds__(kOrderThreads) k_tile_order(TileArgs a, int ct
     const ViewGeom vg = view_geom(a.vt, view);
     const int Tv = vg.tiles_x * vg.tiles_y;
     const uint32_t *col = a.cta_bins + (size_t)ctas * vg.tile_base + (t - vg.tile_base);   // run starts: col[c * Tv]
-    const uint32_t *gkeys = reinterpret_cast<const uint32_t *>(a.keys) + start;
-    uint32_t *runs = osm;                                 // [ctas + 1] when stage_runs
-    uint32_t *staged = osm + (stage_runs ? ctas + 1 : 0);
-    const bool in_smem = count <= key_cap;                // CTA-uniform
-    if (stage_runs) {
-        for (int c = threadIdx.x; c < ctas; c += blockDim.x) runs[c] = col[(size_t)c * Tv];
-        if (threadIdx.x == 0) runs[ctas] = (uint32_t)count;
-    }
-    if (in_smem)
-        for (int j = threadIdx.x; j < count; j += blockDim.x) staged[j] = gkeys[j];
-    __syncthreads();
-    const uint32_t *keys = in_smem ? staged : gkeys;
+    const uint32_t *keys = reinterpret_cast<const uint32_t *>(a.keys) + start;
     const size_t vb = (size_t)view * a.vt.n;
     for (int j = threadIdx.x; j < count; j += blockDim.x) {
         const uint32_t p = keys[j];
         const uint32_t gid = a.gs_val[0][vb + p];
         const int c = (int)(p >> kAggShift);
-        uint32_t rs, re;
-        if (stage_runs) {
-            rs = runs[c];
-            re = runs[c + 1];
-        } else {
-            rs = col[(size_t)c * Tv];
-            re = c + 1 < ctas ? col[(size_t)(c + 1) * Tv] : (uint32_t)count;
-        }
+        const uint32_t rs = col[(size_t)c * Tv];
+        const uint32_t re = c + 1 < ctas ? col[(size_t)(c + 1) * Tv] : (uint32_t)count;
         uint32_t below = 0;
         for (uint32_t q = rs; q < re; q++) below += keys[q] < p ? 1u : 0u;
         const uint32_t dst = rs + below;
@@ -325,14 +308,7 @@ int launch_presorted_build(const TileArgs &a, cudaStream_t s) {
     if (grp) launch_pdl(k_scatter_agg_sorted<true>, dim3(agg_blocks, views), kAggThreads, smem, s, a);
     else launch_pdl(k_scatter_agg_sorted<false>, dim3(agg_blocks, views), kAggThreads, smem, s, a);
     debug_sync(s, "scatter_sorted");
-    // shared memory: the run starts when they take at most two thirds of it,
-    // then up to 4096 keys (a small footprint keeps eight CTAs per SM; larger
-    // tiles count from global memory)
-    const int stage_runs = agg_blocks + 1 <= (2 * kOrderSmemWords) / 3 ? 1 : 0;
-    const int key_cap = std::min(4096, kOrderSmemWords - (stage_runs ? agg_blocks + 1 : 0));
-    const size_t osmem = sizeof(uint32_t) * ((stage_runs ? agg_blocks + 1 : 0) + key_cap);
-    if (a.tile_hi > a.tile_lo)
-        launch_pdl(k_tile_order, a.tile_hi - a.tile_lo, kOrderThreads, osmem, s, a, agg_blocks, stage_runs, key_cap);
+    if (a.tile_hi > a.tile_lo) launch_pdl(k_tile_order, a.tile_hi - a.tile_lo, kOrderThreads, 0, s, a, agg_blocks);
     debug_sync(s, "tile_order");
     return 2;
 }

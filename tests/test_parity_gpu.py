@@ -169,6 +169,28 @@ def test_needles_and_faint_splats(small, raster_mode, tuning):
         assert rel_l2(eo[key], r32[key]) <= GRAD_TOL, key
 
 
+@pytest.mark.parametrize("tuning", [dict(tile_order=0), dict(tile_order=1)])
+def test_large_tile_buckets(small, tuning):
+    """Every Gaussian of the scene large and a 96x64 view: each of the 24
+    tiles holds most of the 16,384 Gaussians, more keys than either tile
+    ordering stages in shared memory, and the depth-presorted ordering's
+    per-CTA runs reach 1024 keys."""
+    sc, cam0, gt0, init = small
+    cam = S.Camera(cam0.cam_to_world, 96, 64, 60.0, 60.0, 48.0, 32.0)
+    gt = gt_image(sc.gt, cam)
+    g = init.copy()
+    g.scales[:] = np.float32(0.3)
+    g.opacities[:] = np.float32(-4.0)   # faint: the lists stay long behind the front
+    step = E.step_scalars(1, 1, width=cam.width, height=cam.height)
+    eo, res = run_pair(g, cam, gt, step, precs=(32,), tuning=tuning)
+    r32 = res[32]
+    assert int(r32["tile_counts"].max()) > 8192
+    _check_forward(eo, r32, g.n)
+    assert rel_l2(eo["v_rendered"], r32["v_rendered"]) <= 1e-5
+    for key in ("v_xy", "v_conic", "v_colors", "v_opacity", "v_mean3d"):
+        assert rel_l2(eo[key], r32[key]) <= GRAD_TOL, key
+
+
 def test_empty_scene(small):
     sc, cam, gt, init = small
     g = S.GaussianSet(*(a[:0].copy() for a in init.arrays()))
