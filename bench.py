@@ -140,18 +140,29 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def cpu_baseline(model, cam_dict, gt, steps=4):
-    """FP64 oracle (OpenMP, all host cores) timed on full iterations of the workload."""
-    from msplat_gb300 import engine as E
+def oracle_camera(cam):
+    """Camera dict of a synthetic camera, matrices from the oracle's
+    prepare_cam (Model::prepareCam, core/src/model.cpp:845-889): the CPU arms
+    never load the engine library."""
     from oracle import oracle as O
+    vm, pm, cp = O.prepare_cam(cam.cam_to_world, cam.width, cam.height, cam.fx, cam.fy)
+    return dict(viewmat=vm, projmat=pm, cam_pos=cp, fx=cam.fx, fy=cam.fy, cx=cam.cx, cy=cam.cy,
+                width=cam.width, height=cam.height)
+
+
+def cpu_baseline(model, cam, gt, steps=4):
+    """FP64 oracle (OpenMP, all host cores) timed on full iterations of the workload."""
+    import numpy as np
+    from msplat_gb300.schedule import step_scalars
+    from oracle import oracle as O
+    cd = oracle_camera(cam)
     g = model.copy()
-    mom = ([__import__("numpy").zeros_like(a) for a in g.arrays()],
-           [__import__("numpy").zeros_like(a) for a in g.arrays()])
+    mom = ([np.zeros_like(a) for a in g.arrays()], [np.zeros_like(a) for a in g.arrays()])
     times = []
     for k in range(steps):
-        st = E.step_scalars(3001 + k, 3001 + k, width=cam_dict["width"], height=cam_dict["height"])
+        st = step_scalars(3001 + k, 3001 + k, width=cam.width, height=cam.height)
         t0 = time.perf_counter()
-        O.train_step(64, g, cam_dict, st, moments=mom, gt=gt, do_sgld=True, want_ids=False)
+        O.train_step(64, g, cd, st, moments=mom, gt=gt, do_sgld=True, want_ids=False)
         times.append(time.perf_counter() - t0)
     sec = statistics.median(times[1:] if len(times) > 2 else times)
     return {"value": 1.0 / sec, "unit": "iters/s", "cores": O.num_threads(), "kind": "port",
@@ -160,16 +171,19 @@ def cpu_baseline(model, cam_dict, gt, steps=4):
 
 
 def run_reference(args):
-    """--impl reference: the CPU restatement of the reference step (oracle)."""
+    """--impl reference: the CPU restatement of the reference step (oracle).
+
+    Camera matrices, step scalars, scene and targets all come from the oracle
+    and pure-Python helpers: the engine library is never loaded by this arm."""
     import numpy as np
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
-    from msplat_gb300 import engine as E
+    from msplat_gb300.schedule import step_scalars
     from oracle import oracle as O
     sc, model = build_workload()
     cam = sc.train_cams[0]
-    cd = E.camera_dict(cam)
+    cd = oracle_camera(cam)
     ref = O.train_step(64, sc.gt.copy(), cd, {"degrees_to_use": 3}, do_backward=False, do_optimizer=False,
                        want_ids=False)
     gt = (np.clip(ref["out_img"], 0, 1) * 255 + 0.5).astype(np.uint8)
@@ -177,7 +191,7 @@ def run_reference(args):
     mom = ([np.zeros_like(a) for a in g.arrays()], [np.zeros_like(a) for a in g.arrays()])
 
     def step(k):
-        st = E.step_scalars(3001 + k, 3001 + k, width=cam.width, height=cam.height)
+        st = step_scalars(3001 + k, 3001 + k, width=cam.width, height=cam.height)
         O.train_step(64, g, cd, st, moments=mom, gt=gt, do_sgld=True, want_ids=False)
 
     for k in range(args.warmup):
@@ -195,8 +209,23 @@ def run_reference(args):
                             "sample": "full FP64 iterations of the workload (the reference is Metal-only: "
                                       "unavailable on this box; its CPU restatement is timed)"},
            "e2e": {"value": v, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    loaded = loaded_libraries()
+    if loaded is not None:
+        out["libraries_loaded"] = loaded
+        if any("libmsplat_gb300" in x for x in loaded):
+            raise RuntimeError("the reference arm loaded the engine library")
     print(json.dumps(out), flush=True)
     return 0
+
+
+def loaded_libraries():
+    """This project's shared libraries mapped into the process (Linux), or None."""
+    try:
+        with open("/proc/self/maps") as f:
+            paths = {line.split()[-1] for line in f if line.rstrip().endswith(".so")}
+    except OSError:
+        return None
+    return sorted(os.path.relpath(p, ROOT) for p in paths if p.startswith(ROOT))
 
 
 BATCH_SIZES = [(1297, 840), (979, 546), (648, 420), (2594, 1680)] * 2
@@ -457,8 +486,7 @@ def run_engine(args):
         except Exception as ex:   # reported, never fatal to the throughput line
             out["time_to_psnr"] = {"error": str(ex)[:200]}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        cd = cams[0]
-        out["cpu_baseline"] = cpu_baseline(model, cd, gts_host[0].numpy(), steps=args.cpu_steps)
+        out["cpu_baseline"] = cpu_baseline(model, sc.train_cams[0], gts_host[0].numpy(), steps=args.cpu_steps)
     if rank == 0:
         print(json.dumps(out), flush=True)
     eng.close()

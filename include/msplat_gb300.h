@@ -134,6 +134,14 @@ int msplat_dataset_points(MsplatDataset ds, float *xyz, uint8_t *rgb);
  * negative code with the reason on stderr. */
 int msplat_image_read(const char *path, float *rgb, int *width, int *height);
 
+/* Reads and validates a checkpoint file (the reference's format,
+ * core/src/model.cpp:698-843) on the host, without a trainer: every tensor
+ * must hold N rows of its group's width and exactly N x width x 4 bytes.
+ * Writes N, the SH degree and the iteration (any output may be NULL).
+ * Returns 0, or -1 when the file is missing or malformed (reason on
+ * stderr).  msplat_trainer_load_checkpoint applies the same checks. */
+int msplat_checkpoint_info(const char *path, int *num_points, int *sh_degree, int *iteration);
+
 /* SSIM + L1 training loss and dL/dimage without any device allocation.
  * No counterpart in the reference: it is for callers that cannot call
  * cudaMalloc (a host application or server that owns all device memory

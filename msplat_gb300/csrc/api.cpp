@@ -232,6 +232,80 @@ struct DeviceModel {
     }
 };
 
+// Checkpoint file (model.cpp:698-843): magic "MSPL", version 1, step, N,
+// SH degree, Adam step; 6 learning rates, means lr init/final; 6 parameter
+// tensors, then 6 first and 6 second moments, each as (ndim, int64 shape,
+// uint64 bytes, float32 data).  Every tensor is checked against the header
+// before any of it is used: N rows, the group's row width (features_rest
+// [N, rest, 3] with rest = (degree+1)^2 - 1 fixes the width of groups 4, 10
+// and 16), and exactly N x width x 4 bytes; anything else is a malformed
+// checkpoint (the reader never reads past what it allocated).
+struct CheckpointData {
+    uint32_t step = 0, n = 0, deg = 0, adam_steps = 0;
+    float adam_lr[6] = {0, 0, 0, 0, 0, 0};
+    float means_lr_init = 0, means_lr_final = 0;
+    int rest = 0;
+    std::vector<float> t[18];
+};
+
+static CheckpointData read_checkpoint(const std::string &path) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) throw std::runtime_error("cannot open checkpoint " + path);
+    auto u32 = [&]() {
+        uint32_t v = 0;
+        f.read(reinterpret_cast<char *>(&v), 4);
+        if (!f) throw std::runtime_error("malformed checkpoint: truncated header");
+        return v;
+    };
+    if (u32() != 0x4C50534Du) throw std::runtime_error("not a msplat checkpoint");
+    const uint32_t ver = u32();
+    if (ver != 1) throw std::runtime_error("unsupported checkpoint version " + std::to_string(ver));
+    CheckpointData ck;
+    ck.step = u32();
+    ck.n = u32();
+    ck.deg = u32();
+    ck.adam_steps = u32();
+    f.read(reinterpret_cast<char *>(ck.adam_lr), sizeof(ck.adam_lr));
+    f.read(reinterpret_cast<char *>(&ck.means_lr_init), 4);
+    f.read(reinterpret_cast<char *>(&ck.means_lr_final), 4);
+    if (!f) throw std::runtime_error("malformed checkpoint: truncated header");
+    if (ck.n > 0x7fffffffu) throw std::runtime_error("malformed checkpoint: N out of range");
+    if (ck.deg > 3) throw std::runtime_error("malformed checkpoint: SH degree " + std::to_string(ck.deg) + " > 3");
+    ck.rest = (int)((ck.deg + 1) * (ck.deg + 1)) - 1;
+    const int width[6] = {3, 3, 4, 3, 3 * ck.rest, 1};
+    const char *names[6] = {"means", "scales", "quats", "features_dc", "features_rest", "opacities"};
+    for (int k = 0; k < 18; k++) {
+        const int g = k % 6;
+        const std::string what = std::string("malformed checkpoint: ") + (k < 6 ? "" : k < 12 ? "exp_avg " : "exp_avg_sq ") +
+                                 names[g];
+        const uint32_t nd = u32();
+        if (nd < 1 || nd > 4) throw std::runtime_error(what + ": " + std::to_string(nd) + " dimensions");
+        int64_t shape[4] = {0, 0, 0, 0};
+        for (uint32_t d = 0; d < nd; d++) {
+            f.read(reinterpret_cast<char *>(&shape[d]), 8);
+            if (!f) throw std::runtime_error(what + ": truncated shape");
+            if (shape[d] < 0) throw std::runtime_error(what + ": negative extent");
+        }
+        int64_t row = 1;
+        for (uint32_t d = 1; d < nd; d++) row *= shape[d];
+        if (shape[0] != (int64_t)ck.n) throw std::runtime_error(what + ": " + std::to_string(shape[0]) +
+                                                                " rows, header says " + std::to_string(ck.n));
+        if (row != width[g] || (g == 4 && nd >= 3 && shape[1] != ck.rest))
+            throw std::runtime_error(what + ": row width " + std::to_string(row) + ", expected " +
+                                     std::to_string(width[g]));
+        uint64_t bytes = 0;
+        f.read(reinterpret_cast<char *>(&bytes), 8);
+        if (!f) throw std::runtime_error(what + ": truncated size");
+        const uint64_t want = (uint64_t)ck.n * (uint64_t)width[g] * 4u;
+        if (bytes != want) throw std::runtime_error(what + ": " + std::to_string(bytes) + " bytes, expected " +
+                                                    std::to_string(want));
+        ck.t[k].resize((size_t)want / 4);
+        f.read(reinterpret_cast<char *>(ck.t[k].data()), (std::streamsize)want);
+        if (!f) throw std::runtime_error(what + ": truncated data");
+    }
+    return ck;
+}
+
 // Reference-layout host copy of a model (means [N,3] ... opacities [N]).
 struct HostGaussians {
     int n = 0, rest = 15;
@@ -771,8 +845,14 @@ struct TrainerImpl {
         u32(0x4C50534Du);
         u32(1);
         u32((uint32_t)current_step);
+        // the degree recorded is the one the stored rest bases belong to
+        int deg = 0;
+        while (deg < 3 && (deg + 1) * (deg + 1) - 1 < model.rest) deg++;
+        if ((deg + 1) * (deg + 1) - 1 != model.rest)
+            throw std::runtime_error("cannot save a checkpoint of " + std::to_string(model.rest) +
+                                     " rest SH bases (not those of degree 0-3)");
         u32((uint32_t)model.n);
-        u32((uint32_t)cfg.shDegree);
+        u32((uint32_t)deg);
         u32((uint32_t)adam_step_count);
         f.write(reinterpret_cast<const char *>(adam_lr), sizeof(adam_lr));
         f.write(reinterpret_cast<const char *>(&means_lr_init), 4);
@@ -805,35 +885,14 @@ struct TrainerImpl {
     }
 
     int load_checkpoint(const std::string &path) {
-        std::ifstream f(path, std::ios::binary);
-        if (!f) throw std::runtime_error("cannot open checkpoint " + path);
-        auto u32 = [&]() { uint32_t v = 0; f.read(reinterpret_cast<char *>(&v), 4); return v; };
-        if (u32() != 0x4C50534Du) throw std::runtime_error("not a msplat checkpoint");
-        const uint32_t ver = u32();
-        if (ver != 1) throw std::runtime_error("unsupported checkpoint version " + std::to_string(ver));
-        const uint32_t step = u32(), n = u32(), deg = u32(), adam_steps = u32();
-        (void)deg;
-        f.read(reinterpret_cast<char *>(adam_lr), sizeof(adam_lr));
-        f.read(reinterpret_cast<char *>(&means_lr_init), 4);
-        f.read(reinterpret_cast<char *>(&means_lr_final), 4);
-        auto tensor = [&](std::vector<int64_t> &shape) {
-            const uint32_t nd = u32();
-            shape.assign(nd, 0);
-            for (auto &s : shape) f.read(reinterpret_cast<char *>(&s), 8);
-            uint64_t bytes = 0;
-            f.read(reinterpret_cast<char *>(&bytes), 8);
-            std::vector<float> data(bytes / 4);
-            f.read(reinterpret_cast<char *>(data.data()), bytes);
-            if (!f) throw std::runtime_error("truncated checkpoint");
-            return data;
-        };
-        std::vector<int64_t> shape;
-        std::vector<float> t[18];
-        int rest = 0;
-        for (int k = 0; k < 18; k++) {
-            t[k] = tensor(shape);
-            if (k == 4) rest = shape.size() >= 3 ? (int)shape[1] : 0;
-        }
+        CheckpointData ck = read_checkpoint(path);
+        const uint32_t n = ck.n;
+        std::memcpy(adam_lr, ck.adam_lr, sizeof(adam_lr));
+        means_lr_init = ck.means_lr_init;
+        means_lr_final = ck.means_lr_final;
+        const uint32_t step = ck.step, adam_steps = ck.adam_steps;
+        const int rest = ck.rest;
+        std::vector<float> *t = ck.t;
         const int cap = std::max((int)n, std::max(1, cfg.capMax));
         model.allocate(cap, rest);
         model.n = (int)n;
@@ -1086,6 +1145,16 @@ int msplat_image_read(const char *path, float *rgb, int *width, int *height) {
         if (rgb) std::memcpy(rgb, im.rgb.data(), im.rgb.size() * sizeof(float));
         return 0;
     }, -2);
+}
+int msplat_checkpoint_info(const char *path, int *num_points, int *sh_degree, int *iteration) {
+    if (!path) return -1;
+    return guard("checkpoint", [&]() {
+        const CheckpointData ck = read_checkpoint(path);
+        if (num_points) *num_points = (int)ck.n;
+        if (sh_degree) *sh_degree = (int)ck.deg;
+        if (iteration) *iteration = (int)ck.step;
+        return 0;
+    }, -1);
 }
 int msplat_dataset_num_train(MsplatDataset ds) { return ds ? (int)DS(ds)->train.size() : 0; }
 int msplat_dataset_num_test(MsplatDataset ds) { return ds ? (int)DS(ds)->test.size() : 0; }

@@ -341,7 +341,9 @@ class Engine {
         la.gt = nullptr; la.mask = nullptr;   // read from StepParams (see common.cuh)
         la.v_img = ptr<float>("v_img");
         la.loss_sum = ptr<float>("loss_sum"); la.nan_counts = pa.nan_counts;
-        launches_ += launch_loss(la, stream_);
+        const int nl = launch_loss(la, stream_);
+        if (nl < 0) throw std::runtime_error("loss kernel set-up failed");
+        launches_ += nl;
         debug_sync(stream_, "loss");
         mark(4);
         if (!backward) { mark(5); mark(6); mark(7); mark(8); return; }

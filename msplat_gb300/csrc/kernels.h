@@ -202,7 +202,9 @@ size_t sort_pack_smem_bytes();
 // cta_bins bytes for these views, 0 when the block-aggregated path is not used
 size_t tile_cta_bins_bytes(const ViewTable &vt);
 void launch_raster_fwd(const RasterArgs &a, cudaStream_t s);
-int launch_loss(const LossArgs &a, cudaStream_t s);   // returns the kernels launched
+// returns the kernels launched (0 or 1), or -1 when the per-device set-up
+// (window upload, shared-memory limit) failed; nothing is launched then
+int launch_loss(const LossArgs &a, cudaStream_t s);
 void launch_raster_bwd(const RasterArgs &a, cudaStream_t s);
 void launch_project_bwd(const ProjectBwdArgs &a, cudaStream_t s);
 void launch_adam(const AdamArgs &a, int num_sms, cudaStream_t s);

@@ -10,16 +10,17 @@
 // this file's static device copy of StepParams, which every GPU that loads
 // the library holds until the process exits.  Any image size.
 //
-// Sharing: every call on a device uses the same scalars, rewritten by each
-// call before its kernel runs, and each call zeroes the caller's loss
-// output, so no state carries over between calls — but calls that overlap on
-// the GPU (different streams, no ordering) race on the scalars.
+// Sharing: every call on a device uses the same scalars, rewritten in stream
+// order by a one-thread kernel (the values travel as kernel arguments, so no
+// host buffer is read after the call returns) before the loss kernel runs,
+// and each call zeroes the caller's loss output, so no state carries over
+// between calls — but calls that overlap on the GPU (different streams, no
+// ordering) race on the scalars.
 //
 // Set-up: the first call on each device looks up the scalars' device address
 // (cudaGetSymbolAddress) with that device current; make that first call
 // before any stream capture.
 #include <cstdio>
-#include <cstring>
 #include <mutex>
 
 #include "common.cuh"
@@ -57,6 +58,15 @@ static int noalloc_setup(int dev, NoAllocDevice &out) {
     return 0;
 }
 
+// Writes the call's scalars into the shared device copy (one thread).
+__global__ void k_noalloc_scalars(StepParams *p, float ssim_weight, float loss_inv_n, int has_mask,
+                                  float *loss_sum) {
+    p->ssim_weight = ssim_weight;
+    p->loss_inv_n = loss_inv_n;
+    p->has_mask = has_mask;
+    *loss_sum = 0.f;
+}
+
 }  // namespace msplat
 
 extern "C" int msplat_loss_ssim_l1_noalloc(const float *img, const uint8_t *gt, const uint8_t *mask, int width,
@@ -76,14 +86,8 @@ extern "C" int msplat_loss_ssim_l1_noalloc(const float *img, const uint8_t *gt, 
     if (int rc = noalloc_setup(dev, d)) return rc;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
 
-    StepParams sp;
-    std::memset(&sp, 0, sizeof(sp));
-    sp.ssim_weight = ssim_weight;
-    sp.loss_inv_n = loss_inv_n;
-    sp.has_mask = mask ? 1 : 0;
-    // pageable source: consumed by the time the call returns
-    e = cudaMemcpyAsync(d.params, &sp, sizeof(sp), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(loss_sum, 0, sizeof(float), s);
+    k_noalloc_scalars<<<1, 1, 0, s>>>(d.params, ssim_weight, loss_inv_n, mask ? 1 : 0, loss_sum);
+    e = cudaGetLastError();
     if (e != cudaSuccess) {
         fprintf(stderr, "msplat_loss_ssim_l1_noalloc: %s\n", cudaGetErrorString(e));
         return -5;
@@ -97,7 +101,7 @@ extern "C" int msplat_loss_ssim_l1_noalloc(const float *img, const uint8_t *gt, 
     la.v_img = v_img;
     la.loss_sum = loss_sum;
     la.nan_counts = nullptr;
-    launch_loss(la, s);
+    if (launch_loss(la, s) < 0) return -4;
     e = cudaGetLastError();
     if (e != cudaSuccess) {
         fprintf(stderr, "msplat_loss_ssim_l1_noalloc: launch: %s\n", cudaGetErrorString(e));

@@ -19,6 +19,9 @@
 // reference's 16x16-tile partition (loss_counted).  One launch covers every view of the
 // step (blocks are numbered view by view; the render and dL/dx are indexed
 // by global pixel, each view's target and mask by its own pixel).
+#include <cstdio>
+#include <mutex>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -386,25 +389,38 @@ __global__ void __launch_bounds__(256, 2) k_ssim_fused(LossArgs a) {
     if (nbad && a.nan_counts) atomicAdd(a.nan_counts + kNanVRendered, nbad);
 }
 
-// The window lives in each device's constant bank: upload it once per device.
-static bool g_gauss_ready[64] = {false};
+// Per-device set-up, done once per device under a lock: the window goes to
+// the device's constant bank and both kernel instantiations get their
+// shared-memory limit.  A device is marked ready only when every call
+// succeeded, so a failed first call is retried by the next one.
+static bool g_loss_ready[64] = {false};
+static std::mutex g_loss_mu;
+
+static cudaError_t loss_setup(int dev) {
+    std::lock_guard<std::mutex> lk(g_loss_mu);
+    if (g_loss_ready[dev]) return cudaSuccess;
+    double g[11], sum = 0;
+    for (int i = 0; i < 11; i++) { g[i] = exp(-((i - 5) * (i - 5)) / (2.0 * 1.5 * 1.5)); sum += g[i]; }
+    float w[11];
+    for (int i = 0; i < 11; i++) w[i] = (float)(g[i] / sum);
+    cudaError_t e = cudaMemcpyToSymbol(kGauss, w, sizeof(w));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_ssim_fused<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sizeof(FusedSmem));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_ssim_fused<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sizeof(FusedSmem));
+    if (e == cudaSuccess) g_loss_ready[dev] = true;
+    return e;
+}
 
 int launch_loss(const LossArgs &a, cudaStream_t s) {
     int dev = 0;
-    cudaGetDevice(&dev);
-    if (dev < 0 || dev >= 64 || !g_gauss_ready[dev]) {
-        double g[11], sum = 0;
-        for (int i = 0; i < 11; i++) { g[i] = exp(-((i - 5) * (i - 5)) / (2.0 * 1.5 * 1.5)); sum += g[i]; }
-        float w[11];
-        for (int i = 0; i < 11; i++) w[i] = (float)(g[i] / sum);
-        cudaMemcpyToSymbol(kGauss, w, sizeof(w));
-        if (dev >= 0 && dev < 64) g_gauss_ready[dev] = true;
-    }
-    static bool attr_set[64] = {false};
-    if (dev < 0 || dev >= 64 || !attr_set[dev]) {
-        cudaFuncSetAttribute(k_ssim_fused<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FusedSmem));
-        cudaFuncSetAttribute(k_ssim_fused<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FusedSmem));
-        if (dev >= 0 && dev < 64) attr_set[dev] = true;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
+    const cudaError_t e = loss_setup(dev);
+    if (e != cudaSuccess) {
+        fprintf(stderr, "msplat loss set-up: %s\n", cudaGetErrorString(e));
+        return -1;
     }
     const size_t smem = sizeof(FusedSmem);
     if (a.vt.count > 1) {
