@@ -169,7 +169,10 @@ int msplat_engine_mcmc(MsplatEngine *e, const MsplatGaussians *g, const MsplatAd
  * write dL/d(parameter) for every Gaussian into the caller's device buffers
  * (shapes of the parameters; zero for culled Gaussians and for SH bands
  * above args->degrees_to_use).  v_img: device float [H,W,3].  Same VJPs as
- * the training step (rasterize_backward_kernel, project_and_sh_backward_kernel). */
+ * the training step (rasterize_backward_kernel, project_and_sh_backward_kernel).
+ * Under a fixed intersection budget (msplat_engine_set_isect_budget) the
+ * view's lists must fit the budget in one tile group (error otherwise);
+ * without one, the legacy 48-per-Gaussian buffer is used. */
 typedef struct {
     float *v_means, *v_scales, *v_quats, *v_features_dc, *v_features_rest, *v_opacities;
 } MsplatGradients;

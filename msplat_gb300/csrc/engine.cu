@@ -460,19 +460,22 @@ class Engine {
         if (!out.v_means || !out.v_scales || !out.v_quats || !out.v_opacities || !out.v_features_dc ||
             (g.rest_bases > 0 && !out.v_features_rest))
             throw std::runtime_error("null gradient pointer");
+        // The raster arguments of this forward are needed below for the whole
+        // view at once: a fixed intersection budget is used when the view's
+        // lists fit it in one group (an error otherwise), else the legacy
+        // per-view buffer.
         const bool graphs = use_graphs_;
-        const long long slots = isect_slots_;
-        use_graphs_ = false;   // the raster arguments of this forward are needed below,
-        isect_slots_ = 0;      // for the whole view at once
+        use_graphs_ = false;
         try {
             train_step(g, nullptr, args, nullptr, nullptr, false);
         } catch (...) {
             use_graphs_ = graphs;
-            isect_slots_ = slots;
             throw;
         }
         use_graphs_ = graphs;
-        isect_slots_ = slots;
+        if (last_groups_ > 1)
+            throw std::runtime_error("backward: the view's intersections need " + std::to_string(last_groups_) +
+                                     " tile groups under the intersection budget; the backward takes one");
         const int N = g.num_points;
         if (N <= 0) return;
         CK(cudaMemsetAsync(ptr<GradRec>("grad"), 0, sizeof(GradRec) * (size_t)N, stream_));

@@ -243,6 +243,11 @@ template <class R> struct Step {
 
     explicit Step(const OrStepIn &i) : in(i) {}
 
+    // the tile-row band of a restricted step (all rows when none is set)
+    bool row_in_band(int ty) const {
+        return in.tile_row_hi <= in.tile_row_lo || (ty >= in.tile_row_lo && ty < in.tile_row_hi);
+    }
+
     void setup() {
         N = in.num_points;
         cam.width = in.width; cam.height = in.height;
@@ -333,8 +338,10 @@ template <class R> struct Step {
             if (!finite_bits(d) || d <= R(0)) continue;
             int x0, y0, x1, y1;
             tile_bbox(xys[2 * i], xys[2 * i + 1], aabb[2 * i], aabb[2 * i + 1], cam.tiles_x, cam.tiles_y, x0, y0, x1, y1);
-            for (int y = y0; y < y1; y++)
+            for (int y = y0; y < y1; y++) {
+                if (!row_in_band(y)) continue;
                 for (int x = x0; x < x1; x++) lists[(size_t)y * cam.tiles_x + x].push_back({d, i});
+            }
         }
         tile_start.assign(T + 1, 0);
         for (int t = 0; t < T; t++) {
@@ -403,6 +410,7 @@ template <class R> struct Step {
 #pragma omp parallel for schedule(dynamic, 1) reduction(+ : pairs, nsig)
             for (int t = 0; t < T; t++) {
                 int tx = t % cam.tiles_x, ty = t / cam.tiles_x;
+                if (!row_in_band(ty)) continue;
                 for (int yy = 0; yy < 16; yy++)
                     for (int xx = 0; xx < 16; xx++) {
                         int x = tx * 16 + xx, y = ty * 16 + yy;
@@ -420,6 +428,7 @@ template <class R> struct Step {
 #pragma omp parallel for schedule(dynamic, 1) reduction(+ : pairs, nsig)
             for (int t = 0; t < T; t++) {
                 int tx = t % cam.tiles_x, ty = t / cam.tiles_x;
+                if (!row_in_band(ty)) continue;
                 for (int k = 0; k < K; k++) {
                     long long cs = tile_start[t] + (long long)k * 512;
                     long long ce = std::min<long long>(tile_start[t] + (long long)(k + 1) * 512, tile_start[t + 1]);
@@ -651,6 +660,7 @@ template <class R> struct Step {
 #pragma omp parallel for schedule(dynamic, 1) reduction(+ : pairs)
         for (int t = 0; t < T; t++) {
             int tx = t % cam.tiles_x, ty = t / cam.tiles_x;
+            if (!row_in_band(ty)) continue;
             for (int yy = 0; yy < 16; yy++)
                 for (int xx = 0; xx < 16; xx++) {
                     int x = tx * 16 + xx, y = ty * 16 + yy;

@@ -69,6 +69,10 @@ typedef struct {
                              cutoffs (finite-difference checks of the VJPs) */
     const float *v_img_in; /* H*W*3 or NULL: backward from this dL/dimage instead
                              of the loss's (the autograd binding's contract) */
+    int tile_row_lo, tile_row_hi; /* hi > lo: only tiles in rows [lo, hi) get
+                             lists and are rasterized forward and backward
+                             (heavy-view checks on a band; other tiles stay
+                             empty) */
 } OrStepIn;
 
 typedef struct {

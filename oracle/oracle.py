@@ -42,6 +42,7 @@ class OrStepIn(C.Structure):
         ("max_disp", C.c_float),
         ("do_backward", C.c_int), ("do_optimizer", C.c_int), ("no_cutoff", C.c_int),
         ("v_img_in", FP),
+        ("tile_row_lo", C.c_int), ("tile_row_hi", C.c_int),
     ]
 
 
@@ -142,7 +143,7 @@ def num_threads() -> int:
 
 def train_step(prec: int, g, cam, step, *, moments=None, gt=None, mask=None, background=(0.0, 0.0, 0.0),
                ssim_weight=0.2, do_backward=True, do_optimizer=True, do_sgld=False, raster_mode=0, k_max=0,
-               isect_capacity=0, want_ids=True, no_cutoff=False, v_img=None):
+               isect_capacity=0, want_ids=True, no_cutoff=False, v_img=None, tile_rows=None, ids_capacity=0):
     """Run one oracle step.
 
     g        : GaussianSet, UPDATED IN PLACE when do_optimizer / do_sgld.
@@ -151,6 +152,10 @@ def train_step(prec: int, g, cam, step, *, moments=None, gt=None, mask=None, bac
                bc2_sqrt[6], beta1, beta2, eps, op_reg, sc_reg, invis_scale,
                loss_inv_n, seed, noise_lr, xyz_lr, max_disp).
     moments  : (exp_avg[6], exp_avg_sq[6]) float32 arrays, updated in place.
+    tile_rows: (lo, hi) or None: only tiles in rows [lo, hi) get lists and
+               are rasterized (forward and backward); the rest stay empty.
+    ids_capacity: slots of the returned id lists (0: the larger of 48 N and
+               isect_capacity).
     Returns a dict of numpy outputs.
     """
     L = lib()
@@ -201,6 +206,8 @@ def train_step(prec: int, g, cam, step, *, moments=None, gt=None, mask=None, bac
         v_img = np.ascontiguousarray(v_img, np.float32)
         keep.append(v_img)
         ins.v_img_in = _fp(v_img)
+    if tile_rows is not None:
+        ins.tile_row_lo, ins.tile_row_hi = int(tile_rows[0]), int(tile_rows[1])
 
     o = {
         "xys": np.zeros((N, 2), np.float32), "depths": np.zeros(N, np.float32), "conics": np.zeros((N, 3), np.float32),
@@ -219,7 +226,7 @@ def train_step(prec: int, g, cam, step, *, moments=None, gt=None, mask=None, bac
         setattr(out, k, a.ctypes.data_as(IP if a.dtype == np.int32 else FP))
     ids = None
     if want_ids:
-        cap = max(1, 48 * N)
+        cap = int(ids_capacity) if ids_capacity > 0 else max(1, 48 * N, int(isect_capacity))
         ids = np.zeros(cap, np.int32)
         out.gaussian_ids = ids.ctypes.data_as(IP)
         out.ids_capacity = cap

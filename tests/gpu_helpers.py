@@ -9,6 +9,39 @@ from msplat_gb300 import synthetic as S
 from oracle import oracle as O
 
 
+C0 = 0.28209479177387814
+C1 = 0.4886025119029199
+C2 = (1.0925484305920792, -1.0925484305920792, 0.31539156525252005, -1.0925484305920792, 0.5462742152960396)
+C3 = (-0.5900435899266435, 2.890611442640554, -0.4570457994644658, 0.3731763325901154, -0.4570457994644658,
+      1.445305721320277, -0.5900435899266435)
+
+
+def sh_basis(d):
+    """Real SH basis without the constant term, bands 1-3 (15 values), for unit directions d [N,3]."""
+    X, Y, Z = d[:, 0], d[:, 1], d[:, 2]
+    xx, yy, zz, xy, yz, xz = X * X, Y * Y, Z * Z, X * Y, Y * Z, X * Z
+    return np.stack([-C1 * Y, C1 * Z, -C1 * X,
+                     C2[0] * xy, C2[1] * yz, C2[2] * (2 * zz - xx - yy), C2[3] * xz, C2[4] * (xx - yy),
+                     C3[0] * Y * (3 * xx - yy), C3[1] * xy * Z, C3[2] * Y * (4 * zz - xx - yy),
+                     C3[3] * Z * (2 * zz - 3 * xx - 3 * yy), C3[4] * X * (4 * zz - xx - yy), C3[5] * Z * (xx - yy),
+                     C3[6] * X * (xx - 3 * yy)], axis=1)
+
+
+def sh_grads(g, cd, r, deg=3):
+    """dL/d(features_dc) and dL/d(features_rest) from the oracle's colour
+    gradient (the SH chain the projection backward applies)."""
+    d = g.means.astype(np.float64) - np.asarray(cd["cam_pos"], np.float64)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    vis = (r["radii"] > 0)[:, None]
+    vc = np.where(vis, r["v_colors"], 0.0)
+    v_dc = C0 * vc
+    nb = {0: 0, 1: 3, 2: 8, 3: 15}[deg]
+    basis = sh_basis(d)
+    v_rest = np.zeros(g.features_rest.shape)
+    v_rest[:, :nb, :] = basis[:, :nb, None] * vc[:, None, :]
+    return v_dc, v_rest
+
+
 def rel_l2(a, b):
     a = np.asarray(a, np.float64).ravel()
     b = np.asarray(b, np.float64).ravel()
@@ -97,3 +130,94 @@ def run_pair(init: S.GaussianSet, cam, gt, step: dict, *, raster_mode=0, k_max=0
         r["params"]["opacities"] = r["params"]["opacities"].reshape(-1)
         res[prec] = r
     return eo, res
+
+
+IMG_TOL = 1e-5
+GRAD_TOL = 1e-4
+FP64_BAR = 1e-3
+GRADS = ("v_xy", "v_conic", "v_colors", "v_opacity", "v_mean3d", "v_scale", "v_quat")
+
+
+def state_of(dg, like):
+    """The engine's parameters and Adam moments as a GaussianSet and moment
+    lists shaped like `like` (read back after a synchronize)."""
+    params, moments = dg.to_numpy()
+    shapes = [a.shape for a in like.arrays()]
+    g = S.GaussianSet(*(np.ascontiguousarray(params[n].reshape(sh)) for n, sh in zip(E.GROUPS, shapes)))
+    mom = tuple([np.ascontiguousarray(m[n].reshape(sh)) for n, sh in zip(E.GROUPS, shapes)] for m in moments)
+    return g, mom
+
+
+def oracle_from(prec, g, moments, cd, step, gt, do_sgld=True, raster_mode=0):
+    """One oracle step from a copy of (g, moments); returns its outputs and the
+    updated parameters."""
+    g = g.copy()
+    mom = ([a.copy() for a in moments[0]], [a.copy() for a in moments[1]])
+    r = O.train_step(prec, g, cd, step, moments=mom, gt=gt, do_sgld=do_sgld, raster_mode=raster_mode)
+    r["params"] = dict(zip(E.GROUPS, g.arrays()))
+    return r
+
+
+def engine_step(eng, dg, cd, cam, step, gt_d, do_sgld=True, raster_mode=0):
+    """One engine training step; its outputs, statistics and updated state."""
+    eng.train_step(dg, E.make_args(cd, step, do_sgld=do_sgld, raster_mode=raster_mode), gt_d.data_ptr())
+    eng.synchronize()
+    eo = engine_outputs(eng, dg.n, cam.width, cam.height)
+    eo["loss"] = eng.loss()
+    st = eng.stats()
+    eo["k_max"] = st.k_max
+    eo["check"] = list(st.check_record)
+    eo["params"], eo["moments"] = dg.to_numpy()
+    return eo
+
+
+def compare_step(eo, r32, before, label, r64=None):
+    """One step's parity bars: integer outputs, lists, last contributors and
+    visible projection outputs identical to the float path, image and final
+    transmittance within 1e-5, loss within 1e-5 relative, dL/dimage within
+    1e-5 and gradients and parameter updates within 1e-4 relative L2.
+    Against FP64 (r64) the errors are printed, returned and held to 1e-3
+    (gradients, updates) and to < 0.2 % of image values over 1e-5."""
+    act = r32["radii"] > 0
+    assert eo["check"][0] == 0
+    assert eo["k_max"] == r32["k_max"], (label, eo["k_max"], r32["k_max"])
+    assert np.array_equal(eo["radii"], r32["radii"]), label
+    assert np.array_equal(eo["num_tiles_hit"], r32["num_tiles_hit"]), label
+    for k in ("depths", "xys", "conics", "colors", "aabb"):
+        assert np.array_equal(eo[k][act], r32[k][act]), (label, k)
+    assert np.array_equal(eo["tile_counts"], r32["tile_counts"]), label
+    assert eo["num_isect"] == r32["num_isect"], label
+    assert np.array_equal(eo["gaussian_ids"], r32["gaussian_ids"]), label
+    assert np.array_equal(eo["final_idx"], r32["final_idx"]), label
+    assert np.max(np.abs(eo["out_img"] - r32["out_img"])) <= IMG_TOL, label
+    assert np.max(np.abs(eo["final_Ts"] - r32["final_Ts"])) <= IMG_TOL, label
+    assert abs(eo["loss"] - r32["loss"]) <= 1e-5 * abs(r32["loss"]), label
+    assert rel_l2(eo["v_rendered"], r32["v_rendered"]) <= 1e-5, label
+    for k in GRADS:
+        e = rel_l2(eo[k], r32[k])
+        assert e <= GRAD_TOL, (label, k, e)
+    for k in E.GROUPS:
+        b = before[k].reshape(eo["params"][k].shape)
+        e = rel_l2(eo["params"][k] - b, r32["params"][k].reshape(b.shape) - b)
+        assert e <= GRAD_TOL, (label, "update", k, e)
+    rep = {}
+    if r64 is not None:
+        d = np.abs(eo["out_img"] - r64["out_img"])
+        rep["image_max_abs"] = float(d.max())
+        rep["image_frac_over_1e-5"] = float(np.mean(d > IMG_TOL))
+        rep["lists_equal"] = bool(np.array_equal(eo["gaussian_ids"], r64["gaussian_ids"]))
+        rep["radii_mismatch"] = int(np.sum(eo["radii"] != r64["radii"]))
+        for k in GRADS:
+            rep[k] = rel_l2(eo[k], r64[k])
+        for k in E.GROUPS:
+            b = before[k].reshape(eo["params"][k].shape)
+            rep["update_" + k] = rel_l2(eo["params"][k] - b, r64["params"][k].reshape(b.shape) - b)
+        print(label, "FP64 errors:", {k: (round(v, 9) if isinstance(v, float) else v) for k, v in rep.items()})
+        assert rep["image_frac_over_1e-5"] < 2e-3
+        for k in GRADS:
+            assert rep[k] <= FP64_BAR, (label, k, rep[k])
+        for k in E.GROUPS:
+            assert rep["update_" + k] <= FP64_BAR, (label, k, rep["update_" + k])
+    return rep
+
+

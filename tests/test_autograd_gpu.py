@@ -9,27 +9,9 @@ from msplat_gb300 import engine as E
 from msplat_gb300 import synthetic as S
 from oracle import oracle as O
 
-from gpu_helpers import rel_l2
+from gpu_helpers import rel_l2, sh_grads
 
 pytestmark = pytest.mark.gpu
-
-C0 = 0.28209479177387814
-C1 = 0.4886025119029199
-C2 = (1.0925484305920792, -1.0925484305920792, 0.31539156525252005, -1.0925484305920792, 0.5462742152960396)
-C3 = (-0.5900435899266435, 2.890611442640554, -0.4570457994644658, 0.3731763325901154, -0.4570457994644658,
-      1.445305721320277, -0.5900435899266435)
-
-
-def _sh_basis(d):
-    """Real SH basis without the constant term, bands 1-3 (15 values), for unit directions d [N,3]."""
-    X, Y, Z = d[:, 0], d[:, 1], d[:, 2]
-    xx, yy, zz, xy, yz, xz = X * X, Y * Y, Z * Z, X * Y, Y * Z, X * Z
-    return np.stack([-C1 * Y, C1 * Z, -C1 * X,
-                     C2[0] * xy, C2[1] * yz, C2[2] * (2 * zz - xx - yy), C2[3] * xz, C2[4] * (xx - yy),
-                     C3[0] * Y * (3 * xx - yy), C3[1] * xy * Z, C3[2] * Y * (4 * zz - xx - yy),
-                     C3[3] * Z * (2 * zz - 3 * xx - 3 * yy), C3[4] * X * (4 * zz - xx - yy), C3[5] * Z * (xx - yy),
-                     C3[6] * X * (xx - 3 * yy)], axis=1)
-
 
 @pytest.fixture(scope="module")
 def scene():
@@ -64,19 +46,6 @@ def _oracle(prec, g, cd, W, deg=3, bg=(0.1, 0.2, 0.3), no_cutoff=False):
                         do_backward=True, do_optimizer=False, want_ids=False, no_cutoff=no_cutoff)
 
 
-def _sh_grads(g, cd, r, deg=3):
-    d = g.means.astype(np.float64) - np.asarray(cd["cam_pos"], np.float64)
-    d /= np.linalg.norm(d, axis=1, keepdims=True)
-    vis = (r["radii"] > 0)[:, None]
-    vc = np.where(vis, r["v_colors"], 0.0)
-    v_dc = C0 * vc
-    nb = {0: 0, 1: 3, 2: 8, 3: 15}[deg]
-    basis = _sh_basis(d)
-    v_rest = np.zeros(g.features_rest.shape)
-    v_rest[:, :nb, :] = basis[:, :nb, None] * vc[:, None, :]
-    return v_dc, v_rest
-
-
 def test_autograd_matches_oracle(scene):
     torch, g, cd, W = scene
     img, (gm, gs, gq, gdc, grest, gop) = _engine_grads(torch, g, cd, W)
@@ -86,7 +55,7 @@ def test_autograd_matches_oracle(scene):
             assert np.max(np.abs(img - r["out_img"])) <= 1e-5
         vis = r["radii"] > 0
         assert vis.sum() > 300
-        v_dc, v_rest = _sh_grads(g, cd, r)
+        v_dc, v_rest = sh_grads(g, cd, r)
         pairs = [("means", gm, np.where(vis[:, None], r["v_mean3d"], 0)),
                  ("scales", gs, np.where(vis[:, None], r["v_scale"], 0)),
                  ("quats", gq, np.where(vis[:, None], r["v_quat"], 0)),

@@ -205,3 +205,35 @@ def test_empty_scene(small):
     assert np.all(img == 0.0)
     assert np.isfinite(eng.loss())
     eng.close()
+
+
+def test_c1_run_sampled_steps(small):
+    """The small configuration as specified: one step, then 100 more (steps
+    1-101 over the 8 ring views in turn, the reference's schedules, SGLD on,
+    the chunked raster that its 256 tiles select).  Steps 1, 2, 51 and 101
+    are checked from the engine's own pre-step parameters and moments against
+    the float path (the usual bars) and FP64 (errors printed)."""
+    from gpu_helpers import compare_step, engine_step, oracle_from, state_of
+    import torch
+    sc, cam0, gt0, init = small
+    cams = sc.train_cams
+    cds = [E.camera_dict(c) for c in cams]
+    gts = [gt_image(sc.gt, c) for c in cams]
+    gts_d = [torch.from_numpy(g).cuda() for g in gts]
+    eng = E.Engine(0)
+    dg = E.DeviceGaussians(init)
+    sampled = {0, 1, 50, 100}
+    for k in range(101):
+        v = k % len(cams)
+        step = E.step_scalars(1 + k, 1 + k, width=cams[v].width, height=cams[v].height)
+        if k in sampled:
+            eng.synchronize()
+            g, mom = state_of(dg, init)
+            eo = engine_step(eng, dg, cds[v], cams[v], step, gts_d[v])
+            assert eo["k_max"] > 1   # chunked
+            r32 = oracle_from(32, g, mom, cds[v], step, gts[v])
+            r64 = oracle_from(64, g, mom, cds[v], step, gts[v])
+            compare_step(eo, r32, dict(zip(E.GROUPS, g.arrays())), f"c1 step {1 + k}", r64)
+        else:
+            eng.train_step(dg, E.make_args(cds[v], step, do_sgld=True), gts_d[v].data_ptr())
+    eng.close()
