@@ -943,8 +943,19 @@ template <class R> struct Step {
         const bool has_gt = in.gt != nullptr;
         if (has_gt) loss();
         if (in.v_img_in) v_rend.assign(in.v_img_in, in.v_img_in + 3 * (size_t)P);
-        if (in.do_backward && (has_gt || in.v_img_in)) {
-            raster_backward();
+        if (in.do_backward && (has_gt || in.v_img_in || in.raster_grads_in)) {
+            if (in.raster_grads_in) {
+                v_xy.assign(2 * (size_t)N, 0); v_conic.assign(3 * (size_t)N, 0);
+                v_col.assign(3 * (size_t)N, 0); v_op.assign(N, 0);
+                for (int i = 0; i < N; i++) {
+                    const float *g = in.raster_grads_in + 9 * (size_t)i;
+                    v_xy[2 * i] = g[0]; v_xy[2 * i + 1] = g[1];
+                    for (int k = 0; k < 3; k++) { v_conic[3 * i + k] = g[2 + k]; v_col[3 * i + k] = g[5 + k]; }
+                    v_op[i] = g[8];
+                }
+            } else {
+                raster_backward();
+            }
             project_backward();
             if (in.do_optimizer) optimizer();
         }
@@ -977,6 +988,9 @@ template <class R> struct Step {
 extern "C" {
 
 float or_det_expf(float x) { return det_expf(x); }
+
+// The SSIM window the float path uses (.metal:3376-3380).
+void or_gauss_1d(float out[11]) { gauss_1d<float>(out); }
 
 int or_train_step(int prec, const OrStepIn *in, OrStepOut *out) {
     if (!in || !out || in->num_points < 0 || in->width <= 0 || in->height <= 0) return -1;

@@ -73,6 +73,11 @@ typedef struct {
                              lists and are rasterized forward and backward
                              (heavy-view checks on a band; other tiles stay
                              empty) */
+    const float *raster_grads_in; /* N*9 or NULL: per-Gaussian rasterizer
+                             gradients (v_xy 2, v_conic 3, v_colors 3,
+                             v_opacity 1) used instead of running the raster
+                             backward (checks of the projection backward,
+                             SH Adam, regularizer and Adam in isolation) */
 } OrStepIn;
 
 typedef struct {
@@ -100,6 +105,7 @@ int or_train_step(int prec, const OrStepIn *in, OrStepOut *out);
 
 /* Deterministic float exp shared (by algorithm) with the CUDA engine. */
 float or_det_expf(float x);
+void or_gauss_1d(float out[11]);   /* the 11-tap SSIM window of the float path */
 
 /* Eq. 9 relocation (model.cpp:311-332), exactly as the reference computes it. */
 void or_compute_relocation(float opacity_old_sig, const float *scale_old_exp, int n,

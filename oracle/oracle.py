@@ -43,6 +43,7 @@ class OrStepIn(C.Structure):
         ("do_backward", C.c_int), ("do_optimizer", C.c_int), ("no_cutoff", C.c_int),
         ("v_img_in", FP),
         ("tile_row_lo", C.c_int), ("tile_row_hi", C.c_int),
+        ("raster_grads_in", FP),
     ]
 
 
@@ -80,6 +81,7 @@ def lib():
             L.or_train_step.restype = C.c_int
             L.or_det_expf.argtypes = [C.c_float]
             L.or_det_expf.restype = C.c_float
+            L.or_gauss_1d.argtypes = [FP]
             L.or_compute_relocation.argtypes = [C.c_float, FP, C.c_int, FP, FP]
             L.or_prepare_cam.argtypes = [FP, C.c_int, C.c_int, C.c_float, C.c_float, FP, FP, FP]
             for n in ("or_psnr", "or_l1"):
@@ -103,6 +105,12 @@ def _fp(a):
 def det_expf(x):
     L = lib()
     return np.array([L.or_det_expf(float(v)) for v in np.asarray(x, np.float32).ravel()], np.float32)
+
+
+def gauss_1d():
+    w = np.zeros(11, np.float32)
+    lib().or_gauss_1d(_fp(w))
+    return w
 
 
 def compute_relocation(o_old: float, s_old, n: int):
@@ -143,7 +151,8 @@ def num_threads() -> int:
 
 def train_step(prec: int, g, cam, step, *, moments=None, gt=None, mask=None, background=(0.0, 0.0, 0.0),
                ssim_weight=0.2, do_backward=True, do_optimizer=True, do_sgld=False, raster_mode=0, k_max=0,
-               isect_capacity=0, want_ids=True, no_cutoff=False, v_img=None, tile_rows=None, ids_capacity=0):
+               isect_capacity=0, want_ids=True, no_cutoff=False, v_img=None, tile_rows=None, ids_capacity=0,
+               raster_grads=None):
     """Run one oracle step.
 
     g        : GaussianSet, UPDATED IN PLACE when do_optimizer / do_sgld.
@@ -156,6 +165,9 @@ def train_step(prec: int, g, cam, step, *, moments=None, gt=None, mask=None, bac
                are rasterized (forward and backward); the rest stay empty.
     ids_capacity: slots of the returned id lists (0: the larger of 48 N and
                isect_capacity).
+    raster_grads: [N, 9] float32 or None: per-Gaussian rasterizer gradients
+               (v_xy, v_conic, v_colors, v_opacity) used in place of the
+               raster backward.
     Returns a dict of numpy outputs.
     """
     L = lib()
@@ -206,6 +218,10 @@ def train_step(prec: int, g, cam, step, *, moments=None, gt=None, mask=None, bac
         v_img = np.ascontiguousarray(v_img, np.float32)
         keep.append(v_img)
         ins.v_img_in = _fp(v_img)
+    if raster_grads is not None:
+        raster_grads = np.ascontiguousarray(raster_grads, np.float32).reshape(N, 9)
+        keep.append(raster_grads)
+        ins.raster_grads_in = _fp(raster_grads)
     if tile_rows is not None:
         ins.tile_row_lo, ins.tile_row_hi = int(tile_rows[0]), int(tile_rows[1])
 

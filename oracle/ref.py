@@ -1,0 +1,139 @@
+"""ctypes front end of oracle/_ref/libmsplat_ref.so — TEST INFRASTRUCTURE ONLY.
+
+The library is the reference's own Metal source for the per-Gaussian stages
+(projection + SH, projection backward + SH Adam, Adam, SGLD, regularizer,
+tile rectangle, sort key, active test, SSIM window), compiled as host C++ by
+oracle/ref_build.py from the reference tree.  It exists only where the
+reference tree does (the build container); the GPU machine never has it.  Only
+tests/ and tests/golden/make_ref_vectors.py use it, to pin the oracle.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_ref", "libmsplat_ref.so")
+REFERENCE = os.environ.get("MSPLAT_REFERENCE", "/root/reference")
+
+FP = C.POINTER(C.c_float)
+IP = C.POINTER(C.c_int)
+UP = C.POINTER(C.c_uint32)
+_lib = None
+
+
+def available() -> bool:
+    return os.path.exists(os.path.join(REFERENCE, "core", "metal", "msplat_metal.metal"))
+
+
+def lib():
+    """Build (from the reference tree) and load the library."""
+    global _lib
+    if _lib is None:
+        from oracle import ref_build
+        ref_build.build(REFERENCE, quiet=True)
+        _lib = C.CDLL(LIB_PATH)
+    return _lib
+
+
+def _p(a, t=FP):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+def set_expf(fn_ptr):
+    """exp() of the compiled source: a C function pointer float(float), or None for libm."""
+    L = lib()
+    L.ref_set_expf.argtypes = [C.c_void_p]
+    L.ref_set_expf(fn_ptr)
+
+
+def project_fwd(g, cam, degrees_to_use, clip=0.01):
+    """Projection + SH colour (project_and_sh_forward_kernel); outputs of culled
+    Gaussians stay zero."""
+    n = g.n
+    o = {"xys": np.zeros((n, 2), np.float32), "depths": np.zeros(n, np.float32), "radii": np.zeros(n, np.int32),
+         "conics": np.zeros((n, 3), np.float32), "num_tiles_hit": np.zeros(n, np.int32),
+         "colors": np.zeros((n, 3), np.float32), "aabb": np.zeros((n, 2), np.float32),
+         "nan_counts": np.zeros(16, np.uint32)}
+    deg = {0: 0, 3: 1, 8: 2, 15: 3}[g.features_rest.shape[1]]
+    cp = np.asarray(cam["cam_pos"], np.float32)
+    vm = np.ascontiguousarray(cam["viewmat"], np.float32).ravel()
+    pm = np.ascontiguousarray(cam["projmat"], np.float32).ravel()
+    lib().ref_project_fwd(
+        n, _p(g.means), _p(g.scales), _p(g.quats), _p(vm), _p(pm), C.c_float(cam["fx"]), C.c_float(cam["fy"]),
+        C.c_float(cam["cx"]), C.c_float(cam["cy"]), int(cam["width"]), int(cam["height"]), C.c_float(clip), deg,
+        int(degrees_to_use), _p(cp), _p(g.features_dc), _p(g.features_rest), _p(o["xys"]), _p(o["depths"]),
+        _p(o["radii"], IP), _p(o["conics"]), _p(o["num_tiles_hit"], IP), _p(o["colors"]), _p(o["aabb"]),
+        _p(o["nan_counts"], UP))
+    return o
+
+
+def step_after_raster(g, mom, cam, step, raster_grads, fwd, do_sgld=True):
+    """The reference's per-Gaussian work after the rasterizer backward, in the
+    host's order (core/src/model.cpp:901-975): projection backward with the
+    fused SH Adam, regularizer gradient, Adam on means/scales/quats/opacity,
+    SGLD.  g and mom (exp_avg[6], exp_avg_sq[6]) are updated in place.
+    raster_grads: [N, 9] (v_xy 2, v_conic 3, v_colors 3, v_opacity 1)."""
+    L = lib()
+    n = g.n
+    rg = np.ascontiguousarray(raster_grads, np.float32).reshape(n, 9)
+    v_xy = np.ascontiguousarray(rg[:, 0:2])
+    v_conic = np.ascontiguousarray(rg[:, 2:5])
+    v_col = np.ascontiguousarray(rg[:, 5:8])
+    v_op = np.ascontiguousarray(rg[:, 8])
+    v_mean = np.zeros((n, 3), np.float32)
+    v_scale = np.zeros((n, 3), np.float32)
+    v_quat = np.zeros((n, 4), np.float32)
+    nan = np.zeros(16, np.uint32)
+    deg = {0: 0, 3: 1, 8: 2, 15: 3}[g.features_rest.shape[1]]
+    cp = np.asarray(cam["cam_pos"], np.float32)
+    vm = np.ascontiguousarray(cam["viewmat"], np.float32).ravel()
+    pm = np.ascontiguousarray(cam["projmat"], np.float32).ravel()
+    ss, bc = step["step_size"], step["bc2_sqrt"]
+    f = C.c_float
+    ea, eas = mom
+    L.ref_project_bwd(
+        n, _p(g.means), _p(g.scales), _p(g.quats), _p(vm), _p(pm), f(cam["fx"]), f(cam["fy"]), f(cam["cx"]),
+        f(cam["cy"]), int(cam["width"]), int(cam["height"]), _p(fwd["radii"], IP), _p(fwd["conics"]), _p(v_xy), None,
+        _p(v_conic), _p(v_col), deg, int(step["degrees_to_use"]), _p(cp), _p(v_mean), _p(v_scale), _p(v_quat),
+        _p(g.features_dc), _p(g.features_rest), _p(ea[3]), _p(eas[3]), _p(ea[4]), _p(eas[4]), f(ss[3]), f(bc[3]),
+        f(ss[4]), f(bc[4]), f(step["beta1"]), f(step["beta2"]), f(step["eps"]), _p(nan, UP))
+    v_op_total = v_op.copy()
+    v_scale_total = v_scale.copy()
+    if step.get("op_reg", 0.0) > 0.0 or step.get("sc_reg", 0.0) > 0.0:
+        L.ref_reg_grad(n, _p(g.opacities), _p(g.scales), _p(v_op_total), _p(v_scale_total), f(step["op_reg"]),
+                       f(step["sc_reg"]), _p(fwd["radii"], IP), f(step.get("invis_scale", 1.0)), _p(eas[3]))
+    for grp, grad in ((0, v_mean), (1, v_scale_total), (2, v_quat), (5, v_op_total)):
+        p = [g.means, g.scales, g.quats, None, None, g.opacities][grp]
+        L.ref_adam(p.size, _p(p), _p(np.ascontiguousarray(grad)), _p(ea[grp]), _p(eas[grp]), f(ss[grp]),
+                   f(step["beta1"]), f(step["beta2"]), f(bc[grp]), f(step["eps"]), grp, _p(nan, UP))
+    noise = np.zeros((n, 3), np.float32)
+    if do_sgld:
+        L.ref_sgld(n, _p(g.means), _p(g.scales), _p(g.quats), _p(g.opacities), C.c_uint32(int(step["seed"])),
+                   f(step["noise_lr"]), f(step["xyz_lr"]), f(step["max_disp"]), _p(noise))
+    return {"v_mean3d": v_mean, "v_scale": v_scale, "v_quat": v_quat, "nan_counts": nan, "noise": noise}
+
+
+def tile_rects(xys, aabb, width, height):
+    n = xys.shape[0]
+    r = np.zeros((n, 4), np.int32)
+    lib().ref_tile_rect(n, _p(np.ascontiguousarray(xys, np.float32)), _p(np.ascontiguousarray(aabb, np.float32)),
+                        int(width), int(height), _p(r, IP))
+    return r
+
+
+def sort_keys(radii, depths):
+    n = radii.shape[0]
+    act = np.zeros(n, np.uint8)
+    keys = np.zeros(n, np.uint64)
+    lib().ref_sort_keys(n, _p(np.ascontiguousarray(radii, np.int32), IP), _p(np.ascontiguousarray(depths, np.float32)),
+                        act.ctypes.data_as(C.POINTER(C.c_uint8)), keys.ctypes.data_as(C.POINTER(C.c_uint64)))
+    return act.astype(bool), keys
+
+
+def gauss_1d():
+    w = np.zeros(11, np.float32)
+    lib().ref_gauss_1d(_p(w))
+    return w

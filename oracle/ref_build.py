@@ -1,0 +1,148 @@
+#!/usr/bin/env python3
+"""Builds oracle/_ref/libmsplat_ref.so: the reference's own Metal source for
+the per-Gaussian stages, compiled unchanged as host C++ — TEST
+INFRASTRUCTURE ONLY (it pins the oracle; nothing in the product uses it).
+
+The reference (semhfe/msplat) is Metal-only, so its kernels cannot run here.
+Its per-Gaussian helper functions and the bodies of its per-Gaussian kernels
+are plain arithmetic, however: this recipe copies those line ranges of
+core/metal/msplat_metal.metal, as they are, into oracle/_ref/ (git-ignored,
+never committed) and compiles them against oracle/metal_shim.h (the MSL
+types and functions) and oracle/ref_kernels.cpp (a host loop around each
+kernel body, with the kernel's own parameter names).
+
+Every range is checked against the text its first and last lines must hold,
+so an edited reference fails loudly instead of compiling something else.
+
+Left out on purpose, with the reason:
+  * the device-memory overloads of scale_rot_to_cov3d, project_cov3d_ewa,
+    cov2d_to_conic_vjp, project_cov3d_ewa_vjp and scale_rot_to_cov3d_vjp
+    (lines 180-197, 215-263, 1272-1286, 1302-1372, 1492-1533): with the
+    address-space qualifiers gone they would redefine the thread-local
+    overloads, which are the ones the fused kernels call;
+  * the device-pointer overloads of read_packed_float2/3 (370-372, 393-395),
+    for the same reason (the constant-pointer overloads take their calls);
+  * kernels that use threadgroup memory, SIMD-group functions or barriers
+    (tile mapping, sort, rasterizers, SSIM): they have no single-threaded
+    host form.
+
+Usage: python oracle/ref_build.py [--reference DIR]   (default: /root/reference)
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "_ref")
+LIB = os.path.join(OUT, "libmsplat_ref.so")
+METAL = os.path.join("core", "metal", "msplat_metal.metal")
+
+# (first line, last line, text of the first line, text of the last line), 1-based, inclusive
+HELPER_RANGES = [
+    (5, 179, "#define BLOCK_X 16", ""),                    # defines, SH constants, geometry helpers
+    (199, 214, "// Thread-local overload: writes cov3d", ""),  # scale_rot_to_cov3d (thread)
+    (265, 344, "// Thread-local overload: reads cov3d", "}"),  # project_cov3d_ewa (thread), bounds, project_pix
+    (349, 369, "inline int2 read_packed_int2(", ""),       # packed helpers
+    (374, 392, "inline void write_packed_float2(", ""),
+    (397, 416, "inline float3 read_packed_float3(device const", "}"),
+    (620, 776, "void sh_coeffs_to_color(", "}"),           # SH forward and VJP
+    (1251, 1271, "// given v_xy_pix, get v_xyz", ""),       # project_pix_vjp
+    (1288, 1301, "// Thread-local overload", ""),           # cov2d_to_conic_vjp (thread)
+    (1374, 1491, "// Thread-local overload: reads cov3d from registers, writes", ""),  # EWA VJP, quat VJP
+    (1535, 1569, "// Thread-local overload: reads v_cov3d", "}"),  # scale_rot_to_cov3d_vjp (thread)
+    (1836, 1858, "// Adam update helper", "};"),           # adam_update_element, SHAdamParams
+    (2248, 2276, "inline uint next_pow2(uint x) {", "}"),  # pad_count, make_sort_key, gaussian_is_active
+    (3376, 3380, "constant float GAUSS_1D[11] = {", "};"),
+    (3862, 3870, "static inline uint pcg_hash32(", "}"),
+]
+
+# kernel name -> parameter names that must appear in its signature (the host
+# wrappers in ref_kernels.cpp declare exactly these)
+KERNELS = {
+    "project_and_sh_forward_kernel": ["num_points", "means3d", "scales", "glob_scale", "quats", "viewmat", "projmat",
+                                      "intrins", "img_size", "tile_bounds", "clip_thresh", "xys", "depths", "radii",
+                                      "conics", "num_tiles_hit", "degree", "degrees_to_use", "cam_pos",
+                                      "features_dc", "features_rest", "colors", "aabb", "nan_counts", "gp"],
+    "project_and_sh_backward_kernel": ["num_points", "means3d", "scales", "glob_scale", "quats", "viewmat",
+                                       "projmat", "intrins", "img_size", "radii", "conics", "v_xy", "v_depth",
+                                       "v_conic", "v_mean3d", "v_scale", "v_quat", "degree", "degrees_to_use",
+                                       "cam_pos", "v_colors", "features_dc", "features_rest", "dc_exp_avg",
+                                       "dc_exp_avg_sq", "rest_exp_avg", "rest_exp_avg_sq", "adam_hp", "nan_counts",
+                                       "idx"],
+    "fused_adam_kernel": ["params", "grads", "exp_avg", "exp_avg_sq", "step_size", "beta1", "beta2", "bc2_sqrt",
+                          "eps", "n", "nan_counts", "group_idx", "tid"],
+    "sgld_noise_gen_kernel": ["noise", "N", "seed", "idx"],
+    "sgld_noise_kernel": ["means", "scales", "quats", "opacities", "noise", "N", "noise_lr", "xyz_lr", "max_disp",
+                          "idx"],
+    "mcmc_reg_grad_kernel": ["opacities", "scales", "v_opacity", "v_scale", "N", "op_reg", "sc_reg", "radii",
+                             "invis_scale", "v_dc_sq", "idx"],
+}
+
+
+def extract(lines, first, last, head, tail):
+    got_head = lines[first - 1].strip()
+    got_tail = lines[last - 1].strip()
+    if not got_head.startswith(head) or got_tail != tail:
+        raise SystemExit(f"{METAL}:{first}-{last}: expected '{head}' ... '{tail}', found '{got_head}' ... "
+                         f"'{got_tail}': the reference changed; review the ranges")
+    return f"#line {first} \"msplat_metal.metal\"\n" + "".join(lines[first - 1:last])
+
+
+def kernel_body(lines, name, params):
+    start = next((i for i, l in enumerate(lines) if l.startswith(f"kernel void {name}(")), None)
+    if start is None:
+        raise SystemExit(f"{METAL}: kernel {name} not found")
+    open_i = next(i for i in range(start, len(lines)) if lines[i].rstrip() == ") {")
+    sig = "".join(lines[start:open_i])
+    import re
+    for p in params:
+        if not re.search(r"\b" + re.escape(p) + r"\b", sig):
+            raise SystemExit(f"{METAL}:{start + 1}: parameter {p} of {name} not found")
+    close_i = next(i for i in range(open_i + 1, len(lines)) if lines[i].rstrip() == "}")
+    return f"#line {open_i + 2} \"msplat_metal.metal\"\n" + "".join(lines[open_i + 1:close_i]), (start + 1, close_i + 1)
+
+
+def build(reference: str, quiet: bool = False) -> str:
+    src = os.path.join(reference, METAL)
+    if not os.path.exists(src):
+        raise SystemExit(f"{src} not found")
+    with open(src) as f:
+        lines = f.readlines()
+    os.makedirs(OUT, exist_ok=True)
+    helpers = "// extracted by oracle/ref_build.py from " + METAL + " (not committed)\n"
+    helpers += "".join(extract(lines, *r) for r in HELPER_RANGES)
+    with open(os.path.join(OUT, "ref_helpers.inc"), "w") as f:
+        f.write(helpers)
+    spans = {}
+    for name, params in KERNELS.items():
+        body, span = kernel_body(lines, name, params)
+        spans[name] = span
+        with open(os.path.join(OUT, f"k_{name}.inc"), "w") as f:
+            f.write(body)
+    cxx = shutil.which("g++") or "c++"
+    cmd = [cxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
+           "-Wno-unknown-pragmas", "-I", HERE, "-I", OUT, os.path.join(HERE, "ref_kernels.cpp"), "-o", LIB]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise SystemExit(f"compile failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    if not quiet:
+        for name, (a, b) in spans.items():
+            print(f"{name}: {METAL}:{a}-{b}")
+        print(LIB)
+    return LIB
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default="/root/reference")
+    a = ap.parse_args()
+    build(a.reference)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,53 @@
+#!/usr/bin/env python3
+"""Writes tests/golden/ref_vectors.npz: inputs and outputs of the reference's
+own per-Gaussian Metal code (projection + SH, projection backward + SH Adam,
+regularizer, Adam, SGLD), compiled as host C++ by oracle/ref_build.py from the
+reference tree, on 512 random Gaussians at step 3001 — the vectors
+tests/test_ref_pin.py::test_golden_vectors holds the oracle to where the
+reference tree is absent.  Needs the reference tree (default /root/reference,
+or MSPLAT_REFERENCE).
+
+Usage: python tests/golden/make_ref_vectors.py
+"""
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.dirname(HERE))
+
+from msplat_gb300.schedule import GROUPS, step_scalars  # noqa: E402
+from oracle import oracle as O, ref as R  # noqa: E402
+from test_ref_pin import FWD_KEYS, random_inputs, ref_run, ring_camera  # noqa: E402
+
+
+def main():
+    R.lib()
+    R.set_expf(ctypes.cast(O.lib().or_det_expf, ctypes.c_void_p).value)
+    cam = ring_camera(640, 416, 500.0, k=3)
+    g, mom, rg = random_inputs(512, 7)
+    step = 3001
+    st = step_scalars(step, step, width=cam["width"], height=cam["height"])
+    fwd, bwd, g_r, mom_r = ref_run(g, mom, rg, cam, st)
+    out = {"step": np.int64(step), "in_raster_grads": rg, "gauss_1d": R.gauss_1d()}
+    for k, v in cam.items():
+        out["cam_" + k] = np.asarray(v)
+    for k, a, b in zip(GROUPS, g.arrays(), g_r.arrays()):
+        out["in_" + k], out["out_" + k] = a, b
+    for k, a, b, c, d in zip(GROUPS, mom[0], mom[1], mom_r[0], mom_r[1]):
+        out["in_m_" + k], out["in_v_" + k], out["out_m_" + k], out["out_v_" + k] = a, b, c, d
+    for k in FWD_KEYS + ("nan_counts",):
+        out["fwd_" + k] = fwd[k]
+    for k in ("v_mean3d", "v_scale", "v_quat"):
+        out["bwd_" + k] = bwd[k]
+    path = os.path.join(HERE, "ref_vectors.npz")
+    np.savez_compressed(path, **out)
+    print(path, os.path.getsize(path), "bytes")
+
+
+if __name__ == "__main__":
+    main()

@@ -171,14 +171,39 @@ def engine_step(eng, dg, cd, cam, step, gt_d, do_sgld=True, raster_mode=0):
     return eo
 
 
+def step_errors(eo, r, before):
+    """Errors of the engine's step outputs against one oracle run."""
+    e = {"image_max_abs": float(np.max(np.abs(eo["out_img"] - r["out_img"]))),
+         "final_T_max_abs": float(np.max(np.abs(eo["final_Ts"] - r["final_Ts"]))),
+         "loss_rel": abs(eo["loss"] - r["loss"]) / max(abs(r["loss"]), 1e-30),
+         "v_rendered": rel_l2(eo["v_rendered"], r["v_rendered"])}
+    for k in GRADS:
+        e[k] = rel_l2(eo[k], r[k])
+    for k in E.GROUPS:
+        b = before[k].reshape(eo["params"][k].shape)
+        e["update_" + k] = rel_l2(eo["params"][k] - b, r["params"][k].reshape(b.shape) - b)
+    return e
+
+
 def compare_step(eo, r32, before, label, r64=None):
     """One step's parity bars: integer outputs, lists, last contributors and
-    visible projection outputs identical to the float path, image and final
-    transmittance within 1e-5, loss within 1e-5 relative, dL/dimage within
-    1e-5 and gradients and parameter updates within 1e-4 relative L2.
-    Against FP64 (r64) the errors are printed, returned and held to 1e-3
-    (gradients, updates) and to < 0.2 % of image values over 1e-5."""
+    visible projection outputs identical to the float path; image and final
+    transmittance within 1e-5 max-abs; loss within 1e-5 relative; dL/dimage,
+    the rasterizer and projection gradients and every parameter update within
+    1e-4 relative L2.  Every error is printed first.  Against FP64 (r64) the
+    errors are printed and returned, and held to 1e-3 (gradients, updates)
+    and to < 0.2 % of image values over 1e-5."""
     act = r32["radii"] > 0
+    e32 = step_errors(eo, r32, before)
+    print(label, "float-path errors:", {k: float("%.3g" % v) for k, v in e32.items()})
+    rep = {}
+    if r64 is not None:
+        rep = step_errors(eo, r64, before)
+        d = np.abs(eo["out_img"] - r64["out_img"])
+        rep["image_frac_over_1e-5"] = float(np.mean(d > IMG_TOL))
+        rep["lists_equal"] = bool(np.array_equal(eo["gaussian_ids"], r64["gaussian_ids"]))
+        rep["radii_mismatch"] = int(np.sum(eo["radii"] != r64["radii"]))
+        print(label, "FP64 errors:", {k: (float("%.3g" % v) if isinstance(v, float) else v) for k, v in rep.items()})
     assert eo["check"][0] == 0
     assert eo["k_max"] == r32["k_max"], (label, eo["k_max"], r32["k_max"])
     assert np.array_equal(eo["radii"], r32["radii"]), label
@@ -189,35 +214,15 @@ def compare_step(eo, r32, before, label, r64=None):
     assert eo["num_isect"] == r32["num_isect"], label
     assert np.array_equal(eo["gaussian_ids"], r32["gaussian_ids"]), label
     assert np.array_equal(eo["final_idx"], r32["final_idx"]), label
-    assert np.max(np.abs(eo["out_img"] - r32["out_img"])) <= IMG_TOL, label
-    assert np.max(np.abs(eo["final_Ts"] - r32["final_Ts"])) <= IMG_TOL, label
-    assert abs(eo["loss"] - r32["loss"]) <= 1e-5 * abs(r32["loss"]), label
-    assert rel_l2(eo["v_rendered"], r32["v_rendered"]) <= 1e-5, label
-    for k in GRADS:
-        e = rel_l2(eo[k], r32[k])
-        assert e <= GRAD_TOL, (label, k, e)
-    for k in E.GROUPS:
-        b = before[k].reshape(eo["params"][k].shape)
-        e = rel_l2(eo["params"][k] - b, r32["params"][k].reshape(b.shape) - b)
-        assert e <= GRAD_TOL, (label, "update", k, e)
-    rep = {}
+    assert e32["image_max_abs"] <= IMG_TOL and e32["final_T_max_abs"] <= IMG_TOL, label
+    assert e32["loss_rel"] <= 1e-5, label
+    for k, v in e32.items():
+        if k not in ("image_max_abs", "final_T_max_abs", "loss_rel"):
+            assert v <= GRAD_TOL, (label, k, v)
     if r64 is not None:
-        d = np.abs(eo["out_img"] - r64["out_img"])
-        rep["image_max_abs"] = float(d.max())
-        rep["image_frac_over_1e-5"] = float(np.mean(d > IMG_TOL))
-        rep["lists_equal"] = bool(np.array_equal(eo["gaussian_ids"], r64["gaussian_ids"]))
-        rep["radii_mismatch"] = int(np.sum(eo["radii"] != r64["radii"]))
-        for k in GRADS:
-            rep[k] = rel_l2(eo[k], r64[k])
-        for k in E.GROUPS:
-            b = before[k].reshape(eo["params"][k].shape)
-            rep["update_" + k] = rel_l2(eo["params"][k] - b, r64["params"][k].reshape(b.shape) - b)
-        print(label, "FP64 errors:", {k: (round(v, 9) if isinstance(v, float) else v) for k, v in rep.items()})
         assert rep["image_frac_over_1e-5"] < 2e-3
         for k in GRADS:
             assert rep[k] <= FP64_BAR, (label, k, rep[k])
         for k in E.GROUPS:
             assert rep["update_" + k] <= FP64_BAR, (label, k, rep["update_" + k])
     return rep
-
-

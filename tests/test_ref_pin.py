@@ -1,0 +1,174 @@
+"""The oracle pinned to the reference's own source (CPU).
+
+oracle/ref_build.py compiles the reference's per-Gaussian Metal code —
+helper functions and the bodies of project_and_sh_forward_kernel,
+project_and_sh_backward_kernel (with its fused SH Adam), fused_adam_kernel,
+sgld_noise_gen/sgld_noise_kernel and mcmc_reg_grad_kernel — unchanged as host
+C++ (oracle/_ref, built from the reference tree).  Its outputs must equal the
+oracle's float path bit for bit: projection (centres, depths, radii, conics,
+tiles hit, colours, extents), the tile rectangles, the sort keys and active
+test that order every per-tile list, the SSIM window, and, from the same
+rasterizer gradients, the projection VJPs, the SH Adam, regularizer, Adam and
+SGLD updates of every parameter and moment.  exp() is the same function on
+both sides (the oracle's det_expf; Metal's exp has no published bits).
+
+Two parts:
+  * live, on 100,000 random Gaussians (with culled, degenerate, non-finite and
+    extreme ones), where the reference tree exists (the build container);
+  * against the committed vectors tests/golden/ref_vectors.npz, made by
+    tests/golden/make_ref_vectors.py from the same library, everywhere.
+"""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+from msplat_gb300 import synthetic as S
+from msplat_gb300.schedule import GROUPS, step_scalars
+from oracle import oracle as O
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_vectors.npz")
+FWD_KEYS = ("xys", "depths", "radii", "conics", "num_tiles_hit", "colors", "aabb")
+
+
+def ring_camera(width=1297, height=840, fx=1000.0, k=1):
+    cam = S.ring_cameras(8, width, height, fx)[k]
+    vm, pm, cp = O.prepare_cam(cam.cam_to_world, cam.width, cam.height, cam.fx, cam.fy)
+    return dict(viewmat=vm, projmat=pm, cam_pos=cp, fx=cam.fx, fy=cam.fy, cx=cam.cx, cy=cam.cy, width=cam.width,
+                height=cam.height)
+
+
+def random_inputs(n, seed):
+    """Gaussians in and around the view (plus extreme, culled, degenerate and
+    non-finite ones), random Adam moments and rasterizer gradients."""
+    rng = np.random.default_rng(seed)
+    g = S.gaussians(n, seed)
+    g.means *= np.float32(1.5)
+    k = rng.permutation(n)
+    g.scales[k[:n // 100]] = rng.uniform(-1.0, 1.0, (n // 100, 3)).astype(np.float32)       # huge
+    g.scales[k[n // 100:n // 50]] = np.float32(-14.0)                                       # tiny (det cut)
+    g.scales[k[n // 50:n // 50 + 4]] = np.float32(-20.0)                                    # below the clamp
+    g.quats[k[200:210]] = 0.0                                                               # epsilon floor
+    g.means[k[300:310]] = np.array([3.0, 0.0, 0.5], np.float32)                             # at the camera
+    g.features_dc[k[400]] = np.nan                                                          # zombie gate
+    g.features_rest[k[401], 3, 1] = np.inf
+    g.opacities[:, 0] = rng.normal(0.0, 3.0, n).astype(np.float32)
+    mom = ([np.abs(rng.normal(0, 1e-3, a.shape)).astype(np.float32) * (rng.random(a.shape) < 0.8) for a in g.arrays()],
+           [np.abs(rng.normal(0, 1e-6, a.shape)).astype(np.float32) * (rng.random(a.shape) < 0.8) for a in g.arrays()])
+    rg = np.concatenate([rng.normal(0, 1e-4, (n, 2)), rng.normal(0, 1e-3, (n, 3)), rng.normal(0, 1e-3, (n, 3)),
+                         rng.normal(0, 1e-3, (n, 1))], axis=1).astype(np.float32)
+    rg[k[500], 5] = np.nan          # SH Adam gate
+    rg[k[501], 0] = np.inf          # Adam gate on the means
+    return g, mom, rg
+
+
+def oracle_run(g, mom, rg, cam, step):
+    g = g.copy()
+    mom = ([a.copy() for a in mom[0]], [a.copy() for a in mom[1]])
+    r = O.train_step(32, g, cam, step, moments=mom, raster_grads=rg, do_backward=True, do_optimizer=True,
+                     do_sgld=True, want_ids=True)
+    return r, g, mom
+
+
+def ref_run(g, mom, rg, cam, step):
+    from oracle import ref as R
+    g = g.copy()
+    mom = ([a.copy() for a in mom[0]], [a.copy() for a in mom[1]])
+    fwd = R.project_fwd(g, cam, step["degrees_to_use"])
+    bwd = R.step_after_raster(g, mom, cam, step, rg, fwd)
+    return fwd, bwd, g, mom
+
+
+def _same(a, b):
+    return np.array_equal(np.asarray(a), np.asarray(b), equal_nan=True)
+
+
+def compare(r, g_o, mom_o, fwd, bwd, g_r, mom_r):
+    act = fwd["radii"] > 0
+    assert act.sum() > 0.3 * act.size
+    assert _same(r["radii"], fwd["radii"]) and _same(r["num_tiles_hit"], fwd["num_tiles_hit"])
+    for k in ("xys", "depths", "conics", "colors", "aabb"):
+        assert _same(r[k][act], fwd[k][act]), k
+    assert _same(r["nan_counts"][7:13], fwd["nan_counts"][7:13])
+    for k in ("v_mean3d", "v_scale", "v_quat"):
+        assert _same(np.where(act[:, None], r[k], 0), bwd[k]), k
+    for name, a, b in zip(GROUPS, g_o.arrays(), g_r.arrays()):
+        assert _same(a, b), name
+    for m in range(2):
+        for name, a, b in zip(GROUPS, mom_o[m], mom_r[m]):
+            assert _same(a, b), (m, name)
+
+
+needs_reference = pytest.mark.skipif(not __import__("oracle.ref", fromlist=["available"]).available(),
+                                     reason="the reference tree is not present (the GPU box)")
+
+
+@pytest.fixture(scope="module")
+def ref_lib():
+    from oracle import ref as R
+    R.lib()
+    R.set_expf(ctypes.cast(O.lib().or_det_expf, ctypes.c_void_p).value)
+    return R
+
+
+@needs_reference
+@pytest.mark.parametrize("step_no,deg", [(1, 0), (1500, 1), (2500, 2), (3001, 3)])
+def test_live_per_gaussian_stages(ref_lib, step_no, deg):
+    cam = ring_camera()
+    g, mom, rg = random_inputs(100_000, 11 + step_no)
+    step = step_scalars(step_no, step_no, width=cam["width"], height=cam["height"])
+    assert step["degrees_to_use"] == deg
+    r, g_o, mom_o = oracle_run(g, mom, rg, cam, step)
+    fwd, bwd, g_r, mom_r = ref_run(g, mom, rg, cam, step)
+    compare(r, g_o, mom_o, fwd, bwd, g_r, mom_r)
+
+
+@needs_reference
+def test_live_tile_lists(ref_lib):
+    """Per-tile lists from the reference's get_tile_bbox, gaussian_is_active and
+    make_sort_key (ascending keys) equal the oracle's lists."""
+    cam = ring_camera(320, 208, 260.0)
+    g, mom, rg = random_inputs(20_000, 5)
+    step = step_scalars(3001, 3001, width=cam["width"], height=cam["height"])
+    r = O.train_step(32, g.copy(), cam, step, do_backward=False, do_optimizer=False, want_ids=True)
+    fwd = ref_lib.project_fwd(g, cam, 3)
+    rect = ref_lib.tile_rects(fwd["xys"], fwd["aabb"], cam["width"], cam["height"])
+    act, keys = ref_lib.sort_keys(fwd["radii"], fwd["depths"])
+    tx, ty = (cam["width"] + 15) // 16, (cam["height"] + 15) // 16
+    lists = [[] for _ in range(tx * ty)]
+    for i in np.flatnonzero(act):
+        x0, y0, x1, y1 = rect[i]
+        for y in range(y0, y1):
+            for x in range(x0, x1):
+                lists[y * tx + x].append(i)
+    ids = np.concatenate([np.array(sorted(L, key=lambda i: int(keys[i])), np.int64) for L in lists if L])
+    assert ids.size == r["num_isect"] > 10_000
+    assert np.array_equal(ids, r["gaussian_ids"])
+    assert np.array_equal([len(L) for L in lists], r["tile_counts"])
+
+
+@needs_reference
+def test_live_ssim_window(ref_lib):
+    assert np.array_equal(ref_lib.gauss_1d(), O.gauss_1d())
+
+
+def test_golden_vectors():
+    """The oracle against the reference library's outputs stored in
+    tests/golden/ref_vectors.npz (no reference tree needed)."""
+    z = np.load(GOLDEN)
+    cam = {k[4:]: z[k] for k in z.files if k.startswith("cam_")}
+    for k in ("fx", "fy", "cx", "cy"):
+        cam[k] = float(cam[k])
+    for k in ("width", "height"):
+        cam[k] = int(cam[k])
+    g = S.GaussianSet(*(z["in_" + k] for k in GROUPS))
+    mom = ([z["in_m_" + k] for k in GROUPS], [z["in_v_" + k] for k in GROUPS])
+    step = step_scalars(int(z["step"]), int(z["step"]), width=cam["width"], height=cam["height"])
+    r, g_o, mom_o = oracle_run(g, mom, z["in_raster_grads"], cam, step)
+    fwd = {k: z["fwd_" + k] for k in FWD_KEYS + ("nan_counts",)}
+    bwd = {k: z["bwd_" + k] for k in ("v_mean3d", "v_scale", "v_quat")}
+    g_r = S.GaussianSet(*(z["out_" + k] for k in GROUPS))
+    mom_r = ([z["out_m_" + k] for k in GROUPS], [z["out_v_" + k] for k in GROUPS])
+    compare(r, g_o, mom_o, fwd, bwd, g_r, mom_r)
+    assert np.array_equal(O.gauss_1d(), z["gauss_1d"])
