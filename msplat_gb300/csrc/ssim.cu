@@ -284,7 +284,9 @@ __global__ void __launch_bounds__(256, 2) k_ssim_fused(LossArgs a) {
                         f3 = mval * dsxy;
                     }
                     if (own && loss_counted(xc, yc, W, H)) {
-                        ssim_acc += mval * (A * B) * iCD;
+                        // the loss value takes the reference's one IEEE division: the fast
+                        // reciprocals' bias, summed over every pixel, is visible at low loss
+                        ssim_acc += mval * __fdiv_rn(A * B, Cd * D);
                         l1_acc += mval * fabsf((float)sm.g[c][fy + 5][fx + 5] * (1.0f / 255.0f) - sm.r[c][fy + 5][fx + 5]);
                     }
                 }

@@ -10,8 +10,9 @@
 // products evaluated as sums over k in increasing order, each product
 // rounded before it is added (the translation unit is compiled with
 // -ffp-contract=off); the MSL functions they call (min, max, clamp, exp,
-// sqrt, rsqrt, ceil, dot, normalize, transpose, fma, as_type, clz, atomics);
-// and empty address-space qualifiers.
+// sqrt, rsqrt, ceil, dot, normalize, transpose, fma, as_type, clz, atomics,
+// threadgroup barriers and the SIMD-group reductions, on host threads); and
+// empty address-space qualifiers (threadgroup storage: see below).
 //
 // Two choices are made where MSL leaves the bits open: exp() calls the
 // function installed by ref_set_expf (the oracle's det_expf on both sides of
@@ -21,12 +22,22 @@
 // reproduced: this compiles the source's written arithmetic, in IEEE order.
 #pragma once
 
+// standard headers first: the address-space macros below would rewrite them
+#include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <condition_variable>
 #include <cstdint>
 #include <cstring>
+#include <mutex>
+#include <thread>
 #include <type_traits>
+#include <vector>
 
 typedef uint32_t uint;
+namespace mshim {
+using HostThread = std::thread;   // named before `thread` becomes an address-space macro
+}
 typedef uint8_t uchar;
 
 #define device
@@ -175,11 +186,113 @@ template <class To, class From> inline To as_type(From f) {
     return t;
 }
 
-// Device atomics of a single-threaded host emulation.
+inline float fabs(float x) { return std::fabs(x); }
+inline float3 max(float3 v, float s) { return {max(v.x, s), max(v.y, s), max(v.z, s)}; }
+inline float3 fma(float3 a, float b, float3 c) { return {fma(a.x, b, c.x), fma(a.y, b, c.y), fma(a.z, b, c.z)}; }
+inline float3 fma(float3 a, float3 b, float3 c) { return {fma(a.x, b.x, c.x), fma(a.y, b.y, c.y), fma(a.z, b.z, c.z)}; }
+inline float3 saturate(float3 v) { return {saturate(v.x), saturate(v.y), saturate(v.z)}; }
+
+// Device atomics: every read-modify-write under one lock (threadgroups are
+// emulated by host threads, see below).
+namespace mshim {
+std::mutex &atomic_lock();
+}
 typedef uint atomic_uint;
+typedef float atomic_float;
 enum mshim_memory_order { memory_order_relaxed };
 inline uint atomic_fetch_add_explicit(atomic_uint *p, uint v, mshim_memory_order) {
+    std::lock_guard<std::mutex> lk(mshim::atomic_lock());
     const uint o = *p;
     *p = o + v;
     return o;
+}
+inline float atomic_fetch_add_explicit(atomic_float *p, float v, mshim_memory_order) {
+    std::lock_guard<std::mutex> lk(mshim::atomic_lock());
+    const float o = *p;
+    *p = o + v;
+    return o;
+}
+
+// Threadgroups on host threads.  A kernel that uses threadgroup memory,
+// threadgroup barriers or SIMD-group functions runs each threadgroup as one
+// host thread per GPU thread; its `threadgroup` arrays become function
+// statics (groups run one after another, so one copy serves each group),
+// threadgroup_barrier is a barrier of the group's threads, and a SIMD group
+// is 32 consecutive threads of the group whose simd_* calls meet at a
+// barrier of their own (the reference calls them from all lanes).  simd_sum
+// adds the lanes in lane order.
+namespace mshim {
+struct HostBarrier {
+    int n = 0;
+    std::atomic<int> waiting{0};
+    std::atomic<uint32_t> generation{0};
+    void wait() {
+        const uint32_t gen = generation.load(std::memory_order_acquire);
+        if (waiting.fetch_add(1, std::memory_order_acq_rel) + 1 == n) {
+            waiting.store(0, std::memory_order_relaxed);
+            generation.fetch_add(1, std::memory_order_acq_rel);
+            generation.notify_all();
+        } else {
+            while (generation.load(std::memory_order_acquire) == gen) generation.wait(gen, std::memory_order_acquire);
+        }
+    }
+};
+struct SimdGroup {
+    HostBarrier bar;
+    alignas(16) unsigned char slot[2][32][16];
+};
+struct GroupState {
+    HostBarrier bar;
+    SimdGroup sg[32];
+};
+extern GroupState *g_group;
+extern thread_local int t_lane, t_sg;
+extern thread_local unsigned t_simd_op;
+
+// One exchange per SIMD-group call: every lane writes its value, meets the
+// others at the barrier, then reduces.  Consecutive calls alternate between
+// two slot sets, so one barrier per call suffices (a lane can only reuse a
+// set after every lane has passed the next call's barrier).
+template <class T, class F> inline T simd_exchange(const T &v, F reduce) {
+    static_assert(sizeof(T) <= 16, "simd value size");
+    SimdGroup &sg = g_group->sg[t_sg];
+    unsigned char (*slot)[16] = sg.slot[t_simd_op++ & 1u];
+    std::memcpy(slot[t_lane], &v, sizeof(T));
+    sg.bar.wait();
+    return reduce(slot);
+}
+template <class T> inline T lane_value(const unsigned char (*slot)[16], int lane) {
+    T v;
+    std::memcpy(&v, slot[lane], sizeof(T));
+    return v;
+}
+}  // namespace mshim
+
+namespace mem_flags {
+enum { mem_none = 0, mem_threadgroup = 1, mem_device = 2 };
+}
+inline void threadgroup_barrier(int) { mshim::g_group->bar.wait(); }
+inline float simd_sum(float v) {
+    return mshim::simd_exchange(v, [](const unsigned char (*sl)[16]) {
+        float s = mshim::lane_value<float>(sl, 0);
+        for (int l = 1; l < 32; l++) s = s + mshim::lane_value<float>(sl, l);
+        return s;
+    });
+}
+inline int simd_max(int v) {
+    return mshim::simd_exchange(v, [](const unsigned char (*sl)[16]) {
+        int s = mshim::lane_value<int>(sl, 0);
+        for (int l = 1; l < 32; l++) s = max(s, mshim::lane_value<int>(sl, l));
+        return s;
+    });
+}
+inline int simd_or(int v) {
+    return mshim::simd_exchange(v, [](const unsigned char (*sl)[16]) {
+        int s = 0;
+        for (int l = 0; l < 32; l++) s |= mshim::lane_value<int>(sl, l);
+        return s;
+    });
+}
+template <class T> inline T simd_broadcast(T v, int lane) {
+    return mshim::simd_exchange(v, [lane](const unsigned char (*sl)[16]) { return mshim::lane_value<T>(sl, lane); });
 }

@@ -137,3 +137,45 @@ def gauss_1d():
     w = np.zeros(11, np.float32)
     lib().ref_gauss_1d(_p(w))
     return w
+
+
+def raster_step(fwd, opacities, cam, gt=None, mask=None, v_img=None, background=(0.0, 0.0, 0.0), ssim_weight=0.2,
+                loss_inv_n=None, ids_capacity=None):
+    """The pixel stages of one monolithic step of one view from the
+    reference's kernels (count, scatter, forward raster, SSIM + L1 loss,
+    backward raster; the sort and pack restated): lists, image, final
+    transmittance and last contributors, loss sum, dL/dimage and the
+    per-Gaussian rasterizer gradients.  gt (uint8 [H,W,3]) runs the loss;
+    otherwise v_img is the image gradient."""
+    W, H = int(cam["width"]), int(cam["height"])
+    n = fwd["radii"].shape[0]
+    T = ((W + 15) // 16) * ((H + 15) // 16)
+    cap = int(ids_capacity or max(1, 64 * n))
+    o = {"tile_bins": np.zeros((T, 2), np.int32), "gaussian_ids": np.zeros(cap, np.int32),
+         "out_img": np.zeros((H, W, 3), np.float32), "final_Ts": np.zeros((H, W), np.float32),
+         "final_idx": np.zeros((H, W), np.int32), "loss_sum": np.zeros(1, np.float32),
+         "v_rendered": np.zeros((H, W, 3), np.float32) if v_img is None else np.ascontiguousarray(v_img, np.float32).copy(),
+         "v_xy": np.zeros((n, 2), np.float32), "v_conic": np.zeros((n, 3), np.float32),
+         "v_colors": np.zeros((n, 3), np.float32), "v_opacity": np.zeros(n, np.float32),
+         "nan_counts": np.zeros(16, np.uint32)}
+    bg = np.asarray(background, np.float32)
+    gt = None if gt is None else np.ascontiguousarray(gt, np.uint8)
+    mask = None if mask is None else np.ascontiguousarray(mask, np.uint8)
+    u8 = C.POINTER(C.c_uint8)
+    L = lib()
+    L.ref_raster_step.restype = C.c_longlong
+    m = L.ref_raster_step(
+        n, _p(fwd["xys"]), _p(fwd["depths"]), _p(fwd["radii"], IP), _p(fwd["conics"]), _p(fwd["colors"]),
+        _p(fwd["aabb"]), _p(np.ascontiguousarray(opacities, np.float32).reshape(-1)), W, H, _p(bg),
+        None if gt is None else gt.ctypes.data_as(u8), None if mask is None else mask.ctypes.data_as(u8),
+        C.c_float(ssim_weight), C.c_float(loss_inv_n if loss_inv_n is not None else 1.0 / (3.0 * W * H)),
+        _p(o["tile_bins"], IP), _p(o["gaussian_ids"], IP), C.c_longlong(cap), _p(o["out_img"]), _p(o["final_Ts"]),
+        _p(o["final_idx"], IP), _p(o["loss_sum"]), _p(o["v_rendered"]), _p(o["v_xy"]), _p(o["v_conic"]),
+        _p(o["v_colors"]), _p(o["v_opacity"]), _p(o["nan_counts"], UP))
+    if m < 0:
+        raise RuntimeError("more intersections than ids_capacity")
+    o["num_isect"] = int(m)
+    o["gaussian_ids"] = o["gaussian_ids"][:m].copy()
+    o["loss"] = float(o["loss_sum"][0]) / (W * H)
+    o["raster_grads"] = np.concatenate([o["v_xy"], o["v_conic"], o["v_colors"], o["v_opacity"][:, None]], axis=1)
+    return o

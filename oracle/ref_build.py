@@ -22,9 +22,14 @@ Left out on purpose, with the reason:
     overloads, which are the ones the fused kernels call;
   * the device-pointer overloads of read_packed_float2/3 (370-372, 393-395),
     for the same reason (the constant-pointer overloads take their calls);
-  * kernels that use threadgroup memory, SIMD-group functions or barriers
-    (tile mapping, sort, rasterizers, SSIM): they have no single-threaded
-    host form.
+  * the tile scan and the per-tile sort + pack (prefix_sum_tiles_kernel,
+    hybrid_sort_pack_kernel): their 1024-thread bitonic networks are not
+    emulated; ref_kernels.cpp restates what they compute (exclusive scans of
+    the padded and exact counts, ascending keys per tile, the pack gates);
+  * the chunked rasterizer (used below 400 tiles), not compiled yet.
+
+The rasterizers and the SSIM kernels use threadgroup memory, barriers and
+SIMD-group functions; metal_shim.h runs their threadgroups on host threads.
 
 Usage: python oracle/ref_build.py [--reference DIR]   (default: /root/reference)
 """
@@ -56,7 +61,9 @@ HELPER_RANGES = [
     (1535, 1569, "// Thread-local overload: reads v_cov3d", "}"),  # scale_rot_to_cov3d_vjp (thread)
     (1836, 1858, "// Adam update helper", "};"),           # adam_update_element, SHAdamParams
     (2248, 2276, "inline uint next_pow2(uint x) {", "}"),  # pad_count, make_sort_key, gaussian_is_active
-    (3376, 3380, "constant float GAUSS_1D[11] = {", "};"),
+    (906, 929, "inline int warp_reduce_all_max(", "}"),   # SIMD-group reductions
+    (2771, 2774, "#define SSIM_WIN 11", "#define SSIM_C2 0.0009f"),
+    (3376, 3382, "constant float GAUSS_1D[11] = {", "#define SSIM_TG 16   // threadgroup dimension (16×16 = 256 threads)"),
     (3862, 3870, "static inline uint pcg_hash32(", "}"),
 ]
 
@@ -80,6 +87,22 @@ KERNELS = {
                           "idx"],
     "mcmc_reg_grad_kernel": ["opacities", "scales", "v_opacity", "v_scale", "N", "op_reg", "sc_reg", "radii",
                              "invis_scale", "v_dc_sq", "idx"],
+    "count_intersections_kernel": ["xys", "radii", "depths", "tile_bounds", "tile_counts", "num_points", "aabb", "gid"],
+    "scatter_intersections_kernel": ["xys", "depths", "radii", "tile_bounds", "sort_offsets", "tile_write_counters",
+                                     "isect_keys_unsorted", "num_points", "aabb", "capacity", "tile_range", "gid"],
+    "nd_rasterize_forward_kernel": ["tile_bounds", "img_size", "channels", "tile_bins", "packed_xy_opac",
+                                    "packed_conic", "packed_rgb", "final_Ts", "final_index", "out_img", "background",
+                                    "blockDim", "tile_range", "blockIdx", "threadIdx", "tr"],
+    "rasterize_backward_kernel": ["tile_bounds", "img_size", "gaussian_ids_sorted", "tile_bins", "packed_xy_opac",
+                                  "packed_conic", "packed_rgb", "background", "final_Ts", "final_index", "v_output",
+                                  "v_xy", "v_conic", "v_rgb", "v_opacity", "tile_range", "gp", "blockIdx", "tr",
+                                  "warp_size", "wr"],
+    "ssim_h_fwd_kernel": ["rendered", "gt", "img_size", "ssim_h_buf", "gid", "lid", "tr", "tgid"],
+    "ssim_fused_v_fwd_h_bwd_kernel": ["rendered", "gt", "ssim_h_buf", "img_size", "ssim_weight", "inv_n",
+                                      "deriv_h_buf", "loss_sum", "nan_counts", "mask", "has_mask", "gid", "lid", "tr",
+                                      "tgid", "tg_size"],
+    "ssim_v_bwd_kernel": ["rendered", "gt", "ssim_h_buf", "img_size", "ssim_weight", "inv_n", "v_rendered",
+                          "nan_counts", "mask", "has_mask", "gid", "lid", "tr", "tgid"],
 }
 
 
@@ -124,8 +147,8 @@ def build(reference: str, quiet: bool = False) -> str:
         with open(os.path.join(OUT, f"k_{name}.inc"), "w") as f:
             f.write(body)
     cxx = shutil.which("g++") or "c++"
-    cmd = [cxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
-           "-Wno-unknown-pragmas", "-I", HERE, "-I", OUT, os.path.join(HERE, "ref_kernels.cpp"), "-o", LIB]
+    cmd = [cxx, "-O2", "-std=c++20", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
+           "-Wno-unknown-pragmas", "-pthread", "-I", HERE, "-I", OUT, os.path.join(HERE, "ref_kernels.cpp"), "-o", LIB]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise SystemExit(f"compile failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

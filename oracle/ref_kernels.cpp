@@ -11,12 +11,16 @@
 // barriers, and each thread writes only its own elements.
 #include "metal_shim.h"
 
-#include <type_traits>
-#include <vector>
-
 namespace mshim {
 ExpFn g_expf = nullptr;
+GroupState *g_group = nullptr;
+thread_local int t_lane = 0, t_sg = 0;
+thread_local unsigned t_simd_op = 0;
+std::mutex &atomic_lock() {
+    static std::mutex m;
+    return m;
 }
+}  // namespace mshim
 
 #include "ref_helpers.inc"
 
@@ -62,6 +66,91 @@ void k_sgld(float *means, float *scales, float *quats, float *opacities, float *
 void k_reg(const float *opacities, const float *scales, float *v_opacity, float *v_scale, int &N, float &op_reg,
            float &sc_reg, const int *radii, float &invis_scale, const float *v_dc_sq, uint idx) {
 #include "k_mcmc_reg_grad_kernel.inc"
+}
+
+// count_intersections_kernel (msplat_metal.metal:2342-2365)
+void k_count(float *xys, int *radii, float *depths, uint3 &tile_bounds, atomic_uint *tile_counts, uint &num_points,
+             float *aabb, uint gid) {
+#include "k_count_intersections_kernel.inc"
+}
+
+// scatter_intersections_kernel (msplat_metal.metal:2440-2480)
+void k_scatter(float *xys, float *depths, int *radii, uint3 &tile_bounds, uint *sort_offsets,
+               atomic_uint *tile_write_counters, uint64_t *isect_keys_unsorted, uint &num_points, float *aabb,
+               uint &capacity, uint2 &tile_range, uint gid) {
+#include "k_scatter_intersections_kernel.inc"
+}
+
+// Kernels below keep per-threadgroup arrays: `threadgroup` storage becomes a
+// function static, shared by the host threads of the group being run.
+#undef threadgroup
+#define threadgroup static
+
+// nd_rasterize_forward_kernel (msplat_metal.metal:499-618)
+void k_raster_fwd(uint3 &tile_bounds, uint3 &img_size, uint &channels, int *tile_bins, float *packed_xy_opac,
+                  float *packed_conic, float *packed_rgb, float *final_Ts, int *final_index, float *out_img,
+                  float *background, uint2 &blockDim, uint2 &tile_range, uint2 blockIdx, uint2 threadIdx, uint tr) {
+#include "k_nd_rasterize_forward_kernel.inc"
+}
+
+// rasterize_backward_kernel (msplat_metal.metal:931-1135)
+void k_raster_bwd(uint3 &tile_bounds, uint2 &img_size, int32_t *gaussian_ids_sorted, int *tile_bins,
+                  float *packed_xy_opac, float *packed_conic, float *packed_rgb, float *background, float *final_Ts,
+                  int *final_index, float *v_output, atomic_float *v_xy, atomic_float *v_conic, atomic_float *v_rgb,
+                  atomic_float *v_opacity, uint2 &tile_range, uint3 gp, uint3 blockIdx, uint tr, uint warp_size,
+                  uint wr) {
+#include "k_rasterize_backward_kernel.inc"
+}
+
+// ssim_h_fwd_kernel (msplat_metal.metal:3388-3450)
+void k_ssim_h_fwd(float *rendered, uchar *gt, uint2 &img_size, float *ssim_h_buf, uint2 gid, uint2 lid, uint tr,
+                  uint2 tgid) {
+#include "k_ssim_h_fwd_kernel.inc"
+}
+
+// ssim_fused_v_fwd_h_bwd_kernel (msplat_metal.metal:3563-3681)
+void k_ssim_fused(float *rendered, uchar *gt, float *ssim_h_buf, uint2 &img_size, float &ssim_weight, float &inv_n,
+                  float *deriv_h_buf, atomic_float *loss_sum, atomic_uint *nan_counts, uchar *mask, int &has_mask,
+                  uint2 gid, uint2 lid, uint tr, uint2 tgid, uint2 tg_size) {
+#include "k_ssim_fused_v_fwd_h_bwd_kernel.inc"
+}
+
+// ssim_v_bwd_kernel (msplat_metal.metal:3764-3850)
+void k_ssim_v_bwd(float *rendered, uchar *gt, float *ssim_h_buf, uint2 &img_size, float &ssim_weight, float &inv_n,
+                  float *v_rendered, atomic_uint *nan_counts, uchar *mask, int &has_mask, uint2 gid, uint2 lid,
+                  uint tr, uint2 tgid) {
+#include "k_ssim_v_bwd_kernel.inc"
+}
+
+#undef threadgroup
+#define threadgroup
+
+// Runs a grid of gx x gy threadgroups of bx x by threads: one host thread
+// per GPU thread, the groups one after another, a barrier between groups.
+// body(group x, group y, thread x, thread y, thread index).
+template <class F> void run_groups(int gx, int gy, int bx, int by, F body) {
+    const int T = bx * by;
+    mshim::GroupState gs;
+    gs.bar.n = T;
+    for (auto &sg : gs.sg) sg.bar.n = 32;
+    mshim::g_group = &gs;
+    mshim::HostBarrier end;
+    end.n = T;
+    std::vector<mshim::HostThread> threads;
+    threads.reserve(T);
+    for (int t = 0; t < T; t++)
+        threads.emplace_back([&, t]() {
+            mshim::t_lane = t % 32;
+            mshim::t_sg = t / 32;
+            mshim::t_simd_op = 0;
+            for (int y = 0; y < gy; y++)
+                for (int x = 0; x < gx; x++) {
+                    body(x, y, t % bx, t / bx, t);
+                    end.wait();
+                }
+        });
+    for (auto &th : threads) th.join();
+    mshim::g_group = nullptr;
 }
 
 template <class T> T *mut(const T *p) { return const_cast<T *>(p); }
@@ -177,6 +266,123 @@ void ref_sort_keys(int n, const int *radii, const float *depths, uint8_t *active
 // pad_count of each count.
 void ref_pad_count(int n, const uint32_t *c, uint32_t *out) {
     for (int i = 0; i < n; i++) out[i] = pad_count(c[i]);
+}
+
+// The pixel stages of one monolithic training step of one view, as the
+// reference runs them (msplat_metal.mm:1255-1400): count and scatter of the
+// tile intersections (compiled kernels), the per-tile sort and pack
+// (restated: hybrid_sort_pack_kernel sorts each tile's keys ascending and
+// packs (x, y, sigmoid(opacity)), conic and raw colour by id, a non-finite
+// record packed as zeros, msplat_metal.metal:2562-2582), the forward
+// rasterizer, the three SSIM + L1 kernels when gt is given (else v_rendered
+// is an input) and the backward rasterizer (compiled kernels).
+// Capacity: ids/packing sized by the exact count; returns the intersection
+// count, or -1 when more than ids_capacity.
+long long ref_raster_step(int n, const float *xys, const float *depths, const int *radii, const float *conics,
+                          const float *colors, const float *aabb, const float *opacities, int width, int height,
+                          const float background[3], const uint8_t *gt, const uint8_t *mask, float ssim_weight,
+                          float loss_inv_n, int *tile_bins_out, int *gaussian_ids, long long ids_capacity,
+                          float *out_img, float *final_Ts, int *final_idx, float *loss_sum, float *v_rendered,
+                          float *v_xy, float *v_conic, float *v_colors, float *v_opacity, uint32_t nan_counts[16]) {
+    const uint W = (uint)width, H = (uint)height;
+    uint3 tile_bounds((W + 15) / 16, (H + 15) / 16, 1u);
+    const uint T = tile_bounds.x * tile_bounds.y;
+    uint np = (uint)n;
+    // count_intersections_kernel
+    std::vector<uint> counts(T, 0u);
+    for (uint i = 0; i < np; i++)
+        k_count(mut(xys), mut(radii), mut(depths), tile_bounds, counts.data(), np, mut(aabb), i);
+    // prefix_sum_tiles_kernel: padded offsets for the sort buckets, exact ones for the lists
+    std::vector<uint> sort_off(T + 1, 0u), exact(T + 1, 0u);
+    for (uint t = 0; t < T; t++) {
+        sort_off[t + 1] = sort_off[t] + pad_count(counts[t]);
+        exact[t + 1] = exact[t] + counts[t];
+    }
+    const long long M = exact[T];
+    if (M > ids_capacity) return -1;
+    // scatter_intersections_kernel (one tile group covering every tile)
+    uint cap = sort_off[T];
+    std::vector<uint64_t> keys(std::max<uint>(cap, 1u), ~0ull);
+    std::vector<uint> wc(T, 0u);
+    uint2 all(0u, T);
+    for (uint i = 0; i < np; i++)
+        k_scatter(mut(xys), mut(depths), mut(radii), tile_bounds, sort_off.data(), wc.data(), keys.data(), np,
+                  mut(aabb), cap, all, i);
+    // sort + pack (restated)
+    std::vector<float> pk_xyo(3 * (size_t)std::max<long long>(M, 1)), pk_con(pk_xyo.size()), pk_rgb(pk_xyo.size());
+    std::vector<int> bins(2 * (size_t)T);
+    for (uint t = 0; t < T; t++) {
+        std::sort(keys.begin() + sort_off[t], keys.begin() + sort_off[t] + counts[t]);
+        bins[2 * t] = (int)exact[t];
+        bins[2 * t + 1] = (int)exact[t + 1];
+        for (uint j = 0; j < counts[t]; j++) {
+            const uint gidx = (uint)(keys[sort_off[t] + j] & 0xFFFFFFFFu);
+            const size_t d = exact[t] + j;
+            gaussian_ids[d] = (int)gidx;
+            const float2 xy(xys[2 * gidx], xys[2 * gidx + 1]);
+            const float opac = 1.f / (1.f + exp(-opacities[gidx]));
+            const float3 conic(conics[3 * gidx], conics[3 * gidx + 1], conics[3 * gidx + 2]);
+            const float3 rgb(colors[3 * gidx], colors[3 * gidx + 1], colors[3 * gidx + 2]);
+            const bool ok = finite_bits(xy.x) && finite_bits(xy.y) && finite_bits(opac) && finite_bits3(conic) &&
+                            finite_bits3(rgb);
+            if (!ok) {
+                nan_counts[13]++;
+                if (!finite_bits(opac)) nan_counts[14]++;
+            }
+            const float3 a = ok ? float3(xy.x, xy.y, opac) : float3(0.f), b = ok ? conic : float3(0.f),
+                         c = ok ? rgb : float3(0.f);
+            pk_xyo[3 * d] = a.x; pk_xyo[3 * d + 1] = a.y; pk_xyo[3 * d + 2] = a.z;
+            pk_con[3 * d] = b.x; pk_con[3 * d + 1] = b.y; pk_con[3 * d + 2] = b.z;
+            pk_rgb[3 * d] = c.x; pk_rgb[3 * d + 1] = c.y; pk_rgb[3 * d + 2] = c.z;
+        }
+    }
+    if (tile_bins_out) std::copy(bins.begin(), bins.end(), tile_bins_out);
+    // forward rasterizer: 8x8 threadgroups
+    uint3 img3(W, H, 1u);
+    uint channels = 3;
+    uint2 block(8u, 8u);
+    float bg[3] = {background[0], background[1], background[2]};
+    const int gx = (int)((W + 7) / 8), gy = (int)((H + 7) / 8);
+    run_groups(gx, gy, 8, 8, [&](int bx, int by, int tx, int ty, int t) {
+        k_raster_fwd(tile_bounds, img3, channels, bins.data(), pk_xyo.data(), pk_con.data(), pk_rgb.data(), final_Ts,
+                     final_idx, out_img, bg, block, all, uint2((uint)bx, (uint)by), uint2((uint)tx, (uint)ty),
+                     (uint)t);
+    });
+    uint2 isz(W, H);
+    if (gt) {
+        // the loss: three kernels over 16x16 threadgroups
+        std::vector<float> hbuf((size_t)W * H * 15, 0.f), dbuf((size_t)W * H * 15, 0.f);
+        float sw = ssim_weight, invn = loss_inv_n;
+        int has_mask = mask ? 1 : 0;
+        uchar *gt8 = mut(gt), *m8 = mut(mask);
+        *loss_sum = 0.f;
+        const int sx = (int)((W + 15) / 16), sy = (int)((H + 15) / 16);
+        run_groups(sx, sy, 16, 16, [&](int bx, int by, int tx, int ty, int t) {
+            k_ssim_h_fwd(out_img, gt8, isz, hbuf.data(), uint2(bx * 16 + tx, by * 16 + ty), uint2(tx, ty), t,
+                         uint2(bx, by));
+        });
+        run_groups(sx, sy, 16, 16, [&](int bx, int by, int tx, int ty, int t) {
+            k_ssim_fused(out_img, gt8, hbuf.data(), isz, sw, invn, dbuf.data(), loss_sum, nan_counts, m8, has_mask,
+                         uint2(bx * 16 + tx, by * 16 + ty), uint2(tx, ty), t, uint2(bx, by), uint2(16u, 16u));
+        });
+        run_groups(sx, sy, 16, 16, [&](int bx, int by, int tx, int ty, int t) {
+            k_ssim_v_bwd(out_img, gt8, dbuf.data(), isz, sw, invn, v_rendered, nan_counts, m8, has_mask,
+                         uint2(bx * 16 + tx, by * 16 + ty), uint2(tx, ty), t, uint2(bx, by));
+        });
+    }
+    // backward rasterizer: 8x8 threadgroups of two SIMD groups
+    std::fill(v_xy, v_xy + 2 * (size_t)n, 0.f);
+    std::fill(v_conic, v_conic + 3 * (size_t)n, 0.f);
+    std::fill(v_colors, v_colors + 3 * (size_t)n, 0.f);
+    std::fill(v_opacity, v_opacity + (size_t)n, 0.f);
+    std::vector<int> gids(gaussian_ids, gaussian_ids + M);
+    run_groups(gx, gy, 8, 8, [&](int bx, int by, int tx, int ty, int t) {
+        k_raster_bwd(tile_bounds, isz, gids.data(), bins.data(), pk_xyo.data(), pk_con.data(), pk_rgb.data(), bg,
+                     final_Ts, final_idx, v_rendered, v_xy, v_conic, v_colors, v_opacity, all,
+                     uint3((uint)(bx * 8 + tx), (uint)(by * 8 + ty), 0u), uint3((uint)bx, (uint)by, 0u), (uint)t, 32u,
+                     (uint)(t % 32));
+    });
+    return M;
 }
 
 // The SSIM window table.

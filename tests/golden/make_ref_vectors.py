@@ -2,9 +2,12 @@
 """Writes tests/golden/ref_vectors.npz: inputs and outputs of the reference's
 own per-Gaussian Metal code (projection + SH, projection backward + SH Adam,
 regularizer, Adam, SGLD), compiled as host C++ by oracle/ref_build.py from the
-reference tree, on 512 random Gaussians at step 3001 — the vectors
-tests/test_ref_pin.py::test_golden_vectors holds the oracle to where the
-reference tree is absent.  Needs the reference tree (default /root/reference,
+reference tree, on 512 random Gaussians at step 3001; and
+tests/golden/ref_pixel_vectors.npz: the outputs of its pixel stages (tile
+lists, forward rasterizer, SSIM + L1 loss, backward rasterizer) on the small
+views of tests/test_ref_pin.py (their inputs are regenerated from seeds) —
+the vectors tests/test_ref_pin.py holds the oracle to where the reference
+tree is absent.  Needs the reference tree (default /root/reference,
 or MSPLAT_REFERENCE).
 
 Usage: python tests/golden/make_ref_vectors.py
@@ -22,7 +25,7 @@ sys.path.insert(0, os.path.dirname(HERE))
 
 from msplat_gb300.schedule import GROUPS, step_scalars  # noqa: E402
 from oracle import oracle as O, ref as R  # noqa: E402
-from test_ref_pin import FWD_KEYS, random_inputs, ref_run, ring_camera  # noqa: E402
+from test_ref_pin import FWD_KEYS, PIXEL_CASES, pixel_case, random_inputs, ref_run, ring_camera  # noqa: E402
 
 
 def main():
@@ -46,6 +49,20 @@ def main():
         out["bwd_" + k] = bwd[k]
     path = os.path.join(HERE, "ref_vectors.npz")
     np.savez_compressed(path, **out)
+    print(path, os.path.getsize(path), "bytes")
+
+    # the pixel stages (tile lists, rasterizers, loss) of small views
+    pix = {}
+    for name in PIXEL_CASES:
+        cam, g, gt, mask, bg = pixel_case(name)
+        st = step_scalars(3001, 3001, width=cam["width"], height=cam["height"])
+        fwd = R.project_fwd(g, cam, 3)
+        o = R.raster_step(fwd, g.opacities, cam, gt=gt, mask=mask, background=bg, loss_inv_n=st["loss_inv_n"])
+        for k in ("num_isect", "gaussian_ids", "tile_bins", "out_img", "final_Ts", "final_idx", "loss", "v_rendered",
+                  "v_xy", "v_conic", "v_colors", "v_opacity"):
+            pix[f"{name}/{k}"] = np.asarray(o[k])
+    path = os.path.join(HERE, "ref_pixel_vectors.npz")
+    np.savez_compressed(path, **pix)
     print(path, os.path.getsize(path), "bytes")
 
 

@@ -1,22 +1,32 @@
 """The oracle pinned to the reference's own source (CPU).
 
-oracle/ref_build.py compiles the reference's per-Gaussian Metal code —
-helper functions and the bodies of project_and_sh_forward_kernel,
-project_and_sh_backward_kernel (with its fused SH Adam), fused_adam_kernel,
-sgld_noise_gen/sgld_noise_kernel and mcmc_reg_grad_kernel — unchanged as host
-C++ (oracle/_ref, built from the reference tree).  Its outputs must equal the
-oracle's float path bit for bit: projection (centres, depths, radii, conics,
-tiles hit, colours, extents), the tile rectangles, the sort keys and active
-test that order every per-tile list, the SSIM window, and, from the same
-rasterizer gradients, the projection VJPs, the SH Adam, regularizer, Adam and
-SGLD updates of every parameter and moment.  exp() is the same function on
-both sides (the oracle's det_expf; Metal's exp has no published bits).
+oracle/ref_build.py compiles the reference's Metal code unchanged as host C++
+(oracle/_ref, built from the reference tree): the per-Gaussian helpers and
+the bodies of project_and_sh_forward_kernel, project_and_sh_backward_kernel
+(with its fused SH Adam), fused_adam_kernel, sgld_noise_gen/sgld_noise_kernel,
+mcmc_reg_grad_kernel, count_intersections_kernel and
+scatter_intersections_kernel, and - threadgroups run on host threads - the
+forward rasterizer, the three SSIM + L1 kernels and the backward rasterizer.
+
+Per-Gaussian stages, bit for bit against the oracle's float path: projection
+(centres, depths, radii, conics, tiles hit, colours, extents), the tile
+rectangles, sort keys and active test that order every per-tile list, the
+SSIM window, and, from the same rasterizer gradients, the projection VJPs,
+the SH Adam, regularizer, Adam and SGLD updates of every parameter and moment.
+Pixel stages: per-tile lists, image, final transmittance, last contributors
+and dL/dimage bit for bit, the loss within 1e-6 and the rasterizer gradients
+within 1e-6 (the reference sums them with atomics), the whole step's updates
+within 1e-5.  exp() is the same function on both sides (the oracle's
+det_expf; Metal's exp has no published bits).
 
 Two parts:
   * live, on 100,000 random Gaussians (with culled, degenerate, non-finite and
-    extreme ones), where the reference tree exists (the build container);
-  * against the committed vectors tests/golden/ref_vectors.npz, made by
-    tests/golden/make_ref_vectors.py from the same library, everywhere.
+    extreme ones) and small views with several splat batches per tile, partial
+    edge tiles, a mask and a background, where the reference tree exists (the
+    build container);
+  * against the committed vectors tests/golden/ref_vectors.npz and
+    ref_pixel_vectors.npz, made by tests/golden/make_ref_vectors.py from the
+    same library, everywhere.
 """
 import ctypes
 import os
@@ -172,3 +182,84 @@ def test_golden_vectors():
     mom_r = ([z["out_m_" + k] for k in GROUPS], [z["out_v_" + k] for k in GROUPS])
     compare(r, g_o, mom_o, fwd, bwd, g_r, mom_r)
     assert np.array_equal(O.gauss_1d(), z["gauss_1d"])
+
+
+PIXEL_CASES = {
+    # width, height, Gaussians, seed, mask, background
+    "plain": (48, 32, 300, 3, False, (0.0, 0.0, 0.0)),
+    "ragged_mask_bg": (50, 34, 350, 4, True, (0.25, 0.5, 0.75)),
+}
+
+
+def pixel_case(name):
+    """A small view (several 64-splat batches per tile), its target and
+    optional mask; the Gaussians include a NaN colour (zombie gate)."""
+    W, H, n, seed, with_mask, bg = PIXEL_CASES[name]
+    cam = ring_camera(W, H, 0.8 * W, k=2)
+    g = S.gaussians(n, seed)
+    g.features_dc[7] = np.nan
+    rng = np.random.default_rng(seed)
+    gt = rng.integers(0, 256, (H, W, 3), dtype=np.uint8)
+    mask = None
+    if with_mask:
+        mask = np.full((H, W), 255, np.uint8)
+        mask[5:15, 10:30] = 0
+        mask[H - 6:, W - 9:] = 0
+    return cam, g, gt, mask, bg
+
+
+def check_pixel_path(r, o):
+    """The oracle's float path (r) against the reference kernels' pixel stages (o)."""
+    assert r["num_isect"] == o["num_isect"]
+    assert np.array_equal(r["gaussian_ids"], o["gaussian_ids"])
+    assert np.array_equal(r["tile_bins"], o["tile_bins"])
+    for k in ("out_img", "final_Ts", "final_idx", "v_rendered"):
+        assert np.array_equal(r[k], o[k]), k
+    assert abs(r["loss"] - o["loss"]) <= 1e-6 * abs(r["loss"])
+    for k in ("v_xy", "v_conic", "v_colors", "v_opacity"):
+        e = np.linalg.norm((r[k] - o[k]).ravel()) / np.linalg.norm(o[k].ravel())
+        assert e <= 1e-6, (k, e)
+
+
+@needs_reference
+@pytest.mark.parametrize("name", list(PIXEL_CASES))
+def test_live_pixel_path(ref_lib, name):
+    """Tile lists, forward rasterizer, SSIM + L1 loss and backward rasterizer
+    of the reference (threadgroups on host threads) against the oracle's
+    float path: lists, image, transmittance, last contributors and dL/dimage
+    identical, loss within 1e-6, rasterizer gradients within 1e-6 (the
+    reference adds them with atomics in no fixed order); then the whole
+    step's updates from the reference's per-Gaussian kernels within 1e-5."""
+    cam, g, gt, mask, bg = pixel_case(name)
+    step = step_scalars(3001, 3001, width=cam["width"], height=cam["height"])
+    mom = ([np.zeros_like(a) for a in g.arrays()], [np.zeros_like(a) for a in g.arrays()])
+    g_o = g.copy()
+    mom_o = ([a.copy() for a in mom[0]], [a.copy() for a in mom[1]])
+    r = O.train_step(32, g_o, cam, step, moments=mom_o, gt=gt, mask=mask, background=bg, raster_mode=1,
+                     do_sgld=True)
+    fwd = ref_lib.project_fwd(g, cam, 3)
+    o = ref_lib.raster_step(fwd, g.opacities, cam, gt=gt, mask=mask, background=bg,
+                            loss_inv_n=step["loss_inv_n"])
+    assert int(np.diff(o["tile_bins"], axis=1).max()) > 128
+    check_pixel_path(r, o)
+    g_r = g.copy()
+    ref_lib.step_after_raster(g_r, mom, cam, step, o["raster_grads"], fwd)
+    for name_, a, b, before in zip(GROUPS, g_o.arrays(), g_r.arrays(), g.arrays()):
+        fin = np.isfinite(before)
+        e = np.linalg.norm((a - b)[fin]) / max(np.linalg.norm((b - before)[fin]), 1e-30)
+        assert e <= 1e-5, (name_, e)
+
+
+def test_golden_pixel_vectors():
+    """The oracle's pixel stages against the reference kernels' outputs stored
+    in tests/golden/ref_pixel_vectors.npz (no reference tree needed)."""
+    z = np.load(os.path.join(os.path.dirname(GOLDEN), "ref_pixel_vectors.npz"))
+    for name in PIXEL_CASES:
+        cam, g, gt, mask, bg = pixel_case(name)
+        step = step_scalars(3001, 3001, width=cam["width"], height=cam["height"])
+        r = O.train_step(32, g.copy(), cam, step, gt=gt, mask=mask, background=bg, raster_mode=1,
+                         do_optimizer=False)
+        o = {k[len(name) + 1:]: z[k] for k in z.files if k.startswith(name + "/")}
+        o["num_isect"] = int(o["num_isect"])
+        o["loss"] = float(o["loss"])
+        check_pixel_path(r, o)
