@@ -63,6 +63,11 @@ float msplat_trainer_last_loss(MsplatTrainer t);
 /* The trainer's engine (for stats, timing and buffer inspection). */
 MsplatEngine *msplat_trainer_engine(MsplatTrainer t);
 
+/* The counts of the trainer's last MCMC relocation round (dead, culled,
+ * non-finite, relocated, grown, active; Model::mcmcAfterTrain's log line,
+ * core/src/model.cpp:566-636).  Returns the number of rounds run so far. */
+int msplat_trainer_mcmc_stats(MsplatTrainer t, MsplatMcmcStats *out);
+
 /* Tensor-core self-test (the MMA path of the learned relocation proposal):
  * D[128 x N] = A[128 x K] * B[N x K]^T for row-major BF16 A, B (host, as
  * uint16 bit patterns) into row-major F32 D (host), N, K in {16, 32, 64}, on

@@ -85,6 +85,7 @@ def _lib():
     L.msplat_trainer_last_loss.restype = C.c_float
     L.msplat_trainer_engine.argtypes = [vp]
     L.msplat_trainer_engine.restype = vp
+    L.msplat_trainer_mcmc_stats.argtypes = [vp, C.POINTER(N.MsplatMcmcStats)]
     L.msplat_viewer_create.argtypes = [cp, C.c_int, C.c_int, C.c_float]
     L.msplat_viewer_create.restype = vp
     L.msplat_viewer_render.argtypes = [vp, fp, C.POINTER(C.c_uint8)]
@@ -304,6 +305,20 @@ class GaussianTrainer:
         rounds = C.c_int()
         on = _lib().msplat_trainer_learned_stats(self.h, loss, C.byref(rounds))
         return {"enabled": on == 1, "last_loss": float(loss[0]), "rounds": rounds.value}
+
+    def mcmc_stats(self) -> dict:
+        """Counts of the last MCMC relocation round and the rounds run so far."""
+        st = N.MsplatMcmcStats()
+        rounds = _lib().msplat_trainer_mcmc_stats(self.h, C.byref(st))
+        d = {k: getattr(st, k) for k, _ in N.MsplatMcmcStats._fields_}
+        d["rounds"] = rounds
+        return d
+
+    def engine_nan_counts(self) -> np.ndarray:
+        """The engine's non-finite telemetry counters (grad_nan_counts slots)."""
+        s = N.MsplatEngineStats()
+        _lib().msplat_engine_stats(_lib().msplat_trainer_engine(self.h), C.byref(s))
+        return np.array(s.nan_counts[:], np.uint32)
 
     def load_ply(self, path: str) -> int:
         """Replace the Gaussians with a trained PLY (fresh optimizer); returns its iteration."""

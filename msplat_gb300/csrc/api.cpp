@@ -461,6 +461,11 @@ struct TrainerImpl {
     float last_loss = 0.f;
     int batch_views = 1;          // views per optimizer step (1 = the reference's one-camera step)
     float batch_lr_scale = 1.0f;  // learning-rate factor of multi-view steps
+    MsplatMcmcStats last_mcmc{};  // the last relocation round's counts
+    int mcmc_rounds = 0;
+    // MSPLAT_NAN_INJECT=<step>, read when the trainer is created (host-side
+    // fault injection of model.cpp:638-659; -1: off)
+    int nan_inject = -1;
 
     // a period boundary crossed between iterations prev (exclusive) and cur (inclusive)
     static bool crossed(int prev, int cur, int period) { return cur / period > prev / period; }
@@ -487,6 +492,7 @@ struct TrainerImpl {
     } lrn;
 
     TrainerImpl(DatasetImpl *d, const MsplatConfig &c) : cfg(c), ds(d) {
+        if (const char *e = std::getenv("MSPLAT_NAN_INJECT")) nan_inject = std::atoi(e);
         int dev = 0;
         CKA(cudaGetDevice(&dev));
         eng = msplat_engine_create(dev, std::max(1, cfg.capMax));
@@ -778,14 +784,11 @@ struct TrainerImpl {
             fprintf(stderr, "MCMC step=%d active=%d dead=%d culled=%d nonfinite=%d grown=%d\n", step, ms.num_active,
                    ms.num_dead, ms.num_culled, ms.num_nonfinite, ms.num_grown);
         if (ms.num_nonfinite > 0) fprintf(stderr, "MCMC nonfinite step=%d count=%d\n", step, ms.num_nonfinite);
+        last_mcmc = ms;
+        mcmc_rounds++;
         // MSPLAT_NAN_INJECT=<step>: poison features_dc of 100 Gaussians (host-side fault injection,
         // model.cpp:638-659)
-        static int inject = -2;
-        if (inject == -2) {
-            const char *e = std::getenv("MSPLAT_NAN_INJECT");
-            inject = e ? std::atoi(e) : -1;
-        }
-        if (inject > prev && inject <= step && model.n > 0) {
+        if (nan_inject > prev && nan_inject <= step && model.n > 0) {
             std::mt19937 r(1234);
             std::uniform_int_distribution<int> pick(0, model.n - 1);
             const float nan3[3] = {NAN, NAN, NAN};
@@ -1382,6 +1385,12 @@ float msplat_trainer_last_loss(MsplatTrainer t) {
 }
 
 MsplatEngine *msplat_trainer_engine(MsplatTrainer t) { return t ? TR(t)->eng : nullptr; }
+
+int msplat_trainer_mcmc_stats(MsplatTrainer t, MsplatMcmcStats *out) {
+    if (!t) return -1;
+    if (out) *out = TR(t)->last_mcmc;
+    return TR(t)->mcmc_rounds;
+}
 
 // ---- viewer ----
 

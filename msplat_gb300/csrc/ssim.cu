@@ -173,7 +173,8 @@ __global__ void __launch_bounds__(256, 2) k_ssim_fused(LossArgs a) {
         // A: (input column, 11 centre rows) per item; the 21 inputs and their
         // products in registers, moments in pairs (paired fp32 arithmetic).
         // The target stays in 0..255 here (exact in float); its moments are
-        // scaled by 1/255 and 1/255^2 at the end.
+        // scaled by 1/255 (mean, cross moment) and by 1/255 twice (second
+        // moment) at the end.
         for (int it = tid; it < kFIn * 4; it += 256) {
             const int ix = it % kFIn, s = it / kFIn;
             const int vy0 = 11 * s, n = min(11, kFF - vy0);
@@ -207,7 +208,10 @@ __global__ void __launch_bounds__(256, 2) k_ssim_fused(LossArgs a) {
                     float2 m23 = make_float2(0.f, 0.f);
 #pragma unroll
                     for (int d = 0; d < 11; d++) m23 = __ffma2_rn(make_float2(kGauss[d], kGauss[d]), gr[k + d], m23);
-                    sm.u.v.m23[vy0 + k][ix] = __fmul2_rn(m23, make_float2(1.0f / 65025.0f, 1.f));
+                    // scaled by 1/255 twice, as the mean is once: a single 1/65025 (one
+                    // ulp below (1/255)^2 in float) biased every variance low
+                    const float2 s255 = make_float2(1.0f / 255.0f, 1.f);
+                    sm.u.v.m23[vy0 + k][ix] = __fmul2_rn(__fmul2_rn(m23, s255), s255);
                 }
             }
         }

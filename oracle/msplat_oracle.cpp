@@ -942,7 +942,11 @@ template <class R> struct Step {
         raster_forward();
         const bool has_gt = in.gt != nullptr;
         if (has_gt) loss();
-        if (in.v_img_in) v_rend.assign(in.v_img_in, in.v_img_in + 3 * (size_t)P);
+        double dot = 0;
+        if (in.v_img_in) {
+            v_rend.assign(in.v_img_in, in.v_img_in + 3 * (size_t)P);
+            for (size_t k = 0; k < 3 * (size_t)P; k++) dot += (double)img[k] * (double)in.v_img_in[k];
+        }
         if (in.do_backward && (has_gt || in.v_img_in || in.raster_grads_in)) {
             if (in.raster_grads_in) {
                 v_xy.assign(2 * (size_t)N, 0); v_conic.assign(3 * (size_t)N, 0);
@@ -979,6 +983,7 @@ template <class R> struct Step {
         for (int k = 0; k < 16; k++) out->nan_counts[k] = nan[k];
         out->k_max_used = K;
         out->pairs_fwd = pairs_fwd; out->pairs_bwd = pairs_bwd;
+        out->img_dot_v = dot;
         return 0;
     }
 };

@@ -98,6 +98,8 @@ typedef struct {
     uint32_t nan_counts[16];
     int k_max_used;        /* 1 = monolithic */
     long long pairs_fwd, pairs_bwd;  /* (pixel, splat) evaluations executed */
+    double img_dot_v;     /* sum of image * v_img_in at the step's precision (the linear
+                             loss whose gradient the backward of v_img_in is) */
 } OrStepOut;
 
 /* One training step (prec = 32 or 64).  Returns 0 on success. */

@@ -58,7 +58,7 @@ class OrStepOut(C.Structure):
         ("v_xy", FP), ("v_conic", FP), ("v_colors", FP), ("v_opacity", FP),
         ("v_mean3d", FP), ("v_scale", FP), ("v_quat", FP),
         ("nan_counts", C.c_uint32 * 16), ("k_max_used", C.c_int),
-        ("pairs_fwd", C.c_longlong), ("pairs_bwd", C.c_longlong),
+        ("pairs_fwd", C.c_longlong), ("pairs_bwd", C.c_longlong), ("img_dot_v", C.c_double),
     ]
 
 
@@ -257,6 +257,7 @@ def train_step(prec: int, g, cam, step, *, moments=None, gt=None, mask=None, bac
     o["nan_counts"] = np.array(out.nan_counts[:], np.uint32)
     o["k_max"] = int(out.k_max_used)
     o["pairs_fwd"], o["pairs_bwd"] = int(out.pairs_fwd), int(out.pairs_bwd)
+    o["img_dot_v"] = float(out.img_dot_v)
     o["moments"] = moments
     return o
 

@@ -1,7 +1,15 @@
 """The torch.autograd binding (msplat_gb300.autograd.rasterize) on a
-512-Gaussian 64x64 view: its gradients against the oracle's analytic
-gradients (FP32 path and FP64) for an arbitrary image gradient, and against
-FP64 central differences (h = 1e-4) of the oracle's forward (GPU only)."""
+512-Gaussian 64x64 view (GPU only).
+
+The chain of checks: the engine's gradients equal the oracle's analytic
+gradients (float path within 1e-4, FP64 within 1e-5) for an arbitrary image
+gradient; the oracle's FP64 analytic gradient without the sigma/alpha
+cutoffs equals central differences of its forward along directions that
+move every visible Gaussian at once within 1e-6
+(tests/test_oracle.py::test_fp64_gradients_directional_fd, CPU).  The last
+test here compares the engine (with the cutoffs) with differences of the
+cutoff-free forward per Gaussian: what separates them is the part of the
+gradient the reference's cutoffs drop."""
 import numpy as np
 import pytest
 
@@ -49,7 +57,7 @@ def _oracle(prec, g, cd, W, deg=3, bg=(0.1, 0.2, 0.3), no_cutoff=False):
 def test_autograd_matches_oracle(scene):
     torch, g, cd, W = scene
     img, (gm, gs, gq, gdc, grest, gop) = _engine_grads(torch, g, cd, W)
-    for prec, tol in ((32, 1e-4), (64, 1e-3)):
+    for prec, tol in ((32, 1e-4), (64, 1e-5)):   # measured ~4e-7 and ~2e-6 on GB300
         r = _oracle(prec, g, cd, W)
         if prec == 32:
             assert np.max(np.abs(img - r["out_img"])) <= 1e-5

@@ -142,3 +142,63 @@ def test_mcmc_nothing_dead_grows_only():
     assert stats.num_dead == 0 and stats.num_relocated == 0
     assert stats.num_grown == 100 and dg.n == n + 100     # capped at cap_max
     assert rc == 1
+
+
+def _mix32(seed, idx):
+    """The engine's counter hash (PCG output step on seed*747796405 + idx*2891336453), vectorised."""
+    x = (np.uint64(seed) * np.uint64(747796405) + idx.astype(np.uint64) * np.uint64(2891336453)) & np.uint64(0xFFFFFFFF)
+    x = (((x >> ((x >> np.uint64(28)) + np.uint64(4))) ^ x) * np.uint64(277803737)) & np.uint64(0xFFFFFFFF)
+    return (x >> np.uint64(22)) ^ x
+
+
+def _unit53(seed, j):
+    hi = _mix32(seed, 2 * j)
+    lo = _mix32(seed ^ 0x85EBCA6B, 2 * j + 1)
+    bits = ((hi << np.uint64(32)) | lo) >> np.uint64(11)
+    return bits.astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+def test_mcmc_draws_exact_and_64_levels():
+    """Every relocation draw equals the first index whose cumulative weight
+    exceeds u * total, u the 53-bit counter-based uniform of that draw (an
+    exact restatement on the device's own cumulative weights: no off-by-one
+    at bucket edges); the weights are the living Gaussians' sigmoid(opacity)
+    and the cumulative weights their running sum; and the sources of 16,384
+    draws over 64 graded opacity levels pass a 63-dof chi-square test."""
+    n = 32768
+    g = S.gaussians(n, seed=6, sh_rest_bases=0)
+    levels = np.linspace(0.02, 0.98, 64).astype(np.float32)
+    op = g.opacities.reshape(-1)
+    alive = np.arange(n) % 2 == 0
+    lv = (np.arange(n) // 2) % 64
+    op[~alive] = -9.0
+    op[alive] = np.log(levels[lv[alive]] / (1 - levels[lv[alive]]))
+    g.means[:] = np.clip(g.means, -1, 1)
+    dg = E.DeviceGaussians(g, cap=n)
+    eng = E.Engine(0, n)
+    stats, rc = eng.mcmc(dg, 0.0, 0)
+    assert stats.num_dead == n // 2 and stats.num_relocated == n // 2 and stats.num_grown == 0
+    moves = eng.read("mcmc_moves", np.int32, 2 * stats.num_relocated).reshape(-1, 2)
+    w = eng.read("mcmc_weights", np.float64, n)
+    cumw = eng.read("mcmc_cumw", np.float64, n)
+    eng.close()
+    sig = (1.0 / (1.0 + np.exp(-op.astype(np.float64)))).astype(np.float32)
+    ref_w = np.where(alive, sig, 0.0)
+    np.testing.assert_allclose(w, ref_w, rtol=3e-7, atol=0)
+    np.testing.assert_allclose(cumw, np.cumsum(w), rtol=1e-12, atol=0)
+    seed = 0x9E3779B9 ^ 1                      # the first relocation round of a run
+    j = np.arange(stats.num_relocated, dtype=np.uint64)
+    target = _unit53(seed, j) * cumw[-1]
+    expect = np.searchsorted(cumw, target, side="right")
+    assert np.array_equal(moves[:, 1], expect)
+    src = moves[:, 1]
+    assert alive[src].all()
+    obs = np.bincount(lv[src], minlength=64).astype(np.float64)
+    exp = levels / levels.sum() * len(src)
+    chi2 = float(((obs - exp) ** 2 / exp).sum())
+    try:
+        from scipy.stats import chi2 as C2
+        bar = float(C2.isf(1e-6, 63))
+    except ImportError:   # the 1e-6 tail of 63 dof
+        bar = 131.4
+    assert chi2 < bar, (chi2, bar)

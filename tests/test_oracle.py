@@ -190,3 +190,119 @@ def test_mlp_oracle_bf16_rounding():
     r = M.bf16(x)
     assert r[0] == 1.0 and r[1] == 1.0 and r[2] == 1.0078125   # ties to even; 1 + 1.5 ulp rounds up
     assert abs(r[3] + 3.140625) < 1e-6 and r[4] == 0.0
+
+
+def _fd_scene(n=512, seed=3, size=64):
+    """The autograd test's scene: 512 Gaussians at a 64x64 view, opacity 0.73
+    (alpha below the 0.999 clamp), dim colours (no saturate clamp)."""
+    gt = S.gaussians(n, seed=seed)
+    g = S.init_from_gt(gt, seed)
+    g.opacities[:] = 1.0
+    rng = np.random.default_rng(11)
+    g.features_dc[:] = rng.uniform(-0.5, 0.3, g.features_dc.shape).astype(np.float32)
+    g.features_rest *= np.float32(0.1)
+    g.scales += rng.normal(0.0, 0.3, g.scales.shape).astype(np.float32)   # anisotropic: the rotation matters
+    cam = S.ring_cameras(4, size, size, 51.25 * size / 64)[1]
+    vm, pm, cp = O.prepare_cam(cam.cam_to_world, cam.width, cam.height, cam.fx, cam.fy)
+    cd = dict(viewmat=vm, projmat=pm, cam_pos=cp, fx=cam.fx, fy=cam.fy, cx=cam.cx, cy=cam.cy, width=size,
+              height=size)
+    w = rng.normal(0.0, 1.0, (size, size, 3)).astype(np.float32)
+    return g, cd, w
+
+
+def _tile_rects(o, cd):
+    f = np.float32
+    tx, ty = (cd["width"] + 15) // 16, (cd["height"] + 15) // 16
+
+    def conv(v, hi):
+        return np.clip(np.trunc(np.clip(np.where(np.isfinite(v), v, 0), -2e9, 2e9)).astype(np.int64), 0, hi)
+    cx, cy = o["xys"][:, 0] / f(16), o["xys"][:, 1] / f(16)
+    rx, ry = o["aabb"][:, 0] / f(16), o["aabb"][:, 1] / f(16)
+    return np.stack([conv(cx - rx, tx), conv(cy - ry, ty), conv(cx + rx + f(1), tx), conv(cy + ry + f(1), ty),
+                     o["radii"] > 0], 1)
+
+
+@pytest.mark.parametrize("group", ["means", "scales", "quats", "features_dc", "features_rest", "opacities"])
+def test_fp64_gradients_directional_fd(group):
+    """The FP64 analytic gradient of L = sum(W * image) (no sigma/alpha
+    cutoffs) against central differences along random directions that move
+    every visible Gaussian at once, three directions per parameter group.
+    Gaussians whose tile rectangle or place in a depth-sorted list changes
+    between the two evaluations are held still (the rendered image jumps
+    there).  Relative error <= 1e-6.  Means: SH degree 0 (the reference does
+    not differentiate the view direction) and the homogeneous w-row term the
+    reference's pixel VJP leaves out added in closed form (.metal:1252-1270);
+    quaternions: directions tangent to the unit sphere (the reference's
+    gradient ignores the normalisation)."""
+    from gpu_helpers import C0, sh_basis
+    g, cd, w = _fd_scene()
+    deg = 0 if group == "means" else 3
+    eps = 1e-5 if group == "means" else 1e-4
+    bg = (0.1, 0.2, 0.3)
+
+    def run(gg, backward):
+        return O.train_step(64, gg, cd, {"degrees_to_use": deg}, gt=None, v_img=w, background=bg,
+                            do_backward=backward, do_optimizer=False, want_ids=not backward, no_cutoff=True)
+    r = run(g.copy(), True)
+    o0 = run(g.copy(), False)
+    vis = r["radii"] > 0
+    assert vis.sum() > 400
+    if group == "means":
+        pm = np.asarray(cd["projmat"], np.float64).reshape(4, 4)
+        p = np.concatenate([g.means.astype(np.float64), np.ones((g.n, 1))], 1)
+        rw = 1.0 / (p @ pm[3] + 1e-6)
+        vnx = 0.5 * cd["width"] * r["v_xy"][:, 0].astype(np.float64)
+        vny = 0.5 * cd["height"] * r["v_xy"][:, 1].astype(np.float64)
+        corr = pm[3, :3][None, :] * (-(vnx * (p @ pm[0]) + vny * (p @ pm[1])) * rw * rw)[:, None]
+        grad = r["v_mean3d"] + corr
+    elif group == "scales":
+        grad = r["v_scale"]
+    elif group == "quats":
+        q = g.quats.astype(np.float64)
+        qn = q / np.linalg.norm(q, axis=1, keepdims=True)
+        vq = r["v_quat"].astype(np.float64)
+        grad = (vq - qn * np.sum(qn * vq, 1, keepdims=True)) / np.linalg.norm(q, axis=1, keepdims=True)
+    elif group == "opacities":
+        grad = r["v_opacity"][:, None]
+    else:
+        d = g.means.astype(np.float64) - np.asarray(cd["cam_pos"], np.float64)
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        grad = C0 * r["v_colors"] if group == "features_dc" else sh_basis(d)[:, :, None] * r["v_colors"][:, None, :]
+    grad = np.where(vis.reshape((-1,) + (1,) * (grad.ndim - 1)), grad, 0.0)
+    rects0 = _tile_rects(o0, cd)
+    rng = np.random.default_rng({"means": 1, "scales": 2, "quats": 3, "features_dc": 4, "features_rest": 5,
+                                 "opacities": 6}[group])
+    base = getattr(g, group).astype(np.float64)
+    for trial in range(3):
+        v = rng.normal(size=base.shape)
+        if group == "quats":
+            v -= qn * np.sum(qn * v, 1, keepdims=True)
+        v[~vis] = 0
+        for _ in range(6):
+            gp, gm = g.copy(), g.copy()
+            getattr(gp, group)[...] = (base + eps * v).astype(np.float32)
+            getattr(gm, group)[...] = (base - eps * v).astype(np.float32)
+            op, om = run(gp.copy(), False), run(gm.copy(), False)
+            still = np.zeros(g.n, bool)
+            for oo in (op, om):
+                still |= np.any(_tile_rects(oo, cd) != rects0, 1)
+                for t in range(o0["tile_bins"].shape[0]):
+                    a = o0["gaussian_ids"][o0["tile_bins"][t, 0]:o0["tile_bins"][t, 1]]
+                    b = oo["gaussian_ids"][oo["tile_bins"][t, 0]:oo["tile_bins"][t, 1]]
+                    if not np.array_equal(a, b):
+                        m = min(len(a), len(b))
+                        k = np.flatnonzero(a[:m] != b[:m])
+                        first = int(k[0]) if len(k) else m
+                        still[a[first:]] = True
+                        still[b[first:]] = True
+            if not (still & np.any(v.reshape(g.n, -1) != 0, 1)).any():
+                break
+            v[still] = 0
+        moved = int(np.any(v.reshape(g.n, -1) != 0, 1).sum())
+        assert moved > 250, moved
+        dth = getattr(gp, group).astype(np.float64) - getattr(gm, group).astype(np.float64)
+        fd = op["img_dot_v"] - om["img_dot_v"]
+        an = float(np.sum(grad * dth))
+        err = abs(fd - an) / abs(fd)
+        print(group, trial, "moved", moved, "fd", fd, "analytic", an, "rel", err)
+        assert err <= 1e-6, (group, trial, err)

@@ -4,8 +4,10 @@ Bars (per the engine's contract):
   * integer outputs (radii, tiles hit, per-tile counts, sorted per-tile id
     lists, last-contributor indices): identical to the oracle's float path;
   * image: <= 1e-5 max-abs against the oracle's float path (same decisions);
-  * gradients and Adam updates: <= 1e-4 relative L2 against the float path
-    and against FP64.
+  * gradients and Adam updates: <= 1e-4 relative L2 against the float path;
+    the first step's gradients also against FP64 (after some training FP64
+    moves sigma/alpha threshold decisions of a few splats, and its errors are
+    printed instead: test_c1_run_sampled_steps, the headline tests).
 The FP64 comparison of integer and image outputs is reported and held to a
 looser statistical bar: FP64 moves a few threshold decisions.
 """
@@ -85,7 +87,7 @@ def test_train_step_parity(small, raster_mode):
         e64 = rel_l2(eo[k], r64[k])
         print(k, "rel_l2 fp32", e32, "fp64", e64)
         assert e32 <= GRAD_TOL, k
-        assert e64 <= 10 * GRAD_TOL, k
+        assert e64 <= GRAD_TOL, k   # measured 2-4e-6 on GB300
     for k in E.GROUPS:
         before = getattr(init, k).reshape(eo["params"][k].shape)
         upd_e = eo["params"][k] - before
