@@ -221,6 +221,16 @@ __device__ __forceinline__ bool ms_guard(bool ok, unsigned code, long long idx, 
 #endif
 constexpr int kDbgSlot = 16;   // nan_counts[16..18]: checked-build violation record
 
+// A fault a kernel detected and survived (a bounded wait that ran out), in
+// every build: the first one is recorded in the same slots as a checked-build
+// violation, which the engine's stats report (check_record).
+__device__ __forceinline__ void record_fault(unsigned *dbg, unsigned code, long long idx) {
+    if (dbg && atomicCAS(dbg, 0u, code) == 0u) {
+        dbg[1] = (unsigned)idx;
+        dbg[2] = (unsigned)(idx >> 32);
+    }
+}
+
 // Splat record behind intersection slot idx.  Tile lists hold Gaussian ids;
 // an id past n (the slots of a tile that overflowed the buffer) reads as a
 // transparent record.  The id rides in a.w.

@@ -7,6 +7,7 @@
 // the oracle's float path.
 #include "common.cuh"
 #include "kernels.h"
+#include "tcgen05.cuh"
 
 namespace msplat {
 
@@ -80,39 +81,12 @@ __device__ __forceinline__ void sh_colour(const float *dc, const float *rest, in
 
 constexpr int kStageFloats = 45;   // 15 SH bases x 3 channels per Gaussian
 
-// kViews: several views (blockIdx.y); false compiles the one-view step with
-// the geometry read straight from the parameter bank.  At degree 3 with 15
-// bases each warp first copies its 32 Gaussians' SH rows (32 x 180 contiguous
-// bytes) to shared memory with coalesced loads, 16 bytes a lane when the rows
-// are 16-byte aligned; a lane's row there (45 floats apart) is conflict-free.
+// One Gaussian's projection (the body of the kernel below).  rest: its SH
+// row staged in shared memory when `staged`; with `bulk` the row arrives by
+// the warp's bulk copy, which is waited for (bounded) before it is read.
 template <bool kViews>
-__global__ void __launch_bounds__(256) k_project_fwd(ProjectArgs a) {
-    pdl_enter();
-    __shared__ __align__(16) float stage[8][32 * kStageFloats];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int view = kViews ? (int)blockIdx.y : 0;
-    const bool staged = a.rest_bases == 15 && a.sp[view].degrees_to_use >= 3;   // uniform over the CTA
-    if (staged) {
-        const int i0 = i - lane;
-        const int cnt = min(32, a.vt.n - i0);
-        if (cnt > 0) {
-            const float *src = a.features_rest + (size_t)i0 * kStageFloats;
-            float *dst = stage[wid];
-            const int nf = cnt * kStageFloats;
-            int done = 0;
-            if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
-                const int nv = nf >> 2;
-                const float4 *s4 = reinterpret_cast<const float4 *>(src);
-                float4 *d4 = reinterpret_cast<float4 *>(dst);
-                for (int k = lane; k < nv; k += 32) d4[k] = s4[k];
-                done = nv << 2;
-            }
-            for (int k = done + lane; k < nf; k += 32) dst[k] = src[k];
-        }
-        __syncwarp();
-    }
-    if (i >= a.vt.n) return;
+__device__ __forceinline__ void project_one(const ProjectArgs &a, int i, int view, bool staged, bool bulk,
+                                            const float *rest, uint64_t *bar) {
     const ViewGeom vg = view_geom(a.vt, view);
     const size_t u = kViews ? (size_t)view * a.vt.n + i : (size_t)i;   // this view's record of Gaussian i
     const StepParams &sp = a.sp[view];
@@ -214,7 +188,12 @@ __global__ void __launch_bounds__(256) k_project_fwd(ProjectArgs a) {
     const int deg = sp.degrees_to_use;
     const float *dc = a.features_dc + 3 * (size_t)i;
     float col[3];
-    if (staged) sh_colour(dc, &stage[wid][lane * kStageFloats], deg, vdx, vdy, vdz, col);
+    bool from_stage = staged;
+    if (bulk && !tc::mbar_wait(bar, 0)) {   // the row did not arrive: read it from global memory
+        record_fault(a.nan_counts ? a.nan_counts + kDbgSlot : nullptr, 40, i);
+        from_stage = false;
+    }
+    if (from_stage) sh_colour(dc, rest, deg, vdx, vdy, vdz, col);
     else sh_colour(dc, a.features_rest + (size_t)a.rest_bases * 3 * i, deg, vdx, vdy, vdz, col);
     // sigmoid(opacity) once per Gaussian (the reference does it per
     // intersection at pack time; same input, same bits)
@@ -255,6 +234,57 @@ __global__ void __launch_bounds__(256) k_project_fwd(ProjectArgs a) {
         if (!okn) atomicAdd(a.nan_counts + kNanProjConic, 1u);
         if (!okr) atomicAdd(a.nan_counts + kNanProjRgb, 1u);
     }
+}
+
+// kViews: several views (blockIdx.y); false compiles the one-view step with
+// the geometry read straight from the parameter bank.  At degree 3 with 15
+// bases each warp stages its 32 Gaussians' SH rows (32 x 180 contiguous
+// bytes) in shared memory: one bulk (TMA) copy issued by lane 0 when the rows
+// are 16-byte aligned and whole 16-byte units, which lands while the warp
+// computes the geometry; otherwise coalesced loads.  A lane's row there (45
+// floats apart) is conflict-free.  Lane 0 waits for its copy before the warp
+// leaves, so no copy outlives the CTA.
+template <bool kViews>
+__global__ void __launch_bounds__(256) k_project_fwd(ProjectArgs a) {
+    pdl_enter();
+    __shared__ __align__(16) float stage[8][32 * kStageFloats];
+    __shared__ __align__(8) uint64_t bar[8];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int view = kViews ? (int)blockIdx.y : 0;
+    const bool staged = a.rest_bases == 15 && a.sp[view].degrees_to_use >= 3;   // uniform over the CTA
+    bool bulk = false;
+    if (staged) {
+        const int i0 = i - lane;
+        const int cnt = min(32, a.vt.n - i0);
+        if (cnt > 0) {
+            const float *src = a.features_rest + (size_t)i0 * kStageFloats;
+            float *dst = stage[wid];
+            const int nf = cnt * kStageFloats;
+            bulk = (reinterpret_cast<uintptr_t>(src) & 15) == 0 && (nf & 3) == 0;   // uniform over the warp
+            if (bulk) {
+                if (lane == 0) {
+                    tc::mbar_init(&bar[wid], 1);
+                    tc::mbar_arrive_expect_tx(&bar[wid], (uint32_t)nf * 4u);
+                    tc::bulk_g2s(dst, src, (uint32_t)nf * 4u, &bar[wid]);
+                }
+            } else {
+                int done = 0;
+                if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+                    const int nv = nf >> 2;
+                    const float4 *s4 = reinterpret_cast<const float4 *>(src);
+                    float4 *d4 = reinterpret_cast<float4 *>(dst);
+                    for (int k = lane; k < nv; k += 32) d4[k] = s4[k];
+                    done = nv << 2;
+                }
+                for (int k = done + lane; k < nf; k += 32) dst[k] = src[k];
+            }
+        }
+        __syncwarp();
+    }
+    if (i < a.vt.n) project_one<kViews>(a, i, view, staged, bulk, &stage[wid][lane * kStageFloats], &bar[wid]);
+    if (bulk && lane == 0 && !tc::mbar_wait(&bar[wid], 0))
+        record_fault(a.nan_counts ? a.nan_counts + kDbgSlot : nullptr, 41, i);
 }
 
 void launch_project_fwd(const ProjectArgs &a, cudaStream_t s) {

@@ -8,8 +8,9 @@
 // shuffles for 8 values plus 5 for the ninth, instead of 45; paired fp32
 // adds), warps combine through shared-memory adds, and each batch flushes one
 // set of three float4 vector atomics per (splat, tile) instead of the
-// reference's nine scalar atomics per (splat, warp).  A warp skips the
-// splats whose reach box misses its block.
+// reference's nine scalar atomics per (splat, warp).  A warp takes only the
+// splats whose reach box meets its block: after each batch is staged it
+// lists their positions (one ballot per 32) and walks that list.
 // Follows rasterize_backward_kernel (msplat_metal.metal:931-1135),
 // compute_chunk_prefix_suffix_kernel (:3139-3175) and
 // rasterize_backward_chunked_kernel (:3179-3366), including its quirk that a
@@ -59,6 +60,8 @@ template <int kBB, int kPx> struct BwdSmem {
     float4 con[kBB];    // conic, bits of the warps the splat reaches
     float4 rgb[kBB];    // clamped colour, w: bits of the channels with raw + 0.5 >= 0
     float acc[kBB][9];  // r g b | ca cb cc | x y | opacity
+    uint32_t wm[kBB];   // bits of the warps the splat reaches
+    uint16_t wl[BwdLayout<kPx>::kThreads / 32][kBB];   // per warp: the batch positions it takes, ascending
     int wmax[BwdLayout<kPx>::kThreads / 32];
 };
 
@@ -158,8 +161,9 @@ __device__ void backward_range(BwdSmem<kBB, kPx> &sm, const RasterArgs &a, int s
             if (idx >= s) {
                 const SplatRec r = isect_record(a.isect_ids, a.rec, a.n, idx);
                 sm.xyo[k] = r.a;
-                sm.con[k] = make_float4(r.b.x, r.b.y, r.b.z,
-                                        __uint_as_float(L::reach(r.a.x, r.a.y, r.b.w, r.c.w, ox, oy)));
+                const uint32_t reach = L::reach(r.a.x, r.a.y, r.b.w, r.c.w, ox, oy);
+                sm.con[k] = make_float4(r.b.x, r.b.y, r.b.z, __uint_as_float(reach));
+                sm.wm[k] = reach;
                 // clamped colour max(raw + 0.5, 0); w: channels whose raw + 0.5 >= 0
                 // (the only ones that pass a colour gradient back)
                 const float cr = r.c.x + 0.5f, cg = r.c.y + 0.5f, cb = r.c.z + 0.5f;
@@ -171,9 +175,24 @@ __device__ void backward_range(BwdSmem<kBB, kPx> &sm, const RasterArgs &a, int s
         }
         __syncthreads();
         const int nb = min(kBB, batch_end - s + 1);
-        for (int t = max(0, batch_end - wbin); t < nb; t++) {
+        // the positions from t0 on whose splat can reach this warp's pixels
+        // (ascending: back to front), listed with one ballot per 32
+        const int t0 = max(0, batch_end - wbin);
+        int cnt = 0;
+        {
+            const unsigned below = (1u << lane) - 1u;
+            for (int base = t0; base < nb; base += 32) {
+                const int t = base + lane;
+                const bool hit = t < nb && ((sm.wm[t] >> warp) & 1u);
+                const unsigned m = __ballot_sync(0xffffffffu, hit);
+                if (hit) sm.wl[warp][cnt + __popc(m & below)] = (uint16_t)t;
+                cnt += __popc(m);
+            }
+            __syncwarp();
+        }
+        for (int i = 0; i < cnt; i++) {
+            const int t = sm.wl[warp][i];
             const float4 cn = sm.con[t];
-            if (!((__float_as_uint(cn.w) >> warp) & 1u)) continue;   // no pixel of this warp takes it
             const int sidx = batch_end - t;
             const float4 xo = sm.xyo[t];
             const float dx = __fsub_rn(xo.x, px);

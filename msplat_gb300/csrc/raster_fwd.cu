@@ -22,7 +22,27 @@ template <int kBatch> struct BatchSmem {
     float4 xyo[kBatch];   // x, y, opacity, bits of the warps the splat reaches (warp_reach)
     float4 con[kBatch];   // conic
     float4 rgb[kBatch];   // clamped colour max(raw + 0.5, 0)
+    uint32_t wm[kBatch];  // bits of the warps the splat reaches (warp_reach)
+    uint16_t wl[kTileThreads / 32][kBatch];   // per warp: the batch positions it takes, ascending
 };
+
+// The positions t < nb of the staged batch whose warp bit is set, written
+// ascending to list (one ballot per 32 positions); returns their count.
+template <int kBatch>
+__device__ __forceinline__ int warp_batch_list(const uint32_t *wm, int nb, int warp, uint16_t *list) {
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    int cnt = 0;
+    for (int base = 0; base < nb; base += 32) {
+        const int t = base + lane;
+        const bool hit = t < nb && ((wm[t] >> warp) & 1u);
+        const unsigned m = __ballot_sync(0xffffffffu, hit);
+        if (hit) list[cnt + __popc(m & below)] = (uint16_t)t;
+        cnt += __popc(m);
+    }
+    __syncwarp();
+    return cnt;
+}
 
 // (px, py): this thread's pixel
 template <int kBatch>
@@ -32,14 +52,18 @@ __device__ __forceinline__ void load_batch(BatchSmem<kBatch> &sm, const RasterAr
     if (t < kBatch && idx < end) {
         const SplatRec r = isect_record(a.isect_ids, a.rec, a.n, idx);
         const float ox = px - (float)tile_px(t), oy = py - (float)tile_py(t);   // the tile's first pixel
-        sm.xyo[t] = make_float4(r.a.x, r.a.y, r.a.z, __uint_as_float(warp_reach(r.a.x, r.a.y, r.b.w, r.c.w, ox, oy)));
+        const uint32_t reach = warp_reach(r.a.x, r.a.y, r.b.w, r.c.w, ox, oy);
+        sm.xyo[t] = make_float4(r.a.x, r.a.y, r.a.z, __uint_as_float(reach));
+        sm.wm[t] = reach;
         sm.con[t] = r.b;
         sm.rgb[t] = make_float4(fmaxf(r.c.x + 0.5f, 0.f), fmaxf(r.c.y + 0.5f, 0.f), fmaxf(r.c.z + 0.5f, 0.f), 0.f);
     }
 }
 
 // Walks [s, e) for this pixel; the whole CTA iterates together.  A warp
-// skips the splats that cannot reach its 8x4 block.
+// takes only the splats that can reach its 8x4 block: after each batch is
+// staged it lists their positions (ballots over the reach bits) and walks
+// that list.
 // done: in/out per-thread flag; returns (T, C, last).
 template <int kBatch>
 __device__ __forceinline__ void composite_range(BatchSmem<kBatch> &sm, const RasterArgs &a, int s, int e, float px,
@@ -53,11 +77,12 @@ __device__ __forceinline__ void composite_range(BatchSmem<kBatch> &sm, const Ras
         if (__syncthreads_count(done) == kTileThreads) break;
         load_batch<kBatch>(sm, a, b0 + (int)threadIdx.x, e, px, py);
         __syncthreads();
-        if (done) continue;
         const int nb = min(kBatch, e - b0);
-        for (int t = 0; t < nb; t++) {
+        const int cnt = warp_batch_list<kBatch>(sm.wm, nb, warp, sm.wl[warp]);
+        if (done) continue;
+        for (int i = 0; i < cnt; i++) {
+            const int t = sm.wl[warp][i];
             const float4 xo = sm.xyo[t];
-            if (!((__float_as_uint(xo.w) >> warp) & 1u)) continue;
             const float4 cn = sm.con[t];
             const float dx = xo.x - px, dy = xo.y - py;
             const float sigma = __fmaf_rn(0.5f, __fmaf_rn(cn.x, dx * dx, cn.z * dy * dy), cn.y * dx * dy);

@@ -1,7 +1,8 @@
-// Blackwell (sm_100 family) tensor-core primitives in inline PTX: tensor
-// memory allocation, shared-memory matrix descriptors, the BF16 x BF16 -> F32
-// tcgen05.mma issued by one thread, its completion through an mbarrier, and
-// the tcgen05.ld that brings accumulator rows back to registers.
+// Blackwell (sm_100 family) primitives in inline PTX: tensor memory
+// allocation, shared-memory matrix descriptors, the BF16 x BF16 -> F32
+// tcgen05.mma issued by one thread, its completion through an mbarrier, the
+// tcgen05.ld that brings accumulator rows back to registers, and the bulk
+// (TMA) global -> shared copy with its mbarrier transaction count.
 //
 // Operand layout used throughout: K-major with no swizzle.  An R x K tile of
 // bf16 is stored as (R/8) x (K/8) core matrices of 8 rows x 16 bytes, core
@@ -87,6 +88,23 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
         if (ok) return true;
     }
     return false;
+}
+
+// arrive once, announcing `bytes` more bytes of asynchronous copies for this phase
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// ---- bulk copy (TMA, untiled) ----
+
+// global -> shared, `bytes` (a multiple of 16, both addresses 16-byte
+// aligned), completing on the mbarrier's transaction count
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
 }
 
 // ---- MMA ----

@@ -185,14 +185,14 @@ def step_errors(eo, r, before):
     return e
 
 
-def compare_step(eo, r32, before, label, r64=None):
+def compare_step(eo, r32, before, label, r64=None, fp64_bar=FP64_BAR):
     """One step's parity bars: integer outputs, lists, last contributors and
     visible projection outputs identical to the float path; image and final
     transmittance within 1e-5 max-abs; loss within 1e-5 relative; dL/dimage,
     the rasterizer and projection gradients and every parameter update within
     1e-4 relative L2.  Every error is printed first.  Against FP64 (r64) the
-    errors are printed and returned, and held to 1e-3 (gradients, updates)
-    and to < 0.2 % of image values over 1e-5."""
+    errors are printed and returned, and held to fp64_bar (gradients,
+    updates: 1e-3 by default) and to < 0.2 % of image values over 1e-5."""
     act = r32["radii"] > 0
     e32 = step_errors(eo, r32, before)
     print(label, "float-path errors:", {k: float("%.3g" % v) for k, v in e32.items()})
@@ -222,7 +222,7 @@ def compare_step(eo, r32, before, label, r64=None):
     if r64 is not None:
         assert rep["image_frac_over_1e-5"] < 2e-3
         for k in GRADS:
-            assert rep[k] <= FP64_BAR, (label, k, rep[k])
+            assert rep[k] <= fp64_bar, (label, k, rep[k])
         for k in E.GROUPS:
-            assert rep["update_" + k] <= FP64_BAR, (label, k, rep["update_" + k])
+            assert rep["update_" + k] <= fp64_bar, (label, k, rep["update_" + k])
     return rep
