@@ -100,6 +100,16 @@ int msplat_trainer_set_learned_relocation(MsplatTrainer t, int enabled);
  * returns 1 when the proposal is enabled, 0 when not, -1 on a bad handle. */
 int msplat_trainer_learned_stats(MsplatTrainer t, float *last_loss, int *rounds);
 
+/* Held-out quality of the learned proposal's predictions (no counterpart in
+ * the reference: it measures this build's MLP).  At each training round after
+ * the first, before the MLP trains on the round's new labels, it predicts
+ * them: mse[0] / mse[1] are the mean squared errors of its opacity forecast
+ * and of the persistence forecast (the Gaussian's opacity at the snapshot),
+ * mse[2] / mse[3] the same for the activity forecast (persistence: its mean
+ * activity at the snapshot), averaged over rounds.  Returns the rounds
+ * evaluated. */
+int msplat_trainer_learned_eval(MsplatTrainer t, float mse[4]);
+
 /* Views per optimizer step (no counterpart in the reference; default 1).
  * With num_views > 1 each msplat_trainer_step renders the next num_views
  * cameras of the shuffled order and applies one update from the mean of

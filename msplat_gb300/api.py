@@ -49,6 +49,7 @@ def _lib():
     L.msplat_trainer_load_ply.argtypes = [vp, cp]
     L.msplat_trainer_set_learned_relocation.argtypes = [vp, C.c_int]
     L.msplat_trainer_learned_stats.argtypes = [vp, fp, C.POINTER(C.c_int)]
+    L.msplat_trainer_learned_eval.argtypes = [vp, fp]
     L.msplat_trainer_set_batch_views.argtypes = [vp, C.c_int, C.c_float]
     L.msplat_trainer_set_isect_budget.argtypes = [vp, C.c_float]
     L.msplat_trainer_autotune.argtypes = [vp, vp]
@@ -305,6 +306,14 @@ class GaussianTrainer:
         rounds = C.c_int()
         on = _lib().msplat_trainer_learned_stats(self.h, loss, C.byref(rounds))
         return {"enabled": on == 1, "last_loss": float(loss[0]), "rounds": rounds.value}
+
+    def learned_eval(self) -> dict:
+        """Held-out mean squared errors of the proposal's forecasts against the
+        persistence forecasts, averaged over the rounds evaluated."""
+        m = (C.c_float * 4)()
+        rounds = _lib().msplat_trainer_learned_eval(self.h, m)
+        return {"rounds_evaluated": rounds, "mse_opacity": m[0], "mse_opacity_persistence": m[1], "mse_activity": m[2],
+                "mse_activity_persistence": m[3]}
 
     def mcmc_stats(self) -> dict:
         """Counts of the last MCMC relocation round and the rounds run so far."""

@@ -480,6 +480,9 @@ struct TrainerImpl {
         int window = 500, samples = 16384, epochs = 40;
         float lr = 1e-3f;
         float *P = nullptr, *G = nullptr, *M = nullptr, *V = nullptr, *loss = nullptr, *score = nullptr;
+        float *eval = nullptr;          // device sums of the held-out check (mlp_eval)
+        double eval_sum[4] = {0, 0, 0, 0};
+        int eval_rounds = 0;
         uint8_t *img = nullptr;
         unsigned *err = nullptr;
         float4 *gstats = nullptr, *snap = nullptr;
@@ -510,7 +513,7 @@ struct TrainerImpl {
 
     void free_learned() {
         void *ptrs[] = {lrn.P, lrn.G, lrn.M, lrn.V, lrn.loss, lrn.score, lrn.img, lrn.err, lrn.gstats, lrn.snap,
-                        lrn.X, lrn.Xs, lrn.Y, lrn.T, lrn.idx};
+                        lrn.X, lrn.Xs, lrn.Y, lrn.T, lrn.idx, lrn.eval};
         for (void *q : ptrs)
             if (q) cudaFree(q);
         lrn = Learned{};
@@ -531,6 +534,7 @@ struct TrainerImpl {
         CKA(cudaMalloc(&lrn.V, kMlpParams * 4));
         CKA(cudaMalloc(&lrn.loss, 4));
         CKA(cudaMalloc(&lrn.err, 4));
+        CKA(cudaMalloc(&lrn.eval, 5 * 4));
         CKA(cudaMalloc(&lrn.img, kImgBytes));
         CKA(cudaMalloc(&lrn.gstats, sizeof(float4) * (size_t)cap));
         CKA(cudaMalloc(&lrn.score, 4 * (size_t)cap));
@@ -581,6 +585,16 @@ struct TrainerImpl {
         cudaStream_t s = stream();
         if (lrn.pending >= 0) {
             mlp_targets(lrn.idx, lrn.snap, lrn.samples, model.p[5], lrn.gstats, lrn.T, s);
+            // held out: once trained, the MLP predicts this round's labels before it sees them
+            float ev[5] = {0, 0, 0, 0, 0};
+            const bool evaluate = lrn.rounds >= 1;
+            if (evaluate) {
+                mlp_pack(lrn.P, lrn.img, s);
+                mlp_forward(lrn.Xs, lrn.samples, lrn.img, lrn.P, lrn.Y, lrn.err, s);
+                CKA(cudaMemsetAsync(lrn.eval, 0, 5 * 4, s));
+                mlp_eval(lrn.Y, lrn.T, lrn.snap, lrn.samples, lrn.eval, s);
+                CKA(cudaMemcpyAsync(ev, lrn.eval, 5 * 4, cudaMemcpyDeviceToHost, s));
+            }
             for (int e = 0; e < lrn.epochs; e++) {
                 mlp_pack(lrn.P, lrn.img, s);
                 CKA(cudaMemsetAsync(lrn.loss, 0, 4, s));
@@ -592,6 +606,10 @@ struct TrainerImpl {
             CKA(cudaMemcpyAsync(&err, lrn.err, 4, cudaMemcpyDeviceToHost, s));
             CKA(cudaStreamSynchronize(s));
             if (err) throw std::runtime_error("learned relocation: tensor-core MMA did not complete");
+            if (evaluate && ev[4] > 0.f) {
+                for (int k = 0; k < 4; k++) lrn.eval_sum[k] += ev[k] / ev[4];
+                lrn.eval_rounds++;
+            }
             lrn.rounds++;
         }
         std::vector<int> idx(lrn.samples);
@@ -599,7 +617,7 @@ struct TrainerImpl {
         for (auto &v : idx) v = pick(lrn.rng);
         CKA(cudaMemcpyAsync(lrn.idx, idx.data(), 4 * idx.size(), cudaMemcpyHostToDevice, s));
         mlp_features(feat_args(lrn.samples, lrn.idx, lrn.Xs), s);
-        mlp_snapshot(lrn.idx, lrn.samples, lrn.gstats, lrn.snap, s);
+        mlp_snapshot(lrn.idx, lrn.samples, lrn.gstats, model.p[5], lrn.snap, s);
         CKA(cudaStreamSynchronize(s));   // idx is a host vector
         lrn.pending = step;
     }
@@ -1370,6 +1388,13 @@ int msplat_trainer_learned_stats(MsplatTrainer t, float *last_loss, int *rounds)
     if (last_loss) *last_loss = TR(t)->lrn.last_loss;
     if (rounds) *rounds = TR(t)->lrn.rounds;
     return TR(t)->lrn.enabled ? 1 : 0;
+}
+
+int msplat_trainer_learned_eval(MsplatTrainer t, float mse[4]) {
+    if (!t) return -1;
+    const auto &l = TR(t)->lrn;
+    for (int k = 0; k < 4; k++) mse[k] = l.eval_rounds ? (float)(l.eval_sum[k] / l.eval_rounds) : 0.f;
+    return l.eval_rounds;
 }
 
 int msplat_trainer_load_ply(MsplatTrainer t, const char *path) {

@@ -455,9 +455,35 @@ __global__ void k_mlp_features(MlpFeatArgs a) {
     for (int k = 0; k < 4; k++) dst[k] = pack8(f + 8 * k);
 }
 
-__global__ void k_mlp_snapshot(const int *idx, int S, const float4 *gstats, float4 *snap) {
+__global__ void k_mlp_snapshot(const int *idx, int S, const float4 *gstats, const float *opacities, float4 *snap) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < S) snap[s] = gstats[idx[s]];
+    if (s >= S) return;
+    float4 st = gstats[idx[s]];
+    const float sig = 1.f / (1.f + __expf(-opacities[idx[s]]));
+    st.w = finite_bits(sig) ? sig : 0.f;
+    snap[s] = st;
+}
+
+__global__ void k_mlp_eval(const float2 *pred, const float2 *T, const float4 *snap, int S, float *sums) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    float e[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    if (s < S) {
+        const float2 p = pred[s], t = T[s];
+        const float4 then = snap[s];
+        const float act_then = then.y > 0.f ? log1pf(kActScale * then.x / then.y) : 0.f;
+        const float naive_act = finite_bits(act_then) ? act_then : 0.f;
+        e[0] = (p.x - t.x) * (p.x - t.x);
+        e[1] = (then.w - t.x) * (then.w - t.x);
+        e[2] = (p.y - t.y) * (p.y - t.y);
+        e[3] = (naive_act - t.y) * (naive_act - t.y);
+        e[4] = 1.f;
+    }
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        float v = e[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) atomicAdd(sums + k, v);
+    }
 }
 
 __global__ void k_mlp_targets(const int *idx, const float4 *snap, int S, const float *opacities, const float4 *gstats,
@@ -489,12 +515,16 @@ __global__ void k_mlp_scores(const float2 *y, int n, float *score) {
 void mlp_features(const MlpFeatArgs &a, cudaStream_t s) {
     if (a.rows > 0) k_mlp_features<<<(a.rows + 255) / 256, 256, 0, s>>>(a);
 }
-void mlp_snapshot(const int *idx, int S, const float4 *gstats, float4 *snap, cudaStream_t s) {
-    if (S > 0) k_mlp_snapshot<<<(S + 255) / 256, 256, 0, s>>>(idx, S, gstats, snap);
+void mlp_snapshot(const int *idx, int S, const float4 *gstats, const float *opacities, float4 *snap,
+                  cudaStream_t s) {
+    if (S > 0) k_mlp_snapshot<<<(S + 255) / 256, 256, 0, s>>>(idx, S, gstats, opacities, snap);
 }
 void mlp_targets(const int *idx, const float4 *snap, int S, const float *opacities, const float4 *gstats, float2 *T,
                  cudaStream_t s) {
     if (S > 0) k_mlp_targets<<<(S + 255) / 256, 256, 0, s>>>(idx, snap, S, opacities, gstats, T);
+}
+void mlp_eval(const float2 *pred, const float2 *T, const float4 *snap, int S, float *sums, cudaStream_t s) {
+    if (S > 0) k_mlp_eval<<<(S + 255) / 256, 256, 0, s>>>(pred, T, snap, S, sums);
 }
 void mlp_scores(const float2 *y, int n, float *score, cudaStream_t s) {
     if (n > 0) k_mlp_scores<<<(n + 255) / 256, 256, 0, s>>>(y, n, score);

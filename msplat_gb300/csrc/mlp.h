@@ -35,7 +35,14 @@ void mlp_features(const MlpFeatArgs &a, cudaStream_t s);
 // now, or (0, 0) when the slot was relocated or regrown since
 void mlp_targets(const int *idx, const float4 *snap, int S, const float *opacities, const float4 *gstats,
                  float2 *T, cudaStream_t s);
-void mlp_snapshot(const int *idx, int S, const float4 *gstats, float4 *snap, cudaStream_t s);
+// the sampled Gaussians' activity statistics, w = sigmoid(opacity), at the snapshot
+void mlp_snapshot(const int *idx, int S, const float4 *gstats, const float *opacities, float4 *snap,
+                  cudaStream_t s);
+// Held-out check of a round's predictions before training on its labels:
+// adds to sums[0..4] the squared errors of the MLP (opacity, activity), of the
+// persistence forecast (the snapshot's own opacity and mean activity) and the
+// sample count
+void mlp_eval(const float2 *pred, const float2 *T, const float4 *snap, int S, float *sums, cudaStream_t s);
 // sampling weights from the MLP outputs
 void mlp_scores(const float2 *y, int n, float *score, cudaStream_t s);
 

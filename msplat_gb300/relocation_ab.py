@@ -1,7 +1,8 @@
 """Time-to-PSNR of the learned relocation proposal against plain
 opacity-weighted MCMC relocation, on the small synthetic scene.
 
-    python -m msplat_gb300.relocation_ab [--iters 6000] [--seed 0] [--arms plain,learned,batch4x3_learned]
+    python -m msplat_gb300.relocation_ab [--iters 6000] [--seeds 0,1,2,3,4]
+        [--arms plain,learned,batch4x3,batch4x3_learned]
 
 Scene: 16,384 ground-truth Gaussians (synthetic.config_small), 8 training
 views at 256x256 and 4 held-out views between them, targets rendered by the
@@ -9,8 +10,10 @@ engine.  Both arms start from the same seed points (jittered ground-truth
 means, colours from the ground truth) and the same configuration (MCMC cap
 32,768, black background); the learned arm switches the proposal on.
 Held-out PSNR is measured every `--eval-every` steps outside the timed
-training time.  Time-to-PSNR: the training wall-clock at which each arm
-first reaches the plain arm's final PSNR minus 0.1 dB.  Optional arms
+training time.  Time-to-PSNR: the training wall-clock at which an arm first
+reaches its plain counterpart's final PSNR minus 0.1 dB (`plain` for the
+one-view arms, the same batch arm without `_learned` for a batched learned
+arm), reported per seed and as mean and sd over seeds.  Optional arms
 `batchB[xS][_learned]` train with B views per optimizer step (the mean
 gradient of B cameras, one update, learning rates x S, default
 `--batch-lr-scale` or B ** 0.75); iterations count views, so every arm sees
@@ -28,7 +31,11 @@ import time
 import numpy as np
 
 
-def _scene(seed):
+def _scene(seed, init="jitter", n_init=4096):
+    """Targets of the small synthetic scene and the seed points: the ground
+    truth's means jittered (init="jitter"), or n_init points uniform in the
+    unit ball with random colours (init="random": most die early, so MCMC
+    relocation and growth do much of the work)."""
     from . import engine as E
     from . import synthetic as S
     sc = S.config_small(seed)
@@ -42,8 +49,13 @@ def _scene(seed):
         imgs.append((np.clip(img, 0, 1) * 255 + 0.5).astype(np.uint8))
     eng.close()
     rng = np.random.default_rng(seed + 1)
-    xyz = (sc.gt.means + rng.normal(0, 0.05, sc.gt.means.shape)).astype(np.float32)
-    col = np.clip((sc.gt.features_dc * 0.28209479177387814 + 0.5) * 255.0, 0, 255).astype(np.uint8)
+    if init == "random":
+        d = rng.normal(size=(n_init, 3))
+        xyz = (d / np.linalg.norm(d, axis=1, keepdims=True) * rng.random((n_init, 1)) ** (1 / 3)).astype(np.float32)
+        col = rng.integers(0, 256, (n_init, 3), dtype=np.uint8)
+    else:
+        xyz = (sc.gt.means + rng.normal(0, 0.05, sc.gt.means.shape)).astype(np.float32)
+        col = np.clip((sc.gt.features_dc * 0.28209479177387814 + 0.5) * 255.0, 0, 255).astype(np.uint8)
     return list(sc.train_cams) + list(test), imgs, xyz, col
 
 
@@ -81,6 +93,7 @@ def run_arm(cams, imgs, xyz, col, learned, iters, eval_every, batch=1, lr_scale=
     out = {"curve": curve, "final_psnr": curve[-1][2], "train_s": train_s, "splats": t.splat_count}
     if learned:
         out["proposal"] = t.learned_stats()
+        out["proposal"].update(t.learned_eval())
     return out
 
 
@@ -106,40 +119,77 @@ def _arm_spec(name, default_lr=0.0):
     raise ValueError(f"unknown arm {name!r}")
 
 
+def compare(cams, imgs, xyz, col, names, iters, eval_every, batch_lr_scale=0.0):
+    """Runs every arm on one scene.  The target of each arm is the final PSNR
+    of its plain counterpart minus 0.1 dB: `plain` for the one-view arms,
+    `batch<B>...` without `_learned` for the batched learned arms."""
+    runs = {}
+    for nm in names:
+        learned, b, lr = _arm_spec(nm, batch_lr_scale)
+        runs[nm] = run_arm(cams, imgs, xyz, col, learned, iters, eval_every, batch=b, lr_scale=lr)
+    res = {}
+    for nm, r in runs.items():
+        base = nm[:-len("_learned")] if nm.endswith("_learned") else nm
+        if base == "learned":
+            base = "plain"
+        ref = runs.get(base, runs["plain"])
+        target = ref["final_psnr"] - 0.1
+        _, t_ref = time_to(ref["curve"], target)
+        st, tt = time_to(r["curve"], target)
+        res[nm] = {"final_psnr": r["final_psnr"], "train_s": r["train_s"], "time_to_target_s": tt,
+                   "step_to_target": st, "splats": r["splats"], "vs": base, "target_psnr": target,
+                   "time_ratio": (tt / t_ref) if (tt is not None and t_ref) else None,
+                   # area under the held-out PSNR curve per evaluation (a deterministic proxy)
+                   "mean_psnr": float(np.mean([p for _, _, p in r["curve"]])),
+                   "curve": r["curve"]}
+        if "proposal" in r:
+            res[nm]["proposal"] = r["proposal"]
+    return res
+
+
+def summarize(per_seed, names):
+    """mean and sd over seeds of each arm's time ratio, final and mean PSNR."""
+    out = {}
+    for nm in names:
+        rows = [ps[nm] for ps in per_seed]
+        ratios = [r["time_ratio"] for r in rows if r["time_ratio"] is not None]
+        out[nm] = {"vs": rows[0]["vs"], "seeds": len(rows), "reached": len(ratios),
+                   "time_ratio_mean": float(np.mean(ratios)) if ratios else None,
+                   "time_ratio_sd": float(np.std(ratios, ddof=1)) if len(ratios) > 1 else None,
+                   "final_psnr_mean": float(np.mean([r["final_psnr"] for r in rows])),
+                   "mean_psnr_mean": float(np.mean([r["mean_psnr"] for r in rows]))}
+    return out
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--iters", type=int, default=6000)
     ap.add_argument("--eval-every", type=int, default=250)
-    ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--arms", default="plain,learned", help="comma-separated; the first is the target's source")
+    ap.add_argument("--seeds", default="0", help="comma-separated scene seeds")
+    ap.add_argument("--arms", default="plain,learned", help="comma-separated arm names")
     ap.add_argument("--batch-lr-scale", type=float, default=0.0, help="learning-rate factor of batch arms (0: B ** 0.75)")
+    ap.add_argument("--curves", action="store_true", help="include the PSNR curves")
+    ap.add_argument("--init", default="jitter", choices=["jitter", "random"],
+                    help="seed points: jittered ground truth, or random points in the unit ball")
+    ap.add_argument("--n-init", type=int, default=4096, help="random seed points (--init random)")
     a = ap.parse_args(argv)
     names = [x.strip() for x in a.arms.split(",") if x.strip()]
-    if "plain" not in names:
-        names.insert(0, "plain")
-    names.remove("plain")
+    if "plain" in names:
+        names.remove("plain")
     names.insert(0, "plain")
-    cams, imgs, xyz, col = _scene(a.seed)
-    runs = {}
-    for nm in names:
-        learned, b, lr = _arm_spec(nm, a.batch_lr_scale)
-        runs[nm] = run_arm(cams, imgs, xyz, col, learned, a.iters, a.eval_every, batch=b, lr_scale=lr)
-    plain = runs["plain"]
-    target = plain["final_psnr"] - 0.1
-    ps, pt = time_to(plain["curve"], target)
+    seeds = [int(x) for x in a.seeds.split(",") if x.strip()]
+    per_seed = []
+    for sd in seeds:
+        cams, imgs, xyz, col = _scene(sd, a.init, a.n_init)
+        per_seed.append(compare(cams, imgs, xyz, col, names, a.iters, a.eval_every, a.batch_lr_scale))
     res = {"workload": "learned vs plain MCMC relocation, 16,384-Gaussian synthetic scene, 8 train + 4 held-out "
-                       "views at 256x256, cap 32,768", "iters": a.iters, "target_psnr": target}
-    for nm, r in runs.items():
-        st, tt = time_to(r["curve"], target)
-        res[nm] = {"final_psnr": r["final_psnr"], "train_s": r["train_s"], "time_to_target_s": tt,
-                   "step_to_target": st, "splats": r["splats"]}
-        if "proposal" in r:
-            res[nm]["proposal"] = r["proposal"]
-        if nm != "plain":
-            res[nm]["time_ratio"] = (tt / pt) if (tt is not None and pt) else None
-    if "learned" in runs:
-        res["time_ratio"] = res["learned"]["time_ratio"]
-    res["curves"] = {nm: r["curve"] for nm, r in runs.items()}
+                       "views at 256x256, cap 32,768", "iters": a.iters, "seeds": seeds,
+           "init": a.init, "summary": summarize(per_seed, names)}
+    if not a.curves:
+        for ps in per_seed:
+            for r in ps.values():
+                r.pop("curve", None)
+    res["per_seed"] = per_seed
     print(json.dumps(res), flush=True)
     return 0
 
