@@ -20,10 +20,20 @@ Arms:
                      (oracle/, FP64, OpenMP on all host cores) on the same
                      workload, one full iteration per step.
 
-Also reported (key "batched"): the multi-view step on the same model, 8
-views of mixed sizes per step (2 each of 1297x840, 979x546, 648x420 and
-2594x1680, same camera poses, focal length scaled with the width), one
-launch per stage over all views, as a captured graph.
+Also reported:
+  batched        the multi-view step on the same model, 8 views of mixed sizes
+                 per step (2 each of 1297x840, 979x546, 648x420 and 2594x1680,
+                 same camera poses, focal length scaled with the width), one
+                 launch per stage over all views, as a captured graph;
+  e2e_trainer    iterations/s through the reference's public trainer API
+                 (msplat_trainer_step), the model resumed at iteration 3001
+                 from a checkpoint, MCMC rounds inside the timed region;
+  time_to_psnr   learned vs plain relocation (and learned + batched vs plain
+                 + batched) on the small scene over three seeds;
+  full_run       the full configuration trained from 100k random points to
+                 the 1M cap over 7000 iterations, with held-out PSNR / SSIM;
+  roofline.fp32  the rasterizer backward's FP32-pipe fraction from the
+                 (pixel, splat) pairs the reference's algorithm walks.
 
 Under torchrun (N > 1) every rank trains its own replica on its own GPU
 ("replicas only": the step has no cross-GPU exchange).
@@ -228,6 +238,82 @@ def loaded_libraries():
     return sorted(os.path.relpath(p, ROOT) for p in paths if p.startswith(ROOT))
 
 
+def sm_max_mhz():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["sm_max_mhz"])
+    except (OSError, KeyError, ValueError):
+        return 2070.0
+
+
+def backward_pairs(eng, cd):
+    """(pixel, splat) pairs the reference's backward walks for the engine's
+    last step of view cd: per pixel inside the image, from min(last
+    contributor, tile end - 1) down to the tile's first splat."""
+    import numpy as np
+    W, H = cd["width"], cd["height"]
+    tx = (W + 15) // 16
+    T = tx * ((H + 15) // 16)
+    offs = eng.read("tile_offsets", np.uint32, T + 1).astype(np.int64)
+    fidx = eng.read("final_idx", np.int32, W * H).reshape(H, W).astype(np.int64)
+    y, x = np.mgrid[0:H, 0:W]
+    t = (y // 16) * tx + (x // 16)
+    s, e = offs[t], offs[t + 1]
+    return int(np.maximum(0, np.minimum(e - 1, fidx) - s + 1).sum())
+
+
+def write_checkpoint(path, model, step, adam_steps):
+    """A checkpoint in the reference's format (core/src/model.cpp:698-843) of
+    the model with zeroed Adam moments at the given iteration: how the public
+    trainer resumes a run (msplat_trainer_load_checkpoint)."""
+    import struct
+    import numpy as np
+    from msplat_gb300.schedule import LR_INIT
+    n = model.n
+    with open(path, "wb") as f:
+        f.write(struct.pack("<6I", 0x4C50534D, 1, step, n, 3, adam_steps))
+        f.write(np.asarray(LR_INIT, np.float32).tobytes() + struct.pack("<2f", 0.00016, 0.0000016))
+        arrays = list(model.arrays())
+        for block in (arrays, [np.zeros_like(a) for a in arrays], [np.zeros_like(a) for a in arrays]):
+            for g, a in enumerate(block):
+                shape = [n, 15, 3] if g == 4 else ([n, 1] if g == 5 else [n, a.shape[1]])
+                data = np.ascontiguousarray(a, np.float32).tobytes()
+                f.write(struct.pack("<I", len(shape)) + struct.pack(f"<{len(shape)}q", *shape))
+                f.write(struct.pack("<Q", len(data)) + data)
+
+
+def run_trainer_e2e(sc, model, gts_host, steps):
+    """Iterations/s of msplat_trainer_step, the reference's public API, at the
+    headline workload: the 1M model resumed at iteration 3001 from a
+    checkpoint, the bench's 8 views in the trainer's own shuffled order, its
+    learning-rate schedule and MCMC relocation every 100 steps (rounds fall
+    in the timed region), wall clock from the first step to the device's
+    completion of the last."""
+    import time
+    import numpy as np
+    from msplat_gb300 import api as A
+    imgs = [g.numpy() for g in gts_host]
+    ds = A.Dataset.from_arrays(sc.train_cams, imgs, model.means[:4096], np.zeros((4096, 3), np.uint8))
+    t = A.GaussianTrainer(ds, A.TrainingConfig(iterations=30000, cap_max=model.n, bg_color=[0.0, 0.0, 0.0]))
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "resume.ckpt")
+        write_checkpoint(path, model, 3000, 3000)
+        assert t.load_checkpoint(path) == 3000
+    for _ in range(5):          # warm-up: uploads, graph capture of each camera
+        t.step()
+    A.sync()
+    rounds0 = t.mcmc_stats()["rounds"]
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        t.step()
+    A.sync()
+    sec = time.perf_counter() - t0
+    return {"value": steps / sec, "unit": "iters/s", "steps": steps, "api": "msplat_trainer_step",
+            "mcmc_rounds_timed": t.mcmc_stats()["rounds"] - rounds0, "gaussians": t.splat_count,
+            "workload": "1M Gaussians resumed at iteration 3001 (checkpoint), 8 views at 1297x840, MCMC every "
+                        "100 steps, the trainer's camera order and schedules"}
+
+
 BATCH_SIZES = [(1297, 840), (979, 546), (648, 420), (2594, 1680)] * 2
 
 
@@ -417,12 +503,23 @@ def run_engine(args):
         raise RuntimeError("non-finite loss in the end-to-end run")
     e2e = {"value": R.job_rate(ws, args.steps, e2e_s), "unit": "iters/s",
            "h2d_bytes_per_step": int(gts_host[0].numel()), "d2h_bytes_per_step": 4}
+    # the same through the reference's public trainer API (msplat_trainer_step)
+    e2e_trainer = None
+    if not args.no_trainer:
+        try:
+            e2e_trainer = run_trainer_e2e(sc, model, gts_host, max(300, args.steps))
+        except Exception as ex:   # reported, never fatal to the throughput line
+            e2e_trainer = {"error": str(ex)[:200]}
 
     # per-stage times: CUDA events between the stages of eager steps (events
     # inside a step need it launched kernel by kernel)
     eng.set_timing(True)
+    pair_counts = []
     for k in range(min(args.steps, 20)):
-        one(args.warmup + 2 * args.steps + k, False)
+        step_k = args.warmup + 2 * args.steps + k
+        one(step_k, False)
+        eng.synchronize()
+        pair_counts.append(backward_pairs(eng, cams[step_k % len(cams)]))
     eng.synchronize()
     st = eng.stats()
     eng.set_timing(False)
@@ -444,6 +541,20 @@ def run_engine(args):
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_kind": kind, "traffic": traffic,
                 "algorithmic_bytes": alg, "ms": stage_ms[dom]}
+    # the rasterizer backward is bound by its FP32 issue, not by HBM: its
+    # FP32-pipe fraction from the (pixel, splat) pairs the reference's
+    # algorithm walks (from each pixel's last contributor down to its tile's
+    # first splat, rasterize_backward_kernel) x 60 FP32 operations
+    try:
+        pairs = float(np.mean(pair_counts))
+        props = torch.cuda.get_device_properties(local)
+        fp32_peak = props.multi_processor_count * 128 * 2 * sm_max_mhz() * 1e6 / 1e12
+        flops = 60.0 * pairs / (stage_ms["raster_bwd"] / 1e3) / 1e12
+        roofline["fp32"] = {"kernel": "raster_bwd", "pairs": pairs, "flops_per_pair": 60,
+                            "achieved": flops, "peak": fp32_peak, "unit": "TFLOP/s", "frac": flops / fp32_peak,
+                            "peak_kind": "nominal: SMs x 128 FP32 lanes x 2 x max SM clock"}
+    except Exception as ex:   # reported, never fatal to the throughput line
+        roofline["fp32"] = {"error": str(ex)[:200]}
 
     batched = None
     if not args.no_batched:
@@ -458,6 +569,7 @@ def run_engine(args):
            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_dict(args),
            "roofline": roofline, "stage_ms": stage_ms, "num_intersections": int(st.num_intersections),
            "max_tile_count": int(st.max_tile_count), "gpu_launches": int(launches), "e2e": e2e,
+           "e2e_trainer": e2e_trainer,
            "cuda_graph": True, "tuning": tuned, "autotune_step_ms": tuned_ms, "batched": batched,
            "clocks": clk.summary()}
     if rank == 0 and not args.no_time_to_psnr:
@@ -486,6 +598,13 @@ def run_engine(args):
                 "proposal_forecast_mse": [ps["learned"].get("proposal") for ps in per_seed]}
         except Exception as ex:   # reported, never fatal to the throughput line
             out["time_to_psnr"] = {"error": str(ex)[:200]}
+    if rank == 0 and not args.no_full_run:
+        try:
+            from msplat_gb300 import full_run
+            eng.close()
+            out["full_run"] = full_run.run()
+        except Exception as ex:   # reported, never fatal to the throughput line
+            out["full_run"] = {"error": str(ex)[:200]}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(model, sc.train_cams[0], gts_host[0].numpy(), steps=args.cpu_steps)
     if rank == 0:
@@ -498,7 +617,7 @@ def run_engine(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=4)
@@ -506,6 +625,10 @@ def main():
     ap.add_argument("--no-time-to-psnr", action="store_true",
                     help="skip the learned-vs-plain relocation time-to-PSNR runs")
     ap.add_argument("--no-batched", action="store_true", help="skip the multi-view (8 views per step) measurement")
+    ap.add_argument("--no-trainer", action="store_true", help="skip the public-API (msplat_trainer_step) measurement")
+    ap.add_argument("--no-full-run", action="store_true",
+                    help="skip the full configuration's run: 7000 iterations from 100k random points to the 1M cap, "
+                         "held-out PSNR/SSIM over 20 views (msplat_gb300.full_run)")
     ap.add_argument("--no-autotune", action="store_true", help="time the default launch configuration")
     ap.add_argument("--tuning", default="", help="fixed launch configuration instead of the autotuner, "
                                                  "e.g. tile_order=1,sort_width=512")
