@@ -132,13 +132,22 @@ __device__ __forceinline__ void pixel_step(PixelState &ps, float dx, float dy, f
     v8 = kAdd ? v8 + c[8] : c[8];
 }
 
-// sigma and alpha exactly as the forward pass rounds them (no contraction),
-// so both passes take the same splats; false when the pixel does not take it
+// sigma exactly as the forward pass rounds it (no contraction) and alpha from
+// the hardware exponential (ex2.approx: within 6e-7 relative for sigma in
+// [0, 5.55)); where that alpha lies within 4e-6 relative of a decision the
+// forward takes (alpha >= 1/255, the 0.999 clamp), alpha is recomputed with
+// the forward's own exponential, so both passes take the same splats and
+// clamp the same ones.  Elsewhere alpha differs from the forward's by at most
+// 6e-7 relative, which only enters the gradients and the transmittance
+// reconstruction.  false when the pixel does not take the splat.
 __device__ __forceinline__ bool splat_alpha(const float4 &xo, const float4 &cn, float dx, float dy, float &alpha) {
     const float sigma = __fmaf_rn(0.5f, __fmaf_rn(cn.x, __fmul_rn(dx, dx), __fmul_rn(__fmul_rn(cn.z, dy), dy)),
                                   __fmul_rn(__fmul_rn(cn.y, dx), dy));
     if (!(sigma >= 0.f && sigma < 5.55f)) return false;   // NaN fails too
-    alpha = fminf(0.999f, __fmul_rn(xo.z, det_expf_neg(-sigma)));
+    float a = __fmul_rn(xo.z, __expf(-sigma));
+    if (fabsf(a - 1.f / 255.f) <= 4e-6f * (1.f / 255.f) || fabsf(a - 0.999f) <= 4e-6f)
+        a = __fmul_rn(xo.z, det_expf_neg(-sigma));
+    alpha = fminf(0.999f, a);
     return !(alpha < 1.f / 255.f);
 }
 

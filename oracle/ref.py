@@ -2,8 +2,10 @@
 
 The library is the reference's own Metal source for the per-Gaussian stages
 (projection + SH, projection backward + SH Adam, Adam, SGLD, regularizer,
-tile rectangle, sort key, active test, SSIM window), compiled as host C++ by
-oracle/ref_build.py from the reference tree.  It exists only where the
+tile rectangle, sort key, active test, SSIM window) and the pixel stages
+(count and scatter of the tile intersections, monolithic and chunked
+rasterizers, SSIM + L1 loss), compiled as host C++ by oracle/ref_build.py
+from the reference tree (threadgroups on host threads).  It exists only where the
 reference tree does (the build container); the GPU machine never has it.  Only
 tests/ and tests/golden/make_ref_vectors.py use it, to pin the oracle.
 """
@@ -140,13 +142,14 @@ def gauss_1d():
 
 
 def raster_step(fwd, opacities, cam, gt=None, mask=None, v_img=None, background=(0.0, 0.0, 0.0), ssim_weight=0.2,
-                loss_inv_n=None, ids_capacity=None):
-    """The pixel stages of one monolithic step of one view from the
-    reference's kernels (count, scatter, forward raster, SSIM + L1 loss,
-    backward raster; the sort and pack restated): lists, image, final
-    transmittance and last contributors, loss sum, dL/dimage and the
-    per-Gaussian rasterizer gradients.  gt (uint8 [H,W,3]) runs the loss;
-    otherwise v_img is the image gradient."""
+                loss_inv_n=None, ids_capacity=None, k_max=1, chunk_size=512):
+    """The pixel stages of one step of one view from the reference's kernels
+    (count, scatter, forward raster, SSIM + L1 loss, backward raster; the sort
+    and pack restated): lists, image, final transmittance and last
+    contributors, loss sum, dL/dimage and the per-Gaussian rasterizer
+    gradients.  gt (uint8 [H,W,3]) runs the loss; otherwise v_img is the image
+    gradient.  k_max > 1: the chunked rasterizers with k_max chunks of
+    chunk_size splats (the caller applies the reference's K rule)."""
     W, H = int(cam["width"]), int(cam["height"])
     n = fwd["radii"].shape[0]
     T = ((W + 15) // 16) * ((H + 15) // 16)
@@ -171,7 +174,7 @@ def raster_step(fwd, opacities, cam, gt=None, mask=None, v_img=None, background=
         C.c_float(ssim_weight), C.c_float(loss_inv_n if loss_inv_n is not None else 1.0 / (3.0 * W * H)),
         _p(o["tile_bins"], IP), _p(o["gaussian_ids"], IP), C.c_longlong(cap), _p(o["out_img"]), _p(o["final_Ts"]),
         _p(o["final_idx"], IP), _p(o["loss_sum"]), _p(o["v_rendered"]), _p(o["v_xy"]), _p(o["v_conic"]),
-        _p(o["v_colors"]), _p(o["v_opacity"]), _p(o["nan_counts"], UP))
+        _p(o["v_colors"]), _p(o["v_opacity"]), _p(o["nan_counts"], UP), int(k_max), int(chunk_size))
     if m < 0:
         raise RuntimeError("more intersections than ids_capacity")
     o["num_isect"] = int(m)

@@ -26,7 +26,11 @@ Left out on purpose, with the reason:
     hybrid_sort_pack_kernel): their 1024-thread bitonic networks are not
     emulated; ref_kernels.cpp restates what they compute (exclusive scans of
     the padded and exact counts, ascending keys per tile, the pack gates);
-  * the chunked rasterizer (used below 400 tiles), not compiled yet.
+  * the chunked backward (compute_chunk_prefix_suffix_kernel,
+    rasterize_backward_chunked_kernel): lanes whose pixel has no contributor
+    in a chunk return before the kernel's SIMD-group broadcasts from lane 0,
+    so its result is undefined when lane 0 is one of them (after a chunked
+    forward only the forward stages and the loss are compared).
 
 The rasterizers and the SSIM kernels use threadgroup memory, barriers and
 SIMD-group functions; metal_shim.h runs their threadgroups on host threads.
@@ -97,6 +101,11 @@ KERNELS = {
                                   "packed_conic", "packed_rgb", "background", "final_Ts", "final_index", "v_output",
                                   "v_xy", "v_conic", "v_rgb", "v_opacity", "tile_range", "gp", "blockIdx", "tr",
                                   "warp_size", "wr"],
+    "rasterize_forward_chunked_kernel": ["tile_bounds", "img_size", "channels", "tile_bins", "packed_xy_opac",
+                                         "packed_conic", "packed_rgb", "chunk_T", "chunk_C", "chunk_final_idx",
+                                         "chunk_size", "K_max", "blockDim", "nan_counts", "blockIdx", "tr"],
+    "rasterize_forward_merge_kernel": ["num_pixels", "K_max", "chunk_T", "chunk_C", "chunk_final_idx", "final_Ts",
+                                       "final_index", "out_img", "background", "img_size", "gp"],
     "ssim_h_fwd_kernel": ["rendered", "gt", "img_size", "ssim_h_buf", "gid", "lid", "tr", "tgid"],
     "ssim_fused_v_fwd_h_bwd_kernel": ["rendered", "gt", "ssim_h_buf", "img_size", "ssim_weight", "inv_n",
                                       "deriv_h_buf", "loss_sum", "nan_counts", "mask", "has_mask", "gid", "lid", "tr",

@@ -102,6 +102,20 @@ void k_raster_bwd(uint3 &tile_bounds, uint2 &img_size, int32_t *gaussian_ids_sor
 #include "k_rasterize_backward_kernel.inc"
 }
 
+// rasterize_forward_chunked_kernel (msplat_metal.metal:2960-3076)
+void k_raster_fwd_chunked(uint3 &tile_bounds, uint3 &img_size, uint &channels, int *tile_bins, float *packed_xy_opac,
+                          float *packed_conic, float *packed_rgb, float *chunk_T, float *chunk_C, int *chunk_final_idx,
+                          uint &chunk_size, uint &K_max, uint2 &blockDim, atomic_uint *nan_counts, uint3 blockIdx,
+                          uint tr) {
+#include "k_rasterize_forward_chunked_kernel.inc"
+}
+
+// rasterize_forward_merge_kernel (msplat_metal.metal:3081-3134)
+void k_raster_merge(uint &num_pixels, uint &K_max, float *chunk_T, float *chunk_C, int *chunk_final_idx,
+                    float *final_Ts, int *final_index, float *out_img, float *background, uint2 &img_size, uint2 gp) {
+#include "k_rasterize_forward_merge_kernel.inc"
+}
+
 // ssim_h_fwd_kernel (msplat_metal.metal:3388-3450)
 void k_ssim_h_fwd(float *rendered, uchar *gt, uint2 &img_size, float *ssim_h_buf, uint2 gid, uint2 lid, uint tr,
                   uint2 tgid) {
@@ -268,8 +282,11 @@ void ref_pad_count(int n, const uint32_t *c, uint32_t *out) {
     for (int i = 0; i < n; i++) out[i] = pad_count(c[i]);
 }
 
-// The pixel stages of one monolithic training step of one view, as the
-// reference runs them (msplat_metal.mm:1255-1400): count and scatter of the
+// The pixel stages of one training step of one view, as the reference runs
+// them (msplat_metal.mm:1255-1400), the forward monolithic (k_max <= 1) or
+// chunked in k_max chunks of chunk_size splats with the merge (the caller
+// applies the reference's K rule, msplat_metal.mm:1204-1224): count and
+// scatter of the
 // tile intersections (compiled kernels), the per-tile sort and pack
 // (restated: hybrid_sort_pack_kernel sorts each tile's keys ascending and
 // packs (x, y, sigmoid(opacity)), conic and raw colour by id, a non-finite
@@ -283,7 +300,8 @@ long long ref_raster_step(int n, const float *xys, const float *depths, const in
                           const float background[3], const uint8_t *gt, const uint8_t *mask, float ssim_weight,
                           float loss_inv_n, int *tile_bins_out, int *gaussian_ids, long long ids_capacity,
                           float *out_img, float *final_Ts, int *final_idx, float *loss_sum, float *v_rendered,
-                          float *v_xy, float *v_conic, float *v_colors, float *v_opacity, uint32_t nan_counts[16]) {
+                          float *v_xy, float *v_conic, float *v_colors, float *v_opacity, uint32_t nan_counts[16],
+                          int k_max, int chunk_size) {
     const uint W = (uint)width, H = (uint)height;
     uint3 tile_bounds((W + 15) / 16, (H + 15) / 16, 1u);
     const uint T = tile_bounds.x * tile_bounds.y;
@@ -343,11 +361,34 @@ long long ref_raster_step(int n, const float *xys, const float *depths, const in
     uint2 block(8u, 8u);
     float bg[3] = {background[0], background[1], background[2]};
     const int gx = (int)((W + 7) / 8), gy = (int)((H + 7) / 8);
-    run_groups(gx, gy, 8, 8, [&](int bx, int by, int tx, int ty, int t) {
-        k_raster_fwd(tile_bounds, img3, channels, bins.data(), pk_xyo.data(), pk_con.data(), pk_rgb.data(), final_Ts,
-                     final_idx, out_img, bg, block, all, uint2((uint)bx, (uint)by), uint2((uint)tx, (uint)ty),
-                     (uint)t);
-    });
+    const uint P = W * H;
+    uint K = (uint)std::max(1, k_max), chunk = (uint)std::max(1, chunk_size);
+    std::vector<float> cT, cC;
+    std::vector<int> cI;
+    if (K <= 1) {
+        run_groups(gx, gy, 8, 8, [&](int bx, int by, int tx, int ty, int t) {
+            k_raster_fwd(tile_bounds, img3, channels, bins.data(), pk_xyo.data(), pk_con.data(), pk_rgb.data(),
+                         final_Ts, final_idx, out_img, bg, block, all, uint2((uint)bx, (uint)by),
+                         uint2((uint)tx, (uint)ty), (uint)t);
+        });
+    } else {
+        // chunked (msplat_metal.mm:1285-1307): one grid layer per chunk, then the merge per pixel
+        cT.assign((size_t)K * P, 1.f);
+        cC.assign((size_t)K * P * 3, 0.f);
+        cI.assign((size_t)K * P, -1);
+        for (uint k = 0; k < K; k++)
+            run_groups(gx, gy, 8, 8, [&](int bx, int by, int, int, int t) {
+                k_raster_fwd_chunked(tile_bounds, img3, channels, bins.data(), pk_xyo.data(), pk_con.data(),
+                                     pk_rgb.data(), cT.data(), cC.data(), cI.data(), chunk, K, block, nan_counts,
+                                     uint3((uint)bx, (uint)by, k), (uint)t);
+            });
+        uint2 isz2(W, H);
+        uint npx = P;
+        for (uint y = 0; y < H; y++)
+            for (uint x = 0; x < W; x++)
+                k_raster_merge(npx, K, cT.data(), cC.data(), cI.data(), final_Ts, final_idx, out_img, bg, isz2,
+                               uint2(x, y));
+    }
     uint2 isz(W, H);
     if (gt) {
         // the loss: three kernels over 16x16 threadgroups
@@ -375,13 +416,21 @@ long long ref_raster_step(int n, const float *xys, const float *depths, const in
     std::fill(v_conic, v_conic + 3 * (size_t)n, 0.f);
     std::fill(v_colors, v_colors + 3 * (size_t)n, 0.f);
     std::fill(v_opacity, v_opacity + (size_t)n, 0.f);
-    std::vector<int> gids(gaussian_ids, gaussian_ids + M);
-    run_groups(gx, gy, 8, 8, [&](int bx, int by, int tx, int ty, int t) {
-        k_raster_bwd(tile_bounds, isz, gids.data(), bins.data(), pk_xyo.data(), pk_con.data(), pk_rgb.data(), bg,
-                     final_Ts, final_idx, v_rendered, v_xy, v_conic, v_colors, v_opacity, all,
-                     uint3((uint)(bx * 8 + tx), (uint)(by * 8 + ty), 0u), uint3((uint)bx, (uint)by, 0u), (uint)t, 32u,
-                     (uint)(t % 32));
-    });
+    std::vector<int> gids(gaussian_ids, gaussian_ids + std::max<long long>(M, 1));
+    // The monolithic backward.  After a chunked forward no backward runs:
+    // rasterize_backward_chunked_kernel is not compiled (lanes whose pixel
+    // has no contributor in a chunk return before its SIMD-group broadcasts
+    // from lane 0, .metal:3245-3247 and 3285-3294, whose value is undefined on
+    // the GPU when lane 0 is one of them), and the monolithic walk is not its
+    // equal (a chunk that saturates locally skips its remaining splats while
+    // later chunks still composite).  The gradients stay zero.
+    if (K <= 1)
+        run_groups(gx, gy, 8, 8, [&](int bx, int by, int tx, int ty, int t) {
+            k_raster_bwd(tile_bounds, isz, gids.data(), bins.data(), pk_xyo.data(), pk_con.data(), pk_rgb.data(), bg,
+                         final_Ts, final_idx, v_rendered, v_xy, v_conic, v_colors, v_opacity, all,
+                         uint3((uint)(bx * 8 + tx), (uint)(by * 8 + ty), 0u), uint3((uint)bx, (uint)by, 0u), (uint)t,
+                         32u, (uint)(t % 32));
+        });
     return M;
 }
 

@@ -4,7 +4,7 @@ own per-Gaussian Metal code (projection + SH, projection backward + SH Adam,
 regularizer, Adam, SGLD), compiled as host C++ by oracle/ref_build.py from the
 reference tree, on 512 random Gaussians at step 3001; and
 tests/golden/ref_pixel_vectors.npz: the outputs of its pixel stages (tile
-lists, forward rasterizer, SSIM + L1 loss, backward rasterizer) on the small
+lists, forward rasterizers, SSIM + L1 loss, monolithic backward rasterizer) on the small
 views of tests/test_ref_pin.py (their inputs are regenerated from seeds) —
 the vectors tests/test_ref_pin.py holds the oracle to where the reference
 tree is absent.  Needs the reference tree (default /root/reference,
@@ -57,9 +57,14 @@ def main():
         cam, g, gt, mask, bg = pixel_case(name)
         st = step_scalars(3001, 3001, width=cam["width"], height=cam["height"])
         fwd = R.project_fwd(g, cam, 3)
-        o = R.raster_step(fwd, g.opacities, cam, gt=gt, mask=mask, background=bg, loss_inv_n=st["loss_inv_n"])
-        for k in ("num_isect", "gaussian_ids", "tile_bins", "out_img", "final_Ts", "final_idx", "loss", "v_rendered",
-                  "v_xy", "v_conic", "v_colors", "v_opacity"):
+        k = O.train_step(32, g.copy(), cam, st, gt=gt, mask=mask, background=bg, raster_mode=PIXEL_CASES[name][-1],
+                         do_backward=False, do_optimizer=False, want_ids=False)["k_max"]
+        o = R.raster_step(fwd, g.opacities, cam, gt=gt, mask=mask, background=bg, loss_inv_n=st["loss_inv_n"],
+                          k_max=k)
+        keys = ["num_isect", "gaussian_ids", "tile_bins", "out_img", "final_Ts", "final_idx", "loss", "v_rendered"]
+        if PIXEL_CASES[name][-1] == 1:   # the chunked backward is not compiled
+            keys += ["v_xy", "v_conic", "v_colors", "v_opacity"]
+        for k in keys:
             pix[f"{name}/{k}"] = np.asarray(o[k])
     path = os.path.join(HERE, "ref_pixel_vectors.npz")
     np.savez_compressed(path, **pix)

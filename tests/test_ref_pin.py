@@ -6,7 +6,9 @@ the bodies of project_and_sh_forward_kernel, project_and_sh_backward_kernel
 (with its fused SH Adam), fused_adam_kernel, sgld_noise_gen/sgld_noise_kernel,
 mcmc_reg_grad_kernel, count_intersections_kernel and
 scatter_intersections_kernel, and - threadgroups run on host threads - the
-forward rasterizer, the three SSIM + L1 kernels and the backward rasterizer.
+monolithic and chunked forward rasterizers with the merge, the three SSIM +
+L1 kernels and the backward rasterizer (the chunked backward is not
+compiled: see oracle/ref_build.py).
 
 Per-Gaussian stages, bit for bit against the oracle's float path: projection
 (centres, depths, radii, conics, tiles hit, colours, extents), the tile
@@ -14,9 +16,10 @@ rectangles, sort keys and active test that order every per-tile list, the
 SSIM window, and, from the same rasterizer gradients, the projection VJPs,
 the SH Adam, regularizer, Adam and SGLD updates of every parameter and moment.
 Pixel stages: per-tile lists, image, final transmittance, last contributors
-and dL/dimage bit for bit, the loss within 1e-6 and the rasterizer gradients
-within 1e-6 (the reference sums them with atomics), the whole step's updates
-within 1e-5.  exp() is the same function on both sides (the oracle's
+and dL/dimage bit for bit (monolithic, and chunked with the reference's K
+rule), the loss within 1e-6; after the monolithic forward the rasterizer
+gradients within 1e-6 (the reference sums them with atomics) and the whole
+step's updates within 1e-5.  exp() is the same function on both sides (the oracle's
 det_expf; Metal's exp has no published bits).
 
 Two parts:
@@ -185,16 +188,18 @@ def test_golden_vectors():
 
 
 PIXEL_CASES = {
-    # width, height, Gaussians, seed, mask, background
-    "plain": (48, 32, 300, 3, False, (0.0, 0.0, 0.0)),
-    "ragged_mask_bg": (50, 34, 350, 4, True, (0.25, 0.5, 0.75)),
+    # width, height, Gaussians, seed, mask, background, raster mode (1: monolithic, 0: the
+    # reference's rule, which takes the chunked rasterizer below 400 tiles)
+    "plain": (48, 32, 300, 3, False, (0.0, 0.0, 0.0), 1),
+    "ragged_mask_bg": (50, 34, 350, 4, True, (0.25, 0.5, 0.75), 1),
+    "chunked": (40, 32, 1800, 5, True, (0.1, 0.2, 0.3), 0),
 }
 
 
 def pixel_case(name):
     """A small view (several 64-splat batches per tile), its target and
     optional mask; the Gaussians include a NaN colour (zombie gate)."""
-    W, H, n, seed, with_mask, bg = PIXEL_CASES[name]
+    W, H, n, seed, with_mask, bg, _ = PIXEL_CASES[name]
     cam = ring_camera(W, H, 0.8 * W, k=2)
     g = S.gaussians(n, seed)
     g.features_dc[7] = np.nan
@@ -208,15 +213,16 @@ def pixel_case(name):
     return cam, g, gt, mask, bg
 
 
-def check_pixel_path(r, o):
-    """The oracle's float path (r) against the reference kernels' pixel stages (o)."""
+def check_pixel_path(r, o, backward=True):
+    """The oracle's float path (r) against the reference kernels' pixel stages
+    (o); the rasterizer gradients only when the reference's backward ran."""
     assert r["num_isect"] == o["num_isect"]
     assert np.array_equal(r["gaussian_ids"], o["gaussian_ids"])
     assert np.array_equal(r["tile_bins"], o["tile_bins"])
     for k in ("out_img", "final_Ts", "final_idx", "v_rendered"):
         assert np.array_equal(r[k], o[k]), k
     assert abs(r["loss"] - o["loss"]) <= 1e-6 * abs(r["loss"])
-    for k in ("v_xy", "v_conic", "v_colors", "v_opacity"):
+    for k in ("v_xy", "v_conic", "v_colors", "v_opacity") if backward else ():
         e = np.linalg.norm((r[k] - o[k]).ravel()) / np.linalg.norm(o[k].ravel())
         assert e <= 1e-6, (k, e)
 
@@ -235,13 +241,17 @@ def test_live_pixel_path(ref_lib, name):
     mom = ([np.zeros_like(a) for a in g.arrays()], [np.zeros_like(a) for a in g.arrays()])
     g_o = g.copy()
     mom_o = ([a.copy() for a in mom[0]], [a.copy() for a in mom[1]])
-    r = O.train_step(32, g_o, cam, step, moments=mom_o, gt=gt, mask=mask, background=bg, raster_mode=1,
+    mode = PIXEL_CASES[name][-1]
+    r = O.train_step(32, g_o, cam, step, moments=mom_o, gt=gt, mask=mask, background=bg, raster_mode=mode,
                      do_sgld=True)
     fwd = ref_lib.project_fwd(g, cam, 3)
     o = ref_lib.raster_step(fwd, g.opacities, cam, gt=gt, mask=mask, background=bg,
-                            loss_inv_n=step["loss_inv_n"])
-    assert int(np.diff(o["tile_bins"], axis=1).max()) > 128
-    check_pixel_path(r, o)
+                            loss_inv_n=step["loss_inv_n"], k_max=r["k_max"])
+    assert int(np.diff(o["tile_bins"], axis=1).max()) > (512 if mode == 0 else 128)
+    assert (r["k_max"] > 2) == (mode == 0)
+    check_pixel_path(r, o, backward=mode == 1)
+    if mode != 1:   # the reference's chunked backward is not compiled (oracle/ref_build.py)
+        return
     g_r = g.copy()
     ref_lib.step_after_raster(g_r, mom, cam, step, o["raster_grads"], fwd)
     for name_, a, b, before in zip(GROUPS, g_o.arrays(), g_r.arrays(), g.arrays()):
@@ -257,9 +267,9 @@ def test_golden_pixel_vectors():
     for name in PIXEL_CASES:
         cam, g, gt, mask, bg = pixel_case(name)
         step = step_scalars(3001, 3001, width=cam["width"], height=cam["height"])
-        r = O.train_step(32, g.copy(), cam, step, gt=gt, mask=mask, background=bg, raster_mode=1,
-                         do_optimizer=False)
+        r = O.train_step(32, g.copy(), cam, step, gt=gt, mask=mask, background=bg,
+                         raster_mode=PIXEL_CASES[name][-1], do_optimizer=False)
         o = {k[len(name) + 1:]: z[k] for k in z.files if k.startswith(name + "/")}
         o["num_isect"] = int(o["num_isect"])
         o["loss"] = float(o["loss"])
-        check_pixel_path(r, o)
+        check_pixel_path(r, o, backward=PIXEL_CASES[name][-1] == 1)
