@@ -181,7 +181,18 @@ class Engine {
         if (P > (1LL << 31) / 16) throw std::runtime_error("views too large for one step");
         const long long legacy = std::max<long long>(48LL * N * B, 1);   // msplat_metal.mm:1142 legacy capacity, per view
         const MsplatTuning tune = tuning_;
-        const int K = choose_k(args[0], T, legacy, tune);
+        // each view's depth chunks from its own tiles, mode and the one-view
+        // capacity (as the reference, which steps one view at a time); the
+        // raster launches cover runs of consecutive views with the same K
+        int Kv[kMaxViews];
+        int K = 1;
+        for (int v = 0; v < B; v++) {
+            Kv[v] = choose_k(args[v], vt.tile_base[v + 1] - vt.tile_base[v], std::max<long long>(48LL * N, 1), tune);
+            K = std::max(K, Kv[v]);
+        }
+        const std::vector<RasterRun> runs = raster_runs(vt, Kv);
+        long long chunk_entries = 0;
+        for (const RasterRun &r : runs) chunk_entries += r.k > 1 ? r.k * (vt.pix_base[r.v1] - vt.pix_base[r.v0]) : 0;
         // fixed intersection budget (monolithic raster only, as in the
         // reference): a view that does not fit is rastered in tile groups
         const bool fixed = isect_slots_ > 0 && K == 1;
@@ -191,7 +202,7 @@ class Engine {
         ensure_tiles(T);
         ensure_isect(cap);
         ensure_pixels(P);
-        if (K > 1) ensure_chunks((long long)K * P);
+        if (chunk_entries > 0) ensure_chunks(chunk_entries);
         last_T_ = T;
         last_K_ = K;
         last_views_ = B;
@@ -238,11 +249,13 @@ class Engine {
         // projection, the tile-mapping and loss launches (counted where they
         // are issued), raster (+ merge when chunked), and for training raster
         // backward (+ prefix/suffix), projection backward, Adam, SGLD
-        launches_ += 1 + (K > 1 ? 2 : 1);
+        long long raster_launches = 0;
+        for (const RasterRun &r : runs) raster_launches += r.k > 1 ? 2 : 1;
+        launches_ += 1 + raster_launches;
         // (the one-view projection backward is two launches with the optimizer:
         // the VJP, then the SH Adam walk)
         if (has_gt && backward)
-            launches_ += (K > 1 ? 2 : 1) + 1 + (opt && B == 1 ? 1 : 0) + (opt ? 1 : 0) + (a0.do_sgld ? 1 : 0);
+            launches_ += raster_launches + 1 + (opt && B == 1 ? 1 : 0) + (opt ? 1 : 0) + (a0.do_sgld ? 1 : 0);
         CK(cudaMemsetAsync(ptr<uint32_t>("tile_counts"), 0, sizeof(uint32_t) * 2 * (size_t)T, stream_));
         CK(cudaMemsetAsync(ptr<float>("loss_sum"), 0, sizeof(float) * B, stream_));
 
@@ -312,18 +325,33 @@ class Engine {
         ra.sp = pa.sp; ra.tile_offsets = ta.tile_offsets; ra.isect_ids = ta.isect_ids;
         ra.n = (uint32_t)((long long)N * B); ra.rec = pa.rec;
         ra.out_img = ptr<float>("out_img"); ra.final_T = ptr<float>("final_T"); ra.final_idx = ptr<int>("final_idx");
-        if (K > 1) {
-            ra.chunk_T = ptr<float>("chunk_T"); ra.chunk_C = ptr<float>("chunk_C"); ra.chunk_idx = ptr<int>("chunk_idx");
-            ra.prefix_T = ptr<float>("prefix_T"); ra.after_C = ptr<float>("after_C");
-        }
+        ra.chunk_p0 = 0; ra.chunk_P = P;
         ra.v_img = ptr<float>("v_img"); ra.grad = ptr<GradRec>("grad"); ra.nan_counts = pa.nan_counts;
         auto group_raster = [&](const TileGroup &gr) {
             RasterArgs rg = ra;
             rg.tile_lo = gr.lo; rg.num_tiles = gr.hi - gr.lo; rg.isect_lo = gr.base;
             return rg;
         };
+        // one run's launch: its tiles, its K, its slice of the chunk buffers
+        long long chunk_off = 0;
+        std::vector<RasterArgs> run_args;
+        for (const RasterRun &r : runs) {
+            RasterArgs rr = ra;
+            rr.tile_lo = vt.tile_base[r.v0];
+            rr.num_tiles = vt.tile_base[r.v1] - vt.tile_base[r.v0];
+            rr.k_max = r.k;
+            rr.chunk_p0 = vt.pix_base[r.v0];
+            rr.chunk_P = vt.pix_base[r.v1] - vt.pix_base[r.v0];
+            if (r.k > 1) {
+                rr.chunk_T = ptr<float>("chunk_T") + chunk_off; rr.chunk_C = ptr<float>("chunk_C") + 3 * chunk_off;
+                rr.chunk_idx = ptr<int>("chunk_idx") + chunk_off;
+                rr.prefix_T = ptr<float>("prefix_T") + chunk_off; rr.after_C = ptr<float>("after_C") + 3 * chunk_off;
+                chunk_off += (long long)r.k * rr.chunk_P;
+            }
+            run_args.push_back(rr);
+        }
         if (!fixed) {
-            launch_raster_fwd(ra, stream_);
+            for (const RasterArgs &rr : run_args) launch_raster_fwd(rr, stream_);
         } else {
             for (const TileGroup &gr : groups) {
                 build_group(gr);
@@ -332,7 +360,7 @@ class Engine {
             launches_ += (long long)groups.size() - 1;
         }
         debug_sync(stream_, "raster_fwd");
-        last_ra_ = ra;
+        last_ra_ = fixed ? ra : run_args[0];   // (backward_image: one view, one run)
         mark(3);
         if (!has_gt) { mark(4); mark(5); mark(6); mark(7); mark(8); return; }
 
@@ -349,7 +377,7 @@ class Engine {
         if (!backward) { mark(5); mark(6); mark(7); mark(8); return; }
 
         if (!fixed) {
-            launch_raster_bwd(ra, stream_);
+            for (const RasterArgs &rr : run_args) launch_raster_bwd(rr, stream_);
         } else {
             // one group: its lists are still in the buffer; several: each
             // group's lists are rebuilt (the same sorted order) for its backward
@@ -408,10 +436,11 @@ class Engine {
         if (graphable) {
             std::string ks;
             auto put = [&](const void *p, size_t n) { ks.append(reinterpret_cast<const char *>(p), n); };
-            const int head[5] = {N, B, K, g.rest_bases,
+            const int head[4] = {N, B, g.rest_bases,
                                  (a0.do_optimizer ? 1 : 0) | (a0.do_sgld ? 2 : 0) | (backward ? 4 : 0) | (st ? 8 : 0) |
                                      (has_gt ? 16 : 0)};
             put(head, sizeof(head));
+            put(Kv, sizeof(int) * B);
             put(&tune, sizeof(tune));
             put(w, sizeof(int) * B);
             put(h, sizeof(int) * B);
@@ -789,6 +818,21 @@ class Engine {
         }
         groups.push_back({lo, (int)counts.size(), base});
         return groups;
+    }
+
+    // Maximal runs of consecutive views with the same depth-chunk count:
+    // one raster launch (and merge / prefix-suffix) per run, so a batch of
+    // equal views is one launch per stage.
+    struct RasterRun {
+        int v0, v1, k;   // views [v0, v1), chunks per tile (1: monolithic)
+    };
+    static std::vector<RasterRun> raster_runs(const ViewTable &vt, const int *Kv) {
+        std::vector<RasterRun> runs;
+        for (int v = 0; v < vt.count; v++) {
+            if (!runs.empty() && runs.back().k == Kv[v]) runs.back().v1 = v + 1;
+            else runs.push_back({v, v + 1, Kv[v]});
+        }
+        return runs;
     }
 
     // K_max rule, msplat_metal.mm:1204-1224; a step in auto mode takes the

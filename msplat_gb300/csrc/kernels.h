@@ -100,7 +100,7 @@ struct TileArgs {
 
 struct RasterArgs {
     ViewTable vt;
-    int num_tiles, k_max;       // tiles of this launch; depth chunks (1 = monolithic)
+    int num_tiles, k_max;       // tiles of this launch; depth chunks of its views (1 = monolithic)
     int tile_lo;                // first global tile of this launch (tile group), 0 otherwise
     long long isect_lo;         // global intersection slot held at isect_ids[0]
     int chunk;                  // splats per depth chunk (chunked raster)
@@ -114,8 +114,12 @@ struct RasterArgs {
     const SplatRec *rec;        // projection records, gathered by id
     float *out_img, *final_T;
     int *final_idx;
+    // chunked raster: this launch's chunk buffers hold the pixels
+    // [chunk_p0, chunk_p0 + chunk_P) of its views, entry (k, p) at
+    // k * chunk_P + p - chunk_p0
     float *chunk_T, *chunk_C, *prefix_T, *after_C;
     int *chunk_idx;
+    long long chunk_p0, chunk_P;
     const float *v_img;
     GradRec *grad;
     unsigned *nan_counts;

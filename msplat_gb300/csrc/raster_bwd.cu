@@ -327,18 +327,18 @@ __global__ void __launch_bounds__(BwdLayout<kPx>::kThreads, kPx == 2 ? 8 : 6) k_
 
 __global__ void __launch_bounds__(256) k_chunk_prefix_suffix(RasterArgs a) {
     pdl_enter();
-    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long P = a.vt.pixels;
-    if (p >= P) return;
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;   // pixel of the launch's views
+    const long long P = a.chunk_P;
+    if (q >= P) return;
     float pT = 1.f;
     for (int k = 0; k < a.k_max; k++) {
-        const size_t o = (size_t)k * P + p;
+        const size_t o = (size_t)k * P + q;
         a.prefix_T[o] = pT;
         pT *= a.chunk_T[o];
     }
     float r = 0.f, g = 0.f, b = 0.f;
     for (int k = a.k_max - 1; k >= 0; k--) {
-        const size_t o = (size_t)k * P + p;
+        const size_t o = (size_t)k * P + q;
         a.after_C[3 * o] = r;
         a.after_C[3 * o + 1] = g;
         a.after_C[3 * o + 2] = b;
@@ -357,14 +357,14 @@ __global__ void __launch_bounds__(BwdLayout<kPx>::kThreads, kPx == 2 ? 8 : 6) k_
     const int s0 = clamp_off(a.tile_offsets[tile], a.isect_lo, a.capacity), e0 = clamp_off(a.tile_offsets[tile + 1], a.isect_lo, a.capacity);
     const int cs = s0 + k * a.chunk, ce = min(s0 + (k + 1) * a.chunk, e0);
     if (cs >= ce) return;
-    const size_t P = (size_t)a.vt.pixels;
+    const size_t P = (size_t)a.chunk_P;
     PixelState ps[kPx];
     float px = 0.f;
     int bmax = -1;
 #pragma unroll
     for (int r = 0; r < kPx; r++) {
         const BwdPixel tp = bwd_pixel<kViews, kPx>(a, tile, r);
-        const size_t o = (size_t)k * P + (size_t)tp.p;
+        const size_t o = (size_t)k * P + (size_t)(tp.p - a.chunk_p0);
         init_pixel(ps[r], a, tp, tp.inside ? a.prefix_T[o] * a.chunk_T[o] : 0.f, tp.inside ? a.after_C[3 * o] : 0.f,
                    tp.inside ? a.after_C[3 * o + 1] : 0.f, tp.inside ? a.after_C[3 * o + 2] : 0.f);
         const int bf = tp.inside ? a.chunk_idx[o] : -1;
@@ -384,8 +384,7 @@ template <int kBB, int kPx> static void raster_bwd_batch(const RasterArgs &a, cu
         if (views) launch_pdl(k_raster_bwd<true, kBB, kPx>, a.num_tiles, kT, 0, s, a);
         else launch_pdl(k_raster_bwd<false, kBB, kPx>, a.num_tiles, kT, 0, s, a);
     } else {
-        const long long P = a.vt.pixels;
-        launch_pdl(k_chunk_prefix_suffix, (unsigned)((P + 255) / 256), 256, 0, s, a);
+        launch_pdl(k_chunk_prefix_suffix, (unsigned)((a.chunk_P + 255) / 256), 256, 0, s, a);
         if (views) launch_pdl(k_raster_bwd_chunked<true, kBB, kPx>, dim3(a.num_tiles, a.k_max), kT, 0, s, a);
         else launch_pdl(k_raster_bwd_chunked<false, kBB, kPx>, dim3(a.num_tiles, a.k_max), kT, 0, s, a);
     }

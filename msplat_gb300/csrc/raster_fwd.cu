@@ -10,7 +10,7 @@
 // per-pixel arithmetic is the reference's, fused only where it writes fma(),
 // so the image is bit-identical to the oracle's float path.  One launch
 // covers the tiles of every view of the step (the view of a CTA is found from
-// its global tile index; chunk buffers are [K, pixels of all views]).
+// its global tile index; chunk buffers are [K, pixels of the launch's views]).
 #include "common.cuh"
 #include "kernels.h"
 
@@ -167,8 +167,7 @@ __global__ void __launch_bounds__(kTileThreads, 8) k_raster_fwd_chunked(RasterAr
     const TilePixel tp = tile_pixel<kViews>(a, tile);
     const int s0 = clamp_off(a.tile_offsets[tile], a.isect_lo, a.capacity), e0 = clamp_off(a.tile_offsets[tile + 1], a.isect_lo, a.capacity);
     const int cs = s0 + k * a.chunk, ce = min(s0 + (k + 1) * a.chunk, e0);
-    const size_t P = (size_t)a.vt.pixels;
-    const size_t o = (size_t)k * P + (size_t)tp.p();
+    const size_t o = (size_t)k * (size_t)a.chunk_P + (size_t)(tp.p() - a.chunk_p0);
     if (cs >= ce) {
         if (tp.inside) {
             a.chunk_T[o] = 1.f;
@@ -192,13 +191,14 @@ __global__ void __launch_bounds__(kTileThreads, 8) k_raster_fwd_chunked(RasterAr
 
 __global__ void __launch_bounds__(256) k_raster_merge(RasterArgs a) {
     pdl_enter();
-    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long P = a.vt.pixels;
-    if (p >= P) return;
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;   // pixel of the launch's views
+    const long long P = a.chunk_P;
+    if (q >= P) return;
+    const long long p = a.chunk_p0 + q;
     float Tr = 1.f, cr = 0.f, cg = 0.f, cb = 0.f;
     int last = -1, cut = a.k_max;
     for (int k = 0; k < a.k_max; k++) {
-        const size_t o = (size_t)k * P + p;
+        const size_t o = (size_t)k * P + q;
         const int cf = a.chunk_idx[o];
         if (cf < 0 && k > 0) break;
         cr = __fmaf_rn(a.chunk_C[3 * o], Tr, cr);
@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(256) k_raster_merge(RasterArgs a) {
         if (cf >= 0) last = cf;
         if (Tr <= 1e-4f) { cut = k + 1; break; }
     }
-    for (int k = cut; k < a.k_max; k++) a.chunk_idx[(size_t)k * P + p] = -1;
+    for (int k = cut; k < a.k_max; k++) a.chunk_idx[(size_t)k * P + q] = -1;
     const StepParams &sp = a.sp[a.vt.count > 1 ? view_of_pixel(a.vt, p) : 0];
     a.final_T[p] = Tr;
     a.final_idx[p] = last;
@@ -225,8 +225,7 @@ template <int kBatch> static void raster_fwd_batch(const RasterArgs &a, cudaStre
     } else {
         if (views) launch_pdl(k_raster_fwd_chunked<true, kBatch>, dim3(a.num_tiles, a.k_max), kTileThreads, 0, s, a);
         else launch_pdl(k_raster_fwd_chunked<false, kBatch>, dim3(a.num_tiles, a.k_max), kTileThreads, 0, s, a);
-        const long long P = a.vt.pixels;
-        launch_pdl(k_raster_merge, (unsigned)((P + 255) / 256), 256, 0, s, a);
+        launch_pdl(k_raster_merge, (unsigned)((a.chunk_P + 255) / 256), 256, 0, s, a);
     }
 }
 

@@ -1,6 +1,7 @@
 """Multi-view training step (msplat_engine_train_step_batch): views of
-different sizes go through one launch per stage and give one update from the
-mean of their gradients.  The batched forward is checked bit for bit against
+different sizes go through one launch per stage (the rasterizers: one per run
+of consecutive views with the same depth-chunk count, each view's count by the
+reference's rule) and give one update from the mean of their gradients.  The batched forward is checked bit for bit against
 one-view renders (records, per-tile sorted lists, images); the update against
 the oracle's per-view gradients (FP32 path) averaged and pushed through Adam
 in numpy with the engine's rules (GPU only)."""
@@ -43,15 +44,29 @@ def _mixed_views(sc):
             S.Camera(base[5].cam_to_world, 128, 96, 100.0, 100.0, 64.0, 48.0)]
 
 
-@pytest.mark.parametrize("raster_mode", [1, 2])
+def _mixed_mode_views(sc):
+    """Views whose own raster modes differ under the reference's rule: 130,
+    520, 256, 48 and 48 tiles (chunked with K = 71, monolithic, K = 36, then
+    two views with K = 192 that share one launch)."""
+    base = sc.train_cams
+    return [S.Camera(base[3].cam_to_world, 200, 150, 160.0, 160.0, 100.0, 75.0),
+            S.Camera(base[1].cam_to_world, 416, 320, 300.0, 300.0, 208.0, 160.0),
+            base[0],
+            S.Camera(base[5].cam_to_world, 128, 96, 100.0, 100.0, 64.0, 48.0),
+            S.Camera(base[6].cam_to_world, 128, 96, 100.0, 100.0, 64.0, 48.0)]
+
+
+@pytest.mark.parametrize("raster_mode", [1, 2, 0])
 def test_batch_forward_matches_single_views(raster_mode):
-    """One launch per stage over three views = three one-view renders: the
+    """One launch per stage over several views = one-view renders: the
     same radii and records, each view's tile lists equal to its own with the
     record ids offset by view * n (depth ties still ordered by Gaussian), and
-    the same image bits.  raster_mode 1: monolithic; 2: 512-splat chunks."""
+    the same image bits.  raster_mode 1: monolithic; 2: 512-splat chunks;
+    0: the reference's rule per view (msplat_metal.mm:1204-1224), on views
+    of both modes and several chunk counts in one batch."""
     torch = pytest.importorskip("torch")
     sc = S.config_small(4)
-    cams = _mixed_views(sc)
+    cams = _mixed_views(sc) if raster_mode else _mixed_mode_views(sc)
     init = S.init_from_gt(sc.gt, 4)
     n = init.n
     kw = dict(raster_mode=raster_mode, k_max=3 if raster_mode == 2 else 0, do_optimizer=False)
@@ -70,14 +85,18 @@ def test_batch_forward_matches_single_views(raster_mode):
     img = eng.read("out_img", np.float32, 3 * sum(Ps))
     radii = eng.read("radii", np.int32, B * n)
     rec = eng.read("rec", np.float32, B * n * 12)
-    assert eng.stats().check_record[0] == 0
+    st = eng.stats()
+    assert st.check_record[0] == 0
+    k_batch = st.k_max
     eng.close()
     t0 = p0 = 0
+    ks = []
     for v, c in enumerate(cams):
         e1 = E.Engine(0)
         dg1 = E.DeviceGaussians(init)
         e1.render(dg1, E.make_args(E.camera_dict(c), E.step_scalars(10, 10, width=c.width, height=c.height), **kw))
         e1.synchronize()
+        ks.append(e1.stats().k_max)
         o1 = e1.read("tile_offsets", np.uint32, Ts[v] + 1).astype(np.int64)
         i1 = e1.read("isect_ids", np.uint32, max(int(o1[-1]), 1))[:int(o1[-1])]
         np.testing.assert_array_equal(e1.read("radii", np.int32, n), radii[v * n:(v + 1) * n])
@@ -89,12 +108,15 @@ def test_batch_forward_matches_single_views(raster_mode):
         e1.close()
         t0 += Ts[v]
         p0 += Ps[v]
+    assert k_batch == max(ks)
+    if raster_mode == 0:
+        assert ks == [71, 1, 36, 192, 192], ks
 
 
 def test_batch_step_matches_oracle_mean_gradient():
     torch = pytest.importorskip("torch")
     sc = S.config_small(2)
-    cams = _mixed_views(sc)
+    cams = _mixed_mode_views(sc)
     gts = [gt_image(sc.gt, c) for c in cams]
     init = S.init_from_gt(sc.gt, 2)
     B = len(cams)
@@ -106,9 +128,9 @@ def test_batch_step_matches_oracle_mean_gradient():
     nb = {0: 0, 1: 3, 2: 8, 3: 15}[steps[0]["degrees_to_use"]]
     assert nb == 15
     cds = [E.camera_dict(c) for c in cams]
-    # SGLD off: deterministic reference; monolithic raster in both (the batch
-    # picks its raster mode from the tiles of all views, the oracle per view)
-    args = [E.make_args(cd, st, raster_mode=1) for cd, st in zip(cds, steps)]
+    # SGLD off: deterministic reference; each view's raster mode and chunk
+    # count by the reference's rule, in the batch as in the one-view oracle
+    args = [E.make_args(cd, st) for cd, st in zip(cds, steps)]
     # engine
     eng = E.Engine(0)
     dg = E.DeviceGaussians(init)
@@ -129,8 +151,7 @@ def test_batch_step_matches_oracle_mean_gradient():
     for cd, st, gt in zip(cds, steps, gts):
         st = dict(st)
         st["loss_inv_n"] = st["loss_inv_n"] / B
-        r = O.train_step(32, init.copy(), cd, st, gt=gt, do_backward=True, do_optimizer=False, want_ids=False,
-                         raster_mode=1)
+        r = O.train_step(32, init.copy(), cd, st, gt=gt, do_backward=True, do_optimizer=False, want_ids=False)
         losses.append(r["loss"])            # the loss value is not scaled by loss_inv_n
         v = r["radii"] > 0
         vis |= v
