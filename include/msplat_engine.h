@@ -226,7 +226,8 @@ int msplat_engine_mcmc_scored(MsplatEngine *e, const MsplatGaussians *g, const M
 int msplat_engine_set_isect_budget(MsplatEngine *e, long long slots);
 
 /* Launch configuration of the tunable stages (no counterpart in the
- * reference; the defaults are the reference's choices).  None changes the
+ * reference; the defaults are the reference's choices except tile_order,
+ * whose default 1 gives the same lists as its per-tile sort).  None changes the
  * tile lists; sort_width, raster_batch and tile_order leave every output
  * bit-identical, bwd_pixels changes the gradients at float rounding (the
  * order of the sums), raster_mode and chunk change the image at float
@@ -241,9 +242,9 @@ typedef struct {
     int raster_mode;   /* used when args->raster_mode is 0: 0 the reference's rule (monolithic
                           from 400 tiles), 1 monolithic, 2 chunked; default 0 */
     int tile_order;    /* how the per-tile lists get their (depth, id) order: 0 a radix sort of
-                          each tile's keys (default), 1 one depth sort per view before the
-                          scatter, then each tile's per-CTA runs put in order (same lists; views
-                          of at most 20480 tiles, else 0) */
+                          each tile's keys, 1 one depth sort per view before the scatter, then
+                          each tile's per-CTA runs put in order (same lists; views of at most
+                          20480 tiles, else 0); default 1 */
     int bwd_pixels;    /* pixels per thread of the raster backward: 1 (256 threads per tile,
                           8x4-pixel warps; default) or 2 (128 threads, 8x8-pixel warps: one
                           warp reduction per 64 pixels, more work per CTA) */

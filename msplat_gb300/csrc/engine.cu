@@ -908,7 +908,7 @@ class Engine {
     long long timed_steps_ = 0, launches_ = 0;
     RasterArgs last_ra_{};   // raster arguments of the last eagerly issued step
     float4 *gstats_ = nullptr;   // caller's activity statistics (learned relocation), or null
-    MsplatTuning tuning_{512, 256, kChunk, 0, 0, 1};   // launch configuration of the tunable stages
+    MsplatTuning tuning_{512, 256, kChunk, 0, 1, 1};   // launch configuration of the tunable stages
     long long isect_slots_ = 0;   // fixed intersection budget in slots (0: legacy 48 per Gaussian and view)
     int last_groups_ = 1;         // tile groups of the last step
 

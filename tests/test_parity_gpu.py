@@ -107,11 +107,12 @@ def test_sgld_parity(small):
     assert e <= GRAD_TOL
 
 
-@pytest.mark.parametrize("tuning", [None, dict(bwd_pixels=2, tile_order=1)])
+@pytest.mark.parametrize("tuning", [dict(tile_order=0), dict(bwd_pixels=2, tile_order=1)])
 def test_edge_cases(small, tuning):
-    """Partial edge tiles, splats behind the camera, a NaN colour, a mask;
-    also with the two-pixels-per-thread raster backward (second pixels below
-    the image in the bottom tiles) and the depth-presorted tile ordering."""
+    """Partial edge tiles, splats behind the camera, a NaN colour, a mask:
+    with the per-tile sort, and with the two-pixels-per-thread raster
+    backward (second pixels below the image in the bottom tiles) and the
+    depth-presorted tile ordering."""
     sc, cam0, gt0, init = small
     cam = S.Camera(cam0.cam_to_world, 203, 150, 160.0, 160.0, 101.5, 75.0)
     gt = gt_image(sc.gt, cam)

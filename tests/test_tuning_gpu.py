@@ -55,12 +55,13 @@ def _step(init, cams, gts, tuning, views, raster_mode=1):
 @pytest.mark.parametrize("views", [1, 2])
 def test_sort_width_tile_batch_and_tile_order_are_bit_identical(scene, views):
     sc, cams, gts, init = scene
-    ref = _step(init, cams, gts, dict(sort_width=512, raster_batch=256), views)
+    ref = _step(init, cams, gts, dict(sort_width=512, raster_batch=256, tile_order=0), views)
     counts = np.diff(ref["offs"].astype(np.int64))
     assert (counts > 0).sum() > 50   # the 256-thread sort class takes the tiles up to 2048 keys
-    for tun in (dict(sort_width=256, raster_batch=256), dict(sort_width=512, raster_batch=128),
-                dict(sort_width=256, raster_batch=128), dict(tile_order=1), dict(tile_order=1, raster_batch=128),
-                dict(bwd_pixels=2), dict(tile_order=1, raster_batch=128, bwd_pixels=2)):
+    for tun in (dict(sort_width=256, raster_batch=256, tile_order=0), dict(sort_width=512, raster_batch=128, tile_order=0),
+                dict(sort_width=256, raster_batch=128, tile_order=0), dict(tile_order=1),
+                dict(tile_order=1, raster_batch=128), dict(bwd_pixels=2, tile_order=0),
+                dict(tile_order=1, raster_batch=128, bwd_pixels=2)):
         o = _step(init, cams, gts, tun, views)
         for k in ("offs", "ids", "img", "v_img"):
             np.testing.assert_array_equal(o[k], ref[k], err_msg=f"{tun} {k}")
