@@ -12,8 +12,12 @@ schedule, SH degree raised every 1000 iterations, MCMC relocation and 5 %
 growth every 100 steps up to the 1,000,000 cap).  Reported: wall-clock
 iterations/s over the whole run (MCMC rounds included), the Gaussian count,
 held-out PSNR / SSIM / L1 over the 20 views (msplat_trainer_evaluate, the
-reference's Trainer::evaluate), and per-stage milliseconds over a few eager
-steps at the end.  Prints one JSON line.
+reference's Trainer::evaluate), per-stage milliseconds over a few eager
+steps at the end, and the trained model's rasterization load on the last
+of those views: intersections, tile list lengths and the (pixel, splat)
+pairs the backward walks, with the raster backward's FP32 rate.  Prints one
+JSON line.  --profile-step adds one more eager step inside a profiler range
+(cudaProfilerStart/Stop), for `ncu --profile-from-start off`.
 """
 from __future__ import annotations
 
@@ -52,7 +56,7 @@ def build(seed=0, n_init=100_000):
     return cams, imgs, xyz, rgb
 
 
-def run(iters=7000, seed=0, n_init=100_000, cap=1_000_000, timing_steps=20):
+def run(iters=7000, seed=0, n_init=100_000, cap=1_000_000, timing_steps=20, profile_step=False):
     from . import api as A
     from . import _native as N
     cams, imgs, xyz, rgb = build(seed, n_init)
@@ -82,12 +86,42 @@ def run(iters=7000, seed=0, n_init=100_000, cap=1_000_000, timing_steps=20):
     L.msplat_engine_stats(e, ctypes.byref(st))
     L.msplat_engine_set_timing(e, 0)
     stage_ms = {name: st.stage_ms[i] / max(1, st.timed_steps) for i, name in enumerate(N.STAGES)}
+    load = raster_load(L, e, cams[1].width, cams[1].height, stage_ms["raster_bwd"])
+    if profile_step:
+        import torch
+        torch.cuda.profiler.start()
+        t.step()
+        A.sync()
+        torch.cuda.profiler.stop()
     return {"workload": f"{iters} iterations from {n_init:,} random points, MCMC to the {cap:,} cap, 160 train + "
                         "20 held-out views at 1297x840 (synthetic 1M + 200k GT scene), public trainer API",
             "iters_per_s": iters / wall, "wall_s": wall, "final_gaussians": t.splat_count,
             "held_out_psnr": ev["psnr"], "held_out_ssim": ev["ssim"], "held_out_l1": ev["l1"],
-            "num_test": ev["num_test"], "curve": curve, "stage_ms_at_end": stage_ms,
+            "num_test": ev["num_test"], "curve": curve, "stage_ms_at_end": stage_ms, "trained_view": load,
             "mcmc_rounds": t.mcmc_stats()["rounds"]}
+
+
+def raster_load(L, e, W, H, bwd_ms):
+    """Tile lists and backward (pixel, splat) pairs of the engine's last step
+    (a W x H view): per pixel inside the image, from min(last contributor,
+    tile end - 1) down to the tile's first splat, the walk of the
+    reference's rasterize_backward_kernel (msplat_metal.metal:931-1135);
+    the FP32 rate counts 60 flops per pair."""
+    tx = (W + 15) // 16
+    T = tx * ((H + 15) // 16)
+    offs = np.zeros(T + 1, np.uint32)
+    fidx = np.zeros(W * H, np.int32)
+    L.msplat_engine_read(e, b"tile_offsets", offs.ctypes.data, offs.nbytes)
+    L.msplat_engine_read(e, b"final_idx", fidx.ctypes.data, fidx.nbytes)
+    offs = offs.astype(np.int64)
+    counts = np.diff(offs)
+    y, x = np.mgrid[0:H, 0:W]
+    tile = (y // 16) * tx + (x // 16)
+    s, end = offs[tile], offs[tile + 1]
+    pairs = int(np.maximum(0, np.minimum(end - 1, fidx.reshape(H, W).astype(np.int64)) - s + 1).sum())
+    return {"width": W, "height": H, "intersections": int(offs[-1]), "max_tile": int(counts.max()),
+            "mean_tile": float(counts.mean()), "pairs_bwd": pairs, "pairs_per_intersection": pairs / max(1, int(offs[-1])),
+            "raster_bwd_tflops_fp32": pairs * 60 / (bwd_ms * 1e-3) / 1e12}
 
 
 def main(argv=None):
@@ -95,8 +129,10 @@ def main(argv=None):
     ap.add_argument("--iters", type=int, default=7000)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--init", type=int, default=100_000)
+    ap.add_argument("--profile-step", action="store_true",
+                    help="one more eager step inside cudaProfilerStart/Stop (ncu --profile-from-start off)")
     a = ap.parse_args(argv)
-    print(json.dumps(run(a.iters, a.seed, a.init)), flush=True)
+    print(json.dumps(run(a.iters, a.seed, a.init, profile_step=a.profile_step)), flush=True)
     return 0
 
 
