@@ -349,7 +349,8 @@ def run_batched(eng, E, sc, dg, warmup, steps, step_base):
 
     # the launch configuration: tuned on this workload (CUDA events, whole
     # steps without updates), then the timed steps replay the tuned graph
-    eng.set_tuning(sort_width=512, raster_batch=256, chunk=512, raster_mode=0, tile_order=1, bwd_pixels=1)   # the defaults
+    eng.set_tuning(sort_width=512, raster_batch=128, chunk=512, raster_mode=0, tile_order=1, bwd_pixels=1,
+                   tile_split=2)   # the defaults
     untuned = eng.tuning()
     args0 = [E.make_args(cd, E.step_scalars(step_base, step_base, width=cd["width"], height=cd["height"]))
              for cd in cams]

@@ -226,17 +226,16 @@ int msplat_engine_mcmc_scored(MsplatEngine *e, const MsplatGaussians *g, const M
 int msplat_engine_set_isect_budget(MsplatEngine *e, long long slots);
 
 /* Launch configuration of the tunable stages (no counterpart in the
- * reference; the defaults are the reference's choices except tile_order,
- * whose default 1 gives the same lists as its per-tile sort).  None changes the
- * tile lists; sort_width, raster_batch and tile_order leave every output
- * bit-identical, bwd_pixels changes the gradients at float rounding (the
+ * reference).  None changes the tile lists; sort_width, raster_batch,
+ * tile_order and tile_split leave the image bit-identical (tile_split and
+ * bwd_pixels change how the backward's sums are grouped), bwd_pixels changes the gradients at float rounding (the
  * order of the sums), raster_mode and chunk change the image at float
  * rounding (as the reference's own monolithic / chunked choice does). */
 typedef struct {
     int sort_width;    /* CTA width of the lightest shared-memory tile sort: 256 (tiles up to
                           2048 keys) or 512 (up to 4096); default 512 */
     int raster_batch;  /* splats staged per shared-memory round in the rasterizers: 128 or 256;
-                          default 256 */
+                          default 128 */
     int chunk;         /* splats per depth chunk of the chunked rasterizer: 256, 512 or 1024;
                           default 512 */
     int raster_mode;   /* used when args->raster_mode is 0: 0 the reference's rule (monolithic
@@ -248,6 +247,10 @@ typedef struct {
     int bwd_pixels;    /* pixels per thread of the raster backward: 1 (256 threads per tile,
                           8x4-pixel warps; default) or 2 (128 threads, 8x8-pixel warps: one
                           warp reduction per 64 pixels, more work per CTA) */
+    int tile_split;    /* CTAs per tile of the monolithic rasterizers (the backward with one
+                          pixel per thread): 1, or 2 (default; each CTA a 16x8 half with four
+                          warps, so a barrier waits on four warps, not eight; each half stages
+                          the whole tile list and flushes its own gradient sums) */
 } MsplatTuning;
 
 int msplat_engine_set_tuning(MsplatEngine *e, const MsplatTuning *t);
@@ -256,7 +259,7 @@ int msplat_engine_get_tuning(MsplatEngine *e, MsplatTuning *t);
 /* Autotuner: times full training steps of the given views (forward, loss,
  * backward; no optimizer update and no SGLD, so the parameters do not
  * change) under candidate configurations, one coordinate at a time (tile
- * order, sort width, tile batch, backward pixels per thread, then raster
+ * order, sort width, CTAs per tile, tile batch, backward pixels per thread, then raster
  * mode with chunk length when args[0].raster_mode is 0), keeps the fastest (the median of `reps` timed
  * steps) and leaves it set.  gt[v] must be given for every view.  `out`
  * receives the chosen configuration and *ms (nullable) its step time. */

@@ -64,7 +64,7 @@ class MsplatGradients(C.Structure):
 class MsplatTuning(C.Structure):
     """include/msplat_engine.h MsplatTuning"""
     _fields_ = [("sort_width", C.c_int), ("raster_batch", C.c_int), ("chunk", C.c_int), ("raster_mode", C.c_int),
-                ("tile_order", C.c_int), ("bwd_pixels", C.c_int)]
+                ("tile_order", C.c_int), ("bwd_pixels", C.c_int), ("tile_split", C.c_int)]
 
 
 def lib(build_if_missing: bool = True):

@@ -321,7 +321,7 @@ class Engine {
 
         RasterArgs ra{};
         ra.vt = vt; ra.num_tiles = T; ra.k_max = K; ra.capacity = cap; ra.tile_lo = 0; ra.isect_lo = 0;
-        ra.chunk = tune.chunk; ra.batch = tune.raster_batch; ra.bwd_px = tune.bwd_pixels;
+        ra.chunk = tune.chunk; ra.batch = tune.raster_batch; ra.bwd_px = tune.bwd_pixels; ra.split = tune.tile_split;
         ra.sp = pa.sp; ra.tile_offsets = ta.tile_offsets; ra.isect_ids = ta.isect_ids;
         ra.n = (uint32_t)((long long)N * B); ra.rec = pa.rec;
         ra.out_img = ptr<float>("out_img"); ra.final_T = ptr<float>("final_T"); ra.final_idx = ptr<int>("final_idx");
@@ -541,6 +541,7 @@ class Engine {
         if (t.chunk != 256 && t.chunk != 512 && t.chunk != 1024) throw std::runtime_error("chunk must be 256, 512 or 1024");
         if (t.raster_mode < 0 || t.raster_mode > 2) throw std::runtime_error("raster_mode must be 0, 1 or 2");
         if (t.tile_order < 0 || t.tile_order > 1) throw std::runtime_error("tile_order must be 0 or 1");
+        if (t.tile_split != 1 && t.tile_split != 2) throw std::runtime_error("tile_split must be 1 or 2");
         if (t.bwd_pixels != 1 && t.bwd_pixels != 2) throw std::runtime_error("bwd_pixels must be 1 or 2");
         if (std::memcmp(&t, &tuning_, sizeof(t)) != 0) clear_graphs();
         tuning_ = t;
@@ -588,6 +589,7 @@ class Engine {
             };
             for (int o : {0, 1}) { MsplatTuning c = best; c.tile_order = o; consider(c); }
             for (int w : {256, 512}) { MsplatTuning c = best; c.sort_width = w; consider(c); }
+            for (int p : {1, 2}) { MsplatTuning c = best; c.tile_split = p; consider(c); }
             for (int b : {128, 256}) { MsplatTuning c = best; c.raster_batch = b; consider(c); }
             for (int p : {1, 2}) { MsplatTuning c = best; c.bwd_pixels = p; consider(c); }
             if (a[0].raster_mode == 0) {
@@ -908,7 +910,7 @@ class Engine {
     long long timed_steps_ = 0, launches_ = 0;
     RasterArgs last_ra_{};   // raster arguments of the last eagerly issued step
     float4 *gstats_ = nullptr;   // caller's activity statistics (learned relocation), or null
-    MsplatTuning tuning_{512, 256, kChunk, 0, 1, 1};   // launch configuration of the tunable stages
+    MsplatTuning tuning_{512, 128, kChunk, 0, 1, 1, 2};   // launch configuration of the tunable stages
     long long isect_slots_ = 0;   // fixed intersection budget in slots (0: legacy 48 per Gaussian and view)
     int last_groups_ = 1;         // tile groups of the last step
 

@@ -106,6 +106,7 @@ struct RasterArgs {
     int chunk;                  // splats per depth chunk (chunked raster)
     int batch;                  // splats staged per shared-memory round: 128 or 256
     int bwd_px;                 // pixels per thread of the backward: 1 (256 threads) or 2 (128)
+    int split;                  // CTAs per tile of the monolithic rasterizers: 1, or 2 (16x8 halves)
     long long capacity;
     const StepParams *sp;       // [views]
     const uint32_t *tile_offsets;

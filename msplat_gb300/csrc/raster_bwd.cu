@@ -22,26 +22,42 @@
 
 namespace msplat {
 
-// Thread layouts.  kPx = 1: warp w covers the 8x4 block of tile_px /
-// tile_py.  kPx = 2: warp w covers x in [8(w&1), 8(w&1)+8), y in
-// [8(w>>1), 8(w>>1)+8); the thread's column is lane & 7, its rows
-// (lane >> 3) and (lane >> 3) + 4.
-template <int kPx> struct BwdLayout;
+// Thread layouts, by CTA and pixel:
+//   1: one CTA per tile, 256 threads, one pixel each; warp w covers the 8x4
+//      block of tile_px / tile_py.
+//   2: one CTA per tile, 128 threads, two pixels each; warp w covers x in
+//      [8(w&1), 8(w&1)+8), y in [8(w>>1), 8(w>>1)+8); the thread's column
+//      is lane & 7, its rows (lane >> 3) and (lane >> 3) + 4.
+//   3: two CTAs per tile (MsplatTuning.tile_split), 128 threads, one pixel
+//      each: CTA `part` is the tile's 16x8 half covered by layout 1's warps
+//      4 part .. 4 part + 3.
+// A thread's place is its index in the tile's layout-1 numbering
+// (threadIdx.x + 128 part in layout 3, threadIdx.x otherwise).
+template <int kL> struct BwdLayout;
 template <> struct BwdLayout<1> {
-    static constexpr int kThreads = 256;
-    static __device__ __forceinline__ int px(int tid) { return tile_px(tid); }
-    static __device__ __forceinline__ int py(int tid) { return tile_py(tid); }
-    static __device__ __forceinline__ uint32_t reach(float x, float y, float hx, float hy, float ox, float oy) {
+    static constexpr int kThreads = 256, kPix = 1, kSplit = 1;
+    static __device__ __forceinline__ int px(int place) { return tile_px(place); }
+    static __device__ __forceinline__ int py(int place) { return tile_py(place); }
+    static __device__ __forceinline__ uint32_t reach(float x, float y, float hx, float hy, float ox, float oy, int) {
         return warp_reach(x, y, hx, hy, ox, oy);
     }
 };
+template <> struct BwdLayout<3> {
+    static constexpr int kThreads = 128, kPix = 1, kSplit = 2;
+    static __device__ __forceinline__ int px(int place) { return tile_px(place); }
+    static __device__ __forceinline__ int py(int place) { return tile_py(place); }
+    static __device__ __forceinline__ uint32_t reach(float x, float y, float hx, float hy, float ox, float oy,
+                                                     int part) {
+        return (warp_reach(x, y, hx, hy, ox, oy) >> (4 * part)) & 0xFu;
+    }
+};
 template <> struct BwdLayout<2> {
-    static constexpr int kThreads = 128;
+    static constexpr int kThreads = 128, kPix = 2, kSplit = 1;
     static __device__ __forceinline__ int px(int tid) { return (tid & 7) | ((tid >> 2) & 8); }
     static __device__ __forceinline__ int py(int tid) { return (tid >> 3) & 11; }
     // warp_reach for the 8x8 blocks: bit w when block w meets the splat's
     // reach box (the same conservative margins)
-    static __device__ __forceinline__ uint32_t reach(float x, float y, float hx, float hy, float ox, float oy) {
+    static __device__ __forceinline__ uint32_t reach(float x, float y, float hx, float hy, float ox, float oy, int) {
         if (!(hx <= 3.0e38f && hy <= 3.0e38f)) return 0xFu;
         if (hx < 0.f || hy < 0.f) return 0u;
         const float lx = x - ox, ly = y - oy;
@@ -55,14 +71,14 @@ template <> struct BwdLayout<2> {
 };
 
 // kBB splats staged per round (the tile batch: 128 or 256)
-template <int kBB, int kPx> struct BwdSmem {
+template <int kBB, int kL> struct BwdSmem {
     float4 xyo[kBB];    // x, y, opacity, id bits
     float4 con[kBB];    // conic, bits of the warps the splat reaches
     float4 rgb[kBB];    // clamped colour, w: bits of the channels with raw + 0.5 >= 0
     float acc[kBB][9];  // r g b | ca cb cc | x y | opacity
     uint32_t wm[kBB];   // bits of the warps the splat reaches
-    uint16_t wl[BwdLayout<kPx>::kThreads / 32][kBB];   // per warp: the batch positions it takes, ascending
-    int wmax[BwdLayout<kPx>::kThreads / 32];
+    uint16_t wl[BwdLayout<kL>::kThreads / 32][kBB];   // per warp: the batch positions it takes, ascending
+    int wmax[BwdLayout<kL>::kThreads / 32];
 };
 
 // Sums over the warp of 8 per-lane values v[] and of one more value w: lane
@@ -152,17 +168,18 @@ __device__ __forceinline__ bool splat_alpha(const float4 &xo, const float4 &cn, 
 }
 
 // Processes splat indices [s, hi] back to front for the whole CTA; px is
-// the thread's column, ps its kPx pixels.
-template <int kBB, int kPx>
-__device__ void backward_range(BwdSmem<kBB, kPx> &sm, const RasterArgs &a, int s, int hi, PixelState (&ps)[kPx],
-                               float px, GradRec *grad) {
-    using L = BwdLayout<kPx>;
+// the thread's column, ps its pixels; place / part: as in BwdLayout.
+template <int kBB, int kL>
+__device__ void backward_range(BwdSmem<kBB, kL> &sm, const RasterArgs &a, int s, int hi,
+                               PixelState (&ps)[BwdLayout<kL>::kPix], float px, int place, int part, GradRec *grad) {
+    using L = BwdLayout<kL>;
+    constexpr int kPx = L::kPix;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     int bmax = ps[0].bin_final;
 #pragma unroll
     for (int r = 1; r < kPx; r++) bmax = max(bmax, ps[r].bin_final);
     const int wbin = __reduce_max_sync(0xffffffffu, bmax);
-    const float ox = px - (float)L::px(tid), oy = ps[0].py - (float)L::py(tid);   // the tile's first pixel
+    const float ox = px - (float)L::px(place), oy = ps[0].py - (float)L::py(place);   // the tile's first pixel
     for (int batch_end = hi; batch_end >= s; batch_end -= kBB) {
         __syncthreads();
         for (int k = tid; k < kBB; k += L::kThreads) {
@@ -170,7 +187,7 @@ __device__ void backward_range(BwdSmem<kBB, kPx> &sm, const RasterArgs &a, int s
             if (idx >= s) {
                 const SplatRec r = isect_record(a.isect_ids, a.rec, a.n, idx);
                 sm.xyo[k] = r.a;
-                const uint32_t reach = L::reach(r.a.x, r.a.y, r.b.w, r.c.w, ox, oy);
+                const uint32_t reach = L::reach(r.a.x, r.a.y, r.b.w, r.c.w, ox, oy, part);
                 sm.con[k] = make_float4(r.b.x, r.b.y, r.b.z, __uint_as_float(reach));
                 sm.wm[k] = reach;
                 // clamped colour max(raw + 0.5, 0); w: channels whose raw + 0.5 >= 0
@@ -274,14 +291,15 @@ struct BwdPixel {
 
 // kViews: look the view up from the global tile index; false: one view
 // row: the thread's r-th pixel (4 r rows down)
-template <bool kViews, int kPx> __device__ __forceinline__ BwdPixel bwd_pixel(const RasterArgs &a, int tile, int row) {
+template <bool kViews, int kL>
+__device__ __forceinline__ BwdPixel bwd_pixel(const RasterArgs &a, int tile, int row, int place) {
     BwdPixel tp;
     tp.view = kViews ? view_of_tile(a.vt, tile) : 0;
     const ViewGeom vg = view_geom(a.vt, tp.view);
     const int lt = tile - vg.tile_base;
     const int tx = lt % vg.tiles_x, ty = lt / vg.tiles_x;
-    tp.x = tx * kTile + BwdLayout<kPx>::px(threadIdx.x);
-    tp.y = ty * kTile + BwdLayout<kPx>::py(threadIdx.x) + 4 * row;
+    tp.x = tx * kTile + BwdLayout<kL>::px(place);
+    tp.y = ty * kTile + BwdLayout<kL>::py(place) + 4 * row;
     tp.inside = tp.x < vg.width && tp.y < vg.height;
     tp.p = tp.inside ? vg.pix_base + (long long)tp.y * vg.width + tp.x : 0;
     return tp;
@@ -301,11 +319,18 @@ __device__ __forceinline__ void init_pixel(PixelState &ps, const RasterArgs &a, 
     ps.py = (float)tp.y;
 }
 
-template <bool kViews, int kBB, int kPx>
-__global__ void __launch_bounds__(BwdLayout<kPx>::kThreads, kPx == 2 ? 8 : 6) k_raster_bwd(RasterArgs a) {
+// blocks per SM each layout is built for (registers and shared memory)
+template <int kL> constexpr int bwd_min_blocks() { return kL == 1 ? 6 : (kL == 2 ? 8 : 12); }
+
+template <bool kViews, int kBB, int kL>
+__global__ void __launch_bounds__(BwdLayout<kL>::kThreads, bwd_min_blocks<kL>()) k_raster_bwd(RasterArgs a) {
     pdl_enter();
-    __shared__ BwdSmem<kBB, kPx> sm;
-    const int tile = blockIdx.x + a.tile_lo;
+    using L = BwdLayout<kL>;
+    constexpr int kPx = L::kPix;
+    __shared__ BwdSmem<kBB, kL> sm;
+    const int tile = (L::kSplit == 1 ? blockIdx.x : blockIdx.x / L::kSplit) + a.tile_lo;
+    const int part = L::kSplit == 1 ? 0 : blockIdx.x % L::kSplit;
+    const int place = threadIdx.x + part * L::kThreads;
     const int s = clamp_off(a.tile_offsets[tile], a.isect_lo, a.capacity), e = clamp_off(a.tile_offsets[tile + 1], a.isect_lo, a.capacity);
     if (s >= e) return;
     PixelState ps[kPx];
@@ -313,16 +338,16 @@ __global__ void __launch_bounds__(BwdLayout<kPx>::kThreads, kPx == 2 ? 8 : 6) k_
     int bmax = -1;
 #pragma unroll
     for (int r = 0; r < kPx; r++) {
-        const BwdPixel tp = bwd_pixel<kViews, kPx>(a, tile, r);
+        const BwdPixel tp = bwd_pixel<kViews, kL>(a, tile, r, place);
         const float Tf = tp.inside ? a.final_T[tp.p] : 0.f;
         init_pixel(ps[r], a, tp, Tf, 0.f, 0.f, 0.f);
         ps[r].bin_final = tp.inside ? a.final_idx[tp.p] : -1;
         bmax = max(bmax, ps[r].bin_final);
         px = (float)tp.x;
     }
-    const int hi = min(e - 1, block_max<BwdLayout<kPx>::kThreads / 32>(bmax, sm.wmax));
+    const int hi = min(e - 1, block_max<L::kThreads / 32>(bmax, sm.wmax));
     if (hi < s) return;
-    backward_range<kBB, kPx>(sm, a, s, hi, ps, px, a.grad);
+    backward_range<kBB, kL>(sm, a, s, hi, ps, px, place, part, a.grad);
 }
 
 __global__ void __launch_bounds__(256) k_chunk_prefix_suffix(RasterArgs a) {
@@ -349,10 +374,11 @@ __global__ void __launch_bounds__(256) k_chunk_prefix_suffix(RasterArgs a) {
     }
 }
 
-template <bool kViews, int kBB, int kPx>
-__global__ void __launch_bounds__(BwdLayout<kPx>::kThreads, kPx == 2 ? 8 : 6) k_raster_bwd_chunked(RasterArgs a) {
+template <bool kViews, int kBB, int kL>
+__global__ void __launch_bounds__(BwdLayout<kL>::kThreads, bwd_min_blocks<kL>()) k_raster_bwd_chunked(RasterArgs a) {
     pdl_enter();
-    __shared__ BwdSmem<kBB, kPx> sm;
+    constexpr int kPx = BwdLayout<kL>::kPix;
+    __shared__ BwdSmem<kBB, kL> sm;
     const int tile = blockIdx.x + a.tile_lo, k = blockIdx.y;
     const int s0 = clamp_off(a.tile_offsets[tile], a.isect_lo, a.capacity), e0 = clamp_off(a.tile_offsets[tile + 1], a.isect_lo, a.capacity);
     const int cs = s0 + k * a.chunk, ce = min(s0 + (k + 1) * a.chunk, e0);
@@ -363,7 +389,7 @@ __global__ void __launch_bounds__(BwdLayout<kPx>::kThreads, kPx == 2 ? 8 : 6) k_
     int bmax = -1;
 #pragma unroll
     for (int r = 0; r < kPx; r++) {
-        const BwdPixel tp = bwd_pixel<kViews, kPx>(a, tile, r);
+        const BwdPixel tp = bwd_pixel<kViews, kL>(a, tile, r, threadIdx.x);
         const size_t o = (size_t)k * P + (size_t)(tp.p - a.chunk_p0);
         init_pixel(ps[r], a, tp, tp.inside ? a.prefix_T[o] * a.chunk_T[o] : 0.f, tp.inside ? a.after_C[3 * o] : 0.f,
                    tp.inside ? a.after_C[3 * o + 1] : 0.f, tp.inside ? a.after_C[3 * o + 2] : 0.f);
@@ -372,21 +398,28 @@ __global__ void __launch_bounds__(BwdLayout<kPx>::kThreads, kPx == 2 ? 8 : 6) k_
         bmax = max(bmax, ps[r].bin_final);
         px = (float)tp.x;
     }
-    const int hi = min(ce - 1, block_max<BwdLayout<kPx>::kThreads / 32>(bmax, sm.wmax));
+    const int hi = min(ce - 1, block_max<BwdLayout<kL>::kThreads / 32>(bmax, sm.wmax));
     if (hi < cs) return;
-    backward_range<kBB, kPx>(sm, a, cs, hi, ps, px, a.grad);
+    backward_range<kBB, kL>(sm, a, cs, hi, ps, px, threadIdx.x, 0, a.grad);
 }
 
-template <int kBB, int kPx> static void raster_bwd_batch(const RasterArgs &a, cudaStream_t s) {
+template <int kBB, int kL> static void raster_bwd_batch(const RasterArgs &a, cudaStream_t s) {
     const bool views = a.vt.count > 1;
-    constexpr int kT = BwdLayout<kPx>::kThreads;
+    constexpr int kT = BwdLayout<kL>::kThreads;
     if (a.k_max <= 1) {
-        if (views) launch_pdl(k_raster_bwd<true, kBB, kPx>, a.num_tiles, kT, 0, s, a);
-        else launch_pdl(k_raster_bwd<false, kBB, kPx>, a.num_tiles, kT, 0, s, a);
+        // monolithic: one pixel per thread takes the tuned CTAs per tile
+        if (kL == 1 && a.split == 2) {
+            constexpr int kT3 = BwdLayout<3>::kThreads;
+            if (views) launch_pdl(k_raster_bwd<true, kBB, 3>, 2 * a.num_tiles, kT3, 0, s, a);
+            else launch_pdl(k_raster_bwd<false, kBB, 3>, 2 * a.num_tiles, kT3, 0, s, a);
+        } else {
+            if (views) launch_pdl(k_raster_bwd<true, kBB, kL>, a.num_tiles, kT, 0, s, a);
+            else launch_pdl(k_raster_bwd<false, kBB, kL>, a.num_tiles, kT, 0, s, a);
+        }
     } else {
         launch_pdl(k_chunk_prefix_suffix, (unsigned)((a.chunk_P + 255) / 256), 256, 0, s, a);
-        if (views) launch_pdl(k_raster_bwd_chunked<true, kBB, kPx>, dim3(a.num_tiles, a.k_max), kT, 0, s, a);
-        else launch_pdl(k_raster_bwd_chunked<false, kBB, kPx>, dim3(a.num_tiles, a.k_max), kT, 0, s, a);
+        if (views) launch_pdl(k_raster_bwd_chunked<true, kBB, kL>, dim3(a.num_tiles, a.k_max), kT, 0, s, a);
+        else launch_pdl(k_raster_bwd_chunked<false, kBB, kL>, dim3(a.num_tiles, a.k_max), kT, 0, s, a);
     }
 }
 

@@ -16,14 +16,22 @@
 
 namespace msplat {
 
-// kBatch splats staged per round (the tile batch: 128 or 256, one per
-// thread of the first kBatch threads)
-template <int kBatch> struct BatchSmem {
+// kSplit CTAs per tile (1, or 2: each a 16x8 half of it, four warps): the
+// CTA's threads take places [part * kCtaThreads, (part + 1) * kCtaThreads)
+// of the 256-thread tile layout (tile_px / tile_py), so a half is the tile's
+// warps 4 part .. 4 part + 3.
+template <int kSplit> struct SplitTile {
+    static constexpr int kCtaThreads = kTileThreads / kSplit;
+    static constexpr int kWarps = kCtaThreads / 32;
+};
+
+// kBatch splats staged per round (the tile batch: 128 or 256)
+template <int kBatch, int kSplit> struct BatchSmem {
     float4 xyo[kBatch];   // x, y, opacity, bits of the warps the splat reaches (warp_reach)
     float4 con[kBatch];   // conic
     float4 rgb[kBatch];   // clamped colour max(raw + 0.5, 0)
-    uint32_t wm[kBatch];  // bits of the warps the splat reaches (warp_reach)
-    uint16_t wl[kTileThreads / 32][kBatch];   // per warp: the batch positions it takes, ascending
+    uint32_t wm[kBatch];  // bits of this CTA's warps the splat reaches (warp_reach)
+    uint16_t wl[SplitTile<kSplit>::kWarps][kBatch];   // per warp: the batch positions it takes, ascending
 };
 
 // The positions t < nb of the staged batch whose warp bit is set, written
@@ -44,15 +52,17 @@ __device__ __forceinline__ int warp_batch_list(const uint32_t *wm, int nb, int w
     return cnt;
 }
 
-// (px, py): this thread's pixel
-template <int kBatch>
-__device__ __forceinline__ void load_batch(BatchSmem<kBatch> &sm, const RasterArgs &a, int idx, int end, float px,
-                                           float py) {
-    const int t = threadIdx.x;
-    if (t < kBatch && idx < end) {
+// Splats [b0, min(b0 + kBatch, end)) into the batch; (ox, oy): the tile's
+// first pixel; part: the CTA's part of the tile (its warps' reach bits).
+template <int kBatch, int kSplit>
+__device__ __forceinline__ void load_batch(BatchSmem<kBatch, kSplit> &sm, const RasterArgs &a, int b0, int end,
+                                           float ox, float oy, int part) {
+    for (int t = threadIdx.x; t < kBatch; t += SplitTile<kSplit>::kCtaThreads) {
+        const int idx = b0 + t;
+        if (idx >= end) break;
         const SplatRec r = isect_record(a.isect_ids, a.rec, a.n, idx);
-        const float ox = px - (float)tile_px(t), oy = py - (float)tile_py(t);   // the tile's first pixel
-        const uint32_t reach = warp_reach(r.a.x, r.a.y, r.b.w, r.c.w, ox, oy);
+        uint32_t reach = warp_reach(r.a.x, r.a.y, r.b.w, r.c.w, ox, oy);
+        if (kSplit == 2) reach = (reach >> (4 * part)) & 0xFu;
         sm.xyo[t] = make_float4(r.a.x, r.a.y, r.a.z, __uint_as_float(reach));
         sm.wm[t] = reach;
         sm.con[t] = r.b;
@@ -65,17 +75,17 @@ __device__ __forceinline__ void load_batch(BatchSmem<kBatch> &sm, const RasterAr
 // staged it lists their positions (ballots over the reach bits) and walks
 // that list.
 // done: in/out per-thread flag; returns (T, C, last).
-template <int kBatch>
-__device__ __forceinline__ void composite_range(BatchSmem<kBatch> &sm, const RasterArgs &a, int s, int e, float px,
-                                                float py, bool done, float &T, float3 &C, int &last,
-                                                unsigned *nan_sigma) {
+template <int kBatch, int kSplit>
+__device__ __forceinline__ void composite_range(BatchSmem<kBatch, kSplit> &sm, const RasterArgs &a, int s, int e,
+                                                float px, float py, float ox, float oy, int part, bool done, float &T,
+                                                float3 &C, int &last, unsigned *nan_sigma) {
     T = 1.f;
     C = make_float3(0.f, 0.f, 0.f);
     last = s - 1;
     const int warp = threadIdx.x >> 5;
     for (int b0 = s; b0 < e; b0 += kBatch) {
-        if (__syncthreads_count(done) == kTileThreads) break;
-        load_batch<kBatch>(sm, a, b0 + (int)threadIdx.x, e, px, py);
+        if (__syncthreads_count(done) == SplitTile<kSplit>::kCtaThreads) break;
+        load_batch<kBatch, kSplit>(sm, a, b0, e, ox, oy, part);
         __syncthreads();
         const int nb = min(kBatch, e - b0);
         const int cnt = warp_batch_list<kBatch>(sm.wm, nb, warp, sm.wl[warp]);
@@ -121,33 +131,37 @@ struct TilePixel {
     __device__ __forceinline__ long long p() const { return pix_base + (long long)y * width + x; }
 };
 
-// kViews: look the view up from the global tile index; false: one view
-template <bool kViews> __device__ __forceinline__ TilePixel tile_pixel(const RasterArgs &a, int tile) {
+// kViews: look the view up from the global tile index; false: one view.
+// place: the thread's place in the 256-thread tile layout.
+template <bool kViews> __device__ __forceinline__ TilePixel tile_pixel(const RasterArgs &a, int tile, int place) {
     TilePixel tp;
     tp.view = kViews ? view_of_tile(a.vt, tile) : 0;
     const ViewGeom vg = view_geom(a.vt, tp.view);
     const int lt = tile - vg.tile_base;
     const int tx = lt % vg.tiles_x, ty = lt / vg.tiles_x;
-    tp.x = tx * kTile + tile_px(threadIdx.x);
-    tp.y = ty * kTile + tile_py(threadIdx.x);
+    tp.x = tx * kTile + tile_px(place);
+    tp.y = ty * kTile + tile_py(place);
     tp.width = vg.width;
     tp.inside = tp.x < vg.width && tp.y < vg.height;
     tp.pix_base = vg.pix_base;
     return tp;
 }
 
-template <bool kViews, int kBatch>
-__global__ void __launch_bounds__(kTileThreads, 8) k_raster_fwd(RasterArgs a) {
+template <bool kViews, int kBatch, int kSplit>
+__global__ void __launch_bounds__(SplitTile<kSplit>::kCtaThreads, 8 * kSplit) k_raster_fwd(RasterArgs a) {
     pdl_enter();
-    __shared__ BatchSmem<kBatch> sm;
-    const int tile = blockIdx.x + a.tile_lo;
-    const TilePixel tp = tile_pixel<kViews>(a, tile);
+    __shared__ BatchSmem<kBatch, kSplit> sm;
+    const int tile = (kSplit == 1 ? blockIdx.x : blockIdx.x / kSplit) + a.tile_lo;
+    const int part = kSplit == 1 ? 0 : blockIdx.x % kSplit;
+    const int place = threadIdx.x + part * SplitTile<kSplit>::kCtaThreads;
+    const TilePixel tp = tile_pixel<kViews>(a, tile, place);
     int s = clamp_off(a.tile_offsets[tile], a.isect_lo, a.capacity), e = clamp_off(a.tile_offsets[tile + 1], a.isect_lo, a.capacity);
     if (!MS_GUARD(s >= 0 && s <= e && e <= a.capacity, 5, tile, a.nan_counts ? a.nan_counts + kDbgSlot : nullptr)) e = s = 0;
     float T;
     float3 C;
     int last;
-    composite_range(sm, a, s, e, (float)tp.x, (float)tp.y, !tp.inside, T, C, last, nullptr);
+    composite_range(sm, a, s, e, (float)tp.x, (float)tp.y, (float)(tp.x - tile_px(place)),
+                    (float)(tp.y - tile_py(place)), part, !tp.inside, T, C, last, nullptr);
     if (!tp.inside) return;
     const long long p = tp.p();
     if (!MS_GUARD(p >= 0 && p < a.vt.pixels, 6, p, a.nan_counts ? a.nan_counts + kDbgSlot : nullptr)) return;
@@ -162,9 +176,9 @@ __global__ void __launch_bounds__(kTileThreads, 8) k_raster_fwd(RasterArgs a) {
 template <bool kViews, int kBatch>
 __global__ void __launch_bounds__(kTileThreads, 8) k_raster_fwd_chunked(RasterArgs a) {
     pdl_enter();
-    __shared__ BatchSmem<kBatch> sm;
+    __shared__ BatchSmem<kBatch, 1> sm;
     const int tile = blockIdx.x + a.tile_lo, k = blockIdx.y;
-    const TilePixel tp = tile_pixel<kViews>(a, tile);
+    const TilePixel tp = tile_pixel<kViews>(a, tile, threadIdx.x);
     const int s0 = clamp_off(a.tile_offsets[tile], a.isect_lo, a.capacity), e0 = clamp_off(a.tile_offsets[tile + 1], a.isect_lo, a.capacity);
     const int cs = s0 + k * a.chunk, ce = min(s0 + (k + 1) * a.chunk, e0);
     const size_t o = (size_t)k * (size_t)a.chunk_P + (size_t)(tp.p() - a.chunk_p0);
@@ -179,7 +193,8 @@ __global__ void __launch_bounds__(kTileThreads, 8) k_raster_fwd_chunked(RasterAr
     float T;
     float3 C;
     int last;
-    composite_range(sm, a, cs, ce, (float)tp.x, (float)tp.y, !tp.inside, T, C, last,
+    composite_range(sm, a, cs, ce, (float)tp.x, (float)tp.y, (float)(tp.x - tile_px(threadIdx.x)),
+                    (float)(tp.y - tile_py(threadIdx.x)), 0, !tp.inside, T, C, last,
                     a.nan_counts ? a.nan_counts + kNanRasterSigma : nullptr);
     if (!tp.inside) return;
     a.chunk_T[o] = T;
@@ -219,9 +234,13 @@ __global__ void __launch_bounds__(256) k_raster_merge(RasterArgs a) {
 
 template <int kBatch> static void raster_fwd_batch(const RasterArgs &a, cudaStream_t s) {
     const bool views = a.vt.count > 1;
-    if (a.k_max <= 1) {
-        if (views) launch_pdl(k_raster_fwd<true, kBatch>, a.num_tiles, kTileThreads, 0, s, a);
-        else launch_pdl(k_raster_fwd<false, kBatch>, a.num_tiles, kTileThreads, 0, s, a);
+    if (a.k_max <= 1 && a.split == 2) {
+        constexpr int kT = SplitTile<2>::kCtaThreads;
+        if (views) launch_pdl(k_raster_fwd<true, kBatch, 2>, 2 * a.num_tiles, kT, 0, s, a);
+        else launch_pdl(k_raster_fwd<false, kBatch, 2>, 2 * a.num_tiles, kT, 0, s, a);
+    } else if (a.k_max <= 1) {
+        if (views) launch_pdl(k_raster_fwd<true, kBatch, 1>, a.num_tiles, kTileThreads, 0, s, a);
+        else launch_pdl(k_raster_fwd<false, kBatch, 1>, a.num_tiles, kTileThreads, 0, s, a);
     } else {
         if (views) launch_pdl(k_raster_fwd_chunked<true, kBatch>, dim3(a.num_tiles, a.k_max), kTileThreads, 0, s, a);
         else launch_pdl(k_raster_fwd_chunked<false, kBatch>, dim3(a.num_tiles, a.k_max), kTileThreads, 0, s, a);

@@ -201,7 +201,7 @@ class Engine:
         """Fixed intersection buffers of `slots` slots (0: legacy); larger views in tile groups."""
         self._check(self.L.msplat_engine_set_isect_budget(self.h, int(slots)))
 
-    TUNING_FIELDS = ("sort_width", "raster_batch", "chunk", "raster_mode", "tile_order", "bwd_pixels")
+    TUNING_FIELDS = ("sort_width", "raster_batch", "chunk", "raster_mode", "tile_order", "bwd_pixels", "tile_split")
 
     def set_tuning(self, **kw):
         """Change fields of the launch configuration (see MsplatTuning)."""

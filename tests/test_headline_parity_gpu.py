@@ -4,9 +4,10 @@ monolithic raster), step 3001 (every SH band, the regularizer and SGLD on) -
 exactly bench.py's workload - against the oracle's float path and FP64.
 
 Every launch configuration the autotuner can pick for it is covered: the
-depth-presorted tile ordering with one pixel per thread in the raster
-backward (its pick for one view), the per-tile radix sort, and the two-pixel
-backward (its pick for the 8-view batch).
+depth-presorted tile ordering with two CTAs per tile and one pixel per
+thread in the raster backward (the default), one CTA per tile with the
+per-tile radix sort, and the two-pixel backward (its pick for the 8-view
+batch).
 
 Bars:
   * radii, tiles hit, per-tile counts, sorted per-tile id lists and
@@ -35,9 +36,9 @@ pytestmark = pytest.mark.gpu
 STEP0 = 3001
 
 TUNINGS = {
-    "presorted_1px": dict(tile_order=1, bwd_pixels=1, sort_width=512, raster_batch=256),
-    "per_tile_sort": dict(tile_order=0, bwd_pixels=1, sort_width=512, raster_batch=256),
-    "presorted_2px": dict(tile_order=1, bwd_pixels=2, sort_width=512, raster_batch=256),
+    "presorted_1px": dict(tile_order=1, bwd_pixels=1, sort_width=512, raster_batch=128, tile_split=2),
+    "per_tile_sort": dict(tile_order=0, bwd_pixels=1, sort_width=512, raster_batch=256, tile_split=1),
+    "presorted_2px": dict(tile_order=1, bwd_pixels=2, sort_width=512, raster_batch=256, tile_split=1),
 }
 
 

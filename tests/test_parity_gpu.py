@@ -107,12 +107,14 @@ def test_sgld_parity(small):
     assert e <= GRAD_TOL
 
 
-@pytest.mark.parametrize("tuning", [dict(tile_order=0), dict(bwd_pixels=2, tile_order=1)])
+@pytest.mark.parametrize("tuning", [dict(tile_order=0, tile_split=1), dict(bwd_pixels=2, tile_order=1),
+                                    dict(tile_order=1, tile_split=2)])
 def test_edge_cases(small, tuning):
     """Partial edge tiles, splats behind the camera, a NaN colour, a mask:
-    with the per-tile sort, and with the two-pixels-per-thread raster
-    backward (second pixels below the image in the bottom tiles) and the
-    depth-presorted tile ordering."""
+    with the per-tile sort and one CTA per tile; with the two-pixels-per-
+    thread raster backward (second pixels below the image in the bottom
+    tiles) and the depth-presorted tile ordering; and with two CTAs per tile
+    (bottom halves of the last tile row wholly below the image)."""
     sc, cam0, gt0, init = small
     cam = S.Camera(cam0.cam_to_world, 203, 150, 160.0, 160.0, 101.5, 75.0)
     gt = gt_image(sc.gt, cam)

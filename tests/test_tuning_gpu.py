@@ -53,15 +53,18 @@ def _step(init, cams, gts, tuning, views, raster_mode=1):
 
 
 @pytest.mark.parametrize("views", [1, 2])
-def test_sort_width_tile_batch_and_tile_order_are_bit_identical(scene, views):
+def test_sort_width_tile_batch_tile_order_and_split_are_bit_identical(scene, views):
     sc, cams, gts, init = scene
-    ref = _step(init, cams, gts, dict(sort_width=512, raster_batch=256, tile_order=0), views)
+    ref = _step(init, cams, gts, dict(sort_width=512, raster_batch=256, tile_order=0, tile_split=1), views)
     counts = np.diff(ref["offs"].astype(np.int64))
     assert (counts > 0).sum() > 50   # the 256-thread sort class takes the tiles up to 2048 keys
-    for tun in (dict(sort_width=256, raster_batch=256, tile_order=0), dict(sort_width=512, raster_batch=128, tile_order=0),
-                dict(sort_width=256, raster_batch=128, tile_order=0), dict(tile_order=1),
-                dict(tile_order=1, raster_batch=128), dict(bwd_pixels=2, tile_order=0),
-                dict(tile_order=1, raster_batch=128, bwd_pixels=2)):
+    for tun in (dict(sort_width=256, raster_batch=256, tile_order=0, tile_split=1),
+                dict(sort_width=512, raster_batch=128, tile_order=0, tile_split=1),
+                dict(sort_width=256, raster_batch=128, tile_order=0, tile_split=1), dict(tile_order=1, tile_split=1),
+                dict(tile_order=1, raster_batch=128, tile_split=1), dict(bwd_pixels=2, tile_order=0, tile_split=1),
+                dict(tile_order=1, raster_batch=128, bwd_pixels=2, tile_split=1),
+                dict(tile_split=2, raster_batch=128, tile_order=0), dict(tile_split=2, raster_batch=256, tile_order=1),
+                dict(tile_split=2, raster_batch=128, tile_order=1, bwd_pixels=2)):
         o = _step(init, cams, gts, tun, views)
         for k in ("offs", "ids", "img", "v_img"):
             np.testing.assert_array_equal(o[k], ref[k], err_msg=f"{tun} {k}")
@@ -101,6 +104,7 @@ def test_autotune(scene):
     assert ms > 0
     assert cfg["sort_width"] in (256, 512) and cfg["raster_batch"] in (128, 256)
     assert cfg["chunk"] in (256, 512, 1024) and cfg["raster_mode"] in (0, 1, 2) and cfg["bwd_pixels"] in (1, 2)
+    assert cfg["tile_split"] in (1, 2)
     assert eng.tuning() == cfg
     p1, _ = dg.to_numpy()
     for k in E.GROUPS:   # timing runs leave the parameters alone
