@@ -39,24 +39,29 @@ __device__ __forceinline__ uint32_t gs_key0(const TileArgs &a, size_t u) {
     return (finite_bits(d) && d > 0.0f) ? __float_as_uint(d) : 0xffffffffu;
 }
 
+constexpr uint32_t kGsMask = kGsDigits - 1;
+constexpr int kGsDigitsPerThread = kGsDigits / kGsThreads;   // digits each thread of a block handles
+static_assert(kGsDigitsPerThread * kGsThreads == kGsDigits, "whole digits per thread");
+
 // Digit counts of one kGsPerCta-key block: hist[view][digit][block].
 template <bool kFirst>
 __global__ void __launch_bounds__(kGsThreads) k_gs_hist(TileArgs a, int shift, const uint32_t *key_in) {
     pdl_enter();
-    __shared__ uint32_t h[256];
+    __shared__ uint32_t h[kGsDigits];
     const int view = blockIdx.y, n = a.vt.n, nb = gridDim.x;
     const size_t vb = (size_t)view * n;
-    h[threadIdx.x] = 0;
+    for (int d = threadIdx.x; d < kGsDigits; d += kGsThreads) h[d] = 0;
     __syncthreads();
     const int e0 = blockIdx.x * kGsPerCta;
     for (int k = threadIdx.x; k < kGsPerCta; k += kGsThreads) {
         const int e = e0 + k;
         if (e >= n) break;
         const uint32_t key = kFirst ? gs_key0(a, vb + e) : key_in[vb + e];
-        atomicAdd(&h[(key >> shift) & 255u], 1u);
+        atomicAdd(&h[(key >> shift) & kGsMask], 1u);
     }
     __syncthreads();
-    a.gs_hist[(size_t)view * 256 * nb + (size_t)threadIdx.x * nb + blockIdx.x] = h[threadIdx.x];
+    for (int d = threadIdx.x; d < kGsDigits; d += kGsThreads)
+        a.gs_hist[(size_t)view * kGsDigits * nb + (size_t)d * nb + blockIdx.x] = h[d];
 }
 
 // Per digit (one warp each), the exclusive scan of its blocks' counts in
@@ -66,7 +71,7 @@ __global__ void __launch_bounds__(256) k_gs_digit_scan(TileArgs a, int nb) {
     pdl_enter();
     const int lane = threadIdx.x & 31;
     const int d = blockIdx.x * 8 + (threadIdx.x >> 5), view = blockIdx.y;
-    uint32_t *h = a.gs_hist + (size_t)view * 256 * nb + (size_t)d * nb;
+    uint32_t *h = a.gs_hist + (size_t)view * kGsDigits * nb + (size_t)d * nb;
     uint32_t carry = 0;
     for (int b0 = 0; b0 < nb; b0 += 128) {
         uint32_t v[4];
@@ -88,7 +93,7 @@ __global__ void __launch_bounds__(256) k_gs_digit_scan(TileArgs a, int nb) {
             carry += __shfl_sync(0xffffffffu, inc, 31);
         }
     }
-    if (lane == 0) a.gs_dtot[(size_t)view * 256 + d] = carry;
+    if (lane == 0) a.gs_dtot[(size_t)view * kGsDigits + d] = carry;
 }
 
 // Stable scatter of one kGsPerCta-key block: warp w holds keys
@@ -103,17 +108,22 @@ __global__ void __launch_bounds__(kGsThreads) k_gs_scatter(TileArgs a, int shift
                                                            const uint32_t *val_in, uint32_t *key_out,
                                                            uint32_t *val_out, ushort4 *srect_out) {
     pdl_enter();
-    __shared__ uint16_t wcnt[kGsThreads / 32][256];
-    __shared__ uint16_t woff[kGsThreads / 32][256];
-    __shared__ uint32_t base[256];
+    // wcnt: per warp and digit the keys counted so far, then (in place) the
+    // earlier warps' keys of the digit
+    __shared__ uint16_t wcnt[kGsThreads / 32][kGsDigits];
+    __shared__ uint32_t base[kGsDigits];
     __shared__ uint32_t wsum[kGsThreads / 32];
     const int view = blockIdx.y, n = a.vt.n, nb = gridDim.x;
     const size_t vb = (size_t)view * n;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    for (int k = tid; k < (kGsThreads / 32) * 256; k += kGsThreads) (&wcnt[0][0])[k] = 0;
-    {   // this block's start for digit tid: the digit's start (exclusive scan of
-        // the digit totals) + the earlier blocks' keys of that digit
-        const uint32_t tot = a.gs_dtot[(size_t)view * 256 + tid];
+    for (int k = tid; k < (kGsThreads / 32) * kGsDigits; k += kGsThreads) (&wcnt[0][0])[k] = 0;
+    {   // this block's start for digits kGsDigitsPerThread tid ..: the digit's
+        // start (exclusive scan of the digit totals) + the earlier blocks' keys
+        // of that digit
+        const uint32_t *dt = a.gs_dtot + (size_t)view * kGsDigits + kGsDigitsPerThread * tid;
+        uint32_t tot = 0;
+#pragma unroll
+        for (int q = 0; q < kGsDigitsPerThread; q++) tot += dt[q];
         uint32_t inc = tot;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -122,9 +132,15 @@ __global__ void __launch_bounds__(kGsThreads) k_gs_scatter(TileArgs a, int shift
         }
         if (lane == 31) wsum[wid] = inc;
         __syncthreads();
-        uint32_t add = 0;
-        for (int w = 0; w < wid; w++) add += wsum[w];
-        base[tid] = add + inc - tot + a.gs_hist[(size_t)view * 256 * nb + (size_t)tid * nb + blockIdx.x];
+        uint32_t run = inc - tot;
+        for (int w = 0; w < wid; w++) run += wsum[w];
+        const uint32_t *hb = a.gs_hist + (size_t)view * kGsDigits * nb + blockIdx.x;
+#pragma unroll
+        for (int q = 0; q < kGsDigitsPerThread; q++) {
+            const int d = kGsDigitsPerThread * tid + q;
+            base[d] = run + hb[(size_t)d * nb];
+            run += dt[q];
+        }
     }
     __syncthreads();
     const int e0 = blockIdx.x * kGsPerCta + wid * (32 * kGsItems);
@@ -136,10 +152,10 @@ __global__ void __launch_bounds__(kGsThreads) k_gs_scatter(TileArgs a, int shift
         const bool valid = e < n;
         kv[j] = valid ? (kFirst ? gs_key0(a, vb + e) : key_in[vb + e]) : 0u;
         vv[j] = valid ? (kFirst ? (uint32_t)e : val_in[vb + e]) : 0u;
-        const uint32_t d = valid ? ((kv[j] >> shift) & 255u) : 256u;
+        const uint32_t d = valid ? ((kv[j] >> shift) & kGsMask) : (uint32_t)kGsDigits;
         uint32_t peers = __ballot_sync(0xffffffffu, valid);
 #pragma unroll
-        for (int bit = 0; bit < 8; bit++) {
+        for (int bit = 0; bit < kGsBits; bit++) {
             const uint32_t m = __ballot_sync(0xffffffffu, (d >> bit) & 1u);
             peers &= ((d >> bit) & 1u) ? m : ~m;
         }
@@ -151,12 +167,13 @@ __global__ void __launch_bounds__(kGsThreads) k_gs_scatter(TileArgs a, int shift
         __syncwarp();
     }
     __syncthreads();
-    {   // per digit (one thread each), the counts of the earlier warps
+    // per digit, the counts of the earlier warps (in place)
+    for (int d = tid; d < kGsDigits; d += kGsThreads) {
         uint32_t run = 0;
 #pragma unroll
         for (int w = 0; w < kGsThreads / 32; w++) {
-            const uint32_t c = wcnt[w][tid];
-            woff[w][tid] = (uint16_t)run;
+            const uint32_t c = wcnt[w][d];
+            wcnt[w][d] = (uint16_t)run;
             run += c;
         }
     }
@@ -164,8 +181,8 @@ __global__ void __launch_bounds__(kGsThreads) k_gs_scatter(TileArgs a, int shift
 #pragma unroll
     for (int j = 0; j < kGsItems; j++) {
         if (rank[j] == 0xffffffffu) continue;
-        const uint32_t d = (kv[j] >> shift) & 255u;
-        const uint32_t pos = base[d] + woff[wid][d] + rank[j];
+        const uint32_t d = (kv[j] >> shift) & kGsMask;
+        const uint32_t pos = base[d] + wcnt[wid][d] + rank[j];
         if (MS_GUARD(pos < (uint32_t)n, 7, pos, a.nan_counts ? a.nan_counts + kDbgSlot : nullptr)) {
             key_out[vb + pos] = kv[j];
             val_out[vb + pos] = vv[j];
@@ -252,7 +269,7 @@ __global__ void __launch_bounds__(kOrderThreads) k_tile_order(TileArgs a, int ct
     const size_t vb = (size_t)view * a.vt.n;
     for (int j = threadIdx.x; j < count; j += blockDim.x) {
         const uint32_t p = keys[j];
-        const uint32_t gid = a.gs_val[0][vb + p];
+        const uint32_t gid = a.gs_val[kGsPasses & 1][vb + p];
         const int c = (int)(p >> kAggShift);
         const uint32_t rs = col[(size_t)c * Tv];
         const uint32_t re = c + 1 < ctas ? col[(size_t)(c + 1) * Tv] : (uint32_t)count;
@@ -268,18 +285,18 @@ int launch_presorted_count(const TileArgs &a, cudaStream_t s) {
     const int n = a.vt.n, views = a.vt.count;
     const int nb = (n + kGsPerCta - 1) / kGsPerCta;
     const dim3 g(nb, views);
-    // pass 0 reads the keys from the projection; passes alternate buffers 1, 0, 1, 0
-    const dim3 gd(32, views);   // 256 digits, 8 per CTA
+    // pass 0 reads the keys from the projection; passes alternate buffers 1, 0, 1, ...
+    const dim3 gd(kGsDigits / 8, views);   // one warp per digit, 8 per CTA
     launch_pdl(k_gs_hist<true>, g, kGsThreads, 0, s, a, 0, nullptr);
     launch_pdl(k_gs_digit_scan, gd, 256, 0, s, a, nb);
     launch_pdl(k_gs_scatter<true>, g, kGsThreads, 0, s, a, 0, nullptr, nullptr, a.gs_key[1], a.gs_val[1],
-               (ushort4 *)nullptr);
-    for (int pass = 1; pass < 4; pass++) {
+               kGsPasses == 1 ? a.srect : (ushort4 *)nullptr);
+    for (int pass = 1; pass < kGsPasses; pass++) {
         const int src = pass & 1, dst = src ^ 1;
-        launch_pdl(k_gs_hist<false>, g, kGsThreads, 0, s, a, 8 * pass, a.gs_key[src]);
+        launch_pdl(k_gs_hist<false>, g, kGsThreads, 0, s, a, kGsBits * pass, a.gs_key[src]);
         launch_pdl(k_gs_digit_scan, gd, 256, 0, s, a, nb);
-        launch_pdl(k_gs_scatter<false>, g, kGsThreads, 0, s, a, 8 * pass, a.gs_key[src], a.gs_val[src], a.gs_key[dst],
-                   a.gs_val[dst], pass == 3 ? a.srect : (ushort4 *)nullptr);
+        launch_pdl(k_gs_scatter<false>, g, kGsThreads, 0, s, a, kGsBits * pass, a.gs_key[src], a.gs_val[src],
+                   a.gs_key[dst], a.gs_val[dst], pass == kGsPasses - 1 ? a.srect : (ushort4 *)nullptr);
     }
     debug_sync(s, "depth_sort");
     const int agg_blocks = (n + kAggPerCta - 1) / kAggPerCta;
@@ -297,7 +314,7 @@ int launch_presorted_count(const TileArgs &a, cudaStream_t s) {
     }
     launch_pdl(k_count_agg_sorted, dim3(agg_blocks, views), kAggThreads, smem, s, a);
     debug_sync(s, "count_sorted");
-    return 12 + 1;
+    return 3 * kGsPasses + 1;
 }
 
 int launch_presorted_build(const TileArgs &a, cudaStream_t s) {

@@ -236,8 +236,8 @@ class Engine {
             const size_t recs = (size_t)N * B;
             alloc("gs_key0", 4 * recs); alloc("gs_key1", 4 * recs);
             alloc("gs_val0", 4 * recs); alloc("gs_val1", 4 * recs);
-            alloc("gs_hist", 4 * (size_t)B * 256 * ((N + kGsPerCta - 1) / kGsPerCta));
-            alloc("gs_dtot", 4 * (size_t)B * 256);
+            alloc("gs_hist", 4 * (size_t)B * kGsDigits * ((N + kGsPerCta - 1) / kGsPerCta));
+            alloc("gs_dtot", 4 * (size_t)B * kGsDigits);
             alloc("srect", 8 * recs);
             alloc("rect", 8 * recs);
         }
