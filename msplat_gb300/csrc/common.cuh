@@ -11,6 +11,8 @@
 //   GradRec     per Gaussian, 48 B: rasterizer gradients (xy, opacity logit;
 //               conic; colour), accumulated with vector atomics
 #pragma once
+
+#include <mutex>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -93,6 +95,22 @@ inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, s
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
+// Runs set_up once per device (kernel attributes and constant banks belong
+// to the device current at the call), under a lock.  A device is marked done
+// only when set_up returned cudaSuccess, so a failed first call is retried
+// by the next one; the error is returned.
+template <class F> inline cudaError_t once_per_device(std::mutex &mu, bool (&done)[64], F &&set_up) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return set_up();
+    std::lock_guard<std::mutex> lk(mu);
+    if (done[dev]) return cudaSuccess;
+    e = set_up();
+    if (e == cudaSuccess) done[dev] = true;
+    return e;
 }
 
 __device__ __forceinline__ bool finite_bits(float x) {

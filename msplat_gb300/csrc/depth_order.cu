@@ -301,17 +301,19 @@ int launch_presorted_count(const TileArgs &a, cudaStream_t s) {
     debug_sync(s, "depth_sort");
     const int agg_blocks = (n + kAggPerCta - 1) / kAggPerCta;
     const size_t smem = (size_t)max_view_tiles(a.vt) * sizeof(uint32_t);
-    static bool attr_set[64] = {false};
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (dev < 0 || dev >= 64 || !attr_set[dev]) {
-        cudaFuncSetAttribute(k_count_agg_sorted, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
-        cudaFuncSetAttribute(k_scatter_agg_sorted<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             kAggMaxTiles * 4);
-        cudaFuncSetAttribute(k_scatter_agg_sorted<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             kAggMaxTiles * 4);
-        if (dev >= 0 && dev < 64) attr_set[dev] = true;
-    }
+    static bool done[64] = {false};
+    static std::mutex mu;
+    once_per_device(mu, done, []() {   // (a failure stays in cudaGetLastError for the launch check)
+        cudaError_t e = cudaFuncSetAttribute(k_count_agg_sorted, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             kAggMaxTiles * 4);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_scatter_agg_sorted<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     kAggMaxTiles * 4);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_scatter_agg_sorted<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     kAggMaxTiles * 4);
+        return e;
+    });
     launch_pdl(k_count_agg_sorted, dim3(agg_blocks, views), kAggThreads, smem, s, a);
     debug_sync(s, "count_sorted");
     return 3 * kGsPasses + 1;

@@ -382,13 +382,13 @@ void mlp_pack(const float *P, uint8_t *img, cudaStream_t s) { k_mlp_pack<<<16, 2
 // Set once on each device (function attributes belong to the current device).
 static void mlp_attrs() {
     static bool done[64] = {false};
-    int dev = 0;
-    cudaGetDevice(&dev);
-    const bool track = dev >= 0 && dev < 64;
-    if (track && done[dev]) return;
-    cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmTrainEnd);
-    cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmTrainEnd);
-    if (track) done[dev] = true;
+    static std::mutex mu;
+    once_per_device(mu, done, []() {   // (a failure stays in cudaGetLastError for the launch check)
+        cudaError_t e = cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmTrainEnd);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmTrainEnd);
+        return e;
+    });
 }
 
 void mlp_forward(const __nv_bfloat16 *X, int n, const uint8_t *img, const float *P, float2 *out, unsigned *err,

@@ -649,27 +649,28 @@ __global__ void __launch_bounds__(kGlobThreads) k_sort_pack_global(TileArgs a, i
 size_t sort_pack_smem_bytes() { return pair_smem_bytes<1024>(); }
 
 // The kernels' shared-memory limits, set once on each device (function
-// attributes belong to the device the call is made on).
+// attributes belong to the device the call is made on).  A failure is left
+// in cudaGetLastError for the caller's launch check.
 static void tile_attrs() {
-    static bool attr_set[64] = {false};
-    int dev = 0;
-    cudaGetDevice(&dev);
-    const bool track = dev >= 0 && dev < 64;
-    if (!track || !attr_set[dev]) {
-        cudaFuncSetAttribute(k_sort_pack_smem<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)pair_smem_bytes<256>());
-        cudaFuncSetAttribute(k_sort_pack_smem<512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)pair_smem_bytes<512>());
-        cudaFuncSetAttribute(k_sort_pack_smem<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)pair_smem_bytes<1024>());
-        cudaFuncSetAttribute(k_count_agg<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
-        cudaFuncSetAttribute(k_count_agg<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
-        cudaFuncSetAttribute(k_scatter_agg<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
-        cudaFuncSetAttribute(k_scatter_agg<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
-        cudaFuncSetAttribute(k_scatter_agg<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
-        cudaFuncSetAttribute(k_scatter_agg<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kAggMaxTiles * 4);
-        if (track) attr_set[dev] = true;
-    }
+    static bool done[64] = {false};
+    static std::mutex mu;
+    once_per_device(mu, done, []() {
+        cudaError_t e = cudaSuccess;
+        auto set = [&](const void *k, int bytes) {
+            const cudaError_t r = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+            if (e == cudaSuccess) e = r;
+        };
+        set((const void *)k_sort_pack_smem<256>, (int)pair_smem_bytes<256>());
+        set((const void *)k_sort_pack_smem<512>, (int)pair_smem_bytes<512>());
+        set((const void *)k_sort_pack_smem<1024>, (int)pair_smem_bytes<1024>());
+        set((const void *)k_count_agg<false>, kAggMaxTiles * 4);
+        set((const void *)k_count_agg<true>, kAggMaxTiles * 4);
+        set((const void *)k_scatter_agg<false, false>, kAggMaxTiles * 4);
+        set((const void *)k_scatter_agg<true, false>, kAggMaxTiles * 4);
+        set((const void *)k_scatter_agg<false, true>, kAggMaxTiles * 4);
+        set((const void *)k_scatter_agg<true, true>, kAggMaxTiles * 4);
+        return e;
+    });
 }
 
 static bool presorted_path(const TileArgs &a) {
