@@ -556,6 +556,15 @@ def run_engine(args):
                             "peak_kind": "nominal: SMs x 128 FP32 lanes x 2 x max SM clock"}
     except Exception as ex:   # reported, never fatal to the throughput line
         roofline["fp32"] = {"error": str(ex)[:200]}
+    # the whole step against HBM: the algorithmic bytes of one iteration
+    # (2140 B per Gaussian, 128 B per intersection, 67 B per pixel: the
+    # per-unit figures of the workload's byte model without the 76 B per
+    # intersection of the reference's pack, which this design does not do)
+    # over the graph-replayed step time
+    step_bytes = 2140.0 * units["g"] + 128.0 * units["i"] + 67.0 * units["p"]
+    roofline["step"] = {"algorithmic_bytes": step_bytes, "ms": ms_step,
+                        "achieved": step_bytes / (ms_step / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                        "frac": step_bytes / (ms_step / 1e3) / 1e9 / peak}
 
     batched = None
     if not args.no_batched:
