@@ -171,6 +171,18 @@ __device__ __forceinline__ float det_expf_neg(float x) {
     return __fmul_rn(p, two_n);
 }
 
+// A sigma beyond which a splat of opacity op composites nothing: alpha =
+// op * exp(-sigma) < 1/255 for every sigma > ln(255 op), and the margin of
+// 1e-4 (a factor e^-1e-4 on alpha) covers the rounding of the exponential,
+// of the product and of this logarithm (each within a few 1e-7 relative), so
+// the rasterizers may skip such a pair without evaluating alpha: its alpha
+// test fails either way.  +inf (nothing skipped) for a NaN opacity, whose
+// alpha the reference's fmin turns into 0.999; -inf for a zero opacity.
+__device__ __forceinline__ float sigma_cut(float op) {
+    if (!(op >= 0.f)) return __int_as_float(0x7f800000);
+    return op > 0.f ? logf(255.f * op) + 1e-4f : __int_as_float(0xff800000);
+}
+
 // Tile rectangle of a splat, inclusive min / exclusive max (get_tile_bbox,
 // msplat_metal.metal:57-87).  Truncating, saturating float->int conversion.
 // The divisions by 16 are exact scalings: multiplying by 1/16 gives the same

@@ -73,7 +73,7 @@ template <> struct BwdLayout<2> {
 // kBB splats staged per round (the tile batch: 128 or 256)
 template <int kBB, int kL> struct BwdSmem {
     float4 xyo[kBB];    // x, y, opacity, id bits
-    float4 con[kBB];    // conic, bits of the warps the splat reaches
+    float4 con[kBB];    // conic, sigma_cut(opacity)
     float4 rgb[kBB];    // clamped colour, w: bits of the channels with raw + 0.5 >= 0
     float acc[kBB][9];  // r g b | ca cb cc | x y | opacity
     uint32_t wm[kBB];   // bits of the warps the splat reaches
@@ -160,6 +160,7 @@ __device__ __forceinline__ bool splat_alpha(const float4 &xo, const float4 &cn, 
     const float sigma = __fmaf_rn(0.5f, __fmaf_rn(cn.x, __fmul_rn(dx, dx), __fmul_rn(__fmul_rn(cn.z, dy), dy)),
                                   __fmul_rn(__fmul_rn(cn.y, dx), dy));
     if (!(sigma >= 0.f && sigma < 5.55f)) return false;   // NaN fails too
+    if (sigma > cn.w) return false;                        // alpha < 1/255 for certain
     float a = __fmul_rn(xo.z, __expf(-sigma));
     if (fabsf(a - 1.f / 255.f) <= 4e-6f * (1.f / 255.f) || fabsf(a - 0.999f) <= 4e-6f)
         a = __fmul_rn(xo.z, det_expf_neg(-sigma));
@@ -188,7 +189,7 @@ __device__ void backward_range(BwdSmem<kBB, kL> &sm, const RasterArgs &a, int s,
                 const SplatRec r = isect_record(a.isect_ids, a.rec, a.n, idx);
                 sm.xyo[k] = r.a;
                 const uint32_t reach = L::reach(r.a.x, r.a.y, r.b.w, r.c.w, ox, oy, part);
-                sm.con[k] = make_float4(r.b.x, r.b.y, r.b.z, __uint_as_float(reach));
+                sm.con[k] = make_float4(r.b.x, r.b.y, r.b.z, sigma_cut(r.a.z));
                 sm.wm[k] = reach;
                 // clamped colour max(raw + 0.5, 0); w: channels whose raw + 0.5 >= 0
                 // (the only ones that pass a colour gradient back)

@@ -27,7 +27,7 @@ template <int kSplit> struct SplitTile {
 
 // kBatch splats staged per round (the tile batch: 128 or 256)
 template <int kBatch, int kSplit> struct BatchSmem {
-    float4 xyo[kBatch];   // x, y, opacity, bits of the warps the splat reaches (warp_reach)
+    float4 xyo[kBatch];   // x, y, opacity, sigma_cut(opacity)
     float4 con[kBatch];   // conic
     float4 rgb[kBatch];   // clamped colour max(raw + 0.5, 0)
     uint32_t wm[kBatch];  // bits of this CTA's warps the splat reaches (warp_reach)
@@ -63,7 +63,7 @@ __device__ __forceinline__ void load_batch(BatchSmem<kBatch, kSplit> &sm, const 
         const SplatRec r = isect_record(a.isect_ids, a.rec, a.n, idx);
         uint32_t reach = warp_reach(r.a.x, r.a.y, r.b.w, r.c.w, ox, oy);
         if (kSplit == 2) reach = (reach >> (4 * part)) & 0xFu;
-        sm.xyo[t] = make_float4(r.a.x, r.a.y, r.a.z, __uint_as_float(reach));
+        sm.xyo[t] = make_float4(r.a.x, r.a.y, r.a.z, sigma_cut(r.a.z));
         sm.wm[t] = reach;
         sm.con[t] = r.b;
         sm.rgb[t] = make_float4(fmaxf(r.c.x + 0.5f, 0.f), fmaxf(r.c.y + 0.5f, 0.f), fmaxf(r.c.z + 0.5f, 0.f), 0.f);
@@ -100,6 +100,7 @@ __device__ __forceinline__ void composite_range(BatchSmem<kBatch, kSplit> &sm, c
                 if (nan_sigma && !finite_bits(sigma)) atomicAdd(nan_sigma, 1u);
                 continue;
             }
+            if (sigma > xo.w) continue;   // alpha < 1/255 for certain
             const float alpha = fminf(0.999f, xo.z * det_expf_neg(-sigma));
             if (alpha < 1.f / 255.f) continue;
             const float nT = T * (1.f - alpha);
