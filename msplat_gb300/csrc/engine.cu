@@ -197,6 +197,8 @@ class Engine {
         // reference): a view that does not fit is rastered in tile groups
         const bool fixed = isect_slots_ > 0 && K == 1;
         const long long cap = fixed ? isect_slots_ : legacy;
+        // slots are addressed with 32-bit offsets and indices
+        if (cap >= (1LL << 31)) throw std::runtime_error("intersection buffer of 2^31 slots or more");
         const bool has_gt = gts != nullptr;
         ensure_points(N, B);
         ensure_tiles(T);
@@ -531,6 +533,7 @@ class Engine {
 
     void set_isect_budget(long long slots) {
         if (slots < 0) throw std::runtime_error("negative intersection budget");
+        if (slots >= (1LL << 31)) throw std::runtime_error("intersection budget of 2^31 slots or more");
         if (slots != isect_slots_) clear_graphs();
         isect_slots_ = slots;
     }
