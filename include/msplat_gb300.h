@@ -92,9 +92,19 @@ MsplatDataset msplat_dataset_create_ex(const char *path, float downscaleFactor, 
  * default): per-Gaussian activity statistics are gathered during the steps,
  * a 22-64-64-2 MLP on the tensor cores is trained every 500 steps on the
  * run's own (state -> opacity and activity 500 steps later) pairs, and once
- * trained its predictions replace sigmoid(opacity) as the weights of the
- * MCMC source draws.  Returns 0 or a negative code. */
+ * trained, at each relocation round, its predictions replace sigmoid(opacity)
+ * as the weights of the MCMC source draws and the Gaussians it forecasts to
+ * fade (opacity one window ahead at most the forecast-pruning threshold,
+ * 0.02 unless set below) are relocated with the dead ones.  Returns 0 or a
+ * negative code. */
 int msplat_trainer_set_learned_relocation(MsplatTrainer t, int enabled);
+
+/* The learned proposal's forecast-pruning threshold (no counterpart in the
+ * reference): Gaussians whose forecast opacity one window ahead is at most
+ * `forecast_opacity` are relocated with the dead ones; 0 turns forecast
+ * pruning off (source weighting only); default 0.02.  Returns 0, or -1 for
+ * a bad handle or a threshold outside [0, 1). */
+int msplat_trainer_set_learned_prune(MsplatTrainer t, float forecast_opacity);
 
 /* Last training loss of the proposal MLP and its training rounds so far;
  * returns 1 when the proposal is enabled, 0 when not, -1 on a bad handle. */

@@ -48,6 +48,7 @@ def _lib():
     L.msplat_dataset_points.argtypes = [vp, fp, C.POINTER(C.c_uint8)]
     L.msplat_trainer_load_ply.argtypes = [vp, cp]
     L.msplat_trainer_set_learned_relocation.argtypes = [vp, C.c_int]
+    L.msplat_trainer_set_learned_prune.argtypes = [vp, C.c_float]
     L.msplat_trainer_learned_stats.argtypes = [vp, fp, C.POINTER(C.c_int)]
     L.msplat_trainer_learned_eval.argtypes = [vp, fp]
     L.msplat_trainer_set_batch_views.argtypes = [vp, C.c_int, C.c_float]
@@ -281,6 +282,13 @@ class GaussianTrainer:
         """Weight MCMC source draws by the online-trained proposal MLP (see msplat_gb300.h)."""
         if _lib().msplat_trainer_set_learned_relocation(self.h, int(enabled)) != 0:
             raise RuntimeError("could not switch the learned relocation proposal")
+
+    def set_learned_prune(self, forecast_opacity: float):
+        """The learned proposal's forecast-pruning threshold: Gaussians whose forecast
+        opacity one window ahead is at most this are relocated with the dead ones
+        (0: off; default 0.02)."""
+        if _lib().msplat_trainer_set_learned_prune(self.h, float(forecast_opacity)) != 0:
+            raise RuntimeError("could not set forecast pruning")
 
     def set_batch_views(self, num_views: int, lr_scale: float = 0.0):
         """Render `num_views` cameras per step and update from their mean gradient,

@@ -79,7 +79,11 @@ def parse(argv=None):
     p.add_argument("--autotune", action="store_true",
                    help="time the engine's launch configurations on the first training views and keep the fastest")
     p.add_argument("--learned-relocation", action="store_true",
-                   help="weight MCMC relocation sources by the online-trained proposal MLP")
+                   help="online-trained proposal MLP: weights MCMC relocation sources and relocates the "
+                        "Gaussians it forecasts to fade")
+    p.add_argument("--learned-prune", type=float, default=None,
+                   help="forecast-pruning threshold of the learned proposal (forecast opacity; 0 = off; "
+                        "default 0.02)")
     a = p.parse_args(argv)
     a.downscale_factor = max(a.downscale_factor, 1.0)
     return a
@@ -109,6 +113,8 @@ def main(argv=None) -> int:
         trainer.set_batch_views(a.batch_views, a.batch_lr_scale)
     if a.learned_relocation:
         trainer.set_learned_relocation(True)
+        if a.learned_prune is not None:
+            trainer.set_learned_prune(a.learned_prune)
     if a.isect_budget > 0:
         trainer.set_isect_budget(a.isect_budget)
     if a.autotune:

@@ -491,6 +491,7 @@ struct TrainerImpl {
         int *idx = nullptr;
         int pending = -1, rounds = 0, adam_steps = 0, cap = 0;
         float last_loss = NAN;
+        float prune = 0.02f;            // forecast-opacity threshold of forecast pruning (0: off)
         std::mt19937 rng{7};
     } lrn;
 
@@ -796,6 +797,7 @@ struct TrainerImpl {
         MsplatAdamState st = model.adam();
         MsplatMcmcStats ms;
         const float *score = learned_scores();
+        if (score && lrn.prune > 0.f) mlp_forecast_prune(lrn.Y, model.n, model.p[5], lrn.prune, stream());
         check(msplat_engine_mcmc_scored(eng, &g, &st, model.cap, cfg.cullRadius, &reloc_count, score, &ms), "mcmc");
         model.n = ms.num_active;
         if (crossed(prev, step, 1000))
@@ -1335,6 +1337,12 @@ int msplat_trainer_get_gaussians(MsplatTrainer t, float *means, float *scales, f
 int msplat_trainer_set_learned_relocation(MsplatTrainer t, int enabled) {
     if (!t) return -1;
     return guard("learned_relocation", [&]() { TR(t)->enable_learned(enabled != 0); return 0; }, -2);
+}
+
+int msplat_trainer_set_learned_prune(MsplatTrainer t, float forecast_opacity) {
+    if (!t || !(forecast_opacity >= 0.f && forecast_opacity < 1.f)) return -1;
+    TR(t)->lrn.prune = forecast_opacity;
+    return 0;
 }
 
 int msplat_trainer_set_batch_views(MsplatTrainer t, int num_views, float lr_scale) {

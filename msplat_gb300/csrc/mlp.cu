@@ -512,6 +512,19 @@ __global__ void k_mlp_scores(const float2 *y, int n, float *score) {
     score[i] = fmaxf(o * (1.f + 0.25f * act), 1e-6f);
 }
 
+// Forecast pruning: a Gaussian whose forecast opacity one window ahead is at
+// most tau gets an opacity logit of -20, so the relocation round that follows
+// classifies it dead (sigmoid <= 0.005) and moves it now.
+__global__ void k_forecast_prune(const float2 *y, int n, float *opacities, float tau) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (y[i].x <= tau) opacities[i] = -20.f;
+}
+
+void mlp_forecast_prune(const float2 *y, int n, float *opacities, float tau, cudaStream_t s) {
+    if (n > 0) k_forecast_prune<<<(n + 255) / 256, 256, 0, s>>>(y, n, opacities, tau);
+}
+
 void mlp_features(const MlpFeatArgs &a, cudaStream_t s) {
     if (a.rows > 0) k_mlp_features<<<(a.rows + 255) / 256, 256, 0, s>>>(a);
 }

@@ -8,12 +8,15 @@ Scene: 16,384 ground-truth Gaussians (synthetic.config_small), 8 training
 views at 256x256 and 4 held-out views between them, targets rendered by the
 engine.  Both arms start from the same seed points (jittered ground-truth
 means, colours from the ground truth) and the same configuration (MCMC cap
-32,768, black background); the learned arm switches the proposal on.
+32,768, black background); the learned arm switches the proposal on (source
+weighting and forecast pruning; `learned_noprune`: source weighting only).
 Held-out PSNR is measured every `--eval-every` steps outside the timed
-training time.  Time-to-PSNR: the training wall-clock at which an arm first
-reaches its plain counterpart's final PSNR minus 0.1 dB (`plain` for the
-one-view arms, the same batch arm without `_learned` for a batched learned
-arm), reported per seed and as mean and sd over seeds.  Optional arms
+training time.  Reported per arm against its plain counterpart (`plain` for
+the one-view arms, the same batch arm without `_learned` for a batched
+learned arm): the held-out PSNR at the fixed iteration count (the gain per
+seed: mean, sd and seeds won), and time-to-PSNR, the training wall-clock at
+which the arm first reaches its counterpart's final PSNR minus 0.1 dB, per
+seed and as mean and sd over seeds.  Optional arms
 `batchB[xS][_learned]` train with B views per optimizer step (the mean
 gradient of B cameras, one update, learning rates x S, default
 `--batch-lr-scale` or B ** 0.75); iterations count views, so every arm sees
@@ -59,7 +62,7 @@ def _scene(seed, init="jitter", n_init=4096):
     return list(sc.train_cams) + list(test), imgs, xyz, col
 
 
-def run_arm(cams, imgs, xyz, col, learned, iters, eval_every, batch=1, lr_scale=0.0):
+def run_arm(cams, imgs, xyz, col, learned, iters, eval_every, batch=1, lr_scale=0.0, prune=None):
     import torch
     from . import api as A
     # the last 4 views are held out: train on the first 8, evaluate the others by pose
@@ -68,6 +71,8 @@ def run_arm(cams, imgs, xyz, col, learned, iters, eval_every, batch=1, lr_scale=
     t = A.GaussianTrainer(ds, cfg)
     if learned:
         t.set_learned_relocation(True)
+        if prune is not None:
+            t.set_learned_prune(prune)
     if batch > 1:
         t.set_batch_views(batch, lr_scale)
 
@@ -105,7 +110,9 @@ def time_to(curve, target):
 
 
 def _arm_spec(name, default_lr=0.0):
-    """'plain' | 'learned' | 'batch<B>[x<lr scale>][_learned]' -> (learned, B, lr scale)"""
+    """'plain' | 'learned' | 'learned_noprune' | 'batch<B>[x<lr scale>][_learned]' -> (learned, B, lr scale)"""
+    if name == "learned_noprune":
+        return True, 1, 0.0
     learned = name.endswith("learned")
     base = name[:-len("_learned")] if name.endswith("_learned") else name
     if base.startswith("batch"):
@@ -126,11 +133,12 @@ def compare(cams, imgs, xyz, col, names, iters, eval_every, batch_lr_scale=0.0):
     runs = {}
     for nm in names:
         learned, b, lr = _arm_spec(nm, batch_lr_scale)
-        runs[nm] = run_arm(cams, imgs, xyz, col, learned, iters, eval_every, batch=b, lr_scale=lr)
+        runs[nm] = run_arm(cams, imgs, xyz, col, learned, iters, eval_every, batch=b, lr_scale=lr,
+                           prune=0.0 if nm == "learned_noprune" else None)
     res = {}
     for nm, r in runs.items():
         base = nm[:-len("_learned")] if nm.endswith("_learned") else nm
-        if base == "learned":
+        if base in ("learned", "learned_noprune"):
             base = "plain"
         ref = runs.get(base, runs["plain"])
         target = ref["final_psnr"] - 0.1
@@ -148,16 +156,22 @@ def compare(cams, imgs, xyz, col, names, iters, eval_every, batch_lr_scale=0.0):
 
 
 def summarize(per_seed, names):
-    """mean and sd over seeds of each arm's time ratio, final and mean PSNR."""
+    """mean and sd over seeds of each arm's time ratio, final and mean PSNR,
+    and its held-out PSNR at the fixed iteration count against its plain
+    counterpart's (the gain per seed: mean, sd, seeds won)."""
     out = {}
     for nm in names:
         rows = [ps[nm] for ps in per_seed]
         ratios = [r["time_ratio"] for r in rows if r["time_ratio"] is not None]
+        gains = [ps[nm]["final_psnr"] - ps[ps[nm]["vs"]]["final_psnr"] for ps in per_seed if ps[nm]["vs"] in ps]
         out[nm] = {"vs": rows[0]["vs"], "seeds": len(rows), "reached": len(ratios),
                    "time_ratio_mean": float(np.mean(ratios)) if ratios else None,
                    "time_ratio_sd": float(np.std(ratios, ddof=1)) if len(ratios) > 1 else None,
                    "final_psnr_mean": float(np.mean([r["final_psnr"] for r in rows])),
-                   "mean_psnr_mean": float(np.mean([r["mean_psnr"] for r in rows]))}
+                   "mean_psnr_mean": float(np.mean([r["mean_psnr"] for r in rows])),
+                   "final_psnr_gain_mean": float(np.mean(gains)) if gains else None,
+                   "final_psnr_gain_sd": float(np.std(gains, ddof=1)) if len(gains) > 1 else None,
+                   "final_psnr_wins": int(sum(g > 0 for g in gains))}
     return out
 
 
