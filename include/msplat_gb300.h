@@ -101,9 +101,9 @@ int msplat_trainer_set_learned_relocation(MsplatTrainer t, int enabled);
 
 /* The learned proposal's forecast-pruning threshold (no counterpart in the
  * reference): Gaussians whose forecast opacity one window ahead is at most
- * `forecast_opacity` are relocated with the dead ones; 0 turns forecast
- * pruning off (source weighting only); default 0.02.  Returns 0, or -1 for
- * a bad handle or a threshold outside [0, 1). */
+ * `forecast_opacity` are relocated with the dead ones (at most 5 % of them
+ * per round); 0 turns forecast pruning off (source weighting only); default
+ * 0.02.  Returns 0, or -1 for a bad handle or a threshold outside [0, 1). */
 int msplat_trainer_set_learned_prune(MsplatTrainer t, float forecast_opacity);
 
 /* Last training loss of the proposal MLP and its training rounds so far;

@@ -484,7 +484,7 @@ struct TrainerImpl {
         double eval_sum[4] = {0, 0, 0, 0};
         int eval_rounds = 0;
         uint8_t *img = nullptr;
-        unsigned *err = nullptr;
+        unsigned *err = nullptr, *pruned = nullptr;
         float4 *gstats = nullptr, *snap = nullptr;
         __nv_bfloat16 *X = nullptr, *Xs = nullptr;
         float2 *Y = nullptr, *T = nullptr;
@@ -514,7 +514,7 @@ struct TrainerImpl {
 
     void free_learned() {
         void *ptrs[] = {lrn.P, lrn.G, lrn.M, lrn.V, lrn.loss, lrn.score, lrn.img, lrn.err, lrn.gstats, lrn.snap,
-                        lrn.X, lrn.Xs, lrn.Y, lrn.T, lrn.idx, lrn.eval};
+                        lrn.X, lrn.Xs, lrn.Y, lrn.T, lrn.idx, lrn.eval, lrn.pruned};
         for (void *q : ptrs)
             if (q) cudaFree(q);
         lrn = Learned{};
@@ -535,6 +535,7 @@ struct TrainerImpl {
         CKA(cudaMalloc(&lrn.V, kMlpParams * 4));
         CKA(cudaMalloc(&lrn.loss, 4));
         CKA(cudaMalloc(&lrn.err, 4));
+        CKA(cudaMalloc(&lrn.pruned, 4));
         CKA(cudaMalloc(&lrn.eval, 5 * 4));
         CKA(cudaMalloc(&lrn.img, kImgBytes));
         CKA(cudaMalloc(&lrn.gstats, sizeof(float4) * (size_t)cap));
@@ -797,7 +798,7 @@ struct TrainerImpl {
         MsplatAdamState st = model.adam();
         MsplatMcmcStats ms;
         const float *score = learned_scores();
-        if (score && lrn.prune > 0.f) mlp_forecast_prune(lrn.Y, model.n, model.p[5], lrn.prune, stream());
+        if (score && lrn.prune > 0.f) mlp_forecast_prune(lrn.Y, model.n, model.p[5], lrn.prune, lrn.pruned, stream());
         check(msplat_engine_mcmc_scored(eng, &g, &st, model.cap, cfg.cullRadius, &reloc_count, score, &ms), "mcmc");
         model.n = ms.num_active;
         if (crossed(prev, step, 1000))

@@ -514,15 +514,20 @@ __global__ void k_mlp_scores(const float2 *y, int n, float *score) {
 
 // Forecast pruning: a Gaussian whose forecast opacity one window ahead is at
 // most tau gets an opacity logit of -20, so the relocation round that follows
-// classifies it dead (sigmoid <= 0.005) and moves it now.
-__global__ void k_forecast_prune(const float2 *y, int n, float *opacities, float tau) {
+// classifies it dead (sigmoid <= 0.005) and moves it now.  At most max_n per
+// round (counted in *count, zeroed by the caller): a forecast that condemns
+// much of the model cannot empty it in one round.
+__global__ void k_forecast_prune(const float2 *y, int n, float *opacities, float tau, unsigned *count,
+                                 unsigned max_n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    if (y[i].x <= tau) opacities[i] = -20.f;
+    if (y[i].x <= tau && atomicAdd(count, 1u) < max_n) opacities[i] = -20.f;
 }
 
-void mlp_forecast_prune(const float2 *y, int n, float *opacities, float tau, cudaStream_t s) {
-    if (n > 0) k_forecast_prune<<<(n + 255) / 256, 256, 0, s>>>(y, n, opacities, tau);
+void mlp_forecast_prune(const float2 *y, int n, float *opacities, float tau, unsigned *count, cudaStream_t s) {
+    if (n <= 0) return;
+    cudaMemsetAsync(count, 0, sizeof(unsigned), s);
+    k_forecast_prune<<<(n + 255) / 256, 256, 0, s>>>(y, n, opacities, tau, count, (unsigned)(n / 20));
 }
 
 void mlp_features(const MlpFeatArgs &a, cudaStream_t s) {
