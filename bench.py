@@ -33,6 +33,8 @@ Also reported:
                  PSNR at the fixed iteration count and time to PSNR;
   full_run       the full configuration trained from 100k random points to
                  the 1M cap over 7000 iterations, with held-out PSNR / SSIM;
+                 full_run_learned the same with the learned relocation
+                 proposal, and its held-out PSNR gain;
   roofline.fp32  the rasterizer backward's FP32-pipe fraction from the
                  (pixel, splat) pairs the reference's algorithm walks.
 
@@ -618,8 +620,15 @@ def run_engine(args):
             from msplat_gb300 import full_run
             eng.close()
             out["full_run"] = full_run.run()
+            # the same run with the learned relocation proposal: held-out
+            # PSNR at the fixed iteration count against the plain run's
+            lr = full_run.run(learned=True)
+            out["full_run_learned"] = {k: lr[k] for k in ("iters_per_s", "wall_s", "final_gaussians", "held_out_psnr",
+                                                          "held_out_ssim", "held_out_l1", "curve", "mcmc_rounds")}
+            out["full_run_learned"]["psnr_gain_vs_plain_db"] = lr["held_out_psnr"] - out["full_run"]["held_out_psnr"]
         except Exception as ex:   # reported, never fatal to the throughput line
-            out["full_run"] = {"error": str(ex)[:200]}
+            out.setdefault("full_run", {"error": str(ex)[:200]})
+            out["full_run_learned"] = {"error": str(ex)[:200]}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(model, sc.train_cams[0], gts_host[0].numpy(), steps=args.cpu_steps)
     if rank == 0:

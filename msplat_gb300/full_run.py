@@ -1,6 +1,6 @@
 """The full-scale training run through the public trainer API.
 
-    python -m msplat_gb300.full_run [--iters 7000] [--seed 0] [--init 100000]
+    python -m msplat_gb300.full_run [--iters 7000] [--seed 0] [--init 100000] [--learned]
 
 Scene (synthetic.config_full): 1,000,000 ground-truth Gaussians plus a
 200,000-Gaussian ground plane; 160 ring/elevation-jittered training views and
@@ -56,7 +56,7 @@ def build(seed=0, n_init=100_000):
     return cams, imgs, xyz, rgb
 
 
-def run(iters=7000, seed=0, n_init=100_000, cap=1_000_000, timing_steps=20, profile_step=False):
+def run(iters=7000, seed=0, n_init=100_000, cap=1_000_000, timing_steps=20, profile_step=False, learned=False):
     from . import api as A
     from . import _native as N
     cams, imgs, xyz, rgb = build(seed, n_init)
@@ -64,6 +64,8 @@ def run(iters=7000, seed=0, n_init=100_000, cap=1_000_000, timing_steps=20, prof
     assert ds.num_train == 160 and ds.num_test == 20
     del imgs
     t = A.GaussianTrainer(ds, A.TrainingConfig(iterations=iters, cap_max=cap, bg_color=[0.0, 0.0, 0.0]))
+    if learned:
+        t.set_learned_relocation(True)
     curve = []
     A.sync()
     t0 = time.perf_counter()
@@ -98,7 +100,7 @@ def run(iters=7000, seed=0, n_init=100_000, cap=1_000_000, timing_steps=20, prof
             "iters_per_s": iters / wall, "wall_s": wall, "final_gaussians": t.splat_count,
             "held_out_psnr": ev["psnr"], "held_out_ssim": ev["ssim"], "held_out_l1": ev["l1"],
             "num_test": ev["num_test"], "curve": curve, "stage_ms_at_end": stage_ms, "trained_view": load,
-            "mcmc_rounds": t.mcmc_stats()["rounds"]}
+            "mcmc_rounds": t.mcmc_stats()["rounds"], "learned": bool(learned)}
 
 
 def raster_load(L, e, W, H, bwd_ms):
@@ -129,10 +131,11 @@ def main(argv=None):
     ap.add_argument("--iters", type=int, default=7000)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--init", type=int, default=100_000)
+    ap.add_argument("--learned", action="store_true", help="with the learned relocation proposal")
     ap.add_argument("--profile-step", action="store_true",
                     help="one more eager step inside cudaProfilerStart/Stop (ncu --profile-from-start off)")
     a = ap.parse_args(argv)
-    print(json.dumps(run(a.iters, a.seed, a.init, profile_step=a.profile_step)), flush=True)
+    print(json.dumps(run(a.iters, a.seed, a.init, profile_step=a.profile_step, learned=a.learned)), flush=True)
     return 0
 
 
