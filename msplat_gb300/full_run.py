@@ -56,26 +56,47 @@ def build(seed=0, n_init=100_000):
     return cams, imgs, xyz, rgb
 
 
-def run(iters=7000, seed=0, n_init=100_000, cap=1_000_000, timing_steps=20, profile_step=False, learned=False):
+def held_out_psnr(t, test_imgs):
+    """Mean over the held-out views of 10 log10(1 / MSE) against the uint8
+    targets / 255 (the reference's Trainer::evaluate PSNR)."""
+    vals = []
+    for i, gt in enumerate(test_imgs):
+        img = t.render(i, True).astype(np.float64)
+        mse = float(np.mean((img - gt.astype(np.float64) / 255.0) ** 2))
+        vals.append(10.0 * np.log10(1.0 / max(mse, 1e-20)))
+    return float(np.mean(vals))
+
+
+def run(iters=7000, seed=0, n_init=100_000, cap=1_000_000, timing_steps=20, profile_step=False, learned=False,
+        eval_every=0):
+    """eval_every > 0: held-out PSNR every that many iterations (outside the
+    timed wall clock) in `psnr_curve` as (iteration, wall s, dB)."""
     from . import api as A
     from . import _native as N
     cams, imgs, xyz, rgb = build(seed, n_init)
     ds = A.Dataset.from_arrays(cams, imgs, xyz, rgb, eval_mode=True, test_every=9)
     assert ds.num_train == 160 and ds.num_test == 20
+    test_imgs = imgs[0::9][:20] if eval_every > 0 else []   # every 9th view is held out
     del imgs
     t = A.GaussianTrainer(ds, A.TrainingConfig(iterations=iters, cap_max=cap, bg_color=[0.0, 0.0, 0.0]))
     if learned:
         t.set_learned_relocation(True)
-    curve = []
+    curve, psnr_curve = [], []
     A.sync()
     t0 = time.perf_counter()
+    paused = 0.0
     while t.iteration < iters:
         t.step()
         if t.iteration % 1000 == 0:
             A.sync()
-            curve.append((t.iteration, time.perf_counter() - t0, t.splat_count))
+            curve.append((t.iteration, time.perf_counter() - t0 - paused, t.splat_count))
+        if eval_every > 0 and t.iteration % eval_every == 0:
+            A.sync()
+            p0 = time.perf_counter()
+            psnr_curve.append((t.iteration, p0 - t0 - paused, held_out_psnr(t, test_imgs)))
+            paused += time.perf_counter() - p0
     A.sync()
-    wall = time.perf_counter() - t0
+    wall = time.perf_counter() - t0 - paused
     ev = t.evaluate()
     # per-stage times: a few more steps with CUDA events between the stages
     L = A._lib()
@@ -100,7 +121,7 @@ def run(iters=7000, seed=0, n_init=100_000, cap=1_000_000, timing_steps=20, prof
             "iters_per_s": iters / wall, "wall_s": wall, "final_gaussians": t.splat_count,
             "held_out_psnr": ev["psnr"], "held_out_ssim": ev["ssim"], "held_out_l1": ev["l1"],
             "num_test": ev["num_test"], "curve": curve, "stage_ms_at_end": stage_ms, "trained_view": load,
-            "mcmc_rounds": t.mcmc_stats()["rounds"], "learned": bool(learned)}
+            "mcmc_rounds": t.mcmc_stats()["rounds"], "learned": bool(learned), "psnr_curve": psnr_curve}
 
 
 def raster_load(L, e, W, H, bwd_ms):
