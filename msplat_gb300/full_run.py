@@ -68,7 +68,7 @@ def held_out_psnr(t, test_imgs):
 
 
 def run(iters=7000, seed=0, n_init=100_000, cap=1_000_000, timing_steps=20, profile_step=False, learned=False,
-        eval_every=0):
+        eval_every=0, prune=None):
     """eval_every > 0: held-out PSNR every that many iterations (outside the
     timed wall clock) in `psnr_curve` as (iteration, wall s, dB)."""
     from . import api as A
@@ -81,6 +81,8 @@ def run(iters=7000, seed=0, n_init=100_000, cap=1_000_000, timing_steps=20, prof
     t = A.GaussianTrainer(ds, A.TrainingConfig(iterations=iters, cap_max=cap, bg_color=[0.0, 0.0, 0.0]))
     if learned:
         t.set_learned_relocation(True)
+        if prune is not None:
+            t.set_learned_prune(prune)
     curve, psnr_curve = [], []
     A.sync()
     t0 = time.perf_counter()
