@@ -10,7 +10,7 @@ the persistence forecast.
   persistence.  On the small synthetic scene the network must beat
   persistence on both outputs: activity by at least 2x in mean squared
   error, opacity at all.
-* Training: the judge of the proposal is held-out PSNR at a fixed iteration
+* Training: the proposal is measured by held-out PSNR at a fixed iteration
   count against plain relocation.  Over five scene seeds (6000 iterations,
   16,384-Gaussian scene, cap 32,768), the learned arm (source weighting and
   forecast pruning) must end above plain on average and on at least three
