@@ -1,6 +1,6 @@
 """The full-scale training run through the public trainer API.
 
-    python -m msplat_gb300.full_run [--iters 7000] [--seed 0] [--init 100000] [--learned]
+    python -m msplat_gb300.full_run [--iters 7000] [--seed 0] [--init 100000] [--learned] [--batch-views B]
 
 Scene (synthetic.config_full): 1,000,000 ground-truth Gaussians plus a
 200,000-Gaussian ground plane; 160 ring/elevation-jittered training views and
@@ -68,7 +68,7 @@ def held_out_psnr(t, test_imgs):
 
 
 def run(iters=7000, seed=0, n_init=100_000, cap=1_000_000, timing_steps=20, profile_step=False, learned=False,
-        eval_every=0, prune=None):
+        eval_every=0, prune=None, batch=1):
     """eval_every > 0: held-out PSNR every that many iterations (outside the
     timed wall clock) in `psnr_curve` as (iteration, wall s, dB)."""
     from . import api as A
@@ -83,6 +83,8 @@ def run(iters=7000, seed=0, n_init=100_000, cap=1_000_000, timing_steps=20, prof
         t.set_learned_relocation(True)
         if prune is not None:
             t.set_learned_prune(prune)
+    if batch > 1:   # views per optimizer step (iterations count views), learning rates x batch ** 0.75
+        t.set_batch_views(batch)
     curve, psnr_curve = [], []
     A.sync()
     t0 = time.perf_counter()
@@ -123,7 +125,8 @@ def run(iters=7000, seed=0, n_init=100_000, cap=1_000_000, timing_steps=20, prof
             "iters_per_s": iters / wall, "wall_s": wall, "final_gaussians": t.splat_count,
             "held_out_psnr": ev["psnr"], "held_out_ssim": ev["ssim"], "held_out_l1": ev["l1"],
             "num_test": ev["num_test"], "curve": curve, "stage_ms_at_end": stage_ms, "trained_view": load,
-            "mcmc_rounds": t.mcmc_stats()["rounds"], "learned": bool(learned), "psnr_curve": psnr_curve}
+            "mcmc_rounds": t.mcmc_stats()["rounds"], "learned": bool(learned), "batch_views": batch,
+            "psnr_curve": psnr_curve}
 
 
 def raster_load(L, e, W, H, bwd_ms):
@@ -155,10 +158,12 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--init", type=int, default=100_000)
     ap.add_argument("--learned", action="store_true", help="with the learned relocation proposal")
+    ap.add_argument("--batch-views", type=int, default=1, help="views per optimizer step")
     ap.add_argument("--profile-step", action="store_true",
                     help="one more eager step inside cudaProfilerStart/Stop (ncu --profile-from-start off)")
     a = ap.parse_args(argv)
-    print(json.dumps(run(a.iters, a.seed, a.init, profile_step=a.profile_step, learned=a.learned)), flush=True)
+    print(json.dumps(run(a.iters, a.seed, a.init, profile_step=a.profile_step, learned=a.learned,
+                         batch=a.batch_views)), flush=True)
     return 0
 
 
