@@ -261,7 +261,8 @@ int msplat_engine_get_tuning(MsplatEngine *e, MsplatTuning *t);
  * change) under candidate configurations, one coordinate at a time (tile
  * order, sort width, CTAs per tile, tile batch, backward pixels per thread, then raster
  * mode with chunk length when args[0].raster_mode is 0), keeps the fastest (the median of `reps` timed
- * steps) and leaves it set.  gt[v] must be given for every view.  `out`
+ * steps, after ten untimed ones; a candidate must beat the best so far by more than 1 %) and leaves
+ * it set.  gt[v] must be given for every view.  `out`
  * receives the chosen configuration and *ms (nullable) its step time. */
 int msplat_engine_autotune(MsplatEngine *e, const MsplatGaussians *g, const MsplatStepArgs *args, int num_views,
                            const uint8_t *const *gt, const uint8_t *const *mask, int reps, MsplatTuning *out,
