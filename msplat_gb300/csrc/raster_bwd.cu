@@ -1,9 +1,10 @@
 // Back-to-front rasterizer VJP w.r.t. splat centre, conic, raw colour and
 // opacity logit.  One CTA per 16x16 tile (chunked: per (tile, chunk)), in one
-// of two layouts (MsplatTuning.bwd_pixels): one pixel per thread, 256
-// threads, each warp an 8x4 block; or two pixels per thread (four rows
-// apart), 128 threads, each warp an 8x8 block, so one warp reduction serves
-// 64 pixels (fewer reductions, more work per CTA).  Per splat each warp
+// of the layouts below (MsplatTuning.bwd_pixels, tile_split): one pixel per
+// thread, 256 threads, each warp an 8x4 block, or the same split into two
+// 128-thread CTAs per tile (16x8 halves); or two pixels per thread (four
+// rows apart), 128 threads, each warp an 8x8 block, so one warp reduction
+// serves 64 pixels (fewer reductions, more work per CTA).  Per splat each warp
 // reduces its pixels' 9 partial gradients with a transpose-reduce (9
 // shuffles for 8 values plus 5 for the ninth, instead of 45; paired fp32
 // adds), warps combine through shared-memory adds, and each batch flushes one

@@ -1,9 +1,9 @@
-// Front-to-back alpha compositing.  Monolithic: one CTA per 16x16 tile, one
-// thread per pixel, splats staged through shared memory in batches of 256
-// (each thread gathers one splat record by the id in the tile list); the
-// CTA leaves as soon as
-// every pixel has saturated.  Chunked: one CTA per (tile, 512-splat depth
-// chunk) with chunk-local transmittance, then a per-pixel merge.
+// Front-to-back alpha compositing.  Monolithic: one CTA per 16x16 tile, or
+// two (its 16x8 halves, MsplatTuning.tile_split), one thread per pixel,
+// splats staged through shared memory in batches of 128 or 256 (each thread
+// gathers splat records by the ids in the tile list); a CTA leaves as soon as
+// all its pixels have saturated.  Chunked: one CTA per (tile, 512-splat
+// depth chunk) with chunk-local transmittance, then a per-pixel merge.
 // Follows nd_rasterize_forward_kernel (msplat_metal.metal:499-618),
 // rasterize_forward_chunked_kernel (:2960-3076) and
 // rasterize_forward_merge_kernel (:3081-3134).  Built with --fmad=false; the
