@@ -631,25 +631,14 @@ def run_engine(args):
             # iterations outside the timed clock, the crossing interpolated
             # linearly between two evaluations)
             target = fr["held_out_psnr"] - 0.1
-
-            def reach(pc):
-                prev = (0.0, float("-inf"))
-                for _, w, p in pc:
-                    if p >= target:
-                        if prev[1] == float("-inf"):
-                            return w
-                        return prev[0] + (w - prev[0]) * (target - prev[1]) / (p - prev[1])
-                    prev = (w, p)
-                return None
-
-            tp = reach(fr["psnr_curve"])
+            tp = full_run.time_to(fr["psnr_curve"], target)
             for key, kw in (("full_run_learned", dict(learned=True)),
                             ("full_run_learned_batched", dict(learned=True, batch=4))):
                 r = full_run.run(eval_every=500, **kw)
                 o = {k: r[k] for k in ("iters_per_s", "wall_s", "final_gaussians", "held_out_psnr", "held_out_ssim",
                                        "held_out_l1", "curve", "psnr_curve", "mcmc_rounds", "batch_views")}
                 o["psnr_gain_vs_plain_db"] = r["held_out_psnr"] - fr["held_out_psnr"]
-                tr = reach(r["psnr_curve"])
+                tr = full_run.time_to(r["psnr_curve"], target)
                 o["time_to_target"] = {"target_db": target, "plain_s": tp, "run_s": tr,
                                        "ratio": (tr / tp) if (tp and tr) else None}
                 out[key] = o

@@ -56,6 +56,21 @@ def build(seed=0, n_init=100_000):
     return cams, imgs, xyz, rgb
 
 
+def time_to(psnr_curve, target):
+    """Wall clock at which a (iteration, wall s, dB) curve first reaches
+    `target` dB, interpolated linearly between the two evaluations around
+    the crossing (the first evaluation's time when it is already there);
+    None when it never does."""
+    prev = None
+    for _, w, p in psnr_curve:
+        if p >= target:
+            if prev is None:
+                return w
+            return prev[0] + (w - prev[0]) * (target - prev[1]) / (p - prev[1])
+        prev = (w, p)
+    return None
+
+
 def held_out_psnr(t, test_imgs):
     """Mean over the held-out views of 10 log10(1 / MSE) against the uint8
     targets / 255 (the reference's Trainer::evaluate PSNR)."""

@@ -51,17 +51,6 @@ def test_learned_relocation_gains_held_out_psnr_at_fixed_iterations():
     assert sum(g > 0 for g in gains) >= 3, gains
 
 
-def _reach(curve, target):
-    """Wall clock at which a (iteration, wall s, dB) curve first reaches
-    target, interpolated linearly between two evaluations."""
-    prev = (0.0, float("-inf"))
-    for _, w, p in curve:
-        if p >= target:
-            return w if prev[1] == float("-inf") else prev[0] + (w - prev[0]) * (target - prev[1]) / (p - prev[1])
-        prev = (w, p)
-    return None
-
-
 def test_learned_batched_full_configuration_reaches_plain_psnr_faster():
     """The full configuration (7000 iterations from 100k random points to the
     1M cap, 160 train / 20 held-out views at 1297x840): the learned proposal
@@ -72,7 +61,7 @@ def test_learned_batched_full_configuration_reaches_plain_psnr_faster():
     plain = F.run(seed=0, eval_every=500, timing_steps=1)
     lb = F.run(seed=0, eval_every=500, timing_steps=1, learned=True, batch=4)
     target = plain["held_out_psnr"] - 0.1
-    tp, tl = _reach(plain["psnr_curve"], target), _reach(lb["psnr_curve"], target)
+    tp, tl = F.time_to(plain["psnr_curve"], target), F.time_to(lb["psnr_curve"], target)
     print("plain", plain["held_out_psnr"], tp, "learned + batched", lb["held_out_psnr"], tl)
     assert tp is not None and tl is not None
     assert tl <= 0.8 * tp, (tl, tp)
