@@ -55,7 +55,7 @@ def test_learned_batched_full_configuration_reaches_plain_psnr_faster():
     """The full configuration (7000 iterations from 100k random points to the
     1M cap, 160 train / 20 held-out views at 1297x840): the learned proposal
     with 4 views per step reaches the plain run's final held-out PSNR - 0.1 dB
-    in at most 0.8x its wall clock (eight runs over four seeds measured 0.66-0.77) and ends
+    in at most 0.8x its wall clock (nine runs over four seeds measured 0.66-0.77) and ends
     above it."""
     from msplat_gb300 import full_run as F
     plain = F.run(seed=0, eval_every=500, timing_steps=1)
