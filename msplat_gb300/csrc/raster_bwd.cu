@@ -150,13 +150,15 @@ __device__ __forceinline__ void pixel_step(PixelState &ps, float dx, float dy, f
 }
 
 // sigma exactly as the forward pass rounds it (no contraction) and alpha from
-// the hardware exponential (ex2.approx: within 6e-7 relative for sigma in
-// [0, 5.55)); where that alpha lies within 4e-6 relative of a decision the
-// forward takes (alpha >= 1/255, the 0.999 clamp), alpha is recomputed with
-// the forward's own exponential, so both passes take the same splats and
-// clamp the same ones.  Elsewhere alpha differs from the forward's by at most
-// 6e-7 relative, which only enters the gradients and the transmittance
-// reconstruction.  false when the pixel does not take the splat.
+// the hardware exponential (__expf: documented within 2 + floor(1.173 |x|)
+// ulp, so 8 ulp or 1e-6 relative for x = -sigma in (-5.55, 0]); with the
+// forward's det_expf (2 ulp) and the product's rounding the two alphas differ
+// by less than 1.5e-6 relative.  Where this alpha lies within 4e-6 relative
+// of a decision the forward takes (alpha >= 1/255, the 0.999 clamp), alpha is
+// recomputed with the forward's own exponential, so both passes take the same
+// splats and clamp the same ones; elsewhere the difference only enters the
+// gradients and the transmittance reconstruction.  false when the pixel does
+// not take the splat.
 __device__ __forceinline__ bool splat_alpha(const float4 &xo, const float4 &cn, float dx, float dy, float &alpha) {
     const float sigma = __fmaf_rn(0.5f, __fmaf_rn(cn.x, __fmul_rn(dx, dx), __fmul_rn(__fmul_rn(cn.z, dy), dy)),
                                   __fmul_rn(__fmul_rn(cn.y, dx), dy));
