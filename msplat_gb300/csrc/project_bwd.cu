@@ -381,12 +381,16 @@ __global__ void __launch_bounds__(256, 4) k_project_bwd(ProjectBwdArgs a) {
     }
     float vm[3] = {0.f, 0.f, 0.f}, vsc[3] = {0.f, 0.f, 0.f}, vq[4] = {0.f, 0.f, 0.f, 0.f};
     float4 shin = make_float4(0.f, 0.f, 0.f, __int_as_float(0));   // colour gradient, w = 1 when it feeds SH
-    if (a.radii[i] > 0) {
-        const GradRec gr = a.grad[i];
-        const PixConicVjp pc = pix_conic_vjp(a.means[3 * i], a.means[3 * i + 1], a.means[3 * i + 2], sp,
-                                             (float)a.vt.width[0], (float)a.vt.height[0], gr, a.rec[i]);
-        CovState cs;
-        cov_state(a, i, cs);
+    // every input read before the visibility test, so the loads are in
+    // flight together (a culled Gaussian's are not used)
+    const int rad = a.radii[i];
+    const GradRec gr = a.grad[i];
+    const SplatRec rc = a.rec[i];
+    const float mx = a.means[3 * i], my = a.means[3 * i + 1], mz = a.means[3 * i + 2];
+    CovState cs;
+    cov_state(a, i, cs);
+    if (rad > 0) {
+        const PixConicVjp pc = pix_conic_vjp(mx, my, mz, sp, (float)a.vt.width[0], (float)a.vt.height[0], gr, rc);
         cov_vjp(cs, sp, pc, vm, vsc, vq);
         if (want_sh) {
             if (!(finite_bits(gr.c.x) && finite_bits(gr.c.y) && finite_bits(gr.c.z))) {
