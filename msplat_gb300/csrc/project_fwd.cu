@@ -101,6 +101,14 @@ __device__ __forceinline__ void project_one(const ProjectArgs &a, int i, int vie
     a.tiles_hit[u] = 0;
 
     const float px = a.means[3 * i], py = a.means[3 * i + 1], pz = a.means[3 * i + 2];
+    // the Gaussian's other inputs, read with its centre (before the
+    // near-plane test) so that all the loads are in flight together
+    if (!MS_GUARD(((uintptr_t)a.quats & 15) == 0, 1, i, a.nan_counts ? a.nan_counts + kDbgSlot : nullptr)) return;
+    const float4 q = *reinterpret_cast<const float4 *>(a.quats + 4 * (size_t)i);
+    const float sc0 = a.scales[3 * i], sc1 = a.scales[3 * i + 1], sc2 = a.scales[3 * i + 2];
+    const float opl = a.opacities[i];
+    const float dcv[3] = {a.features_dc[3 * (size_t)i], a.features_dc[3 * (size_t)i + 1],
+                          a.features_dc[3 * (size_t)i + 2]};
     const float *v = sp.viewmat;
     // transform_4x3 + clip_near_plane
     const float vx = v[0] * px + v[1] * py + v[2] * pz + v[3];
@@ -110,10 +118,9 @@ __device__ __forceinline__ void project_one(const ProjectArgs &a, int i, int vie
 
     // exp_scale_clamped + quat_to_rotmat + scale_rot_to_cov3d (in registers)
     float s[3];
-#pragma unroll
-    for (int k = 0; k < 3; k++) s[k] = det_expf(fminf(fmaxf(a.scales[3 * i + k], -15.f), 15.f));
-    if (!MS_GUARD(((uintptr_t)a.quats & 15) == 0, 1, i, a.nan_counts ? a.nan_counts + kDbgSlot : nullptr)) return;
-    const float4 q = *reinterpret_cast<const float4 *>(a.quats + 4 * (size_t)i);
+    s[0] = det_expf(fminf(fmaxf(sc0, -15.f), 15.f));
+    s[1] = det_expf(fminf(fmaxf(sc1, -15.f), 15.f));
+    s[2] = det_expf(fminf(fmaxf(sc2, -15.f), 15.f));
     const float qn = 1.0f / sqrtf(fmaxf(q.w * q.w + q.x * q.x + q.y * q.y + q.z * q.z, 1e-8f));
     const float w = q.x * qn, x = q.y * qn, y = q.z * qn, z = q.w * qn;
     float R[3][3];
@@ -186,7 +193,7 @@ __device__ __forceinline__ void project_one(const ProjectArgs &a, int i, int vie
     const float inv = 1.f / sqrtf(dx * dx + dy * dy + dz * dz);
     const float vdx = dx * inv, vdy = dy * inv, vdz = dz * inv;
     const int deg = sp.degrees_to_use;
-    const float *dc = a.features_dc + 3 * (size_t)i;
+    const float *dc = dcv;
     float col[3];
     bool from_stage = staged;
     if (bulk && !tc::mbar_wait(bar, 0)) {   // the row did not arrive: read it from global memory
@@ -197,7 +204,7 @@ __device__ __forceinline__ void project_one(const ProjectArgs &a, int i, int vie
     else sh_colour(dc, a.features_rest + (size_t)a.rest_bases * 3 * i, deg, vdx, vdy, vdz, col);
     // sigmoid(opacity) once per Gaussian (the reference does it per
     // intersection at pack time; same input, same bits)
-    const float opac = 1.f / (1.f + det_expf(-a.opacities[i]));
+    const float opac = 1.f / (1.f + det_expf(-opl));
 
     // A non-finite opacity does not cull (the reference zeroes such a record
     // when it packs each intersection, hybrid_sort_pack_kernel): store 0,
