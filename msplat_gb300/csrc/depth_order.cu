@@ -192,6 +192,18 @@ __global__ void __launch_bounds__(kGsThreads) k_gs_scatter(TileArgs a, int shift
     }
 }
 
+// The tile rectangles of this thread's sorted positions g0 + threadIdx.x +
+// u kAggThreads (empty past the view's last Gaussian).
+constexpr int kAggPerThread = kAggPerCta / kAggThreads;
+static_assert(kAggPerThread * kAggThreads == kAggPerCta, "whole positions per thread");
+__device__ __forceinline__ void srect_rows(const TileArgs &a, size_t vb, int g0, ushort4 (&r)[kAggPerThread]) {
+#pragma unroll
+    for (int u = 0; u < kAggPerThread; u++) {
+        const int p = g0 + (int)threadIdx.x + u * kAggThreads;
+        r[u] = p < a.vt.n ? a.srect[vb + p] : make_ushort4(0, 0, 0, 0);
+    }
+}
+
 // Block-aggregated count over sorted positions (k_count_agg's rows).
 __global__ void __launch_bounds__(kAggThreads) k_count_agg_sorted(TileArgs a) {
     pdl_enter();
@@ -199,15 +211,14 @@ __global__ void __launch_bounds__(kAggThreads) k_count_agg_sorted(TileArgs a) {
     const int view = blockIdx.y;
     const ViewGeom vg = view_geom(a.vt, view);
     const int T = vg.tiles_x * vg.tiles_y;
+    ushort4 r[kAggPerThread];   // this thread's rectangles, loaded while the histogram is cleared
+    srect_rows(a, (size_t)view * a.vt.n, blockIdx.x * kAggPerCta, r);
     for (int t = threadIdx.x; t < T; t += blockDim.x) bins[t] = 0;
     __syncthreads();
-    const size_t vb = (size_t)view * a.vt.n;
-    const int g0 = blockIdx.x * kAggPerCta, g1 = min(a.vt.n, g0 + kAggPerCta);
-    for (int p = g0 + threadIdx.x; p < g1; p += blockDim.x) {
-        const ushort4 r = a.srect[vb + p];
-        for (int y = r.y; y < r.w; y++)
-            for (int x = r.x; x < r.z; x++) atomicAdd(&bins[y * vg.tiles_x + x], 1u);
-    }
+#pragma unroll
+    for (int u = 0; u < kAggPerThread; u++)
+        for (int y = r[u].y; y < r[u].w; y++)
+            for (int x = r[u].x; x < r[u].z; x++) atomicAdd(&bins[y * vg.tiles_x + x], 1u);
     __syncthreads();
     uint32_t *row = a.cta_bins + (size_t)gridDim.x * vg.tile_base + (size_t)blockIdx.x * T;
     for (int t = threadIdx.x; t < T; t += blockDim.x) row[t] = bins[t];
@@ -221,20 +232,22 @@ __global__ void __launch_bounds__(kAggThreads) k_scatter_agg_sorted(TileArgs a) 
     const int view = blockIdx.y;
     const ViewGeom vg = view_geom(a.vt, view);
     const int T = vg.tiles_x * vg.tiles_y;
+    const int g0 = blockIdx.x * kAggPerCta;
+    ushort4 r[kAggPerThread];   // this thread's rectangles, loaded while the slot table is filled
+    srect_rows(a, (size_t)view * a.vt.n, g0, r);
     const uint32_t *row = a.cta_bins + (size_t)gridDim.x * vg.tile_base + (size_t)blockIdx.x * T;
     for (int t = threadIdx.x; t < T; t += blockDim.x) bins[t] = a.tile_offsets[vg.tile_base + t] + row[t];
     __syncthreads();
     uint32_t *keys = reinterpret_cast<uint32_t *>(a.keys);
-    const size_t vb = (size_t)view * a.vt.n;
-    const int g0 = blockIdx.x * kAggPerCta, g1 = min(a.vt.n, g0 + kAggPerCta);
-    for (int p = g0 + threadIdx.x; p < g1; p += blockDim.x) {
-        const ushort4 r = a.srect[vb + p];
-        for (int y = r.y; y < r.w; y++)
-            for (int x = r.x; x < r.z; x++) {
+#pragma unroll
+    for (int u = 0; u < kAggPerThread; u++) {
+        const uint32_t p = (uint32_t)(g0 + threadIdx.x + u * kAggThreads);
+        for (int y = r[u].y; y < r[u].w; y++)
+            for (int x = r[u].x; x < r[u].z; x++) {
                 const int lt = y * vg.tiles_x + x;
                 if (kGroup && (vg.tile_base + lt < a.tile_lo || vg.tile_base + lt >= a.tile_hi)) continue;
                 const uint64_t dst = (uint64_t)atomicAdd(&bins[lt], 1u) - (kGroup ? (uint64_t)a.isect_lo : 0ull);
-                if (dst < (uint64_t)a.capacity) keys[dst] = (uint32_t)p;   // overflow is dropped, never written
+                if (dst < (uint64_t)a.capacity) keys[dst] = p;   // overflow is dropped, never written
             }
     }
 }
