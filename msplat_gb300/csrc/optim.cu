@@ -126,23 +126,26 @@ __global__ void __launch_bounds__(256) k_sgld(AdamArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     const StepParams &sp = *a.sp;
+    // every input is loaded before the arithmetic, so the loads are in flight together
+    const float opl = a.opacities[i];
+    const float4 q = *reinterpret_cast<const float4 *>(a.quats + 4 * (size_t)i);
+    const float sc0 = a.scales[3 * i], sc1 = a.scales[3 * i + 1], sc2 = a.scales[3 * i + 2];
+    const float m0 = a.means[3 * i], m1 = a.means[3 * i + 1], m2 = a.means[3 * i + 2];
     const uint32_t base = (uint32_t)i * 4u;
     const float u0 = pcg_unit(pcg_hash32(sp.seed, base)), u1 = pcg_unit(pcg_hash32(sp.seed, base + 1u));
     const float u2 = pcg_unit(pcg_hash32(sp.seed, base + 2u)), u3 = pcg_unit(pcg_hash32(sp.seed, base + 3u));
     const float r01 = sqrtf(-2.0f * logf(u0)), r23 = sqrtf(-2.0f * logf(u2));
     const float a01 = 6.283185307179586f * u1, a23 = 6.283185307179586f * u3;
-    const float op = 1.0f / (1.0f + det_expf(-a.opacities[i]));
+    const float op = 1.0f / (1.0f + det_expf(-opl));
     const float wgt = 1.0f / (1.0f + det_expf(-100.0f * ((1.0f - op) - 0.995f)));
     const float ns = sp.noise_lr * sp.xyz_lr * wgt;
     float s01, c01;
     sincosf(a01, &s01, &c01);   // one range reduction for both
     const float n0 = r01 * c01 * ns, n1 = r01 * s01 * ns, n2 = r23 * cosf(a23) * ns;
-    const float4 q = *reinterpret_cast<const float4 *>(a.quats + 4 * (size_t)i);
     const float rql = 1.0f / sqrtf(fmaxf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w, 1e-8f));
     const float qw = q.x * rql, qx = q.y * rql, qy = q.z * rql, qz = q.w * rql;
-    float s[3];
-#pragma unroll
-    for (int k = 0; k < 3; k++) s[k] = det_expf(fminf(fmaxf(a.scales[3 * i + k], -15.0f), 15.0f));
+    const float s[3] = {det_expf(fminf(fmaxf(sc0, -15.0f), 15.0f)), det_expf(fminf(fmaxf(sc1, -15.0f), 15.0f)),
+                        det_expf(fminf(fmaxf(sc2, -15.0f), 15.0f))};
     const float r00 = 1 - 2 * (qy * qy + qz * qz), r01_ = 2 * (qx * qy - qw * qz), r02 = 2 * (qx * qz + qw * qy);
     const float r10 = 2 * (qx * qy + qw * qz), r11 = 1 - 2 * (qx * qx + qz * qz), r12 = 2 * (qy * qz - qw * qx);
     const float r20 = 2 * (qx * qz - qw * qy), r21 = 2 * (qy * qz + qw * qx), r22 = 1 - 2 * (qx * qx + qy * qy);
@@ -160,9 +163,9 @@ __global__ void __launch_bounds__(256) k_sgld(AdamArgs a) {
         const float inv = sp.max_disp / sqrtf(len2);
         v0 *= inv; v1 *= inv; v2 *= inv;
     }
-    a.means[3 * i] += v0;
-    a.means[3 * i + 1] += v1;
-    a.means[3 * i + 2] += v2;
+    a.means[3 * i] = m0 + v0;
+    a.means[3 * i + 1] = m1 + v1;
+    a.means[3 * i + 2] = m2 + v2;
 }
 
 void launch_adam(const AdamArgs &a, int num_sms, cudaStream_t s) {
