@@ -603,6 +603,7 @@ struct TrainerImpl {
                 mlp_train_batch(lrn.Xs, lrn.T, lrn.samples, lrn.img, lrn.P, lrn.G, lrn.loss, lrn.err, s);
                 mlp_adam(lrn.P, lrn.G, lrn.M, lrn.V, lrn.lr, ++lrn.adam_steps, s);
             }
+            CKA(cudaGetLastError());   // the launches above
             CKA(cudaMemcpyAsync(&lrn.last_loss, lrn.loss, 4, cudaMemcpyDeviceToHost, s));
             unsigned err = 0;
             CKA(cudaMemcpyAsync(&err, lrn.err, 4, cudaMemcpyDeviceToHost, s));
@@ -620,6 +621,7 @@ struct TrainerImpl {
         CKA(cudaMemcpyAsync(lrn.idx, idx.data(), 4 * idx.size(), cudaMemcpyHostToDevice, s));
         mlp_features(feat_args(lrn.samples, lrn.idx, lrn.Xs), s);
         mlp_snapshot(lrn.idx, lrn.samples, lrn.gstats, model.p[5], lrn.snap, s);
+        CKA(cudaGetLastError());
         CKA(cudaStreamSynchronize(s));   // idx is a host vector
         lrn.pending = step;
     }
@@ -632,6 +634,7 @@ struct TrainerImpl {
         mlp_features(feat_args(model.n, nullptr, lrn.X), s);
         mlp_forward(lrn.X, model.n, lrn.img, lrn.P, lrn.Y, lrn.err, s);
         mlp_scores(lrn.Y, model.n, lrn.score, s);
+        CKA(cudaGetLastError());
         return lrn.score;
     }
 
@@ -798,7 +801,7 @@ struct TrainerImpl {
         MsplatAdamState st = model.adam();
         MsplatMcmcStats ms;
         const float *score = learned_scores();
-        if (score && lrn.prune > 0.f) mlp_forecast_prune(lrn.Y, model.n, model.p[5], lrn.prune, lrn.pruned, stream());
+        if (score && lrn.prune > 0.f) CKA(mlp_forecast_prune(lrn.Y, model.n, model.p[5], lrn.prune, lrn.pruned, stream()));
         check(msplat_engine_mcmc_scored(eng, &g, &st, model.cap, cfg.cullRadius, &reloc_count, score, &ms), "mcmc");
         model.n = ms.num_active;
         if (crossed(prev, step, 1000))

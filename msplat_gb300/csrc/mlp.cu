@@ -524,10 +524,12 @@ __global__ void k_forecast_prune(const float2 *y, int n, float *opacities, float
     if (y[i].x <= tau && atomicAdd(count, 1u) < max_n) opacities[i] = -20.f;
 }
 
-void mlp_forecast_prune(const float2 *y, int n, float *opacities, float tau, unsigned *count, cudaStream_t s) {
-    if (n <= 0) return;
-    cudaMemsetAsync(count, 0, sizeof(unsigned), s);
+cudaError_t mlp_forecast_prune(const float2 *y, int n, float *opacities, float tau, unsigned *count, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    const cudaError_t e = cudaMemsetAsync(count, 0, sizeof(unsigned), s);
+    if (e != cudaSuccess) return e;
     k_forecast_prune<<<(n + 255) / 256, 256, 0, s>>>(y, n, opacities, tau, count, (unsigned)(n / 20));
+    return cudaGetLastError();
 }
 
 void mlp_features(const MlpFeatArgs &a, cudaStream_t s) {

@@ -45,6 +45,8 @@ void mlp_snapshot(const int *idx, int S, const float4 *gstats, const float *opac
 void mlp_eval(const float2 *pred, const float2 *T, const float4 *snap, int S, float *sums, cudaStream_t s);
 // sampling weights from the MLP outputs
 void mlp_scores(const float2 *y, int n, float *score, cudaStream_t s);
-void mlp_forecast_prune(const float2 *y, int n, float *opacities, float tau, unsigned *count, cudaStream_t s);
+// forecast pruning: the logit of each Gaussian whose forecast opacity is at
+// most tau becomes -20 (at most n / 20 of them); returns the launch status
+cudaError_t mlp_forecast_prune(const float2 *y, int n, float *opacities, float tau, unsigned *count, cudaStream_t s);
 
 }  // namespace msplat
