@@ -47,7 +47,9 @@ MsplatDataset msplat_dataset_create_from_memory(int num_cameras, const float *ca
 
 /* Replaces the trainer's Gaussians (host arrays in the reference layouts, n
  * rows) and resets the optimizer, as loading a trained PLY does
- * (Model::loadPly, core/src/model.cpp:675-690). */
+ * (Model::loadPly, core/src/model.cpp:675-690).  rest_bases in [0, 15];
+ * every array is required when n > 0 (features_rest only when rest_bases >
+ * 0).  Returns 0, -1 for invalid arguments, -2 on a failure. */
 int msplat_trainer_set_gaussians(MsplatTrainer t, int n, int rest_bases, const float *means, const float *scales,
                                  const float *quats, const float *features_dc, const float *features_rest,
                                  const float *opacities);

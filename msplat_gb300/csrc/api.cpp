@@ -1313,14 +1313,19 @@ void msplat_cleanup(void) {}
 int msplat_trainer_set_gaussians(MsplatTrainer t, int n, int rest_bases, const float *means, const float *scales,
                                  const float *quats, const float *features_dc, const float *features_rest,
                                  const float *opacities) {
-    if (!t || n < 0) return -1;
+    // the engine takes up to 15 rest bases (SH degree 3); every array must be
+    // given when there are rows (features_rest only with rest bases)
+    if (!t || n < 0 || rest_bases < 0 || rest_bases > 15) return -1;
+    if (n > 0 && (!means || !scales || !quats || !features_dc || !opacities || (rest_bases > 0 && !features_rest)))
+        return -1;
     return guard("set_gaussians", [&]() {
         HostGaussians h;
         h.n = n;
         h.rest = rest_bases;
         const float *src[6] = {means, scales, quats, features_dc, features_rest, opacities};
         const size_t s[6] = {3, 3, 4, 3, (size_t)3 * rest_bases, 1};
-        for (int g = 0; g < 6; g++) h.a[g].assign(src[g], src[g] + (size_t)n * s[g]);
+        for (int g = 0; g < 6; g++)
+            if (src[g]) h.a[g].assign(src[g], src[g] + (size_t)n * s[g]);
         TR(t)->set_model(h, false);
         return 0;
     }, -2);
@@ -1403,7 +1408,7 @@ int msplat_trainer_learned_stats(MsplatTrainer t, float *last_loss, int *rounds)
 }
 
 int msplat_trainer_learned_eval(MsplatTrainer t, float mse[4]) {
-    if (!t) return -1;
+    if (!t || !mse) return -1;
     const auto &l = TR(t)->lrn;
     for (int k = 0; k < 4; k++) mse[k] = l.eval_rounds ? (float)(l.eval_sum[k] / l.eval_rounds) : 0.f;
     return l.eval_rounds;

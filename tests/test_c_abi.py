@@ -47,3 +47,40 @@ def test_prepare_camera_matches_oracle():
         b = O.prepare_cam(cam.cam_to_world, cam.width, cam.height, cam.fx, cam.fy)
         for x, y in zip(a, b):
             assert np.array_equal(x, y)
+
+
+def test_null_handles_and_bad_arguments_rejected(lib):
+    """Every entry point checks its handle and arguments before any CUDA
+    call: a null engine or trainer, or an invalid argument, returns -1."""
+    c = ctypes
+    vp, fp = c.c_void_p, c.POINTER(c.c_float)
+    lib.msplat_engine_set_tuning.argtypes = [vp, vp]
+    lib.msplat_engine_get_tuning.argtypes = [vp, vp]
+    lib.msplat_engine_set_graphs.argtypes = [vp, c.c_int]
+    lib.msplat_engine_set_isect_budget.argtypes = [vp, c.c_longlong]
+    lib.msplat_engine_synchronize.argtypes = [vp]
+    lib.msplat_engine_read.argtypes = [vp, c.c_char_p, vp, c.c_longlong]
+    lib.msplat_engine_last_error.argtypes = [vp]
+    lib.msplat_engine_last_error.restype = c.c_char_p
+    buf = (c.c_byte * 256)()
+    assert lib.msplat_engine_set_tuning(None, buf) == -1
+    assert lib.msplat_engine_get_tuning(None, buf) == -1
+    assert lib.msplat_engine_set_graphs(None, 1) == -1
+    assert lib.msplat_engine_set_isect_budget(None, 1 << 20) == -1
+    assert lib.msplat_engine_synchronize(None) == -1
+    assert lib.msplat_engine_read(None, b"out_img", buf, 4) == -1
+    assert lib.msplat_engine_last_error(None) == b"null engine"
+
+    lib.msplat_trainer_set_gaussians.argtypes = [vp, c.c_int, c.c_int, fp, fp, fp, fp, fp, fp]
+    lib.msplat_trainer_set_learned_prune.argtypes = [vp, c.c_float]
+    lib.msplat_trainer_set_batch_views.argtypes = [vp, c.c_int, c.c_float]
+    lib.msplat_trainer_set_isect_budget.argtypes = [vp, c.c_float]
+    lib.msplat_trainer_learned_eval.argtypes = [vp, fp]
+    lib.msplat_trainer_splat_count.argtypes = [vp]
+    mse = (c.c_float * 4)()
+    assert lib.msplat_trainer_set_gaussians(None, 1, 15, None, None, None, None, None, None) == -1
+    assert lib.msplat_trainer_set_learned_prune(None, 0.02) == -1
+    assert lib.msplat_trainer_set_batch_views(None, 4, 0.0) == -1
+    assert lib.msplat_trainer_set_isect_budget(None, 64.0) == -1
+    assert lib.msplat_trainer_learned_eval(None, mse) == -1
+    assert lib.msplat_trainer_splat_count(None) == 0
