@@ -39,7 +39,9 @@ float msplat_ssim_eval(const float *img, const float *gt, int height, int width)
  * plus the seed point cloud (xyz float, rgb uint8).  normalize applies the
  * reference's camera centring and scaling (input_data.cpp:115-169); with
  * eval_mode every test_every-th camera is a test camera
- * (input_data.cpp:199-208).  All inputs are copied. */
+ * (input_data.cpp:199-208).  All inputs are copied.  NULL for negative
+ * counts, missing pose, intrinsics, size or point arrays, or an empty image
+ * size. */
 MsplatDataset msplat_dataset_create_from_memory(int num_cameras, const float *cam_to_world, const float *intrinsics,
                                                const int *sizes, const uint8_t *const *images,
                                                const uint8_t *const *masks, int num_points, const float *xyz,

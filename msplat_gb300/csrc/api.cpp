@@ -1108,6 +1108,11 @@ MsplatDataset msplat_dataset_create_from_memory(int num_cameras, const float *ca
                                                const int *sizes, const uint8_t *const *images,
                                                const uint8_t *const *masks, int num_points, const float *xyz,
                                                const uint8_t *rgb, bool eval_mode, int test_every, bool normalize) {
+    if (num_cameras < 0 || num_points < 0) return nullptr;
+    if (num_cameras > 0 && (!cam_to_world || !intrinsics || !sizes)) return nullptr;
+    if (num_points > 0 && (!xyz || !rgb)) return nullptr;
+    for (int i = 0; i < num_cameras; i++)
+        if (sizes[2 * i] <= 0 || sizes[2 * i + 1] <= 0) return nullptr;
     return guard("dataset", [&]() -> MsplatDataset {
         auto d = std::make_unique<DatasetImpl>();
         std::vector<HostCamera> cams(num_cameras);
@@ -1187,7 +1192,7 @@ int msplat_dataset_num_train(MsplatDataset ds) { return ds ? (int)DS(ds)->train.
 int msplat_dataset_num_test(MsplatDataset ds) { return ds ? (int)DS(ds)->test.size() : 0; }
 
 void msplat_dataset_camera_pose(MsplatDataset ds, int i, float c2w[16]) {
-    if (ds && i >= 0 && i < (int)DS(ds)->train.size()) std::memcpy(c2w, DS(ds)->train[i].c2w, 64);
+    if (ds && c2w && i >= 0 && i < (int)DS(ds)->train.size()) std::memcpy(c2w, DS(ds)->train[i].c2w, 64);
 }
 
 MsplatTrainer msplat_trainer_create(MsplatDataset ds, MsplatConfig config) {
@@ -1240,7 +1245,7 @@ MsplatPixelBuffer msplat_trainer_render(MsplatTrainer t, int i, bool useTest) {
 
 MsplatPixelBuffer msplat_trainer_render_pose(MsplatTrainer t, const float c2w[16], int ref) {
     MsplatPixelBuffer empty{nullptr, 0, 0};
-    if (!t) return empty;
+    if (!t || !c2w) return empty;
     return guard("render_pose", [&]() {
         auto &cams = TR(t)->ds->train;
         if (ref < 0 || ref >= (int)cams.size()) return empty;
@@ -1256,7 +1261,7 @@ void msplat_trainer_render_pose_to_buffer(MsplatTrainer t, const float c2w[16], 
                                           int *oh) {
     if (ow) *ow = 0;
     if (oh) *oh = 0;
-    if (!t) return;
+    if (!t || !c2w) return;
     guard("render_pose_to_buffer", [&]() {
         auto &cams = TR(t)->ds->train;
         if (ref < 0 || ref >= (int)cams.size()) return 0;
@@ -1463,7 +1468,7 @@ void msplat_viewer_set_background(MsplatViewer v, float r, float g, float b) {
 }
 
 void msplat_viewer_render(MsplatViewer v, const float c2w[16], uint8_t *out) {
-    if (!v || !out) return;
+    if (!v || !c2w || !out) return;
     guard("viewer_render", [&]() {
         ViewerImpl *vw = VW(v);
         vw->render(c2w);
@@ -1486,7 +1491,7 @@ void msplat_viewer_get_size(MsplatViewer v, int *w, int *h) {
 void *msplat_viewer_render_buffer(MsplatViewer v, const float c2w[16], int *w, int *h) {
     if (w) *w = 0;
     if (h) *h = 0;
-    if (!v) return nullptr;
+    if (!v || !c2w) return nullptr;
     return guard("viewer_render_buffer", [&]() -> void * {
         ViewerImpl *vw = VW(v);
         vw->render(c2w);
@@ -1500,12 +1505,12 @@ void *msplat_viewer_render_buffer(MsplatViewer v, const float c2w[16], int *w, i
 
 void msplat_viewer_bounds(MsplatViewer v, float lo[3], float hi[3]) {
     if (!v) return;
-    std::memcpy(lo, VW(v)->bmin, 12);
-    std::memcpy(hi, VW(v)->bmax, 12);
+    if (lo) std::memcpy(lo, VW(v)->bmin, 12);
+    if (hi) std::memcpy(hi, VW(v)->bmax, 12);
 }
 
 void msplat_viewer_density_center(MsplatViewer v, float c[3]) {
-    if (v) std::memcpy(c, VW(v)->dcenter, 12);
+    if (v && c) std::memcpy(c, VW(v)->dcenter, 12);
 }
 
 void *msplat_viewer_command_queue(MsplatViewer v) { return v ? msplat_engine_stream(VW(v)->eng) : nullptr; }

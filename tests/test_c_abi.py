@@ -84,3 +84,20 @@ def test_null_handles_and_bad_arguments_rejected(lib):
     assert lib.msplat_trainer_set_isect_budget(None, 64.0) == -1
     assert lib.msplat_trainer_learned_eval(None, mse) == -1
     assert lib.msplat_trainer_splat_count(None) == 0
+
+
+def test_dataset_from_memory_rejects_bad_arguments(lib):
+    """msplat_dataset_create_from_memory returns NULL (no dataset, no CUDA
+    call) for negative counts, missing arrays or empty image sizes."""
+    c = ctypes
+    vp = c.c_void_p
+    f = lib.msplat_dataset_create_from_memory
+    f.restype = vp
+    f.argtypes = [c.c_int, vp, vp, vp, vp, vp, c.c_int, vp, vp, c.c_bool, c.c_int, c.c_bool]
+    c2w = (c.c_float * 16)()
+    intr = (c.c_float * 4)(100.0, 100.0, 32.0, 32.0)
+    zero = (c.c_int * 2)(0, 64)
+    assert f(-1, None, None, None, None, None, 0, None, None, False, 8, False) is None
+    assert f(1, None, intr, zero, None, None, 0, None, None, False, 8, False) is None
+    assert f(1, c2w, intr, zero, None, None, 0, None, None, False, 8, False) is None
+    assert f(0, None, None, None, None, None, 5, None, None, False, 8, False) is None
