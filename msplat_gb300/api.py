@@ -188,6 +188,8 @@ class Dataset:
                                                 ptrs, mptrs, xyz.shape[0], _fp(xyz),
                                                 rgb.ctypes.data_as(C.POINTER(C.c_uint8)), eval_mode, test_every,
                                                 normalize)
+        if not h:
+            raise RuntimeError("could not build a dataset from the arrays (empty image size or missing points?)")
         return cls(_handle=h)
 
     @property

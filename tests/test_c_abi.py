@@ -101,3 +101,23 @@ def test_dataset_from_memory_rejects_bad_arguments(lib):
     assert f(1, None, intr, zero, None, None, 0, None, None, False, 8, False) is None
     assert f(1, c2w, intr, zero, None, None, 0, None, None, False, 8, False) is None
     assert f(0, None, None, None, None, None, 5, None, None, False, 8, False) is None
+
+
+def test_dataset_from_arrays_on_host():
+    """Dataset.from_arrays builds the dataset on the host (no GPU): train/test
+    split by test_every, an empty point cloud allowed, and an image size of
+    zero refused with an error."""
+    import numpy as np
+    from msplat_gb300 import api as A, synthetic as S
+    cams = S.config_small(0).train_cams[:3]
+    imgs = [np.zeros((c.height, c.width, 3), np.uint8) for c in cams]
+    xyz = np.zeros((10, 3), np.float32)
+    rgb = np.full((10, 3), 128, np.uint8)
+    ds = A.Dataset.from_arrays(cams, imgs, xyz, rgb, eval_mode=True, test_every=2)
+    assert (ds.num_train, ds.num_test) == (1, 2)
+    ds = A.Dataset.from_arrays(cams, imgs, np.zeros((0, 3), np.float32), np.zeros((0, 3), np.uint8))
+    assert (ds.num_train, ds.num_test) == (3, 0)
+    bad = S.config_small(0).train_cams[0]
+    bad.width = 0
+    with pytest.raises(RuntimeError):
+        A.Dataset.from_arrays([bad], [np.zeros((1, 1, 3), np.uint8)], xyz, rgb)
