@@ -65,33 +65,60 @@ __global__ void __launch_bounds__(kGsThreads) k_gs_hist(TileArgs a, int shift, c
 }
 
 // Per digit (one warp each), the exclusive scan of its blocks' counts in
-// place, and the digit's total to dtot[view][digit].  Each lane takes every
-// 32nd block; four rounds of loads are issued before they are scanned.
+// place, and the digit's total to dtot[view][digit].  In rounds of 1024
+// blocks: the warp loads the round's counts at once (coalesced) into its
+// shared buffer, each lane sums a contiguous run of 32, a warp scan of the
+// run sums gives each run's offset, and the lane rewrites its run as
+// offsets; the buffer is padded by a word per 32 (no bank conflicts either
+// way).
+constexpr int kDsPer = 32;                       // counts per lane per round
+constexpr int kDsRound = 32 * kDsPer;            // counts per warp per round
+__device__ __forceinline__ int ds_pad(int i) { return i + (i >> 5); }
+
 __global__ void __launch_bounds__(256) k_gs_digit_scan(TileArgs a, int nb) {
     pdl_enter();
-    const int lane = threadIdx.x & 31;
-    const int d = blockIdx.x * 8 + (threadIdx.x >> 5), view = blockIdx.y;
+    __shared__ uint32_t buf[8][kDsRound + kDsRound / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int d = blockIdx.x * 8 + w, view = blockIdx.y;
     uint32_t *h = a.gs_hist + (size_t)view * kGsDigits * nb + (size_t)d * nb;
+    uint32_t *sb = buf[w];
     uint32_t carry = 0;
-    for (int b0 = 0; b0 < nb; b0 += 128) {
-        uint32_t v[4];
+    for (int b0 = 0; b0 < nb; b0 += kDsRound) {
+        const int m = min(nb - b0, kDsRound);
+        uint32_t v[kDsPer];
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const int b = b0 + 32 * k + lane;
-            v[k] = b < nb ? h[b] : 0u;
+        for (int k = 0; k < kDsPer; k++) {
+            const int b = 32 * k + lane;
+            v[k] = b < m ? h[b0 + b] : 0u;
         }
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
-            uint32_t inc = v[k];
+        for (int k = 0; k < kDsPer; k++) sb[ds_pad(32 * k + lane)] = v[k];
+        __syncwarp();
+        uint32_t sum = 0;
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
-                if (lane >= o) inc += u;
-            }
-            const int b = b0 + 32 * k + lane;
-            if (b < nb) h[b] = carry + inc - v[k];
-            carry += __shfl_sync(0xffffffffu, inc, 31);
+        for (int j = 0; j < kDsPer; j++) sum += sb[ds_pad(lane * kDsPer + j)];
+        uint32_t inc = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += u;
         }
+        uint32_t run = carry + inc - sum;
+#pragma unroll
+        for (int j = 0; j < kDsPer; j++) {
+            const int i = ds_pad(lane * kDsPer + j);
+            const uint32_t x = sb[i];
+            sb[i] = run;
+            run += x;
+        }
+        carry += __shfl_sync(0xffffffffu, inc, 31);
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < kDsPer; k++) {
+            const int b = 32 * k + lane;
+            if (b < m) h[b0 + b] = sb[ds_pad(b)];
+        }
+        __syncwarp();   // the buffer is refilled by the next round
     }
     if (lane == 0) a.gs_dtot[(size_t)view * kGsDigits + d] = carry;
 }
