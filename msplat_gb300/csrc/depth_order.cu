@@ -33,10 +33,12 @@ constexpr int kGsItems = kGsPerCta / kGsThreads;   // keys per thread of a radix
 static_assert(kGsItems * kGsThreads == kGsPerCta, "whole rounds of 32 keys per warp");
 static_assert(kAggPerCta == 1 << kAggShift, "a run is the positions p with equal p >> kAggShift");
 
+// (radius and depth are loaded together: a culled record's depth is read
+// but not used)
 __device__ __forceinline__ uint32_t gs_key0(const TileArgs &a, size_t u) {
-    if (a.radii[u] <= 0) return 0xffffffffu;
+    const int r = a.radii[u];
     const float d = a.depths[u];
-    return (finite_bits(d) && d > 0.0f) ? __float_as_uint(d) : 0xffffffffu;
+    return (r > 0 && finite_bits(d) && d > 0.0f) ? __float_as_uint(d) : 0xffffffffu;
 }
 
 constexpr uint32_t kGsMask = kGsDigits - 1;
@@ -50,15 +52,18 @@ __global__ void __launch_bounds__(kGsThreads) k_gs_hist(TileArgs a, int shift, c
     __shared__ uint32_t h[kGsDigits];
     const int view = blockIdx.y, n = a.vt.n, nb = gridDim.x;
     const size_t vb = (size_t)view * n;
+    const int e0 = blockIdx.x * kGsPerCta;
+    uint32_t key[kGsItems];   // all of the thread's keys, loaded while the counts are cleared
+#pragma unroll
+    for (int j = 0; j < kGsItems; j++) {
+        const int e = e0 + j * kGsThreads + (int)threadIdx.x;
+        key[j] = e < n ? (kFirst ? gs_key0(a, vb + e) : key_in[vb + e]) : 0u;
+    }
     for (int d = threadIdx.x; d < kGsDigits; d += kGsThreads) h[d] = 0;
     __syncthreads();
-    const int e0 = blockIdx.x * kGsPerCta;
-    for (int k = threadIdx.x; k < kGsPerCta; k += kGsThreads) {
-        const int e = e0 + k;
-        if (e >= n) break;
-        const uint32_t key = kFirst ? gs_key0(a, vb + e) : key_in[vb + e];
-        atomicAdd(&h[(key >> shift) & kGsMask], 1u);
-    }
+#pragma unroll
+    for (int j = 0; j < kGsItems; j++)
+        if (e0 + j * kGsThreads + (int)threadIdx.x < n) atomicAdd(&h[(key[j] >> shift) & kGsMask], 1u);
     __syncthreads();
     for (int d = threadIdx.x; d < kGsDigits; d += kGsThreads)
         a.gs_hist[(size_t)view * kGsDigits * nb + (size_t)d * nb + blockIdx.x] = h[d];
@@ -143,6 +148,23 @@ __global__ void __launch_bounds__(kGsThreads) k_gs_scatter(TileArgs a, int shift
     const int view = blockIdx.y, n = a.vt.n, nb = gridDim.x;
     const size_t vb = (size_t)view * n;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    // the warp's keys, ids and (last pass) tile rectangles, all loaded before
+    // the block's digit starts are computed
+    const int e0 = blockIdx.x * kGsPerCta + wid * (32 * kGsItems);
+    uint32_t kv[kGsItems], vv[kGsItems], rank[kGsItems];
+    ushort4 rc[kGsItems];
+#pragma unroll
+    for (int j = 0; j < kGsItems; j++) {
+        const int e = e0 + j * 32 + lane;
+        const bool valid = e < n;
+        kv[j] = valid ? (kFirst ? gs_key0(a, vb + e) : key_in[vb + e]) : 0u;
+        vv[j] = valid ? (kFirst ? (uint32_t)e : val_in[vb + e]) : 0u;
+    }
+    if (srect_out) {
+#pragma unroll
+        for (int j = 0; j < kGsItems; j++)
+            rc[j] = (e0 + j * 32 + lane < n && kv[j] != 0xffffffffu) ? a.rect[vb + vv[j]] : make_ushort4(0, 0, 0, 0);
+    }
     for (int k = tid; k < (kGsThreads / 32) * kGsDigits; k += kGsThreads) (&wcnt[0][0])[k] = 0;
     {   // this block's start for digits kGsDigitsPerThread tid ..: the digit's
         // start (exclusive scan of the digit totals) + the earlier blocks' keys
@@ -170,15 +192,11 @@ __global__ void __launch_bounds__(kGsThreads) k_gs_scatter(TileArgs a, int shift
         }
     }
     __syncthreads();
-    const int e0 = blockIdx.x * kGsPerCta + wid * (32 * kGsItems);
     const uint32_t lt = (1u << lane) - 1u;
-    uint32_t kv[kGsItems], vv[kGsItems], rank[kGsItems];
 #pragma unroll
     for (int j = 0; j < kGsItems; j++) {
         const int e = e0 + j * 32 + lane;
         const bool valid = e < n;
-        kv[j] = valid ? (kFirst ? gs_key0(a, vb + e) : key_in[vb + e]) : 0u;
-        vv[j] = valid ? (kFirst ? (uint32_t)e : val_in[vb + e]) : 0u;
         const uint32_t d = valid ? ((kv[j] >> shift) & kGsMask) : (uint32_t)kGsDigits;
         uint32_t peers = __ballot_sync(0xffffffffu, valid);
 #pragma unroll
@@ -213,8 +231,7 @@ __global__ void __launch_bounds__(kGsThreads) k_gs_scatter(TileArgs a, int shift
         if (MS_GUARD(pos < (uint32_t)n, 7, pos, a.nan_counts ? a.nan_counts + kDbgSlot : nullptr)) {
             key_out[vb + pos] = kv[j];
             val_out[vb + pos] = vv[j];
-            if (srect_out)
-                srect_out[vb + pos] = kv[j] == 0xffffffffu ? make_ushort4(0, 0, 0, 0) : a.rect[vb + vv[j]];
+            if (srect_out) srect_out[vb + pos] = rc[j];
         }
     }
 }
