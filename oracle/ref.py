@@ -58,7 +58,7 @@ def project_fwd(g, cam, degrees_to_use, clip=0.01):
     o = {"xys": np.zeros((n, 2), np.float32), "depths": np.zeros(n, np.float32), "radii": np.zeros(n, np.int32),
          "conics": np.zeros((n, 3), np.float32), "num_tiles_hit": np.zeros(n, np.int32),
          "colors": np.zeros((n, 3), np.float32), "aabb": np.zeros((n, 2), np.float32),
-         "nan_counts": np.zeros(16, np.uint32)}
+         "nan_counts": np.zeros(16, np.uint32), "backward_ran": np.zeros(1, np.int32)}
     deg = {0: 0, 3: 1, 8: 2, 15: 3}[g.features_rest.shape[1]]
     cp = np.asarray(cam["cam_pos"], np.float32)
     vm = np.ascontiguousarray(cam["viewmat"], np.float32).ravel()
@@ -149,7 +149,10 @@ def raster_step(fwd, opacities, cam, gt=None, mask=None, v_img=None, background=
     contributors, loss sum, dL/dimage and the per-Gaussian rasterizer
     gradients.  gt (uint8 [H,W,3]) runs the loss; otherwise v_img is the image
     gradient.  k_max > 1: the chunked rasterizers with k_max chunks of
-    chunk_size splats (the caller applies the reference's K rule)."""
+    chunk_size splats (the caller applies the reference's K rule); the
+    chunked backward runs only where it is defined (every 8x8 threadgroup's
+    lanes all leave or all stay at its early exit in each chunk), and
+    "backward_ran" says whether the gradients were computed."""
     W, H = int(cam["width"]), int(cam["height"])
     n = fwd["radii"].shape[0]
     T = ((W + 15) // 16) * ((H + 15) // 16)
@@ -160,7 +163,7 @@ def raster_step(fwd, opacities, cam, gt=None, mask=None, v_img=None, background=
          "v_rendered": np.zeros((H, W, 3), np.float32) if v_img is None else np.ascontiguousarray(v_img, np.float32).copy(),
          "v_xy": np.zeros((n, 2), np.float32), "v_conic": np.zeros((n, 3), np.float32),
          "v_colors": np.zeros((n, 3), np.float32), "v_opacity": np.zeros(n, np.float32),
-         "nan_counts": np.zeros(16, np.uint32)}
+         "nan_counts": np.zeros(16, np.uint32), "backward_ran": np.zeros(1, np.int32)}
     bg = np.asarray(background, np.float32)
     gt = None if gt is None else np.ascontiguousarray(gt, np.uint8)
     mask = None if mask is None else np.ascontiguousarray(mask, np.uint8)
@@ -174,10 +177,12 @@ def raster_step(fwd, opacities, cam, gt=None, mask=None, v_img=None, background=
         C.c_float(ssim_weight), C.c_float(loss_inv_n if loss_inv_n is not None else 1.0 / (3.0 * W * H)),
         _p(o["tile_bins"], IP), _p(o["gaussian_ids"], IP), C.c_longlong(cap), _p(o["out_img"]), _p(o["final_Ts"]),
         _p(o["final_idx"], IP), _p(o["loss_sum"]), _p(o["v_rendered"]), _p(o["v_xy"]), _p(o["v_conic"]),
-        _p(o["v_colors"]), _p(o["v_opacity"]), _p(o["nan_counts"], UP), int(k_max), int(chunk_size))
+        _p(o["v_colors"]), _p(o["v_opacity"]), _p(o["nan_counts"], UP), int(k_max), int(chunk_size),
+        _p(o["backward_ran"], IP))
     if m < 0:
         raise RuntimeError("more intersections than ids_capacity")
     o["num_isect"] = int(m)
+    o["backward_ran"] = bool(o["backward_ran"][0])
     o["gaussian_ids"] = o["gaussian_ids"][:m].copy()
     o["loss"] = float(o["loss_sum"][0]) / (W * H)
     o["raster_grads"] = np.concatenate([o["v_xy"], o["v_conic"], o["v_colors"], o["v_opacity"][:, None]], axis=1)

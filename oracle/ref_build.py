@@ -25,12 +25,16 @@ Left out on purpose, with the reason:
   * the tile scan and the per-tile sort + pack (prefix_sum_tiles_kernel,
     hybrid_sort_pack_kernel): their 1024-thread bitonic networks are not
     emulated; ref_kernels.cpp restates what they compute (exclusive scans of
-    the padded and exact counts, ascending keys per tile, the pack gates);
-  * the chunked backward (compute_chunk_prefix_suffix_kernel,
-    rasterize_backward_chunked_kernel): lanes whose pixel has no contributor
-    in a chunk return before the kernel's SIMD-group broadcasts from lane 0,
-    so its result is undefined when lane 0 is one of them (after a chunked
-    forward only the forward stages and the loss are compared).
+    the padded and exact counts, ascending keys per tile, the pack gates).
+
+The chunked backward (compute_chunk_prefix_suffix_kernel,
+rasterize_backward_chunked_kernel) is compiled but run only where it is
+defined: a lane whose pixel has no contributor in a chunk (or lies outside
+the image) returns before the kernel's barriers and SIMD-group broadcasts
+from lane 0, which is undefined on the GPU when lane 0 is such a lane and
+would leave the host emulation's barriers waiting.  ref_kernels.cpp runs it
+only when, for every (8x8 threadgroup, chunk), either all of the group's
+lanes return there or none does, and reports whether it ran.
 
 The rasterizers and the SSIM kernels use threadgroup memory, barriers and
 SIMD-group functions; metal_shim.h runs their threadgroups on host threads.
@@ -104,6 +108,13 @@ KERNELS = {
     "rasterize_forward_chunked_kernel": ["tile_bounds", "img_size", "channels", "tile_bins", "packed_xy_opac",
                                          "packed_conic", "packed_rgb", "chunk_T", "chunk_C", "chunk_final_idx",
                                          "chunk_size", "K_max", "blockDim", "nan_counts", "blockIdx", "tr"],
+    "compute_chunk_prefix_suffix_kernel": ["num_pixels", "K_max", "chunk_T", "chunk_C", "chunk_final_idx",
+                                           "prefix_T", "after_C", "img_size", "gp"],
+    "rasterize_backward_chunked_kernel": ["tile_bounds", "img_size", "gaussian_ids_sorted", "tile_bins",
+                                          "packed_xy_opac", "packed_conic", "packed_rgb", "background", "final_Ts",
+                                          "chunk_final_idx", "prefix_T_buf", "chunk_T_buf", "after_C_buf",
+                                          "v_output", "v_xy", "v_conic", "v_rgb", "v_opacity", "chunk_size", "K_max",
+                                          "gp", "blockIdx", "tr", "warp_size", "wr"],
     "rasterize_forward_merge_kernel": ["num_pixels", "K_max", "chunk_T", "chunk_C", "chunk_final_idx", "final_Ts",
                                        "final_index", "out_img", "background", "img_size", "gp"],
     "ssim_h_fwd_kernel": ["rendered", "gt", "img_size", "ssim_h_buf", "gid", "lid", "tr", "tgid"],

@@ -110,6 +110,16 @@ void k_raster_fwd_chunked(uint3 &tile_bounds, uint3 &img_size, uint &channels, i
 #include "k_rasterize_forward_chunked_kernel.inc"
 }
 
+// rasterize_backward_chunked_kernel (msplat_metal.metal:3179-3366)
+void k_raster_bwd_chunked(uint3 &tile_bounds, uint2 &img_size, int32_t *gaussian_ids_sorted, int *tile_bins,
+                          float *packed_xy_opac, float *packed_conic, float *packed_rgb, float *background,
+                          float *final_Ts, int *chunk_final_idx, float *prefix_T_buf, float *chunk_T_buf,
+                          float *after_C_buf, float *v_output, atomic_float *v_xy, atomic_float *v_conic,
+                          atomic_float *v_rgb, atomic_float *v_opacity, uint &chunk_size, uint &K_max, uint3 gp,
+                          uint3 blockIdx, uint tr, uint warp_size, uint wr) {
+#include "k_rasterize_backward_chunked_kernel.inc"
+}
+
 // rasterize_forward_merge_kernel (msplat_metal.metal:3081-3134)
 void k_raster_merge(uint &num_pixels, uint &K_max, float *chunk_T, float *chunk_C, int *chunk_final_idx,
                     float *final_Ts, int *final_index, float *out_img, float *background, uint2 &img_size, uint2 gp) {
@@ -138,6 +148,41 @@ void k_ssim_v_bwd(float *rendered, uchar *gt, float *ssim_h_buf, uint2 &img_size
 
 #undef threadgroup
 #define threadgroup
+
+// compute_chunk_prefix_suffix_kernel (msplat_metal.metal:3139-3175)
+void k_chunk_prefix_suffix(uint &num_pixels, uint &K_max, float *chunk_T, float *chunk_C, int *chunk_final_idx,
+                           float *prefix_T, float *after_C, uint2 &img_size, uint2 gp) {
+#include "k_compute_chunk_prefix_suffix_kernel.inc"
+}
+
+// Whether rasterize_backward_chunked_kernel is defined on these inputs: in
+// every (8x8 threadgroup, chunk) either every lane returns at its early exit
+// (empty chunk, pixel outside the image, or no contributor in the chunk:
+// .metal:3242-3247) or none does; otherwise lanes that returned would miss
+// the group's barriers and the SIMD-group broadcasts from lane 0.
+bool chunked_backward_defined(uint W, uint H, uint tiles_x, const int *bins, const int *chunk_final_idx, uint K,
+                              uint chunk) {
+    const uint P = W * H;
+    for (uint k = 0; k < K; k++)
+        for (uint by = 0; by < (H + 7) / 8; by++)
+            for (uint bx = 0; bx < (W + 7) / 8; bx++) {
+                const uint tile = (by * 8 / 16) * tiles_x + (bx * 8 / 16);
+                const int cs = bins[2 * tile] + (int)(k * chunk);
+                const int ce = std::min(bins[2 * tile] + (int)((k + 1) * chunk), bins[2 * tile + 1]);
+                if (cs >= ce) continue;   // the whole group returns
+                int ret = 0;
+                for (uint ty = 0; ty < 8; ty++)
+                    for (uint tx = 0; tx < 8; tx++) {
+                        const uint i = by * 8 + ty, j = bx * 8 + tx;
+                        const bool inside = i < H && j < W;
+                        const uint pix = std::min(i * W + j, P - 1);
+                        const int bin_final = inside ? chunk_final_idx[(size_t)k * P + pix] : -1;
+                        ret += bin_final < cs ? 1 : 0;
+                    }
+                if (ret != 0 && ret != 64) return false;
+            }
+    return true;
+}
 
 // Runs a grid of gx x gy threadgroups of bx x by threads: one host thread
 // per GPU thread, the groups one after another, a barrier between groups.
@@ -301,7 +346,7 @@ long long ref_raster_step(int n, const float *xys, const float *depths, const in
                           float loss_inv_n, int *tile_bins_out, int *gaussian_ids, long long ids_capacity,
                           float *out_img, float *final_Ts, int *final_idx, float *loss_sum, float *v_rendered,
                           float *v_xy, float *v_conic, float *v_colors, float *v_opacity, uint32_t nan_counts[16],
-                          int k_max, int chunk_size) {
+                          int k_max, int chunk_size, int *backward_ran) {
     const uint W = (uint)width, H = (uint)height;
     uint3 tile_bounds((W + 15) / 16, (H + 15) / 16, 1u);
     const uint T = tile_bounds.x * tile_bounds.y;
@@ -417,20 +462,35 @@ long long ref_raster_step(int n, const float *xys, const float *depths, const in
     std::fill(v_colors, v_colors + 3 * (size_t)n, 0.f);
     std::fill(v_opacity, v_opacity + (size_t)n, 0.f);
     std::vector<int> gids(gaussian_ids, gaussian_ids + std::max<long long>(M, 1));
-    // The monolithic backward.  After a chunked forward no backward runs:
-    // rasterize_backward_chunked_kernel is not compiled (lanes whose pixel
-    // has no contributor in a chunk return before its SIMD-group broadcasts
-    // from lane 0, .metal:3245-3247 and 3285-3294, whose value is undefined on
-    // the GPU when lane 0 is one of them), and the monolithic walk is not its
-    // equal (a chunk that saturates locally skips its remaining splats while
-    // later chunks still composite).  The gradients stay zero.
-    if (K <= 1)
+    if (backward_ran) *backward_ran = 0;
+    if (K <= 1) {
         run_groups(gx, gy, 8, 8, [&](int bx, int by, int tx, int ty, int t) {
             k_raster_bwd(tile_bounds, isz, gids.data(), bins.data(), pk_xyo.data(), pk_con.data(), pk_rgb.data(), bg,
                          final_Ts, final_idx, v_rendered, v_xy, v_conic, v_colors, v_opacity, all,
                          uint3((uint)(bx * 8 + tx), (uint)(by * 8 + ty), 0u), uint3((uint)bx, (uint)by, 0u), (uint)t,
                          32u, (uint)(t % 32));
         });
+        if (backward_ran) *backward_ran = 1;
+    } else if (chunked_backward_defined(W, H, tile_bounds.x, bins.data(), cI.data(), K, chunk)) {
+        // chunked (msplat_metal.mm:1370-1400): prefix transmittance and suffix
+        // colour per pixel, then one grid layer of 8x8 threadgroups per chunk
+        std::vector<float> pT((size_t)K * P, 0.f), aC((size_t)K * P * 3, 0.f);
+        uint npx = P, KK = K;
+        for (uint y = 0; y < H; y++)
+            for (uint x = 0; x < W; x++)
+                k_chunk_prefix_suffix(npx, KK, cT.data(), cC.data(), cI.data(), pT.data(), aC.data(), isz, uint2(x, y));
+        for (uint k = 0; k < K; k++)
+            run_groups(gx, gy, 8, 8, [&](int bx, int by, int tx, int ty, int t) {
+                k_raster_bwd_chunked(tile_bounds, isz, gids.data(), bins.data(), pk_xyo.data(), pk_con.data(),
+                                     pk_rgb.data(), bg, final_Ts, cI.data(), pT.data(), cT.data(), aC.data(),
+                                     v_rendered, v_xy, v_conic, v_colors, v_opacity, chunk, KK,
+                                     uint3((uint)(bx * 8 + tx), (uint)(by * 8 + ty), k), uint3((uint)bx, (uint)by, k),
+                                     (uint)t, 32u, (uint)(t % 32));
+            });
+        if (backward_ran) *backward_ran = 1;
+    }
+    // Otherwise (a chunked forward whose backward is undefined on these
+    // inputs) the gradients stay zero and backward_ran says so.
     return M;
 }
 

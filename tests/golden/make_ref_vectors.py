@@ -4,8 +4,9 @@ own per-Gaussian Metal code (projection + SH, projection backward + SH Adam,
 regularizer, Adam, SGLD), compiled as host C++ by oracle/ref_build.py from the
 reference tree, on 512 random Gaussians at step 3001; and
 tests/golden/ref_pixel_vectors.npz: the outputs of its pixel stages (tile
-lists, forward rasterizers, SSIM + L1 loss, monolithic backward rasterizer) on the small
-views of tests/test_ref_pin.py (their inputs are regenerated from seeds) —
+lists, forward rasterizers, SSIM + L1 loss, monolithic and chunked backward
+rasterizers) on the small views of tests/test_ref_pin.py (their inputs are
+regenerated from seeds) —
 the vectors tests/test_ref_pin.py holds the oracle to where the reference
 tree is absent.  Needs the reference tree (default /root/reference,
 or MSPLAT_REFERENCE).
@@ -25,7 +26,8 @@ sys.path.insert(0, os.path.dirname(HERE))
 
 from msplat_gb300.schedule import GROUPS, step_scalars  # noqa: E402
 from oracle import oracle as O, ref as R  # noqa: E402
-from test_ref_pin import FWD_KEYS, PIXEL_CASES, pixel_case, random_inputs, ref_run, ring_camera  # noqa: E402
+from test_ref_pin import (FWD_KEYS, PIXEL_CASES, chunked_backward_case, pixel_case, random_inputs,  # noqa: E402
+                          ref_run, ring_camera)
 
 
 def main():
@@ -62,10 +64,18 @@ def main():
         o = R.raster_step(fwd, g.opacities, cam, gt=gt, mask=mask, background=bg, loss_inv_n=st["loss_inv_n"],
                           k_max=k)
         keys = ["num_isect", "gaussian_ids", "tile_bins", "out_img", "final_Ts", "final_idx", "loss", "v_rendered"]
-        if PIXEL_CASES[name][-1] == 1:   # the chunked backward is not compiled
+        if o["backward_ran"]:   # the chunked backward runs only where it is defined
             keys += ["v_xy", "v_conic", "v_colors", "v_opacity"]
         for k in keys:
             pix[f"{name}/{k}"] = np.asarray(o[k])
+    # the chunked backward, on a view where it is defined
+    cam, g, gt = chunked_backward_case()
+    st = step_scalars(3001, 3001, width=cam["width"], height=cam["height"])
+    o = R.raster_step(R.project_fwd(g, cam, 3), g.opacities, cam, gt=gt, loss_inv_n=st["loss_inv_n"], k_max=3)
+    assert o["backward_ran"]
+    for k in ["num_isect", "gaussian_ids", "tile_bins", "out_img", "final_Ts", "final_idx", "loss", "v_rendered",
+              "v_xy", "v_conic", "v_colors", "v_opacity"]:
+        pix[f"chunked_bwd/{k}"] = np.asarray(o[k])
     path = os.path.join(HERE, "ref_pixel_vectors.npz")
     np.savez_compressed(path, **pix)
     print(path, os.path.getsize(path), "bytes")

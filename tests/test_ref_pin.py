@@ -7,8 +7,8 @@ the bodies of project_and_sh_forward_kernel, project_and_sh_backward_kernel
 mcmc_reg_grad_kernel, count_intersections_kernel and
 scatter_intersections_kernel, and - threadgroups run on host threads - the
 monolithic and chunked forward rasterizers with the merge, the three SSIM +
-L1 kernels and the backward rasterizer (the chunked backward is not
-compiled: see oracle/ref_build.py).
+L1 kernels and the monolithic and chunked backward rasterizers (the chunked
+one where it is defined: see oracle/ref_build.py).
 
 Per-Gaussian stages, bit for bit against the oracle's float path: projection
 (centres, depths, radii, conics, tiles hit, colours, extents), the tile
@@ -17,9 +17,10 @@ SSIM window, and, from the same rasterizer gradients, the projection VJPs,
 the SH Adam, regularizer, Adam and SGLD updates of every parameter and moment.
 Pixel stages: per-tile lists, image, final transmittance, last contributors
 and dL/dimage bit for bit (monolithic, and chunked with the reference's K
-rule), the loss within 1e-6; after the monolithic forward the rasterizer
-gradients within 1e-6 (the reference sums them with atomics) and the whole
-step's updates within 1e-5.  exp() is the same function on both sides (the oracle's
+rule), the loss within 1e-6; the rasterizer gradients within 1e-6 (the
+reference sums them with atomics) and the whole step's updates within 1e-5,
+after the monolithic backward and, on a view where it is defined, the
+chunked one.  exp() is the same function on both sides (the oracle's
 det_expf; Metal's exp has no published bits).
 
 Two parts:
@@ -213,6 +214,29 @@ def pixel_case(name):
     return cam, g, gt, mask, bg
 
 
+def chunked_backward_case():
+    """One 16x16 tile under 560 Gaussians: 520 wide, faint ones (screen
+    sigma about 50 px, opacity 0.0055-0.009) that reach every pixel with
+    alpha >= 1/255, so every pixel has a contributor in each chunk (where the
+    reference's chunked backward is defined), and 40 small ones; three
+    chunks of 512 splats (the last empty), final transmittance 0.002-0.03,
+    so the second chunk's splats carry gradient."""
+    W = H = 16
+    cam = ring_camera(W, H, 0.8 * W, k=2)
+    rng = np.random.default_rng(11)
+    nb, ns = 520, 40
+    g = S.gaussians(nb + ns, 11)
+    g.means[:nb] = rng.uniform(-0.3, 0.3, (nb, 3)).astype(np.float32)
+    g.scales[:nb] = rng.uniform(2.3, 2.6, (nb, 3)).astype(np.float32)
+    op = rng.uniform(0.0055, 0.009, nb)
+    g.opacities[:nb, 0] = np.log(op / (1 - op)).astype(np.float32)
+    g.features_dc[:nb] = rng.uniform(-1.0, 1.0, (nb, 3)).astype(np.float32)
+    g.scales[nb:] = rng.normal(-1.8, 0.2, (ns, 3)).astype(np.float32)
+    g.opacities[nb:, 0] = rng.normal(-1.0, 0.5, ns).astype(np.float32)
+    gt = np.random.default_rng(12).integers(0, 256, (H, W, 3), dtype=np.uint8)
+    return cam, g, gt
+
+
 def check_pixel_path(r, o, backward=True):
     """The oracle's float path (r) against the reference kernels' pixel stages
     (o); the rasterizer gradients only when the reference's backward ran."""
@@ -249,15 +273,48 @@ def test_live_pixel_path(ref_lib, name):
                             loss_inv_n=step["loss_inv_n"], k_max=r["k_max"])
     assert int(np.diff(o["tile_bins"], axis=1).max()) > (512 if mode == 0 else 128)
     assert (r["k_max"] > 2) == (mode == 0)
-    check_pixel_path(r, o, backward=mode == 1)
-    if mode != 1:   # the reference's chunked backward is not compiled (oracle/ref_build.py)
-        return
+    # the chunked backward runs where it is defined (oracle/ref_build.py)
+    assert o["backward_ran"] or mode != 1
+    check_pixel_path(r, o, backward=o["backward_ran"])
+    if o["backward_ran"]:
+        check_step_updates(ref_lib, g, g_o, mom, cam, step, o, fwd)
+
+
+def check_step_updates(ref_lib, g, g_o, mom, cam, step, o, fwd):
+    """The whole step's updates from the reference's per-Gaussian kernels,
+    fed with its rasterizer gradients, against the oracle's (g_o): within
+    1e-5 relative of each group's update."""
     g_r = g.copy()
     ref_lib.step_after_raster(g_r, mom, cam, step, o["raster_grads"], fwd)
     for name_, a, b, before in zip(GROUPS, g_o.arrays(), g_r.arrays(), g.arrays()):
         fin = np.isfinite(before)
         e = np.linalg.norm((a - b)[fin]) / max(np.linalg.norm((b - before)[fin]), 1e-30)
         assert e <= 1e-5, (name_, e)
+
+
+@needs_reference
+def test_live_chunked_backward(ref_lib):
+    """The reference's chunked backward (compute_chunk_prefix_suffix_kernel,
+    then rasterize_backward_chunked_kernel per chunk, threadgroups on host
+    threads) on a view where it is defined, against the oracle's chunked
+    float path: lists, image, transmittance, last contributors and dL/dimage
+    identical, rasterizer gradients within 1e-6 (atomics), every splat of
+    the second chunk with gradient; then the step's updates within 1e-5."""
+    cam, g, gt = chunked_backward_case()
+    step = step_scalars(3001, 3001, width=cam["width"], height=cam["height"])
+    mom = ([np.zeros_like(a) for a in g.arrays()], [np.zeros_like(a) for a in g.arrays()])
+    g_o = g.copy()
+    mom_o = ([a.copy() for a in mom[0]], [a.copy() for a in mom[1]])
+    r = O.train_step(32, g_o, cam, step, moments=mom_o, gt=gt, raster_mode=0, k_max=3, do_sgld=True)
+    assert r["k_max"] == 3
+    fwd = ref_lib.project_fwd(g, cam, 3)
+    o = ref_lib.raster_step(fwd, g.opacities, cam, gt=gt, loss_inv_n=step["loss_inv_n"], k_max=3)
+    assert o["backward_ran"]
+    assert int(np.diff(o["tile_bins"], axis=1).max()) > 512
+    check_pixel_path(r, o, backward=True)
+    late = o["gaussian_ids"][512:]
+    assert late.size > 0 and np.count_nonzero(o["v_opacity"][late]) == late.size
+    check_step_updates(ref_lib, g, g_o, mom, cam, step, o, fwd)
 
 
 def test_golden_pixel_vectors():
@@ -272,4 +329,18 @@ def test_golden_pixel_vectors():
         o = {k[len(name) + 1:]: z[k] for k in z.files if k.startswith(name + "/")}
         o["num_isect"] = int(o["num_isect"])
         o["loss"] = float(o["loss"])
-        check_pixel_path(r, o, backward=PIXEL_CASES[name][-1] == 1)
+        check_pixel_path(r, o, backward="v_xy" in o)
+
+
+def test_golden_chunked_backward():
+    """The oracle's chunked forward and backward against the reference
+    kernels' outputs on chunked_backward_case(), stored in
+    tests/golden/ref_pixel_vectors.npz (no reference tree needed)."""
+    z = np.load(os.path.join(os.path.dirname(GOLDEN), "ref_pixel_vectors.npz"))
+    cam, g, gt = chunked_backward_case()
+    step = step_scalars(3001, 3001, width=cam["width"], height=cam["height"])
+    r = O.train_step(32, g.copy(), cam, step, gt=gt, raster_mode=0, k_max=3, do_optimizer=False)
+    o = {k[len("chunked_bwd/"):]: z[k] for k in z.files if k.startswith("chunked_bwd/")}
+    o["num_isect"] = int(o["num_isect"])
+    o["loss"] = float(o["loss"])
+    check_pixel_path(r, o, backward=True)
