@@ -144,8 +144,8 @@ def gauss_1d():
 def raster_step(fwd, opacities, cam, gt=None, mask=None, v_img=None, background=(0.0, 0.0, 0.0), ssim_weight=0.2,
                 loss_inv_n=None, ids_capacity=None, k_max=1, chunk_size=512):
     """The pixel stages of one step of one view from the reference's kernels
-    (count, scatter, forward raster, SSIM + L1 loss, backward raster; the sort
-    and pack restated): lists, image, final transmittance and last
+    (count, tile scan, scatter, per-tile sort + pack, forward raster, SSIM +
+    L1 loss, backward raster): lists, image, final transmittance and last
     contributors, loss sum, dL/dimage and the per-Gaussian rasterizer
     gradients.  gt (uint8 [H,W,3]) runs the loss; otherwise v_img is the image
     gradient.  k_max > 1: the chunked rasterizers with k_max chunks of

@@ -21,11 +21,11 @@ Left out on purpose, with the reason:
     address-space qualifiers gone they would redefine the thread-local
     overloads, which are the ones the fused kernels call;
   * the device-pointer overloads of read_packed_float2/3 (370-372, 393-395),
-    for the same reason (the constant-pointer overloads take their calls);
-  * the tile scan and the per-tile sort + pack (prefix_sum_tiles_kernel,
-    hybrid_sort_pack_kernel): their 1024-thread bitonic networks are not
-    emulated; ref_kernels.cpp restates what they compute (exclusive scans of
-    the padded and exact counts, ascending keys per tile, the pack gates).
+    for the same reason (the constant-pointer overloads take their calls).
+
+The tile scan and the per-tile sort + pack (prefix_sum_tiles_kernel,
+hybrid_sort_pack_kernel) run as single 1024-thread threadgroups on host
+threads, their bitonic networks and Hillis-Steele scans as written.
 
 The chunked backward (compute_chunk_prefix_suffix_kernel,
 rasterize_backward_chunked_kernel) is compiled but run only where it is
@@ -68,7 +68,9 @@ HELPER_RANGES = [
     (1374, 1491, "// Thread-local overload: reads cov3d from registers, writes", ""),  # EWA VJP, quat VJP
     (1535, 1569, "// Thread-local overload: reads v_cov3d", "}"),  # scale_rot_to_cov3d_vjp (thread)
     (1836, 1858, "// Adam update helper", "};"),           # adam_update_element, SHAdamParams
+    (2242, 2244, "#define BITONIC_TG_CAP 2048u", "constant constexpr uint64_t SORT_KEY_SENTINEL = 0xFFFFFFFFFFFFFFFFULL;"),
     (2248, 2276, "inline uint next_pow2(uint x) {", "}"),  # pad_count, make_sort_key, gaussian_is_active
+    (2278, 2337, "// Hillis-Steele exclusive scan over threadgroup memory.", "}"),  # tile scan, bitonic sorts
     (906, 929, "inline int warp_reduce_all_max(", "}"),   # SIMD-group reductions
     (2771, 2774, "#define SSIM_WIN 11", "#define SSIM_C2 0.0009f"),
     (3376, 3382, "constant float GAUSS_1D[11] = {", "#define SSIM_TG 16   // threadgroup dimension (16×16 = 256 threads)"),
@@ -96,6 +98,12 @@ KERNELS = {
     "mcmc_reg_grad_kernel": ["opacities", "scales", "v_opacity", "v_scale", "N", "op_reg", "sc_reg", "radii",
                              "invis_scale", "v_dc_sq", "idx"],
     "count_intersections_kernel": ["xys", "radii", "depths", "tile_bounds", "tile_counts", "num_points", "aabb", "gid"],
+    "prefix_sum_tiles_kernel": ["tile_counts_in", "exact_offsets", "sort_offsets", "tile_bins", "num_tiles",
+                                "capacity", "tile_range", "tid"],
+    "hybrid_sort_pack_kernel": ["tile_counts_in", "sort_offsets", "exact_offsets", "isect_keys_unsorted", "xys_in",
+                                "conics_in", "opacities_in", "colors_in", "packed_xy_opac", "packed_conic",
+                                "packed_rgb", "gaussian_ids", "capacity", "num_points", "nan_counts", "tile_range",
+                                "key_capacity", "tg_id", "tid"],
     "scatter_intersections_kernel": ["xys", "depths", "radii", "tile_bounds", "sort_offsets", "tile_write_counters",
                                      "isect_keys_unsorted", "num_points", "aabb", "capacity", "tile_range", "gid"],
     "nd_rasterize_forward_kernel": ["tile_bounds", "img_size", "channels", "tile_bins", "packed_xy_opac",

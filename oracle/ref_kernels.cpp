@@ -86,6 +86,20 @@ void k_scatter(float *xys, float *depths, int *radii, uint3 &tile_bounds, uint *
 #undef threadgroup
 #define threadgroup static
 
+// prefix_sum_tiles_kernel (msplat_metal.metal:2376-2433)
+void k_prefix_sum_tiles(uint *tile_counts_in, uint *exact_offsets, uint *sort_offsets, int *tile_bins,
+                        uint &num_tiles, uint &capacity, uint2 &tile_range, uint tid) {
+#include "k_prefix_sum_tiles_kernel.inc"
+}
+
+// hybrid_sort_pack_kernel (msplat_metal.metal:2489-2627)
+void k_sort_pack(uint *tile_counts_in, uint *sort_offsets, uint *exact_offsets, uint64_t *isect_keys_unsorted,
+                 float *xys_in, float *conics_in, float *opacities_in, float *colors_in, float *packed_xy_opac,
+                 float *packed_conic, float *packed_rgb, int *gaussian_ids, uint &capacity, uint &num_points,
+                 atomic_uint *nan_counts, uint2 &tile_range, uint &key_capacity, uint tg_id, uint tid) {
+#include "k_hybrid_sort_pack_kernel.inc"
+}
+
 // nd_rasterize_forward_kernel (msplat_metal.metal:499-618)
 void k_raster_fwd(uint3 &tile_bounds, uint3 &img_size, uint &channels, int *tile_bins, float *packed_xy_opac,
                   float *packed_conic, float *packed_rgb, float *final_Ts, int *final_index, float *out_img,
@@ -328,16 +342,13 @@ void ref_pad_count(int n, const uint32_t *c, uint32_t *out) {
 }
 
 // The pixel stages of one training step of one view, as the reference runs
-// them (msplat_metal.mm:1255-1400), the forward monolithic (k_max <= 1) or
-// chunked in k_max chunks of chunk_size splats with the merge (the caller
-// applies the reference's K rule, msplat_metal.mm:1204-1224): count and
-// scatter of the
-// tile intersections (compiled kernels), the per-tile sort and pack
-// (restated: hybrid_sort_pack_kernel sorts each tile's keys ascending and
-// packs (x, y, sigmoid(opacity)), conic and raw colour by id, a non-finite
-// record packed as zeros, msplat_metal.metal:2562-2582), the forward
-// rasterizer, the three SSIM + L1 kernels when gt is given (else v_rendered
-// is an input) and the backward rasterizer (compiled kernels).
+// them (msplat_metal.mm:1255-1400), every stage a compiled kernel: count,
+// tile scan, scatter, per-tile sort + pack (one 1024-thread threadgroup per
+// tile), the forward rasterizer, monolithic (k_max <= 1) or chunked in k_max
+// chunks of chunk_size splats with the merge (the caller applies the
+// reference's K rule, msplat_metal.mm:1204-1224), the three SSIM + L1
+// kernels when gt is given (else v_rendered is an input) and the backward
+// rasterizer (the chunked one where it is defined).
 // Capacity: ids/packing sized by the exact count; returns the intersection
 // count, or -1 when more than ids_capacity.
 long long ref_raster_step(int n, const float *xys, const float *depths, const int *radii, const float *conics,
@@ -355,49 +366,35 @@ long long ref_raster_step(int n, const float *xys, const float *depths, const in
     std::vector<uint> counts(T, 0u);
     for (uint i = 0; i < np; i++)
         k_count(mut(xys), mut(radii), mut(depths), tile_bounds, counts.data(), np, mut(aabb), i);
-    // prefix_sum_tiles_kernel: padded offsets for the sort buckets, exact ones for the lists
-    std::vector<uint> sort_off(T + 1, 0u), exact(T + 1, 0u);
-    for (uint t = 0; t < T; t++) {
-        sort_off[t + 1] = sort_off[t] + pad_count(counts[t]);
-        exact[t + 1] = exact[t] + counts[t];
+    // prefix_sum_tiles_kernel: one 1024-thread threadgroup; padded offsets for
+    // the sort buckets, exact ones and the [start, end) bins for the lists
+    std::vector<uint> sort_off(T + 1, 0u), exact(T, 0u);
+    std::vector<int> bins(2 * (size_t)T);
+    uint2 all(0u, T);
+    {
+        uint nt = T, cap_any = 0xffffffffu;
+        run_groups(1, 1, 1024, 1, [&](int, int, int, int, int t) {
+            k_prefix_sum_tiles(counts.data(), exact.data(), sort_off.data(), bins.data(), nt, cap_any, all, (uint)t);
+        });
     }
-    const long long M = exact[T];
+    const long long M = T ? (long long)bins[2 * (T - 1) + 1] : 0;
     if (M > ids_capacity) return -1;
     // scatter_intersections_kernel (one tile group covering every tile)
     uint cap = sort_off[T];
     std::vector<uint64_t> keys(std::max<uint>(cap, 1u), ~0ull);
     std::vector<uint> wc(T, 0u);
-    uint2 all(0u, T);
     for (uint i = 0; i < np; i++)
         k_scatter(mut(xys), mut(depths), mut(radii), tile_bounds, sort_off.data(), wc.data(), keys.data(), np,
                   mut(aabb), cap, all, i);
-    // sort + pack (restated)
+    // hybrid_sort_pack_kernel: one 1024-thread threadgroup per tile
     std::vector<float> pk_xyo(3 * (size_t)std::max<long long>(M, 1)), pk_con(pk_xyo.size()), pk_rgb(pk_xyo.size());
-    std::vector<int> bins(2 * (size_t)T);
-    for (uint t = 0; t < T; t++) {
-        std::sort(keys.begin() + sort_off[t], keys.begin() + sort_off[t] + counts[t]);
-        bins[2 * t] = (int)exact[t];
-        bins[2 * t + 1] = (int)exact[t + 1];
-        for (uint j = 0; j < counts[t]; j++) {
-            const uint gidx = (uint)(keys[sort_off[t] + j] & 0xFFFFFFFFu);
-            const size_t d = exact[t] + j;
-            gaussian_ids[d] = (int)gidx;
-            const float2 xy(xys[2 * gidx], xys[2 * gidx + 1]);
-            const float opac = 1.f / (1.f + exp(-opacities[gidx]));
-            const float3 conic(conics[3 * gidx], conics[3 * gidx + 1], conics[3 * gidx + 2]);
-            const float3 rgb(colors[3 * gidx], colors[3 * gidx + 1], colors[3 * gidx + 2]);
-            const bool ok = finite_bits(xy.x) && finite_bits(xy.y) && finite_bits(opac) && finite_bits3(conic) &&
-                            finite_bits3(rgb);
-            if (!ok) {
-                nan_counts[13]++;
-                if (!finite_bits(opac)) nan_counts[14]++;
-            }
-            const float3 a = ok ? float3(xy.x, xy.y, opac) : float3(0.f), b = ok ? conic : float3(0.f),
-                         c = ok ? rgb : float3(0.f);
-            pk_xyo[3 * d] = a.x; pk_xyo[3 * d + 1] = a.y; pk_xyo[3 * d + 2] = a.z;
-            pk_con[3 * d] = b.x; pk_con[3 * d + 1] = b.y; pk_con[3 * d + 2] = b.z;
-            pk_rgb[3 * d] = c.x; pk_rgb[3 * d + 1] = c.y; pk_rgb[3 * d + 2] = c.z;
-        }
+    {
+        uint out_cap = (uint)std::max<long long>(M, 1), key_cap = std::max<uint>(cap, 1u);
+        run_groups((int)T, 1, 1024, 1, [&](int bx, int, int, int, int t) {
+            k_sort_pack(counts.data(), sort_off.data(), exact.data(), keys.data(), mut(xys), mut(conics),
+                        mut(opacities), mut(colors), pk_xyo.data(), pk_con.data(), pk_rgb.data(), gaussian_ids,
+                        out_cap, np, nan_counts, all, key_cap, (uint)bx, (uint)t);
+        });
     }
     if (tile_bins_out) std::copy(bins.begin(), bins.end(), tile_bins_out);
     // forward rasterizer: 8x8 threadgroups

@@ -6,7 +6,8 @@ the bodies of project_and_sh_forward_kernel, project_and_sh_backward_kernel
 (with its fused SH Adam), fused_adam_kernel, sgld_noise_gen/sgld_noise_kernel,
 mcmc_reg_grad_kernel, count_intersections_kernel and
 scatter_intersections_kernel, and - threadgroups run on host threads - the
-monolithic and chunked forward rasterizers with the merge, the three SSIM +
+tile scan and per-tile bitonic sort + pack, the monolithic and chunked
+forward rasterizers with the merge, the three SSIM +
 L1 kernels and the monolithic and chunked backward rasterizers (the chunked
 one where it is defined: see oracle/ref_build.py).
 
