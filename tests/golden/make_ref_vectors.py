@@ -26,8 +26,8 @@ sys.path.insert(0, os.path.dirname(HERE))
 
 from msplat_gb300.schedule import GROUPS, step_scalars  # noqa: E402
 from oracle import oracle as O, ref as R  # noqa: E402
-from test_ref_pin import (FWD_KEYS, PIXEL_CASES, chunked_backward_case, pixel_case, random_inputs,  # noqa: E402
-                          ref_run, ring_camera)
+from test_ref_pin import (FWD_KEYS, PIXEL_CASES, chunked_backward_case, dense_tile_case, pixel_case,  # noqa: E402
+                          random_inputs, ref_run, ring_camera)
 
 
 def main():
@@ -76,6 +76,13 @@ def main():
     for k in ["num_isect", "gaussian_ids", "tile_bins", "out_img", "final_Ts", "final_idx", "loss", "v_rendered",
               "v_xy", "v_conic", "v_colors", "v_opacity"]:
         pix[f"chunked_bwd/{k}"] = np.asarray(o[k])
+    # a tile of more than 2048 keys (the device-memory bitonic sort)
+    cam, g, gt = dense_tile_case()
+    st = step_scalars(3001, 3001, width=cam["width"], height=cam["height"])
+    o = R.raster_step(R.project_fwd(g, cam, 3), g.opacities, cam, gt=gt, loss_inv_n=st["loss_inv_n"])
+    for k in ["num_isect", "gaussian_ids", "tile_bins", "out_img", "final_Ts", "final_idx", "loss", "v_rendered",
+              "v_xy", "v_conic", "v_colors", "v_opacity"]:
+        pix[f"dense/{k}"] = np.asarray(o[k])
     path = os.path.join(HERE, "ref_pixel_vectors.npz")
     np.savez_compressed(path, **pix)
     print(path, os.path.getsize(path), "bytes")

@@ -238,6 +238,22 @@ def chunked_backward_case():
     return cam, g, gt
 
 
+def dense_tile_case():
+    """One 16x16 tile under 2200 small Gaussians: more than 2048 keys, so the
+    reference sorts the tile with its device-memory bitonic network (4096
+    padded keys); monolithic raster, transmittance down to the 1e-4 stop."""
+    W = H = 16
+    cam = ring_camera(W, H, 0.8 * W, k=2)
+    rng = np.random.default_rng(21)
+    n = 2200
+    g = S.gaussians(n, 21)
+    g.means[:] = rng.uniform(-0.25, 0.25, (n, 3)).astype(np.float32)
+    g.scales[:] = rng.normal(-1.2, 0.3, (n, 3)).astype(np.float32)
+    g.opacities[:, 0] = rng.normal(-2.5, 1.0, n).astype(np.float32)
+    gt = rng.integers(0, 256, (H, W, 3), dtype=np.uint8)
+    return cam, g, gt
+
+
 def check_pixel_path(r, o, backward=True):
     """The oracle's float path (r) against the reference kernels' pixel stages
     (o); the rasterizer gradients only when the reference's backward ran."""
@@ -331,6 +347,35 @@ def test_golden_pixel_vectors():
         o["num_isect"] = int(o["num_isect"])
         o["loss"] = float(o["loss"])
         check_pixel_path(r, o, backward="v_xy" in o)
+
+
+@needs_reference
+def test_live_dense_tile(ref_lib):
+    """A tile of more than 2048 keys (the reference's device-memory bitonic
+    sort) through the reference's pixel stages against the oracle's float
+    path: lists, image, transmittance, last contributors and dL/dimage
+    identical, rasterizer gradients within 1e-6."""
+    cam, g, gt = dense_tile_case()
+    step = step_scalars(3001, 3001, width=cam["width"], height=cam["height"])
+    r = O.train_step(32, g.copy(), cam, step, gt=gt, raster_mode=1, do_optimizer=False)
+    o = ref_lib.raster_step(ref_lib.project_fwd(g, cam, 3), g.opacities, cam, gt=gt, loss_inv_n=step["loss_inv_n"])
+    assert int(np.diff(o["tile_bins"], axis=1).max()) > 2048 and o["backward_ran"]
+    assert float(o["final_Ts"].min()) < 1.01e-4
+    check_pixel_path(r, o, backward=True)
+
+
+def test_golden_dense_tile():
+    """The oracle on dense_tile_case() against the reference kernels' outputs
+    stored in tests/golden/ref_pixel_vectors.npz (no reference tree needed)."""
+    z = np.load(os.path.join(os.path.dirname(GOLDEN), "ref_pixel_vectors.npz"))
+    cam, g, gt = dense_tile_case()
+    step = step_scalars(3001, 3001, width=cam["width"], height=cam["height"])
+    r = O.train_step(32, g.copy(), cam, step, gt=gt, raster_mode=1, do_optimizer=False)
+    o = {k[len("dense/"):]: z[k] for k in z.files if k.startswith("dense/")}
+    o["num_isect"] = int(o["num_isect"])
+    o["loss"] = float(o["loss"])
+    assert int(np.diff(o["tile_bins"], axis=1).max()) > 2048
+    check_pixel_path(r, o, backward=True)
 
 
 def test_golden_chunked_backward():
