@@ -187,3 +187,26 @@ def raster_step(fwd, opacities, cam, gt=None, mask=None, v_img=None, background=
     o["loss"] = float(o["loss_sum"][0]) / (W * H)
     o["raster_grads"] = np.concatenate([o["v_xy"], o["v_conic"], o["v_colors"], o["v_opacity"][:, None]], axis=1)
     return o
+
+
+def mcmc_after_train(g, moments, num_active, step, max_steps, cull_radius, reloc_count=0):
+    """One pass of the reference's Model::mcmcAfterTrain (model.cpp:497-660,
+    compiled unchanged) over g (a GaussianSet of cap rows, the first
+    num_active in use) and moments (exp_avg[6], exp_avg_sq[6], the same
+    shapes), both updated in place: dead Gaussians relocated onto alive ones
+    and growth toward the cap, with the reference's own draws
+    (std::discrete_distribution over mt19937).  Returns (num_active,
+    reloc_count) after the pass."""
+    L = lib()
+    arrays = g.arrays()
+    for a in list(arrays) + list(moments[0]) + list(moments[1]):
+        assert a.dtype == np.float32 and a.flags["C_CONTIGUOUS"]
+    cap = arrays[0].shape[0]
+    strides = np.array([a.size // a.shape[0] for a in arrays], np.int32)
+    ea = (FP * 6)(*[_p(a) for a in moments[0]])
+    eas = (FP * 6)(*[_p(a) for a in moments[1]])
+    rc = C.c_int(int(reloc_count))
+    L.ref_mcmc_after_train.restype = C.c_int
+    n = L.ref_mcmc_after_train(cap, int(num_active), int(strides[4]), *[_p(a) for a in arrays], ea, eas,
+                               _p(strides, IP), int(step), int(max_steps), C.c_float(cull_radius), C.byref(rc))
+    return int(n), int(rc.value)

@@ -39,6 +39,11 @@ lanes return there or none does, and reports whether it ran.
 The rasterizers and the SSIM kernels use threadgroup memory, barriers and
 SIMD-group functions; metal_shim.h runs their threadgroups on host threads.
 
+The MCMC host code of core/src/model.cpp (computeRelocation, relocate,
+addNewGaussians, mcmcAfterTrain: lines 311-660) is copied the same way and
+compiled by ref_model.cpp against model_shim.h, a host stand-in for the
+Model class with the members that code uses.
+
 Usage: python oracle/ref_build.py [--reference DIR]   (default: /root/reference)
 """
 from __future__ import annotations
@@ -53,6 +58,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 LIB = os.path.join(OUT, "libmsplat_ref.so")
 METAL = os.path.join("core", "metal", "msplat_metal.metal")
+MODEL = os.path.join("core", "src", "model.cpp")
+# The MCMC host code: computeRelocation, relocate, addNewGaussians and
+# mcmcAfterTrain, one contiguous range of model.cpp compiled against
+# model_shim.h (a host stand-in for the Model class) by ref_model.cpp.
+MODEL_RANGE = (311, 660, "void Model::computeRelocation(float opacity_old_sig, float* scale_old_exp, int N,", "}")
 
 # (first line, last line, text of the first line, text of the last line), 1-based, inclusive
 HELPER_RANGES = [
@@ -134,13 +144,13 @@ KERNELS = {
 }
 
 
-def extract(lines, first, last, head, tail):
+def extract(lines, first, last, head, tail, path=METAL):
     got_head = lines[first - 1].strip()
     got_tail = lines[last - 1].strip()
     if not got_head.startswith(head) or got_tail != tail:
-        raise SystemExit(f"{METAL}:{first}-{last}: expected '{head}' ... '{tail}', found '{got_head}' ... "
+        raise SystemExit(f"{path}:{first}-{last}: expected '{head}' ... '{tail}', found '{got_head}' ... "
                          f"'{got_tail}': the reference changed; review the ranges")
-    return f"#line {first} \"msplat_metal.metal\"\n" + "".join(lines[first - 1:last])
+    return f"#line {first} \"{os.path.basename(path)}\"\n" + "".join(lines[first - 1:last])
 
 
 def kernel_body(lines, name, params):
@@ -174,15 +184,25 @@ def build(reference: str, quiet: bool = False) -> str:
         spans[name] = span
         with open(os.path.join(OUT, f"k_{name}.inc"), "w") as f:
             f.write(body)
+    model_src = os.path.join(reference, MODEL)
+    if not os.path.exists(model_src):
+        raise SystemExit(f"{model_src} not found")
+    with open(model_src) as f:
+        model_lines = f.readlines()
+    with open(os.path.join(OUT, "model_mcmc.inc"), "w") as f:
+        f.write("// extracted by oracle/ref_build.py from " + MODEL + " (not committed)\n")
+        f.write(extract(model_lines, *MODEL_RANGE, path=MODEL))
     cxx = shutil.which("g++") or "c++"
     cmd = [cxx, "-O2", "-std=c++20", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
-           "-Wno-unknown-pragmas", "-pthread", "-I", HERE, "-I", OUT, os.path.join(HERE, "ref_kernels.cpp"), "-o", LIB]
+           "-Wno-unknown-pragmas", "-pthread", "-I", HERE, "-I", OUT, os.path.join(HERE, "ref_kernels.cpp"),
+           os.path.join(HERE, "ref_model.cpp"), "-o", LIB]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise SystemExit(f"compile failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     if not quiet:
         for name, (a, b) in spans.items():
             print(f"{name}: {METAL}:{a}-{b}")
+        print(f"MCMC host code: {MODEL}:{MODEL_RANGE[0]}-{MODEL_RANGE[1]}")
         print(LIB)
     return LIB
 

@@ -6,7 +6,9 @@ reference tree, on 512 random Gaussians at step 3001; and
 tests/golden/ref_pixel_vectors.npz: the outputs of its pixel stages (tile
 lists, forward rasterizers, SSIM + L1 loss, monolithic and chunked backward
 rasterizers) on the small views of tests/test_ref_pin.py (their inputs are
-regenerated from seeds) —
+regenerated from seeds); and tests/golden/ref_mcmc_vectors.npz: the moves
+and a SHA-256 of the output state of the reference's MCMC host pass
+(model.cpp:311-660) on the states of tests/test_ref_pin.py —
 the vectors tests/test_ref_pin.py holds the oracle to where the reference
 tree is absent.  Needs the reference tree (default /root/reference,
 or MSPLAT_REFERENCE).
@@ -24,9 +26,11 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.dirname(HERE))
 
+from msplat_gb300 import synthetic as S  # noqa: E402
 from msplat_gb300.schedule import GROUPS, step_scalars  # noqa: E402
 from oracle import oracle as O, ref as R  # noqa: E402
-from test_ref_pin import (FWD_KEYS, PIXEL_CASES, chunked_backward_case, dense_tile_case, pixel_case,  # noqa: E402
+from test_ref_pin import (FWD_KEYS, MCMC_CASES, PIXEL_CASES, _copy_state, _state_digest,  # noqa: E402
+                          chunked_backward_case, dense_tile_case, mcmc_pairs, mcmc_state, pixel_case,
                           random_inputs, ref_run, ring_camera)
 
 
@@ -85,6 +89,22 @@ def main():
         pix[f"dense/{k}"] = np.asarray(o[k])
     path = os.path.join(HERE, "ref_pixel_vectors.npz")
     np.savez_compressed(path, **pix)
+    print(path, os.path.getsize(path), "bytes")
+
+    # the MCMC host code: each case's moves and a digest of the output state
+    mc = {}
+    for name, (n, cap, seed, with_dead) in MCMC_CASES.items():
+        g0, m0 = mcmc_state(n, cap, seed, with_dead)
+        g_r, m_r = _copy_state(g0, m0)
+        n_new, _ = R.mcmc_after_train(g_r, m_r, n, 600, 30000, 3.0, 0)
+        dead = None
+        if with_dead:
+            dead, _ = O.mcmc_dead_mask(S.GaussianSet(*(a[:n] for a in g0.arrays())), 3.0)
+        dst, src = mcmc_pairs(g0, g_r, n, n_new, dead)
+        mc[name + "/dst"], mc[name + "/src"] = dst, src
+        mc[name + "/sha256"] = np.array(_state_digest(g_r, m_r))
+    path = os.path.join(HERE, "ref_mcmc_vectors.npz")
+    np.savez_compressed(path, **mc)
     print(path, os.path.getsize(path), "bytes")
 
 

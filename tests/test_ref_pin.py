@@ -34,6 +34,7 @@ Two parts:
     same library, everywhere.
 """
 import ctypes
+import hashlib
 import os
 
 import numpy as np
@@ -390,3 +391,112 @@ def test_golden_chunked_backward():
     o["num_isect"] = int(o["num_isect"])
     o["loss"] = float(o["loss"])
     check_pixel_path(r, o, backward=True)
+
+
+# ---- MCMC host code (model.cpp:311-660, compiled against oracle/model_shim.h) ----
+
+def mcmc_state(n, cap, seed, dead=True):
+    """cap rows, the first n in use.  With dead: 8 % faded (sigmoid(opacity)
+    in (0.0005, 0.005)), 1 % with one non-finite parameter (mean, scale,
+    quaternion, DC or rest coefficient), 1 % outside a cull radius of 3; the
+    rest alive.  Random Adam moments; rows past n zero."""
+    rng = np.random.default_rng(seed)
+    g = S.gaussians(cap, seed)
+    g.opacities[:, 0] = np.maximum(rng.normal(0.5, 1.0, cap), -5.0).astype(np.float32)
+    if dead:
+        k = rng.permutation(n)
+        nf, nn, nc = n * 8 // 100, n // 100, n // 100
+        op = rng.uniform(0.0005, 0.005, nf)
+        g.opacities[k[:nf], 0] = np.log(op / (1 - op)).astype(np.float32)
+        bad = k[nf:nf + nn]
+        g.means[bad[0::5], 1] = np.nan
+        g.scales[bad[1::5], 2] = np.inf
+        g.quats[bad[2::5], 0] = np.nan
+        g.features_dc[bad[3::5], 0] = -np.inf
+        g.features_rest[bad[4::5], 7, 2] = np.nan
+        far = k[nf + nn:nf + nn + nc]
+        g.means[far] *= np.float32(4.0) / np.maximum(np.linalg.norm(g.means[far], axis=1, keepdims=True), 1e-3)
+    for a in g.arrays():
+        a[n:] = 0
+    mom = ([np.abs(rng.normal(0, 1e-3, a.shape)).astype(np.float32) for a in g.arrays()],
+           [np.abs(rng.normal(0, 1e-6, a.shape)).astype(np.float32) for a in g.arrays()])
+    return g, mom
+
+
+def _copy_state(g, mom):
+    return g.copy(), ([a.copy() for a in mom[0]], [a.copy() for a in mom[1]])
+
+
+def _state_digest(g, mom):
+    h = hashlib.sha256()
+    for a in list(g.arrays()) + list(mom[0]) + list(mom[1]):
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def mcmc_pairs(g0, g_r, n, n_new, dead):
+    """The (dst, src) moves of a pass, recovered from its output: a dead row
+    or a new row holds a copy of its source's mean, and sources keep their
+    means, so each copied mean names one row of the input."""
+    rows = np.flatnonzero(~dead) if dead is not None else np.arange(n)
+    key = {g0.means[i].tobytes(): i for i in rows}
+    assert len(key) == rows.size
+    dst = np.concatenate([np.flatnonzero(dead) if dead is not None else np.zeros(0, np.int64),
+                          np.arange(n, n_new)]).astype(np.int32)
+    src = np.array([key[g_r.means[d].tobytes()] for d in dst], np.int32)
+    return dst, src
+
+
+MCMC_CASES = {
+    # rows in use, rows, seed, with dead rows: relocation only (no room to grow), growth only
+    "relocate": (2000, 2000, 5, True),
+    "grow": (2000, 2400, 6, False),
+}
+
+
+@needs_reference
+@pytest.mark.parametrize("name", list(MCMC_CASES))
+def test_live_mcmc_host_code(ref_lib, name):
+    """The reference's Model::mcmcAfterTrain pass at step 600 (classification
+    of faded, non-finite and culled Gaussians, relocation with Eq. 9 and the
+    copies, growth by 5 % toward the cap, moments zeroed) against the
+    oracle's restatement given the reference's own draws: the dead rows are
+    the oracle's (or_mcmc_dead_mask), alive rows keep their means, and every
+    parameter and moment after or_mcmc_apply is bit-identical."""
+    n, cap, seed, with_dead = MCMC_CASES[name]
+    g0, m0 = mcmc_state(n, cap, seed, with_dead)
+    g_r, m_r = _copy_state(g0, m0)
+    n_new, rc = ref_lib.mcmc_after_train(g_r, m_r, n, 600, 30000, 3.0, 0)
+    dead, cnt = O.mcmc_dead_mask(S.GaussianSet(*(a[:n] for a in g0.arrays())), 3.0)
+    if with_dead:
+        assert cnt == n // 10 and n_new == n and rc == 1
+        assert np.array_equal(g_r.means[:n][~dead], g0.means[:n][~dead])
+    else:
+        assert cnt == 0 and n_new == int(np.float32(1.05) * np.float32(n)) and rc == 1
+    dst, src = mcmc_pairs(g0, g_r, n, n_new, dead if with_dead else None)
+    g_o, m_o = _copy_state(g0, m0)
+    O.mcmc_apply(g_o, m_o, dst, src)
+    for k, a, b in zip(GROUPS, g_o.arrays(), g_r.arrays()):
+        assert a.tobytes() == b.tobytes(), k
+    for k, a, b in zip(GROUPS * 2, m_o[0] + m_o[1], m_r[0] + m_r[1]):
+        assert a.tobytes() == b.tobytes(), k
+    # the pass is a no-op before step 500, off the 100-step cadence and in the last 16.7 %
+    for step in (400, 650, 25000):
+        g_n, m_n = _copy_state(g0, m0)
+        assert ref_lib.mcmc_after_train(g_n, m_n, n, step, 30000, 3.0, 0) == (n, 0)
+        assert _state_digest(g_n, m_n) == _state_digest(g0, m0)
+
+
+def test_golden_mcmc_host_code():
+    """The oracle's MCMC restatement against tests/golden/ref_mcmc_vectors.npz
+    (the reference pass's moves and a SHA-256 of its output state, written
+    by tests/golden/make_ref_vectors.py): the same moves applied by
+    or_mcmc_apply give the same bytes (no reference tree needed)."""
+    z = np.load(os.path.join(os.path.dirname(GOLDEN), "ref_mcmc_vectors.npz"))
+    for name, (n, cap, seed, with_dead) in MCMC_CASES.items():
+        g0, m0 = mcmc_state(n, cap, seed, with_dead)
+        if with_dead:
+            dead, _ = O.mcmc_dead_mask(S.GaussianSet(*(a[:n] for a in g0.arrays())), 3.0)
+            assert np.array_equal(np.flatnonzero(dead), z[name + "/dst"][:int(dead.sum())])
+        O.mcmc_apply(g0, m0, z[name + "/dst"], z[name + "/src"])
+        assert _state_digest(g0, m0) == str(z[name + "/sha256"])
