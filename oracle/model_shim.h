@@ -1,14 +1,17 @@
-// Host stand-in for the reference's Model class (core/include/model.hpp:
-// 17-130), with only the members its MCMC host code reads and writes, so
-// that code compiles unchanged — TEST INFRASTRUCTURE ONLY (it pins the
-// oracle's MCMC restatement; nothing in the product uses it).
+// Host stand-ins for the reference's Model class (core/include/model.hpp:
+// 17-130), its Camera (core/include/input_data.hpp:19-48) and MTensor, with
+// only the members the host code compiled by ref_model.cpp uses (the MCMC
+// pass, camera setup, evaluation metrics), so that code compiles unchanged
+// — TEST INFRASTRUCTURE ONLY (it pins the oracle's restatements; nothing in
+// the product uses it).
 //
 // The reference keeps each parameter group and Adam moment as an MTensor
 // (core/include/metal_tensor.hpp) whose storage is shared with the GPU; here
-// a HostTensor is a row-major float array with the two accessors the code
-// calls (data<T>() and stride0(), the floats per row).  The `*_buf` tensors
-// and their active views (means, opacities, ...) are the same arrays, as in
-// the reference after refreshViews().
+// a HostTensor is a row-major float array with the accessors the code calls
+// (data<T>(), stride0() = the floats per row, size(d), numel(), defined(),
+// data_ptr()).  The `*_buf` tensors and their active views (means,
+// opacities, ...) are the same arrays, as in the reference after
+// refreshViews().
 #pragma once
 
 #include <algorithm>
@@ -18,15 +21,50 @@
 #include <cstring>
 #include <iostream>
 #include <limits>
+#include <memory>
 #include <random>
+#include <tuple>
 #include <vector>
+
+#define BLOCK_X 16
+#define BLOCK_Y 16
 
 struct HostTensor {
     float *p = nullptr;
     int64_t row = 1;
+    std::vector<int64_t> shape;                  // for size(d) and numel()
+    std::shared_ptr<std::vector<float>> owned;   // storage of gpu_empty tensors
     template <class T> T *data() { return reinterpret_cast<T *>(p); }
     template <class T> const T *data() const { return reinterpret_cast<const T *>(p); }
     int64_t stride0() const { return row; }
+    int64_t size(int d) const { return shape[d < 0 ? (int)shape.size() + d : d]; }
+    int64_t numel() const {
+        int64_t n = 1;
+        for (int64_t s : shape) n *= s;
+        return n;
+    }
+    bool defined() const { return p != nullptr; }
+    void *data_ptr() { return p; }
+};
+using MTensor = HostTensor;
+
+enum class DType { Float32 };
+inline HostTensor gpu_empty(std::initializer_list<int64_t> shape, DType) {
+    HostTensor t;
+    t.shape.assign(shape.begin(), shape.end());
+    t.owned = std::make_shared<std::vector<float>>((size_t)t.numel());
+    t.p = t.owned->data();
+    t.row = t.shape.size() > 1 ? t.numel() / t.shape[0] : 1;
+    return t;
+}
+
+struct Camera {
+    int width = 0, height = 0;
+    float fx = 0, fy = 0, cx = 0, cy = 0;
+    float camToWorld[16] = {};
+    MTensor cachedViewMat, cachedProjViewMat;
+    float cachedCamPos[3] = {};
+    float cachedFovX = 0, cachedFovY = 0;
 };
 
 // GPU hooks the MCMC pass calls (core/metal/bindings.h): nothing to wait for
@@ -50,6 +88,17 @@ public:
     int maxSteps = 0;
     int cap_max = 0;
     float cull_radius = 0.0f;
+    int shDegree = 3;
+    int shDegreeInterval = 1000;
+
+    struct CamSetup {
+        float fx, fy, cx, cy;
+        int height, width, degree, degreesToUse;
+        std::tuple<int, int, int> tileBounds;
+        float cam_pos[3];
+    };
+    CamSetup prepareCam(Camera &cam, int step);
+    int getDownscaleFactor(int step);
 
     void refreshViews() {}
     void computeRelocation(float opacity_old_sig, float *scale_old_exp, int N, float &opacity_new_sig,

@@ -210,3 +210,33 @@ def mcmc_after_train(g, moments, num_active, step, max_steps, cull_radius, reloc
     n = L.ref_mcmc_after_train(cap, int(num_active), int(strides[4]), *[_p(a) for a in arrays], ea, eas,
                                _p(strides, IP), int(step), int(max_steps), C.c_float(cull_radius), C.byref(rc))
     return int(n), int(rc.value)
+
+
+def prepare_cam(c2w, width, height, fx, fy, cx, cy, step=0, sh_degree=3, sh_interval=1000, rest_bases=15):
+    """The reference's Model::prepareCam (model.cpp:845-889, compiled
+    unchanged): view matrix, projection-view matrix, camera centre and
+    (width, height, SH degree, degrees to use, tiles across, tiles down)."""
+    L = lib()
+    c2w = np.ascontiguousarray(c2w, np.float32).reshape(16)
+    vm, pvm, cp = np.zeros(16, np.float32), np.zeros(16, np.float32), np.zeros(3, np.float32)
+    ints = np.zeros(6, np.int32)
+    L.ref_prepare_cam(_p(c2w), int(width), int(height), C.c_float(fx), C.c_float(fy), C.c_float(cx),
+                      C.c_float(cy), int(step), int(sh_degree), int(sh_interval), int(rest_bases), _p(vm), _p(pvm),
+                      _p(cp), _p(ints, IP))
+    return vm, pvm, cp, tuple(int(v) for v in ints)
+
+
+def metrics(img, gt):
+    """The reference's evaluation metrics (psnr, l1_loss: model.cpp:33-49;
+    ssim_eval: ssim.cpp:61-123, window 11, sigma 1.5) of two [H, W, 3]
+    float32 images."""
+    L = lib()
+    img = np.ascontiguousarray(img, np.float32)
+    gt = np.ascontiguousarray(gt, np.float32)
+    h, w = img.shape[:2]
+    out = []
+    for name in ("ref_psnr", "ref_l1", "ref_ssim_eval"):
+        f = getattr(L, name)
+        f.restype = C.c_float
+        out.append(float(np.float32(f(_p(img), _p(gt), h, w))))
+    return tuple(out)

@@ -39,10 +39,12 @@ lanes return there or none does, and reports whether it ran.
 The rasterizers and the SSIM kernels use threadgroup memory, barriers and
 SIMD-group functions; metal_shim.h runs their threadgroups on host threads.
 
-The MCMC host code of core/src/model.cpp (computeRelocation, relocate,
-addNewGaussians, mcmcAfterTrain: lines 311-660) is copied the same way and
-compiled by ref_model.cpp against model_shim.h, a host stand-in for the
-Model class with the members that code uses.
+The host code on the path is copied the same way and compiled by
+ref_model.cpp against model_shim.h (host stand-ins for the Model, Camera and
+MTensor types with the members that code uses): from core/src/model.cpp the
+MCMC pass (computeRelocation, relocate, addNewGaussians, mcmcAfterTrain:
+lines 311-660), the camera setup (prepareCam, getDownscaleFactor) and the
+psnr / l1_loss metrics; from core/src/ssim.cpp ssim_eval and its blur.
 
 Usage: python oracle/ref_build.py [--reference DIR]   (default: /root/reference)
 """
@@ -59,10 +61,16 @@ OUT = os.path.join(HERE, "_ref")
 LIB = os.path.join(OUT, "libmsplat_ref.so")
 METAL = os.path.join("core", "metal", "msplat_metal.metal")
 MODEL = os.path.join("core", "src", "model.cpp")
-# The MCMC host code: computeRelocation, relocate, addNewGaussians and
-# mcmcAfterTrain, one contiguous range of model.cpp compiled against
-# model_shim.h (a host stand-in for the Model class) by ref_model.cpp.
-MODEL_RANGE = (311, 660, "void Model::computeRelocation(float opacity_old_sig, float* scale_old_exp, int N,", "}")
+SSIM = os.path.join("core", "src", "ssim.cpp")
+# Host code compiled by ref_model.cpp against model_shim.h (host stand-ins
+# for Model, Camera and MTensor): (file, first, last, first-line text, last-line text)
+HOST_RANGES = [
+    (MODEL, 33, 49, "// Metrics on CPU MTensor data", "}"),                      # psnr, l1_loss
+    (MODEL, 276, 282, "int Model::getDownscaleFactor(int step) {", "}"),
+    (MODEL, 311, 660, "void Model::computeRelocation(float opacity_old_sig, float* scale_old_exp, int N,", "}"),
+    (MODEL, 845, 889, "Model::CamSetup Model::prepareCam(Camera& cam, int step) {", "}"),
+    (SSIM, 26, 123, "// Separable Gaussian blur on a single-channel (H, W) image.", "}"),  # gaussianBlur, ssim_eval
+]
 
 # (first line, last line, text of the first line, text of the last line), 1-based, inclusive
 HELPER_RANGES = [
@@ -184,14 +192,18 @@ def build(reference: str, quiet: bool = False) -> str:
         spans[name] = span
         with open(os.path.join(OUT, f"k_{name}.inc"), "w") as f:
             f.write(body)
-    model_src = os.path.join(reference, MODEL)
-    if not os.path.exists(model_src):
-        raise SystemExit(f"{model_src} not found")
-    with open(model_src) as f:
-        model_lines = f.readlines()
-    with open(os.path.join(OUT, "model_mcmc.inc"), "w") as f:
-        f.write("// extracted by oracle/ref_build.py from " + MODEL + " (not committed)\n")
-        f.write(extract(model_lines, *MODEL_RANGE, path=MODEL))
+    host = "// extracted by oracle/ref_build.py from " + MODEL + " and " + SSIM + " (not committed)\n"
+    sources = {}
+    for path, first, last, head, tail in HOST_RANGES:
+        if path not in sources:
+            full = os.path.join(reference, path)
+            if not os.path.exists(full):
+                raise SystemExit(f"{full} not found")
+            with open(full) as f:
+                sources[path] = f.readlines()
+        host += extract(sources[path], first, last, head, tail, path=path)
+    with open(os.path.join(OUT, "model_host.inc"), "w") as f:
+        f.write(host)
     cxx = shutil.which("g++") or "c++"
     cmd = [cxx, "-O2", "-std=c++20", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
            "-Wno-unknown-pragmas", "-pthread", "-I", HERE, "-I", OUT, os.path.join(HERE, "ref_kernels.cpp"),
@@ -202,7 +214,8 @@ def build(reference: str, quiet: bool = False) -> str:
     if not quiet:
         for name, (a, b) in spans.items():
             print(f"{name}: {METAL}:{a}-{b}")
-        print(f"MCMC host code: {MODEL}:{MODEL_RANGE[0]}-{MODEL_RANGE[1]}")
+        for path, first, last, _, _ in HOST_RANGES:
+            print(f"host code: {path}:{first}-{last}")
         print(LIB)
     return LIB
 

@@ -1,11 +1,24 @@
-// The reference's MCMC host code (core/src/model.cpp:311-660:
-// computeRelocation, relocate, addNewGaussians, mcmcAfterTrain), compiled
-// unchanged against oracle/model_shim.h — TEST INFRASTRUCTURE ONLY.  The
-// code is copied into oracle/_ref/model_mcmc.inc by oracle/ref_build.py
-// (never committed); this file only wraps it for ctypes.
+// The reference's host code on the path, compiled unchanged against
+// oracle/model_shim.h — TEST INFRASTRUCTURE ONLY: from core/src/model.cpp
+// the MCMC pass (computeRelocation, relocate, addNewGaussians,
+// mcmcAfterTrain: 311-660), the camera setup (prepareCam: 845-889,
+// getDownscaleFactor: 276-282) and the psnr / l1_loss metrics (33-49); from
+// core/src/ssim.cpp ssim_eval (26-123).  The code is copied into
+// oracle/_ref/model_host.inc by oracle/ref_build.py (never committed); this
+// file only wraps it for ctypes.
 #include "model_shim.h"
 
-#include "model_mcmc.inc"
+#include "model_host.inc"
+
+namespace {
+HostTensor host_image(const float *img, int h, int w) {
+    HostTensor t;
+    t.p = const_cast<float *>(img);
+    t.shape = {h, w, 3};
+    t.row = (int64_t)w * 3;
+    return t;
+}
+}  // namespace
 
 extern "C" {
 
@@ -42,6 +55,49 @@ int ref_mcmc_after_train(int cap, int num_active, int rest_floats, float *means,
     m.mcmcAfterTrain(step);
     *reloc_count = m.mcmc_relocation_count;
     return m.num_active;
+}
+
+// Model::prepareCam (model.cpp:845-889) for a camera-to-world pose (row
+// major 4x4), size and intrinsics at a step: the view and projection-view
+// matrices, the camera centre, and (width, height, SH degree, degrees to
+// use, tiles across, tiles down) in ints[6].
+void ref_prepare_cam(const float c2w[16], int width, int height, float fx, float fy, float cx, float cy, int step,
+                     int sh_degree, int sh_interval, int rest_bases, float viewmat[16], float projviewmat[16],
+                     float cam_pos[3], int ints[6]) {
+    Model m;
+    m.shDegree = sh_degree;
+    m.shDegreeInterval = sh_interval;
+    m.featuresRest.shape = {1, rest_bases, 3};
+    Camera cam;
+    cam.width = width;
+    cam.height = height;
+    cam.fx = fx;
+    cam.fy = fy;
+    cam.cx = cx;
+    cam.cy = cy;
+    std::memcpy(cam.camToWorld, c2w, sizeof(cam.camToWorld));
+    const Model::CamSetup s = m.prepareCam(cam, step);
+    std::memcpy(viewmat, cam.cachedViewMat.data_ptr(), 64);
+    std::memcpy(projviewmat, cam.cachedProjViewMat.data_ptr(), 64);
+    for (int k = 0; k < 3; k++) cam_pos[k] = s.cam_pos[k];
+    ints[0] = s.width;
+    ints[1] = s.height;
+    ints[2] = s.degree;
+    ints[3] = s.degreesToUse;
+    ints[4] = std::get<0>(s.tileBounds);
+    ints[5] = std::get<1>(s.tileBounds);
+}
+
+// psnr, l1_loss (model.cpp:33-49) and ssim_eval with its defaults, window 11
+// and sigma 1.5 (ssim.cpp:61-123, ssim.hpp:17-18), of two [h, w, 3] images.
+float ref_psnr(const float *img, const float *gt, int h, int w) {
+    return psnr(host_image(img, h, w), host_image(gt, h, w));
+}
+float ref_l1(const float *img, const float *gt, int h, int w) {
+    return l1_loss(host_image(img, h, w), host_image(gt, h, w));
+}
+float ref_ssim_eval(const float *img, const float *gt, int h, int w) {
+    return ssim_eval(host_image(img, h, w), host_image(gt, h, w), 11, 1.5f);
 }
 
 }  // extern "C"

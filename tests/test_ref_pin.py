@@ -500,3 +500,59 @@ def test_golden_mcmc_host_code():
             assert np.array_equal(np.flatnonzero(dead), z[name + "/dst"][:int(dead.sum())])
         O.mcmc_apply(g0, m0, z[name + "/dst"], z[name + "/src"])
         assert _state_digest(g0, m0) == str(z[name + "/sha256"])
+
+
+# ---- camera setup and evaluation metrics (model.cpp:33-49, 845-889; ssim.cpp:26-123) ----
+
+@needs_reference
+def test_live_prepare_cam(ref_lib):
+    """The reference's Model::prepareCam against the oracle's prepare_cam and
+    the engine library's msplat_prepare_camera: view and projection-view
+    matrices and camera centre bit for bit over random poses, sizes and focal
+    lengths; its SH degree and degrees-to-use bands as the step schedule's."""
+    from msplat_gb300 import engine as E
+    from msplat_gb300.schedule import step_scalars
+    rng = np.random.default_rng(3)
+    cams = S.ring_cameras(8, 640, 480, 500.0, seed=3, jitter=1.0)
+    for k in range(64):
+        c = cams[k % 8]
+        c2w = np.asarray(c.cam_to_world, np.float32).copy()
+        c2w[:3, 3] += rng.normal(0, 0.5, 3).astype(np.float32)
+        w, h = int(rng.integers(16, 2000)), int(rng.integers(16, 2000))
+        fx, fy = float(rng.uniform(100, 3000)), float(rng.uniform(100, 3000))
+        cx, cy = w / 2.0, h / 2.0
+        step = int(rng.integers(0, 30000))
+        vm, pvm, cp, ints = ref_lib.prepare_cam(c2w, w, h, fx, fy, cx, cy, step)
+        for got in (O.prepare_cam(c2w, w, h, np.float32(fx), np.float32(fy)),
+                    E.prepare_cam(c2w, w, h, np.float32(fx), np.float32(fy))):
+            assert np.array_equal(np.asarray(got[0]).ravel(), vm)
+            assert np.array_equal(np.asarray(got[1]).ravel(), pvm)
+            assert np.array_equal(np.asarray(got[2]).ravel(), cp)
+        assert ints == (w, h, 3, step_scalars(step, max(step, 1))["degrees_to_use"], (w + 15) // 16, (h + 15) // 16)
+
+
+@needs_reference
+def test_live_eval_metrics(ref_lib):
+    """The reference's psnr, l1_loss and ssim_eval against the oracle's and
+    the engine library's host metrics (msplat_psnr, msplat_l1,
+    msplat_ssim_eval, which the trainer's evaluate uses) on random images of
+    odd sizes: identical floats."""
+    import ctypes as C
+    from msplat_gb300 import build
+    lib = C.CDLL(build.build())
+    fp = C.POINTER(C.c_float)
+    lib.msplat_psnr.restype = lib.msplat_l1.restype = lib.msplat_ssim_eval.restype = C.c_float
+    lib.msplat_psnr.argtypes = lib.msplat_l1.argtypes = [fp, fp, C.c_longlong]
+    lib.msplat_ssim_eval.argtypes = [fp, fp, C.c_int, C.c_int]
+    rng = np.random.default_rng(9)
+    for h, w in ((17, 23), (64, 48), (101, 7), (5, 130)):
+        gt = rng.random((h, w, 3), dtype=np.float32)
+        img = np.clip(gt + rng.normal(0, 0.05, gt.shape), 0, 1).astype(np.float32)
+        ref = ref_lib.metrics(img, gt)
+        mine = (float(O.psnr(img, gt)), float(O.l1(img, gt)), float(O.ssim_eval(img, gt)))
+        pi, pg = img.ctypes.data_as(fp), gt.ctypes.data_as(fp)
+        eng = (float(lib.msplat_psnr(pi, pg, img.size)), float(lib.msplat_l1(pi, pg, img.size)),
+               float(lib.msplat_ssim_eval(pi, pg, h, w)))
+        assert np.float32(mine[0]) == np.float32(ref[0]) and np.float32(eng[0]) == np.float32(ref[0])
+        assert np.float32(mine[1]) == np.float32(ref[1]) and np.float32(eng[1]) == np.float32(ref[1])
+        assert np.float32(mine[2]) == np.float32(ref[2]) and np.float32(eng[2]) == np.float32(ref[2])
