@@ -3,9 +3,11 @@
 The library is the reference's own Metal source for the per-Gaussian stages
 (projection + SH, projection backward + SH Adam, Adam, SGLD, regularizer,
 tile rectangle, sort key, active test, SSIM window) and the pixel stages
-(count and scatter of the tile intersections, monolithic and chunked
-rasterizers, SSIM + L1 loss), compiled as host C++ by oracle/ref_build.py
-from the reference tree (threadgroups on host threads).  It exists only where the
+(count, tile scan, scatter, per-tile sort + pack, monolithic and chunked
+rasterizers forward and backward, SSIM + L1 loss), and its host code on the
+path (camera setup, the MCMC relocation and growth pass, evaluation
+metrics), compiled as host C++ by oracle/ref_build.py from the reference
+tree (threadgroups on host threads).  It exists only where the
 reference tree does (the build container); the GPU machine never has it.  Only
 tests/ and tests/golden/make_ref_vectors.py use it, to pin the oracle.
 """
