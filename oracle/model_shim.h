@@ -1,9 +1,10 @@
 // Host stand-ins for the reference's Model class (core/include/model.hpp:
-// 17-130), its Camera (core/include/input_data.hpp:19-48) and MTensor, with
-// only the members the host code compiled by ref_model.cpp uses (the MCMC
-// pass, camera setup, evaluation metrics), so that code compiles unchanged
-// — TEST INFRASTRUCTURE ONLY (it pins the oracle's restatements; nothing in
-// the product uses it).
+// 17-130), its Camera, Points and InputData (core/include/input_data.hpp:
+// 19-65), the loader declarations (core/include/loaders.hpp) and MTensor,
+// with only the members the host code compiled by ref_model.cpp uses (the
+// MCMC pass, camera setup, evaluation metrics, the COLMAP loader), so that
+// code compiles unchanged — TEST INFRASTRUCTURE ONLY (it pins the oracle's
+// and the library's restatements; nothing in the product uses it).
 //
 // The reference keeps each parameter group and Adam moment as an MTensor
 // (core/include/metal_tensor.hpp) whose storage is shared with the GPU; here
@@ -20,10 +21,16 @@
 #include <cstdlib>
 #include <cstring>
 #include <iostream>
+#include <filesystem>
+#include <fstream>
 #include <limits>
 #include <memory>
 #include <random>
+#include <sstream>
+#include <stdexcept>
+#include <string>
 #include <tuple>
+#include <unordered_map>
 #include <vector>
 
 #define BLOCK_X 16
@@ -61,11 +68,34 @@ inline HostTensor gpu_empty(std::initializer_list<int64_t> shape, DType) {
 struct Camera {
     int width = 0, height = 0;
     float fx = 0, fy = 0, cx = 0, cy = 0;
+    float k1 = 0, k2 = 0, k3 = 0, p1 = 0, p2 = 0;
     float camToWorld[16] = {};
+    std::string filePath;
+    std::string relativeName;
     MTensor cachedViewMat, cachedProjViewMat;
     float cachedCamPos[3] = {};
     float cachedFovX = 0, cachedFovY = 0;
 };
+
+struct Points {
+    std::vector<float> xyz;
+    std::vector<uint8_t> rgb;
+    int64_t count = 0;
+};
+
+struct InputData {
+    std::vector<Camera> cameras;
+    float scale = 1.0f;
+    float translation[3] = {};
+    Points points;
+};
+
+namespace loaders {
+InputData loadColmap(const std::string &projectRoot, const std::string &imageSourcePath = "");
+}
+Points readPly(const std::string &path);
+Points readColmapPoints(const std::string &path);
+void autoScaleAndCenter(InputData &data);
 
 // GPU hooks the MCMC pass calls (core/metal/bindings.h): nothing to wait for
 // on the host, and no gradient NaN counters to report.

@@ -242,3 +242,35 @@ def metrics(img, gt):
         f.restype = C.c_float
         out.append(float(np.float32(f(_p(img), _p(gt), h, w))))
     return tuple(out)
+
+
+def load_colmap(root):
+    """The reference's loaders::loadColmap (load_colmap.cpp, compiled
+    unchanged) of a COLMAP binary dataset: a list of cameras (dicts with
+    c2w [4,4], intr (fx, fy, cx, cy), size (w, h), dist (k1, k2, k3, p1, p2),
+    name) in its order, the point cloud (xyz, rgb) after its centring and
+    scaling, and (scale, translation)."""
+    L = lib()
+    L.ref_colmap_load.restype = C.c_void_p
+    h = L.ref_colmap_load(str(root).encode())
+    if not h:
+        raise RuntimeError(f"the reference's loader rejected {root}")
+    h = C.c_void_p(h)
+    try:
+        cams = []
+        for i in range(L.ref_colmap_num_cameras(h)):
+            c2w, intr = np.zeros(16, np.float32), np.zeros(4, np.float32)
+            size, dist = np.zeros(2, np.int32), np.zeros(5, np.float32)
+            name = C.create_string_buffer(512)
+            L.ref_colmap_camera(h, i, _p(c2w), _p(intr), _p(size, IP), _p(dist), name, 512)
+            cams.append(dict(c2w=c2w.reshape(4, 4), intr=intr, size=tuple(int(v) for v in size), dist=dist,
+                             name=name.value.decode()))
+        L.ref_colmap_points.restype = C.c_longlong
+        n = L.ref_colmap_points(h, None, None)
+        xyz, rgb = np.zeros((n, 3), np.float32), np.zeros((n, 3), np.uint8)
+        L.ref_colmap_points(h, _p(xyz), rgb.ctypes.data_as(C.POINTER(C.c_uint8)))
+        scale, tr = C.c_float(), np.zeros(3, np.float32)
+        L.ref_colmap_transform(h, C.byref(scale), _p(tr))
+        return cams, (xyz, rgb), (float(scale.value), tr)
+    finally:
+        L.ref_colmap_free(h)

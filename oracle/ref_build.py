@@ -40,11 +40,14 @@ The rasterizers and the SSIM kernels use threadgroup memory, barriers and
 SIMD-group functions; metal_shim.h runs their threadgroups on host threads.
 
 The host code on the path is copied the same way and compiled by
-ref_model.cpp against model_shim.h (host stand-ins for the Model, Camera and
-MTensor types with the members that code uses): from core/src/model.cpp the
-MCMC pass (computeRelocation, relocate, addNewGaussians, mcmcAfterTrain:
-lines 311-660), the camera setup (prepareCam, getDownscaleFactor) and the
-psnr / l1_loss metrics; from core/src/ssim.cpp ssim_eval and its blur.
+ref_model.cpp against model_shim.h (host stand-ins for the Model, Camera,
+InputData and MTensor types with the members that code uses): from
+core/src/model.cpp the MCMC pass (computeRelocation, relocate,
+addNewGaussians, mcmcAfterTrain: lines 311-660), the camera setup
+(prepareCam, getDownscaleFactor) and the psnr / l1_loss metrics; from
+core/src/ssim.cpp ssim_eval and its blur; the COLMAP binary loader
+(loaders/load_colmap.cpp), the point-cloud readers (loaders/load_ply.cpp)
+and autoScaleAndCenter (input_data.cpp).
 
 Usage: python oracle/ref_build.py [--reference DIR]   (default: /root/reference)
 """
@@ -62,6 +65,9 @@ LIB = os.path.join(OUT, "libmsplat_ref.so")
 METAL = os.path.join("core", "metal", "msplat_metal.metal")
 MODEL = os.path.join("core", "src", "model.cpp")
 SSIM = os.path.join("core", "src", "ssim.cpp")
+COLMAP = os.path.join("core", "src", "loaders", "load_colmap.cpp")
+PLY = os.path.join("core", "src", "loaders", "load_ply.cpp")
+INPUT = os.path.join("core", "src", "input_data.cpp")
 # Host code compiled by ref_model.cpp against model_shim.h (host stand-ins
 # for Model, Camera and MTensor): (file, first, last, first-line text, last-line text)
 HOST_RANGES = [
@@ -70,6 +76,9 @@ HOST_RANGES = [
     (MODEL, 311, 660, "void Model::computeRelocation(float opacity_old_sig, float* scale_old_exp, int N,", "}"),
     (MODEL, 845, 889, "Model::CamSetup Model::prepareCam(Camera& cam, int step) {", "}"),
     (SSIM, 26, 123, "// Separable Gaussian blur on a single-channel (H, W) image.", "}"),  # gaussianBlur, ssim_eval
+    (COLMAP, 7, 165, "namespace fs = std::filesystem;", "}"),               # the COLMAP binary loader
+    (PLY, 6, 205, "// Property types in PLY files", "}"),                   # readPly, readColmapPoints
+    (INPUT, 115, 169, "void autoScaleAndCenter(InputData &data) {", "}"),   # pose centring and scaling
 ]
 
 # (first line, last line, text of the first line, text of the last line), 1-based, inclusive
@@ -192,7 +201,7 @@ def build(reference: str, quiet: bool = False) -> str:
         spans[name] = span
         with open(os.path.join(OUT, f"k_{name}.inc"), "w") as f:
             f.write(body)
-    host = "// extracted by oracle/ref_build.py from " + MODEL + " and " + SSIM + " (not committed)\n"
+    host = "// extracted by oracle/ref_build.py from the reference's host sources (not committed)\n"
     sources = {}
     for path, first, last, head, tail in HOST_RANGES:
         if path not in sources:

@@ -3,9 +3,14 @@
 // the MCMC pass (computeRelocation, relocate, addNewGaussians,
 // mcmcAfterTrain: 311-660), the camera setup (prepareCam: 845-889,
 // getDownscaleFactor: 276-282) and the psnr / l1_loss metrics (33-49); from
-// core/src/ssim.cpp ssim_eval (26-123).  The code is copied into
+// core/src/ssim.cpp ssim_eval (26-123); the COLMAP binary loader
+// (loaders/load_colmap.cpp:7-165) with the point readers
+// (loaders/load_ply.cpp:6-205) and autoScaleAndCenter (input_data.cpp:
+// 115-169).  The code is copied into
 // oracle/_ref/model_host.inc by oracle/ref_build.py (never committed); this
 // file only wraps it for ctypes.
+#include <cstdio>
+
 #include "model_shim.h"
 
 #include "model_host.inc"
@@ -99,5 +104,42 @@ float ref_l1(const float *img, const float *gt, int h, int w) {
 float ref_ssim_eval(const float *img, const float *gt, int h, int w) {
     return ssim_eval(host_image(img, h, w), host_image(gt, h, w), 11, 1.5f);
 }
+
+// loaders::loadColmap (load_colmap.cpp:122-165) of a dataset directory:
+// its cameras in the reference's order with their poses after
+// autoScaleAndCenter, and the point cloud.  Returns a handle, or NULL when
+// the loader threw.
+void *ref_colmap_load(const char *root) {
+    try {
+        return new InputData(loaders::loadColmap(root));
+    } catch (const std::exception &) {
+        return nullptr;
+    }
+}
+int ref_colmap_num_cameras(void *h) { return (int)static_cast<InputData *>(h)->cameras.size(); }
+// Camera i: camera-to-world pose, (fx, fy, cx, cy), (width, height),
+// (k1, k2, k3, p1, p2) and its file name relative to the image folder.
+void ref_colmap_camera(void *h, int i, float c2w[16], float intr[4], int size[2], float dist[5], char *name,
+                       int name_cap) {
+    const Camera &c = static_cast<InputData *>(h)->cameras[(size_t)i];
+    std::memcpy(c2w, c.camToWorld, 64);
+    intr[0] = c.fx; intr[1] = c.fy; intr[2] = c.cx; intr[3] = c.cy;
+    size[0] = c.width; size[1] = c.height;
+    dist[0] = c.k1; dist[1] = c.k2; dist[2] = c.k3; dist[3] = c.p1; dist[4] = c.p2;
+    std::snprintf(name, (size_t)name_cap, "%s", c.relativeName.c_str());
+}
+// The point cloud (xyz, rgb; either may be NULL): returns the point count.
+long long ref_colmap_points(void *h, float *xyz, uint8_t *rgb) {
+    const Points &p = static_cast<InputData *>(h)->points;
+    if (xyz) std::memcpy(xyz, p.xyz.data(), p.xyz.size() * sizeof(float));
+    if (rgb) std::memcpy(rgb, p.rgb.data(), p.rgb.size());
+    return p.count;
+}
+void ref_colmap_transform(void *h, float *scale, float translation[3]) {
+    const InputData *d = static_cast<InputData *>(h);
+    *scale = d->scale;
+    for (int k = 0; k < 3; k++) translation[k] = d->translation[k];
+}
+void ref_colmap_free(void *h) { delete static_cast<InputData *>(h); }
 
 }  // extern "C"

@@ -556,3 +556,77 @@ def test_live_eval_metrics(ref_lib):
         assert np.float32(mine[0]) == np.float32(ref[0]) and np.float32(eng[0]) == np.float32(ref[0])
         assert np.float32(mine[1]) == np.float32(ref[1]) and np.float32(eng[1]) == np.float32(ref[1])
         assert np.float32(mine[2]) == np.float32(ref[2]) and np.float32(eng[2]) == np.float32(ref[2])
+
+
+# ---- dataset ingestion (loaders/load_colmap.cpp, load_ply.cpp, input_data.cpp:115-169) ----
+
+def write_colmap_scene(root, seed, ply_points=False):
+    """A COLMAP binary dataset: 12 views from two cameras (PINHOLE and
+    SIMPLE_PINHOLE) written in shuffled order with unsorted names, small PNG
+    images, and 200 points with tracks (points3D.bin), or as a binary PLY
+    (points3D.ply) with ply_points; returns nothing (files only)."""
+    import struct
+    from test_dataset_io import _pose, _w2c, _write_ply_points, write_png
+    rng = np.random.default_rng(seed)
+    sp = root / "sparse" / "0"
+    os.makedirs(sp)
+    os.makedirs(root / "images")
+    with open(sp / "cameras.bin", "wb") as f:
+        f.write(struct.pack("<Q", 2))
+        f.write(struct.pack("<IiQQ", 1, 1, 32, 24) + struct.pack("<4d", 29.5, 31.25, 16.0, 12.0))
+        f.write(struct.pack("<IiQQ", 2, 0, 40, 20) + struct.pack("<3d", 27.0, 20.0, 10.0))
+    names = [f"v{int(k):03d}_{int(rng.integers(1000))}.png" for k in rng.permutation(12)]
+    with open(sp / "images.bin", "wb") as f:
+        f.write(struct.pack("<Q", 12))
+        for k, name in enumerate(names):
+            a = rng.uniform(0, 2 * np.pi)
+            eye = (rng.uniform(3, 6) * np.cos(a), rng.uniform(3, 6) * np.sin(a), rng.uniform(-1, 2))
+            q, t = _w2c(_pose(eye))
+            cam = 1 + (k % 2)
+            f.write(struct.pack("<I4d3dI", k + 1, *q, *t, cam) + name.encode() + b"\0")
+            f.write(struct.pack("<Q", 1) + struct.pack("<ddQ", 1.0, 2.0, 7))
+            w, h = (32, 24) if cam == 1 else (40, 20)
+            img = rng.integers(0, 256, (h, w, 3), dtype=np.uint8)
+            write_png(root / "images" / name, [img[y].tobytes() for y in range(h)], 2, 8)
+    xyz = rng.normal(0, 1.5, (200, 3))
+    rgb = rng.integers(0, 256, (200, 3), dtype=np.uint8)
+    if ply_points:
+        _write_ply_points(sp / "points3D.ply", xyz.astype(np.float32), rgb)
+        return
+    with open(sp / "points3D.bin", "wb") as f:
+        f.write(struct.pack("<Q", 200))
+        for i in range(200):
+            f.write(struct.pack("<Q3d3Bd", i, *xyz[i], *rgb[i], 0.5))
+            f.write(struct.pack("<Q", 2) + struct.pack("<IIII", 1, 0, 2, 0))
+
+
+@needs_reference
+@pytest.mark.parametrize("seed,ply_points", [(1, False), (2, False), (3, True)])
+def test_live_colmap_loader(ref_lib, tmp_path, seed, ply_points):
+    """The reference's COLMAP binary loader with its point readers
+    (points3D.bin, or points3D.ply) and autoScaleAndCenter against the
+    library's msplat_dataset_create: the same cameras in the same order
+    (sorted by file name), identical intrinsics and sizes, camera-to-world
+    poses and centred, scaled points bit for bit."""
+    import ctypes as C
+    from msplat_gb300 import api as A
+    write_colmap_scene(tmp_path, seed, ply_points)
+    cams, (xyz, rgb), _ = ref_lib.load_colmap(tmp_path)
+    assert [c["name"] for c in cams] == sorted(c["name"] for c in cams)
+    ds = A.Dataset(str(tmp_path))
+    L = A._lib()
+    assert ds.num_train == len(cams) == 12
+    for i, c in enumerate(cams):
+        intr, size, c2w = np.zeros(4, np.float32), np.zeros(2, np.int32), np.zeros(16, np.float32)
+        img = np.zeros((c["size"][1], c["size"][0], 3), np.uint8)
+        assert L.msplat_dataset_camera(ds.h, i, 0, intr.ctypes.data_as(C.POINTER(C.c_float)),
+                                       size.ctypes.data_as(C.POINTER(C.c_int)),
+                                       c2w.ctypes.data_as(C.POINTER(C.c_float)),
+                                       img.ctypes.data_as(C.POINTER(C.c_uint8))) == 0
+        assert tuple(size) == c["size"]
+        assert np.array_equal(intr, c["intr"]) and not c["dist"].any()
+        assert np.array_equal(c2w, c["c2w"].ravel()), (i, c2w - c["c2w"].ravel())
+    pts, cols = np.zeros_like(xyz), np.zeros_like(rgb)
+    assert L.msplat_dataset_points(ds.h, pts.ctypes.data_as(C.POINTER(C.c_float)),
+                                   cols.ctypes.data_as(C.POINTER(C.c_uint8))) == len(xyz)
+    assert np.array_equal(pts, xyz) and np.array_equal(cols, rgb)
