@@ -171,6 +171,35 @@ int msplat_image_read(const char *path, float *rgb, int *width, int *height);
  * stderr).  msplat_trainer_load_checkpoint applies the same checks. */
 int msplat_checkpoint_info(const char *path, int *num_points, int *sh_degree, int *iteration);
 
+/* Host-side PLY and .splat files of Gaussians held by the caller (host
+ * arrays in the reference layouts, n rows: means [n,3], log-scales [n,3],
+ * quaternions [n,4], features_dc [n,3], features_rest [n,rest_bases,3],
+ * opacity logits [n]), without a trainer — for models trained through the
+ * differentiable renderer, say.  They are the trainer's own writers:
+ * msplat_write_ply is saveGaussianPly (core/src/loaders/save_gaussians.cpp:
+ * 10-88: non-finite Gaussians dropped, f_rest channel-major, the iteration
+ * comment), msplat_write_splat is saveGaussianSplat (:90-139: 32 B per
+ * Gaussian, largest first).  With keep_crs the positions and scales are
+ * mapped back to the dataset's frame: x / scale + translation, log(e^s /
+ * scale).  Return 0, -1 for invalid arguments, -2 when the file cannot be
+ * written (reason on stderr). */
+int msplat_write_ply(const char *path, int n, int rest_bases, const float *means, const float *scales,
+                     const float *quats, const float *features_dc, const float *features_rest,
+                     const float *opacities, int step, int keep_crs, float scale, const float translation[3]);
+int msplat_write_splat(const char *path, int n, int rest_bases, const float *means, const float *scales,
+                       const float *quats, const float *features_dc, const float *features_rest,
+                       const float *opacities, int keep_crs, float scale, const float translation[3]);
+
+/* A Gaussian PLY read as loadGaussianPly does (save_gaussians.cpp:141-231):
+ * msplat_ply_info gives its rows, rest bases and iteration (any output may
+ * be NULL); msplat_read_ply fills caller arrays of those sizes (the layouts
+ * above), with keep_crs mapping the file's frame into the dataset's:
+ * (x - translation) * scale, log(scale e^s).  Return 0, -1 for invalid
+ * arguments, -2 for a missing or malformed file (reason on stderr). */
+int msplat_ply_info(const char *path, int *num_points, int *rest_bases, int *iteration);
+int msplat_read_ply(const char *path, int keep_crs, float scale, const float translation[3], float *means,
+                    float *scales, float *quats, float *features_dc, float *features_rest, float *opacities);
+
 /* SSIM + L1 training loss and dL/dimage without any device allocation.
  * No counterpart in the reference: it is for callers that cannot call
  * cudaMalloc (a host application or server that owns all device memory

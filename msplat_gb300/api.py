@@ -88,6 +88,11 @@ def _lib():
     L.msplat_trainer_engine.argtypes = [vp]
     L.msplat_trainer_engine.restype = vp
     L.msplat_trainer_mcmc_stats.argtypes = [vp, C.POINTER(N.MsplatMcmcStats)]
+    hg = [C.c_int, C.c_int, fp, fp, fp, fp, fp, fp]
+    L.msplat_write_ply.argtypes = [cp] + hg + [C.c_int, C.c_int, C.c_float, fp]
+    L.msplat_write_splat.argtypes = [cp] + hg + [C.c_int, C.c_float, fp]
+    L.msplat_ply_info.argtypes = [cp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.msplat_read_ply.argtypes = [cp, C.c_int, C.c_float, fp, fp, fp, fp, fp, fp, fp]
     L.msplat_viewer_create.argtypes = [cp, C.c_int, C.c_int, C.c_float]
     L.msplat_viewer_create.restype = vp
     L.msplat_viewer_render.argtypes = [vp, fp, C.POINTER(C.c_uint8)]
@@ -417,6 +422,52 @@ class Viewer:
         if getattr(self, "h", None):
             _lib().msplat_viewer_destroy(self.h)
             self.h = None
+
+
+def _host_arrays(gaussians):
+    """(means, scales, quats, features_dc, features_rest [n, R, 3], opacities)
+    as contiguous float32 arrays, and the rest bases R."""
+    arrs = [np.ascontiguousarray(a, np.float32) for a in gaussians]
+    n = arrs[0].shape[0]
+    rest = arrs[4].reshape(n, -1, 3).shape[1] if arrs[4].size else 0
+    return arrs, n, rest
+
+
+def write_ply(path: str, gaussians, step: int = 0, keep_crs: bool = False, scale: float = 1.0,
+              translation=(0.0, 0.0, 0.0)) -> None:
+    """Writes Gaussians held on the host (the arrays get_gaussians returns,
+    or a GaussianSet's arrays) as the trainer's PLY export does."""
+    arrs, n, rest = _host_arrays(gaussians)
+    t = np.asarray(translation, np.float32)
+    if _lib().msplat_write_ply(path.encode(), n, rest, *[_fp(a) for a in arrs], int(step), int(keep_crs),
+                               float(scale), _fp(t)) != 0:
+        raise RuntimeError(f"could not write {path}")
+
+
+def write_splat(path: str, gaussians, keep_crs: bool = False, scale: float = 1.0,
+                translation=(0.0, 0.0, 0.0)) -> None:
+    """Writes Gaussians held on the host as the trainer's .splat export does."""
+    arrs, n, rest = _host_arrays(gaussians)
+    t = np.asarray(translation, np.float32)
+    if _lib().msplat_write_splat(path.encode(), n, rest, *[_fp(a) for a in arrs], int(keep_crs), float(scale),
+                                 _fp(t)) != 0:
+        raise RuntimeError(f"could not write {path}")
+
+
+def read_ply(path: str, keep_crs: bool = False, scale: float = 1.0, translation=(0.0, 0.0, 0.0)):
+    """A Gaussian PLY as the trainer loads it: ([means, scales, quats,
+    features_dc, features_rest [n, R, 3], opacities], iteration)."""
+    L = _lib()
+    n, rest, step = C.c_int(), C.c_int(), C.c_int()
+    if L.msplat_ply_info(path.encode(), C.byref(n), C.byref(rest), C.byref(step)) != 0:
+        raise RuntimeError(f"could not read {path}")
+    n = n.value
+    shapes = [(n, 3), (n, 3), (n, 4), (n, 3), (n, rest.value, 3), (n,)]
+    arrs = [np.zeros(s, np.float32) for s in shapes]
+    t = np.asarray(translation, np.float32)
+    if L.msplat_read_ply(path.encode(), int(keep_crs), float(scale), _fp(t), *[_fp(a) for a in arrs]) != 0:
+        raise RuntimeError(f"could not read {path}")
+    return arrs, step.value
 
 
 def sync():

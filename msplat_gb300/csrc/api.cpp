@@ -1188,6 +1188,73 @@ int msplat_checkpoint_info(const char *path, int *num_points, int *sh_degree, in
         return 0;
     }, -1);
 }
+static bool host_gaussians_args(int n, int rest_bases, const float *means, const float *scales, const float *quats,
+                                const float *features_dc, const float *features_rest, const float *opacities) {
+    if (n < 0 || rest_bases < 0 || rest_bases > 24) return false;
+    return n == 0 || (means && scales && quats && features_dc && opacities && (rest_bases == 0 || features_rest));
+}
+static HostGaussians host_gaussians(int n, int rest_bases, const float *means, const float *scales,
+                                    const float *quats, const float *features_dc, const float *features_rest,
+                                    const float *opacities) {
+    HostGaussians h;
+    h.n = n;
+    h.rest = rest_bases;
+    const float *src[6] = {means, scales, quats, features_dc, features_rest, opacities};
+    const size_t w[6] = {3, 3, 4, 3, (size_t)3 * rest_bases, 1};
+    for (int g = 0; g < 6; g++)
+        if (src[g]) h.a[g].assign(src[g], src[g] + (size_t)n * w[g]);
+    return h;
+}
+int msplat_write_ply(const char *path, int n, int rest_bases, const float *means, const float *scales,
+                     const float *quats, const float *features_dc, const float *features_rest,
+                     const float *opacities, int step, int keep_crs, float scale, const float translation[3]) {
+    if (!path || !host_gaussians_args(n, rest_bases, means, scales, quats, features_dc, features_rest, opacities) ||
+        (keep_crs && (!translation || !(scale > 0.f))))
+        return -1;
+    return guard("write_ply", [&]() {
+        const float zero[3] = {0.f, 0.f, 0.f};
+        write_ply(path, host_gaussians(n, rest_bases, means, scales, quats, features_dc, features_rest, opacities),
+                  step, keep_crs != 0, scale, translation ? translation : zero);
+        return 0;
+    }, -2);
+}
+int msplat_write_splat(const char *path, int n, int rest_bases, const float *means, const float *scales,
+                       const float *quats, const float *features_dc, const float *features_rest,
+                       const float *opacities, int keep_crs, float scale, const float translation[3]) {
+    if (!path || !host_gaussians_args(n, rest_bases, means, scales, quats, features_dc, features_rest, opacities) ||
+        (keep_crs && (!translation || !(scale > 0.f))))
+        return -1;
+    return guard("write_splat", [&]() {
+        const float zero[3] = {0.f, 0.f, 0.f};
+        write_splat(path, host_gaussians(n, rest_bases, means, scales, quats, features_dc, features_rest, opacities),
+                    keep_crs != 0, scale, translation ? translation : zero);
+        return 0;
+    }, -2);
+}
+int msplat_ply_info(const char *path, int *num_points, int *rest_bases, int *iteration) {
+    if (!path) return -1;
+    return guard("ply_info", [&]() {
+        int step = 0;
+        const HostGaussians h = read_ply(path, &step, false, 1.f, nullptr);
+        if (num_points) *num_points = h.n;
+        if (rest_bases) *rest_bases = h.rest;
+        if (iteration) *iteration = step;
+        return 0;
+    }, -2);
+}
+int msplat_read_ply(const char *path, int keep_crs, float scale, const float translation[3], float *means,
+                    float *scales, float *quats, float *features_dc, float *features_rest, float *opacities) {
+    if (!path || !means || !scales || !quats || !features_dc || !opacities ||
+        (keep_crs && (!translation || !(scale > 0.f))))
+        return -1;
+    return guard("read_ply", [&]() {
+        const HostGaussians h = read_ply(path, nullptr, keep_crs != 0, scale, translation);
+        float *dst[6] = {means, scales, quats, features_dc, features_rest, opacities};
+        for (int g = 0; g < 6; g++)
+            if (dst[g] && !h.a[g].empty()) std::memcpy(dst[g], h.a[g].data(), h.a[g].size() * sizeof(float));
+        return 0;
+    }, -2);
+}
 int msplat_dataset_num_train(MsplatDataset ds) { return ds ? (int)DS(ds)->train.size() : 0; }
 int msplat_dataset_num_test(MsplatDataset ds) { return ds ? (int)DS(ds)->test.size() : 0; }
 

@@ -1,8 +1,10 @@
 // Host stand-ins for the reference's Model class (core/include/model.hpp:
 // 17-130), its Camera, Points and InputData (core/include/input_data.hpp:
-// 19-65), the loader declarations (core/include/loaders.hpp) and MTensor,
+// 19-65), the loader and Gaussian-file declarations (core/include/
+// loaders.hpp) and MTensor,
 // with only the members the host code compiled by ref_model.cpp uses (the
-// MCMC pass, camera setup, evaluation metrics, the COLMAP loader), so that
+// MCMC pass, camera setup, evaluation metrics, the COLMAP loader, the
+// Gaussian PLY / .splat files), so that
 // code compiles unchanged — TEST INFRASTRUCTURE ONLY (it pins the oracle's
 // and the library's restatements; nothing in the product uses it).
 //
@@ -18,6 +20,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <iostream>
@@ -25,6 +28,7 @@
 #include <fstream>
 #include <limits>
 #include <memory>
+#include <numeric>
 #include <random>
 #include <sstream>
 #include <stdexcept>
@@ -56,13 +60,16 @@ struct HostTensor {
 using MTensor = HostTensor;
 
 enum class DType { Float32 };
-inline HostTensor gpu_empty(std::initializer_list<int64_t> shape, DType) {
+inline HostTensor gpu_empty(const std::vector<int64_t> &shape, DType) {
     HostTensor t;
-    t.shape.assign(shape.begin(), shape.end());
+    t.shape = shape;
     t.owned = std::make_shared<std::vector<float>>((size_t)t.numel());
     t.p = t.owned->data();
     t.row = t.shape.size() > 1 ? t.numel() / t.shape[0] : 1;
     return t;
+}
+inline HostTensor gpu_empty(std::initializer_list<int64_t> shape, DType d) {
+    return gpu_empty(std::vector<int64_t>(shape), d);
 }
 
 struct Camera {
@@ -96,6 +103,20 @@ InputData loadColmap(const std::string &projectRoot, const std::string &imageSou
 Points readPly(const std::string &path);
 Points readColmapPoints(const std::string &path);
 void autoScaleAndCenter(InputData &data);
+
+struct GaussianParams {
+    MTensor &means, &scales, &quats, &featuresDc, &featuresRest, &opacities;
+    float scale;
+    float translation[3];
+    bool keepCrs;
+};
+struct LoadedGaussians {
+    MTensor means, scales, quats, featuresDc, featuresRest, opacities;
+    int step;
+};
+void saveGaussianPly(const std::string &path, GaussianParams &p, int step);
+void saveGaussianSplat(const std::string &path, GaussianParams &p);
+LoadedGaussians loadGaussianPly(const std::string &path, float scale, const float translation[3], bool keepCrs);
 
 // GPU hooks the MCMC pass calls (core/metal/bindings.h): nothing to wait for
 // on the host, and no gradient NaN counters to report.

@@ -274,3 +274,38 @@ def load_colmap(root):
         return cams, (xyz, rgb), (float(scale.value), tr)
     finally:
         L.ref_colmap_free(h)
+
+
+def save_gaussians(path, arrays, splat=False, step=0, keep_crs=False, scale=1.0, translation=(0.0, 0.0, 0.0)):
+    """The reference's saveGaussianPly, or saveGaussianSplat with splat
+    (save_gaussians.cpp:10-139, compiled unchanged), of host arrays (means,
+    scales, quats, features_dc, features_rest [n, R, 3], opacities)."""
+    L = lib()
+    a = [np.ascontiguousarray(x, np.float32) for x in arrays]
+    n = a[0].shape[0]
+    rest = a[4].reshape(n, -1, 3).shape[1]
+    t = np.asarray(translation, np.float32)
+    L.ref_save_gaussians(str(path).encode(), int(splat), n, rest, *[_p(x) for x in a], int(step), int(keep_crs),
+                         C.c_float(scale), _p(t))
+
+
+def load_gaussians(path, keep_crs=False, scale=1.0, translation=(0.0, 0.0, 0.0)):
+    """The reference's loadGaussianPly (save_gaussians.cpp:141-231):
+    ([means, scales, quats, features_dc, features_rest [n, R, 3],
+    opacities], iteration)."""
+    L = lib()
+    t = np.asarray(translation, np.float32)
+    L.ref_load_gaussians.restype = C.c_void_p
+    h = L.ref_load_gaussians(str(path).encode(), C.c_float(scale), _p(t), int(keep_crs))
+    if not h:
+        raise RuntimeError(f"the reference's loader rejected {path}")
+    h = C.c_void_p(h)
+    try:
+        info = np.zeros(3, np.int32)
+        L.ref_loaded_info(h, _p(info, IP))
+        n, rest, step = (int(v) for v in info)
+        arrs = [np.zeros(s, np.float32) for s in ((n, 3), (n, 3), (n, 4), (n, 3), (n, rest, 3), (n,))]
+        L.ref_loaded_arrays(h, *[_p(x) for x in arrs])
+        return arrs, step
+    finally:
+        L.ref_loaded_free(h)

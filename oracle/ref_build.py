@@ -46,8 +46,9 @@ core/src/model.cpp the MCMC pass (computeRelocation, relocate,
 addNewGaussians, mcmcAfterTrain: lines 311-660), the camera setup
 (prepareCam, getDownscaleFactor) and the psnr / l1_loss metrics; from
 core/src/ssim.cpp ssim_eval and its blur; the COLMAP binary loader
-(loaders/load_colmap.cpp), the point-cloud readers (loaders/load_ply.cpp)
-and autoScaleAndCenter (input_data.cpp).
+(loaders/load_colmap.cpp), the point-cloud readers (loaders/load_ply.cpp),
+autoScaleAndCenter (input_data.cpp) and the Gaussian PLY / .splat writers
+and PLY reader (loaders/save_gaussians.cpp).
 
 Usage: python oracle/ref_build.py [--reference DIR]   (default: /root/reference)
 """
@@ -68,6 +69,7 @@ SSIM = os.path.join("core", "src", "ssim.cpp")
 COLMAP = os.path.join("core", "src", "loaders", "load_colmap.cpp")
 PLY = os.path.join("core", "src", "loaders", "load_ply.cpp")
 INPUT = os.path.join("core", "src", "input_data.cpp")
+SAVE = os.path.join("core", "src", "loaders", "save_gaussians.cpp")
 # Host code compiled by ref_model.cpp against model_shim.h (host stand-ins
 # for Model, Camera and MTensor): (file, first, last, first-line text, last-line text)
 HOST_RANGES = [
@@ -79,6 +81,7 @@ HOST_RANGES = [
     (COLMAP, 7, 165, "namespace fs = std::filesystem;", "}"),               # the COLMAP binary loader
     (PLY, 6, 205, "// Property types in PLY files", "}"),                   # readPly, readColmapPoints
     (INPUT, 115, 169, "void autoScaleAndCenter(InputData &data) {", "}"),   # pose centring and scaling
+    (SAVE, 8, 231, "static const double C0 = 0.28209479177387814;", "}"),  # Gaussian PLY / .splat files
 ]
 
 # (first line, last line, text of the first line, text of the last line), 1-based, inclusive

@@ -6,7 +6,8 @@
 // core/src/ssim.cpp ssim_eval (26-123); the COLMAP binary loader
 // (loaders/load_colmap.cpp:7-165) with the point readers
 // (loaders/load_ply.cpp:6-205) and autoScaleAndCenter (input_data.cpp:
-// 115-169).  The code is copied into
+// 115-169); the Gaussian PLY / .splat files (loaders/save_gaussians.cpp:
+// 8-231).  The code is copied into
 // oracle/_ref/model_host.inc by oracle/ref_build.py (never committed); this
 // file only wraps it for ctypes.
 #include <cstdio>
@@ -141,5 +142,57 @@ void ref_colmap_transform(void *h, float *scale, float translation[3]) {
     for (int k = 0; k < 3; k++) translation[k] = d->translation[k];
 }
 void ref_colmap_free(void *h) { delete static_cast<InputData *>(h); }
+
+namespace {
+HostTensor host_rows(const float *a, int64_t n, std::vector<int64_t> shape) {
+    HostTensor t;
+    t.p = const_cast<float *>(a);
+    t.shape = std::move(shape);
+    t.row = n ? t.numel() / n : 1;
+    return t;
+}
+}  // namespace
+
+// saveGaussianPly (save_gaussians.cpp:10-88) or, with splat, saveGaussianSplat
+// (:90-139) of n Gaussians in host arrays (means [n,3], scales [n,3], quats
+// [n,4], features_dc [n,3], features_rest [n,rest_bases,3], opacities [n]).
+void ref_save_gaussians(const char *path, int splat, int n, int rest_bases, const float *means, const float *scales,
+                        const float *quats, const float *features_dc, const float *features_rest,
+                        const float *opacities, int step, int keep_crs, float scale, const float translation[3]) {
+    HostTensor m = host_rows(means, n, {n, 3}), s = host_rows(scales, n, {n, 3}), q = host_rows(quats, n, {n, 4});
+    HostTensor dc = host_rows(features_dc, n, {n, 3}), fr = host_rows(features_rest, n, {n, rest_bases, 3});
+    HostTensor op = host_rows(opacities, n, {n, 1});
+    GaussianParams p{m, s, q, dc, fr, op, scale, {translation[0], translation[1], translation[2]}, keep_crs != 0};
+    if (splat)
+        saveGaussianSplat(path, p);
+    else
+        saveGaussianPly(path, p, step);
+}
+
+// loadGaussianPly (save_gaussians.cpp:141-231): returns a handle (NULL when
+// it threw); ref_loaded_info gives (rows, rest bases, iteration) and
+// ref_loaded_arrays copies the arrays out in the layouts above.
+void *ref_load_gaussians(const char *path, float scale, const float translation[3], int keep_crs) {
+    try {
+        return new LoadedGaussians(loadGaussianPly(path, scale, translation, keep_crs != 0));
+    } catch (const std::exception &) {
+        return nullptr;
+    }
+}
+void ref_loaded_info(void *h, int info[3]) {
+    const LoadedGaussians *g = static_cast<LoadedGaussians *>(h);
+    info[0] = (int)g->means.size(0);
+    info[1] = (int)g->featuresRest.size(1);
+    info[2] = g->step;
+}
+void ref_loaded_arrays(void *h, float *means, float *scales, float *quats, float *features_dc, float *features_rest,
+                       float *opacities) {
+    LoadedGaussians *g = static_cast<LoadedGaussians *>(h);
+    HostTensor *src[6] = {&g->means, &g->scales, &g->quats, &g->featuresDc, &g->featuresRest, &g->opacities};
+    float *dst[6] = {means, scales, quats, features_dc, features_rest, opacities};
+    for (int k = 0; k < 6; k++)
+        if (dst[k]) std::memcpy(dst[k], src[k]->p, (size_t)src[k]->numel() * sizeof(float));
+}
+void ref_loaded_free(void *h) { delete static_cast<LoadedGaussians *>(h); }
 
 }  // extern "C"

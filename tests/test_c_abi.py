@@ -121,3 +121,32 @@ def test_dataset_from_arrays_on_host():
     bad.width = 0
     with pytest.raises(RuntimeError):
         A.Dataset.from_arrays([bad], [np.zeros((1, 1, 3), np.uint8)], xyz, rgb)
+
+
+def test_gaussian_files_round_trip(tmp_path):
+    """msplat_write_ply / msplat_read_ply on the host: the finite rows come
+    back bit for bit with the iteration, the dataset-frame mapping inverts to
+    within float rounding, the .splat has 32 bytes per finite Gaussian, and
+    bad arguments return -1."""
+    import numpy as np
+    from msplat_gb300 import api as A, synthetic as S
+    g = S.gaussians(300, 2)
+    arrs = [g.means, g.scales, g.quats, g.features_dc, g.features_rest, g.opacities[:, 0].copy()]
+    arrs[0][4, 2] = np.nan
+    A.write_ply(str(tmp_path / "a.ply"), arrs, step=1234)
+    got, step = A.read_ply(str(tmp_path / "a.ply"))
+    keep = np.ones(300, bool)
+    keep[4] = False
+    assert step == 1234 and got[0].shape[0] == 299
+    for a, b in zip(got, arrs):
+        assert np.array_equal(a, b[keep])
+    crs = dict(keep_crs=True, scale=0.5, translation=(1.0, 2.0, 3.0))
+    A.write_ply(str(tmp_path / "b.ply"), arrs, **crs)
+    back, _ = A.read_ply(str(tmp_path / "b.ply"), **crs)
+    np.testing.assert_allclose(back[0], arrs[0][keep], atol=1e-5)
+    np.testing.assert_allclose(back[1], arrs[1][keep], atol=1e-5)
+    A.write_splat(str(tmp_path / "c.splat"), arrs)
+    assert (tmp_path / "c.splat").stat().st_size == 32 * 299
+    L = A._lib()
+    assert L.msplat_write_ply(None, 0, 15, None, None, None, None, None, None, 0, 0, 1.0, None) == -1
+    assert L.msplat_ply_info(str(tmp_path / "missing.ply").encode(), None, None, None) == -2

@@ -630,3 +630,48 @@ def test_live_colmap_loader(ref_lib, tmp_path, seed, ply_points):
     assert L.msplat_dataset_points(ds.h, pts.ctypes.data_as(C.POINTER(C.c_float)),
                                    cols.ctypes.data_as(C.POINTER(C.c_uint8))) == len(xyz)
     assert np.array_equal(pts, xyz) and np.array_equal(cols, rgb)
+
+
+# ---- Gaussian PLY / .splat files (loaders/save_gaussians.cpp:8-231) ----
+
+def file_gaussians(n, seed):
+    """n Gaussians with extreme values and a few non-finite rows (which the
+    writers drop), in the layouts of the C API."""
+    rng = np.random.default_rng(seed)
+    g = S.gaussians(n, seed)
+    arrs = [g.means * np.float32(3.0), g.scales, g.quats, g.features_dc, g.features_rest, g.opacities[:, 0].copy()]
+    arrs[1][::17] = rng.uniform(-12, 3, (len(arrs[1][::17]), 3)).astype(np.float32)
+    arrs[5][::13] = rng.normal(0, 8, len(arrs[5][::13])).astype(np.float32)
+    arrs[2][5] = 0.0
+    arrs[0][7, 1] = np.nan
+    arrs[4][11, 3, 2] = np.inf
+    arrs[5][19] = -np.inf
+    arrs[3][23, 0] = np.nan
+    return [np.ascontiguousarray(a, np.float32) for a in arrs]
+
+
+@needs_reference
+@pytest.mark.parametrize("keep_crs", [False, True])
+def test_live_gaussian_files(ref_lib, tmp_path, keep_crs):
+    """The library's PLY and .splat writers (msplat_write_ply /
+    msplat_write_splat, the trainer's export code) against the reference's
+    saveGaussianPly / saveGaussianSplat: byte-identical files, non-finite
+    Gaussians dropped, with and without the dataset-frame mapping; and its
+    PLY reader (msplat_read_ply) against loadGaussianPly: identical arrays
+    and iteration."""
+    from msplat_gb300 import api as A
+    arrs = file_gaussians(500, 4)
+    crs = dict(keep_crs=keep_crs, scale=0.37, translation=(1.5, -2.25, 0.125)) if keep_crs else {}
+    for splat in (False, True):
+        mine, ref = tmp_path / f"mine{int(splat)}", tmp_path / f"ref{int(splat)}"
+        if splat:
+            A.write_splat(str(mine), arrs, **crs)
+        else:
+            A.write_ply(str(mine), arrs, step=7000, **crs)
+        ref_lib.save_gaussians(ref, arrs, splat=splat, step=7000, **crs)
+        assert mine.read_bytes() == ref.read_bytes()
+    got, step = A.read_ply(str(tmp_path / "ref0"), **crs)
+    want, step_r = ref_lib.load_gaussians(tmp_path / "ref0", **crs)
+    assert step == step_r == 7000 and got[0].shape[0] == 496
+    for a, b in zip(got, want):
+        assert a.tobytes() == b.tobytes()
