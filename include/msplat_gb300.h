@@ -171,6 +171,22 @@ int msplat_image_read(const char *path, float *rgb, int *width, int *height);
  * stderr).  msplat_trainer_load_checkpoint applies the same checks. */
 int msplat_checkpoint_info(const char *path, int *num_points, int *sh_degree, int *iteration);
 
+/* Writes and reads a checkpoint (Model::saveCheckpoint / loadCheckpoint,
+ * core/src/model.cpp:698-843) from host arrays, with the trainer's own code:
+ * params, exp_avg and exp_avg_sq each point at the six groups (means [n,3],
+ * log-scales [n,3], quaternions [n,4], features_dc [n,3], features_rest
+ * [n,(sh_degree+1)^2-1,3], opacity logits [n]); adam_lr holds the six
+ * groups' learning rates.  msplat_read_checkpoint fills arrays of the sizes
+ * msplat_checkpoint_info gives (any output may be NULL) after the same
+ * validation.  Return 0, -1 for invalid arguments, -2 when the file cannot
+ * be written or is missing or malformed (reason on stderr). */
+int msplat_write_checkpoint(const char *path, int iteration, int n, int sh_degree, int adam_steps,
+                            const float adam_lr[6], float means_lr_init, float means_lr_final,
+                            const float *const params[6], const float *const exp_avg[6],
+                            const float *const exp_avg_sq[6]);
+int msplat_read_checkpoint(const char *path, float adam_lr[6], float means_lr[2], int *adam_steps,
+                           float *const params[6], float *const exp_avg[6], float *const exp_avg_sq[6]);
+
 /* Host-side PLY and .splat files of Gaussians held by the caller (host
  * arrays in the reference layouts, n rows: means [n,3], log-scales [n,3],
  * quaternions [n,4], features_dc [n,3], features_rest [n,rest_bases,3],

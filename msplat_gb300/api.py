@@ -93,6 +93,11 @@ def _lib():
     L.msplat_write_splat.argtypes = [cp] + hg + [C.c_int, C.c_float, fp]
     L.msplat_ply_info.argtypes = [cp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.msplat_read_ply.argtypes = [cp, C.c_int, C.c_float, fp, fp, fp, fp, fp, fp, fp]
+    fpp = C.POINTER(fp)
+    L.msplat_write_checkpoint.argtypes = [cp, C.c_int, C.c_int, C.c_int, C.c_int, fp, C.c_float, C.c_float,
+                                          fpp, fpp, fpp]
+    L.msplat_read_checkpoint.argtypes = [cp, fp, fp, C.POINTER(C.c_int), fpp, fpp, fpp]
+    L.msplat_checkpoint_info.argtypes = [cp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.msplat_viewer_create.argtypes = [cp, C.c_int, C.c_int, C.c_float]
     L.msplat_viewer_create.restype = vp
     L.msplat_viewer_render.argtypes = [vp, fp, C.POINTER(C.c_uint8)]
@@ -468,6 +473,38 @@ def read_ply(path: str, keep_crs: bool = False, scale: float = 1.0, translation=
     if L.msplat_read_ply(path.encode(), int(keep_crs), float(scale), _fp(t), *[_fp(a) for a in arrs]) != 0:
         raise RuntimeError(f"could not read {path}")
     return arrs, step.value
+
+
+def write_checkpoint(path: str, iteration: int, params, exp_avg, exp_avg_sq, adam_steps: int, adam_lr,
+                     means_lr=(0.00016, 0.0000016), sh_degree: int = 3) -> None:
+    """Writes a checkpoint (the trainer's format and code) of a model held on
+    the host: six groups each of parameters and Adam moments (the arrays
+    get_gaussians returns), the six learning rates and the Adam step."""
+    grps = [[np.ascontiguousarray(a, np.float32) for a in g] for g in (params, exp_avg, exp_avg_sq)]
+    ptrs = [(C.POINTER(C.c_float) * 6)(*[_fp(a) for a in g]) for g in grps]
+    lr = np.asarray(adam_lr, np.float32)
+    if _lib().msplat_write_checkpoint(path.encode(), int(iteration), grps[0][0].shape[0], int(sh_degree),
+                                      int(adam_steps), _fp(lr), float(means_lr[0]), float(means_lr[1]),
+                                      *ptrs) != 0:
+        raise RuntimeError(f"could not write {path}")
+
+
+def read_checkpoint(path: str):
+    """A checkpoint read and validated as the trainer loads it: (iteration,
+    Adam step, learning rates [8] (six groups, means init, means final),
+    params [6], exp_avg [6], exp_avg_sq [6])."""
+    L = _lib()
+    n, deg, it = C.c_int(), C.c_int(), C.c_int()
+    if L.msplat_checkpoint_info(path.encode(), C.byref(n), C.byref(deg), C.byref(it)) != 0:
+        raise RuntimeError(f"could not read {path}")
+    n, rest = n.value, (deg.value + 1) ** 2 - 1
+    shapes = [(n, 3), (n, 3), (n, 4), (n, 3), (n, rest, 3), (n,)]
+    grps = [[np.zeros(s, np.float32) for s in shapes] for _ in range(3)]
+    lr, mlr, steps = np.zeros(6, np.float32), np.zeros(2, np.float32), C.c_int()
+    ptrs = [(C.POINTER(C.c_float) * 6)(*[_fp(a) for a in g]) for g in grps]
+    if L.msplat_read_checkpoint(path.encode(), _fp(lr), _fp(mlr), C.byref(steps), *ptrs) != 0:
+        raise RuntimeError(f"could not read {path}")
+    return it.value, steps.value, np.concatenate([lr, mlr]), grps[0], grps[1], grps[2]
 
 
 def sync():

@@ -306,6 +306,44 @@ static CheckpointData read_checkpoint(const std::string &path) {
     return ck;
 }
 
+// Writes a checkpoint in the same format: the header, then the 18 tensors
+// with the reference's shapes (means, scales [N,3], quats [N,4],
+// features_dc [N,3], features_rest [N,rest,3], opacities [N,1]; each
+// moment as its parameter).  ck.t[k] holds N rows of its group's width.
+static void write_checkpoint(const std::string &path, const CheckpointData &ck) {
+    const int rest = (int)((ck.deg + 1) * (ck.deg + 1)) - 1;
+    const int width[6] = {3, 3, 4, 3, 3 * rest, 1};
+    for (int k = 0; k < 18; k++)
+        if (ck.t[k].size() != (size_t)ck.n * width[k % 6])
+            throw std::runtime_error("checkpoint tensor " + std::to_string(k) + " has the wrong size");
+    std::ofstream f(path, std::ios::binary);
+    if (!f) throw std::runtime_error("cannot write checkpoint " + path);
+    auto u32 = [&](uint32_t v) { f.write(reinterpret_cast<const char *>(&v), 4); };
+    u32(0x4C50534Du);
+    u32(1);
+    u32(ck.step);
+    u32(ck.n);
+    u32(ck.deg);
+    u32(ck.adam_steps);
+    f.write(reinterpret_cast<const char *>(ck.adam_lr), sizeof(ck.adam_lr));
+    f.write(reinterpret_cast<const char *>(&ck.means_lr_init), 4);
+    f.write(reinterpret_cast<const char *>(&ck.means_lr_final), 4);
+    for (int k = 0; k < 18; k++) {
+        const int g = k % 6;
+        const int64_t n = ck.n;
+        std::vector<int64_t> shape;
+        if (g == 4) shape = {n, rest, 3};
+        else if (g == 5) shape = {n, 1};
+        else shape = {n, g == 2 ? 4 : 3};
+        u32((uint32_t)shape.size());
+        for (int64_t e : shape) f.write(reinterpret_cast<const char *>(&e), 8);
+        const uint64_t bytes = ck.t[k].size() * 4;
+        f.write(reinterpret_cast<const char *>(&bytes), 8);
+        f.write(reinterpret_cast<const char *>(ck.t[k].data()), (std::streamsize)bytes);
+    }
+    if (!f) throw std::runtime_error("cannot write checkpoint " + path);
+}
+
 // Reference-layout host copy of a model (means [N,3] ... opacities [N]).
 struct HostGaussians {
     int n = 0, rest = 15;
@@ -866,39 +904,27 @@ struct TrainerImpl {
     // then 6 first and 6 second moments as (ndim, shape, bytes, data)
     void save_checkpoint(const std::string &path) {
         CKA(cudaDeviceSynchronize());
-        std::ofstream f(path, std::ios::binary);
-        if (!f) throw std::runtime_error("cannot write checkpoint " + path);
-        auto u32 = [&](uint32_t v) { f.write(reinterpret_cast<const char *>(&v), 4); };
-        u32(0x4C50534Du);
-        u32(1);
-        u32((uint32_t)current_step);
         // the degree recorded is the one the stored rest bases belong to
         int deg = 0;
         while (deg < 3 && (deg + 1) * (deg + 1) - 1 < model.rest) deg++;
         if ((deg + 1) * (deg + 1) - 1 != model.rest)
             throw std::runtime_error("cannot save a checkpoint of " + std::to_string(model.rest) +
                                      " rest SH bases (not those of degree 0-3)");
-        u32((uint32_t)model.n);
-        u32((uint32_t)deg);
-        u32((uint32_t)adam_step_count);
-        f.write(reinterpret_cast<const char *>(adam_lr), sizeof(adam_lr));
-        f.write(reinterpret_cast<const char *>(&means_lr_init), 4);
-        f.write(reinterpret_cast<const char *>(&means_lr_final), 4);
-        auto tensor = [&](float *const *arr, int g) {
-            std::vector<int64_t> shape;
-            if (g == 4) shape = {model.n, model.rest, 3};
-            else if (g == 5) shape = {model.n, 1};
-            else shape = {model.n, g == 2 ? 4 : 3};
-            u32((uint32_t)shape.size());
-            for (auto s : shape) f.write(reinterpret_cast<const char *>(&s), 8);
-            auto data = model.read(arr, g);
-            const uint64_t bytes = data.size() * 4;
-            f.write(reinterpret_cast<const char *>(&bytes), 8);
-            f.write(reinterpret_cast<const char *>(data.data()), bytes);
-        };
-        for (int g = 0; g < 6; g++) tensor(model.p, g);
-        for (int g = 0; g < 6; g++) tensor(model.m, g);
-        for (int g = 0; g < 6; g++) tensor(model.v, g);
+        CheckpointData ck;
+        ck.step = (uint32_t)current_step;
+        ck.n = (uint32_t)model.n;
+        ck.deg = (uint32_t)deg;
+        ck.adam_steps = (uint32_t)adam_step_count;
+        std::memcpy(ck.adam_lr, adam_lr, sizeof(ck.adam_lr));
+        ck.means_lr_init = means_lr_init;
+        ck.means_lr_final = means_lr_final;
+        ck.rest = model.rest;
+        for (int g = 0; g < 6; g++) {
+            ck.t[g] = model.read(model.p, g);
+            ck.t[6 + g] = model.read(model.m, g);
+            ck.t[12 + g] = model.read(model.v, g);
+        }
+        write_checkpoint(path, ck);
     }
 
     // Model::loadPly (model.cpp:683-694): trained Gaussians, fresh optimizer
@@ -1187,6 +1213,52 @@ int msplat_checkpoint_info(const char *path, int *num_points, int *sh_degree, in
         if (iteration) *iteration = (int)ck.step;
         return 0;
     }, -1);
+}
+int msplat_write_checkpoint(const char *path, int iteration, int n, int sh_degree, int adam_steps,
+                            const float adam_lr[6], float means_lr_init, float means_lr_final,
+                            const float *const params[6], const float *const exp_avg[6],
+                            const float *const exp_avg_sq[6]) {
+    if (!path || n < 0 || sh_degree < 0 || sh_degree > 3 || iteration < 0 || adam_steps < 0 || !adam_lr ||
+        !params || !exp_avg || !exp_avg_sq)
+        return -1;
+    const int rest = (sh_degree + 1) * (sh_degree + 1) - 1;
+    const int width[6] = {3, 3, 4, 3, 3 * rest, 1};
+    const float *const *src[3] = {params, exp_avg, exp_avg_sq};
+    for (int k = 0; k < 18; k++)
+        if (n > 0 && width[k % 6] > 0 && !src[k / 6][k % 6]) return -1;
+    return guard("write_checkpoint", [&]() {
+        CheckpointData ck;
+        ck.step = (uint32_t)iteration;
+        ck.n = (uint32_t)n;
+        ck.deg = (uint32_t)sh_degree;
+        ck.adam_steps = (uint32_t)adam_steps;
+        std::memcpy(ck.adam_lr, adam_lr, sizeof(ck.adam_lr));
+        ck.means_lr_init = means_lr_init;
+        ck.means_lr_final = means_lr_final;
+        ck.rest = rest;
+        for (int k = 0; k < 18; k++) {
+            const float *a = src[k / 6][k % 6];
+            const size_t cnt = (size_t)n * width[k % 6];
+            if (cnt) ck.t[k].assign(a, a + cnt);
+        }
+        write_checkpoint(path, ck);
+        return 0;
+    }, -2);
+}
+int msplat_read_checkpoint(const char *path, float adam_lr[6], float means_lr[2], int *adam_steps,
+                           float *const params[6], float *const exp_avg[6], float *const exp_avg_sq[6]) {
+    if (!path) return -1;
+    return guard("read_checkpoint", [&]() {
+        const CheckpointData ck = read_checkpoint(path);
+        if (adam_lr) std::memcpy(adam_lr, ck.adam_lr, sizeof(ck.adam_lr));
+        if (means_lr) { means_lr[0] = ck.means_lr_init; means_lr[1] = ck.means_lr_final; }
+        if (adam_steps) *adam_steps = (int)ck.adam_steps;
+        float *const *dst[3] = {params, exp_avg, exp_avg_sq};
+        for (int k = 0; k < 18; k++)
+            if (dst[k / 6] && dst[k / 6][k % 6] && !ck.t[k].empty())
+                std::memcpy(dst[k / 6][k % 6], ck.t[k].data(), ck.t[k].size() * sizeof(float));
+        return 0;
+    }, -2);
 }
 static bool host_gaussians_args(int n, int rest_bases, const float *means, const float *scales, const float *quats,
                                 const float *features_dc, const float *features_rest, const float *opacities) {

@@ -3,8 +3,8 @@
 // 19-65), the loader and Gaussian-file declarations (core/include/
 // loaders.hpp) and MTensor,
 // with only the members the host code compiled by ref_model.cpp uses (the
-// MCMC pass, camera setup, evaluation metrics, the COLMAP loader, the
-// Gaussian PLY / .splat files), so that
+// MCMC pass, camera setup, evaluation metrics, checkpoints, the COLMAP
+// loader, the Gaussian PLY / .splat files), so that
 // code compiles unchanged — TEST INFRASTRUCTURE ONLY (it pins the oracle's
 // and the library's restatements; nothing in the product uses it).
 //
@@ -43,34 +43,41 @@
 struct HostTensor {
     float *p = nullptr;
     int64_t row = 1;
-    std::vector<int64_t> shape;                  // for size(d) and numel()
+    std::vector<int64_t> dims;                   // for size(d), numel() and shape()
     std::shared_ptr<std::vector<float>> owned;   // storage of gpu_empty tensors
     template <class T> T *data() { return reinterpret_cast<T *>(p); }
     template <class T> const T *data() const { return reinterpret_cast<const T *>(p); }
     int64_t stride0() const { return row; }
-    int64_t size(int d) const { return shape[d < 0 ? (int)shape.size() + d : d]; }
+    int64_t size(int d) const { return dims[d < 0 ? (int)dims.size() + d : d]; }
     int64_t numel() const {
         int64_t n = 1;
-        for (int64_t s : shape) n *= s;
+        for (int64_t s : dims) n *= s;
         return n;
     }
+    std::vector<int64_t> shape() const { return dims; }
     bool defined() const { return p != nullptr; }
     void *data_ptr() { return p; }
+    const void *data_ptr() const { return p; }
+    uint32_t ndim() const { return (uint32_t)dims.size(); }
+    uint64_t nbytes() const { return (uint64_t)numel() * sizeof(float); }
 };
 using MTensor = HostTensor;
 
 enum class DType { Float32 };
 inline HostTensor gpu_empty(const std::vector<int64_t> &shape, DType) {
     HostTensor t;
-    t.shape = shape;
+    t.dims = shape;
     t.owned = std::make_shared<std::vector<float>>((size_t)t.numel());
     t.p = t.owned->data();
-    t.row = t.shape.size() > 1 ? t.numel() / t.shape[0] : 1;
+    t.row = t.dims.size() > 1 ? t.numel() / t.dims[0] : 1;
     return t;
 }
 inline HostTensor gpu_empty(std::initializer_list<int64_t> shape, DType d) {
     return gpu_empty(std::vector<int64_t>(shape), d);
 }
+inline HostTensor gpu_zeros(const std::vector<int64_t> &shape, DType d) { return gpu_empty(shape, d); }
+
+namespace fs = std::filesystem;
 
 struct Camera {
     int width = 0, height = 0;
@@ -141,6 +148,13 @@ public:
     float cull_radius = 0.0f;
     int shDegree = 3;
     int shDegreeInterval = 1000;
+    float adam_lr[N_ADAM_GROUPS] = {};
+    float means_lr_init = 0.f, means_lr_final = 0.f;
+    int adam_step_count = 0;
+    int buf_capacity = 0;
+    HostTensor sgld_noise_buf;
+    void saveCheckpoint(const std::string &filename, int step);
+    int loadCheckpoint(const std::string &filename);
 
     struct CamSetup {
         float fx, fy, cx, cy;

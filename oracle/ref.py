@@ -309,3 +309,38 @@ def load_gaussians(path, keep_crs=False, scale=1.0, translation=(0.0, 0.0, 0.0))
         return arrs, step
     finally:
         L.ref_loaded_free(h)
+
+
+def save_checkpoint(path, step, params, exp_avg, exp_avg_sq, adam_steps, adam_lr, means_lr=(0.00016, 0.0000016),
+                    sh_degree=3):
+    """The reference's Model::saveCheckpoint (model.cpp:725-764, compiled
+    unchanged) of a model in host arrays (six groups each of parameters and
+    Adam moments in the C API's layouts)."""
+    L = lib()
+    n = int(np.asarray(params[0]).shape[0])
+    keep = [[np.ascontiguousarray(a, np.float32) for a in grp] for grp in (params, exp_avg, exp_avg_sq)]
+    ptrs = [(FP * 6)(*[_p(a) for a in grp]) for grp in keep]
+    lr = np.asarray(adam_lr, np.float32)
+    L.ref_save_checkpoint(str(path).encode(), int(step), n, int(sh_degree), int(adam_steps), _p(lr),
+                          C.c_float(means_lr[0]), C.c_float(means_lr[1]), *ptrs)
+
+
+def load_checkpoint(path):
+    """The reference's Model::loadCheckpoint (model.cpp:766-843): (step, Adam
+    step, learning rates [8], params [6], exp_avg [6], exp_avg_sq [6])."""
+    L = lib()
+    L.ref_load_checkpoint.restype = C.c_void_p
+    h = L.ref_load_checkpoint(str(path).encode())
+    if not h:
+        raise RuntimeError(f"the reference's loader rejected {path}")
+    h = C.c_void_p(h)
+    try:
+        ints, lr = np.zeros(4, np.int32), np.zeros(8, np.float32)
+        L.ref_checkpoint_state(h, _p(ints, IP), _p(lr))
+        step, n, adam_steps, rest = (int(v) for v in ints)
+        shapes = [(n, 3), (n, 3), (n, 4), (n, 3), (n, rest, 3), (n,)]
+        grps = [[np.zeros(s, np.float32) for s in shapes] for _ in range(3)]
+        L.ref_checkpoint_arrays(h, *[(FP * 6)(*[_p(a) for a in g]) for g in grps])
+        return step, adam_steps, lr, grps[0], grps[1], grps[2]
+    finally:
+        L.ref_checkpoint_free(h)

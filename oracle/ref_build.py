@@ -43,8 +43,9 @@ The host code on the path is copied the same way and compiled by
 ref_model.cpp against model_shim.h (host stand-ins for the Model, Camera,
 InputData and MTensor types with the members that code uses): from
 core/src/model.cpp the MCMC pass (computeRelocation, relocate,
-addNewGaussians, mcmcAfterTrain: lines 311-660), the camera setup
-(prepareCam, getDownscaleFactor) and the psnr / l1_loss metrics; from
+addNewGaussians, mcmcAfterTrain: lines 311-660), the checkpoint save and
+load (696-843), the camera setup (prepareCam, getDownscaleFactor) and the
+psnr / l1_loss metrics; from
 core/src/ssim.cpp ssim_eval and its blur; the COLMAP binary loader
 (loaders/load_colmap.cpp), the point-cloud readers (loaders/load_ply.cpp),
 autoScaleAndCenter (input_data.cpp) and the Gaussian PLY / .splat writers
@@ -76,6 +77,7 @@ HOST_RANGES = [
     (MODEL, 33, 49, "// Metrics on CPU MTensor data", "}"),                      # psnr, l1_loss
     (MODEL, 276, 282, "int Model::getDownscaleFactor(int step) {", "}"),
     (MODEL, 311, 660, "void Model::computeRelocation(float opacity_old_sig, float* scale_old_exp, int N,", "}"),
+    (MODEL, 696, 843, "// ── Checkpoint save/load", "}"),             # saveCheckpoint, loadCheckpoint
     (MODEL, 845, 889, "Model::CamSetup Model::prepareCam(Camera& cam, int step) {", "}"),
     (SSIM, 26, 123, "// Separable Gaussian blur on a single-channel (H, W) image.", "}"),  # gaussianBlur, ssim_eval
     (COLMAP, 7, 165, "namespace fs = std::filesystem;", "}"),               # the COLMAP binary loader

@@ -20,7 +20,7 @@ namespace {
 HostTensor host_image(const float *img, int h, int w) {
     HostTensor t;
     t.p = const_cast<float *>(img);
-    t.shape = {h, w, 3};
+    t.dims = {h, w, 3};
     t.row = (int64_t)w * 3;
     return t;
 }
@@ -73,7 +73,7 @@ void ref_prepare_cam(const float c2w[16], int width, int height, float fx, float
     Model m;
     m.shDegree = sh_degree;
     m.shDegreeInterval = sh_interval;
-    m.featuresRest.shape = {1, rest_bases, 3};
+    m.featuresRest.dims = {1, rest_bases, 3};
     Camera cam;
     cam.width = width;
     cam.height = height;
@@ -147,7 +147,7 @@ namespace {
 HostTensor host_rows(const float *a, int64_t n, std::vector<int64_t> shape) {
     HostTensor t;
     t.p = const_cast<float *>(a);
-    t.shape = std::move(shape);
+    t.dims = std::move(shape);
     t.row = n ? t.numel() / n : 1;
     return t;
 }
@@ -194,5 +194,82 @@ void ref_loaded_arrays(void *h, float *means, float *scales, float *quats, float
         if (dst[k]) std::memcpy(dst[k], src[k]->p, (size_t)src[k]->numel() * sizeof(float));
 }
 void ref_loaded_free(void *h) { delete static_cast<LoadedGaussians *>(h); }
+
+namespace {
+struct LoadedCheckpoint {
+    Model m;
+    int step = 0;
+};
+const int kCkptWidth[6] = {3, 3, 4, 3, 0, 1};   // group 4: 3 x rest bases
+std::vector<int64_t> ckpt_shape(int g, int64_t n, int rest) {
+    if (g == 4) return {n, rest, 3};
+    if (g == 5) return {n, 1};
+    return {n, kCkptWidth[g]};
+}
+}  // namespace
+
+// Model::saveCheckpoint (model.cpp:725-764) of a model held in host arrays:
+// n Gaussians at SH degree sh_degree, the six groups' parameters and Adam
+// moments (layouts of the C API), learning rates and the Adam step.
+void ref_save_checkpoint(const char *path, int step, int n, int sh_degree, int adam_steps, const float adam_lr[6],
+                         float means_lr_init, float means_lr_final, const float *const params[6],
+                         const float *const exp_avg[6], const float *const exp_avg_sq[6]) {
+    Model m;
+    const int rest = (sh_degree + 1) * (sh_degree + 1) - 1;
+    m.shDegree = sh_degree;
+    m.num_active = n;
+    m.adam_step_count = adam_steps;
+    for (int g = 0; g < 6; g++) m.adam_lr[g] = adam_lr[g];
+    m.means_lr_init = means_lr_init;
+    m.means_lr_final = means_lr_final;
+    HostTensor *views[6] = {&m.means, &m.scales, &m.quats, &m.featuresDc, &m.featuresRest, &m.opacities};
+    for (int g = 0; g < 6; g++) {
+        *views[g] = host_rows(params[g], n, ckpt_shape(g, n, rest));
+        m.adam_exp_avg[g] = host_rows(exp_avg[g], n, ckpt_shape(g, n, rest));
+        m.adam_exp_avg_sq[g] = host_rows(exp_avg_sq[g], n, ckpt_shape(g, n, rest));
+    }
+    m.saveCheckpoint(path, step);
+}
+
+// Model::loadCheckpoint (model.cpp:766-843): a handle (NULL when it threw)
+// whose ref_checkpoint_state gives (step, rows, Adam step, rest bases) and
+// the eight learning rates, and ref_checkpoint_arrays the tensors.
+void *ref_load_checkpoint(const char *path) {
+    uint32_t head[4] = {0, 0, 0, 0};   // magic, version, step, rows: the rows size the model's buffers
+    {
+        std::ifstream f(path, std::ios::binary);
+        f.read(reinterpret_cast<char *>(head), sizeof(head));
+    }
+    auto *c = new LoadedCheckpoint;
+    c->m.cap_max = (int)head[3];
+    try {
+        c->step = c->m.loadCheckpoint(path);
+        return c;
+    } catch (const std::exception &) {
+        delete c;
+        return nullptr;
+    }
+}
+void ref_checkpoint_state(void *h, int ints[4], float lr[8]) {
+    const LoadedCheckpoint *c = static_cast<LoadedCheckpoint *>(h);
+    const Model *m = &c->m;
+    ints[0] = c->step;
+    ints[1] = m->num_active;
+    ints[2] = m->adam_step_count;
+    ints[3] = (int)m->featuresRest.size(1);
+    for (int g = 0; g < 6; g++) lr[g] = m->adam_lr[g];
+    lr[6] = m->means_lr_init;
+    lr[7] = m->means_lr_final;
+}
+void ref_checkpoint_arrays(void *h, float *const params[6], float *const exp_avg[6], float *const exp_avg_sq[6]) {
+    Model *m = &static_cast<LoadedCheckpoint *>(h)->m;
+    HostTensor *views[6] = {&m->means, &m->scales, &m->quats, &m->featuresDc, &m->featuresRest, &m->opacities};
+    for (int g = 0; g < 6; g++) {
+        std::memcpy(params[g], views[g]->p, views[g]->nbytes());
+        std::memcpy(exp_avg[g], m->adam_exp_avg[g].p, m->adam_exp_avg[g].nbytes());
+        std::memcpy(exp_avg_sq[g], m->adam_exp_avg_sq[g].p, m->adam_exp_avg_sq[g].nbytes());
+    }
+}
+void ref_checkpoint_free(void *h) { delete static_cast<LoadedCheckpoint *>(h); }
 
 }  // extern "C"

@@ -675,3 +675,33 @@ def test_live_gaussian_files(ref_lib, tmp_path, keep_crs):
     assert step == step_r == 7000 and got[0].shape[0] == 496
     for a, b in zip(got, want):
         assert a.tobytes() == b.tobytes()
+
+
+@needs_reference
+def test_live_checkpoint_files(ref_lib, tmp_path):
+    """The library's checkpoint writer (msplat_write_checkpoint, the
+    trainer's save code) against the reference's Model::saveCheckpoint:
+    byte-identical files; and each side's reader on the other's file
+    (msplat_read_checkpoint with its validation, Model::loadCheckpoint):
+    the same iteration, Adam step, learning rates, parameters and moments."""
+    from msplat_gb300 import api as A
+    rng = np.random.default_rng(8)
+    n = 257
+    params = file_gaussians(n, 8)
+    params[0][7, 1] = 1.0          # a checkpoint keeps every Gaussian, finite or not; keep these finite
+    params[4][11, 3, 2] = 0.5
+    params[5][19] = -3.0
+    params[3][23, 0] = 0.25
+    ea = [np.abs(rng.normal(0, 1e-3, a.shape)).astype(np.float32) for a in params]
+    eas = [np.abs(rng.normal(0, 1e-6, a.shape)).astype(np.float32) for a in params]
+    lr = np.array([1.3e-4, 5e-3, 1e-3, 2.5e-3, 1.25e-4, 5e-2], np.float32)
+    mine, ref = tmp_path / "mine.ckpt", tmp_path / "ref.ckpt"
+    A.write_checkpoint(str(mine), 4321, params, ea, eas, 4321, lr)
+    ref_lib.save_checkpoint(ref, 4321, params, ea, eas, 4321, lr)
+    assert mine.read_bytes() == ref.read_bytes()
+    for got in (A.read_checkpoint(str(ref)), ref_lib.load_checkpoint(mine)):
+        it, steps, lrs, p, m1, m2 = got
+        assert (it, steps) == (4321, 4321)
+        assert np.array_equal(lrs, np.concatenate([lr, np.float32([0.00016, 0.0000016])]))
+        for a, b in zip(p + m1 + m2, params + ea + eas):
+            assert a.tobytes() == np.ascontiguousarray(b, np.float32).reshape(a.shape).tobytes()
