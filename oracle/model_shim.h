@@ -3,8 +3,8 @@
 // 19-65), the loader and Gaussian-file declarations (core/include/
 // loaders.hpp) and MTensor,
 // with only the members the host code compiled by ref_model.cpp uses (the
-// MCMC pass, camera setup, evaluation metrics, checkpoints, the COLMAP
-// loader, the Gaussian PLY / .splat files), so that
+// MCMC pass, camera setup, evaluation metrics, checkpoints, the COLMAP,
+// Nerfstudio and Polycam loaders, the Gaussian PLY / .splat files), so that
 // code compiles unchanged — TEST INFRASTRUCTURE ONLY (it pins the oracle's
 // and the library's restatements; nothing in the product uses it).
 //
@@ -16,6 +16,8 @@
 // opacities, ...) are the same arrays, as in the reference after
 // refreshViews().
 #pragma once
+
+#include "json_shim.h"   // nlohmann::json, for the Nerfstudio and Polycam loaders
 
 #include <algorithm>
 #include <cmath>
@@ -106,6 +108,8 @@ struct InputData {
 
 namespace loaders {
 InputData loadColmap(const std::string &projectRoot, const std::string &imageSourcePath = "");
+InputData loadNerfstudio(const std::string &projectRoot);
+InputData loadPolycam(const std::string &projectRoot);
 }
 Points readPly(const std::string &path);
 Points readColmapPoints(const std::string &path);

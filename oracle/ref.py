@@ -244,15 +244,16 @@ def metrics(img, gt):
     return tuple(out)
 
 
-def load_colmap(root):
-    """The reference's loaders::loadColmap (load_colmap.cpp, compiled
-    unchanged) of a COLMAP binary dataset: a list of cameras (dicts with
-    c2w [4,4], intr (fx, fy, cx, cy), size (w, h), dist (k1, k2, k3, p1, p2),
+def load_colmap(root, fmt="colmap"):
+    """The reference's loaders::loadColmap (load_colmap.cpp), or with fmt
+    "nerfstudio" / "polycam" loadNerfstudio / loadPolycam (compiled
+    unchanged) of a dataset directory: a list of cameras (dicts with c2w
+    [4,4], intr (fx, fy, cx, cy), size (w, h), dist (k1, k2, k3, p1, p2),
     name) in its order, the point cloud (xyz, rgb) after its centring and
     scaling, and (scale, translation)."""
     L = lib()
-    L.ref_colmap_load.restype = C.c_void_p
-    h = L.ref_colmap_load(str(root).encode())
+    L.ref_dataset_load.restype = C.c_void_p
+    h = L.ref_dataset_load(str(root).encode(), {"colmap": 0, "nerfstudio": 1, "polycam": 2}[fmt])
     if not h:
         raise RuntimeError(f"the reference's loader rejected {root}")
     h = C.c_void_p(h)

@@ -48,8 +48,10 @@ load (696-843), the camera setup (prepareCam, getDownscaleFactor) and the
 psnr / l1_loss metrics; from
 core/src/ssim.cpp ssim_eval and its blur; the COLMAP binary loader
 (loaders/load_colmap.cpp), the point-cloud readers (loaders/load_ply.cpp),
-autoScaleAndCenter (input_data.cpp) and the Gaussian PLY / .splat writers
-and PLY reader (loaders/save_gaussians.cpp).
+autoScaleAndCenter (input_data.cpp), the Nerfstudio and Polycam loaders
+(loaders/load_nerfstudio.cpp, load_polycam.cpp, whose nlohmann::json calls
+json_shim.h answers) and the Gaussian PLY / .splat writers and PLY reader
+(loaders/save_gaussians.cpp).
 
 Usage: python oracle/ref_build.py [--reference DIR]   (default: /root/reference)
 """
@@ -71,6 +73,8 @@ COLMAP = os.path.join("core", "src", "loaders", "load_colmap.cpp")
 PLY = os.path.join("core", "src", "loaders", "load_ply.cpp")
 INPUT = os.path.join("core", "src", "input_data.cpp")
 SAVE = os.path.join("core", "src", "loaders", "save_gaussians.cpp")
+NERF = os.path.join("core", "src", "loaders", "load_nerfstudio.cpp")
+POLY = os.path.join("core", "src", "loaders", "load_polycam.cpp")
 # Host code compiled by ref_model.cpp against model_shim.h (host stand-ins
 # for Model, Camera and MTensor): (file, first, last, first-line text, last-line text)
 HOST_RANGES = [
@@ -84,6 +88,8 @@ HOST_RANGES = [
     (PLY, 6, 205, "// Property types in PLY files", "}"),                   # readPly, readColmapPoints
     (INPUT, 115, 169, "void autoScaleAndCenter(InputData &data) {", "}"),   # pose centring and scaling
     (SAVE, 8, 231, "static const double C0 = 0.28209479177387814;", "}"),  # Gaussian PLY / .splat files
+    (NERF, 7, 72, "namespace fs = std::filesystem;", "}"),                  # the Nerfstudio loader
+    (POLY, 7, 95, "namespace fs = std::filesystem;", "}"),                  # the Polycam loader
 ]
 
 # (first line, last line, text of the first line, text of the last line), 1-based, inclusive

@@ -4,7 +4,8 @@
 // mcmcAfterTrain: 311-660), the camera setup (prepareCam: 845-889,
 // getDownscaleFactor: 276-282) and the psnr / l1_loss metrics (33-49); from
 // core/src/ssim.cpp ssim_eval (26-123); the COLMAP binary loader
-// (loaders/load_colmap.cpp:7-165) with the point readers
+// (loaders/load_colmap.cpp:7-165), the Nerfstudio and Polycam loaders
+// (load_nerfstudio.cpp:7-72, load_polycam.cpp:7-95) with the point readers
 // (loaders/load_ply.cpp:6-205) and autoScaleAndCenter (input_data.cpp:
 // 115-169); the Gaussian PLY / .splat files (loaders/save_gaussians.cpp:
 // 8-231).  The code is copied into
@@ -106,12 +107,15 @@ float ref_ssim_eval(const float *img, const float *gt, int h, int w) {
     return ssim_eval(host_image(img, h, w), host_image(gt, h, w), 11, 1.5f);
 }
 
-// loaders::loadColmap (load_colmap.cpp:122-165) of a dataset directory:
-// its cameras in the reference's order with their poses after
-// autoScaleAndCenter, and the point cloud.  Returns a handle, or NULL when
-// the loader threw.
-void *ref_colmap_load(const char *root) {
+// loaders::loadColmap (load_colmap.cpp:122-165), loadNerfstudio
+// (load_nerfstudio.cpp:18-72) or loadPolycam (load_polycam.cpp:18-95) of a
+// dataset directory (format 0, 1, 2): its cameras in the reference's order
+// with their poses after autoScaleAndCenter, and the point cloud.  Returns a
+// handle, or NULL when the loader threw.
+void *ref_dataset_load(const char *root, int format) {
     try {
+        if (format == 1) return new InputData(loaders::loadNerfstudio(root));
+        if (format == 2) return new InputData(loaders::loadPolycam(root));
         return new InputData(loaders::loadColmap(root));
     } catch (const std::exception &) {
         return nullptr;

@@ -705,3 +705,107 @@ def test_live_checkpoint_files(ref_lib, tmp_path):
         assert np.array_equal(lrs, np.concatenate([lr, np.float32([0.00016, 0.0000016])]))
         for a, b in zip(p + m1 + m2, params + ea + eas):
             assert a.tobytes() == np.ascontiguousarray(b, np.float32).reshape(a.shape).tobytes()
+
+
+def _compare_dataset(ref_lib, root, fmt, n):
+    """The reference's loader (fmt) and the library's msplat_dataset_create
+    on one directory: the same n cameras in the same order, identical sizes,
+    intrinsics and camera-to-world poses, the same centred, scaled points."""
+    import ctypes as C
+    from msplat_gb300 import api as A
+    cams, (xyz, rgb), _ = ref_lib.load_colmap(root, fmt)
+    ds = A.Dataset(str(root))
+    L = A._lib()
+    assert ds.num_train == len(cams) == n
+    for i, c in enumerate(cams):
+        intr, size, c2w = np.zeros(4, np.float32), np.zeros(2, np.int32), np.zeros(16, np.float32)
+        img = np.zeros((c["size"][1], c["size"][0], 3), np.uint8)
+        assert L.msplat_dataset_camera(ds.h, i, 0, intr.ctypes.data_as(C.POINTER(C.c_float)),
+                                       size.ctypes.data_as(C.POINTER(C.c_int)),
+                                       c2w.ctypes.data_as(C.POINTER(C.c_float)),
+                                       img.ctypes.data_as(C.POINTER(C.c_uint8))) == 0
+        assert tuple(size) == c["size"], i
+        assert np.array_equal(intr, c["intr"]), (i, intr, c["intr"])
+        assert np.array_equal(c2w, c["c2w"].ravel()), (i, c2w - c["c2w"].ravel())
+    pts, cols = np.zeros_like(xyz), np.zeros_like(rgb)
+    assert L.msplat_dataset_points(ds.h, pts.ctypes.data_as(C.POINTER(C.c_float)),
+                                   cols.ctypes.data_as(C.POINTER(C.c_uint8))) == len(xyz)
+    assert np.array_equal(pts, xyz) and np.array_equal(cols, rgb)
+
+
+def _write_image(path, w, h, rng):
+    from test_dataset_io import write_png
+    img = rng.integers(0, 256, (h, w, 3), dtype=np.uint8)
+    write_png(path, [img[y].tobytes() for y in range(h)], 2, 8)
+
+
+@needs_reference
+def test_live_nerfstudio_loader(ref_lib, tmp_path):
+    """The reference's loadNerfstudio (nlohmann's calls answered by
+    oracle/json_shim.h) against the library's loader on a transforms.json
+    with global intrinsics, per-frame overrides, frames listed unsorted,
+    file paths with and without extensions and long decimal poses."""
+    import json
+    from test_dataset_io import _pose, _write_ply_points
+    rng = np.random.default_rng(5)
+    os.makedirs(tmp_path / "images")
+    frames = []
+    for k in rng.permutation(9):
+        a = rng.uniform(0, 2 * np.pi)
+        eye = (rng.uniform(3, 6) * np.cos(a), rng.uniform(3, 6) * np.sin(a), rng.uniform(-1, 2))
+        fr = {"file_path": f"images/v{k}" + (".png" if k % 2 else ""),
+              "transform_matrix": [[float(v) for v in row] for row in _pose(eye)]}
+        w, h = 32, 24
+        if k % 3 == 0:
+            fr.update({"w": 40, "h": 20, "fl_x": 27.123456789, "fl_y": 21.5, "cx": 20.25, "cy": 10})
+            w, h = 40, 20
+        _write_image(tmp_path / "images" / f"v{k}.png", w, h, rng)
+        frames.append(fr)
+    json.dump({"w": 32, "h": 24, "fl_x": 30.0, "fl_y": 31.7, "cx": 16.0, "cy": 12.0, "frames": frames,
+               "ply_file_path": "points.ply"}, open(tmp_path / "transforms.json", "w"))
+    _write_ply_points(tmp_path / "points.ply", rng.normal(0, 1.3, (80, 3)).astype(np.float32),
+                      rng.integers(0, 256, (80, 3), dtype=np.uint8))
+    _compare_dataset(ref_lib, tmp_path, "nerfstudio", 9)
+
+
+@needs_reference
+@pytest.mark.parametrize("layout", [1, 2])
+def test_live_polycam_loader(ref_lib, tmp_path, layout):
+    """The reference's loadPolycam against the library's loader: layout 1
+    (one JSON per keyframe with R_ij, t_2j and intrinsics, cx/cy defaulted
+    on some) and layout 2 (one cameras.json of frames with 4x4 matrices)."""
+    import json
+    from test_dataset_io import _pose, _write_ply_points
+    rng = np.random.default_rng(6 + layout)
+    poses = []
+    for k in range(7):
+        a = rng.uniform(0, 2 * np.pi)
+        poses.append(_pose((rng.uniform(3, 6) * np.cos(a), rng.uniform(3, 6) * np.sin(a), rng.uniform(-1, 2))))
+    if layout == 1:
+        kd, idir = tmp_path / "keyframes" / "corrected_cameras", tmp_path / "keyframes" / "corrected_images"
+        os.makedirs(kd)
+        os.makedirs(idir)
+        for k, c2w in enumerate(poses):
+            R, t = c2w[:3, :3].copy(), c2w[:3, 3].copy()
+            R[1:] *= -1
+            t[1:] *= -1
+            d = {"width": 32, "height": 24, "fx": 30.0 + k / 7.0, "fy": 29.5}
+            if k % 2:
+                d.update({"cx": 15.75, "cy": 12.5})
+            d.update({"t_20": float(t[0]), "t_21": float(t[1]), "t_22": float(t[2])})
+            d.update({f"R_{a}{b}": float(R[a, b]) for a in range(3) for b in range(3)})
+            json.dump(d, open(kd / f"{k:03d}.json", "w"))
+            _write_image(idir / f"{k:03d}.png", 32, 24, rng)
+        ply = tmp_path / "keyframes" / "point_cloud.ply"
+    else:
+        os.makedirs(tmp_path / "images")
+        frames = []
+        for k, c2w in enumerate(poses):
+            frames.append({"width": 32, "height": 24, "fx": 30.0, "fy": 30.0 + k, "cx": 16.0, "cy": 12.0,
+                           "transform_matrix": [[float(v) for v in row] for row in c2w],
+                           "file_path": f"images/p{k}.png"})
+            _write_image(tmp_path / "images" / f"p{k}.png", 32, 24, rng)
+        json.dump({"frames": frames}, open(tmp_path / "cameras.json", "w"))
+        ply = tmp_path / "point_cloud.ply"
+    _write_ply_points(ply, rng.normal(0, 1.3, (60, 3)).astype(np.float32), rng.integers(0, 256, (60, 3), dtype=np.uint8))
+    _compare_dataset(ref_lib, tmp_path, "polycam", 7)
