@@ -47,6 +47,39 @@ MsplatDataset msplat_dataset_create_from_memory(int num_cameras, const float *ca
                                                const uint8_t *const *masks, int num_points, const float *xyz,
                                                const uint8_t *rgb, bool eval_mode, int test_every, bool normalize);
 
+/* Trainer options the reference's CLI sets on its Model (cli/msplat.mm:
+ * 90-131, 182-195) beyond MsplatConfig: the seed opacity and the seed scale
+ * as a multiple of the mean distance to the 3 nearest seed points
+ * (Model::Model, core/src/model.cpp:80-166), the subsampling of seeds above
+ * 75 % of the cap to 50 % (setupOptimizers, :168-200), the length of the
+ * means learning-rate decay (schedulersStep, :256-261) and the scale of the
+ * opacity/scale regularizer for Gaussians not seen in a step (the step's
+ * mcmc_reg_invis_scale).  msplat_default_trainer_options gives the
+ * reference's defaults: 0.5, 0.1, 1, 30000, 1. */
+typedef struct {
+    float initOpacity;
+    float initScaleMult;
+    int seedDecimation;
+    int positionLrMaxSteps;
+    float regVisibilityDuty;
+} MsplatTrainerOptions;
+void msplat_default_trainer_options(MsplatTrainerOptions *options);
+
+/* msplat_trainer_create with options (NULL: the defaults).  NULL when the
+ * options are out of range (opacity in (0, 1), scale multiplier > 0,
+ * decay length > 0, duty >= 0) or the trainer cannot be created. */
+MsplatTrainer msplat_trainer_create_ex(MsplatDataset ds, MsplatConfig config, const MsplatTrainerOptions *options);
+
+/* The trainer's seed initialisation on the host (Model::Model and
+ * setupOptimizers, model.cpp:80-254): from num_points seed points (xyz
+ * float [n,3], rgb uint8 [n,3]) at SH degree sh_degree and a cap of
+ * cap_max, Gaussians in the layouts of msplat_trainer_set_gaussians written
+ * to arrays of num_points rows; returns the rows in use (after seed
+ * decimation or truncation to the cap), or -1 for invalid arguments. */
+int msplat_seed_gaussians(int num_points, const float *xyz, const uint8_t *rgb, int sh_degree, int cap_max,
+                          const MsplatTrainerOptions *options, float *means, float *scales, float *quats,
+                          float *features_dc, float *features_rest, float *opacities);
+
 /* Replaces the trainer's Gaussians (host arrays in the reference layouts, n
  * rows) and resets the optimizer, as loading a trained PLY does
  * (Model::loadPly, core/src/model.cpp:675-690).  rest_bases in [0, 15];

@@ -18,6 +18,11 @@ class _MsplatConfig(C.Structure):
                 ("downscaleFactor", C.c_float), ("bgColor", C.c_float * 3)]
 
 
+class _TrainerOptions(C.Structure):
+    _fields_ = [("initOpacity", C.c_float), ("initScaleMult", C.c_float), ("seedDecimation", C.c_int),
+                ("positionLrMaxSteps", C.c_int), ("regVisibilityDuty", C.c_float)]
+
+
 class _Stats(C.Structure):
     _fields_ = [("iteration", C.c_int), ("splatCount", C.c_int), ("msPerStep", C.c_float)]
 
@@ -64,6 +69,11 @@ def _lib():
     L.msplat_dataset_camera_pose.argtypes = [vp, C.c_int, fp]
     L.msplat_trainer_create.argtypes = [vp, _MsplatConfig]
     L.msplat_trainer_create.restype = vp
+    L.msplat_trainer_create_ex.argtypes = [vp, _MsplatConfig, C.POINTER(_TrainerOptions)]
+    L.msplat_trainer_create_ex.restype = vp
+    L.msplat_default_trainer_options.argtypes = [C.POINTER(_TrainerOptions)]
+    L.msplat_seed_gaussians.argtypes = [C.c_int, fp, C.POINTER(C.c_uint8), C.c_int, C.c_int,
+                                        C.POINTER(_TrainerOptions), fp, fp, fp, fp, fp, fp]
     L.msplat_trainer_destroy.argtypes = [vp]
     L.msplat_trainer_step.argtypes = [vp]
     L.msplat_trainer_step.restype = _Stats
@@ -245,11 +255,49 @@ def _take(px: _Pixels) -> np.ndarray:
     return out
 
 
+@dataclass
+class TrainerOptions:
+    """Options the reference's CLI sets on its model (seed opacity and scale,
+    seed decimation, the means learning-rate decay length, the regularizer's
+    visibility duty); the defaults are the reference's."""
+    init_opacity: float = 0.5
+    init_scale_mult: float = 0.1
+    seed_decimation: bool = True
+    position_lr_max_steps: int = 30000
+    reg_visibility_duty: float = 1.0
+
+    def native(self) -> _TrainerOptions:
+        return _TrainerOptions(self.init_opacity, self.init_scale_mult, int(self.seed_decimation),
+                               self.position_lr_max_steps, self.reg_visibility_duty)
+
+
+def seed_gaussians(points_xyz, points_rgb, sh_degree: int = 3, cap_max: int = 1_000_000,
+                   options: TrainerOptions | None = None):
+    """The trainer's seed initialisation on the host: Gaussians [means,
+    scales, quats, features_dc, features_rest, opacities] from a point
+    cloud, after seed decimation or truncation to the cap."""
+    xyz = np.ascontiguousarray(points_xyz, np.float32)
+    rgb = np.ascontiguousarray(points_rgb, np.uint8)
+    n = xyz.shape[0]
+    rest = (sh_degree + 1) ** 2 - 1
+    shapes = [(n, 3), (n, 3), (n, 4), (n, 3), (n, rest, 3), (n,)]
+    arrs = [np.zeros(s, np.float32) for s in shapes]
+    opt = (options or TrainerOptions()).native()
+    rows = _lib().msplat_seed_gaussians(n, _fp(xyz), rgb.ctypes.data_as(C.POINTER(C.c_uint8)), int(sh_degree),
+                                        int(cap_max), C.byref(opt), *[_fp(a) for a in arrs])
+    if rows < 0:
+        raise RuntimeError("invalid seed arguments")
+    return [a[:rows] for a in arrs]
+
+
 class GaussianTrainer:
-    def __init__(self, dataset: Dataset, config: TrainingConfig):
+    def __init__(self, dataset: Dataset, config: TrainingConfig, options: TrainerOptions | None = None):
         self.dataset = dataset   # the dataset must outlive the trainer
         self.config = config
-        self.h = _lib().msplat_trainer_create(dataset.h, config.native())
+        if options is None:
+            self.h = _lib().msplat_trainer_create(dataset.h, config.native())
+        else:
+            self.h = _lib().msplat_trainer_create_ex(dataset.h, config.native(), C.byref(options.native()))
         if not self.h:
             raise RuntimeError("could not create trainer")
 

@@ -68,6 +68,14 @@ def parse(argv=None):
     p.add_argument("--colmap-image-path", default="", help="override the COLMAP image directory")
     p.add_argument("--early-stop", type=float, default=0.0,
                    help="stop when test-subset PSNR improves less than this (dB) over 5000 steps (needs --eval)")
+    p.add_argument("--reg-visibility-duty", type=float, default=1.0,
+                   help="scale of the opacity/scale regularizer for Gaussians not seen in a step (1 = full)")
+    p.add_argument("--no-seed-decimation", action="store_true",
+                   help="keep every seed point (no 50%% subsample above 75%% of --cap-max)")
+    p.add_argument("--position-lr-max-steps", type=int, default=30000,
+                   help="steps over which the position learning rate decays")
+    p.add_argument("--init-opacity", type=float, default=0.5, help="seed opacity at init")
+    p.add_argument("--init-scale", type=float, default=0.1, help="seed scale multiplier on the kNN spacing")
     p.add_argument("--log-every", type=int, default=100, help="print progress every N steps")
     p.add_argument("--batch-views", type=int, default=1,
                    help="cameras per optimizer step (mean gradient; iterations count views; 1 = one camera per step)")
@@ -108,7 +116,11 @@ def main(argv=None) -> int:
                            opacity_reg=a.opacity_reg, scale_reg=a.scale_reg, cull_radius=a.cull_radius,
                            keep_crs=a.keep_crs, downscale_factor=a.downscale_factor, bg_color=list(a.bg_color),
                            output=a.output, save_every=a.save_every)
-    trainer = A.GaussianTrainer(ds, cfg)
+    opts = A.TrainerOptions(init_opacity=a.init_opacity, init_scale_mult=a.init_scale,
+                            seed_decimation=not a.no_seed_decimation,
+                            position_lr_max_steps=a.position_lr_max_steps,
+                            reg_visibility_duty=a.reg_visibility_duty)
+    trainer = A.GaussianTrainer(ds, cfg, opts if opts != A.TrainerOptions() else None)
     if a.batch_views > 1:
         trainer.set_batch_views(a.batch_views, a.batch_lr_scale)
     if a.learned_relocation:

@@ -484,8 +484,66 @@ static void write_splat(const std::string &path, const HostGaussians &h, bool ke
 
 static const float kLrInit[6] = {0.00016f, 0.005f, 0.001f, 0.0025f, 0.000125f, 0.05f};   // model.cpp:223
 
+static MsplatTrainerOptions default_trainer_options() { return MsplatTrainerOptions{0.5f, 0.1f, 1, 30000, 1.0f}; }
+static bool trainer_options_valid(const MsplatTrainerOptions &o) {
+    return o.initOpacity > 0.f && o.initOpacity < 1.f && o.initScaleMult > 0.f && o.positionLrMaxSteps > 0 &&
+           o.regVisibilityDuty >= 0.f;
+}
+
+// Model::Model (model.cpp:80-166): KNN scale x initScaleMult, random unit
+// quaternions from mt19937(42), DC from the point colours, rest 0, opacity
+// logit(initOpacity).
+static HostGaussians seed_gaussians(const std::vector<float> &xyz, const std::vector<uint8_t> &rgb, int sh_degree,
+                                    const MsplatTrainerOptions &o) {
+    const int64_t n = (int64_t)xyz.size() / 3;
+    const int rest = sh_bases_for_degree(sh_degree) - 1;
+    HostGaussians h;
+    h.n = (int)n;
+    h.rest = rest;
+    h.a[0] = xyz;
+    auto sc = knn3_mean_distance(xyz);
+    h.a[1].resize(3 * n);
+    for (int64_t i = 0; i < n; i++) h.a[1][3 * i] = h.a[1][3 * i + 1] = h.a[1][3 * i + 2] = std::log(sc[i] * o.initScaleMult);
+    std::mt19937 qr(42);
+    std::uniform_real_distribution<float> u01(0.0f, 1.0f);
+    h.a[2].resize(4 * n);
+    for (int64_t i = 0; i < n; i++) {
+        const float u = u01(qr), v = u01(qr), w = u01(qr);
+        // float radius times a double-precision angle term, rounded once
+        h.a[2][4 * i + 0] = (float)(std::sqrt(1 - u) * std::sin(2 * M_PI * v));
+        h.a[2][4 * i + 1] = (float)(std::sqrt(1 - u) * std::cos(2 * M_PI * v));
+        h.a[2][4 * i + 2] = (float)(std::sqrt(u) * std::sin(2 * M_PI * w));
+        h.a[2][4 * i + 3] = (float)(std::sqrt(u) * std::cos(2 * M_PI * w));
+    }
+    h.a[3].resize(3 * n);
+    for (int64_t i = 0; i < 3 * n; i++) h.a[3][i] = (float)((rgb[i] / 255.0 - 0.5) / kShC0);
+    h.a[4].assign((size_t)3 * rest * n, 0.f);
+    h.a[5].assign(n, std::log(o.initOpacity / (1.0f - o.initOpacity)));
+    return h;
+}
+
+// setupOptimizers (model.cpp:168-200): the rows kept of n at a cap of cap:
+// above 75 % of the cap (with decimation) a sorted random half of the cap
+// (mt19937(42) shuffle), else the first min(n, cap).  Returns the count;
+// keep is empty when the rows are the first ones.
+static int seed_rows(int n, int cap, bool decimate, std::vector<int> &keep) {
+    keep.clear();
+    if (decimate && n > (int)(cap * 0.75)) {
+        const int rows = (int)(cap * 0.5);
+        keep.resize(n);
+        std::iota(keep.begin(), keep.end(), 0);
+        std::mt19937 r(42);
+        std::shuffle(keep.begin(), keep.end(), r);
+        keep.resize(rows);
+        std::sort(keep.begin(), keep.end());
+        return rows;
+    }
+    return std::min(n, cap);
+}
+
 struct TrainerImpl {
     MsplatConfig cfg;
+    MsplatTrainerOptions opt = default_trainer_options();
     DatasetImpl *ds = nullptr;
     MsplatEngine *eng = nullptr;
     DeviceModel model;
@@ -533,7 +591,8 @@ struct TrainerImpl {
         std::mt19937 rng{7};
     } lrn;
 
-    TrainerImpl(DatasetImpl *d, const MsplatConfig &c) : cfg(c), ds(d) {
+    TrainerImpl(DatasetImpl *d, const MsplatConfig &c, const MsplatTrainerOptions &o) : cfg(c), opt(o), ds(d) {
+        position_lr_max_steps = opt.positionLrMaxSteps;
         if (const char *e = std::getenv("MSPLAT_NAN_INJECT")) nan_inject = std::atoi(e);
         int dev = 0;
         CKA(cudaGetDevice(&dev));
@@ -689,47 +748,15 @@ struct TrainerImpl {
     // quaternions from mt19937(42), DC from the point colours, rest 0,
     // opacity 0.5; then setupOptimizers (model.cpp:168-254).
     void init_from_points() {
-        const int64_t n = (int64_t)ds->xyz.size() / 3;
-        const int rest = sh_bases_for_degree(cfg.shDegree) - 1;
-        HostGaussians h;
-        h.n = (int)n;
-        h.rest = rest;
-        h.a[0] = ds->xyz;
-        auto sc = knn3_mean_distance(ds->xyz);
-        h.a[1].resize(3 * n);
-        for (int64_t i = 0; i < n; i++) h.a[1][3 * i] = h.a[1][3 * i + 1] = h.a[1][3 * i + 2] = std::log(sc[i] * 0.1f);
-        std::mt19937 qr(42);
-        std::uniform_real_distribution<float> u01(0.0f, 1.0f);
-        h.a[2].resize(4 * n);
-        for (int64_t i = 0; i < n; i++) {
-            const float u = u01(qr), v = u01(qr), w = u01(qr);
-            // float radius times a double-precision angle term, rounded once
-            h.a[2][4 * i + 0] = (float)(std::sqrt(1 - u) * std::sin(2 * M_PI * v));
-            h.a[2][4 * i + 1] = (float)(std::sqrt(1 - u) * std::cos(2 * M_PI * v));
-            h.a[2][4 * i + 2] = (float)(std::sqrt(u) * std::sin(2 * M_PI * w));
-            h.a[2][4 * i + 3] = (float)(std::sqrt(u) * std::cos(2 * M_PI * w));
-        }
-        h.a[3].resize(3 * n);
-        for (int64_t i = 0; i < 3 * n; i++) h.a[3][i] = (float)((ds->rgb[i] / 255.0 - 0.5) / kShC0);
-        h.a[4].assign((size_t)3 * rest * n, 0.f);
-        h.a[5].assign(n, std::log(0.5f / (1.0f - 0.5f)));
-        set_model(h, true);
+        HostGaussians h = seed_gaussians(ds->xyz, ds->rgb, cfg.shDegree, opt);
+        set_model(h, opt.seedDecimation != 0);
     }
 
     // setupOptimizers: cap-sized buffers, seed decimation above 75 % of cap
     void set_model(HostGaussians &h, bool decimate) {
         const int cap = std::max(1, cfg.capMax);
         std::vector<int> keep;
-        int rows = std::min(h.n, cap);
-        if (decimate && h.n > (int)(cap * 0.75)) {
-            rows = (int)(cap * 0.5);
-            keep.resize(h.n);
-            std::iota(keep.begin(), keep.end(), 0);
-            std::mt19937 r(42);
-            std::shuffle(keep.begin(), keep.end(), r);
-            keep.resize(rows);
-            std::sort(keep.begin(), keep.end());
-        }
+        const int rows = seed_rows(h.n, cap, decimate, keep);
         model.allocate(cap, h.rest);
         model.n = rows;
         for (int g = 0; g < 6; g++) {
@@ -762,7 +789,7 @@ struct TrainerImpl {
         a.degrees_to_use = std::min(a.degrees_to_use, degree_for_rest(model.rest));
         a.ssim_weight = cfg.ssimWeight;
         a.beta1 = 0.9f; a.beta2 = 0.999f; a.eps = 1e-8f;
-        a.invis_scale = 1.0f;
+        a.invis_scale = opt.regVisibilityDuty;
         if (!training) return;
         // float beta raised to an int power: evaluated in double, rounded once
         const float bc1 = (float)(1.0 - std::pow((double)0.9f, (double)adam_step_count));
@@ -1335,8 +1362,44 @@ void msplat_dataset_camera_pose(MsplatDataset ds, int i, float c2w[16]) {
 }
 
 MsplatTrainer msplat_trainer_create(MsplatDataset ds, MsplatConfig config) {
-    if (!ds) return nullptr;
-    return guard("trainer", [&]() -> MsplatTrainer { return new TrainerImpl(DS(ds), config); }, (MsplatTrainer) nullptr);
+    return msplat_trainer_create_ex(ds, config, nullptr);
+}
+
+void msplat_default_trainer_options(MsplatTrainerOptions *options) {
+    if (options) *options = default_trainer_options();
+}
+
+MsplatTrainer msplat_trainer_create_ex(MsplatDataset ds, MsplatConfig config, const MsplatTrainerOptions *options) {
+    const MsplatTrainerOptions o = options ? *options : default_trainer_options();
+    if (!ds || !trainer_options_valid(o)) return nullptr;
+    return guard("trainer", [&]() -> MsplatTrainer { return new TrainerImpl(DS(ds), config, o); },
+                 (MsplatTrainer) nullptr);
+}
+
+int msplat_seed_gaussians(int num_points, const float *xyz, const uint8_t *rgb, int sh_degree, int cap_max,
+                          const MsplatTrainerOptions *options, float *means, float *scales, float *quats,
+                          float *features_dc, float *features_rest, float *opacities) {
+    const MsplatTrainerOptions o = options ? *options : default_trainer_options();
+    if (num_points < 0 || sh_degree < 0 || sh_degree > 3 || cap_max < 1 || !trainer_options_valid(o)) return -1;
+    if (num_points > 0 && (!xyz || !rgb || !means || !scales || !quats || !features_dc || !opacities ||
+                           (sh_degree > 0 && !features_rest)))
+        return -1;
+    return guard("seed_gaussians", [&]() {
+        const std::vector<float> p(xyz, xyz + 3 * (size_t)num_points);
+        const std::vector<uint8_t> c(rgb, rgb + 3 * (size_t)num_points);
+        const HostGaussians h = seed_gaussians(p, c, sh_degree, o);
+        std::vector<int> keep;
+        const int rows = seed_rows(h.n, cap_max, o.seedDecimation != 0, keep);
+        float *dst[6] = {means, scales, quats, features_dc, features_rest, opacities};
+        const size_t w[6] = {3, 3, 4, 3, (size_t)3 * h.rest, 1};
+        for (int g = 0; g < 6; g++) {
+            if (!dst[g] || !w[g]) continue;
+            for (int i = 0; i < rows; i++)
+                std::memcpy(dst[g] + (size_t)i * w[g], &h.a[g][(size_t)(keep.empty() ? i : keep[i]) * w[g]],
+                            w[g] * sizeof(float));
+        }
+        return rows;
+    }, -1);
 }
 
 void msplat_trainer_destroy(MsplatTrainer t) { delete TR(t); }

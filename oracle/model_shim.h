@@ -3,8 +3,9 @@
 // 19-65), the loader and Gaussian-file declarations (core/include/
 // loaders.hpp) and MTensor,
 // with only the members the host code compiled by ref_model.cpp uses (the
-// MCMC pass, camera setup, evaluation metrics, checkpoints, the COLMAP,
-// Nerfstudio and Polycam loaders, the Gaussian PLY / .splat files), so that
+// seed initialisation, MCMC pass, camera setup, evaluation metrics,
+// checkpoints, the COLMAP, Nerfstudio and Polycam loaders, the Gaussian PLY
+// / .splat files), so that
 // code compiles unchanged — TEST INFRASTRUCTURE ONLY (it pins the oracle's
 // and the library's restatements; nothing in the product uses it).
 //
@@ -17,7 +18,8 @@
 // refreshViews().
 #pragma once
 
-#include "json_shim.h"   // nlohmann::json, for the Nerfstudio and Polycam loaders
+#include "json_shim.h"        // nlohmann::json, for the Nerfstudio and Polycam loaders
+#include "nanoflann_shim.h"   // nanoflann, for the seed scales' k-nearest search
 
 #include <algorithm>
 #include <cmath>
@@ -58,6 +60,7 @@ struct HostTensor {
     }
     std::vector<int64_t> shape() const { return dims; }
     bool defined() const { return p != nullptr; }
+    void reset() { *this = HostTensor(); }
     void *data_ptr() { return p; }
     const void *data_ptr() const { return p; }
     uint32_t ndim() const { return (uint32_t)dims.size(); }
@@ -78,6 +81,7 @@ inline HostTensor gpu_empty(std::initializer_list<int64_t> shape, DType d) {
     return gpu_empty(std::vector<int64_t>(shape), d);
 }
 inline HostTensor gpu_zeros(const std::vector<int64_t> &shape, DType d) { return gpu_empty(shape, d); }
+inline HostTensor gpu_zeros(std::initializer_list<int64_t> shape, DType d) { return gpu_empty(shape, d); }
 
 namespace fs = std::filesystem;
 
@@ -138,6 +142,20 @@ inline void msplat_grad_nan_counts(uint32_t out[16]) {
 
 class Model {
 public:
+    Model() = default;
+    Model(const InputData &inputData, int numCameras, int shDegree, int shDegreeInterval, int capMax, float noiseLr,
+          float opacityReg, float scaleReg, int maxSteps, bool keepCrs, const float *bgColor = nullptr,
+          int positionLrMaxSteps = 30000, bool decimateSeeds = true, float initOpacity = 0.5f,
+          float initScaleMult = 0.1f);
+    void setupOptimizers(bool decimateSeeds);
+    void releaseOptimizers();
+    int numCameras = 0;
+    bool keepCrs = false;
+    float noise_lr = 0.f, opacity_reg = 0.f, scale_reg = 0.f;
+    int position_lr_max_steps_ = 30000;
+    float scale = 1.f;
+    float translation[3] = {};
+    HostTensor backgroundColor;
     static constexpr int N_ADAM_GROUPS = 6;
     HostTensor means_buf, scales_buf, quats_buf, featuresDc_buf, featuresRest_buf, opacities_buf;
     HostTensor means, scales, quats, featuresDc, featuresRest, opacities;

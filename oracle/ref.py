@@ -345,3 +345,20 @@ def load_checkpoint(path):
         return step, adam_steps, lr, grps[0], grps[1], grps[2]
     finally:
         L.ref_checkpoint_free(h)
+
+
+def seed_model(xyz, rgb, sh_degree=3, cap_max=1_000_000, init_opacity=0.5, init_scale_mult=0.1, decimate=True):
+    """The reference's seed initialisation (Model::Model and
+    setupOptimizers, model.cpp:80-254, compiled unchanged; its k-nearest
+    query answered by oracle/nanoflann_shim.h): the Gaussians in use
+    [means, scales, quats, features_dc, features_rest, opacities]."""
+    L = lib()
+    xyz = np.ascontiguousarray(xyz, np.float32)
+    rgb = np.ascontiguousarray(rgb, np.uint8)
+    n = xyz.shape[0]
+    rest = (sh_degree + 1) ** 2 - 1
+    arrs = [np.zeros(s, np.float32) for s in ((n, 3), (n, 3), (n, 4), (n, 3), (n, rest, 3), (n,))]
+    L.ref_seed_model.restype = C.c_int
+    rows = L.ref_seed_model(n, _p(xyz), rgb.ctypes.data_as(C.POINTER(C.c_uint8)), int(sh_degree), int(cap_max),
+                            C.c_float(init_opacity), C.c_float(init_scale_mult), int(decimate), *[_p(a) for a in arrs])
+    return [a[:rows] for a in arrs]

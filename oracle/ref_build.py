@@ -42,7 +42,9 @@ SIMD-group functions; metal_shim.h runs their threadgroups on host threads.
 The host code on the path is copied the same way and compiled by
 ref_model.cpp against model_shim.h (host stand-ins for the Model, Camera,
 InputData and MTensor types with the members that code uses): from
-core/src/model.cpp the MCMC pass (computeRelocation, relocate,
+core/src/model.cpp the seed initialisation (Model::Model, setupOptimizers,
+with the k-nearest adapter of core/include/kdtree_tensor.hpp, whose
+nanoflann query nanoflann_shim.h answers), the MCMC pass (computeRelocation, relocate,
 addNewGaussians, mcmcAfterTrain: lines 311-660), the checkpoint save and
 load (696-843), the camera setup (prepareCam, getDownscaleFactor) and the
 psnr / l1_loss metrics; from
@@ -73,12 +75,16 @@ COLMAP = os.path.join("core", "src", "loaders", "load_colmap.cpp")
 PLY = os.path.join("core", "src", "loaders", "load_ply.cpp")
 INPUT = os.path.join("core", "src", "input_data.cpp")
 SAVE = os.path.join("core", "src", "loaders", "save_gaussians.cpp")
+KDTREE = os.path.join("core", "include", "kdtree_tensor.hpp")
 NERF = os.path.join("core", "src", "loaders", "load_nerfstudio.cpp")
 POLY = os.path.join("core", "src", "loaders", "load_polycam.cpp")
 # Host code compiled by ref_model.cpp against model_shim.h (host stand-ins
 # for Model, Camera and MTensor): (file, first, last, first-line text, last-line text)
 HOST_RANGES = [
+    (KDTREE, 8, 41, "// nanoflann adapter for a flat float array of 3D points.", "};"),  # PointsTensor (k nearest)
+    (MODEL, 21, 31, "static const double C0 = 0.28209479177387814;", "}"),     # C0, numShBases
     (MODEL, 33, 49, "// Metrics on CPU MTensor data", "}"),                      # psnr, l1_loss
+    (MODEL, 80, 254, "// Model constructor", "}"),                               # seeds, setupOptimizers
     (MODEL, 276, 282, "int Model::getDownscaleFactor(int step) {", "}"),
     (MODEL, 311, 660, "void Model::computeRelocation(float opacity_old_sig, float* scale_old_exp, int N,", "}"),
     (MODEL, 696, 843, "// ── Checkpoint save/load", "}"),             # saveCheckpoint, loadCheckpoint
@@ -87,7 +93,7 @@ HOST_RANGES = [
     (COLMAP, 7, 165, "namespace fs = std::filesystem;", "}"),               # the COLMAP binary loader
     (PLY, 6, 205, "// Property types in PLY files", "}"),                   # readPly, readColmapPoints
     (INPUT, 115, 169, "void autoScaleAndCenter(InputData &data) {", "}"),   # pose centring and scaling
-    (SAVE, 8, 231, "static const double C0 = 0.28209479177387814;", "}"),  # Gaussian PLY / .splat files
+    (SAVE, 10, 231, "void saveGaussianPly(const std::string &path, GaussianParams &p, int step) {", "}"),  # PLY / .splat
     (NERF, 7, 72, "namespace fs = std::filesystem;", "}"),                  # the Nerfstudio loader
     (POLY, 7, 95, "namespace fs = std::filesystem;", "}"),                  # the Polycam loader
 ]

@@ -1,14 +1,16 @@
 // The reference's host code on the path, compiled unchanged against
 // oracle/model_shim.h — TEST INFRASTRUCTURE ONLY: from core/src/model.cpp
-// the MCMC pass (computeRelocation, relocate, addNewGaussians,
-// mcmcAfterTrain: 311-660), the camera setup (prepareCam: 845-889,
-// getDownscaleFactor: 276-282) and the psnr / l1_loss metrics (33-49); from
-// core/src/ssim.cpp ssim_eval (26-123); the COLMAP binary loader
-// (loaders/load_colmap.cpp:7-165), the Nerfstudio and Polycam loaders
-// (load_nerfstudio.cpp:7-72, load_polycam.cpp:7-95) with the point readers
-// (loaders/load_ply.cpp:6-205) and autoScaleAndCenter (input_data.cpp:
-// 115-169); the Gaussian PLY / .splat files (loaders/save_gaussians.cpp:
-// 8-231).  The code is copied into
+// the seed initialisation (Model::Model, setupOptimizers: 80-254, with the
+// k-nearest adapter of core/include/kdtree_tensor.hpp), the MCMC pass
+// (computeRelocation, relocate, addNewGaussians, mcmcAfterTrain: 311-660),
+// checkpoint save and load (696-843), the camera setup (prepareCam:
+// 845-889, getDownscaleFactor: 276-282) and the psnr / l1_loss metrics
+// (33-49); from core/src/ssim.cpp ssim_eval (26-123); the COLMAP binary
+// loader (loaders/load_colmap.cpp:7-165), the Nerfstudio and Polycam
+// loaders (load_nerfstudio.cpp:7-72, load_polycam.cpp:7-95) with the point
+// readers (loaders/load_ply.cpp:6-205) and autoScaleAndCenter
+// (input_data.cpp:115-169); the Gaussian PLY / .splat files
+// (loaders/save_gaussians.cpp:10-231).  The code is copied into
 // oracle/_ref/model_host.inc by oracle/ref_build.py (never committed); this
 // file only wraps it for ctypes.
 #include <cstdio>
@@ -275,5 +277,27 @@ void ref_checkpoint_arrays(void *h, float *const params[6], float *const exp_avg
     }
 }
 void ref_checkpoint_free(void *h) { delete static_cast<LoadedCheckpoint *>(h); }
+
+// Model::Model and setupOptimizers (model.cpp:80-254) from n seed points:
+// the Gaussians in use (the first rows of the model's cap-sized buffers)
+// written to arrays of n rows in the C API's layouts; returns their count.
+int ref_seed_model(int n, const float *xyz, const uint8_t *rgb, int sh_degree, int cap_max, float init_opacity,
+                   float init_scale_mult, int decimate, float *means, float *scales, float *quats, float *features_dc,
+                   float *features_rest, float *opacities) {
+    InputData d;
+    d.points.count = n;
+    d.points.xyz.assign(xyz, xyz + 3 * (size_t)n);
+    d.points.rgb.assign(rgb, rgb + 3 * (size_t)n);
+    Model m(d, 1, sh_degree, 1000, cap_max, 5e5f, 0.01f, 0.01f, 30000, false, nullptr, 30000, decimate != 0,
+            init_opacity, init_scale_mult);
+    HostTensor *bufs[6] = {&m.means_buf, &m.scales_buf, &m.quats_buf, &m.featuresDc_buf, &m.featuresRest_buf,
+                           &m.opacities_buf};
+    float *dst[6] = {means, scales, quats, features_dc, features_rest, opacities};
+    for (int g = 0; g < 6; g++) {
+        const int64_t row = bufs[g]->numel() / bufs[g]->size(0);
+        if (dst[g] && row) std::memcpy(dst[g], bufs[g]->p, (size_t)m.num_active * row * sizeof(float));
+    }
+    return m.num_active;
+}
 
 }  // extern "C"

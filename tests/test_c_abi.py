@@ -150,3 +150,29 @@ def test_gaussian_files_round_trip(tmp_path):
     L = A._lib()
     assert L.msplat_write_ply(None, 0, 15, None, None, None, None, None, None, 0, 0, 1.0, None) == -1
     assert L.msplat_ply_info(str(tmp_path / "missing.ply").encode(), None, None, None) == -2
+
+
+def test_trainer_options_and_seed_gaussians():
+    """The Python TrainerOptions defaults are msplat_default_trainer_options
+    (the reference's: opacity 0.5, scale x0.1, decimation on, 30000-step LR
+    decay, duty 1); msplat_seed_gaussians applies them on the host (opacity
+    logits, decimation to half the cap above 75 %) and refuses options out
+    of range."""
+    import ctypes as C
+    import numpy as np
+    from msplat_gb300 import api as A
+    d = A._TrainerOptions()
+    A._lib().msplat_default_trainer_options(C.byref(d))
+    o = A.TrainerOptions()
+    assert (d.initOpacity, d.initScaleMult, d.seedDecimation, d.positionLrMaxSteps, d.regVisibilityDuty) == \
+        (np.float32(o.init_opacity), np.float32(o.init_scale_mult), 1, o.position_lr_max_steps,
+         np.float32(o.reg_visibility_duty))
+    rng = np.random.default_rng(0)
+    xyz = rng.normal(0, 1, (400, 3)).astype(np.float32)
+    rgb = rng.integers(0, 256, (400, 3), dtype=np.uint8)
+    g = A.seed_gaussians(xyz, rgb, cap_max=10_000)
+    assert g[0].shape[0] == 400 and np.allclose(g[5], 0.0) and np.array_equal(g[0], xyz)
+    g = A.seed_gaussians(xyz, rgb, cap_max=500, options=A.TrainerOptions(init_opacity=0.25))
+    assert g[0].shape[0] == 250 and np.allclose(g[5], np.log(0.25 / 0.75))
+    with pytest.raises(RuntimeError):
+        A.seed_gaussians(xyz, rgb, options=A.TrainerOptions(init_opacity=1.5))

@@ -449,3 +449,11 @@ def test_cli_arguments():
     a = cli.parse(["data", "-n", "7000", "-d", "0.5", "--eval", "--bg-color", "0", "0.5", "1", "--early-stop", "0.1"])
     assert (a.input, a.num_iters, a.downscale_factor, a.eval) == ("data", 7000, 1.0, True)
     assert a.bg_color == [0.0, 0.5, 1.0] and a.early_stop == 0.1 and a.cap_max == 1_000_000
+    # the reference CLI's model options (cli/msplat.mm:90-131)
+    a = cli.parse(["data", "--init-opacity", "0.2", "--init-scale", "0.5", "--no-seed-decimation",
+                   "--position-lr-max-steps", "7000", "--reg-visibility-duty", "0.25"])
+    assert (a.init_opacity, a.init_scale, a.no_seed_decimation, a.position_lr_max_steps,
+            a.reg_visibility_duty) == (0.2, 0.5, True, 7000, 0.25)
+    d = cli.parse(["data"])
+    assert (d.init_opacity, d.init_scale, d.no_seed_decimation, d.position_lr_max_steps,
+            d.reg_visibility_duty) == (0.5, 0.1, False, 30000, 1.0)

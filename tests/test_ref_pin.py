@@ -809,3 +809,41 @@ def test_live_polycam_loader(ref_lib, tmp_path, layout):
         ply = tmp_path / "point_cloud.ply"
     _write_ply_points(ply, rng.normal(0, 1.3, (60, 3)).astype(np.float32), rng.integers(0, 256, (60, 3), dtype=np.uint8))
     _compare_dataset(ref_lib, tmp_path, "polycam", 7)
+
+
+# ---- seed initialisation (model.cpp:80-254, kdtree_tensor.hpp) ----
+
+SEED_CASES = {
+    # points, cap, options: defaults; seed decimation (points above 75 % of the cap);
+    # decimation off (truncation to the cap); other opacity and scale multiplier, SH degree 1
+    "default": (1500, 100_000, {}, 3),
+    "decimated": (1500, 1800, {}, 3),
+    "truncated": (1500, 1200, {"seed_decimation": False}, 3),
+    "options": (900, 100_000, {"init_opacity": 0.1, "init_scale_mult": 1.0}, 1),
+}
+
+
+@needs_reference
+@pytest.mark.parametrize("name", list(SEED_CASES))
+def test_live_seed_initialisation(ref_lib, name):
+    """The reference's Model::Model and setupOptimizers (its nanoflann
+    k-nearest query answered by a brute-force stand-in with nanoflann's
+    metric) against the library's seed initialisation (msplat_seed_gaussians,
+    the trainer's own code, with its grid search): identical Gaussians in use
+    (KNN scales, mt19937 quaternions, DC from colours, opacity logits,
+    decimation or truncation), duplicate points included."""
+    from msplat_gb300 import api as A
+    n, cap, opts, deg = SEED_CASES[name]
+    rng = np.random.default_rng(len(name))
+    xyz = rng.normal(0, 2.0, (n, 3)).astype(np.float32)
+    xyz[10:14] = xyz[3]                              # duplicates: distance 0 counts
+    xyz[50:60] *= np.float32(40.0)                   # far-out points: sparse neighbourhoods
+    rgb = rng.integers(0, 256, (n, 3), dtype=np.uint8)
+    o = A.TrainerOptions(**opts)
+    mine = A.seed_gaussians(xyz, rgb, sh_degree=deg, cap_max=cap, options=o)
+    ref = ref_lib.seed_model(xyz, rgb, sh_degree=deg, cap_max=cap, init_opacity=o.init_opacity,
+                             init_scale_mult=o.init_scale_mult, decimate=o.seed_decimation)
+    want_rows = {"default": n, "decimated": cap // 2, "truncated": cap, "options": n}[name]
+    assert mine[0].shape[0] == ref[0].shape[0] == want_rows
+    for k, a, b in zip(GROUPS, mine, ref):
+        assert a.tobytes() == b.reshape(a.shape).tobytes(), (k, np.abs(a - b.reshape(a.shape)).max())
