@@ -125,6 +125,31 @@ int msplat_dataset_camera(MsplatDataset ds, int i, int use_test, float intrinsic
 MsplatDataset msplat_dataset_create_ex(const char *path, float downscaleFactor, bool evalMode, int testEvery,
                                        const char *colmapImagePath);
 
+/* msplat_dataset_create_ex with training masks from maskDir (the reference
+ * CLI's --mask-dir, Camera::loadMask, core/src/input_data.cpp:81-111): for
+ * each camera "<maskDir>/<name>.png", else the name with its extension
+ * replaced by .png (name: the image's path under the image folder), resized
+ * to the camera's final size by area averaging; a pixel contributes where
+ * the mask's first channel is above 0.5; an all-white mask, or none, leaves
+ * the camera unmasked.  As in the reference, only COLMAP datasets name their
+ * images for the lookup.  maskDir NULL or "": no masks. */
+MsplatDataset msplat_dataset_create_masked(const char *path, float downscaleFactor, bool evalMode, int testEvery,
+                                           const char *colmapImagePath, const char *maskDir);
+
+/* The reference CLI's --val (InputData::getCameras, core/src/input_data.cpp:
+ * 173-194): withholds one training camera as the dataset's only test camera
+ * — val_image "random" (or NULL) picks mt19937(42)'s first draw modulo the
+ * camera count, otherwise the first camera whose image path contains
+ * val_image (the first camera when none does).  Returns the index it had
+ * among the training cameras, or -1 when the dataset already has test
+ * cameras (eval mode) or no cameras. */
+int msplat_dataset_hold_out(MsplatDataset ds, const char *val_image);
+
+/* Camera i's training mask (255 = contributes, 0 = ignored; [H,W], may be
+ * NULL to ask only): returns the number of contributing pixels, -1 when the
+ * camera has no mask, -2 for a bad index. */
+long long msplat_dataset_mask(MsplatDataset ds, int i, int use_test, uint8_t *mask);
+
 /* Learned relocation proposal (no counterpart in the reference; off by
  * default): per-Gaussian activity statistics are gathered during the steps,
  * a 22-64-64-2 MLP on the tensor cores is trained every 500 steps on the

@@ -108,6 +108,11 @@ def _lib():
                                           fpp, fpp, fpp]
     L.msplat_read_checkpoint.argtypes = [cp, fp, fp, C.POINTER(C.c_int), fpp, fpp, fpp]
     L.msplat_checkpoint_info.argtypes = [cp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.msplat_dataset_create_masked.argtypes = [cp, C.c_float, C.c_bool, C.c_int, cp, cp]
+    L.msplat_dataset_create_masked.restype = vp
+    L.msplat_dataset_mask.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_uint8)]
+    L.msplat_dataset_hold_out.argtypes = [vp, cp]
+    L.msplat_dataset_mask.restype = C.c_longlong
     L.msplat_viewer_create.argtypes = [cp, C.c_int, C.c_int, C.c_float]
     L.msplat_viewer_create.restype = vp
     L.msplat_viewer_render.argtypes = [vp, fp, C.POINTER(C.c_uint8)]
@@ -177,10 +182,15 @@ class TrainingStats:
 
 class Dataset:
     def __init__(self, path: str | None = None, downscale_factor: float = 1.0, eval_mode: bool = False,
-                 test_every: int = 8, colmap_image_path: str | None = None, _handle=None):
+                 test_every: int = 8, colmap_image_path: str | None = None, mask_dir: str | None = None,
+                 _handle=None):
         L = _lib()
         if _handle is not None:
             self.h = _handle
+        elif mask_dir:
+            self.h = L.msplat_dataset_create_masked(path.encode(), downscale_factor, eval_mode, test_every,
+                                                    colmap_image_path.encode() if colmap_image_path else None,
+                                                    mask_dir.encode())
         else:
             self.h = L.msplat_dataset_create_ex(path.encode(), downscale_factor, eval_mode, test_every,
                                                 colmap_image_path.encode() if colmap_image_path else None)
@@ -211,6 +221,29 @@ class Dataset:
         if not h:
             raise RuntimeError("could not build a dataset from the arrays (empty image size or missing points?)")
         return cls(_handle=h)
+
+    def hold_out(self, val_image: str = "random") -> int:
+        """Withholds one training camera for validation (the reference CLI's
+        --val / --val-image): it becomes test camera 0.  Returns its former
+        training index."""
+        i = _lib().msplat_dataset_hold_out(self.h, val_image.encode())
+        if i < 0:
+            raise RuntimeError("cannot hold out a validation camera (eval mode, or no cameras)")
+        return i
+
+    def mask(self, i: int, use_test: bool = False):
+        """Camera i's training mask (uint8 [H, W], 255 = contributes), or None."""
+        L = _lib()
+        n = L.msplat_dataset_mask(self.h, i, int(use_test), None)
+        if n == -2:
+            raise IndexError(i)
+        if n < 0:
+            return None
+        size = np.zeros(2, np.int32)
+        L.msplat_dataset_camera(self.h, i, int(use_test), None, size.ctypes.data_as(C.POINTER(C.c_int)), None, None)
+        m = np.zeros((size[1], size[0]), np.uint8)
+        L.msplat_dataset_mask(self.h, i, int(use_test), m.ctypes.data_as(C.POINTER(C.c_uint8)))
+        return m
 
     @property
     def num_train(self) -> int:

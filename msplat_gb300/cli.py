@@ -50,6 +50,9 @@ def parse(argv=None):
     p.add_argument("-o", "--output", default="splat.ply", help="output scene (.ply or .splat)")
     p.add_argument("-s", "--save-every", type=int, default=-1, help="save every N steps (-1 to disable)")
     p.add_argument("--resume", default="", help="resume training from a PLY file")
+    p.add_argument("--val", action="store_true", help="withhold a camera for validation")
+    p.add_argument("--val-image", default="random", help="validation image (file name substring, or random)")
+    p.add_argument("--val-render", default="", help="directory for the validation camera's render every 10 steps")
     p.add_argument("--eval", action="store_true", help="evaluate on held-out test views")
     p.add_argument("--test-every", type=int, default=8, help="hold out every Nth image for eval")
     p.add_argument("--eval-render", default="", help="directory for each eval view's render and ground truth (PNG)")
@@ -66,6 +69,9 @@ def parse(argv=None):
     p.add_argument("--keep-crs", action="store_true", help="export in the input coordinate system")
     p.add_argument("--bg-color", type=float, nargs=3, default=[0.6130, 0.0101, 0.3984], help="background RGB (0-1)")
     p.add_argument("--colmap-image-path", default="", help="override the COLMAP image directory")
+    p.add_argument("--mask-dir", default="",
+                   help="training masks: <dir>/<image name>.png (or the name's extension swapped); "
+                        "white = train, black = ignore (COLMAP datasets)")
     p.add_argument("--early-stop", type=float, default=0.0,
                    help="stop when test-subset PSNR improves less than this (dB) over 5000 steps (needs --eval)")
     p.add_argument("--reg-visibility-duty", type=float, default=1.0,
@@ -108,9 +114,15 @@ def main(argv=None) -> int:
     a = parse(argv)
     t0 = time.time()
     ds = A.Dataset(a.input, downscale_factor=a.downscale_factor, eval_mode=a.eval, test_every=a.test_every,
-                   colmap_image_path=a.colmap_image_path or None)
+                   colmap_image_path=a.colmap_image_path or None, mask_dir=a.mask_dir or None)
     print(f"Loaded {ds.num_train} train cameras" + (f", {ds.num_test} test cameras" if a.eval else "") +
           f" in {time.time() - t0:.1f} s", flush=True)
+    # validation camera (the reference CLI: --val-render implies --val; eval mode splits instead)
+    val = (a.val or bool(a.val_render)) and not a.eval
+    if val:
+        ds.hold_out(a.val_image)
+        if a.val_render:
+            os.makedirs(a.val_render, exist_ok=True)
     cfg = A.TrainingConfig(iterations=a.num_iters, sh_degree=a.sh_degree, sh_degree_interval=a.sh_degree_interval,
                            ssim_weight=a.ssim_weight, cap_max=a.cap_max, noise_lr=a.noise_lr,
                            opacity_reg=a.opacity_reg, scale_reg=a.scale_reg, cull_radius=a.cull_radius,
@@ -154,6 +166,8 @@ def main(argv=None) -> int:
         if crossed(prev, step, a.save_every):
             root, ext = os.path.splitext(a.output)
             _save(trainer, f"{root}_{step}{ext or '.ply'}")
+        if val and a.val_render and crossed(prev, step, 10):
+            _write_png(os.path.join(a.val_render, f"{step}.png"), trainer.render(0, use_test=True))
         if (a.early_stop > 0 and a.eval and ds.num_test > 0 and step >= 10000 and crossed(prev, step, 5000) and
                 step < a.num_iters):
             n_sub = min(30, ds.num_test)

@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <filesystem>
 #include <fstream>
 #include <memory>
 #include <numeric>
@@ -49,6 +50,7 @@ static int degree_for_rest(int rest) {
 // ---------------------------------------------------------------------------
 
 struct HostCamera {
+    std::string path;             // image file (disk datasets; the validation pick matches it)
     float c2w[16];
     int width = 0, height = 0;
     float fx = 0, fy = 0, cx = 0, cy = 0;
@@ -1078,8 +1080,37 @@ using namespace msplat;
 // intrinsics rescaled to the decoded size, area-downscaled by the factor,
 // undistorted when the camera has distortion, and quantised to 8 bits.
 // Images decode on all host threads.
+// Camera::loadMask (core/src/input_data.cpp:81-111): "<dir>/<name>.png",
+// else the name with its extension replaced by .png; resized to the
+// camera's final size by area averaging; kept where the first channel is
+// above 0.5; all-white leaves the camera unmasked.
+static void load_mask(HostCamera &c, const std::string &dir, const std::string &name) {
+    if (dir.empty() || name.empty() || c.width <= 0 || c.height <= 0) return;
+    namespace fs = std::filesystem;
+    const fs::path appended = fs::path(dir) / (name + ".png");
+    const fs::path swapped = (fs::path(dir) / name).replace_extension(".png");
+    std::string file;
+    if (fs::exists(appended)) file = appended.string();
+    else if (fs::exists(swapped)) file = swapped.string();
+    else return;
+    io::Image m = io::read_image(file);
+    if (m.width <= 0 || m.height <= 0) return;
+    if (m.width != c.width || m.height != c.height) m = io::resize_area(m, c.width, c.height);
+    const size_t n = (size_t)c.width * (size_t)c.height;
+    std::vector<uint8_t> keep(n);
+    long long kept = 0;
+    for (size_t i = 0; i < n; i++) {
+        const bool k = m.rgb[i * 3] > 0.5f;
+        keep[i] = k ? 255 : 0;
+        kept += k ? 1 : 0;
+    }
+    if (kept == (long long)n) return;
+    c.mask = std::move(keep);
+    c.unmasked = kept;
+}
+
 static MsplatDataset msplat_dataset_load(const char *path, float downscale, bool eval_mode, int test_every,
-                                         const char *colmap_image_dir = nullptr) {
+                                         const char *colmap_image_dir = nullptr, const char *mask_dir = nullptr) {
     if (!path) throw std::runtime_error("dataset path is null");
     io::LoadedScene sc = io::load_scene(path, colmap_image_dir ? colmap_image_dir : "");
     auto d = std::make_unique<DatasetImpl>();
@@ -1096,6 +1127,7 @@ static MsplatDataset msplat_dataset_load(const char *path, float downscale, bool
             try {
                 const io::LoadedCamera &lc = sc.cameras[i];
                 HostCamera &c = cams[i];
+                c.path = lc.path;
                 io::Image img = io::read_image(lc.path);
                 c.width = lc.width; c.height = lc.height;
                 c.fx = lc.fx; c.fy = lc.fy; c.cx = lc.cx; c.cy = lc.cy;
@@ -1118,6 +1150,7 @@ static MsplatDataset msplat_dataset_load(const char *path, float downscale, bool
                 c.image.resize(img.rgb.size());
                 for (size_t k = 0; k < img.rgb.size(); k++)
                     c.image[k] = (uint8_t)std::min(std::max(std::round(img.rgb[k] * 255.0f), 0.0f), 255.0f);
+                if (mask_dir) load_mask(c, mask_dir, lc.relative_name);
             } catch (const std::exception &e) {
                 errors[i] = e.what();
             }
@@ -1155,6 +1188,44 @@ MsplatDataset msplat_dataset_create_ex(const char *path, float downscaleFactor, 
     return guard("dataset", [&]() -> MsplatDataset {
         return msplat_dataset_load(path, downscaleFactor, evalMode, testEvery, colmapImagePath);
     }, (MsplatDataset) nullptr);
+}
+
+MsplatDataset msplat_dataset_create_masked(const char *path, float downscaleFactor, bool evalMode, int testEvery,
+                                           const char *colmapImagePath, const char *maskDir) {
+    return guard("dataset", [&]() -> MsplatDataset {
+        return msplat_dataset_load(path, downscaleFactor, evalMode, testEvery, colmapImagePath,
+                                   maskDir && maskDir[0] ? maskDir : nullptr);
+    }, (MsplatDataset) nullptr);
+}
+
+int msplat_dataset_hold_out(MsplatDataset ds, const char *val_image) {
+    if (!ds) return -1;
+    DatasetImpl *d = DS(ds);
+    if (d->train.empty() || !d->test.empty()) return -1;
+    // InputData::getCameras (core/src/input_data.cpp:173-194)
+    int idx = -1;
+    const std::string want = val_image ? val_image : "random";
+    if (want == "random") {
+        std::mt19937 rng(42);
+        idx = (int)(rng() % d->train.size());
+    } else {
+        for (int i = 0; i < (int)d->train.size(); i++)
+            if (d->train[i].path.find(want) != std::string::npos) { idx = i; break; }
+    }
+    if (idx < 0) idx = 0;
+    d->test.push_back(std::move(d->train[idx]));
+    d->train.erase(d->train.begin() + idx);
+    return idx;
+}
+
+long long msplat_dataset_mask(MsplatDataset ds, int i, int use_test, uint8_t *mask) {
+    if (!ds) return -2;
+    auto &cams = use_test ? DS(ds)->test : DS(ds)->train;
+    if (i < 0 || i >= (int)cams.size()) return -2;
+    const HostCamera &c = cams[i];
+    if (c.mask.empty()) return -1;
+    if (mask) std::memcpy(mask, c.mask.data(), c.mask.size());
+    return c.unmasked;
 }
 
 MsplatDataset msplat_dataset_create_from_memory(int num_cameras, const float *cam_to_world, const float *intrinsics,

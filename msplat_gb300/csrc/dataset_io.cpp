@@ -1178,7 +1178,8 @@ void load_nerfstudio(const std::string &root, LoadedScene &sc) {
         c.p1 = (float)fr.number("p1", gp1); c.p2 = (float)fr.number("p2", gp2);
         const std::string fp = fr.string("file_path", "");
         c.path = (!fp.empty() && (fp[0] == '/' || fp[0] == '.')) ? resolve_image(fp) : resolve_image((r / fp).string());
-        c.relative_name = fp;
+        // no relative_name: the reference's loadNerfstudio leaves relativeName
+        // empty, so training masks (--mask-dir) apply to COLMAP datasets only
         const Json &tm = fr["transform_matrix"];
         if (tm.kind != Json::Arr || tm.arr.size() < 4) throw std::runtime_error("frame without transform_matrix");
         for (int a = 0; a < 4; a++)
@@ -1236,7 +1237,6 @@ void load_polycam(const std::string &root, LoadedScene &sc) {
             c.path = (idir / (stem + ".png")).string();
             for (const char *ext : {".png", ".jpg", ".jpeg", ".JPG"})
                 if (fs::exists(idir / (stem + ext))) { c.path = (idir / (stem + ext)).string(); break; }
-            c.relative_name = stem;
             sc.cameras.push_back(c);
         }
     } else {
@@ -1253,7 +1253,7 @@ void load_polycam(const std::string &root, LoadedScene &sc) {
                     for (int b = 0; b < 4; b++) c.c2w[4 * a + b] = (float)tm.arr[a].arr.at(b).num;
             c.path = fr.string("file_path", "");
             if (!c.path.empty() && c.path[0] != '/') c.path = (r / c.path).string();
-            c.relative_name = fr.string("file_path", "");
+            // no relative_name: the reference's loadPolycam leaves it empty (masks are COLMAP's)
             sc.cameras.push_back(c);
         }
     }

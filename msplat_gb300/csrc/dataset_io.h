@@ -35,7 +35,7 @@ Image undistort(const Image &src, float fx, float fy, float cx, float cy, float 
 
 struct LoadedCamera {
     std::string path;            // image file
-    std::string relative_name;   // name under the image folder (mask lookup)
+    std::string relative_name;   // COLMAP: name under the image folder (mask lookup); else empty
     int width = 0, height = 0;   // from the metadata; 0 = take the image's
     float fx = 0, fy = 0, cx = 0, cy = 0;
     float k1 = 0, k2 = 0, k3 = 0, p1 = 0, p2 = 0;

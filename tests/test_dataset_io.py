@@ -457,3 +457,73 @@ def test_cli_arguments():
     d = cli.parse(["data"])
     assert (d.init_opacity, d.init_scale, d.no_seed_decimation, d.position_lr_max_steps,
             d.reg_visibility_duty) == (0.5, 0.1, False, 30000, 1.0)
+
+
+def test_colmap_mask_dir(tmp_path):
+    """--mask-dir (Camera::loadMask): "<dir>/<name>.png" or the name with its
+    extension swapped; resized to the image by area averaging; a pixel
+    trains where the mask's first channel is above 0.5; an all-white mask or
+    a missing one leaves the camera unmasked."""
+    eyes, imgs, xyz, rgb = _scene(tmp_path)
+    sp = tmp_path / "sparse" / "0"
+    os.makedirs(sp)
+    os.makedirs(tmp_path / "images")
+    md = tmp_path / "masks"
+    os.makedirs(md)
+    for k in range(5):
+        write_png(tmp_path / "images" / f"im{k}.png", [imgs[k][y].tobytes() for y in range(24)], 2, 8)
+    with open(sp / "cameras.bin", "wb") as f:
+        f.write(struct.pack("<Q", 1) + struct.pack("<IiQQ", 1, 1, 32, 24) + struct.pack("<4d", 30, 30, 16, 12))
+    with open(sp / "images.bin", "wb") as f:
+        f.write(struct.pack("<Q", 5))
+        for k in range(5):
+            q, t = _w2c(_pose(eyes[k]))
+            f.write(struct.pack("<I4d3dI", k + 1, *q, *t, 1) + f"im{k}.png".encode() + b"\0")
+            f.write(struct.pack("<Q", 0))
+    with open(sp / "points3D.bin", "wb") as f:
+        f.write(struct.pack("<Q", len(xyz)))
+        for i in range(len(xyz)):
+            f.write(struct.pack("<Q3d3Bd", i, *xyz[i].astype(np.float64), *rgb[i], 0.5) + struct.pack("<Q", 0))
+    m0 = np.full((24, 32), 255, np.uint8)
+    m0[4:10, 6:20] = 0
+    write_png(md / "im0.png.png", [m0[y].tobytes() for y in range(24)], 0, 8)          # appended name, grey PNG
+    m1 = np.full((12, 16), 255, np.uint8)
+    m1[:6] = 0
+    write_png(md / "im1.png", [m1[y].tobytes() for y in range(12)], 0, 8)              # swapped name, half size
+    write_png(md / "im2.png.png", [bytes([255] * 32)] * 24, 0, 8)                     # all white: unmasked
+    ds = A.Dataset(str(tmp_path), mask_dir=str(md))
+    assert np.array_equal(ds.mask(0), np.where(m0 > 127, 255, 0).astype(np.uint8))
+    want1 = np.full((24, 32), 255, np.uint8)
+    want1[:12] = 0
+    assert np.array_equal(ds.mask(1), want1)
+    assert ds.mask(2) is None and ds.mask(3) is None and ds.mask(4) is None
+    assert A.Dataset(str(tmp_path)).mask(0) is None
+
+
+def test_validation_hold_out(tmp_path):
+    """--val / --val-image (InputData::getCameras): one training camera
+    becomes the only test camera — "random" picks std::mt19937(42)'s first
+    draw (1608637542) modulo the count, a name picks the first camera whose
+    path contains it; eval-mode datasets refuse."""
+    eyes, imgs, xyz, rgb = _scene(tmp_path)
+    os.makedirs(tmp_path / "images")
+    frames = []
+    for k in range(5):
+        write_png(tmp_path / "images" / f"f{k}.png", [imgs[k][y].tobytes() for y in range(24)], 2, 8)
+        frames.append({"file_path": f"images/f{k}.png", "transform_matrix": _pose(eyes[k]).tolist()})
+    json.dump({"w": 32, "h": 24, "fl_x": 30.0, "fl_y": 30.0, "cx": 16.0, "cy": 12.0, "frames": frames,
+               "ply_file_path": "points.ply"}, open(tmp_path / "transforms.json", "w"))
+    _write_ply_points(tmp_path / "points.ply", xyz, rgb)
+    ds = A.Dataset(str(tmp_path))
+    before = [ds.camera(i)["image"] for i in range(5)]
+    assert ds.hold_out("random") == 1608637542 % 5
+    assert (ds.num_train, ds.num_test) == (4, 1)
+    assert np.array_equal(ds.camera(0, use_test=True)["image"], before[1608637542 % 5])
+    ds = A.Dataset(str(tmp_path))
+    assert ds.hold_out("f3") == 3 and np.array_equal(ds.camera(0, use_test=True)["image"], before[3])
+    ds = A.Dataset(str(tmp_path), eval_mode=True, test_every=2)
+    with pytest.raises(RuntimeError):
+        ds.hold_out()
+    from msplat_gb300 import cli
+    a = cli.parse(["data", "--val-render", "out", "--val-image", "f3"])
+    assert (a.val, a.val_render, a.val_image) == (False, "out", "f3")
