@@ -686,7 +686,7 @@ struct TrainerImpl {
         cudaStream_t s = stream();
         if (lrn.pending >= 0) {
             mlp_targets(lrn.idx, lrn.snap, lrn.samples, model.p[5], lrn.gstats, lrn.T, s);
-            // held out: once trained, the MLP predicts this round's labels before it sees them
+            // held out: once trained, the MLP predicts this window's labels before it sees them
             float ev[5] = {0, 0, 0, 0, 0};
             const bool evaluate = lrn.rounds >= 1;
             if (evaluate) {
