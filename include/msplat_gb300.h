@@ -221,6 +221,12 @@ int msplat_dataset_points(MsplatDataset ds, float *xyz, uint8_t *rgb);
  * negative code with the reason on stderr. */
 int msplat_image_read(const char *path, float *rgb, int *width, int *height);
 
+/* Area-averaging resize of a float RGB image [height, width, 3] to
+ * [out_height, out_width, 3] (resizeArea, core/src/loaders/image_io.cpp:
+ * 115-161: the dataset's --downscale-factor and the masks' resize).
+ * Returns 0, or -1 for invalid arguments. */
+int msplat_image_resize(const float *rgb, int width, int height, int out_width, int out_height, float *out);
+
 /* Reads and validates a checkpoint file (the reference's format,
  * core/src/model.cpp:698-843) on the host, without a trainer: every tensor
  * must hold N rows of its group's width and exactly N x width x 4 bytes.

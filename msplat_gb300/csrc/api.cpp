@@ -1302,6 +1302,18 @@ int msplat_image_read(const char *path, float *rgb, int *width, int *height) {
         return 0;
     }, -2);
 }
+int msplat_image_resize(const float *rgb, int width, int height, int out_width, int out_height, float *out) {
+    if (!rgb || !out || width <= 0 || height <= 0 || out_width <= 0 || out_height <= 0) return -1;
+    return guard("image_resize", [&]() {
+        io::Image im;
+        im.width = width;
+        im.height = height;
+        im.rgb.assign(rgb, rgb + (size_t)width * height * 3);
+        const io::Image r = io::resize_area(im, out_width, out_height);
+        std::memcpy(out, r.rgb.data(), r.rgb.size() * sizeof(float));
+        return 0;
+    }, -2);
+}
 int msplat_checkpoint_info(const char *path, int *num_points, int *sh_degree, int *iteration) {
     if (!path) return -1;
     return guard("checkpoint", [&]() {

@@ -97,6 +97,14 @@ struct Camera {
     float cachedFovX = 0, cachedFovY = 0;
 };
 
+struct Image {
+    std::vector<float> data;
+    int width = 0, height = 0;
+    bool empty() const { return data.empty(); }
+    float *ptr() { return data.data(); }
+    const float *ptr() const { return data.data(); }
+};
+
 struct Points {
     std::vector<float> xyz;
     std::vector<uint8_t> rgb;

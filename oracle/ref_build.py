@@ -76,6 +76,7 @@ PLY = os.path.join("core", "src", "loaders", "load_ply.cpp")
 INPUT = os.path.join("core", "src", "input_data.cpp")
 SAVE = os.path.join("core", "src", "loaders", "save_gaussians.cpp")
 KDTREE = os.path.join("core", "include", "kdtree_tensor.hpp")
+IMAGE_IO = os.path.join("core", "src", "loaders", "image_io.cpp")
 NERF = os.path.join("core", "src", "loaders", "load_nerfstudio.cpp")
 POLY = os.path.join("core", "src", "loaders", "load_polycam.cpp")
 # Host code compiled by ref_model.cpp against model_shim.h (host stand-ins
@@ -96,6 +97,7 @@ HOST_RANGES = [
     (SAVE, 10, 231, "void saveGaussianPly(const std::string &path, GaussianParams &p, int step) {", "}"),  # PLY / .splat
     (NERF, 7, 72, "namespace fs = std::filesystem;", "}"),                  # the Nerfstudio loader
     (POLY, 7, 95, "namespace fs = std::filesystem;", "}"),                  # the Polycam loader
+    (IMAGE_IO, 115, 161, "Image resizeArea(const Image &src, int dstW, int dstH) {", "}"),  # area resize
 ]
 
 # (first line, last line, text of the first line, text of the last line), 1-based, inclusive

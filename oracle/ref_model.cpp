@@ -10,7 +10,8 @@
 // loaders (load_nerfstudio.cpp:7-72, load_polycam.cpp:7-95) with the point
 // readers (loaders/load_ply.cpp:6-205) and autoScaleAndCenter
 // (input_data.cpp:115-169); the Gaussian PLY / .splat files
-// (loaders/save_gaussians.cpp:10-231).  The code is copied into
+// (loaders/save_gaussians.cpp:10-231); resizeArea (loaders/image_io.cpp:
+// 115-161).  The code is copied into
 // oracle/_ref/model_host.inc by oracle/ref_build.py (never committed); this
 // file only wraps it for ctypes.
 #include <cstdio>
@@ -298,6 +299,16 @@ int ref_seed_model(int n, const float *xyz, const uint8_t *rgb, int sh_degree, i
         if (dst[g] && row) std::memcpy(dst[g], bufs[g]->p, (size_t)m.num_active * row * sizeof(float));
     }
     return m.num_active;
+}
+
+// resizeArea (loaders/image_io.cpp:115-161) of a float RGB image.
+void ref_resize_area(const float *rgb, int w, int h, int dw, int dh, float *out) {
+    Image src;
+    src.width = w;
+    src.height = h;
+    src.data.assign(rgb, rgb + (size_t)w * h * 3);
+    const Image r = resizeArea(src, dw, dh);
+    std::memcpy(out, r.data.data(), r.data.size() * sizeof(float));
 }
 
 }  // extern "C"

@@ -847,3 +847,26 @@ def test_live_seed_initialisation(ref_lib, name):
     assert mine[0].shape[0] == ref[0].shape[0] == want_rows
     for k, a, b in zip(GROUPS, mine, ref):
         assert a.tobytes() == b.reshape(a.shape).tobytes(), (k, np.abs(a - b.reshape(a.shape)).max())
+
+
+@needs_reference
+def test_live_resize_area(ref_lib):
+    """The reference's resizeArea (loaders/image_io.cpp:115-161) against the
+    library's (msplat_image_resize: the dataset's --downscale-factor and the
+    training masks' resize): identical floats for downscales by integer and
+    fractional factors and for upscales."""
+    import ctypes as C
+    from msplat_gb300 import build
+    lib = C.CDLL(build.build())
+    fp = C.POINTER(C.c_float)
+    lib.msplat_image_resize.argtypes = [fp, C.c_int, C.c_int, C.c_int, C.c_int, fp]
+    L = ref_lib.lib()
+    L.ref_resize_area.argtypes = [fp, C.c_int, C.c_int, C.c_int, C.c_int, fp]
+    rng = np.random.default_rng(13)
+    img = (rng.integers(0, 256, (37, 53, 3)) / np.float32(255.0)).astype(np.float32)
+    for dw, dh in ((26, 18), (17, 12), (53, 37), (20, 30), (106, 74), (7, 5)):
+        a = np.zeros((dh, dw, 3), np.float32)
+        b = np.zeros_like(a)
+        assert lib.msplat_image_resize(img.ctypes.data_as(fp), 53, 37, dw, dh, a.ctypes.data_as(fp)) == 0
+        L.ref_resize_area(img.ctypes.data_as(fp), 53, 37, dw, dh, b.ctypes.data_as(fp))
+        assert a.tobytes() == b.tobytes(), (dw, dh, np.abs(a - b).max())
