@@ -116,6 +116,8 @@ struct InputData {
     float scale = 1.0f;
     float translation[3] = {};
     Points points;
+    std::tuple<std::vector<Camera>, Camera *> getCameras(bool validate, const std::string &valImage = "random");
+    std::tuple<std::vector<Camera>, std::vector<Camera>> splitTrainTest(int testEvery);
 };
 
 namespace loaders {

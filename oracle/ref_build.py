@@ -94,6 +94,7 @@ HOST_RANGES = [
     (COLMAP, 7, 165, "namespace fs = std::filesystem;", "}"),               # the COLMAP binary loader
     (PLY, 6, 205, "// Property types in PLY files", "}"),                   # readPly, readColmapPoints
     (INPUT, 115, 169, "void autoScaleAndCenter(InputData &data) {", "}"),   # pose centring and scaling
+    (INPUT, 173, 205, "std::tuple<std::vector<Camera>, Camera*> InputData::getCameras(", "}"),  # --val, --eval split
     (SAVE, 10, 231, "void saveGaussianPly(const std::string &path, GaussianParams &p, int step) {", "}"),  # PLY / .splat
     (NERF, 7, 72, "namespace fs = std::filesystem;", "}"),                  # the Nerfstudio loader
     (POLY, 7, 95, "namespace fs = std::filesystem;", "}"),                  # the Polycam loader

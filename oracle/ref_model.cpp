@@ -9,7 +9,8 @@
 // loader (loaders/load_colmap.cpp:7-165), the Nerfstudio and Polycam
 // loaders (load_nerfstudio.cpp:7-72, load_polycam.cpp:7-95) with the point
 // readers (loaders/load_ply.cpp:6-205) and autoScaleAndCenter
-// (input_data.cpp:115-169); the Gaussian PLY / .splat files
+// (input_data.cpp:115-169), getCameras and splitTrainTest (173-205); the
+// Gaussian PLY / .splat files
 // (loaders/save_gaussians.cpp:10-231); resizeArea (loaders/image_io.cpp:
 // 115-161).  The code is copied into
 // oracle/_ref/model_host.inc by oracle/ref_build.py (never committed); this
@@ -299,6 +300,27 @@ int ref_seed_model(int n, const float *xyz, const uint8_t *rgb, int sh_degree, i
         if (dst[g] && row) std::memcpy(dst[g], bufs[g]->p, (size_t)m.num_active * row * sizeof(float));
     }
     return m.num_active;
+}
+
+// InputData::getCameras (input_data.cpp:173-194) over cameras with the given
+// image paths: the validation camera's index (or -1 without validation);
+// and splitTrainTest (:196-205): test[i] = 1 for the test cameras.
+int ref_val_camera(int n, const char *const *paths, int validate, const char *val_image) {
+    InputData d;
+    d.cameras.resize((size_t)n);
+    for (int i = 0; i < n; i++) d.cameras[(size_t)i].filePath = paths[i];
+    auto [train, val] = d.getCameras(validate != 0, val_image);
+    (void)train;
+    return val ? (int)(val - d.cameras.data()) : -1;
+}
+void ref_split_train_test(int n, int test_every, int *test) {
+    InputData d;
+    d.cameras.resize((size_t)n);
+    for (int i = 0; i < n; i++) d.cameras[(size_t)i].filePath = std::to_string(i);
+    auto [train, tst] = d.splitTrainTest(test_every);
+    for (int i = 0; i < n; i++) test[i] = 0;
+    for (const Camera &c : tst) test[std::stoi(c.filePath)] = 1;
+    (void)train;
 }
 
 // resizeArea (loaders/image_io.cpp:115-161) of a float RGB image.

@@ -870,3 +870,41 @@ def test_live_resize_area(ref_lib):
         assert lib.msplat_image_resize(img.ctypes.data_as(fp), 53, 37, dw, dh, a.ctypes.data_as(fp)) == 0
         L.ref_resize_area(img.ctypes.data_as(fp), 53, 37, dw, dh, b.ctypes.data_as(fp))
         assert a.tobytes() == b.tobytes(), (dw, dh, np.abs(a - b).max())
+
+
+@needs_reference
+def test_live_camera_selection(ref_lib, tmp_path):
+    """The reference's InputData::getCameras (--val: mt19937(42) pick or
+    file-name match) and splitTrainTest (--eval) against the library's
+    msplat_dataset_hold_out and eval split, on 11 cameras."""
+    import ctypes as C
+    import json
+    from msplat_gb300 import api as A
+    from test_dataset_io import _pose, _write_ply_points
+    rng = np.random.default_rng(2)
+    os.makedirs(tmp_path / "images")
+    frames = []
+    n = 11
+    for k in range(n):
+        _write_image(tmp_path / "images" / f"cam{k:02d}.png", 16, 12, rng)
+        a = 2 * np.pi * k / n
+        frames.append({"file_path": f"images/cam{k:02d}.png", "transform_matrix": _pose((4 * np.cos(a), 4 * np.sin(a), 1.0)).tolist()})
+    json.dump({"w": 16, "h": 12, "fl_x": 15.0, "fl_y": 15.0, "cx": 8.0, "cy": 6.0, "frames": frames,
+               "ply_file_path": "p.ply"}, open(tmp_path / "transforms.json", "w"))
+    _write_ply_points(tmp_path / "p.ply", rng.normal(0, 1, (20, 3)).astype(np.float32),
+                      rng.integers(0, 256, (20, 3), dtype=np.uint8))
+    paths = [str(tmp_path / "images" / f"cam{k:02d}.png").encode() for k in range(n)]
+    L = ref_lib.lib()
+    arr = (C.c_char_p * n)(*paths)
+    for pick in ("random", "cam07", "no_such_name"):
+        want = L.ref_val_camera(n, arr, 1, pick.encode())
+        assert A.Dataset(str(tmp_path)).hold_out(pick) == want
+    for every in (1, 3, 8):
+        test = np.zeros(n, np.int32)
+        L.ref_split_train_test(n, every, test.ctypes.data_as(C.POINTER(C.c_int)))
+        ds = A.Dataset(str(tmp_path), eval_mode=True, test_every=every)
+        assert (ds.num_test, ds.num_train) == (int(test.sum()), n - int(test.sum()))
+        full = A.Dataset(str(tmp_path))
+        imgs = [full.camera(i)["image"].tobytes() for i in range(n)]
+        got = sorted(imgs.index(ds.camera(i, use_test=True)["image"].tobytes()) for i in range(ds.num_test))
+        assert got == list(np.flatnonzero(test))
