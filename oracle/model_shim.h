@@ -68,7 +68,7 @@ struct HostTensor {
 };
 using MTensor = HostTensor;
 
-enum class DType { Float32 };
+enum class DType { Float32, UInt8 };
 inline HostTensor gpu_empty(const std::vector<int64_t> &shape, DType) {
     HostTensor t;
     t.dims = shape;
@@ -92,6 +92,9 @@ struct Camera {
     float camToWorld[16] = {};
     std::string filePath;
     std::string relativeName;
+    MTensor gpuMask;
+    int64_t unmaskedPixels = -1;
+    void loadMask(const std::string &maskDir);
     MTensor cachedViewMat, cachedProjViewMat;
     float cachedCamPos[3] = {};
     float cachedFovX = 0, cachedFovY = 0;
@@ -104,6 +107,30 @@ struct Image {
     float *ptr() { return data.data(); }
     const float *ptr() const { return data.data(); }
 };
+
+// The reference decodes images through CoreGraphics (loaders/image_io.cpp:
+// 13-56), which is not here; this stand-in decodes 8-bit binary PGM / PPM
+// (grey replicated to RGB, values / 255), enough for the masks the tests
+// write.  An unreadable file decodes empty.
+inline Image imreadRGB(const std::string &path) {
+    Image im;
+    std::ifstream f(path, std::ios::binary);
+    std::string magic;
+    int w = 0, h = 0, maxv = 0;
+    if (!(f >> magic >> w >> h >> maxv) || (magic != "P5" && magic != "P6") || maxv != 255 || w <= 0 || h <= 0)
+        return im;
+    f.get();
+    const int ch = magic == "P6" ? 3 : 1;
+    std::vector<unsigned char> raw((size_t)w * h * ch);
+    f.read(reinterpret_cast<char *>(raw.data()), (std::streamsize)raw.size());
+    im.width = w;
+    im.height = h;
+    im.data.resize((size_t)w * h * 3);
+    for (size_t i = 0; i < (size_t)w * h; i++)
+        for (int c = 0; c < 3; c++) im.data[i * 3 + c] = raw[i * ch + (ch == 3 ? c : 0)] / 255.0f;
+    return im;
+}
+Image resizeArea(const Image &src, int dstW, int dstH);
 
 struct Points {
     std::vector<float> xyz;

@@ -93,6 +93,7 @@ HOST_RANGES = [
     (SSIM, 26, 123, "// Separable Gaussian blur on a single-channel (H, W) image.", "}"),  # gaussianBlur, ssim_eval
     (COLMAP, 7, 165, "namespace fs = std::filesystem;", "}"),               # the COLMAP binary loader
     (PLY, 6, 205, "// Property types in PLY files", "}"),                   # readPly, readColmapPoints
+    (INPUT, 81, 111, "void Camera::loadMask(const std::string &maskDir) {", "}"),  # training masks
     (INPUT, 115, 169, "void autoScaleAndCenter(InputData &data) {", "}"),   # pose centring and scaling
     (INPUT, 173, 205, "std::tuple<std::vector<Camera>, Camera*> InputData::getCameras(", "}"),  # --val, --eval split
     (SAVE, 10, 231, "void saveGaussianPly(const std::string &path, GaussianParams &p, int step) {", "}"),  # PLY / .splat

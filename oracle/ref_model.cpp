@@ -9,7 +9,8 @@
 // loader (loaders/load_colmap.cpp:7-165), the Nerfstudio and Polycam
 // loaders (load_nerfstudio.cpp:7-72, load_polycam.cpp:7-95) with the point
 // readers (loaders/load_ply.cpp:6-205) and autoScaleAndCenter
-// (input_data.cpp:115-169), getCameras and splitTrainTest (173-205); the
+// (input_data.cpp:115-169), Camera::loadMask (81-111), getCameras and
+// splitTrainTest (173-205); the
 // Gaussian PLY / .splat files
 // (loaders/save_gaussians.cpp:10-231); resizeArea (loaders/image_io.cpp:
 // 115-161).  The code is copied into
@@ -321,6 +322,20 @@ void ref_split_train_test(int n, int test_every, int *test) {
     for (int i = 0; i < n; i++) test[i] = 0;
     for (const Camera &c : tst) test[std::stoi(c.filePath)] = 1;
     (void)train;
+}
+
+// Camera::loadMask (input_data.cpp:81-111) for a camera of the given size
+// and image name: the mask (255 / 0, [height, width]) and the contributing
+// pixel count, or -1 when the camera stays unmasked.
+long long ref_load_mask(const char *mask_dir, const char *relative_name, int width, int height, uint8_t *out) {
+    Camera c;
+    c.width = width;
+    c.height = height;
+    c.relativeName = relative_name;
+    c.loadMask(mask_dir);
+    if (!c.gpuMask.defined()) return -1;
+    std::memcpy(out, c.gpuMask.p, (size_t)width * height);
+    return c.unmaskedPixels;
 }
 
 // resizeArea (loaders/image_io.cpp:115-161) of a float RGB image.

@@ -908,3 +908,45 @@ def test_live_camera_selection(ref_lib, tmp_path):
         imgs = [full.camera(i)["image"].tobytes() for i in range(n)]
         got = sorted(imgs.index(ds.camera(i, use_test=True)["image"].tobytes()) for i in range(ds.num_test))
         assert got == list(np.flatnonzero(test))
+
+
+@needs_reference
+def test_live_mask_loading(ref_lib, tmp_path):
+    """The reference's Camera::loadMask (its image decoding replaced by an
+    8-bit PGM reader; both sides then see the same pixels) against the
+    library's --mask-dir loading: the same lookup (appended, then swapped
+    name), area resize to the camera, > 0.5 threshold and all-white rule,
+    masks and contributing counts identical."""
+    import ctypes as C
+    from msplat_gb300 import api as A
+    write_colmap_scene(tmp_path, 9)
+    md = tmp_path / "masks"
+    os.makedirs(md)
+    rng = np.random.default_rng(9)
+    cams, _, _ = ref_lib.load_colmap(tmp_path)
+
+    def pgm(path, m):
+        path.write_bytes(b"P5 %d %d 255\n" % (m.shape[1], m.shape[0]) + m.tobytes())
+
+    for i, c in enumerate(cams):
+        w, h = c["size"]
+        name = c["name"]
+        kind = i % 4
+        if kind == 0:       # same size, appended name
+            pgm(md / (name + ".png"), (rng.random((h, w)) > 0.3).astype(np.uint8) * 255)
+        elif kind == 1:     # other size, swapped name
+            pgm(md / (name.rsplit(".", 1)[0] + ".png"), rng.integers(0, 256, (h // 2 + 3, w // 3 + 1), dtype=np.uint8))
+        elif kind == 2:     # all white
+            pgm(md / (name + ".png"), np.full((h, w), 255, np.uint8))
+    ds = A.Dataset(str(tmp_path), mask_dir=str(md))
+    L = ref_lib.lib()
+    L.ref_load_mask.restype = C.c_longlong
+    for i, c in enumerate(cams):
+        w, h = c["size"]
+        ref = np.zeros((h, w), np.uint8)
+        n = L.ref_load_mask(str(md).encode(), c["name"].encode(), w, h, ref.ctypes.data_as(C.POINTER(C.c_uint8)))
+        mine = ds.mask(i)
+        if n < 0:
+            assert mine is None, i
+        else:
+            assert mine is not None and np.array_equal(mine, ref) and int((mine > 0).sum()) == n, i
