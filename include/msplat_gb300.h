@@ -136,6 +136,14 @@ MsplatDataset msplat_dataset_create_ex(const char *path, float downscaleFactor, 
 MsplatDataset msplat_dataset_create_masked(const char *path, float downscaleFactor, bool evalMode, int testEvery,
                                            const char *colmapImagePath, const char *maskDir);
 
+/* Camera i's image file (disk datasets; "" for in-memory ones) written to
+ * path (capacity bytes, NUL-terminated): returns its length, or -1 for a
+ * bad index.  msplat_dataset_transform gives the centring and scaling the
+ * loader applied (autoScaleAndCenter, core/src/input_data.cpp:115-169):
+ * positions in the dataset's own frame are x / scale + translation. */
+int msplat_dataset_camera_file(MsplatDataset ds, int i, int use_test, char *path, int capacity);
+int msplat_dataset_transform(MsplatDataset ds, float *scale, float translation[3]);
+
 /* The reference CLI's --val (InputData::getCameras, core/src/input_data.cpp:
  * 173-194): withholds one training camera as the dataset's only test camera
  * — val_image "random" (or NULL) picks mt19937(42)'s first draw modulo the

@@ -112,6 +112,8 @@ def _lib():
     L.msplat_dataset_create_masked.restype = vp
     L.msplat_dataset_mask.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_uint8)]
     L.msplat_dataset_hold_out.argtypes = [vp, cp]
+    L.msplat_dataset_camera_file.argtypes = [vp, C.c_int, C.c_int, C.c_char_p, C.c_int]
+    L.msplat_dataset_transform.argtypes = [vp, fp, fp]
     L.msplat_dataset_mask.restype = C.c_longlong
     L.msplat_viewer_create.argtypes = [cp, C.c_int, C.c_int, C.c_float]
     L.msplat_viewer_create.restype = vp
@@ -221,6 +223,23 @@ class Dataset:
         if not h:
             raise RuntimeError("could not build a dataset from the arrays (empty image size or missing points?)")
         return cls(_handle=h)
+
+    def camera_file(self, i: int, use_test: bool = False) -> str:
+        """Camera i's image file ("" for in-memory datasets)."""
+        L = _lib()
+        n = L.msplat_dataset_camera_file(self.h, i, int(use_test), None, 0)
+        if n < 0:
+            raise IndexError(i)
+        buf = C.create_string_buffer(n + 1)
+        L.msplat_dataset_camera_file(self.h, i, int(use_test), buf, n + 1)
+        return buf.value.decode()
+
+    @property
+    def transform(self):
+        """(scale, translation): dataset-frame positions are x / scale + translation."""
+        sc, t = np.zeros(1, np.float32), np.zeros(3, np.float32)
+        _lib().msplat_dataset_transform(self.h, _fp(sc), _fp(t))
+        return float(sc[0]), t
 
     def hold_out(self, val_image: str = "random") -> int:
         """Withholds one training camera for validation (the reference CLI's

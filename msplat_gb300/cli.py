@@ -12,6 +12,7 @@ the library's C API; no training math lives here.
 from __future__ import annotations
 
 import argparse
+import json
 import math
 import os
 import struct
@@ -103,6 +104,44 @@ def parse(argv=None):
     return a
 
 
+def save_cameras(path: str, ds: A.Dataset, keep_crs: bool, test_every: int = 0, held: int = -1) -> None:
+    """cameras.json as the reference writes it next to the scene
+    (InputData::saveCameras, core/src/input_data.cpp:209-240): every camera
+    in the loader's order with its image file name, size, intrinsics,
+    rotation (OpenCV axes: the pose's columns 1 and 2 negated back) and
+    position (in the dataset's own frame with keep_crs).  test_every: the
+    eval split the dataset was made with; held: the --val camera's index."""
+    n = ds.num_train + ds.num_test
+    order = []
+    if test_every > 0:
+        t = r = 0
+        for i in range(n):
+            if i % test_every == 0:
+                order.append((True, t)); t += 1
+            else:
+                order.append((False, r)); r += 1
+    else:
+        order = [(False, i) for i in range(ds.num_train)]
+        if held >= 0:
+            order.insert(held, (True, 0))
+    scale, tr = ds.transform
+    out = []
+    for use_test, i in order:
+        c = ds.camera(i, use_test)
+        m = np.asarray(c["cam_to_world"], np.float32).reshape(4, 4)
+        R = m[:3, :3].copy()
+        R[:, 1:] *= np.float32(-1.0)
+        T = m[:3, 3].copy()
+        if keep_crs:
+            T = T / np.float32(scale) + tr
+        fx, fy, cx, cy = (float(np.float32(c[k])) for k in ("fx", "fy", "cx", "cy"))
+        out.append({"file_path": os.path.basename(ds.camera_file(i, use_test)), "width": int(c["width"]),
+                    "height": int(c["height"]), "fx": fx, "fy": fy, "cx": cx, "cy": cy,
+                    "rotation": [[float(v) for v in row] for row in R], "translation": [float(v) for v in T]})
+    with open(path, "w") as f:
+        json.dump(out, f, indent=2, sort_keys=True)
+
+
 def _save(trainer: A.GaussianTrainer, path: str):
     if path.endswith(".splat"):
         trainer.export_splat(path)
@@ -119,8 +158,9 @@ def main(argv=None) -> int:
           f" in {time.time() - t0:.1f} s", flush=True)
     # validation camera (the reference CLI: --val-render implies --val; eval mode splits instead)
     val = (a.val or bool(a.val_render)) and not a.eval
+    held = -1
     if val:
-        ds.hold_out(a.val_image)
+        held = ds.hold_out(a.val_image)
         if a.val_render:
             os.makedirs(a.val_render, exist_ok=True)
     cfg = A.TrainingConfig(iterations=a.num_iters, sh_degree=a.sh_degree, sh_degree_interval=a.sh_degree_interval,
@@ -189,6 +229,8 @@ def main(argv=None) -> int:
             last_gate = gate
             if stopped:
                 break
+    save_cameras(os.path.join(os.path.dirname(a.output) or ".", "cameras.json"), ds, a.keep_crs,
+                 a.test_every if a.eval else 0, held)
     _save(trainer, a.output)
     print(f"Saved {a.output} ({trainer.splat_count:,} Gaussians, {time.time() - t_start:.1f} s of training)")
     if a.eval and ds.num_test > 0:

@@ -1198,6 +1198,23 @@ MsplatDataset msplat_dataset_create_masked(const char *path, float downscaleFact
     }, (MsplatDataset) nullptr);
 }
 
+int msplat_dataset_camera_file(MsplatDataset ds, int i, int use_test, char *path, int capacity) {
+    if (!ds) return -1;
+    auto &cams = use_test ? DS(ds)->test : DS(ds)->train;
+    if (i < 0 || i >= (int)cams.size()) return -1;
+    const std::string &p = cams[i].path;
+    if (path && capacity > 0) std::snprintf(path, (size_t)capacity, "%s", p.c_str());
+    return (int)p.size();
+}
+
+int msplat_dataset_transform(MsplatDataset ds, float *scale, float translation[3]) {
+    if (!ds) return -1;
+    if (scale) *scale = DS(ds)->scale;
+    if (translation)
+        for (int k = 0; k < 3; k++) translation[k] = DS(ds)->translation[k];
+    return 0;
+}
+
 int msplat_dataset_hold_out(MsplatDataset ds, const char *val_image) {
     if (!ds) return -1;
     DatasetImpl *d = DS(ds);

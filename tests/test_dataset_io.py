@@ -527,3 +527,42 @@ def test_validation_hold_out(tmp_path):
     from msplat_gb300 import cli
     a = cli.parse(["data", "--val-render", "out", "--val-image", "f3"])
     assert (a.val, a.val_render, a.val_image) == (False, "out", "f3")
+
+
+def test_cli_cameras_json(tmp_path):
+    """The CLI's cameras.json (InputData::saveCameras): every camera in the
+    loader's order (the eval split and a --val camera put back in place),
+    file names, sizes, intrinsics, the rotation with the pose's columns 1 and
+    2 negated (OpenCV axes) and the position, in the dataset's own frame
+    with keep_crs; keys in std::map order as nlohmann writes them."""
+    from msplat_gb300 import cli
+    eyes, imgs, xyz, rgb = _scene(tmp_path)
+    os.makedirs(tmp_path / "images")
+    frames = []
+    for k in range(5):
+        write_png(tmp_path / "images" / f"f{k}.png", [imgs[k][y].tobytes() for y in range(24)], 2, 8)
+        frames.append({"file_path": f"images/f{k}.png", "transform_matrix": _pose(eyes[k]).tolist()})
+    json.dump({"w": 32, "h": 24, "fl_x": 30.0, "fl_y": 30.0, "cx": 16.0, "cy": 12.0, "frames": frames,
+               "ply_file_path": "points.ply"}, open(tmp_path / "transforms.json", "w"))
+    _write_ply_points(tmp_path / "points.ply", xyz, rgb)
+    full = A.Dataset(str(tmp_path))
+    pos = np.array([_pose(e)[:3, 3] for e in eyes], np.float32)
+    for kind in ("plain", "eval", "val"):
+        if kind == "eval":
+            ds, held, every = A.Dataset(str(tmp_path), eval_mode=True, test_every=2), -1, 2
+        else:
+            ds, every = A.Dataset(str(tmp_path)), 0
+            held = ds.hold_out("f3") if kind == "val" else -1
+        for keep in (False, True):
+            path = tmp_path / f"cams_{kind}_{int(keep)}.json"
+            cli.save_cameras(str(path), ds, keep, every, held)
+            cams = json.load(open(path))
+            assert [c["file_path"] for c in cams] == [f"f{k}.png" for k in range(5)]
+            assert list(cams[0].keys()) == sorted(cams[0].keys())
+            for k, c in enumerate(cams):
+                m = full.camera(k)["cam_to_world"]
+                assert (c["width"], c["height"], c["fx"], c["cx"]) == (32, 24, 30.0, 16.0)
+                R = np.array(c["rotation"], np.float32)
+                assert np.array_equal(R[:, 0], m[:3, 0]) and np.array_equal(R[:, 1:], -m[:3, 1:3])
+                want = pos[k] if keep else m[:3, 3]
+                np.testing.assert_allclose(c["translation"], want, atol=2e-6 if keep else 0)
